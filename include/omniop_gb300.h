@@ -1,0 +1,225 @@
+/*
+ * omniop_gb300.h -- C ABI of the GB300-native hash aggregation / hash join operators.
+ *
+ * Every entry point is plain C: opaque handles, plain pointers and sizes, an int32
+ * status code (OMG_OK == 0) and a thread-local error message (omg_last_error()).
+ * No C++ exception, torch type or CUDA type crosses this boundary; CUDA streams are
+ * passed as `void*` (a cudaStream_t) and may be NULL for the operator's own stream.
+ *
+ * The operator API mirrors OmniOperator's C++ operator surface, which its JNI layer
+ * binds (bindings/java/src/main/cpp/src/jni_operator.cpp:159-215 and
+ * jni_operator_factory.cpp:177-236,585-606,620-).  Each declaration below names
+ * the reference interface it replaces.
+ *
+ * Memory model.  Vectors are either HOST vectors (page-locked host memory the GPU
+ * reads directly, the OmniVec layout: flat values + LSB-first null bitmap where a
+ * set bit means NULL) or DEVICE vectors (HBM; owned, or a non-owning view of memory
+ * the caller owns).  AddInput accepts either; GetOutput returns host vectors unless
+ * the operator was switched to device output.
+ */
+#ifndef OMNIOP_GB300_H
+#define OMNIOP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define OMG_OK 0
+#define OMG_ERR_INVALID_ARG (-1)
+#define OMG_ERR_UNSUPPORTED (-2)
+#define OMG_ERR_CUDA (-3)
+#define OMG_ERR_OOM (-4)
+#define OMG_ERR_OVERFLOW (-5)      /* sum overflow with overflow-as-null off (OmniException) */
+#define OMG_ERR_STATE (-6)         /* call not valid in the operator's current state */
+#define OMG_ERR_TIMEOUT (-7)       /* a bounded device-side wait ran out */
+#define OMG_ERR_NO_DEVICE (-8)     /* no CUDA device: compute entry points refuse to run */
+#define OMG_ERR_INTERNAL (-9)
+
+/* Data type ids: same numbering as type/data_type.h:40-74 (DataTypeId). */
+#define OMG_TYPE_INT 1
+#define OMG_TYPE_LONG 2
+#define OMG_TYPE_DOUBLE 3
+#define OMG_TYPE_BOOLEAN 4
+#define OMG_TYPE_SHORT 5
+#define OMG_TYPE_DECIMAL64 6
+#define OMG_TYPE_DECIMAL128 7
+#define OMG_TYPE_DATE32 8
+#define OMG_TYPE_DATE64 9
+#define OMG_TYPE_TIMESTAMP 12
+#define OMG_TYPE_BYTE 18
+#define OMG_TYPE_FLOAT 19
+#define OMG_TYPE_FIXEDBINARY 40 /* fixed-width byte string (width bytes per row); no reference id */
+
+/* Aggregate function ids: same numbering as operator/util/function_type.h:11-27. */
+#define OMG_AGG_SUM 0
+#define OMG_AGG_COUNT_COLUMN 1
+#define OMG_AGG_COUNT_ALL 2
+#define OMG_AGG_AVG 3
+#define OMG_AGG_MAX 5
+#define OMG_AGG_MIN 6
+
+/* Join types: plannode/planNode.h:406-414.  Only INNER is built. */
+#define OMG_JOIN_INNER 0
+
+/* Operator status: operator/status.h:9-13. */
+#define OMG_STATUS_NORMAL 0
+#define OMG_STATUS_FINISHED 1
+#define OMG_STATUS_ERROR (-1)
+
+/* Policy knobs: util/policy.h:160-186 (SupportContainerVecRule) and
+ * operator/config/operator_config.h:168-190 (OverflowConfig). */
+#define OMG_POLICY_SPARK 0   /* SupportContainerVecRule::NOT_SUPPORT (reference default) */
+#define OMG_POLICY_GENERIC 1 /* SupportContainerVecRule::SUPPORT */
+
+/* Aggregation strategy hints (GB300-specific; results never depend on them). */
+#define OMG_AGG_STRATEGY_AUTO 0
+#define OMG_AGG_STRATEGY_SMEM 1   /* shared-memory pre-aggregation, global overflow */
+#define OMG_AGG_STRATEGY_GLOBAL 2 /* global open-addressing table only */
+
+/* A column type: id plus decimal precision/scale (or FIXEDBINARY width). */
+typedef struct OmgDataType {
+    int32_t id;
+    int32_t precision;
+    int32_t scale;
+    int32_t width;
+} OmgDataType;
+
+/* ---- errors / runtime ------------------------------------------------------------- */
+/* Thread-local message of the last failing call on this thread ("" if none). */
+const char *omg_last_error(void);
+/* Library version string. */
+const char *omg_version(void);
+/* 1 if a CUDA device is usable by this process, else 0. */
+int32_t omg_device_available(void);
+/* Set the policy used by factories created afterwards (ConfigUtil::SetSupportContainerVecRule,
+ * util/config_util.h).  OMG_POLICY_SPARK is the default. */
+int32_t omg_config_set_policy(int32_t policy);
+int32_t omg_config_get_policy(void);
+/* Fault injection on the host: the next `n` device allocations of this library fail
+ * with OMG_ERR_OOM (0 disables).  Used by the tests; never touches the GPU. */
+int32_t omg_debug_fail_next_allocs(int32_t n);
+/* Device-side bounded-wait budget in clock64 ticks (0 = library default). */
+int32_t omg_debug_set_wait_budget(int64_t ticks);
+
+/* ---- OmniVec: vectors and batches -------------------------------------------------- */
+/* New flat host vector (VectorHelper::CreateFlatVector, vector/vector_helper.h).
+ * Values are zeroed, no nulls.  FIXEDBINARY needs omg_vec_new_fixed. */
+int32_t omg_vec_new(int32_t type_id, int32_t size, void **out_vec);
+int32_t omg_vec_new_fixed(int32_t width, int32_t size, void **out_vec);
+/* New flat device vector (HBM, owned by the vector). */
+int32_t omg_vec_new_device(int32_t type_id, int32_t width, int32_t size, void **out_vec);
+/* Non-owning device view over caller memory.  `nulls` may be NULL (no nulls); when given
+ * it is an LSB-first bitmap, set bit = NULL, of ceil(size/8) bytes at least. */
+int32_t omg_vec_wrap_device(int32_t type_id, int32_t width, int32_t size, void *values, void *nulls,
+    void **out_vec);
+/* Delete a vector that is not owned by a batch. */
+int32_t omg_vec_free(void *vec);
+/* Raw accessors (unsafe/unsafe_vector.h:19-48).  Pointers are host or device
+ * addresses according to omg_vec_is_device. */
+void *omg_vec_values(void *vec);
+uint8_t *omg_vec_nulls(void *vec);
+int32_t omg_vec_size(void *vec);
+int32_t omg_vec_type(void *vec);
+int32_t omg_vec_width(void *vec);
+int32_t omg_vec_is_device(void *vec);
+/* BaseVector::HasNull / SetNullFlag (vector/vector.h:45-). */
+int32_t omg_vec_has_null(void *vec);
+int32_t omg_vec_set_null_flag(void *vec, int32_t has_null);
+
+/* VectorBatch (vector/vector_batch.h:10-66). */
+int32_t omg_batch_new(int32_t row_count, void **out_batch);
+int32_t omg_batch_append(void *batch, void *vec); /* batch takes ownership of vec */
+void *omg_batch_get(void *batch, int32_t index);
+int32_t omg_batch_row_count(void *batch);
+int32_t omg_batch_vector_count(void *batch);
+/* VectorHelper::FreeVecBatch: frees the batch and all its vectors. */
+int32_t omg_batch_free(void *batch);
+/* Copy a batch between host and device residency (new batch, caller owns it). */
+int32_t omg_batch_to_device(void *batch, void **out_batch);
+int32_t omg_batch_to_host(void *batch, void **out_batch);
+
+/* ---- factories ---------------------------------------------------------------------- */
+/* HashAggregationOperatorFactory(groupByCol, groupInputTypes, aggsCols, aggInputTypes,
+ *     aggOutputTypes, aggFuncTypes, maskColsVector, inputRaws, outputPartials, overflowAsNull)
+ *   -- operator/aggregation/group_aggregation.h:217-249; JNI createHashAggregationOperatorFactory
+ *   (jni_operator_factory.cpp:177-236).
+ * Aggregator i reads the columns agg_cols[agg_col_offsets[i] .. agg_col_offsets[i+1]) whose
+ * types are agg_input_types at the same positions; its output types are
+ * agg_output_types[agg_out_offsets[i] .. agg_out_offsets[i+1]).  Mask columns must all be -1
+ * (no mask) and input_raws/output_partials must be 1/0 (single-stage); other values return
+ * OMG_ERR_UNSUPPORTED. */
+int32_t omg_hashagg_factory_create(const uint32_t *group_cols, const OmgDataType *group_types,
+    int32_t n_group, const uint32_t *agg_func_types, int32_t n_agg, const int32_t *agg_col_offsets,
+    const uint32_t *agg_cols, const OmgDataType *agg_input_types, const int32_t *agg_out_offsets,
+    const OmgDataType *agg_output_types, const int32_t *mask_cols, const uint8_t *input_raws,
+    const uint8_t *output_partials, int32_t overflow_as_null, void **out_factory);
+
+/* HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(joinType, buildTypes,
+ *     buildHashCols, buildHashColsCount, operatorCount) -- operator/join/hash_builder.h:28-31. */
+int32_t omg_hashbuilder_factory_create(int32_t join_type, const OmgDataType *build_types,
+    int32_t n_build_types, const int32_t *build_hash_cols, int32_t n_hash_cols, int32_t operator_count,
+    void **out_factory);
+
+/* LookupJoinOperatorFactory::CreateLookupJoinOperatorFactory(probeTypes, probeOutputCols, n,
+ *     probeHashCols, n, buildOutputCols, n, buildOutputTypes, hashBuilderFactoryAddr, filterExpr,
+ *     isShuffleExchangeBuildPlan, overflowConfig) -- operator/join/lookup_join.h:148-152.
+ * `filter_expr` must be NULL (join filters are not built). */
+int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_probe_types,
+    const int32_t *probe_output_cols, int32_t n_probe_output, const int32_t *probe_hash_cols,
+    int32_t n_probe_hash, const int32_t *build_output_cols, int32_t n_build_output,
+    const OmgDataType *build_output_types, int64_t hash_builder_factory_addr, const void *filter_expr,
+    int32_t is_shuffle_exchange_build_plan, void **out_factory);
+
+/* OperatorFactory::CreateOperator (operator/operator_factory.h:18). */
+int32_t omg_factory_create_operator(void *factory, void **out_op);
+/* Factory destructor (the JNI closeNative on a factory). */
+int32_t omg_factory_destroy(void *factory);
+
+/* ---- operators ---------------------------------------------------------------------- */
+/* Operator::Init (operator/operator.h:56). */
+int32_t omg_op_init(void *op);
+/* Operator::AddInput (operator.h:36).  Takes ownership of `batch` as the reference does
+ * (group_aggregation.cpp:395-396, lookup_join.cpp:464-466; the builder retains it).
+ * `*ret` receives the reference's int32 return value (0). */
+int32_t omg_op_add_input(void *op, void *batch, int32_t *ret);
+/* Operator::GetOutput (operator.h:38).  `*out_batch` is NULL or a new batch owned by the
+ * caller; `*ret` is the reference's return value (agg: 1 if a batch was produced). */
+int32_t omg_op_get_output(void *op, void **out_batch, int32_t *ret);
+/* Operator::GetStatus (operator.h:46-49): OMG_STATUS_*. */
+int32_t omg_op_status(void *op);
+/* Operator::noMoreInput / setNoMoreInput / needsInput (operator.h:117-130). */
+int32_t omg_op_no_more_input(void *op);
+int32_t omg_op_set_no_more_input(void *op, int32_t no_more_input);
+int32_t omg_op_needs_input(void *op);
+/* LookupJoinOperator::IsBlocked (lookup_join.cpp:270-277): 1 while the build is unfinished. */
+int32_t omg_op_is_blocked(void *op);
+/* Operator::GetHashMapUniqueKeys (operator.h:87). */
+int64_t omg_op_hashmap_unique_keys(void *op);
+/* Operator::Close (operator.h:61) and Operator::DeleteOperator (operator.h:40-44). */
+int32_t omg_op_close(void *op);
+int32_t omg_op_delete(void *op);
+
+/* ---- GB300-specific operator controls (no reference counterpart) --------------------- */
+/* Run the operator's kernels on `stream` (a cudaStream_t; NULL = the operator's own). */
+int32_t omg_op_set_stream(void *op, void *stream);
+/* 1: GetOutput returns DEVICE vectors (HBM) instead of host vectors. */
+int32_t omg_op_set_device_output(void *op, int32_t on);
+/* Aggregation: strategy hint and initial global-table capacity (groups); 0 = automatic. */
+int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hint);
+/* Counters of the last run: [0]=kernel launches, [1]=table resizes, [2]=retried rows,
+ * [3]=groups, [4]=ordered-fallback groups, [5]=output rows. */
+int32_t omg_op_get_counters(void *op, int64_t *out, int32_t n);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* OMNIOP_GB300_H */

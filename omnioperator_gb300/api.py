@@ -1,0 +1,353 @@
+"""Python mirror of OmniOperator's operator interface for the hash aggregation / hash join path.
+
+Names and argument meaning follow the reference's C++ API (operator/operator.h,
+operator/aggregation/group_aggregation.h:217-249, operator/join/hash_builder.h:28-31,
+operator/join/lookup_join.h:148-152); every call goes through the C ABI of
+libomniop_gb300.so.  Batches are OmniVec VectorBatch handles: ``make_batch`` builds a host
+batch from numpy columns, ``batch_to_numpy`` reads one back.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._capi import OmgDataType, OmgError, check, lib
+
+# DataTypeId (type/data_type.h:40-74)
+OMNI_INT, OMNI_LONG, OMNI_DOUBLE, OMNI_BOOLEAN, OMNI_SHORT = 1, 2, 3, 4, 5
+OMNI_DECIMAL64, OMNI_DECIMAL128, OMNI_DATE32, OMNI_DATE64, OMNI_TIMESTAMP = 6, 7, 8, 9, 12
+OMNI_BYTE, OMNI_FLOAT, OMNI_FIXEDBINARY = 18, 19, 40
+# FunctionType (operator/util/function_type.h:11-27)
+OMNI_AGGREGATION_TYPE_SUM, OMNI_AGGREGATION_TYPE_COUNT_COLUMN = 0, 1
+OMNI_AGGREGATION_TYPE_COUNT_ALL, OMNI_AGGREGATION_TYPE_AVG = 2, 3
+OMNI_AGGREGATION_TYPE_MAX, OMNI_AGGREGATION_TYPE_MIN = 5, 6
+# JoinType (plannode/planNode.h:406-414)
+OMNI_JOIN_TYPE_INNER = 0
+# OmniStatus (operator/status.h:9-13)
+OMNI_STATUS_NORMAL, OMNI_STATUS_FINISHED, OMNI_STATUS_ERROR = 0, 1, -1
+# SupportContainerVecRule (util/policy.h:160-167)
+POLICY_SPARK, POLICY_GENERIC = 0, 1
+AGG_STRATEGY_AUTO, AGG_STRATEGY_SMEM, AGG_STRATEGY_GLOBAL = 0, 1, 2
+
+_NP = {OMNI_INT: np.int32, OMNI_LONG: np.int64, OMNI_DOUBLE: np.float64, OMNI_BOOLEAN: np.int8,
+       OMNI_SHORT: np.int16, OMNI_DECIMAL64: np.int64, OMNI_DATE32: np.int32, OMNI_DATE64: np.int64,
+       OMNI_TIMESTAMP: np.int64, OMNI_BYTE: np.int8, OMNI_FLOAT: np.float32}
+_WIDTH = {OMNI_DECIMAL128: 16, **{k: np.dtype(v).itemsize for k, v in _NP.items()}}
+
+
+@dataclass(frozen=True)
+class DataType:
+    id: int
+    precision: int = 0
+    scale: int = 0
+    width: int = 0
+
+    @property
+    def byte_width(self) -> int:
+        return self.width if self.id == OMNI_FIXEDBINARY else _WIDTH[self.id]
+
+
+def IntType():
+    return DataType(OMNI_INT)
+
+
+def LongType():
+    return DataType(OMNI_LONG)
+
+
+def ShortType():
+    return DataType(OMNI_SHORT)
+
+
+def DoubleType():
+    return DataType(OMNI_DOUBLE)
+
+
+def Decimal64Type(precision=18, scale=0):
+    return DataType(OMNI_DECIMAL64, precision, scale)
+
+
+def Decimal128Type(precision=38, scale=0):
+    return DataType(OMNI_DECIMAL128, precision, scale)
+
+
+def FixedBinaryType(width):
+    return DataType(OMNI_FIXEDBINARY, 0, 0, width)
+
+
+def _types(types):
+    arr = (OmgDataType * max(len(types), 1))()
+    for i, t in enumerate(types):
+        arr[i] = OmgDataType(t.id, t.precision, t.scale, t.width)
+    return arr
+
+
+def _i32(vals):
+    return (C.c_int32 * max(len(vals), 1))(*vals)
+
+
+def _u32(vals):
+    return (C.c_uint32 * max(len(vals), 1))(*vals)
+
+
+def set_policy(policy: int) -> None:
+    """ConfigUtil::SetSupportContainerVecRule: POLICY_SPARK (default) or POLICY_GENERIC."""
+    check(lib().omg_config_set_policy(policy))
+
+
+def device_available() -> bool:
+    return bool(lib().omg_device_available())
+
+
+# ----------------------------------------------------------------------------------- vectors
+def _np_view(ptr: int, dtype, count: int) -> np.ndarray:
+    if count == 0:
+        return np.zeros(0, dtype=dtype)
+    buf = (C.c_uint8 * (count * np.dtype(dtype).itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype, count=count)
+
+
+def new_host_vector(dtype: DataType, values: np.ndarray, nulls: np.ndarray | None = None) -> int:
+    """A host (pinned) OmniVec flat vector holding `values` (decimal128: (n, 2) uint64 low/high;
+    fixed binary: (n, width) uint8) with an optional boolean null mask."""
+    n = len(values)
+    out = C.c_void_p()
+    if dtype.id == OMNI_FIXEDBINARY:
+        check(lib().omg_vec_new_fixed(dtype.width, n, C.byref(out)))
+    else:
+        check(lib().omg_vec_new(dtype.id, n, C.byref(out)))
+    vec = out.value
+    raw = np.ascontiguousarray(values).view(np.uint8).reshape(-1)
+    if raw.size:
+        C.memmove(lib().omg_vec_values(vec), raw.ctypes.data, raw.size)
+    if nulls is not None and np.any(nulls):
+        bits = np.packbits(np.asarray(nulls, dtype=bool), bitorder="little")
+        C.memmove(lib().omg_vec_nulls(vec), bits.ctypes.data, bits.size)
+        check(lib().omg_vec_set_null_flag(vec, 1))
+    return vec
+
+
+def make_batch(types, columns, nulls=None) -> int:
+    """A host VectorBatch from numpy columns (all of equal length)."""
+    n = len(columns[0]) if columns else 0
+    out = C.c_void_p()
+    check(lib().omg_batch_new(n, C.byref(out)))
+    batch = out.value
+    for i, (t, col) in enumerate(zip(types, columns)):
+        m = None if nulls is None else nulls[i]
+        check(lib().omg_batch_append(batch, new_host_vector(t, col, m)))
+    return batch
+
+
+def wrap_device_batch(types, rows: int, value_ptrs, null_ptrs=None) -> int:
+    """A VectorBatch of non-owning DEVICE vectors over caller memory (e.g. torch tensors)."""
+    out = C.c_void_p()
+    check(lib().omg_batch_new(rows, C.byref(out)))
+    batch = out.value
+    for i, (t, vp) in enumerate(zip(types, value_ptrs)):
+        v = C.c_void_p()
+        np_ = None if null_ptrs is None else null_ptrs[i]
+        check(lib().omg_vec_wrap_device(t.id, t.width, rows, C.c_void_p(vp), C.c_void_p(np_) if np_ else None,
+                                        C.byref(v)))
+        check(lib().omg_batch_append(batch, v.value))
+    return batch
+
+
+def batch_to_device(batch: int) -> int:
+    out = C.c_void_p()
+    check(lib().omg_batch_to_device(batch, C.byref(out)))
+    return out.value
+
+
+def batch_to_host(batch: int) -> int:
+    out = C.c_void_p()
+    check(lib().omg_batch_to_host(batch, C.byref(out)))
+    return out.value
+
+
+def free_batch(batch: int | None) -> None:
+    if batch:
+        check(lib().omg_batch_free(batch))
+
+
+def batch_row_count(batch: int) -> int:
+    return lib().omg_batch_row_count(batch)
+
+
+def batch_to_numpy(batch: int):
+    """[(values, null_mask)] of a host batch (copies)."""
+    L = lib()
+    n = L.omg_batch_row_count(batch)
+    cols = []
+    for i in range(L.omg_batch_vector_count(batch)):
+        v = L.omg_batch_get(batch, i)
+        if L.omg_vec_is_device(v):
+            raise ValueError("device batch: copy it to the host first (batch_to_host)")
+        t = L.omg_vec_type(v)
+        w = L.omg_vec_width(v)
+        ptr = L.omg_vec_values(v)
+        if t == OMNI_DECIMAL128:
+            vals = _np_view(ptr, np.uint64, 2 * n).reshape(n, 2).copy()
+        elif t == OMNI_FIXEDBINARY:
+            vals = _np_view(ptr, np.uint8, w * n).reshape(n, w).copy()
+        else:
+            vals = _np_view(ptr, _NP[t], n).copy()
+        nptr = L.omg_vec_nulls(v)
+        if nptr:
+            bits = _np_view(nptr, np.uint8, (n + 7) // 8)
+            mask = np.unpackbits(bits, bitorder="little")[:n].astype(bool)
+        else:
+            mask = np.zeros(n, dtype=bool)
+        cols.append((vals, mask))
+    return cols
+
+
+# --------------------------------------------------------------------------------- operators
+class Operator:
+    """operator/operator.h:22-266 through the C ABI."""
+
+    def __init__(self, handle: int):
+        self.handle = handle
+
+    def init(self):
+        check(lib().omg_op_init(self.handle))
+
+    def add_input(self, batch: int) -> int:
+        """Operator::AddInput: the operator takes ownership of `batch`."""
+        ret = C.c_int32(0)
+        check(lib().omg_op_add_input(self.handle, batch, C.byref(ret)))
+        return ret.value
+
+    def get_output(self):
+        """Operator::GetOutput -> (return value, batch handle or None)."""
+        out = C.c_void_p()
+        ret = C.c_int32(0)
+        check(lib().omg_op_get_output(self.handle, C.byref(out), C.byref(ret)))
+        return ret.value, out.value
+
+    def get_status(self) -> int:
+        return lib().omg_op_status(self.handle)
+
+    def no_more_input(self):
+        check(lib().omg_op_no_more_input(self.handle))
+
+    def set_no_more_input(self, flag: bool):
+        check(lib().omg_op_set_no_more_input(self.handle, 1 if flag else 0))
+
+    def needs_input(self) -> bool:
+        return bool(lib().omg_op_needs_input(self.handle))
+
+    def is_blocked(self) -> bool:
+        return bool(lib().omg_op_is_blocked(self.handle))
+
+    def get_hashmap_unique_keys(self) -> int:
+        return lib().omg_op_hashmap_unique_keys(self.handle)
+
+    def set_stream(self, stream_handle: int):
+        check(lib().omg_op_set_stream(self.handle, C.c_void_p(stream_handle)))
+
+    def set_device_output(self, on: bool):
+        check(lib().omg_op_set_device_output(self.handle, 1 if on else 0))
+
+    def set_agg_strategy(self, strategy: int, capacity_hint: int = 0):
+        check(lib().omg_op_set_agg_strategy(self.handle, strategy, capacity_hint))
+
+    def counters(self):
+        arr = (C.c_int64 * 8)()
+        check(lib().omg_op_get_counters(self.handle, arr, 8))
+        return {"launches": arr[0], "resizes": arr[1], "retried_rows": arr[2], "groups": arr[3],
+                "ordered_groups": arr[4], "output_rows": arr[5]}
+
+    def close(self):
+        check(lib().omg_op_close(self.handle))
+
+    def delete(self):
+        """Operator::DeleteOperator (Close + delete)."""
+        if self.handle:
+            check(lib().omg_op_delete(self.handle))
+            self.handle = None
+
+    def drain(self):
+        """GetOutput until nothing more comes: list of output batch handles."""
+        outs = []
+        while True:
+            _, b = self.get_output()
+            if not b:
+                return outs
+            outs.append(b)
+
+
+class OperatorFactory:
+    def __init__(self, handle: int):
+        self.handle = handle
+
+    def create_operator(self) -> Operator:
+        out = C.c_void_p()
+        check(lib().omg_factory_create_operator(self.handle, C.byref(out)))
+        return Operator(out.value)
+
+    def close(self):
+        if self.handle:
+            check(lib().omg_factory_destroy(self.handle))
+            self.handle = None
+
+
+class HashAggregationOperatorFactory(OperatorFactory):
+    """HashAggregationOperatorFactory(groupByCol, groupInputTypes, aggsCols, aggInputTypes,
+    aggOutputTypes, aggFuncTypes, maskColsVector, inputRaws, outputPartials, overflowAsNull)."""
+
+    def __init__(self, group_by_cols, group_input_types, aggs_cols, agg_input_types, agg_output_types,
+                 agg_func_types, mask_cols=None, input_raws=None, output_partials=None, overflow_as_null=False):
+        n_agg = len(agg_func_types)
+        col_off, cols, in_types = [0], [], []
+        for c, t in zip(aggs_cols, agg_input_types):
+            cols.extend(c)
+            in_types.extend(t)
+            col_off.append(len(cols))
+        out_off, out_types = [0], []
+        for t in agg_output_types:
+            out_types.extend(t)
+            out_off.append(len(out_types))
+        masks = [-1] * n_agg if mask_cols is None else [(-1 if m in (None, -1, 0xFFFFFFFF) else m) for m in mask_cols]
+        raws = [1] * n_agg if input_raws is None else [1 if r else 0 for r in input_raws]
+        partials = [0] * n_agg if output_partials is None else [1 if p else 0 for p in output_partials]
+        out = C.c_void_p()
+        check(lib().omg_hashagg_factory_create(
+            _u32(group_by_cols), _types(group_input_types), len(group_by_cols), _u32(agg_func_types), n_agg,
+            _i32(col_off), _u32(cols), _types(in_types), _i32(out_off), _types(out_types), _i32(masks),
+            (C.c_uint8 * max(n_agg, 1))(*raws), (C.c_uint8 * max(n_agg, 1))(*partials),
+            1 if overflow_as_null else 0, C.byref(out)))
+        super().__init__(out.value)
+
+
+class HashBuilderOperatorFactory(OperatorFactory):
+    """HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(joinType, buildTypes,
+    buildHashCols, buildHashColsCount, operatorCount)."""
+
+    def __init__(self, join_type, build_types, build_hash_cols, operator_count=1):
+        out = C.c_void_p()
+        check(lib().omg_hashbuilder_factory_create(join_type, _types(build_types), len(build_types),
+                                                   _i32(build_hash_cols), len(build_hash_cols), operator_count,
+                                                   C.byref(out)))
+        super().__init__(out.value)
+
+
+class LookupJoinOperatorFactory(OperatorFactory):
+    """LookupJoinOperatorFactory::CreateLookupJoinOperatorFactory(probeTypes, probeOutputCols,
+    probeHashCols, buildOutputCols, buildOutputTypes, hashBuilderFactoryAddr, filterExpr,
+    isShuffleExchangeBuildPlan, overflowConfig)."""
+
+    def __init__(self, probe_types, probe_output_cols, probe_hash_cols, build_output_cols, build_output_types,
+                 hash_builder_factory: HashBuilderOperatorFactory, filter_expr=None,
+                 is_shuffle_exchange_build_plan=False):
+        if filter_expr is not None:
+            raise OmgError(-2, "join filter expressions are not supported")
+        out = C.c_void_p()
+        check(lib().omg_lookupjoin_factory_create(
+            _types(probe_types), len(probe_types), _i32(probe_output_cols), len(probe_output_cols),
+            _i32(probe_hash_cols), len(probe_hash_cols), _i32(build_output_cols), len(build_output_cols),
+            _types(build_output_types), int(hash_builder_factory.handle), None,
+            1 if is_shuffle_exchange_build_plan else 0, C.byref(out)))
+        super().__init__(out.value)

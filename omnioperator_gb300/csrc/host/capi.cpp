@@ -1,0 +1,439 @@
+// extern "C" boundary (include/omniop_gb300.h).  No exception crosses it: every entry point
+// returns a status code and leaves a thread-local message for omg_last_error().
+#include "omniop_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "host/gpu_runtime.h"
+#include "omniop/hash_aggregation.h"
+#include "omniop/hash_join.h"
+#include "omniop/memory.h"
+#include "omniop/operator.h"
+#include "omniop/vector.h"
+
+using omniruntime::exception::OmniException;
+using omniruntime::op::HashAggregationOperator;
+using omniruntime::op::HashAggregationOperatorFactory;
+using omniruntime::op::HashBuilderOperatorFactory;
+using omniruntime::op::LookupJoinOperatorFactory;
+using omniruntime::op::Operator;
+using omniruntime::op::OperatorFactory;
+using omniruntime::type::DataType;
+using omniruntime::type::DataTypeId;
+using omniruntime::type::DataTypePtr;
+using omniruntime::type::DataTypes;
+using omniruntime::vec::BaseVector;
+using omniruntime::vec::VectorBatch;
+using omniruntime::vec::VectorHelper;
+
+namespace {
+thread_local std::string g_error;
+
+void SetError(const std::string &m) { g_error = m; }
+
+template <typename F> int32_t Guard(F &&f)
+{
+    try {
+        g_error.clear();
+        f();
+        return OMG_OK;
+    } catch (const OmniException &e) {
+        SetError(e.what());
+        return e.GetStatus();
+    } catch (const std::bad_alloc &e) {
+        SetError(std::string("out of host memory: ") + e.what());
+        return OMG_ERR_OOM;
+    } catch (const std::exception &e) {
+        SetError(e.what());
+        return OMG_ERR_INTERNAL;
+    } catch (...) {
+        SetError("unknown error");
+        return OMG_ERR_INTERNAL;
+    }
+}
+
+void Require(bool cond, const char *msg)
+{
+    if (!cond) {
+        throw OmniException("INVALID_ARGUMENT", msg, OMG_ERR_INVALID_ARG);
+    }
+}
+
+DataTypePtr ToType(const OmgDataType &t)
+{
+    return std::make_shared<DataType>(static_cast<DataTypeId>(t.id), t.precision, t.scale, t.width);
+}
+
+DataTypes ToTypes(const OmgDataType *t, int32_t n)
+{
+    std::vector<DataTypePtr> v;
+    for (int32_t i = 0; i < n; ++i) {
+        v.push_back(ToType(t[i]));
+    }
+    return DataTypes(v);
+}
+
+Operator *AsOp(void *op)
+{
+    Require(op != nullptr, "null operator handle");
+    return static_cast<Operator *>(op);
+}
+}  // namespace
+
+extern "C" {
+
+const char *omg_last_error(void) { return g_error.c_str(); }
+
+const char *omg_version(void) { return "omniop-gb300 0.1 (sm_103a)"; }
+
+int32_t omg_device_available(void) { return omg::DeviceAvailable() ? 1 : 0; }
+
+int32_t omg_config_set_policy(int32_t policy)
+{
+    return Guard([&] {
+        Require(policy == OMG_POLICY_SPARK || policy == OMG_POLICY_GENERIC, "unknown policy");
+        omniruntime::op::SetSupportContainerVecRule(policy == OMG_POLICY_SPARK
+                ? omniruntime::op::SupportContainerVecRule::NOT_SUPPORT
+                : omniruntime::op::SupportContainerVecRule::SUPPORT);
+    });
+}
+
+int32_t omg_config_get_policy(void)
+{
+    return omniruntime::op::GetSupportContainerVecRule() == omniruntime::op::SupportContainerVecRule::NOT_SUPPORT
+        ? OMG_POLICY_SPARK
+        : OMG_POLICY_GENERIC;
+}
+
+int32_t omg_debug_fail_next_allocs(int32_t n)
+{
+    omg::SetFailNextDeviceAllocs(n < 0 ? 0 : n);
+    return OMG_OK;
+}
+
+int32_t omg_debug_set_wait_budget(int64_t ticks)
+{
+    omg::SetWaitBudget(ticks < 0 ? 0 : ticks);
+    return OMG_OK;
+}
+
+// ---- vectors
+int32_t omg_vec_new(int32_t type_id, int32_t size, void **out_vec)
+{
+    return Guard([&] {
+        Require(out_vec != nullptr && size >= 0, "invalid arguments");
+        const int32_t w = omniruntime::type::TypeWidth(static_cast<DataTypeId>(type_id));
+        Require(w > 0, "unsupported vector type");
+        *out_vec = new BaseVector(static_cast<DataTypeId>(type_id), w, size, false);
+    });
+}
+
+int32_t omg_vec_new_fixed(int32_t width, int32_t size, void **out_vec)
+{
+    return Guard([&] {
+        Require(out_vec != nullptr && size >= 0 && width > 0, "invalid arguments");
+        *out_vec = new BaseVector(omniruntime::type::OMNI_FIXEDBINARY, width, size, false);
+    });
+}
+
+int32_t omg_vec_new_device(int32_t type_id, int32_t width, int32_t size, void **out_vec)
+{
+    return Guard([&] {
+        Require(out_vec != nullptr && size >= 0, "invalid arguments");
+        omg::RequireDevice();
+        const int32_t w = omniruntime::type::TypeWidth(static_cast<DataTypeId>(type_id), width);
+        Require(w > 0, "unsupported vector type");
+        *out_vec = new BaseVector(static_cast<DataTypeId>(type_id), w, size, true, nullptr);
+        omg::CudaCheck(cudaStreamSynchronize(nullptr), "zero device vector");
+    });
+}
+
+int32_t omg_vec_wrap_device(int32_t type_id, int32_t width, int32_t size, void *values, void *nulls, void **out_vec)
+{
+    return Guard([&] {
+        Require(out_vec != nullptr && size >= 0 && values != nullptr, "invalid arguments");
+        const int32_t w = omniruntime::type::TypeWidth(static_cast<DataTypeId>(type_id), width);
+        Require(w > 0, "unsupported vector type");
+        auto vb = omg::Buffer::DeviceView(values, static_cast<size_t>(w) * size);
+        omg::BufferPtr nb = nulls != nullptr ? omg::Buffer::DeviceView(nulls, (size + 7) / 8) : nullptr;
+        *out_vec = new BaseVector(static_cast<DataTypeId>(type_id), w, size, vb, 0, nb, 0, nulls != nullptr);
+    });
+}
+
+int32_t omg_vec_free(void *vec)
+{
+    return Guard([&] { delete static_cast<BaseVector *>(vec); });
+}
+
+void *omg_vec_values(void *vec) { return vec ? static_cast<BaseVector *>(vec)->RawValues() : nullptr; }
+uint8_t *omg_vec_nulls(void *vec) { return vec ? static_cast<BaseVector *>(vec)->RawNulls() : nullptr; }
+int32_t omg_vec_size(void *vec) { return vec ? static_cast<BaseVector *>(vec)->GetSize() : -1; }
+int32_t omg_vec_type(void *vec) { return vec ? static_cast<BaseVector *>(vec)->GetTypeId() : -1; }
+int32_t omg_vec_width(void *vec) { return vec ? static_cast<BaseVector *>(vec)->GetWidth() : -1; }
+int32_t omg_vec_is_device(void *vec) { return vec ? (static_cast<BaseVector *>(vec)->IsDevice() ? 1 : 0) : -1; }
+int32_t omg_vec_has_null(void *vec) { return vec ? (static_cast<BaseVector *>(vec)->HasNull() ? 1 : 0) : -1; }
+int32_t omg_vec_set_null_flag(void *vec, int32_t has_null)
+{
+    return Guard([&] {
+        Require(vec != nullptr, "null vector");
+        static_cast<BaseVector *>(vec)->SetNullFlag(has_null != 0);
+    });
+}
+
+// ---- batches
+int32_t omg_batch_new(int32_t row_count, void **out_batch)
+{
+    return Guard([&] {
+        Require(out_batch != nullptr && row_count >= 0, "invalid arguments");
+        *out_batch = new VectorBatch(row_count);
+    });
+}
+
+int32_t omg_batch_append(void *batch, void *vec)
+{
+    return Guard([&] {
+        Require(batch != nullptr && vec != nullptr, "null handle");
+        static_cast<VectorBatch *>(batch)->Append(static_cast<BaseVector *>(vec));
+    });
+}
+
+void *omg_batch_get(void *batch, int32_t index)
+{
+    auto *b = static_cast<VectorBatch *>(batch);
+    if (b == nullptr || index < 0 || index >= b->GetVectorCount()) {
+        return nullptr;
+    }
+    return b->Get(index);
+}
+
+int32_t omg_batch_row_count(void *batch) { return batch ? static_cast<VectorBatch *>(batch)->GetRowCount() : -1; }
+int32_t omg_batch_vector_count(void *batch)
+{
+    return batch ? static_cast<VectorBatch *>(batch)->GetVectorCount() : -1;
+}
+
+int32_t omg_batch_free(void *batch)
+{
+    return Guard([&] { VectorHelper::FreeVecBatch(static_cast<VectorBatch *>(batch)); });
+}
+
+int32_t omg_batch_to_device(void *batch, void **out_batch)
+{
+    return Guard([&] {
+        Require(batch != nullptr && out_batch != nullptr, "null handle");
+        omg::RequireDevice();
+        *out_batch = VectorHelper::CopyBatch(static_cast<VectorBatch *>(batch), true, nullptr);
+    });
+}
+
+int32_t omg_batch_to_host(void *batch, void **out_batch)
+{
+    return Guard([&] {
+        Require(batch != nullptr && out_batch != nullptr, "null handle");
+        omg::RequireDevice();
+        *out_batch = VectorHelper::CopyBatch(static_cast<VectorBatch *>(batch), false, nullptr);
+    });
+}
+
+// ---- factories
+int32_t omg_hashagg_factory_create(const uint32_t *group_cols, const OmgDataType *group_types, int32_t n_group,
+    const uint32_t *agg_func_types, int32_t n_agg, const int32_t *agg_col_offsets, const uint32_t *agg_cols,
+    const OmgDataType *agg_input_types, const int32_t *agg_out_offsets, const OmgDataType *agg_output_types,
+    const int32_t *mask_cols, const uint8_t *input_raws, const uint8_t *output_partials, int32_t overflow_as_null,
+    void **out_factory)
+{
+    return Guard([&] {
+        Require(out_factory != nullptr && n_group >= 0 && n_agg >= 0, "invalid arguments");
+        Require(n_group == 0 || (group_cols != nullptr && group_types != nullptr), "null group arrays");
+        Require(n_agg == 0 || (agg_func_types != nullptr && agg_col_offsets != nullptr && agg_out_offsets != nullptr),
+            "null aggregator arrays");
+        std::vector<uint32_t> groupCols(group_cols, group_cols + n_group);
+        DataTypes groupTypes = ToTypes(group_types, n_group);
+        std::vector<std::vector<uint32_t>> aggCols;
+        std::vector<DataTypes> aggIn;
+        std::vector<DataTypes> aggOut;
+        std::vector<uint32_t> funcs(agg_func_types, agg_func_types + n_agg);
+        std::vector<uint32_t> masks;
+        std::vector<bool> raws;
+        std::vector<bool> partials;
+        for (int32_t i = 0; i < n_agg; ++i) {
+            const int32_t a0 = agg_col_offsets[i];
+            const int32_t a1 = agg_col_offsets[i + 1];
+            Require(a1 >= a0, "bad aggregator column offsets");
+            aggCols.emplace_back(agg_cols + a0, agg_cols + a1);
+            aggIn.push_back(ToTypes(agg_input_types + a0, a1 - a0));
+            const int32_t o0 = agg_out_offsets[i];
+            const int32_t o1 = agg_out_offsets[i + 1];
+            Require(o1 >= o0, "bad aggregator output offsets");
+            aggOut.push_back(ToTypes(agg_output_types + o0, o1 - o0));
+            masks.push_back(mask_cols == nullptr || mask_cols[i] < 0 ? UINT32_MAX : static_cast<uint32_t>(mask_cols[i]));
+            raws.push_back(input_raws == nullptr ? true : input_raws[i] != 0);
+            partials.push_back(output_partials == nullptr ? false : output_partials[i] != 0);
+        }
+        auto *f = new HashAggregationOperatorFactory(groupCols, groupTypes, aggCols, aggIn, aggOut, funcs, masks, raws,
+            partials, overflow_as_null != 0);
+        try {
+            f->Init();
+        } catch (...) {
+            delete f;
+            throw;
+        }
+        *out_factory = static_cast<OperatorFactory *>(f);
+    });
+}
+
+int32_t omg_hashbuilder_factory_create(int32_t join_type, const OmgDataType *build_types, int32_t n_build_types,
+    const int32_t *build_hash_cols, int32_t n_hash_cols, int32_t operator_count, void **out_factory)
+{
+    return Guard([&] {
+        Require(out_factory != nullptr && build_types != nullptr && n_build_types > 0, "invalid arguments");
+        auto *f = HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(
+            static_cast<omniruntime::op::JoinType>(join_type), ToTypes(build_types, n_build_types), build_hash_cols,
+            n_hash_cols, operator_count);
+        *out_factory = static_cast<OperatorFactory *>(f);
+    });
+}
+
+int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_probe_types,
+    const int32_t *probe_output_cols, int32_t n_probe_output, const int32_t *probe_hash_cols, int32_t n_probe_hash,
+    const int32_t *build_output_cols, int32_t n_build_output, const OmgDataType *build_output_types,
+    int64_t hash_builder_factory_addr, const void *filter_expr, int32_t is_shuffle_exchange_build_plan,
+    void **out_factory)
+{
+    return Guard([&] {
+        Require(out_factory != nullptr && probe_types != nullptr && n_probe_types > 0, "invalid arguments");
+        auto *base = reinterpret_cast<OperatorFactory *>(hash_builder_factory_addr);
+        auto *builder = dynamic_cast<HashBuilderOperatorFactory *>(base);
+        Require(builder != nullptr, "hash_builder_factory_addr is not a hash builder factory");
+        std::vector<int32_t> po(probe_output_cols, probe_output_cols + n_probe_output);
+        std::vector<int32_t> ph(probe_hash_cols, probe_hash_cols + n_probe_hash);
+        std::vector<int32_t> bo(build_output_cols, build_output_cols + n_build_output);
+        auto *f = LookupJoinOperatorFactory::CreateLookupJoinOperatorFactory(ToTypes(probe_types, n_probe_types),
+            po.data(), n_probe_output, ph.data(), n_probe_hash, bo.data(), n_build_output,
+            ToTypes(build_output_types, n_build_output), reinterpret_cast<int64_t>(builder), filter_expr,
+            is_shuffle_exchange_build_plan != 0, nullptr);
+        *out_factory = static_cast<OperatorFactory *>(f);
+    });
+}
+
+int32_t omg_factory_create_operator(void *factory, void **out_op)
+{
+    return Guard([&] {
+        Require(factory != nullptr && out_op != nullptr, "null handle");
+        *out_op = static_cast<OperatorFactory *>(factory)->CreateOperator();
+    });
+}
+
+int32_t omg_factory_destroy(void *factory)
+{
+    return Guard([&] { delete static_cast<OperatorFactory *>(factory); });
+}
+
+// ---- operators
+int32_t omg_op_init(void *op)
+{
+    return Guard([&] { AsOp(op)->Init(); });
+}
+
+int32_t omg_op_add_input(void *op, void *batch, int32_t *ret)
+{
+    return Guard([&] {
+        Operator *o = AsOp(op);
+        Require(batch != nullptr, "null batch");
+        const int32_t r = o->AddInput(static_cast<VectorBatch *>(batch));
+        if (ret != nullptr) {
+            *ret = r;
+        }
+    });
+}
+
+int32_t omg_op_get_output(void *op, void **out_batch, int32_t *ret)
+{
+    return Guard([&] {
+        Operator *o = AsOp(op);
+        Require(out_batch != nullptr, "null output pointer");
+        VectorBatch *b = nullptr;
+        const int32_t r = o->GetOutput(&b);
+        *out_batch = b;
+        if (ret != nullptr) {
+            *ret = r;
+        }
+    });
+}
+
+int32_t omg_op_status(void *op) { return op ? static_cast<int32_t>(static_cast<Operator *>(op)->GetStatus()) : -1; }
+
+int32_t omg_op_no_more_input(void *op)
+{
+    return Guard([&] { AsOp(op)->noMoreInput(); });
+}
+
+int32_t omg_op_set_no_more_input(void *op, int32_t no_more_input)
+{
+    return Guard([&] { AsOp(op)->setNoMoreInput(no_more_input != 0); });
+}
+
+int32_t omg_op_needs_input(void *op) { return op ? (static_cast<Operator *>(op)->needsInput() ? 1 : 0) : -1; }
+
+int32_t omg_op_is_blocked(void *op)
+{
+    if (op == nullptr) {
+        return -1;
+    }
+    return static_cast<Operator *>(op)->IsBlocked() == omniruntime::op::BlockingReason::kNotBlocked ? 0 : 1;
+}
+
+int64_t omg_op_hashmap_unique_keys(void *op)
+{
+    return op ? static_cast<int64_t>(static_cast<Operator *>(op)->GetHashMapUniqueKeys()) : -1;
+}
+
+int32_t omg_op_close(void *op)
+{
+    return Guard([&] { AsOp(op)->Close(); });
+}
+
+int32_t omg_op_delete(void *op)
+{
+    return Guard([&] {
+        if (op != nullptr) {
+            Operator::DeleteOperator(static_cast<Operator *>(op));
+        }
+    });
+}
+
+int32_t omg_op_set_stream(void *op, void *stream)
+{
+    return Guard([&] { AsOp(op)->SetStream(stream); });
+}
+
+int32_t omg_op_set_device_output(void *op, int32_t on)
+{
+    return Guard([&] { AsOp(op)->SetDeviceOutput(on != 0); });
+}
+
+int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hint)
+{
+    return Guard([&] {
+        auto *a = dynamic_cast<HashAggregationOperator *>(AsOp(op));
+        Require(a != nullptr, "not a hash aggregation operator");
+        Require(strategy >= OMG_AGG_STRATEGY_AUTO && strategy <= OMG_AGG_STRATEGY_GLOBAL, "unknown strategy");
+        a->SetStrategy(strategy, capacity_hint);
+    });
+}
+
+int32_t omg_op_get_counters(void *op, int64_t *out, int32_t n)
+{
+    return Guard([&] {
+        Require(out != nullptr && n >= 0, "invalid arguments");
+        const auto &c = AsOp(op)->Counters();
+        for (int32_t i = 0; i < n; ++i) {
+            out[i] = i < static_cast<int32_t>(c.size()) ? c[i] : 0;
+        }
+    });
+}
+
+}  // extern "C"

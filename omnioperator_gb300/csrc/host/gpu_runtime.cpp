@@ -1,0 +1,144 @@
+// Host-side launch helpers (see gpu_runtime.h).
+#include "host/gpu_runtime.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+
+namespace omg {
+
+using omniruntime::vec::BaseVector;
+using omniruntime::vec::VectorBatch;
+
+void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vector<int32_t> &inputCols,
+    int32_t tileRows)
+{
+    if (inputCols.size() > static_cast<size_t>(kMaxInputs)) {
+        throw OmniException("UNSUPPORTED_ERROR", "too many input columns for one kernel", -2);
+    }
+    descs_.Reset(batches.size());
+    anyNulls_.assign(inputCols.size(), false);
+    size_t nTiles = 0;
+    for (auto *b : batches) {
+        nTiles += (static_cast<size_t>(b->GetRowCount()) + tileRows - 1) / tileRows;
+    }
+    tiles_.Reset(nTiles);
+    tileOut_.Reset(nTiles);
+    totalRows_ = 0;
+    size_t t = 0;
+    for (size_t bi = 0; bi < batches.size(); ++bi) {
+        VectorBatch *b = batches[bi];
+        BatchDesc &d = descs_[bi];
+        std::memset(&d, 0, sizeof(d));
+        d.rows = b->GetRowCount();
+        d.rowBase = totalRows_;
+        for (size_t i = 0; i < inputCols.size(); ++i) {
+            const int32_t c = inputCols[i];
+            if (c < 0 || c >= b->GetVectorCount()) {
+                throw OmniException("OPERATOR_RUNTIME_ERROR",
+                    "input batch has " + std::to_string(b->GetVectorCount()) + " vectors, column " +
+                        std::to_string(c) + " requested",
+                    -1);
+            }
+            BaseVector *v = b->Get(c);
+            if (v->GetSize() < b->GetRowCount()) {
+                throw OmniException("OPERATOR_RUNTIME_ERROR", "vector shorter than the batch row count", -1);
+            }
+            d.cols[i] = v->RawValues();
+            const bool hasNull = v->RawNulls() != nullptr && v->HasNull();
+            d.nulls[i] = hasNull ? v->RawNulls() : nullptr;
+            if (hasNull) {
+                anyNulls_[i] = true;
+            }
+        }
+        for (int64_t r = 0; r < d.rows; r += tileRows) {
+            TileDesc &td = tiles_[t];
+            td.batch = static_cast<int32_t>(bi);
+            td.row0 = static_cast<int32_t>(r);
+            td.rows = static_cast<int32_t>(std::min<int64_t>(tileRows, d.rows - r));
+            td.pad = 0;
+            tileOut_[t] = totalRows_ + r;
+            ++t;
+        }
+        totalRows_ += d.rows;
+    }
+}
+
+void BatchTable::Upload(cudaStream_t s)
+{
+    dBatches_.Reset(std::max<size_t>(descs_.Size(), 1), s);
+    dTiles_.Reset(std::max<size_t>(tiles_.Size(), 1), s);
+    dTileOut_.Reset(std::max<size_t>(tileOut_.Size(), 1), s);
+    if (descs_.Size() > 0) {
+        CudaCheck(cudaMemcpyAsync(dBatches_.Get(), descs_.Get(), sizeof(BatchDesc) * descs_.Size(),
+                      cudaMemcpyHostToDevice, s),
+            "upload batch descriptors");
+    }
+    if (tiles_.Size() > 0) {
+        CudaCheck(cudaMemcpyAsync(dTiles_.Get(), tiles_.Get(), sizeof(TileDesc) * tiles_.Size(),
+                      cudaMemcpyHostToDevice, s),
+            "upload tile descriptors");
+        CudaCheck(cudaMemcpyAsync(dTileOut_.Get(), tileOut_.Get(), sizeof(int64_t) * tileOut_.Size(),
+                      cudaMemcpyHostToDevice, s),
+            "upload tile offsets");
+    }
+}
+
+size_t NullBitmapBytes(int64_t rows) { return static_cast<size_t>(((rows + 31) / 32) * 4 + 8); }
+
+namespace {
+std::atomic<long long> g_waitBudget{0};
+}
+long long WaitBudget()
+{
+    const long long b = g_waitBudget.load();
+    return b > 0 ? b : kDefaultWaitBudget;
+}
+void SetWaitBudget(long long ticks) { g_waitBudget.store(ticks); }
+
+std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows, int32_t rowsPerBatch)
+{
+    std::vector<VectorBatch *> out;
+    if (rows <= 0) {
+        return out;
+    }
+    const int32_t step = AlignedBatchRows(rowsPerBatch);
+    for (int64_t r0 = 0; r0 < rows; r0 += step) {
+        const int32_t n = static_cast<int32_t>(std::min<int64_t>(step, rows - r0));
+        auto *b = new VectorBatch(n);
+        for (const auto &c : cols) {
+            const size_t vOff = static_cast<size_t>(r0) * c.width;
+            const size_t nOff = static_cast<size_t>(r0 / 8);
+            b->Append(new BaseVector(c.type, c.width, n, c.values, vOff, c.nulls, nOff, c.hasNull));
+        }
+        out.push_back(b);
+    }
+    return out;
+}
+
+std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int64_t rows, cudaStream_t s)
+{
+    std::vector<OutColumn> host;
+    for (const auto &c : cols) {
+        OutColumn h = c;
+        const size_t vb = static_cast<size_t>(rows) * c.width;
+        h.values = Buffer::NewHost(vb == 0 ? 16 : vb, false);
+        if (vb > 0) {
+            CudaCheck(cudaMemcpyAsync(h.values->Data(), c.values->Data(), vb, cudaMemcpyDeviceToHost, s),
+                "copy output values to host");
+        }
+        const size_t nb = NullBitmapBytes(rows);
+        if (c.nulls != nullptr && c.hasNull) {
+            h.nulls = Buffer::NewHost(nb, false);
+            CudaCheck(cudaMemcpyAsync(h.nulls->Data(), c.nulls->Data(), nb, cudaMemcpyDeviceToHost, s),
+                "copy output nulls to host");
+        } else {
+            h.nulls = Buffer::NewHost(nb, true);
+            h.hasNull = false;
+        }
+        host.push_back(h);
+    }
+    return host;
+}
+
+}  // namespace omg

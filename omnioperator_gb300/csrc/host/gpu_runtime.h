@@ -1,0 +1,159 @@
+// Host-side helpers for launching the operator kernels: error checks, streams, scratch
+// buffers and the batch/tile descriptor tables that let one launch cover many VectorBatches.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "kernels/plan.h"
+#include "omniop/memory.h"
+#include "omniop/types.h"
+#include "omniop/vector.h"
+
+namespace omg {
+
+using omniruntime::exception::OmniException;
+
+inline void CudaCheck(cudaError_t err, const char *what)
+{
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        throw OmniException("CUDA_ERROR", std::string(what) + ": " + cudaGetErrorString(err), -3);
+    }
+}
+
+inline void RequireDevice()
+{
+    if (!DeviceAvailable()) {
+        throw OmniException("CUDA_ERROR", "no CUDA device is available; the GB300 operators do not run on the CPU", -8);
+    }
+}
+
+// The stream an operator issues its work on: the caller's, or one it owns.
+class OpStream {
+public:
+    OpStream() = default;
+    ~OpStream()
+    {
+        if (own_ != nullptr) {
+            cudaStreamSynchronize(own_);
+            cudaStreamDestroy(own_);
+        }
+    }
+    OpStream(const OpStream &) = delete;
+    OpStream &operator=(const OpStream &) = delete;
+    void SetUser(void *s) { user_ = static_cast<cudaStream_t>(s); }
+    cudaStream_t Get()
+    {
+        if (user_ != nullptr) {
+            return user_;
+        }
+        if (own_ == nullptr) {
+            RequireDevice();
+            CudaCheck(cudaStreamCreateWithFlags(&own_, cudaStreamNonBlocking), "cudaStreamCreate");
+        }
+        return own_;
+    }
+    void Sync() { CudaCheck(cudaStreamSynchronize(Get()), "cudaStreamSynchronize"); }
+
+private:
+    cudaStream_t user_ = nullptr;
+    cudaStream_t own_ = nullptr;
+};
+
+// A device scratch allocation, stream-ordered.
+template <typename T> class DevArray {
+public:
+    DevArray() = default;
+    DevArray(size_t n, cudaStream_t s, bool zero = false) { Reset(n, s, zero); }
+    void Reset(size_t n, cudaStream_t s, bool zero = false)
+    {
+        n_ = n;
+        buf_ = Buffer::NewDevice(sizeof(T) * (n == 0 ? 1 : n), s, zero);
+    }
+    void Release() { buf_.reset(); n_ = 0; }
+    T *Get() const { return buf_ ? static_cast<T *>(buf_->Data()) : nullptr; }
+    size_t Size() const { return n_; }
+    const BufferPtr &Buf() const { return buf_; }
+
+private:
+    BufferPtr buf_;
+    size_t n_ = 0;
+};
+
+// Pinned host staging array (kept alive until the stream work that reads it has finished).
+template <typename T> class PinnedArray {
+public:
+    explicit PinnedArray(size_t n = 0) { Reset(n); }
+    void Reset(size_t n)
+    {
+        n_ = n;
+        buf_ = Buffer::NewHost(sizeof(T) * (n == 0 ? 1 : n), true);
+    }
+    T *Get() const { return static_cast<T *>(buf_->Data()); }
+    T &operator[](size_t i) { return Get()[i]; }
+    size_t Size() const { return n_; }
+
+private:
+    BufferPtr buf_;
+    size_t n_ = 0;
+};
+
+// Descriptors of a list of batches for one launch.  Kernel input i of batch b is column
+// inputCols[i] of the batch.
+class BatchTable {
+public:
+    void Build(const std::vector<omniruntime::vec::VectorBatch *> &batches, const std::vector<int32_t> &inputCols,
+        int32_t tileRows = kTileRows);
+    // Copy descriptors to the device on `s`.
+    void Upload(cudaStream_t s);
+    const BatchDesc *DeviceBatches() const { return dBatches_.Get(); }
+    const TileDesc *DeviceTiles() const { return dTiles_.Get(); }
+    const int64_t *DeviceTileOutRows() const { return dTileOut_.Get(); }
+    int32_t NumTiles() const { return static_cast<int32_t>(tiles_.Size()); }
+    int64_t TotalRows() const { return totalRows_; }
+    bool AnyNulls(int32_t input) const { return input < static_cast<int32_t>(anyNulls_.size()) && anyNulls_[input]; }
+
+private:
+    PinnedArray<BatchDesc> descs_;
+    PinnedArray<TileDesc> tiles_;
+    PinnedArray<int64_t> tileOut_;
+    DevArray<BatchDesc> dBatches_;
+    DevArray<TileDesc> dTiles_;
+    DevArray<int64_t> dTileOut_;
+    std::vector<bool> anyNulls_;
+    int64_t totalRows_ = 0;
+};
+
+// Round a row count per output batch down so every batch starts on a 64-row boundary,
+// which keeps every batch's null bitmap a byte-aligned view of one large bitmap.
+inline int32_t AlignedBatchRows(int32_t maxRows)
+{
+    return maxRows >= 128 ? (maxRows / 64) * 64 : maxRows;
+}
+
+size_t NullBitmapBytes(int64_t rows);
+
+// Budget of device-side bounded waits (clock64 ticks); 0 restores the default.
+long long WaitBudget();
+void SetWaitBudget(long long ticks);
+
+// Cut `rows` rows of contiguous output columns into VectorBatches of at most
+// `rowsPerBatch` rows that are views of the given buffers (host or device).
+struct OutColumn {
+    omniruntime::type::DataTypeId type;
+    int32_t width;
+    BufferPtr values;
+    BufferPtr nulls;  // may be null
+    bool hasNull;
+};
+std::vector<omniruntime::vec::VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows,
+    int32_t rowsPerBatch);
+
+// Copy device output columns to new pinned host buffers (one copy per column) on `s`.
+std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int64_t rows, cudaStream_t s);
+
+}  // namespace omg

@@ -1,0 +1,724 @@
+// HashAggregationOperatorFactory / HashAggregationOperator (see omniop/hash_aggregation.h).
+//
+// Plan compilation follows the reference's aggregator selection
+// (operator/aggregation/aggregation.cpp:20-88, aggregator/aggregator_factory.cpp:78-125):
+//  Spark policy (default):  SUM int -> wrapping int64 (sum_flatim_aggregator.h:33),
+//                           SUM decimal -> exact with sticky overflow (sum_spark_decimal_aggregator.h),
+//                           AVG -> double sum / count (average_flatim_aggregator.h:225-290);
+//  generic policy:          SUM int64 -> exact with sticky overflow (sum_aggregator.h:43-49).
+// COUNT, MIN and MAX are policy independent (count_*_aggregator.h, min/max_aggregator.h).
+#include "omniop/hash_aggregation.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cstring>
+#include <map>
+
+#include "host/gpu_runtime.h"
+#include "kernels/launch.h"
+
+namespace omniruntime {
+namespace op {
+
+using omg::AccSpec;
+using omg::CudaCheck;
+using omg::DevArray;
+using omg::OutSpec;
+using exception::OmniException;
+using namespace type;
+
+namespace {
+
+bool IsIntegerLike(DataTypeId id)
+{
+    switch (id) {
+        case OMNI_BYTE:
+        case OMNI_BOOLEAN:
+        case OMNI_SHORT:
+        case OMNI_INT:
+        case OMNI_LONG:
+        case OMNI_DATE32:
+        case OMNI_DATE64:
+        case OMNI_TIMESTAMP:
+        case OMNI_DECIMAL64:
+            return true;
+        default:
+            return false;
+    }
+}
+
+int64_t IntMaxForWidth(int w)
+{
+    switch (w) {
+        case 1:
+            return INT8_MAX;
+        case 2:
+            return INT16_MAX;
+        case 4:
+            return INT32_MAX;
+        default:
+            return INT64_MAX;
+    }
+}
+int64_t IntMinForWidth(int w)
+{
+    switch (w) {
+        case 1:
+            return INT8_MIN;
+        case 2:
+            return INT16_MIN;
+        case 4:
+            return INT32_MIN;
+        default:
+            return INT64_MIN;
+    }
+}
+
+int64_t OrderedBits(double x)
+{
+    int64_t b;
+    std::memcpy(&b, &x, sizeof(b));
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+
+uint64_t NextPow2(uint64_t v)
+{
+    uint64_t p = 1;
+    while (p < v) {
+        p <<= 1;
+    }
+    return p;
+}
+
+constexpr uint64_t kDefaultCapacity = uint64_t(1) << 16;
+constexpr int kGlobalMaxProbe = 96;
+constexpr int64_t kFlushRows = int64_t(1) << 25;     // aggregate at most 32M staged rows per launch
+constexpr size_t kSmemBudget = 200 * 1024;           // shared bytes per CTA for pre-aggregation
+
+}  // namespace
+
+// ------------------------------------------------------------------------------ factory
+HashAggregationOperatorFactory::HashAggregationOperatorFactory(std::vector<uint32_t> &groupByCol,
+    const DataTypes &groupInputTypes, std::vector<std::vector<uint32_t>> &aggsCols,
+    std::vector<DataTypes> &aggInputTypes, std::vector<DataTypes> &aggOutputTypes,
+    std::vector<uint32_t> &aggFuncTypes, std::vector<uint32_t> &maskColsVector, std::vector<bool> inputRaws,
+    std::vector<bool> outputPartials, bool overflowAsNull)
+    : groupByCols_(groupByCol), groupTypes_(groupInputTypes), aggCols_(aggsCols), aggInputTypes_(aggInputTypes),
+      aggOutputTypes_(aggOutputTypes), aggFuncTypes_(aggFuncTypes), maskCols_(maskColsVector),
+      inputRaws_(std::move(inputRaws)), outputPartials_(std::move(outputPartials)), overflowAsNull_(overflowAsNull),
+      policy_(GetSupportContainerVecRule())
+{}
+
+OmniStatus HashAggregationOperatorFactory::Init()
+{
+    if (inited_) {
+        return OMNI_STATUS_NORMAL;
+    }
+    const size_t nAgg = aggFuncTypes_.size();
+    if (groupByCols_.size() != static_cast<size_t>(groupTypes_.GetSize()) || groupByCols_.empty()) {
+        throw OmniException("INVALID_ARGUMENT", "group-by columns and types disagree", -1);
+    }
+    if (aggCols_.size() != nAgg || aggInputTypes_.size() != nAgg || aggOutputTypes_.size() != nAgg) {
+        throw OmniException("INVALID_ARGUMENT", "aggregator columns/types/functions disagree", -1);
+    }
+    for (uint32_t m : maskCols_) {
+        if (m != UINT32_MAX) {
+            throw OmniException("UNSUPPORTED_ERROR", "aggregation mask columns are not supported", -2);
+        }
+    }
+    for (size_t i = 0; i < inputRaws_.size(); ++i) {
+        if (!inputRaws_[i]) {
+            throw OmniException("UNSUPPORTED_ERROR", "final-stage (inputRaw=false) aggregation is not supported", -2);
+        }
+    }
+    for (size_t i = 0; i < outputPartials_.size(); ++i) {
+        if (outputPartials_[i]) {
+            throw OmniException("UNSUPPORTED_ERROR", "partial (outputPartial=true) aggregation is not supported", -2);
+        }
+    }
+    AggPlan &p = plan_;
+    p = AggPlan();
+    p.overflowAsNull = overflowAsNull_;
+    std::map<uint32_t, int32_t> inputOf;  // batch column -> kernel input
+    auto inputFor = [&](uint32_t col) {
+        auto it = inputOf.find(col);
+        if (it != inputOf.end()) {
+            return it->second;
+        }
+        const int32_t idx = static_cast<int32_t>(p.inputCols.size());
+        if (idx >= omg::kMaxInputs) {
+            throw OmniException("UNSUPPORTED_ERROR", "too many distinct input columns", -2);
+        }
+        p.inputCols.push_back(static_cast<int32_t>(col));
+        inputOf[col] = idx;
+        return idx;
+    };
+
+    // ---- key
+    const int nKey = static_cast<int>(groupByCols_.size());
+    if (nKey > omg::kMaxKeyCols) {
+        throw OmniException("UNSUPPORTED_ERROR", "at most 4 group-by columns are supported", -2);
+    }
+    std::memset(&p.key, 0, sizeof(p.key));
+    p.key.nCols = nKey;
+    int rowBytes = 0;
+    for (int i = 0; i < nKey; ++i) {
+        const auto &t = groupTypes_.GetType(i);
+        const int w = t->ByteWidth();
+        if (w == 0 || (w > 8 && w != 16)) {
+            throw OmniException("UNSUPPORTED_ERROR", "unsupported group-by type " + std::to_string(t->GetId()), -2);
+        }
+        p.key.cols[i].input = static_cast<int16_t>(inputFor(groupByCols_[i]));
+        p.key.cols[i].width = static_cast<int16_t>(w);
+        p.outTypes.push_back(t);
+        rowBytes += w;
+    }
+    if (nKey == 1 && p.key.cols[0].width <= 8) {
+        p.key.kind = omg::KEY_SINGLE;
+        p.key.words = 1;
+        p.keyWords = 1;
+    } else {
+        // Pack widest first at natural alignment so no value straddles a word.
+        std::vector<int> order(nKey);
+        for (int i = 0; i < nKey; ++i) {
+            order[i] = i;
+        }
+        std::stable_sort(order.begin(), order.end(),
+            [&](int a, int b) { return p.key.cols[a].width > p.key.cols[b].width; });
+        int off = 0;
+        for (int i : order) {
+            p.key.cols[i].byteOffset = static_cast<int16_t>(off);
+            off += p.key.cols[i].width;
+        }
+        p.key.maskByte = off;
+        const int bytes = off + 1;
+        if (bytes > 24) {
+            throw OmniException("UNSUPPORTED_ERROR", "packed group-by key wider than 23 bytes", -2);
+        }
+        p.key.kind = omg::KEY_PACKED;
+        p.key.words = (bytes + 7) / 8;
+        p.keyWords = 1 + p.key.words;  // tag + key words
+    }
+
+    // ---- accumulators
+    std::map<std::pair<int, int>, int> accOf;  // (kind, input) -> acc index
+    int word = 0;
+    auto accFor = [&](int kind, int input, int inKind, int inWidth, int64_t init) {
+        auto key = std::make_pair(kind, input);
+        auto it = accOf.find(key);
+        if (it != accOf.end()) {
+            return it->second;
+        }
+        if (static_cast<int>(p.accs.size()) >= omg::kMaxAccs) {
+            throw OmniException("UNSUPPORTED_ERROR", "too many aggregate states", -2);
+        }
+        AccSpec a{};
+        a.kind = static_cast<int16_t>(kind);
+        a.input = static_cast<int16_t>(input);
+        a.inKind = static_cast<int16_t>(inKind);
+        a.inWidth = static_cast<int16_t>(inWidth);
+        a.word = word;
+        a.init = init;
+        word += omg::AccWords(kind);
+        p.accs.push_back(a);
+        const int idx = static_cast<int>(p.accs.size()) - 1;
+        accOf[key] = idx;
+        return idx;
+    };
+    accFor(omg::ACC_COUNT_ALL, -1, omg::IN_NONE, 0, 0);  // always accs[0]
+
+    // Output key columns.
+    for (int i = 0; i < nKey; ++i) {
+        OutSpec o{};
+        o.kind = omg::OUT_KEY;
+        o.src = static_cast<int16_t>(i);
+        o.countAcc = -1;
+        o.outWidth = p.key.cols[i].width;
+        o.outType = static_cast<int16_t>(groupTypes_.GetType(i)->GetId());
+        p.outs.push_back(o);
+    }
+    int exactIndex = 0;
+    const bool spark = policy_ == SupportContainerVecRule::NOT_SUPPORT;
+    for (size_t a = 0; a < nAgg; ++a) {
+        const uint32_t fn = aggFuncTypes_[a];
+        const auto &outTypes = aggOutputTypes_[a];
+        if (outTypes.GetSize() != 1) {
+            throw OmniException("UNSUPPORTED_ERROR", "aggregators with several output columns are not supported", -2);
+        }
+        const DataTypePtr &outT = outTypes.GetType(0);
+        OutSpec o{};
+        o.outType = static_cast<int16_t>(outT->GetId());
+        o.outWidth = static_cast<int16_t>(outT->ByteWidth());
+        o.countAcc = -1;
+        if (fn == OMNI_AGGREGATION_TYPE_COUNT_ALL) {
+            o.kind = omg::OUT_COUNT;
+            o.src = 0;
+            p.outs.push_back(o);
+            p.outTypes.push_back(outT);
+            rowBytes += o.outWidth;
+            continue;
+        }
+        if (aggCols_[a].size() != 1 || aggInputTypes_[a].GetSize() != 1) {
+            throw OmniException("UNSUPPORTED_ERROR", "aggregator must read exactly one column", -2);
+        }
+        const DataTypePtr &inT = aggInputTypes_[a].GetType(0);
+        const DataTypeId inId = inT->GetId();
+        const int inW = inT->ByteWidth();
+        const int input = inputFor(aggCols_[a][0]);
+        const int nulls = accFor(omg::ACC_NULLS, input, omg::IN_NONE, 0, 0);
+        o.countAcc = static_cast<int16_t>(nulls);
+        const bool isInt = IsIntegerLike(inId);
+        const bool isDouble = inId == OMNI_DOUBLE || inId == OMNI_FLOAT;
+        const int inKind = inId == OMNI_DOUBLE ? omg::IN_DOUBLE
+                                               : (inId == OMNI_FLOAT ? omg::IN_FLOAT
+                                                                     : (inId == OMNI_DECIMAL128 ? omg::IN_DEC128 : omg::IN_INT));
+        switch (fn) {
+            case OMNI_AGGREGATION_TYPE_COUNT_COLUMN:
+                o.kind = omg::OUT_COUNT;
+                o.src = 0;
+                break;
+            case OMNI_AGGREGATION_TYPE_SUM: {
+                if (isDouble) {
+                    o.kind = omg::OUT_SUM_DOUBLE;
+                    o.src = static_cast<int16_t>(accFor(omg::ACC_DSUM, input, inKind, inW, 0));
+                } else if (inId == OMNI_DECIMAL64 || inId == OMNI_DECIMAL128) {
+                    o.kind = omg::OUT_SUM_EXACT;
+                    const int kind = inId == OMNI_DECIMAL128 ? omg::ACC_WSUM3 : omg::ACC_WSUM2;
+                    o.src = static_cast<int16_t>(accFor(kind, input, inKind, inW, 0));
+                    o.boundKind = outT->GetId() == OMNI_DECIMAL128 ? 1 : 0;
+                    const int diff = outT->GetScale() - inT->GetScale();
+                    if (diff < 0 || diff > 38) {
+                        throw OmniException("UNSUPPORTED_ERROR", "decimal SUM output scale below input scale", -2);
+                    }
+                    o.rescalePow = static_cast<int16_t>(diff);
+                    o.pad = static_cast<int16_t>(exactIndex++);
+                } else if (isInt) {
+                    // SumOp checks overflow only for int64 inputs (sum_aggregator.h:36-60), so
+                    // narrower inputs wrap under either policy.
+                    if (spark || inW != 8) {
+                        o.kind = omg::OUT_SUM_WRAP;
+                        o.src = static_cast<int16_t>(accFor(omg::ACC_ISUM, input, inKind, inW, 0));
+                    } else {
+                        o.kind = omg::OUT_SUM_EXACT;
+                        o.src = static_cast<int16_t>(accFor(omg::ACC_WSUM2, input, inKind, inW, 0));
+                        o.boundKind = 0;
+                        o.pad = static_cast<int16_t>(exactIndex++);
+                    }
+                } else {
+                    throw OmniException("UNSUPPORTED_ERROR", "unsupported SUM input type " + std::to_string(inId), -2);
+                }
+                break;
+            }
+            case OMNI_AGGREGATION_TYPE_AVG: {
+                if (!isInt && !isDouble) {
+                    throw OmniException("UNSUPPORTED_ERROR", "unsupported AVG input type " + std::to_string(inId), -2);
+                }
+                if (inId == OMNI_DECIMAL64) {
+                    throw OmniException("UNSUPPORTED_ERROR", "decimal AVG is not supported", -2);
+                }
+                o.kind = omg::OUT_AVG;
+                o.src = static_cast<int16_t>(accFor(omg::ACC_DSUM, input, inKind, inW, 0));
+                break;
+            }
+            case OMNI_AGGREGATION_TYPE_MIN:
+            case OMNI_AGGREGATION_TYPE_MAX: {
+                const bool isMin = fn == OMNI_AGGREGATION_TYPE_MIN;
+                if (isInt) {
+                    const int outW = o.outWidth;
+                    o.kind = isMin ? omg::OUT_MIN_INT : omg::OUT_MAX_INT;
+                    o.src = static_cast<int16_t>(accFor(isMin ? omg::ACC_IMIN : omg::ACC_IMAX, input, inKind, inW,
+                        isMin ? IntMaxForWidth(outW) : IntMinForWidth(outW)));
+                } else if (isDouble) {
+                    const double lim = inId == OMNI_FLOAT ? static_cast<double>(FLT_MAX) : DBL_MAX;
+                    o.kind = isMin ? omg::OUT_MIN_DOUBLE : omg::OUT_MAX_DOUBLE;
+                    o.src = static_cast<int16_t>(accFor(isMin ? omg::ACC_DMIN : omg::ACC_DMAX, input, inKind, inW,
+                        OrderedBits(isMin ? lim : -lim)));
+                } else {
+                    throw OmniException("UNSUPPORTED_ERROR", "unsupported MIN/MAX input type " + std::to_string(inId), -2);
+                }
+                break;
+            }
+            default:
+                throw OmniException("UNSUPPORTED_ERROR", "No such agg func type " + std::to_string(fn), -2);
+        }
+        p.outs.push_back(o);
+        p.outTypes.push_back(outT);
+        rowBytes += o.outWidth;
+    }
+    if (p.outs.size() > static_cast<size_t>(omg::kMaxOutCols)) {
+        throw OmniException("UNSUPPORTED_ERROR", "too many output columns", -2);
+    }
+    if (exactIndex > 8) {
+        throw OmniException("UNSUPPORTED_ERROR", "at most 8 exact SUM columns", -2);
+    }
+    p.orderDependent = exactIndex > 0;
+    p.stateWords = word;
+    p.slotWords = p.keyWords + p.stateWords;
+    p.rowsPerBatch = GetMaxRowCount(rowBytes);
+    inited_ = true;
+    return OMNI_STATUS_NORMAL;
+}
+
+Operator *HashAggregationOperatorFactory::CreateOperator()
+{
+    Init();
+    return new HashAggregationOperator(plan_);
+}
+
+// ------------------------------------------------------------------------------ operator
+struct HashAggregationOperator::Impl {
+    omg::OpStream stream;
+    DevArray<uint64_t> slots;
+    DevArray<uint32_t> special;
+    // stats[0] = groupCount, [1] = nRetry, [2] = nSpill, [3] = error
+    DevArray<unsigned long long> stats;
+    uint64_t capacity = 0;
+    uint64_t groups = 0;
+    // Batches kept for the ordered sticky-overflow path (order-dependent plans only).
+    std::vector<VectorBatch *> retained;
+};
+
+HashAggregationOperator::HashAggregationOperator(const AggPlan &plan) : plan_(plan), impl_(new Impl()) {}
+
+HashAggregationOperator::~HashAggregationOperator()
+{
+    Close();
+}
+
+OmniStatus HashAggregationOperator::Close()
+{
+    ReleasePending();
+    for (auto *b : impl_->retained) {
+        vec::VectorHelper::FreeVecBatch(b);
+    }
+    impl_->retained.clear();
+    for (auto *b : outputs_) {
+        vec::VectorHelper::FreeVecBatch(b);
+    }
+    outputs_.clear();
+    return OMNI_STATUS_NORMAL;
+}
+
+void HashAggregationOperator::ReleasePending()
+{
+    for (auto *b : pending_) {
+        vec::VectorHelper::FreeVecBatch(b);
+    }
+    pending_.clear();
+    pendingRows_ = 0;
+}
+
+int32_t HashAggregationOperator::AddInput(VectorBatch *vecBatch)
+{
+    hasInputedData_ = true;
+    if (vecBatch == nullptr) {
+        throw OmniException("INVALID_ARGUMENT", "AddInput of a null batch", -1);
+    }
+    if (vecBatch->GetRowCount() <= 0) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+        return 0;
+    }
+    for (int32_t c : plan_.inputCols) {
+        if (c >= vecBatch->GetVectorCount()) {
+            vec::VectorHelper::FreeVecBatch(vecBatch);
+            throw OmniException("OPERATOR_RUNTIME_ERROR", "input batch lacks column " + std::to_string(c), -1);
+        }
+    }
+    if (extracted_) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "AddInput after GetOutput started", -6);
+    }
+    pending_.push_back(vecBatch);
+    pendingRows_ += vecBatch->GetRowCount();
+    if (pendingRows_ >= kFlushRows) {
+        Flush();
+    }
+    return 0;
+}
+
+namespace {
+omg::AggLaunch MakeLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacity, uint32_t *special,
+    unsigned long long *stats)
+{
+    omg::AggLaunch p;
+    std::memset(&p, 0, sizeof(p));
+    p.key = plan.key;
+    p.nAccs = static_cast<int32_t>(plan.accs.size());
+    for (int i = 0; i < p.nAccs; ++i) {
+        p.accs[i] = plan.accs[i];
+    }
+    p.stateWords = plan.stateWords;
+    p.maxProbe = kGlobalMaxProbe;
+    p.table.slots = slots;
+    p.table.capacity = capacity;
+    p.table.slotWords = plan.slotWords;
+    p.table.keyWords = plan.keyWords;
+    p.table.specialUsed = special;
+    p.table.groupCount = stats;
+    p.nRetry = reinterpret_cast<unsigned int *>(stats + 1);
+    p.error = reinterpret_cast<int32_t *>(stats + 3);
+    p.waitBudget = omg::WaitBudget();
+    return p;
+}
+}  // namespace
+
+void HashAggregationOperator::Flush()
+{
+    if (pending_.empty()) {
+        return;
+    }
+    omg::RequireDevice();
+    Impl &im = *impl_;
+    im.stream.SetUser(userStream_);
+    cudaStream_t s = im.stream.Get();
+    if (im.stats.Get() == nullptr) {
+        im.stats.Reset(8, s, true);
+    }
+    // Create the table on first use.
+    if (im.capacity == 0) {
+        uint64_t cap = capacityHint_ > 0 ? NextPow2(static_cast<uint64_t>(capacityHint_) * 2) : kDefaultCapacity;
+        cap = std::max<uint64_t>(cap, 1024);
+        im.slots.Reset((cap + 2) * plan_.slotWords, s);
+        im.special.Reset(2, s, true);
+        im.capacity = cap;
+        omg::AggLaunch init = MakeLaunch(plan_, im.slots.Get(), cap, im.special.Get(), im.stats.Get());
+        CudaCheck(omg::LaunchAggInitTable(init, s), "init aggregation table");
+        ++counters_[0];
+    }
+    omg::BatchTable bt;
+    bt.Build(pending_, plan_.inputCols);
+    bt.Upload(s);
+    const int64_t rows = bt.TotalRows();
+
+    const int sms = omg::DeviceSMCount();
+    int smemSlots = 0;
+    if (strategy_ != 2) {  // OMG_AGG_STRATEGY_GLOBAL
+        smemSlots = static_cast<int>(kSmemBudget / (plan_.slotWords * sizeof(uint64_t)));
+    }
+    const int grid = smemSlots > 0 ? sms : sms * 4;
+    DevArray<unsigned long long> retryA(static_cast<size_t>(rows), s);
+    DevArray<unsigned long long> retryB;
+    const size_t spillCap = static_cast<size_t>(smemSlots) * grid;
+    DevArray<uint64_t> spillA(std::max<size_t>(spillCap, 1) * plan_.slotWords, s);
+    DevArray<uint64_t> spillB;
+    CudaCheck(cudaMemsetAsync(im.stats.Get() + 1, 0, 3 * sizeof(unsigned long long), s), "reset stats");
+
+    omg::AggLaunch p = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
+    p.batches = bt.DeviceBatches();
+    p.tiles = bt.DeviceTiles();
+    p.nTiles = bt.NumTiles();
+    p.retry = retryA.Get();
+    p.retryCap = static_cast<uint32_t>(rows);
+    p.smemSlots = smemSlots;
+    unsigned int *nSpill = reinterpret_cast<unsigned int *>(im.stats.Get() + 2);
+    CudaCheck(omg::LaunchAgg(p, spillA.Get(), nSpill, static_cast<uint32_t>(spillCap), nullptr, 0, grid, s),
+        "aggregation kernel");
+    ++counters_[0];
+    unsigned long long h[4];
+    CudaCheck(cudaMemcpyAsync(h, im.stats.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read stats");
+    im.stream.Sync();
+    uint64_t nRetry = static_cast<unsigned int>(h[1]);
+    uint64_t nSpillH = static_cast<unsigned int>(h[2]);
+    int32_t err = static_cast<int32_t>(h[3]);
+    if (err != 0) {
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "aggregation kernel error " + std::to_string(err),
+            err == 7 ? -7 : -9);
+    }
+    im.groups = h[0];
+    // Exact resize path: grow the table and re-run the rows (and partial states) that could
+    // not be placed.  Each round at least doubles the capacity.
+    while (nRetry > 0 || nSpillH > 0) {
+        const uint64_t need = NextPow2(std::max<uint64_t>(im.capacity * 2, 2 * (im.groups + nRetry + nSpillH)));
+        DevArray<uint64_t> newSlots((need + 2) * plan_.slotWords, s);
+        DevArray<uint32_t> newSpecial(2, s, true);
+        omg::AggLaunch to = MakeLaunch(plan_, newSlots.Get(), need, newSpecial.Get(), im.stats.Get());
+        CudaCheck(omg::LaunchAggInitTable(to, s), "init grown table");
+        omg::AggLaunch from = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
+        CudaCheck(omg::LaunchAggRehash(to, from.table, to.table, s), "rehash");
+        im.slots = newSlots;
+        im.special = newSpecial;
+        im.capacity = need;
+        ++counters_[1];
+        counters_[2] += static_cast<int64_t>(nRetry);
+        retryB.Reset(std::max<uint64_t>(nRetry, 1), s);
+        spillB.Reset(std::max<uint64_t>(nSpillH, 1) * plan_.slotWords, s);
+        CudaCheck(cudaMemsetAsync(im.stats.Get() + 1, 0, 3 * sizeof(unsigned long long), s), "reset stats");
+        omg::AggLaunch r = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
+        r.batches = bt.DeviceBatches();
+        r.retry = retryB.Get();
+        r.retryCap = static_cast<uint32_t>(std::max<uint64_t>(nRetry, 1));
+        r.retryIn = retryA.Get();
+        r.nRetryIn = static_cast<uint32_t>(nRetry);
+        const int rgrid = static_cast<int>(std::min<uint64_t>((nRetry + nSpillH + 511) / 512 + 1, sms * 8ull));
+        CudaCheck(omg::LaunchAgg(r, spillB.Get(), nSpill, static_cast<uint32_t>(std::max<uint64_t>(nSpillH, 1)),
+                      spillA.Get(), static_cast<uint32_t>(nSpillH), rgrid, s),
+            "aggregation retry kernel");
+        ++counters_[0];
+        CudaCheck(cudaMemcpyAsync(h, im.stats.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read stats");
+        im.stream.Sync();
+        std::swap(retryA, retryB);
+        std::swap(spillA, spillB);
+        nRetry = static_cast<unsigned int>(h[1]);
+        nSpillH = static_cast<unsigned int>(h[2]);
+        err = static_cast<int32_t>(h[3]);
+        im.groups = h[0];
+        if (err != 0) {
+            throw OmniException("OPERATOR_RUNTIME_ERROR", "aggregation retry error " + std::to_string(err), -9);
+        }
+    }
+    // Keep the load factor under one half for the next batches (the reference grows x4).
+    if (im.groups * 2 > im.capacity) {
+        const uint64_t need = NextPow2(im.groups * 4);
+        DevArray<uint64_t> newSlots((need + 2) * plan_.slotWords, s);
+        DevArray<uint32_t> newSpecial(2, s, true);
+        omg::AggLaunch to = MakeLaunch(plan_, newSlots.Get(), need, newSpecial.Get(), im.stats.Get());
+        CudaCheck(omg::LaunchAggInitTable(to, s), "init grown table");
+        omg::AggLaunch from = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
+        CudaCheck(omg::LaunchAggRehash(to, from.table, to.table, s), "rehash");
+        im.slots = newSlots;
+        im.special = newSpecial;
+        im.capacity = need;
+        ++counters_[1];
+        im.stream.Sync();
+    }
+    counters_[3] = static_cast<int64_t>(im.groups);
+    if (plan_.orderDependent) {
+        for (auto *b : pending_) {
+            im.retained.push_back(b);
+        }
+        pending_.clear();
+        pendingRows_ = 0;
+    } else {
+        ReleasePending();
+    }
+}
+
+void HashAggregationOperator::Extract()
+{
+    Flush();
+    Impl &im = *impl_;
+    if (im.capacity == 0) {
+        uniqueKeys_ = 0;
+        return;
+    }
+    im.stream.SetUser(userStream_);
+    cudaStream_t s = im.stream.Get();
+    omg::AggLaunch base = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
+    DevArray<unsigned long long> cnt(4, s, true);
+    CudaCheck(omg::LaunchAggCount(base.table, plan_.key.kind, cnt.Get(), s), "count groups");
+    unsigned long long nGroups = 0;
+    CudaCheck(cudaMemcpyAsync(&nGroups, cnt.Get(), sizeof(nGroups), cudaMemcpyDeviceToHost, s), "read group count");
+    im.stream.Sync();
+    uniqueKeys_ = nGroups;
+    counters_[3] = static_cast<int64_t>(nGroups);
+    if (nGroups == 0) {
+        return;
+    }
+    const size_t nOut = plan_.outs.size();
+    std::vector<omg::OutColumn> cols(nOut);
+    for (size_t o = 0; o < nOut; ++o) {
+        const OutSpec &os = plan_.outs[o];
+        cols[o].type = plan_.outTypes[o]->GetId();
+        cols[o].width = os.outWidth;
+        cols[o].values = omg::Buffer::NewDevice(static_cast<size_t>(nGroups) * os.outWidth + 16, s, false);
+        cols[o].nulls = omg::Buffer::NewDevice(omg::NullBitmapBytes(static_cast<int64_t>(nGroups)), s, true);
+        cols[o].hasNull = os.kind != omg::OUT_COUNT;
+    }
+    omg::AggExtract e;
+    std::memset(&e, 0, sizeof(e));
+    e.table = base.table;
+    e.key = plan_.key;
+    e.nAccs = static_cast<int32_t>(plan_.accs.size());
+    for (int i = 0; i < e.nAccs; ++i) {
+        e.accs[i] = plan_.accs[i];
+    }
+    e.nOut = static_cast<int32_t>(nOut);
+    for (size_t o = 0; o < nOut; ++o) {
+        e.out[o] = plan_.outs[o];
+        e.out[o].values = cols[o].values->Data();
+        e.out[o].nulls = static_cast<uint8_t *>(cols[o].nulls->Data());
+    }
+    e.overflowAsNull = plan_.overflowAsNull ? 1 : 0;
+    // cnt[0] = nGroups (reused as outCount after reset), cnt[1] = error, cnt[2] = nAmbiguous
+    const uint32_t ambCap = static_cast<uint32_t>(std::min<unsigned long long>(nGroups, 1ull << 22));
+    DevArray<unsigned long long> ambSlots(ambCap, s);
+    CudaCheck(cudaMemsetAsync(cnt.Get(), 0, 4 * sizeof(unsigned long long), s), "reset counters");
+    e.outCount = cnt.Get();
+    e.error = reinterpret_cast<int32_t *>(cnt.Get() + 1);
+    e.nAmbiguous = cnt.Get() + 2;
+    e.ambiguousSlots = ambSlots.Get();
+    e.ambiguousCap = ambCap;
+    CudaCheck(omg::LaunchAggExtract(e, s), "extract groups");
+    ++counters_[0];
+    unsigned long long hc[4];
+    CudaCheck(cudaMemcpyAsync(hc, cnt.Get(), sizeof(hc), cudaMemcpyDeviceToHost, s), "read extract counters");
+    im.stream.Sync();
+    if (hc[2] > 0) {
+        // Some groups' sticky-overflow outcome depends on row order: replay those groups in
+        // arrival order over the retained batches, then extract again with the answers.
+        if (hc[2] > ambCap) {
+            throw OmniException("UNSUPPORTED_ERROR", "too many order-dependent overflow groups", -2);
+        }
+        counters_[4] = static_cast<int64_t>(hc[2]);
+        omg::BatchTable bt;
+        bt.Build(im.retained, plan_.inputCols, 1 << 30);
+        bt.Upload(s);
+        DevArray<uint8_t> forced(im.capacity + 2, s, true);
+        omg::AggLaunch p = base;
+        p.batches = bt.DeviceBatches();
+        CudaCheck(omg::LaunchAggOrdered(p, static_cast<int32_t>(im.retained.size()), e, ambSlots.Get(),
+                      static_cast<uint32_t>(hc[2]), forced.Get(), s),
+            "ordered overflow replay");
+        for (size_t o = 0; o < nOut; ++o) {
+            CudaCheck(cudaMemsetAsync(cols[o].nulls->Data(), 0, cols[o].nulls->Bytes(), s), "reset nulls");
+        }
+        CudaCheck(cudaMemsetAsync(cnt.Get(), 0, 4 * sizeof(unsigned long long), s), "reset counters");
+        e.forcedOverflow = forced.Get();
+        CudaCheck(omg::LaunchAggExtract(e, s), "extract groups");
+        counters_[0] += 2;
+        CudaCheck(cudaMemcpyAsync(hc, cnt.Get(), sizeof(hc), cudaMemcpyDeviceToHost, s), "read extract counters");
+        im.stream.Sync();
+    }
+    if (hc[1] != 0) {
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "sum_aggregator overflow.", -5);
+    }
+    const int64_t rows = static_cast<int64_t>(hc[0]);
+    std::vector<omg::OutColumn> outCols = cols;
+    if (!deviceOutput_) {
+        outCols = omg::CopyColumnsToHost(cols, rows, s);
+        im.stream.Sync();
+        for (auto &c : outCols) {
+            c.hasNull = false;  // host vectors: HasNull() scans the bitmap
+        }
+    }
+    for (auto *b : omg::CarveBatches(outCols, rows, plan_.rowsPerBatch)) {
+        outputs_.push_back(b);
+    }
+    counters_[5] = rows;
+}
+
+int32_t HashAggregationOperator::GetOutput(VectorBatch **outputVecBatch)
+{
+    *outputVecBatch = nullptr;
+    if (!hasInputedData_) {
+        return 0;
+    }
+    if (!extracted_) {
+        extracted_ = true;
+        Extract();
+    }
+    if (outputs_.empty()) {
+        SetStatus(OMNI_STATUS_FINISHED);
+        return 0;
+    }
+    *outputVecBatch = outputs_.front();
+    outputs_.pop_front();
+    if (outputs_.empty()) {
+        SetStatus(OMNI_STATUS_FINISHED);
+    }
+    return 1;
+}
+
+}  // namespace op
+}  // namespace omniruntime

@@ -1,0 +1,532 @@
+// HashBuilder / LookupJoin operators (see omniop/hash_join.h).
+#include "omniop/hash_join.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+#include "host/gpu_runtime.h"
+#include "kernels/launch.h"
+
+namespace omniruntime {
+namespace op {
+
+using exception::OmniException;
+using omg::CudaCheck;
+using omg::DevArray;
+using namespace type;
+
+namespace {
+constexpr int64_t kProbeChunkRows = int64_t(1) << 22;  // pipelined callers: probe 4M rows per launch
+
+uint64_t NextPow2(uint64_t v)
+{
+    uint64_t p = 1;
+    while (p < v) {
+        p <<= 1;
+    }
+    return p;
+}
+
+bool JoinKeyType(DataTypeId id)
+{
+    switch (id) {
+        case OMNI_BYTE:
+        case OMNI_SHORT:
+        case OMNI_INT:
+        case OMNI_LONG:
+        case OMNI_DATE32:
+        case OMNI_DATE64:
+        case OMNI_TIMESTAMP:
+        case OMNI_DECIMAL64:
+            return true;
+        default:
+            return false;
+    }
+}
+}  // namespace
+
+// Device-side build: contiguous build columns plus the ARRAY or HASH table.
+struct JoinBuildState {
+    JoinType joinType;
+    DataTypes buildTypes;
+    std::vector<int32_t> hashCols;
+    int32_t operatorCount;
+    int32_t operatorIndex = 0;
+    int32_t finished = 0;
+    bool built = false;
+    std::mutex mu;
+    std::vector<vec::VectorBatch *> batches;  // retained until the factory is destroyed
+    omg::OpStream stream;
+    int64_t rows = 0;
+    std::vector<DevArray<uint8_t>> colValues;
+    std::vector<DevArray<uint8_t>> colNulls;
+    std::vector<bool> colHasNull;
+    DevArray<int64_t> entries;
+    DevArray<uint64_t> hashKeys;
+    DevArray<int32_t> csr;
+    omg::JoinTable table{};
+    uint32_t maxDup = 0;
+
+    ~JoinBuildState()
+    {
+        for (auto *b : batches) {
+            vec::VectorHelper::FreeVecBatch(b);
+        }
+    }
+
+    void Build();
+};
+
+void JoinBuildState::Build()
+{
+    omg::RequireDevice();
+    cudaStream_t s = stream.Get();
+    std::memset(&table, 0, sizeof(table));
+    table.mode = omg::JOIN_ARRAY;
+    table.unique = 1;
+    table.sentinelEntry = -1;
+    rows = 0;
+    for (auto *b : batches) {
+        rows += b->GetRowCount();
+    }
+    const int nCols = buildTypes.GetSize();
+    colValues.assign(nCols, DevArray<uint8_t>());
+    colNulls.assign(nCols, DevArray<uint8_t>());
+    colHasNull.assign(nCols, false);
+    const int32_t keyCol = hashCols[0];
+    const int32_t keyWidth = buildTypes.GetType(keyCol)->ByteWidth();
+    table.keyWidth = keyWidth;
+    // Gather every build column into one contiguous HBM array (reading host-pinned or
+    // device batches directly).
+    for (int c = 0; c < nCols; ++c) {
+        const int w = buildTypes.GetType(c)->ByteWidth();
+        if (w <= 0) {
+            throw OmniException("UNSUPPORTED_ERROR", "unsupported build column type", -2);
+        }
+        colValues[c].Reset(static_cast<size_t>(rows) * w + 16, s);
+        if (rows == 0) {
+            continue;
+        }
+        omg::BatchTable bt;
+        bt.Build(batches, {c});
+        bt.Upload(s);
+        if (bt.AnyNulls(0)) {
+            colHasNull[c] = true;
+            colNulls[c].Reset(omg::NullBitmapBytes(rows), s, true);
+        }
+        CudaCheck(omg::LaunchGatherColumn(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(), bt.DeviceTileOutRows(),
+                      0, w, colValues[c].Get(), colHasNull[c] ? colNulls[c].Get() : nullptr, s),
+            "gather build column");
+        stream.Sync();  // the batch table's staging must outlive the copy
+    }
+    if (rows == 0) {
+        built = true;
+        return;
+    }
+    const void *keys = colValues[keyCol].Get();
+    const uint8_t *keyNulls = colHasNull[keyCol] ? colNulls[keyCol].Get() : nullptr;
+    DevArray<long long> stats(8, s, true);
+    CudaCheck(omg::LaunchKeyStats(keys, keyNulls, rows, keyWidth, stats.Get(), s), "key stats");
+    long long h[3];
+    CudaCheck(cudaMemcpyAsync(h, stats.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read key stats");
+    stream.Sync();
+    const int64_t nonNull = h[2];
+    if (nonNull == 0) {
+        built = true;
+        return;
+    }
+    table.minKey = h[0];
+    const uint64_t range = static_cast<uint64_t>(h[1]) - static_cast<uint64_t>(h[0]) + 1;
+    const bool arrayMode = range != 0 && range <= std::max<uint64_t>(2 * NextPow2(nonNull), 1024) &&
+        range <= (uint64_t(1) << 31);
+    DevArray<int32_t> err(4, s, true);
+    unsigned int *maxCount = reinterpret_cast<unsigned int *>(stats.Get() + 3);
+    uint32_t *sentinelCount = reinterpret_cast<uint32_t *>(stats.Get() + 4);
+    unsigned int *sentinelCursor = reinterpret_cast<unsigned int *>(stats.Get() + 5);
+    int64_t *sentinelEntry = reinterpret_cast<int64_t *>(stats.Get() + 6);
+    CudaCheck(cudaMemsetAsync(stats.Get() + 3, 0, 3 * sizeof(long long), s), "reset");
+    CudaCheck(omg::LaunchFillI64(sentinelEntry, -1, 1, s), "reset");
+    uint64_t n;
+    if (arrayMode) {
+        table.mode = omg::JOIN_ARRAY;
+        table.range = range;
+        n = range;
+    } else {
+        table.mode = omg::JOIN_HASH;
+        table.capacity = std::max<uint64_t>(NextPow2(2 * static_cast<uint64_t>(nonNull)), 1024);
+        n = table.capacity;
+        hashKeys.Reset(n, s);
+        CudaCheck(omg::LaunchFillU64(hashKeys.Get(), omg::kEmptyKey, static_cast<int64_t>(n), s), "init hash keys");
+    }
+    DevArray<uint32_t> counts(n, s, true);
+    CudaCheck(omg::LaunchBuildCount(table, keys, keyNulls, rows, keyWidth, hashKeys.Get(), counts.Get(), sentinelCount,
+                  maxCount, err.Get(), s),
+        "build count");
+    long long h2[3];
+    CudaCheck(cudaMemcpyAsync(h2, stats.Get() + 3, sizeof(h2), cudaMemcpyDeviceToHost, s), "read build stats");
+    int32_t herr = 0;
+    CudaCheck(cudaMemcpyAsync(&herr, err.Get(), sizeof(herr), cudaMemcpyDeviceToHost, s), "read error");
+    stream.Sync();
+    if (herr != 0) {
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "join build failed", -9);
+    }
+    maxDup = static_cast<uint32_t>(h2[0] & 0xffffffffll);
+    const uint32_t nSentinel = static_cast<uint32_t>(h2[1] & 0xffffffffll);
+    table.unique = (maxDup <= 1 && nSentinel <= 1) ? 1 : 0;
+    entries.Reset(n, s);
+    CudaCheck(omg::LaunchFillI64(entries.Get(), -1, static_cast<int64_t>(n), s), "init entries");
+    DevArray<int64_t> offsets;
+    DevArray<uint32_t> cursor;
+    int64_t total = 0;
+    if (!table.unique) {
+        offsets.Reset(n, s);
+        DevArray<int64_t> blockSums((n + 1023) / 1024 + 1, s);
+        DevArray<long long> tot(1, s, true);
+        CudaCheck(omg::LaunchScanCounts(counts.Get(), static_cast<int64_t>(n), offsets.Get(), blockSums.Get(), tot.Get(), s),
+            "scan counts");
+        long long ht = 0;
+        CudaCheck(cudaMemcpyAsync(&ht, tot.Get(), sizeof(ht), cudaMemcpyDeviceToHost, s), "read total");
+        stream.Sync();
+        total = ht;
+        csr.Reset(static_cast<size_t>(total + nSentinel + 1), s);
+        cursor.Reset(n, s, true);
+    }
+    table.arrayEntries = entries.Get();
+    table.hashEntries = entries.Get();
+    table.hashKeys = hashKeys.Get();
+    CudaCheck(omg::LaunchBuildFill(table, keys, keyNulls, rows, keyWidth, counts.Get(), offsets.Get(), cursor.Get(),
+                  entries.Get(), csr.Get(), nSentinel, total, sentinelCursor, sentinelEntry, err.Get(), s),
+        "build fill");
+    int64_t hs = -1;
+    CudaCheck(cudaMemcpyAsync(&hs, sentinelEntry, sizeof(hs), cudaMemcpyDeviceToHost, s), "read sentinel");
+    CudaCheck(cudaMemcpyAsync(&herr, err.Get(), sizeof(herr), cudaMemcpyDeviceToHost, s), "read error");
+    stream.Sync();
+    if (herr != 0) {
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "join build failed", -9);
+    }
+    if (table.unique) {
+        table.sentinelEntry = hs;
+    } else {
+        table.sentinelEntry = nSentinel > 0 ? ((total << 32) | static_cast<int64_t>(nSentinel)) : -1;
+    }
+    table.csrRows = csr.Get();
+    built = true;
+}
+
+// ------------------------------------------------------------------------------ builder
+HashBuilderOperatorFactory::HashBuilderOperatorFactory(JoinType joinType, const DataTypes &buildTypes,
+    const int32_t *buildHashCols, int32_t buildHashColsCount, int32_t operatorCount)
+    : state_(new JoinBuildState())
+{
+    if (joinType != OMNI_JOIN_TYPE_INNER) {
+        throw OmniException("UNSUPPORTED_ERROR", "only inner joins are supported", -2);
+    }
+    if (buildHashColsCount != 1 || buildHashCols == nullptr) {
+        throw OmniException("UNSUPPORTED_ERROR", "only single-column join keys are supported", -2);
+    }
+    if (operatorCount < 1) {
+        throw OmniException("INVALID_ARGUMENT", "operatorCount must be positive", -1);
+    }
+    const int32_t k = buildHashCols[0];
+    if (k < 0 || k >= buildTypes.GetSize() || !JoinKeyType(buildTypes.GetType(k)->GetId())) {
+        throw OmniException("UNSUPPORTED_ERROR", "unsupported join key column", -2);
+    }
+    state_->joinType = joinType;
+    state_->buildTypes = buildTypes;
+    state_->hashCols.assign(buildHashCols, buildHashCols + buildHashColsCount);
+    state_->operatorCount = operatorCount;
+}
+
+HashBuilderOperatorFactory::~HashBuilderOperatorFactory() = default;
+
+HashBuilderOperatorFactory *HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(JoinType joinType,
+    const DataTypes &buildTypes, const int32_t *buildHashCols, int32_t buildHashColsCount, int32_t operatorCount)
+{
+    return new HashBuilderOperatorFactory(joinType, buildTypes, buildHashCols, buildHashColsCount, operatorCount);
+}
+
+Operator *HashBuilderOperatorFactory::CreateOperator()
+{
+    std::lock_guard<std::mutex> g(state_->mu);
+    ++state_->operatorIndex;
+    return new HashBuilderOperator(state_.get());
+}
+
+int32_t HashBuilderOperator::AddInput(VectorBatch *vecBatch)
+{
+    if (vecBatch == nullptr) {
+        throw OmniException("INVALID_ARGUMENT", "AddInput of a null batch", -1);
+    }
+    if (vecBatch->GetRowCount() <= 0) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+        return 0;
+    }
+    if (vecBatch->GetVectorCount() < state_->buildTypes.GetSize()) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "build batch has fewer vectors than build types", -1);
+    }
+    std::lock_guard<std::mutex> g(state_->mu);
+    if (state_->built) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "AddInput after the hash table was built", -6);
+    }
+    state_->batches.push_back(vecBatch);
+    return 0;
+}
+
+int32_t HashBuilderOperator::GetOutput(VectorBatch **outputVecBatch)
+{
+    if (outputVecBatch != nullptr) {
+        *outputVecBatch = nullptr;
+    }
+    if (!noMoreInput_) {
+        SetStatus(OMNI_STATUS_NORMAL);
+        return 0;
+    }
+    if (isFinished()) {
+        return 0;
+    }
+    std::lock_guard<std::mutex> g(state_->mu);
+    if (!counted_) {
+        counted_ = true;
+        ++state_->finished;
+    }
+    // The single GPU table is built once every builder of the factory has finished (the
+    // reference builds one partition per builder and unblocks probes when all are built).
+    if (!state_->built && state_->finished >= state_->operatorCount) {
+        state_->stream.SetUser(userStream_);
+        state_->Build();
+    }
+    SetStatus(OMNI_STATUS_FINISHED);
+    return 0;
+}
+
+// ------------------------------------------------------------------------------ probe
+LookupJoinOperatorFactory::LookupJoinOperatorFactory(const DataTypes &probeTypes_, const int32_t *probeOutputCols_,
+    int32_t probeOutputColsCount, const int32_t *probeHashCols_, int32_t probeHashColsCount,
+    const int32_t *buildOutputCols_, int32_t buildOutputColsCount, const DataTypes &buildOutputTypes_,
+    HashBuilderOperatorFactory *builder)
+    : probeTypes(probeTypes_), buildOutputTypes(buildOutputTypes_), build(builder->GetBuildState())
+{
+    if (probeHashColsCount != 1) {
+        throw OmniException("UNSUPPORTED_ERROR", "only single-column join keys are supported", -2);
+    }
+    probeOutputCols.assign(probeOutputCols_, probeOutputCols_ + probeOutputColsCount);
+    probeHashCols.assign(probeHashCols_, probeHashCols_ + probeHashColsCount);
+    buildOutputCols.assign(buildOutputCols_, buildOutputCols_ + buildOutputColsCount);
+    const int32_t k = probeHashCols[0];
+    if (k < 0 || k >= probeTypes.GetSize() || !JoinKeyType(probeTypes.GetType(k)->GetId())) {
+        throw OmniException("UNSUPPORTED_ERROR", "unsupported probe key column", -2);
+    }
+    if (buildOutputTypes.GetSize() != buildOutputColsCount) {
+        throw OmniException("INVALID_ARGUMENT", "build output types and columns disagree", -1);
+    }
+    if (probeOutputColsCount + buildOutputColsCount > omg::kMaxOutCols) {
+        throw OmniException("UNSUPPORTED_ERROR", "too many join output columns", -2);
+    }
+    int32_t rowSize = 0;
+    for (int32_t c : probeOutputCols) {
+        if (c < 0 || c >= probeTypes.GetSize()) {
+            throw OmniException("INVALID_ARGUMENT", "probe output column out of range", -1);
+        }
+        rowSize += probeTypes.GetType(c)->ByteWidth();
+    }
+    for (int32_t i = 0; i < buildOutputColsCount; ++i) {
+        const int32_t c = buildOutputCols[i];
+        if (c < 0 || c >= build->buildTypes.GetSize()) {
+            throw OmniException("INVALID_ARGUMENT", "build output column out of range", -1);
+        }
+        rowSize += buildOutputTypes.GetType(i)->ByteWidth();
+    }
+    rowsPerBatch = GetMaxRowCount(rowSize);
+}
+
+LookupJoinOperatorFactory *LookupJoinOperatorFactory::CreateLookupJoinOperatorFactory(const DataTypes &probeTypes,
+    int32_t *probeOutputCols, int32_t probeOutputColsCount, int32_t *probeHashCols, int32_t probeHashColsCount,
+    int32_t *buildOutputCols, int32_t buildOutputColsCount, const DataTypes &buildOutputTypes,
+    int64_t hashBuilderFactoryAddr, const void *filterExpr, bool isShuffleExchangeBuildPlan, const void *overflowConfig)
+{
+    (void)isShuffleExchangeBuildPlan;
+    (void)overflowConfig;
+    if (filterExpr != nullptr) {
+        throw OmniException("UNSUPPORTED_ERROR", "join filter expressions are not supported", -2);
+    }
+    auto *builder = reinterpret_cast<HashBuilderOperatorFactory *>(hashBuilderFactoryAddr);
+    if (builder == nullptr) {
+        throw OmniException("INVALID_ARGUMENT", "null hash builder factory", -1);
+    }
+    return new LookupJoinOperatorFactory(probeTypes, probeOutputCols, probeOutputColsCount, probeHashCols,
+        probeHashColsCount, buildOutputCols, buildOutputColsCount, buildOutputTypes, builder);
+}
+
+Operator *LookupJoinOperatorFactory::CreateOperator() { return new LookupJoinOperator(*this); }
+
+struct LookupJoinOperator::Impl {
+    omg::OpStream stream;
+};
+
+LookupJoinOperator::LookupJoinOperator(const LookupJoinOperatorFactory &f) : f_(f), impl_(new Impl()) {}
+
+LookupJoinOperator::~LookupJoinOperator() { Close(); }
+
+OmniStatus LookupJoinOperator::Close()
+{
+    for (auto *b : pending_) {
+        vec::VectorHelper::FreeVecBatch(b);
+    }
+    pending_.clear();
+    pendingRows_ = 0;
+    for (auto *b : outputs_) {
+        vec::VectorHelper::FreeVecBatch(b);
+    }
+    outputs_.clear();
+    return OMNI_STATUS_NORMAL;
+}
+
+BlockingReason LookupJoinOperator::IsBlocked()
+{
+    std::lock_guard<std::mutex> g(f_.build->mu);
+    return f_.build->built ? BlockingReason::kNotBlocked : BlockingReason::kWaitForJoinBuild;
+}
+
+int32_t LookupJoinOperator::AddInput(VectorBatch *vecBatch)
+{
+    if (vecBatch == nullptr) {
+        throw OmniException("INVALID_ARGUMENT", "AddInput of a null batch", -1);
+    }
+    if (vecBatch->GetRowCount() <= 0) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+        SetStatus(OMNI_STATUS_NORMAL);
+        return 0;
+    }
+    if (vecBatch->GetVectorCount() < f_.probeTypes.GetSize()) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "probe batch has fewer vectors than probe types", -1);
+    }
+    pending_.push_back(vecBatch);
+    pendingRows_ += vecBatch->GetRowCount();
+    SetStatus(OMNI_STATUS_NORMAL);
+    return 0;
+}
+
+void LookupJoinOperator::ProcessPending()
+{
+    JoinBuildState &b = *f_.build;
+    omg::RequireDevice();
+    impl_->stream.SetUser(userStream_);
+    cudaStream_t s = impl_->stream.Get();
+    // Kernel inputs: probe key first, then the probe output columns.
+    std::vector<int32_t> inputCols{f_.probeHashCols[0]};
+    std::map<int32_t, int32_t> inputOf{{f_.probeHashCols[0], 0}};
+    for (int32_t c : f_.probeOutputCols) {
+        if (inputOf.count(c) == 0) {
+            inputOf[c] = static_cast<int32_t>(inputCols.size());
+            inputCols.push_back(c);
+        }
+    }
+    omg::BatchTable bt;
+    bt.Build(pending_, inputCols);
+    bt.Upload(s);
+    const int64_t probeRows = bt.TotalRows();
+    const size_t nProbeOut = f_.probeOutputCols.size();
+    const size_t nOut = nProbeOut + f_.buildOutputCols.size();
+    std::vector<omg::OutColumn> cols(nOut);
+    omg::ProbeLaunch p;
+    std::memset(&p, 0, sizeof(p));
+    p.batches = bt.DeviceBatches();
+    p.tiles = bt.DeviceTiles();
+    p.nTiles = bt.NumTiles();
+    p.keyInput = 0;
+    p.keyWidth = f_.probeTypes.GetType(f_.probeHashCols[0])->ByteWidth();
+    p.table = b.table;
+    p.nOut = static_cast<int32_t>(nOut);
+    for (size_t o = 0; o < nOut; ++o) {
+        omg::JoinOutCol &oc = p.out[o];
+        if (o < nProbeOut) {
+            const int32_t c = f_.probeOutputCols[o];
+            const auto &t = f_.probeTypes.GetType(c);
+            oc.side = 0;
+            oc.src = static_cast<int16_t>(inputOf[c]);
+            oc.width = static_cast<int16_t>(t->ByteWidth());
+            cols[o].type = t->GetId();
+            cols[o].hasNull = bt.AnyNulls(oc.src);
+        } else {
+            const size_t j = o - nProbeOut;
+            const int32_t c = f_.buildOutputCols[j];
+            const auto &t = f_.buildOutputTypes.GetType(static_cast<int32_t>(j));
+            oc.side = 1;
+            oc.src = static_cast<int16_t>(c);
+            oc.width = static_cast<int16_t>(b.buildTypes.GetType(c)->ByteWidth());
+            oc.buildValues = b.colValues[c].Get();
+            oc.buildNulls = b.colHasNull[c] ? b.colNulls[c].Get() : nullptr;
+            cols[o].type = t->GetId();
+            cols[o].hasNull = b.colHasNull[c];
+        }
+        cols[o].width = oc.width;
+    }
+    DevArray<unsigned long long> count(2, s, true);
+    p.outCount = count.Get();
+    uint64_t capacity = static_cast<uint64_t>(std::max<int64_t>(probeRows, 1));
+    if (!b.table.unique) {
+        capacity *= std::min<uint32_t>(b.maxDup, 2);
+    }
+    unsigned long long total = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        for (size_t o = 0; o < nOut; ++o) {
+            cols[o].values = omg::Buffer::NewDevice(capacity * cols[o].width + 16, s, false);
+            cols[o].nulls = cols[o].hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(capacity), s, true) : nullptr;
+            p.out[o].values = cols[o].values->Data();
+            p.out[o].nulls = cols[o].nulls ? static_cast<uint8_t *>(cols[o].nulls->Data()) : nullptr;
+        }
+        p.outCapacity = capacity;
+        CudaCheck(cudaMemsetAsync(count.Get(), 0, sizeof(unsigned long long), s), "reset count");
+        CudaCheck(omg::LaunchProbe(p, s), "probe kernel");
+        ++counters_[0];
+        CudaCheck(cudaMemcpyAsync(&total, count.Get(), sizeof(total), cudaMemcpyDeviceToHost, s), "read count");
+        impl_->stream.Sync();
+        if (total <= capacity) {
+            break;
+        }
+        capacity = total;  // exact size known now: run once more
+        ++counters_[1];
+    }
+    const int64_t rows = static_cast<int64_t>(total);
+    std::vector<omg::OutColumn> outCols = cols;
+    if (!deviceOutput_) {
+        outCols = omg::CopyColumnsToHost(cols, rows, s);
+        impl_->stream.Sync();
+        for (auto &c : outCols) {
+            c.hasNull = false;
+        }
+    }
+    for (auto *ob : omg::CarveBatches(outCols, rows, f_.rowsPerBatch)) {
+        outputs_.push_back(ob);
+    }
+    counters_[5] += rows;
+    for (auto *pb : pending_) {
+        vec::VectorHelper::FreeVecBatch(pb);
+    }
+    pending_.clear();
+    pendingRows_ = 0;
+}
+
+int32_t LookupJoinOperator::GetOutput(VectorBatch **outputVecBatch)
+{
+    *outputVecBatch = nullptr;
+    if (outputs_.empty() && !pending_.empty() && f_.build->built &&
+        (noMoreInput_ || pendingRows_ >= kProbeChunkRows)) {
+        ProcessPending();
+    }
+    if (!outputs_.empty()) {
+        *outputVecBatch = outputs_.front();
+        outputs_.pop_front();
+    }
+    if (outputs_.empty() && pending_.empty() && noMoreInput_) {
+        SetStatus(OMNI_STATUS_FINISHED);
+    }
+    return 0;
+}
+
+}  // namespace op
+}  // namespace omniruntime

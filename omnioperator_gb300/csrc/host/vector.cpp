@@ -1,0 +1,146 @@
+// OmniVec vectors and batches (see omniop/vector.h).
+#include "omniop/vector.h"
+
+#include <cuda_runtime.h>
+
+#include "omniop/types.h"
+
+namespace omniruntime {
+namespace vec {
+
+namespace {
+size_t ValuesBytes(int32_t width, int32_t size)
+{
+    // Round up to 16 bytes so vectorised device loads never cross the allocation.
+    size_t b = static_cast<size_t>(width) * static_cast<size_t>(size < 1 ? 1 : size);
+    return (b + 15) & ~size_t(15);
+}
+size_t NullsBytes(int32_t size)
+{
+    // Whole 32-bit words plus the reference's 8 spare bytes: device kernels set null bits
+    // with 32-bit atomicOr.
+    return static_cast<size_t>(((size + 31) / 32) * 4 + 8);
+}
+}  // namespace
+
+BaseVector::BaseVector(DataTypeId type, int32_t width, int32_t size, bool device, void *stream)
+    : type_(type), width_(width), size_(size)
+{
+    if (width <= 0) {
+        throw exception::OmniException("UNSUPPORTED_ERROR", "unsupported vector type " + std::to_string(type), -2);
+    }
+    if (device) {
+        values_ = omg::Buffer::NewDevice(ValuesBytes(width, size), stream, true);
+        nulls_ = omg::Buffer::NewDevice(NullsBytes(size), stream, true);
+    } else {
+        values_ = omg::Buffer::NewHost(ValuesBytes(width, size), true);
+        nulls_ = omg::Buffer::NewHost(NullsBytes(size), true);
+    }
+}
+
+BaseVector::BaseVector(DataTypeId type, int32_t width, int32_t size, omg::BufferPtr values, size_t valuesOffset,
+    omg::BufferPtr nulls, size_t nullsOffset, bool hasNull)
+    : type_(type), width_(width), size_(size), hasNull_(hasNull), values_(std::move(values)),
+      valuesOffset_(valuesOffset), nulls_(std::move(nulls)), nullsOffset_(nullsOffset)
+{}
+
+bool BaseVector::HasNull()
+{
+    if (hasNull_) {
+        return true;
+    }
+    if (nulls_ == nullptr || IsDevice()) {
+        return false;  // device vectors rely on the writer's flag
+    }
+    const uint8_t *n = RawNulls();
+    const int32_t fullBytes = size_ >> 3;
+    for (int32_t i = 0; i < fullBytes; ++i) {
+        if (n[i] != 0) {
+            hasNull_ = true;
+            return true;
+        }
+    }
+    for (int32_t i = fullBytes * 8; i < size_; ++i) {
+        if (IsNull(i)) {
+            hasNull_ = true;
+            return true;
+        }
+    }
+    return false;
+}
+
+int32_t BaseVector::GetNullCount()
+{
+    if (IsDevice() || nulls_ == nullptr) {
+        return 0;
+    }
+    int32_t c = 0;
+    for (int32_t i = 0; i < size_; ++i) {
+        c += IsNull(i) ? 1 : 0;
+    }
+    return c;
+}
+
+VectorBatch::~VectorBatch() = default;
+
+void VectorBatch::FreeAllVectors()
+{
+    for (auto *v : vectors_) {
+        delete v;
+    }
+    vectors_.clear();
+}
+
+bool VectorBatch::IsDevice() const
+{
+    for (auto *v : vectors_) {
+        if (v->IsDevice()) {
+            return true;
+        }
+    }
+    return false;
+}
+
+VectorBatch *VectorHelper::CopyBatch(VectorBatch *batch, bool toDevice, void *stream)
+{
+    auto *out = new VectorBatch(batch->GetRowCount());
+    try {
+        for (int32_t i = 0; i < batch->GetVectorCount(); ++i) {
+            BaseVector *src = batch->Get(i);
+            auto *dst = new BaseVector(src->GetTypeId(), src->GetWidth(), src->GetSize(), toDevice, stream);
+            out->Append(dst);
+            const size_t vb = static_cast<size_t>(src->GetWidth()) * src->GetSize();
+            cudaMemcpyKind kind = cudaMemcpyDefault;
+            if (vb > 0 && cudaMemcpyAsync(dst->RawValues(), src->RawValues(), vb, kind,
+                              static_cast<cudaStream_t>(stream)) != cudaSuccess) {
+                throw exception::OmniException("CUDA_ERROR", "batch copy failed", -3);
+            }
+            if (src->RawNulls() != nullptr) {
+                const size_t nb = static_cast<size_t>((src->GetSize() + 7) / 8);
+                if (nb > 0 && cudaMemcpyAsync(dst->RawNulls(), src->RawNulls(), nb, kind,
+                                  static_cast<cudaStream_t>(stream)) != cudaSuccess) {
+                    throw exception::OmniException("CUDA_ERROR", "batch copy failed", -3);
+                }
+            }
+            dst->SetNullFlag(src->HasNull());
+        }
+        if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess) {
+            throw exception::OmniException("CUDA_ERROR", "batch copy failed", -3);
+        }
+    } catch (...) {
+        VectorHelper::FreeVecBatch(out);
+        throw;
+    }
+    return out;
+}
+
+}  // namespace vec
+
+namespace op {
+namespace {
+SupportContainerVecRule g_rule = SupportContainerVecRule::NOT_SUPPORT;
+}
+SupportContainerVecRule GetSupportContainerVecRule() { return g_rule; }
+void SetSupportContainerVecRule(SupportContainerVecRule rule) { g_rule = rule; }
+}  // namespace op
+}  // namespace omniruntime

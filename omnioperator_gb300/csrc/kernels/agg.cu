@@ -1,0 +1,1121 @@
+// Hash aggregation kernels for sm_103a.
+//
+// Replaces the row loop of HashAggregationOperator::AddInput / Emplace
+// (operator/aggregation/group_aggregation.cpp:320-406,811-890): find-or-insert the group of
+// every row, then update its aggregate states (operations_hash_aggregator.h:16-76).
+//
+// Design:
+//  * One persistent grid walks the tile list of many VectorBatches (host-pinned or HBM).
+//  * Each CTA keeps a shared-memory pre-aggregation table; a row whose group is found or
+//    placed there is updated with shared-memory atomics.  Rows that miss (table full) go to
+//    the global open-addressing table with 64-bit atomicCAS insertion and global atomics.
+//    At the end each CTA merges its shared table into the global one.
+//  * States are exact or order-free: wrapping int64 sums, exact 128/192-bit sums kept as
+//    separate positive and negative magnitudes (so Sum|x| is known for the sticky-overflow
+//    rule), compensated double sums, and monotone min/max with a read-before-atomic filter.
+//  * A row that cannot be placed within `maxProbe` probes is queued, never half-applied; the
+//    host grows the table and re-runs the queue.  A shared-table entry that cannot be merged
+//    is spilled as a partial record and merged after the growth.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "launch.h"
+#include "plan.h"
+
+namespace omg {
+namespace {
+
+constexpr int kSmemProbe = 8;
+constexpr uint64_t kTagLocked = 1;
+
+// ------------------------------------------------------------------ key handling
+struct RowKey {
+    uint64_t w[3];  // KEY_SINGLE: w[0] = key; KEY_PACKED: packed words
+    uint64_t hash;
+    int special;    // -1 normal, kNullSlotOffset / kSentinelSlotOffset for the special groups
+};
+
+__device__ __forceinline__ RowKey ReadKey(const KeySpec &ks, const BatchDesc &b, int64_t row)
+{
+    RowKey k;
+    k.w[0] = k.w[1] = k.w[2] = 0;
+    k.special = -1;
+    if (ks.kind == KEY_SINGLE) {
+        const KeyCol &c = ks.cols[0];
+        if (RowIsNull(b.nulls[c.input], row)) {
+            k.special = kNullSlotOffset;
+            k.hash = 0;
+            return k;
+        }
+        uint64_t v = static_cast<uint64_t>(LoadInt(b.cols[c.input], row, c.width));
+        k.w[0] = v;
+        if (v == kEmptyKey) {
+            k.special = kSentinelSlotOffset;
+        }
+        k.hash = Mix64(v);
+        return k;
+    }
+    uint32_t mask = 0;
+    for (int ci = 0; ci < ks.nCols; ++ci) {
+        const KeyCol &c = ks.cols[ci];
+        if (RowIsNull(b.nulls[c.input], row)) {
+            mask |= 1u << ci;
+            continue;
+        }
+        const int wi = c.byteOffset >> 3;
+        const int sh = (c.byteOffset & 7) * 8;
+        if (c.width == 16) {
+            const uint64_t *p = static_cast<const uint64_t *>(b.cols[c.input]) + 2 * row;
+            k.w[wi] = p[0];
+            k.w[wi + 1] = p[1];
+        } else {
+            k.w[wi] |= LoadBits(b.cols[c.input], row, c.width) << sh;
+        }
+    }
+    k.w[ks.maskByte >> 3] |= static_cast<uint64_t>(mask) << ((ks.maskByte & 7) * 8);
+    uint64_t h = 0x9e3779b97f4a7c15ull;
+    for (int i = 0; i < ks.words; ++i) {
+        h = Mix64(h ^ k.w[i]);
+    }
+    k.hash = h;
+    return k;
+}
+
+// Published tag of a packed slot: never 0 (free) or 1 (locked).
+__device__ __forceinline__ uint64_t PublishedTag(uint64_t hash) { return (hash | 2ull) & ~1ull; }
+
+// ------------------------------------------------------------------ state updates
+// `st` points at the group's state words, in shared or global memory.
+__device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc &b, int64_t row, uint64_t *st)
+{
+    for (int a = 0; a < p.nAccs; ++a) {
+        const AccSpec &s = p.accs[a];
+        uint64_t *w = st + s.word;
+        if (s.kind == ACC_COUNT_ALL) {
+            atomicAdd(reinterpret_cast<unsigned long long *>(w), 1ull);
+            continue;
+        }
+        const bool isNull = RowIsNull(b.nulls[s.input], row);
+        if (s.kind == ACC_NULLS) {
+            if (isNull) {
+                atomicAdd(reinterpret_cast<unsigned long long *>(w), 1ull);
+            }
+            continue;
+        }
+        if (isNull) {
+            continue;
+        }
+        const void *col = b.cols[s.input];
+        switch (s.kind) {
+            case ACC_ISUM: {
+                int64_t x = LoadInt(col, row, s.inWidth);
+                if (x != 0) {
+                    atomicAdd(reinterpret_cast<unsigned long long *>(w), static_cast<unsigned long long>(x));
+                }
+                break;
+            }
+            case ACC_WSUM2: {
+                int64_t x = LoadInt(col, row, s.inWidth);
+                if (x >= 0) {
+                    AtomicAddU128(w, static_cast<uint64_t>(x), 0);
+                } else {
+                    AtomicAddU128(w + 2, 0ull - static_cast<uint64_t>(x), 0);
+                }
+                break;
+            }
+            case ACC_WSUM3: {
+                const uint64_t *v = static_cast<const uint64_t *>(col) + 2 * row;
+                uint64_t lo = v[0];
+                uint64_t hi = v[1];
+                if (static_cast<int64_t>(hi) >= 0) {
+                    AtomicAddU192(w, lo, hi, 0);
+                } else {
+                    // magnitude = -(hi:lo)
+                    uint64_t nlo = ~lo + 1;
+                    uint64_t nhi = ~hi + (nlo == 0 ? 1u : 0u);
+                    AtomicAddU192(w + 3, nlo, nhi, 0);
+                }
+                break;
+            }
+            case ACC_DSUM: {
+                double x = LoadAsDouble(col, row, s.inKind, s.inWidth);
+                AtomicAddCompensated(w, x, 0.0);
+                break;
+            }
+            case ACC_IMIN:
+                AtomicMinI64(w, LoadInt(col, row, s.inWidth));
+                break;
+            case ACC_IMAX:
+                AtomicMaxI64(w, LoadInt(col, row, s.inWidth));
+                break;
+            case ACC_DMIN: {
+                double x = LoadAsDouble(col, row, s.inKind, s.inWidth);
+                if (!isnan(x)) {
+                    AtomicMinI64(w, OrderedFromDouble(x));
+                }
+                break;
+            }
+            case ACC_DMAX: {
+                double x = LoadAsDouble(col, row, s.inKind, s.inWidth);
+                if (!isnan(x)) {
+                    AtomicMaxI64(w, OrderedFromDouble(x));
+                }
+                break;
+            }
+            default:
+                break;
+        }
+    }
+}
+
+// Merge a partial state (shared table entry or spilled record) into `dst`.
+__device__ __forceinline__ void MergeStates(const AccSpec *accs, int nAccs, const uint64_t *src, uint64_t *dst)
+{
+    for (int a = 0; a < nAccs; ++a) {
+        const AccSpec &s = accs[a];
+        const uint64_t *v = src + s.word;
+        uint64_t *w = dst + s.word;
+        switch (s.kind) {
+            case ACC_COUNT_ALL:
+            case ACC_NULLS:
+            case ACC_ISUM:
+                if (v[0] != 0) {
+                    atomicAdd(reinterpret_cast<unsigned long long *>(w), static_cast<unsigned long long>(v[0]));
+                }
+                break;
+            case ACC_WSUM2:
+                AtomicAddU128(w, v[0], v[1]);
+                AtomicAddU128(w + 2, v[2], v[3]);
+                break;
+            case ACC_WSUM3:
+                AtomicAddU192(w, v[0], v[1], v[2]);
+                AtomicAddU192(w + 3, v[3], v[4], v[5]);
+                break;
+            case ACC_DSUM: {
+                double s0 = __longlong_as_double(static_cast<long long>(v[0]));
+                double c0 = __longlong_as_double(static_cast<long long>(v[1]));
+                if (s0 != 0.0 || c0 != 0.0) {
+                    AtomicAddCompensated(w, s0, c0);
+                }
+                break;
+            }
+            case ACC_IMIN:
+            case ACC_DMIN:
+                if (static_cast<int64_t>(v[0]) != s.init) {
+                    AtomicMinI64(w, static_cast<int64_t>(v[0]));
+                }
+                break;
+            case ACC_IMAX:
+            case ACC_DMAX:
+                if (static_cast<int64_t>(v[0]) != s.init) {
+                    AtomicMaxI64(w, static_cast<int64_t>(v[0]));
+                }
+                break;
+            default:
+                break;
+        }
+    }
+}
+
+__device__ __forceinline__ void InitStates(const AccSpec *accs, int nAccs, int stateWords, uint64_t *st)
+{
+    for (int i = 0; i < stateWords; ++i) {
+        st[i] = 0;
+    }
+    for (int a = 0; a < nAccs; ++a) {
+        st[accs[a].word] = static_cast<uint64_t>(accs[a].init);
+    }
+}
+
+// ------------------------------------------------------------------ global table
+// Returns the slot index or -1 when no slot was found within maxProbe probes.
+__device__ __forceinline__ int64_t GlobalFind(const AggTable &t, const KeySpec &ks, const RowKey &k, int maxProbe,
+    int32_t *error, bool *inserted, long long waitBudget)
+{
+    *inserted = false;
+    if (k.special >= 0) {
+        const uint64_t slot = t.capacity + static_cast<uint64_t>(k.special);
+        if (t.specialUsed[k.special] == 0) {
+            atomicExch(&t.specialUsed[k.special], 1u);
+        }
+        return static_cast<int64_t>(slot);
+    }
+    const uint64_t mask = t.capacity - 1;
+    uint64_t i = k.hash & mask;
+    if (ks.kind == KEY_SINGLE) {
+        for (int probe = 0; probe < maxProbe; ++probe) {
+            unsigned long long *kp = reinterpret_cast<unsigned long long *>(t.slots + i * t.slotWords);
+            unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(kp);
+            if (cur == k.w[0]) {
+                return static_cast<int64_t>(i);
+            }
+            if (cur == kEmptyKey) {
+                unsigned long long prev = atomicCAS(kp, kEmptyKey, k.w[0]);
+                if (prev == kEmptyKey) {
+                    *inserted = true;
+                    return static_cast<int64_t>(i);
+                }
+                if (prev == k.w[0]) {
+                    return static_cast<int64_t>(i);
+                }
+            }
+            i = (i + 1) & mask;
+        }
+        return -1;
+    }
+    const uint64_t tag = PublishedTag(k.hash);
+    for (int probe = 0; probe < maxProbe; ++probe) {
+        uint64_t *slot = t.slots + i * t.slotWords;
+        uint64_t cur = LoadAcquire(slot);
+        if (cur == 0) {
+            unsigned long long prev =
+                atomicCAS(reinterpret_cast<unsigned long long *>(slot), 0ull, static_cast<unsigned long long>(kTagLocked));
+            if (prev == 0) {
+                for (int j = 0; j < ks.words; ++j) {
+                    slot[1 + j] = k.w[j];
+                }
+                StoreRelease(slot, tag);
+                *inserted = true;
+                return static_cast<int64_t>(i);
+            }
+            cur = prev;
+        }
+        if (cur == kTagLocked) {
+            // Another thread is publishing this slot's key: wait a bounded time.
+            long long start = clock64();
+            while ((cur = LoadAcquire(slot)) == kTagLocked) {
+                if (clock64() - start > waitBudget) {
+                    SetError(error, 7);
+                    return -1;
+                }
+            }
+        }
+        if (cur == tag) {
+            bool eq = true;
+            for (int j = 0; j < ks.words; ++j) {
+                eq = eq && (slot[1 + j] == k.w[j]);
+            }
+            if (eq) {
+                return static_cast<int64_t>(i);
+            }
+        }
+        i = (i + 1) & mask;
+    }
+    return -1;
+}
+
+// ------------------------------------------------------------------ shared-memory table
+// Same layout as the global table (slotWords words per slot), nSlots slots, no special
+// slots (those rows go straight to the global table).  Returns the slot or -1.
+__device__ __forceinline__ int SmemFind(uint64_t *sm, int nSlots, int slotWords, const KeySpec &ks, const RowKey &k)
+{
+    int i = static_cast<int>((static_cast<uint64_t>(static_cast<uint32_t>(k.hash >> 32)) * nSlots) >> 32);
+    if (ks.kind == KEY_SINGLE) {
+        for (int probe = 0; probe < kSmemProbe; ++probe) {
+            unsigned long long *kp = reinterpret_cast<unsigned long long *>(sm + static_cast<int64_t>(i) * slotWords);
+            unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(kp);
+            if (cur == k.w[0]) {
+                return i;
+            }
+            if (cur == kEmptyKey) {
+                unsigned long long prev = atomicCAS(kp, kEmptyKey, k.w[0]);
+                if (prev == kEmptyKey || prev == k.w[0]) {
+                    return i;
+                }
+            }
+            if (++i == nSlots) {
+                i = 0;
+            }
+        }
+        return -1;
+    }
+    const uint64_t tag = PublishedTag(k.hash);
+    for (int probe = 0; probe < kSmemProbe; ++probe) {
+        uint64_t *slot = sm + static_cast<int64_t>(i) * slotWords;
+        volatile uint64_t *vs = slot;
+        uint64_t cur = vs[0];
+        if (cur == 0) {
+            unsigned long long prev =
+                atomicCAS(reinterpret_cast<unsigned long long *>(slot), 0ull, static_cast<unsigned long long>(kTagLocked));
+            if (prev == 0) {
+                for (int j = 0; j < ks.words; ++j) {
+                    vs[1 + j] = k.w[j];
+                }
+                __threadfence_block();
+                vs[0] = tag;
+                return i;
+            }
+            cur = prev;
+        }
+        if (cur == kTagLocked) {
+            int spins = 0;
+            while ((cur = vs[0]) == kTagLocked) {
+                if (++spins > (1 << 20)) {
+                    return -1;  // give up on the shared table; the row goes global
+                }
+            }
+        }
+        if (cur == tag) {
+            __threadfence_block();
+            bool eq = true;
+            for (int j = 0; j < ks.words; ++j) {
+                eq = eq && (vs[1 + j] == k.w[j]);
+            }
+            if (eq) {
+                return i;
+            }
+        }
+        if (++i == nSlots) {
+            i = 0;
+        }
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool SlotOccupied(const KeySpec &ks, uint64_t firstWord)
+{
+    return ks.kind == KEY_SINGLE ? firstWord != kEmptyKey : (firstWord != 0 && firstWord != kTagLocked);
+}
+
+__device__ __forceinline__ void QueueRetry(const AggLaunch &p, int32_t batch, int64_t row)
+{
+    unsigned int pos = atomicAdd(p.nRetry, 1u);
+    if (pos < p.retryCap) {
+        p.retry[pos] = (static_cast<unsigned long long>(batch) << 32) | static_cast<unsigned long long>(row);
+    } else {
+        SetError(p.error, 4);  // queue overflow: the host sized it for every row, so this is a bug
+    }
+}
+
+__device__ __forceinline__ void ProcessRow(const AggLaunch &p, int32_t batchIdx, int64_t row, uint64_t *sm, int smSlots,
+    unsigned int *newGroups)
+{
+    const BatchDesc &b = p.batches[batchIdx];
+    const RowKey k = ReadKey(p.key, b, row);
+    const int sw = p.table.slotWords;
+    const int kw = p.table.keyWords;
+    if (smSlots > 0 && k.special < 0) {
+        int i = SmemFind(sm, smSlots, sw, p.key, k);
+        if (i >= 0) {
+            UpdateStates(p, b, row, sm + static_cast<int64_t>(i) * sw + kw);
+            return;
+        }
+    }
+    bool inserted = false;
+    int64_t g = GlobalFind(p.table, p.key, k, p.maxProbe, p.error, &inserted, p.waitBudget);
+    if (g < 0) {
+        QueueRetry(p, batchIdx, row);
+        return;
+    }
+    if (inserted) {
+        atomicAdd(newGroups, 1u);
+    }
+    UpdateStates(p, b, row, p.table.slots + g * sw + kw);
+}
+
+// Spill records: [key words (keyWords)][state words], slotWords words each.
+struct SpillArgs {
+    uint64_t *spill;
+    unsigned int *nSpill;
+    uint32_t spillCap;
+    const uint64_t *spillIn;
+    uint32_t nSpillIn;
+};
+
+__device__ __forceinline__ void MergeRecord(const AggLaunch &p, const SpillArgs &sp, const uint64_t *rec,
+    unsigned int *newGroups)
+{
+    const int sw = p.table.slotWords;
+    const int kw = p.table.keyWords;
+    RowKey k;
+    k.special = -1;
+    k.w[0] = k.w[1] = k.w[2] = 0;
+    if (p.key.kind == KEY_SINGLE) {
+        k.w[0] = rec[0];
+        k.hash = Mix64(k.w[0]);
+    } else {
+        uint64_t h = 0x9e3779b97f4a7c15ull;
+        for (int i = 0; i < p.key.words; ++i) {
+            k.w[i] = rec[1 + i];
+            h = Mix64(h ^ k.w[i]);
+        }
+        k.hash = h;
+    }
+    bool inserted = false;
+    int64_t g = GlobalFind(p.table, p.key, k, p.maxProbe, p.error, &inserted, p.waitBudget);
+    if (g < 0) {
+        unsigned int pos = atomicAdd(sp.nSpill, 1u);
+        if (pos < sp.spillCap) {
+            uint64_t *dst = sp.spill + static_cast<int64_t>(pos) * sw;
+            for (int i = 0; i < sw; ++i) {
+                dst[i] = rec[i];
+            }
+        } else {
+            SetError(p.error, 4);
+        }
+        return;
+    }
+    if (inserted) {
+        atomicAdd(newGroups, 1u);
+    }
+    MergeStates(p.accs, p.nAccs, rec + kw, p.table.slots + g * sw + kw);
+}
+
+__global__ void __launch_bounds__(512) AggKernel(const __grid_constant__ AggLaunch p, const SpillArgs sp)
+{
+    extern __shared__ __align__(16) uint64_t smem[];
+    __shared__ unsigned int newGroups;
+    const int sw = p.table.slotWords;
+    const int kw = p.table.keyWords;
+    const int smSlots = (p.retryIn == nullptr && sp.spillIn == nullptr) ? p.smemSlots : 0;
+    if (threadIdx.x == 0) {
+        newGroups = 0;
+    }
+    for (int i = threadIdx.x; i < smSlots; i += blockDim.x) {
+        uint64_t *slot = smem + static_cast<int64_t>(i) * sw;
+        slot[0] = (p.key.kind == KEY_SINGLE) ? kEmptyKey : 0ull;
+        for (int j = 1; j < kw; ++j) {
+            slot[j] = 0;
+        }
+        InitStates(p.accs, p.nAccs, p.stateWords, slot + kw);
+    }
+    __syncthreads();
+
+    if (p.retryIn != nullptr || sp.spillIn != nullptr) {
+        const int64_t gtid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+        const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+        for (int64_t i = gtid; i < p.nRetryIn; i += stride) {
+            unsigned long long e = p.retryIn[i];
+            ProcessRow(p, static_cast<int32_t>(e >> 32), static_cast<int64_t>(e & 0xffffffffull), smem, 0, &newGroups);
+        }
+        for (int64_t i = gtid; i < sp.nSpillIn; i += stride) {
+            MergeRecord(p, sp, sp.spillIn + i * sw, &newGroups);
+        }
+    } else {
+        for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+            const TileDesc tile = p.tiles[t];
+            for (int r = threadIdx.x; r < tile.rows; r += blockDim.x) {
+                ProcessRow(p, tile.batch, static_cast<int64_t>(tile.row0) + r, smem, smSlots, &newGroups);
+            }
+        }
+    }
+    __syncthreads();
+
+    // Merge the shared table into the global table.
+    for (int i = threadIdx.x; i < smSlots; i += blockDim.x) {
+        const uint64_t *slot = smem + static_cast<int64_t>(i) * sw;
+        if (SlotOccupied(p.key, slot[0])) {
+            MergeRecord(p, sp, slot, &newGroups);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && newGroups != 0) {
+        atomicAdd(p.table.groupCount, static_cast<unsigned long long>(newGroups));
+    }
+}
+
+// ------------------------------------------------------------------ table maintenance
+__global__ void InitTableKernel(AggTable t, int keyKind, const __grid_constant__ AggLaunch p)
+{
+    const uint64_t n = t.capacity + 2;
+    for (uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < n;
+         s += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint64_t *slot = t.slots + s * t.slotWords;
+        slot[0] = (keyKind == KEY_SINGLE) ? kEmptyKey : 0ull;
+        for (int j = 1; j < t.keyWords; ++j) {
+            slot[j] = 0;
+        }
+        InitStates(p.accs, p.nAccs, p.stateWords, slot + t.keyWords);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 2) {
+        t.specialUsed[threadIdx.x] = 0;
+    }
+}
+
+// Move every group of `from` into the (initialised, larger) table `to`.
+__global__ void RehashKernel(AggTable from, AggTable to, const __grid_constant__ AggLaunch p)
+{
+    const uint64_t n = from.capacity + 2;
+    for (uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < n;
+         s += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t *src = from.slots + s * from.slotWords;
+        uint64_t *dst = nullptr;
+        if (s >= from.capacity) {
+            const int sp = static_cast<int>(s - from.capacity);
+            if (from.specialUsed[sp] == 0) {
+                continue;
+            }
+            to.specialUsed[sp] = 1;
+            dst = to.slots + (to.capacity + sp) * to.slotWords;
+        } else {
+            if (!SlotOccupied(p.key, src[0])) {
+                continue;
+            }
+            RowKey k;
+            k.special = -1;
+            k.w[0] = k.w[1] = k.w[2] = 0;
+            if (p.key.kind == KEY_SINGLE) {
+                k.w[0] = src[0];
+                k.hash = Mix64(k.w[0]);
+            } else {
+                uint64_t h = 0x9e3779b97f4a7c15ull;
+                for (int i = 0; i < p.key.words; ++i) {
+                    k.w[i] = src[1 + i];
+                    h = Mix64(h ^ k.w[i]);
+                }
+                k.hash = h;
+            }
+            bool inserted = false;
+            int64_t g = GlobalFind(to, p.key, k, static_cast<int>(to.capacity < (1ull << 30) ? to.capacity : (1ull << 30)),
+                p.error, &inserted, p.waitBudget);
+            if (g < 0) {
+                SetError(p.error, 4);
+                continue;
+            }
+            dst = to.slots + g * to.slotWords;
+        }
+        for (int j = to.keyWords; j < to.slotWords; ++j) {
+            dst[j] = src[j];
+        }
+    }
+}
+
+__global__ void CountGroupsKernel(AggTable t, int keyKind, unsigned long long *out)
+{
+    unsigned int local = 0;
+    for (uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < t.capacity;
+         s += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t w = t.slots[s * t.slotWords];
+        local += (keyKind == KEY_SINGLE) ? (w != kEmptyKey) : (w != 0 && w != kTagLocked);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        local += __shfl_down_sync(0xffffffffu, local, o);
+    }
+    if ((threadIdx.x & 31) == 0 && local != 0) {
+        atomicAdd(out, static_cast<unsigned long long>(local));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(out, static_cast<unsigned long long>(t.specialUsed[0] + t.specialUsed[1]));
+    }
+}
+
+// ------------------------------------------------------------------ output extraction
+__device__ __forceinline__ void SetOutNull(uint8_t *nulls, uint64_t pos)
+{
+    atomicOr(reinterpret_cast<unsigned int *>(nulls) + (pos >> 5), 1u << (pos & 31));
+}
+
+__device__ __forceinline__ void StoreWidth(void *col, uint64_t pos, int width, uint64_t bits)
+{
+    switch (width) {
+        case 1:
+            static_cast<uint8_t *>(col)[pos] = static_cast<uint8_t>(bits);
+            break;
+        case 2:
+            static_cast<uint16_t *>(col)[pos] = static_cast<uint16_t>(bits);
+            break;
+        case 4:
+            static_cast<uint32_t *>(col)[pos] = static_cast<uint32_t>(bits);
+            break;
+        default:
+            static_cast<uint64_t *>(col)[pos] = bits;
+            break;
+    }
+}
+
+// 10^38 - 1 as a 128-bit unsigned value (type/base_operations.h:20-21).
+__device__ __forceinline__ unsigned __int128 Dec38Max()
+{
+    return (static_cast<unsigned __int128>(5421010862427522170ull) << 64) | 687399551400673279ull;
+}
+
+// Decode a WSUM accumulator: exact signed sum (as sign + 192-bit magnitude) and Sum|x|.
+struct WideSum {
+    bool negative;
+    uint64_t mag[3];   // |sum|
+    uint64_t abs[3];   // Sum|x| (saturated bit set in abs[2] top bit if it overflowed 192 bits)
+};
+
+__device__ __forceinline__ int Cmp192(const uint64_t *a, const uint64_t *b)
+{
+    for (int i = 2; i >= 0; --i) {
+        if (a[i] != b[i]) {
+            return a[i] < b[i] ? -1 : 1;
+        }
+    }
+    return 0;
+}
+
+__device__ __forceinline__ void Sub192(const uint64_t *a, const uint64_t *b, uint64_t *r)
+{
+    uint64_t borrow = 0;
+    for (int i = 0; i < 3; ++i) {
+        uint64_t d = a[i] - b[i];
+        uint64_t b1 = a[i] < b[i];
+        uint64_t d2 = d - borrow;
+        uint64_t b2 = d < borrow;
+        r[i] = d2;
+        borrow = b1 | b2;
+    }
+}
+
+__device__ __forceinline__ void Add192(const uint64_t *a, const uint64_t *b, uint64_t *r)
+{
+    uint64_t carry = 0;
+    for (int i = 0; i < 3; ++i) {
+        uint64_t s = a[i] + b[i];
+        uint64_t c1 = s < a[i];
+        uint64_t s2 = s + carry;
+        uint64_t c2 = s2 < s;
+        r[i] = s2;
+        carry = c1 | c2;
+    }
+}
+
+__device__ __forceinline__ WideSum DecodeWide(const AccSpec &s, const uint64_t *w)
+{
+    uint64_t pos[3] = {0, 0, 0};
+    uint64_t neg[3] = {0, 0, 0};
+    if (s.kind == ACC_WSUM2) {
+        pos[0] = w[0];
+        pos[1] = w[1];
+        neg[0] = w[2];
+        neg[1] = w[3];
+    } else {
+        pos[0] = w[0];
+        pos[1] = w[1];
+        pos[2] = w[2];
+        neg[0] = w[3];
+        neg[1] = w[4];
+        neg[2] = w[5];
+    }
+    WideSum r;
+    if (Cmp192(pos, neg) >= 0) {
+        r.negative = false;
+        Sub192(pos, neg, r.mag);
+    } else {
+        r.negative = true;
+        Sub192(neg, pos, r.mag);
+    }
+    Add192(pos, neg, r.abs);
+    return r;
+}
+
+// True if magnitude `m` (192-bit) exceeds the bound of the output: int64 range (negative
+// sums may reach 2^63) or 10^38 - 1.
+__device__ __forceinline__ bool ExceedsBound(const uint64_t *m, bool negative, int boundKind)
+{
+    if (boundKind == 0) {
+        if (m[2] != 0 || m[1] != 0) {
+            return true;
+        }
+        return negative ? (m[0] > 0x8000000000000000ull) : (m[0] > 0x7fffffffffffffffull);
+    }
+    if (m[2] != 0) {
+        return true;
+    }
+    const unsigned __int128 v = (static_cast<unsigned __int128>(m[1]) << 64) | m[0];
+    return v > Dec38Max();
+}
+
+__global__ void ExtractKernel(const __grid_constant__ AggExtract e)
+{
+    __shared__ unsigned int warpCounts[32];
+    __shared__ unsigned long long blockBase;
+    const AggTable &t = e.table;
+    const uint64_t nSlots = t.capacity + 2;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nWarps = blockDim.x >> 5;
+    for (uint64_t base = static_cast<uint64_t>(blockIdx.x) * blockDim.x; base < nSlots;
+         base += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t s = base + threadIdx.x;
+        bool occ = false;
+        const uint64_t *slot = nullptr;
+        if (s < nSlots) {
+            slot = t.slots + s * t.slotWords;
+            occ = (s >= t.capacity) ? (t.specialUsed[s - t.capacity] != 0) : SlotOccupied(e.key, slot[0]);
+        }
+        const unsigned int ballot = __ballot_sync(0xffffffffu, occ);
+        if (lane == 0) {
+            warpCounts[warp] = __popc(ballot);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned int total = 0;
+            for (int w = 0; w < nWarps; ++w) {
+                unsigned int c = warpCounts[w];
+                warpCounts[w] = total;
+                total += c;
+            }
+            blockBase = total ? atomicAdd(e.outCount, static_cast<unsigned long long>(total)) : 0ull;
+        }
+        __syncthreads();
+        if (occ) {
+            const uint64_t pos = blockBase + warpCounts[warp] + __popc(ballot & ((1u << lane) - 1u));
+            const uint64_t *st = slot + t.keyWords;
+            const bool nullSlot = (s == t.capacity + kNullSlotOffset);
+            const bool sentinelSlot = (s == t.capacity + kSentinelSlotOffset);
+            for (int o = 0; o < e.nOut; ++o) {
+                const OutSpec &os = e.out[o];
+                if (os.kind == OUT_KEY) {
+                    const KeyCol &kc = e.key.cols[os.src];
+                    if (e.key.kind == KEY_SINGLE) {
+                        if (nullSlot) {
+                            SetOutNull(os.nulls, pos);
+                            StoreWidth(os.values, pos, os.outWidth, 0);
+                        } else {
+                            StoreWidth(os.values, pos, os.outWidth, sentinelSlot ? kEmptyKey : slot[0]);
+                        }
+                    } else {
+                        const uint64_t *kwds = slot + 1;
+                        const uint32_t mask = static_cast<uint32_t>(
+                            (kwds[e.key.maskByte >> 3] >> ((e.key.maskByte & 7) * 8)) & 0xffu);
+                        const bool isNull = (mask >> os.src) & 1u;
+                        const int wi = kc.byteOffset >> 3;
+                        if (kc.width == 16) {
+                            uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
+                            dst[0] = isNull ? 0 : kwds[wi];
+                            dst[1] = isNull ? 0 : kwds[wi + 1];
+                        } else {
+                            const int sh = (kc.byteOffset & 7) * 8;
+                            uint64_t bits = kwds[wi] >> sh;
+                            StoreWidth(os.values, pos, os.outWidth, isNull ? 0 : bits);
+                        }
+                        if (isNull) {
+                            SetOutNull(os.nulls, pos);
+                        }
+                    }
+                    continue;
+                }
+                int64_t cnt = static_cast<int64_t>(st[e.accs[0].word]);  // accs[0] is COUNT_ALL
+                if (os.countAcc >= 0) {
+                    cnt -= static_cast<int64_t>(st[e.accs[os.countAcc].word]);
+                }
+                if (os.kind == OUT_COUNT) {
+                    StoreWidth(os.values, pos, 8, static_cast<uint64_t>(cnt));
+                    continue;
+                }
+                if (cnt == 0) {
+                    SetOutNull(os.nulls, pos);
+                    StoreWidth(os.values, pos, os.outWidth == 16 ? 8 : os.outWidth, 0);
+                    if (os.outWidth == 16) {
+                        static_cast<uint64_t *>(os.values)[2 * pos + 1] = 0;
+                    }
+                    continue;
+                }
+                const AccSpec &acc = e.accs[os.src];
+                const uint64_t *w = st + acc.word;
+                switch (os.kind) {
+                    case OUT_SUM_WRAP:
+                    case OUT_MIN_INT:
+                    case OUT_MAX_INT:
+                        StoreWidth(os.values, pos, os.outWidth, w[0]);
+                        break;
+                    case OUT_SUM_DOUBLE:
+                    case OUT_AVG: {
+                        double sum = __dadd_rn(__longlong_as_double(static_cast<long long>(w[0])),
+                            __longlong_as_double(static_cast<long long>(w[1])));
+                        if (!isfinite(__longlong_as_double(static_cast<long long>(w[0])))) {
+                            sum = __longlong_as_double(static_cast<long long>(w[0]));
+                        }
+                        const double v = (os.kind == OUT_AVG) ? sum / static_cast<double>(cnt) : sum;
+                        static_cast<double *>(os.values)[pos] = v;
+                        break;
+                    }
+                    case OUT_MIN_DOUBLE:
+                    case OUT_MAX_DOUBLE: {
+                        const double v = DoubleFromOrdered(static_cast<int64_t>(w[0]));
+                        if (os.outWidth == 4) {
+                            static_cast<float *>(os.values)[pos] = static_cast<float>(v);
+                        } else {
+                            static_cast<double *>(os.values)[pos] = v;
+                        }
+                        break;
+                    }
+                    case OUT_SUM_EXACT: {
+                        WideSum ws = DecodeWide(acc, w);
+                        bool overflow = ExceedsBound(ws.mag, ws.negative, os.boundKind);
+                        if (!overflow && ExceedsBound(ws.abs, false, os.boundKind)) {
+                            // Some prefix of the row-ordered sum may have overflowed: decided by
+                            // the ordered path on the host side of this operator.
+                            if (e.forcedOverflow != nullptr) {
+                                overflow = ((e.forcedOverflow[s] >> os.pad) & 1u) != 0;
+                            } else {
+                                unsigned long long k = atomicAdd(e.nAmbiguous, 1ull);
+                                if (k < e.ambiguousCap) {
+                                    e.ambiguousSlots[k] = s;
+                                }
+                            }
+                        }
+                        unsigned __int128 mag = (static_cast<unsigned __int128>(ws.mag[1]) << 64) | ws.mag[0];
+                        if (!overflow && os.rescalePow > 0) {
+                            unsigned __int128 f = 1;
+                            for (int i = 0; i < os.rescalePow; ++i) {
+                                f *= 10;
+                            }
+                            // |mag| <= 10^38 - 1 < 2^127 and f <= 10^38: check mag * f <= bound.
+                            if (mag != 0 && mag > Dec38Max() / f) {
+                                overflow = true;
+                            } else {
+                                mag *= f;
+                            }
+                        }
+                        if (overflow) {
+                            SetOutNull(os.nulls, pos);
+                            if (!e.overflowAsNull) {
+                                SetError(e.error, 5);
+                            }
+                            mag = 0;
+                        }
+                        unsigned __int128 v = ws.negative ? (~mag + 1) : mag;
+                        if (os.outWidth == 16) {
+                            uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
+                            dst[0] = static_cast<uint64_t>(v);
+                            dst[1] = static_cast<uint64_t>(v >> 64);
+                        } else {
+                            StoreWidth(os.values, pos, os.outWidth, static_cast<uint64_t>(v));
+                        }
+                        break;
+                    }
+                    default:
+                        break;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ ordered overflow replay
+// For a group whose sticky-overflow outcome depends on row order (|exact sum| within the
+// bound but Sum|x| beyond it), the reference marks the sum overflowed as soon as one
+// row-ordered prefix leaves the bound (sum_aggregator.h:43-49, sum_spark_decimal_aggregator.h:
+// 16-66).  This kernel replays those groups' rows in arrival order (batch, then row) on one
+// thread and records, per group and exact-SUM column, whether a prefix left the bound.
+// It only runs when such groups exist.
+__device__ __forceinline__ int64_t FindSlot(const AggTable &t, const KeySpec &ks, const RowKey &k)
+{
+    if (k.special >= 0) {
+        return static_cast<int64_t>(t.capacity) + k.special;
+    }
+    const uint64_t mask = t.capacity - 1;
+    uint64_t i = k.hash & mask;
+    const uint64_t tag = PublishedTag(k.hash);
+    for (uint64_t probe = 0; probe < t.capacity; ++probe) {
+        const uint64_t *slot = t.slots + i * t.slotWords;
+        if (ks.kind == KEY_SINGLE) {
+            if (slot[0] == k.w[0]) {
+                return static_cast<int64_t>(i);
+            }
+            if (slot[0] == kEmptyKey) {
+                return -1;
+            }
+        } else {
+            if (slot[0] == 0) {
+                return -1;
+            }
+            if (slot[0] == tag) {
+                bool eq = true;
+                for (int j = 0; j < ks.words; ++j) {
+                    eq = eq && (slot[1 + j] == k.w[j]);
+                }
+                if (eq) {
+                    return static_cast<int64_t>(i);
+                }
+            }
+        }
+        i = (i + 1) & mask;
+    }
+    return -1;
+}
+
+__global__ void OrderedOverflowKernel(const __grid_constant__ AggLaunch p, int32_t nBatches,
+    const __grid_constant__ AggExtract e, const unsigned long long *ambSlots, uint32_t nAmb, int32_t *denseOf,
+    uint64_t *prefix, uint8_t *forced)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) {
+        return;
+    }
+    for (uint32_t i = 0; i < nAmb; ++i) {
+        denseOf[ambSlots[i]] = static_cast<int32_t>(i);
+    }
+    for (int32_t bi = 0; bi < nBatches; ++bi) {
+        const BatchDesc &b = p.batches[bi];
+        for (int64_t row = 0; row < b.rows; ++row) {
+            const RowKey k = ReadKey(p.key, b, row);
+            const int64_t slot = FindSlot(p.table, p.key, k);
+            if (slot < 0 || denseOf[slot] < 0) {
+                continue;
+            }
+            const int32_t d = denseOf[slot];
+            for (int o = 0; o < e.nOut; ++o) {
+                const OutSpec &os = e.out[o];
+                if (os.kind != OUT_SUM_EXACT) {
+                    continue;
+                }
+                const uint8_t bit = static_cast<uint8_t>(1u << os.pad);
+                if (forced[slot] & bit) {
+                    continue;  // sticky: no further additions once overflowed
+                }
+                const AccSpec &acc = e.accs[os.src];
+                if (RowIsNull(b.nulls[acc.input], row)) {
+                    continue;
+                }
+                uint64_t x0, x1, x2;
+                if (acc.kind == ACC_WSUM3) {
+                    const uint64_t *v = static_cast<const uint64_t *>(b.cols[acc.input]) + 2 * row;
+                    x0 = v[0];
+                    x1 = v[1];
+                    x2 = (static_cast<int64_t>(x1) < 0) ? ~0ull : 0ull;
+                } else {
+                    const int64_t v = LoadInt(b.cols[acc.input], row, acc.inWidth);
+                    x0 = static_cast<uint64_t>(v);
+                    x1 = x2 = (v < 0) ? ~0ull : 0ull;
+                }
+                uint64_t *pw = prefix + (static_cast<int64_t>(d) * 8 + os.pad) * 3;
+                uint64_t a[3] = {pw[0], pw[1], pw[2]};
+                uint64_t x[3] = {x0, x1, x2};
+                uint64_t r[3];
+                Add192(a, x, r);
+                pw[0] = r[0];
+                pw[1] = r[1];
+                pw[2] = r[2];
+                const bool neg = static_cast<int64_t>(r[2]) < 0;
+                uint64_t mag[3];
+                if (neg) {
+                    const uint64_t zero[3] = {0, 0, 0};
+                    Sub192(zero, r, mag);
+                } else {
+                    mag[0] = r[0];
+                    mag[1] = r[1];
+                    mag[2] = r[2];
+                }
+                if (ExceedsBound(mag, neg, os.boundKind)) {
+                    forced[slot] |= bit;
+                }
+            }
+        }
+    }
+}
+
+int NumSMs()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) {
+            n = 1;
+        }
+    }
+    return n;
+}
+
+}  // namespace
+
+cudaError_t LaunchAggInitTable(const AggLaunch &p, cudaStream_t stream)
+{
+    const uint64_t n = p.table.capacity + 2;
+    const int threads = 256;
+    uint64_t blocks = (n + threads - 1) / threads;
+    const uint64_t maxBlocks = static_cast<uint64_t>(NumSMs()) * 16;
+    if (blocks > maxBlocks) {
+        blocks = maxBlocks;
+    }
+    InitTableKernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(p.table, p.key.kind, p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggRehash(const AggLaunch &p, const AggTable &from, const AggTable &to, cudaStream_t stream)
+{
+    const uint64_t n = from.capacity + 2;
+    const int threads = 256;
+    uint64_t blocks = (n + threads - 1) / threads;
+    const uint64_t maxBlocks = static_cast<uint64_t>(NumSMs()) * 16;
+    if (blocks > maxBlocks) {
+        blocks = maxBlocks;
+    }
+    RehashKernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(from, to, p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAgg(const AggLaunch &p, uint64_t *spill, unsigned int *nSpill, uint32_t spillCap,
+    const uint64_t *spillIn, uint32_t nSpillIn, int gridBlocks, cudaStream_t stream)
+{
+    SpillArgs sp{spill, nSpill, spillCap, spillIn, nSpillIn};
+    const size_t smemBytes = static_cast<size_t>(p.smemSlots) * p.table.slotWords * sizeof(uint64_t);
+    static size_t configured = 0;
+    if (smemBytes > 48 * 1024 && smemBytes > configured) {
+        cudaError_t err =
+            cudaFuncSetAttribute(AggKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smemBytes));
+        if (err != cudaSuccess) {
+            return err;
+        }
+        configured = smemBytes;
+    }
+    if (gridBlocks <= 0) {
+        gridBlocks = NumSMs();
+    }
+    AggKernel<<<gridBlocks, 512, smemBytes, stream>>>(p, sp);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggCount(const AggTable &t, int keyKind, unsigned long long *out, cudaStream_t stream)
+{
+    const int threads = 256;
+    uint64_t blocks = (t.capacity + threads - 1) / threads;
+    const uint64_t maxBlocks = static_cast<uint64_t>(NumSMs()) * 8;
+    if (blocks > maxBlocks) {
+        blocks = maxBlocks;
+    }
+    if (blocks == 0) {
+        blocks = 1;
+    }
+    CountGroupsKernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(t, keyKind, out);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggExtract(const AggExtract &e, cudaStream_t stream)
+{
+    const int threads = 256;
+    const uint64_t n = e.table.capacity + 2;
+    uint64_t blocks = (n + threads - 1) / threads;
+    const uint64_t maxBlocks = static_cast<uint64_t>(NumSMs()) * 8;
+    if (blocks > maxBlocks) {
+        blocks = maxBlocks;
+    }
+    ExtractKernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(e);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtract &e,
+    const unsigned long long *ambSlots, uint32_t nAmb, uint8_t *forced, cudaStream_t stream)
+{
+    const uint64_t nSlots = p.table.capacity + 2;
+    int32_t *denseOf = nullptr;
+    uint64_t *prefix = nullptr;
+    cudaError_t err = cudaMallocAsync(reinterpret_cast<void **>(&denseOf), nSlots * sizeof(int32_t), stream);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    err = cudaMallocAsync(reinterpret_cast<void **>(&prefix), static_cast<size_t>(nAmb) * 8 * 3 * sizeof(uint64_t) + 8,
+        stream);
+    if (err != cudaSuccess) {
+        cudaFreeAsync(denseOf, stream);
+        return err;
+    }
+    cudaMemsetAsync(denseOf, 0xff, nSlots * sizeof(int32_t), stream);
+    cudaMemsetAsync(prefix, 0, static_cast<size_t>(nAmb) * 8 * 3 * sizeof(uint64_t) + 8, stream);
+    OrderedOverflowKernel<<<1, 1, 0, stream>>>(p, nBatches, e, ambSlots, nAmb, denseOf, prefix, forced);
+    err = cudaGetLastError();
+    cudaFreeAsync(denseOf, stream);
+    cudaFreeAsync(prefix, stream);
+    return err;
+}
+
+int DeviceSMCount() { return NumSMs(); }
+
+}  // namespace omg

@@ -1,0 +1,539 @@
+// Hash join build and probe kernels for sm_103a.
+//
+// Build replaces JoinHashTableVariants::BuildHashTable (operator/join/join_hash_table_variants.cpp:
+// 695-863): min/max scan of the keys, then either a direct-index ARRAY table (dense keys) or an
+// open-addressing HASH table.  Duplicate build keys, which the reference chains in RowRefList
+// blocks (operator/join/row_ref.h:27-169), become a CSR of build rows per key.
+//
+// Probe replaces LookupJoinOperator::ProbeBatchForInnerJoin / ArrayJoinProbeSIMDNeon and the
+// output builder (operator/join/lookup_join.cpp:847-1035,1667-1985): a CTA takes a tile of up to
+// 4096 probe rows, looks every non-null key up in registers, prefix-sums the match counts per
+// (round, warp) so that the tile's matches get one contiguous output range from a single
+// atomicAdd, and writes probe columns plus gathered build columns in probe-row order within the
+// tile.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+#include "launch.h"
+#include "plan.h"
+
+namespace omg {
+namespace {
+
+constexpr int kProbeThreads = 256;
+constexpr int kProbeRounds = kTileRows / kProbeThreads;  // 16
+
+int SMs() { return DeviceSMCount(); }
+
+unsigned GridFor(int64_t n, int threads, int perSM)
+{
+    int64_t blocks = (n + threads - 1) / threads;
+    const int64_t cap = static_cast<int64_t>(SMs()) * perSM;
+    if (blocks > cap) {
+        blocks = cap;
+    }
+    return static_cast<unsigned>(blocks < 1 ? 1 : blocks);
+}
+
+__device__ __forceinline__ void CopyValue(void *dst, uint64_t dpos, const void *src, int64_t spos, int width)
+{
+    switch (width) {
+        case 1:
+            static_cast<uint8_t *>(dst)[dpos] = static_cast<const uint8_t *>(src)[spos];
+            break;
+        case 2:
+            static_cast<uint16_t *>(dst)[dpos] = static_cast<const uint16_t *>(src)[spos];
+            break;
+        case 4:
+            static_cast<uint32_t *>(dst)[dpos] = static_cast<const uint32_t *>(src)[spos];
+            break;
+        case 8:
+            static_cast<uint64_t *>(dst)[dpos] = static_cast<const uint64_t *>(src)[spos];
+            break;
+        case 16: {
+            const uint64_t *s = static_cast<const uint64_t *>(src) + 2 * spos;
+            uint64_t *d = static_cast<uint64_t *>(dst) + 2 * dpos;
+            d[0] = s[0];
+            d[1] = s[1];
+            break;
+        }
+        default: {
+            const uint8_t *s = static_cast<const uint8_t *>(src) + static_cast<int64_t>(width) * spos;
+            uint8_t *d = static_cast<uint8_t *>(dst) + static_cast<uint64_t>(width) * dpos;
+            for (int i = 0; i < width; ++i) {
+                d[i] = s[i];
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void SetBit(uint8_t *bitmap, uint64_t pos)
+{
+    atomicOr(reinterpret_cast<unsigned int *>(bitmap) + (pos >> 5), 1u << (pos & 31));
+}
+
+__global__ void GatherColumnKernel(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, int32_t input, int32_t width, void *valuesOut, uint8_t *nullsOut)
+{
+    for (int t = blockIdx.x; t < nTiles; t += gridDim.x) {
+        const TileDesc tile = tiles[t];
+        const BatchDesc &b = batches[tile.batch];
+        const int64_t out0 = tileOutRow[t];
+        const void *col = b.cols[input];
+        const uint8_t *nulls = b.nulls[input];
+        for (int r = threadIdx.x; r < tile.rows; r += blockDim.x) {
+            const int64_t row = static_cast<int64_t>(tile.row0) + r;
+            CopyValue(valuesOut, static_cast<uint64_t>(out0 + r), col, row, width);
+            if (nullsOut != nullptr && RowIsNull(nulls, row)) {
+                SetBit(nullsOut, static_cast<uint64_t>(out0 + r));
+            }
+        }
+    }
+}
+
+__global__ void KeyStatsKernel(const void *keys, const uint8_t *nulls, int64_t n, int32_t width, long long *stats)
+{
+    long long mn = 0x7fffffffffffffffll;
+    long long mx = static_cast<long long>(0x8000000000000000ull);
+    unsigned long long cnt = 0;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (RowIsNull(nulls, i)) {
+            continue;
+        }
+        const long long k = LoadInt(keys, i, width);
+        mn = k < mn ? k : mn;
+        mx = k > mx ? k : mx;
+        ++cnt;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        long long omn = __shfl_down_sync(0xffffffffu, mn, o);
+        long long omx = __shfl_down_sync(0xffffffffu, mx, o);
+        unsigned long long oc = __shfl_down_sync(0xffffffffu, cnt, o);
+        mn = omn < mn ? omn : mn;
+        mx = omx > mx ? omx : mx;
+        cnt += oc;
+    }
+    if ((threadIdx.x & 31) == 0 && cnt != 0) {
+        atomicMin(&stats[0], mn);
+        atomicMax(&stats[1], mx);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&stats[2]), cnt);
+    }
+}
+
+// Find the hash slot of `key` (inserting it when `insert`), -1 if absent.
+__device__ __forceinline__ int64_t HashSlot(uint64_t *keys, uint64_t capacity, uint64_t key, bool insert)
+{
+    const uint64_t mask = capacity - 1;
+    uint64_t i = Mix64(key) & mask;
+    for (uint64_t probe = 0; probe < capacity; ++probe) {
+        unsigned long long *kp = reinterpret_cast<unsigned long long *>(keys + i);
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(kp);
+        if (cur == key) {
+            return static_cast<int64_t>(i);
+        }
+        if (cur == kEmptyKey) {
+            if (!insert) {
+                return -1;
+            }
+            unsigned long long prev = atomicCAS(kp, kEmptyKey, key);
+            if (prev == kEmptyKey || prev == key) {
+                return static_cast<int64_t>(i);
+            }
+        }
+        i = (i + 1) & mask;
+    }
+    return -1;
+}
+
+__global__ void BuildCountKernel(JoinTable t, const void *keys, const uint8_t *nulls, int64_t n, int32_t width,
+    uint64_t *hashKeys, uint32_t *counts, uint32_t *sentinelCount, unsigned int *maxCount, int32_t *error)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (RowIsNull(nulls, i)) {
+            continue;
+        }
+        const uint64_t key = static_cast<uint64_t>(LoadInt(keys, i, width));
+        uint32_t old;
+        if (t.mode == JOIN_ARRAY) {
+            old = atomicAdd(&counts[key - static_cast<uint64_t>(t.minKey)], 1u);
+        } else if (key == kEmptyKey) {
+            old = atomicAdd(sentinelCount, 1u);
+        } else {
+            const int64_t s = HashSlot(hashKeys, t.capacity, key, true);
+            if (s < 0) {
+                SetError(error, 4);
+                continue;
+            }
+            old = atomicAdd(&counts[s], 1u);
+        }
+        if (old >= 1) {
+            atomicMax(maxCount, old + 1);
+        }
+    }
+}
+
+__global__ void BuildFillKernel(JoinTable t, const void *keys, const uint8_t *nulls, int64_t n, int32_t width,
+    const uint32_t *counts, const int64_t *offsets, uint32_t *cursor, int64_t *entries, int32_t *csrRows,
+    uint32_t sentinelCount, int64_t sentinelOffset, unsigned int *sentinelCursor, int64_t *sentinelEntryOut,
+    int32_t *error)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (RowIsNull(nulls, i)) {
+            continue;
+        }
+        const uint64_t key = static_cast<uint64_t>(LoadInt(keys, i, width));
+        int64_t slot;
+        if (t.mode == JOIN_ARRAY) {
+            slot = static_cast<int64_t>(key - static_cast<uint64_t>(t.minKey));
+        } else if (key == kEmptyKey) {
+            slot = -2;
+        } else {
+            slot = HashSlot(const_cast<uint64_t *>(t.hashKeys), t.capacity, key, false);
+            if (slot < 0) {
+                SetError(error, 4);
+                continue;
+            }
+        }
+        if (t.unique) {
+            if (slot >= 0) {
+                entries[slot] = i;
+            } else {
+                *sentinelEntryOut = i;
+            }
+            continue;
+        }
+        if (slot == -2) {
+            const uint32_t c = atomicAdd(sentinelCursor, 1u);
+            csrRows[sentinelOffset + c] = static_cast<int32_t>(i);
+            continue;
+        }
+        const uint32_t c = atomicAdd(&cursor[slot], 1u);
+        const int64_t off = offsets[slot];
+        csrRows[off + c] = static_cast<int32_t>(i);
+        if (c == 0) {
+            entries[slot] = (off << 32) | static_cast<int64_t>(counts[slot]);
+        }
+    }
+}
+
+__global__ void FillI64Kernel(int64_t *p, int64_t v, int64_t n)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        p[i] = v;
+    }
+}
+
+__global__ void FillU64Kernel(uint64_t *p, uint64_t v, int64_t n)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        p[i] = v;
+    }
+}
+
+// ---- exclusive scan of uint32 counts (three passes: block sums, scan of sums, block scans)
+constexpr int kScanThreads = 1024;
+
+__global__ void ScanBlockSumsKernel(const uint32_t *counts, int64_t n, int64_t *blockSums)
+{
+    __shared__ long long warpSums[32];
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * kScanThreads + threadIdx.x;
+    long long v = i < n ? counts[i] : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        warpSums[threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long s = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) {
+            s += warpSums[w];
+        }
+        blockSums[blockIdx.x] = s;
+    }
+}
+
+__global__ void ScanSumsKernel(int64_t *blockSums, int64_t nBlocks, long long *total)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        long long run = 0;
+        for (int64_t b = 0; b < nBlocks; ++b) {
+            const long long v = blockSums[b];
+            blockSums[b] = run;
+            run += v;
+        }
+        *total = run;
+    }
+}
+
+__global__ void ScanApplyKernel(const uint32_t *counts, int64_t n, const int64_t *blockSums, int64_t *offsets)
+{
+    __shared__ long long warpSums[32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * kScanThreads + threadIdx.x;
+    const long long v = i < n ? counts[i] : 0;
+    long long inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        long long y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) {
+            inc += y;
+        }
+    }
+    if (lane == 31) {
+        warpSums[warp] = inc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long s = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) {
+            const long long c = warpSums[w];
+            warpSums[w] = s;
+            s += c;
+        }
+    }
+    __syncthreads();
+    if (i < n) {
+        offsets[i] = blockSums[blockIdx.x] + warpSums[warp] + inc - v;
+    }
+}
+
+// ---- probe
+struct Match {
+    int64_t entry;  // build row (unique) or CSR offset
+    uint32_t count;
+};
+
+__device__ __forceinline__ Match Lookup(const JoinTable &t, uint64_t key)
+{
+    Match m{0, 0};
+    int64_t e = -1;
+    if (t.mode == JOIN_ARRAY) {
+        const uint64_t d = key - static_cast<uint64_t>(t.minKey);
+        if (static_cast<int64_t>(key) >= t.minKey && d < t.range) {
+            e = t.arrayEntries[d];
+        }
+    } else if (key == kEmptyKey) {
+        e = t.sentinelEntry;
+    } else {
+        const uint64_t mask = t.capacity - 1;
+        uint64_t i = Mix64(key) & mask;
+        for (uint64_t probe = 0; probe < t.capacity; ++probe) {
+            const uint64_t k = t.hashKeys[i];
+            if (k == key) {
+                e = t.hashEntries[i];
+                break;
+            }
+            if (k == kEmptyKey) {
+                break;
+            }
+            i = (i + 1) & mask;
+        }
+    }
+    if (e >= 0) {
+        if (t.unique) {
+            m.entry = e;
+            m.count = 1;
+        } else {
+            m.entry = e >> 32;
+            m.count = static_cast<uint32_t>(e & 0xffffffffll);
+        }
+    }
+    return m;
+}
+
+__global__ void __launch_bounds__(kProbeThreads) ProbeKernel(const __grid_constant__ ProbeLaunch p)
+{
+    __shared__ unsigned int roundWarp[kProbeRounds][kProbeThreads / 32];
+    __shared__ unsigned long long blockBase;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        const void *keyCol = b.cols[p.keyInput];
+        const uint8_t *keyNulls = b.nulls[p.keyInput];
+        int64_t entry[kProbeRounds];
+        uint32_t cnt[kProbeRounds];
+        uint32_t prefix[kProbeRounds];
+#pragma unroll
+        for (int i = 0; i < kProbeRounds; ++i) {
+            const int r = i * kProbeThreads + threadIdx.x;
+            cnt[i] = 0;
+            entry[i] = 0;
+            if (r < tile.rows) {
+                const int64_t row = static_cast<int64_t>(tile.row0) + r;
+                if (!RowIsNull(keyNulls, row)) {
+                    const Match m = Lookup(p.table, static_cast<uint64_t>(LoadInt(keyCol, row, p.keyWidth)));
+                    cnt[i] = m.count;
+                    entry[i] = m.entry;
+                }
+            }
+            uint32_t inc = cnt[i];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) {
+                    inc += y;
+                }
+            }
+            prefix[i] = inc - cnt[i];
+            if (lane == 31) {
+                roundWarp[i][warp] = inc;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long run = 0;
+            for (int i = 0; i < kProbeRounds; ++i) {
+                for (int w = 0; w < kProbeThreads / 32; ++w) {
+                    const unsigned int c = roundWarp[i][w];
+                    roundWarp[i][w] = static_cast<unsigned int>(run);
+                    run += c;
+                }
+            }
+            blockBase = run ? atomicAdd(p.outCount, run) : 0ull;
+        }
+        __syncthreads();
+        if (!p.countOnly) {
+#pragma unroll
+            for (int i = 0; i < kProbeRounds; ++i) {
+                if (cnt[i] == 0) {
+                    continue;
+                }
+                const int64_t row = static_cast<int64_t>(tile.row0) + i * kProbeThreads + threadIdx.x;
+                const uint64_t pos0 = blockBase + roundWarp[i][warp] + prefix[i];
+                for (uint32_t k = 0; k < cnt[i]; ++k) {
+                    const uint64_t pos = pos0 + k;
+                    if (pos >= p.outCapacity) {
+                        break;
+                    }
+                    const int64_t buildRow = p.table.unique ? entry[i] : p.table.csrRows[entry[i] + k];
+                    for (int o = 0; o < p.nOut; ++o) {
+                        const JoinOutCol &oc = p.out[o];
+                        if (oc.side == 0) {
+                            CopyValue(oc.values, pos, b.cols[oc.src], row, oc.width);
+                            if (oc.nulls != nullptr && RowIsNull(b.nulls[oc.src], row)) {
+                                SetBit(oc.nulls, pos);
+                            }
+                        } else {
+                            CopyValue(oc.values, pos, oc.buildValues, buildRow, oc.width);
+                            if (oc.nulls != nullptr && RowIsNull(oc.buildNulls, buildRow)) {
+                                SetBit(oc.nulls, pos);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+cudaError_t LaunchGatherColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, int32_t input, int32_t width, void *valuesOut, uint8_t *nullsOut,
+    cudaStream_t stream)
+{
+    if (nTiles <= 0) {
+        return cudaSuccess;
+    }
+    const unsigned grid = static_cast<unsigned>(nTiles < SMs() * 8 ? nTiles : SMs() * 8);
+    GatherColumnKernel<<<grid, 256, 0, stream>>>(batches, tiles, nTiles, tileOutRow, input, width, valuesOut,
+        nullsOut);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchKeyStats(const void *keys, const uint8_t *nulls, int64_t n, int32_t width, long long *stats,
+    cudaStream_t stream)
+{
+    const long long init[3] = {0x7fffffffffffffffll, static_cast<long long>(0x8000000000000000ull), 0};
+    cudaError_t err = cudaMemcpyAsync(stats, init, sizeof(init), cudaMemcpyHostToDevice, stream);
+    if (err != cudaSuccess || n == 0) {
+        return err;
+    }
+    KeyStatsKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(keys, nulls, n, width, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchBuildCount(JoinTable t, const void *keys, const uint8_t *nulls, int64_t n, int32_t width,
+    uint64_t *hashKeysMutable, uint32_t *counts, uint32_t *sentinelCount, unsigned int *maxCount, int32_t *error,
+    cudaStream_t stream)
+{
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    BuildCountKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(t, keys, nulls, n, width, hashKeysMutable, counts,
+        sentinelCount, maxCount, error);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchScanCounts(const uint32_t *counts, int64_t n, int64_t *offsets, int64_t *blockSums,
+    long long *total, cudaStream_t stream)
+{
+    const int64_t nBlocks = (n + kScanThreads - 1) / kScanThreads;
+    if (nBlocks == 0) {
+        return cudaMemsetAsync(total, 0, sizeof(long long), stream);
+    }
+    ScanBlockSumsKernel<<<static_cast<unsigned>(nBlocks), kScanThreads, 0, stream>>>(counts, n, blockSums);
+    ScanSumsKernel<<<1, 32, 0, stream>>>(blockSums, nBlocks, total);
+    ScanApplyKernel<<<static_cast<unsigned>(nBlocks), kScanThreads, 0, stream>>>(counts, n, blockSums, offsets);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchBuildFill(JoinTable t, const void *keys, const uint8_t *nulls, int64_t n, int32_t width,
+    const uint32_t *counts, const int64_t *offsets, uint32_t *cursor, int64_t *entriesMutable,
+    int32_t *csrRowsMutable, uint32_t sentinelCount, int64_t sentinelOffset, unsigned int *sentinelCursor,
+    int64_t *sentinelEntryOut, int32_t *error, cudaStream_t stream)
+{
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    BuildFillKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(t, keys, nulls, n, width, counts, offsets, cursor,
+        entriesMutable, csrRowsMutable, sentinelCount, sentinelOffset, sentinelCursor, sentinelEntryOut, error);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
+{
+    if (p.nTiles <= 0) {
+        return cudaSuccess;
+    }
+    int blocksPerSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM, ProbeKernel, kProbeThreads, 0);
+    if (blocksPerSM <= 0) {
+        blocksPerSM = 1;
+    }
+    const int maxGrid = SMs() * blocksPerSM;
+    const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
+    ProbeKernel<<<grid, kProbeThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchFillI64(int64_t *p, int64_t v, int64_t n, cudaStream_t stream)
+{
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    FillI64Kernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(p, v, n);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchFillU64(uint64_t *p, uint64_t v, int64_t n, cudaStream_t stream)
+{
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    FillU64Kernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(p, v, n);
+    return cudaGetLastError();
+}
+
+}  // namespace omg

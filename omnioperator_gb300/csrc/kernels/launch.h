@@ -1,0 +1,51 @@
+// Host-callable launchers of the operator kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "plan.h"
+
+namespace omg {
+
+int DeviceSMCount();
+
+// ---- aggregation (agg.cu)
+cudaError_t LaunchAggInitTable(const AggLaunch &p, cudaStream_t stream);
+cudaError_t LaunchAggRehash(const AggLaunch &p, const AggTable &from, const AggTable &to, cudaStream_t stream);
+cudaError_t LaunchAgg(const AggLaunch &p, uint64_t *spill, unsigned int *nSpill, uint32_t spillCap,
+    const uint64_t *spillIn, uint32_t nSpillIn, int gridBlocks, cudaStream_t stream);
+cudaError_t LaunchAggCount(const AggTable &t, int keyKind, unsigned long long *out, cudaStream_t stream);
+cudaError_t LaunchAggExtract(const AggExtract &e, cudaStream_t stream);
+// Ordered replay of order-dependent sticky-overflow groups; sets forced[slot] bit k when
+// exact-SUM output k of that group overflowed on some row-ordered prefix.
+cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtract &e,
+    const unsigned long long *ambSlots, uint32_t nAmb, uint8_t *forced, cudaStream_t stream);
+
+// ---- join (join.cu)
+// Copy column `input` of every batch into one contiguous device array (values) and, if
+// `nullsOut` is given, one contiguous null bitmap (zeroed by the caller).
+cudaError_t LaunchGatherColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, int32_t input, int32_t width, void *valuesOut, uint8_t *nullsOut,
+    cudaStream_t stream);
+// Min / max / count of the non-null keys of a contiguous key column.
+// stats[0] = min, stats[1] = max, stats[2] = count (initialised by the launcher).
+cudaError_t LaunchKeyStats(const void *keys, const uint8_t *nulls, int64_t n, int32_t width,
+    long long *stats, cudaStream_t stream);
+// ARRAY mode: counts[key - min] += 1; HASH mode: insert keys, counts per slot.
+cudaError_t LaunchBuildCount(JoinTable t, const void *keys, const uint8_t *nulls, int64_t n, int32_t width,
+    uint64_t *hashKeysMutable, uint32_t *counts, uint32_t *sentinelCount, unsigned int *maxCount,
+    int32_t *error, cudaStream_t stream);
+// Exclusive scan of uint32 counts into int64 offsets; total written to *total.
+cudaError_t LaunchScanCounts(const uint32_t *counts, int64_t n, int64_t *offsets, int64_t *blockSums,
+    long long *total, cudaStream_t stream);
+// Fill entries: unique -> row, else (offset << 32 | count), and the CSR row lists.
+cudaError_t LaunchBuildFill(JoinTable t, const void *keys, const uint8_t *nulls, int64_t n, int32_t width,
+    const uint32_t *counts, const int64_t *offsets, uint32_t *cursor, int64_t *entriesMutable,
+    int32_t *csrRowsMutable, uint32_t sentinelCount, int64_t sentinelOffset, unsigned int *sentinelCursor,
+    int64_t *sentinelEntryOut, int32_t *error, cudaStream_t stream);
+cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream);
+cudaError_t LaunchFillI64(int64_t *p, int64_t v, int64_t n, cudaStream_t stream);
+cudaError_t LaunchFillU64(uint64_t *p, uint64_t v, int64_t n, cudaStream_t stream);
+
+}  // namespace omg

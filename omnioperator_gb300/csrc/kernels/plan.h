@@ -1,0 +1,242 @@
+// Launch descriptors shared by the host operators and the CUDA kernels.
+//
+// A kernel reads its input as a list of VectorBatch descriptors (one per OmniVec batch, host
+// pinned or HBM) cut into tiles of at most kTileRows rows, so one launch covers any number of
+// batches of uneven sizes.
+#pragma once
+
+#include <cstdint>
+
+namespace omg {
+
+constexpr int kMaxInputs = 12;   // distinct input columns a kernel reads
+constexpr int kMaxAccs = 24;     // accumulators per group
+constexpr int kMaxKeyCols = 4;   // composite group-by / join key columns
+constexpr int kMaxOutCols = 16;  // output columns of an aggregation or join
+constexpr int kTileRows = 4096;  // rows per tile
+
+// One VectorBatch as the kernels see it.  cols[i] / nulls[i] are the values and the null
+// bitmap (LSB-first, set bit = NULL) of kernel input i; nulls[i] == nullptr means the
+// column has no nulls in this batch.
+struct BatchDesc {
+    const void *cols[kMaxInputs];
+    const uint8_t *nulls[kMaxInputs];
+    int64_t rows;
+    int64_t rowBase;  // index of the batch's first row in arrival order
+};
+
+struct TileDesc {
+    int32_t batch;
+    int32_t row0;
+    int32_t rows;
+    int32_t pad;
+};
+
+// How kernel input values are widened.
+enum InKind : int16_t { IN_INT = 0, IN_DOUBLE = 1, IN_FLOAT = 2, IN_DEC128 = 3, IN_NONE = 4 };
+
+// ---- group-by key -------------------------------------------------------------------------
+// KEY_SINGLE: one integer-like column widened to int64; the NULL key is its own group.
+// KEY_PACKED: several fixed-width columns packed little-endian into `words` 64-bit words,
+// followed by a null-mask byte (bit c set = column c is NULL; its value bytes are zero).
+enum KeyKind : int32_t { KEY_SINGLE = 0, KEY_PACKED = 1 };
+
+struct KeyCol {
+    int16_t input;       // kernel input index
+    int16_t width;       // bytes: 1, 2, 4, 8, 16
+    int16_t byteOffset;  // offset inside the packed key
+    int16_t pad;
+};
+
+struct KeySpec {
+    int32_t kind;
+    int32_t nCols;
+    int32_t words;       // packed words (KEY_PACKED), 1 for KEY_SINGLE
+    int32_t maskByte;    // byte offset of the null mask (KEY_PACKED)
+    KeyCol cols[kMaxKeyCols];
+};
+
+// ---- accumulators -----------------------------------------------------------------------------
+// Per-group state is a row of 64-bit words.  Every aggregate is computed from these:
+//  COUNT_ALL  rows of the group                          1 word
+//  NULLS      NULL rows of input column `input`          1 word   (COUNT(col) = COUNT_ALL - NULLS)
+//  ISUM       wrapping int64 sum                         1 word
+//  WSUM2      exact sum as two unsigned 128-bit halves   4 words  (pos lo/hi, neg lo/hi)
+//  WSUM3      the same with 192-bit halves               6 words
+//  DSUM       compensated double sum (s, c)              2 words
+//  IMIN/IMAX  int64 min / max                            1 word
+//  DMIN/DMAX  double min / max as order-preserving int64 1 word
+enum AccKind : int16_t {
+    ACC_COUNT_ALL = 0,
+    ACC_NULLS = 1,
+    ACC_ISUM = 2,
+    ACC_WSUM2 = 3,
+    ACC_WSUM3 = 4,
+    ACC_DSUM = 5,
+    ACC_IMIN = 6,
+    ACC_IMAX = 7,
+    ACC_DMIN = 8,
+    ACC_DMAX = 9,
+};
+
+struct AccSpec {
+    int16_t kind;
+    int16_t input;    // kernel input index (-1 for COUNT_ALL)
+    int16_t inKind;   // InKind
+    int16_t inWidth;  // bytes per input value
+    int32_t word;     // first state word
+    int32_t pad;
+    int64_t init;     // initial value of the first word
+};
+
+inline int AccWords(int kind)
+{
+    switch (kind) {
+        case ACC_WSUM2:
+            return 4;
+        case ACC_WSUM3:
+            return 6;
+        case ACC_DSUM:
+            return 2;
+        default:
+            return 1;
+    }
+}
+
+// Global open-addressing group table.  Slot s occupies slotWords words at
+// slots + s * slotWords: [key words][state words].  KEY_SINGLE: one key word, EMPTY marks a
+// free slot (a real key equal to EMPTY lives in the special slot kSentinelSlot).  KEY_PACKED:
+// a tag word (0 free, 1 being written, else published) and `words` key words.  Two special
+// slots follow the `capacity` hashed slots: the NULL-key group and the EMPTY-key group.
+constexpr uint64_t kEmptyKey = 0x8000000000000000ull;
+constexpr int kNullSlotOffset = 0;      // slot capacity + 0
+constexpr int kSentinelSlotOffset = 1;  // slot capacity + 1
+
+struct AggTable {
+    uint64_t *slots;
+    uint64_t capacity;  // power of two
+    int32_t slotWords;
+    int32_t keyWords;   // words before the state
+    uint32_t *specialUsed;            // [2] flags of the special slots
+    unsigned long long *groupCount;   // groups inserted so far (block-aggregated)
+};
+
+struct AggLaunch {
+    const BatchDesc *batches;
+    const TileDesc *tiles;
+    int32_t nTiles;
+    int32_t nAccs;
+    KeySpec key;
+    AccSpec accs[kMaxAccs];
+    int32_t stateWords;
+    int32_t maxProbe;
+    AggTable table;
+    // Rows whose group could not be placed (probe limit hit) are queued here as
+    // (batch << 32 | row) and re-run after the table grows.
+    unsigned long long *retry;
+    unsigned int *nRetry;
+    uint32_t retryCap;
+    // When non-null the kernel processes these queued rows instead of the tiles.
+    const unsigned long long *retryIn;
+    uint32_t nRetryIn;
+    int32_t smemSlots;  // per-CTA shared-memory pre-aggregation slots (0 = off)
+    int32_t *error;     // sticky device error code (0 = none)
+    long long waitBudget;  // clock64 ticks a thread may wait for another's slot publication
+};
+
+// Default bounded-wait budget (clock64 ticks, about two seconds at 2 GHz).
+constexpr long long kDefaultWaitBudget = 1ll << 32;
+
+// ---- aggregation output ---------------------------------------------------------------------
+enum OutKind : int16_t {
+    OUT_KEY = 0,         // group-by column `src`
+    OUT_COUNT = 1,       // COUNT(col) / COUNT(*)
+    OUT_SUM_WRAP = 2,    // Spark int SUM (wrapping)
+    OUT_SUM_EXACT = 3,   // generic int SUM / decimal SUM from WSUM2/WSUM3
+    OUT_SUM_DOUBLE = 4,  // double SUM
+    OUT_AVG = 5,         // double AVG
+    OUT_MIN_INT = 6,
+    OUT_MAX_INT = 7,
+    OUT_MIN_DOUBLE = 8,
+    OUT_MAX_DOUBLE = 9,
+};
+
+struct OutSpec {
+    int16_t kind;
+    int16_t src;        // key column (OUT_KEY) or main accumulator index
+    int16_t countAcc;   // NULLS accumulator of the input column (-1 = COUNT(*))
+    int16_t outWidth;   // bytes per output value
+    int16_t outType;    // DataTypeId of the output
+    int16_t boundKind;  // OUT_SUM_EXACT: 0 = int64 range, 1 = decimal(38) range
+    int16_t rescalePow; // OUT_SUM_EXACT: multiply the sum by 10^rescalePow
+    int16_t pad;
+    void *values;       // device output column
+    uint8_t *nulls;     // device output null bitmap (zeroed by the host)
+};
+
+struct AggExtract {
+    AggTable table;
+    KeySpec key;
+    AccSpec accs[kMaxAccs];
+    int32_t nAccs;
+    int32_t nOut;
+    OutSpec out[kMaxOutCols];
+    unsigned long long *outCount;  // rows written
+    int32_t overflowAsNull;
+    int32_t *error;                // set to 1 on overflow when overflow is an error
+    unsigned long long *nAmbiguous;    // groups whose sticky-overflow result is order dependent
+    unsigned long long *ambiguousSlots;  // their slot ids (capacity ambiguousCap)
+    uint32_t ambiguousCap;
+    // Groups resolved by the ordered path: slot -> forced state (per OUT_SUM_EXACT column):
+    // 0 = use the exact sum, 1 = overflowed.  nullptr when there are none.
+    const uint8_t *forcedOverflow;
+};
+
+// ---- join ---------------------------------------------------------------------------------------
+// Build side columns are gathered into contiguous HBM arrays.  ARRAY mode indexes a table by
+// key - minKey; HASH mode is open addressing on the 64-bit key.  An entry holds either the
+// build row (unique keys) or an offset/count pair into a CSR of build rows (duplicates).
+enum JoinMode : int32_t { JOIN_ARRAY = 0, JOIN_HASH = 1 };
+
+struct JoinTable {
+    int32_t mode;
+    int32_t unique;           // 1: entries are rows, 0: entries are (offset << 32 | count)
+    int64_t minKey;
+    uint64_t range;           // ARRAY: number of entries
+    uint64_t capacity;        // HASH: power of two
+    const int64_t *arrayEntries;   // ARRAY: entry per key - minKey, -1 = none
+    const uint64_t *hashKeys;      // HASH: keys, kEmptyKey = free
+    const int64_t *hashEntries;    // HASH: entry per slot
+    int64_t sentinelEntry;         // entry of the key equal to kEmptyKey (-1 = none)
+    const int32_t *csrRows;        // build rows grouped by key
+    int32_t keyWidth;              // probe key width in bytes
+    int32_t pad;
+};
+
+struct JoinOutCol {
+    int16_t side;    // 0 = probe column, 1 = build column
+    int16_t src;     // probe kernel input index / build column index
+    int16_t width;   // bytes
+    int16_t pad;
+    const void *buildValues;     // side 1: contiguous build column in HBM
+    const uint8_t *buildNulls;   // side 1: contiguous build null bitmap (nullptr = no nulls)
+    void *values;                // output column
+    uint8_t *nulls;              // output null bitmap (nullptr = output has no nulls)
+};
+
+struct ProbeLaunch {
+    const BatchDesc *batches;
+    const TileDesc *tiles;
+    int32_t nTiles;
+    int32_t keyInput;     // kernel input index of the probe key
+    int32_t keyWidth;
+    int32_t nOut;
+    JoinTable table;
+    JoinOutCol out[kMaxOutCols];
+    unsigned long long *outCount;  // total matches (also counted past capacity)
+    uint64_t outCapacity;
+    int32_t countOnly;
+    int32_t *error;
+};
+
+}  // namespace omg

@@ -1,0 +1,110 @@
+// HashAggregationOperatorFactory / HashAggregationOperator for GB300.
+//
+// Same constructor and call surface as the reference
+// (operator/aggregation/group_aggregation.h:203-301): the factory takes the group-by
+// columns and types, per-aggregator input columns, input and output types and function
+// ids, mask columns, the inputRaw/outputPartial flags and overflowAsNull.  The operator
+// takes ownership of each AddInput batch, aggregates on the GPU, and GetOutput returns the
+// groups in batches of ceil(1 MiB / rowBytes) rows, returning 1 per produced batch and
+// setting OMNI_STATUS_FINISHED after the last (group_aggregation.cpp:454-474,1486-1538).
+#pragma once
+
+#include <cstdint>
+#include <deque>
+#include <memory>
+#include <vector>
+
+#include "kernels/plan.h"
+#include "operator.h"
+
+namespace omg {
+class OpStream;
+template <typename T> class DevArray;
+}
+
+namespace omniruntime {
+namespace op {
+
+// The compiled form of a factory's aggregation: kernel inputs, key packing, accumulators
+// and output columns.
+struct AggPlan {
+    std::vector<int32_t> inputCols;        // batch column of each kernel input
+    omg::KeySpec key{};
+    std::vector<omg::AccSpec> accs;
+    int32_t stateWords = 0;
+    int32_t keyWords = 0;                  // words before the state in a table slot
+    int32_t slotWords = 0;
+    std::vector<omg::OutSpec> outs;        // pointers filled at extraction
+    std::vector<type::DataTypePtr> outTypes;
+    int32_t rowsPerBatch = 0;
+    bool overflowAsNull = false;
+    bool orderDependent = false;           // has an OUT_SUM_EXACT column (sticky overflow)
+};
+
+class HashAggregationOperatorFactory : public OperatorFactory {
+public:
+    HashAggregationOperatorFactory(std::vector<uint32_t> &groupByCol, const type::DataTypes &groupInputTypes,
+        std::vector<std::vector<uint32_t>> &aggsCols, std::vector<type::DataTypes> &aggInputTypes,
+        std::vector<type::DataTypes> &aggOutputTypes, std::vector<uint32_t> &aggFuncTypes,
+        std::vector<uint32_t> &maskColsVector, std::vector<bool> inputRaws, std::vector<bool> outputPartials,
+        bool overflowAsNull = false);
+    ~HashAggregationOperatorFactory() override = default;
+
+    // Compiles and validates the plan; throws OmniException on unsupported shapes.
+    OmniStatus Init();
+    Operator *CreateOperator() override;
+    const AggPlan &Plan() const { return plan_; }
+
+private:
+    std::vector<uint32_t> groupByCols_;
+    type::DataTypes groupTypes_;
+    std::vector<std::vector<uint32_t>> aggCols_;
+    std::vector<type::DataTypes> aggInputTypes_;
+    std::vector<type::DataTypes> aggOutputTypes_;
+    std::vector<uint32_t> aggFuncTypes_;
+    std::vector<uint32_t> maskCols_;
+    std::vector<bool> inputRaws_;
+    std::vector<bool> outputPartials_;
+    bool overflowAsNull_;
+    SupportContainerVecRule policy_;
+    AggPlan plan_;
+    bool inited_ = false;
+};
+
+class HashAggregationOperator : public Operator {
+public:
+    explicit HashAggregationOperator(const AggPlan &plan);
+    ~HashAggregationOperator() override;
+
+    int32_t AddInput(VectorBatch *vecBatch) override;
+    int32_t GetOutput(VectorBatch **outputVecBatch) override;
+    OmniStatus Close() override;
+    uint64_t GetHashMapUniqueKeys() override { return uniqueKeys_; }
+
+    // Strategy hint (OMG_AGG_STRATEGY_*) and initial capacity in groups (0 = default).
+    void SetStrategy(int32_t strategy, int64_t capacityHint)
+    {
+        strategy_ = strategy;
+        capacityHint_ = capacityHint;
+    }
+
+private:
+    struct Impl;
+    void Flush();
+    void Extract();
+    void ReleasePending();
+
+    AggPlan plan_;
+    std::unique_ptr<Impl> impl_;
+    std::vector<VectorBatch *> pending_;
+    int64_t pendingRows_ = 0;
+    std::deque<VectorBatch *> outputs_;
+    bool hasInputedData_ = false;
+    bool extracted_ = false;
+    uint64_t uniqueKeys_ = 0;
+    int32_t strategy_ = 0;
+    int64_t capacityHint_ = 0;
+};
+
+}  // namespace op
+}  // namespace omniruntime

@@ -1,0 +1,99 @@
+// HashBuilderOperator(Factory) and LookupJoinOperator(Factory) for GB300, inner equi-join.
+//
+// Call surface as in the reference (operator/join/hash_builder.h:18-80,
+// operator/join/lookup_join.h:136-200): builder operators retain their batches and build the
+// table when GetOutput runs after noMoreInput (hash_builder.cpp:169-213); probe operators
+// report kWaitForJoinBuild until every builder finished (lookup_join.cpp:270-277), take
+// ownership of probe batches and emit (probe output columns, build output columns) rows in
+// batches of at most ceil(1 MiB / rowSize) rows (lookup_join.cpp:419-480,1628-1640).
+//
+// GB300 specifics: the build table and build columns live in HBM; the probe of one or many
+// queued batches is one kernel launch.  With noMoreInput left true (per-batch callers) each
+// AddInput batch is probed at the next GetOutput; pipelined callers that set it false get
+// their batches probed in large chunks.
+#pragma once
+
+#include <cstdint>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "kernels/plan.h"
+#include "operator.h"
+
+namespace omniruntime {
+namespace op {
+
+struct JoinBuildState;
+
+class HashBuilderOperatorFactory : public OperatorFactory {
+public:
+    HashBuilderOperatorFactory(JoinType joinType, const type::DataTypes &buildTypes, const int32_t *buildHashCols,
+        int32_t buildHashColsCount, int32_t operatorCount);
+    ~HashBuilderOperatorFactory() override;
+    static HashBuilderOperatorFactory *CreateHashBuilderOperatorFactory(JoinType joinType,
+        const type::DataTypes &buildTypes, const int32_t *buildHashCols, int32_t buildHashColsCount,
+        int32_t operatorCount);
+    Operator *CreateOperator() override;
+    JoinBuildState *GetBuildState() { return state_.get(); }
+
+private:
+    std::unique_ptr<JoinBuildState> state_;
+};
+
+class HashBuilderOperator : public Operator {
+public:
+    explicit HashBuilderOperator(JoinBuildState *state) : state_(state) {}
+    int32_t AddInput(VectorBatch *vecBatch) override;
+    int32_t GetOutput(VectorBatch **outputVecBatch) override;
+    OmniStatus Close() override { return OMNI_STATUS_NORMAL; }
+
+private:
+    JoinBuildState *state_;
+    bool counted_ = false;
+};
+
+class LookupJoinOperatorFactory : public OperatorFactory {
+public:
+    LookupJoinOperatorFactory(const type::DataTypes &probeTypes, const int32_t *probeOutputCols,
+        int32_t probeOutputColsCount, const int32_t *probeHashCols, int32_t probeHashColsCount,
+        const int32_t *buildOutputCols, int32_t buildOutputColsCount, const type::DataTypes &buildOutputTypes,
+        HashBuilderOperatorFactory *builder);
+    static LookupJoinOperatorFactory *CreateLookupJoinOperatorFactory(const type::DataTypes &probeTypes,
+        int32_t *probeOutputCols, int32_t probeOutputColsCount, int32_t *probeHashCols, int32_t probeHashColsCount,
+        int32_t *buildOutputCols, int32_t buildOutputColsCount, const type::DataTypes &buildOutputTypes,
+        int64_t hashBuilderFactoryAddr, const void *filterExpr, bool isShuffleExchangeBuildPlan,
+        const void *overflowConfig);
+    Operator *CreateOperator() override;
+
+    type::DataTypes probeTypes;
+    std::vector<int32_t> probeOutputCols;
+    std::vector<int32_t> probeHashCols;
+    std::vector<int32_t> buildOutputCols;
+    type::DataTypes buildOutputTypes;
+    JoinBuildState *build;
+    int32_t rowsPerBatch;
+};
+
+class LookupJoinOperator : public Operator {
+public:
+    explicit LookupJoinOperator(const LookupJoinOperatorFactory &f);
+    ~LookupJoinOperator() override;
+    int32_t AddInput(VectorBatch *vecBatch) override;
+    int32_t GetOutput(VectorBatch **outputVecBatch) override;
+    OmniStatus Close() override;
+    BlockingReason IsBlocked() override;
+
+private:
+    struct Impl;
+    void ProcessPending();
+    const LookupJoinOperatorFactory &f_;
+    std::unique_ptr<Impl> impl_;
+    std::vector<VectorBatch *> pending_;
+    int64_t pendingRows_ = 0;
+    std::deque<VectorBatch *> outputs_;
+};
+
+}  // namespace op
+}  // namespace omniruntime

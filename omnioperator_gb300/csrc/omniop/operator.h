@@ -1,0 +1,72 @@
+// Operator / OperatorFactory base classes with the reference's method names and state
+// machine (operator/operator.h:22-266, operator/operator_factory.h:13-29).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "types.h"
+#include "vector.h"
+
+namespace omniruntime {
+namespace op {
+using vec::VectorBatch;
+
+enum class BlockingReason { kNotBlocked = 0, kWaitForJoinBuild = 1 };
+
+class Operator {
+public:
+    Operator() = default;
+    virtual ~Operator() = default;
+
+    virtual int32_t AddInput(VectorBatch *vecBatch) = 0;
+    virtual int32_t GetOutput(VectorBatch **result) = 0;
+
+    static void DeleteOperator(Operator *op)
+    {
+        op->Close();
+        delete op;
+    }
+
+    OmniStatus GetStatus() const { return status_; }
+    void SetStatus(OmniStatus s) { status_ = s; }
+    virtual OmniStatus Init() { return OMNI_STATUS_NORMAL; }
+    virtual OmniStatus Close() { return OMNI_STATUS_NORMAL; }
+    virtual uint64_t GetHashMapUniqueKeys() { return 0; }
+    virtual BlockingReason IsBlocked() { return BlockingReason::kNotBlocked; }
+
+    // noMoreInput_ defaults to true, as in the reference (operator.h:204): a caller that
+    // feeds one batch and drains it needs no further call.  Pipelined callers (the
+    // reference's LocalPlanner, compute/local_planner.cpp:34) set it false and call
+    // noMoreInput() at the end, which lets the GB300 operators batch many VectorBatches
+    // into one kernel launch.
+    virtual void noMoreInput() { noMoreInput_ = true; }
+    virtual void setNoMoreInput(bool v) { noMoreInput_ = v; }
+    virtual bool needsInput() { return status_ != OMNI_STATUS_FINISHED && !noMoreInput_; }
+    bool isFinished() const { return status_ == OMNI_STATUS_FINISHED; }
+
+    // GB300 controls.
+    void SetStream(void *stream) { userStream_ = stream; }
+    void SetDeviceOutput(bool on) { deviceOutput_ = on; }
+    const std::vector<int64_t> &Counters() const { return counters_; }
+
+protected:
+    bool noMoreInput_ = true;
+    void *userStream_ = nullptr;
+    bool deviceOutput_ = false;
+    std::vector<int64_t> counters_ = std::vector<int64_t>(8, 0);
+
+private:
+    OmniStatus status_ = OMNI_STATUS_NORMAL;
+};
+
+class OperatorFactory {
+public:
+    OperatorFactory() = default;
+    virtual ~OperatorFactory() = default;
+    virtual Operator *CreateOperator() { return nullptr; }
+};
+
+}  // namespace op
+}  // namespace omniruntime

@@ -1,0 +1,141 @@
+// OmniVec columnar format for the GB300 operators.
+//
+// Layout follows the reference (vector/vector.h:45-404, vector/nulls_buffer.h:16-114):
+//  - flat values, one fixed-width element per row;
+//  - a null bitmap, LSB-first, bit set = NULL, of NullsBuffer::CalculateNbytes(n) =
+//    ceil(n/8) + 8 bytes (the 8 spare bytes let 64-bit word loads run past the end).
+// Both live in one Buffer each, host-pinned or in HBM (Residency).  A vector may be a
+// view into a larger buffer (offset), which is how GetOutput carves many output batches
+// out of one device->host copy without per-batch allocations.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "memory.h"
+#include "types.h"
+
+namespace omniruntime {
+namespace vec {
+using namespace omniruntime::type;
+
+enum Encoding { OMNI_FLAT = 0, OMNI_DICTIONARY = 1 };
+
+class NullsBuffer {
+public:
+    static constexpr int32_t CalculateNbytes(int32_t bits) { return (bits + 7) / 8 + 8; }
+};
+
+class BaseVector {
+public:
+    // New owned flat vector, host or device.  Values and nulls are zeroed.
+    BaseVector(DataTypeId type, int32_t width, int32_t size, bool device, void *stream = nullptr);
+    // View over existing buffers (values at byte offset `valuesOffset`, nulls at byte offset
+    // `nullsOffset`; nulls may be null).
+    BaseVector(DataTypeId type, int32_t width, int32_t size, omg::BufferPtr values, size_t valuesOffset,
+        omg::BufferPtr nulls, size_t nullsOffset, bool hasNull);
+    virtual ~BaseVector() = default;
+
+    int32_t GetSize() const { return size_; }
+    DataTypeId GetTypeId() const { return type_; }
+    int32_t GetWidth() const { return width_; }
+    Encoding GetEncoding() const { return OMNI_FLAT; }
+    bool IsDevice() const { return values_->IsDevice(); }
+
+    uint8_t *RawValues() const { return static_cast<uint8_t *>(values_->Data()) + valuesOffset_; }
+    // Null bitmap (nullptr for a device view created without nulls).
+    uint8_t *RawNulls() const
+    {
+        return nulls_ ? static_cast<uint8_t *>(nulls_->Data()) + nullsOffset_ : nullptr;
+    }
+
+    // Host-only accessors (vector/vector.h SetNull/IsNull/HasNull).
+    void SetNull(int32_t i)
+    {
+        RawNulls()[i >> 3] |= static_cast<uint8_t>(1u << (i & 7));
+        hasNull_ = true;
+    }
+    void SetNotNull(int32_t i) { RawNulls()[i >> 3] &= static_cast<uint8_t>(~(1u << (i & 7))); }
+    bool IsNull(int32_t i) const
+    {
+        const uint8_t *n = RawNulls();
+        return n != nullptr && ((n[i >> 3] >> (i & 7)) & 1u);
+    }
+    // hasNull is a hint kept by the writer (NullsBuffer::SetNullFlag); HasNull() scans the
+    // bitmap of a host vector when the hint is false, as NullsBuffer::HasNull does.
+    bool HasNull();
+    void SetNullFlag(bool hasNull) { hasNull_ = hasNull; }
+    bool NullFlag() const { return hasNull_; }
+    int32_t GetNullCount();
+
+    const omg::BufferPtr &ValuesBuffer() const { return values_; }
+    const omg::BufferPtr &NullsBufferPtr() const { return nulls_; }
+    size_t ValuesOffset() const { return valuesOffset_; }
+    size_t NullsOffset() const { return nullsOffset_; }
+
+protected:
+    DataTypeId type_;
+    int32_t width_;
+    int32_t size_;
+    bool hasNull_ = false;
+    omg::BufferPtr values_;
+    size_t valuesOffset_ = 0;
+    omg::BufferPtr nulls_;
+    size_t nullsOffset_ = 0;
+};
+
+// Typed host accessor (vector/vector.h Vector<T>::GetValue/SetValue).
+template <typename T> class Vector : public BaseVector {
+public:
+    using BaseVector::BaseVector;
+    T GetValue(int32_t i) const
+    {
+        T v;
+        std::memcpy(&v, RawValues() + static_cast<size_t>(i) * sizeof(T), sizeof(T));
+        return v;
+    }
+    void SetValue(int32_t i, T v) { std::memcpy(RawValues() + static_cast<size_t>(i) * sizeof(T), &v, sizeof(T)); }
+};
+
+class VectorBatch {
+public:
+    explicit VectorBatch(size_t rowCnt) : rowCnt_(rowCnt) {}
+    ~VectorBatch();
+    VectorBatch(const VectorBatch &) = delete;
+    VectorBatch &operator=(const VectorBatch &) = delete;
+
+    void Append(BaseVector *vector) { vectors_.push_back(vector); }
+    BaseVector *Get(int32_t index) const { return vectors_.at(index); }
+    int32_t GetRowCount() const { return static_cast<int32_t>(rowCnt_); }
+    int32_t GetVectorCount() const { return static_cast<int32_t>(vectors_.size()); }
+    void Resize(size_t rowCount) { rowCnt_ = rowCount; }
+    void FreeAllVectors();
+    void ClearVectors() { vectors_.clear(); }
+    bool IsDevice() const;
+
+private:
+    size_t rowCnt_;
+    std::vector<BaseVector *> vectors_;
+};
+
+class VectorHelper {
+public:
+    // VectorHelper::FreeVecBatch: delete the batch and its vectors.
+    static void FreeVecBatch(VectorBatch *batch)
+    {
+        if (batch != nullptr) {
+            batch->FreeAllVectors();
+            delete batch;
+        }
+    }
+    static BaseVector *CreateFlatVector(DataTypeId type, int32_t size, int32_t width = 0)
+    {
+        return new BaseVector(type, TypeWidth(type, width), size, false);
+    }
+    // Deep copy of a batch into host or device residency.
+    static VectorBatch *CopyBatch(VectorBatch *batch, bool toDevice, void *stream);
+};
+
+}  // namespace vec
+}  // namespace omniruntime

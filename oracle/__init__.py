@@ -1,0 +1,173 @@
+"""CPU oracle of the hash aggregation / inner hash join path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may import this
+package, and only as the checker or the timed CPU baseline; the product never does.
+
+``oracle.c`` restates the reference's algorithms (file:line citations at its top).  The
+reference itself cannot be compiled here or on the GPU machine: its hot-path translation units need
+jemalloc, libboundscheck (securec), LLVM (via filter_and_project.h), nlohmann-json and JNI
+logging, and the build uses the reference's own CMake.  Parity of the restatement is pinned by
+the reference's test vectors in tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "oracle.c"
+BUILD = HERE / "_build"
+LIB = BUILD / "liboracle.so"
+
+_lib = None
+
+# Type / function ids (reference numbering, type/data_type.h:40-74, function_type.h:11-27).
+T_INT, T_LONG, T_DOUBLE, T_BOOLEAN, T_SHORT, T_DEC64, T_DEC128 = 1, 2, 3, 4, 5, 6, 7
+T_DATE32, T_BYTE, T_FLOAT = 8, 18, 19
+F_SUM, F_COUNT_COL, F_COUNT_ALL, F_AVG, F_MAX, F_MIN = 0, 1, 2, 3, 5, 6
+
+WIDTH = {T_INT: 4, T_LONG: 8, T_DOUBLE: 8, T_BOOLEAN: 1, T_SHORT: 2, T_DEC64: 8, T_DEC128: 16,
+         T_DATE32: 4, T_BYTE: 1, T_FLOAT: 4}
+
+
+def build() -> Path:
+    """Compile oracle.c with gcc (portable flags: the same source builds on x86 and Arm)."""
+    BUILD.mkdir(exist_ok=True)
+    if not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+        tmp = LIB.with_suffix(".tmp.so")
+        subprocess.run(["gcc", "-O3", "-fPIC", "-shared", "-std=gnu11", "-o", str(tmp), str(SRC), "-lpthread"],
+                       check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P, I32, I64 = C.c_void_p, C.c_int32, C.c_int64
+        L.orc_hashagg.restype = I64
+        L.orc_hashagg.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P]
+        L.orc_join_inner.restype = I64
+        L.orc_join_inner.argtypes = [I64, P, I32, P, I64, P, I32, P, P, P, I64]
+        L.orc_join_probe_bench.restype = I64
+        L.orc_join_probe_bench.argtypes = [I64, P, P, I32, P, I64, P, P, I32, P]
+        L.orc_agg_bench.restype = I64
+        L.orc_agg_bench.argtypes = [I64, P, P, P, I32]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _ptr_array(arrs):
+    return (C.c_void_p * max(len(arrs), 1))(*[(a.ctypes.data if a is not None else None) for a in arrs])
+
+
+def hashagg(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=False):
+    """Single-stage hash aggregation with the reference's semantics.
+
+    keys: list of value arrays (int types as their numpy ints, decimal128 as (n, 2) uint64).
+    key_nulls: list of bool arrays or None.  aggs: list of dicts with keys func, col (array or
+    None for COUNT(*)), in_type, out_type, nulls (bool array or None), rescale (int).
+    Returns (key_values, key_nulls, agg_values, agg_nulls) per group (unordered), or raises
+    OverflowError when an overflow must raise (overflow-as-null off)."""
+    L = lib()
+    n = len(keys[0]) if keys else 0
+    kw = [WIDTH[t] for t in key_types]
+    kcols = [np.ascontiguousarray(k) for k in keys]
+    knulls = [None if m is None else np.ascontiguousarray(m, dtype=np.uint8) for m in key_nulls]
+    funcs = np.array([a["func"] for a in aggs], dtype=np.int32)
+    cols, in_types, in_widths, anulls, out_types, rescale = [], [], [], [], [], []
+    for a in aggs:
+        col = a.get("col")
+        if col is None:
+            col = np.zeros(max(n, 1), dtype=np.int64)
+            in_types.append(T_LONG)
+        else:
+            in_types.append(a["in_type"])
+        cols.append(np.ascontiguousarray(col))
+        in_widths.append(WIDTH[in_types[-1]])
+        m = a.get("nulls")
+        anulls.append(None if m is None else np.ascontiguousarray(m, dtype=np.uint8))
+        out_types.append(a["out_type"])
+        rescale.append(a.get("rescale", 0))
+    in_types = np.array(in_types, dtype=np.int32)
+    in_widths = np.array(in_widths, dtype=np.int32)
+    out_types = np.array(out_types, dtype=np.int32)
+    rescale = np.array(rescale, dtype=np.int32)
+    maxg = max(n, 1)
+    okeys = [np.zeros((maxg, 2) if w == 16 else maxg, dtype=np.uint64 if w == 16 else
+                      {1: np.int8, 2: np.int16, 4: np.int32, 8: np.int64}[w]) for w in kw]
+    oknulls = [np.zeros(maxg, dtype=np.uint8) for _ in kw]
+    ovals = [np.zeros((maxg, 2), dtype=np.uint64) for _ in aggs]
+    ovnulls = [np.zeros(maxg, dtype=np.uint8) for _ in aggs]
+    g = L.orc_hashagg(n, len(keys), _ptr_array(kcols), _ptr(np.array(kw, dtype=np.int32)),
+                      _ptr_array(knulls), len(aggs), _ptr(funcs), _ptr_array(cols), _ptr(in_types),
+                      _ptr(in_widths), _ptr_array(anulls), _ptr(out_types), _ptr(rescale), policy,
+                      1 if overflow_as_null else 0, maxg, _ptr_array(okeys), _ptr_array(oknulls),
+                      _ptr_array(ovals), _ptr_array(ovnulls))
+    if g == -2:
+        raise OverflowError("sum_aggregator overflow.")
+    if g < 0:
+        raise RuntimeError(f"oracle hashagg failed ({g})")
+    vals = []
+    for a, ov in zip(aggs, ovals):
+        t = a["out_type"]
+        raw = ov.reshape(-1)  # the oracle writes a dense array of the output type
+        if t == T_DEC128:
+            vals.append(raw.reshape(maxg, 2)[:g].copy())
+        else:
+            dt = {T_DOUBLE: np.float64, T_FLOAT: np.float32, T_INT: np.int32, T_DATE32: np.int32,
+                  T_SHORT: np.int16, T_BYTE: np.int8, T_BOOLEAN: np.int8}.get(t, np.int64)
+            vals.append(raw.view(np.uint8).view(dt)[:g].copy())
+    return ([k[:g] for k in okeys], [m[:g].astype(bool) for m in oknulls], vals,
+            [m[:g].astype(bool) for m in ovnulls])
+
+
+def join_inner(build_keys, build_nulls, probe_keys, probe_nulls):
+    """(probe_row, build_row) index pairs of the inner equi-join, NULL keys never matching."""
+    L = lib()
+    bk = np.ascontiguousarray(build_keys)
+    pk = np.ascontiguousarray(probe_keys)
+    bn = None if build_nulls is None else np.ascontiguousarray(build_nulls, dtype=np.uint8)
+    pn = None if probe_nulls is None else np.ascontiguousarray(probe_nulls, dtype=np.uint8)
+    cap = max(len(pk), 1)
+    while True:
+        op = np.empty(cap, dtype=np.int64)
+        ob = np.empty(cap, dtype=np.int64)
+        n = L.orc_join_inner(len(bk), _ptr(bk), bk.dtype.itemsize, _ptr(bn), len(pk), _ptr(pk),
+                             pk.dtype.itemsize, _ptr(pn), _ptr(op), _ptr(ob), cap)
+        if n < 0:
+            raise RuntimeError("oracle join failed")
+        if n <= cap:
+            return op[:n], ob[:n]
+        cap = n
+
+
+def exact_group_sums(group_ids: np.ndarray, values: np.ndarray, valid: np.ndarray | None, ngroups: int):
+    """Correctly rounded per-group sums (math.fsum) and per-group sums of |x|, the reference
+    values of the double tolerance."""
+    if valid is not None:
+        group_ids = group_ids[valid]
+        values = values[valid]
+    order = np.argsort(group_ids, kind="stable")
+    g = group_ids[order]
+    v = values[order]
+    bounds = np.searchsorted(g, np.arange(ngroups + 1))
+    exact = np.zeros(ngroups)
+    absum = np.zeros(ngroups)
+    for i in range(ngroups):
+        seg = v[bounds[i]:bounds[i + 1]]
+        if len(seg):
+            exact[i] = math.fsum(seg.tolist())
+            absum[i] = math.fsum(np.abs(seg).tolist())
+    return exact, absum

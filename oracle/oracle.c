@@ -1,0 +1,741 @@
+/*
+ * oracle.c -- CPU restatement of OmniOperator's hash aggregation and inner hash join,
+ * used ONLY as test infrastructure: the parity checker of the GB300 kernels and the timed
+ * CPU baseline.  Nothing in the product links or calls this file.
+ *
+ * It follows the reference's semantics, not its data structures:
+ *  - aggregation states are updated row by row in arrival order, exactly as the reference's
+ *    AddUseRowIndex / AddConditionalUseRowIndex loops do
+ *    (operator/aggregation/aggregator/operations_hash_aggregator.h:16-76);
+ *  - SUM of integers under the Spark policy wraps (sum_flatim_aggregator.h:33 with
+ *    SumOp<..., CareOverFlow=false>, sum_aggregator.h:49-52); under the generic policy it is
+ *    checked with __builtin_add_overflow and sticky (sum_aggregator.h:43-49, count = -1);
+ *  - SUM of decimals adds in int128 with AddCheckedOverflow against +-(10^38-1)
+ *    (type/base_operations.h:20-28) and is sticky (sum_spark_decimal_aggregator.h:16-66); a
+ *    decimal64 result adds in int64 with __builtin_add_overflow; the result is rescaled by
+ *    10^(outScale-inScale) with MulCheckedOverflow (sum_spark_decimal_aggregator.h:180-245);
+ *  - SUM/AVG of doubles is the naive fold `value += x` (operations_hash_aggregator.h:28-30,
+ *    average_flatim_aggregator.h:225-290); AVG of integers converts each value to double first;
+ *  - MIN/MAX start at the type's max/lowest and apply std::min/std::max in row order
+ *    (min_aggregator.h:16-45, max_aggregator.h:16-45), so NaN inputs never replace the state;
+ *  - COUNT(col) counts non-null values, COUNT(*) all rows (count_*_aggregator.h);
+ *  - a NULL group-by key is its own group (hashmap/base_hash_map.h:579-589); keys compare by
+ *    value bytes (fixed-width handlers and the serialized composite key of
+ *    hashmap/column_marshaller.h:27-287, where a NULL column differs from any value);
+ *  - inner join: NULL keys never match; every (probe row, build row) pair with equal keys is
+ *    emitted (operator/join/lookup_join.cpp:924-1035, join_hash_table_variants.cpp:695-863).
+ * Output order is not part of the contract (the reference emits in hash-slot order), so the
+ * tables here are plain open addressing.  Parity of this file is pinned by the reference's
+ * own test vectors (tests/golden/).
+ */
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef __int128 i128;
+
+enum { T_INT = 1, T_LONG = 2, T_DOUBLE = 3, T_BOOLEAN = 4, T_SHORT = 5, T_DEC64 = 6, T_DEC128 = 7, T_DATE32 = 8,
+    T_DATE64 = 9, T_TIMESTAMP = 12, T_BYTE = 18, T_FLOAT = 19 };
+enum { F_SUM = 0, F_COUNT_COL = 1, F_COUNT_ALL = 2, F_AVG = 3, F_MAX = 5, F_MIN = 6 };
+enum { ST_EMPTY = 0, ST_NORMAL = 1, ST_OVERFLOW = 2 };
+
+static const i128 DEC38_MAX = (((i128)5421010862427522170LL) << 64) + (i128)687399551400673279ULL;
+
+static int64_t load_int(const void *col, int64_t r, int w)
+{
+    switch (w) {
+        case 1: return ((const int8_t *)col)[r];
+        case 2: return ((const int16_t *)col)[r];
+        case 4: return ((const int32_t *)col)[r];
+        default: return ((const int64_t *)col)[r];
+    }
+}
+
+static int is_int_type(int t)
+{
+    return t == T_INT || t == T_LONG || t == T_SHORT || t == T_BYTE || t == T_BOOLEAN || t == T_DATE32 ||
+        t == T_DATE64 || t == T_TIMESTAMP || t == T_DEC64;
+}
+
+static double load_double(const void *col, int64_t r, int t, int w)
+{
+    if (t == T_DOUBLE) return ((const double *)col)[r];
+    if (t == T_FLOAT) return (double)((const float *)col)[r];
+    return (double)load_int(col, r, w);
+}
+
+/* ---------------------------------------------------------------- group table */
+typedef struct {
+    int nkey;
+    int keybytes;        /* packed key: per column [null byte][width bytes] */
+    uint64_t cap;
+    uint8_t *keys;       /* cap * keybytes */
+    uint8_t *used;
+    int64_t *gid;        /* slot -> group id */
+    int64_t ngroups;
+    int64_t gcap;
+    uint8_t *gkeys;      /* group id -> key bytes */
+} table_t;
+
+static uint64_t hash_bytes(const uint8_t *p, int n)
+{
+    uint64_t h = 1469598103934665603ULL;
+    for (int i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ULL;
+    }
+    h ^= h >> 29;
+    h *= 0xbf58476d1ce4e5b9ULL;
+    h ^= h >> 32;
+    return h;
+}
+
+static int table_init(table_t *t, int nkey, int keybytes, uint64_t cap)
+{
+    memset(t, 0, sizeof(*t));
+    t->nkey = nkey;
+    t->keybytes = keybytes;
+    t->cap = cap;
+    t->keys = (uint8_t *)malloc(cap * (uint64_t)keybytes);
+    t->used = (uint8_t *)calloc(cap, 1);
+    t->gid = (int64_t *)malloc(cap * sizeof(int64_t));
+    t->gcap = 1024;
+    t->gkeys = (uint8_t *)malloc((uint64_t)t->gcap * keybytes);
+    return (t->keys && t->used && t->gid && t->gkeys) ? 0 : -1;
+}
+
+static void table_free(table_t *t)
+{
+    free(t->keys);
+    free(t->used);
+    free(t->gid);
+    free(t->gkeys);
+}
+
+static int table_grow(table_t *t)
+{
+    table_t n;
+    if (table_init(&n, t->nkey, t->keybytes, t->cap * 2) != 0) return -1;
+    for (uint64_t s = 0; s < t->cap; ++s) {
+        if (!t->used[s]) continue;
+        const uint8_t *k = t->keys + s * (uint64_t)t->keybytes;
+        uint64_t i = hash_bytes(k, t->keybytes) & (n.cap - 1);
+        while (n.used[i]) i = (i + 1) & (n.cap - 1);
+        n.used[i] = 1;
+        memcpy(n.keys + i * (uint64_t)n.keybytes, k, t->keybytes);
+        n.gid[i] = t->gid[s];
+    }
+    free(n.gkeys);
+    n.gkeys = t->gkeys;
+    n.gcap = t->gcap;
+    n.ngroups = t->ngroups;
+    free(t->keys);
+    free(t->used);
+    free(t->gid);
+    *t = n;
+    return 0;
+}
+
+/* Returns the group id of the key, inserting it (new id) if absent; -1 on allocation failure. */
+static int64_t table_find_insert(table_t *t, const uint8_t *k, int *isnew)
+{
+    if ((uint64_t)(t->ngroups + 1) * 2 > t->cap && table_grow(t) != 0) return -1;
+    uint64_t i = hash_bytes(k, t->keybytes) & (t->cap - 1);
+    while (t->used[i]) {
+        if (memcmp(t->keys + i * (uint64_t)t->keybytes, k, t->keybytes) == 0) {
+            *isnew = 0;
+            return t->gid[i];
+        }
+        i = (i + 1) & (t->cap - 1);
+    }
+    if (t->ngroups == t->gcap) {
+        uint8_t *g = (uint8_t *)realloc(t->gkeys, (uint64_t)t->gcap * 2 * t->keybytes);
+        if (!g) return -1;
+        t->gkeys = g;
+        t->gcap *= 2;
+    }
+    t->used[i] = 1;
+    memcpy(t->keys + i * (uint64_t)t->keybytes, k, t->keybytes);
+    t->gid[i] = t->ngroups;
+    memcpy(t->gkeys + (uint64_t)t->ngroups * t->keybytes, k, t->keybytes);
+    *isnew = 1;
+    return t->ngroups++;
+}
+
+/* ---------------------------------------------------------------- aggregation */
+typedef struct {
+    int func, in_type, in_width, out_type, rescale;
+    const void *col;
+    const uint8_t *nulls; /* byte per row, 1 = null; NULL = no nulls */
+} agg_t;
+
+typedef struct {
+    /* per group, per aggregator */
+    int64_t i64;      /* int sums, min/max, counts */
+    i128 wide;        /* decimal sums */
+    double d;         /* double sums / min / max */
+    int64_t count;    /* non-null count; -1 = sticky overflow (generic int sum) */
+    int8_t state;     /* ST_* */
+} state_t;
+
+typedef struct {
+    int nagg;
+    agg_t *aggs;
+    int policy; /* 0 spark, 1 generic */
+    state_t *st;
+    int64_t stcap;
+} aggctx_t;
+
+static void state_init(const agg_t *a, state_t *s)
+{
+    memset(s, 0, sizeof(*s));
+    if (a->func == F_MIN || a->func == F_MAX) {
+        int w = a->in_width;
+        int ow = 8;
+        if (a->out_type == T_INT || a->out_type == T_DATE32) ow = 4;
+        else if (a->out_type == T_SHORT) ow = 2;
+        else if (a->out_type == T_BYTE || a->out_type == T_BOOLEAN) ow = 1;
+        (void)w;
+        if (a->in_type == T_DOUBLE || a->in_type == T_FLOAT) {
+            const double lim = a->in_type == T_FLOAT ? 3.4028234663852886e38 : 1.7976931348623157e308;
+            s->d = a->func == F_MIN ? lim : -lim;
+        } else {
+            int64_t mx = ow == 1 ? INT8_MAX : ow == 2 ? INT16_MAX : ow == 4 ? INT32_MAX : INT64_MAX;
+            int64_t mn = ow == 1 ? INT8_MIN : ow == 2 ? INT16_MIN : ow == 4 ? INT32_MIN : INT64_MIN;
+            s->i64 = a->func == F_MIN ? mx : mn;
+        }
+    }
+}
+
+static void state_update(const aggctx_t *c, const agg_t *a, state_t *s, int64_t r)
+{
+    if (a->func == F_COUNT_ALL) {
+        s->i64++;
+        return;
+    }
+    if (a->nulls && a->nulls[r]) return;
+    switch (a->func) {
+        case F_COUNT_COL:
+            s->i64++;
+            return;
+        case F_SUM:
+            if (a->in_type == T_DOUBLE || a->in_type == T_FLOAT) {
+                s->d += load_double(a->col, r, a->in_type, a->in_width);
+                s->state = ST_NORMAL;
+            } else if (a->in_type == T_DEC64 || a->in_type == T_DEC128) {
+                if (s->state == ST_OVERFLOW) return;
+                if (a->out_type == T_DEC128) {
+                    i128 x;
+                    if (a->in_type == T_DEC128) {
+                        const uint64_t *p = (const uint64_t *)a->col + 2 * r;
+                        x = (i128)(((unsigned __int128)p[1] << 64) | p[0]);
+                    } else {
+                        x = (i128)load_int(a->col, r, 8);
+                    }
+                    i128 res;
+                    int ov = __builtin_add_overflow(s->wide, x, &res) || res > DEC38_MAX || res < -DEC38_MAX;
+                    s->wide = res;
+                    s->state = ov ? ST_OVERFLOW : ST_NORMAL;
+                } else {
+                    int64_t res;
+                    int ov = __builtin_add_overflow(s->i64, load_int(a->col, r, 8), &res);
+                    s->i64 = res;
+                    s->state = ov ? ST_OVERFLOW : ST_NORMAL;
+                }
+            } else if (c->policy == 0 || a->in_width != 8) {
+                /* Spark policy, or a narrower-than-int64 input under the generic policy (SumOp
+                 * checks overflow only for int64 inputs, sum_aggregator.h:36-60): wrap. */
+                s->i64 = (int64_t)((uint64_t)s->i64 + (uint64_t)load_int(a->col, r, a->in_width));
+                s->state = ST_NORMAL;
+            } else {
+                if (s->count < 0) return;
+                int64_t res;
+                if (__builtin_add_overflow(s->i64, load_int(a->col, r, a->in_width), &res)) {
+                    s->count = -1;
+                } else {
+                    s->i64 = res;
+                    s->count++;
+                }
+            }
+            return;
+        case F_AVG:
+            s->d += load_double(a->col, r, a->in_type, a->in_width);
+            s->count++;
+            return;
+        case F_MIN:
+        case F_MAX:
+            if (a->in_type == T_DOUBLE || a->in_type == T_FLOAT) {
+                double x = load_double(a->col, r, a->in_type, a->in_width);
+                if (a->func == F_MIN) s->d = (x < s->d) ? x : s->d;
+                else s->d = (s->d < x) ? x : s->d;
+            } else {
+                int64_t x = load_int(a->col, r, a->in_width);
+                if (a->func == F_MIN) s->i64 = (x < s->i64) ? x : s->i64;
+                else s->i64 = (s->i64 < x) ? x : s->i64;
+            }
+            s->state = ST_NORMAL;
+            return;
+    }
+}
+
+static i128 pow10_i128(int n)
+{
+    i128 p = 1;
+    for (int i = 0; i < n; ++i) p *= 10;
+    return p;
+}
+
+/* Writes the output value of one aggregator; returns 1 if NULL, 2 on an overflow error. */
+static int state_extract(const aggctx_t *c, const agg_t *a, const state_t *s, int overflow_as_null, void *out,
+    int64_t g)
+{
+    switch (a->func) {
+        case F_COUNT_ALL:
+        case F_COUNT_COL:
+            ((int64_t *)out)[g] = s->i64;
+            return 0;
+        case F_AVG:
+            if (s->count == 0) return 1;
+            ((double *)out)[g] = s->d / (double)s->count;
+            return 0;
+        case F_MIN:
+        case F_MAX: {
+            if (s->state == ST_EMPTY) return 1;
+            if (a->out_type == T_DOUBLE) ((double *)out)[g] = s->d;
+            else if (a->out_type == T_FLOAT) ((float *)out)[g] = (float)s->d;
+            else if (a->out_type == T_INT || a->out_type == T_DATE32) ((int32_t *)out)[g] = (int32_t)s->i64;
+            else if (a->out_type == T_SHORT) ((int16_t *)out)[g] = (int16_t)s->i64;
+            else if (a->out_type == T_BYTE || a->out_type == T_BOOLEAN) ((int8_t *)out)[g] = (int8_t)s->i64;
+            else ((int64_t *)out)[g] = s->i64;
+            return 0;
+        }
+        case F_SUM:
+            if (a->in_type == T_DOUBLE || a->in_type == T_FLOAT) {
+                if (s->state == ST_EMPTY) return 1;
+                ((double *)out)[g] = s->d;
+                return 0;
+            }
+            if (a->in_type == T_DEC64 || a->in_type == T_DEC128) {
+                if (s->state == ST_EMPTY) return 1;
+                if (s->state == ST_OVERFLOW) return overflow_as_null ? 1 : 2;
+                i128 v = a->out_type == T_DEC128 ? s->wide : (i128)s->i64;
+                i128 res;
+                int ov = __builtin_mul_overflow(v, pow10_i128(a->rescale), &res) || res > DEC38_MAX || res < -DEC38_MAX;
+                if (ov) return overflow_as_null ? 1 : 2;
+                if (a->out_type == T_DEC128) {
+                    uint64_t *o = (uint64_t *)out + 2 * g;
+                    o[0] = (uint64_t)res;
+                    o[1] = (uint64_t)((unsigned __int128)res >> 64);
+                } else {
+                    ((int64_t *)out)[g] = (int64_t)res;
+                }
+                return 0;
+            }
+            if (c->policy == 0 || a->in_width != 8) {
+                if (s->state == ST_EMPTY) return 1;
+                ((int64_t *)out)[g] = s->i64;
+                return 0;
+            }
+            if (s->count < 0) return overflow_as_null ? 1 : 2;
+            if (s->count == 0) return 1;
+            ((int64_t *)out)[g] = s->i64;
+            return 0;
+    }
+    return 1;
+}
+
+static int pack_key(int nkey, const void **key_cols, const int32_t *key_widths, const uint8_t **key_nulls, int64_t r,
+    uint8_t *k)
+{
+    int off = 0;
+    for (int i = 0; i < nkey; ++i) {
+        const int w = key_widths[i];
+        const int isnull = key_nulls && key_nulls[i] && key_nulls[i][r];
+        k[off++] = (uint8_t)isnull;
+        if (isnull) memset(k + off, 0, w);
+        else memcpy(k + off, (const uint8_t *)key_cols[i] + (int64_t)w * r, w);
+        off += w;
+    }
+    return off;
+}
+
+/*
+ * Single-stage hash aggregation over `n_rows` rows (all batches concatenated in arrival
+ * order).  Outputs are written for up to `max_groups` groups: key columns (values + byte
+ * nulls) and one value column per aggregator (16 bytes per row reserved for decimal128).
+ * Returns the number of groups, -1 on allocation failure, -2 if an overflow must raise
+ * (overflow-as-null off), -3 if max_groups is too small.
+ */
+int64_t orc_hashagg(int64_t n_rows, int32_t nkey, const void **key_cols, const int32_t *key_widths,
+    const uint8_t **key_nulls, int32_t nagg, const int32_t *funcs, const void **agg_cols, const int32_t *in_types,
+    const int32_t *in_widths, const uint8_t **agg_nulls, const int32_t *out_types, const int32_t *rescale,
+    int32_t policy, int32_t overflow_as_null, int64_t max_groups, void **out_keys, uint8_t **out_key_nulls,
+    void **out_vals, uint8_t **out_val_nulls)
+{
+    int keybytes = 0;
+    for (int i = 0; i < nkey; ++i) keybytes += 1 + key_widths[i];
+    table_t t;
+    if (table_init(&t, nkey, keybytes, 1024) != 0) return -1;
+    aggctx_t c;
+    c.nagg = nagg;
+    c.policy = policy;
+    c.aggs = (agg_t *)calloc(nagg > 0 ? nagg : 1, sizeof(agg_t));
+    c.stcap = 1024;
+    c.st = (state_t *)malloc((uint64_t)c.stcap * (nagg > 0 ? nagg : 1) * sizeof(state_t));
+    uint8_t *k = (uint8_t *)malloc(keybytes + 1);
+    if (!c.aggs || !c.st || !k) return -1;
+    for (int a = 0; a < nagg; ++a) {
+        c.aggs[a].func = funcs[a];
+        c.aggs[a].col = agg_cols[a];
+        c.aggs[a].in_type = in_types[a];
+        c.aggs[a].in_width = in_widths[a];
+        c.aggs[a].nulls = agg_nulls ? agg_nulls[a] : NULL;
+        c.aggs[a].out_type = out_types[a];
+        c.aggs[a].rescale = rescale ? rescale[a] : 0;
+    }
+    int64_t ret = 0;
+    for (int64_t r = 0; r < n_rows; ++r) {
+        pack_key(nkey, key_cols, key_widths, key_nulls, r, k);
+        int isnew = 0;
+        int64_t g = table_find_insert(&t, k, &isnew);
+        if (g < 0) { ret = -1; goto done; }
+        if (isnew) {
+            if (g >= c.stcap) {
+                state_t *ns = (state_t *)realloc(c.st, (uint64_t)c.stcap * 2 * (nagg > 0 ? nagg : 1) * sizeof(state_t));
+                if (!ns) { ret = -1; goto done; }
+                c.st = ns;
+                c.stcap *= 2;
+            }
+            for (int a = 0; a < nagg; ++a) state_init(&c.aggs[a], &c.st[g * nagg + a]);
+        }
+        for (int a = 0; a < nagg; ++a) state_update(&c, &c.aggs[a], &c.st[g * nagg + a], r);
+    }
+    if (t.ngroups > max_groups) { ret = -3; goto done; }
+    for (int64_t g = 0; g < t.ngroups; ++g) {
+        const uint8_t *gk = t.gkeys + (uint64_t)g * keybytes;
+        int off = 0;
+        for (int i = 0; i < nkey; ++i) {
+            out_key_nulls[i][g] = gk[off];
+            memcpy((uint8_t *)out_keys[i] + (int64_t)key_widths[i] * g, gk + off + 1, key_widths[i]);
+            off += 1 + key_widths[i];
+        }
+        for (int a = 0; a < nagg; ++a) {
+            int rc = state_extract(&c, &c.aggs[a], &c.st[g * nagg + a], overflow_as_null, out_vals[a], g);
+            if (rc == 2) { ret = -2; goto done; }
+            out_val_nulls[a][g] = (uint8_t)(rc == 1);
+        }
+    }
+    ret = t.ngroups;
+done:
+    free(k);
+    free(c.aggs);
+    free(c.st);
+    table_free(&t);
+    return ret;
+}
+
+/* ---------------------------------------------------------------- inner join */
+typedef struct {
+    int array_mode;
+    int64_t min;
+    uint64_t range;
+    int64_t *head;   /* array: head row per key-min; hash: per slot */
+    int64_t *next;   /* chain: next build row with the same key, -1 end */
+    uint64_t cap;
+    int64_t *hkeys;
+    uint8_t *hused;
+} jtable_t;
+
+static uint64_t mix64(uint64_t k)
+{
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdULL;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ULL;
+    k ^= k >> 33;
+    return k;
+}
+
+static int jbuild(jtable_t *t, int64_t n, const void *keys, int w, const uint8_t *nulls)
+{
+    memset(t, 0, sizeof(*t));
+    int64_t mn = INT64_MAX, mx = INT64_MIN, cnt = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (nulls && nulls[i]) continue;
+        int64_t k = load_int(keys, i, w);
+        if (k < mn) mn = k;
+        if (k > mx) mx = k;
+        cnt++;
+    }
+    t->next = (int64_t *)malloc((n > 0 ? n : 1) * sizeof(int64_t));
+    if (!t->next) return -1;
+    if (cnt == 0) { t->array_mode = 1; t->range = 0; return 0; }
+    uint64_t range = (uint64_t)mx - (uint64_t)mn + 1;
+    uint64_t p2 = 1;
+    while (p2 < (uint64_t)cnt) p2 <<= 1;
+    if (range != 0 && range <= 8 * p2 && range <= 0xffffffffULL) {
+        t->array_mode = 1;
+        t->min = mn;
+        t->range = range;
+        t->head = (int64_t *)malloc(range * sizeof(int64_t));
+        if (!t->head) return -1;
+        for (uint64_t i = 0; i < range; ++i) t->head[i] = -1;
+        for (int64_t i = n - 1; i >= 0; --i) {
+            if (nulls && nulls[i]) continue;
+            uint64_t s = (uint64_t)load_int(keys, i, w) - (uint64_t)mn;
+            t->next[i] = t->head[s];
+            t->head[s] = i;
+        }
+        return 0;
+    }
+    t->cap = 2 * p2;
+    t->hkeys = (int64_t *)malloc(t->cap * sizeof(int64_t));
+    t->hused = (uint8_t *)calloc(t->cap, 1);
+    t->head = (int64_t *)malloc(t->cap * sizeof(int64_t));
+    if (!t->hkeys || !t->hused || !t->head) return -1;
+    for (int64_t i = n - 1; i >= 0; --i) {
+        if (nulls && nulls[i]) continue;
+        int64_t k = load_int(keys, i, w);
+        uint64_t s = mix64((uint64_t)k) & (t->cap - 1);
+        while (t->hused[s] && t->hkeys[s] != k) s = (s + 1) & (t->cap - 1);
+        if (!t->hused[s]) { t->hused[s] = 1; t->hkeys[s] = k; t->head[s] = -1; }
+        t->next[i] = t->head[s];
+        t->head[s] = i;
+    }
+    return 0;
+}
+
+static int64_t jfind(const jtable_t *t, int64_t k)
+{
+    if (t->array_mode) {
+        uint64_t d = (uint64_t)k - (uint64_t)t->min;
+        if (t->range == 0 || k < t->min || d >= t->range) return -1;
+        return t->head[d];
+    }
+    uint64_t s = mix64((uint64_t)k) & (t->cap - 1);
+    while (t->hused[s]) {
+        if (t->hkeys[s] == k) return t->head[s];
+        s = (s + 1) & (t->cap - 1);
+    }
+    return -1;
+}
+
+static void jfree(jtable_t *t)
+{
+    free(t->head);
+    free(t->next);
+    free(t->hkeys);
+    free(t->hused);
+}
+
+/*
+ * Inner join of probe keys against build keys: writes (probe row, build row) pairs for
+ * every match, probe rows in order.  Returns the number of pairs (which may exceed
+ * `capacity`; only the first `capacity` are written) or -1 on allocation failure.
+ */
+int64_t orc_join_inner(int64_t n_build, const void *build_keys, int32_t build_width, const uint8_t *build_nulls,
+    int64_t n_probe, const void *probe_keys, int32_t probe_width, const uint8_t *probe_nulls, int64_t *out_probe,
+    int64_t *out_build, int64_t capacity)
+{
+    jtable_t t;
+    if (jbuild(&t, n_build, build_keys, build_width, build_nulls) != 0) { jfree(&t); return -1; }
+    int64_t n = 0;
+    for (int64_t r = 0; r < n_probe; ++r) {
+        if (probe_nulls && probe_nulls[r]) continue;
+        for (int64_t b = jfind(&t, load_int(probe_keys, r, probe_width)); b >= 0; b = t.next[b]) {
+            if (n < capacity) {
+                out_probe[n] = r;
+                out_build[n] = b;
+            }
+            n++;
+        }
+    }
+    jfree(&t);
+    return n;
+}
+
+/* ---------------------------------------------------------------- timed CPU baselines */
+/*
+ * Join probe baseline: the reference's probe loop materialising (probe key, payload columns)
+ * output rows, over `nthreads` threads that each own a contiguous slice of the probe rows and
+ * share the read-only build table (the reference runs one LookupJoin operator per task over a
+ * shared build, join_test.cpp:525-770).  Payload columns are int32.
+ */
+typedef struct {
+    const jtable_t *t;
+    const int64_t *pkeys;
+    const uint8_t *pnulls;
+    int64_t r0, r1;
+    int32_t npay;
+    const int32_t **pay;
+    int64_t *okey;
+    int32_t **opay;
+    int64_t n;
+} jwork_t;
+
+static void *jprobe_thread(void *arg)
+{
+    jwork_t *w = (jwork_t *)arg;
+    int64_t n = 0;
+    for (int64_t r = w->r0; r < w->r1; ++r) {
+        if (w->pnulls && w->pnulls[r]) continue;
+        const int64_t k = w->pkeys[r];
+        for (int64_t b = jfind(w->t, k); b >= 0; b = w->t->next[b]) {
+            w->okey[n] = k;
+            for (int p = 0; p < w->npay; ++p) w->opay[p][n] = w->pay[p][b];
+            n++;
+        }
+    }
+    w->n = n;
+    return NULL;
+}
+
+int64_t orc_join_probe_bench(int64_t n_build, const int64_t *build_keys, const uint8_t *build_nulls, int32_t npay,
+    const int32_t **payloads, int64_t n_probe, const int64_t *probe_keys, const uint8_t *probe_nulls, int32_t nthreads,
+    double *build_seconds_unused)
+{
+    (void)build_seconds_unused;
+    jtable_t t;
+    if (jbuild(&t, n_build, build_keys, 8, build_nulls) != 0) { jfree(&t); return -1; }
+    if (nthreads < 1) nthreads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    jwork_t *w = (jwork_t *)calloc(nthreads, sizeof(jwork_t));
+    int64_t total = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        w[i].t = &t;
+        w[i].pkeys = probe_keys;
+        w[i].pnulls = probe_nulls;
+        w[i].r0 = n_probe * i / nthreads;
+        w[i].r1 = n_probe * (i + 1) / nthreads;
+        w[i].npay = npay;
+        w[i].pay = payloads;
+        const int64_t cap = (w[i].r1 - w[i].r0) * 2 + 16;
+        w[i].okey = (int64_t *)malloc(cap * sizeof(int64_t));
+        w[i].opay = (int32_t **)malloc(sizeof(int32_t *) * (npay > 0 ? npay : 1));
+        for (int p = 0; p < npay; ++p) w[i].opay[p] = (int32_t *)malloc(cap * sizeof(int32_t));
+        pthread_create(&th[i], NULL, jprobe_thread, &w[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) {
+        pthread_join(th[i], NULL);
+        total += w[i].n;
+        free(w[i].okey);
+        for (int p = 0; p < npay; ++p) free(w[i].opay[p]);
+        free(w[i].opay);
+    }
+    free(th);
+    free(w);
+    jfree(&t);
+    return total;
+}
+
+/*
+ * Aggregation baseline: `nthreads` operator instances each aggregate a contiguous slice of
+ * the rows with orc_hashagg's row loop (partial stage); the partial groups are then merged
+ * into one table (final stage) -- the reference's partial/final split.  Single int64 key,
+ * aggregates SUM/COUNT/MIN/MAX of an int64 column and SUM/AVG of a double column (the
+ * uniform-key workload).  Returns the number of groups.
+ */
+typedef struct {
+    int64_t r0, r1;
+    const int64_t *key, *v1;
+    const double *v2;
+    table_t t;
+    int64_t *sum, *cnt, *mn, *mx;
+    double *dsum;
+    int64_t cap;
+} awork_t;
+
+static void *agg_thread(void *arg)
+{
+    awork_t *w = (awork_t *)arg;
+    table_init(&w->t, 1, 9, 1024);
+    w->cap = 1024;
+    w->sum = (int64_t *)malloc(w->cap * 8);
+    w->cnt = (int64_t *)malloc(w->cap * 8);
+    w->mn = (int64_t *)malloc(w->cap * 8);
+    w->mx = (int64_t *)malloc(w->cap * 8);
+    w->dsum = (double *)malloc(w->cap * 8);
+    uint8_t k[9];
+    k[0] = 0;
+    for (int64_t r = w->r0; r < w->r1; ++r) {
+        memcpy(k + 1, &w->key[r], 8);
+        int isnew = 0;
+        int64_t g = table_find_insert(&w->t, k, &isnew);
+        if (isnew) {
+            if (g >= w->cap) {
+                w->cap *= 2;
+                w->sum = (int64_t *)realloc(w->sum, w->cap * 8);
+                w->cnt = (int64_t *)realloc(w->cnt, w->cap * 8);
+                w->mn = (int64_t *)realloc(w->mn, w->cap * 8);
+                w->mx = (int64_t *)realloc(w->mx, w->cap * 8);
+                w->dsum = (double *)realloc(w->dsum, w->cap * 8);
+            }
+            w->sum[g] = 0;
+            w->cnt[g] = 0;
+            w->mn[g] = INT64_MAX;
+            w->mx[g] = INT64_MIN;
+            w->dsum[g] = 0;
+        }
+        const int64_t x = w->v1[r];
+        w->sum[g] = (int64_t)((uint64_t)w->sum[g] + (uint64_t)x);
+        w->cnt[g]++;
+        w->mn[g] = x < w->mn[g] ? x : w->mn[g];
+        w->mx[g] = w->mx[g] < x ? x : w->mx[g];
+        w->dsum[g] += w->v2[r];
+    }
+    return NULL;
+}
+
+int64_t orc_agg_bench(int64_t n, const int64_t *key, const int64_t *v1, const double *v2, int32_t nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    awork_t *w = (awork_t *)calloc(nthreads, sizeof(awork_t));
+    for (int i = 0; i < nthreads; ++i) {
+        w[i].r0 = n * i / nthreads;
+        w[i].r1 = n * (i + 1) / nthreads;
+        w[i].key = key;
+        w[i].v1 = v1;
+        w[i].v2 = v2;
+        pthread_create(&th[i], NULL, agg_thread, &w[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    /* final stage: merge the partial tables */
+    table_t t;
+    table_init(&t, 1, 9, 1024);
+    int64_t cap = 1024;
+    int64_t *sum = (int64_t *)malloc(cap * 8), *cnt = (int64_t *)malloc(cap * 8);
+    int64_t *mn = (int64_t *)malloc(cap * 8), *mx = (int64_t *)malloc(cap * 8);
+    double *dsum = (double *)malloc(cap * 8);
+    for (int i = 0; i < nthreads; ++i) {
+        for (int64_t g = 0; g < w[i].t.ngroups; ++g) {
+            int isnew = 0;
+            int64_t h = table_find_insert(&t, w[i].t.gkeys + g * 9, &isnew);
+            if (isnew) {
+                if (h >= cap) {
+                    cap *= 2;
+                    sum = (int64_t *)realloc(sum, cap * 8);
+                    cnt = (int64_t *)realloc(cnt, cap * 8);
+                    mn = (int64_t *)realloc(mn, cap * 8);
+                    mx = (int64_t *)realloc(mx, cap * 8);
+                    dsum = (double *)realloc(dsum, cap * 8);
+                }
+                sum[h] = 0; cnt[h] = 0; mn[h] = INT64_MAX; mx[h] = INT64_MIN; dsum[h] = 0;
+            }
+            sum[h] = (int64_t)((uint64_t)sum[h] + (uint64_t)w[i].sum[g]);
+            cnt[h] += w[i].cnt[g];
+            mn[h] = w[i].mn[g] < mn[h] ? w[i].mn[g] : mn[h];
+            mx[h] = mx[h] < w[i].mx[g] ? w[i].mx[g] : mx[h];
+            dsum[h] += w[i].dsum[g];
+        }
+        table_free(&w[i].t);
+        free(w[i].sum); free(w[i].cnt); free(w[i].mn); free(w[i].mx); free(w[i].dsum);
+    }
+    const int64_t groups = t.ngroups;
+    table_free(&t);
+    free(sum); free(cnt); free(mn); free(mx); free(dsum);
+    free(th);
+    free(w);
+    return groups;
+}

@@ -1,0 +1,117 @@
+"""Writes agg_kats.json and join_kats.json: known-answer tests of the reference's own C++ tests,
+transcribed (inputs and expected outputs as literals) with the file:line they come from.
+
+The reference is C++ and cannot be built here, so its test vectors are carried over by reading
+the test sources; each entry below restates one test's inputs and EXPECT_* values.  Run
+`python tests/golden/make_golden.py` to regenerate the JSON files.
+"""
+import json
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+INT64_MAX = 9223372036854775807
+DEC38 = 10**38 - 1
+
+AGG = {
+    # core/test/operator/aggregation_test.cpp:4386-4422 -- Spark long SUM wraps:
+    # 3 x 9223372036854774807 -> 9223372036854772805.
+    "spark_sum_long_overflow": dict(
+        source="core/test/operator/aggregation_test.cpp:4386-4422", policy="spark",
+        func="SUM", in_type="LONG", out_type="LONG", values=[9223372036854774807] * 3,
+        nulls=None, expected=9223372036854772805),
+    # aggregation_test.cpp:4424-4466 -- 851451 + 9223372036854775807 = -9223372036853924358 and
+    # -9223372036854775807 + -256 = 9223372036854775553 ("overflow but same with vanilla spark").
+    "spark_sum_long_wrap_positive": dict(
+        source="core/test/operator/aggregation_test.cpp:4424-4466", policy="spark",
+        func="SUM", in_type="LONG", out_type="LONG", values=[851451, INT64_MAX], nulls=None,
+        expected=-9223372036853924358),
+    "spark_sum_long_wrap_negative": dict(
+        source="core/test/operator/aggregation_test.cpp:4424-4466", policy="spark",
+        func="SUM", in_type="LONG", out_type="LONG", values=[-INT64_MAX, -256], nulls=None,
+        expected=9223372036854775553),
+    # aggregation_test.cpp:4468-4500 -- Spark double SUM of three values -> 7.037035803703704E11.
+    "spark_sum_double": dict(
+        source="core/test/operator/aggregation_test.cpp:4468-4500", policy="spark",
+        func="SUM", in_type="DOUBLE", out_type="DOUBLE",
+        values=[123456789012.3456789, 234567890123.4567891, 345678901234.5678912], nulls=None,
+        expected=7.037035803703704e11),
+    # aggregation_test.cpp:4598-4641 -- Spark AVG of 3 x 9223372036854774807 -> 9.2233720368547748E18.
+    "spark_avg_long": dict(
+        source="core/test/operator/aggregation_test.cpp:4598-4641", policy="spark",
+        func="AVG", in_type="LONG", out_type="DOUBLE", values=[9223372036854774807] * 3, nulls=None,
+        expected=9.2233720368547748e18),
+    # aggregation_test.cpp:4643-4683 -- Spark AVG of the three doubles -> 2.345678601234568E11.
+    "spark_avg_double": dict(
+        source="core/test/operator/aggregation_test.cpp:4643-4683", policy="spark",
+        func="AVG", in_type="DOUBLE", out_type="DOUBLE",
+        values=[123456789012.3456789, 234567890123.4567891, 345678901234.5678912], nulls=None,
+        expected=2.345678601234568e11),
+    # aggregation_test.cpp:3790-3848 / 3849-3900 -- decimal128(38,0) SUM of 3 x (10^38 - 1):
+    # overflow raises with overflow-as-null off, gives NULL with it on.
+    "spark_sum_decimal128_overflow": dict(
+        source="core/test/operator/aggregation_test.cpp:3790-3900", policy="spark",
+        func="SUM", in_type="DECIMAL128", out_type="DECIMAL128", scale=0, values=[DEC38] * 3, nulls=None,
+        expected="overflow"),
+    # aggregation_test.cpp:3167-3229 (sum_test, SUPPORT policy) -- SUM of 200 ones = 200; SUM of
+    # an all-NULL column is NULL.
+    "generic_sum_long_ones": dict(
+        source="core/test/operator/aggregation_test.cpp:3167-3229", policy="generic",
+        func="SUM", in_type="LONG", out_type="LONG", values=[1] * 200, nulls=None, expected=200),
+    "generic_sum_all_null": dict(
+        source="core/test/operator/aggregation_test.cpp:3167-3229", policy="generic",
+        func="SUM", in_type="LONG", out_type="LONG", values=[0] * 200, nulls=[True] * 200, expected=None),
+    "generic_sum_short_decimal_ones": dict(
+        source="core/test/operator/aggregation_test.cpp:3167-3229", policy="generic",
+        func="SUM", in_type="DECIMAL64", out_type="DECIMAL128", scale=0, values=[1] * 200, nulls=None,
+        expected=200),
+}
+
+# aggregation_test.cpp:1292-1350 (verify_null_correctness): one group of 6 rows, all agg inputs
+# are ones (BuildAggregateInput, :180-252); col 2 NULL at rows 0-4, cols 3,4,5 NULL at row 1.
+# SUM(c1), AVG(c2), COUNT(c3), MIN(c4), MAX(c5) -> {key 0, 6, 1.0, 5, 1, 1}.
+AGG_MULTI = {
+    "verify_null_correctness": dict(
+        source="core/test/operator/aggregation_test.cpp:1292-1350",
+        key=[0] * 6,
+        columns=[[1] * 6] * 5,
+        nulls=[[False] * 6, [True] * 5 + [False], [False, True, False, False, False, False],
+               [False, True, False, False, False, False], [False, True, False, False, False, False]],
+        funcs=["SUM", "AVG", "COUNT_COLUMN", "MIN", "MAX"],
+        out_types=["LONG", "DOUBLE", "LONG", "LONG", "LONG"],
+        expected=[[0, 6, 1.0, 5, 1, 1]]),
+}
+
+
+def _join_one_build_op():
+    # core/test/operator/join_test.cpp:52-59 (build), :81-88 (probe), :90-109 (expected), :283-305.
+    build = [[1, 2, 1, 2, 3, 4, 5, 6, 7, 1], [79, 79, 70, 70, 70, 70, 70, 70, 70, 70]]
+    probe = [[1, 2, 3, 4, 5, 6, 1, 1, 2, 3], [78, 78, 78, 78, 78, 78, 78, 82, 82, 65]]
+    expected0 = [78, 78, 78, 78, 78, 78, 78, 82, 82, 65]
+    ids = [0, 0, 0, 1, 1, 2, 3, 4, 5, 6, 6, 6, 7, 7, 7, 8, 8, 9]
+    expected1 = [79, 70, 70, 79, 70, 70, 70, 70, 70, 79, 70, 70, 79, 70, 70, 79, 70, 70]
+    rows = [[expected0[i], e1] for i, e1 in zip(ids, expected1)]
+    return dict(source="core/test/operator/join_test.cpp:52-109,137-160,283-305", build=build, probe=probe,
+                build_hash_col=0, probe_hash_col=0, probe_output_cols=[1], build_output_cols=[1],
+                expected_rows=rows)
+
+
+def _join_array_table_short():
+    # core/test/operator/join_test.cpp:4265-4313 (TestInnerEqualityJoinOfArrayTable).
+    build = [[1, 2, 3, 4, 1, 2], [111, 11, 333, 33, 20, 16]]
+    probe = [[1, 2, 3, 4], [11, 22, 33, 44]]
+    exp = [[1, 1, 2, 2, 3, 4], [11, 11, 22, 22, 33, 44], [1, 1, 2, 2, 3, 4], [111, 20, 11, 16, 333, 33]]
+    rows = [list(r) for r in zip(*exp)]
+    return dict(source="core/test/operator/join_test.cpp:4265-4313", build=build, probe=probe, build_hash_col=0,
+                probe_hash_col=0, probe_output_cols=[0, 1], build_output_cols=[0, 1], expected_rows=rows)
+
+
+def main():
+    (HERE / "agg_kats.json").write_text(json.dumps({"single": AGG, "multi": AGG_MULTI}, indent=1) + "\n")
+    (HERE / "join_kats.json").write_text(json.dumps({"inner_join_one_build_op": _join_one_build_op(),
+                                                    "array_table_short": _join_array_table_short()}, indent=1)
+                                         + "\n")
+
+
+if __name__ == "__main__":
+    main()

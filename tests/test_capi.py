@@ -1,0 +1,127 @@
+"""C ABI and host-logic tests that need no GPU: the library loads, exports every symbol the
+header declares, builds OmniVec batches in the reference layout, validates factory arguments
+the way the reference does, and refuses to compute without a device."""
+import ctypes as C
+import subprocess
+
+import numpy as np
+import pytest
+
+import omnioperator_gb300 as omg
+from omnioperator_gb300 import _capi
+
+
+def test_library_exports_every_header_symbol():
+    syms = omg.header_symbols()
+    assert len(syms) >= 45
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_capi.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    L = omg.lib()
+    for s in syms:
+        assert hasattr(L, s)
+
+
+def test_version_and_policy_roundtrip():
+    assert b"sm_103a" in omg.lib().omg_version()
+    assert omg.lib().omg_config_get_policy() == omg.POLICY_SPARK
+    omg.set_policy(omg.POLICY_GENERIC)
+    assert omg.lib().omg_config_get_policy() == omg.POLICY_GENERIC
+    omg.set_policy(omg.POLICY_SPARK)
+    with pytest.raises(omg.OmgError):
+        omg.set_policy(7)
+
+
+def test_vector_layout_matches_omnivec():
+    """Flat values plus LSB-first null bitmap with set bit = NULL (nulls_buffer.h:18-21)."""
+    vals = np.arange(-5, 12, dtype=np.int64)
+    mask = np.zeros(len(vals), bool)
+    mask[[0, 3, 9, 16]] = True
+    b = omg.make_batch([omg.LongType()], [vals], [mask])
+    L = omg.lib()
+    v = L.omg_batch_get(b, 0)
+    assert L.omg_vec_size(v) == len(vals) and L.omg_vec_type(v) == omg.OMNI_LONG and L.omg_vec_width(v) == 8
+    raw = (C.c_uint8 * 3).from_address(L.omg_vec_nulls(v))
+    assert list(raw) == [0b00001001, 0b00000010, 0b00000001]
+    assert L.omg_vec_has_null(v) == 1
+    (got, gmask), = omg.batch_to_numpy(b)
+    assert np.array_equal(got, vals) and np.array_equal(gmask, mask)
+    omg.free_batch(b)
+
+
+def test_decimal128_and_fixed_binary_vectors():
+    d = np.array([[1, 0], [2**64 - 1, 2**64 - 1]], dtype=np.uint64)
+    fb = np.arange(32, dtype=np.uint8).reshape(2, 16)
+    b = omg.make_batch([omg.Decimal128Type(38, 2), omg.FixedBinaryType(16)], [d, fb])
+    (dv, _), (fv, _) = omg.batch_to_numpy(b)
+    assert np.array_equal(dv, d) and np.array_equal(fv, fb)
+    omg.free_batch(b)
+
+
+def test_factory_validation_matches_reference_rules():
+    L = omg.LongType()
+    # unsupported function id -> UNSUPPORTED (aggregation.cpp:81-85 throws for unknown types)
+    with pytest.raises(omg.OmgError) as e:
+        omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [9])
+    assert e.value.status == -2
+    # partial / final stages are not built
+    with pytest.raises(omg.OmgError) as e:
+        omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [0], output_partials=[True])
+    assert e.value.status == -2
+    # outer joins are not built
+    with pytest.raises(omg.OmgError) as e:
+        omg.HashBuilderOperatorFactory(1, [L], [0])
+    assert e.value.status == -2
+    # join filters are not built
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L], [0])
+    with pytest.raises(omg.OmgError):
+        omg.LookupJoinOperatorFactory([L], [0], [0], [1], [L], bf, filter_expr=object())
+    bf.close()
+
+
+def test_operator_state_machine_without_gpu():
+    """AddInput takes ownership and queues; compute refuses loudly without a device."""
+    if omg.device_available():
+        pytest.skip("a GPU is visible: covered by the gpu tests")
+    L = omg.LongType()
+    fac = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [0])
+    op = fac.create_operator()
+    assert op.get_status() == omg.OMNI_STATUS_NORMAL
+    assert op.get_output() == (0, None)  # no input yet: group_aggregation.cpp:456-458
+    op.add_input(omg.make_batch([L, L], [np.arange(4, dtype=np.int64), np.arange(4, dtype=np.int64)]))
+    with pytest.raises(omg.OmgError) as e:
+        op.get_output()
+    assert e.value.status == -8
+    op.delete()
+    fac.close()
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L], [0])
+    bop = bf.create_operator()
+    bop.add_input(omg.make_batch([L], [np.arange(4, dtype=np.int64)]))
+    bop.set_no_more_input(False)
+    assert bop.get_output() == (0, None) and bop.get_status() == omg.OMNI_STATUS_NORMAL  # hash_builder.cpp:184-187
+    bop.set_no_more_input(True)
+    with pytest.raises(omg.OmgError) as e:
+        bop.get_output()
+    assert e.value.status == -8
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [0], [L], bf)
+    pop = pf.create_operator()
+    assert pop.is_blocked()  # kWaitForJoinBuild until the build finished (lookup_join.cpp:270-277)
+    pop.delete()
+    bop.delete()
+    pf.close()
+    bf.close()
+
+
+def test_device_alloc_fault_injection_is_host_side():
+    omg.lib().omg_debug_fail_next_allocs(2)
+    omg.lib().omg_debug_fail_next_allocs(0)
+    assert omg.lib().omg_last_error() == b""
+
+
+def test_null_handles_are_rejected():
+    L = omg.lib()
+    assert L.omg_op_add_input(None, None, None) == -1
+    assert b"null" in L.omg_last_error()
+    assert L.omg_batch_row_count(None) == -1

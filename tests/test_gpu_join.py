@@ -1,0 +1,133 @@
+"""GPU parity of HashBuilder + LookupJoin (inner) against the oracle: the output row multiset must
+equal the oracle's exactly, NULLs included."""
+import numpy as np
+import pytest
+
+import omnioperator_gb300 as omg
+from helpers import expected_join_rows, join_rows_canonical, run_join
+
+pytestmark = pytest.mark.gpu
+
+L, I, S = omg.LongType(), omg.IntType(), omg.ShortType()
+
+
+def _cfg2_like(nb, npb, seed, dup=False, sparse=False):
+    rng = np.random.default_rng(seed)
+    if sparse:
+        bkey = (rng.choice(2**39, nb, replace=False) * 2).astype(np.int64)
+    else:
+        bkey = rng.permutation(nb).astype(np.int64)
+    if dup:
+        bkey = np.concatenate([bkey, bkey[: nb // 3], bkey[: nb // 10]])
+    p1 = rng.integers(-2**31, 2**31, len(bkey), dtype=np.int64).astype(np.int32)
+    p2 = rng.integers(-2**31, 2**31, len(bkey), dtype=np.int64).astype(np.int32)
+    match = rng.random(npb) < 0.8
+    if sparse:
+        miss = (rng.integers(0, 2**39, npb) * 2 + 1).astype(np.int64)
+    else:
+        miss = rng.integers(nb, 2 * nb, npb).astype(np.int64)
+    pkey = np.where(match, bkey[rng.integers(0, nb, npb)], miss)
+    pnull = rng.random(npb) < 0.01
+    return bkey, p1, p2, pkey, pnull
+
+
+def _check(bkey, p1, p2, pkey, pnull, bnulls=None, **kw):
+    bcols = [bkey, p1, p2]
+    got, max_rows = run_join([L, I, I], bcols, bnulls, [0], [L], [pkey], [pnull], [0], [0], [1, 2], **kw)
+    exp = expected_join_rows([pkey], [pnull], bcols, bnulls, 0, 0, [0], [1, 2])
+    assert join_rows_canonical(got) == exp
+    # 16-byte rows: at most ceil(1 MiB / 16) = 65536 rows per output batch (lookup_join.cpp:1628-1640)
+    assert max_rows <= 65536
+    return got
+
+
+def test_config2_shape_array_table(gpu):
+    _check(*_cfg2_like(50_000, 400_000, 1))
+
+
+def test_config2_shape_pipeline_mode(gpu):
+    _check(*_cfg2_like(50_000, 300_000, 2), pipeline=True, batch_sizes=(4096, 100, 3000))
+
+
+def test_device_resident_probe(gpu):
+    _check(*_cfg2_like(20_000, 200_000, 3), device_input=True, batch_sizes=(200_000,))
+
+
+def test_duplicate_build_keys_array_mode(gpu):
+    _check(*_cfg2_like(30_000, 200_000, 4, dup=True))
+
+
+def test_sparse_keys_hash_mode(gpu):
+    _check(*_cfg2_like(40_000, 200_000, 5, sparse=True))
+
+
+def test_sparse_keys_hash_mode_duplicates(gpu):
+    _check(*_cfg2_like(40_000, 200_000, 6, sparse=True, dup=True))
+
+
+def test_nulls_in_build_keys_and_payloads(gpu):
+    bkey, p1, p2, pkey, pnull = _cfg2_like(20_000, 100_000, 7)
+    rng = np.random.default_rng(70)
+    bn = [rng.random(len(bkey)) < 0.05, rng.random(len(bkey)) < 0.1, None]
+    _check(bkey, p1, p2, pkey, pnull, bnulls=bn)
+
+
+def test_extreme_keys_including_int64_min(gpu):
+    mn, mx = np.iinfo(np.int64).min, np.iinfo(np.int64).max
+    bkey = np.array([mn, mx, 0, -1, mn, 5], dtype=np.int64)
+    p1 = np.arange(6, dtype=np.int32)
+    p2 = -np.arange(6, dtype=np.int32)
+    pkey = np.array([mn, mx, 0, 7, -1, mn, 5, 5], dtype=np.int64)
+    pnull = np.array([0, 0, 0, 0, 0, 0, 1, 0], dtype=bool)
+    _check(bkey, p1, p2, pkey, pnull)
+
+
+def test_probe_payload_columns_and_narrow_keys(gpu):
+    rng = np.random.default_rng(8)
+    nb, npb = 5000, 60_000
+    bkey = rng.integers(-20000, 20000, nb).astype(np.int32)
+    bval = rng.integers(0, 100, nb).astype(np.int16)
+    pkey = rng.integers(-20000, 20000, npb).astype(np.int32)
+    pval = rng.standard_normal(npb)
+    pvn = rng.random(npb) < 0.05
+    D = omg.DoubleType()
+    got, _ = run_join([I, S], [bkey, bval], None, [0], [D, I], [pval, pkey], [pvn, None], [1], [1, 0], [1, 0])
+    exp = expected_join_rows([pval, pkey], [pvn, None], [bkey, bval], None, 1, 0, [1, 0], [1, 0])
+    assert join_rows_canonical(got) == exp
+
+
+def test_empty_build_and_no_matches(gpu):
+    bkey = np.zeros(0, dtype=np.int64)
+    p = np.zeros(0, dtype=np.int32)
+    pkey = np.arange(100, dtype=np.int64)
+    got, _ = run_join([L, I, I], [bkey, p, p], None, [0], [L], [pkey], None, [0], [0], [1, 2])
+    assert got is None
+    bkey = np.arange(100, 200, dtype=np.int64)
+    p = np.arange(100, dtype=np.int32)
+    got, _ = run_join([L, I, I], [bkey, p, p], None, [0], [L], [pkey], None, [0], [0], [1, 2])
+    assert got is None
+
+
+def test_reference_kat_inner_join_one_build_op(gpu):
+    """join_test.cpp:52-109,283-305 (TestInnerEqualityJoinWithOneBuildOp)."""
+    import json
+    from pathlib import Path
+
+    g = json.loads((Path(__file__).parent / "golden" / "join_kats.json").read_text())["inner_join_one_build_op"]
+    got, _ = run_join([L, L], [np.array(g["build"][0], np.int64), np.array(g["build"][1], np.int64)], None, [0],
+                      [L, L], [np.array(g["probe"][0], np.int64), np.array(g["probe"][1], np.int64)], None, [0],
+                      [1], [1])
+    exp = sorted(tuple(r) for r in g["expected_rows"])
+    assert join_rows_canonical(got) == exp
+
+
+def test_reference_kat_array_table_short_keys(gpu):
+    """join_test.cpp:4265-4313 (TestInnerEqualityJoinOfArrayTable)."""
+    import json
+    from pathlib import Path
+
+    g = json.loads((Path(__file__).parent / "golden" / "join_kats.json").read_text())["array_table_short"]
+    got, _ = run_join([S, S], [np.array(c, np.int16) for c in g["build"]], None, [0], [S, S],
+                      [np.array(c, np.int16) for c in g["probe"]], None, [0], [0, 1], [0, 1])
+    exp = sorted(tuple(r) for r in g["expected_rows"])
+    assert join_rows_canonical(got) == exp
