@@ -258,7 +258,7 @@ class Operator:
         arr = (C.c_int64 * 8)()
         check(lib().omg_op_get_counters(self.handle, arr, 8))
         return {"launches": arr[0], "resizes": arr[1], "retried_rows": arr[2], "groups": arr[3],
-                "ordered_groups": arr[4], "output_rows": arr[5]}
+                "ordered_groups": arr[4], "output_rows": arr[5], "kernel_ns": arr[6], "kernel_launches": arr[7]}
 
     def close(self):
         check(lib().omg_op_close(self.handle))

@@ -64,6 +64,41 @@ private:
     cudaStream_t own_ = nullptr;
 };
 
+// Times one kernel launch with CUDA events recorded on the launching stream; the elapsed
+// time is read after the stream has been synchronised (ElapsedNs).
+class KernelTimer {
+public:
+    ~KernelTimer()
+    {
+        if (start_ != nullptr) {
+            cudaEventDestroy(start_);
+            cudaEventDestroy(stop_);
+        }
+    }
+    void Start(cudaStream_t s)
+    {
+        if (start_ == nullptr) {
+            CudaCheck(cudaEventCreate(&start_), "cudaEventCreate");
+            CudaCheck(cudaEventCreate(&stop_), "cudaEventCreate");
+        }
+        CudaCheck(cudaEventRecord(start_, s), "cudaEventRecord");
+    }
+    void Stop(cudaStream_t s) { CudaCheck(cudaEventRecord(stop_, s), "cudaEventRecord"); }
+    int64_t ElapsedNs() const
+    {
+        float ms = 0.f;
+        if (start_ == nullptr || cudaEventElapsedTime(&ms, start_, stop_) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return static_cast<int64_t>(static_cast<double>(ms) * 1e6);
+    }
+
+private:
+    cudaEvent_t start_ = nullptr;
+    cudaEvent_t stop_ = nullptr;
+};
+
 // A device scratch allocation, stream-ordered.
 template <typename T> class DevArray {
 public:

@@ -369,6 +369,7 @@ Operator *HashAggregationOperatorFactory::CreateOperator()
 // ------------------------------------------------------------------------------ operator
 struct HashAggregationOperator::Impl {
     omg::OpStream stream;
+    omg::KernelTimer timer;
     DevArray<uint64_t> slots;
     DevArray<uint32_t> special;
     // stats[0] = groupCount, [1] = nRetry, [2] = nSpill, [3] = error
@@ -512,12 +513,16 @@ void HashAggregationOperator::Flush()
     p.retryCap = static_cast<uint32_t>(rows);
     p.smemSlots = smemSlots;
     unsigned int *nSpill = reinterpret_cast<unsigned int *>(im.stats.Get() + 2);
+    im.timer.Start(s);
     CudaCheck(omg::LaunchAgg(p, spillA.Get(), nSpill, static_cast<uint32_t>(spillCap), nullptr, 0, grid, s),
         "aggregation kernel");
+    im.timer.Stop(s);
     ++counters_[0];
     unsigned long long h[4];
     CudaCheck(cudaMemcpyAsync(h, im.stats.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read stats");
     im.stream.Sync();
+    counters_[6] += im.timer.ElapsedNs();
+    ++counters_[7];
     uint64_t nRetry = static_cast<unsigned int>(h[1]);
     uint64_t nSpillH = static_cast<unsigned int>(h[2]);
     int32_t err = static_cast<int32_t>(h[3]);

@@ -364,6 +364,7 @@ Operator *LookupJoinOperatorFactory::CreateOperator() { return new LookupJoinOpe
 
 struct LookupJoinOperator::Impl {
     omg::OpStream stream;
+    omg::KernelTimer timer;
 };
 
 LookupJoinOperator::LookupJoinOperator(const LookupJoinOperatorFactory &f) : f_(f), impl_(new Impl()) {}
@@ -481,10 +482,14 @@ void LookupJoinOperator::ProcessPending()
         }
         p.outCapacity = capacity;
         CudaCheck(cudaMemsetAsync(count.Get(), 0, sizeof(unsigned long long), s), "reset count");
+        impl_->timer.Start(s);
         CudaCheck(omg::LaunchProbe(p, s), "probe kernel");
+        impl_->timer.Stop(s);
         ++counters_[0];
         CudaCheck(cudaMemcpyAsync(&total, count.Get(), sizeof(total), cudaMemcpyDeviceToHost, s), "read count");
         impl_->stream.Sync();
+        counters_[6] += impl_->timer.ElapsedNs();
+        ++counters_[7];
         if (total <= capacity) {
             break;
         }

@@ -32,6 +32,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 typedef __int128 i128;
 
@@ -591,13 +592,22 @@ static void *jprobe_thread(void *arg)
     return NULL;
 }
 
+static double now_seconds(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* seconds[0] = build time, seconds[1] = probe time (output buffers allocated beforehand). */
 int64_t orc_join_probe_bench(int64_t n_build, const int64_t *build_keys, const uint8_t *build_nulls, int32_t npay,
     const int32_t **payloads, int64_t n_probe, const int64_t *probe_keys, const uint8_t *probe_nulls, int32_t nthreads,
-    double *build_seconds_unused)
+    double *seconds)
 {
-    (void)build_seconds_unused;
     jtable_t t;
+    const double t0 = now_seconds();
     if (jbuild(&t, n_build, build_keys, 8, build_nulls) != 0) { jfree(&t); return -1; }
+    const double t1 = now_seconds();
     if (nthreads < 1) nthreads = 1;
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
     jwork_t *w = (jwork_t *)calloc(nthreads, sizeof(jwork_t));
@@ -614,10 +624,16 @@ int64_t orc_join_probe_bench(int64_t n_build, const int64_t *build_keys, const u
         w[i].okey = (int64_t *)malloc(cap * sizeof(int64_t));
         w[i].opay = (int32_t **)malloc(sizeof(int32_t *) * (npay > 0 ? npay : 1));
         for (int p = 0; p < npay; ++p) w[i].opay[p] = (int32_t *)malloc(cap * sizeof(int32_t));
-        pthread_create(&th[i], NULL, jprobe_thread, &w[i]);
+    }
+    const double t2 = now_seconds();
+    for (int i = 0; i < nthreads; ++i) pthread_create(&th[i], NULL, jprobe_thread, &w[i]);
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    const double t3 = now_seconds();
+    if (seconds) {
+        seconds[0] = t1 - t0;
+        seconds[1] = t3 - t2;
     }
     for (int i = 0; i < nthreads; ++i) {
-        pthread_join(th[i], NULL);
         total += w[i].n;
         free(w[i].okey);
         for (int p = 0; p < npay; ++p) free(w[i].opay[p]);

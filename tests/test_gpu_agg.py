@@ -277,7 +277,7 @@ def test_narrow_key_types(gpu, ktype):
 
 def test_output_split_into_reference_batch_size(gpu):
     """rowsPerBatch = ceil(1 MiB / rowBytes): 56-byte rows -> at most 18725 rows per batch."""
-    key, v1, v2, km, m1, m2 = _uniform_case(100_000, 40_000, 13)
+    key, v1, v2, km, m1, m2 = _uniform_case(300_000, 60_000, 13)
     fac = omg.HashAggregationOperatorFactory(**{k: v for k, v in zip(
         ["group_by_cols", "group_input_types", "aggs_cols", "agg_input_types", "agg_output_types", "agg_func_types"],
         _cfg1_aggs().values())})
