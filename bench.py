@@ -245,6 +245,10 @@ def run_gpu(args, rank, world):
     stream = torch.cuda.current_stream()
     g = torch.Generator(device=dev)
     g.manual_seed(1234 + rank)
+    if args.only == "agg":
+        agg = run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world)
+        return dict(value=agg["value"], ms=agg["ms_per_step"], build_ms=0.0, launches=agg["gpu_launches"],
+                    roofline=agg["roofline"], clocks=None, e2e=None, agg=agg, rows=AGG_GROUPS)
 
     # ---- device-resident join inputs (torch tensors seen as OmniVec device vectors)
     bkey = torch.randperm(N_BUILD, generator=g, device=dev).to(torch.int64)
@@ -325,7 +329,7 @@ def run_gpu(args, rank, world):
 def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
     """Same probe through host (pinned) VectorBatches of 4096 rows in, host batches out."""
     L, I = omg.LongType(), omg.IntType()
-    bkey, p1, p2, pkey, pnull = join_data_numpy(7 + rank)
+    bkey, p1, p2, pkey, pnull = join_data_numpy(7 + rank, N_PROBE)
     # The e2e operator probes against a build of this step's host data (same shape, same table kind).
     bf2 = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, I, I], [0])
     bop = bf2.create_operator()
@@ -444,7 +448,12 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-agg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "agg"],
+                    help="agg: time only the aggregation workload (profiling runs)")
+    ap.add_argument("--probe-log2", type=int, default=26, help="log2 of probe rows (profiling runs use fewer)")
     args = ap.parse_args()
+    global N_PROBE
+    N_PROBE = 1 << args.probe_log2
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":

@@ -349,91 +349,111 @@ __device__ __forceinline__ Match Lookup(const JoinTable &t, uint64_t key)
     return m;
 }
 
-__global__ void __launch_bounds__(kProbeThreads) ProbeKernel(const __grid_constant__ ProbeLaunch p)
+// Write one output row: probe columns from the probe batch, build columns gathered by build row.
+__device__ __forceinline__ void WriteJoinRow(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t buildRow,
+    uint64_t pos)
 {
-    __shared__ unsigned int roundWarp[kProbeRounds][kProbeThreads / 32];
-    __shared__ unsigned long long blockBase;
+    for (int o = 0; o < p.nOut; ++o) {
+        const JoinOutCol &oc = p.out[o];
+        if (oc.side == 0) {
+            CopyValue(oc.values, pos, b.cols[oc.src], row, oc.width);
+            if (oc.nulls != nullptr && RowIsNull(b.nulls[oc.src], row)) {
+                SetBit(oc.nulls, pos);
+            }
+        } else {
+            CopyValue(oc.values, pos, oc.buildValues, buildRow, oc.width);
+            if (oc.nulls != nullptr && RowIsNull(oc.buildNulls, buildRow)) {
+                SetBit(oc.nulls, pos);
+            }
+        }
+    }
+}
+
+// Each warp owns kWarpRounds * 32 consecutive rows of a tile and works on its own: lane i reads
+// rows base + 32r + i (coalesced), looks the keys up, reserves its output range with one
+// atomicAdd, and writes its matches compacted in row order.  kUnique: every key has at most one
+// build row, so a ballot gives the compaction; otherwise counts are prefix-summed per round.
+constexpr int kWarpRounds = 16;
+constexpr int kRowsPerWarp = kWarpRounds * 32;
+
+template <bool kUnique>
+__global__ void __launch_bounds__(kProbeThreads, 4) ProbeKernel(const __grid_constant__ ProbeLaunch p)
+{
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    const unsigned int lanesBelow = (1u << lane) - 1u;
     for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
         const TileDesc tile = p.tiles[t];
+        const int w0 = warp * kRowsPerWarp;
+        if (w0 >= tile.rows) {
+            continue;
+        }
         const BatchDesc &b = p.batches[tile.batch];
         const void *keyCol = b.cols[p.keyInput];
         const uint8_t *keyNulls = b.nulls[p.keyInput];
-        int64_t entry[kProbeRounds];
-        uint32_t cnt[kProbeRounds];
-        uint32_t prefix[kProbeRounds];
+        const int64_t base = static_cast<int64_t>(tile.row0) + w0;
+        const int nRows = min(kRowsPerWarp, tile.rows - w0);
+        int32_t entry[kWarpRounds];
+        uint32_t cnt[kWarpRounds];
+        uint32_t total = 0;
 #pragma unroll
-        for (int i = 0; i < kProbeRounds; ++i) {
-            const int r = i * kProbeThreads + threadIdx.x;
+        for (int i = 0; i < kWarpRounds; ++i) {
+            const int r = i * 32 + lane;
             cnt[i] = 0;
             entry[i] = 0;
-            if (r < tile.rows) {
-                const int64_t row = static_cast<int64_t>(tile.row0) + r;
-                if (!RowIsNull(keyNulls, row)) {
-                    const Match m = Lookup(p.table, static_cast<uint64_t>(LoadInt(keyCol, row, p.keyWidth)));
-                    cnt[i] = m.count;
-                    entry[i] = m.entry;
-                }
+            if (r < nRows && !RowIsNull(keyNulls, base + r)) {
+                const Match m = Lookup(p.table, static_cast<uint64_t>(LoadInt(keyCol, base + r, p.keyWidth)));
+                cnt[i] = m.count;
+                entry[i] = static_cast<int32_t>(m.entry);
             }
-            uint32_t inc = cnt[i];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) {
-                    inc += y;
-                }
-            }
-            prefix[i] = inc - cnt[i];
-            if (lane == 31) {
-                roundWarp[i][warp] = inc;
+            if (kUnique) {
+                total += __popc(__ballot_sync(0xffffffffu, cnt[i] != 0));
+            } else {
+                total += cnt[i];
             }
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long run = 0;
-            for (int i = 0; i < kProbeRounds; ++i) {
-                for (int w = 0; w < kProbeThreads / 32; ++w) {
-                    const unsigned int c = roundWarp[i][w];
-                    roundWarp[i][w] = static_cast<unsigned int>(run);
-                    run += c;
-                }
-            }
-            blockBase = run ? atomicAdd(p.outCount, run) : 0ull;
+        if (!kUnique) {
+            total = __reduce_add_sync(0xffffffffu, total);
         }
-        __syncthreads();
-        if (!p.countOnly) {
+        unsigned long long pos = 0;
+        if (lane == 0 && total != 0) {
+            pos = atomicAdd(p.outCount, static_cast<unsigned long long>(total));
+        }
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (p.countOnly || total == 0) {
+            continue;
+        }
 #pragma unroll
-            for (int i = 0; i < kProbeRounds; ++i) {
-                if (cnt[i] == 0) {
-                    continue;
+        for (int i = 0; i < kWarpRounds; ++i) {
+            const int64_t row = base + i * 32 + lane;
+            if (kUnique) {
+                const unsigned int m = __ballot_sync(0xffffffffu, cnt[i] != 0);
+                if (cnt[i] != 0) {
+                    const uint64_t at = pos + __popc(m & lanesBelow);
+                    if (at < p.outCapacity) {
+                        WriteJoinRow(p, b, row, entry[i], at);
+                    }
                 }
-                const int64_t row = static_cast<int64_t>(tile.row0) + i * kProbeThreads + threadIdx.x;
-                const uint64_t pos0 = blockBase + roundWarp[i][warp] + prefix[i];
+                pos += __popc(m);
+            } else {
+                uint32_t inc = cnt[i];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) {
+                        inc += y;
+                    }
+                }
+                const uint64_t at = pos + inc - cnt[i];
                 for (uint32_t k = 0; k < cnt[i]; ++k) {
-                    const uint64_t pos = pos0 + k;
-                    if (pos >= p.outCapacity) {
+                    if (at + k >= p.outCapacity) {
                         break;
                     }
-                    const int64_t buildRow = p.table.unique ? entry[i] : p.table.csrRows[entry[i] + k];
-                    for (int o = 0; o < p.nOut; ++o) {
-                        const JoinOutCol &oc = p.out[o];
-                        if (oc.side == 0) {
-                            CopyValue(oc.values, pos, b.cols[oc.src], row, oc.width);
-                            if (oc.nulls != nullptr && RowIsNull(b.nulls[oc.src], row)) {
-                                SetBit(oc.nulls, pos);
-                            }
-                        } else {
-                            CopyValue(oc.values, pos, oc.buildValues, buildRow, oc.width);
-                            if (oc.nulls != nullptr && RowIsNull(oc.buildNulls, buildRow)) {
-                                SetBit(oc.nulls, pos);
-                            }
-                        }
-                    }
+                    WriteJoinRow(p, b, row, p.table.csrRows[entry[i] + k], at + k);
                 }
+                pos += __shfl_sync(0xffffffffu, inc, 31);
             }
         }
-        __syncthreads();
     }
 }
 
@@ -508,13 +528,21 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         return cudaSuccess;
     }
     int blocksPerSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM, ProbeKernel, kProbeThreads, 0);
+    if (p.table.unique) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM, ProbeKernel<true>, kProbeThreads, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM, ProbeKernel<false>, kProbeThreads, 0);
+    }
     if (blocksPerSM <= 0) {
         blocksPerSM = 1;
     }
     const int maxGrid = SMs() * blocksPerSM;
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
-    ProbeKernel<<<grid, kProbeThreads, 0, stream>>>(p);
+    if (p.table.unique) {
+        ProbeKernel<true><<<grid, kProbeThreads, 0, stream>>>(p);
+    } else {
+        ProbeKernel<false><<<grid, kProbeThreads, 0, stream>>>(p);
+    }
     return cudaGetLastError();
 }
 
