@@ -94,7 +94,7 @@ uint64_t NextPow2(uint64_t v)
 constexpr uint64_t kDefaultCapacity = uint64_t(1) << 16;
 constexpr int kGlobalMaxProbe = 96;
 constexpr int64_t kFlushRows = int64_t(1) << 25;     // aggregate at most 32M staged rows per launch
-constexpr size_t kSmemBudget = 200 * 1024;           // shared bytes per CTA for pre-aggregation
+constexpr size_t kSmemBudget = 96 * 1024;            // shared bytes per CTA for pre-aggregation
 
 }  // namespace
 
@@ -353,6 +353,34 @@ OmniStatus HashAggregationOperatorFactory::Init()
         throw OmniException("UNSUPPORTED_ERROR", "at most 8 exact SUM columns", -2);
     }
     p.orderDependent = exactIndex > 0;
+    // Register cache: the first kRegInputs distinct narrow (<= 8 byte) inputs the accumulators
+    // read are loaded once per row, up front.
+    for (auto &a : p.accs) {
+        a.reg = -1;
+        if (a.input < 0 || a.kind == omg::ACC_NULLS || a.inWidth <= 0 || a.inWidth > 8 || a.kind == omg::ACC_WSUM3) {
+            continue;
+        }
+        for (size_t r = 0; r < p.regInput.size(); ++r) {
+            if (p.regInput[r] == a.input) {
+                a.reg = static_cast<int32_t>(r);
+            }
+        }
+        if (a.reg < 0 && p.regInput.size() < static_cast<size_t>(omg::kRegInputs)) {
+            a.reg = static_cast<int32_t>(p.regInput.size());
+            p.regInput.push_back(a.input);
+            p.regWidth.push_back(a.inWidth);
+        }
+    }
+    // NULLS accumulators of an input share its register slot even though they carry no width.
+    for (auto &a : p.accs) {
+        if (a.kind == omg::ACC_NULLS) {
+            for (size_t r = 0; r < p.regInput.size(); ++r) {
+                if (p.regInput[r] == a.input) {
+                    a.reg = static_cast<int32_t>(r);
+                }
+            }
+        }
+    }
     p.stateWords = word;
     p.slotWords = p.keyWords + p.stateWords;
     p.rowsPerBatch = GetMaxRowCount(rowBytes);
@@ -449,6 +477,11 @@ omg::AggLaunch MakeLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacit
     for (int i = 0; i < p.nAccs; ++i) {
         p.accs[i] = plan.accs[i];
     }
+    p.nRegInputs = static_cast<int32_t>(plan.regInput.size());
+    for (int i = 0; i < p.nRegInputs; ++i) {
+        p.regInput[i] = plan.regInput[i];
+        p.regWidth[i] = plan.regWidth[i];
+    }
     p.stateWords = plan.stateWords;
     p.maxProbe = kGlobalMaxProbe;
     p.table.slots = slots;
@@ -497,10 +530,11 @@ void HashAggregationOperator::Flush()
     if (strategy_ != 2) {  // OMG_AGG_STRATEGY_GLOBAL
         smemSlots = static_cast<int>(kSmemBudget / (plan_.slotWords * sizeof(uint64_t)));
     }
-    const int grid = smemSlots > 0 ? sms : sms * 4;
+    const int grid = 0;  // the launcher fills every SM to its occupancy limit
+    const int maxGrid = sms * 4;
     DevArray<unsigned long long> retryA(static_cast<size_t>(rows), s);
     DevArray<unsigned long long> retryB;
-    const size_t spillCap = static_cast<size_t>(smemSlots) * grid;
+    const size_t spillCap = static_cast<size_t>(smemSlots) * maxGrid;
     DevArray<uint64_t> spillA(std::max<size_t>(spillCap, 1) * plan_.slotWords, s);
     DevArray<uint64_t> spillB;
     CudaCheck(cudaMemsetAsync(im.stats.Get() + 1, 0, 3 * sizeof(unsigned long long), s), "reset stats");

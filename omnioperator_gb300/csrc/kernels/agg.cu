@@ -28,6 +28,7 @@ namespace {
 
 constexpr int kSmemProbe = 8;
 constexpr uint64_t kTagLocked = 1;
+constexpr int kAggThreads = 512;
 
 // ------------------------------------------------------------------ key handling
 struct RowKey {
@@ -36,19 +37,19 @@ struct RowKey {
     int special;    // -1 normal, kNullSlotOffset / kSentinelSlotOffset for the special groups
 };
 
-__device__ __forceinline__ RowKey ReadKey(const KeySpec &ks, const BatchDesc &b, int64_t row)
+__device__ __forceinline__ RowKey ReadKey(const KeySpec &ks, const BatchDesc &b, int64_t row, int kind)
 {
     RowKey k;
     k.w[0] = k.w[1] = k.w[2] = 0;
     k.special = -1;
-    if (ks.kind == KEY_SINGLE) {
+    if (kind == KEY_SINGLE) {
         const KeyCol &c = ks.cols[0];
-        if (RowIsNull(b.nulls[c.input], row)) {
+        if (NullRO(b.nulls[c.input], row)) {
             k.special = kNullSlotOffset;
             k.hash = 0;
             return k;
         }
-        uint64_t v = static_cast<uint64_t>(LoadInt(b.cols[c.input], row, c.width));
+        uint64_t v = static_cast<uint64_t>(SignExtend(LoadBitsRO(b.cols[c.input], row, c.width), c.width));
         k.w[0] = v;
         if (v == kEmptyKey) {
             k.special = kSentinelSlotOffset;
@@ -59,7 +60,7 @@ __device__ __forceinline__ RowKey ReadKey(const KeySpec &ks, const BatchDesc &b,
     uint32_t mask = 0;
     for (int ci = 0; ci < ks.nCols; ++ci) {
         const KeyCol &c = ks.cols[ci];
-        if (RowIsNull(b.nulls[c.input], row)) {
+        if (NullRO(b.nulls[c.input], row)) {
             mask |= 1u << ci;
             continue;
         }
@@ -70,7 +71,7 @@ __device__ __forceinline__ RowKey ReadKey(const KeySpec &ks, const BatchDesc &b,
             k.w[wi] = p[0];
             k.w[wi + 1] = p[1];
         } else {
-            k.w[wi] |= LoadBits(b.cols[c.input], row, c.width) << sh;
+            k.w[wi] |= LoadBitsRO(b.cols[c.input], row, c.width) << sh;
         }
     }
     k.w[ks.maskByte >> 3] |= static_cast<uint64_t>(mask) << ((ks.maskByte & 7) * 8);
@@ -85,9 +86,79 @@ __device__ __forceinline__ RowKey ReadKey(const KeySpec &ks, const BatchDesc &b,
 // Published tag of a packed slot: never 0 (free) or 1 (locked).
 __device__ __forceinline__ uint64_t PublishedTag(uint64_t hash) { return (hash | 2ull) & ~1ull; }
 
+// ------------------------------------------------------------------ row inputs
+// A row's key plus the values and null bits of up to kRegInputs narrow inputs, all loaded up
+// front through the read-only path so their latencies overlap.
+struct RowIn {
+    RowKey k;
+    uint64_t v[kRegInputs];  // raw bits, zero-extended
+    uint32_t nulls;          // bit i: register input i is NULL
+};
+
+template <int kKind>
+__device__ __forceinline__ RowIn LoadRow(const AggLaunch &p, const BatchDesc &b, int64_t row)
+{
+    RowIn in;
+    in.k = ReadKey(p.key, b, row, kKind);
+    in.nulls = 0;
+#pragma unroll
+    for (int i = 0; i < kRegInputs; ++i) {
+        in.v[i] = 0;
+        if (i < p.nRegInputs) {
+            const int c = p.regInput[i];
+            in.v[i] = LoadBitsRO(b.cols[c], row, p.regWidth[i]);
+            in.nulls |= (NullRO(b.nulls[c], row) ? 1u : 0u) << i;
+        }
+    }
+    return in;
+}
+
+__device__ __forceinline__ uint64_t CachedBits(const AccSpec &s, const RowIn &in)
+{
+    uint64_t r = 0;
+#pragma unroll
+    for (int i = 0; i < kRegInputs; ++i) {
+        r = (i == s.reg) ? in.v[i] : r;
+    }
+    return r;
+}
+
+__device__ __forceinline__ int64_t AccInt(const AccSpec &s, const BatchDesc &b, int64_t row, const RowIn &in)
+{
+    return s.reg >= 0 ? SignExtend(CachedBits(s, in), s.inWidth) : LoadInt(b.cols[s.input], row, s.inWidth);
+}
+
+__device__ __forceinline__ double AccDouble(const AccSpec &s, const BatchDesc &b, int64_t row, const RowIn &in)
+{
+    if (s.reg < 0) {
+        return LoadAsDouble(b.cols[s.input], row, s.inKind, s.inWidth);
+    }
+    const uint64_t bits = CachedBits(s, in);
+    if (s.inKind == IN_DOUBLE) {
+        return __longlong_as_double(static_cast<long long>(bits));
+    }
+    if (s.inKind == IN_FLOAT) {
+        return static_cast<double>(__int_as_float(static_cast<int>(bits)));
+    }
+    return static_cast<double>(SignExtend(bits, s.inWidth));
+}
+
+__device__ __forceinline__ bool AccNull(const AccSpec &s, const BatchDesc &b, int64_t row, const RowIn &in)
+{
+    return s.reg >= 0 ? ((in.nulls >> s.reg) & 1u) != 0 : RowIsNull(b.nulls[s.input], row);
+}
+
+__device__ __forceinline__ void Red(uint64_t *w, uint64_t v)
+{
+    if (v != 0) {
+        atomicAdd(reinterpret_cast<unsigned long long *>(w), static_cast<unsigned long long>(v));
+    }
+}
+
 // ------------------------------------------------------------------ state updates
 // `st` points at the group's state words, in shared or global memory.
-__device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc &b, int64_t row, uint64_t *st)
+__device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc &b, int64_t row, const RowIn &in,
+    uint64_t *st)
 {
     for (int a = 0; a < p.nAccs; ++a) {
         const AccSpec &s = p.accs[a];
@@ -96,7 +167,7 @@ __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc
             atomicAdd(reinterpret_cast<unsigned long long *>(w), 1ull);
             continue;
         }
-        const bool isNull = RowIsNull(b.nulls[s.input], row);
+        const bool isNull = AccNull(s, b, row, in);
         if (s.kind == ACC_NULLS) {
             if (isNull) {
                 atomicAdd(reinterpret_cast<unsigned long long *>(w), 1ull);
@@ -106,58 +177,52 @@ __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc
         if (isNull) {
             continue;
         }
-        const void *col = b.cols[s.input];
         switch (s.kind) {
-            case ACC_ISUM: {
-                int64_t x = LoadInt(col, row, s.inWidth);
-                if (x != 0) {
-                    atomicAdd(reinterpret_cast<unsigned long long *>(w), static_cast<unsigned long long>(x));
-                }
+            case ACC_ISUM:
+                Red(w, static_cast<uint64_t>(AccInt(s, b, row, in)));
                 break;
-            }
             case ACC_WSUM2: {
-                int64_t x = LoadInt(col, row, s.inWidth);
-                if (x >= 0) {
-                    AtomicAddU128(w, static_cast<uint64_t>(x), 0);
-                } else {
-                    AtomicAddU128(w + 2, 0ull - static_cast<uint64_t>(x), 0);
-                }
+                const int64_t x = AccInt(s, b, row, in);
+                const uint64_t m = x >= 0 ? static_cast<uint64_t>(x) : 0ull - static_cast<uint64_t>(x);
+                uint64_t *side = x >= 0 ? w : w + 2;
+                Red(side, m & 0xffffffffull);
+                Red(side + 1, m >> 32);
                 break;
             }
             case ACC_WSUM3: {
-                const uint64_t *v = static_cast<const uint64_t *>(col) + 2 * row;
+                const uint64_t *v = static_cast<const uint64_t *>(b.cols[s.input]) + 2 * row;
                 uint64_t lo = v[0];
                 uint64_t hi = v[1];
-                if (static_cast<int64_t>(hi) >= 0) {
-                    AtomicAddU192(w, lo, hi, 0);
-                } else {
-                    // magnitude = -(hi:lo)
-                    uint64_t nlo = ~lo + 1;
-                    uint64_t nhi = ~hi + (nlo == 0 ? 1u : 0u);
-                    AtomicAddU192(w + 3, nlo, nhi, 0);
+                uint64_t *side = w;
+                if (static_cast<int64_t>(hi) < 0) {  // magnitude = -(hi:lo)
+                    lo = ~lo + 1;
+                    hi = ~hi + (lo == 0 ? 1u : 0u);
+                    side = w + 4;
                 }
+                Red(side, lo & 0xffffffffull);
+                Red(side + 1, lo >> 32);
+                Red(side + 2, hi & 0xffffffffull);
+                Red(side + 3, hi >> 32);
                 break;
             }
-            case ACC_DSUM: {
-                double x = LoadAsDouble(col, row, s.inKind, s.inWidth);
-                AtomicAddCompensated(w, x, 0.0);
+            case ACC_DSUM:
+                AtomicAddCompensated(w, AccDouble(s, b, row, in), 0.0);
                 break;
-            }
             case ACC_IMIN:
-                AtomicMinI64(w, LoadInt(col, row, s.inWidth));
+                AtomicMinI64(w, AccInt(s, b, row, in));
                 break;
             case ACC_IMAX:
-                AtomicMaxI64(w, LoadInt(col, row, s.inWidth));
+                AtomicMaxI64(w, AccInt(s, b, row, in));
                 break;
             case ACC_DMIN: {
-                double x = LoadAsDouble(col, row, s.inKind, s.inWidth);
+                const double x = AccDouble(s, b, row, in);
                 if (!isnan(x)) {
                     AtomicMinI64(w, OrderedFromDouble(x));
                 }
                 break;
             }
             case ACC_DMAX: {
-                double x = LoadAsDouble(col, row, s.inKind, s.inWidth);
+                const double x = AccDouble(s, b, row, in);
                 if (!isnan(x)) {
                     AtomicMaxI64(w, OrderedFromDouble(x));
                 }
@@ -185,12 +250,11 @@ __device__ __forceinline__ void MergeStates(const AccSpec *accs, int nAccs, cons
                 }
                 break;
             case ACC_WSUM2:
-                AtomicAddU128(w, v[0], v[1]);
-                AtomicAddU128(w + 2, v[2], v[3]);
-                break;
             case ACC_WSUM3:
-                AtomicAddU192(w, v[0], v[1], v[2]);
-                AtomicAddU192(w + 3, v[3], v[4], v[5]);
+                // chunk sums add word by word
+                for (int j = 0; j < (s.kind == ACC_WSUM2 ? 4 : 8); ++j) {
+                    Red(w + j, v[j]);
+                }
                 break;
             case ACC_DSUM: {
                 double s0 = __longlong_as_double(static_cast<long long>(v[0]));
@@ -231,7 +295,7 @@ __device__ __forceinline__ void InitStates(const AccSpec *accs, int nAccs, int s
 // ------------------------------------------------------------------ global table
 // Returns the slot index or -1 when no slot was found within maxProbe probes.
 __device__ __forceinline__ int64_t GlobalFind(const AggTable &t, const KeySpec &ks, const RowKey &k, int maxProbe,
-    int32_t *error, bool *inserted, long long waitBudget)
+    int32_t *error, bool *inserted, long long waitBudget, int kind)
 {
     *inserted = false;
     if (k.special >= 0) {
@@ -243,7 +307,7 @@ __device__ __forceinline__ int64_t GlobalFind(const AggTable &t, const KeySpec &
     }
     const uint64_t mask = t.capacity - 1;
     uint64_t i = k.hash & mask;
-    if (ks.kind == KEY_SINGLE) {
+    if (kind == KEY_SINGLE) {
         for (int probe = 0; probe < maxProbe; ++probe) {
             unsigned long long *kp = reinterpret_cast<unsigned long long *>(t.slots + i * t.slotWords);
             unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(kp);
@@ -308,10 +372,11 @@ __device__ __forceinline__ int64_t GlobalFind(const AggTable &t, const KeySpec &
 // ------------------------------------------------------------------ shared-memory table
 // Same layout as the global table (slotWords words per slot), nSlots slots, no special
 // slots (those rows go straight to the global table).  Returns the slot or -1.
-__device__ __forceinline__ int SmemFind(uint64_t *sm, int nSlots, int slotWords, const KeySpec &ks, const RowKey &k)
+__device__ __forceinline__ int SmemFind(uint64_t *sm, int nSlots, int slotWords, const KeySpec &ks, const RowKey &k,
+    int kind)
 {
     int i = static_cast<int>((static_cast<uint64_t>(static_cast<uint32_t>(k.hash >> 32)) * nSlots) >> 32);
-    if (ks.kind == KEY_SINGLE) {
+    if (kind == KEY_SINGLE) {
         for (int probe = 0; probe < kSmemProbe; ++probe) {
             unsigned long long *kp = reinterpret_cast<unsigned long long *>(sm + static_cast<int64_t>(i) * slotWords);
             unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(kp);
@@ -388,22 +453,21 @@ __device__ __forceinline__ void QueueRetry(const AggLaunch &p, int32_t batch, in
     }
 }
 
-__device__ __forceinline__ void ProcessRow(const AggLaunch &p, int32_t batchIdx, int64_t row, uint64_t *sm, int smSlots,
-    unsigned int *newGroups)
+template <int kKind>
+__device__ __forceinline__ void ProcessRow(const AggLaunch &p, int32_t batchIdx, const BatchDesc &b, int64_t row,
+    const RowIn &in, uint64_t *sm, int smSlots, unsigned int *newGroups)
 {
-    const BatchDesc &b = p.batches[batchIdx];
-    const RowKey k = ReadKey(p.key, b, row);
     const int sw = p.table.slotWords;
     const int kw = p.table.keyWords;
-    if (smSlots > 0 && k.special < 0) {
-        int i = SmemFind(sm, smSlots, sw, p.key, k);
+    if (smSlots > 0 && in.k.special < 0) {
+        int i = SmemFind(sm, smSlots, sw, p.key, in.k, kKind);
         if (i >= 0) {
-            UpdateStates(p, b, row, sm + static_cast<int64_t>(i) * sw + kw);
+            UpdateStates(p, b, row, in, sm + static_cast<int64_t>(i) * sw + kw);
             return;
         }
     }
     bool inserted = false;
-    int64_t g = GlobalFind(p.table, p.key, k, p.maxProbe, p.error, &inserted, p.waitBudget);
+    int64_t g = GlobalFind(p.table, p.key, in.k, p.maxProbe, p.error, &inserted, p.waitBudget, kKind);
     if (g < 0) {
         QueueRetry(p, batchIdx, row);
         return;
@@ -411,7 +475,7 @@ __device__ __forceinline__ void ProcessRow(const AggLaunch &p, int32_t batchIdx,
     if (inserted) {
         atomicAdd(newGroups, 1u);
     }
-    UpdateStates(p, b, row, p.table.slots + g * sw + kw);
+    UpdateStates(p, b, row, in, p.table.slots + g * sw + kw);
 }
 
 // Spill records: [key words (keyWords)][state words], slotWords words each.
@@ -423,6 +487,7 @@ struct SpillArgs {
     uint32_t nSpillIn;
 };
 
+template <int kKind>
 __device__ __forceinline__ void MergeRecord(const AggLaunch &p, const SpillArgs &sp, const uint64_t *rec,
     unsigned int *newGroups)
 {
@@ -431,7 +496,7 @@ __device__ __forceinline__ void MergeRecord(const AggLaunch &p, const SpillArgs 
     RowKey k;
     k.special = -1;
     k.w[0] = k.w[1] = k.w[2] = 0;
-    if (p.key.kind == KEY_SINGLE) {
+    if (kKind == KEY_SINGLE) {
         k.w[0] = rec[0];
         k.hash = Mix64(k.w[0]);
     } else {
@@ -443,7 +508,7 @@ __device__ __forceinline__ void MergeRecord(const AggLaunch &p, const SpillArgs 
         k.hash = h;
     }
     bool inserted = false;
-    int64_t g = GlobalFind(p.table, p.key, k, p.maxProbe, p.error, &inserted, p.waitBudget);
+    int64_t g = GlobalFind(p.table, p.key, k, p.maxProbe, p.error, &inserted, p.waitBudget, kKind);
     if (g < 0) {
         unsigned int pos = atomicAdd(sp.nSpill, 1u);
         if (pos < sp.spillCap) {
@@ -462,7 +527,9 @@ __device__ __forceinline__ void MergeRecord(const AggLaunch &p, const SpillArgs 
     MergeStates(p.accs, p.nAccs, rec + kw, p.table.slots + g * sw + kw);
 }
 
-__global__ void __launch_bounds__(512) AggKernel(const __grid_constant__ AggLaunch p, const SpillArgs sp)
+template <int kKind>
+__global__ void __launch_bounds__(kAggThreads, 2) AggKernel(const __grid_constant__ AggLaunch p,
+    const __grid_constant__ SpillArgs sp)
 {
     extern __shared__ __align__(16) uint64_t smem[];
     __shared__ unsigned int newGroups;
@@ -487,16 +554,31 @@ __global__ void __launch_bounds__(512) AggKernel(const __grid_constant__ AggLaun
         const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
         for (int64_t i = gtid; i < p.nRetryIn; i += stride) {
             unsigned long long e = p.retryIn[i];
-            ProcessRow(p, static_cast<int32_t>(e >> 32), static_cast<int64_t>(e & 0xffffffffull), smem, 0, &newGroups);
+            const int32_t bi = static_cast<int32_t>(e >> 32);
+            const int64_t row = static_cast<int64_t>(e & 0xffffffffull);
+            const BatchDesc &b = p.batches[bi];
+            ProcessRow<kKind>(p, bi, b, row, LoadRow<kKind>(p, b, row), smem, 0, &newGroups);
         }
         for (int64_t i = gtid; i < sp.nSpillIn; i += stride) {
-            MergeRecord(p, sp, sp.spillIn + i * sw, &newGroups);
+            MergeRecord<kKind>(p, sp, sp.spillIn + i * sw, &newGroups);
         }
     } else {
+        // Two rows per thread per step: both rows' loads are issued before either is processed.
         for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
             const TileDesc tile = p.tiles[t];
-            for (int r = threadIdx.x; r < tile.rows; r += blockDim.x) {
-                ProcessRow(p, tile.batch, static_cast<int64_t>(tile.row0) + r, smem, smSlots, &newGroups);
+            const BatchDesc &b = p.batches[tile.batch];
+            for (int r = threadIdx.x; r < tile.rows; r += 2 * blockDim.x) {
+                const int64_t row0 = static_cast<int64_t>(tile.row0) + r;
+                const bool second = r + static_cast<int>(blockDim.x) < tile.rows;
+                const RowIn a = LoadRow<kKind>(p, b, row0);
+                RowIn c;
+                if (second) {
+                    c = LoadRow<kKind>(p, b, row0 + blockDim.x);
+                }
+                ProcessRow<kKind>(p, tile.batch, b, row0, a, smem, smSlots, &newGroups);
+                if (second) {
+                    ProcessRow<kKind>(p, tile.batch, b, row0 + blockDim.x, c, smem, smSlots, &newGroups);
+                }
             }
         }
     }
@@ -506,7 +588,7 @@ __global__ void __launch_bounds__(512) AggKernel(const __grid_constant__ AggLaun
     for (int i = threadIdx.x; i < smSlots; i += blockDim.x) {
         const uint64_t *slot = smem + static_cast<int64_t>(i) * sw;
         if (SlotOccupied(p.key, slot[0])) {
-            MergeRecord(p, sp, slot, &newGroups);
+            MergeRecord<kKind>(p, sp, slot, &newGroups);
         }
     }
     __syncthreads();
@@ -568,7 +650,7 @@ __global__ void RehashKernel(AggTable from, AggTable to, const __grid_constant__
             }
             bool inserted = false;
             int64_t g = GlobalFind(to, p.key, k, static_cast<int>(to.capacity < (1ull << 30) ? to.capacity : (1ull << 30)),
-                p.error, &inserted, p.waitBudget);
+                p.error, &inserted, p.waitBudget, p.key.kind);
             if (g < 0) {
                 SetError(p.error, 4);
                 continue;
@@ -675,20 +757,24 @@ __device__ __forceinline__ void Add192(const uint64_t *a, const uint64_t *b, uin
 
 __device__ __forceinline__ WideSum DecodeWide(const AccSpec &s, const uint64_t *w)
 {
+    // Side value = sum over k of word_k * 2^(32k) (each word is a sum of 32-bit chunks).
+    const int n = s.kind == ACC_WSUM2 ? 2 : 4;
     uint64_t pos[3] = {0, 0, 0};
     uint64_t neg[3] = {0, 0, 0};
-    if (s.kind == ACC_WSUM2) {
-        pos[0] = w[0];
-        pos[1] = w[1];
-        neg[0] = w[2];
-        neg[1] = w[3];
-    } else {
-        pos[0] = w[0];
-        pos[1] = w[1];
-        pos[2] = w[2];
-        neg[0] = w[3];
-        neg[1] = w[4];
-        neg[2] = w[5];
+    for (int k = 0; k < n; ++k) {
+        uint64_t a[3] = {0, 0, 0};
+        uint64_t b[3] = {0, 0, 0};
+        const int sh = 32 * k;
+        const int wi = sh >> 6;
+        const int bi = sh & 63;
+        a[wi] = w[k] << bi;
+        b[wi] = w[n + k] << bi;
+        if (bi != 0 && wi + 1 < 3) {
+            a[wi + 1] = w[k] >> (64 - bi);
+            b[wi + 1] = w[n + k] >> (64 - bi);
+        }
+        Add192(pos, a, pos);
+        Add192(neg, b, neg);
     }
     WideSum r;
     if (Cmp192(pos, neg) >= 0) {
@@ -944,7 +1030,7 @@ __global__ void OrderedOverflowKernel(const __grid_constant__ AggLaunch p, int32
     for (int32_t bi = 0; bi < nBatches; ++bi) {
         const BatchDesc &b = p.batches[bi];
         for (int64_t row = 0; row < b.rows; ++row) {
-            const RowKey k = ReadKey(p.key, b, row);
+            const RowKey k = ReadKey(p.key, b, row, p.key.kind);
             const int64_t slot = FindSlot(p.table, p.key, k);
             if (slot < 0 || denseOf[slot] < 0) {
                 continue;
@@ -1047,19 +1133,23 @@ cudaError_t LaunchAgg(const AggLaunch &p, uint64_t *spill, unsigned int *nSpill,
 {
     SpillArgs sp{spill, nSpill, spillCap, spillIn, nSpillIn};
     const size_t smemBytes = static_cast<size_t>(p.smemSlots) * p.table.slotWords * sizeof(uint64_t);
-    static size_t configured = 0;
-    if (smemBytes > 48 * 1024 && smemBytes > configured) {
+    auto kernel = p.key.kind == KEY_SINGLE ? AggKernel<KEY_SINGLE> : AggKernel<KEY_PACKED>;
+    static size_t configured[2] = {0, 0};
+    size_t &conf = configured[p.key.kind == KEY_SINGLE ? 0 : 1];
+    if (smemBytes > 48 * 1024 && smemBytes > conf) {
         cudaError_t err =
-            cudaFuncSetAttribute(AggKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smemBytes));
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smemBytes));
         if (err != cudaSuccess) {
             return err;
         }
-        configured = smemBytes;
+        conf = smemBytes;
     }
     if (gridBlocks <= 0) {
-        gridBlocks = NumSMs();
+        int perSM = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, kAggThreads, smemBytes);
+        gridBlocks = NumSMs() * (perSM > 0 ? perSM : 1);
     }
-    AggKernel<<<gridBlocks, 512, smemBytes, stream>>>(p, sp);
+    kernel<<<gridBlocks, kAggThreads, smemBytes, stream>>>(p, sp);
     return cudaGetLastError();
 }
 

@@ -55,6 +55,40 @@ __device__ __forceinline__ uint64_t LoadBits(const void *col, int64_t row, int w
     }
 }
 
+// Read-only (non-coherent path) loads of input columns the kernels never write.
+__device__ __forceinline__ uint64_t LoadBitsRO(const void *col, int64_t row, int width)
+{
+    switch (width) {
+        case 1:
+            return static_cast<uint8_t>(__ldg(static_cast<const char *>(col) + row));
+        case 2:
+            return static_cast<uint16_t>(__ldg(static_cast<const short *>(col) + row));
+        case 4:
+            return static_cast<uint32_t>(__ldg(static_cast<const int *>(col) + row));
+        default:
+            return static_cast<uint64_t>(__ldg(static_cast<const long long *>(col) + row));
+    }
+}
+
+__device__ __forceinline__ bool NullRO(const uint8_t *nulls, int64_t row)
+{
+    return nulls != nullptr && ((__ldg(reinterpret_cast<const unsigned char *>(nulls) + (row >> 3)) >> (row & 7)) & 1u);
+}
+
+__device__ __forceinline__ int64_t SignExtend(uint64_t bits, int width)
+{
+    switch (width) {
+        case 1:
+            return static_cast<int8_t>(bits);
+        case 2:
+            return static_cast<int16_t>(bits);
+        case 4:
+            return static_cast<int32_t>(bits);
+        default:
+            return static_cast<int64_t>(bits);
+    }
+}
+
 __device__ __forceinline__ double LoadAsDouble(const void *col, int64_t row, int inKind, int width)
 {
     if (inKind == IN_DOUBLE) {

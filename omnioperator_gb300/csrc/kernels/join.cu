@@ -68,6 +68,23 @@ __device__ __forceinline__ void CopyValue(void *dst, uint64_t dpos, const void *
     }
 }
 
+__device__ __forceinline__ void StoreKey(void *dst, uint64_t pos, int width, int64_t v)
+{
+    switch (width) {
+        case 1:
+            static_cast<int8_t *>(dst)[pos] = static_cast<int8_t>(v);
+            break;
+        case 2:
+            static_cast<int16_t *>(dst)[pos] = static_cast<int16_t>(v);
+            break;
+        case 4:
+            static_cast<int32_t *>(dst)[pos] = static_cast<int32_t>(v);
+            break;
+        default:
+            static_cast<int64_t *>(dst)[pos] = v;
+    }
+}
+
 __device__ __forceinline__ void SetBit(uint8_t *bitmap, uint64_t pos)
 {
     atomicOr(reinterpret_cast<unsigned int *>(bitmap) + (pos >> 5), 1u << (pos & 31));
@@ -349,20 +366,71 @@ __device__ __forceinline__ Match Lookup(const JoinTable &t, uint64_t key)
     return m;
 }
 
-// Write one output row: probe columns from the probe batch, build columns gathered by build row.
-__device__ __forceinline__ void WriteJoinRow(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t buildRow,
-    uint64_t pos)
+// Read-only loads (non-coherent path): the probe never writes what it reads, so these may be
+// issued ahead of the output stores.
+__device__ __forceinline__ int64_t LoadIntRO(const void *col, int64_t row, int width)
+{
+    switch (width) {
+        case 1:
+            return static_cast<int8_t>(__ldg(static_cast<const char *>(col) + row));
+        case 2:
+            return __ldg(static_cast<const short *>(col) + row);
+        case 4:
+            return __ldg(static_cast<const int *>(col) + row);
+        default:
+            return __ldg(static_cast<const long long *>(col) + row);
+    }
+}
+
+__device__ __forceinline__ bool RowIsNullRO(const uint8_t *nulls, int64_t row)
+{
+    return nulls != nullptr && ((__ldg(reinterpret_cast<const unsigned char *>(nulls) + (row >> 3)) >> (row & 7)) & 1u);
+}
+
+__device__ __forceinline__ void CopyValueRO(void *dst, uint64_t dpos, const void *src, int64_t spos, int width)
+{
+    switch (width) {
+        case 1:
+            static_cast<uint8_t *>(dst)[dpos] = static_cast<uint8_t>(__ldg(static_cast<const char *>(src) + spos));
+            break;
+        case 2:
+            static_cast<uint16_t *>(dst)[dpos] = static_cast<uint16_t>(__ldg(static_cast<const short *>(src) + spos));
+            break;
+        case 4:
+            static_cast<uint32_t *>(dst)[dpos] = static_cast<uint32_t>(__ldg(static_cast<const int *>(src) + spos));
+            break;
+        case 8:
+            static_cast<uint64_t *>(dst)[dpos] = static_cast<uint64_t>(__ldg(static_cast<const long long *>(src) + spos));
+            break;
+        case 16: {
+            const longlong2 v = __ldg(static_cast<const longlong2 *>(src) + spos);
+            static_cast<longlong2 *>(dst)[dpos] = v;
+            break;
+        }
+        default:
+            CopyValue(dst, dpos, src, spos, width);
+    }
+}
+
+// Write one output row: probe columns from the probe batch (the key from registers), build
+// columns gathered by build row.
+__device__ __forceinline__ void WriteJoinRow(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t key,
+    int64_t buildRow, uint64_t pos)
 {
     for (int o = 0; o < p.nOut; ++o) {
         const JoinOutCol &oc = p.out[o];
         if (oc.side == 0) {
-            CopyValue(oc.values, pos, b.cols[oc.src], row, oc.width);
-            if (oc.nulls != nullptr && RowIsNull(b.nulls[oc.src], row)) {
-                SetBit(oc.nulls, pos);
+            if (oc.src == p.keyInput) {
+                StoreKey(oc.values, pos, oc.width, key);
+            } else {
+                CopyValueRO(oc.values, pos, b.cols[oc.src], row, oc.width);
+                if (oc.nulls != nullptr && RowIsNullRO(b.nulls[oc.src], row)) {
+                    SetBit(oc.nulls, pos);
+                }
             }
         } else {
-            CopyValue(oc.values, pos, oc.buildValues, buildRow, oc.width);
-            if (oc.nulls != nullptr && RowIsNull(oc.buildNulls, buildRow)) {
+            CopyValueRO(oc.values, pos, oc.buildValues, buildRow, oc.width);
+            if (oc.nulls != nullptr && RowIsNullRO(oc.buildNulls, buildRow)) {
                 SetBit(oc.nulls, pos);
             }
         }
@@ -377,11 +445,12 @@ constexpr int kWarpRounds = 16;
 constexpr int kRowsPerWarp = kWarpRounds * 32;
 
 template <bool kUnique>
-__global__ void __launch_bounds__(kProbeThreads, 4) ProbeKernel(const __grid_constant__ ProbeLaunch p)
+__global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_constant__ ProbeLaunch p)
 {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const unsigned int lanesBelow = (1u << lane) - 1u;
+    const bool arrayMode = p.table.mode == JOIN_ARRAY;
     for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
         const TileDesc tile = p.tiles[t];
         const int w0 = warp * kRowsPerWarp;
@@ -393,26 +462,59 @@ __global__ void __launch_bounds__(kProbeThreads, 4) ProbeKernel(const __grid_con
         const uint8_t *keyNulls = b.nulls[p.keyInput];
         const int64_t base = static_cast<int64_t>(tile.row0) + w0;
         const int nRows = min(kRowsPerWarp, tile.rows - w0);
-        int32_t entry[kWarpRounds];
-        uint32_t cnt[kWarpRounds];
-        uint32_t total = 0;
+        // Phase 1: all keys and validity bits of the warp's rows (independent loads).
+        int64_t key[kWarpRounds];
+        uint32_t live = 0;  // bit i: this lane's row of round i exists and its key is not NULL
 #pragma unroll
         for (int i = 0; i < kWarpRounds; ++i) {
             const int r = i * 32 + lane;
-            cnt[i] = 0;
-            entry[i] = 0;
-            if (r < nRows && !RowIsNull(keyNulls, base + r)) {
-                const Match m = Lookup(p.table, static_cast<uint64_t>(LoadInt(keyCol, base + r, p.keyWidth)));
-                cnt[i] = m.count;
-                entry[i] = static_cast<int32_t>(m.entry);
-            }
-            if (kUnique) {
-                total += __popc(__ballot_sync(0xffffffffu, cnt[i] != 0));
-            } else {
-                total += cnt[i];
+            key[i] = 0;
+            if (r < nRows) {
+                key[i] = LoadIntRO(keyCol, base + r, p.keyWidth);
+                if (!RowIsNullRO(keyNulls, base + r)) {
+                    live |= 1u << i;
+                }
             }
         }
-        if (!kUnique) {
+        // Phase 2: table lookups (independent of each other).
+        int32_t entry[kWarpRounds];
+        uint32_t cnt[kWarpRounds];
+        uint32_t hit = 0;
+        if (arrayMode) {
+#pragma unroll
+            for (int i = 0; i < kWarpRounds; ++i) {
+                const uint64_t d = static_cast<uint64_t>(key[i]) - static_cast<uint64_t>(p.table.minKey);
+                int64_t e = -1;
+                if (((live >> i) & 1u) && key[i] >= p.table.minKey && d < p.table.range) {
+                    e = __ldg(reinterpret_cast<const long long *>(p.table.arrayEntries) + d);
+                }
+                entry[i] = kUnique ? static_cast<int32_t>(e) : static_cast<int32_t>(e >> 32);
+                cnt[i] = e < 0 ? 0u : (kUnique ? 1u : static_cast<uint32_t>(e & 0xffffffffll));
+                hit |= (cnt[i] != 0 ? 1u : 0u) << i;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < kWarpRounds; ++i) {
+                Match m{0, 0};
+                if ((live >> i) & 1u) {
+                    m = Lookup(p.table, static_cast<uint64_t>(key[i]));
+                }
+                entry[i] = static_cast<int32_t>(m.entry);
+                cnt[i] = m.count;
+                hit |= (m.count != 0 ? 1u : 0u) << i;
+            }
+        }
+        uint32_t total = 0;
+        if (kUnique) {
+#pragma unroll
+            for (int i = 0; i < kWarpRounds; ++i) {
+                total += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < kWarpRounds; ++i) {
+                total += cnt[i];
+            }
             total = __reduce_add_sync(0xffffffffu, total);
         }
         unsigned long long pos = 0;
@@ -423,15 +525,17 @@ __global__ void __launch_bounds__(kProbeThreads, 4) ProbeKernel(const __grid_con
         if (p.countOnly || total == 0) {
             continue;
         }
+        // Phase 3: compacted writes in row order.
 #pragma unroll
         for (int i = 0; i < kWarpRounds; ++i) {
             const int64_t row = base + i * 32 + lane;
             if (kUnique) {
-                const unsigned int m = __ballot_sync(0xffffffffu, cnt[i] != 0);
-                if (cnt[i] != 0) {
+                const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
+                if ((hit >> i) & 1u) {
                     const uint64_t at = pos + __popc(m & lanesBelow);
                     if (at < p.outCapacity) {
-                        WriteJoinRow(p, b, row, entry[i], at);
+                        // The key is re-read (an L1/L2 hit) rather than kept live in registers.
+                        WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), entry[i], at);
                     }
                 }
                 pos += __popc(m);
@@ -449,7 +553,8 @@ __global__ void __launch_bounds__(kProbeThreads, 4) ProbeKernel(const __grid_con
                     if (at + k >= p.outCapacity) {
                         break;
                     }
-                    WriteJoinRow(p, b, row, p.table.csrRows[entry[i] + k], at + k);
+                    WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), __ldg(p.table.csrRows + entry[i] + k),
+                        at + k);
                 }
                 pos += __shfl_sync(0xffffffffu, inc, 31);
             }

@@ -61,11 +61,15 @@ struct KeySpec {
 //  COUNT_ALL  rows of the group                          1 word
 //  NULLS      NULL rows of input column `input`          1 word   (COUNT(col) = COUNT_ALL - NULLS)
 //  ISUM       wrapping int64 sum                         1 word
-//  WSUM2      exact sum as two unsigned 128-bit halves   4 words  (pos lo/hi, neg lo/hi)
-//  WSUM3      the same with 192-bit halves               6 words
+//  WSUM2      exact sum of int64 values                  4 words
+//  WSUM3      exact sum of int128 (decimal128) values    8 words
 //  DSUM       compensated double sum (s, c)              2 words
 //  IMIN/IMAX  int64 min / max                            1 word
 //  DMIN/DMAX  double min / max as order-preserving int64 1 word
+// WSUM keeps the positive and the negative values apart, each as sums of 32-bit chunks: word k
+// of a side accumulates bits [32k, 32k+32) of every magnitude.  A word therefore never carries
+// for fewer than 2^32 rows per group, every update is a fire-and-forget atomic add, the exact
+// sum is pos - neg and sum|x| is pos + neg (the sticky-overflow rule needs both).
 enum AccKind : int16_t {
     ACC_COUNT_ALL = 0,
     ACC_NULLS = 1,
@@ -85,7 +89,7 @@ struct AccSpec {
     int16_t inKind;   // InKind
     int16_t inWidth;  // bytes per input value
     int32_t word;     // first state word
-    int32_t pad;
+    int32_t reg;      // slot of the input in the per-row register cache (-1: load directly)
     int64_t init;     // initial value of the first word
 };
 
@@ -95,7 +99,7 @@ inline int AccWords(int kind)
         case ACC_WSUM2:
             return 4;
         case ACC_WSUM3:
-            return 6;
+            return 8;
         case ACC_DSUM:
             return 2;
         default:
@@ -121,11 +125,16 @@ struct AggTable {
     unsigned long long *groupCount;   // groups inserted so far (block-aggregated)
 };
 
+constexpr int kRegInputs = 4;  // kernel inputs of <= 8 bytes loaded into registers per row
+
 struct AggLaunch {
     const BatchDesc *batches;
     const TileDesc *tiles;
     int32_t nTiles;
     int32_t nAccs;
+    int32_t nRegInputs;               // inputs cached in registers (<= kRegInputs)
+    int16_t regInput[kRegInputs];     // their kernel input indices
+    int16_t regWidth[kRegInputs];     // their widths in bytes
     KeySpec key;
     AccSpec accs[kMaxAccs];
     int32_t stateWords;

@@ -31,6 +31,8 @@ struct AggPlan {
     std::vector<int32_t> inputCols;        // batch column of each kernel input
     omg::KeySpec key{};
     std::vector<omg::AccSpec> accs;
+    std::vector<int16_t> regInput;         // kernel inputs cached in registers per row
+    std::vector<int16_t> regWidth;
     int32_t stateWords = 0;
     int32_t keyWords = 0;                  // words before the state in a table slot
     int32_t slotWords = 0;
