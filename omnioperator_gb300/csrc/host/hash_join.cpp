@@ -466,6 +466,30 @@ void LookupJoinOperator::ProcessPending()
         }
         cols[o].width = oc.width;
     }
+    // Unique build keys and <= 8 bytes of NULL-free build output per row: fetch the build
+    // values with the table entry from a per-slot packed copy (built once per factory).
+    {
+        bool eligible = b.table.unique && nOut > nProbeOut;
+        int shift = 0;
+        for (size_t o = nProbeOut; o < nOut && eligible; ++o) {
+            const int w = p.out[o].width;
+            eligible = (w == 1 || w == 2 || w == 4 || w == 8) && !cols[o].hasNull && shift + 8 * w <= 64;
+            p.out[o].shift = static_cast<int16_t>(shift);
+            shift += 8 * w;
+        }
+        std::lock_guard<std::mutex> g(f_.payloadMu);
+        if (eligible && !f_.payloadDecided) {
+            const uint64_t nSlots = b.table.mode == omg::JOIN_ARRAY ? b.table.range : b.table.capacity;
+            f_.slotPayload = omg::Buffer::NewDevice((nSlots + 1) * sizeof(uint64_t), s, false);
+            CudaCheck(omg::LaunchBuildSlotPayload(p, nSlots, static_cast<uint64_t *>(f_.slotPayload->Data()), s),
+                "build slot payload");
+            impl_->stream.Sync();
+            f_.payloadDecided = true;
+        }
+        if (eligible && f_.slotPayload) {
+            p.table.slotPayload = static_cast<const uint64_t *>(f_.slotPayload->Data());
+        }
+    }
     DevArray<unsigned long long> count(2, s, true);
     p.outCount = count.Get();
     uint64_t capacity = static_cast<uint64_t>(std::max<int64_t>(probeRows, 1));

@@ -326,26 +326,30 @@ __global__ void ScanApplyKernel(const uint32_t *counts, int64_t n, const int64_t
 struct Match {
     int64_t entry;  // build row (unique) or CSR offset
     uint32_t count;
+    uint64_t slot;  // table slot of the key (the slot payload index)
 };
 
 __device__ __forceinline__ Match Lookup(const JoinTable &t, uint64_t key)
 {
-    Match m{0, 0};
+    Match m{0, 0, 0};
     int64_t e = -1;
     if (t.mode == JOIN_ARRAY) {
         const uint64_t d = key - static_cast<uint64_t>(t.minKey);
         if (static_cast<int64_t>(key) >= t.minKey && d < t.range) {
-            e = t.arrayEntries[d];
+            e = __ldg(reinterpret_cast<const long long *>(t.arrayEntries) + d);
+            m.slot = d;
         }
     } else if (key == kEmptyKey) {
         e = t.sentinelEntry;
+        m.slot = t.capacity;
     } else {
         const uint64_t mask = t.capacity - 1;
         uint64_t i = Mix64(key) & mask;
         for (uint64_t probe = 0; probe < t.capacity; ++probe) {
-            const uint64_t k = t.hashKeys[i];
+            const uint64_t k = __ldg(reinterpret_cast<const unsigned long long *>(t.hashKeys) + i);
             if (k == key) {
-                e = t.hashEntries[i];
+                e = __ldg(reinterpret_cast<const long long *>(t.hashEntries) + i);
+                m.slot = i;
                 break;
             }
             if (k == kEmptyKey) {
@@ -437,6 +441,49 @@ __device__ __forceinline__ void WriteJoinRow(const ProbeLaunch &p, const BatchDe
     }
 }
 
+// Same as WriteJoinRow with the build columns taken from the packed slot payload.
+__device__ __forceinline__ void WriteJoinRowPayload(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t key,
+    uint64_t payload, uint64_t pos)
+{
+    for (int o = 0; o < p.nOut; ++o) {
+        const JoinOutCol &oc = p.out[o];
+        if (oc.side == 0) {
+            if (oc.src == p.keyInput) {
+                StoreKey(oc.values, pos, oc.width, key);
+            } else {
+                CopyValueRO(oc.values, pos, b.cols[oc.src], row, oc.width);
+                if (oc.nulls != nullptr && RowIsNullRO(b.nulls[oc.src], row)) {
+                    SetBit(oc.nulls, pos);
+                }
+            }
+        } else {
+            StoreKey(oc.values, pos, oc.width, static_cast<int64_t>(payload >> oc.shift));
+        }
+    }
+}
+
+// Packs the build output values of every unique-table slot (<= 8 bytes in total).
+__global__ void BuildSlotPayloadKernel(const int64_t *entries, uint64_t nSlots, int64_t sentinelEntry,
+    const __grid_constant__ ProbeLaunch p, uint64_t *payload)
+{
+    for (uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s <= nSlots;
+         s += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const int64_t row = s < nSlots ? entries[s] : sentinelEntry;
+        uint64_t v = 0;
+        if (row >= 0) {
+            for (int o = 0; o < p.nOut; ++o) {
+                const JoinOutCol &oc = p.out[o];
+                if (oc.side == 1) {
+                    const uint64_t bits = LoadBits(oc.buildValues, row, oc.width);
+                    const uint64_t mask = oc.width >= 8 ? ~0ull : ((1ull << (8 * oc.width)) - 1);
+                    v |= (bits & mask) << oc.shift;
+                }
+            }
+        }
+        payload[s] = v;
+    }
+}
+
 // Each warp owns kWarpRounds * 32 consecutive rows of a tile and works on its own: lane i reads
 // rows base + 32r + i (coalesced), looks the keys up, reserves its output range with one
 // atomicAdd, and writes its matches compacted in row order.  kUnique: every key has at most one
@@ -444,7 +491,7 @@ __device__ __forceinline__ void WriteJoinRow(const ProbeLaunch &p, const BatchDe
 constexpr int kWarpRounds = 16;
 constexpr int kRowsPerWarp = kWarpRounds * 32;
 
-template <bool kUnique>
+template <bool kUnique, bool kPayload>
 __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_constant__ ProbeLaunch p)
 {
     const int lane = threadIdx.x & 31;
@@ -479,14 +526,19 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
         // Phase 2: table lookups (independent of each other).
         int32_t entry[kWarpRounds];
         uint32_t cnt[kWarpRounds];
+        uint64_t payload[kWarpRounds];  // kPayload: the build output values of the match
         uint32_t hit = 0;
         if (arrayMode) {
 #pragma unroll
             for (int i = 0; i < kWarpRounds; ++i) {
                 const uint64_t d = static_cast<uint64_t>(key[i]) - static_cast<uint64_t>(p.table.minKey);
                 int64_t e = -1;
+                payload[i] = 0;
                 if (((live >> i) & 1u) && key[i] >= p.table.minKey && d < p.table.range) {
                     e = __ldg(reinterpret_cast<const long long *>(p.table.arrayEntries) + d);
+                    if (kPayload) {
+                        payload[i] = __ldg(reinterpret_cast<const unsigned long long *>(p.table.slotPayload) + d);
+                    }
                 }
                 entry[i] = kUnique ? static_cast<int32_t>(e) : static_cast<int32_t>(e >> 32);
                 cnt[i] = e < 0 ? 0u : (kUnique ? 1u : static_cast<uint32_t>(e & 0xffffffffll));
@@ -495,9 +547,13 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
         } else {
 #pragma unroll
             for (int i = 0; i < kWarpRounds; ++i) {
-                Match m{0, 0};
+                Match m{0, 0, 0};
+                payload[i] = 0;
                 if ((live >> i) & 1u) {
                     m = Lookup(p.table, static_cast<uint64_t>(key[i]));
+                    if (kPayload && m.count != 0) {
+                        payload[i] = __ldg(reinterpret_cast<const unsigned long long *>(p.table.slotPayload) + m.slot);
+                    }
                 }
                 entry[i] = static_cast<int32_t>(m.entry);
                 cnt[i] = m.count;
@@ -535,7 +591,11 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
                     const uint64_t at = pos + __popc(m & lanesBelow);
                     if (at < p.outCapacity) {
                         // The key is re-read (an L1/L2 hit) rather than kept live in registers.
-                        WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), entry[i], at);
+                        if (kPayload) {
+                            WriteJoinRowPayload(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), payload[i], at);
+                        } else {
+                            WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), entry[i], at);
+                        }
                     }
                 }
                 pos += __popc(m);
@@ -632,22 +692,27 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     if (p.nTiles <= 0) {
         return cudaSuccess;
     }
-    int blocksPerSM = 0;
-    if (p.table.unique) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM, ProbeKernel<true>, kProbeThreads, 0);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM, ProbeKernel<false>, kProbeThreads, 0);
+    auto kernel = !p.table.unique ? ProbeKernel<false, false>
+                                  : (p.table.slotPayload != nullptr ? ProbeKernel<true, true> : ProbeKernel<true, false>);
+    static int blocksPerSM[3] = {0, 0, 0};
+    const int which = !p.table.unique ? 0 : (p.table.slotPayload != nullptr ? 2 : 1);
+    if (blocksPerSM[which] <= 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM[which], kernel, kProbeThreads, 0);
+        if (blocksPerSM[which] <= 0) {
+            blocksPerSM[which] = 1;
+        }
     }
-    if (blocksPerSM <= 0) {
-        blocksPerSM = 1;
-    }
-    const int maxGrid = SMs() * blocksPerSM;
+    const int maxGrid = SMs() * blocksPerSM[which];
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
-    if (p.table.unique) {
-        ProbeKernel<true><<<grid, kProbeThreads, 0, stream>>>(p);
-    } else {
-        ProbeKernel<false><<<grid, kProbeThreads, 0, stream>>>(p);
-    }
+    kernel<<<grid, kProbeThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchBuildSlotPayload(const ProbeLaunch &p, uint64_t nSlots, uint64_t *payload, cudaStream_t stream)
+{
+    const int64_t n = static_cast<int64_t>(nSlots) + 1;
+    const int64_t *entries = p.table.mode == JOIN_ARRAY ? p.table.arrayEntries : p.table.hashEntries;
+    BuildSlotPayloadKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(entries, nSlots, p.table.sentinelEntry, p, payload);
     return cudaGetLastError();
 }
 

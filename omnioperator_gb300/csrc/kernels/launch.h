@@ -45,6 +45,9 @@ cudaError_t LaunchBuildFill(JoinTable t, const void *keys, const uint8_t *nulls,
     int32_t *csrRowsMutable, uint32_t sentinelCount, int64_t sentinelOffset, unsigned int *sentinelCursor,
     int64_t *sentinelEntryOut, int32_t *error, cudaStream_t stream);
 cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream);
+// Packs the build output columns named by p.out (side 1, with shifts set) per table slot into
+// payload[nSlots + 1] (the last slot holds the EMPTY-key row of a HASH table).
+cudaError_t LaunchBuildSlotPayload(const ProbeLaunch &p, uint64_t nSlots, uint64_t *payload, cudaStream_t stream);
 cudaError_t LaunchFillI64(int64_t *p, int64_t v, int64_t n, cudaStream_t stream);
 cudaError_t LaunchFillU64(uint64_t *p, uint64_t v, int64_t n, cudaStream_t stream);
 

@@ -220,13 +220,17 @@ struct JoinTable {
     const int32_t *csrRows;        // build rows grouped by key
     int32_t keyWidth;              // probe key width in bytes
     int32_t pad;
+    // Unique tables whose build output values fit in 8 bytes and hold no NULLs: those values
+    // packed per table slot (ARRAY: key - minKey; HASH: slot; the EMPTY-key row at `capacity`),
+    // so the probe fetches them with the entry instead of gathering by build row afterwards.
+    const uint64_t *slotPayload;
 };
 
 struct JoinOutCol {
     int16_t side;    // 0 = probe column, 1 = build column
     int16_t src;     // probe kernel input index / build column index
     int16_t width;   // bytes
-    int16_t pad;
+    int16_t shift;   // side 1 with a slot payload: bit offset of the value in the packed payload
     const void *buildValues;     // side 1: contiguous build column in HBM
     const uint8_t *buildNulls;   // side 1: contiguous build null bitmap (nullptr = no nulls)
     void *values;                // output column

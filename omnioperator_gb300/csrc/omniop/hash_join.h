@@ -74,6 +74,10 @@ public:
     type::DataTypes buildOutputTypes;
     JoinBuildState *build;
     int32_t rowsPerBatch;
+    // Build output values packed per table slot, built by the first probe that can use it.
+    mutable std::mutex payloadMu;
+    mutable omg::BufferPtr slotPayload;
+    mutable bool payloadDecided = false;
 };
 
 class LookupJoinOperator : public Operator {
