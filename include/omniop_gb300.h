@@ -216,6 +216,30 @@ int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hin
  * [3]=groups, [4]=ordered-fallback groups, [5]=output rows. */
 int32_t omg_op_get_counters(void *op, int64_t *out, int32_t n);
 
+/* ---- allocation-free aggregation (no counterpart in the reference) ----------------------
+ * Runs the aggregation compiled by a hash aggregation factory over one batch of
+ * device-resident columns without allocating any memory, device or host.  For callers that
+ * cannot let this library allocate: a host engine that accounts for every byte of device
+ * memory in its own pre-reserved pool, or code running where allocation calls are not allowed.
+ * The group table and launch descriptors live in a fixed 64 MiB device array inside the
+ * library (held by every GPU that loads it, until the process exits); a call is rejected with
+ * OMG_ERR_INVALID_ARG when max_groups and n_rows would not fit in it, or when the input turns
+ * out to have more than max_groups groups.
+ *   d_cols[n_cols], d_nulls[n_cols]: device values / null bitmaps by batch column index
+ *     (d_nulls or an entry may be NULL: no nulls); the factory's column indices select from them.
+ *   d_out_values[n_out], d_out_nulls[n_out]: the caller's device output columns (group-by
+ *     columns, then one per aggregate, in the factory's output order) with room for max_groups
+ *     rows; null bitmaps need ((max_groups + 31) / 32) * 4 bytes and are cleared by the call.
+ *   *num_groups receives the number of rows written.  The call synchronises `stream`.
+ * The first call on a device looks up the device address of the array for that device; make
+ * that first call before any stream capture.  Every call shares the array, so calls that overlap
+ * on the GPU (e.g. issued concurrently on two streams) race on it and must be serialised by the
+ * caller.  Order-dependent sticky overflows (generic-policy int64 SUM, decimal128 SUM) that
+ * would need the operator's ordered replay return OMG_ERR_UNSUPPORTED. */
+int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const uint8_t *const *d_nulls,
+    int32_t n_cols, int64_t n_rows, void *const *d_out_values, uint8_t *const *d_out_nulls, int32_t n_out,
+    int64_t max_groups, int64_t *num_groups, void *stream);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -69,6 +69,7 @@ _SIGS = {
     "omg_op_set_device_output": (I32, [P, I32]),
     "omg_op_set_agg_strategy": (I32, [P, I32, I64]),
     "omg_op_get_counters": (I32, [P, C.POINTER(I64), I32]),
+    "omg_hashagg_run_noalloc": (I32, [P, P, P, I32, I64, P, P, I32, I64, C.POINTER(I64), P]),
 }
 
 _lib = None

@@ -4,10 +4,12 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <string>
 #include <vector>
 
 #include "host/gpu_runtime.h"
+#include "kernels/agg_noalloc.h"
 #include "omniop/hash_aggregation.h"
 #include "omniop/hash_join.h"
 #include "omniop/memory.h"
@@ -30,14 +32,18 @@ using omniruntime::vec::VectorBatch;
 using omniruntime::vec::VectorHelper;
 
 namespace {
-thread_local std::string g_error;
+// Per-thread message of the last failing call, in a fixed buffer so that reporting an error
+// never allocates.
+thread_local char g_error[512];
 
-void SetError(const std::string &m) { g_error = m; }
+void ClearError() { g_error[0] = '\0'; }
+void SetError(const char *m) { std::snprintf(g_error, sizeof(g_error), "%s", m); }
+void SetError(const std::string &m) { SetError(m.c_str()); }
 
 template <typename F> int32_t Guard(F &&f)
 {
     try {
-        g_error.clear();
+        ClearError();
         f();
         return OMG_OK;
     } catch (const OmniException &e) {
@@ -85,7 +91,7 @@ Operator *AsOp(void *op)
 
 extern "C" {
 
-const char *omg_last_error(void) { return g_error.c_str(); }
+const char *omg_last_error(void) { return g_error; }
 
 const char *omg_version(void) { return "omniop-gb300 0.1 (sm_103a)"; }
 
@@ -423,6 +429,53 @@ int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hin
         Require(strategy >= OMG_AGG_STRATEGY_AUTO && strategy <= OMG_AGG_STRATEGY_GLOBAL, "unknown strategy");
         a->SetStrategy(strategy, capacity_hint);
     });
+}
+
+int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const uint8_t *const *d_nulls,
+    int32_t n_cols, int64_t n_rows, void *const *d_out_values, uint8_t *const *d_out_nulls, int32_t n_out,
+    int64_t max_groups, int64_t *num_groups, void *stream)
+{
+    ClearError();
+    auto *f = dynamic_cast<HashAggregationOperatorFactory *>(static_cast<OperatorFactory *>(factory));
+    if (f == nullptr) {
+        SetError("not a hash aggregation factory");
+        return OMG_ERR_INVALID_ARG;
+    }
+    if (!omg::DeviceAvailable()) {
+        SetError("no CUDA device is available");
+        return OMG_ERR_NO_DEVICE;
+    }
+    const auto &ap = f->Plan();
+    omg::NoAllocPlan np;
+    np.nInputs = static_cast<int32_t>(ap.inputCols.size());
+    for (int32_t i = 0; i < np.nInputs; ++i) {
+        np.inputCols[i] = ap.inputCols[i];
+    }
+    np.key = ap.key;
+    np.nAccs = static_cast<int32_t>(ap.accs.size());
+    for (int32_t i = 0; i < np.nAccs; ++i) {
+        np.accs[i] = ap.accs[i];
+    }
+    np.nRegInputs = static_cast<int32_t>(ap.regInput.size());
+    for (int32_t i = 0; i < np.nRegInputs; ++i) {
+        np.regInput[i] = ap.regInput[i];
+        np.regWidth[i] = ap.regWidth[i];
+    }
+    np.stateWords = ap.stateWords;
+    np.keyWords = ap.keyWords;
+    np.slotWords = ap.slotWords;
+    np.nOut = static_cast<int32_t>(ap.outs.size());
+    for (int32_t i = 0; i < np.nOut; ++i) {
+        np.outs[i] = ap.outs[i];
+    }
+    np.overflowAsNull = ap.overflowAsNull;
+    np.smemSlots = ap.smemSlots;
+    const omg::NoAllocStatus st = omg::RunAggNoAlloc(np, d_cols, d_nulls, n_cols, n_rows, d_out_values, d_out_nulls,
+        n_out, max_groups, num_groups, static_cast<cudaStream_t>(stream));
+    if (st.code != 0) {
+        SetError(st.message);
+    }
+    return st.code;
 }
 
 int32_t omg_op_get_counters(void *op, int64_t *out, int32_t n)

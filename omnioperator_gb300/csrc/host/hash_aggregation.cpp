@@ -383,6 +383,7 @@ OmniStatus HashAggregationOperatorFactory::Init()
     }
     p.stateWords = word;
     p.slotWords = p.keyWords + p.stateWords;
+    p.smemSlots = static_cast<int32_t>(kSmemBudget / (p.slotWords * sizeof(uint64_t)));
     p.rowsPerBatch = GetMaxRowCount(rowBytes);
     inited_ = true;
     return OMNI_STATUS_NORMAL;
@@ -528,7 +529,7 @@ void HashAggregationOperator::Flush()
     const int sms = omg::DeviceSMCount();
     int smemSlots = 0;
     if (strategy_ != 2) {  // OMG_AGG_STRATEGY_GLOBAL
-        smemSlots = static_cast<int>(kSmemBudget / (plan_.slotWords * sizeof(uint64_t)));
+        smemSlots = plan_.smemSlots;
     }
     const int grid = 0;  // the launcher fills every SM to its occupancy limit
     const int maxGrid = sms * 4;

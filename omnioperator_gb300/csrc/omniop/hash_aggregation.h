@@ -39,6 +39,7 @@ struct AggPlan {
     std::vector<omg::OutSpec> outs;        // pointers filled at extraction
     std::vector<type::DataTypePtr> outTypes;
     int32_t rowsPerBatch = 0;
+    int32_t smemSlots = 0;                 // per-CTA shared pre-aggregation slots
     bool overflowAsNull = false;
     bool orderDependent = false;           // has an OUT_SUM_EXACT column (sticky overflow)
 };
