@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <mutex>
 
 namespace omg {
 
@@ -88,6 +89,29 @@ size_t NullBitmapBytes(int64_t rows) { return static_cast<size_t>(((rows + 31) /
 
 namespace {
 std::atomic<long long> g_waitBudget{0};
+std::mutex g_poolMu;
+std::vector<cudaStream_t> *g_streamPool = new std::vector<cudaStream_t>();  // never freed, like its streams
+}
+
+cudaStream_t AcquirePooledStream()
+{
+    {
+        std::lock_guard<std::mutex> g(g_poolMu);
+        if (!g_streamPool->empty()) {
+            cudaStream_t s = g_streamPool->back();
+            g_streamPool->pop_back();
+            return s;
+        }
+    }
+    cudaStream_t s = nullptr;
+    CudaCheck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+    return s;
+}
+
+void ReleasePooledStream(cudaStream_t s)
+{
+    std::lock_guard<std::mutex> g(g_poolMu);
+    g_streamPool->push_back(s);
 }
 long long WaitBudget()
 {

@@ -32,7 +32,14 @@ inline void RequireDevice()
     }
 }
 
-// The stream an operator issues its work on: the caller's, or one it owns.
+// Operator-owned streams come from a process-wide pool and are never destroyed: device buffers
+// are freed stream-ordered on the stream they were allocated on, and such a buffer (an output
+// batch, a factory's packed payload) may outlive the operator that allocated it.
+cudaStream_t AcquirePooledStream();
+void ReleasePooledStream(cudaStream_t s);
+
+// The stream an operator issues its work on: the caller's (which must stay valid while any
+// device batch the operator produced is alive), or one from the pool.
 class OpStream {
 public:
     OpStream() = default;
@@ -40,20 +47,26 @@ public:
     {
         if (own_ != nullptr) {
             cudaStreamSynchronize(own_);
-            cudaStreamDestroy(own_);
+            ReleasePooledStream(own_);
         }
     }
     OpStream(const OpStream &) = delete;
     OpStream &operator=(const OpStream &) = delete;
-    void SetUser(void *s) { user_ = static_cast<cudaStream_t>(s); }
+    // Set the caller's stream; a previous call's stream counts as "unset" only via ClearUser.
+    void SetUser(void *s)
+    {
+        user_ = static_cast<cudaStream_t>(s);
+        userSet_ = true;
+    }
+    void ClearUser() { userSet_ = false; }
     cudaStream_t Get()
     {
-        if (user_ != nullptr) {
+        if (userSet_) {
             return user_;
         }
         if (own_ == nullptr) {
             RequireDevice();
-            CudaCheck(cudaStreamCreateWithFlags(&own_, cudaStreamNonBlocking), "cudaStreamCreate");
+            own_ = AcquirePooledStream();
         }
         return own_;
     }
@@ -61,6 +74,7 @@ public:
 
 private:
     cudaStream_t user_ = nullptr;
+    bool userSet_ = false;
     cudaStream_t own_ = nullptr;
 };
 

@@ -505,7 +505,9 @@ void HashAggregationOperator::Flush()
     }
     omg::RequireDevice();
     Impl &im = *impl_;
-    im.stream.SetUser(userStream_);
+    if (userStreamSet_) {
+        im.stream.SetUser(userStream_);
+    }
     cudaStream_t s = im.stream.Get();
     if (im.stats.Get() == nullptr) {
         im.stats.Reset(8, s, true);
@@ -528,7 +530,9 @@ void HashAggregationOperator::Flush()
 
     const int sms = omg::DeviceSMCount();
     int smemSlots = 0;
-    if (strategy_ != 2) {  // OMG_AGG_STRATEGY_GLOBAL
+    // AUTO (0) and GLOBAL (2): global table only.  The per-CTA shared table pays off only when
+    // a few groups take most rows (skew), which the sizing model detects and asks for (SMEM, 1).
+    if (strategy_ == 1) {  // OMG_AGG_STRATEGY_SMEM
         smemSlots = plan_.smemSlots;
     }
     const int grid = 0;  // the launcher fills every SM to its occupancy limit
@@ -642,7 +646,9 @@ void HashAggregationOperator::Extract()
         uniqueKeys_ = 0;
         return;
     }
-    im.stream.SetUser(userStream_);
+    if (userStreamSet_) {
+        im.stream.SetUser(userStream_);
+    }
     cudaStream_t s = im.stream.Get();
     omg::AggLaunch base = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
     DevArray<unsigned long long> cnt(4, s, true);

@@ -295,7 +295,9 @@ int32_t HashBuilderOperator::GetOutput(VectorBatch **outputVecBatch)
     // The single GPU table is built once every builder of the factory has finished (the
     // reference builds one partition per builder and unblocks probes when all are built).
     if (!state_->built && state_->finished >= state_->operatorCount) {
-        state_->stream.SetUser(userStream_);
+        if (userStreamSet_) {
+            state_->stream.SetUser(userStream_);
+        }
         state_->Build();
     }
     SetStatus(OMNI_STATUS_FINISHED);
@@ -415,7 +417,9 @@ void LookupJoinOperator::ProcessPending()
 {
     JoinBuildState &b = *f_.build;
     omg::RequireDevice();
-    impl_->stream.SetUser(userStream_);
+    if (userStreamSet_) {
+        impl_->stream.SetUser(userStream_);
+    }
     cudaStream_t s = impl_->stream.Get();
     // Kernel inputs: probe key first, then the probe output columns.
     std::vector<int32_t> inputCols{f_.probeHashCols[0]};

@@ -47,13 +47,19 @@ public:
     bool isFinished() const { return status_ == OMNI_STATUS_FINISHED; }
 
     // GB300 controls.
-    void SetStream(void *stream) { userStream_ = stream; }
+    // Run on the caller's stream (the legacy default stream when `stream` is null).
+    void SetStream(void *stream)
+    {
+        userStream_ = stream;
+        userStreamSet_ = true;
+    }
     void SetDeviceOutput(bool on) { deviceOutput_ = on; }
     const std::vector<int64_t> &Counters() const { return counters_; }
 
 protected:
     bool noMoreInput_ = true;
     void *userStream_ = nullptr;
+    bool userStreamSet_ = false;
     bool deviceOutput_ = false;
     std::vector<int64_t> counters_ = std::vector<int64_t>(8, 0);
 
