@@ -622,6 +622,121 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
     }
 }
 
+// Specialised probe for the common shape: 8-byte key, unique build with a slot payload, and up
+// to kFastMaxOut output columns that are each either the probe key or a field of the payload.
+// Column metadata lives in registers and no width is dispatched at run time per row.
+constexpr int kFastMaxOut = 4;
+
+template <int kNumOut>
+__global__ void __launch_bounds__(kProbeThreads, 3) ProbeFastKernel(const __grid_constant__ ProbeLaunch p)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const unsigned int lanesBelow = (1u << lane) - 1u;
+    const bool arrayMode = p.table.mode == JOIN_ARRAY;
+    const unsigned long long *payloadTab = reinterpret_cast<const unsigned long long *>(p.table.slotPayload);
+    void *vals[kNumOut];
+    int width[kNumOut];
+    int shift[kNumOut];
+    bool isKey[kNumOut];
+#pragma unroll
+    for (int o = 0; o < kNumOut; ++o) {
+        vals[o] = p.out[o].values;
+        width[o] = p.out[o].width;
+        shift[o] = p.out[o].shift;
+        isKey[o] = p.out[o].side == 0;
+    }
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const int w0 = warp * kRowsPerWarp;
+        if (w0 >= tile.rows) {
+            continue;
+        }
+        const BatchDesc &b = p.batches[tile.batch];
+        const long long *keyCol = static_cast<const long long *>(b.cols[p.keyInput]);
+        const uint8_t *keyNulls = b.nulls[p.keyInput];
+        const int64_t base = static_cast<int64_t>(tile.row0) + w0;
+        const int nRows = min(kRowsPerWarp, tile.rows - w0);
+        int64_t key[kWarpRounds];
+        uint32_t live = 0;
+#pragma unroll
+        for (int i = 0; i < kWarpRounds; ++i) {
+            const int r = i * 32 + lane;
+            key[i] = 0;
+            if (r < nRows) {
+                key[i] = __ldg(keyCol + base + r);
+                if (!RowIsNullRO(keyNulls, base + r)) {
+                    live |= 1u << i;
+                }
+            }
+        }
+        uint64_t payload[kWarpRounds];
+        uint32_t hit = 0;
+        if (arrayMode) {
+#pragma unroll
+            for (int i = 0; i < kWarpRounds; ++i) {
+                const uint64_t d = static_cast<uint64_t>(key[i]) - static_cast<uint64_t>(p.table.minKey);
+                payload[i] = 0;
+                if (((live >> i) & 1u) && key[i] >= p.table.minKey && d < p.table.range) {
+                    const long long e = __ldg(reinterpret_cast<const long long *>(p.table.arrayEntries) + d);
+                    payload[i] = __ldg(payloadTab + d);
+                    hit |= (e >= 0 ? 1u : 0u) << i;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < kWarpRounds; ++i) {
+                payload[i] = 0;
+                if ((live >> i) & 1u) {
+                    const Match m = Lookup(p.table, static_cast<uint64_t>(key[i]));
+                    if (m.count != 0) {
+                        payload[i] = __ldg(payloadTab + m.slot);
+                        hit |= 1u << i;
+                    }
+                }
+            }
+        }
+        uint32_t total = 0;
+#pragma unroll
+        for (int i = 0; i < kWarpRounds; ++i) {
+            total += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
+        }
+        unsigned long long pos = 0;
+        if (lane == 0 && total != 0) {
+            pos = atomicAdd(p.outCount, static_cast<unsigned long long>(total));
+        }
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (p.countOnly || total == 0) {
+            continue;
+        }
+#pragma unroll
+        for (int i = 0; i < kWarpRounds; ++i) {
+            const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
+            if ((hit >> i) & 1u) {
+                const uint64_t at = pos + __popc(m & lanesBelow);
+                if (at < p.outCapacity) {
+                    // Re-read the key (an L1 hit) rather than keeping 16 keys live in registers.
+                    const int64_t kv = __ldg(keyCol + base + i * 32 + lane);
+#pragma unroll
+                    for (int o = 0; o < kNumOut; ++o) {
+                        const int64_t v = isKey[o] ? kv : static_cast<int64_t>(payload[i] >> shift[o]);
+                        if (width[o] == 8) {
+                            static_cast<int64_t *>(vals[o])[at] = v;
+                        } else if (width[o] == 4) {
+                            static_cast<int32_t *>(vals[o])[at] = static_cast<int32_t>(v);
+                        } else if (width[o] == 2) {
+                            static_cast<int16_t *>(vals[o])[at] = static_cast<int16_t>(v);
+                        } else {
+                            static_cast<int8_t *>(vals[o])[at] = static_cast<int8_t>(v);
+                        }
+                    }
+                }
+            }
+            pos += __popc(m);
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t LaunchGatherColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
@@ -692,10 +807,25 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     if (p.nTiles <= 0) {
         return cudaSuccess;
     }
+    // Fast path: 8-byte key, unique build with slot payload, outputs = probe key / payload fields.
+    bool fast = p.table.unique && p.table.slotPayload != nullptr && p.keyWidth == 8 && p.nOut >= 1 &&
+        p.nOut <= kFastMaxOut;
+    for (int o = 0; fast && o < p.nOut; ++o) {
+        const JoinOutCol &oc = p.out[o];
+        fast = (oc.side == 1 || (oc.side == 0 && oc.src == p.keyInput && oc.width == 8)) &&
+            (oc.width == 1 || oc.width == 2 || oc.width == 4 || oc.width == 8);
+    }
     auto kernel = !p.table.unique ? ProbeKernel<false, false>
                                   : (p.table.slotPayload != nullptr ? ProbeKernel<true, true> : ProbeKernel<true, false>);
-    static int blocksPerSM[3] = {0, 0, 0};
-    const int which = !p.table.unique ? 0 : (p.table.slotPayload != nullptr ? 2 : 1);
+    int which = !p.table.unique ? 0 : (p.table.slotPayload != nullptr ? 2 : 1);
+    if (fast) {
+        const void *fk[kFastMaxOut] = {reinterpret_cast<const void *>(ProbeFastKernel<1>),
+            reinterpret_cast<const void *>(ProbeFastKernel<2>), reinterpret_cast<const void *>(ProbeFastKernel<3>),
+            reinterpret_cast<const void *>(ProbeFastKernel<4>)};
+        kernel = reinterpret_cast<decltype(kernel)>(fk[p.nOut - 1]);
+        which = 2 + p.nOut;
+    }
+    static int blocksPerSM[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (blocksPerSM[which] <= 0) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM[which], kernel, kProbeThreads, 0);
         if (blocksPerSM[which] <= 0) {
