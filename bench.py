@@ -281,10 +281,8 @@ def run_gpu(args, rank, world):
 
     def probe_step():
         pop.add_input(omg.wrap_device_batch([L], N_PROBE, [pkey.data_ptr()], [pbits.data_ptr()]))
-        rows = 0
-        for b in pop.drain():
-            rows += omg.batch_row_count(b)
-            omg.free_batch(b)
+        outs, rows = pop.get_outputs(1 << 16)  # GetOutput until drained, one C call
+        omg.free_batches(outs)
         return rows
 
     for _ in range(args.warmup):
@@ -340,24 +338,23 @@ def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
     expected = int((~pnull & (pkey < N_BUILD)).sum())
 
     def make_batches():
-        return [omg.make_batch([L], [pkey[s:s + BATCH]], [pnull[s:s + BATCH]]) for s in range(0, N_PROBE, BATCH)]
+        """Host batches of 4096 rows, grouped 1024 to a C array (one AddInput call chain each)."""
+        hs = [omg.make_batch([L], [pkey[s:s + BATCH]], [pnull[s:s + BATCH]]) for s in range(0, N_PROBE, BATCH)]
+        return [(C.c_void_p * len(hs[i:i + 1024]))(*hs[i:i + 1024]) for i in range(0, len(hs), 1024)]
 
-    def step(batches):
+    def step(chunks):
         op = pf.create_operator()
         op.set_no_more_input(False)
-        rows = out_bytes = 0
-        for b in batches:
-            op.add_input(b)
-            while True:
-                _, o = op.get_output()
-                if not o:
-                    break
-                rows += omg.batch_row_count(o)
-                omg.free_batch(o)
+        rows = 0
+        for chunk in chunks:
+            op.add_inputs(chunk)  # AddInput per batch, in C
+            outs, n = op.get_outputs(1 << 16)
+            rows += n
+            omg.free_batches(outs)
         op.no_more_input()
-        for o in op.drain():
-            rows += omg.batch_row_count(o)
-            omg.free_batch(o)
+        outs, n = op.get_outputs(1 << 16)
+        rows += n
+        omg.free_batches(outs)
         op.delete()
         return rows
 

@@ -191,6 +191,17 @@ int32_t omg_op_add_input(void *op, void *batch, int32_t *ret);
 /* Operator::GetOutput (operator.h:38).  `*out_batch` is NULL or a new batch owned by the
  * caller; `*ret` is the reference's return value (agg: 1 if a batch was produced). */
 int32_t omg_op_get_output(void *op, void **out_batch, int32_t *ret);
+/* Bulk forms with no reference counterpart (a native caller makes the per-batch calls above;
+ * these exist so that a caller behind a slow FFI, such as ctypes, pays one crossing for many
+ * batches).  omg_op_add_inputs is n calls of Operator::AddInput in order: it stops at the
+ * first error, and `*consumed` receives how many batches the operator took (the failing batch
+ * counts as taken, as AddInput frees it; later batches stay with the caller).
+ * omg_op_get_outputs calls Operator::GetOutput until it yields no batch or `max` batches were
+ * returned; `*n` receives the count and `*rows` (may be NULL) their total row count. */
+int32_t omg_op_add_inputs(void *op, void *const *batches, int32_t n, int32_t *consumed);
+int32_t omg_op_get_outputs(void *op, void **out_batches, int32_t max, int32_t *n, int64_t *rows);
+/* Frees n batches (VectorHelper::FreeVecBatch each); NULL entries are skipped. */
+int32_t omg_batch_free_many(void *const *batches, int32_t n);
 /* Operator::GetStatus (operator.h:46-49): OMG_STATUS_*. */
 int32_t omg_op_status(void *op);
 /* Operator::noMoreInput / setNoMoreInput / needsInput (operator.h:117-130). */

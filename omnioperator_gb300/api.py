@@ -176,6 +176,14 @@ def batch_row_count(batch: int) -> int:
     return lib().omg_batch_row_count(batch)
 
 
+def free_batches(batches) -> None:
+    """Free many batches with one call (omg_batch_free_many)."""
+    n = len(batches)
+    if n:
+        arr = (C.c_void_p * n)(*batches)
+        check(lib().omg_batch_free_many(arr, n))
+
+
 def batch_to_numpy(batch: int):
     """[(values, null_mask)] of a host batch (copies)."""
     L = lib()
@@ -226,6 +234,22 @@ class Operator:
         ret = C.c_int32(0)
         check(lib().omg_op_get_output(self.handle, C.byref(out), C.byref(ret)))
         return ret.value, out.value
+
+    def add_inputs(self, batches) -> None:
+        """AddInput of each batch in order, one C call (omg_op_add_inputs).  `batches` is a
+        sequence of handles or a prepared ctypes array of c_void_p."""
+        arr = batches if isinstance(batches, C.Array) else (C.c_void_p * len(batches))(*batches)
+        consumed = C.c_int32(0)
+        check(lib().omg_op_add_inputs(self.handle, arr, len(arr), C.byref(consumed)))
+
+    def get_outputs(self, max_batches: int = 4096):
+        """GetOutput until no batch is produced or `max_batches` were returned, one C call
+        (omg_op_get_outputs) -> (list of batch handles, total rows)."""
+        arr = (C.c_void_p * max_batches)()
+        n = C.c_int32(0)
+        rows = C.c_int64(0)
+        check(lib().omg_op_get_outputs(self.handle, arr, max_batches, C.byref(n), C.byref(rows)))
+        return list(arr[: n.value]), rows.value
 
     def get_status(self) -> int:
         return lib().omg_op_status(self.handle)

@@ -370,6 +370,61 @@ int32_t omg_op_get_output(void *op, void **out_batch, int32_t *ret)
     });
 }
 
+int32_t omg_op_add_inputs(void *op, void *const *batches, int32_t n, int32_t *consumed)
+{
+    if (consumed != nullptr) {
+        *consumed = 0;
+    }
+    return Guard([&] {
+        Operator *o = AsOp(op);
+        Require(n >= 0 && (n == 0 || batches != nullptr), "null batch array");
+        for (int32_t i = 0; i < n; ++i) {
+            Require(batches[i] != nullptr, "null batch");
+            if (consumed != nullptr) {
+                *consumed = i + 1;  // AddInput owns the batch from here on, also when it throws
+            }
+            o->AddInput(static_cast<VectorBatch *>(batches[i]));
+        }
+    });
+}
+
+int32_t omg_op_get_outputs(void *op, void **out_batches, int32_t max, int32_t *n, int64_t *rows)
+{
+    if (n != nullptr) {
+        *n = 0;
+    }
+    if (rows != nullptr) {
+        *rows = 0;
+    }
+    return Guard([&] {
+        Operator *o = AsOp(op);
+        Require(n != nullptr && max >= 0 && (max == 0 || out_batches != nullptr), "null output array");
+        while (*n < max) {
+            VectorBatch *b = nullptr;
+            o->GetOutput(&b);
+            if (b == nullptr) {
+                break;
+            }
+            out_batches[(*n)++] = b;
+            if (rows != nullptr) {
+                *rows += b->GetRowCount();
+            }
+        }
+    });
+}
+
+int32_t omg_batch_free_many(void *const *batches, int32_t n)
+{
+    return Guard([&] {
+        Require(n >= 0 && (n == 0 || batches != nullptr), "null batch array");
+        for (int32_t i = 0; i < n; ++i) {
+            if (batches[i] != nullptr) {
+                VectorHelper::FreeVecBatch(static_cast<VectorBatch *>(batches[i]));
+            }
+        }
+    });
+}
+
 int32_t omg_op_status(void *op) { return op ? static_cast<int32_t>(static_cast<Operator *>(op)->GetStatus()) : -1; }
 
 int32_t omg_op_no_more_input(void *op)

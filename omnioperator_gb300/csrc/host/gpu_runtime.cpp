@@ -85,6 +85,16 @@ void BatchTable::Upload(cudaStream_t s)
     }
 }
 
+std::vector<int64_t> BatchTable::RegionRows(int32_t nRegions) const
+{
+    std::vector<int64_t> rows(static_cast<size_t>(nRegions > 0 ? nRegions : 1), 0);
+    const TileDesc *t = tiles_.Get();
+    for (size_t i = 0; i < tiles_.Size(); ++i) {
+        rows[i % rows.size()] += t[i].rows;
+    }
+    return rows;
+}
+
 size_t NullBitmapBytes(int64_t rows) { return static_cast<size_t>(((rows + 31) / 32) * 4 + 8); }
 
 namespace {
@@ -120,7 +130,8 @@ long long WaitBudget()
 }
 void SetWaitBudget(long long ticks) { g_waitBudget.store(ticks); }
 
-std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows, int32_t rowsPerBatch)
+std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows, int32_t rowsPerBatch,
+    int64_t firstRow)
 {
     std::vector<VectorBatch *> out;
     if (rows <= 0) {
@@ -131,8 +142,8 @@ std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int6
         const int32_t n = static_cast<int32_t>(std::min<int64_t>(step, rows - r0));
         auto *b = new VectorBatch(n);
         for (const auto &c : cols) {
-            const size_t vOff = static_cast<size_t>(r0) * c.width;
-            const size_t nOff = static_cast<size_t>(r0 / 8);
+            const size_t vOff = static_cast<size_t>(firstRow + r0) * c.width;
+            const size_t nOff = static_cast<size_t>((firstRow + r0) / 8);
             b->Append(new BaseVector(c.type, c.width, n, c.values, vOff, c.nulls, nOff, c.hasNull));
         }
         out.push_back(b);
@@ -140,7 +151,8 @@ std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int6
     return out;
 }
 
-std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int64_t rows, cudaStream_t s)
+std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int64_t rows, cudaStream_t s,
+    int64_t firstRow)
 {
     std::vector<OutColumn> host;
     for (const auto &c : cols) {
@@ -148,13 +160,16 @@ std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int
         const size_t vb = static_cast<size_t>(rows) * c.width;
         h.values = Buffer::NewHost(vb == 0 ? 16 : vb, false);
         if (vb > 0) {
-            CudaCheck(cudaMemcpyAsync(h.values->Data(), c.values->Data(), vb, cudaMemcpyDeviceToHost, s),
+            const char *src = static_cast<const char *>(c.values->Data()) + static_cast<size_t>(firstRow) * c.width;
+            CudaCheck(cudaMemcpyAsync(h.values->Data(), src, vb, cudaMemcpyDeviceToHost, s),
                 "copy output values to host");
         }
         const size_t nb = NullBitmapBytes(rows);
         if (c.nulls != nullptr && c.hasNull) {
+            // The source bitmap holds NullBitmapBytes(firstRow + rows) bytes or more.
             h.nulls = Buffer::NewHost(nb, false);
-            CudaCheck(cudaMemcpyAsync(h.nulls->Data(), c.nulls->Data(), nb, cudaMemcpyDeviceToHost, s),
+            const char *src = static_cast<const char *>(c.nulls->Data()) + static_cast<size_t>(firstRow / 8);
+            CudaCheck(cudaMemcpyAsync(h.nulls->Data(), src, nb, cudaMemcpyDeviceToHost, s),
                 "copy output nulls to host");
         } else {
             h.nulls = Buffer::NewHost(nb, true);

@@ -163,6 +163,8 @@ public:
     const TileDesc *DeviceTiles() const { return dTiles_.Get(); }
     const int64_t *DeviceTileOutRows() const { return dTileOut_.Get(); }
     int32_t NumTiles() const { return static_cast<int32_t>(tiles_.Size()); }
+    // Rows of the tiles t with t % nRegions == r, per r.
+    std::vector<int64_t> RegionRows(int32_t nRegions) const;
     int64_t TotalRows() const { return totalRows_; }
     bool AnyNulls(int32_t input) const { return input < static_cast<int32_t>(anyNulls_.size()) && anyNulls_[input]; }
 
@@ -199,10 +201,13 @@ struct OutColumn {
     BufferPtr nulls;  // may be null
     bool hasNull;
 };
+// The rows start at row `firstRow` of the buffers (a multiple of 8).
 std::vector<omniruntime::vec::VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows,
-    int32_t rowsPerBatch);
+    int32_t rowsPerBatch, int64_t firstRow = 0);
 
-// Copy device output columns to new pinned host buffers (one copy per column) on `s`.
-std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int64_t rows, cudaStream_t s);
+// Copy rows [firstRow, firstRow + rows) of device output columns to new pinned host buffers
+// (one copy per column) on `s`; firstRow is a multiple of 8.
+std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int64_t rows, cudaStream_t s,
+    int64_t firstRow = 0);
 
 }  // namespace omg

@@ -487,54 +487,93 @@ void LookupJoinOperator::ProcessPending()
             f_.slotPayload = omg::Buffer::NewDevice((nSlots + 1) * sizeof(uint64_t), s, false);
             CudaCheck(omg::LaunchBuildSlotPayload(p, nSlots, static_cast<uint64_t *>(f_.slotPayload->Data()), s),
                 "build slot payload");
+            if (b.table.mode == omg::JOIN_ARRAY) {
+                f_.slotBits = omg::Buffer::NewDevice(omg::SlotBitsBytes(b.table.range), s, false);
+                CudaCheck(omg::LaunchBuildSlotBits(b.table.arrayEntries, b.table.range,
+                              static_cast<uint32_t *>(f_.slotBits->Data()), s),
+                    "build slot bitmap");
+            }
             impl_->stream.Sync();
             f_.payloadDecided = true;
         }
         if (eligible && f_.slotPayload) {
             p.table.slotPayload = static_cast<const uint64_t *>(f_.slotPayload->Data());
+            p.table.slotBits = f_.slotBits ? static_cast<const uint32_t *>(f_.slotBits->Data()) : nullptr;
         }
     }
-    DevArray<unsigned long long> count(2, s, true);
-    p.outCount = count.Get();
-    uint64_t capacity = static_cast<uint64_t>(std::max<int64_t>(probeRows, 1));
-    if (!b.table.unique) {
-        capacity *= std::min<uint32_t>(b.maxDup, 2);
+    // Output regions: tile t writes into region t % nRegions (see ProbeLaunch).  A region's
+    // capacity starts at its probe rows (times up to 2 for duplicate build keys), rounded to 64
+    // rows so that every region starts on a byte of the null bitmaps.
+    const int32_t nRegions = std::max(1, std::min<int32_t>(omg::kMaxRegions, bt.NumTiles()));
+    const std::vector<int64_t> regionRows = bt.RegionRows(nRegions);
+    uint64_t regionCap = 1;
+    for (int64_t r : regionRows) {
+        regionCap = std::max<uint64_t>(regionCap, static_cast<uint64_t>(r));
     }
-    unsigned long long total = 0;
+    if (!b.table.unique) {
+        regionCap *= std::min<uint32_t>(b.maxDup, 2);
+    }
+    regionCap = (regionCap + 63) / 64 * 64;
+    DevArray<unsigned long long> count(static_cast<size_t>(nRegions) * omg::kRegionStride, s, true);
+    omg::PinnedArray<unsigned long long> hostCount(static_cast<size_t>(nRegions) * omg::kRegionStride);
+    p.outCount = count.Get();
+    p.nRegions = nRegions;
+    p.singleBatch = pending_.size() == 1 ? 1 : 0;
+    std::vector<int64_t> regionCount(nRegions, 0);
     for (int attempt = 0; attempt < 2; ++attempt) {
+        const uint64_t capacity = regionCap * static_cast<uint64_t>(nRegions);
         for (size_t o = 0; o < nOut; ++o) {
             cols[o].values = omg::Buffer::NewDevice(capacity * cols[o].width + 16, s, false);
             cols[o].nulls = cols[o].hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(capacity), s, true) : nullptr;
             p.out[o].values = cols[o].values->Data();
             p.out[o].nulls = cols[o].nulls ? static_cast<uint8_t *>(cols[o].nulls->Data()) : nullptr;
         }
-        p.outCapacity = capacity;
-        CudaCheck(cudaMemsetAsync(count.Get(), 0, sizeof(unsigned long long), s), "reset count");
+        p.regionCap = regionCap;
+        CudaCheck(cudaMemsetAsync(count.Get(), 0, sizeof(unsigned long long) * count.Size(), s), "reset counts");
         impl_->timer.Start(s);
         CudaCheck(omg::LaunchProbe(p, s), "probe kernel");
         impl_->timer.Stop(s);
         ++counters_[0];
-        CudaCheck(cudaMemcpyAsync(&total, count.Get(), sizeof(total), cudaMemcpyDeviceToHost, s), "read count");
+        CudaCheck(cudaMemcpyAsync(hostCount.Get(), count.Get(), sizeof(unsigned long long) * count.Size(),
+                      cudaMemcpyDeviceToHost, s),
+            "read counts");
         impl_->stream.Sync();
         counters_[6] += impl_->timer.ElapsedNs();
         ++counters_[7];
-        if (total <= capacity) {
+        uint64_t most = 0;
+        for (int32_t r = 0; r < nRegions; ++r) {
+            regionCount[r] = static_cast<int64_t>(hostCount[static_cast<size_t>(r) * omg::kRegionStride]);
+            most = std::max<uint64_t>(most, static_cast<uint64_t>(regionCount[r]));
+        }
+        if (most <= regionCap) {
             break;
         }
-        capacity = total;  // exact size known now: run once more
+        regionCap = (most + 63) / 64 * 64;  // exact size known now: run once more
         ++counters_[1];
     }
-    const int64_t rows = static_cast<int64_t>(total);
-    std::vector<omg::OutColumn> outCols = cols;
-    if (!deviceOutput_) {
-        outCols = omg::CopyColumnsToHost(cols, rows, s);
-        impl_->stream.Sync();
-        for (auto &c : outCols) {
-            c.hasNull = false;
+    int64_t rows = 0;
+    for (int32_t r = 0; r < nRegions; ++r) {
+        const int64_t n = regionCount[r];
+        if (n == 0) {
+            continue;
         }
+        const int64_t first = static_cast<int64_t>(r) * static_cast<int64_t>(regionCap);
+        std::vector<omg::OutColumn> outCols = cols;
+        int64_t firstRow = first;
+        if (!deviceOutput_) {
+            outCols = omg::CopyColumnsToHost(cols, n, s, first);
+            firstRow = 0;
+            for (auto &c : outCols) {
+                c.hasNull = false;  // host vectors: HasNull() scans the bitmap
+            }
+        }
+        for (auto *ob : omg::CarveBatches(outCols, n, f_.rowsPerBatch, firstRow)) {
+            outputs_.push_back(ob);
+        }
+        rows += n;
     }
-    for (auto *ob : omg::CarveBatches(outCols, rows, f_.rowsPerBatch)) {
-        outputs_.push_back(ob);
+    if (!deviceOutput_) {
+        impl_->stream.Sync();
     }
     counters_[5] += rows;
     for (auto *pb : pending_) {

@@ -573,14 +573,16 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
             }
             total = __reduce_add_sync(0xffffffffu, total);
         }
+        const int region = t % p.nRegions;
         unsigned long long pos = 0;
         if (lane == 0 && total != 0) {
-            pos = atomicAdd(p.outCount, static_cast<unsigned long long>(total));
+            pos = atomicAdd(p.outCount + region * kRegionStride, static_cast<unsigned long long>(total));
         }
         pos = __shfl_sync(0xffffffffu, pos, 0);
         if (p.countOnly || total == 0) {
             continue;
         }
+        const uint64_t regionBase = static_cast<uint64_t>(region) * p.regionCap;
         // Phase 3: compacted writes in row order.
 #pragma unroll
         for (int i = 0; i < kWarpRounds; ++i) {
@@ -589,12 +591,13 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
                 const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
                 if ((hit >> i) & 1u) {
                     const uint64_t at = pos + __popc(m & lanesBelow);
-                    if (at < p.outCapacity) {
+                    if (at < p.regionCap) {
                         // The key is re-read (an L1/L2 hit) rather than kept live in registers.
                         if (kPayload) {
-                            WriteJoinRowPayload(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), payload[i], at);
+                            WriteJoinRowPayload(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), payload[i],
+                                regionBase + at);
                         } else {
-                            WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), entry[i], at);
+                            WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), entry[i], regionBase + at);
                         }
                     }
                 }
@@ -610,11 +613,11 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
                 }
                 const uint64_t at = pos + inc - cnt[i];
                 for (uint32_t k = 0; k < cnt[i]; ++k) {
-                    if (at + k >= p.outCapacity) {
+                    if (at + k >= p.regionCap) {
                         break;
                     }
                     WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), __ldg(p.table.csrRows + entry[i] + k),
-                        at + k);
+                        regionBase + at + k);
                 }
                 pos += __shfl_sync(0xffffffffu, inc, 31);
             }
@@ -701,20 +704,23 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeFastKernel(const __grid
         for (int i = 0; i < kWarpRounds; ++i) {
             total += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
         }
+        const int region = t % p.nRegions;
         unsigned long long pos = 0;
         if (lane == 0 && total != 0) {
-            pos = atomicAdd(p.outCount, static_cast<unsigned long long>(total));
+            pos = atomicAdd(p.outCount + region * kRegionStride, static_cast<unsigned long long>(total));
         }
         pos = __shfl_sync(0xffffffffu, pos, 0);
         if (p.countOnly || total == 0) {
             continue;
         }
+        const uint64_t regionBase = static_cast<uint64_t>(region) * p.regionCap;
 #pragma unroll
         for (int i = 0; i < kWarpRounds; ++i) {
             const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
             if ((hit >> i) & 1u) {
-                const uint64_t at = pos + __popc(m & lanesBelow);
-                if (at < p.outCapacity) {
+                const uint64_t rat = pos + __popc(m & lanesBelow);
+                if (rat < p.regionCap) {
+                    const uint64_t at = regionBase + rat;
                     // Re-read the key (an L1 hit) rather than keeping 16 keys live in registers.
                     const int64_t kv = __ldg(keyCol + base + i * 32 + lane);
 #pragma unroll
@@ -734,6 +740,226 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeFastKernel(const __grid
             }
             pos += __popc(m);
         }
+    }
+}
+
+// ARRAY-table probe with the slot-occupancy bitmap staged in shared memory.  The hit test is a
+// shared-memory load, so only matched rows send a request (the payload fetch) through L1 to L2;
+// with the bitmap in L1 or a table entry per row, the random requests of the lookups bound the
+// kernel.  Warps take 128-row segments (4 rounds of 32 rows), 32 warps per CTA, one CTA per SM
+// (the bitmap is up to kBitsMaxSmem bytes).  Outputs as in ProbeFastKernel.
+constexpr int kBitsThreads = 1024;
+constexpr int kBitsRounds = 4;
+constexpr int kBitsSegRows = kBitsRounds * 32;
+constexpr int kBitsSegsPerTile = kTileRows / kBitsSegRows;
+constexpr uint32_t kBitsMaxSmem = 200u * 1024u;
+constexpr int32_t kBitsMinTiles = 64;  // 256K probe rows
+
+// Output layouts known at compile time: 3 bits per output column (1, 2, 3, 4 = 1, 2, 4, 8
+// bytes; 0 = read the width at run time).
+constexpr uint32_t OutLayout(int w0, int w1 = 0, int w2 = 0, int w3 = 0)
+{
+    return static_cast<uint32_t>(w0) | (static_cast<uint32_t>(w1) << 3) | (static_cast<uint32_t>(w2) << 6) |
+        (static_cast<uint32_t>(w3) << 9);
+}
+constexpr int kW1 = 1, kW2 = 2, kW4 = 3, kW8 = 4;
+
+template <uint32_t kLayout, int kO>
+__device__ __forceinline__ void StoreOut(void *col, uint64_t at, int width, int64_t v)
+{
+    constexpr int code = static_cast<int>((kLayout >> (3 * kO)) & 7u);
+    const int w = code == 0 ? width : (1 << (code - 1));
+    if (w == 8) {
+        static_cast<int64_t *>(col)[at] = v;
+    } else if (w == 4) {
+        static_cast<int32_t *>(col)[at] = static_cast<int32_t>(v);
+    } else if (w == 2) {
+        static_cast<int16_t *>(col)[at] = static_cast<int16_t>(v);
+    } else {
+        static_cast<int8_t *>(col)[at] = static_cast<int8_t>(v);
+    }
+}
+
+// Keys and validity of one warp segment of kBitsSegRows rows starting at `base` (a multiple of
+// 32).  The common segment (all rows inside the batch, bitmap absent or 4-byte aligned) runs
+// branch-free so that all its loads issue back to back: the validity of 32 rows is one 32-bit
+// word.  Other segments check every row and read validity bytes.
+__device__ __forceinline__ uint32_t LoadKeySegment(const long long *keyCol, const uint8_t *keyNulls, int64_t base,
+    int64_t batchRows, int lane, int64_t (&key)[kBitsRounds])
+{
+    uint32_t live = 0;
+    if (base + kBitsSegRows <= batchRows && (reinterpret_cast<uintptr_t>(keyNulls) & 3u) == 0) {
+        if (keyNulls == nullptr) {
+#pragma unroll
+            for (int i = 0; i < kBitsRounds; ++i) {
+                key[i] = __ldg(keyCol + base + i * 32 + lane);
+            }
+            return (1u << kBitsRounds) - 1u;
+        }
+        uint32_t w[kBitsRounds];
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            key[i] = __ldg(keyCol + base + i * 32 + lane);
+            w[i] = __ldg(reinterpret_cast<const unsigned int *>(keyNulls) + ((base >> 5) + i));
+        }
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            live |= (((w[i] >> lane) & 1u) ^ 1u) << i;
+        }
+        return live;
+    }
+#pragma unroll
+    for (int i = 0; i < kBitsRounds; ++i) {
+        const int64_t row = base + i * 32 + lane;
+        key[i] = 0;
+        if (row < batchRows) {
+            key[i] = __ldg(keyCol + row);
+            if (!RowIsNullRO(keyNulls, row)) {
+                live |= 1u << i;
+            }
+        }
+    }
+    return live;
+}
+
+template <int kNumOut, uint32_t kLayout, bool kSingle>
+__global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_constant__ ProbeLaunch p)
+{
+    extern __shared__ uint4 sBitsVec[];
+    const uint32_t *sBits = reinterpret_cast<const uint32_t *>(sBitsVec);
+    {
+        // The bitmap buffer holds a whole number of 16-byte vectors (see LaunchBuildSlotBits).
+        const uint32_t nVec = static_cast<uint32_t>((p.table.range + 127) / 128);
+        const uint4 *g = reinterpret_cast<const uint4 *>(p.table.slotBits);
+        for (uint32_t i = threadIdx.x; i < nVec; i += kBitsThreads) {
+            sBitsVec[i] = __ldg(g + i);
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const unsigned int lanesBelow = (1u << lane) - 1u;
+    const unsigned long long *payloadTab = reinterpret_cast<const unsigned long long *>(p.table.slotPayload);
+    const uint64_t minKey = static_cast<uint64_t>(p.table.minKey);
+    const uint64_t range = p.table.range;
+    void *vals[kNumOut];
+    int width[kNumOut];
+    int shift[kNumOut];
+    bool isKey[kNumOut];
+#pragma unroll
+    for (int o = 0; o < kNumOut; ++o) {
+        vals[o] = p.out[o].values;
+        width[o] = p.out[o].width;
+        shift[o] = p.out[o].shift;
+        isKey[o] = p.out[o].side == 0;
+    }
+    // kSingle: the segments of the one batch are indexed directly (no descriptor loads per segment).
+    const long long *singleKeys = nullptr;
+    const uint8_t *singleNulls = nullptr;
+    int64_t singleRows = 0;
+    if (kSingle) {
+        singleKeys = static_cast<const long long *>(p.batches[0].cols[p.keyInput]);
+        singleNulls = p.batches[0].nulls[p.keyInput];
+        singleRows = p.batches[0].rows;
+    }
+    const int64_t nItems = kSingle ? (singleRows + kBitsSegRows - 1) / kBitsSegRows
+                                   : static_cast<int64_t>(p.nTiles) * kBitsSegsPerTile;
+    const int64_t warpsTotal = static_cast<int64_t>(gridDim.x) * (kBitsThreads / 32);
+    for (int64_t item = static_cast<int64_t>(blockIdx.x) * (kBitsThreads / 32) + (threadIdx.x >> 5); item < nItems;
+         item += warpsTotal) {
+        const int t = static_cast<int>(item / kBitsSegsPerTile);
+        const long long *keyCol;
+        const uint8_t *keyNulls;
+        int64_t base;
+        int64_t batchRows;
+        if (kSingle) {
+            keyCol = singleKeys;
+            keyNulls = singleNulls;
+            base = item * kBitsSegRows;
+            batchRows = singleRows;
+        } else {
+            const int s0 = static_cast<int>(item % kBitsSegsPerTile) * kBitsSegRows;
+            const TileDesc tile = p.tiles[t];
+            if (s0 >= tile.rows) {
+                continue;
+            }
+            const BatchDesc &b = p.batches[tile.batch];
+            keyCol = static_cast<const long long *>(b.cols[p.keyInput]);
+            keyNulls = b.nulls[p.keyInput];
+            base = static_cast<int64_t>(tile.row0) + s0;
+            batchRows = static_cast<int64_t>(tile.row0) + tile.rows;  // rows of the batch up to this tile's end
+        }
+        int64_t key[kBitsRounds];
+        const uint32_t live = LoadKeySegment(keyCol, keyNulls, base, batchRows, lane, key);
+        uint32_t hit = 0;
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            const uint64_t d = static_cast<uint64_t>(key[i]) - minKey;
+            if (((live >> i) & 1u) && key[i] >= p.table.minKey && d < range) {
+                hit |= ((sBits[d >> 5] >> (d & 31)) & 1u) << i;
+            }
+        }
+        uint64_t payload[kBitsRounds];
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            payload[i] = ((hit >> i) & 1u) ? __ldg(payloadTab + (static_cast<uint64_t>(key[i]) - minKey)) : 0ull;
+        }
+        uint32_t total = 0;
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            total += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
+        }
+        const int region = t % p.nRegions;
+        unsigned long long pos = 0;
+        if (lane == 0 && total != 0) {
+            pos = atomicAdd(p.outCount + region * kRegionStride, static_cast<unsigned long long>(total));
+        }
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (p.countOnly || total == 0) {
+            continue;
+        }
+        const uint64_t regionBase = static_cast<uint64_t>(region) * p.regionCap;
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
+            if ((hit >> i) & 1u) {
+                const uint64_t rat = pos + __popc(m & lanesBelow);
+                if (rat < p.regionCap) {
+                    const uint64_t at = regionBase + rat;
+                    StoreOut<kLayout, 0>(vals[0], at, width[0],
+                        isKey[0] ? key[i] : static_cast<int64_t>(payload[i] >> shift[0]));
+                    if (kNumOut > 1) {
+                        StoreOut<kLayout, 1>(vals[1], at, width[1],
+                            isKey[1] ? key[i] : static_cast<int64_t>(payload[i] >> shift[1]));
+                    }
+                    if (kNumOut > 2) {
+                        StoreOut<kLayout, 2>(vals[2], at, width[2],
+                            isKey[2] ? key[i] : static_cast<int64_t>(payload[i] >> shift[2]));
+                    }
+                    if (kNumOut > 3) {
+                        StoreOut<kLayout, 3>(vals[3], at, width[3],
+                            isKey[3] ? key[i] : static_cast<int64_t>(payload[i] >> shift[3]));
+                    }
+                }
+            }
+            pos += __popc(m);
+        }
+    }
+}
+
+// Occupancy bitmap of an ARRAY table: bit d of word d / 32 set iff entries[d] >= 0.  Words past
+// the range (up to the 16-byte padding) are zero.
+__global__ void BuildSlotBitsKernel(const int64_t *entries, uint64_t range, uint32_t *bits, uint64_t nWords)
+{
+    for (uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < nWords;
+         w += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint32_t v = 0;
+        for (int j = 0; j < 32; ++j) {
+            const uint64_t d = w * 32 + j;
+            if (d < range && entries[d] >= 0) {
+                v |= 1u << j;
+            }
+        }
+        bits[w] = v;
     }
 }
 
@@ -802,6 +1028,8 @@ cudaError_t LaunchBuildFill(JoinTable t, const void *keys, const uint8_t *nulls,
     return cudaGetLastError();
 }
 
+uint64_t SlotBitsBytes(uint64_t range) { return ((range + 127) / 128) * 16; }
+
 cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
 {
     if (p.nTiles <= 0) {
@@ -814,6 +1042,66 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         const JoinOutCol &oc = p.out[o];
         fast = (oc.side == 1 || (oc.side == 0 && oc.src == p.keyInput && oc.width == 8)) &&
             (oc.width == 1 || oc.width == 2 || oc.width == 4 || oc.width == 8);
+    }
+    // ARRAY tables whose occupancy bitmap fits in shared memory, on launches large enough to
+    // amortise staging it into every CTA.
+    const uint64_t bitsBytes = SlotBitsBytes(p.table.range);
+    if (fast && p.table.mode == JOIN_ARRAY && p.table.slotBits != nullptr && bitsBytes <= kBitsMaxSmem &&
+        p.nTiles >= kBitsMinTiles) {
+        // Instances: run-time widths for 1-4 outputs, and compile-time widths for the common
+        // layouts (8-byte key followed by payload fields).
+        struct Inst {
+            uint32_t layout;
+            int nOut;
+            const void *single;
+            const void *tiled;
+        };
+        static const Inst insts[] = {
+            {OutLayout(kW8, kW4, kW4), 3, reinterpret_cast<const void *>(ProbeBitsKernel<3, OutLayout(kW8, kW4, kW4), true>),
+                reinterpret_cast<const void *>(ProbeBitsKernel<3, OutLayout(kW8, kW4, kW4), false>)},
+            {OutLayout(kW8, kW8), 2, reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW8), true>),
+                reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW8), false>)},
+            {OutLayout(kW8, kW4), 2, reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW4), true>),
+                reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW4), false>)},
+            {0, 1, reinterpret_cast<const void *>(ProbeBitsKernel<1, 0, true>),
+                reinterpret_cast<const void *>(ProbeBitsKernel<1, 0, false>)},
+            {0, 2, reinterpret_cast<const void *>(ProbeBitsKernel<2, 0, true>),
+                reinterpret_cast<const void *>(ProbeBitsKernel<2, 0, false>)},
+            {0, 3, reinterpret_cast<const void *>(ProbeBitsKernel<3, 0, true>),
+                reinterpret_cast<const void *>(ProbeBitsKernel<3, 0, false>)},
+            {0, 4, reinterpret_cast<const void *>(ProbeBitsKernel<4, 0, true>),
+                reinterpret_cast<const void *>(ProbeBitsKernel<4, 0, false>)},
+        };
+        constexpr int kInsts = static_cast<int>(sizeof(insts) / sizeof(insts[0]));
+        static bool smemSet[kInsts][2] = {};
+        int pick = -1;
+        for (int i = 0; i < kInsts && pick < 0; ++i) {
+            if (insts[i].nOut != p.nOut) {
+                continue;
+            }
+            bool match = true;
+            for (int o = 0; o < p.nOut && insts[i].layout != 0; ++o) {
+                const int code = static_cast<int>((insts[i].layout >> (3 * o)) & 7u);
+                match = match && (1 << (code - 1)) == p.out[o].width;
+            }
+            pick = match ? i : -1;
+        }
+        const int single = p.singleBatch ? 0 : 1;
+        const void *kernel = single == 0 ? insts[pick].single : insts[pick].tiled;
+        if (!smemSet[pick][single]) {
+            cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                static_cast<int>(kBitsMaxSmem));
+            if (err != cudaSuccess) {
+                return err;
+            }
+            smemSet[pick][single] = true;
+        }
+        const int64_t items = static_cast<int64_t>(p.nTiles) * kBitsSegsPerTile;
+        const int64_t warpsPerCta = kBitsThreads / 32;
+        const int64_t wanted = (items + warpsPerCta - 1) / warpsPerCta;
+        const int grid = static_cast<int>(wanted < SMs() ? wanted : SMs());
+        void *args[] = {const_cast<ProbeLaunch *>(&p)};
+        return cudaLaunchKernel(kernel, dim3(grid), dim3(kBitsThreads), args, static_cast<size_t>(bitsBytes), stream);
     }
     auto kernel = !p.table.unique ? ProbeKernel<false, false>
                                   : (p.table.slotPayload != nullptr ? ProbeKernel<true, true> : ProbeKernel<true, false>);
@@ -835,6 +1123,14 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     const int maxGrid = SMs() * blocksPerSM[which];
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
     kernel<<<grid, kProbeThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchBuildSlotBits(const int64_t *arrayEntries, uint64_t range, uint32_t *bits, cudaStream_t stream)
+{
+    const uint64_t nWords = SlotBitsBytes(range) / 4;
+    BuildSlotBitsKernel<<<GridFor(static_cast<int64_t>(nWords), 256, 8), 256, 0, stream>>>(arrayEntries, range, bits,
+        nWords);
     return cudaGetLastError();
 }
 

@@ -48,6 +48,10 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream);
 // Packs the build output columns named by p.out (side 1, with shifts set) per table slot into
 // payload[nSlots + 1] (the last slot holds the EMPTY-key row of a HASH table).
 cudaError_t LaunchBuildSlotPayload(const ProbeLaunch &p, uint64_t nSlots, uint64_t *payload, cudaStream_t stream);
+// Occupancy bitmap of an ARRAY table (bit d set iff arrayEntries[d] >= 0) into a buffer of
+// SlotBitsBytes(range) bytes.
+uint64_t SlotBitsBytes(uint64_t range);
+cudaError_t LaunchBuildSlotBits(const int64_t *arrayEntries, uint64_t range, uint32_t *bits, cudaStream_t stream);
 cudaError_t LaunchFillI64(int64_t *p, int64_t v, int64_t n, cudaStream_t stream);
 cudaError_t LaunchFillU64(uint64_t *p, uint64_t v, int64_t n, cudaStream_t stream);
 

@@ -224,6 +224,8 @@ struct JoinTable {
     // packed per table slot (ARRAY: key - minKey; HASH: slot; the EMPTY-key row at `capacity`),
     // so the probe fetches them with the entry instead of gathering by build row afterwards.
     const uint64_t *slotPayload;
+    // ARRAY tables with a slot payload: bit d set iff slot d holds a build row.
+    const uint32_t *slotBits;
 };
 
 struct JoinOutCol {
@@ -237,6 +239,9 @@ struct JoinOutCol {
     uint8_t *nulls;              // output null bitmap (nullptr = output has no nulls)
 };
 
+constexpr int kRegionStride = 16;  // counters 128 bytes apart
+constexpr int kMaxRegions = 16;
+
 struct ProbeLaunch {
     const BatchDesc *batches;
     const TileDesc *tiles;
@@ -246,8 +251,14 @@ struct ProbeLaunch {
     int32_t nOut;
     JoinTable table;
     JoinOutCol out[kMaxOutCols];
-    unsigned long long *outCount;  // total matches (also counted past capacity)
-    uint64_t outCapacity;
+    // The output is cut into nRegions regions of regionCap rows; tile t writes its matches
+    // compacted into region t % nRegions, counted by outCount[region * kRegionStride] (matches
+    // past regionCap are counted but not written).  Regions spread the output-range atomics
+    // over several addresses.
+    unsigned long long *outCount;
+    int32_t nRegions;
+    int32_t singleBatch;  // 1: one batch, tiles t cover its rows [t * kTileRows, ...) in order
+    uint64_t regionCap;
     int32_t countOnly;
     int32_t *error;
 };

@@ -77,6 +77,7 @@ public:
     // Build output values packed per table slot, built by the first probe that can use it.
     mutable std::mutex payloadMu;
     mutable omg::BufferPtr slotPayload;
+    mutable omg::BufferPtr slotBits;  // ARRAY tables: occupancy bitmap of the slots
     mutable bool payloadDecided = false;
 };
 

@@ -53,6 +53,29 @@ def test_device_resident_probe(gpu):
     _check(*_cfg2_like(20_000, 200_000, 3), device_input=True, batch_sizes=(200_000,))
 
 
+def test_bitmap_probe_large_device_batch(gpu):
+    # >= 64 tiles on an ARRAY table with a packed payload: the shared-memory bitmap kernel,
+    # output spread over 16 regions.
+    _check(*_cfg2_like(100_000, 1_200_000, 11), device_input=True, batch_sizes=(1_200_000,))
+
+
+def test_bitmap_probe_negative_key_range(gpu):
+    bkey, p1, p2, pkey, pnull = _cfg2_like(60_000, 700_000, 12)
+    _check(bkey - 30_000, p1, p2, pkey - 30_000, pnull, pipeline=True, batch_sizes=(4096, 1000, 64))
+
+
+def test_regions_with_duplicates_retry(gpu):
+    # Duplicate build keys: region capacities start at 2x their probe rows and are re-sized
+    # from the exact per-region counts when exceeded.
+    bkey, p1, p2, pkey, pnull = _cfg2_like(20_000, 500_000, 13, dup=True)
+    hot = bkey[:50]
+    bkey = np.concatenate([bkey] + [hot] * 6)
+    p1 = np.concatenate([p1, np.tile(p1[:50], 6)])
+    p2 = np.concatenate([p2, np.tile(p2[:50], 6)])
+    pkey = np.where(np.arange(len(pkey)) % 3 == 0, hot[np.arange(len(pkey)) % 50], pkey)
+    _check(bkey, p1, p2, pkey, pnull, pipeline=True, batch_sizes=(4096,))
+
+
 def test_duplicate_build_keys_array_mode(gpu):
     _check(*_cfg2_like(30_000, 200_000, 4, dup=True))
 
@@ -131,3 +154,33 @@ def test_reference_kat_array_table_short_keys(gpu):
                       [np.array(c, np.int16) for c in g["probe"]], None, [0], [0, 1], [0, 1])
     exp = sorted(tuple(r) for r in g["expected_rows"])
     assert join_rows_canonical(got) == exp
+
+
+def test_bulk_add_inputs_and_get_outputs(gpu):
+    """omg_op_add_inputs / omg_op_get_outputs equal the per-batch AddInput / GetOutput calls."""
+    bkey, p1, p2, pkey, pnull = _cfg2_like(30_000, 300_000, 14)
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, I, I], [0])
+    bop = bf.create_operator()
+    bop.add_input(omg.make_batch([L, I, I], [bkey, p1, p2]))
+    bop.get_output()
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1, 2], [I, I], bf)
+    op = pf.create_operator()
+    op.set_no_more_input(False)
+    batches = [omg.make_batch([L], [pkey[s:s + 4096]], [pnull[s:s + 4096]]) for s in range(0, len(pkey), 4096)]
+    op.add_inputs(batches[:40])
+    outs, rows = op.get_outputs(1 << 12)
+    op.add_inputs(batches[40:])
+    op.no_more_input()
+    more, rows2 = op.get_outputs(1 << 12)
+    outs += more
+    assert op.get_status() == omg.OMNI_STATUS_FINISHED
+    per = [omg.batch_to_numpy(b) for b in outs]
+    cols = [(np.concatenate([p[c][0] for p in per]), np.concatenate([p[c][1] for p in per])) for c in range(3)]
+    assert rows + rows2 == len(cols[0][0])
+    omg.free_batches(outs)
+    op.delete()
+    pf.close()
+    bop.delete()
+    bf.close()
+    exp = expected_join_rows([pkey], [pnull], [bkey, p1, p2], None, 0, 0, [0], [1, 2])
+    assert join_rows_canonical(cols) == exp
