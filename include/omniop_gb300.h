@@ -81,6 +81,7 @@ extern "C" {
 #define OMG_AGG_STRATEGY_AUTO 0
 #define OMG_AGG_STRATEGY_SMEM 1   /* shared-memory pre-aggregation, global overflow */
 #define OMG_AGG_STRATEGY_GLOBAL 2 /* global open-addressing table only */
+#define OMG_AGG_STRATEGY_PARTITIONED 3 /* hash partitions, a shared-memory table per partition */
 
 /* A column type: id plus decimal precision/scale (or FIXEDBINARY width). */
 typedef struct OmgDataType {
@@ -202,6 +203,13 @@ int32_t omg_op_add_inputs(void *op, void *const *batches, int32_t n, int32_t *co
 int32_t omg_op_get_outputs(void *op, void **out_batches, int32_t max, int32_t *n, int64_t *rows);
 /* Frees n batches (VectorHelper::FreeVecBatch each); NULL entries are skipped. */
 int32_t omg_batch_free_many(void *const *batches, int32_t n);
+/* Sizing record of a HashAggregation operator (no reference counterpart): [0] rows of the first
+ * flush, [1..16] the key sketch of a row sample of that flush (sampled rows, special-key rows,
+ * distinct hashes, frequency classes f1, f2, f3, f4-7, f8+, largest count, rows of the 8+
+ * class, 6 reserved), [17] the group estimate used for sizing, [18] the partition bits of the
+ * partitioned strategy (-1 = global table), [19] the group count so far.  `*written` receives
+ * the number of values stored (at most n). */
+int32_t omg_op_get_sizing_log(void *op, int64_t *out, int32_t n, int32_t *written);
 /* Operator::GetStatus (operator.h:46-49): OMG_STATUS_*. */
 int32_t omg_op_status(void *op);
 /* Operator::noMoreInput / setNoMoreInput / needsInput (operator.h:117-130). */

@@ -60,6 +60,7 @@ _SIGS = {
     "omg_op_add_inputs": (I32, [P, C.POINTER(P), I32, C.POINTER(I32)]),
     "omg_op_get_outputs": (I32, [P, C.POINTER(P), I32, C.POINTER(I32), C.POINTER(I64)]),
     "omg_batch_free_many": (I32, [C.POINTER(P), I32]),
+    "omg_op_get_sizing_log": (I32, [P, C.POINTER(I64), I32, C.POINTER(I32)]),
     "omg_op_status": (I32, [P]),
     "omg_op_no_more_input": (I32, [P]),
     "omg_op_set_no_more_input": (I32, [P, I32]),

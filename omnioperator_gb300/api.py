@@ -29,7 +29,7 @@ OMNI_JOIN_TYPE_INNER = 0
 OMNI_STATUS_NORMAL, OMNI_STATUS_FINISHED, OMNI_STATUS_ERROR = 0, 1, -1
 # SupportContainerVecRule (util/policy.h:160-167)
 POLICY_SPARK, POLICY_GENERIC = 0, 1
-AGG_STRATEGY_AUTO, AGG_STRATEGY_SMEM, AGG_STRATEGY_GLOBAL = 0, 1, 2
+AGG_STRATEGY_AUTO, AGG_STRATEGY_SMEM, AGG_STRATEGY_GLOBAL, AGG_STRATEGY_PARTITIONED = 0, 1, 2, 3
 
 _NP = {OMNI_INT: np.int32, OMNI_LONG: np.int64, OMNI_DOUBLE: np.float64, OMNI_BOOLEAN: np.int8,
        OMNI_SHORT: np.int16, OMNI_DECIMAL64: np.int64, OMNI_DATE32: np.int32, OMNI_DATE64: np.int64,
@@ -250,6 +250,14 @@ class Operator:
         rows = C.c_int64(0)
         check(lib().omg_op_get_outputs(self.handle, arr, max_batches, C.byref(n), C.byref(rows)))
         return list(arr[: n.value]), rows.value
+
+    def sizing_log(self) -> dict:
+        """HashAggregation sizing record (omg_op_get_sizing_log)."""
+        arr = (C.c_int64 * 32)()
+        n = C.c_int32(0)
+        check(lib().omg_op_get_sizing_log(self.handle, arr, 32, C.byref(n)))
+        v = list(arr[: n.value])
+        return {"rows": v[0], "sketch": v[1:17], "estimate": v[17], "part_bits": v[18], "groups": v[19]}
 
     def get_status(self) -> int:
         return lib().omg_op_status(self.handle)

@@ -413,6 +413,16 @@ int32_t omg_op_get_outputs(void *op, void **out_batches, int32_t max, int32_t *n
     });
 }
 
+int32_t omg_op_get_sizing_log(void *op, int64_t *out, int32_t n, int32_t *written)
+{
+    return Guard([&] {
+        auto *agg = dynamic_cast<HashAggregationOperator *>(AsOp(op));
+        Require(agg != nullptr, "not a HashAggregation operator");
+        Require(out != nullptr && n >= 0 && written != nullptr, "null output");
+        *written = agg->GetSizingLog(out, n);
+    });
+}
+
 int32_t omg_batch_free_many(void *const *batches, int32_t n)
 {
     return Guard([&] {
@@ -481,7 +491,7 @@ int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hin
     return Guard([&] {
         auto *a = dynamic_cast<HashAggregationOperator *>(AsOp(op));
         Require(a != nullptr, "not a hash aggregation operator");
-        Require(strategy >= OMG_AGG_STRATEGY_AUTO && strategy <= OMG_AGG_STRATEGY_GLOBAL, "unknown strategy");
+        Require(strategy >= OMG_AGG_STRATEGY_AUTO && strategy <= OMG_AGG_STRATEGY_PARTITIONED, "unknown strategy");
         a->SetStrategy(strategy, capacity_hint);
     });
 }

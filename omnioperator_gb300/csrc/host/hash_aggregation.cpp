@@ -10,6 +10,7 @@
 #include "omniop/hash_aggregation.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cfloat>
 #include <climits>
 #include <cstring>
@@ -141,9 +142,10 @@ OmniStatus HashAggregationOperatorFactory::Init()
     p = AggPlan();
     p.overflowAsNull = overflowAsNull_;
     std::map<uint32_t, int32_t> inputOf;  // batch column -> kernel input
-    auto inputFor = [&](uint32_t col) {
+    auto inputFor = [&](uint32_t col, int width) {
         auto it = inputOf.find(col);
         if (it != inputOf.end()) {
+            p.inputWidths[it->second] = std::max(p.inputWidths[it->second], width);
             return it->second;
         }
         const int32_t idx = static_cast<int32_t>(p.inputCols.size());
@@ -151,6 +153,7 @@ OmniStatus HashAggregationOperatorFactory::Init()
             throw OmniException("UNSUPPORTED_ERROR", "too many distinct input columns", -2);
         }
         p.inputCols.push_back(static_cast<int32_t>(col));
+        p.inputWidths.push_back(width);
         inputOf[col] = idx;
         return idx;
     };
@@ -169,7 +172,7 @@ OmniStatus HashAggregationOperatorFactory::Init()
         if (w == 0 || (w > 8 && w != 16)) {
             throw OmniException("UNSUPPORTED_ERROR", "unsupported group-by type " + std::to_string(t->GetId()), -2);
         }
-        p.key.cols[i].input = static_cast<int16_t>(inputFor(groupByCols_[i]));
+        p.key.cols[i].input = static_cast<int16_t>(inputFor(groupByCols_[i], w));
         p.key.cols[i].width = static_cast<int16_t>(w);
         p.outTypes.push_back(t);
         rowBytes += w;
@@ -265,7 +268,7 @@ OmniStatus HashAggregationOperatorFactory::Init()
         const DataTypePtr &inT = aggInputTypes_[a].GetType(0);
         const DataTypeId inId = inT->GetId();
         const int inW = inT->ByteWidth();
-        const int input = inputFor(aggCols_[a][0]);
+        const int input = inputFor(aggCols_[a][0], inW);
         const int nulls = accFor(omg::ACC_NULLS, input, omg::IN_NONE, 0, 0);
         o.countAcc = static_cast<int16_t>(nulls);
         const bool isInt = IsIntegerLike(inId);
@@ -407,6 +410,13 @@ struct HashAggregationOperator::Impl {
     uint64_t groups = 0;
     // Batches kept for the ordered sticky-overflow path (order-dependent plans only).
     std::vector<VectorBatch *> retained;
+    // Sizing, decided at the first flush: the sketch of a row sample, the group estimate used,
+    // and the partition bits of the partitioned strategy (-1: global table).
+    bool decided = false;
+    unsigned long long sketch[omg::kSketchStats] = {};
+    int64_t sketchRows = 0;  // rows of the flush the sketch sampled
+    uint64_t estimate = 0;
+    int32_t partBits = -1;
 };
 
 HashAggregationOperator::HashAggregationOperator(const AggPlan &plan) : plan_(plan), impl_(new Impl()) {}
@@ -498,6 +508,146 @@ omg::AggLaunch MakeLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacit
 }
 }  // namespace
 
+namespace {
+constexpr int64_t kSketchMinRows = int64_t(1) << 18;  // smaller flushes: default sizing, global table
+constexpr int32_t kSketchSample = 1 << 16;
+constexpr double kPartLoad = 0.6;  // target load of a partition's shared table
+
+// Plain group-count estimate from the sketch of n sampled rows out of N: the GEE estimator
+// (sqrt(N / n) * f1 + sum of the other frequency classes), clamped to [d, N].
+uint64_t EstimateGroups(const unsigned long long *st, int64_t total)
+{
+    const double n = static_cast<double>(st[0] - st[1]);
+    const double d = static_cast<double>(st[2]);
+    const double f1 = static_cast<double>(st[3]);
+    const double specials = st[1] > 0 ? 2.0 : 0.0;  // the NULL and EMPTY groups at most
+    if (n <= 0) {
+        return static_cast<uint64_t>(specials) + 1;
+    }
+    double est = n >= static_cast<double>(total) ? d : std::sqrt(static_cast<double>(total) / n) * f1 + (d - f1);
+    est = std::min(std::max(est, d), static_cast<double>(total));
+    return static_cast<uint64_t>(est + specials);
+}
+}  // namespace
+
+// Partition buffers of one flush (see Partition).
+struct HashAggregationOperator::PartBuffers {
+    std::vector<omg::BufferPtr> cols;
+    std::vector<omg::BufferPtr> nulls;
+    DevArray<unsigned long long> counters;  // hist then cursor
+    DevArray<omg::BatchDesc> batches;
+    DevArray<omg::TileDesc> tiles;
+    DevArray<int32_t> tileStart;
+};
+
+int32_t HashAggregationOperator::GetSizingLog(int64_t *out, int32_t n) const
+{
+    const Impl &im = *impl_;
+    std::vector<int64_t> v;
+    v.push_back(im.sketchRows);
+    for (int i = 0; i < omg::kSketchStats; ++i) {
+        v.push_back(static_cast<int64_t>(im.sketch[i]));
+    }
+    v.push_back(static_cast<int64_t>(im.estimate));
+    v.push_back(im.partBits);
+    v.push_back(static_cast<int64_t>(std::max<uint64_t>(im.groups, uniqueKeys_)));
+    const int32_t m = std::min<int32_t>(n, static_cast<int32_t>(v.size()));
+    for (int32_t i = 0; i < m; ++i) {
+        out[i] = v[i];
+    }
+    return m;
+}
+
+void HashAggregationOperator::Decide(omg::BatchTable &bt, cudaStream_t s)
+{
+    Impl &im = *impl_;
+    im.decided = true;
+    const int64_t rows = bt.TotalRows();
+    if (capacityHint_ > 0) {
+        im.estimate = static_cast<uint64_t>(capacityHint_);  // the caller's (or a sizing model's) estimate
+    } else if (rows >= kSketchMinRows && (strategy_ == 0 || strategy_ == 3)) {
+        DevArray<unsigned long long> tabKeys(omg::kSketchCap, s);
+        DevArray<unsigned int> tabCounts(omg::kSketchCap, s);
+        DevArray<unsigned long long> st(omg::kSketchStats, s);
+        omg::AggLaunch p = MakeLaunch(plan_, nullptr, 0, nullptr, nullptr);
+        p.batches = bt.DeviceBatches();
+        p.tiles = bt.DeviceTiles();
+        p.nTiles = bt.NumTiles();
+        const int32_t n = static_cast<int32_t>(std::min<int64_t>(rows, kSketchSample));
+        CudaCheck(omg::LaunchAggSketch(p, bt.DeviceTileOutRows(), rows, n, tabKeys.Get(), tabCounts.Get(), st.Get(), s),
+            "key sketch");
+        ++counters_[0];
+        CudaCheck(cudaMemcpyAsync(im.sketch, st.Get(), sizeof(im.sketch), cudaMemcpyDeviceToHost, s), "read sketch");
+        im.stream.Sync();
+        im.sketchRows = rows;
+        im.estimate = EstimateGroups(im.sketch, rows);
+    }
+    // Partitions: enough that one partition's groups fill a CTA's shared table to kPartLoad.
+    const bool wantPart = strategy_ == 3 || (strategy_ == 0 && rows >= kSketchMinRows);
+    if (wantPart && im.estimate > 0) {
+        const double perCta = kPartLoad * omg::AggPartSmemSlots(plan_.slotWords);
+        const uint64_t need = NextPow2(static_cast<uint64_t>(std::ceil(static_cast<double>(im.estimate) / perCta)));
+        if (need <= static_cast<uint64_t>(omg::kMaxParts) && perCta >= 1.0) {
+            int bits = 0;
+            while ((uint64_t(1) << bits) < need) {
+                ++bits;
+            }
+            im.partBits = bits;
+        }
+    }
+    if (strategy_ == 3 && im.partBits < 0) {
+        im.partBits = 0;  // forced: one partition (the shared tables still sit in front of the global one)
+    }
+}
+
+void HashAggregationOperator::Partition(omg::BatchTable &bt, omg::AggLaunch &p, PartBuffers &pb, cudaStream_t s)
+{
+    Impl &im = *impl_;
+    const int32_t nParts = 1 << im.partBits;
+    const int64_t rows = bt.TotalRows();
+    pb.tileStart.Reset(nParts + 1, s);
+    if (im.partBits == 0) {
+        // One partition: the batches themselves, no copy.
+        const int32_t h[2] = {0, bt.NumTiles()};
+        CudaCheck(cudaMemcpyAsync(pb.tileStart.Get(), h, sizeof(h), cudaMemcpyHostToDevice, s), "partition tiles");
+        im.stream.Sync();  // h is on the stack
+        p.nParts = 1;
+        p.partTileStart = pb.tileStart.Get();
+        return;
+    }
+    omg::PartArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.partBits = im.partBits;
+    a.nInputs = static_cast<int32_t>(plan_.inputCols.size());
+    const int64_t capRows = rows + static_cast<int64_t>(nParts) * 64;
+    for (int32_t i = 0; i < a.nInputs; ++i) {
+        const int32_t w = std::max(plan_.inputWidths[i], 1);
+        a.width[i] = w;
+        pb.cols.push_back(omg::Buffer::NewDevice(static_cast<size_t>(capRows) * w + 16, s, false));
+        a.cols[i] = pb.cols.back()->Data();
+        if (bt.AnyNulls(i)) {
+            pb.nulls.push_back(omg::Buffer::NewDevice(omg::NullBitmapBytes(capRows), s, true));
+            a.nulls[i] = static_cast<uint32_t *>(pb.nulls.back()->Data());
+        }
+    }
+    pb.counters.Reset(2 * static_cast<size_t>(nParts), s, true);
+    a.hist = pb.counters.Get();
+    a.cursor = pb.counters.Get() + nParts;
+    pb.batches.Reset(nParts, s);
+    a.partBatches = pb.batches.Get();
+    a.maxTiles = static_cast<int32_t>(rows / omg::kTileRows + nParts + 1);
+    pb.tiles.Reset(a.maxTiles, s);
+    a.partTiles = pb.tiles.Get();
+    a.partTileStart = pb.tileStart.Get();
+    CudaCheck(omg::LaunchAggPartition(p, a, s), "hash partition");
+    counters_[0] += 3;
+    p.batches = pb.batches.Get();
+    p.tiles = pb.tiles.Get();
+    p.nTiles = a.maxTiles;
+    p.nParts = nParts;
+    p.partTileStart = pb.tileStart.Get();
+}
+
 void HashAggregationOperator::Flush()
 {
     if (pending_.empty()) {
@@ -512,9 +662,16 @@ void HashAggregationOperator::Flush()
     if (im.stats.Get() == nullptr) {
         im.stats.Reset(8, s, true);
     }
-    // Create the table on first use.
+    omg::BatchTable bt;
+    bt.Build(pending_, plan_.inputCols);
+    bt.Upload(s);
+    const int64_t rows = bt.TotalRows();
+    if (!im.decided) {
+        Decide(bt, s);
+    }
+    // Create the table on first use, sized for the group estimate (load factor <= 1/2).
     if (im.capacity == 0) {
-        uint64_t cap = capacityHint_ > 0 ? NextPow2(static_cast<uint64_t>(capacityHint_) * 2) : kDefaultCapacity;
+        uint64_t cap = im.estimate > 0 ? NextPow2(im.estimate * 2) : kDefaultCapacity;
         cap = std::max<uint64_t>(cap, 1024);
         im.slots.Reset((cap + 2) * plan_.slotWords, s);
         im.special.Reset(2, s, true);
@@ -523,31 +680,34 @@ void HashAggregationOperator::Flush()
         CudaCheck(omg::LaunchAggInitTable(init, s), "init aggregation table");
         ++counters_[0];
     }
-    omg::BatchTable bt;
-    bt.Build(pending_, plan_.inputCols);
-    bt.Upload(s);
-    const int64_t rows = bt.TotalRows();
-
     const int sms = omg::DeviceSMCount();
     int smemSlots = 0;
-    // AUTO (0) and GLOBAL (2): global table only.  The per-CTA shared table pays off only when
-    // a few groups take most rows (skew), which the sizing model detects and asks for (SMEM, 1).
+    // GLOBAL (2): global table only.  SMEM (1): a per-CTA shared table in front of the global
+    // one.  PARTITIONED (3, or AUTO when the estimate says the groups fit): rows are hash
+    // partitioned so that each CTA's shared table holds one partition's groups.
     if (strategy_ == 1) {  // OMG_AGG_STRATEGY_SMEM
         smemSlots = plan_.smemSlots;
     }
     const int grid = 0;  // the launcher fills every SM to its occupancy limit
     const int maxGrid = sms * 4;
+    // Partition buffers live until the retries (which address rows of the partitions) are done.
+    PartBuffers part;
+    const omg::BatchDesc *rowBatches = bt.DeviceBatches();
     DevArray<unsigned long long> retryA(static_cast<size_t>(rows), s);
     DevArray<unsigned long long> retryB;
-    const size_t spillCap = static_cast<size_t>(smemSlots) * maxGrid;
-    DevArray<uint64_t> spillA(std::max<size_t>(spillCap, 1) * plan_.slotWords, s);
-    DevArray<uint64_t> spillB;
-    CudaCheck(cudaMemsetAsync(im.stats.Get() + 1, 0, 3 * sizeof(unsigned long long), s), "reset stats");
-
     omg::AggLaunch p = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
     p.batches = bt.DeviceBatches();
     p.tiles = bt.DeviceTiles();
     p.nTiles = bt.NumTiles();
+    if (im.partBits >= 0) {
+        smemSlots = omg::AggPartSmemSlots(plan_.slotWords);
+        Partition(bt, p, part, s);
+        rowBatches = p.batches;
+    }
+    const size_t spillCap = static_cast<size_t>(smemSlots) * maxGrid;
+    DevArray<uint64_t> spillA(std::max<size_t>(spillCap, 1) * plan_.slotWords, s);
+    DevArray<uint64_t> spillB;
+    CudaCheck(cudaMemsetAsync(im.stats.Get() + 1, 0, 3 * sizeof(unsigned long long), s), "reset stats");
     p.retry = retryA.Get();
     p.retryCap = static_cast<uint32_t>(rows);
     p.smemSlots = smemSlots;
@@ -589,7 +749,7 @@ void HashAggregationOperator::Flush()
         spillB.Reset(std::max<uint64_t>(nSpillH, 1) * plan_.slotWords, s);
         CudaCheck(cudaMemsetAsync(im.stats.Get() + 1, 0, 3 * sizeof(unsigned long long), s), "reset stats");
         omg::AggLaunch r = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
-        r.batches = bt.DeviceBatches();
+        r.batches = rowBatches;
         r.retry = retryB.Get();
         r.retryCap = static_cast<uint32_t>(std::max<uint64_t>(nRetry, 1));
         r.retryIn = retryA.Get();

@@ -527,12 +527,188 @@ __device__ __forceinline__ void MergeRecord(const AggLaunch &p, const SpillArgs 
     MergeStates(p.accs, p.nAccs, rec + kw, p.table.slots + g * sw + kw);
 }
 
-template <int kKind>
-__global__ void __launch_bounds__(kAggThreads, 2) AggKernel(const __grid_constant__ AggLaunch p,
-    const __grid_constant__ SpillArgs sp)
+// ------------------------------------------------------------------ partitioned tiles
+// Partitioned launches process a tile in two passes.  Pass 1 resolves each of the thread's rows
+// to a slot of the CTA's shared table (a row whose group does not fit, or a NULL / EMPTY key,
+// goes through the generic global path at once).  Pass 2 walks the accumulators once per tile:
+// the accumulator's kind and input width are dispatched once, then applied to the thread's rows,
+// so the per-row work is the value load and the shared-memory atomic.
+constexpr int kPartRows = kTileRows / 1024;
+
+template <int kW>
+__device__ __forceinline__ int64_t LoadIntW(const void *col, int64_t row)
 {
-    extern __shared__ __align__(16) uint64_t smem[];
-    __shared__ unsigned int newGroups;
+    if (kW == 8) {
+        return __ldg(static_cast<const long long *>(col) + row);
+    } else if (kW == 4) {
+        return __ldg(static_cast<const int *>(col) + row);
+    } else if (kW == 2) {
+        return __ldg(static_cast<const short *>(col) + row);
+    } else {
+        return static_cast<int64_t>(static_cast<signed char>(__ldg(static_cast<const char *>(col) + row)));
+    }
+}
+
+template <int kW>
+__device__ __forceinline__ void ApplyIntAcc(const AccSpec &s, const void *col, const uint8_t *nulls, int64_t row0,
+    const int (&slot)[kPartRows], uint64_t *sm, int sw)
+{
+    int64_t x[kPartRows];
+    bool ok[kPartRows];
+#pragma unroll
+    for (int k = 0; k < kPartRows; ++k) {
+        const int64_t row = row0 + k * 1024;
+        ok[k] = slot[k] >= 0 && !NullRO(nulls, row);
+        x[k] = ok[k] ? LoadIntW<kW>(col, row) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kPartRows; ++k) {
+        if (!ok[k]) {
+            continue;
+        }
+        uint64_t *w = sm + slot[k] * sw + s.word;
+        if (s.kind == ACC_ISUM) {
+            atomicAdd(reinterpret_cast<unsigned long long *>(w), static_cast<unsigned long long>(x[k]));
+        } else if (s.kind == ACC_WSUM2) {
+            const uint64_t m = x[k] >= 0 ? static_cast<uint64_t>(x[k]) : 0ull - static_cast<uint64_t>(x[k]);
+            uint64_t *side = x[k] >= 0 ? w : w + 2;
+            atomicAdd(reinterpret_cast<unsigned long long *>(side), m & 0xffffffffull);
+            if ((m >> 32) != 0) {
+                atomicAdd(reinterpret_cast<unsigned long long *>(side + 1), m >> 32);
+            }
+        } else if (s.kind == ACC_IMIN) {
+            AtomicMinI64(w, x[k]);
+        } else {
+            AtomicMaxI64(w, x[k]);
+        }
+    }
+}
+
+template <int kKind>
+__device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batchIdx, const BatchDesc &b,
+    const TileDesc &tile, uint64_t *sm, int smSlots, unsigned int *newGroups)
+{
+    const int sw = p.table.slotWords;
+    const int kw = p.table.keyWords;
+    const int64_t row0 = static_cast<int64_t>(tile.row0) + threadIdx.x;
+    int slot[kPartRows];  // >= 0: slot index in the shared table, -1: nothing to do in pass 2
+#pragma unroll
+    for (int k = 0; k < kPartRows; ++k) {
+        slot[k] = -1;
+        const int r = static_cast<int>(threadIdx.x) + k * 1024;
+        if (r < tile.rows) {
+            const RowKey key = ReadKey(p.key, b, row0 + k * 1024, kKind);
+            const int i = key.special < 0 ? SmemFind(sm, smSlots, sw, p.key, key, kKind) : -1;
+            slot[k] = i >= 0 ? i : -2;
+        }
+    }
+    // Rows whose group is not in the shared table: the generic global path.
+#pragma unroll 1
+    for (int k = 0; k < kPartRows; ++k) {
+        if (slot[k] == -2) {
+            const int64_t row = row0 + k * 1024;
+            ProcessRow<kKind>(p, batchIdx, b, row, LoadRow<kKind>(p, b, row), sm, 0, newGroups);
+        }
+    }
+    uint64_t *st = sm + kw;  // state words of slot i start at st + i * sw
+    for (int a = 0; a < p.nAccs; ++a) {
+        const AccSpec s = p.accs[a];
+        const void *col = s.input >= 0 ? b.cols[s.input] : nullptr;
+        const uint8_t *nulls = s.input >= 0 ? b.nulls[s.input] : nullptr;
+        switch (s.kind) {
+            case ACC_COUNT_ALL:
+#pragma unroll
+                for (int k = 0; k < kPartRows; ++k) {
+                    if (slot[k] >= 0) {
+                        atomicAdd(reinterpret_cast<unsigned long long *>(st + slot[k] * sw + s.word), 1ull);
+                    }
+                }
+                break;
+            case ACC_NULLS:
+                if (nulls != nullptr) {
+#pragma unroll
+                    for (int k = 0; k < kPartRows; ++k) {
+                        if (slot[k] >= 0 && NullRO(nulls, row0 + k * 1024)) {
+                            atomicAdd(reinterpret_cast<unsigned long long *>(st + slot[k] * sw + s.word), 1ull);
+                        }
+                    }
+                }
+                break;
+            case ACC_ISUM:
+            case ACC_WSUM2:
+            case ACC_IMIN:
+            case ACC_IMAX:
+                if (s.inWidth == 8) {
+                    ApplyIntAcc<8>(s, col, nulls, row0, slot, st, sw);
+                } else if (s.inWidth == 4) {
+                    ApplyIntAcc<4>(s, col, nulls, row0, slot, st, sw);
+                } else if (s.inWidth == 2) {
+                    ApplyIntAcc<2>(s, col, nulls, row0, slot, st, sw);
+                } else {
+                    ApplyIntAcc<1>(s, col, nulls, row0, slot, st, sw);
+                }
+                break;
+            case ACC_DSUM:
+            case ACC_DMIN:
+            case ACC_DMAX: {
+                double x[kPartRows];
+                bool ok[kPartRows];
+#pragma unroll
+                for (int k = 0; k < kPartRows; ++k) {
+                    const int64_t row = row0 + k * 1024;
+                    ok[k] = slot[k] >= 0 && !NullRO(nulls, row);
+                    x[k] = ok[k] ? LoadAsDoubleRO(col, row, s.inKind, s.inWidth) : 0.0;
+                }
+#pragma unroll
+                for (int k = 0; k < kPartRows; ++k) {
+                    if (!ok[k]) {
+                        continue;
+                    }
+                    uint64_t *w = st + slot[k] * sw + s.word;
+                    if (s.kind == ACC_DSUM) {
+                        AtomicAddCompensated(w, x[k], 0.0);
+                    } else if (!isnan(x[k])) {
+                        if (s.kind == ACC_DMIN) {
+                            AtomicMinI64(w, OrderedFromDouble(x[k]));
+                        } else {
+                            AtomicMaxI64(w, OrderedFromDouble(x[k]));
+                        }
+                    }
+                }
+                break;
+            }
+            case ACC_WSUM3:
+#pragma unroll
+                for (int k = 0; k < kPartRows; ++k) {
+                    const int64_t row = row0 + k * 1024;
+                    if (slot[k] < 0 || NullRO(nulls, row)) {
+                        continue;
+                    }
+                    const ulonglong2 v = __ldg(static_cast<const ulonglong2 *>(col) + row);
+                    uint64_t lo = v.x;
+                    uint64_t hi = v.y;
+                    uint64_t *side = st + slot[k] * sw + s.word;
+                    if (static_cast<int64_t>(hi) < 0) {  // magnitude = -(hi:lo)
+                        lo = ~lo + 1;
+                        hi = ~hi + (lo == 0 ? 1u : 0u);
+                        side += 4;
+                    }
+                    Red(side, lo & 0xffffffffull);
+                    Red(side + 1, lo >> 32);
+                    Red(side + 2, hi & 0xffffffffull);
+                    Red(side + 3, hi >> 32);
+                }
+                break;
+            default:
+                break;
+        }
+    }
+}
+
+template <int kKind, bool kPart>
+__device__ __forceinline__ void AggBody(const AggLaunch &p, const SpillArgs &sp, uint64_t *smem,
+    unsigned int &newGroups)
+{
     const int sw = p.table.slotWords;
     const int kw = p.table.keyWords;
     const int smSlots = (p.retryIn == nullptr && sp.spillIn == nullptr) ? p.smemSlots : 0;
@@ -564,7 +740,23 @@ __global__ void __launch_bounds__(kAggThreads, 2) AggKernel(const __grid_constan
         }
     } else {
         // Two rows per thread per step: both rows' loads are issued before either is processed.
-        for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        int tFirst = blockIdx.x;
+        int tEnd = p.nTiles;
+        int tStep = gridDim.x;
+        if (p.nParts > 0) {  // gridDim.x is a multiple of nParts
+            const int q = blockIdx.x % p.nParts;
+            tFirst = p.partTileStart[q] + blockIdx.x / p.nParts;
+            tEnd = p.partTileStart[q + 1];
+            tStep = gridDim.x / p.nParts;
+        }
+        if (kPart && smSlots > 0) {
+            for (int t = tFirst; t < tEnd; t += tStep) {
+                const TileDesc tile = p.tiles[t];
+                ProcessPartTile<kKind>(p, tile.batch, p.batches[tile.batch], tile, smem, smSlots, &newGroups);
+            }
+            tEnd = tFirst;  // done
+        }
+        for (int t = tFirst; t < tEnd; t += tStep) {
             const TileDesc tile = p.tiles[t];
             const BatchDesc &b = p.batches[tile.batch];
             for (int r = threadIdx.x; r < tile.rows; r += 2 * blockDim.x) {
@@ -595,6 +787,29 @@ __global__ void __launch_bounds__(kAggThreads, 2) AggKernel(const __grid_constan
     if (threadIdx.x == 0 && newGroups != 0) {
         atomicAdd(p.table.groupCount, static_cast<unsigned long long>(newGroups));
     }
+}
+
+template <int kKind>
+__global__ void __launch_bounds__(kAggThreads, 2) AggKernel(const __grid_constant__ AggLaunch p,
+    const __grid_constant__ SpillArgs sp)
+{
+    extern __shared__ __align__(16) uint64_t smem[];
+    __shared__ unsigned int newGroups;
+    AggBody<kKind, false>(p, sp, smem, newGroups);
+}
+
+// Partitioned launches: one 1024-thread CTA per SM with a shared table of up to
+// kPartSmemBytes (the partition's groups).
+constexpr int kPartThreads = 1024;
+constexpr size_t kPartSmemBytes = 200 * 1024;
+
+template <int kKind>
+__global__ void __launch_bounds__(kPartThreads, 1) AggPartKernel(const __grid_constant__ AggLaunch p,
+    const __grid_constant__ SpillArgs sp)
+{
+    extern __shared__ __align__(16) uint64_t smem[];
+    __shared__ unsigned int newGroups;
+    AggBody<kKind, true>(p, sp, smem, newGroups);
 }
 
 // ------------------------------------------------------------------ table maintenance
@@ -1086,6 +1301,283 @@ __global__ void OrderedOverflowKernel(const __grid_constant__ AggLaunch p, int32
     }
 }
 
+// ------------------------------------------------------------------ hash partitioning
+__device__ __forceinline__ int PartOf(uint64_t hash, int partBits)
+{
+    return static_cast<int>((hash >> kPartShift) & ((1u << partBits) - 1u));
+}
+
+// Warp-aggregated increment of counter[part]: lanes with the same part elect one leader that adds
+// the group's size; returns this lane's rank within its group plus the counter's old value.
+__device__ __forceinline__ unsigned int WarpAggAdd(unsigned int *counter, int part, unsigned int active)
+{
+    const unsigned int peers = __match_any_sync(active, part);
+    const int leader = __ffs(peers) - 1;
+    const int lane = threadIdx.x & 31;
+    unsigned int base = 0;
+    if (lane == leader) {
+        base = atomicAdd(&counter[part], static_cast<unsigned int>(__popc(peers)));
+    }
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+template <int kKind>
+__global__ void __launch_bounds__(512) PartHistKernel(const __grid_constant__ AggLaunch p,
+    const __grid_constant__ PartArgs a)
+{
+    __shared__ unsigned int h[kMaxParts];
+    const int nParts = 1 << a.partBits;
+    for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+        h[i] = 0;
+    }
+    __syncthreads();
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        for (int r0 = 0; r0 < tile.rows; r0 += blockDim.x) {
+            const int r = r0 + threadIdx.x;
+            const unsigned int active = __ballot_sync(0xffffffffu, r < tile.rows);
+            if (r < tile.rows) {
+                const RowKey k = ReadKey(p.key, b, static_cast<int64_t>(tile.row0) + r, kKind);
+                WarpAggAdd(h, PartOf(k.hash, a.partBits), active);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+        if (h[i] != 0) {
+            atomicAdd(&a.hist[i], static_cast<unsigned long long>(h[i]));
+        }
+    }
+}
+
+// One block: partition offsets (64-row aligned so every partition's NULL bitmap starts on a
+// byte), the cursors, one batch descriptor per partition and the partitions' tiles.
+__global__ void PartLayoutKernel(const __grid_constant__ PartArgs a)
+{
+    __shared__ unsigned long long offset[kMaxParts];
+    const int nParts = 1 << a.partBits;
+    if (threadIdx.x == 0) {
+        unsigned long long off = 0;
+        int tiles = 0;
+        for (int q = 0; q < nParts; ++q) {
+            offset[q] = off;
+            a.cursor[q] = off;
+            off += (a.hist[q] + 63) / 64 * 64;
+            a.partTileStart[q] = tiles;
+            tiles += static_cast<int>((a.hist[q] + kTileRows - 1) / kTileRows);
+        }
+        a.partTileStart[nParts] = tiles;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nParts; q += blockDim.x) {
+        BatchDesc d;
+        for (int i = 0; i < kMaxInputs; ++i) {
+            d.cols[i] = nullptr;
+            d.nulls[i] = nullptr;
+        }
+        for (int i = 0; i < a.nInputs; ++i) {
+            d.cols[i] = static_cast<char *>(a.cols[i]) + offset[q] * a.width[i];
+            d.nulls[i] = a.nulls[i] != nullptr ? reinterpret_cast<const uint8_t *>(a.nulls[i]) + offset[q] / 8 : nullptr;
+        }
+        d.rows = static_cast<int64_t>(a.hist[q]);
+        d.rowBase = static_cast<int64_t>(offset[q]);
+        a.partBatches[q] = d;
+        const int first = a.partTileStart[q];
+        const int n = a.partTileStart[q + 1] - first;
+        for (int k = 0; k < n && first + k < a.maxTiles; ++k) {
+            TileDesc td;
+            td.batch = q;
+            td.row0 = k * kTileRows;
+            td.rows = static_cast<int32_t>(min(static_cast<unsigned long long>(kTileRows), a.hist[q] - k * kTileRows));
+            td.pad = 0;
+            a.partTiles[first + k] = td;
+        }
+    }
+}
+
+__device__ __forceinline__ void CopyInput(const void *src, int64_t row, void *dst, uint64_t pos, int width)
+{
+    switch (width) {
+        case 1:
+            static_cast<uint8_t *>(dst)[pos] = static_cast<uint8_t>(__ldg(static_cast<const unsigned char *>(src) + row));
+            break;
+        case 2:
+            static_cast<uint16_t *>(dst)[pos] = static_cast<uint16_t>(__ldg(static_cast<const unsigned short *>(src) + row));
+            break;
+        case 4:
+            static_cast<uint32_t *>(dst)[pos] = __ldg(static_cast<const unsigned int *>(src) + row);
+            break;
+        case 8:
+            static_cast<uint64_t *>(dst)[pos] = __ldg(static_cast<const unsigned long long *>(src) + row);
+            break;
+        default: {
+            const ulonglong2 v = __ldg(static_cast<const ulonglong2 *>(src) + row);
+            static_cast<ulonglong2 *>(dst)[pos] = v;
+            break;
+        }
+    }
+}
+
+// Per tile: partition of every row, one cursor reservation per partition, then each row's
+// inputs copied to its partition (rows of a partition from one warp land contiguously).
+constexpr int kScatterThreads = 512;
+constexpr int kScatterRows = kTileRows / kScatterThreads;
+
+template <int kKind>
+__global__ void __launch_bounds__(kScatterThreads) PartScatterKernel(const __grid_constant__ AggLaunch p,
+    const __grid_constant__ PartArgs a)
+{
+    __shared__ unsigned int cnt[kMaxParts];
+    __shared__ unsigned long long base[kMaxParts];
+    const int nParts = 1 << a.partBits;
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+            cnt[i] = 0;
+        }
+        __syncthreads();
+        uint8_t part[kScatterRows];
+#pragma unroll
+        for (int j = 0; j < kScatterRows; ++j) {
+            const int r = j * kScatterThreads + threadIdx.x;
+            const unsigned int active = __ballot_sync(0xffffffffu, r < tile.rows);
+            part[j] = 0;
+            if (r < tile.rows) {
+                const RowKey k = ReadKey(p.key, b, static_cast<int64_t>(tile.row0) + r, kKind);
+                part[j] = static_cast<uint8_t>(PartOf(k.hash, a.partBits));
+                WarpAggAdd(cnt, part[j], active);
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+            base[i] = cnt[i] != 0 ? atomicAdd(&a.cursor[i], static_cast<unsigned long long>(cnt[i])) : 0ull;
+            cnt[i] = 0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kScatterRows; ++j) {
+            const int r = j * kScatterThreads + threadIdx.x;
+            const unsigned int active = __ballot_sync(0xffffffffu, r < tile.rows);
+            if (r < tile.rows) {
+                const int q = part[j];
+                const uint64_t pos = base[q] + WarpAggAdd(cnt, q, active);
+                const int64_t row = static_cast<int64_t>(tile.row0) + r;
+                for (int i = 0; i < a.nInputs; ++i) {
+                    CopyInput(b.cols[i], row, a.cols[i], pos, a.width[i]);
+                    if (a.nulls[i] != nullptr && RowIsNull(b.nulls[i], row)) {
+                        atomicOr(&a.nulls[i][pos >> 5], 1u << (pos & 31));
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ key sketch
+// An evenly strided sample of the rows (across all batches of the launch) is hashed into an
+// open-addressing table of (hash, count); SketchStatsKernel then summarises the counts.
+template <int kKind>
+__global__ void SketchKernel(const __grid_constant__ AggLaunch p, const int64_t *tileOutRow, int64_t totalRows,
+    int32_t nSample, unsigned long long *tabKeys, unsigned int *tabCounts, unsigned long long *stats)
+{
+    const uint32_t mask = kSketchCap - 1;
+    unsigned long long seen = 0, special = 0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nSample; s += gridDim.x * blockDim.x) {
+        const int64_t g = static_cast<int64_t>((static_cast<unsigned long long>(s) * static_cast<unsigned long long>(totalRows)) /
+            static_cast<unsigned long long>(nSample));
+        int lo = 0, hi = p.nTiles - 1;  // last tile whose first row <= g
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tileOutRow[mid] <= g) {
+                lo = mid;
+            } else {
+                hi = mid - 1;
+            }
+        }
+        const TileDesc tile = p.tiles[lo];
+        const int64_t off = g - tileOutRow[lo];
+        if (off < 0 || off >= tile.rows) {
+            continue;
+        }
+        const RowKey k = ReadKey(p.key, p.batches[tile.batch], static_cast<int64_t>(tile.row0) + off, kKind);
+        ++seen;
+        if (k.special >= 0) {
+            ++special;
+            continue;
+        }
+        const unsigned long long h = k.hash == kEmptyKey ? (k.hash ^ 1ull) : k.hash;
+        uint32_t i = static_cast<uint32_t>(h) & mask;
+        for (int probe = 0; probe < kSketchCap; ++probe) {
+            const unsigned long long prev = atomicCAS(&tabKeys[i], kEmptyKey, h);
+            if (prev == kEmptyKey || prev == h) {
+                atomicAdd(&tabCounts[i], 1u);
+                break;
+            }
+            i = (i + 1) & mask;
+        }
+    }
+    atomicAdd(&stats[0], seen);
+    if (special != 0) {
+        atomicAdd(&stats[1], special);
+    }
+}
+
+__global__ void SketchInitKernel(unsigned long long *tabKeys, unsigned int *tabCounts, unsigned long long *stats)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kSketchCap; i += gridDim.x * blockDim.x) {
+        tabKeys[i] = kEmptyKey;
+        tabCounts[i] = 0;
+        if (i < kSketchStats) {
+            stats[i] = 0;
+        }
+    }
+}
+
+__global__ void SketchStatsKernel(const unsigned long long *tabKeys, const unsigned int *tabCounts,
+    unsigned long long *stats)
+{
+    unsigned long long v[7] = {0, 0, 0, 0, 0, 0, 0};  // d, f1, f2, f3, f4-7, f8+, heavy rows
+    unsigned long long mx = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kSketchCap; i += gridDim.x * blockDim.x) {
+        if (tabKeys[i] == kEmptyKey) {
+            continue;
+        }
+        const unsigned int c = tabCounts[i];
+        v[0] += 1;
+        v[1] += c == 1;
+        v[2] += c == 2;
+        v[3] += c == 3;
+        v[4] += (c >= 4 && c < 8);
+        v[5] += c >= 8;
+        v[6] += c >= 8 ? c : 0;
+        mx = c > mx ? c : mx;
+    }
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+        for (int o = 16; o > 0; o >>= 1) {
+            v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long om = __shfl_down_sync(0xffffffffu, mx, o);
+        mx = om > mx ? om : mx;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&stats[2], v[0]);
+        atomicAdd(&stats[3], v[1]);
+        atomicAdd(&stats[4], v[2]);
+        atomicAdd(&stats[5], v[3]);
+        atomicAdd(&stats[6], v[4]);
+        atomicAdd(&stats[7], v[5]);
+        atomicMax(&stats[8], mx);
+        atomicAdd(&stats[9], v[6]);
+    }
+}
+
 int NumSMs()
 {
     static int n = 0;
@@ -1133,6 +1625,25 @@ cudaError_t LaunchAgg(const AggLaunch &p, uint64_t *spill, unsigned int *nSpill,
 {
     SpillArgs sp{spill, nSpill, spillCap, spillIn, nSpillIn};
     const size_t smemBytes = static_cast<size_t>(p.smemSlots) * p.table.slotWords * sizeof(uint64_t);
+    if (p.nParts > 0) {
+        if (smemBytes > kPartSmemBytes) {
+            return cudaErrorInvalidValue;
+        }
+        auto pk = p.key.kind == KEY_SINGLE ? AggPartKernel<KEY_SINGLE> : AggPartKernel<KEY_PACKED>;
+        static bool partConfigured[2] = {false, false};
+        bool &pc = partConfigured[p.key.kind == KEY_SINGLE ? 0 : 1];
+        if (!pc) {
+            cudaError_t err =
+                cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kPartSmemBytes));
+            if (err != cudaSuccess) {
+                return err;
+            }
+            pc = true;
+        }
+        const int perPart = NumSMs() / p.nParts > 0 ? NumSMs() / p.nParts : 1;
+        pk<<<perPart * p.nParts, kPartThreads, smemBytes, stream>>>(p, sp);
+        return cudaGetLastError();
+    }
     auto kernel = p.key.kind == KEY_SINGLE ? AggKernel<KEY_SINGLE> : AggKernel<KEY_PACKED>;
     static size_t configured[2] = {0, 0};
     size_t &conf = configured[p.key.kind == KEY_SINGLE ? 0 : 1];
@@ -1207,5 +1718,47 @@ cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtr
 }
 
 int DeviceSMCount() { return NumSMs(); }
+
+int32_t AggPartSmemSlots(int32_t slotWords)
+{
+    return static_cast<int32_t>(kPartSmemBytes / (static_cast<size_t>(slotWords) * sizeof(uint64_t)));
+}
+
+cudaError_t LaunchAggPartition(const AggLaunch &p, const PartArgs &a, cudaStream_t stream)
+{
+    if (p.nTiles <= 0) {
+        return cudaSuccess;
+    }
+    const int grid = p.nTiles < NumSMs() * 4 ? p.nTiles : NumSMs() * 4;
+    if (p.key.kind == KEY_SINGLE) {
+        PartHistKernel<KEY_SINGLE><<<grid, 512, 0, stream>>>(p, a);
+    } else {
+        PartHistKernel<KEY_PACKED><<<grid, 512, 0, stream>>>(p, a);
+    }
+    PartLayoutKernel<<<1, kMaxParts, 0, stream>>>(a);
+    if (p.key.kind == KEY_SINGLE) {
+        PartScatterKernel<KEY_SINGLE><<<grid, kScatterThreads, 0, stream>>>(p, a);
+    } else {
+        PartScatterKernel<KEY_PACKED><<<grid, kScatterThreads, 0, stream>>>(p, a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggSketch(const AggLaunch &p, const int64_t *tileOutRow, int64_t totalRows, int32_t nSample,
+    unsigned long long *tabKeys, unsigned int *tabCounts, unsigned long long *stats, cudaStream_t stream)
+{
+    if (p.nTiles <= 0 || nSample <= 0) {
+        return cudaSuccess;
+    }
+    SketchInitKernel<<<64, 256, 0, stream>>>(tabKeys, tabCounts, stats);
+    const int blocks = (nSample + 255) / 256;
+    if (p.key.kind == KEY_SINGLE) {
+        SketchKernel<KEY_SINGLE><<<blocks, 256, 0, stream>>>(p, tileOutRow, totalRows, nSample, tabKeys, tabCounts, stats);
+    } else {
+        SketchKernel<KEY_PACKED><<<blocks, 256, 0, stream>>>(p, tileOutRow, totalRows, nSample, tabKeys, tabCounts, stats);
+    }
+    SketchStatsKernel<<<64, 256, 0, stream>>>(tabKeys, tabCounts, stats);
+    return cudaGetLastError();
+}
 
 }  // namespace omg

@@ -100,6 +100,17 @@ __device__ __forceinline__ double LoadAsDouble(const void *col, int64_t row, int
     return static_cast<double>(LoadInt(col, row, width));
 }
 
+__device__ __forceinline__ double LoadAsDoubleRO(const void *col, int64_t row, int inKind, int width)
+{
+    if (inKind == IN_DOUBLE) {
+        return __ldg(static_cast<const double *>(col) + row);
+    }
+    if (inKind == IN_FLOAT) {
+        return static_cast<double>(__ldg(static_cast<const float *>(col) + row));
+    }
+    return static_cast<double>(SignExtend(LoadBitsRO(col, row, width), width));
+}
+
 // Order-preserving map of a non-NaN double onto int64 (-0.0 sorts just below +0.0).
 __device__ __forceinline__ int64_t OrderedFromDouble(double x)
 {

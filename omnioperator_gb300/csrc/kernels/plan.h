@@ -151,7 +151,39 @@ struct AggLaunch {
     int32_t smemSlots;  // per-CTA shared-memory pre-aggregation slots (0 = off)
     int32_t *error;     // sticky device error code (0 = none)
     long long waitBudget;  // clock64 ticks a thread may wait for another's slot publication
+    // Partitioned launches (nParts > 0): the batches are hash partitions, tiles
+    // [partTileStart[q], partTileStart[q + 1]) belong to partition q, and CTA c works on
+    // partition c % nParts only, so its shared table sees only that partition's groups.
+    int32_t nParts;
+    const int32_t *partTileStart;
 };
+
+// ---- hash partitioning of aggregation input -------------------------------------------------
+// Rows go to partition (hash >> kPartShift) & (nParts - 1); the shared tables index slots with
+// the hash's top 32 bits and the global table with its low bits, so the three are independent.
+constexpr int kPartShift = 24;
+constexpr int kMaxParts = 64;
+
+struct PartArgs {
+    int32_t partBits;                  // nParts = 1 << partBits
+    int32_t nInputs;                   // kernel inputs copied into the partitions
+    int32_t width[kMaxInputs];         // bytes per value (1, 2, 4, 8, 16)
+    void *cols[kMaxInputs];            // partitioned values, rows + kMaxParts * 64 rows each
+    uint32_t *nulls[kMaxInputs];       // partitioned NULL bitmaps (zeroed) or nullptr
+    unsigned long long *hist;          // [nParts] rows per partition
+    unsigned long long *cursor;        // [nParts] next free row of each partition
+    BatchDesc *partBatches;            // [nParts] one batch per partition
+    TileDesc *partTiles;               // [maxTiles]
+    int32_t *partTileStart;            // [nParts + 1]
+    int32_t maxTiles;
+};
+
+// ---- key sketch of a row sample (feeds the group-count estimate) ----------------------------
+constexpr int kSketchCap = 1 << 17;  // sketch table slots (sample <= kSketchCap / 2 rows)
+constexpr int kSketchStats = 16;
+// stats: [0] sampled rows, [1] special-key rows (NULL / EMPTY key), [2] distinct hashes d,
+// [3] f1 (hashes seen once), [4] f2, [5] f3, [6] hashes seen 4-7 times, [7] 8+ times,
+// [8] largest count, [9] rows held by hashes seen 8+ times.
 
 // Default bounded-wait budget (clock64 ticks, about two seconds at 2 GHz).
 constexpr long long kDefaultWaitBudget = 1ll << 32;

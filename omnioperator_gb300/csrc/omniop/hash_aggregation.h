@@ -14,8 +14,14 @@
 #include <memory>
 #include <vector>
 
+#include <cuda_runtime_api.h>
+
 #include "kernels/plan.h"
 #include "operator.h"
+
+namespace omg {
+class BatchTable;
+}
 
 namespace omg {
 class OpStream;
@@ -29,6 +35,7 @@ namespace op {
 // and output columns.
 struct AggPlan {
     std::vector<int32_t> inputCols;        // batch column of each kernel input
+    std::vector<int32_t> inputWidths;      // value bytes of each kernel input
     omg::KeySpec key{};
     std::vector<omg::AccSpec> accs;
     std::vector<int16_t> regInput;         // kernel inputs cached in registers per row
@@ -91,8 +98,16 @@ public:
         capacityHint_ = capacityHint;
     }
 
+    // Sizing record of the first flush: [0] rows flushed, [1..kSketchStats] the key sketch of a
+    // row sample, then the group estimate used, the partition bits (-1 = global table) and the
+    // group count so far.  Returns the number of values written.
+    int32_t GetSizingLog(int64_t *out, int32_t n) const;
+
 private:
     struct Impl;
+    struct PartBuffers;
+    void Decide(omg::BatchTable &bt, cudaStream_t s);
+    void Partition(omg::BatchTable &bt, omg::AggLaunch &p, PartBuffers &pb, cudaStream_t s);
     void Flush();
     void Extract();
     void ReleasePending();

@@ -54,6 +54,7 @@ def run_agg(group_cols, group_types, aggs_cols, agg_in_types, agg_out_types, fun
             cols = c if cols is None else [(np.concatenate([a[0], x[0]]), np.concatenate([a[1], x[1]]))
                                            for a, x in zip(cols, c)]
         counters = op.counters()
+        counters["sizing"] = op.sizing_log()
     finally:
         op.delete()
         fac.close()

@@ -313,3 +313,59 @@ def test_no_input_and_empty_batches(gpu):
 def test_pipeline_mode_many_small_batches(gpu):
     key, v1, v2, km, m1, m2 = _uniform_case(120_000, 2_000, 14)
     _check_cfg1(key, v1, v2, km, m1, m2, batch_sizes=(1, 17, 300, 4096), pipeline=True)
+
+
+# ---- partitioned strategy: hash partitions, one shared-memory table per partition
+
+
+def test_partitioned_auto_on_uniform_config1_shape(gpu):
+    # AUTO sizes from the sketch (10,000 groups) and picks several partitions.
+    key, v1, v2, km, m1, m2 = _uniform_case(1_000_000, 10_000, 21)
+    ctr = _check_cfg1(key, v1, v2, km, m1, m2, batch_sizes=(1_000_000,))
+    sz = ctr["sizing"]
+    assert sz["part_bits"] >= 1, sz
+    assert 8_000 <= sz["estimate"] <= 12_500, sz
+    assert ctr["resizes"] == 0
+
+
+def test_partitioned_forced_with_nulls_and_ragged_batches(gpu):
+    key, v1, v2, km, m1, m2 = _uniform_case(400_000, 3_000, 22, nulls=0.02, key_nulls=0.01)
+    ctr = _check_cfg1(key, v1, v2, km, m1, m2, strategy=omg.AGG_STRATEGY_PARTITIONED,
+                      batch_sizes=(4096, 1000, 777, 65536))
+    assert ctr["sizing"]["part_bits"] >= 0
+
+
+@pytest.mark.parametrize("hint", [100, 20_000])
+def test_partitioned_underestimate_falls_back_to_global(gpu, hint):
+    # The estimate (capacity hint) is far below the real 200,000 groups: the shared tables
+    # overflow into the global table, which grows; the result stays exact.
+    key, v1, v2, km, m1, m2 = _uniform_case(600_000, 200_000, 23)
+    ctr = _check_cfg1(key, v1, v2, km, m1, m2, strategy=omg.AGG_STRATEGY_PARTITIONED, capacity_hint=hint,
+                      batch_sizes=(600_000,))
+    assert ctr["resizes"] >= 1
+    assert ctr["sizing"]["estimate"] == hint
+
+
+def test_partitioned_composite_key_decimal_count_all_avg(gpu):
+    rng = np.random.default_rng(24)
+    n = 500_000
+    pairs = rng.integers(0, 20_000, n)
+    k1 = (pairs % 97).astype(np.int32)
+    k2 = (pairs * 2654435761 % 1000003).astype(np.int64)
+    km1 = rng.random(n) < 0.005
+    dec = rng.integers(-10**9, 10**9, n, dtype=np.int64)
+    dm = rng.random(n) < 0.02
+    v = rng.standard_normal(n)
+    vm = rng.random(n) < 0.02
+    d64 = omg.Decimal64Type(18, 2)
+    d128 = omg.Decimal128Type(38, 2)
+    cols, ctr = run_agg([0, 1], [I, L], [[2], [], [3]], [[d64], [], [D]], [[d128], [L], [D]], [SUM, CALL, AVG],
+                        [k1, k2, dec, v], [I, L, d64, D], nulls=[km1, None, dm, vm],
+                        strategy=omg.AGG_STRATEGY_PARTITIONED, batch_sizes=(65536,))
+    assert ctr["sizing"]["part_bits"] >= 1
+    ora = oracle.hashagg([k1, k2], [oracle.T_INT, oracle.T_LONG], [km1, None],
+                         [dict(func=oracle.F_SUM, col=dec, in_type=oracle.T_DEC64, out_type=oracle.T_DEC128, nulls=dm),
+                          dict(func=oracle.F_COUNT_ALL, col=None, out_type=oracle.T_LONG),
+                          dict(func=oracle.F_AVG, col=v, in_type=oracle.T_DOUBLE, out_type=oracle.T_DOUBLE, nulls=vm)])
+    ex_a = exact_by_key([k1, k2], [km1, None], v, ~vm, divide_by_count=True)
+    assert_agg_equal(cols, ora, 2, double_aggs=(2,), exact={2: ex_a})
