@@ -207,9 +207,37 @@ int32_t omg_batch_free_many(void *const *batches, int32_t n);
  * flush, [1..16] the key sketch of a row sample of that flush (sampled rows, special-key rows,
  * distinct hashes, frequency classes f1, f2, f3, f4-7, f8+, largest count, rows of the 8+
  * class, 6 reserved), [17] the group estimate used for sizing, [18] the partition bits of the
- * partitioned strategy (-1 = global table), [19] the group count so far.  `*written` receives
+ * partitioned strategy (-1 = global table), [19] the group count so far, [20] the plain
+ * (sketch) estimate, [21] 1 if a sizing model made the estimate used.  `*written` receives
  * the number of values stored (at most n). */
 int32_t omg_op_get_sizing_log(void *op, int64_t *out, int32_t n, int32_t *written);
+/* ---- learned sizing model (no reference counterpart) ---------------------------------
+ * A small fully connected network (ReLU hidden layers, one output) that maps the features of a
+ * sizing record (omg_op_get_sizing_log) to a group-count estimate.  Parameters live in HBM;
+ * forward, backward and Adam run as CUDA kernels.  dims = {12, hidden..., 1}.  Host arrays:
+ * X is n x dims[0] row-major, T and Y have n entries, parameters are the layers' W (dims[l] x
+ * dims[l+1], row-major) and b in layer order. */
+int32_t omg_sizer_create(const int32_t *dims, int32_t n_dims, uint64_t seed, void **out_model);
+int32_t omg_sizer_destroy(void *model);
+int32_t omg_sizer_num_params(void *model, int64_t *n_params);
+int32_t omg_sizer_get_params(void *model, float *params, int64_t n_params);
+int32_t omg_sizer_set_params(void *model, const float *params, int64_t n_params);
+int32_t omg_sizer_predict(void *model, const float *X, int32_t n, float *Y);
+/* Gradient of the mean squared error over the batch; *loss receives the loss. */
+int32_t omg_sizer_gradients(void *model, const float *X, const float *T, int32_t n, float *grad, float *loss);
+/* `epochs` full-batch Adam steps at learning rate lr; *loss receives the loss of the last step. */
+int32_t omg_sizer_train(void *model, const float *X, const float *T, int32_t n, int32_t epochs, float lr,
+    float *loss);
+/* Feature vector (12 floats) of a sizing record of n_log >= 17 values; the training target of a
+ * record whose true group count is `groups`; the estimate of a model output y. */
+int32_t omg_sizer_features(const int64_t *sizing_log, int32_t n_log, float *features);
+int32_t omg_sizer_target(const int64_t *sizing_log, int32_t n_log, int64_t groups, float *target);
+int32_t omg_sizer_estimate(const int64_t *sizing_log, int32_t n_log, float y, int64_t *estimate);
+/* Attach a model to a HashAggregation factory: operators created afterwards size their table
+ * and choose their strategy from the model's estimate instead of the plain sketch estimate
+ * (the exact resize path still corrects any misprediction).  NULL detaches.  The model must
+ * outlive those operators. */
+int32_t omg_hashagg_factory_set_sizer(void *factory, void *model);
 /* Operator::GetStatus (operator.h:46-49): OMG_STATUS_*. */
 int32_t omg_op_status(void *op);
 /* Operator::noMoreInput / setNoMoreInput / needsInput (operator.h:117-130). */

@@ -61,6 +61,20 @@ _SIGS = {
     "omg_op_get_outputs": (I32, [P, C.POINTER(P), I32, C.POINTER(I32), C.POINTER(I64)]),
     "omg_batch_free_many": (I32, [C.POINTER(P), I32]),
     "omg_op_get_sizing_log": (I32, [P, C.POINTER(I64), I32, C.POINTER(I32)]),
+    "omg_sizer_create": (I32, [C.POINTER(I32), I32, C.c_uint64, C.POINTER(P)]),
+    "omg_sizer_destroy": (I32, [P]),
+    "omg_sizer_num_params": (I32, [P, C.POINTER(I64)]),
+    "omg_sizer_get_params": (I32, [P, C.POINTER(C.c_float), I64]),
+    "omg_sizer_set_params": (I32, [P, C.POINTER(C.c_float), I64]),
+    "omg_sizer_predict": (I32, [P, C.POINTER(C.c_float), I32, C.POINTER(C.c_float)]),
+    "omg_sizer_gradients": (I32, [P, C.POINTER(C.c_float), C.POINTER(C.c_float), I32, C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)]),
+    "omg_sizer_train": (I32, [P, C.POINTER(C.c_float), C.POINTER(C.c_float), I32, I32, C.c_float,
+                              C.POINTER(C.c_float)]),
+    "omg_sizer_features": (I32, [C.POINTER(I64), I32, C.POINTER(C.c_float)]),
+    "omg_sizer_target": (I32, [C.POINTER(I64), I32, I64, C.POINTER(C.c_float)]),
+    "omg_sizer_estimate": (I32, [C.POINTER(I64), I32, C.c_float, C.POINTER(I64)]),
+    "omg_hashagg_factory_set_sizer": (I32, [P, P]),
     "omg_op_status": (I32, [P]),
     "omg_op_no_more_input": (I32, [P]),
     "omg_op_set_no_more_input": (I32, [P, I32]),

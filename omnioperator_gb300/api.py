@@ -257,7 +257,8 @@ class Operator:
         n = C.c_int32(0)
         check(lib().omg_op_get_sizing_log(self.handle, arr, 32, C.byref(n)))
         v = list(arr[: n.value])
-        return {"rows": v[0], "sketch": v[1:17], "estimate": v[17], "part_bits": v[18], "groups": v[19]}
+        return {"rows": v[0], "sketch": v[1:17], "estimate": v[17], "part_bits": v[18], "groups": v[19],
+                "plain_estimate": v[20], "learned": bool(v[21]), "raw": v}
 
     def get_status(self) -> int:
         return lib().omg_op_status(self.handle)
@@ -352,6 +353,13 @@ class HashAggregationOperatorFactory(OperatorFactory):
             (C.c_uint8 * max(n_agg, 1))(*raws), (C.c_uint8 * max(n_agg, 1))(*partials),
             1 if overflow_as_null else 0, C.byref(out)))
         super().__init__(out.value)
+        self._sizer = None
+
+    def set_sizer(self, model) -> None:
+        """Size the operators created afterwards with a learned model (sizer.SizingModel), or
+        the plain sketch estimate when `model` is None."""
+        check(lib().omg_hashagg_factory_set_sizer(self.handle, None if model is None else model.handle))
+        self._sizer = model  # keep the model alive while the factory may use it
 
 
 class HashBuilderOperatorFactory(OperatorFactory):

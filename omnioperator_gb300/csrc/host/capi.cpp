@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "host/gpu_runtime.h"
+#include "host/sizer.h"
 #include "kernels/agg_noalloc.h"
 #include "omniop/hash_aggregation.h"
 #include "omniop/hash_join.h"
@@ -420,6 +421,121 @@ int32_t omg_op_get_sizing_log(void *op, int64_t *out, int32_t n, int32_t *writte
         Require(agg != nullptr, "not a HashAggregation operator");
         Require(out != nullptr && n >= 0 && written != nullptr, "null output");
         *written = agg->GetSizingLog(out, n);
+    });
+}
+
+// ---- learned sizing model
+namespace {
+omg::SizingModel *AsSizer(void *m)
+{
+    Require(m != nullptr, "null model");
+    return static_cast<omg::SizingModel *>(m);
+}
+}  // namespace
+
+int32_t omg_sizer_create(const int32_t *dims, int32_t n_dims, uint64_t seed, void **out_model)
+{
+    return Guard([&] {
+        Require(dims != nullptr && n_dims >= 2 && n_dims <= 16 && out_model != nullptr, "bad model dims");
+        *out_model = new omg::SizingModel(std::vector<int32_t>(dims, dims + n_dims), seed);
+    });
+}
+
+int32_t omg_sizer_destroy(void *model)
+{
+    return Guard([&] { delete static_cast<omg::SizingModel *>(model); });
+}
+
+int32_t omg_sizer_num_params(void *model, int64_t *n_params)
+{
+    return Guard([&] {
+        Require(n_params != nullptr, "null output");
+        *n_params = AsSizer(model)->NumParams();
+    });
+}
+
+int32_t omg_sizer_get_params(void *model, float *params, int64_t n_params)
+{
+    return Guard([&] {
+        omg::SizingModel *m = AsSizer(model);
+        Require(params != nullptr && n_params == m->NumParams(), "parameter count mismatch");
+        m->GetParams(params);
+    });
+}
+
+int32_t omg_sizer_set_params(void *model, const float *params, int64_t n_params)
+{
+    return Guard([&] {
+        omg::SizingModel *m = AsSizer(model);
+        Require(params != nullptr && n_params == m->NumParams(), "parameter count mismatch");
+        m->SetParams(params);
+    });
+}
+
+int32_t omg_sizer_predict(void *model, const float *X, int32_t n, float *Y)
+{
+    return Guard([&] {
+        Require(n >= 0 && (n == 0 || (X != nullptr && Y != nullptr)), "null array");
+        AsSizer(model)->Predict(X, n, Y);
+    });
+}
+
+int32_t omg_sizer_gradients(void *model, const float *X, const float *T, int32_t n, float *grad, float *loss)
+{
+    return Guard([&] {
+        Require(n > 0 && X != nullptr && T != nullptr && grad != nullptr, "null array");
+        const float l = AsSizer(model)->Gradients(X, T, n, grad);
+        if (loss != nullptr) {
+            *loss = l;
+        }
+    });
+}
+
+int32_t omg_sizer_train(void *model, const float *X, const float *T, int32_t n, int32_t epochs, float lr,
+    float *loss)
+{
+    return Guard([&] {
+        Require(n > 0 && X != nullptr && T != nullptr && epochs > 0 && lr > 0.f, "bad training arguments");
+        const float l = AsSizer(model)->Train(X, T, n, epochs, lr);
+        if (loss != nullptr) {
+            *loss = l;
+        }
+    });
+}
+
+int32_t omg_sizer_features(const int64_t *sizing_log, int32_t n_log, float *features)
+{
+    return Guard([&] {
+        Require(sizing_log != nullptr && n_log >= 1 + omg::kSketchStats && features != nullptr, "bad sizing log");
+        omg::SizerFeatures(sizing_log, features);
+    });
+}
+
+int32_t omg_sizer_target(const int64_t *sizing_log, int32_t n_log, int64_t groups, float *target)
+{
+    return Guard([&] {
+        Require(sizing_log != nullptr && n_log >= 1 + omg::kSketchStats && target != nullptr, "bad sizing log");
+        *target = omg::SizerTarget(sizing_log, groups);
+    });
+}
+
+int32_t omg_sizer_estimate(const int64_t *sizing_log, int32_t n_log, float y, int64_t *estimate)
+{
+    return Guard([&] {
+        Require(sizing_log != nullptr && n_log >= 1 + omg::kSketchStats && estimate != nullptr, "bad sizing log");
+        *estimate = static_cast<int64_t>(omg::SizerEstimate(sizing_log, y));
+    });
+}
+
+int32_t omg_hashagg_factory_set_sizer(void *factory, void *model)
+{
+    return Guard([&] {
+        auto *f = dynamic_cast<HashAggregationOperatorFactory *>(static_cast<OperatorFactory *>(factory));
+        Require(f != nullptr, "not a HashAggregation factory");
+        if (model != nullptr) {
+            Require(AsSizer(model)->Dims()[0] == omg::kSizerFeatures, "model input width must be 12");
+        }
+        f->SetSizer(static_cast<omg::SizingModel *>(model));
     });
 }
 

@@ -17,6 +17,7 @@
 #include <map>
 
 #include "host/gpu_runtime.h"
+#include "host/sizer.h"
 #include "kernels/launch.h"
 
 namespace omniruntime {
@@ -395,7 +396,7 @@ OmniStatus HashAggregationOperatorFactory::Init()
 Operator *HashAggregationOperatorFactory::CreateOperator()
 {
     Init();
-    return new HashAggregationOperator(plan_);
+    return new HashAggregationOperator(plan_, sizer_);
 }
 
 // ------------------------------------------------------------------------------ operator
@@ -416,10 +417,14 @@ struct HashAggregationOperator::Impl {
     unsigned long long sketch[omg::kSketchStats] = {};
     int64_t sketchRows = 0;  // rows of the flush the sketch sampled
     uint64_t estimate = 0;
+    uint64_t plainEstimate = 0;
+    bool learned = false;
     int32_t partBits = -1;
 };
 
-HashAggregationOperator::HashAggregationOperator(const AggPlan &plan) : plan_(plan), impl_(new Impl()) {}
+HashAggregationOperator::HashAggregationOperator(const AggPlan &plan, omg::SizingModel *sizer)
+    : plan_(plan), impl_(new Impl()), sizer_(sizer)
+{}
 
 HashAggregationOperator::~HashAggregationOperator()
 {
@@ -551,6 +556,8 @@ int32_t HashAggregationOperator::GetSizingLog(int64_t *out, int32_t n) const
     v.push_back(static_cast<int64_t>(im.estimate));
     v.push_back(im.partBits);
     v.push_back(static_cast<int64_t>(std::max<uint64_t>(im.groups, uniqueKeys_)));
+    v.push_back(static_cast<int64_t>(im.plainEstimate));
+    v.push_back(im.learned ? 1 : 0);
     const int32_t m = std::min<int32_t>(n, static_cast<int32_t>(v.size()));
     for (int32_t i = 0; i < m; ++i) {
         out[i] = v[i];
@@ -574,13 +581,26 @@ void HashAggregationOperator::Decide(omg::BatchTable &bt, cudaStream_t s)
         p.tiles = bt.DeviceTiles();
         p.nTiles = bt.NumTiles();
         const int32_t n = static_cast<int32_t>(std::min<int64_t>(rows, kSketchSample));
-        CudaCheck(omg::LaunchAggSketch(p, bt.DeviceTileOutRows(), rows, n, tabKeys.Get(), tabCounts.Get(), st.Get(), s),
-            "key sketch");
+        CudaCheck(omg::LaunchAggSketch(p, n, tabKeys.Get(), tabCounts.Get(), st.Get(), s), "key sketch");
         ++counters_[0];
         CudaCheck(cudaMemcpyAsync(im.sketch, st.Get(), sizeof(im.sketch), cudaMemcpyDeviceToHost, s), "read sketch");
         im.stream.Sync();
         im.sketchRows = rows;
-        im.estimate = EstimateGroups(im.sketch, rows);
+        im.plainEstimate = EstimateGroups(im.sketch, rows);
+        im.estimate = im.plainEstimate;
+        if (sizer_ != nullptr && sizer_->Dims()[0] == omg::kSizerFeatures) {
+            int64_t log[1 + omg::kSketchStats];
+            log[0] = rows;
+            for (int i = 0; i < omg::kSketchStats; ++i) {
+                log[1 + i] = static_cast<int64_t>(im.sketch[i]);
+            }
+            float x[omg::kSizerFeatures];
+            float y = 0.f;
+            omg::SizerFeatures(log, x);
+            sizer_->Predict(x, 1, &y);
+            im.estimate = omg::SizerEstimate(log, y);
+            im.learned = true;
+        }
     }
     // Partitions: enough that one partition's groups fill a CTA's shared table to kPartLoad.
     const bool wantPart = strategy_ == 3 || (strategy_ == 0 && rows >= kSketchMinRows);

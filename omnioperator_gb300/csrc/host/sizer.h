@@ -1,0 +1,64 @@
+// Learned sizing model: a small fully connected network that maps the key sketch an aggregation
+// operator takes of its first flush to a group-count estimate.  Its parameters live in HBM and
+// it is trained and evaluated by the kernels of kernels/mlp.cu.
+#pragma once
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "host/gpu_runtime.h"
+
+namespace omg {
+
+// Features of a sizing record (the layout written by HashAggregationOperator::GetSizingLog):
+// scale-free functions of the rows N, the sampled rows n, the distinct hashes d of the sample,
+// its frequency classes and the plain estimate.
+constexpr int kSizerFeatures = 12;
+void SizerFeatures(const int64_t *log, float *features);
+// Estimate from the model output y: d * 2^(16 y), clamped to [d, N].
+uint64_t SizerEstimate(const int64_t *log, float y);
+// Target of a sizing record with known group count G: log2(G / d) / 16.
+float SizerTarget(const int64_t *log, int64_t groups);
+
+class SizingModel {
+public:
+    // dims: input width, hidden widths..., 1.  Weights: He-uniform from `seed`, biases zero.
+    SizingModel(const std::vector<int32_t> &dims, uint64_t seed);
+    ~SizingModel();
+    SizingModel(const SizingModel &) = delete;
+    SizingModel &operator=(const SizingModel &) = delete;
+
+    int64_t NumParams() const { return nParams_; }
+    const std::vector<int32_t> &Dims() const { return dims_; }
+    void GetParams(float *out);
+    void SetParams(const float *in);
+    // Y[n] = model(X[n, dims[0]]); host pointers.
+    void Predict(const float *X, int32_t n, float *Y);
+    // Gradient of the mean squared error over the batch w.r.t. every parameter (layout as
+    // GetParams); returns the loss.
+    float Gradients(const float *X, const float *T, int32_t n, float *grad);
+    // `epochs` full-batch Adam steps; returns the loss before the last step.
+    float Train(const float *X, const float *T, int32_t n, int32_t epochs, float lr);
+
+private:
+    void Forward(int32_t n);
+    float Backward(int32_t n);
+    void Upload(const float *X, const float *T, int32_t n);
+
+    std::vector<int32_t> dims_;
+    std::vector<int64_t> wOff_, bOff_;  // offsets of each layer's W and b in the parameter vector
+    int64_t nParams_ = 0;
+    std::mutex mu_;
+    cudaStream_t stream_ = nullptr;
+    DevArray<float> params_, grads_, adamM_, adamV_;
+    DevArray<float> x_, t_, loss_;
+    std::vector<DevArray<float>> act_;   // activations per layer output
+    std::vector<DevArray<float>> dact_;  // their gradients
+    int32_t capacity_ = 0;
+    int32_t step_ = 0;
+};
+
+}  // namespace omg

@@ -1478,31 +1478,22 @@ __global__ void __launch_bounds__(kScatterThreads) PartScatterKernel(const __gri
 }
 
 // ------------------------------------------------------------------ key sketch
-// An evenly strided sample of the rows (across all batches of the launch) is hashed into an
-// open-addressing table of (hash, count); SketchStatsKernel then summarises the counts.
+// A sample of the rows, stratified over the tiles of the launch (sample s reads a hashed row of
+// tile s * nTiles / nSample), is hashed into an open-addressing table of (hash, count);
+// SketchStatsKernel then summarises the counts.
 template <int kKind>
-__global__ void SketchKernel(const __grid_constant__ AggLaunch p, const int64_t *tileOutRow, int64_t totalRows,
-    int32_t nSample, unsigned long long *tabKeys, unsigned int *tabCounts, unsigned long long *stats)
+__global__ void SketchKernel(const __grid_constant__ AggLaunch p, int32_t nSample, unsigned long long *tabKeys,
+    unsigned int *tabCounts, unsigned long long *stats)
 {
     const uint32_t mask = kSketchCap - 1;
     unsigned long long seen = 0, special = 0;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nSample; s += gridDim.x * blockDim.x) {
-        const int64_t g = static_cast<int64_t>((static_cast<unsigned long long>(s) * static_cast<unsigned long long>(totalRows)) /
-            static_cast<unsigned long long>(nSample));
-        int lo = 0, hi = p.nTiles - 1;  // last tile whose first row <= g
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (tileOutRow[mid] <= g) {
-                lo = mid;
-            } else {
-                hi = mid - 1;
-            }
-        }
-        const TileDesc tile = p.tiles[lo];
-        const int64_t off = g - tileOutRow[lo];
-        if (off < 0 || off >= tile.rows) {
+        const int t = static_cast<int>((static_cast<int64_t>(s) * p.nTiles) / nSample);
+        const TileDesc tile = p.tiles[t];
+        if (tile.rows <= 0) {
             continue;
         }
+        const int off = static_cast<int>(Mix64(static_cast<uint64_t>(s)) % static_cast<uint64_t>(tile.rows));
         const RowKey k = ReadKey(p.key, p.batches[tile.batch], static_cast<int64_t>(tile.row0) + off, kKind);
         ++seen;
         if (k.special >= 0) {
@@ -1520,9 +1511,15 @@ __global__ void SketchKernel(const __grid_constant__ AggLaunch p, const int64_t 
             i = (i + 1) & mask;
         }
     }
-    atomicAdd(&stats[0], seen);
-    if (special != 0) {
-        atomicAdd(&stats[1], special);
+    for (int o = 16; o > 0; o >>= 1) {
+        seen += __shfl_down_sync(0xffffffffu, seen, o);
+        special += __shfl_down_sync(0xffffffffu, special, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&stats[0], seen);
+        if (special != 0) {
+            atomicAdd(&stats[1], special);
+        }
     }
 }
 
@@ -1744,8 +1741,8 @@ cudaError_t LaunchAggPartition(const AggLaunch &p, const PartArgs &a, cudaStream
     return cudaGetLastError();
 }
 
-cudaError_t LaunchAggSketch(const AggLaunch &p, const int64_t *tileOutRow, int64_t totalRows, int32_t nSample,
-    unsigned long long *tabKeys, unsigned int *tabCounts, unsigned long long *stats, cudaStream_t stream)
+cudaError_t LaunchAggSketch(const AggLaunch &p, int32_t nSample, unsigned long long *tabKeys,
+    unsigned int *tabCounts, unsigned long long *stats, cudaStream_t stream)
 {
     if (p.nTiles <= 0 || nSample <= 0) {
         return cudaSuccess;
@@ -1753,9 +1750,9 @@ cudaError_t LaunchAggSketch(const AggLaunch &p, const int64_t *tileOutRow, int64
     SketchInitKernel<<<64, 256, 0, stream>>>(tabKeys, tabCounts, stats);
     const int blocks = (nSample + 255) / 256;
     if (p.key.kind == KEY_SINGLE) {
-        SketchKernel<KEY_SINGLE><<<blocks, 256, 0, stream>>>(p, tileOutRow, totalRows, nSample, tabKeys, tabCounts, stats);
+        SketchKernel<KEY_SINGLE><<<blocks, 256, 0, stream>>>(p, nSample, tabKeys, tabCounts, stats);
     } else {
-        SketchKernel<KEY_PACKED><<<blocks, 256, 0, stream>>>(p, tileOutRow, totalRows, nSample, tabKeys, tabCounts, stats);
+        SketchKernel<KEY_PACKED><<<blocks, 256, 0, stream>>>(p, nSample, tabKeys, tabCounts, stats);
     }
     SketchStatsKernel<<<64, 256, 0, stream>>>(tabKeys, tabCounts, stats);
     return cudaGetLastError();

@@ -19,11 +19,10 @@ cudaError_t LaunchAgg(const AggLaunch &p, uint64_t *spill, unsigned int *nSpill,
 // (histogram, layout, scatter) over p's batches into a's buffers; a.hist must be zero.
 int32_t AggPartSmemSlots(int32_t slotWords);
 cudaError_t LaunchAggPartition(const AggLaunch &p, const PartArgs &a, cudaStream_t stream);
-// Key sketch of nSample rows spread evenly over p's tiles (tileOutRow: first row of each tile in
-// arrival order); stats as described at kSketchStats.  tabKeys / tabCounts hold kSketchCap
-// entries.
-cudaError_t LaunchAggSketch(const AggLaunch &p, const int64_t *tileOutRow, int64_t totalRows, int32_t nSample,
-    unsigned long long *tabKeys, unsigned int *tabCounts, unsigned long long *stats, cudaStream_t stream);
+// Key sketch of nSample rows stratified over p's tiles; stats as described at kSketchStats.
+// tabKeys / tabCounts hold kSketchCap entries.
+cudaError_t LaunchAggSketch(const AggLaunch &p, int32_t nSample, unsigned long long *tabKeys,
+    unsigned int *tabCounts, unsigned long long *stats, cudaStream_t stream);
 cudaError_t LaunchAggCount(const AggTable &t, int keyKind, unsigned long long *out, cudaStream_t stream);
 cudaError_t LaunchAggExtract(const AggExtract &e, cudaStream_t stream);
 // Ordered replay of order-dependent sticky-overflow groups; sets forced[slot] bit k when

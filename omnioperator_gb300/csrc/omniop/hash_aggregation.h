@@ -21,6 +21,7 @@
 
 namespace omg {
 class BatchTable;
+class SizingModel;
 }
 
 namespace omg {
@@ -64,6 +65,9 @@ public:
     OmniStatus Init();
     Operator *CreateOperator() override;
     const AggPlan &Plan() const { return plan_; }
+    // Learned sizing model consulted by the operators created afterwards (nullptr: the plain
+    // estimate).  The model must outlive those operators.
+    void SetSizer(omg::SizingModel *sizer) { sizer_ = sizer; }
 
 private:
     std::vector<uint32_t> groupByCols_;
@@ -79,11 +83,12 @@ private:
     SupportContainerVecRule policy_;
     AggPlan plan_;
     bool inited_ = false;
+    omg::SizingModel *sizer_ = nullptr;
 };
 
 class HashAggregationOperator : public Operator {
 public:
-    explicit HashAggregationOperator(const AggPlan &plan);
+    explicit HashAggregationOperator(const AggPlan &plan, omg::SizingModel *sizer = nullptr);
     ~HashAggregationOperator() override;
 
     int32_t AddInput(VectorBatch *vecBatch) override;
@@ -99,8 +104,9 @@ public:
     }
 
     // Sizing record of the first flush: [0] rows flushed, [1..kSketchStats] the key sketch of a
-    // row sample, then the group estimate used, the partition bits (-1 = global table) and the
-    // group count so far.  Returns the number of values written.
+    // row sample, then the group estimate used, the partition bits (-1 = global table), the
+    // group count so far, the plain (sketch) estimate and whether a sizing model made the
+    // estimate used.  Returns the number of values written.
     int32_t GetSizingLog(int64_t *out, int32_t n) const;
 
 private:
@@ -122,6 +128,7 @@ private:
     uint64_t uniqueKeys_ = 0;
     int32_t strategy_ = 0;
     int64_t capacityHint_ = 0;
+    omg::SizingModel *sizer_ = nullptr;
 };
 
 }  // namespace op
