@@ -311,7 +311,7 @@ def run_gpu(args, rank, world):
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                 "traffic": None if traffic_per_row is None else traffic_per_row * N_PROBE,
-                "kernel": "ProbeKernel", "kernel_ms": round(kernel_s * 1e3, 4),
+                "kernel": "ProbeBitsKernel", "kernel_ms": round(kernel_s * 1e3, 4),
                 "algorithmic_bytes": int(alg_bytes)}
 
     e2e = None if args.skip_e2e else run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank)
@@ -426,13 +426,15 @@ def run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world):
     kernel_s = kern_ns / args.steps / 1e9
     alg = AGG_ROWS * 24 + AGG_GROUPS * 56
     peak, kind = measured_peak_gbs()
+    traffic_per_row = profiled_traffic("agg_partitioned_kernel_agg2e22.md")
     fac.close()
     return {"value": world * AGG_ROWS / (ms / 1e3), "unit": "rows/s", "ms_per_step": ms, "gpu_launches": launches,
             "workload": "hash aggregation: 2^22 rows, int64 key over 10,000 values, SUM/COUNT/MIN/MAX(int64), "
                         "SUM/AVG(double); input resident in HBM, L2 flushed between steps",
             "roofline": {"bound": "hbm", "achieved": round(alg / kernel_s / 1e9, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(alg / kernel_s / 1e9 / peak, 4), "peak_kind": kind,
-                         "traffic": None, "kernel": "AggKernel", "kernel_ms": round(kernel_s * 1e3, 4),
+                         "traffic": None if traffic_per_row is None else round(traffic_per_row * AGG_ROWS),
+                         "kernel": "AggPartKernel", "kernel_ms": round(kernel_s * 1e3, 4),
                          "algorithmic_bytes": alg}}
 
 

@@ -258,7 +258,7 @@ class Operator:
         check(lib().omg_op_get_sizing_log(self.handle, arr, 32, C.byref(n)))
         v = list(arr[: n.value])
         return {"rows": v[0], "sketch": v[1:17], "estimate": v[17], "part_bits": v[18], "groups": v[19],
-                "plain_estimate": v[20], "learned": bool(v[21]), "raw": v}
+                "plain_estimate": v[20], "learned": bool(v[21]), "smem_front": bool(v[22]), "raw": v}
 
     def get_status(self) -> int:
         return lib().omg_op_status(self.handle)

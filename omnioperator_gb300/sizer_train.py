@@ -1,0 +1,125 @@
+"""Train the aggregation sizing model on records the plain operator logs.
+
+    python -m omnioperator_gb300.sizer_train --out omnioperator_gb300/models/agg_sizer.json
+
+Each training workload is a device-resident int64 key column (sizer_data's family, generated
+on the GPU): N rows, D distinct values, uniform or Zipf(s) by rank.  The plain operator
+aggregates it (COUNT(*) by key) and logs its sizing record (the key sketch of its first flush)
+and the group count it found; the network is then trained on those records by the library's
+CUDA kernels and saved as JSON (dims + flat parameters).
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import time
+
+import numpy as np
+
+from . import api as omg
+from . import sizer as sz
+
+
+def zipf_cdf(torch, domain: int, s: float, dev):
+    w = torch.arange(1, domain + 1, device=dev, dtype=torch.float64).pow_(-s)
+    cdf = torch.cumsum(w, 0)
+    cdf /= cdf[-1].clone()
+    return cdf
+
+
+def gpu_keys(torch, gen, n: int, domain: int, kind: str, s: float, salt: int, dev, cdf=None):
+    """n int64 keys on the GPU: rank uniform or Zipf(s) over `domain`, mixed to 64 bits."""
+    if kind == "uniform":
+        r = torch.randint(0, domain, (n,), generator=gen, device=dev, dtype=torch.int64)
+    else:
+        if cdf is None:
+            cdf = zipf_cdf(torch, domain, s, dev)
+        u = torch.rand(n, generator=gen, device=dev, dtype=torch.float64)
+        r = torch.searchsorted(cdf, u).clamp_(max=domain - 1)
+    # SplitMix64-style mixing in int64 arithmetic (wrapping multiplies).
+    x = r * 0x100000001B3 + salt
+    x = x ^ (x >> 30) & 0x3FFFFFFFF
+    x = x * -4658895280553007687  # 0xBF58476D1CE4E5B9 as int64
+    x = x ^ ((x >> 27) & 0x1FFFFFFFFF)
+    x = x * -7723592293110705685  # 0x94D049BB133111EB as int64
+    return x ^ ((x >> 31) & 0x1FFFFFFFF)
+
+
+def plain_record(torch, keys, L, stream=None):
+    """(sizing record, groups) of the plain operator (AUTO sizing) on a device key column."""
+    fac = omg.HashAggregationOperatorFactory([0], [L], [[]], [[]], [[L]], [omg.OMNI_AGGREGATION_TYPE_COUNT_ALL])
+    op = fac.create_operator()
+    if stream is not None:
+        op.set_stream(stream)
+    op.set_device_output(True)
+    op.add_input(omg.wrap_device_batch([L], keys.numel(), [keys.data_ptr()]))
+    outs, _ = op.get_outputs(1 << 16)
+    omg.free_batches(outs)
+    rec, groups = sz.record_from_operator(op)
+    op.delete()
+    fac.close()
+    return rec, groups
+
+
+def collect(torch, count: int, seed: int, n_min=1 << 18, n_max=1 << 27, d_max=1 << 26, log=print):
+    dev = torch.device("cuda", torch.cuda.current_device())
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    rng = np.random.default_rng(seed)
+    L = omg.LongType()
+    records = []
+    t0 = time.time()
+    for i in range(count):
+        n = int(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))
+        domain = int(math.exp(rng.uniform(math.log(10), math.log(min(d_max, 4 * n)))))
+        kind = "zipf" if rng.random() < 0.6 else "uniform"
+        s = float(rng.uniform(0.6, 1.5))
+        keys = gpu_keys(torch, gen, n, domain, kind, s, int(rng.integers(0, 2**31)), dev)
+        torch.cuda.synchronize()
+        rec, groups = plain_record(torch, keys, L)
+        records.append((rec, groups, dict(n=n, domain=domain, kind=kind, s=s)))
+        del keys
+        if log and (i + 1) % 25 == 0:
+            log(f"  {i + 1}/{count} records ({time.time() - t0:.1f} s)")
+    return records
+
+
+def train(records, epochs=4000, lr=3e-3, seed=1):
+    X, T = sz.dataset([(r, g) for r, g, _ in records])
+    m = sz.SizingModel(seed=seed)
+    loss = m.train(X, T, epochs=epochs, lr=lr)
+    return m, loss
+
+
+def evaluate(m, records):
+    """Mean |log2(estimate / groups)| of the model and of the plain estimate."""
+    X, _ = sz.dataset([(r, g) for r, g, _ in records])
+    y = m.predict(X)
+    learned = [abs(math.log2(sz.estimate(r, v) / g)) for (r, g, _), v in zip(records, y)]
+    plain = [abs(math.log2(max(r[20], 1) / g)) for r, g, _ in records]
+    return float(np.mean(learned)), float(np.mean(plain))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--train", type=int, default=160)
+    ap.add_argument("--test", type=int, default=40)
+    ap.add_argument("--epochs", type=int, default=4000)
+    ap.add_argument("--seed", type=int, default=2026)
+    a = ap.parse_args(argv)
+    import torch
+
+    torch.cuda.init()
+    print(f"collecting {a.train} training and {a.test} held-out sizing records from the plain operator")
+    tr = collect(torch, a.train, a.seed)
+    te = collect(torch, a.test, a.seed + 1)
+    m, loss = train(tr, epochs=a.epochs)
+    lt, pt = evaluate(m, te)
+    print(f"train loss {loss:.5f}; held-out mean |log2 error|: learned {lt:.3f}, plain {pt:.3f}")
+    m.save(a.out)
+    print(f"saved {a.out}")
+
+
+if __name__ == "__main__":
+    main()
