@@ -248,7 +248,11 @@ def run_gpu(args, rank, world):
     if args.only == "agg":
         agg = run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world)
         return dict(value=agg["value"], ms=agg["ms_per_step"], build_ms=0.0, launches=agg["gpu_launches"],
-                    roofline=agg["roofline"], clocks=None, e2e=None, agg=agg, rows=AGG_GROUPS)
+                    roofline=agg["roofline"], clocks=None, e2e=None, agg=agg, rows=AGG_GROUPS, skew=None)
+    if args.only == "skew":
+        sk = run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
+        return dict(value=sk["learned"]["value"], ms=sk["learned"]["ms_per_step"], build_ms=0.0, launches=0,
+                    roofline=None, clocks=None, e2e=None, agg=None, rows=sk["learned"]["groups"], skew=sk)
 
     # ---- device-resident join inputs (torch tensors seen as OmniVec device vectors)
     bkey = torch.randperm(N_BUILD, generator=g, device=dev).to(torch.int64)
@@ -320,8 +324,11 @@ def run_gpu(args, rank, world):
     bop.delete()
     pf.close()
     bf.close()
+    del bkey, p1, p2, pkey, pnull, pbits
+    skew = None if args.skip_skew else run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks,
+                                                       world, rank)
     return dict(value=value, ms=ms / args.steps, build_ms=build_ms, launches=launches, roofline=roofline,
-                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows)
+                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew)
 
 
 def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
@@ -438,6 +445,117 @@ def run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world):
                          "algorithmic_bytes": alg}}
 
 
+SKEW_ROWS = 1 << 28
+SKEW_PAIRS = 50_000_000
+SKEW_WORKLOAD = ("hash aggregation, high-cardinality skewed: 2^28 rows, key (int32, int64) pair of Zipf(1.1) "
+                 "rank over 50,000,000 pairs; SUM(decimal64(18,2) uniform unscaled [-1e9, 1e9]) -> "
+                 "decimal128(38,2), COUNT(*), AVG(double N(0,1)); 2% NULLs per value column; input resident in "
+                 "HBM (7.6 GB, larger than L2)")
+
+
+def nulls_bitmap(torch, mask):
+    """LSB-first validity bitmap (set bit = NULL) of a bool tensor, padded to whole words."""
+    n = mask.numel()
+    pad = (-n) % 64
+    m = torch.cat([mask, torch.zeros(pad + 64, dtype=torch.bool, device=mask.device)])
+    weights = torch.tensor([1, 2, 4, 8, 16, 32, 64, 128], device=mask.device, dtype=torch.int32)
+    return (m.view(-1, 8).to(torch.int32) * weights).sum(1).to(torch.uint8)
+
+
+def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank):
+    """Plain vs learned sizing on the skewed high-cardinality aggregation (one operator per step)."""
+    from omnioperator_gb300 import sizer, sizer_train
+
+    I, L, D = omg.IntType(), omg.LongType(), omg.DoubleType()
+    d64, d128 = omg.Decimal64Type(18, 2), omg.Decimal128Type(38, 2)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4242 + rank)
+    n = SKEW_ROWS if args.skew_log2 is None else 1 << args.skew_log2
+    cdf = sizer_train.zipf_cdf(torch, SKEW_PAIRS, 1.1, dev)
+    rank_ = torch.empty(n, dtype=torch.int64, device=dev)
+    chunk = 1 << 25
+    for s0 in range(0, n, chunk):
+        u = torch.rand(min(chunk, n - s0), generator=g, device=dev, dtype=torch.float64)
+        rank_[s0:s0 + len(u)] = torch.searchsorted(cdf, u).clamp_(max=SKEW_PAIRS - 1)
+    del cdf
+    k1 = (rank_ % 65521).to(torch.int32)
+    x = rank_ * 0x100000001B3 + 7
+    x = x ^ ((x >> 30) & 0x3FFFFFFFF)
+    x = x * -4658895280553007687
+    x = x ^ ((x >> 27) & 0x1FFFFFFFFF)
+    x = x * -7723592293110705685
+    k2 = x ^ ((x >> 31) & 0x1FFFFFFFF)
+    del x, rank_
+    dec = torch.randint(-10**9, 10**9 + 1, (n,), generator=g, device=dev, dtype=torch.int64)
+    dbl = torch.randn(n, generator=g, device=dev, dtype=torch.float64)
+    dec_nulls = nulls_bitmap(torch, torch.rand(n, generator=g, device=dev) < 0.02)
+    dbl_nulls = nulls_bitmap(torch, torch.rand(n, generator=g, device=dev) < 0.02)
+    torch.cuda.synchronize()
+
+    model_path = Path(args.sizer) if args.sizer else ROOT / "omnioperator_gb300" / "models" / "agg_sizer.json"
+    if model_path.exists():
+        model = sizer.SizingModel.load(str(model_path))
+        model_src = str(model_path.relative_to(ROOT)) if model_path.is_relative_to(ROOT) else str(model_path)
+    else:  # no trained weights shipped: train on the plain operator's records now
+        recs = sizer_train.collect(torch, 48, 99, n_max=1 << 26, log=None)
+        model, _ = sizer_train.train(recs, epochs=3000)
+        model_src = "trained at bench start on 48 plain-operator records"
+
+    def factory(arm):
+        f = omg.HashAggregationOperatorFactory(
+            [0, 1], [I, L], [[2], [], [3]], [[d64], [], [D]], [[d128], [L], [D]],
+            [omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_COUNT_ALL, omg.OMNI_AGGREGATION_TYPE_AVG])
+        if arm == "learned":
+            f.set_sizer(model)
+        return f
+
+    hint = {}
+
+    def step(fac):
+        op = fac.create_operator()
+        if hint.get("groups"):
+            op.set_agg_strategy(omg.AGG_STRATEGY_AUTO, hint["groups"])
+        op.set_stream(stream.cuda_stream)
+        op.set_device_output(True)
+        op.add_input(omg.wrap_device_batch([I, L, d64, D], n, [k1.data_ptr(), k2.data_ptr(), dec.data_ptr(),
+                                                              dbl.data_ptr()],
+                                           [None, None, dec_nulls.data_ptr(), dbl_nulls.data_ptr()]))
+        outs, groups = op.get_outputs(1 << 16)
+        omg.free_batches(outs)
+        c = op.counters()
+        log = op.sizing_log()
+        op.delete()
+        return groups, c, log
+
+    steps = max(1, min(args.steps, 3))
+    res = {}
+    # exact_count: the true group count given as the capacity hint (the best any estimate can do).
+    for arm in ("plain", "learned", "exact_count"):
+        fac = factory(arm)
+        if arm == "exact_count":
+            hint["groups"] = res["plain"]["groups"]
+        step(fac)  # warm-up
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            groups, c, log = step(fac)
+        e1.record(stream)
+        barrier()
+        ms = max_over_ranks(e0.elapsed_time(e1)) / steps
+        fac.close()
+        res[arm] = {"value": world * n / (ms / 1e3), "unit": "rows/s", "ms_per_step": round(ms, 3),
+                    "groups": groups, "estimate": log["estimate"], "plain_estimate": log["plain_estimate"],
+                    "table_resizes": c["resizes"], "retried_rows": c["retried_rows"],
+                    "shared_front_table": log["smem_front"], "part_bits": log["part_bits"]}
+    assert res["plain"]["groups"] == res["learned"]["groups"] == res["exact_count"]["groups"]
+    model.close()
+    return {"workload": SKEW_WORKLOAD if n == SKEW_ROWS else SKEW_WORKLOAD.replace("2^28", f"2^{n.bit_length() - 1}"),
+            "steps": steps, "sizer": model_src, "plain": res["plain"], "learned": res["learned"],
+            "exact_count": res["exact_count"],
+            "learned_over_plain": round(res["learned"]["value"] / res["plain"]["value"], 3)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -447,9 +565,12 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-agg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "agg"],
-                    help="agg: time only the aggregation workload (profiling runs)")
+    ap.add_argument("--only", default="all", choices=["all", "agg", "skew"],
+                    help="agg / skew: time only that aggregation workload (profiling runs)")
     ap.add_argument("--probe-log2", type=int, default=26, help="log2 of probe rows (profiling runs use fewer)")
+    ap.add_argument("--skip-skew", action="store_true", help="skip the skewed aggregation (plain vs learned)")
+    ap.add_argument("--skew-log2", type=int, default=None, help="log2 rows of the skewed aggregation (default 28)")
+    ap.add_argument("--sizer", default=None, help="sizing model weights (JSON) for the learned arm")
     args = ap.parse_args()
     global N_PROBE
     N_PROBE = 1 << args.probe_log2
@@ -480,7 +601,7 @@ def main():
                             "l2": "inputs+outputs (1.4 GB/step) larger than L2; no flush needed",
                             "build_ms": round(r["build_ms"], 3), "output_rows_per_step": r["rows"]},
                  "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"],
-                 "clocks": r["clocks"], "agg": r["agg"]})
+                 "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"]})
     print(json.dumps(line), flush=True)
 
 

@@ -208,8 +208,8 @@ int32_t omg_batch_free_many(void *const *batches, int32_t n);
  * distinct hashes, frequency classes f1, f2, f3, f4-7, f8+, largest count, rows of the 8+
  * class, 6 reserved), [17] the group estimate used for sizing, [18] the partition bits of the
  * partitioned strategy (-1 = global table), [19] the group count so far, [20] the plain
- * (sketch) estimate, [21] 1 if a sizing model made the estimate used, [22] 1 if AUTO put the
- * shared-memory front table before the global one (many groups with heavy hitters).
+ * (sketch) estimate, [21] 1 if a sizing model made the estimate used, [22] 1 if a shared-memory
+ * front table sat before the global one (OMG_AGG_STRATEGY_SMEM).
  * `*written` receives the number of values stored (at most n). */
 int32_t omg_op_get_sizing_log(void *op, int64_t *out, int32_t n, int32_t *written);
 /* ---- learned sizing model (no reference counterpart) ---------------------------------

@@ -420,7 +420,6 @@ struct HashAggregationOperator::Impl {
     uint64_t plainEstimate = 0;
     bool learned = false;
     int32_t partBits = -1;
-    bool smemFront = false;  // AUTO chose the shared front table (skewed, many groups)
 };
 
 HashAggregationOperator::HashAggregationOperator(const AggPlan &plan, omg::SizingModel *sizer)
@@ -518,7 +517,6 @@ namespace {
 constexpr int64_t kSketchMinRows = int64_t(1) << 18;  // smaller flushes: default sizing, global table
 constexpr int32_t kSketchSample = 1 << 16;
 constexpr double kPartLoad = 0.6;  // target load of a partition's shared table
-constexpr double kHeavyShare = 0.1;
 
 // Plain group-count estimate from the sketch of n sampled rows out of N: the GEE estimator
 // (sqrt(N / n) * f1 + sum of the other frequency classes), clamped to [d, N].
@@ -560,7 +558,7 @@ int32_t HashAggregationOperator::GetSizingLog(int64_t *out, int32_t n) const
     v.push_back(static_cast<int64_t>(std::max<uint64_t>(im.groups, uniqueKeys_)));
     v.push_back(static_cast<int64_t>(im.plainEstimate));
     v.push_back(im.learned ? 1 : 0);
-    v.push_back(im.smemFront ? 1 : 0);
+    v.push_back(strategy_ == 1 ? 1 : 0);
     const int32_t m = std::min<int32_t>(n, static_cast<int32_t>(v.size()));
     for (int32_t i = 0; i < m; ++i) {
         out[i] = v[i];
@@ -620,14 +618,6 @@ void HashAggregationOperator::Decide(omg::BatchTable &bt, cudaStream_t s)
     }
     if (strategy_ == 3 && im.partBits < 0) {
         im.partBits = 0;  // forced: one partition (the shared tables still sit in front of the global one)
-    }
-    // Too many groups to partition, but heavy hitters in the sample (keys seen 8+ times hold at
-    // least kHeavyShare of the sampled rows): a per-CTA shared table in front of the global one
-    // absorbs the hot groups' updates, which would otherwise serialise on their global slots.
-    const double sampled = static_cast<double>(im.sketch[0] - im.sketch[1]);
-    if (strategy_ == 0 && im.partBits < 0 && sampled > 0 &&
-        static_cast<double>(im.sketch[9]) >= kHeavyShare * sampled) {
-        im.smemFront = true;
     }
 }
 
@@ -716,7 +706,7 @@ void HashAggregationOperator::Flush()
     // GLOBAL (2): global table only.  SMEM (1): a per-CTA shared table in front of the global
     // one.  PARTITIONED (3, or AUTO when the estimate says the groups fit): rows are hash
     // partitioned so that each CTA's shared table holds one partition's groups.
-    if (strategy_ == 1 || im.smemFront) {  // OMG_AGG_STRATEGY_SMEM
+    if (strategy_ == 1) {  // OMG_AGG_STRATEGY_SMEM
         smemSlots = plan_.smemSlots;
     }
     const int grid = 0;  // the launcher fills every SM to its occupancy limit

@@ -2,8 +2,8 @@
 
     python -m omnioperator_gb300.sizer_train --out omnioperator_gb300/models/agg_sizer.json
 
-Each training workload is a device-resident int64 key column (sizer_data's family, generated
-on the GPU): N rows, D distinct values, uniform or Zipf(s) by rank.  The plain operator
+Each training workload is a device-resident int64 key column generated on the GPU: N rows over
+a domain of D values (a fraction of N), uniform or Zipf(s) by rank.  The plain operator
 aggregates it (COUNT(*) by key) and logs its sizing record (the key sketch of its first flush)
 and the group count it found; the network is then trained on those records by the library's
 CUDA kernels and saved as JSON (dims + flat parameters).
@@ -61,7 +61,10 @@ def plain_record(torch, keys, L, stream=None):
     return rec, groups
 
 
-def collect(torch, count: int, seed: int, n_min=1 << 18, n_max=1 << 27, d_max=1 << 26, log=print):
+def collect(torch, count: int, seed: int, n_min=1 << 20, n_max=1 << 28, d_max=1 << 27, log=print):
+    """Sizing records of `count` workloads: N log-uniform in [n_min, n_max], the key domain a
+    log-uniform fraction 2^-12 .. 2 of N (at least 10, at most d_max), Zipf(s in [0.7, 1.4]) by
+    rank for 70% of them, uniform otherwise."""
     dev = torch.device("cuda", torch.cuda.current_device())
     gen = torch.Generator(device=dev)
     gen.manual_seed(seed)
@@ -71,9 +74,9 @@ def collect(torch, count: int, seed: int, n_min=1 << 18, n_max=1 << 27, d_max=1 
     t0 = time.time()
     for i in range(count):
         n = int(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))
-        domain = int(math.exp(rng.uniform(math.log(10), math.log(min(d_max, 4 * n)))))
-        kind = "zipf" if rng.random() < 0.6 else "uniform"
-        s = float(rng.uniform(0.6, 1.5))
+        domain = int(min(d_max, max(10, n * 2.0 ** rng.uniform(-12, 1))))
+        kind = "zipf" if rng.random() < 0.7 else "uniform"
+        s = float(rng.uniform(0.7, 1.4))
         keys = gpu_keys(torch, gen, n, domain, kind, s, int(rng.integers(0, 2**31)), dev)
         torch.cuda.synchronize()
         rec, groups = plain_record(torch, keys, L)
@@ -103,17 +106,18 @@ def evaluate(m, records):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--out", required=True)
-    ap.add_argument("--train", type=int, default=160)
-    ap.add_argument("--test", type=int, default=40)
+    ap.add_argument("--train", type=int, default=320)
+    ap.add_argument("--test", type=int, default=60)
     ap.add_argument("--epochs", type=int, default=4000)
     ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--n-max-log2", type=int, default=28, help="largest workload, log2 rows")
     a = ap.parse_args(argv)
     import torch
 
     torch.cuda.init()
     print(f"collecting {a.train} training and {a.test} held-out sizing records from the plain operator")
-    tr = collect(torch, a.train, a.seed)
-    te = collect(torch, a.test, a.seed + 1)
+    tr = collect(torch, a.train, a.seed, n_max=1 << a.n_max_log2)
+    te = collect(torch, a.test, a.seed + 1, n_max=1 << a.n_max_log2)
     m, loss = train(tr, epochs=a.epochs)
     lt, pt = evaluate(m, te)
     print(f"train loss {loss:.5f}; held-out mean |log2 error|: learned {lt:.3f}, plain {pt:.3f}")
