@@ -239,6 +239,32 @@ int32_t omg_sizer_estimate(const int64_t *sizing_log, int32_t n_log, float y, in
  * (the exact resize path still corrects any misprediction).  NULL detaches.  The model must
  * outlive those operators. */
 int32_t omg_hashagg_factory_set_sizer(void *factory, void *model);
+/* ---- batched aggregation of many tasks (no reference counterpart) ---------------------
+ * The reference runs one HashAggregation operator per task.  These entry points run n tasks of
+ * one factory's plan (task i = one VectorBatch, aggregated alone) together: per-task tables in
+ * one slab sized by a batched key sketch or by `sizer` (may be NULL), one persistent kernel over
+ * all tasks' tiles with an autotuned launch shape, the whole per-run sequence captured once as a
+ * CUDA graph and replayed by every omg_agg_batch_run.  A task whose groups outgrow its table is
+ * re-run through a regular operator, so results equal n separate operators.  The task batches
+ * stay owned by the caller and must outlive the batch object.  Plans with sticky-overflow sums
+ * (decimal SUM, generic-policy int64 SUM) are rejected with OMG_ERR_UNSUPPORTED. */
+#define OMG_BATCH_DEVICE_OUTPUT 1    /* output batches stay in HBM */
+#define OMG_BATCH_NO_GRAPH 2         /* launch the sequence directly instead of a CUDA graph */
+#define OMG_BATCH_NO_TUNE 4          /* default launch shape */
+#define OMG_BATCH_DEBUG_TINY_TABLES 8 /* tests: 64-slot tables, forcing the exact re-run path */
+int32_t omg_agg_batch_create(void *factory, void *const *task_batches, int32_t n_tasks, void *sizer, int32_t flags,
+    void **out_batch);
+int32_t omg_agg_batch_run(void *batch, void *stream);
+/* Output batches of the last run in task order (caller frees each); call until *n == 0.
+ * task_of[i] receives the task of out_batches[i]. */
+int32_t omg_agg_batch_outputs(void *batch, void **out_batches, int32_t *task_of, int32_t max, int32_t *n);
+/* [0] tasks, [1] input rows, [2] table slots, [3] tasks re-run exactly, [4] threads per CTA,
+ * [5] CTAs per SM, [6] runs, [7] groups, [8] tuning us, [9] preparation us, [10] last run's
+ * device time us, [11] 1 if a sizing model sized the tables, [12] 1 if runs replay a graph. */
+int32_t omg_agg_batch_info(void *batch, int64_t *out, int32_t n, int32_t *written);
+/* Per task, a sizing record laid out as omg_op_get_sizing_log's (23 values per task). */
+int32_t omg_agg_batch_sizing_logs(void *batch, int64_t *out, int64_t n, int64_t *written);
+int32_t omg_agg_batch_destroy(void *batch);
 /* Operator::GetStatus (operator.h:46-49): OMG_STATUS_*. */
 int32_t omg_op_status(void *op);
 /* Operator::noMoreInput / setNoMoreInput / needsInput (operator.h:117-130). */

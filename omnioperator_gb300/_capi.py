@@ -75,6 +75,12 @@ _SIGS = {
     "omg_sizer_target": (I32, [C.POINTER(I64), I32, I64, C.POINTER(C.c_float)]),
     "omg_sizer_estimate": (I32, [C.POINTER(I64), I32, C.c_float, C.POINTER(I64)]),
     "omg_hashagg_factory_set_sizer": (I32, [P, P]),
+    "omg_agg_batch_create": (I32, [P, C.POINTER(P), I32, P, I32, C.POINTER(P)]),
+    "omg_agg_batch_run": (I32, [P, P]),
+    "omg_agg_batch_outputs": (I32, [P, C.POINTER(P), C.POINTER(I32), I32, C.POINTER(I32)]),
+    "omg_agg_batch_info": (I32, [P, C.POINTER(I64), I32, C.POINTER(I32)]),
+    "omg_agg_batch_sizing_logs": (I32, [P, C.POINTER(I64), I64, C.POINTER(I64)]),
+    "omg_agg_batch_destroy": (I32, [P]),
     "omg_op_status": (I32, [P]),
     "omg_op_no_more_input": (I32, [P]),
     "omg_op_set_no_more_input": (I32, [P, I32]),

@@ -391,3 +391,57 @@ class LookupJoinOperatorFactory(OperatorFactory):
             _types(build_output_types), int(hash_builder_factory.handle), None,
             1 if is_shuffle_exchange_build_plan else 0, C.byref(out)))
         super().__init__(out.value)
+
+
+# --------------------------------------------------------------------------- batched aggregation
+BATCH_DEVICE_OUTPUT, BATCH_NO_GRAPH, BATCH_NO_TUNE, BATCH_DEBUG_TINY_TABLES = 1, 2, 4, 8
+_BATCH_INFO = ["tasks", "rows", "table_slots", "reruns", "threads", "ctas_per_sm", "runs", "groups", "tune_us",
+               "prepare_us", "run_us", "learned", "graph"]
+
+
+class AggBatch:
+    """Many HashAggregation tasks of one factory in one launch (omg_agg_batch_*).  `tasks` are
+    batch handles the caller keeps alive (and frees) until close()."""
+
+    def __init__(self, factory, tasks, sizer=None, flags=0):
+        arr = (C.c_void_p * len(tasks))(*tasks)
+        out = C.c_void_p()
+        check(lib().omg_agg_batch_create(factory.handle, arr, len(tasks), None if sizer is None else sizer.handle,
+                                         flags, C.byref(out)))
+        self.handle = out.value
+        self._sizer = sizer
+
+    def run(self, stream: int | None = None):
+        check(lib().omg_agg_batch_run(self.handle, C.c_void_p(stream) if stream else None))
+
+    def outputs(self, chunk: int = 1 << 14):
+        """[(task, batch handle)] of the last run (the caller frees the batches)."""
+        res = []
+        out = (C.c_void_p * chunk)()
+        task = (C.c_int32 * chunk)()
+        n = C.c_int32(0)
+        while True:
+            check(lib().omg_agg_batch_outputs(self.handle, out, task, chunk, C.byref(n)))
+            if n.value == 0:
+                return res
+            res.extend(zip(task[: n.value], out[: n.value]))
+
+    def info(self) -> dict:
+        arr = (C.c_int64 * 32)()
+        n = C.c_int32(0)
+        check(lib().omg_agg_batch_info(self.handle, arr, 32, C.byref(n)))
+        return dict(zip(_BATCH_INFO, arr[: n.value]))
+
+    def sizing_logs(self):
+        info = self.info()
+        total = info["tasks"] * 23
+        arr = (C.c_int64 * total)()
+        n = C.c_int64(0)
+        check(lib().omg_agg_batch_sizing_logs(self.handle, arr, total, C.byref(n)))
+        v = list(arr[: n.value])
+        return [v[i:i + 23] for i in range(0, len(v), 23)]
+
+    def close(self):
+        if self.handle:
+            check(lib().omg_agg_batch_destroy(self.handle))
+            self.handle = None

@@ -11,6 +11,7 @@
 #include "host/gpu_runtime.h"
 #include "host/sizer.h"
 #include "kernels/agg_noalloc.h"
+#include "omniop/batched_agg.h"
 #include "omniop/hash_aggregation.h"
 #include "omniop/hash_join.h"
 #include "omniop/memory.h"
@@ -536,6 +537,109 @@ int32_t omg_hashagg_factory_set_sizer(void *factory, void *model)
             Require(AsSizer(model)->Dims()[0] == omg::kSizerFeatures, "model input width must be 12");
         }
         f->SetSizer(static_cast<omg::SizingModel *>(model));
+    });
+}
+
+// ---- batched aggregation
+namespace {
+struct AggBatchHandle {
+    std::unique_ptr<omniruntime::op::BatchedAggregation> agg;
+    std::vector<VectorBatch *> pending;
+    std::vector<int32_t> pendingTask;
+    size_t next = 0;
+    void DropPending()
+    {
+        for (size_t i = next; i < pending.size(); ++i) {
+            VectorHelper::FreeVecBatch(pending[i]);
+        }
+        pending.clear();
+        pendingTask.clear();
+        next = 0;
+    }
+};
+AggBatchHandle *AsAggBatch(void *b)
+{
+    Require(b != nullptr, "null batch handle");
+    return static_cast<AggBatchHandle *>(b);
+}
+}  // namespace
+
+int32_t omg_agg_batch_create(void *factory, void *const *task_batches, int32_t n_tasks, void *sizer, int32_t flags,
+    void **out_batch)
+{
+    return Guard([&] {
+        auto *f = dynamic_cast<HashAggregationOperatorFactory *>(static_cast<OperatorFactory *>(factory));
+        Require(f != nullptr, "not a HashAggregation factory");
+        Require(n_tasks > 0 && task_batches != nullptr && out_batch != nullptr, "no tasks");
+        std::vector<VectorBatch *> tasks(n_tasks);
+        for (int32_t i = 0; i < n_tasks; ++i) {
+            tasks[i] = static_cast<VectorBatch *>(task_batches[i]);
+        }
+        auto h = std::make_unique<AggBatchHandle>();
+        h->agg.reset(new omniruntime::op::BatchedAggregation(*f, tasks, static_cast<omg::SizingModel *>(sizer), flags));
+        *out_batch = h.release();
+    });
+}
+
+int32_t omg_agg_batch_run(void *batch, void *stream)
+{
+    return Guard([&] {
+        AggBatchHandle *h = AsAggBatch(batch);
+        h->DropPending();
+        h->agg->Run(stream);
+        h->agg->Outputs(h->pending, h->pendingTask);
+    });
+}
+
+int32_t omg_agg_batch_outputs(void *batch, void **out_batches, int32_t *task_of, int32_t max, int32_t *n)
+{
+    return Guard([&] {
+        AggBatchHandle *h = AsAggBatch(batch);
+        Require(n != nullptr && max >= 0 && (max == 0 || out_batches != nullptr), "null output array");
+        int32_t k = 0;
+        while (k < max && h->next < h->pending.size()) {
+            out_batches[k] = h->pending[h->next];
+            if (task_of != nullptr) {
+                task_of[k] = h->pendingTask[h->next];
+            }
+            ++k;
+            ++h->next;
+        }
+        *n = k;
+    });
+}
+
+int32_t omg_agg_batch_info(void *batch, int64_t *out, int32_t n, int32_t *written)
+{
+    return Guard([&] {
+        Require(out != nullptr && written != nullptr && n >= 0, "null output");
+        const std::vector<int64_t> v = AsAggBatch(batch)->agg->Info();
+        const int32_t m = std::min<int32_t>(n, static_cast<int32_t>(v.size()));
+        std::copy(v.begin(), v.begin() + m, out);
+        *written = m;
+    });
+}
+
+int32_t omg_agg_batch_sizing_logs(void *batch, int64_t *out, int64_t n, int64_t *written)
+{
+    return Guard([&] {
+        Require(out != nullptr && written != nullptr && n >= 0, "null output");
+        const std::vector<int64_t> v = AsAggBatch(batch)->agg->SizingLogs();
+        const int64_t m = std::min<int64_t>(n, static_cast<int64_t>(v.size()));
+        std::copy(v.begin(), v.begin() + m, out);
+        *written = m;
+    });
+}
+
+int32_t omg_agg_batch_destroy(void *batch)
+{
+    return Guard([&] {
+        if (batch == nullptr) {
+            return;
+        }
+        auto *h = static_cast<AggBatchHandle *>(batch);
+        h->DropPending();
+        delete h;
     });
 }
 

@@ -482,8 +482,7 @@ int32_t HashAggregationOperator::AddInput(VectorBatch *vecBatch)
     return 0;
 }
 
-namespace {
-omg::AggLaunch MakeLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacity, uint32_t *special,
+omg::AggLaunch MakeAggLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacity, uint32_t *special,
     unsigned long long *stats)
 {
     omg::AggLaunch p;
@@ -506,33 +505,22 @@ omg::AggLaunch MakeLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacit
     p.table.keyWords = plan.keyWords;
     p.table.specialUsed = special;
     p.table.groupCount = stats;
-    p.nRetry = reinterpret_cast<unsigned int *>(stats + 1);
-    p.error = reinterpret_cast<int32_t *>(stats + 3);
+    p.nRetry = stats != nullptr ? reinterpret_cast<unsigned int *>(stats + 1) : nullptr;
+    p.error = stats != nullptr ? reinterpret_cast<int32_t *>(stats + 3) : nullptr;
     p.waitBudget = omg::WaitBudget();
     return p;
 }
-}  // namespace
 
 namespace {
+omg::AggLaunch MakeLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacity, uint32_t *special,
+    unsigned long long *stats)
+{
+    return MakeAggLaunch(plan, slots, capacity, special, stats);
+}
+
 constexpr int64_t kSketchMinRows = int64_t(1) << 18;  // smaller flushes: default sizing, global table
 constexpr int32_t kSketchSample = 1 << 16;
 constexpr double kPartLoad = 0.6;  // target load of a partition's shared table
-
-// Plain group-count estimate from the sketch of n sampled rows out of N: the GEE estimator
-// (sqrt(N / n) * f1 + sum of the other frequency classes), clamped to [d, N].
-uint64_t EstimateGroups(const unsigned long long *st, int64_t total)
-{
-    const double n = static_cast<double>(st[0] - st[1]);
-    const double d = static_cast<double>(st[2]);
-    const double f1 = static_cast<double>(st[3]);
-    const double specials = st[1] > 0 ? 2.0 : 0.0;  // the NULL and EMPTY groups at most
-    if (n <= 0) {
-        return static_cast<uint64_t>(specials) + 1;
-    }
-    double est = n >= static_cast<double>(total) ? d : std::sqrt(static_cast<double>(total) / n) * f1 + (d - f1);
-    est = std::min(std::max(est, d), static_cast<double>(total));
-    return static_cast<uint64_t>(est + specials);
-}
 }  // namespace
 
 // Partition buffers of one flush (see Partition).
@@ -587,7 +575,7 @@ void HashAggregationOperator::Decide(omg::BatchTable &bt, cudaStream_t s)
         CudaCheck(cudaMemcpyAsync(im.sketch, st.Get(), sizeof(im.sketch), cudaMemcpyDeviceToHost, s), "read sketch");
         im.stream.Sync();
         im.sketchRows = rows;
-        im.plainEstimate = EstimateGroups(im.sketch, rows);
+        im.plainEstimate = omg::PlainGroupEstimate(im.sketch, rows);
         im.estimate = im.plainEstimate;
         if (sizer_ != nullptr && sizer_->Dims()[0] == omg::kSizerFeatures) {
             int64_t log[1 + omg::kSketchStats];

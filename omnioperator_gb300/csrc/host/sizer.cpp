@@ -39,6 +39,20 @@ struct SplitMix {
 };
 }  // namespace
 
+uint64_t PlainGroupEstimate(const unsigned long long *st, int64_t total)
+{
+    const double n = static_cast<double>(st[0] - st[1]);
+    const double d = static_cast<double>(st[2]);
+    const double f1 = static_cast<double>(st[3]);
+    const double specials = st[1] > 0 ? 2.0 : 0.0;  // the NULL and EMPTY groups at most
+    if (n <= 0) {
+        return static_cast<uint64_t>(specials) + 1;
+    }
+    double est = n >= static_cast<double>(total) ? d : std::sqrt(static_cast<double>(total) / n) * f1 + (d - f1);
+    est = std::min(std::max(est, d), static_cast<double>(total));
+    return static_cast<uint64_t>(est + specials);
+}
+
 void SizerFeatures(const int64_t *log, float *x)
 {
     const double N = static_cast<double>(std::max<int64_t>(log[kLogRows], 1));

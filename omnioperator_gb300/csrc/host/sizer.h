@@ -13,6 +13,11 @@
 
 namespace omg {
 
+// Plain group-count estimate from a key sketch (kSketchStats values) of n sampled rows out of
+// `rows`: the GEE estimator sqrt(rows / n) * f1 + (d - f1), clamped to [d, rows], plus the
+// special groups the sample saw.
+uint64_t PlainGroupEstimate(const unsigned long long *sketch, int64_t rows);
+
 // Features of a sizing record (the layout written by HashAggregationOperator::GetSizingLog):
 // scale-free functions of the rows N, the sampled rows n, the distinct hashes d of the sample,
 // its frequency classes and the plain estimate.

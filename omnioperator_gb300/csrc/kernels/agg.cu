@@ -1020,6 +1020,141 @@ __device__ __forceinline__ bool ExceedsBound(const uint64_t *m, bool negative, i
     return v > Dec38Max();
 }
 
+// Output row `pos` of the group in slot s (occupied) of table t: keys, counts and aggregates.
+__device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &t, uint64_t s, const uint64_t *slot,
+    uint64_t pos)
+{
+    const uint64_t *st = slot + t.keyWords;
+    const bool nullSlot = (s == t.capacity + kNullSlotOffset);
+    const bool sentinelSlot = (s == t.capacity + kSentinelSlotOffset);
+    for (int o = 0; o < e.nOut; ++o) {
+        const OutSpec &os = e.out[o];
+        if (os.kind == OUT_KEY) {
+            const KeyCol &kc = e.key.cols[os.src];
+            if (e.key.kind == KEY_SINGLE) {
+                if (nullSlot) {
+                    SetOutNull(os.nulls, pos);
+                    StoreWidth(os.values, pos, os.outWidth, 0);
+                } else {
+                    StoreWidth(os.values, pos, os.outWidth, sentinelSlot ? kEmptyKey : slot[0]);
+                }
+            } else {
+                const uint64_t *kwds = slot + 1;
+                const uint32_t mask = static_cast<uint32_t>(
+                    (kwds[e.key.maskByte >> 3] >> ((e.key.maskByte & 7) * 8)) & 0xffu);
+                const bool isNull = (mask >> os.src) & 1u;
+                const int wi = kc.byteOffset >> 3;
+                if (kc.width == 16) {
+                    uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
+                    dst[0] = isNull ? 0 : kwds[wi];
+                    dst[1] = isNull ? 0 : kwds[wi + 1];
+                } else {
+                    const int sh = (kc.byteOffset & 7) * 8;
+                    uint64_t bits = kwds[wi] >> sh;
+                    StoreWidth(os.values, pos, os.outWidth, isNull ? 0 : bits);
+                }
+                if (isNull) {
+                    SetOutNull(os.nulls, pos);
+                }
+            }
+            continue;
+        }
+        int64_t cnt = static_cast<int64_t>(st[e.accs[0].word]);  // accs[0] is COUNT_ALL
+        if (os.countAcc >= 0) {
+            cnt -= static_cast<int64_t>(st[e.accs[os.countAcc].word]);
+        }
+        if (os.kind == OUT_COUNT) {
+            StoreWidth(os.values, pos, 8, static_cast<uint64_t>(cnt));
+            continue;
+        }
+        if (cnt == 0) {
+            SetOutNull(os.nulls, pos);
+            StoreWidth(os.values, pos, os.outWidth == 16 ? 8 : os.outWidth, 0);
+            if (os.outWidth == 16) {
+                static_cast<uint64_t *>(os.values)[2 * pos + 1] = 0;
+            }
+            continue;
+        }
+        const AccSpec &acc = e.accs[os.src];
+        const uint64_t *w = st + acc.word;
+        switch (os.kind) {
+            case OUT_SUM_WRAP:
+            case OUT_MIN_INT:
+            case OUT_MAX_INT:
+                StoreWidth(os.values, pos, os.outWidth, w[0]);
+                break;
+            case OUT_SUM_DOUBLE:
+            case OUT_AVG: {
+                double sum = __dadd_rn(__longlong_as_double(static_cast<long long>(w[0])),
+                    __longlong_as_double(static_cast<long long>(w[1])));
+                if (!isfinite(__longlong_as_double(static_cast<long long>(w[0])))) {
+                    sum = __longlong_as_double(static_cast<long long>(w[0]));
+                }
+                const double v = (os.kind == OUT_AVG) ? sum / static_cast<double>(cnt) : sum;
+                static_cast<double *>(os.values)[pos] = v;
+                break;
+            }
+            case OUT_MIN_DOUBLE:
+            case OUT_MAX_DOUBLE: {
+                const double v = DoubleFromOrdered(static_cast<int64_t>(w[0]));
+                if (os.outWidth == 4) {
+                    static_cast<float *>(os.values)[pos] = static_cast<float>(v);
+                } else {
+                    static_cast<double *>(os.values)[pos] = v;
+                }
+                break;
+            }
+            case OUT_SUM_EXACT: {
+                WideSum ws = DecodeWide(acc, w);
+                bool overflow = ExceedsBound(ws.mag, ws.negative, os.boundKind);
+                if (!overflow && ExceedsBound(ws.abs, false, os.boundKind)) {
+                    // Some prefix of the row-ordered sum may have overflowed: decided by
+                    // the ordered path on the host side of this operator.
+                    if (e.forcedOverflow != nullptr) {
+                        overflow = ((e.forcedOverflow[s] >> os.pad) & 1u) != 0;
+                    } else {
+                        unsigned long long k = atomicAdd(e.nAmbiguous, 1ull);
+                        if (k < e.ambiguousCap) {
+                            e.ambiguousSlots[k] = s;
+                        }
+                    }
+                }
+                unsigned __int128 mag = (static_cast<unsigned __int128>(ws.mag[1]) << 64) | ws.mag[0];
+                if (!overflow && os.rescalePow > 0) {
+                    unsigned __int128 f = 1;
+                    for (int i = 0; i < os.rescalePow; ++i) {
+                        f *= 10;
+                    }
+                    // |mag| <= 10^38 - 1 < 2^127 and f <= 10^38: check mag * f <= bound.
+                    if (mag != 0 && mag > Dec38Max() / f) {
+                        overflow = true;
+                    } else {
+                        mag *= f;
+                    }
+                }
+                if (overflow) {
+                    SetOutNull(os.nulls, pos);
+                    if (!e.overflowAsNull) {
+                        SetError(e.error, 5);
+                    }
+                    mag = 0;
+                }
+                unsigned __int128 v = ws.negative ? (~mag + 1) : mag;
+                if (os.outWidth == 16) {
+                    uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
+                    dst[0] = static_cast<uint64_t>(v);
+                    dst[1] = static_cast<uint64_t>(v >> 64);
+                } else {
+                    StoreWidth(os.values, pos, os.outWidth, static_cast<uint64_t>(v));
+                }
+                break;
+            }
+            default:
+                break;
+        }
+    }
+}
+
 __global__ void ExtractKernel(const __grid_constant__ AggExtract e)
 {
     __shared__ unsigned int warpCounts[32];
@@ -1055,137 +1190,193 @@ __global__ void ExtractKernel(const __grid_constant__ AggExtract e)
         __syncthreads();
         if (occ) {
             const uint64_t pos = blockBase + warpCounts[warp] + __popc(ballot & ((1u << lane) - 1u));
-            const uint64_t *st = slot + t.keyWords;
-            const bool nullSlot = (s == t.capacity + kNullSlotOffset);
-            const bool sentinelSlot = (s == t.capacity + kSentinelSlotOffset);
-            for (int o = 0; o < e.nOut; ++o) {
-                const OutSpec &os = e.out[o];
-                if (os.kind == OUT_KEY) {
-                    const KeyCol &kc = e.key.cols[os.src];
-                    if (e.key.kind == KEY_SINGLE) {
-                        if (nullSlot) {
-                            SetOutNull(os.nulls, pos);
-                            StoreWidth(os.values, pos, os.outWidth, 0);
-                        } else {
-                            StoreWidth(os.values, pos, os.outWidth, sentinelSlot ? kEmptyKey : slot[0]);
-                        }
-                    } else {
-                        const uint64_t *kwds = slot + 1;
-                        const uint32_t mask = static_cast<uint32_t>(
-                            (kwds[e.key.maskByte >> 3] >> ((e.key.maskByte & 7) * 8)) & 0xffu);
-                        const bool isNull = (mask >> os.src) & 1u;
-                        const int wi = kc.byteOffset >> 3;
-                        if (kc.width == 16) {
-                            uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
-                            dst[0] = isNull ? 0 : kwds[wi];
-                            dst[1] = isNull ? 0 : kwds[wi + 1];
-                        } else {
-                            const int sh = (kc.byteOffset & 7) * 8;
-                            uint64_t bits = kwds[wi] >> sh;
-                            StoreWidth(os.values, pos, os.outWidth, isNull ? 0 : bits);
-                        }
-                        if (isNull) {
-                            SetOutNull(os.nulls, pos);
-                        }
-                    }
-                    continue;
+            WriteGroup(e, t, s, slot, pos);
+        }
+        __syncthreads();
+    }
+}
+
+
+// ------------------------------------------------------------------ batched tasks
+// Many independent aggregations (tasks) in one launch: task i is batch i and owns table
+// taskTables[i] inside one slab.  AggTasksKernel walks the tiles of all tasks (tiles of a task are
+// adjacent); per-task sketch, count and extraction kernels run one CTA per task.
+
+template <int kKind, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) AggTasksKernel(const __grid_constant__ AggLaunch p)
+{
+    const int sw = p.table.slotWords;
+    const int kw = p.table.keyWords;
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        const AggTable tab = p.taskTables[tile.batch];
+        for (int r = threadIdx.x; r < tile.rows; r += blockDim.x) {
+            const int64_t row = static_cast<int64_t>(tile.row0) + r;
+            const RowIn in = LoadRow<kKind>(p, b, row);
+            bool inserted = false;
+            const int64_t g = GlobalFind(tab, p.key, in.k, p.maxProbe, p.error, &inserted, p.waitBudget, kKind);
+            if (g < 0) {
+                p.taskFailed[tile.batch] = 1u;
+                continue;
+            }
+            UpdateStates(p, b, row, in, tab.slots + g * sw + kw);
+        }
+    }
+}
+
+// Per task: a sketch of up to kTaskSketchRows rows (stratified over the task's rows) in a
+// shared-memory table; stats laid out as the operator's sketch (kSketchStats per task).
+template <int kKind>
+__global__ void __launch_bounds__(256) TaskSketchKernel(const __grid_constant__ AggLaunch p, int32_t nTasks,
+    unsigned long long *stats)
+{
+    __shared__ unsigned long long keys[kTaskSketchSlots];
+    __shared__ unsigned int counts[kTaskSketchSlots];
+    __shared__ unsigned long long acc[kSketchStats];
+    for (int task = blockIdx.x; task < nTasks; task += gridDim.x) {
+        for (int i = threadIdx.x; i < kTaskSketchSlots; i += blockDim.x) {
+            keys[i] = kEmptyKey;
+            counts[i] = 0;
+        }
+        for (int i = threadIdx.x; i < kSketchStats; i += blockDim.x) {
+            acc[i] = 0;
+        }
+        __syncthreads();
+        const BatchDesc &b = p.batches[task];
+        const int64_t rows = b.rows;
+        const int n = static_cast<int>(rows < kTaskSketchRows ? rows : kTaskSketchRows);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int64_t row = (static_cast<int64_t>(i) * rows) / n;
+            const RowKey k = ReadKey(p.key, b, row, kKind);
+            atomicAdd(&acc[0], 1ull);
+            if (k.special >= 0) {
+                atomicAdd(&acc[1], 1ull);
+                continue;
+            }
+            const unsigned long long h = k.hash == kEmptyKey ? (k.hash ^ 1ull) : k.hash;
+            uint32_t j = static_cast<uint32_t>(h) & (kTaskSketchSlots - 1);
+            for (int probe = 0; probe < kTaskSketchSlots; ++probe) {
+                const unsigned long long prev = atomicCAS(&keys[j], kEmptyKey, h);
+                if (prev == kEmptyKey || prev == h) {
+                    atomicAdd(&counts[j], 1u);
+                    break;
                 }
-                int64_t cnt = static_cast<int64_t>(st[e.accs[0].word]);  // accs[0] is COUNT_ALL
-                if (os.countAcc >= 0) {
-                    cnt -= static_cast<int64_t>(st[e.accs[os.countAcc].word]);
-                }
-                if (os.kind == OUT_COUNT) {
-                    StoreWidth(os.values, pos, 8, static_cast<uint64_t>(cnt));
-                    continue;
-                }
-                if (cnt == 0) {
-                    SetOutNull(os.nulls, pos);
-                    StoreWidth(os.values, pos, os.outWidth == 16 ? 8 : os.outWidth, 0);
-                    if (os.outWidth == 16) {
-                        static_cast<uint64_t *>(os.values)[2 * pos + 1] = 0;
-                    }
-                    continue;
-                }
-                const AccSpec &acc = e.accs[os.src];
-                const uint64_t *w = st + acc.word;
-                switch (os.kind) {
-                    case OUT_SUM_WRAP:
-                    case OUT_MIN_INT:
-                    case OUT_MAX_INT:
-                        StoreWidth(os.values, pos, os.outWidth, w[0]);
-                        break;
-                    case OUT_SUM_DOUBLE:
-                    case OUT_AVG: {
-                        double sum = __dadd_rn(__longlong_as_double(static_cast<long long>(w[0])),
-                            __longlong_as_double(static_cast<long long>(w[1])));
-                        if (!isfinite(__longlong_as_double(static_cast<long long>(w[0])))) {
-                            sum = __longlong_as_double(static_cast<long long>(w[0]));
-                        }
-                        const double v = (os.kind == OUT_AVG) ? sum / static_cast<double>(cnt) : sum;
-                        static_cast<double *>(os.values)[pos] = v;
-                        break;
-                    }
-                    case OUT_MIN_DOUBLE:
-                    case OUT_MAX_DOUBLE: {
-                        const double v = DoubleFromOrdered(static_cast<int64_t>(w[0]));
-                        if (os.outWidth == 4) {
-                            static_cast<float *>(os.values)[pos] = static_cast<float>(v);
-                        } else {
-                            static_cast<double *>(os.values)[pos] = v;
-                        }
-                        break;
-                    }
-                    case OUT_SUM_EXACT: {
-                        WideSum ws = DecodeWide(acc, w);
-                        bool overflow = ExceedsBound(ws.mag, ws.negative, os.boundKind);
-                        if (!overflow && ExceedsBound(ws.abs, false, os.boundKind)) {
-                            // Some prefix of the row-ordered sum may have overflowed: decided by
-                            // the ordered path on the host side of this operator.
-                            if (e.forcedOverflow != nullptr) {
-                                overflow = ((e.forcedOverflow[s] >> os.pad) & 1u) != 0;
-                            } else {
-                                unsigned long long k = atomicAdd(e.nAmbiguous, 1ull);
-                                if (k < e.ambiguousCap) {
-                                    e.ambiguousSlots[k] = s;
-                                }
-                            }
-                        }
-                        unsigned __int128 mag = (static_cast<unsigned __int128>(ws.mag[1]) << 64) | ws.mag[0];
-                        if (!overflow && os.rescalePow > 0) {
-                            unsigned __int128 f = 1;
-                            for (int i = 0; i < os.rescalePow; ++i) {
-                                f *= 10;
-                            }
-                            // |mag| <= 10^38 - 1 < 2^127 and f <= 10^38: check mag * f <= bound.
-                            if (mag != 0 && mag > Dec38Max() / f) {
-                                overflow = true;
-                            } else {
-                                mag *= f;
-                            }
-                        }
-                        if (overflow) {
-                            SetOutNull(os.nulls, pos);
-                            if (!e.overflowAsNull) {
-                                SetError(e.error, 5);
-                            }
-                            mag = 0;
-                        }
-                        unsigned __int128 v = ws.negative ? (~mag + 1) : mag;
-                        if (os.outWidth == 16) {
-                            uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
-                            dst[0] = static_cast<uint64_t>(v);
-                            dst[1] = static_cast<uint64_t>(v >> 64);
-                        } else {
-                            StoreWidth(os.values, pos, os.outWidth, static_cast<uint64_t>(v));
-                        }
-                        break;
-                    }
-                    default:
-                        break;
-                }
+                j = (j + 1) & (kTaskSketchSlots - 1);
             }
         }
         __syncthreads();
+        for (int i = threadIdx.x; i < kTaskSketchSlots; i += blockDim.x) {
+            if (keys[i] == kEmptyKey) {
+                continue;
+            }
+            const unsigned int c = counts[i];
+            atomicAdd(&acc[2], 1ull);
+            if (c == 1) {
+                atomicAdd(&acc[3], 1ull);
+            } else if (c == 2) {
+                atomicAdd(&acc[4], 1ull);
+            } else if (c == 3) {
+                atomicAdd(&acc[5], 1ull);
+            } else if (c < 8) {
+                atomicAdd(&acc[6], 1ull);
+            } else {
+                atomicAdd(&acc[7], 1ull);
+                atomicAdd(&acc[9], static_cast<unsigned long long>(c));
+            }
+            atomicMax(&acc[8], static_cast<unsigned long long>(c));
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < kSketchStats; i += blockDim.x) {
+            stats[static_cast<int64_t>(task) * kSketchStats + i] = acc[i];
+        }
+        __syncthreads();
+    }
+}
+
+// Per task: occupied slots (special slots included).
+__global__ void __launch_bounds__(256) TaskCountKernel(const AggTable *tables, int32_t nTasks, int32_t keyKind,
+    uint32_t *counts)
+{
+    __shared__ unsigned int total;
+    KeySpec ks;
+    ks.kind = keyKind;
+    for (int task = blockIdx.x; task < nTasks; task += gridDim.x) {
+        if (threadIdx.x == 0) {
+            total = 0;
+        }
+        __syncthreads();
+        const AggTable t = tables[task];
+        unsigned int mine = 0;
+        for (uint64_t s = threadIdx.x; s < t.capacity + 2; s += blockDim.x) {
+            const uint64_t *slot = t.slots + s * t.slotWords;
+            mine += (s >= t.capacity) ? (t.specialUsed[s - t.capacity] != 0) : SlotOccupied(ks, slot[0]);
+        }
+        mine = __reduce_add_sync(0xffffffffu, mine);
+        if ((threadIdx.x & 31) == 0 && mine != 0) {
+            atomicAdd(&total, mine);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            counts[task] = total;
+        }
+        __syncthreads();
+    }
+}
+
+// Output region of each task: its group count rounded up to 64 rows, so that every region of the
+// shared output columns starts on a byte of their null bitmaps.
+__global__ void TaskPadKernel(const uint32_t *groups, int32_t nTasks, uint32_t *padded)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nTasks) {
+        padded[t] = (groups[t] + 63u) / 64u * 64u;
+    }
+}
+
+// Per task: the task's groups written at rows [offsets[task], offsets[task] + count) of the
+// output columns, in slot order.
+__global__ void __launch_bounds__(256) TaskExtractKernel(const __grid_constant__ AggExtract e, const AggTable *tables,
+    int32_t nTasks, const int64_t *offsets)
+{
+    __shared__ unsigned int warpCounts[8];
+    __shared__ unsigned long long running;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    for (int task = blockIdx.x; task < nTasks; task += gridDim.x) {
+        const AggTable t = tables[task];
+        if (threadIdx.x == 0) {
+            running = static_cast<unsigned long long>(offsets[task]);
+        }
+        __syncthreads();
+        const uint64_t nSlots = t.capacity + 2;
+        for (uint64_t base = 0; base < nSlots; base += blockDim.x) {
+            const uint64_t s = base + threadIdx.x;
+            bool occ = false;
+            const uint64_t *slot = nullptr;
+            if (s < nSlots) {
+                slot = t.slots + s * t.slotWords;
+                occ = (s >= t.capacity) ? (t.specialUsed[s - t.capacity] != 0) : SlotOccupied(e.key, slot[0]);
+            }
+            const unsigned int ballot = __ballot_sync(0xffffffffu, occ);
+            if (lane == 0) {
+                warpCounts[warp] = __popc(ballot);
+            }
+            __syncthreads();
+            unsigned int below = 0, total = 0;
+            for (int w = 0; w < (static_cast<int>(blockDim.x) >> 5); ++w) {
+                below += w < warp ? warpCounts[w] : 0u;
+                total += warpCounts[w];
+            }
+            if (occ) {
+                WriteGroup(e, t, s, slot, running + below + __popc(ballot & ((1u << lane) - 1u)));
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                running += total;
+            }
+            __syncthreads();
+        }
     }
 }
 
@@ -1715,6 +1906,97 @@ cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtr
 }
 
 int DeviceSMCount() { return NumSMs(); }
+
+cudaError_t LaunchAggTaskSketch(const AggLaunch &p, int32_t nTasks, unsigned long long *stats, cudaStream_t stream)
+{
+    if (nTasks <= 0) {
+        return cudaSuccess;
+    }
+    const int grid = nTasks < NumSMs() * 8 ? nTasks : NumSMs() * 8;
+    if (p.key.kind == KEY_SINGLE) {
+        TaskSketchKernel<KEY_SINGLE><<<grid, 256, 0, stream>>>(p, nTasks, stats);
+    } else {
+        TaskSketchKernel<KEY_PACKED><<<grid, 256, 0, stream>>>(p, nTasks, stats);
+    }
+    return cudaGetLastError();
+}
+
+namespace {
+// Launch shapes the autotuner chooses from: threads per CTA and the CTAs per SM the kernel is
+// compiled for (the persistent grid is that many CTAs on every SM).
+using TasksKernelFn = void (*)(AggLaunch);
+struct TasksVariant {
+    int32_t threads;
+    int32_t blocksPerSM;
+    TasksKernelFn single;
+    TasksKernelFn packed;
+};
+const TasksVariant kTasksVariants[] = {
+    {128, 8, AggTasksKernel<KEY_SINGLE, 128, 8>, AggTasksKernel<KEY_PACKED, 128, 8>},
+    {256, 4, AggTasksKernel<KEY_SINGLE, 256, 4>, AggTasksKernel<KEY_PACKED, 256, 4>},
+    {512, 2, AggTasksKernel<KEY_SINGLE, 512, 2>, AggTasksKernel<KEY_PACKED, 512, 2>},
+    {1024, 1, AggTasksKernel<KEY_SINGLE, 1024, 1>, AggTasksKernel<KEY_PACKED, 1024, 1>},
+};
+}  // namespace
+
+int32_t AggTasksVariants() { return static_cast<int32_t>(sizeof(kTasksVariants) / sizeof(kTasksVariants[0])); }
+
+void AggTasksVariantShape(int32_t v, int32_t *threads, int32_t *blocksPerSM)
+{
+    *threads = kTasksVariants[v].threads;
+    *blocksPerSM = kTasksVariants[v].blocksPerSM;
+}
+
+cudaError_t LaunchAggTasks(const AggLaunch &p, int32_t variant, cudaStream_t stream)
+{
+    if (p.nTiles <= 0) {
+        return cudaSuccess;
+    }
+    if (variant < 0 || variant >= AggTasksVariants()) {
+        return cudaErrorInvalidValue;
+    }
+    const TasksVariant &v = kTasksVariants[variant];
+    int perSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, p.key.kind == KEY_SINGLE ? v.single : v.packed, v.threads, 0);
+    perSM = perSM < 1 ? 1 : (perSM > v.blocksPerSM ? v.blocksPerSM : perSM);
+    int grid = NumSMs() * perSM;
+    if (grid > p.nTiles) {
+        grid = p.nTiles;
+    }
+    (p.key.kind == KEY_SINGLE ? v.single : v.packed)<<<grid, v.threads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggTaskCount(const AggTable *tables, int32_t nTasks, int32_t keyKind, uint32_t *counts,
+    cudaStream_t stream)
+{
+    if (nTasks <= 0) {
+        return cudaSuccess;
+    }
+    const int grid = nTasks < NumSMs() * 8 ? nTasks : NumSMs() * 8;
+    TaskCountKernel<<<grid, 256, 0, stream>>>(tables, nTasks, keyKind, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggTaskPad(const uint32_t *groups, int32_t nTasks, uint32_t *padded, cudaStream_t stream)
+{
+    if (nTasks <= 0) {
+        return cudaSuccess;
+    }
+    TaskPadKernel<<<(nTasks + 255) / 256, 256, 0, stream>>>(groups, nTasks, padded);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAggTaskExtract(const AggExtract &e, const AggTable *tables, int32_t nTasks, const int64_t *offsets,
+    cudaStream_t stream)
+{
+    if (nTasks <= 0) {
+        return cudaSuccess;
+    }
+    const int grid = nTasks < NumSMs() * 8 ? nTasks : NumSMs() * 8;
+    TaskExtractKernel<<<grid, 256, 0, stream>>>(e, tables, nTasks, offsets);
+    return cudaGetLastError();
+}
 
 int32_t AggPartSmemSlots(int32_t slotWords)
 {

@@ -23,6 +23,18 @@ cudaError_t LaunchAggPartition(const AggLaunch &p, const PartArgs &a, cudaStream
 // tabKeys / tabCounts hold kSketchCap entries.
 cudaError_t LaunchAggSketch(const AggLaunch &p, int32_t nSample, unsigned long long *tabKeys,
     unsigned int *tabCounts, unsigned long long *stats, cudaStream_t stream);
+// Batched tasks: per-task sketch (kSketchStats per task), the persistent aggregation over all
+// tasks' tiles (autotuned threads per CTA and grid), per-task group counts and extraction at
+// per-task output offsets.
+cudaError_t LaunchAggTaskSketch(const AggLaunch &p, int32_t nTasks, unsigned long long *stats, cudaStream_t stream);
+int32_t AggTasksVariants();
+void AggTasksVariantShape(int32_t variant, int32_t *threads, int32_t *blocksPerSM);
+cudaError_t LaunchAggTasks(const AggLaunch &p, int32_t variant, cudaStream_t stream);
+cudaError_t LaunchAggTaskCount(const AggTable *tables, int32_t nTasks, int32_t keyKind, uint32_t *counts,
+    cudaStream_t stream);
+cudaError_t LaunchAggTaskPad(const uint32_t *groups, int32_t nTasks, uint32_t *padded, cudaStream_t stream);
+cudaError_t LaunchAggTaskExtract(const AggExtract &e, const AggTable *tables, int32_t nTasks, const int64_t *offsets,
+    cudaStream_t stream);
 cudaError_t LaunchAggCount(const AggTable &t, int keyKind, unsigned long long *out, cudaStream_t stream);
 cudaError_t LaunchAggExtract(const AggExtract &e, cudaStream_t stream);
 // Ordered replay of order-dependent sticky-overflow groups; sets forced[slot] bit k when

@@ -156,7 +156,14 @@ struct AggLaunch {
     // partition c % nParts only, so its shared table sees only that partition's groups.
     int32_t nParts;
     const int32_t *partTileStart;
+    // Batched tasks (AggTasksKernel): batch i is task i with its own table taskTables[i]; a
+    // task whose group does not fit sets taskFailed[i] (the host re-runs it exactly).
+    const AggTable *taskTables;
+    uint32_t *taskFailed;
 };
+
+constexpr int kTaskSketchRows = 1024;   // rows sampled per task by the batched sketch
+constexpr int kTaskSketchSlots = 2048;
 
 // ---- hash partitioning of aggregation input -------------------------------------------------
 // Rows go to partition (hash >> kPartShift) & (nParts - 1); the shared tables index slots with

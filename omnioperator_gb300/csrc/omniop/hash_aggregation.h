@@ -52,6 +52,11 @@ struct AggPlan {
     bool orderDependent = false;           // has an OUT_SUM_EXACT column (sticky overflow)
 };
 
+// Kernel launch parameters of a plan (table fields as given; stats: [groups, retry count,
+// spill count, error] words, may be null).
+omg::AggLaunch MakeAggLaunch(const AggPlan &plan, uint64_t *slots, uint64_t capacity, uint32_t *special,
+    unsigned long long *stats);
+
 class HashAggregationOperatorFactory : public OperatorFactory {
 public:
     HashAggregationOperatorFactory(std::vector<uint32_t> &groupByCol, const type::DataTypes &groupInputTypes,

@@ -125,3 +125,23 @@ def test_null_handles_are_rejected():
     assert L.omg_op_add_input(None, None, None) == -1
     assert b"null" in L.omg_last_error()
     assert L.omg_batch_row_count(None) == -1
+
+
+def test_batched_aggregation_rejects_sticky_overflow_plans_and_empty_tasks():
+    """Batched tasks run only plans without order-dependent (sticky-overflow) sums; that and the
+    task list are checked before any device work."""
+    L = omg.LongType()
+    d64, d128 = omg.Decimal64Type(18, 2), omg.Decimal128Type(38, 2)
+    fac = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[d64]], [[d128]], [omg.OMNI_AGGREGATION_TYPE_SUM])
+    b = omg.make_batch([L, d64], [np.arange(10, dtype=np.int64), np.arange(10, dtype=np.int64)])
+    with pytest.raises(omg.OmgError) as ei:
+        omg.AggBatch(fac, [b])
+    assert ei.value.status == -2  # OMG_ERR_UNSUPPORTED
+    fac2 = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [omg.OMNI_AGGREGATION_TYPE_SUM])
+    empty = omg.make_batch([L, L], [np.zeros(0, np.int64), np.zeros(0, np.int64)])
+    with pytest.raises(omg.OmgError) as ei:
+        omg.AggBatch(fac2, [b, empty])
+    assert ei.value.status == -1  # OMG_ERR_INVALID_ARG
+    omg.free_batches([b, empty])
+    fac.close()
+    fac2.close()
