@@ -248,7 +248,13 @@ def run_gpu(args, rank, world):
     if args.only == "agg":
         agg = run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world)
         return dict(value=agg["value"], ms=agg["ms_per_step"], build_ms=0.0, launches=agg["gpu_launches"],
-                    roofline=agg["roofline"], clocks=None, e2e=None, agg=agg, rows=AGG_GROUPS, skew=None)
+                    roofline=agg["roofline"], clocks=None, e2e=None, agg=agg, rows=AGG_GROUPS, skew=None,
+                    batched=None)
+    if args.only == "batched":
+        bt = run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
+        arm = bt.get("batched_learned", bt["batched_plain"])
+        return dict(value=arm["value"], ms=arm["ms_per_step"], build_ms=0.0, launches=0, roofline=None, clocks=None,
+                    e2e=None, agg=None, rows=arm["groups"], skew=None, batched=bt)
     if args.only == "skew":
         sk = run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
         return dict(value=sk["learned"]["value"], ms=sk["learned"]["ms_per_step"], build_ms=0.0, launches=0,
@@ -327,8 +333,10 @@ def run_gpu(args, rank, world):
     del bkey, p1, p2, pkey, pnull, pbits
     skew = None if args.skip_skew else run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                        world, rank)
+    batched = None if args.skip_batched else run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks,
+                                                              world, rank)
     return dict(value=value, ms=ms / args.steps, build_ms=build_ms, launches=launches, roofline=roofline,
-                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew)
+                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew, batched=batched)
 
 
 def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
@@ -556,6 +564,99 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
             "learned_over_plain": round(res["learned"]["value"] / res["plain"]["value"], 3)}
 
 
+BATCH_TASKS = 10_000
+BATCH_WORKLOAD = ("batched small aggregations: 10,000 independent tasks, rows per task log-uniform [1e3, 1e6], "
+                  "int64 key uniform over a per-task domain log-uniform [10, min(rows, 1e6)], SUM and COUNT of an "
+                  "int64 value; inputs resident in HBM (one batch per task)")
+
+
+def run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank):
+    """10,000 tasks: one operator per task (sample) vs one batched launch, plain and learned sizing."""
+    from omnioperator_gb300 import sizer, sizer_train
+
+    L = omg.LongType()
+    n_tasks = BATCH_TASKS if args.batch_tasks is None else args.batch_tasks
+    keys, vals, spans = sizer_train.make_tasks(torch, n_tasks, 77 + rank, dev)
+    torch.cuda.synchronize()
+    total_rows = sum(n for _, n in spans)
+
+    def factory():
+        return omg.HashAggregationOperatorFactory(
+            [0], [L], [[1], [1]], [[L], [L]], [[L], [L]],
+            [omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_COUNT_COLUMN])
+
+    def views():
+        return [omg.wrap_device_batch([L, L], n, [keys.data_ptr() + 8 * o, vals.data_ptr() + 8 * o]) for o, n in spans]
+
+    res = {}
+    # One operator per task (the reference's structure), on a bounded sample of the tasks.
+    sample = spans[: max(1, min(len(spans), args.batch_operator_sample))]
+    fac = factory()
+    barrier()
+    t0 = time.perf_counter()
+    groups_sample = 0
+    for o, n in sample:
+        op = fac.create_operator()
+        op.set_stream(stream.cuda_stream)
+        op.set_device_output(True)
+        op.add_input(omg.wrap_device_batch([L, L], n, [keys.data_ptr() + 8 * o, vals.data_ptr() + 8 * o]))
+        outs, g = op.get_outputs(1 << 12)
+        groups_sample += g
+        omg.free_batches(outs)
+        op.delete()
+    barrier()
+    dt = max_over_ranks(time.perf_counter() - t0)
+    fac.close()
+    sample_rows = sum(n for _, n in sample)
+    res["operators"] = {"value": world * sample_rows / dt, "unit": "rows/s", "tasks": len(sample),
+                        "rows": sample_rows, "ms": round(dt * 1e3, 2)}
+
+    model_path = ROOT / "omnioperator_gb300" / "models" / "agg_task_sizer.json"
+    model = sizer.SizingModel.load(str(model_path)) if model_path.exists() else None
+    steps = max(1, min(args.steps, 5))
+    for arm in ("batched_plain", "batched_learned"):
+        if arm == "batched_learned" and model is None:
+            continue
+        fac = factory()
+        handles = views()
+        b = omg.AggBatch(fac, handles, sizer=model if arm == "batched_learned" else None,
+                         flags=omg.BATCH_DEVICE_OUTPUT)
+        barrier()
+        t0 = time.perf_counter()
+        b.run(stream.cuda_stream)  # sizing, tuning, graph capture, first run
+        outs = b.outputs()
+        omg.free_batches([x for _, x in outs])
+        first_ms = (time.perf_counter() - t0) * 1e3
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            b.run(stream.cuda_stream)  # graph replay
+            outs = b.outputs()
+            omg.free_batches([x for _, x in outs])
+        e1.record(stream)
+        barrier()
+        ms = max_over_ranks(e0.elapsed_time(e1)) / steps
+        info = b.info()
+        b.close()
+        omg.free_batches(handles)
+        fac.close()
+        res[arm] = {"value": world * total_rows / (ms / 1e3), "unit": "rows/s", "ms_per_step": round(ms, 3),
+                    "first_run_ms": round(first_ms, 1), "groups": info["groups"], "table_slots": info["table_slots"],
+                    "tasks_rerun_exactly": info["reruns"], "threads": info["threads"],
+                    "ctas_per_sm": info["ctas_per_sm"], "graph": bool(info["graph"]), "tune_ms": info["tune_us"] / 1e3,
+                    "device_ms": info["run_us"] / 1e3}
+    if model is not None:
+        model.close()
+    out = {"workload": BATCH_WORKLOAD if n_tasks == BATCH_TASKS else BATCH_WORKLOAD.replace("10,000", str(n_tasks)),
+           "tasks": n_tasks, "rows": total_rows, "steps": steps, **res}
+    if "batched_plain" in res:
+        out["batched_over_operators"] = round(res["batched_plain"]["value"] / res["operators"]["value"], 2)
+    if "batched_learned" in res:
+        out["learned_over_plain"] = round(res["batched_learned"]["value"] / res["batched_plain"]["value"], 3)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,12 +666,16 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-agg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "agg", "skew"],
+    ap.add_argument("--only", default="all", choices=["all", "agg", "skew", "batched"],
                     help="agg / skew: time only that aggregation workload (profiling runs)")
     ap.add_argument("--probe-log2", type=int, default=26, help="log2 of probe rows (profiling runs use fewer)")
     ap.add_argument("--skip-skew", action="store_true", help="skip the skewed aggregation (plain vs learned)")
     ap.add_argument("--skew-log2", type=int, default=None, help="log2 rows of the skewed aggregation (default 28)")
     ap.add_argument("--sizer", default=None, help="sizing model weights (JSON) for the learned arm")
+    ap.add_argument("--skip-batched", action="store_true", help="skip the batched small aggregations")
+    ap.add_argument("--batch-tasks", type=int, default=None, help="tasks of the batched aggregation (default 10,000)")
+    ap.add_argument("--batch-operator-sample", type=int, default=500,
+                    help="tasks run one operator each for the per-operator comparison")
     args = ap.parse_args()
     global N_PROBE
     N_PROBE = 1 << args.probe_log2
@@ -601,7 +706,7 @@ def main():
                             "l2": "inputs+outputs (1.4 GB/step) larger than L2; no flush needed",
                             "build_ms": round(r["build_ms"], 3), "output_rows_per_step": r["rows"]},
                  "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"],
-                 "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"]})
+                 "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"], "agg_batched": r["batched"]})
     print(json.dumps(line), flush=True)
 
 

@@ -87,6 +87,45 @@ def collect(torch, count: int, seed: int, n_min=1 << 20, n_max=1 << 28, d_max=1 
     return records
 
 
+def make_tasks(torch, n_tasks: int, seed: int, dev, rows_min=1000, rows_max=1_000_000, d_max=1_000_000):
+    """Batched-task workload on the GPU: per task, rows log-uniform in [rows_min, rows_max] and a
+    key domain log-uniform in [10, min(rows, d_max)], uniform keys; an int64 value column.
+    Returns (keys, values, per-task (offset, rows)) with all tasks in two device tensors."""
+    rng = np.random.default_rng(seed)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    rows = np.exp(rng.uniform(math.log(rows_min), math.log(rows_max), n_tasks)).astype(np.int64)
+    doms = np.exp(rng.uniform(math.log(10), np.log(np.minimum(rows, d_max)))).astype(np.int64)
+    doms = np.maximum(doms, 2)
+    offs = np.concatenate([[0], np.cumsum(rows)])
+    keys = torch.empty(int(offs[-1]), dtype=torch.int64, device=dev)
+    for t in range(n_tasks):
+        keys[offs[t]:offs[t + 1]] = gpu_keys(torch, gen, int(rows[t]), int(doms[t]), "uniform", 0.0, t * 7919 + seed,
+                                             dev)
+    vals = torch.randint(-10**6, 10**6, (int(offs[-1]),), generator=gen, device=dev, dtype=torch.int64)
+    return keys, vals, [(int(offs[t]), int(rows[t])) for t in range(n_tasks)]
+
+
+def collect_tasks(torch, n_tasks: int, seed: int, **kw):
+    """Per-task sizing records logged by a plain batched run (SUM and COUNT of an int64 value by
+    an int64 key, the batched-task plan)."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    keys, vals, spans = make_tasks(torch, n_tasks, seed, dev, **kw)
+    torch.cuda.synchronize()
+    L = omg.LongType()
+    fac = omg.HashAggregationOperatorFactory([0], [L], [[1], [1]], [[L], [L]], [[L], [L]],
+                                             [omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_COUNT_COLUMN])
+    batches = [omg.wrap_device_batch([L, L], n, [keys.data_ptr() + 8 * o, vals.data_ptr() + 8 * o]) for o, n in spans]
+    b = omg.AggBatch(fac, batches, flags=omg.BATCH_DEVICE_OUTPUT)
+    b.run()
+    omg.free_batches([x for _, x in b.outputs()])
+    logs = b.sizing_logs()
+    b.close()
+    omg.free_batches(batches)
+    fac.close()
+    return [(lg[:22], lg[19], {}) for lg in logs]
+
+
 def train(records, epochs=4000, lr=3e-3, seed=1):
     X, T = sz.dataset([(r, g) for r, g, _ in records])
     m = sz.SizingModel(seed=seed)
@@ -111,13 +150,20 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=4000)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--n-max-log2", type=int, default=28, help="largest workload, log2 rows")
+    ap.add_argument("--tasks", action="store_true",
+                    help="train on the per-task records of batched runs (the batched-task sizer)")
     a = ap.parse_args(argv)
     import torch
 
     torch.cuda.init()
-    print(f"collecting {a.train} training and {a.test} held-out sizing records from the plain operator")
-    tr = collect(torch, a.train, a.seed, n_max=1 << a.n_max_log2)
-    te = collect(torch, a.test, a.seed + 1, n_max=1 << a.n_max_log2)
+    if a.tasks:
+        print(f"collecting per-task sizing records from plain batched runs ({a.train}0 + {a.test}0 tasks)")
+        tr = collect_tasks(torch, 10 * a.train, a.seed)
+        te = collect_tasks(torch, 10 * a.test, a.seed + 1)
+    else:
+        print(f"collecting {a.train} training and {a.test} held-out sizing records from the plain operator")
+        tr = collect(torch, a.train, a.seed, n_max=1 << a.n_max_log2)
+        te = collect(torch, a.test, a.seed + 1, n_max=1 << a.n_max_log2)
     m, loss = train(tr, epochs=a.epochs)
     lt, pt = evaluate(m, te)
     print(f"train loss {loss:.5f}; held-out mean |log2 error|: learned {lt:.3f}, plain {pt:.3f}")
