@@ -265,6 +265,22 @@ int32_t omg_agg_batch_info(void *batch, int64_t *out, int32_t n, int32_t *writte
 /* Per task, a sizing record laid out as omg_op_get_sizing_log's (23 values per task). */
 int32_t omg_agg_batch_sizing_logs(void *batch, int64_t *out, int64_t n, int64_t *written);
 int32_t omg_agg_batch_destroy(void *batch);
+/* ---- partitioned join (no reference counterpart) ---------------------------------------
+ * LookupJoin probe strategy for the batches processed afterwards: OMG_JOIN_DIRECT (one table,
+ * the default), OMG_JOIN_HASH_PARTITIONED or OMG_JOIN_RANGE_PARTITIONED (both sides split into
+ * 2^bits partitions, 1 <= bits <= 12, each with its own small table; the range strategy takes
+ * 2^bits - 1 sorted splits).  Partitioning applies to unique builds with 8-byte keys, NULL-free
+ * build output columns and the probe key as the only probe output column; other shapes keep
+ * the direct probe.  The output row multiset does not depend on the strategy. */
+#define OMG_JOIN_DIRECT 0
+#define OMG_JOIN_HASH_PARTITIONED 1
+#define OMG_JOIN_RANGE_PARTITIONED 2
+int32_t omg_op_set_join_strategy(void *op, int32_t strategy, int32_t bits, const int64_t *splits, int32_t n_splits);
+/* Range splits learned from a sample of probe keys: a two-stage model of the keys' CDF (a small
+ * network trained on the GPU routes each key to a linear leaf); splits are its 1/2^bits quantile
+ * crossings.  Writes 2^bits - 1 sorted splits to `splits`. */
+int32_t omg_join_learn_splits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed,
+    int64_t *splits);
 /* Operator::GetStatus (operator.h:46-49): OMG_STATUS_*. */
 int32_t omg_op_status(void *op);
 /* Operator::noMoreInput / setNoMoreInput / needsInput (operator.h:117-130). */

@@ -251,6 +251,15 @@ class Operator:
         check(lib().omg_op_get_outputs(self.handle, arr, max_batches, C.byref(n), C.byref(rows)))
         return list(arr[: n.value]), rows.value
 
+    def set_join_strategy(self, strategy: int, bits: int = 12, splits=None):
+        """LookupJoin probe strategy (JOIN_DIRECT, JOIN_HASH_PARTITIONED, JOIN_RANGE_PARTITIONED)."""
+        if splits is None:
+            check(lib().omg_op_set_join_strategy(self.handle, strategy, bits, None, 0))
+        else:
+            a = np.ascontiguousarray(splits, dtype=np.int64)
+            check(lib().omg_op_set_join_strategy(self.handle, strategy, bits,
+                                                 a.ctypes.data_as(C.POINTER(C.c_int64)), len(a)))
+
     def sizing_log(self) -> dict:
         """HashAggregation sizing record (omg_op_get_sizing_log)."""
         arr = (C.c_int64 * 32)()
@@ -445,3 +454,15 @@ class AggBatch:
         if self.handle:
             check(lib().omg_agg_batch_destroy(self.handle))
             self.handle = None
+
+
+JOIN_DIRECT, JOIN_HASH_PARTITIONED, JOIN_RANGE_PARTITIONED = 0, 1, 2
+
+
+def learn_splits(sample, bits: int = 12, epochs: int = 2000, seed: int = 1) -> np.ndarray:
+    """2^bits - 1 range splits learned on the GPU from a sample of probe keys."""
+    a = np.ascontiguousarray(sample, dtype=np.int64)
+    out = np.zeros((1 << bits) - 1, dtype=np.int64)
+    check(lib().omg_join_learn_splits(a.ctypes.data_as(C.POINTER(C.c_int64)), len(a), bits, epochs, seed,
+                                      out.ctypes.data_as(C.POINTER(C.c_int64))))
+    return out

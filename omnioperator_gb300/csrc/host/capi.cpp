@@ -643,6 +643,24 @@ int32_t omg_agg_batch_destroy(void *batch)
     });
 }
 
+int32_t omg_op_set_join_strategy(void *op, int32_t strategy, int32_t bits, const int64_t *splits, int32_t n_splits)
+{
+    return Guard([&] {
+        auto *j = dynamic_cast<omniruntime::op::LookupJoinOperator *>(AsOp(op));
+        Require(j != nullptr, "not a LookupJoin operator");
+        j->SetJoinStrategy(strategy, bits, splits, n_splits);
+    });
+}
+
+int32_t omg_join_learn_splits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed,
+    int64_t *splits)
+{
+    return Guard([&] {
+        Require(sample != nullptr && splits != nullptr, "null array");
+        omg::LearnRangeSplits(sample, n, bits, epochs, seed, splits);
+    });
+}
+
 int32_t omg_batch_free_many(void *const *batches, int32_t n)
 {
     return Guard([&] {

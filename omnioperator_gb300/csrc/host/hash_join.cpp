@@ -4,8 +4,10 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <memory>
 
 #include "host/gpu_runtime.h"
+#include "kernels/join_part.h"
 #include "kernels/launch.h"
 
 namespace omniruntime {
@@ -415,6 +417,9 @@ int32_t LookupJoinOperator::AddInput(VectorBatch *vecBatch)
 
 void LookupJoinOperator::ProcessPending()
 {
+    if (strategy_ != kJoinDirect && ProcessPartitioned()) {
+        return;
+    }
     JoinBuildState &b = *f_.build;
     omg::RequireDevice();
     if (userStreamSet_) {
@@ -581,6 +586,286 @@ void LookupJoinOperator::ProcessPending()
     }
     pending_.clear();
     pendingRows_ = 0;
+}
+
+
+// ---------------------------------------------------------------------------------- partitioned
+struct JoinPartBuild {
+    int32_t kind = 0;
+    int32_t bits = 0;
+    std::vector<int64_t> hostSplits;
+    DevArray<int64_t> splits;
+    DevArray<int64_t> start;     // [P + 1] partitioned build rows
+    DevArray<int64_t> tabStart;  // [P + 1] table slab offsets
+    DevArray<uint64_t> tabKeys;
+    DevArray<int32_t> tabRow;
+    DevArray<uint8_t> pay;
+    int32_t payBytes = 0;
+    bool ok = false;  // false: this build cannot be partitioned (the direct probe is used)
+
+    omg::JoinPartFn Fn() const
+    {
+        omg::JoinPartFn f;
+        f.kind = kind;
+        f.bits = bits;
+        f.splits = kind == omg::JOIN_PART_RANGE ? splits.Get() : nullptr;
+        f.nSplits = kind == omg::JOIN_PART_RANGE ? static_cast<int32_t>(hostSplits.size()) : 0;
+        f.pad = 0;
+        return f;
+    }
+};
+
+namespace {
+int32_t PartChunks(int64_t n) { return static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(1024, n / 65536))); }
+
+std::shared_ptr<JoinPartBuild> MakePartBuild(JoinBuildState &b, const std::vector<int32_t> &buildOutputCols,
+    int32_t kind, int32_t bits, const std::vector<int64_t> &splits, cudaStream_t s)
+{
+    auto pb = std::make_shared<JoinPartBuild>();
+    pb->kind = kind;
+    pb->bits = bits;
+    pb->hostSplits = splits;
+    const int32_t P = 1 << bits;
+    const int32_t keyCol = b.hashCols[0];
+    omg::PayloadCols pay;
+    std::memset(&pay, 0, sizeof(pay));
+    pay.nCols = static_cast<int32_t>(buildOutputCols.size());
+    for (int32_t k = 0; k < pay.nCols; ++k) {
+        const int32_t c = buildOutputCols[k];
+        const int32_t w = b.buildTypes.GetType(c)->ByteWidth();
+        if (b.colHasNull[c] || (w != 1 && w != 2 && w != 4 && w != 8 && w != 16)) {
+            return pb;  // not eligible
+        }
+        pay.width[k] = w;
+        pay.cols[k] = b.colValues[c].Get();
+        pay.rowBytes += w;
+    }
+    pb->payBytes = pay.rowBytes;
+    if (kind == omg::JOIN_PART_RANGE) {
+        pb->splits.Reset(splits.size(), s);
+        CudaCheck(cudaMemcpyAsync(pb->splits.Get(), splits.data(), sizeof(int64_t) * splits.size(),
+                      cudaMemcpyHostToDevice, s),
+            "upload splits");
+    }
+    const int64_t n = b.rows;
+    const int32_t chunks = PartChunks(n);
+    DevArray<uint32_t> hist(static_cast<size_t>(chunks) * P, s);
+    DevArray<int64_t> place(static_cast<size_t>(chunks) * P, s);
+    DevArray<int64_t> pkeys(std::max<int64_t>(n, 1), s);
+    pb->start.Reset(P + 1, s);
+    pb->pay.Reset(static_cast<size_t>(std::max<int64_t>(n, 1)) * std::max(pay.rowBytes, 1) + 16, s);
+    const uint8_t *keyNulls = b.colHasNull[keyCol] ? b.colNulls[keyCol].Get() : nullptr;
+    CudaCheck(omg::LaunchKeyPartition(reinterpret_cast<const int64_t *>(b.colValues[keyCol].Get()), keyNulls, n,
+                  pb->Fn(), chunks, hist.Get(), pb->start.Get(), place.Get(), pkeys.Get(), pay, pb->pay.Get(), s),
+        "partition build keys");
+    std::vector<int64_t> start(P + 1);
+    CudaCheck(cudaMemcpyAsync(start.data(), pb->start.Get(), sizeof(int64_t) * (P + 1), cudaMemcpyDeviceToHost, s),
+        "read partition sizes");
+    CudaCheck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    std::vector<int64_t> tabStart(P + 1, 0);
+    for (int32_t p = 0; p < P; ++p) {
+        const uint64_t rows = static_cast<uint64_t>(start[p + 1] - start[p]);
+        tabStart[p + 1] = tabStart[p] + static_cast<int64_t>(std::max<uint64_t>(16, NextPow2(2 * rows)));
+    }
+    pb->tabStart.Reset(P + 1, s);
+    CudaCheck(cudaMemcpyAsync(pb->tabStart.Get(), tabStart.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s),
+        "upload table offsets");
+    pb->tabKeys.Reset(static_cast<size_t>(tabStart[P]), s);
+    pb->tabRow.Reset(static_cast<size_t>(tabStart[P]), s);
+    DevArray<int32_t> err(1, s, true);
+    CudaCheck(omg::LaunchPartTableBuild(pkeys.Get(), pb->start.Get(), P, pb->tabStart.Get(), tabStart[P],
+                  pb->tabKeys.Get(), pb->tabRow.Get(), err.Get(), s),
+        "partition tables");
+    int32_t herr = 0;
+    CudaCheck(cudaMemcpyAsync(&herr, err.Get(), sizeof(herr), cudaMemcpyDeviceToHost, s), "read build error");
+    CudaCheck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    pb->ok = herr == 0;
+    return pb;
+}
+}  // namespace
+
+void LookupJoinOperator::SetJoinStrategy(int32_t strategy, int32_t bits, const int64_t *splits, int32_t nSplits)
+{
+    if (strategy == kJoinDirect) {
+        strategy_ = kJoinDirect;
+        return;
+    }
+    if ((strategy != kJoinHashPartitioned && strategy != kJoinRangePartitioned) || bits < 1 ||
+        (1 << bits) > omg::kMaxJoinParts) {
+        throw OmniException("INVALID_ARGUMENT", "join strategy: unknown strategy or bits outside [1, 12]", -1);
+    }
+    if (strategy == kJoinRangePartitioned) {
+        if (splits == nullptr || nSplits != (1 << bits) - 1) {
+            throw OmniException("INVALID_ARGUMENT", "range partitioning needs 2^bits - 1 splits", -1);
+        }
+        for (int32_t i = 1; i < nSplits; ++i) {
+            if (splits[i] < splits[i - 1]) {
+                throw OmniException("INVALID_ARGUMENT", "range splits must be sorted", -1);
+            }
+        }
+        splits_.assign(splits, splits + nSplits);
+    } else {
+        splits_.clear();
+    }
+    strategy_ = strategy;
+    partBits_ = bits;
+}
+
+bool LookupJoinOperator::ProcessPartitioned()
+{
+    JoinBuildState &b = *f_.build;
+    const int32_t keyCol = f_.probeHashCols[0];
+    if (!b.table.unique || b.table.keyWidth != 8 || f_.probeTypes.GetType(keyCol)->ByteWidth() != 8) {
+        return false;
+    }
+    for (int32_t c : f_.probeOutputCols) {
+        if (c != keyCol) {
+            return false;
+        }
+    }
+    omg::RequireDevice();
+    if (userStreamSet_) {
+        impl_->stream.SetUser(userStream_);
+    }
+    cudaStream_t s = impl_->stream.Get();
+    const int32_t kind = strategy_ == kJoinRangePartitioned ? omg::JOIN_PART_RANGE : omg::JOIN_PART_HASH;
+    std::shared_ptr<JoinPartBuild> pb;
+    {
+        std::lock_guard<std::mutex> g(f_.partMu);
+        for (auto &x : f_.partBuilds) {
+            if (x->kind == kind && x->bits == partBits_ && x->hostSplits == splits_) {
+                pb = x;
+            }
+        }
+        if (!pb) {
+            pb = MakePartBuild(b, f_.buildOutputCols, kind, partBits_, splits_, s);
+            ++counters_[0];
+            f_.partBuilds.push_back(pb);
+        }
+    }
+    if (!pb->ok) {
+        return false;
+    }
+    // The probe key column, contiguous on the device.
+    const int64_t *keys = nullptr;
+    const uint8_t *keyNulls = nullptr;
+    int64_t n = 0;
+    DevArray<uint8_t> gathered, gatheredNulls;
+    if (pending_.size() == 1 && pending_[0]->Get(keyCol)->IsDevice()) {
+        vec::BaseVector *v = pending_[0]->Get(keyCol);
+        keys = reinterpret_cast<const int64_t *>(v->RawValues());
+        keyNulls = v->HasNull() ? v->RawNulls() : nullptr;
+        n = pending_[0]->GetRowCount();
+    } else {
+        omg::BatchTable bt;
+        bt.Build(pending_, {keyCol});
+        bt.Upload(s);
+        n = bt.TotalRows();
+        gathered.Reset(static_cast<size_t>(n) * 8 + 16, s);
+        if (bt.AnyNulls(0)) {
+            gatheredNulls.Reset(omg::NullBitmapBytes(n), s, true);
+        }
+        CudaCheck(omg::LaunchGatherColumn(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(), bt.DeviceTileOutRows(), 0,
+                      8, gathered.Get(), bt.AnyNulls(0) ? gatheredNulls.Get() : nullptr, s),
+            "gather probe keys");
+        impl_->stream.Sync();  // the batch table's staging must outlive the copy
+        keys = reinterpret_cast<const int64_t *>(gathered.Get());
+        keyNulls = bt.AnyNulls(0) ? gatheredNulls.Get() : nullptr;
+    }
+    const int32_t P = 1 << partBits_;
+    const int32_t chunks = PartChunks(n);
+    DevArray<uint32_t> hist(static_cast<size_t>(chunks) * P, s);
+    DevArray<int64_t> place(static_cast<size_t>(chunks) * P, s);
+    DevArray<int64_t> start(P + 1, s);
+    DevArray<int64_t> pkeys(std::max<int64_t>(n, 1), s);
+    omg::PayloadCols none;
+    std::memset(&none, 0, sizeof(none));
+    impl_->timer.Start(s);
+    CudaCheck(omg::LaunchKeyPartition(keys, keyNulls, n, pb->Fn(), chunks, hist.Get(), start.Get(), place.Get(),
+                  pkeys.Get(), none, nullptr, s),
+        "partition probe keys");
+    int64_t live = 0;
+    CudaCheck(cudaMemcpyAsync(&live, start.Get() + P, sizeof(live), cudaMemcpyDeviceToHost, s), "read probe rows");
+    impl_->stream.Sync();
+    // Output: the probe key (if requested) and the build output columns, in regions.
+    const size_t nProbeOut = f_.probeOutputCols.size();
+    const size_t nOut = nProbeOut + f_.buildOutputCols.size();
+    constexpr int64_t kSeg = 128;
+    const int64_t segs = (live + kSeg - 1) / kSeg;
+    const int32_t nRegions = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(omg::kMaxRegions, segs)));
+    const uint64_t regionCap = static_cast<uint64_t>((segs + nRegions - 1) / nRegions * kSeg);
+    std::vector<omg::OutColumn> cols(nOut);
+    omg::PartProbeLaunch q;
+    std::memset(&q, 0, sizeof(q));
+    q.fn = pb->Fn();
+    q.keys = pkeys.Get();
+    q.n = live;
+    q.tabStart = pb->tabStart.Get();
+    q.tabKeys = pb->tabKeys.Get();
+    q.tabRow = pb->tabRow.Get();
+    q.start = pb->start.Get();
+    q.pay = pb->pay.Get();
+    q.payBytes = pb->payBytes;
+    const uint64_t capacity = regionCap * static_cast<uint64_t>(nRegions);
+    for (size_t o = 0; o < nOut; ++o) {
+        const bool probeSide = o < nProbeOut;
+        const int32_t c = probeSide ? f_.probeOutputCols[o] : f_.buildOutputCols[o - nProbeOut];
+        const auto &t = probeSide ? f_.probeTypes.GetType(c) : f_.buildOutputTypes.GetType(static_cast<int32_t>(o - nProbeOut));
+        cols[o].type = t->GetId();
+        cols[o].width = probeSide ? 8 : b.buildTypes.GetType(c)->ByteWidth();
+        cols[o].values = omg::Buffer::NewDevice(capacity * cols[o].width + 16, s, false);
+        cols[o].nulls = nullptr;
+        cols[o].hasNull = false;
+        if (probeSide) {
+            q.keyOut = static_cast<int64_t *>(cols[o].values->Data());
+        } else {
+            q.payWidth[q.nPayOut] = cols[o].width;
+            q.payOut[q.nPayOut] = cols[o].values->Data();
+            ++q.nPayOut;
+        }
+    }
+    DevArray<unsigned long long> count(static_cast<size_t>(nRegions) * omg::kRegionStride, s, true);
+    omg::PinnedArray<unsigned long long> hostCount(static_cast<size_t>(nRegions) * omg::kRegionStride);
+    q.outCount = count.Get();
+    q.nRegions = nRegions;
+    q.regionCap = regionCap;
+    CudaCheck(omg::LaunchPartProbe(q, s), "partitioned probe");
+    impl_->timer.Stop(s);
+    counters_[0] += 5;
+    CudaCheck(cudaMemcpyAsync(hostCount.Get(), count.Get(), sizeof(unsigned long long) * count.Size(),
+                  cudaMemcpyDeviceToHost, s),
+        "read counts");
+    impl_->stream.Sync();
+    counters_[6] += impl_->timer.ElapsedNs();
+    ++counters_[7];
+    int64_t rows = 0;
+    for (int32_t r = 0; r < nRegions; ++r) {
+        const int64_t cnt = static_cast<int64_t>(hostCount[static_cast<size_t>(r) * omg::kRegionStride]);
+        if (cnt == 0) {
+            continue;
+        }
+        const int64_t first = static_cast<int64_t>(r) * static_cast<int64_t>(regionCap);
+        std::vector<omg::OutColumn> outCols = cols;
+        int64_t firstRow = first;
+        if (!deviceOutput_) {
+            outCols = omg::CopyColumnsToHost(cols, cnt, s, first);
+            firstRow = 0;
+        }
+        for (auto *ob : omg::CarveBatches(outCols, cnt, f_.rowsPerBatch, firstRow)) {
+            outputs_.push_back(ob);
+        }
+        rows += cnt;
+    }
+    if (!deviceOutput_) {
+        impl_->stream.Sync();
+    }
+    counters_[5] += rows;
+    for (auto *pbatch : pending_) {
+        vec::VectorHelper::FreeVecBatch(pbatch);
+    }
+    pending_.clear();
+    pendingRows_ = 0;
+    return true;
 }
 
 int32_t LookupJoinOperator::GetOutput(VectorBatch **outputVecBatch)

@@ -293,4 +293,74 @@ float SizingModel::Train(const float *X, const float *T, int32_t n, int32_t epoc
     return loss;
 }
 
+void LearnRangeSplits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed, int64_t *splits)
+{
+    if (n <= 0 || bits < 1 || bits > 12) {
+        throw OmniException("INVALID_ARGUMENT", "learned splits need a sample and 1 <= bits <= 12", -1);
+    }
+    std::vector<int64_t> keys(sample, sample + n);
+    std::sort(keys.begin(), keys.end());
+    const double lo = static_cast<double>(keys.front());
+    const double span = std::max(static_cast<double>(keys.back()) - lo, 1.0);
+    // Training points: up to 16,384 evenly spaced sample ranks, target = empirical CDF.
+    const int64_t m = std::min<int64_t>(n, 16384);
+    std::vector<float> X(m), T(m);
+    for (int64_t j = 0; j < m; ++j) {
+        const int64_t i = (j * n) / m;
+        X[j] = static_cast<float>((static_cast<double>(keys[i]) - lo) / span);
+        T[j] = static_cast<float>((static_cast<double>(i) + 0.5) / static_cast<double>(n));
+    }
+    SizingModel model({1, 32, 32, 1}, seed);
+    model.Train(X.data(), T.data(), static_cast<int32_t>(m), std::max(epochs, 1), 3e-3f);
+    // Two stages (a recursive model index): the network's CDF routes each key to one of K leaf
+    // models, each a least-squares line of the empirical CDF over the keys routed to it.  The
+    // network alone cannot resolve the CDF finely enough for thousands of equal ranges.
+    std::vector<float> xs(n), y1(n);
+    for (int64_t i = 0; i < n; ++i) {
+        xs[i] = static_cast<float>((static_cast<double>(keys[i]) - lo) / span);
+    }
+    model.Predict(xs.data(), static_cast<int32_t>(n), y1.data());
+    const int64_t K = std::min<int64_t>(4096, std::max<int64_t>(16, n / 32));
+    std::vector<int64_t> leaf(n);
+    std::vector<double> sx(K, 0), sy(K, 0), sxx(K, 0), sxy(K, 0), cnt(K, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t l = std::min<int64_t>(K - 1, std::max<int64_t>(0, static_cast<int64_t>(y1[i] * K)));
+        leaf[i] = l;
+        const double x = xs[i];
+        const double y = (static_cast<double>(i) + 0.5) / static_cast<double>(n);
+        sx[l] += x;
+        sy[l] += y;
+        sxx[l] += x * x;
+        sxy[l] += x * y;
+        cnt[l] += 1;
+    }
+    std::vector<double> a(K, 0), b(K, 0);
+    for (int64_t l = 0; l < K; ++l) {
+        if (cnt[l] == 0) {
+            continue;
+        }
+        const double mx = sx[l] / cnt[l];
+        const double my = sy[l] / cnt[l];
+        const double vx = sxx[l] / cnt[l] - mx * mx;
+        b[l] = (cnt[l] >= 2 && vx > 1e-18) ? (sxy[l] / cnt[l] - mx * my) / vx : 0.0;
+        a[l] = my - b[l] * mx;
+    }
+    // Predicted CDF of every sample key (made monotone), then the crossing points.
+    std::vector<double> ys(n);
+    double run = -1e300;
+    for (int64_t i = 0; i < n; ++i) {
+        run = std::max(run, a[leaf[i]] + b[leaf[i]] * xs[i]);
+        ys[i] = run;
+    }
+    const int32_t P = 1 << bits;
+    int64_t i = 0;
+    for (int32_t k = 1; k < P; ++k) {
+        const double q = static_cast<double>(k) / static_cast<double>(P);
+        while (i < n && ys[i] < q) {
+            ++i;
+        }
+        splits[k - 1] = i < n ? keys[i] : keys.back();
+    }
+}
+
 }  // namespace omg

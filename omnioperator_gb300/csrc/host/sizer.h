@@ -28,6 +28,13 @@ uint64_t SizerEstimate(const int64_t *log, float y);
 // Target of a sizing record with known group count G: log2(G / d) / 16.
 float SizerTarget(const int64_t *log, int64_t groups);
 
+// Range-partition splits learned from a key sample, a two-stage model of the keys' CDF: a network
+// 1 -> 32 -> 32 -> 1 trained on the GPU (by the same kernels) maps a normalised key to its
+// empirical CDF and routes the key to one of K leaves, each a least-squares line of the CDF over
+// its keys.  Split i (1 <= i < 2^bits) is the first sample key whose predicted CDF reaches
+// i / 2^bits (predictions made monotone by a running maximum).  Writes 2^bits - 1 sorted splits.
+void LearnRangeSplits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed, int64_t *splits);
+
 class SizingModel {
 public:
     // dims: input width, hidden widths..., 1.  Weights: He-uniform from `seed`, biases zero.

@@ -26,6 +26,12 @@ namespace omniruntime {
 namespace op {
 
 struct JoinBuildState;
+struct JoinPartBuild;
+
+// Probe strategies of a LookupJoin operator (no reference counterpart).
+constexpr int32_t kJoinDirect = 0;           // one table for the whole build (default)
+constexpr int32_t kJoinHashPartitioned = 1;  // 2^bits hash partitions per side
+constexpr int32_t kJoinRangePartitioned = 2; // 2^bits key ranges per side, from 2^bits - 1 splits
 
 class HashBuilderOperatorFactory : public OperatorFactory {
 public:
@@ -79,6 +85,10 @@ public:
     mutable omg::BufferPtr slotPayload;
     mutable omg::BufferPtr slotBits;  // ARRAY tables: occupancy bitmap of the slots
     mutable bool payloadDecided = false;
+    // Partitioned builds, one per partition function (kind, bits, splits), made by the first
+    // partitioned probe that uses it.
+    mutable std::mutex partMu;
+    mutable std::vector<std::shared_ptr<JoinPartBuild>> partBuilds;
 };
 
 class LookupJoinOperator : public Operator {
@@ -89,10 +99,19 @@ public:
     int32_t GetOutput(VectorBatch **outputVecBatch) override;
     OmniStatus Close() override;
     BlockingReason IsBlocked() override;
+    // Probe strategy for the batches processed afterwards (kJoin*; `splits` for the range
+    // strategy: 2^bits - 1 sorted keys).  A partitioned strategy applies to unique builds with
+    // 8-byte keys, NULL-free build output columns and the probe key as the only probe output;
+    // other shapes keep the direct probe.  Results do not depend on the strategy.
+    void SetJoinStrategy(int32_t strategy, int32_t bits, const int64_t *splits, int32_t nSplits);
 
 private:
     struct Impl;
     void ProcessPending();
+    bool ProcessPartitioned();
+    int32_t strategy_ = kJoinDirect;
+    int32_t partBits_ = 0;
+    std::vector<int64_t> splits_;
     const LookupJoinOperatorFactory &f_;
     std::unique_ptr<Impl> impl_;
     std::vector<VectorBatch *> pending_;
