@@ -249,12 +249,17 @@ def run_gpu(args, rank, world):
         agg = run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world)
         return dict(value=agg["value"], ms=agg["ms_per_step"], build_ms=0.0, launches=agg["gpu_launches"],
                     roofline=agg["roofline"], clocks=None, e2e=None, agg=agg, rows=AGG_GROUPS, skew=None,
-                    batched=None)
+                    batched=None, join5=None)
+    if args.only == "join5":
+        j5 = run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
+        d = j5["s=1.1"]["learned_range_partitioned"]
+        return dict(value=d["value"], ms=d["ms_per_step"], build_ms=0.0, launches=0, roofline=None, clocks=None,
+                    e2e=None, agg=None, rows=d["output_rows"], skew=None, batched=None, join5=j5)
     if args.only == "batched":
         bt = run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
         arm = bt.get("batched_learned", bt["batched_plain"])
         return dict(value=arm["value"], ms=arm["ms_per_step"], build_ms=0.0, launches=0, roofline=None, clocks=None,
-                    e2e=None, agg=None, rows=arm["groups"], skew=None, batched=bt)
+                    e2e=None, agg=None, rows=arm["groups"], skew=None, batched=bt, join5=None)
     if args.only == "skew":
         sk = run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
         return dict(value=sk["learned"]["value"], ms=sk["learned"]["ms_per_step"], build_ms=0.0, launches=0,
@@ -335,8 +340,10 @@ def run_gpu(args, rank, world):
                                                        world, rank)
     batched = None if args.skip_batched else run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                               world, rank)
+    join5 = None if args.skip_join5 else run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks,
+                                                          world, rank)
     return dict(value=value, ms=ms / args.steps, build_ms=build_ms, launches=launches, roofline=roofline,
-                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew, batched=batched)
+                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew, batched=batched, join5=join5)
 
 
 def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
@@ -564,6 +571,104 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
             "learned_over_plain": round(res["learned"]["value"] / res["plain"]["value"], 3)}
 
 
+JOIN5_BUILD = 1 << 26
+JOIN5_PROBE = 1 << 30
+JOIN5_WORKLOAD = ("skewed inner hash join: build 2^26 rows, key 2u for distinct u < 2^39, 16-byte payload (two int64); "
+                  "probe 2^30 rows, 90% a build key of Zipf(s) rank through a seeded rank->key permutation, 10% odd "
+                  "keys (no match); output (probe key, payload); 4096 partitions: direct probe vs hash partitioning "
+                  "vs learned range partitioning")
+
+
+def _bij39(x):
+    """A bijection on [0, 2^39) (odd multiplies and an xor-shift, all mod 2^39)."""
+    m = (1 << 39) - 1
+    x = (x * 0x9E3779B1) & m
+    x = x ^ (x >> 19)
+    return (x * 0x85EBCA77) & m
+
+
+def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank):
+    """cfg 5: one build, three probe distributions, three probe strategies; every strategy's output
+    must have the same row-multiset fingerprint as the direct probe's."""
+    from omnioperator_gb300 import sizer_train
+
+    L = omg.LongType()
+    nb = JOIN5_BUILD if args.join5_build_log2 is None else 1 << args.join5_build_log2
+    npb = JOIN5_PROBE if args.join5_probe_log2 is None else 1 << args.join5_probe_log2
+    g = torch.Generator(device=dev)
+    g.manual_seed(5150 + rank)
+    idx = torch.arange(nb, device=dev, dtype=torch.int64)
+    bkey = 2 * _bij39(idx)
+    pay1 = torch.randint(-2**62, 2**62, (nb,), generator=g, device=dev, dtype=torch.int64)
+    pay2 = torch.randint(-2**62, 2**62, (nb,), generator=g, device=dev, dtype=torch.int64)
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L, L], [0])
+    bop = bf.create_operator()
+    bop.set_stream(stream.cuda_stream)
+    bop.add_input(omg.wrap_device_batch([L, L, L], nb, [bkey.data_ptr(), pay1.data_ptr(), pay2.data_ptr()]))
+    bop.get_output()
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1, 2], [L, L], bf)
+    steps = max(1, min(args.steps, 3))
+    bits = 12
+    out = {"workload": JOIN5_WORKLOAD, "build_rows": nb, "probe_rows": npb, "partitions": 1 << bits, "steps": steps}
+    for s in (0.9, 1.1, 1.3):
+        cdf = sizer_train.zipf_cdf(torch, nb, s, dev)
+        pkey = torch.empty(npb, dtype=torch.int64, device=dev)
+        chunk = 1 << 26
+        for s0 in range(0, npb, chunk):
+            m = min(chunk, npb - s0)
+            r = torch.searchsorted(cdf, torch.rand(m, generator=g, device=dev, dtype=torch.float64)).clamp_(max=nb - 1)
+            hit = bkey[(r * 0x9E3779B1) & (nb - 1)]  # rank -> build row (odd multiply mod 2^26)
+            miss = 2 * torch.randint(0, 1 << 39, (m,), generator=g, device=dev, dtype=torch.int64) + 1
+            pkey[s0:s0 + m] = torch.where(torch.rand(m, generator=g, device=dev) < 0.9, hit, miss)
+        del cdf
+        torch.cuda.synchronize()
+        sample = pkey[:: max(1, npb // 65536)].cpu().numpy()
+        t0 = time.perf_counter()
+        splits = omg.learn_splits(sample, bits=bits, epochs=2000)
+        learn_ms = (time.perf_counter() - t0) * 1e3
+        per = {}
+        for name, strat in (("direct", omg.JOIN_DIRECT), ("hash_partitioned", omg.JOIN_HASH_PARTITIONED),
+                            ("learned_range_partitioned", omg.JOIN_RANGE_PARTITIONED)):
+            def step(fp=False):
+                op = pf.create_operator()
+                op.set_stream(stream.cuda_stream)
+                op.set_device_output(True)
+                op.set_join_strategy(strat, bits, splits if strat == omg.JOIN_RANGE_PARTITIONED else None)
+                op.add_input(omg.wrap_device_batch([L], npb, [pkey.data_ptr()]))
+                outs, rows = op.get_outputs(1 << 20)
+                f = omg.batches_fingerprint(outs) if fp else None
+                omg.free_batches(outs)
+                op.delete()
+                return rows, f
+            rows, fp = step(fp=True)  # warm-up (also builds the partitioned build tables) + fingerprint
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                step()
+            e1.record(stream)
+            barrier()
+            ms = max_over_ranks(e0.elapsed_time(e1)) / steps
+            per[name] = {"value": world * npb / (ms / 1e3), "unit": "rows/s", "ms_per_step": round(ms, 2),
+                         "output_rows": rows, "fingerprint": f"{fp[1]:016x}{fp[2]:016x}"}
+        ref = per["direct"]["fingerprint"]
+        assert all(v["fingerprint"] == ref and v["output_rows"] == per["direct"]["output_rows"] for v in per.values())
+        top = float(cdf_top_share(torch, nb, s, dev))
+        per["splits_learn_ms"] = round(learn_ms, 1)
+        per["top_key_share"] = round(top, 4)
+        out[f"s={s}"] = per
+        del pkey
+    pf.close()
+    bop.delete()
+    bf.close()
+    return out
+
+
+def cdf_top_share(torch, n, s, dev):
+    w = torch.arange(1, n + 1, device=dev, dtype=torch.float64).pow_(-s)
+    return 0.9 * (w[0] / w.sum()).item()
+
+
 BATCH_TASKS = 10_000
 BATCH_WORKLOAD = ("batched small aggregations: 10,000 independent tasks, rows per task log-uniform [1e3, 1e6], "
                   "int64 key uniform over a per-task domain log-uniform [10, min(rows, 1e6)], SUM and COUNT of an "
@@ -666,13 +771,16 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-agg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "agg", "skew", "batched"],
+    ap.add_argument("--only", default="all", choices=["all", "agg", "skew", "batched", "join5"],
                     help="agg / skew: time only that aggregation workload (profiling runs)")
     ap.add_argument("--probe-log2", type=int, default=26, help="log2 of probe rows (profiling runs use fewer)")
     ap.add_argument("--skip-skew", action="store_true", help="skip the skewed aggregation (plain vs learned)")
     ap.add_argument("--skew-log2", type=int, default=None, help="log2 rows of the skewed aggregation (default 28)")
     ap.add_argument("--sizer", default=None, help="sizing model weights (JSON) for the learned arm")
     ap.add_argument("--skip-batched", action="store_true", help="skip the batched small aggregations")
+    ap.add_argument("--skip-join5", action="store_true", help="skip the skewed join (partitioners)")
+    ap.add_argument("--join5-build-log2", type=int, default=None)
+    ap.add_argument("--join5-probe-log2", type=int, default=None)
     ap.add_argument("--batch-tasks", type=int, default=None, help="tasks of the batched aggregation (default 10,000)")
     ap.add_argument("--batch-operator-sample", type=int, default=500,
                     help="tasks run one operator each for the per-operator comparison")
@@ -706,7 +814,8 @@ def main():
                             "l2": "inputs+outputs (1.4 GB/step) larger than L2; no flush needed",
                             "build_ms": round(r["build_ms"], 3), "output_rows_per_step": r["rows"]},
                  "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"],
-                 "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"], "agg_batched": r["batched"]})
+                 "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"], "agg_batched": r["batched"],
+                 "join_skewed": r["join5"]})
     print(json.dumps(line), flush=True)
 
 

@@ -281,6 +281,11 @@ int32_t omg_op_set_join_strategy(void *op, int32_t strategy, int32_t bits, const
  * crossings.  Writes 2^bits - 1 sorted splits to `splits`. */
 int32_t omg_join_learn_splits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed,
     int64_t *splits);
+/* Order-independent fingerprint of the rows of n batches (host or device, same column
+ * layout): out[0] = rows, out[1], out[2] = two 64-bit sums of per-row hashes over all columns
+ * (NULLs included).  Equal row multisets give equal fingerprints (no reference counterpart;
+ * used to compare large outputs on the device). */
+int32_t omg_batches_fingerprint(void *const *batches, int32_t n, uint64_t *out);
 /* Operator::GetStatus (operator.h:46-49): OMG_STATUS_*. */
 int32_t omg_op_status(void *op);
 /* Operator::noMoreInput / setNoMoreInput / needsInput (operator.h:117-130). */

@@ -466,3 +466,11 @@ def learn_splits(sample, bits: int = 12, epochs: int = 2000, seed: int = 1) -> n
     check(lib().omg_join_learn_splits(a.ctypes.data_as(C.POINTER(C.c_int64)), len(a), bits, epochs, seed,
                                       out.ctypes.data_as(C.POINTER(C.c_int64))))
     return out
+
+
+def batches_fingerprint(batches):
+    """(rows, f1, f2): order-independent fingerprint of the rows of the batches (GPU)."""
+    arr = (C.c_void_p * max(len(batches), 1))(*batches)
+    out = (C.c_uint64 * 3)()
+    check(lib().omg_batches_fingerprint(arr, len(batches), out))
+    return tuple(out)

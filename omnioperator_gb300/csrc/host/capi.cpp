@@ -11,6 +11,7 @@
 #include "host/gpu_runtime.h"
 #include "host/sizer.h"
 #include "kernels/agg_noalloc.h"
+#include "kernels/launch.h"
 #include "omniop/batched_agg.h"
 #include "omniop/hash_aggregation.h"
 #include "omniop/hash_join.h"
@@ -658,6 +659,53 @@ int32_t omg_join_learn_splits(const int64_t *sample, int64_t n, int32_t bits, in
     return Guard([&] {
         Require(sample != nullptr && splits != nullptr, "null array");
         omg::LearnRangeSplits(sample, n, bits, epochs, seed, splits);
+    });
+}
+
+int32_t omg_batches_fingerprint(void *const *batches, int32_t n, uint64_t *out)
+{
+    return Guard([&] {
+        Require(out != nullptr && n >= 0 && (n == 0 || batches != nullptr), "null array");
+        out[0] = out[1] = out[2] = 0;
+        if (n == 0) {
+            return;
+        }
+        omg::RequireDevice();
+        std::vector<VectorBatch *> list(n);
+        for (int32_t i = 0; i < n; ++i) {
+            list[i] = static_cast<VectorBatch *>(batches[i]);
+            Require(list[i] != nullptr, "null batch");
+        }
+        const int32_t nCols = list[0]->GetVectorCount();
+        Require(nCols <= omg::kMaxInputs, "too many columns");
+        std::vector<int32_t> cols(nCols), widths(nCols);
+        for (int32_t c = 0; c < nCols; ++c) {
+            cols[c] = c;
+            widths[c] = list[0]->Get(c)->GetWidth();
+        }
+        cudaStream_t s = omg::AcquirePooledStream();
+        try {
+            omg::BatchTable bt;
+            bt.Build(list, cols);
+            bt.Upload(s);
+            omg::DevArray<int32_t> w(nCols, s);
+            omg::DevArray<unsigned long long> fp(3, s);
+            omg::CudaCheck(cudaMemcpyAsync(w.Get(), widths.data(), sizeof(int32_t) * nCols, cudaMemcpyHostToDevice, s),
+                "upload widths");
+            omg::CudaCheck(omg::LaunchFingerprint(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(), nCols, w.Get(),
+                               fp.Get(), s),
+                "fingerprint");
+            unsigned long long h[3];
+            omg::CudaCheck(cudaMemcpyAsync(h, fp.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read fingerprint");
+            omg::CudaCheck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+            out[0] = h[0];
+            out[1] = h[1];
+            out[2] = h[2];
+        } catch (...) {
+            omg::ReleasePooledStream(s);
+            throw;
+        }
+        omg::ReleasePooledStream(s);
     });
 }
 

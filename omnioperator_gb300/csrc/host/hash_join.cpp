@@ -595,6 +595,9 @@ struct JoinPartBuild {
     int32_t bits = 0;
     std::vector<int64_t> hostSplits;
     DevArray<int64_t> splits;
+    DevArray<uint16_t> lut;  // RANGE: first split index per key bucket
+    int64_t lutBase = 0;
+    int32_t lutShift = 0;
     DevArray<int64_t> start;     // [P + 1] partitioned build rows
     DevArray<int64_t> tabStart;  // [P + 1] table slab offsets
     DevArray<uint64_t> tabKeys;
@@ -610,7 +613,9 @@ struct JoinPartBuild {
         f.bits = bits;
         f.splits = kind == omg::JOIN_PART_RANGE ? splits.Get() : nullptr;
         f.nSplits = kind == omg::JOIN_PART_RANGE ? static_cast<int32_t>(hostSplits.size()) : 0;
-        f.pad = 0;
+        f.lutShift = lutShift;
+        f.lutBase = lutBase;
+        f.lut = kind == omg::JOIN_PART_RANGE ? lut.Get() : nullptr;
         return f;
     }
 };
@@ -641,11 +646,33 @@ std::shared_ptr<JoinPartBuild> MakePartBuild(JoinBuildState &b, const std::vecto
         pay.rowBytes += w;
     }
     pb->payBytes = pay.rowBytes;
+    std::vector<uint16_t> lut;
     if (kind == omg::JOIN_PART_RANGE) {
         pb->splits.Reset(splits.size(), s);
         CudaCheck(cudaMemcpyAsync(pb->splits.Get(), splits.data(), sizeof(int64_t) * splits.size(),
                       cudaMemcpyHostToDevice, s),
             "upload splits");
+        // Buckets of width 2^shift from the first split cover every split; lut[bb] = the number of
+        // splits below bucket bb's first key.
+        pb->lutBase = splits.front();
+        const uint64_t span = static_cast<uint64_t>(splits.back()) - static_cast<uint64_t>(splits.front());
+        while ((span >> pb->lutShift) >= static_cast<uint64_t>(omg::kJoinLutBuckets)) {
+            ++pb->lutShift;
+        }
+        lut.resize(omg::kJoinLutBuckets + 1);
+        size_t i = 0;
+        for (int bb = 0; bb <= omg::kJoinLutBuckets; ++bb) {
+            // offsets from the first split, unsigned (splits are sorted, so they are >= it)
+            const uint64_t first = static_cast<uint64_t>(bb) << pb->lutShift;
+            while (i < splits.size() &&
+                static_cast<uint64_t>(splits[i]) - static_cast<uint64_t>(pb->lutBase) < first) {
+                ++i;
+            }
+            lut[bb] = static_cast<uint16_t>(i);
+        }
+        pb->lut.Reset(lut.size(), s);
+        CudaCheck(cudaMemcpyAsync(pb->lut.Get(), lut.data(), sizeof(uint16_t) * lut.size(), cudaMemcpyHostToDevice, s),
+            "upload range table");
     }
     const int64_t n = b.rows;
     const int32_t chunks = PartChunks(n);

@@ -21,13 +21,26 @@ int SMs() { return DeviceSMCount(); }
 
 constexpr int kPartThreads = 512;
 
-__device__ __forceinline__ int PartOfKey(int64_t key, int32_t kind, int32_t bits, const int64_t *splits, int32_t nSplits)
+struct RangeLut {
+    const int64_t *splits;   // shared memory
+    const uint16_t *lut;     // shared memory
+    int64_t base;
+    int32_t shift;
+    int32_t nSplits;
+};
+
+__device__ __forceinline__ int PartOfKey(int64_t key, int32_t kind, int32_t bits, const RangeLut &r)
 {
     if (kind == JOIN_PART_HASH) {
         return static_cast<int>(Mix64(static_cast<uint64_t>(key)) >> (64 - bits));
     }
-    // upper_bound: the number of splits <= key.
-    int lo = 0, hi = nSplits;
+    // upper_bound (the number of splits <= key), searched within the key's bucket: the bucket's
+    // splits are [lut[b], lut[b + 1]) and every split before lut[b] is <= any key of bucket b.
+    uint64_t b = key < r.base ? 0 : ((static_cast<uint64_t>(key) - static_cast<uint64_t>(r.base)) >> r.shift);
+    b = b < static_cast<uint64_t>(kJoinLutBuckets) ? b : kJoinLutBuckets - 1;
+    int lo = r.lut[b];
+    int hi = key < r.base ? lo : r.lut[b + 1];
+    const int64_t *splits = r.splits;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (splits[mid] <= key) {
@@ -39,17 +52,27 @@ __device__ __forceinline__ int PartOfKey(int64_t key, int32_t kind, int32_t bits
     return lo;
 }
 
-// Stage the splits in shared memory (range partitioning); returns the pointer to use.
-__device__ __forceinline__ const int64_t *StageSplits(const JoinPartFn &f, int64_t *sSplits)
+// Stage the splits and the bucket table in shared memory (range partitioning).
+constexpr size_t kRangeSmem = sizeof(int64_t) * kMaxJoinSplits + sizeof(uint16_t) * (kJoinLutBuckets + 8);
+
+__device__ __forceinline__ RangeLut StageSplits(const JoinPartFn &f, unsigned char *smem)
 {
+    RangeLut r{nullptr, nullptr, f.lutBase, f.lutShift, f.nSplits};
     if (f.kind != JOIN_PART_RANGE) {
-        return nullptr;
+        return r;
     }
+    int64_t *sSplits = reinterpret_cast<int64_t *>(smem);
+    uint16_t *sLut = reinterpret_cast<uint16_t *>(smem + sizeof(int64_t) * kMaxJoinSplits);
     for (int i = threadIdx.x; i < f.nSplits; i += blockDim.x) {
         sSplits[i] = f.splits[i];
     }
+    for (int i = threadIdx.x; i <= kJoinLutBuckets; i += blockDim.x) {
+        sLut[i] = f.lut[i];
+    }
     __syncthreads();
-    return sSplits;
+    r.splits = sSplits;
+    r.lut = sLut;
+    return r;
 }
 
 // Rows [begin, end) of chunk c of a key column.
@@ -65,10 +88,9 @@ __global__ void __launch_bounds__(kPartThreads) KeyHistKernel(const int64_t *key
     const __grid_constant__ JoinPartFn f, int32_t nChunks, uint32_t *hist)
 {
     extern __shared__ unsigned char smem[];
-    int64_t *sSplits = reinterpret_cast<int64_t *>(smem);
-    unsigned int *h = reinterpret_cast<unsigned int *>(smem + sizeof(int64_t) * kMaxJoinSplits);
+    unsigned int *h = reinterpret_cast<unsigned int *>(smem + kRangeSmem);
     const int P = 1 << f.bits;
-    const int64_t *splits = StageSplits(f, sSplits);
+    const RangeLut rl = StageSplits(f, smem);
     for (int c = blockIdx.x; c < nChunks; c += gridDim.x) {
         for (int i = threadIdx.x; i < P; i += blockDim.x) {
             h[i] = 0;
@@ -78,7 +100,7 @@ __global__ void __launch_bounds__(kPartThreads) KeyHistKernel(const int64_t *key
         ChunkRange(n, nChunks, c, &b, &e);
         for (int64_t r = b + threadIdx.x; r < e; r += blockDim.x) {
             if (!NullRO(nulls, r)) {
-                atomicAdd(&h[PartOfKey(__ldg(keys + r), f.kind, f.bits, splits, f.nSplits)], 1u);
+                atomicAdd(&h[PartOfKey(__ldg(keys + r), f.kind, f.bits, rl)], 1u);
             }
         }
         __syncthreads();
@@ -179,10 +201,9 @@ __global__ void __launch_bounds__(kPartThreads) KeyScatterKernel(const int64_t *
     const __grid_constant__ PayloadCols pay, uint8_t *outPay)
 {
     extern __shared__ unsigned char smem[];
-    int64_t *sSplits = reinterpret_cast<int64_t *>(smem);
-    unsigned long long *cur = reinterpret_cast<unsigned long long *>(smem + sizeof(int64_t) * kMaxJoinSplits);
+    unsigned long long *cur = reinterpret_cast<unsigned long long *>(smem + kRangeSmem);
     const int P = 1 << f.bits;
-    const int64_t *splits = StageSplits(f, sSplits);
+    const RangeLut rl = StageSplits(f, smem);
     for (int c = blockIdx.x; c < nChunks; c += gridDim.x) {
         for (int i = threadIdx.x; i < P; i += blockDim.x) {
             cur[i] = static_cast<unsigned long long>(place[static_cast<int64_t>(c) * P + i]);
@@ -195,7 +216,7 @@ __global__ void __launch_bounds__(kPartThreads) KeyScatterKernel(const int64_t *
                 continue;
             }
             const int64_t key = __ldg(keys + r);
-            const int p = PartOfKey(key, f.kind, f.bits, splits, f.nSplits);
+            const int p = PartOfKey(key, f.kind, f.bits, rl);
             const unsigned long long pos = atomicAdd(&cur[p], 1ull);
             outKeys[pos] = key;
             if (outPay != nullptr) {
@@ -268,9 +289,8 @@ constexpr int kProbeRounds = 4;
 __global__ void __launch_bounds__(256) PartProbeKernel(const __grid_constant__ PartProbeLaunch q)
 {
     extern __shared__ unsigned char smem[];
-    int64_t *sSplits = reinterpret_cast<int64_t *>(smem);
     const JoinPartFn &f = q.fn;
-    const int64_t *splits = StageSplits(f, sSplits);
+    const RangeLut rl = StageSplits(f, smem);
     const int lane = threadIdx.x & 31;
     const unsigned int lanesBelow = (1u << lane) - 1u;
     constexpr int kSegRows = kProbeRounds * 32;
@@ -294,7 +314,7 @@ __global__ void __launch_bounds__(256) PartProbeKernel(const __grid_constant__ P
             hitRow[i] = -1;
             hitPart[i] = 0;
             if (r < q.n && static_cast<uint64_t>(key[i]) != kEmptyKey) {
-                const int p = PartOfKey(key[i], f.kind, f.bits, splits, f.nSplits);
+                const int p = PartOfKey(key[i], f.kind, f.bits, rl);
                 const int64_t t0 = __ldg(q.tabStart + p);
                 const uint64_t mask = static_cast<uint64_t>(__ldg(q.tabStart + p + 1) - t0) - 1;
                 uint64_t s = Mix64(static_cast<uint64_t>(key[i])) & mask;
@@ -352,7 +372,7 @@ __global__ void __launch_bounds__(256) PartProbeKernel(const __grid_constant__ P
     }
 }
 
-size_t SplitsSmem(const JoinPartFn &f) { return f.kind == JOIN_PART_RANGE ? sizeof(int64_t) * kMaxJoinSplits : 0; }
+size_t SplitsSmem(const JoinPartFn &f) { return f.kind == JOIN_PART_RANGE ? kRangeSmem : 0; }
 
 }  // namespace
 
@@ -362,10 +382,10 @@ cudaError_t LaunchKeyPartition(const int64_t *keys, const uint8_t *nulls, int64_
 {
     const int P = 1 << f.bits;
     static bool configured = false;
-    const size_t smemHist = sizeof(int64_t) * kMaxJoinSplits + sizeof(unsigned int) * P;
-    const size_t smemScatter = sizeof(int64_t) * kMaxJoinSplits + sizeof(unsigned long long) * P;
+    const size_t smemHist = kRangeSmem + sizeof(unsigned int) * P;
+    const size_t smemScatter = kRangeSmem + sizeof(unsigned long long) * P;
     if (!configured) {
-        const int maxBytes = static_cast<int>(sizeof(int64_t) * kMaxJoinSplits + sizeof(unsigned long long) * kMaxJoinParts);
+        const int maxBytes = static_cast<int>(kRangeSmem + sizeof(unsigned long long) * kMaxJoinParts);
         cudaError_t err = cudaFuncSetAttribute(KeyHistKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxBytes);
         if (err == cudaSuccess) {
             err = cudaFuncSetAttribute(KeyScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxBytes);
@@ -401,7 +421,7 @@ cudaError_t LaunchPartProbe(const PartProbeLaunch &q, cudaStream_t stream)
     static bool configured = false;
     if (!configured) {
         cudaError_t err = cudaFuncSetAttribute(PartProbeKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-            static_cast<int>(sizeof(int64_t) * kMaxJoinSplits));
+            static_cast<int>(kRangeSmem));
         if (err != cudaSuccess) {
             return err;
         }

@@ -19,8 +19,14 @@ struct JoinPartFn {
     int32_t bits;
     const int64_t *splits;
     int32_t nSplits;
-    int32_t pad;
+    int32_t lutShift;        // RANGE: bucket of a key = (key - lutBase) >> lutShift (clamped)
+    int64_t lutBase;
+    const uint16_t *lut;     // RANGE: [kJoinLutBuckets + 1] first split index of each bucket
 };
+
+// Range lookup table: kJoinLutBuckets buckets over [min split, max split]; a key's partition
+// is found by a binary search over the splits of its bucket only.
+constexpr int kJoinLutBuckets = 1 << 14;
 
 // Build output columns copied with the key into partition order, packed per row.
 struct PayloadCols {

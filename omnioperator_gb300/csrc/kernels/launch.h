@@ -42,6 +42,11 @@ cudaError_t LaunchAggExtract(const AggExtract &e, cudaStream_t stream);
 cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtract &e,
     const unsigned long long *ambSlots, uint32_t nAmb, uint8_t *forced, cudaStream_t stream);
 
+// ---- utilities (util.cu)
+// [0] rows, [1] and [2] two order-independent 64-bit sums of per-row column hashes.
+cudaError_t LaunchFingerprint(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, int32_t nCols,
+    const int32_t *widths, unsigned long long *out, cudaStream_t stream);
+
 // ---- join (join.cu)
 // Copy column `input` of every batch into one contiguous device array (values) and, if
 // `nullsOut` is given, one contiguous null bitmap (zeroed by the caller).

@@ -125,3 +125,21 @@ def test_learned_splits_balance_a_skewed_sample(gpu):
     counts_w = np.bincount(np.searchsorted(width, sample, side="right"), minlength=64)
     assert counts.max() < 0.5 * counts_w.max()
     assert counts.max() <= 2.5 * len(sample) / 64
+
+
+def test_fingerprint_is_order_independent_and_sensitive(gpu):
+    rng = np.random.default_rng(7)
+    a = rng.integers(-2**62, 2**62, 100_000, dtype=np.int64)
+    b = rng.integers(-2**62, 2**62, 100_000, dtype=np.int64)
+    m = rng.random(100_000) < 0.1
+    perm = rng.permutation(100_000)
+    x = [omg.make_batch([L, L], [a[:60_000], b[:60_000]], [m[:60_000], None]),
+         omg.make_batch([L, L], [a[60_000:], b[60_000:]], [m[60_000:], None])]
+    y = [omg.make_batch([L, L], [a[perm], b[perm]], [m[perm], None])]
+    b2 = b.copy()
+    b2[123] ^= 1
+    z = [omg.make_batch([L, L], [a, b2], [m, None])]
+    fx, fy, fz = omg.batches_fingerprint(x), omg.batches_fingerprint(y), omg.batches_fingerprint(z)
+    assert fx == fy and fx[0] == 100_000
+    assert fz[0] == fx[0] and fz[1:] != fx[1:]
+    omg.free_batches(x + y + z)
