@@ -15,8 +15,20 @@ The "agg" object reports the uniform-key HashAggregation the same way: 2^22 rows
 over 10,000 distinct values, SUM/COUNT/MIN/MAX(int64), SUM/AVG(double); its 101 MB input fits
 in L2, so a 512 MB buffer is rewritten between its timed steps.
 
+Further objects, each a workload of its own with its own timing:
+  agg_skewed   2^28 rows, (int32, int64) key Zipf(1.1) over 50M pairs, SUM(decimal64) ->
+               decimal128, COUNT(*), AVG(double), 2% NULLs: the table sized by the plain sketch
+               estimate vs by the learned sizing model vs by the exact group count;
+  agg_batched  10,000 independent aggregations (1e3-1e6 rows each, SUM and COUNT): one operator
+               per task (a sample) vs one batched, graph-replayed launch sized plainly or by the
+               learned task sizer;
+  join_skewed  build 2^26 (16-byte payload), probe 2^30 Zipf(s), s in {0.9, 1.1, 1.3}: the direct
+               probe vs hash partitioning vs learned range partitioning (4096 partitions), every
+               output checked against the direct probe's by a row-multiset fingerprint.
+Inputs of these legs are larger than L2.
+
 `--impl reference` times the reference's CPU algorithm (the oracle restatement; the reference
-itself does not build) on all host cores for the same workload.
+itself does not build) on all host cores for the headline workload.
 """
 from __future__ import annotations
 
