@@ -24,6 +24,9 @@ using vec::VectorBatch;
 namespace {
 constexpr uint64_t kMinTaskSlots = 64;
 constexpr int32_t kDefaultVariant = 1;  // 256 threads, 4 CTAs per SM
+// Probe limit of the task tables (sized for a load of 1/2 or less): a task whose rows need more
+// probes has outgrown its table and is re-run exactly.
+constexpr int32_t kTaskMaxProbe = 96;
 
 uint64_t NextPow2(uint64_t v)
 {
@@ -130,6 +133,7 @@ struct BatchedAggregation::Impl {
     omg::AggLaunch Launch()
     {
         omg::AggLaunch p = MakeAggLaunch(plan, slab.Get(), totalSlots - 2, specials.Get(), nullptr);
+        p.maxProbe = kTaskMaxProbe;
         p.error = reinterpret_cast<int32_t *>(scratch.Get());
         p.batches = bt.DeviceBatches();
         p.tiles = bt.DeviceTiles();

@@ -621,7 +621,13 @@ struct JoinPartBuild {
 };
 
 namespace {
-int32_t PartChunks(int64_t n) { return static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(1024, n / 65536))); }
+// Chunks of the radix passes: about 16K rows each, at least one per SM (so small inputs still fill
+// the GPU) and at most 1024 (the histogram matrix stays small).
+int32_t PartChunks(int64_t n)
+{
+    const int64_t want = std::max<int64_t>(n / 16384, omg::DeviceSMCount());
+    return static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>({1024, want, std::max<int64_t>(n, 1)})));
+}
 
 std::shared_ptr<JoinPartBuild> MakePartBuild(JoinBuildState &b, const std::vector<int32_t> &buildOutputCols,
     int32_t kind, int32_t bits, const std::vector<int64_t> &splits, cudaStream_t s)

@@ -1202,6 +1202,9 @@ __global__ void ExtractKernel(const __grid_constant__ AggExtract e)
 // taskTables[i] inside one slab.  AggTasksKernel walks the tiles of all tasks (tiles of a task are
 // adjacent); per-task sketch, count and extraction kernels run one CTA per task.
 
+// Rows per thread per step: their loads and first probes are issued together.
+constexpr int kTaskRows = 1;
+
 template <int kKind, int kThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) AggTasksKernel(const __grid_constant__ AggLaunch p)
 {
@@ -1209,18 +1212,39 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) AggTasksKernel(const __g
     const int kw = p.table.keyWords;
     for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
         const TileDesc tile = p.tiles[t];
+        // A task that already overflowed its table is re-run exactly by the host: skip its rows.
+        if (*reinterpret_cast<volatile uint32_t *>(p.taskFailed + tile.batch) != 0u) {
+            continue;
+        }
         const BatchDesc &b = p.batches[tile.batch];
         const AggTable tab = p.taskTables[tile.batch];
-        for (int r = threadIdx.x; r < tile.rows; r += blockDim.x) {
-            const int64_t row = static_cast<int64_t>(tile.row0) + r;
-            const RowIn in = LoadRow<kKind>(p, b, row);
-            bool inserted = false;
-            const int64_t g = GlobalFind(tab, p.key, in.k, p.maxProbe, p.error, &inserted, p.waitBudget, kKind);
-            if (g < 0) {
-                p.taskFailed[tile.batch] = 1u;
-                continue;
+        for (int r0 = threadIdx.x; r0 < tile.rows; r0 += kThreads * kTaskRows) {
+            RowIn in[kTaskRows];
+            int64_t g[kTaskRows];
+#pragma unroll
+            for (int k = 0; k < kTaskRows; ++k) {
+                const int r = r0 + k * kThreads;
+                if (r < tile.rows) {
+                    in[k] = LoadRow<kKind>(p, b, static_cast<int64_t>(tile.row0) + r);
+                }
             }
-            UpdateStates(p, b, row, in, tab.slots + g * sw + kw);
+#pragma unroll
+            for (int k = 0; k < kTaskRows; ++k) {
+                g[k] = -2;
+                if (r0 + k * kThreads < tile.rows) {
+                    bool inserted = false;
+                    g[k] = GlobalFind(tab, p.key, in[k].k, p.maxProbe, p.error, &inserted, p.waitBudget, kKind);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kTaskRows; ++k) {
+                if (g[k] == -1) {
+                    p.taskFailed[tile.batch] = 1u;
+                } else if (g[k] >= 0) {
+                    UpdateStates(p, b, static_cast<int64_t>(tile.row0) + r0 + k * kThreads, in[k],
+                        tab.slots + g[k] * sw + kw);
+                }
+            }
         }
     }
 }

@@ -98,9 +98,21 @@ __global__ void __launch_bounds__(kPartThreads) KeyHistKernel(const int64_t *key
         __syncthreads();
         int64_t b, e;
         ChunkRange(n, nChunks, c, &b, &e);
-        for (int64_t r = b + threadIdx.x; r < e; r += blockDim.x) {
-            if (!NullRO(nulls, r)) {
-                atomicAdd(&h[PartOfKey(__ldg(keys + r), f.kind, f.bits, rl)], 1u);
+        // Four rows per thread per step: their loads are in flight together.
+        for (int64_t r0 = b + threadIdx.x; r0 < e; r0 += 4 * static_cast<int64_t>(blockDim.x)) {
+            int64_t k4[4];
+            bool ok[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t r = r0 + j * static_cast<int64_t>(blockDim.x);
+                ok[j] = r < e && !NullRO(nulls, r);
+                k4[j] = r < e ? __ldg(keys + r) : 0;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (ok[j]) {
+                    atomicAdd(&h[PartOfKey(k4[j], f.kind, f.bits, rl)], 1u);
+                }
             }
         }
         __syncthreads();
@@ -211,20 +223,32 @@ __global__ void __launch_bounds__(kPartThreads) KeyScatterKernel(const int64_t *
         __syncthreads();
         int64_t b, e;
         ChunkRange(n, nChunks, c, &b, &e);
-        for (int64_t r = b + threadIdx.x; r < e; r += blockDim.x) {
-            if (NullRO(nulls, r)) {
-                continue;
+        for (int64_t r0 = b + threadIdx.x; r0 < e; r0 += 4 * static_cast<int64_t>(blockDim.x)) {
+            int64_t k4[4];
+            bool ok[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t r = r0 + j * static_cast<int64_t>(blockDim.x);
+                ok[j] = r < e && !NullRO(nulls, r);
+                k4[j] = r < e ? __ldg(keys + r) : 0;
             }
-            const int64_t key = __ldg(keys + r);
-            const int p = PartOfKey(key, f.kind, f.bits, rl);
-            const unsigned long long pos = atomicAdd(&cur[p], 1ull);
-            outKeys[pos] = key;
-            if (outPay != nullptr) {
-                int off = 0;
-                for (int k = 0; k < pay.nCols; ++k) {
-                    const int w = pay.width[k];
-                    CopyBytes(outPay + pos * pay.rowBytes + off, static_cast<const uint8_t *>(pay.cols[k]) + r * w, w);
-                    off += w;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (!ok[j]) {
+                    continue;
+                }
+                const int64_t r = r0 + j * static_cast<int64_t>(blockDim.x);
+                const int p = PartOfKey(k4[j], f.kind, f.bits, rl);
+                const unsigned long long pos = atomicAdd(&cur[p], 1ull);
+                outKeys[pos] = k4[j];
+                if (outPay != nullptr) {
+                    int off = 0;
+                    for (int k = 0; k < pay.nCols; ++k) {
+                        const int w = pay.width[k];
+                        CopyBytes(outPay + pos * pay.rowBytes + off, static_cast<const uint8_t *>(pay.cols[k]) + r * w,
+                            w);
+                        off += w;
+                    }
                 }
             }
         }
@@ -395,7 +419,7 @@ cudaError_t LaunchKeyPartition(const int64_t *keys, const uint8_t *nulls, int64_
         }
         configured = true;
     }
-    const int grid = nChunks < SMs() * 2 ? nChunks : SMs() * 2;
+    const int grid = nChunks < SMs() * 4 ? nChunks : SMs() * 4;
     KeyHistKernel<<<grid, kPartThreads, smemHist, stream>>>(keys, nulls, n, f, nChunks, hist);
     PartTotalsKernel<<<1, 1024, 0, stream>>>(hist, nChunks, P, start);
     PlaceKernel<<<(P + 255) / 256, 256, 0, stream>>>(hist, nChunks, P, start, place);

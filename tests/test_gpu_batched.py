@@ -73,7 +73,8 @@ def test_batched_equals_separate_aggregations(gpu):
     tasks = _tasks(1, 120, nulls=True)
     (per,), info = _run(tasks)
     _check(tasks, per)
-    assert info["tasks"] == 120 and info["graph"] == 1 and info["reruns"] == 0
+    # plain sizing may undersize a few tables; those tasks take the exact re-run path
+    assert info["tasks"] == 120 and info["graph"] == 1 and info["reruns"] <= 12
     assert info["threads"] in (128, 256, 512, 1024)
 
 
