@@ -129,16 +129,7 @@ OmniStatus HashAggregationOperatorFactory::Init()
             throw OmniException("UNSUPPORTED_ERROR", "aggregation mask columns are not supported", -2);
         }
     }
-    for (size_t i = 0; i < inputRaws_.size(); ++i) {
-        if (!inputRaws_[i]) {
-            throw OmniException("UNSUPPORTED_ERROR", "final-stage (inputRaw=false) aggregation is not supported", -2);
-        }
-    }
-    for (size_t i = 0; i < outputPartials_.size(); ++i) {
-        if (outputPartials_[i]) {
-            throw OmniException("UNSUPPORTED_ERROR", "partial (outputPartial=true) aggregation is not supported", -2);
-        }
-    }
+
     AggPlan &p = plan_;
     p = AggPlan();
     p.overflowAsNull = overflowAsNull_;
@@ -244,23 +235,88 @@ OmniStatus HashAggregationOperatorFactory::Init()
     }
     int exactIndex = 0;
     const bool spark = policy_ == SupportContainerVecRule::NOT_SUPPORT;
+    // Two-stage aggregation (group_aggregation.cpp:1182-1218): a partial stage (outputPartial)
+    // emits per-group intermediate values, a final stage (inputRaw = false) merges them.  SUM,
+    // MIN and MAX partials are their plain results; COUNT partials are counts the final stage
+    // sums (never NULL); an AVG partial is two columns, the double sum (0 for a group without
+    // values) and the count, and the final AVG is their summed sum over their summed count
+    // (average_flatim_aggregator.h:81-175,225-290, count_column_aggregator.cpp:54-160).
+    auto pushOut = [&](OutSpec o, const DataTypePtr &t) {
+        o.outType = static_cast<int16_t>(t->GetId());
+        o.outWidth = static_cast<int16_t>(t->ByteWidth());
+        p.outs.push_back(o);
+        p.outTypes.push_back(t);
+        rowBytes += o.outWidth;
+    };
     for (size_t a = 0; a < nAgg; ++a) {
         const uint32_t fn = aggFuncTypes_[a];
+        const bool raw = a < inputRaws_.size() ? static_cast<bool>(inputRaws_[a]) : true;
+        const bool partial = a < outputPartials_.size() ? static_cast<bool>(outputPartials_[a]) : false;
         const auto &outTypes = aggOutputTypes_[a];
-        if (outTypes.GetSize() != 1) {
-            throw OmniException("UNSUPPORTED_ERROR", "aggregators with several output columns are not supported", -2);
+        const bool avgPair = fn == OMNI_AGGREGATION_TYPE_AVG && partial;
+        if (outTypes.GetSize() != (avgPair ? 2 : 1)) {
+            throw OmniException("INVALID_ARGUMENT",
+                avgPair ? "a partial AVG has two output types (double sum, long count)"
+                        : "this aggregator has one output type", -1);
         }
         const DataTypePtr &outT = outTypes.GetType(0);
         OutSpec o{};
         o.outType = static_cast<int16_t>(outT->GetId());
         o.outWidth = static_cast<int16_t>(outT->ByteWidth());
         o.countAcc = -1;
+        if (!raw && (fn == OMNI_AGGREGATION_TYPE_COUNT_ALL || fn == OMNI_AGGREGATION_TYPE_COUNT_COLUMN)) {
+            // final COUNT / COUNT(*): the sum of the partial counts
+            if (aggCols_[a].size() != 1 || aggInputTypes_[a].GetSize() != 1 ||
+                !IsIntegerLike(aggInputTypes_[a].GetType(0)->GetId())) {
+                throw OmniException("INVALID_ARGUMENT", "a final COUNT reads one integer column of partial counts", -1);
+            }
+            const int in = inputFor(aggCols_[a][0], aggInputTypes_[a].GetType(0)->ByteWidth());
+            accFor(omg::ACC_NULLS, in, omg::IN_NONE, 0, 0);
+            o.kind = omg::OUT_COUNT_MERGE;
+            o.src = static_cast<int16_t>(
+                accFor(omg::ACC_ISUM, in, omg::IN_INT, aggInputTypes_[a].GetType(0)->ByteWidth(), 0));
+            pushOut(o, outT);
+            continue;
+        }
         if (fn == OMNI_AGGREGATION_TYPE_COUNT_ALL) {
             o.kind = omg::OUT_COUNT;
             o.src = 0;
             p.outs.push_back(o);
             p.outTypes.push_back(outT);
             rowBytes += o.outWidth;
+            continue;
+        }
+        if (fn == OMNI_AGGREGATION_TYPE_AVG && !raw) {
+            // final AVG over (double sum, long count) partial columns
+            if (aggCols_[a].size() != 2 || aggInputTypes_[a].GetSize() != 2 ||
+                aggInputTypes_[a].GetType(0)->GetId() != OMNI_DOUBLE ||
+                !IsIntegerLike(aggInputTypes_[a].GetType(1)->GetId())) {
+                throw OmniException("INVALID_ARGUMENT", "a final AVG reads (double sum, long count) partial columns", -1);
+            }
+            const int inSum = inputFor(aggCols_[a][0], 8);
+            const int inCnt = inputFor(aggCols_[a][1], aggInputTypes_[a].GetType(1)->ByteWidth());
+            accFor(omg::ACC_NULLS, inSum, omg::IN_NONE, 0, 0);
+            accFor(omg::ACC_NULLS, inCnt, omg::IN_NONE, 0, 0);
+            const int sumAcc = accFor(omg::ACC_DSUM, inSum, omg::IN_DOUBLE, 8, 0);
+            const int cntAcc = accFor(omg::ACC_ISUM, inCnt, omg::IN_INT, aggInputTypes_[a].GetType(1)->ByteWidth(), 0);
+            if (partial) {  // an intermediate merge: still (sum, count)
+                OutSpec s1{};
+                s1.kind = omg::OUT_AVG_PARTIAL_SUM;
+                s1.src = static_cast<int16_t>(sumAcc);
+                s1.countAcc = static_cast<int16_t>(cntAcc);
+                s1.boundKind = 1;  // countAcc holds a summed count
+                pushOut(s1, outTypes.GetType(0));
+                OutSpec s2{};
+                s2.kind = omg::OUT_COUNT_MERGE;
+                s2.src = static_cast<int16_t>(cntAcc);
+                s2.countAcc = -1;
+                pushOut(s2, outTypes.GetType(1));
+            } else {
+                o.kind = omg::OUT_AVG_MERGE;
+                o.src = static_cast<int16_t>(sumAcc);
+                o.countAcc = static_cast<int16_t>(cntAcc);
+                pushOut(o, outT);
+            }
             continue;
         }
         if (aggCols_[a].size() != 1 || aggInputTypes_[a].GetSize() != 1) {
@@ -283,6 +339,10 @@ OmniStatus HashAggregationOperatorFactory::Init()
                 o.src = 0;
                 break;
             case OMNI_AGGREGATION_TYPE_SUM: {
+                if ((!raw || partial) && (inId == OMNI_DECIMAL64 || inId == OMNI_DECIMAL128 || (!spark && inW == 8))) {
+                    throw OmniException("UNSUPPORTED_ERROR",
+                        "two-stage SUM with sticky overflow (decimal, generic-policy int64) is not supported", -2);
+                }
                 if (isDouble) {
                     o.kind = omg::OUT_SUM_DOUBLE;
                     o.src = static_cast<int16_t>(accFor(omg::ACC_DSUM, input, inKind, inW, 0));
@@ -321,8 +381,21 @@ OmniStatus HashAggregationOperatorFactory::Init()
                 if (inId == OMNI_DECIMAL64) {
                     throw OmniException("UNSUPPORTED_ERROR", "decimal AVG is not supported", -2);
                 }
-                o.kind = omg::OUT_AVG;
                 o.src = static_cast<int16_t>(accFor(omg::ACC_DSUM, input, inKind, inW, 0));
+                if (partial) {  // (double sum, long count); 0 and 0 for a group without values
+                    OutSpec s1 = o;
+                    s1.kind = omg::OUT_AVG_PARTIAL_SUM;
+                    s1.countAcc = static_cast<int16_t>(nulls);
+                    s1.boundKind = 0;  // countAcc holds the NULL count
+                    pushOut(s1, outTypes.GetType(0));
+                    OutSpec s2{};
+                    s2.kind = omg::OUT_COUNT;
+                    s2.src = 0;
+                    s2.countAcc = static_cast<int16_t>(nulls);
+                    pushOut(s2, outTypes.GetType(1));
+                    continue;
+                }
+                o.kind = omg::OUT_AVG;
                 break;
             }
             case OMNI_AGGREGATION_TYPE_MIN:

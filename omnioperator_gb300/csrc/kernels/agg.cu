@@ -1059,6 +1059,33 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
             }
             continue;
         }
+        if (os.kind == OUT_COUNT_MERGE) {
+            StoreWidth(os.values, pos, 8, st[e.accs[os.src].word]);
+            continue;
+        }
+        if (os.kind == OUT_AVG_MERGE || os.kind == OUT_AVG_PARTIAL_SUM) {
+            const uint64_t *w = st + e.accs[os.src].word;
+            double sum = __dadd_rn(__longlong_as_double(static_cast<long long>(w[0])),
+                __longlong_as_double(static_cast<long long>(w[1])));
+            if (!isfinite(__longlong_as_double(static_cast<long long>(w[0])))) {
+                sum = __longlong_as_double(static_cast<long long>(w[0]));
+            }
+            int64_t n;
+            if (os.kind == OUT_AVG_MERGE || os.boundKind == 1) {
+                n = static_cast<int64_t>(st[e.accs[os.countAcc].word]);  // summed partial counts
+            } else {
+                n = static_cast<int64_t>(st[e.accs[0].word]) - static_cast<int64_t>(st[e.accs[os.countAcc].word]);
+            }
+            if (n == 0) {
+                if (os.kind == OUT_AVG_MERGE) {
+                    SetOutNull(os.nulls, pos);
+                }
+                static_cast<double *>(os.values)[pos] = 0.0;
+            } else {
+                static_cast<double *>(os.values)[pos] = os.kind == OUT_AVG_MERGE ? sum / static_cast<double>(n) : sum;
+            }
+            continue;
+        }
         int64_t cnt = static_cast<int64_t>(st[e.accs[0].word]);  // accs[0] is COUNT_ALL
         if (os.countAcc >= 0) {
             cnt -= static_cast<int64_t>(st[e.accs[os.countAcc].word]);

@@ -207,6 +207,11 @@ enum OutKind : int16_t {
     OUT_MAX_INT = 7,
     OUT_MIN_DOUBLE = 8,
     OUT_MAX_DOUBLE = 9,
+    OUT_COUNT_MERGE = 10,      // final COUNT: the sum of partial counts (acc src, ISUM), never NULL
+    OUT_AVG_PARTIAL_SUM = 11,  // partial AVG sum: the double sum, 0 for a group without values
+                               // (count: COUNT_ALL - NULLS(countAcc), or the ISUM countAcc when
+                               // boundKind == 1)
+    OUT_AVG_MERGE = 12,        // final AVG: sum (acc src, DSUM) / count (acc countAcc, ISUM), NULL if 0
 };
 
 struct OutSpec {

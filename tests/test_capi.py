@@ -66,10 +66,18 @@ def test_factory_validation_matches_reference_rules():
     with pytest.raises(omg.OmgError) as e:
         omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [9])
     assert e.value.status == -2
-    # partial / final stages are not built
+    # two-stage decimal SUM is not built (plain int/double SUM, COUNT, MIN, MAX, AVG are)
+    d64, d128 = omg.Decimal64Type(18, 2), omg.Decimal128Type(38, 2)
     with pytest.raises(omg.OmgError) as e:
-        omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [0], output_partials=[True])
+        omg.HashAggregationOperatorFactory([0], [L], [[1]], [[d64]], [[d128]], [0], output_partials=[True])
     assert e.value.status == -2
+    # a partial AVG emits (double sum, long count): two output types
+    with pytest.raises(omg.OmgError) as e:
+        omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[omg.DoubleType()]], [omg.OMNI_AGGREGATION_TYPE_AVG],
+                                           output_partials=[True])
+    assert e.value.status == -1
+    omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[omg.DoubleType(), L]],
+                                       [omg.OMNI_AGGREGATION_TYPE_AVG], output_partials=[True]).close()
     # outer joins are not built
     with pytest.raises(omg.OmgError) as e:
         omg.HashBuilderOperatorFactory(1, [L], [0])

@@ -1,0 +1,176 @@
+"""Two-stage (partial -> final) HashAggregation on the GPU.
+
+A partial stage (outputPartial) emits per-group intermediate columns; a final stage (inputRaw =
+false) merges them (group_aggregation.cpp:1182-1218).  SUM/MIN/MAX partials are plain results,
+COUNT partials are summed, and an AVG partial is the pair (double sum, long count) that the
+final stage divides.  The reference passes the AVG pair as one container column; the flat form
+here passes it as two adjacent columns, the final AVG reading both."""
+import numpy as np
+import pytest
+
+import omnioperator_gb300 as omg
+import oracle
+from helpers import assert_agg_equal, exact_by_key, split
+
+pytestmark = pytest.mark.gpu
+
+SUM, CNT, CNT_ALL, AVG, MAX, MIN = (omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_COUNT_COLUMN,
+                                    omg.OMNI_AGGREGATION_TYPE_COUNT_ALL, omg.OMNI_AGGREGATION_TYPE_AVG,
+                                    omg.OMNI_AGGREGATION_TYPE_MAX, omg.OMNI_AGGREGATION_TYPE_MIN)
+L, D = omg.LongType(), omg.DoubleType()
+
+
+def _batches(types, cols, nulls, sizes):
+    n = len(cols[0])
+    return [omg.make_batch(types, [c[s:e] for c in cols],
+                           None if nulls is None else [None if m is None else m[s:e] for m in nulls])
+            for s, e in split(n, sizes)]
+
+
+def _run(fac, batches, strategy=None):
+    """Feed batches (ownership passes) and return the output batches."""
+    op = fac.create_operator()
+    try:
+        if strategy is not None:
+            op.set_agg_strategy(strategy, 0)
+        for b in batches:
+            op.add_input(b)
+        outs = op.drain()
+        assert op.get_status() == omg.OMNI_STATUS_FINISHED
+    finally:
+        op.delete()
+    return outs
+
+
+def _columns(batches):
+    cols = None
+    for b in batches:
+        c = omg.batch_to_numpy(b)
+        omg.free_batch(b)
+        cols = c if cols is None else [(np.concatenate([a[0], x[0]]), np.concatenate([a[1], x[1]]))
+                                       for a, x in zip(cols, c)]
+    return cols
+
+
+def test_verify_correctness_two_stage_kat():
+    """Flat form of aggregation_test.cpp:544-631: keys (j % 10, j % 10), all values 1, two partial
+    operators over 10 batches x 2000 rows each, one final operator; every group has SUM 4000,
+    AVG 1.0, COUNT 4000, MIN 1, MAX 1."""
+    funcs = [SUM, AVG, CNT, MIN, MAX]
+    keys = np.arange(2000, dtype=np.int64) % 10
+    ones = np.ones(2000, dtype=np.int64)
+    part = omg.HashAggregationOperatorFactory([0, 1], [L, L], [[2], [3], [4], [5], [6]], [[L]] * 5,
+                                              [[L], [D, L], [L], [L], [L]], funcs, output_partials=[True] * 5)
+    partials = []
+    for _ in range(2):
+        batches = [omg.make_batch([L] * 7, [keys, keys, ones, ones, ones, ones, ones]) for _ in range(10)]
+        outs = _run(part, batches)
+        assert len(outs) == 1  # one output batch per partial operator, as the reference expects
+        partials += outs
+    part.close()
+    # partial columns: k0 k1 | sum | avg sum, avg count | count | min | max
+    fin = omg.HashAggregationOperatorFactory([0, 1], [L, L], [[2], [3, 4], [5], [6], [7]],
+                                             [[L], [D, L], [L], [L], [L]], [[L], [D], [L], [L], [L]], funcs,
+                                             input_raws=[False] * 5)
+    cols = _columns(_run(fin, partials))
+    fin.close()
+    assert len(cols) == 7
+    order = np.argsort(cols[0][0])
+    assert np.array_equal(cols[0][0][order], np.arange(10)) and np.array_equal(cols[1][0][order], np.arange(10))
+    assert np.all(cols[2][0] == 4000) and np.all(cols[3][0] == 1.0) and np.all(cols[4][0] == 4000)
+    assert np.all(cols[5][0] == 1) and np.all(cols[6][0] == 1)
+    assert not any(c[1].any() for c in cols)
+
+
+def test_verify_distinct_correctness_two_stage_kat():
+    """aggregation_test.cpp:1381-1460 with its aggregation masks restated as NULL values (a row
+    whose mask is false does not reach that aggregator, exactly like a NULL value): one group,
+    COUNT 3, SUM 6, AVG 5.0, MAX 4, MIN 1 after partial -> final."""
+    key = np.ones(4, dtype=np.int64)
+    data = [np.array(v, dtype=np.int64) for v in ([10, 20, 10, 30], [1, 1, 2, 3], [3, 5, 5, 7], [4, 2, 1, 2],
+                                                   [4, 2, 1, 2])]
+    masks = [np.array(m) for m in ([1, 1, 0, 1], [1, 0, 1, 1], [1, 1, 0, 1], [1, 1, 1, 0], [1, 1, 1, 0])]
+    nulls = [None] + [m == 0 for m in masks]
+    funcs = [CNT, SUM, AVG, MAX, MIN]
+    part = omg.HashAggregationOperatorFactory([0], [L], [[1], [2], [3], [4], [5]], [[L]] * 5,
+                                              [[L], [L], [D, L], [L], [L]], funcs, output_partials=[True] * 5)
+    outs = _run(part, [omg.make_batch([L] * 6, [key] + data, nulls)])
+    part.close()
+    fin = omg.HashAggregationOperatorFactory([0], [L], [[1], [2], [3, 4], [5], [6]], [[L], [L], [D, L], [L], [L]],
+                                             [[L], [L], [D], [L], [L]], funcs, input_raws=[False] * 5)
+    cols = _columns(_run(fin, outs))
+    fin.close()
+    assert [c[0].tolist() for c in cols] == [[1], [3], [6], [5.0], [4], [1]]
+    assert not any(c[1].any() for c in cols)
+
+
+def _random_input(n, seed):
+    rng = np.random.default_rng(seed)
+    pool = rng.choice(np.arange(-2**40, 2**40, 7919, dtype=np.int64), 3000, replace=False)
+    key = pool[rng.integers(0, len(pool), n)]
+    knull = rng.random(n) < 0.01
+    key[knull] = 0
+    dead = pool[:5]  # groups whose values are all NULL
+    vlong = rng.integers(-2**62, 2**62, n, dtype=np.int64)  # large enough that SUM wraps (Spark policy)
+    vdbl = rng.standard_normal(n) * 1e3
+    vnull = (rng.random(n) < 0.1) | np.isin(key, dead)
+    dnull = (rng.random(n) < 0.1) | np.isin(key, dead)
+    return key, knull, vlong, vnull, vdbl, dnull, dead
+
+
+@pytest.mark.parametrize("strategy", [None, omg.AGG_STRATEGY_GLOBAL, omg.AGG_STRATEGY_PARTITIONED])
+def test_partial_intermediate_final_equals_single_stage(strategy):
+    """Three partial operators over disjoint row ranges -> an intermediate merge (AVG stays a
+    pair) -> a final operator; the result equals single-stage aggregation of all rows."""
+    n = 300_000
+    key, knull, vlong, vnull, vdbl, dnull, dead = _random_input(n, 11)
+    types = [L, L, D]
+    funcs = [SUM, CNT, CNT_ALL, MIN, MAX, AVG, AVG, SUM]
+    agg_cols = [[1], [1], [], [1], [1], [2], [1], [2]]
+    in_types = [[L], [L], [], [L], [L], [D], [L], [D]]
+    part_out = [[L], [L], [L], [L], [L], [D, L], [D, L], [D]]
+    part = omg.HashAggregationOperatorFactory([0], [L], agg_cols, in_types, part_out, funcs,
+                                              output_partials=[True] * len(funcs))
+    partials = []
+    thirds = [(0, n // 3), (n // 3, 2 * n // 3), (2 * n // 3, n)]
+    for i, (s, e) in enumerate(thirds):
+        batches = _batches(types, [key[s:e], vlong[s:e], vdbl[s:e]], [knull[s:e], vnull[s:e], dnull[s:e]],
+                           [4096, 1000, 3333][i:] + [4096])
+        partials += _run(part, batches, strategy)
+    part.close()
+    # partial layout: key | sum | cnt | cnt_all | min | max | avgd sum, cnt | avgl sum, cnt | sumd
+    merge_cols = [[1], [2], [3], [4], [5], [6, 7], [8, 9], [10]]
+    merge_in = [[L], [L], [L], [L], [L], [D, L], [D, L], [D]]
+    mid = omg.HashAggregationOperatorFactory([0], [L], merge_cols, merge_in, part_out, funcs,
+                                             input_raws=[False] * len(funcs), output_partials=[True] * len(funcs))
+    merged = _run(mid, partials, strategy)
+    mid.close()
+    fin_out = [[L], [L], [L], [L], [L], [D], [D], [D]]
+    fin = omg.HashAggregationOperatorFactory([0], [L], merge_cols, merge_in, fin_out, funcs,
+                                             input_raws=[False] * len(funcs))
+    cols = _columns(_run(fin, merged, strategy))
+    fin.close()
+
+    T_LONG, T_DOUBLE = oracle.T_LONG, oracle.T_DOUBLE
+    ora = oracle.hashagg([key], [T_LONG], [knull], [
+        dict(func=SUM, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=CNT, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=CNT_ALL, col=None, out_type=T_LONG),
+        dict(func=MIN, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=MAX, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=AVG, col=vdbl, in_type=T_DOUBLE, out_type=T_DOUBLE, nulls=dnull),
+        dict(func=AVG, col=vlong, in_type=T_LONG, out_type=T_DOUBLE, nulls=vnull),
+        dict(func=SUM, col=vdbl, in_type=T_DOUBLE, out_type=T_DOUBLE, nulls=dnull),
+    ])
+    exact = {5: exact_by_key([key], [knull], vdbl, ~dnull, divide_by_count=True),
+             6: exact_by_key([key], [knull], vlong.astype(np.float64), ~vnull, divide_by_count=True),
+             7: exact_by_key([key], [knull], vdbl, ~dnull)}
+    # AVG(long) sums int64 values as doubles: each partial adds one rounding of |x| <= 2^62 per row
+    # at most, covered by the Sum|x| term of the tolerance.
+    assert_agg_equal(cols, ora, 1, double_aggs=(5, 6, 7), exact=exact)
+    # all-NULL groups: SUM/MIN/MAX/AVG NULL, COUNT 0 after the merge (the partial AVG was (0, 0))
+    rows = [i for i in range(len(cols[0][0])) if not cols[0][1][i] and cols[0][0][i] in set(dead.tolist())]
+    assert len(rows) == len(dead)
+    for r in rows:
+        assert cols[1][1][r] and cols[4][1][r] and cols[5][1][r] and cols[6][1][r] and cols[7][1][r] and cols[8][1][r]
+        assert not cols[2][1][r] and cols[2][0][r] == 0 and cols[3][0][r] > 0
