@@ -162,10 +162,32 @@ int32_t omg_hashagg_factory_create(const uint32_t *group_cols, const OmgDataType
     const uint8_t *output_partials, int32_t overflow_as_null, void **out_factory);
 
 /* HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(joinType, buildTypes,
- *     buildHashCols, buildHashColsCount, operatorCount) -- operator/join/hash_builder.h:28-31. */
+ *     buildHashCols, buildHashColsCount, operatorCount) -- operator/join/hash_builder.h:28-29.
+ * join_type: OMNI_JOIN_TYPE_* (inner 0, left 1, right 2, full 3, left semi 4, left anti 5,
+ * existence 6); one key column. */
 int32_t omg_hashbuilder_factory_create(int32_t join_type, const OmgDataType *build_types,
     int32_t n_build_types, const int32_t *build_hash_cols, int32_t n_hash_cols, int32_t operator_count,
     void **out_factory);
+
+/* CreateHashBuilderOperatorFactory(joinType, buildSide, buildTypes, buildHashCols,
+ *     buildHashColsCount, operatorCount) -- operator/join/hash_builder.h:30-31.
+ * build_side: OMNI_BUILD_UNKNOWN 0, LEFT 1, RIGHT 2 (plannode/planNode.h:29-33).  A left (right)
+ * join built on its left (right) input keeps its unmatched build rows, which a
+ * LookupOuterJoin operator emits after the probes; with build side LEFT every output batch
+ * lists the build columns first. */
+int32_t omg_hashbuilder_factory_create_side(int32_t join_type, int32_t build_side,
+    const OmgDataType *build_types, int32_t n_build_types, const int32_t *build_hash_cols, int32_t n_hash_cols,
+    int32_t operator_count, void **out_factory);
+
+/* LookupOuterJoinOperatorFactory::CreateLookupOuterJoinOperatorFactory(probeTypes,
+ *     probeOutputCols, probeOutputColsCount, buildOutputCols, buildOutputTypes,
+ *     hashBuilderFactoryAddr, buildSide) -- operator/join/lookup_outer_join.h:28-33.
+ * For full joins and build-side outer joins: its operator's GetOutput emits the build rows no
+ * probe matched (NULL probe columns), once every probe operator has drained. */
+int32_t omg_lookupouterjoin_factory_create(const OmgDataType *probe_types, int32_t n_probe_types,
+    const int32_t *probe_output_cols, int32_t n_probe_output, const int32_t *build_output_cols,
+    int32_t n_build_output, const OmgDataType *build_output_types, int64_t hash_builder_factory_addr,
+    int32_t build_side, void **out_factory);
 
 /* LookupJoinOperatorFactory::CreateLookupJoinOperatorFactory(probeTypes, probeOutputCols, n,
  *     probeHashCols, n, buildOutputCols, n, buildOutputTypes, hashBuilderFactoryAddr, filterExpr,

@@ -52,6 +52,8 @@ _SIGS = {
     "omg_hashagg_factory_create": (I32, [P, P, I32, P, I32, P, P, P, P, P, P, P, P, I32, C.POINTER(P)]),
     "omg_hashbuilder_factory_create": (I32, [I32, P, I32, P, I32, I32, C.POINTER(P)]),
     "omg_lookupjoin_factory_create": (I32, [P, I32, P, I32, P, I32, P, I32, P, I64, P, I32, C.POINTER(P)]),
+    "omg_hashbuilder_factory_create_side": (I32, [I32, I32, P, I32, P, I32, I32, C.POINTER(P)]),
+    "omg_lookupouterjoin_factory_create": (I32, [P, I32, P, I32, P, I32, P, I64, I32, C.POINTER(P)]),
     "omg_factory_create_operator": (I32, [P, C.POINTER(P)]),
     "omg_factory_destroy": (I32, [P]),
     "omg_op_init": (I32, [P]),

@@ -24,7 +24,9 @@ OMNI_AGGREGATION_TYPE_SUM, OMNI_AGGREGATION_TYPE_COUNT_COLUMN = 0, 1
 OMNI_AGGREGATION_TYPE_COUNT_ALL, OMNI_AGGREGATION_TYPE_AVG = 2, 3
 OMNI_AGGREGATION_TYPE_MAX, OMNI_AGGREGATION_TYPE_MIN = 5, 6
 # JoinType (plannode/planNode.h:406-414)
-OMNI_JOIN_TYPE_INNER = 0
+OMNI_JOIN_TYPE_INNER, OMNI_JOIN_TYPE_LEFT, OMNI_JOIN_TYPE_RIGHT, OMNI_JOIN_TYPE_FULL = 0, 1, 2, 3
+OMNI_JOIN_TYPE_LEFT_SEMI, OMNI_JOIN_TYPE_LEFT_ANTI, OMNI_JOIN_TYPE_EXISTENCE = 4, 5, 6
+OMNI_BUILD_UNKNOWN, OMNI_BUILD_LEFT, OMNI_BUILD_RIGHT = 0, 1, 2
 # OmniStatus (operator/status.h:9-13)
 OMNI_STATUS_NORMAL, OMNI_STATUS_FINISHED, OMNI_STATUS_ERROR = 0, 1, -1
 # SupportContainerVecRule (util/policy.h:160-167)
@@ -372,14 +374,19 @@ class HashAggregationOperatorFactory(OperatorFactory):
 
 
 class HashBuilderOperatorFactory(OperatorFactory):
-    """HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(joinType, buildTypes,
-    buildHashCols, buildHashColsCount, operatorCount)."""
+    """HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(joinType[, buildSide],
+    buildTypes, buildHashCols, buildHashColsCount, operatorCount)."""
 
-    def __init__(self, join_type, build_types, build_hash_cols, operator_count=1):
+    def __init__(self, join_type, build_types, build_hash_cols, operator_count=1, build_side=None):
         out = C.c_void_p()
-        check(lib().omg_hashbuilder_factory_create(join_type, _types(build_types), len(build_types),
-                                                   _i32(build_hash_cols), len(build_hash_cols), operator_count,
-                                                   C.byref(out)))
+        if build_side is None:
+            check(lib().omg_hashbuilder_factory_create(join_type, _types(build_types), len(build_types),
+                                                       _i32(build_hash_cols), len(build_hash_cols), operator_count,
+                                                       C.byref(out)))
+        else:
+            check(lib().omg_hashbuilder_factory_create_side(join_type, build_side, _types(build_types),
+                                                            len(build_types), _i32(build_hash_cols),
+                                                            len(build_hash_cols), operator_count, C.byref(out)))
         super().__init__(out.value)
 
 
@@ -399,6 +406,22 @@ class LookupJoinOperatorFactory(OperatorFactory):
             _i32(probe_hash_cols), len(probe_hash_cols), _i32(build_output_cols), len(build_output_cols),
             _types(build_output_types), int(hash_builder_factory.handle), None,
             1 if is_shuffle_exchange_build_plan else 0, C.byref(out)))
+        super().__init__(out.value)
+
+
+class LookupOuterJoinOperatorFactory(OperatorFactory):
+    """LookupOuterJoinOperatorFactory::CreateLookupOuterJoinOperatorFactory(probeTypes,
+    probeOutputCols, probeOutputColsCount, buildOutputCols, buildOutputTypes,
+    hashBuilderFactoryAddr[, buildSide]): the unmatched build rows of a full or build-side outer
+    join, read after every probe operator drained."""
+
+    def __init__(self, probe_types, probe_output_cols, build_output_cols, build_output_types,
+                 hash_builder_factory: HashBuilderOperatorFactory, build_side=OMNI_BUILD_UNKNOWN):
+        out = C.c_void_p()
+        check(lib().omg_lookupouterjoin_factory_create(
+            _types(probe_types), len(probe_types), _i32(probe_output_cols), len(probe_output_cols),
+            _i32(build_output_cols), len(build_output_cols), _types(build_output_types),
+            int(hash_builder_factory.handle), build_side, C.byref(out)))
         super().__init__(out.value)
 
 

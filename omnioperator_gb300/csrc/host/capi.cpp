@@ -306,6 +306,39 @@ int32_t omg_hashbuilder_factory_create(int32_t join_type, const OmgDataType *bui
     });
 }
 
+int32_t omg_hashbuilder_factory_create_side(int32_t join_type, int32_t build_side, const OmgDataType *build_types,
+    int32_t n_build_types, const int32_t *build_hash_cols, int32_t n_hash_cols, int32_t operator_count,
+    void **out_factory)
+{
+    return Guard([&] {
+        Require(out_factory != nullptr && build_types != nullptr && n_build_types > 0, "invalid arguments");
+        auto *f = HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(
+            static_cast<omniruntime::op::JoinType>(join_type), static_cast<omniruntime::op::BuildSide>(build_side),
+            ToTypes(build_types, n_build_types), build_hash_cols, n_hash_cols, operator_count);
+        *out_factory = static_cast<OperatorFactory *>(f);
+    });
+}
+
+int32_t omg_lookupouterjoin_factory_create(const OmgDataType *probe_types, int32_t n_probe_types,
+    const int32_t *probe_output_cols, int32_t n_probe_output, const int32_t *build_output_cols, int32_t n_build_output,
+    const OmgDataType *build_output_types, int64_t hash_builder_factory_addr, int32_t build_side, void **out_factory)
+{
+    return Guard([&] {
+        Require(out_factory != nullptr && probe_types != nullptr && n_probe_types > 0 && n_probe_output >= 0 &&
+                n_build_output >= 0, "invalid arguments");
+        auto *base = reinterpret_cast<OperatorFactory *>(hash_builder_factory_addr);
+        auto *builder = dynamic_cast<HashBuilderOperatorFactory *>(base);
+        Require(builder != nullptr, "hash_builder_factory_addr is not a hash builder factory");
+        std::vector<int32_t> po(probe_output_cols, probe_output_cols + n_probe_output);
+        std::vector<int32_t> bo(build_output_cols, build_output_cols + n_build_output);
+        auto *f = omniruntime::op::LookupOuterJoinOperatorFactory::CreateLookupOuterJoinOperatorFactory(
+            ToTypes(probe_types, n_probe_types), po.data(), n_probe_output, bo.data(),
+            ToTypes(build_output_types, n_build_output), reinterpret_cast<int64_t>(builder),
+            static_cast<omniruntime::op::BuildSide>(build_side));
+        *out_factory = static_cast<OperatorFactory *>(f);
+    });
+}
+
 int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_probe_types,
     const int32_t *probe_output_cols, int32_t n_probe_output, const int32_t *probe_hash_cols, int32_t n_probe_hash,
     const int32_t *build_output_cols, int32_t n_build_output, const OmgDataType *build_output_types,

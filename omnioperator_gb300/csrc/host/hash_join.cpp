@@ -51,6 +51,8 @@ bool JoinKeyType(DataTypeId id)
 // Device-side build: contiguous build columns plus the ARRAY or HASH table.
 struct JoinBuildState {
     JoinType joinType;
+    BuildSide buildSide = OMNI_BUILD_UNKNOWN;
+    int32_t kind = omg::JOIN_KIND_INNER;  // what the probes emit (omg::JoinKind)
     DataTypes buildTypes;
     std::vector<int32_t> hashCols;
     int32_t operatorCount;
@@ -69,6 +71,9 @@ struct JoinBuildState {
     DevArray<int32_t> csr;
     omg::JoinTable table{};
     uint32_t maxDup = 0;
+    DevArray<uint8_t> visited;  // BUILD_OUTER / FULL: one byte per build row, set by the probes
+
+    bool TracksVisits() const { return kind == omg::JOIN_KIND_BUILD_OUTER || kind == omg::JOIN_KIND_FULL; }
 
     ~JoinBuildState()
     {
@@ -125,6 +130,9 @@ void JoinBuildState::Build()
     if (rows == 0) {
         built = true;
         return;
+    }
+    if (TracksVisits()) {
+        visited.Reset(static_cast<size_t>(rows), s, true);
     }
     const void *keys = colValues[keyCol].Get();
     const uint8_t *keyNulls = colHasNull[keyCol] ? colNulls[keyCol].Get() : nullptr;
@@ -219,10 +227,45 @@ void JoinBuildState::Build()
 // ------------------------------------------------------------------------------ builder
 HashBuilderOperatorFactory::HashBuilderOperatorFactory(JoinType joinType, const DataTypes &buildTypes,
     const int32_t *buildHashCols, int32_t buildHashColsCount, int32_t operatorCount)
+    : HashBuilderOperatorFactory(joinType, OMNI_BUILD_UNKNOWN, buildTypes, buildHashCols, buildHashColsCount,
+          operatorCount)
+{}
+
+HashBuilderOperatorFactory::HashBuilderOperatorFactory(JoinType joinType, BuildSide buildSide,
+    const DataTypes &buildTypes, const int32_t *buildHashCols, int32_t buildHashColsCount, int32_t operatorCount)
     : state_(new JoinBuildState())
 {
-    if (joinType != OMNI_JOIN_TYPE_INNER) {
-        throw OmniException("UNSUPPORTED_ERROR", "only inner joins are supported", -2);
+    // The probe a join type selects (lookup_join.cpp:330-411): a LEFT (RIGHT) join whose build is
+    // the left (right) input keeps the unmatched build rows (same-side outer join), otherwise the
+    // unmatched probe rows (opposite-side outer join).
+    int32_t kind;
+    switch (joinType) {
+        case OMNI_JOIN_TYPE_INNER:
+            kind = omg::JOIN_KIND_INNER;
+            break;
+        case OMNI_JOIN_TYPE_LEFT:
+        case OMNI_JOIN_TYPE_RIGHT:
+            kind = buildSide == (joinType == OMNI_JOIN_TYPE_LEFT ? OMNI_BUILD_LEFT : OMNI_BUILD_RIGHT)
+                ? omg::JOIN_KIND_BUILD_OUTER
+                : omg::JOIN_KIND_PROBE_OUTER;
+            break;
+        case OMNI_JOIN_TYPE_FULL:
+            kind = omg::JOIN_KIND_FULL;
+            break;
+        case OMNI_JOIN_TYPE_LEFT_SEMI:
+            kind = omg::JOIN_KIND_SEMI;
+            break;
+        case OMNI_JOIN_TYPE_LEFT_ANTI:
+            kind = omg::JOIN_KIND_ANTI;
+            break;
+        case OMNI_JOIN_TYPE_EXISTENCE:
+            kind = omg::JOIN_KIND_EXISTENCE;
+            break;
+        default:
+            throw OmniException("UNSUPPORTED_ERROR", "unknown join type " + std::to_string(joinType), -2);
+    }
+    if (buildSide != OMNI_BUILD_UNKNOWN && buildSide != OMNI_BUILD_LEFT && buildSide != OMNI_BUILD_RIGHT) {
+        throw OmniException("INVALID_ARGUMENT", "unknown build side", -1);
     }
     if (buildHashColsCount != 1 || buildHashCols == nullptr) {
         throw OmniException("UNSUPPORTED_ERROR", "only single-column join keys are supported", -2);
@@ -235,6 +278,8 @@ HashBuilderOperatorFactory::HashBuilderOperatorFactory(JoinType joinType, const 
         throw OmniException("UNSUPPORTED_ERROR", "unsupported join key column", -2);
     }
     state_->joinType = joinType;
+    state_->buildSide = buildSide;
+    state_->kind = kind;
     state_->buildTypes = buildTypes;
     state_->hashCols.assign(buildHashCols, buildHashCols + buildHashColsCount);
     state_->operatorCount = operatorCount;
@@ -246,6 +291,14 @@ HashBuilderOperatorFactory *HashBuilderOperatorFactory::CreateHashBuilderOperato
     const DataTypes &buildTypes, const int32_t *buildHashCols, int32_t buildHashColsCount, int32_t operatorCount)
 {
     return new HashBuilderOperatorFactory(joinType, buildTypes, buildHashCols, buildHashColsCount, operatorCount);
+}
+
+HashBuilderOperatorFactory *HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(JoinType joinType,
+    BuildSide buildSide, const DataTypes &buildTypes, const int32_t *buildHashCols, int32_t buildHashColsCount,
+    int32_t operatorCount)
+{
+    return new HashBuilderOperatorFactory(joinType, buildSide, buildTypes, buildHashCols, buildHashColsCount,
+        operatorCount);
 }
 
 Operator *HashBuilderOperatorFactory::CreateOperator()
@@ -326,7 +379,20 @@ LookupJoinOperatorFactory::LookupJoinOperatorFactory(const DataTypes &probeTypes
     if (buildOutputTypes.GetSize() != buildOutputColsCount) {
         throw OmniException("INVALID_ARGUMENT", "build output types and columns disagree", -1);
     }
-    if (probeOutputColsCount + buildOutputColsCount > omg::kMaxOutCols) {
+    const bool existence = build->kind == omg::JOIN_KIND_EXISTENCE;
+    if (build->kind == omg::JOIN_KIND_SEMI && buildOutputColsCount != 0) {
+        // The reference's plan path passes none (lookup_join.cpp:117-121); which build row a
+        // semi join would pair with a probe row is not part of its contract.
+        throw OmniException("UNSUPPORTED_ERROR", "a left semi join has no build output columns", -2);
+    }
+    if (existence) {
+        // The output is the probe columns and one BOOLEAN existence column; build output columns
+        // are not read (lookup_join.cpp:1934-1938).
+        buildOutputCols.clear();
+        buildOutputTypes = DataTypes(std::vector<DataTypePtr>{BooleanType()});
+    }
+    if (probeOutputColsCount + static_cast<int32_t>(buildOutputCols.size()) + (existence ? 1 : 0) >
+        omg::kMaxOutCols) {
         throw OmniException("UNSUPPORTED_ERROR", "too many join output columns", -2);
     }
     int32_t rowSize = 0;
@@ -336,12 +402,15 @@ LookupJoinOperatorFactory::LookupJoinOperatorFactory(const DataTypes &probeTypes
         }
         rowSize += probeTypes.GetType(c)->ByteWidth();
     }
-    for (int32_t i = 0; i < buildOutputColsCount; ++i) {
+    for (size_t i = 0; i < buildOutputCols.size(); ++i) {
         const int32_t c = buildOutputCols[i];
         if (c < 0 || c >= build->buildTypes.GetSize()) {
             throw OmniException("INVALID_ARGUMENT", "build output column out of range", -1);
         }
-        rowSize += buildOutputTypes.GetType(i)->ByteWidth();
+        rowSize += buildOutputTypes.GetType(static_cast<int32_t>(i))->ByteWidth();
+    }
+    if (existence) {
+        rowSize += 1;
     }
     rowsPerBatch = GetMaxRowCount(rowSize);
 }
@@ -440,7 +509,7 @@ void LookupJoinOperator::ProcessPending()
     bt.Upload(s);
     const int64_t probeRows = bt.TotalRows();
     const size_t nProbeOut = f_.probeOutputCols.size();
-    const size_t nOut = nProbeOut + f_.buildOutputCols.size();
+    const size_t nOut = nProbeOut + (b.kind == omg::JOIN_KIND_EXISTENCE ? 1 : f_.buildOutputCols.size());
     std::vector<omg::OutColumn> cols(nOut);
     omg::ProbeLaunch p;
     std::memset(&p, 0, sizeof(p));
@@ -450,6 +519,10 @@ void LookupJoinOperator::ProcessPending()
     p.keyInput = 0;
     p.keyWidth = f_.probeTypes.GetType(f_.probeHashCols[0])->ByteWidth();
     p.table = b.table;
+    p.joinKind = b.kind;
+    p.visited = b.TracksVisits() ? b.visited.Get() : nullptr;
+    const bool nullBuild = b.kind == omg::JOIN_KIND_PROBE_OUTER || b.kind == omg::JOIN_KIND_FULL ||
+        b.kind == omg::JOIN_KIND_ANTI;  // rows without a match carry NULL build columns
     p.nOut = static_cast<int32_t>(nOut);
     for (size_t o = 0; o < nOut; ++o) {
         omg::JoinOutCol &oc = p.out[o];
@@ -461,6 +534,12 @@ void LookupJoinOperator::ProcessPending()
             oc.width = static_cast<int16_t>(t->ByteWidth());
             cols[o].type = t->GetId();
             cols[o].hasNull = bt.AnyNulls(oc.src);
+        } else if (b.kind == omg::JOIN_KIND_EXISTENCE) {
+            oc.side = 2;
+            oc.src = 0;
+            oc.width = 1;
+            cols[o].type = OMNI_BOOLEAN;
+            cols[o].hasNull = false;
         } else {
             const size_t j = o - nProbeOut;
             const int32_t c = f_.buildOutputCols[j];
@@ -471,14 +550,14 @@ void LookupJoinOperator::ProcessPending()
             oc.buildValues = b.colValues[c].Get();
             oc.buildNulls = b.colHasNull[c] ? b.colNulls[c].Get() : nullptr;
             cols[o].type = t->GetId();
-            cols[o].hasNull = b.colHasNull[c];
+            cols[o].hasNull = b.colHasNull[c] || nullBuild;
         }
         cols[o].width = oc.width;
     }
     // Unique build keys and <= 8 bytes of NULL-free build output per row: fetch the build
     // values with the table entry from a per-slot packed copy (built once per factory).
     {
-        bool eligible = b.table.unique && nOut > nProbeOut;
+        bool eligible = b.table.unique && nOut > nProbeOut && b.kind == omg::JOIN_KIND_INNER;
         int shift = 0;
         for (size_t o = nProbeOut; o < nOut && eligible; ++o) {
             const int w = p.out[o].width;
@@ -571,6 +650,9 @@ void LookupJoinOperator::ProcessPending()
             for (auto &c : outCols) {
                 c.hasNull = false;  // host vectors: HasNull() scans the bitmap
             }
+        }
+        if (b.buildSide == OMNI_BUILD_LEFT) {
+            std::rotate(outCols.begin(), outCols.begin() + static_cast<std::ptrdiff_t>(nProbeOut), outCols.end());
         }
         for (auto *ob : omg::CarveBatches(outCols, n, f_.rowsPerBatch, firstRow)) {
             outputs_.push_back(ob);
@@ -748,7 +830,8 @@ bool LookupJoinOperator::ProcessPartitioned()
 {
     JoinBuildState &b = *f_.build;
     const int32_t keyCol = f_.probeHashCols[0];
-    if (!b.table.unique || b.table.keyWidth != 8 || f_.probeTypes.GetType(keyCol)->ByteWidth() != 8) {
+    if (!b.table.unique || b.table.keyWidth != 8 || f_.probeTypes.GetType(keyCol)->ByteWidth() != 8 ||
+        b.kind != omg::JOIN_KIND_INNER || b.buildSide == OMNI_BUILD_LEFT) {
         return false;
     }
     for (int32_t c : f_.probeOutputCols) {
@@ -913,6 +996,189 @@ int32_t LookupJoinOperator::GetOutput(VectorBatch **outputVecBatch)
         outputs_.pop_front();
     }
     if (outputs_.empty() && pending_.empty() && noMoreInput_) {
+        SetStatus(OMNI_STATUS_FINISHED);
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------------------ outer join
+LookupOuterJoinOperatorFactory::LookupOuterJoinOperatorFactory(const DataTypes &probeTypes,
+    const int32_t *probeOutputCols, int32_t probeOutputColsCount, const int32_t *buildOutputCols_,
+    const DataTypes &buildOutputTypes_, HashBuilderOperatorFactory *builder, BuildSide buildSide_)
+    : buildOutputTypes(buildOutputTypes_), build(builder->GetBuildState()), buildSide(buildSide_)
+{
+    if (!build->TracksVisits()) {
+        throw OmniException("UNSUPPORTED_ERROR",
+            "the outer-join operator follows a full join or a build-side outer join", -2);
+    }
+    std::vector<DataTypePtr> pt;
+    int32_t rowSize = 0;
+    for (int32_t i = 0; i < probeOutputColsCount; ++i) {
+        const int32_t c = probeOutputCols[i];
+        if (c < 0 || c >= probeTypes.GetSize()) {
+            throw OmniException("INVALID_ARGUMENT", "probe output column out of range", -1);
+        }
+        pt.push_back(probeTypes.GetType(c));
+        rowSize += probeTypes.GetType(c)->ByteWidth();
+    }
+    probeOutputTypes = DataTypes(pt);
+    const int32_t nBuild = buildOutputTypes.GetSize();
+    buildOutputCols.assign(buildOutputCols_, buildOutputCols_ + nBuild);
+    for (int32_t i = 0; i < nBuild; ++i) {
+        const int32_t c = buildOutputCols[i];
+        if (c < 0 || c >= build->buildTypes.GetSize() ||
+            build->buildTypes.GetType(c)->ByteWidth() != buildOutputTypes.GetType(i)->ByteWidth()) {
+            throw OmniException("INVALID_ARGUMENT", "build output column out of range", -1);
+        }
+        rowSize += buildOutputTypes.GetType(i)->ByteWidth();
+    }
+    // lookup_outer_join.cpp:111-118: a row of no columns counts as DEFAULT_ROW_SIZE (4 bytes).
+    rowsPerBatch = GetMaxRowCount(probeOutputColsCount + nBuild == 0 ? 4 : rowSize);
+}
+
+LookupOuterJoinOperatorFactory *LookupOuterJoinOperatorFactory::CreateLookupOuterJoinOperatorFactory(
+    const DataTypes &probeTypes, int32_t *probeOutputCols, int32_t probeOutputColsCount, int32_t *buildOutputCols,
+    const DataTypes &buildOutputTypes, int64_t hashBuilderFactoryAddr)
+{
+    return CreateLookupOuterJoinOperatorFactory(probeTypes, probeOutputCols, probeOutputColsCount, buildOutputCols,
+        buildOutputTypes, hashBuilderFactoryAddr, OMNI_BUILD_UNKNOWN);
+}
+
+LookupOuterJoinOperatorFactory *LookupOuterJoinOperatorFactory::CreateLookupOuterJoinOperatorFactory(
+    const DataTypes &probeTypes, int32_t *probeOutputCols, int32_t probeOutputColsCount, int32_t *buildOutputCols,
+    const DataTypes &buildOutputTypes, int64_t hashBuilderFactoryAddr, BuildSide buildSide)
+{
+    auto *builder = reinterpret_cast<HashBuilderOperatorFactory *>(hashBuilderFactoryAddr);
+    if (builder == nullptr) {
+        throw OmniException("INVALID_ARGUMENT", "null hash builder factory", -1);
+    }
+    return new LookupOuterJoinOperatorFactory(probeTypes, probeOutputCols, probeOutputColsCount, buildOutputCols,
+        buildOutputTypes, builder, buildSide);
+}
+
+Operator *LookupOuterJoinOperatorFactory::CreateOperator() { return new LookupOuterJoinOperator(*this); }
+
+struct LookupOuterJoinOperator::Impl {
+    omg::OpStream stream;
+};
+
+LookupOuterJoinOperator::LookupOuterJoinOperator(const LookupOuterJoinOperatorFactory &f) : f_(f), impl_(new Impl()) {}
+
+LookupOuterJoinOperator::~LookupOuterJoinOperator() { Close(); }
+
+OmniStatus LookupOuterJoinOperator::Close()
+{
+    for (auto *b : outputs_) {
+        vec::VectorHelper::FreeVecBatch(b);
+    }
+    outputs_.clear();
+    return OMNI_STATUS_NORMAL;
+}
+
+int32_t LookupOuterJoinOperator::AddInput(VectorBatch *vecBatch)
+{
+    if (vecBatch != nullptr) {
+        vec::VectorHelper::FreeVecBatch(vecBatch);
+    }
+    return 0;
+}
+
+// Every build row no probe marked, in build-row order, as output batches: probe columns NULL,
+// build columns gathered on the device.
+void LookupOuterJoinOperator::Prepare()
+{
+    JoinBuildState &b = *f_.build;
+    {
+        std::lock_guard<std::mutex> g(b.mu);
+        if (!b.built) {
+            throw OmniException("OPERATOR_RUNTIME_ERROR", "the outer-join rows are read before the build finished", -6);
+        }
+    }
+    prepared_ = true;
+    if (b.rows == 0) {
+        return;
+    }
+    omg::RequireDevice();
+    if (userStreamSet_) {
+        impl_->stream.SetUser(userStream_);
+    }
+    cudaStream_t s = impl_->stream.Get();
+    const int64_t n = b.rows;
+    DevArray<uint32_t> flags(static_cast<size_t>(n), s);
+    DevArray<int64_t> offsets(static_cast<size_t>(n), s);
+    DevArray<int64_t> blockSums(static_cast<size_t>((n + 1023) / 1024 + 1), s);
+    DevArray<long long> total(1, s, true);
+    CudaCheck(omg::LaunchUnvisitedFlags(b.visited.Get(), n, flags.Get(), s), "unvisited flags");
+    CudaCheck(omg::LaunchScanCounts(flags.Get(), n, offsets.Get(), blockSums.Get(), total.Get(), s), "scan flags");
+    long long m = 0;
+    CudaCheck(cudaMemcpyAsync(&m, total.Get(), sizeof(m), cudaMemcpyDeviceToHost, s), "read unvisited count");
+    impl_->stream.Sync();
+    ++counters_[0];
+    if (m == 0) {
+        return;
+    }
+    DevArray<int32_t> rows(static_cast<size_t>(m), s);
+    CudaCheck(omg::LaunchUnvisitedRows(b.visited.Get(), offsets.Get(), n, rows.Get(), s), "unvisited rows");
+    const int32_t nProbe = f_.probeOutputTypes.GetSize();
+    const int32_t nBuild = f_.buildOutputTypes.GetSize();
+    std::vector<omg::OutColumn> cols(static_cast<size_t>(nProbe + nBuild));
+    for (int32_t o = 0; o < nProbe + nBuild; ++o) {
+        omg::OutColumn &c = cols[o];
+        const bool probe = o < nProbe;
+        const auto &t = probe ? f_.probeOutputTypes.GetType(o) : f_.buildOutputTypes.GetType(o - nProbe);
+        c.type = t->GetId();
+        c.width = t->ByteWidth();
+        c.values = omg::Buffer::NewDevice(static_cast<size_t>(m) * c.width + 16, s, probe);
+        if (probe) {
+            c.hasNull = true;
+            c.nulls = omg::Buffer::NewDevice(omg::NullBitmapBytes(m), s, false);
+            CudaCheck(cudaMemsetAsync(c.nulls->Data(), 0xff, omg::NullBitmapBytes(m), s), "NULL probe columns");
+        } else {
+            const int32_t bc = f_.buildOutputCols[o - nProbe];
+            c.hasNull = b.colHasNull[bc];
+            c.nulls = c.hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(m), s, true) : nullptr;
+            CudaCheck(omg::LaunchGatherRows(b.colValues[bc].Get(), c.hasNull ? b.colNulls[bc].Get() : nullptr,
+                          rows.Get(), m, c.width, c.values->Data(),
+                          c.hasNull ? static_cast<uint8_t *>(c.nulls->Data()) : nullptr, s),
+                "gather unvisited build rows");
+        }
+    }
+    std::vector<omg::OutColumn> outCols = cols;
+    if (!deviceOutput_) {
+        outCols = omg::CopyColumnsToHost(cols, m, s, 0);
+        for (auto &c : outCols) {
+            c.hasNull = false;  // host vectors: HasNull() scans the bitmap
+        }
+    }
+    impl_->stream.Sync();
+    if (f_.buildSide == OMNI_BUILD_LEFT) {
+        std::rotate(outCols.begin(), outCols.begin() + nProbe, outCols.end());
+    }
+    for (auto *ob : omg::CarveBatches(outCols, m, f_.rowsPerBatch, 0)) {
+        outputs_.push_back(ob);
+    }
+    counters_[5] += m;
+}
+
+int32_t LookupOuterJoinOperator::GetOutput(VectorBatch **outputVecBatch)
+{
+    if (outputVecBatch != nullptr) {
+        *outputVecBatch = nullptr;
+    }
+    if (!prepared_) {
+        Prepare();
+    }
+    if (outputs_.empty()) {
+        SetStatus(OMNI_STATUS_FINISHED);
+        return 0;
+    }
+    if (outputVecBatch != nullptr) {
+        *outputVecBatch = outputs_.front();
+    } else {
+        vec::VectorHelper::FreeVecBatch(outputs_.front());
+    }
+    outputs_.pop_front();
+    if (outputs_.empty()) {
         SetStatus(OMNI_STATUS_FINISHED);
     }
     return 0;

@@ -625,6 +625,157 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
     }
 }
 
+// An output row without a build match: probe columns copied, build columns NULL (value 0),
+// the existence flag (side 2) set to `matched`.
+__device__ __forceinline__ void WriteProbeOnlyRow(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t key,
+    bool matched, uint64_t pos)
+{
+    for (int o = 0; o < p.nOut; ++o) {
+        const JoinOutCol &oc = p.out[o];
+        if (oc.side == 0) {
+            // Unlike a matched row, this one may carry a NULL probe key (outer and anti joins).
+            if (oc.src == p.keyInput) {
+                StoreKey(oc.values, pos, oc.width, key);
+            } else {
+                CopyValueRO(oc.values, pos, b.cols[oc.src], row, oc.width);
+            }
+            if (oc.nulls != nullptr && RowIsNullRO(b.nulls[oc.src], row)) {
+                SetBit(oc.nulls, pos);
+            }
+        } else if (oc.side == 1) {
+            uint8_t *d = static_cast<uint8_t *>(oc.values) + static_cast<uint64_t>(oc.width) * pos;
+            for (int i = 0; i < oc.width; ++i) {
+                d[i] = 0;
+            }
+            SetBit(oc.nulls, pos);
+        } else {
+            static_cast<uint8_t *>(oc.values)[pos] = matched ? 1 : 0;
+        }
+    }
+}
+
+// Probe for the join kinds other than INNER (lookup_join.cpp:1037-1430).  Each warp takes 32
+// consecutive probe rows at a time: lane i looks row i up and decides how many rows it emits
+// (by kind), the warp prefix-sums those counts, reserves its output range with one atomicAdd and
+// writes the rows in probe-row order.  BUILD_OUTER and FULL also mark every matched build row
+// visited (a plain byte store: every writer stores the same value).
+__global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_constant__ ProbeLaunch p)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    constexpr int kWarps = kProbeThreads / 32;
+    const int kind = p.joinKind;
+    const bool emitMatches = kind == JOIN_KIND_INNER || kind == JOIN_KIND_PROBE_OUTER ||
+        kind == JOIN_KIND_BUILD_OUTER || kind == JOIN_KIND_FULL;
+    const bool unique = p.table.unique != 0;
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        const void *keyCol = b.cols[p.keyInput];
+        const uint8_t *keyNulls = b.nulls[p.keyInput];
+        const int region = t % p.nRegions;
+        const uint64_t regionBase = static_cast<uint64_t>(region) * p.regionCap;
+        for (int r0 = warp * 32; r0 < tile.rows; r0 += kWarps * 32) {
+            const int r = r0 + lane;
+            const bool exists = r < tile.rows;
+            const int64_t row = static_cast<int64_t>(tile.row0) + r;
+            int64_t key = 0;
+            Match m{0, 0, 0};
+            if (exists) {
+                key = LoadIntRO(keyCol, row, p.keyWidth);
+                if (!RowIsNullRO(keyNulls, row)) {
+                    m = Lookup(p.table, static_cast<uint64_t>(key));
+                }
+            }
+            const bool matched = m.count != 0;
+            uint32_t emit = 0;
+            switch (kind) {
+                case JOIN_KIND_PROBE_OUTER:
+                case JOIN_KIND_FULL:
+                    emit = exists ? (matched ? m.count : 1u) : 0u;
+                    break;
+                case JOIN_KIND_SEMI:
+                    emit = matched ? 1u : 0u;
+                    break;
+                case JOIN_KIND_ANTI:
+                    emit = exists && !matched ? 1u : 0u;
+                    break;
+                case JOIN_KIND_EXISTENCE:
+                    emit = exists ? 1u : 0u;
+                    break;
+                default:  // INNER, BUILD_OUTER
+                    emit = m.count;
+            }
+            if (p.visited != nullptr && matched) {
+                for (uint32_t k = 0; k < m.count; ++k) {
+                    const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
+                    p.visited[br] = 1;
+                }
+            }
+            uint32_t inc = emit;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) {
+                    inc += y;
+                }
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+            unsigned long long pos = 0;
+            if (lane == 0 && total != 0) {
+                pos = atomicAdd(p.outCount + region * kRegionStride, static_cast<unsigned long long>(total));
+            }
+            pos = __shfl_sync(0xffffffffu, pos, 0);
+            if (p.countOnly || emit == 0) {
+                continue;
+            }
+            const uint64_t at = pos + inc - emit;
+            if (emitMatches && matched) {
+                for (uint32_t k = 0; k < m.count && at + k < p.regionCap; ++k) {
+                    const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
+                    WriteJoinRow(p, b, row, key, br, regionBase + at + k);
+                }
+            } else if (at < p.regionCap) {
+                WriteProbeOnlyRow(p, b, row, key, matched, regionBase + at);
+            }
+        }
+    }
+}
+
+// Build rows no probe matched (lookup_outer_join.cpp:270-374): flags, then their row numbers in
+// build-row order after a scan of the flags.
+__global__ void UnvisitedFlagsKernel(const uint8_t *visited, int64_t n, uint32_t *flags)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        flags[i] = visited[i] == 0 ? 1u : 0u;
+    }
+}
+
+__global__ void UnvisitedRowsKernel(const uint8_t *visited, const int64_t *offsets, int64_t n, int32_t *rows)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (visited[i] == 0) {
+            rows[offsets[i]] = static_cast<int32_t>(i);
+        }
+    }
+}
+
+// dst[i] = src[rows[i]] with its NULL bit.
+__global__ void GatherRowsKernel(const void *src, const uint8_t *srcNulls, const int32_t *rows, int64_t n, int32_t width,
+    void *dst, uint8_t *dstNulls)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int32_t r = rows[i];
+        CopyValueRO(dst, static_cast<uint64_t>(i), src, r, width);
+        if (dstNulls != nullptr && RowIsNullRO(srcNulls, r)) {
+            SetBit(dstNulls, static_cast<uint64_t>(i));
+        }
+    }
+}
+
 // Specialised probe for the common shape: 8-byte key, unique build with a slot payload, and up
 // to kFastMaxOut output columns that are each either the probe key or a field of the payload.
 // Column metadata lives in registers and no width is dispatched at run time per row.
@@ -1035,6 +1186,16 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     if (p.nTiles <= 0) {
         return cudaSuccess;
     }
+    if (p.joinKind != JOIN_KIND_INNER) {
+        static int kindBlocks = 0;
+        if (kindBlocks <= 0) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kindBlocks, ProbeKindKernel, kProbeThreads, 0);
+            kindBlocks = kindBlocks <= 0 ? 1 : kindBlocks;
+        }
+        const int maxGrid = SMs() * kindBlocks;
+        ProbeKindKernel<<<p.nTiles < maxGrid ? p.nTiles : maxGrid, kProbeThreads, 0, stream>>>(p);
+        return cudaGetLastError();
+    }
     // Fast path: 8-byte key, unique build with slot payload, outputs = probe key / payload fields.
     bool fast = p.table.unique && p.table.slotPayload != nullptr && p.keyWidth == 8 && p.nOut >= 1 &&
         p.nOut <= kFastMaxOut;
@@ -1123,6 +1284,35 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     const int maxGrid = SMs() * blocksPerSM[which];
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
     kernel<<<grid, kProbeThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchUnvisitedFlags(const uint8_t *visited, int64_t n, uint32_t *flags, cudaStream_t stream)
+{
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    UnvisitedFlagsKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(visited, n, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchUnvisitedRows(const uint8_t *visited, const int64_t *offsets, int64_t n, int32_t *rows,
+    cudaStream_t stream)
+{
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    UnvisitedRowsKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(visited, offsets, n, rows);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchGatherRows(const void *src, const uint8_t *srcNulls, const int32_t *rows, int64_t n, int32_t width,
+    void *dst, uint8_t *dstNulls, cudaStream_t stream)
+{
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    GatherRowsKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(src, srcNulls, rows, n, width, dst, dstNulls);
     return cudaGetLastError();
 }
 

@@ -70,6 +70,13 @@ cudaError_t LaunchBuildFill(JoinTable t, const void *keys, const uint8_t *nulls,
     int32_t *csrRowsMutable, uint32_t sentinelCount, int64_t sentinelOffset, unsigned int *sentinelCursor,
     int64_t *sentinelEntryOut, int32_t *error, cudaStream_t stream);
 cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream);
+// Outer joins: flags[i] = 1 for build rows never matched; their row numbers in order (offsets =
+// exclusive scan of the flags); dst[i] = src[rows[i]] with NULL bits.
+cudaError_t LaunchUnvisitedFlags(const uint8_t *visited, int64_t n, uint32_t *flags, cudaStream_t stream);
+cudaError_t LaunchUnvisitedRows(const uint8_t *visited, const int64_t *offsets, int64_t n, int32_t *rows,
+    cudaStream_t stream);
+cudaError_t LaunchGatherRows(const void *src, const uint8_t *srcNulls, const int32_t *rows, int64_t n, int32_t width,
+    void *dst, uint8_t *dstNulls, cudaStream_t stream);
 // Packs the build output columns named by p.out (side 1, with shifts set) per table slot into
 // payload[nSlots + 1] (the last slot holds the EMPTY-key row of a HASH table).
 cudaError_t LaunchBuildSlotPayload(const ProbeLaunch &p, uint64_t nSlots, uint64_t *payload, cudaStream_t stream);

@@ -272,8 +272,20 @@ struct JoinTable {
     const uint32_t *slotBits;
 };
 
+// What a probe emits per probe row (lookup_join.cpp:330-411 selects one of these from the join
+// type and the build side).
+enum JoinKind : int32_t {
+    JOIN_KIND_INNER = 0,        // one row per match
+    JOIN_KIND_PROBE_OUTER = 1,  // one row per match, else one row with NULL build columns
+    JOIN_KIND_BUILD_OUTER = 2,  // one row per match, matched build rows marked visited
+    JOIN_KIND_FULL = 3,         // PROBE_OUTER rows, matched build rows marked visited
+    JOIN_KIND_SEMI = 4,         // the probe row once if it has a match
+    JOIN_KIND_ANTI = 5,         // the probe row (NULL build columns) if it has no match
+    JOIN_KIND_EXISTENCE = 6,    // every probe row with a BOOLEAN "has a match" column
+};
+
 struct JoinOutCol {
-    int16_t side;    // 0 = probe column, 1 = build column
+    int16_t side;    // 0 = probe column, 1 = build column, 2 = existence flag (1 byte)
     int16_t src;     // probe kernel input index / build column index
     int16_t width;   // bytes
     int16_t shift;   // side 1 with a slot payload: bit offset of the value in the packed payload
@@ -305,6 +317,8 @@ struct ProbeLaunch {
     uint64_t regionCap;
     int32_t countOnly;
     int32_t *error;
+    int32_t joinKind;   // JoinKind
+    uint8_t *visited;   // BUILD_OUTER / FULL: one byte per build row, set to 1 when matched
 };
 
 }  // namespace omg

@@ -1,4 +1,6 @@
-// HashBuilderOperator(Factory) and LookupJoinOperator(Factory) for GB300, inner equi-join.
+// HashBuilderOperator(Factory), LookupJoinOperator(Factory) and LookupOuterJoinOperator(Factory)
+// for GB300: equi-joins on one key column, of every join type the reference probes
+// (inner, left/right/full outer, left semi, left anti, existence).
 //
 // Call surface as in the reference (operator/join/hash_builder.h:18-80,
 // operator/join/lookup_join.h:136-200): builder operators retain their batches and build the
@@ -37,8 +39,13 @@ class HashBuilderOperatorFactory : public OperatorFactory {
 public:
     HashBuilderOperatorFactory(JoinType joinType, const type::DataTypes &buildTypes, const int32_t *buildHashCols,
         int32_t buildHashColsCount, int32_t operatorCount);
+    HashBuilderOperatorFactory(JoinType joinType, BuildSide buildSide, const type::DataTypes &buildTypes,
+        const int32_t *buildHashCols, int32_t buildHashColsCount, int32_t operatorCount);
     ~HashBuilderOperatorFactory() override;
     static HashBuilderOperatorFactory *CreateHashBuilderOperatorFactory(JoinType joinType,
+        const type::DataTypes &buildTypes, const int32_t *buildHashCols, int32_t buildHashColsCount,
+        int32_t operatorCount);
+    static HashBuilderOperatorFactory *CreateHashBuilderOperatorFactory(JoinType joinType, BuildSide buildSide,
         const type::DataTypes &buildTypes, const int32_t *buildHashCols, int32_t buildHashColsCount,
         int32_t operatorCount);
     Operator *CreateOperator() override;
@@ -116,6 +123,49 @@ private:
     std::unique_ptr<Impl> impl_;
     std::vector<VectorBatch *> pending_;
     int64_t pendingRows_ = 0;
+    std::deque<VectorBatch *> outputs_;
+};
+
+// Emits the build rows no probe matched, with NULL probe columns, after every probe operator of
+// a build-side outer or full join finished (operator/join/lookup_outer_join.h:19-100).
+class LookupOuterJoinOperatorFactory : public OperatorFactory {
+public:
+    LookupOuterJoinOperatorFactory(const type::DataTypes &probeTypes, const int32_t *probeOutputCols,
+        int32_t probeOutputColsCount, const int32_t *buildOutputCols, const type::DataTypes &buildOutputTypes,
+        HashBuilderOperatorFactory *builder, BuildSide buildSide);
+    static LookupOuterJoinOperatorFactory *CreateLookupOuterJoinOperatorFactory(const type::DataTypes &probeTypes,
+        int32_t *probeOutputCols, int32_t probeOutputColsCount, int32_t *buildOutputCols,
+        const type::DataTypes &buildOutputTypes, int64_t hashBuilderFactoryAddr);
+    static LookupOuterJoinOperatorFactory *CreateLookupOuterJoinOperatorFactory(const type::DataTypes &probeTypes,
+        int32_t *probeOutputCols, int32_t probeOutputColsCount, int32_t *buildOutputCols,
+        const type::DataTypes &buildOutputTypes, int64_t hashBuilderFactoryAddr, BuildSide buildSide);
+    Operator *CreateOperator() override;
+
+    type::DataTypes probeOutputTypes;  // types of the probe output columns (all NULL here)
+    std::vector<int32_t> buildOutputCols;
+    type::DataTypes buildOutputTypes;
+    JoinBuildState *build;
+    BuildSide buildSide;
+    int32_t rowsPerBatch;
+};
+
+class LookupOuterJoinOperator : public Operator {
+public:
+    explicit LookupOuterJoinOperator(const LookupOuterJoinOperatorFactory &f);
+    ~LookupOuterJoinOperator() override;
+    // Nothing to do: the rows come from the build (lookup_outer_join.cpp:167-171).
+    int32_t AddInput(VectorBatch *vecBatch) override;
+    // One batch of unmatched build rows per call; FINISHED after the last (or at once when there
+    // are none), lookup_outer_join.cpp:173-203.
+    int32_t GetOutput(VectorBatch **outputVecBatch) override;
+    OmniStatus Close() override;
+
+private:
+    struct Impl;
+    void Prepare();
+    const LookupOuterJoinOperatorFactory &f_;
+    std::unique_ptr<Impl> impl_;
+    bool prepared_ = false;
     std::deque<VectorBatch *> outputs_;
 };
 

@@ -97,6 +97,7 @@ inline DataTypePtr IntType() { return std::make_shared<DataType>(OMNI_INT); }
 inline DataTypePtr LongType() { return std::make_shared<DataType>(OMNI_LONG); }
 inline DataTypePtr ShortType() { return std::make_shared<DataType>(OMNI_SHORT); }
 inline DataTypePtr DoubleType() { return std::make_shared<DataType>(OMNI_DOUBLE); }
+inline DataTypePtr BooleanType() { return std::make_shared<DataType>(OMNI_BOOLEAN); }
 inline DataTypePtr Decimal64Type(int32_t p = 18, int32_t s = 0)
 {
     return std::make_shared<DataType>(OMNI_DECIMAL64, p, s);
@@ -173,6 +174,10 @@ enum JoinType {
     OMNI_JOIN_TYPE_LEFT_ANTI,
     OMNI_JOIN_TYPE_EXISTENCE
 };
+
+// Which input of the join was built (plannode/planNode.h:29-33).  With OMNI_BUILD_LEFT the
+// output vectors are rotated so that the build columns come first (lookup_join.cpp:1959-1962).
+enum BuildSide { OMNI_BUILD_UNKNOWN = 0, OMNI_BUILD_LEFT, OMNI_BUILD_RIGHT };
 
 // SupportContainerVecRule (util/policy.h:160-167): NOT_SUPPORT is the Spark policy.
 enum class SupportContainerVecRule { NOT_SUPPORT = 0, SUPPORT = 1 };

@@ -56,6 +56,8 @@ def lib() -> C.CDLL:
         L.orc_hashagg.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P]
         L.orc_join_inner.restype = I64
         L.orc_join_inner.argtypes = [I64, P, I32, P, I64, P, I32, P, P, P, I64]
+        L.orc_join.restype = I64
+        L.orc_join.argtypes = [I32, I64, P, I32, P, I64, P, I32, P, P, P, I64]
         L.orc_join_probe_bench.restype = I64
         L.orc_join_probe_bench.argtypes = [I64, P, P, I32, P, I64, P, P, I32, P]
         L.orc_agg_bench.restype = I64
@@ -146,6 +148,43 @@ def join_inner(build_keys, build_nulls, probe_keys, probe_nulls):
         ob = np.empty(cap, dtype=np.int64)
         n = L.orc_join_inner(len(bk), _ptr(bk), bk.dtype.itemsize, _ptr(bn), len(pk), _ptr(pk),
                              pk.dtype.itemsize, _ptr(pn), _ptr(op), _ptr(ob), cap)
+        if n < 0:
+            raise RuntimeError("oracle join failed")
+        if n <= cap:
+            return op[:n], ob[:n]
+        cap = n
+
+
+JOIN_KINDS = {"inner": 0, "probe_outer": 1, "build_outer": 2, "full": 3, "semi": 4, "anti": 5, "existence": 6}
+
+
+JOIN_TYPES = {"INNER": 0, "LEFT": 1, "RIGHT": 2, "FULL": 3, "LEFT_SEMI": 4, "LEFT_ANTI": 5, "EXISTENCE": 6}
+BUILD_SIDES = {"UNKNOWN": 0, "LEFT": 1, "RIGHT": 2}
+
+
+def join_kind(join_type, build_side="UNKNOWN"):
+    """The probe a join type selects (lookup_join.cpp:330-411): a LEFT (RIGHT) join built on its
+    left (right) input keeps unmatched build rows, otherwise unmatched probe rows."""
+    if join_type in ("LEFT", "RIGHT"):
+        return "build_outer" if build_side == join_type else "probe_outer"
+    return {"INNER": "inner", "FULL": "full", "LEFT_SEMI": "semi", "LEFT_ANTI": "anti",
+            "EXISTENCE": "existence"}[join_type]
+
+
+def join(kind, build_keys, build_nulls, probe_keys, probe_nulls):
+    """(probe_row, build_row) pairs of one output row each for a join kind (JOIN_KINDS); -1
+    marks the side an outer row lacks, and for "existence" build_row is the 0/1 flag."""
+    L = lib()
+    bk = np.ascontiguousarray(build_keys)
+    pk = np.ascontiguousarray(probe_keys)
+    bn = None if build_nulls is None else np.ascontiguousarray(build_nulls, dtype=np.uint8)
+    pn = None if probe_nulls is None else np.ascontiguousarray(probe_nulls, dtype=np.uint8)
+    cap = max(len(pk) + len(bk), 1)
+    while True:
+        op = np.empty(cap, dtype=np.int64)
+        ob = np.empty(cap, dtype=np.int64)
+        n = L.orc_join(JOIN_KINDS[kind], len(bk), _ptr(bk), bk.dtype.itemsize, _ptr(bn), len(pk), _ptr(pk),
+                       pk.dtype.itemsize, _ptr(pn), _ptr(op), _ptr(ob), cap)
         if n < 0:
             raise RuntimeError("oracle join failed")
         if n <= cap:

@@ -23,7 +23,9 @@
  *    value bytes (fixed-width handlers and the serialized composite key of
  *    hashmap/column_marshaller.h:27-287, where a NULL column differs from any value);
  *  - inner join: NULL keys never match; every (probe row, build row) pair with equal keys is
- *    emitted (operator/join/lookup_join.cpp:924-1035, join_hash_table_variants.cpp:695-863).
+ *    emitted (operator/join/lookup_join.cpp:924-1035, join_hash_table_variants.cpp:695-863);
+ *  - the other join types follow the probe loops of lookup_join.cpp:1037-1430 and the
+ *    unmatched-build-row pass of lookup_outer_join.cpp:173-374 (see orc_join).
  * Output order is not part of the contract (the reference emits in hash-slot order), so the
  * tables here are plain open addressing.  Parity of this file is pinned by the reference's
  * own test vectors (tests/golden/).
@@ -552,6 +554,67 @@ int64_t orc_join_inner(int64_t n_build, const void *build_keys, int32_t build_wi
             n++;
         }
     }
+    jfree(&t);
+    return n;
+}
+
+/*
+ * Equi-join of every kind a probe emits (kind: 0 inner, 1 probe-side outer, 2 build-side
+ * outer, 3 full, 4 left semi, 5 left anti, 6 existence).  Writes one (probe row, build row)
+ * pair per output row, -1 for the side an outer row does not have:
+ *  - probe-side outer (lookup_join.cpp:1037-1105): all matches of a probe row, else (r, -1);
+ *    a NULL probe key gives (r, -1);
+ *  - build-side outer (:1107-1174): the matches only, marking the matched build rows; then
+ *    every unmarked build row, NULL keys included, as (-1, b) (lookup_outer_join.cpp:173-374:
+ *    these builds keep NULL-key rows in the table, join_hash_table_variants.cpp:80-82);
+ *  - full (:1176-1245): probe-side outer rows, marking matches, then the unmarked build rows;
+ *  - left semi (:1247-1311): (r, -1) once for a probe row with a match (NULL keys skipped);
+ *  - left anti (:1313-1379): (r, -1) for a probe row without a match, NULL keys included;
+ *  - existence (:1381-1430): (r, 1 or 0) for every probe row, 1 iff it has a match.
+ * Returns the number of output rows (only the first `capacity` are written), -1 on allocation
+ * failure or an unknown kind.
+ */
+int64_t orc_join(int32_t kind, int64_t n_build, const void *build_keys, int32_t build_width,
+    const uint8_t *build_nulls, int64_t n_probe, const void *probe_keys, int32_t probe_width,
+    const uint8_t *probe_nulls, int64_t *out_probe, int64_t *out_build, int64_t capacity)
+{
+    if (kind < 0 || kind > 6) return -1;
+    jtable_t t;
+    if (jbuild(&t, n_build, build_keys, build_width, build_nulls) != 0) { jfree(&t); return -1; }
+    uint8_t *visited = (uint8_t *)calloc((size_t)(n_build > 0 ? n_build : 1), 1);
+    if (!visited) { jfree(&t); return -1; }
+    int64_t n = 0;
+#define EMIT(pr, br) do { if (n < capacity) { out_probe[n] = (pr); out_build[n] = (br); } n++; } while (0)
+    for (int64_t r = 0; r < n_probe; ++r) {
+        const int null_key = probe_nulls && probe_nulls[r];
+        const int64_t head = null_key ? -1 : jfind(&t, load_int(probe_keys, r, probe_width));
+        switch (kind) {
+            case 0:
+            case 2:
+                for (int64_t b = head; b >= 0; b = t.next[b]) { EMIT(r, b); visited[b] = 1; }
+                break;
+            case 1:
+            case 3:
+                if (head < 0) { EMIT(r, -1); break; }
+                for (int64_t b = head; b >= 0; b = t.next[b]) { EMIT(r, b); visited[b] = 1; }
+                break;
+            case 4:
+                if (head >= 0) EMIT(r, -1);
+                break;
+            case 5:
+                if (head < 0) EMIT(r, -1);
+                break;
+            default:
+                EMIT(r, head >= 0 ? 1 : 0);
+        }
+    }
+    if (kind == 2 || kind == 3) {
+        for (int64_t b = 0; b < n_build; ++b) {
+            if (!visited[b]) EMIT(-1, b);
+        }
+    }
+#undef EMIT
+    free(visited);
     jfree(&t);
     return n;
 }

@@ -106,11 +106,106 @@ def _join_array_table_short():
                 probe_hash_col=0, probe_output_cols=[0, 1], build_output_cols=[0, 1], expected_rows=rows)
 
 
+# Join types other than inner.  Each entry restates one test of core/test/operator/join_test.cpp:
+# columns are int64 unless "types" says otherwise, "*_nulls" list the NULL rows per column,
+# expected rows list the probe output values then the build output values (None = NULL) in the
+# probe-first order the test checks, and "outer_rows" are the rows of the LookupOuterJoin operator
+# (None for an operator that is not run).  The reference tests that use VARCHAR payloads are
+# restated with the strings replaced by distinct integers (STR below): joins never read payload
+# values, so the pairing of rows is unchanged.
+STR = {"11": 11, "22": 22, "33": 33, "44": 44, "aaa": 1001, "aa": 1002, "ccc": 1003}
+
+
+def _s(vals):
+    return [STR[v] for v in vals]
+
+
+JOIN_TYPED = {
+    "left_join": dict(
+        source="core/test/operator/join_test.cpp:773-833", join_type="LEFT", build_side="UNKNOWN",
+        build=[[1, 2, 3, 4], [111, 11, 333, 33]], build_nulls=None, build_hash_col=1,
+        probe=[[1, 2, 3, 4], [11, 22, 33, 44]], probe_nulls=None, probe_hash_col=1,
+        probe_output_cols=[0, 1], build_output_cols=[0, 1],
+        expected_rows=[[1, 11, 2, 11], [2, 22, None, None], [3, 33, 4, 33], [4, 44, None, None]],
+        outer_rows=None),
+    "left_join_build_left": dict(
+        source="core/test/operator/join_test.cpp:835-918", join_type="LEFT", build_side="LEFT",
+        build=[[1, 2, 3, 4], [111, 11, 333, 33]], build_nulls=None, build_hash_col=1,
+        probe=[[1, 2, 3, 4], [11, 22, 33, 44]], probe_nulls=None, probe_hash_col=1,
+        probe_output_cols=[0, 1], build_output_cols=[0, 1],
+        expected_rows=[[1, 11, 2, 11], [3, 33, 4, 33]],
+        outer_rows=[[None, None, 3, 333], [None, None, 1, 111]]),
+    "full_join_one_build_op": dict(
+        source="core/test/operator/join_test.cpp:52-109,137-170,2589-2632", join_type="FULL", build_side="UNKNOWN",
+        build=[[1, 2, 1, 2, 3, 4, 5, 6, 7, 1], [79, 79, 70, 70, 70, 70, 70, 70, 70, 70]], build_nulls=None,
+        build_hash_col=0,
+        probe=[[1, 2, 3, 4, 5, 6, 1, 1, 2, 3], [78, 78, 78, 78, 78, 78, 78, 82, 82, 65]], probe_nulls=None,
+        probe_hash_col=0, probe_output_cols=[1], build_output_cols=[1],
+        expected_rows=None,  # the inner join's rows (every probe row matches): filled in main()
+        outer_rows=[[None, 70]]),
+    "full_join_build_null": dict(
+        source="core/test/operator/join_test.cpp:2881-2973", join_type="FULL", build_side="UNKNOWN",
+        build=[[1, 2, 3, 4, 5, 6], [111, 11, 333, 33, 11, 11]], build_nulls=[[], [0, 2]], build_hash_col=1,
+        probe=[[1, 2, 3, 4], [11, 22, 33, 44]], probe_nulls=None, probe_hash_col=1,
+        probe_output_cols=[0, 1], build_output_cols=[0, 1],
+        expected_rows=[[1, 11, 2, 11], [1, 11, 5, 11], [1, 11, 6, 11], [2, 22, None, None], [3, 33, 4, 33],
+                       [4, 44, None, None]],
+        outer_rows=[[None, None, 1, None], [None, None, 3, None]]),
+    "left_semi_join": dict(
+        source="core/test/operator/join_test.cpp:3831-3889", join_type="LEFT_SEMI", build_side="UNKNOWN",
+        build=[[1, 0, 3, 0, 1, 0, 2, 2], _s(["aaa", "11", "ccc", "33", "aaa", "11", "ccc", "33"])],
+        build_nulls=[[1], []], build_hash_col=0,
+        probe=[[0, 2, 0, 1, 0, 2, 0, 4], _s(["11", "22", "33", "44", "11", "22", "33", "44"])],
+        probe_nulls=[[2], []], probe_hash_col=0, probe_output_cols=[0, 1], build_output_cols=[],
+        expected_rows=[[0, 11], [2, 22], [1, 44], [0, 11], [2, 22], [0, 33]], outer_rows=None),
+    "right_join": dict(
+        source="core/test/operator/join_test.cpp:4014-4081", join_type="RIGHT", build_side="UNKNOWN",
+        build=[[1, 0, 3, 0, 1, 0, 2, 2], _s(["aaa", "11", "ccc", "33", "aa", "11", "ccc", "33"])],
+        build_nulls=None, build_hash_col=0,
+        probe=[[0, 2, 0, 1], _s(["11", "22", "33", "44"])], probe_nulls=[[2], []], probe_hash_col=0,
+        probe_output_cols=[0, 1], build_output_cols=[0, 1],
+        expected_rows=[[0, 11, 0, 11], [0, 11, 0, 33], [0, 11, 0, 11], [2, 22, 2, 1003], [2, 22, 2, 33],
+                       [1, 44, 1, 1001], [1, 44, 1, 1002], [None, 33, None, None]],
+        outer_rows=None),
+    "left_anti_join": dict(
+        source="core/test/operator/join_test.cpp:4157-4207", join_type="LEFT_ANTI", build_side="UNKNOWN",
+        build=[[1, 2, 3, 4], [111, 11, 333, 33]], build_nulls=None, build_hash_col=1,
+        probe=[[1, 2, 3, 4, 3, 6], [11, 22, 33, 44, 22, 44]], probe_nulls=None, probe_hash_col=1,
+        probe_output_cols=[0, 1], build_output_cols=[],
+        expected_rows=[[2, 22], [4, 44], [3, 22], [6, 44]], outer_rows=None),
+    # join_test.cpp:4329 lists 8 initialisers for a 7-row column: the first 7 are the data.
+    "left_anti_join_array_probe": dict(
+        source="core/test/operator/join_test.cpp:4323-4380", join_type="LEFT_ANTI", build_side="UNKNOWN",
+        build=[[1, 2, 3, 4, 6, 7, 8], [2, 11, 7, 3, 4, 5, 5]], build_nulls=None, build_hash_col=1,
+        probe=[[1, 2, 3, 4, 3, 6, 7], [28, 2, 3, 10, 0, 15, 8]], probe_nulls=None, probe_hash_col=1,
+        probe_output_cols=[0, 1], build_output_cols=[],
+        expected_rows=[[1, 28], [4, 10], [3, 0], [6, 15], [7, 8]], outer_rows=None),
+    "full_join_array_table": dict(
+        source="core/test/operator/join_test.cpp:4382-4471", join_type="FULL", build_side="UNKNOWN",
+        types="SHORT",
+        build=[[1, 2, 3, 4, 1, 2], [111, 11, 333, 33, 20, 16]], build_nulls=[[4, 5], []], build_hash_col=0,
+        probe=[[1, 2, 3, 4], [11, 22, 33, 44]], probe_nulls=None, probe_hash_col=0,
+        probe_output_cols=[0, 1], build_output_cols=[0, 1],
+        expected_rows=[[1, 11, 1, 111], [2, 22, 2, 11], [3, 33, 3, 333], [4, 44, 4, 33]],
+        outer_rows=[[None, None, None, 20], [None, None, None, 16]]),
+    "existence_join": dict(
+        source="core/test/operator/join_test.cpp:4584-4635", join_type="EXISTENCE", build_side="UNKNOWN",
+        build=[[1, 2, 3, 4], [111, 11, 333, 33]], build_nulls=None, build_hash_col=1,
+        probe=[[1, 2, 3, 4, 3, 6], [11, 22, 33, 44, 22, 44]], probe_nulls=None, probe_hash_col=1,
+        probe_output_cols=[], build_output_cols=[],
+        expected_rows=[[1], [0], [1], [0], [0], [0]], outer_rows=None),
+}
+
+
 def main():
     (HERE / "agg_kats.json").write_text(json.dumps({"single": AGG, "multi": AGG_MULTI}, indent=1) + "\n")
     (HERE / "join_kats.json").write_text(json.dumps({"inner_join_one_build_op": _join_one_build_op(),
                                                     "array_table_short": _join_array_table_short()}, indent=1)
                                          + "\n")
+    typed = dict(JOIN_TYPED)
+    typed["full_join_one_build_op"] = dict(typed["full_join_one_build_op"],
+                                           expected_rows=_join_one_build_op()["expected_rows"])
+    (HERE / "join_type_kats.json").write_text(json.dumps(typed, indent=1) + "\n")
 
 
 if __name__ == "__main__":

@@ -213,3 +213,53 @@ def expected_join_rows(probe_cols, probe_nulls, build_cols, build_nulls, pk, bk,
         m = build_nulls[c] if build_nulls is not None and build_nulls[c] is not None else np.zeros(len(build_cols[c]), bool)
         cols.append((build_cols[c][bi], m[bi]))
     return join_rows_canonical(cols)
+
+
+def kat_columns(k):
+    """Build/probe columns and NULL masks of a typed join KAT."""
+    dt = np.int16 if k.get("types") == "SHORT" else np.int64
+
+    def side(cols, nulls):
+        vals = [np.array(c, dtype=dt) for c in cols]
+        masks = [np.zeros(len(c), bool) for c in cols]
+        for m, rows in zip(masks, nulls or []):
+            m[rows] = True
+        return vals, masks
+    return side(k["build"], k["build_nulls"]), side(k["probe"], k["probe_nulls"])
+
+
+def oracle_join_rows(k):
+    """Output rows (probe output values, build output values or the existence flag; None =
+    NULL) of a typed join KAT computed by the oracle."""
+    (b, bm), (p, pm) = kat_columns(k)
+    kind = oracle.join_kind(k["join_type"], k["build_side"])
+    pi, bi = oracle.join(kind, b[k["build_hash_col"]], bm[k["build_hash_col"]], p[k["probe_hash_col"]],
+                         pm[k["probe_hash_col"]])
+    rows = []
+    for i, j in zip(pi.tolist(), bi.tolist()):
+        r = [None if i < 0 or pm[c][i] else int(p[c][i]) for c in k["probe_output_cols"]]
+        if kind == "existence":
+            r.append(j)
+        else:
+            r += [None if j < 0 or bm[c][j] else int(b[c][j]) for c in k["build_output_cols"]]
+        rows.append(r)
+    return rows
+
+
+def row_key(r):
+    return tuple((v is None, 0 if v is None else v) for v in r)
+
+
+def rows_matrix(cols):
+    """Row multiset of output columns [(values, NULL mask)] as a lexicographically sorted int64
+    matrix with a (NULL flag, value) pair per column (value 0 when NULL)."""
+    if not cols:
+        return np.zeros((0, 0), dtype=np.int64)
+    parts = []
+    for v, m in cols:
+        m = np.asarray(m, dtype=bool)
+        parts.append(m.astype(np.int64))
+        parts.append(np.where(m, 0, np.asarray(v).astype(np.int64)))
+    mat = np.stack(parts, axis=1)
+    order = np.lexsort(mat.T[::-1])
+    return mat[order]

@@ -78,10 +78,28 @@ def test_factory_validation_matches_reference_rules():
     assert e.value.status == -1
     omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[omg.DoubleType(), L]],
                                        [omg.OMNI_AGGREGATION_TYPE_AVG], output_partials=[True]).close()
-    # outer joins are not built
+    # every join type of planNode.h:406-414 builds; an unknown one is UNSUPPORTED
+    for jt in range(7):
+        omg.HashBuilderOperatorFactory(jt, [L], [0]).close()
     with pytest.raises(omg.OmgError) as e:
-        omg.HashBuilderOperatorFactory(1, [L], [0])
+        omg.HashBuilderOperatorFactory(7, [L], [0])
     assert e.value.status == -2
+    with pytest.raises(omg.OmgError) as e:
+        omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_LEFT, [L], [0], build_side=5)
+    assert e.value.status == -1
+    # a semi join emits probe columns only; the outer-join operator follows full and
+    # build-side outer joins only
+    sf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_LEFT_SEMI, [L, L], [0])
+    with pytest.raises(omg.OmgError) as e:
+        omg.LookupJoinOperatorFactory([L], [0], [0], [1], [L], sf)
+    assert e.value.status == -2
+    with pytest.raises(omg.OmgError) as e:
+        omg.LookupOuterJoinOperatorFactory([L], [0], [1], [L], sf)
+    assert e.value.status == -2
+    sf.close()
+    ff = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_FULL, [L, L], [0])
+    omg.LookupOuterJoinOperatorFactory([L], [0], [1], [L], ff).close()
+    ff.close()
     # join filters are not built
     bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L], [0])
     with pytest.raises(omg.OmgError):

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
+from helpers import oracle_join_rows, row_key
 
 G = Path(__file__).parent / "golden"
 TYPES = {"LONG": oracle.T_LONG, "DOUBLE": oracle.T_DOUBLE, "DECIMAL64": oracle.T_DEC64,
@@ -88,6 +89,35 @@ def test_oracle_join_kats(name):
     rows = sorted(tuple(int(p[c][i]) for c in k["probe_output_cols"]) + tuple(int(b[c][j]) for c in k["build_output_cols"])
                   for i, j in zip(pi, bi))
     assert rows == sorted(tuple(r) for r in k["expected_rows"])
+
+
+JOIN_TYPED = json.loads((G / "join_type_kats.json").read_text())
+
+
+@pytest.mark.parametrize("name", sorted(JOIN_TYPED))
+def test_oracle_join_type_kats(name):
+    k = JOIN_TYPED[name]
+    expected = k["expected_rows"] + (k["outer_rows"] or [])
+    assert sorted(map(row_key, oracle_join_rows(k))) == sorted(map(row_key, expected))
+
+
+def test_oracle_join_kinds_match_bruteforce():
+    rng = np.random.default_rng(5)
+    bk = rng.integers(-20, 20, 200).astype(np.int64)
+    bn = rng.random(200) < 0.1
+    pk = rng.integers(-25, 25, 300).astype(np.int64)
+    pn = rng.random(300) < 0.1
+    match = [[j for j in range(200) if not pn[i] and not bn[j] and bk[j] == pk[i]] for i in range(300)]
+    hit = set(j for m in match for j in m)
+    unhit = [(-1, j) for j in range(200) if j not in hit]
+    pairs = [(i, j) for i in range(300) for j in match[i]]
+    lone = [(i, -1) for i in range(300) if not match[i]]
+    expect = {"inner": pairs, "probe_outer": pairs + lone, "build_outer": pairs + unhit,
+              "full": pairs + lone + unhit, "semi": [(i, -1) for i in range(300) if match[i]],
+              "anti": lone, "existence": [(i, 1 if match[i] else 0) for i in range(300)]}
+    for kind, exp in expect.items():
+        pi, bi = oracle.join(kind, bk, bn, pk, pn)
+        assert sorted(zip(pi.tolist(), bi.tolist())) == sorted(exp), kind
 
 
 def test_oracle_join_matches_bruteforce():
