@@ -318,6 +318,12 @@ int32_t omg_op_needs_input(void *op);
 int32_t omg_op_is_blocked(void *op);
 /* Operator::GetHashMapUniqueKeys (operator.h:87). */
 int64_t omg_op_hashmap_unique_keys(void *op);
+/* Operator::AlignSchema (operator.h:92-95; HashAggregationOperator::AlignSchema,
+ * group_aggregation.cpp:1182-1218; JNI alignSchemaNative, jni_operator.cpp:249-260): the batch
+ * as one-row partial results of a partial aggregation (every aggregator raw input, partial
+ * output), written to `*out`; the input batch is freed whatever the status.  Operators without
+ * a partial schema hand the batch back unchanged. */
+int32_t omg_op_align_schema(void *op, void *batch, void **out);
 /* Operator::Close (operator.h:61) and Operator::DeleteOperator (operator.h:40-44). */
 int32_t omg_op_close(void *op);
 int32_t omg_op_delete(void *op);

@@ -92,6 +92,7 @@ _SIGS = {
     "omg_op_needs_input": (I32, [P]),
     "omg_op_is_blocked": (I32, [P]),
     "omg_op_hashmap_unique_keys": (I64, [P]),
+    "omg_op_align_schema": (I32, [P, P, C.POINTER(P)]),
     "omg_op_close": (I32, [P]),
     "omg_op_delete": (I32, [P]),
     "omg_op_set_stream": (I32, [P, P]),

@@ -289,6 +289,12 @@ class Operator:
     def get_hashmap_unique_keys(self) -> int:
         return lib().omg_op_hashmap_unique_keys(self.handle)
 
+    def align_schema(self, batch: int) -> int:
+        """AlignSchema: the batch (consumed) as one-row partial results; a new batch handle."""
+        out = C.c_void_p()
+        check(lib().omg_op_align_schema(self.handle, batch, C.byref(out)))
+        return out.value
+
     def set_stream(self, stream_handle: int):
         check(lib().omg_op_set_stream(self.handle, C.c_void_p(stream_handle)))
 

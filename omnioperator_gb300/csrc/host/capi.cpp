@@ -781,6 +781,23 @@ int64_t omg_op_hashmap_unique_keys(void *op)
     return op ? static_cast<int64_t>(static_cast<Operator *>(op)->GetHashMapUniqueKeys()) : -1;
 }
 
+int32_t omg_op_align_schema(void *op, void *batch, void **out)
+{
+    return Guard([&] {
+        if (out != nullptr) {
+            *out = nullptr;
+        }
+        auto *b = static_cast<VectorBatch *>(batch);
+        if (op == nullptr || b == nullptr || out == nullptr) {
+            if (b != nullptr) {
+                omniruntime::vec::VectorHelper::FreeVecBatch(b);
+            }
+            Require(false, "null handle");
+        }
+        *out = AsOp(op)->AlignSchema(b);
+    });
+}
+
 int32_t omg_op_close(void *op)
 {
     return Guard([&] { AsOp(op)->Close(); });

@@ -462,6 +462,54 @@ OmniStatus HashAggregationOperatorFactory::Init()
     p.slotWords = p.keyWords + p.stateWords;
     p.smemSlots = static_cast<int32_t>(kSmemBudget / (p.slotWords * sizeof(uint64_t)));
     p.rowsPerBatch = GetMaxRowCount(rowBytes);
+    // AlignSchema columns: each output of a raw-input partial plan restated for one row.
+    bool alignable = nAgg > 0;
+    for (size_t a = 0; a < nAgg; ++a) {
+        const bool raw = a < inputRaws_.size() ? static_cast<bool>(inputRaws_[a]) : true;
+        const bool partial = a < outputPartials_.size() ? static_cast<bool>(outputPartials_[a]) : false;
+        alignable = alignable && raw && partial;
+    }
+    for (size_t i = 0; alignable && i < p.outs.size(); ++i) {
+        const OutSpec &o = p.outs[i];
+        omg::AlignCol c{};
+        c.outWidth = o.outWidth;
+        c.input = -1;
+        switch (o.kind) {
+            case omg::OUT_KEY:
+                c.op = omg::ALIGN_COPY;
+                c.input = p.key.cols[o.src].input;
+                c.inWidth = p.key.cols[o.src].width;
+                break;
+            case omg::OUT_COUNT:
+                c.op = o.countAcc < 0 ? omg::ALIGN_ONE : omg::ALIGN_VALID;
+                c.input = o.countAcc < 0 ? -1 : p.accs[o.countAcc].input;
+                break;
+            case omg::OUT_SUM_WRAP:
+            case omg::OUT_MIN_INT:
+            case omg::OUT_MAX_INT:
+            case omg::OUT_SUM_DOUBLE:
+            case omg::OUT_MIN_DOUBLE:
+            case omg::OUT_MAX_DOUBLE:
+            case omg::OUT_AVG_PARTIAL_SUM: {
+                const AccSpec &acc = p.accs[o.src];
+                c.op = o.kind == omg::OUT_AVG_PARTIAL_SUM
+                    ? omg::ALIGN_AVG_SUM
+                    : ((o.kind == omg::OUT_SUM_WRAP || o.kind == omg::OUT_MIN_INT || o.kind == omg::OUT_MAX_INT)
+                              ? omg::ALIGN_INT
+                              : omg::ALIGN_DOUBLE);
+                c.input = acc.input;
+                c.inKind = acc.inKind;
+                c.inWidth = acc.inWidth;
+                break;
+            }
+            default:
+                alignable = false;
+        }
+        p.align.push_back(c);
+    }
+    if (!alignable) {
+        p.align.clear();
+    }
     inited_ = true;
     return OMNI_STATUS_NORMAL;
 }
@@ -605,6 +653,78 @@ struct HashAggregationOperator::PartBuffers {
     DevArray<omg::TileDesc> tiles;
     DevArray<int32_t> tileStart;
 };
+
+VectorBatch *HashAggregationOperator::AlignSchema(VectorBatch *inputVecBatch)
+{
+    if (inputVecBatch == nullptr) {
+        throw OmniException("INVALID_ARGUMENT", "AlignSchema of a null batch", -1);
+    }
+    std::unique_ptr<VectorBatch, void (*)(VectorBatch *)> in(inputVecBatch,
+        [](VectorBatch *b) { vec::VectorHelper::FreeVecBatch(b); });
+    if (plan_.align.empty()) {
+        throw OmniException("UNSUPPORTED_ERROR",
+            "AlignSchema needs every aggregator to read raw input and emit partials", -2);
+    }
+    const int64_t rows = inputVecBatch->GetRowCount();
+    int32_t maxCol = 0;
+    for (int32_t c : plan_.inputCols) {
+        maxCol = std::max(maxCol, c + 1);
+    }
+    if (inputVecBatch->GetVectorCount() < maxCol) {
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "AlignSchema batch has too few vectors", -1);
+    }
+    omg::RequireDevice();
+    if (userStreamSet_) {
+        impl_->stream.SetUser(userStream_);
+    }
+    cudaStream_t s = impl_->stream.Get();
+    std::vector<omg::OutColumn> cols(plan_.align.size());
+    omg::BatchTable bt;
+    if (rows > 0) {
+        bt.Build({inputVecBatch}, plan_.inputCols);
+        bt.Upload(s);
+    }
+    for (size_t o = 0; o < cols.size(); ++o) {
+        const omg::AlignCol &c = plan_.align[o];
+        omg::OutColumn &oc = cols[o];
+        oc.type = plan_.outTypes[o]->GetId();
+        oc.width = plan_.outTypes[o]->ByteWidth();
+        oc.hasNull = c.input >= 0 && rows > 0 && bt.AnyNulls(c.input) &&
+            (c.op == omg::ALIGN_COPY || c.op == omg::ALIGN_INT || c.op == omg::ALIGN_DOUBLE);
+        oc.values = omg::Buffer::NewDevice(static_cast<size_t>(rows) * oc.width + 16, s, false);
+        oc.nulls = oc.hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(rows), s, true) : nullptr;
+        if (rows > 0) {
+            CudaCheck(omg::LaunchAlignColumn(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(), bt.DeviceTileOutRows(),
+                          c, oc.values->Data(), oc.hasNull ? static_cast<uint8_t *>(oc.nulls->Data()) : nullptr, s),
+                "align schema");
+            ++counters_[0];
+        }
+    }
+    std::vector<omg::OutColumn> outCols = cols;
+    if (!deviceOutput_ && rows > 0) {
+        outCols = omg::CopyColumnsToHost(cols, rows, s, 0);
+        for (auto &c : outCols) {
+            c.hasNull = false;  // host vectors: HasNull() scans the bitmap
+        }
+    }
+    impl_->stream.Sync();
+    if (rows == 0) {
+        auto *b = new VectorBatch(0);
+        for (const auto &c : cols) {
+            b->Append(new vec::BaseVector(c.type, c.width, 0, omg::Buffer::NewHost(16, false), 0, nullptr, 0, false));
+        }
+        return b;
+    }
+    // One batch: CarveBatches cuts at multiples of 64 rows.
+    auto batches = omg::CarveBatches(outCols, rows, static_cast<int32_t>((rows + 63) / 64 * 64), 0);
+    if (batches.size() != 1) {
+        for (auto *b : batches) {
+            vec::VectorHelper::FreeVecBatch(b);
+        }
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "AlignSchema produced no batch", -9);
+    }
+    return batches[0];
+}
 
 int32_t HashAggregationOperator::GetSizingLog(int64_t *out, int32_t n) const
 {

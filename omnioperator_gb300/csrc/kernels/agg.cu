@@ -921,6 +921,57 @@ __device__ __forceinline__ void StoreWidth(void *col, uint64_t pos, int width, u
     }
 }
 
+// One output column of AlignSchema over the tiles of the input batches (row order kept).
+__global__ void AlignColumnKernel(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, const AlignCol c, void *out, uint8_t *outNulls)
+{
+    for (int t = blockIdx.x; t < nTiles; t += gridDim.x) {
+        const TileDesc tile = tiles[t];
+        const BatchDesc &b = batches[tile.batch];
+        const int64_t out0 = tileOutRow[t];
+        const void *col = c.input >= 0 ? b.cols[c.input] : nullptr;
+        const uint8_t *nulls = c.input >= 0 ? b.nulls[c.input] : nullptr;
+        for (int r = threadIdx.x; r < tile.rows; r += blockDim.x) {
+            const int64_t row = static_cast<int64_t>(tile.row0) + r;
+            const uint64_t pos = static_cast<uint64_t>(out0 + r);
+            const bool isNull = NullRO(nulls, row);
+            switch (c.op) {
+                case ALIGN_COPY:
+                    if (c.inWidth == 16) {
+                        static_cast<longlong2 *>(out)[pos] = __ldg(static_cast<const longlong2 *>(col) + row);
+                    } else {
+                        StoreWidth(out, pos, c.outWidth, LoadBitsRO(col, row, c.inWidth));
+                    }
+                    break;
+                case ALIGN_INT:
+                    StoreWidth(out, pos, c.outWidth,
+                        static_cast<uint64_t>(SignExtend(LoadBitsRO(col, row, c.inWidth), c.inWidth)));
+                    break;
+                case ALIGN_DOUBLE: {
+                    const double v = LoadAsDoubleRO(col, row, c.inKind, c.inWidth);
+                    if (c.outWidth == 4) {
+                        static_cast<float *>(out)[pos] = static_cast<float>(v);
+                    } else {
+                        static_cast<double *>(out)[pos] = v;
+                    }
+                    break;
+                }
+                case ALIGN_ONE:
+                    static_cast<int64_t *>(out)[pos] = 1;
+                    break;
+                case ALIGN_VALID:
+                    static_cast<int64_t *>(out)[pos] = isNull ? 0 : 1;
+                    break;
+                default:  // ALIGN_AVG_SUM
+                    static_cast<double *>(out)[pos] = isNull ? 0.0 : LoadAsDoubleRO(col, row, c.inKind, c.inWidth);
+            }
+            if (isNull && outNulls != nullptr) {
+                SetOutNull(outNulls, pos);
+            }
+        }
+    }
+}
+
 // 10^38 - 1 as a 128-bit unsigned value (type/base_operations.h:20-21).
 __device__ __forceinline__ unsigned __int128 Dec38Max()
 {
@@ -2088,6 +2139,17 @@ cudaError_t LaunchAggSketch(const AggLaunch &p, int32_t nSample, unsigned long l
         SketchKernel<KEY_PACKED><<<blocks, 256, 0, stream>>>(p, nSample, tabKeys, tabCounts, stats);
     }
     SketchStatsKernel<<<64, 256, 0, stream>>>(tabKeys, tabCounts, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchAlignColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, const AlignCol &c, void *out, uint8_t *outNulls, cudaStream_t stream)
+{
+    if (nTiles <= 0) {
+        return cudaSuccess;
+    }
+    const int grid = nTiles < DeviceSMCount() * 8 ? nTiles : DeviceSMCount() * 8;
+    AlignColumnKernel<<<grid, 256, 0, stream>>>(batches, tiles, nTiles, tileOutRow, c, out, outNulls);
     return cudaGetLastError();
 }
 

@@ -70,6 +70,9 @@ cudaError_t LaunchBuildFill(JoinTable t, const void *keys, const uint8_t *nulls,
     int32_t *csrRowsMutable, uint32_t sentinelCount, int64_t sentinelOffset, unsigned int *sentinelCursor,
     int64_t *sentinelEntryOut, int32_t *error, cudaStream_t stream);
 cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream);
+// One output column of AlignSchema (adaptive partial aggregation) for every input row.
+cudaError_t LaunchAlignColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, const AlignCol &c, void *out, uint8_t *outNulls, cudaStream_t stream);
 // Outer joins: flags[i] = 1 for build rows never matched; their row numbers in order (offsets =
 // exclusive scan of the flags); dst[i] = src[rows[i]] with NULL bits.
 cudaError_t LaunchUnvisitedFlags(const uint8_t *visited, int64_t n, uint32_t *flags, cudaStream_t stream);

@@ -227,6 +227,27 @@ struct OutSpec {
     uint8_t *nulls;     // device output null bitmap (zeroed by the host)
 };
 
+// Adaptive partial aggregation (HashAggregationOperator::AlignSchema,
+// group_aggregation.cpp:1182-1218): every input row becomes a one-row partial result.  One
+// descriptor per output column of the partial schema.
+enum AlignOp : int16_t {
+    ALIGN_COPY = 0,     // the input value and NULL bit (group-by columns)
+    ALIGN_INT = 1,      // integer input cast to the output width, NULL bit kept (SUM/MIN/MAX partials)
+    ALIGN_DOUBLE = 2,   // input converted to double (or float), NULL bit kept
+    ALIGN_ONE = 3,      // 1 (COUNT(*) partial)
+    ALIGN_VALID = 4,    // 1 for a non-NULL input, else 0 (COUNT(col) and AVG count partials)
+    ALIGN_AVG_SUM = 5,  // the input as double, 0 for NULL, never NULL (AVG sum partial)
+};
+
+struct AlignCol {
+    int16_t op;
+    int16_t input;     // kernel input (-1 for ALIGN_ONE)
+    int16_t inKind;    // IN_INT / IN_FLOAT / IN_DOUBLE
+    int16_t inWidth;
+    int16_t outWidth;
+    int16_t pad[3];
+};
+
 struct AggExtract {
     AggTable table;
     KeySpec key;

@@ -50,6 +50,8 @@ struct AggPlan {
     int32_t smemSlots = 0;                 // per-CTA shared pre-aggregation slots
     bool overflowAsNull = false;
     bool orderDependent = false;           // has an OUT_SUM_EXACT column (sticky overflow)
+    std::vector<omg::AlignCol> align;      // AlignSchema columns; empty unless every aggregator
+                                           // reads raw input and emits partials
 };
 
 // Kernel launch parameters of a plan (table fields as given; stats: [groups, retry count,
@@ -100,6 +102,10 @@ public:
     int32_t GetOutput(VectorBatch **outputVecBatch) override;
     OmniStatus Close() override;
     uint64_t GetHashMapUniqueKeys() override { return uniqueKeys_; }
+    // Adaptive partial aggregation (group_aggregation.cpp:1182-1218): the input batch as
+    // one-row partial results in the partial output schema, computed on the device; the input
+    // is freed.  Only for plans whose aggregators all read raw input and emit partials.
+    VectorBatch *AlignSchema(VectorBatch *inputVecBatch) override;
 
     // Strategy hint (OMG_AGG_STRATEGY_*) and initial capacity in groups (0 = default).
     void SetStrategy(int32_t strategy, int64_t capacityHint)

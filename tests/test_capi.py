@@ -140,6 +140,19 @@ def test_operator_state_machine_without_gpu():
     bf.close()
 
 
+def test_align_schema_needs_a_raw_partial_plan():
+    """AlignSchema of a single-stage aggregation is refused before any device work (and frees
+    the batch, as the reference's AlignSchema does)."""
+    L = omg.LongType()
+    fac = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [omg.OMNI_AGGREGATION_TYPE_SUM])
+    op = fac.create_operator()
+    with pytest.raises(omg.OmgError) as e:
+        op.align_schema(omg.make_batch([L, L], [np.arange(4, dtype=np.int64)] * 2))
+    assert e.value.status == -2
+    op.delete()
+    fac.close()
+
+
 def test_device_alloc_fault_injection_is_host_side():
     omg.lib().omg_debug_fail_next_allocs(2)
     omg.lib().omg_debug_fail_next_allocs(0)

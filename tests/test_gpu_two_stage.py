@@ -174,3 +174,85 @@ def test_partial_intermediate_final_equals_single_stage(strategy):
     for r in rows:
         assert cols[1][1][r] and cols[4][1][r] and cols[5][1][r] and cols[6][1][r] and cols[7][1][r] and cols[8][1][r]
         assert not cols[2][1][r] and cols[2][0][r] == 0 and cols[3][0][r] > 0
+
+
+def test_align_schema_restates_each_row_as_a_partial():
+    """AlignSchema (group_aggregation.cpp:1182-1218 and the aggregators' ProcessAlignAggSchema):
+    keys copied, SUM/MIN/MAX partials are the value (NULL kept, int widened to the output type),
+    COUNT(col) 1 or 0, COUNT(*) 1, AVG (double(value) or 0, 1 or 0)."""
+    rng = np.random.default_rng(4)
+    n = 10_000
+    key = rng.integers(-5, 5, n).astype(np.int64)
+    knull = rng.random(n) < 0.05
+    vint = rng.integers(-2**31, 2**31, n, dtype=np.int64).astype(np.int32)
+    inull = rng.random(n) < 0.2
+    vdbl = rng.standard_normal(n)
+    dnull = rng.random(n) < 0.2
+    I = omg.IntType()
+    funcs = [SUM, CNT, CNT_ALL, MIN, MAX, AVG, AVG, SUM]
+    agg_cols = [[1], [1], [], [1], [1], [2], [1], [2]]
+    in_types = [[I], [I], [], [I], [I], [D], [I], [D]]
+    out_types = [[L], [L], [L], [I], [I], [D, L], [D, L], [D]]
+    fac = omg.HashAggregationOperatorFactory([0], [L], agg_cols, in_types, out_types, funcs,
+                                             output_partials=[True] * len(funcs))
+    op = fac.create_operator()
+    out = op.align_schema(omg.make_batch([L, I, D], [key, vint, vdbl], [knull, inull, dnull]))
+    cols = omg.batch_to_numpy(out)
+    omg.free_batch(out)
+    empty = op.align_schema(omg.make_batch([L, I, D], [np.zeros(0, np.int64), np.zeros(0, np.int32),
+                                                       np.zeros(0, np.float64)]))
+    assert omg.batch_row_count(empty) == 0 and omg.lib().omg_batch_vector_count(empty) == 11
+    omg.free_batch(empty)
+    op.delete()
+    fac.close()
+    assert len(cols) == 11
+    valid_i, valid_d = ~inull, ~dnull
+    expect = [(key, knull), (vint.astype(np.int64), inull), (valid_i.astype(np.int64), None), (np.ones(n), None),
+              (vint, inull), (vint, inull), (np.where(valid_d, vdbl, 0.0), None), (valid_d.astype(np.int64), None),
+              (np.where(valid_i, vint.astype(np.float64), 0.0), None), (valid_i.astype(np.int64), None),
+              (vdbl, dnull)]
+    for j, ((gv, gm), (ev, em)) in enumerate(zip(cols, expect)):
+        em = np.zeros(n, bool) if em is None else em
+        assert np.array_equal(gm, em), j
+        assert np.array_equal(gv[~em], np.asarray(ev)[~em]), j
+
+
+@pytest.mark.parametrize("strategy", [None, omg.AGG_STRATEGY_PARTITIONED])
+def test_adaptive_partial_aggregation_equals_single_stage(strategy):
+    """Spark's adaptive partial aggregation: some batches are aggregated by the partial
+    operator, the rest only aligned to its output schema (AlignSchema); the final stage merges
+    both kinds of partial rows into the single-stage result."""
+    n = 200_000
+    key, knull, vlong, vnull, vdbl, dnull, dead = _random_input(n, 21)
+    types = [L, L, D]
+    funcs = [SUM, CNT, CNT_ALL, MIN, MAX, AVG, SUM]
+    agg_cols = [[1], [1], [], [1], [1], [2], [2]]
+    in_types = [[L], [L], [], [L], [L], [D], [D]]
+    part_out = [[L], [L], [L], [L], [L], [D, L], [D]]
+    part = omg.HashAggregationOperatorFactory([0], [L], agg_cols, in_types, part_out, funcs,
+                                              output_partials=[True] * len(funcs))
+    batches = _batches(types, [key, vlong, vdbl], [knull, vnull, dnull], [4096, 3000])
+    aggregated = _run(part, batches[::2], strategy)
+    aligner = part.create_operator()
+    aligned = [aligner.align_schema(b) for b in batches[1::2]]
+    aligner.delete()
+    part.close()
+    merge_cols = [[1], [2], [3], [4], [5], [6, 7], [8]]
+    merge_in = [[L], [L], [L], [L], [L], [D, L], [D]]
+    fin = omg.HashAggregationOperatorFactory([0], [L], merge_cols, merge_in, [[L], [L], [L], [L], [L], [D], [D]],
+                                             funcs, input_raws=[False] * len(funcs))
+    cols = _columns(_run(fin, aligned + aggregated, strategy))
+    fin.close()
+    T_LONG, T_DOUBLE = oracle.T_LONG, oracle.T_DOUBLE
+    ora = oracle.hashagg([key], [T_LONG], [knull], [
+        dict(func=SUM, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=CNT, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=CNT_ALL, col=None, out_type=T_LONG),
+        dict(func=MIN, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=MAX, col=vlong, in_type=T_LONG, out_type=T_LONG, nulls=vnull),
+        dict(func=AVG, col=vdbl, in_type=T_DOUBLE, out_type=T_DOUBLE, nulls=dnull),
+        dict(func=SUM, col=vdbl, in_type=T_DOUBLE, out_type=T_DOUBLE, nulls=dnull),
+    ])
+    exact = {5: exact_by_key([key], [knull], vdbl, ~dnull, divide_by_count=True),
+             6: exact_by_key([key], [knull], vdbl, ~dnull)}
+    assert_agg_equal(cols, ora, 1, double_aggs=(5, 6), exact=exact)
