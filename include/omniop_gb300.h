@@ -164,7 +164,7 @@ int32_t omg_hashagg_factory_create(const uint32_t *group_cols, const OmgDataType
 /* HashBuilderOperatorFactory::CreateHashBuilderOperatorFactory(joinType, buildTypes,
  *     buildHashCols, buildHashColsCount, operatorCount) -- operator/join/hash_builder.h:28-29.
  * join_type: OMNI_JOIN_TYPE_* (inner 0, left 1, right 2, full 3, left semi 4, left anti 5,
- * existence 6); one key column. */
+ * existence 6); 1 to 4 key columns of fixed width (probe key columns of the same widths). */
 int32_t omg_hashbuilder_factory_create(int32_t join_type, const OmgDataType *build_types,
     int32_t n_build_types, const int32_t *build_hash_cols, int32_t n_hash_cols, int32_t operator_count,
     void **out_factory);

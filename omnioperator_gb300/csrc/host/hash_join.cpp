@@ -41,6 +41,7 @@ bool JoinKeyType(DataTypeId id)
         case OMNI_DATE64:
         case OMNI_TIMESTAMP:
         case OMNI_DECIMAL64:
+        case OMNI_DECIMAL128:
             return true;
         default:
             return false;
@@ -72,6 +73,10 @@ struct JoinBuildState {
     omg::JoinTable table{};
     uint32_t maxDup = 0;
     DevArray<uint8_t> visited;  // BUILD_OUTER / FULL: one byte per build row, set by the probes
+    // Several key columns (or one 16-byte key): the table is keyed by the tuple hash of each row.
+    bool multiKey = false;
+    DevArray<uint64_t> keyHash;
+    DevArray<uint8_t> keyHashNulls;
 
     bool TracksVisits() const { return kind == omg::JOIN_KIND_BUILD_OUTER || kind == omg::JOIN_KIND_FULL; }
 
@@ -102,7 +107,7 @@ void JoinBuildState::Build()
     colNulls.assign(nCols, DevArray<uint8_t>());
     colHasNull.assign(nCols, false);
     const int32_t keyCol = hashCols[0];
-    const int32_t keyWidth = buildTypes.GetType(keyCol)->ByteWidth();
+    const int32_t keyWidth = multiKey ? 8 : buildTypes.GetType(keyCol)->ByteWidth();
     table.keyWidth = keyWidth;
     // Gather every build column into one contiguous HBM array (reading host-pinned or
     // device batches directly).
@@ -136,6 +141,26 @@ void JoinBuildState::Build()
     }
     const void *keys = colValues[keyCol].Get();
     const uint8_t *keyNulls = colHasNull[keyCol] ? colNulls[keyCol].Get() : nullptr;
+    if (multiKey) {
+        omg::JoinKeyCols kc{};
+        kc.nKeys = static_cast<int32_t>(hashCols.size());
+        bool anyNull = false;
+        for (int k = 0; k < kc.nKeys; ++k) {
+            const int32_t c = hashCols[k];
+            kc.widths[k] = buildTypes.GetType(c)->ByteWidth();
+            kc.cols[k] = colValues[c].Get();
+            kc.nulls[k] = colHasNull[c] ? colNulls[c].Get() : nullptr;
+            anyNull = anyNull || colHasNull[c];
+        }
+        keyHash.Reset(static_cast<size_t>(rows), s);
+        if (anyNull) {
+            keyHashNulls.Reset(omg::NullBitmapBytes(rows), s, true);
+        }
+        CudaCheck(omg::LaunchJoinKeyHash(kc, rows, keyHash.Get(), anyNull ? keyHashNulls.Get() : nullptr, s),
+            "hash key tuples");
+        keys = keyHash.Get();
+        keyNulls = anyNull ? keyHashNulls.Get() : nullptr;
+    }
     DevArray<long long> stats(8, s, true);
     CudaCheck(omg::LaunchKeyStats(keys, keyNulls, rows, keyWidth, stats.Get(), s), "key stats");
     long long h[3];
@@ -267,21 +292,24 @@ HashBuilderOperatorFactory::HashBuilderOperatorFactory(JoinType joinType, BuildS
     if (buildSide != OMNI_BUILD_UNKNOWN && buildSide != OMNI_BUILD_LEFT && buildSide != OMNI_BUILD_RIGHT) {
         throw OmniException("INVALID_ARGUMENT", "unknown build side", -1);
     }
-    if (buildHashColsCount != 1 || buildHashCols == nullptr) {
-        throw OmniException("UNSUPPORTED_ERROR", "only single-column join keys are supported", -2);
+    if (buildHashColsCount < 1 || buildHashColsCount > omg::kMaxJoinKeys || buildHashCols == nullptr) {
+        throw OmniException("UNSUPPORTED_ERROR", "join keys have 1 to 4 columns", -2);
     }
     if (operatorCount < 1) {
         throw OmniException("INVALID_ARGUMENT", "operatorCount must be positive", -1);
     }
-    const int32_t k = buildHashCols[0];
-    if (k < 0 || k >= buildTypes.GetSize() || !JoinKeyType(buildTypes.GetType(k)->GetId())) {
-        throw OmniException("UNSUPPORTED_ERROR", "unsupported join key column", -2);
+    for (int32_t i = 0; i < buildHashColsCount; ++i) {
+        const int32_t k = buildHashCols[i];
+        if (k < 0 || k >= buildTypes.GetSize() || !JoinKeyType(buildTypes.GetType(k)->GetId())) {
+            throw OmniException("UNSUPPORTED_ERROR", "unsupported join key column", -2);
+        }
     }
     state_->joinType = joinType;
     state_->buildSide = buildSide;
     state_->kind = kind;
     state_->buildTypes = buildTypes;
     state_->hashCols.assign(buildHashCols, buildHashCols + buildHashColsCount);
+    state_->multiKey = buildHashColsCount > 1 || buildTypes.GetType(buildHashCols[0])->ByteWidth() == 16;
     state_->operatorCount = operatorCount;
 }
 
@@ -366,15 +394,23 @@ LookupJoinOperatorFactory::LookupJoinOperatorFactory(const DataTypes &probeTypes
     HashBuilderOperatorFactory *builder)
     : probeTypes(probeTypes_), buildOutputTypes(buildOutputTypes_), build(builder->GetBuildState())
 {
-    if (probeHashColsCount != 1) {
-        throw OmniException("UNSUPPORTED_ERROR", "only single-column join keys are supported", -2);
+    if (probeHashColsCount != static_cast<int32_t>(build->hashCols.size())) {
+        throw OmniException("INVALID_ARGUMENT", "probe and build key column counts differ", -1);
     }
     probeOutputCols.assign(probeOutputCols_, probeOutputCols_ + probeOutputColsCount);
     probeHashCols.assign(probeHashCols_, probeHashCols_ + probeHashColsCount);
     buildOutputCols.assign(buildOutputCols_, buildOutputCols_ + buildOutputColsCount);
-    const int32_t k = probeHashCols[0];
-    if (k < 0 || k >= probeTypes.GetSize() || !JoinKeyType(probeTypes.GetType(k)->GetId())) {
-        throw OmniException("UNSUPPORTED_ERROR", "unsupported probe key column", -2);
+    for (int32_t i = 0; i < probeHashColsCount; ++i) {
+        const int32_t k = probeHashCols[i];
+        if (k < 0 || k >= probeTypes.GetSize() || !JoinKeyType(probeTypes.GetType(k)->GetId())) {
+            throw OmniException("UNSUPPORTED_ERROR", "unsupported probe key column", -2);
+        }
+        // A hashed key tuple compares value bytes, so each probe key column has its build
+        // column's width.
+        if (build->multiKey &&
+            probeTypes.GetType(k)->ByteWidth() != build->buildTypes.GetType(build->hashCols[i])->ByteWidth()) {
+            throw OmniException("INVALID_ARGUMENT", "probe and build key columns differ in width", -1);
+        }
     }
     if (buildOutputTypes.GetSize() != buildOutputColsCount) {
         throw OmniException("INVALID_ARGUMENT", "build output types and columns disagree", -1);
@@ -496,8 +532,15 @@ void LookupJoinOperator::ProcessPending()
     }
     cudaStream_t s = impl_->stream.Get();
     // Kernel inputs: probe key first, then the probe output columns.
-    std::vector<int32_t> inputCols{f_.probeHashCols[0]};
-    std::map<int32_t, int32_t> inputOf{{f_.probeHashCols[0], 0}};
+    // Kernel inputs: the probe key column(s) first, then the probe output columns.
+    std::vector<int32_t> inputCols;
+    std::map<int32_t, int32_t> inputOf;
+    for (int32_t c : f_.probeHashCols) {
+        if (inputOf.count(c) == 0) {
+            inputOf[c] = static_cast<int32_t>(inputCols.size());
+            inputCols.push_back(c);
+        }
+    }
     for (int32_t c : f_.probeOutputCols) {
         if (inputOf.count(c) == 0) {
             inputOf[c] = static_cast<int32_t>(inputCols.size());
@@ -516,8 +559,16 @@ void LookupJoinOperator::ProcessPending()
     p.batches = bt.DeviceBatches();
     p.tiles = bt.DeviceTiles();
     p.nTiles = bt.NumTiles();
-    p.keyInput = 0;
+    p.keyInput = b.multiKey ? -1 : 0;
     p.keyWidth = f_.probeTypes.GetType(f_.probeHashCols[0])->ByteWidth();
+    if (b.multiKey) {
+        p.nKeyCols = static_cast<int32_t>(f_.probeHashCols.size());
+        for (int32_t k = 0; k < p.nKeyCols; ++k) {
+            p.keyCols[k].input = static_cast<int16_t>(inputOf[f_.probeHashCols[k]]);
+            p.keyCols[k].width = static_cast<int16_t>(f_.probeTypes.GetType(f_.probeHashCols[k])->ByteWidth());
+            p.keyCols[k].buildValues = b.colValues[b.hashCols[k]].Get();
+        }
+    }
     p.table = b.table;
     p.joinKind = b.kind;
     p.visited = b.TracksVisits() ? b.visited.Get() : nullptr;
@@ -557,7 +608,7 @@ void LookupJoinOperator::ProcessPending()
     // Unique build keys and <= 8 bytes of NULL-free build output per row: fetch the build
     // values with the table entry from a per-slot packed copy (built once per factory).
     {
-        bool eligible = b.table.unique && nOut > nProbeOut && b.kind == omg::JOIN_KIND_INNER;
+        bool eligible = b.table.unique && nOut > nProbeOut && b.kind == omg::JOIN_KIND_INNER && !b.multiKey;
         int shift = 0;
         for (size_t o = nProbeOut; o < nOut && eligible; ++o) {
             const int w = p.out[o].width;
@@ -831,7 +882,7 @@ bool LookupJoinOperator::ProcessPartitioned()
     JoinBuildState &b = *f_.build;
     const int32_t keyCol = f_.probeHashCols[0];
     if (!b.table.unique || b.table.keyWidth != 8 || f_.probeTypes.GetType(keyCol)->ByteWidth() != 8 ||
-        b.kind != omg::JOIN_KIND_INNER || b.buildSide == OMNI_BUILD_LEFT) {
+        b.kind != omg::JOIN_KIND_INNER || b.buildSide == OMNI_BUILD_LEFT || b.multiKey) {
         return false;
     }
     for (int32_t c : f_.probeOutputCols) {

@@ -111,6 +111,13 @@ __device__ __forceinline__ double LoadAsDoubleRO(const void *col, int64_t row, i
     return static_cast<double>(SignExtend(LoadBitsRO(col, row, width), width));
 }
 
+// One step of the hash of a join key tuple; build and probe sides feed the same value bits
+// (zero-extended, 16-byte values as two words) in key-column order.
+__device__ __forceinline__ uint64_t KeyTupleStep(uint64_t h, uint64_t v)
+{
+    return Mix64(h ^ (v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2)));
+}
+
 // Order-preserving map of a non-NaN double onto int64 (-0.0 sorts just below +0.0).
 __device__ __forceinline__ int64_t OrderedFromDouble(double x)
 {

@@ -654,7 +654,46 @@ __device__ __forceinline__ void WriteProbeOnlyRow(const ProbeLaunch &p, const Ba
     }
 }
 
-// Probe for the join kinds other than INNER (lookup_join.cpp:1037-1430).  Each warp takes 32
+// Hash of the probe row's key tuple; false when a key column is NULL (never matches).
+__device__ __forceinline__ bool ProbeTupleHash(const ProbeLaunch &p, const BatchDesc &b, int64_t row, uint64_t &h)
+{
+    h = static_cast<uint64_t>(p.nKeyCols);
+    for (int k = 0; k < p.nKeyCols; ++k) {
+        const JoinKeyCol &kc = p.keyCols[k];
+        if (RowIsNullRO(b.nulls[kc.input], row)) {
+            return false;
+        }
+        if (kc.width == 16) {
+            const longlong2 v = __ldg(static_cast<const longlong2 *>(b.cols[kc.input]) + row);
+            h = KeyTupleStep(KeyTupleStep(h, static_cast<uint64_t>(v.x)), static_cast<uint64_t>(v.y));
+        } else {
+            h = KeyTupleStep(h, LoadBitsRO(b.cols[kc.input], row, kc.width));
+        }
+    }
+    return true;
+}
+
+// The probe row's key tuple equals build row `br`'s, column by column.
+__device__ __forceinline__ bool TupleEquals(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br)
+{
+    for (int k = 0; k < p.nKeyCols; ++k) {
+        const JoinKeyCol &kc = p.keyCols[k];
+        if (kc.width == 16) {
+            const longlong2 x = __ldg(static_cast<const longlong2 *>(b.cols[kc.input]) + row);
+            const longlong2 y = __ldg(static_cast<const longlong2 *>(kc.buildValues) + br);
+            if (x.x != y.x || x.y != y.y) {
+                return false;
+            }
+        } else if (LoadBitsRO(b.cols[kc.input], row, kc.width) != LoadBitsRO(kc.buildValues, br, kc.width)) {
+            return false;
+        }
+    }
+    return true;
+}
+
+// Probe for the join kinds other than INNER (lookup_join.cpp:1037-1430), and for every kind
+// when the key has several columns (then the table is keyed by the tuple hash and candidates
+// are compared column by column).  Each warp takes 32
 // consecutive probe rows at a time: lane i looks row i up and decides how many rows it emits
 // (by kind), the warp prefix-sums those counts, reserves its output range with one atomicAdd and
 // writes the rows in probe-row order.  BUILD_OUTER and FULL also mark every matched build row
@@ -668,11 +707,12 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
     const bool emitMatches = kind == JOIN_KIND_INNER || kind == JOIN_KIND_PROBE_OUTER ||
         kind == JOIN_KIND_BUILD_OUTER || kind == JOIN_KIND_FULL;
     const bool unique = p.table.unique != 0;
+    const bool multi = p.nKeyCols > 0;
     for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
         const TileDesc tile = p.tiles[t];
         const BatchDesc &b = p.batches[tile.batch];
-        const void *keyCol = b.cols[p.keyInput];
-        const uint8_t *keyNulls = b.nulls[p.keyInput];
+        const void *keyCol = multi ? nullptr : b.cols[p.keyInput];
+        const uint8_t *keyNulls = multi ? nullptr : b.nulls[p.keyInput];
         const int region = t % p.nRegions;
         const uint64_t regionBase = static_cast<uint64_t>(region) * p.regionCap;
         for (int r0 = warp * 32; r0 < tile.rows; r0 += kWarps * 32) {
@@ -681,18 +721,31 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
             const int64_t row = static_cast<int64_t>(tile.row0) + r;
             int64_t key = 0;
             Match m{0, 0, 0};
+            uint32_t nMatch = 0;  // candidates whose key equals the probe key
             if (exists) {
-                key = LoadIntRO(keyCol, row, p.keyWidth);
-                if (!RowIsNullRO(keyNulls, row)) {
-                    m = Lookup(p.table, static_cast<uint64_t>(key));
+                if (multi) {
+                    uint64_t h;
+                    if (ProbeTupleHash(p, b, row, h)) {
+                        m = Lookup(p.table, h);
+                        for (uint32_t k = 0; k < m.count; ++k) {
+                            const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
+                            nMatch += TupleEquals(p, b, row, br) ? 1u : 0u;
+                        }
+                    }
+                } else {
+                    key = LoadIntRO(keyCol, row, p.keyWidth);
+                    if (!RowIsNullRO(keyNulls, row)) {
+                        m = Lookup(p.table, static_cast<uint64_t>(key));
+                        nMatch = m.count;
+                    }
                 }
             }
-            const bool matched = m.count != 0;
+            const bool matched = nMatch != 0;
             uint32_t emit = 0;
             switch (kind) {
                 case JOIN_KIND_PROBE_OUTER:
                 case JOIN_KIND_FULL:
-                    emit = exists ? (matched ? m.count : 1u) : 0u;
+                    emit = exists ? (matched ? nMatch : 1u) : 0u;
                     break;
                 case JOIN_KIND_SEMI:
                     emit = matched ? 1u : 0u;
@@ -704,12 +757,14 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
                     emit = exists ? 1u : 0u;
                     break;
                 default:  // INNER, BUILD_OUTER
-                    emit = m.count;
+                    emit = nMatch;
             }
             if (p.visited != nullptr && matched) {
                 for (uint32_t k = 0; k < m.count; ++k) {
                     const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
-                    p.visited[br] = 1;
+                    if (!multi || TupleEquals(p, b, row, br)) {
+                        p.visited[br] = 1;
+                    }
                 }
             }
             uint32_t inc = emit;
@@ -731,13 +786,42 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
             }
             const uint64_t at = pos + inc - emit;
             if (emitMatches && matched) {
-                for (uint32_t k = 0; k < m.count && at + k < p.regionCap; ++k) {
+                uint64_t j = at;
+                for (uint32_t k = 0; k < m.count && j < p.regionCap; ++k) {
                     const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
-                    WriteJoinRow(p, b, row, key, br, regionBase + at + k);
+                    if (!multi || TupleEquals(p, b, row, br)) {
+                        WriteJoinRow(p, b, row, key, br, regionBase + j);
+                        ++j;
+                    }
                 }
             } else if (at < p.regionCap) {
                 WriteProbeOnlyRow(p, b, row, key, matched, regionBase + at);
             }
+        }
+    }
+}
+
+// Build side of a multi-column key: the tuple hash of every build row, NULL when a key column
+// is NULL (such rows never enter the table).
+__global__ void JoinKeyHashKernel(const JoinKeyCols kc, int64_t n, uint64_t *out, uint8_t *outNulls)
+{
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint64_t h = static_cast<uint64_t>(kc.nKeys);
+        bool isNull = false;
+        for (int k = 0; k < kc.nKeys; ++k) {
+            if (RowIsNull(kc.nulls[k], i)) {
+                isNull = true;
+            } else if (kc.widths[k] == 16) {
+                const uint64_t *v = static_cast<const uint64_t *>(kc.cols[k]) + 2 * i;
+                h = KeyTupleStep(KeyTupleStep(h, v[0]), v[1]);
+            } else {
+                h = KeyTupleStep(h, LoadBits(kc.cols[k], i, kc.widths[k]));
+            }
+        }
+        out[i] = isNull ? 0 : h;
+        if (isNull) {
+            SetBit(outNulls, static_cast<uint64_t>(i));
         }
     }
 }
@@ -1186,7 +1270,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     if (p.nTiles <= 0) {
         return cudaSuccess;
     }
-    if (p.joinKind != JOIN_KIND_INNER) {
+    if (p.joinKind != JOIN_KIND_INNER || p.nKeyCols > 0) {
         static int kindBlocks = 0;
         if (kindBlocks <= 0) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kindBlocks, ProbeKindKernel, kProbeThreads, 0);
@@ -1284,6 +1368,15 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     const int maxGrid = SMs() * blocksPerSM[which];
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
     kernel<<<grid, kProbeThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchJoinKeyHash(const JoinKeyCols &kc, int64_t n, uint64_t *out, uint8_t *outNulls, cudaStream_t stream)
+{
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    JoinKeyHashKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(kc, n, out, outNulls);
     return cudaGetLastError();
 }
 

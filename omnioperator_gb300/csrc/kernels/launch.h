@@ -73,6 +73,8 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream);
 // One output column of AlignSchema (adaptive partial aggregation) for every input row.
 cudaError_t LaunchAlignColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
     const int64_t *tileOutRow, const AlignCol &c, void *out, uint8_t *outNulls, cudaStream_t stream);
+// Multi-column join keys: the tuple hash of each build row (NULL if a key column is NULL).
+cudaError_t LaunchJoinKeyHash(const JoinKeyCols &kc, int64_t n, uint64_t *out, uint8_t *outNulls, cudaStream_t stream);
 // Outer joins: flags[i] = 1 for build rows never matched; their row numbers in order (offsets =
 // exclusive scan of the flags); dst[i] = src[rows[i]] with NULL bits.
 cudaError_t LaunchUnvisitedFlags(const uint8_t *visited, int64_t n, uint32_t *flags, cudaStream_t stream);

@@ -316,6 +316,25 @@ struct JoinOutCol {
     uint8_t *nulls;              // output null bitmap (nullptr = output has no nulls)
 };
 
+// Multi-column (or 16-byte) join keys: the table is keyed by a 64-bit hash of the key tuple and
+// every candidate build row is compared column by column before it counts as a match.
+constexpr int kMaxJoinKeys = 4;
+
+struct JoinKeyCol {
+    int16_t input;             // probe kernel input index
+    int16_t width;             // bytes (1, 2, 4, 8 or 16); build and probe widths are equal
+    int32_t pad;
+    const void *buildValues;   // contiguous build key column in HBM
+};
+
+// Key columns of one side, for hashing (build: contiguous columns).
+struct JoinKeyCols {
+    int32_t nKeys;
+    int32_t widths[kMaxJoinKeys];
+    const void *cols[kMaxJoinKeys];
+    const uint8_t *nulls[kMaxJoinKeys];
+};
+
 constexpr int kRegionStride = 16;  // counters 128 bytes apart
 constexpr int kMaxRegions = 16;
 
@@ -340,6 +359,8 @@ struct ProbeLaunch {
     int32_t *error;
     int32_t joinKind;   // JoinKind
     uint8_t *visited;   // BUILD_OUTER / FULL: one byte per build row, set to 1 when matched
+    int32_t nKeyCols;   // > 0: hashed multi-column key (keyInput unused, -1)
+    JoinKeyCol keyCols[kMaxJoinKeys];
 };
 
 }  // namespace omg

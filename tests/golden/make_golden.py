@@ -6,6 +6,7 @@ the test sources; each entry below restates one test's inputs and EXPECT_* value
 `python tests/golden/make_golden.py` to regenerate the JSON files.
 """
 import json
+import struct
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
@@ -120,6 +121,11 @@ def _s(vals):
     return [STR[v] for v in vals]
 
 
+def _bits(vals):
+    """IEEE-754 bit patterns of doubles as signed int64."""
+    return [struct.unpack("<q", struct.pack("<d", v))[0] for v in vals]
+
+
 JOIN_TYPED = {
     "left_join": dict(
         source="core/test/operator/join_test.cpp:773-833", join_type="LEFT", build_side="UNKNOWN",
@@ -194,6 +200,31 @@ JOIN_TYPED = {
         probe=[[1, 2, 3, 4, 3, 6], [11, 22, 33, 44, 22, 44]], probe_nulls=None, probe_hash_col=1,
         probe_output_cols=[], build_output_cols=[],
         expected_rows=[[1], [0], [1], [0], [0], [0]], outer_rows=None),
+    # Multi-column keys (short, int, long); the test reads the probe operator's rows only.
+    "multi_keys_full_integer": dict(
+        source="core/test/operator/join_test.cpp:4637-4704", join_type="FULL", build_side="UNKNOWN",
+        types=["SHORT", "INT", "LONG"],
+        build=[[1, 2, 3, 4, 5, 6], [11, 22, 33, 44, 55, 66], [111, 222, 333, 444, 555, 666]], build_nulls=None,
+        build_hash_cols=[0, 1, 2],
+        probe=[[1, 3, 5, 7], [11, 33, 55, 77], [111, 333, 555, 777]], probe_nulls=None, probe_hash_cols=[0, 1, 2],
+        probe_output_cols=[0, 1, 2], build_output_cols=[0, 1, 2],
+        expected_rows=[[1, 11, 111, 1, 11, 111], [3, 33, 333, 3, 33, 333], [5, 55, 555, 5, 55, 555],
+                       [7, 77, 777, None, None, None]],
+        outer_rows=None),
+    # join_test.cpp:4706-4772 fills its Decimal64 key column from doubles; the values here are
+    # those doubles' 64-bit patterns, which is what the decimal64 column holds.
+    "multi_keys_full_decimal64": dict(
+        source="core/test/operator/join_test.cpp:4706-4772", join_type="FULL", build_side="UNKNOWN",
+        types=["SHORT", "INT", "LONG"],
+        build=[[1, 2, 3, 4, 5, 6], [11, 22, 33, 44, 55, 66], _bits([1.11, 2.22, 3.33, 4.44, 5.55, 6.66])],
+        build_nulls=None, build_hash_cols=[0, 1, 2],
+        probe=[[1, 3, 5, 7], [11, 33, 55, 77], _bits([1.11, 3.33, 5.55, 7.77])], probe_nulls=None,
+        probe_hash_cols=[0, 1, 2], probe_output_cols=[0, 1, 2], build_output_cols=[0, 1, 2],
+        expected_rows=[[1, 11, _bits([1.11])[0], 1, 11, _bits([1.11])[0]],
+                       [3, 33, _bits([3.33])[0], 3, 33, _bits([3.33])[0]],
+                       [5, 55, _bits([5.55])[0], 5, 55, _bits([5.55])[0]],
+                       [7, 77, _bits([7.77])[0], None, None, None]],
+        outer_rows=None),
 }
 
 

@@ -216,11 +216,14 @@ def expected_join_rows(probe_cols, probe_nulls, build_cols, build_nulls, pk, bk,
 
 
 def kat_columns(k):
-    """Build/probe columns and NULL masks of a typed join KAT."""
-    dt = np.int16 if k.get("types") == "SHORT" else np.int64
+    """Build/probe columns and NULL masks of a typed join KAT ("types": one type for all
+    columns or a list per column)."""
+    dts = {"SHORT": np.int16, "INT": np.int32, "LONG": np.int64}
+    t = k.get("types", "LONG")
 
     def side(cols, nulls):
-        vals = [np.array(c, dtype=dt) for c in cols]
+        kinds = t if isinstance(t, list) else [t] * len(cols)
+        vals = [np.array(c, dtype=dts[kd]) for c, kd in zip(cols, kinds)]
         masks = [np.zeros(len(c), bool) for c in cols]
         for m, rows in zip(masks, nulls or []):
             m[rows] = True
@@ -228,22 +231,50 @@ def kat_columns(k):
     return side(k["build"], k["build_nulls"]), side(k["probe"], k["probe_nulls"])
 
 
+def kat_hash_cols(k, side):
+    """Key columns of a KAT side ("build"/"probe"): one column or a list."""
+    v = k.get(side + "_hash_cols", k.get(side + "_hash_col"))
+    return v if isinstance(v, list) else [v]
+
+
+def tuple_ids(build_keys, build_masks, probe_keys, probe_masks):
+    """Dense ids of key tuples over both sides (equal tuples, equal ids; decimal128 as (n, 2)
+    words) and each row's NULL flag (any key column NULL): a multi-column key restated as one
+    column for the oracle's join."""
+    nb = len(build_keys[0])
+    cols = []
+    for bk, pk in zip(build_keys, probe_keys):
+        a = np.concatenate([np.asarray(bk), np.asarray(pk)])
+        if a.ndim == 2:
+            cols += [a[:, 0].astype(np.int64), a[:, 1].astype(np.int64)]
+        else:
+            cols.append(a.astype(np.int64))
+    mat = np.stack(cols, axis=1)
+    _, inv = np.unique(mat, axis=0, return_inverse=True)
+    inv = np.asarray(inv).reshape(-1).astype(np.int64)
+    nulls = np.zeros(len(mat), bool)
+    for bm, pm in zip(build_masks, probe_masks):
+        nulls |= np.concatenate([bm, pm])
+    return inv[:nb], nulls[:nb], inv[nb:], nulls[nb:]
+
+
 def oracle_join_rows(k):
-    """Output rows (probe output values, build output values or the existence flag; None =
-    NULL) of a typed join KAT computed by the oracle."""
+    """(probe-side rows, outer-join rows) of a typed join KAT computed by the oracle: probe
+    output values, then build output values or the existence flag; None = NULL."""
     (b, bm), (p, pm) = kat_columns(k)
     kind = oracle.join_kind(k["join_type"], k["build_side"])
-    pi, bi = oracle.join(kind, b[k["build_hash_col"]], bm[k["build_hash_col"]], p[k["probe_hash_col"]],
-                         pm[k["probe_hash_col"]])
-    rows = []
+    bh, ph = kat_hash_cols(k, "build"), kat_hash_cols(k, "probe")
+    bid, bn, pid, pn = tuple_ids([b[c] for c in bh], [bm[c] for c in bh], [p[c] for c in ph], [pm[c] for c in ph])
+    pi, bi = oracle.join(kind, bid, bn, pid, pn)
+    rows, outer = [], []
     for i, j in zip(pi.tolist(), bi.tolist()):
         r = [None if i < 0 or pm[c][i] else int(p[c][i]) for c in k["probe_output_cols"]]
         if kind == "existence":
             r.append(j)
         else:
             r += [None if j < 0 or bm[c][j] else int(b[c][j]) for c in k["build_output_cols"]]
-        rows.append(r)
-    return rows
+        (outer if i < 0 else rows).append(r)
+    return rows, outer
 
 
 def row_key(r):

@@ -10,7 +10,7 @@ import pytest
 
 import omnioperator_gb300 as omg
 import oracle
-from helpers import kat_columns, row_key, rows_matrix, split
+from helpers import kat_columns, kat_hash_cols, row_key, rows_matrix, split, tuple_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -35,7 +35,9 @@ def run_typed_join(join_type, build_side, build_types, build_cols, build_masks, 
     outer output batches).  Probe output of a build-left join is rotated back to probe-first."""
     kind = oracle.join_kind(join_type, build_side)
     jt, bs = oracle.JOIN_TYPES[join_type], oracle.BUILD_SIDES[build_side]
-    bf = omg.HashBuilderOperatorFactory(jt, build_types, [bhash], operator_count=build_batches, build_side=bs)
+    bhash = bhash if isinstance(bhash, list) else [bhash]
+    phash = phash if isinstance(phash, list) else [phash]
+    bf = omg.HashBuilderOperatorFactory(jt, build_types, bhash, operator_count=build_batches, build_side=bs)
     builders = [bf.create_operator() for _ in range(build_batches)]
     nb = len(build_cols[0])
     step = -(-nb // build_batches) if nb else 1
@@ -47,7 +49,7 @@ def run_typed_join(join_type, build_side, build_types, build_cols, build_masks, 
         bop.get_output()
         assert bop.get_status() == omg.OMNI_STATUS_FINISHED
     bo_types = [build_types[c] for c in build_out]
-    pf = omg.LookupJoinOperatorFactory(probe_types, probe_out, [phash], build_out, bo_types, bf)
+    pf = omg.LookupJoinOperatorFactory(probe_types, probe_out, phash, build_out, bo_types, bf)
     pop = pf.create_operator()
     assert not pop.is_blocked()
     outs = []
@@ -101,12 +103,14 @@ def test_join_type_kats_on_gpu(name):
     """The reference's own outer/semi/anti/existence join tests, row multisets compared."""
     k = JOIN_TYPED[name]
     (b, bm), (p, pm) = kat_columns(k)
-    t = S if k.get("types") == "SHORT" else L
-    cols, outer, _ = run_typed_join(k["join_type"], k["build_side"], [t] * len(b), b, bm, k["build_hash_col"],
-                                    [t] * len(p), p, pm, k["probe_hash_col"], k["probe_output_cols"],
+    t = k.get("types", "LONG")
+    types = [{"SHORT": S, "INT": I, "LONG": L}[x] for x in (t if isinstance(t, list) else [t] * len(b))]
+    cols, outer, _ = run_typed_join(k["join_type"], k["build_side"], types, b, bm, kat_hash_cols(k, "build"),
+                                    types, p, pm, kat_hash_cols(k, "probe"), k["probe_output_cols"],
                                     k["build_output_cols"])
     assert sorted(map(row_key, _rows(cols))) == sorted(map(row_key, k["expected_rows"]))
-    assert sorted(map(row_key, _rows(outer))) == sorted(map(row_key, k["outer_rows"] or []))
+    if k["outer_rows"] is not None:
+        assert sorted(map(row_key, _rows(outer))) == sorted(map(row_key, k["outer_rows"]))
 
 
 def test_existence_column_is_boolean():
@@ -219,3 +223,79 @@ def test_full_join_without_probe_rows_emits_every_build_row():
                                           [np.zeros(0, bool)], 0, [0], [1])
     assert cols is None and n_outer == 1
     assert sorted(map(row_key, _rows(outer))) == sorted(map(row_key, [[None, 3 * i] for i in range(10)]))
+
+
+@pytest.mark.parametrize("join_type", ["INNER", "LEFT", "FULL", "LEFT_SEMI", "LEFT_ANTI", "EXISTENCE"])
+@pytest.mark.parametrize("shape", ["int_long", "short_long_int", "decimal128"])
+def test_multi_column_keys_match_oracle(join_type, shape):
+    """Keys of several columns (and one 16-byte decimal key): the table holds the tuple hash and
+    every candidate is compared column by column, so equal hashes of different tuples never
+    match.  Duplicates, NULL key columns (any NULL: no match) and every output row checked."""
+    rng = np.random.default_rng(["int_long", "short_long_int", "decimal128"].index(shape) * 10 + len(join_type))
+    nb, npr = 40_000, 150_000
+    pool = 12_000
+    if shape == "int_long":
+        kt = [I, L]
+        dom = [rng.integers(-50, 50, pool).astype(np.int32), rng.integers(-2**40, 2**40, pool)]
+    elif shape == "short_long_int":
+        kt = [S, L, I]
+        dom = [rng.integers(-3, 3, pool).astype(np.int16), rng.integers(0, 40, pool).astype(np.int64),
+               rng.integers(-2**31, 2**31, pool, dtype=np.int64).astype(np.int32)]
+    else:
+        kt = [omg.Decimal128Type(38, 2)]
+        lo = rng.integers(0, 2**63, pool, dtype=np.int64).astype(np.uint64)
+        hi = rng.integers(-3, 3, pool).astype(np.int64).astype(np.uint64)
+        dom = [np.stack([lo, hi], axis=1)]
+    bsel = rng.integers(0, pool // 2, nb)
+    psel = rng.integers(0, pool, npr)
+    nk = len(kt)
+    bkeys = [d[bsel] for d in dom]
+    pkeys = [d[psel] for d in dom]
+    bkm = [rng.random(nb) < 0.02 for _ in range(nk)]
+    pkm = [rng.random(npr) < 0.02 for _ in range(nk)]
+    bpay = rng.integers(-2**62, 2**62, nb)
+    ppay = rng.integers(-2**31, 2**31, npr, dtype=np.int64).astype(np.int32)
+    bcols, bmasks = bkeys + [bpay], bkm + [np.zeros(nb, bool)]
+    pcols, pmasks = pkeys + [ppay], pkm + [rng.random(npr) < 0.05]
+    kind = oracle.join_kind(join_type, "UNKNOWN")
+    probe_out = list(range(nk + 1))
+    build_out = [] if kind in ("semi", "existence", "anti") else [nk] + list(range(nk))
+    cols, outer, _ = run_typed_join(join_type, "UNKNOWN", kt + [L], bcols, bmasks, list(range(nk)), kt + [I],
+                                    pcols, pmasks, list(range(nk)), probe_out, build_out, batch_sizes=(4096, 5000))
+    bid, bn, pid, pn = tuple_ids(bkeys, bkm, pkeys, pkm)
+    pi_all, bi_all = oracle.join(kind, bid, bn, pid, pn)
+
+    def flat(values, masks, idx, cols_):
+        out = []
+        ok = idx >= 0
+        j = np.where(ok, idx, 0)
+        for c in cols_:
+            v, m = values[c], masks[c]
+            if v.ndim == 2:  # decimal128: compare both words
+                out += [(v[j, 0].astype(np.int64), ~ok | m[j]), (v[j, 1].astype(np.int64), ~ok | m[j])]
+            else:
+                out.append((v[j], ~ok | m[j]))
+        return out
+    def split_words(cols_):
+        out = []
+        for v, m in (cols_ or []):
+            if v.ndim == 2:
+                out += [(v[:, 0].astype(np.int64), m), (v[:, 1].astype(np.int64), m)]
+            else:
+                out.append((v, m))
+        return out
+
+    # Probe-operator rows, then (full joins) the outer-join operator's unmatched build rows.
+    for part, got_cols in (("probe", cols), ("outer", outer)):
+        sel = (pi_all >= 0) if part == "probe" else (pi_all < 0)
+        if part == "outer" and kind != "full":
+            assert outer is None
+            continue
+        pi, bi = pi_all[sel], bi_all[sel]
+        want = flat(pcols, pmasks, pi, probe_out)
+        want += [(bi, np.zeros(len(bi), bool))] if kind == "existence" else flat(bcols, bmasks, bi, build_out)
+        got = split_words(got_cols)
+        got_m = rows_matrix(got) if got else np.zeros((0, 0), np.int64)
+        want_m = rows_matrix(want)
+        assert got_m.shape[0] == want_m.shape[0] and len(pi) > 0, part
+        assert np.array_equal(got_m, want_m), part

@@ -97,8 +97,10 @@ JOIN_TYPED = json.loads((G / "join_type_kats.json").read_text())
 @pytest.mark.parametrize("name", sorted(JOIN_TYPED))
 def test_oracle_join_type_kats(name):
     k = JOIN_TYPED[name]
-    expected = k["expected_rows"] + (k["outer_rows"] or [])
-    assert sorted(map(row_key, oracle_join_rows(k))) == sorted(map(row_key, expected))
+    rows, outer = oracle_join_rows(k)
+    assert sorted(map(row_key, rows)) == sorted(map(row_key, k["expected_rows"]))
+    if k["outer_rows"] is not None:  # None: the reference test does not read the outer rows
+        assert sorted(map(row_key, outer)) == sorted(map(row_key, k["outer_rows"]))
 
 
 def test_oracle_join_kinds_match_bruteforce():
