@@ -24,7 +24,10 @@ Further objects, each a workload of its own with its own timing:
                learned task sizer;
   join_skewed  build 2^26 (16-byte payload), probe 2^30 Zipf(s), s in {0.9, 1.1, 1.3}: the direct
                probe vs hash partitioning vs learned range partitioning (4096 partitions), every
-               output checked against the direct probe's by a row-multiset fingerprint.
+               output checked against the direct probe's by a row-multiset fingerprint;
+  join_kinds   the headline data through left outer, left semi, left anti, existence and full
+               outer joins (with the outer-join operator), and an inner join on a two-column key;
+  agg_two_stage  the uniform aggregation as 4 partial + 1 final operator, and AlignSchema.
 Inputs of these legs are larger than L2.
 
 `--impl reference` times the reference's CPU algorithm (the oracle restatement; the reference
@@ -342,7 +345,11 @@ def run_gpu(args, rank, world):
                 "algorithmic_bytes": int(alg_bytes)}
 
     e2e = None if args.skip_e2e else run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank)
+    kinds = None if args.skip_ext else run_join_kinds(args, omg, torch, stream, barrier, max_over_ranks, world, bkey,
+                                                       p1, p2, pkey, pbits, pnull)
     agg = None if args.skip_agg else run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world)
+    two_stage = None if args.skip_ext else run_agg_two_stage(args, omg, torch, dev, stream, barrier, max_over_ranks,
+                                                              world)
     pop.delete()
     bop.delete()
     pf.close()
@@ -355,7 +362,194 @@ def run_gpu(args, rank, world):
     join5 = None if args.skip_join5 else run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                           world, rank)
     return dict(value=value, ms=ms / args.steps, build_ms=build_ms, launches=launches, roofline=roofline,
-                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew, batched=batched, join5=join5)
+                clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew, batched=batched, join5=join5,
+                kinds=kinds, two_stage=two_stage)
+
+
+def run_join_kinds(args, omg, torch, stream, barrier, max_over_ranks, world, bkey, p1, p2, pkey, pbits, pnull):
+    """The headline build and probe data through the other join kinds: outer (probe side),
+    semi, anti, existence, full (probe plus the outer-join operator), and an inner join on a
+    two-column key (the probe key split into two int32 columns).  Inputs resident in HBM,
+    outputs left in HBM; the probe kernel's roofline counts 8 B key + 1/8 B validity per probe
+    row and the output bytes."""
+    L, I = omg.LongType(), omg.IntType()
+    matched = int(((pkey < N_BUILD) & ~pnull).sum().item())
+    hits = torch.zeros(N_BUILD, dtype=torch.bool, device=pkey.device)
+    hits[pkey[(pkey < N_BUILD) & ~pnull]] = True
+    unmatched_build = N_BUILD - int(hits.sum().item())
+    del hits
+    bhi, blo = (bkey >> 10).to(torch.int32), (bkey & 1023).to(torch.int32)
+    phi, plo = (pkey >> 10).to(torch.int32), (pkey & 1023).to(torch.int32)
+    cases = [
+        # name, join type, probe output cols, build output cols, output row bytes, probe-operator rows
+        ("left_outer", omg.OMNI_JOIN_TYPE_LEFT, [0], [1, 2], 16, N_PROBE),
+        ("left_semi", omg.OMNI_JOIN_TYPE_LEFT_SEMI, [0], [], 8, matched),
+        ("left_anti", omg.OMNI_JOIN_TYPE_LEFT_ANTI, [0], [], 8, N_PROBE - matched),
+        ("existence", omg.OMNI_JOIN_TYPE_EXISTENCE, [0], [], 9, N_PROBE),
+        ("full_outer", omg.OMNI_JOIN_TYPE_FULL, [0], [1, 2], 16, N_PROBE),
+        ("inner_two_column_key", omg.OMNI_JOIN_TYPE_INNER, [0, 1], [2, 3], 16, matched),
+    ]
+    peak, peak_kind = measured_peak_gbs()
+    out = {"workload": "the headline build (2^20) and probe (2^26) data, per join kind; inputs and outputs in HBM"}
+    for name, jt, pout, bout, row_bytes, rows in cases:
+        two = name == "inner_two_column_key"
+        btypes = [I, I, I, I] if two else [L, I, I]
+        bcols = [bhi, blo, p1, p2] if two else [bkey, p1, p2]
+        bf = omg.HashBuilderOperatorFactory(jt, btypes, [0, 1] if two else [0])
+        bop = bf.create_operator()
+        bop.set_stream(stream.cuda_stream)
+        bop.add_input(omg.wrap_device_batch(btypes, N_BUILD, [c.data_ptr() for c in bcols]))
+        bop.get_output()
+        ptypes = [I, I] if two else [L]
+        pcols = [phi, plo] if two else [pkey]
+        pnulls = [pbits.data_ptr(), None] if two else [pbits.data_ptr()]
+        bo_types = [btypes[c] for c in bout]
+        pf = omg.LookupJoinOperatorFactory(ptypes, pout, [0, 1] if two else [0], bout, bo_types, bf)
+        of = (omg.LookupOuterJoinOperatorFactory(ptypes, pout, bout, bo_types, bf)
+              if jt == omg.OMNI_JOIN_TYPE_FULL else None)
+        pop = pf.create_operator()
+        pop.set_stream(stream.cuda_stream)
+        pop.set_device_output(True)
+
+        def step():
+            pop.add_input(omg.wrap_device_batch(ptypes, N_PROBE, [c.data_ptr() for c in pcols], pnulls))
+            outs, n = pop.get_outputs(1 << 16)
+            omg.free_batches(outs)
+            n_outer = 0
+            if of is not None:
+                oop = of.create_operator()
+                oop.set_stream(stream.cuda_stream)
+                oop.set_device_output(True)
+                for b in oop.drain():
+                    n_outer += omg.batch_row_count(b)
+                    omg.free_batch(b)
+                oop.delete()
+            return n, n_outer
+
+        for _ in range(args.warmup):
+            n, n_outer = step()
+            assert n == rows and n_outer == (unmatched_build if of is not None else 0), (name, n, n_outer)
+        c0 = pop.counters()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            n, n_outer = step()
+        e1.record(stream)
+        barrier()
+        c1 = pop.counters()
+        ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
+        kernel_s = (c1["kernel_ns"] - c0["kernel_ns"]) / max(c1["kernel_launches"] - c0["kernel_launches"], 1) / 1e9
+        alg = (N_PROBE * (8 if not two else 8) + N_PROBE / 8 + rows * row_bytes)
+        achieved = alg / kernel_s / 1e9
+        out[name] = {"value": world * N_PROBE / (ms / 1e3), "unit": "probe rows/s", "ms_per_step": round(ms, 4),
+                     "output_rows": n, "outer_rows": n_outer,
+                     "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                                  "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                                  "kernel": "ProbeKindKernel", "kernel_ms": round(kernel_s * 1e3, 4),
+                                  "algorithmic_bytes": int(alg)}}
+        pop.delete()
+        bop.delete()
+        if of is not None:
+            of.close()
+        pf.close()
+        bf.close()
+    return out
+
+
+def run_agg_two_stage(args, omg, torch, dev, stream, barrier, max_over_ranks, world):
+    """The uniform aggregation's data split over 4 partial operators, merged by one final
+    operator; and AlignSchema (adaptive partial aggregation) over all 2^22 rows.  Inputs in HBM,
+    outputs in HBM, L2 flushed between steps."""
+    L, D = omg.LongType(), omg.DoubleType()
+    SUM, CNT, MIN, MAX, AVG = (omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_COUNT_COLUMN,
+                               omg.OMNI_AGGREGATION_TYPE_MIN, omg.OMNI_AGGREGATION_TYPE_MAX,
+                               omg.OMNI_AGGREGATION_TYPE_AVG)
+    key, v1, v2 = agg_data_numpy(2)
+    tk, t1, t2 = (torch.from_numpy(x).to(dev) for x in (key, v1, v2))
+    flush = torch.empty(1 << 27, dtype=torch.int32, device=dev)
+    funcs = [SUM, CNT, MIN, MAX, SUM, AVG]
+    part = omg.HashAggregationOperatorFactory([0], [L], [[1], [1], [1], [1], [2], [2]], [[L]] * 4 + [[D], [D]],
+                                              [[L], [L], [L], [L], [D], [D, L]], funcs,
+                                              output_partials=[True] * 6)
+    fin = omg.HashAggregationOperatorFactory([0], [L], [[1], [2], [3], [4], [5], [6, 7]],
+                                             [[L]] * 4 + [[D], [D, L]], [[L]] * 4 + [[D], [D]], funcs,
+                                             input_raws=[False] * 6)
+    quarter = AGG_ROWS // 4
+
+    def run(fac, batches):
+        op = fac.create_operator()
+        op.set_stream(stream.cuda_stream)
+        op.set_device_output(True)
+        for b in batches:
+            op.add_input(b)
+        outs = op.drain()
+        op.delete()
+        return outs
+
+    def step():
+        partials = []
+        for q in range(4):
+            o = q * quarter
+            partials += run(part, [omg.wrap_device_batch([L, L, D], quarter, [tk.data_ptr() + 8 * o,
+                                                                            t1.data_ptr() + 8 * o,
+                                                                            t2.data_ptr() + 8 * o])])
+        e_mid = torch.cuda.Event(enable_timing=True)
+        e_mid.record(stream)
+        final = run(fin, partials)
+        groups = sum(omg.batch_row_count(b) for b in final)
+        omg.free_batches(final)
+        return groups, e_mid
+
+    def align_step():
+        op = part.create_operator()
+        op.set_stream(stream.cuda_stream)
+        op.set_device_output(True)
+        b = op.align_schema(omg.wrap_device_batch([L, L, D], AGG_ROWS, [tk.data_ptr(), t1.data_ptr(), t2.data_ptr()]))
+        n = omg.batch_row_count(b)
+        omg.free_batch(b)
+        op.delete()
+        return n
+
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        assert step()[0] == AGG_GROUPS
+        assert align_step() == AGG_ROWS
+    tot = partial_ms = align_ms = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        groups, e_mid = step()
+        e1.record(stream)
+        barrier()
+        tot += e0.elapsed_time(e1)
+        partial_ms += e0.elapsed_time(e_mid)
+        assert groups == AGG_GROUPS
+        flush.fill_(1)
+        barrier()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        assert align_step() == AGG_ROWS
+        a1.record(stream)
+        barrier()
+        align_ms += a0.elapsed_time(a1)
+    ms = max_over_ranks(tot) / args.steps
+    part.close()
+    fin.close()
+    peak, kind = measured_peak_gbs()
+    align_s = max_over_ranks(align_ms) / args.steps / 1e3
+    # AlignSchema moves 24 B in and 72 B out per row (key, SUM, COUNT, MIN, MAX, SUM, AVG sum + count).
+    return {"workload": "the uniform aggregation (2^22 rows, 10,000 groups) as 4 partial operators + 1 final "
+                        "operator; AlignSchema of all 2^22 rows; L2 flushed between steps",
+            "two_stage": {"value": world * AGG_ROWS / (ms / 1e3), "unit": "rows/s", "ms_per_step": round(ms, 4),
+                          "partial_ms": round(partial_ms / args.steps, 4),
+                          "final_ms": round(ms - partial_ms / args.steps, 4), "partial_rows": 4 * AGG_GROUPS},
+            "align_schema": {"value": world * AGG_ROWS / align_s, "unit": "rows/s",
+                             "ms_per_step": round(align_s * 1e3, 4),
+                             "achieved_gbs": round(AGG_ROWS * 96 / align_s / 1e9, 1), "peak": peak,
+                             "frac_of_peak": round(AGG_ROWS * 96 / align_s / 1e9 / peak, 4), "peak_kind": kind}}
 
 
 def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
@@ -791,6 +985,8 @@ def main():
     ap.add_argument("--sizer", default=None, help="sizing model weights (JSON) for the learned arm")
     ap.add_argument("--skip-batched", action="store_true", help="skip the batched small aggregations")
     ap.add_argument("--skip-join5", action="store_true", help="skip the skewed join (partitioners)")
+    ap.add_argument("--skip-ext", action="store_true",
+                    help="skip the other join kinds and the two-stage aggregation")
     ap.add_argument("--join5-build-log2", type=int, default=None)
     ap.add_argument("--join5-probe-log2", type=int, default=None)
     ap.add_argument("--batch-tasks", type=int, default=None, help="tasks of the batched aggregation (default 10,000)")
@@ -827,7 +1023,7 @@ def main():
                             "build_ms": round(r["build_ms"], 3), "output_rows_per_step": r["rows"]},
                  "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"],
                  "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"], "agg_batched": r["batched"],
-                 "join_skewed": r["join5"]})
+                 "join_skewed": r["join5"], "join_kinds": r.get("kinds"), "agg_two_stage": r.get("two_stage")})
     print(json.dumps(line), flush=True)
 
 

@@ -608,11 +608,11 @@ void LookupJoinOperator::ProcessPending()
     // Unique build keys and <= 8 bytes of NULL-free build output per row: fetch the build
     // values with the table entry from a per-slot packed copy (built once per factory).
     {
-        bool eligible = b.table.unique && nOut > nProbeOut && b.kind == omg::JOIN_KIND_INNER && !b.multiKey;
+        bool eligible = b.table.unique && nOut > nProbeOut && b.kind != omg::JOIN_KIND_EXISTENCE && !b.multiKey;
         int shift = 0;
         for (size_t o = nProbeOut; o < nOut && eligible; ++o) {
             const int w = p.out[o].width;
-            eligible = (w == 1 || w == 2 || w == 4 || w == 8) && !cols[o].hasNull && shift + 8 * w <= 64;
+            eligible = (w == 1 || w == 2 || w == 4 || w == 8) && !b.colHasNull[p.out[o].src] && shift + 8 * w <= 64;
             p.out[o].shift = static_cast<int16_t>(shift);
             shift += 8 * w;
         }
@@ -622,18 +622,24 @@ void LookupJoinOperator::ProcessPending()
             f_.slotPayload = omg::Buffer::NewDevice((nSlots + 1) * sizeof(uint64_t), s, false);
             CudaCheck(omg::LaunchBuildSlotPayload(p, nSlots, static_cast<uint64_t *>(f_.slotPayload->Data()), s),
                 "build slot payload");
-            if (b.table.mode == omg::JOIN_ARRAY) {
-                f_.slotBits = omg::Buffer::NewDevice(omg::SlotBitsBytes(b.table.range), s, false);
-                CudaCheck(omg::LaunchBuildSlotBits(b.table.arrayEntries, b.table.range,
-                              static_cast<uint32_t *>(f_.slotBits->Data()), s),
-                    "build slot bitmap");
-            }
             impl_->stream.Sync();
             f_.payloadDecided = true;
         }
+        // Occupancy bitmap of a unique ARRAY table, for the bitmap probe (kinds that mark no
+        // build rows; with or without a slot payload).
+        const bool wantBits = b.table.unique && b.table.mode == omg::JOIN_ARRAY && !b.multiKey && !b.TracksVisits();
+        if (wantBits && !f_.slotBits) {
+            f_.slotBits = omg::Buffer::NewDevice(omg::SlotBitsBytes(b.table.range), s, false);
+            CudaCheck(omg::LaunchBuildSlotBits(b.table.arrayEntries, b.table.range,
+                          static_cast<uint32_t *>(f_.slotBits->Data()), s),
+                "build slot bitmap");
+            impl_->stream.Sync();
+        }
         if (eligible && f_.slotPayload) {
             p.table.slotPayload = static_cast<const uint64_t *>(f_.slotPayload->Data());
-            p.table.slotBits = f_.slotBits ? static_cast<const uint32_t *>(f_.slotBits->Data()) : nullptr;
+        }
+        if (wantBits && f_.slotBits) {
+            p.table.slotBits = static_cast<const uint32_t *>(f_.slotBits->Data());
         }
     }
     // Output regions: tile t writes into region t % nRegions (see ProbeLaunch).  A region's

@@ -484,6 +484,54 @@ __global__ void BuildSlotPayloadKernel(const int64_t *entries, uint64_t nSlots, 
     }
 }
 
+// An output row without a build match: probe columns copied, build columns NULL (value 0),
+// the existence flag (side 2) set to `matched`.
+__device__ __forceinline__ void WriteProbeOnlyRow(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t key,
+    bool matched, uint64_t pos)
+{
+    for (int o = 0; o < p.nOut; ++o) {
+        const JoinOutCol &oc = p.out[o];
+        if (oc.side == 0) {
+            // Unlike a matched row, this one may carry a NULL probe key (outer and anti joins).
+            if (oc.src == p.keyInput) {
+                StoreKey(oc.values, pos, oc.width, key);
+            } else {
+                CopyValueRO(oc.values, pos, b.cols[oc.src], row, oc.width);
+            }
+            if (oc.nulls != nullptr && RowIsNullRO(b.nulls[oc.src], row)) {
+                SetBit(oc.nulls, pos);
+            }
+        } else if (oc.side == 1) {
+            uint8_t *d = static_cast<uint8_t *>(oc.values) + static_cast<uint64_t>(oc.width) * pos;
+            for (int i = 0; i < oc.width; ++i) {
+                d[i] = 0;
+            }
+            SetBit(oc.nulls, pos);
+        } else {
+            static_cast<uint8_t *>(oc.values)[pos] = matched ? 1 : 0;
+        }
+    }
+}
+
+// Output rows a probe row yields for a join kind, given whether the row exists (inside the
+// tile) and its number of matching build rows.
+__device__ __forceinline__ uint32_t EmitCount(int kind, bool exists, uint32_t cnt)
+{
+    switch (kind) {
+        case JOIN_KIND_PROBE_OUTER:
+        case JOIN_KIND_FULL:
+            return exists ? (cnt != 0 ? cnt : 1u) : 0u;
+        case JOIN_KIND_SEMI:
+            return cnt != 0 ? 1u : 0u;
+        case JOIN_KIND_ANTI:
+            return exists && cnt == 0 ? 1u : 0u;
+        case JOIN_KIND_EXISTENCE:
+            return exists ? 1u : 0u;
+        default:  // INNER, BUILD_OUTER
+            return cnt;
+    }
+}
+
 // Each warp owns kWarpRounds * 32 consecutive rows of a tile and works on its own: lane i reads
 // rows base + 32r + i (coalesced), looks the keys up, reserves its output range with one
 // atomicAdd, and writes its matches compacted in row order.  kUnique: every key has at most one
@@ -491,13 +539,19 @@ __global__ void BuildSlotPayloadKernel(const int64_t *entries, uint64_t nSlots, 
 constexpr int kWarpRounds = 16;
 constexpr int kRowsPerWarp = kWarpRounds * 32;
 
-template <bool kUnique, bool kPayload>
+// kKinds: any join kind (p.joinKind) -- the rows each probe row yields follow EmitCount, rows
+// without a match get NULL build columns, and matched build rows are marked visited when the
+// kind keeps unmatched build rows.
+template <bool kUnique, bool kPayload, bool kKinds>
 __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_constant__ ProbeLaunch p)
 {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const unsigned int lanesBelow = (1u << lane) - 1u;
     const bool arrayMode = p.table.mode == JOIN_ARRAY;
+    const int kind = kKinds ? p.joinKind : static_cast<int>(JOIN_KIND_INNER);
+    const bool emitMatches = kind == JOIN_KIND_INNER || kind == JOIN_KIND_PROBE_OUTER ||
+        kind == JOIN_KIND_BUILD_OUTER || kind == JOIN_KIND_FULL;
     for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
         const TileDesc tile = p.tiles[t];
         const int w0 = warp * kRowsPerWarp;
@@ -511,12 +565,14 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
         const int nRows = min(kRowsPerWarp, tile.rows - w0);
         // Phase 1: all keys and validity bits of the warp's rows (independent loads).
         int64_t key[kWarpRounds];
-        uint32_t live = 0;  // bit i: this lane's row of round i exists and its key is not NULL
+        uint32_t live = 0;   // bit i: this lane's row of round i exists and its key is not NULL
+        uint32_t exist = 0;  // bit i: this lane's row of round i exists
 #pragma unroll
         for (int i = 0; i < kWarpRounds; ++i) {
             const int r = i * 32 + lane;
             key[i] = 0;
             if (r < nRows) {
+                exist |= 1u << i;
                 key[i] = LoadIntRO(keyCol, base + r, p.keyWidth);
                 if (!RowIsNullRO(keyNulls, base + r)) {
                     live |= 1u << i;
@@ -560,16 +616,41 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
                 hit |= (m.count != 0 ? 1u : 0u) << i;
             }
         }
+        if (kKinds && p.visited != nullptr) {
+#pragma unroll
+            for (int i = 0; i < kWarpRounds; ++i) {
+                if ((hit >> i) & 1u) {
+                    // Most matches hit rows already marked: read first, store only the first time
+                    // (a lost race stores the same value twice).
+                    if (kUnique) {
+                        if (p.visited[entry[i]] == 0) {
+                            p.visited[entry[i]] = 1;
+                        }
+                    } else {
+                        for (uint32_t k = 0; k < cnt[i]; ++k) {
+                            const int32_t br = __ldg(p.table.csrRows + entry[i] + k);
+                            if (p.visited[br] == 0) {
+                                p.visited[br] = 1;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        // emitBits (unique tables) / emit[] (duplicates): rows each probe row yields.
+        uint32_t emitBits = 0;
         uint32_t total = 0;
         if (kUnique) {
 #pragma unroll
             for (int i = 0; i < kWarpRounds; ++i) {
-                total += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
+                const bool e = kKinds ? EmitCount(kind, (exist >> i) & 1u, (hit >> i) & 1u) != 0 : ((hit >> i) & 1u);
+                emitBits |= (e ? 1u : 0u) << i;
+                total += __popc(__ballot_sync(0xffffffffu, e));
             }
         } else {
 #pragma unroll
             for (int i = 0; i < kWarpRounds; ++i) {
-                total += cnt[i];
+                total += kKinds ? EmitCount(kind, (exist >> i) & 1u, cnt[i]) : cnt[i];
             }
             total = __reduce_add_sync(0xffffffffu, total);
         }
@@ -587,23 +668,28 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
 #pragma unroll
         for (int i = 0; i < kWarpRounds; ++i) {
             const int64_t row = base + i * 32 + lane;
+            const bool matched = (hit >> i) & 1u;
             if (kUnique) {
-                const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
-                if ((hit >> i) & 1u) {
+                const bool e = (emitBits >> i) & 1u;
+                const unsigned int m = __ballot_sync(0xffffffffu, e);
+                if (e) {
                     const uint64_t at = pos + __popc(m & lanesBelow);
                     if (at < p.regionCap) {
                         // The key is re-read (an L1/L2 hit) rather than kept live in registers.
-                        if (kPayload) {
-                            WriteJoinRowPayload(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), payload[i],
-                                regionBase + at);
+                        const int64_t k = LoadIntRO(keyCol, row, p.keyWidth);
+                        if (kKinds && !(matched && emitMatches)) {
+                            WriteProbeOnlyRow(p, b, row, k, matched, regionBase + at);
+                        } else if (kPayload) {
+                            WriteJoinRowPayload(p, b, row, k, payload[i], regionBase + at);
                         } else {
-                            WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), entry[i], regionBase + at);
+                            WriteJoinRow(p, b, row, k, entry[i], regionBase + at);
                         }
                     }
                 }
                 pos += __popc(m);
             } else {
-                uint32_t inc = cnt[i];
+                const uint32_t e = kKinds ? EmitCount(kind, (exist >> i) & 1u, cnt[i]) : cnt[i];
+                uint32_t inc = e;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
@@ -611,45 +697,22 @@ __global__ void __launch_bounds__(kProbeThreads, 3) ProbeKernel(const __grid_con
                         inc += y;
                     }
                 }
-                const uint64_t at = pos + inc - cnt[i];
-                for (uint32_t k = 0; k < cnt[i]; ++k) {
-                    if (at + k >= p.regionCap) {
-                        break;
+                const uint64_t at = pos + inc - e;
+                if (kKinds && e != 0 && !(matched && emitMatches)) {
+                    if (at < p.regionCap) {
+                        WriteProbeOnlyRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), matched, regionBase + at);
                     }
-                    WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth), __ldg(p.table.csrRows + entry[i] + k),
-                        regionBase + at + k);
+                } else {
+                    for (uint32_t k = 0; k < e; ++k) {
+                        if (at + k >= p.regionCap) {
+                            break;
+                        }
+                        WriteJoinRow(p, b, row, LoadIntRO(keyCol, row, p.keyWidth),
+                            __ldg(p.table.csrRows + entry[i] + k), regionBase + at + k);
+                    }
                 }
                 pos += __shfl_sync(0xffffffffu, inc, 31);
             }
-        }
-    }
-}
-
-// An output row without a build match: probe columns copied, build columns NULL (value 0),
-// the existence flag (side 2) set to `matched`.
-__device__ __forceinline__ void WriteProbeOnlyRow(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t key,
-    bool matched, uint64_t pos)
-{
-    for (int o = 0; o < p.nOut; ++o) {
-        const JoinOutCol &oc = p.out[o];
-        if (oc.side == 0) {
-            // Unlike a matched row, this one may carry a NULL probe key (outer and anti joins).
-            if (oc.src == p.keyInput) {
-                StoreKey(oc.values, pos, oc.width, key);
-            } else {
-                CopyValueRO(oc.values, pos, b.cols[oc.src], row, oc.width);
-            }
-            if (oc.nulls != nullptr && RowIsNullRO(b.nulls[oc.src], row)) {
-                SetBit(oc.nulls, pos);
-            }
-        } else if (oc.side == 1) {
-            uint8_t *d = static_cast<uint8_t *>(oc.values) + static_cast<uint64_t>(oc.width) * pos;
-            for (int i = 0; i < oc.width; ++i) {
-                d[i] = 0;
-            }
-            SetBit(oc.nulls, pos);
-        } else {
-            static_cast<uint8_t *>(oc.values)[pos] = matched ? 1 : 0;
         }
     }
 }
@@ -691,9 +754,9 @@ __device__ __forceinline__ bool TupleEquals(const ProbeLaunch &p, const BatchDes
     return true;
 }
 
-// Probe for the join kinds other than INNER (lookup_join.cpp:1037-1430), and for every kind
-// when the key has several columns (then the table is keyed by the tuple hash and candidates
-// are compared column by column).  Each warp takes 32
+// Probe for keys of several columns (or one 16-byte column), every join kind
+// (lookup_join.cpp:924-1430): the table is keyed by the tuple hash and each candidate is
+// compared column by column before it counts as a match.  Each warp takes 32
 // consecutive probe rows at a time: lane i looks row i up and decides how many rows it emits
 // (by kind), the warp prefix-sums those counts, reserves its output range with one atomicAdd and
 // writes the rows in probe-row order.  BUILD_OUTER and FULL also mark every matched build row
@@ -762,7 +825,7 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
             if (p.visited != nullptr && matched) {
                 for (uint32_t k = 0; k < m.count; ++k) {
                     const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
-                    if (!multi || TupleEquals(p, b, row, br)) {
+                    if ((!multi || TupleEquals(p, b, row, br)) && p.visited[br] == 0) {
                         p.visited[br] = 1;
                     }
                 }
@@ -1080,13 +1143,20 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
     int width[kNumOut];
     int shift[kNumOut];
     bool isKey[kNumOut];
+    bool isFlag[kNumOut];
 #pragma unroll
     for (int o = 0; o < kNumOut; ++o) {
         vals[o] = p.out[o].values;
         width[o] = p.out[o].width;
         shift[o] = p.out[o].shift;
         isKey[o] = p.out[o].side == 0;
+        isFlag[o] = p.out[o].side == 2;
     }
+    // Join kinds without visited marks (inner, probe-side outer, semi, anti, existence): which
+    // rows are emitted follows EmitCount; unmatched rows get NULL build fields, emitted rows of a
+    // NULL probe key a NULL key.
+    const int kind = p.joinKind;
+    const bool inner = kind == JOIN_KIND_INNER;
     // kSingle: the segments of the one batch are indexed directly (no descriptor loads per segment).
     const long long *singleKeys = nullptr;
     const uint8_t *singleNulls = nullptr;
@@ -1136,12 +1206,23 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
         uint64_t payload[kBitsRounds];
 #pragma unroll
         for (int i = 0; i < kBitsRounds; ++i) {
-            payload[i] = ((hit >> i) & 1u) ? __ldg(payloadTab + (static_cast<uint64_t>(key[i]) - minKey)) : 0ull;
+            payload[i] = ((hit >> i) & 1u) && payloadTab != nullptr
+                ? __ldg(payloadTab + (static_cast<uint64_t>(key[i]) - minKey))
+                : 0ull;
+        }
+        uint32_t emit = hit;  // bit i: this lane's row of round i yields an output row
+        if (!inner) {
+            emit = 0;
+#pragma unroll
+            for (int i = 0; i < kBitsRounds; ++i) {
+                const bool exists = base + i * 32 + lane < batchRows;
+                emit |= (EmitCount(kind, exists, (hit >> i) & 1u) != 0 ? 1u : 0u) << i;
+            }
         }
         uint32_t total = 0;
 #pragma unroll
         for (int i = 0; i < kBitsRounds; ++i) {
-            total += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
+            total += __popc(__ballot_sync(0xffffffffu, (emit >> i) & 1u));
         }
         const int region = t % p.nRegions;
         unsigned long long pos = 0;
@@ -1155,24 +1236,36 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
         const uint64_t regionBase = static_cast<uint64_t>(region) * p.regionCap;
 #pragma unroll
         for (int i = 0; i < kBitsRounds; ++i) {
-            const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
-            if ((hit >> i) & 1u) {
+            const unsigned int m = __ballot_sync(0xffffffffu, (emit >> i) & 1u);
+            if ((emit >> i) & 1u) {
                 const uint64_t rat = pos + __popc(m & lanesBelow);
                 if (rat < p.regionCap) {
                     const uint64_t at = regionBase + rat;
+                    const bool h = (hit >> i) & 1u;
+                    // Unmatched rows of a probe-side outer join carry zero build fields (NULL below).
+                    const int64_t flag = h ? 1 : 0;
                     StoreOut<kLayout, 0>(vals[0], at, width[0],
-                        isKey[0] ? key[i] : static_cast<int64_t>(payload[i] >> shift[0]));
+                        isKey[0] ? key[i] : (isFlag[0] ? flag : static_cast<int64_t>(payload[i] >> shift[0])));
                     if (kNumOut > 1) {
                         StoreOut<kLayout, 1>(vals[1], at, width[1],
-                            isKey[1] ? key[i] : static_cast<int64_t>(payload[i] >> shift[1]));
+                            isKey[1] ? key[i] : (isFlag[1] ? flag : static_cast<int64_t>(payload[i] >> shift[1])));
                     }
                     if (kNumOut > 2) {
                         StoreOut<kLayout, 2>(vals[2], at, width[2],
-                            isKey[2] ? key[i] : static_cast<int64_t>(payload[i] >> shift[2]));
+                            isKey[2] ? key[i] : (isFlag[2] ? flag : static_cast<int64_t>(payload[i] >> shift[2])));
                     }
                     if (kNumOut > 3) {
                         StoreOut<kLayout, 3>(vals[3], at, width[3],
-                            isKey[3] ? key[i] : static_cast<int64_t>(payload[i] >> shift[3]));
+                            isKey[3] ? key[i] : (isFlag[3] ? flag : static_cast<int64_t>(payload[i] >> shift[3])));
+                    }
+                    if (!inner) {
+                        const bool nullKey = !((live >> i) & 1u);
+#pragma unroll
+                        for (int o = 0; o < kNumOut; ++o) {
+                            if ((isKey[o] && nullKey) || (!isKey[o] && !isFlag[o] && !h)) {
+                                SetBit(p.out[o].nulls, at);
+                            }
+                        }
                     }
                 }
             }
@@ -1270,7 +1363,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     if (p.nTiles <= 0) {
         return cudaSuccess;
     }
-    if (p.joinKind != JOIN_KIND_INNER || p.nKeyCols > 0) {
+    if (p.nKeyCols > 0) {
         static int kindBlocks = 0;
         if (kindBlocks <= 0) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kindBlocks, ProbeKindKernel, kProbeThreads, 0);
@@ -1288,10 +1381,22 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         fast = (oc.side == 1 || (oc.side == 0 && oc.src == p.keyInput && oc.width == 8)) &&
             (oc.width == 1 || oc.width == 2 || oc.width == 4 || oc.width == 8);
     }
+    // The bitmap kernel also takes the kinds that mark no build rows; its outputs are the probe
+    // key, payload fields (a slot payload present) and the existence flag.
+    const bool bitsKind = p.joinKind == JOIN_KIND_INNER || p.joinKind == JOIN_KIND_PROBE_OUTER ||
+        p.joinKind == JOIN_KIND_SEMI || p.joinKind == JOIN_KIND_ANTI || p.joinKind == JOIN_KIND_EXISTENCE;
+    bool bitsOk = bitsKind && p.nKeyCols == 0 && p.table.unique && p.keyWidth == 8 && p.nOut >= 1 &&
+        p.nOut <= kFastMaxOut;
+    for (int o = 0; bitsOk && o < p.nOut; ++o) {
+        const JoinOutCol &oc = p.out[o];
+        bitsOk = ((oc.side == 1 && p.table.slotPayload != nullptr) ||
+                     (oc.side == 0 && oc.src == p.keyInput && oc.width == 8) || oc.side == 2) &&
+            (oc.width == 1 || oc.width == 2 || oc.width == 4 || oc.width == 8);
+    }
     // ARRAY tables whose occupancy bitmap fits in shared memory, on launches large enough to
     // amortise staging it into every CTA.
     const uint64_t bitsBytes = SlotBitsBytes(p.table.range);
-    if (fast && p.table.mode == JOIN_ARRAY && p.table.slotBits != nullptr && bitsBytes <= kBitsMaxSmem &&
+    if (bitsOk && p.table.mode == JOIN_ARRAY && p.table.slotBits != nullptr && bitsBytes <= kBitsMaxSmem &&
         p.nTiles >= kBitsMinTiles) {
         // Instances: run-time widths for 1-4 outputs, and compile-time widths for the common
         // layouts (8-byte key followed by payload fields).
@@ -1348,8 +1453,23 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         void *args[] = {const_cast<ProbeLaunch *>(&p)};
         return cudaLaunchKernel(kernel, dim3(grid), dim3(kBitsThreads), args, static_cast<size_t>(bitsBytes), stream);
     }
-    auto kernel = !p.table.unique ? ProbeKernel<false, false>
-                                  : (p.table.slotPayload != nullptr ? ProbeKernel<true, true> : ProbeKernel<true, false>);
+    if (p.nKeyCols == 0 && p.joinKind != JOIN_KIND_INNER) {
+        auto kk = !p.table.unique ? ProbeKernel<false, false, true>
+                                  : (p.table.slotPayload != nullptr ? ProbeKernel<true, true, true>
+                                                                    : ProbeKernel<true, false, true>);
+        static int kkBlocks[3] = {0, 0, 0};
+        const int w = !p.table.unique ? 0 : (p.table.slotPayload != nullptr ? 2 : 1);
+        if (kkBlocks[w] <= 0) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kkBlocks[w], kk, kProbeThreads, 0);
+            kkBlocks[w] = kkBlocks[w] <= 0 ? 1 : kkBlocks[w];
+        }
+        const int maxGrid = SMs() * kkBlocks[w];
+        kk<<<p.nTiles < maxGrid ? p.nTiles : maxGrid, kProbeThreads, 0, stream>>>(p);
+        return cudaGetLastError();
+    }
+    auto kernel = !p.table.unique ? ProbeKernel<false, false, false>
+                                  : (p.table.slotPayload != nullptr ? ProbeKernel<true, true, false>
+                                                                    : ProbeKernel<true, false, false>);
     int which = !p.table.unique ? 0 : (p.table.slotPayload != nullptr ? 2 : 1);
     if (fast) {
         const void *fk[kFastMaxOut] = {reinterpret_cast<const void *>(ProbeFastKernel<1>),
