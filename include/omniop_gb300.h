@@ -113,6 +113,14 @@ int32_t omg_debug_set_wait_budget(int64_t ticks);
  * Values are zeroed, no nulls.  FIXEDBINARY needs omg_vec_new_fixed. */
 int32_t omg_vec_new(int32_t type_id, int32_t size, void **out_vec);
 int32_t omg_vec_new_fixed(int32_t width, int32_t size, void **out_vec);
+/* New host VARCHAR (15) or CHAR (16) vector: size + 1 int32 offsets (zeroed) into a character
+ * buffer of `data_bytes` bytes; value i is bytes [offsets[i], offsets[i + 1]) -- the
+ * LargeStringContainer layout (vector/vector.h, vector/large_string_container.h). */
+int32_t omg_vec_new_varchar(int32_t type_id, int32_t size, int64_t data_bytes, void **out_vec);
+/* VARCHAR/CHAR accessors: the offsets array (NULL for fixed-width vectors; omg_vec_values is
+ * the character buffer) and the character buffer's size in bytes. */
+int32_t *omg_vec_offsets(void *vec);
+int64_t omg_vec_data_bytes(void *vec);
 /* New flat device vector (HBM, owned by the vector). */
 int32_t omg_vec_new_device(int32_t type_id, int32_t width, int32_t size, void **out_vec);
 /* Non-owning device view over caller memory.  `nulls` may be NULL (no nulls); when given

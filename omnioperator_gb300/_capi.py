@@ -30,6 +30,9 @@ _SIGS = {
     "omg_debug_set_wait_budget": (I32, [I64]),
     "omg_vec_new": (I32, [I32, I32, C.POINTER(P)]),
     "omg_vec_new_fixed": (I32, [I32, I32, C.POINTER(P)]),
+    "omg_vec_new_varchar": (I32, [I32, I32, I64, C.POINTER(P)]),
+    "omg_vec_offsets": (P, [P]),
+    "omg_vec_data_bytes": (I64, [P]),
     "omg_vec_new_device": (I32, [I32, I32, I32, C.POINTER(P)]),
     "omg_vec_wrap_device": (I32, [I32, I32, I32, P, P, C.POINTER(P)]),
     "omg_vec_free": (I32, [P]),

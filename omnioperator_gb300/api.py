@@ -19,6 +19,7 @@ from ._capi import OmgDataType, OmgError, check, lib
 OMNI_INT, OMNI_LONG, OMNI_DOUBLE, OMNI_BOOLEAN, OMNI_SHORT = 1, 2, 3, 4, 5
 OMNI_DECIMAL64, OMNI_DECIMAL128, OMNI_DATE32, OMNI_DATE64, OMNI_TIMESTAMP = 6, 7, 8, 9, 12
 OMNI_BYTE, OMNI_FLOAT, OMNI_FIXEDBINARY = 18, 19, 40
+OMNI_VARCHAR, OMNI_CHAR = 15, 16
 # FunctionType (operator/util/function_type.h:11-27)
 OMNI_AGGREGATION_TYPE_SUM, OMNI_AGGREGATION_TYPE_COUNT_COLUMN = 0, 1
 OMNI_AGGREGATION_TYPE_COUNT_ALL, OMNI_AGGREGATION_TYPE_AVG = 2, 3
@@ -48,6 +49,8 @@ class DataType:
 
     @property
     def byte_width(self) -> int:
+        if self.id in (OMNI_VARCHAR, OMNI_CHAR):
+            return 0  # variable length
         return self.width if self.id == OMNI_FIXEDBINARY else _WIDTH[self.id]
 
 
@@ -77,6 +80,11 @@ def Decimal128Type(precision=38, scale=0):
 
 def FixedBinaryType(width):
     return DataType(OMNI_FIXEDBINARY, 0, 0, width)
+
+
+def VarcharType(width=0):
+    """VARCHAR of at most `width` bytes (type/data_type.h VarcharDataType)."""
+    return DataType(OMNI_VARCHAR, 0, 0, width)
 
 
 def _types(types):
@@ -116,6 +124,23 @@ def new_host_vector(dtype: DataType, values: np.ndarray, nulls: np.ndarray | Non
     fixed binary: (n, width) uint8) with an optional boolean null mask."""
     n = len(values)
     out = C.c_void_p()
+    if dtype.id in (OMNI_VARCHAR, OMNI_CHAR):
+        # values: a sequence of bytes / str
+        enc = [v.encode() if isinstance(v, str) else bytes(v) for v in values]
+        offs = np.zeros(n + 1, dtype=np.int32)
+        if n:
+            offs[1:] = np.cumsum([len(v) for v in enc])
+        data = b"".join(enc)
+        check(lib().omg_vec_new_varchar(dtype.id, n, len(data), C.byref(out)))
+        vec = out.value
+        C.memmove(lib().omg_vec_offsets(vec), offs.ctypes.data, offs.nbytes)
+        if data:
+            C.memmove(lib().omg_vec_values(vec), data, len(data))
+        if nulls is not None and np.any(nulls):
+            bits = np.packbits(np.asarray(nulls, dtype=bool), bitorder="little")
+            C.memmove(lib().omg_vec_nulls(vec), bits.ctypes.data, bits.size)
+            check(lib().omg_vec_set_null_flag(vec, 1))
+        return vec
     if dtype.id == OMNI_FIXEDBINARY:
         check(lib().omg_vec_new_fixed(dtype.width, n, C.byref(out)))
     else:
@@ -198,7 +223,14 @@ def batch_to_numpy(batch: int):
         t = L.omg_vec_type(v)
         w = L.omg_vec_width(v)
         ptr = L.omg_vec_values(v)
-        if t == OMNI_DECIMAL128:
+        if t in (OMNI_VARCHAR, OMNI_CHAR):
+            offs = _np_view(L.omg_vec_offsets(v), np.int32, n + 1).copy() if n else np.zeros(1, np.int32)
+            total = int(offs[-1]) if n else 0
+            raw = bytes(_np_view(ptr, np.uint8, total)) if total else b""
+            vals = np.empty(n, dtype=object)
+            for j in range(n):
+                vals[j] = raw[offs[j]:offs[j + 1]]
+        elif t == OMNI_DECIMAL128:
             vals = _np_view(ptr, np.uint64, 2 * n).reshape(n, 2).copy()
         elif t == OMNI_FIXEDBINARY:
             vals = _np_view(ptr, np.uint8, w * n).reshape(n, w).copy()

@@ -148,6 +148,20 @@ int32_t omg_vec_new_fixed(int32_t width, int32_t size, void **out_vec)
     });
 }
 
+int32_t omg_vec_new_varchar(int32_t type_id, int32_t size, int64_t data_bytes, void **out_vec)
+{
+    return Guard([&] {
+        Require(out_vec != nullptr && size >= 0 && data_bytes >= 0 && data_bytes < (int64_t(1) << 31),
+            "invalid arguments");
+        Require(type_id == omniruntime::type::OMNI_VARCHAR || type_id == omniruntime::type::OMNI_CHAR,
+            "not a VARCHAR/CHAR type");
+        *out_vec = new BaseVector(static_cast<DataTypeId>(type_id), size, data_bytes, false);
+    });
+}
+
+int32_t *omg_vec_offsets(void *vec) { return vec ? static_cast<BaseVector *>(vec)->RawOffsets() : nullptr; }
+int64_t omg_vec_data_bytes(void *vec) { return vec ? static_cast<BaseVector *>(vec)->DataBytes() : -1; }
+
 int32_t omg_vec_new_device(int32_t type_id, int32_t width, int32_t size, void **out_vec)
 {
     return Guard([&] {

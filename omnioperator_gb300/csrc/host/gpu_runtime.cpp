@@ -46,6 +46,7 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
                 throw OmniException("OPERATOR_RUNTIME_ERROR", "vector shorter than the batch row count", -1);
             }
             d.cols[i] = v->RawValues();
+            d.offs[i] = v->RawOffsets();
             const bool hasNull = v->RawNulls() != nullptr && v->HasNull();
             d.nulls[i] = hasNull ? v->RawNulls() : nullptr;
             if (hasNull) {
@@ -142,8 +143,13 @@ std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int6
         const int32_t n = static_cast<int32_t>(std::min<int64_t>(step, rows - r0));
         auto *b = new VectorBatch(n);
         for (const auto &c : cols) {
-            const size_t vOff = static_cast<size_t>(firstRow + r0) * c.width;
             const size_t nOff = static_cast<size_t>((firstRow + r0) / 8);
+            if (c.width == 0) {
+                const size_t oOff = static_cast<size_t>(firstRow + r0) * sizeof(int32_t);
+                b->Append(new BaseVector(c.type, n, c.values, c.dataBytes, c.offsets, oOff, c.nulls, nOff, c.hasNull));
+                continue;
+            }
+            const size_t vOff = static_cast<size_t>(firstRow + r0) * c.width;
             b->Append(new BaseVector(c.type, c.width, n, c.values, vOff, c.nulls, nOff, c.hasNull));
         }
         out.push_back(b);
@@ -157,12 +163,36 @@ std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int
     std::vector<OutColumn> host;
     for (const auto &c : cols) {
         OutColumn h = c;
+        if (c.width == 0) {
+            // VARCHAR: the offsets of these rows, then the characters they span, rebased to 0.
+            const size_t ob = (static_cast<size_t>(rows) + 1) * sizeof(int32_t);
+            h.offsets = Buffer::NewHost(ob, false);
+            CudaCheck(cudaMemcpyAsync(h.offsets->Data(),
+                          static_cast<const char *>(c.offsets->Data()) + static_cast<size_t>(firstRow) * sizeof(int32_t),
+                          ob, cudaMemcpyDeviceToHost, s),
+                "copy output offsets to host");
+            CudaCheck(cudaStreamSynchronize(s), "copy output offsets to host");
+            int32_t *o = static_cast<int32_t *>(h.offsets->Data());
+            const int32_t base = o[0];
+            const int64_t bytes = static_cast<int64_t>(o[rows]) - base;
+            h.values = Buffer::NewHost(static_cast<size_t>(bytes) + 16, false);
+            h.dataBytes = bytes;
+            if (bytes > 0) {
+                CudaCheck(cudaMemcpyAsync(h.values->Data(), static_cast<const char *>(c.values->Data()) + base,
+                              static_cast<size_t>(bytes), cudaMemcpyDeviceToHost, s),
+                    "copy output characters to host");
+            }
+            for (int64_t i = 0; i <= rows; ++i) {
+                o[i] -= base;
+            }
+        } else {
         const size_t vb = static_cast<size_t>(rows) * c.width;
         h.values = Buffer::NewHost(vb == 0 ? 16 : vb, false);
         if (vb > 0) {
             const char *src = static_cast<const char *>(c.values->Data()) + static_cast<size_t>(firstRow) * c.width;
             CudaCheck(cudaMemcpyAsync(h.values->Data(), src, vb, cudaMemcpyDeviceToHost, s),
                 "copy output values to host");
+        }
         }
         const size_t nb = NullBitmapBytes(rows);
         if (c.nulls != nullptr && c.hasNull) {

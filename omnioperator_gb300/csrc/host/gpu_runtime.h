@@ -196,10 +196,12 @@ void SetWaitBudget(long long ticks);
 // `rowsPerBatch` rows that are views of the given buffers (host or device).
 struct OutColumn {
     omniruntime::type::DataTypeId type;
-    int32_t width;
+    int32_t width;    // 0: VARCHAR/CHAR (values = characters, offsets = rows + 1 int32)
     BufferPtr values;
     BufferPtr nulls;  // may be null
     bool hasNull;
+    BufferPtr offsets;       // VARCHAR/CHAR: absolute positions in `values`
+    int64_t dataBytes = 0;   // VARCHAR/CHAR: size of `values`
 };
 // The rows start at row `firstRow` of the buffers (a multiple of 8).
 std::vector<omniruntime::vec::VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows,

@@ -42,10 +42,30 @@ bool JoinKeyType(DataTypeId id)
         case OMNI_TIMESTAMP:
         case OMNI_DECIMAL64:
         case OMNI_DECIMAL128:
+        case OMNI_VARCHAR:
+        case OMNI_CHAR:
             return true;
         default:
             return false;
     }
+}
+
+bool Varlen(const DataTypePtr &t) { return t->GetId() == OMNI_VARCHAR || t->GetId() == OMNI_CHAR; }
+
+// A VARCHAR column from per-row lengths: exclusive offsets (n + 1, 64-bit) and the total.
+int64_t ScanLengths(const uint32_t *lens, int64_t n, DevArray<int64_t> &offs, cudaStream_t s)
+{
+    offs.Reset(static_cast<size_t>(n) + 1, s);
+    DevArray<int64_t> blockSums(static_cast<size_t>((n + 1023) / 1024 + 1), s);
+    DevArray<long long> total(1, s, true);
+    if (n > 0) {
+        CudaCheck(omg::LaunchScanCounts(lens, n, offs.Get(), blockSums.Get(), total.Get(), s), "scan lengths");
+    }
+    CudaCheck(omg::LaunchOffsetsTail(offs.Get(), n, total.Get(), s), "offsets tail");
+    long long h = 0;
+    CudaCheck(cudaMemcpyAsync(&h, total.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read total length");
+    CudaCheck(cudaStreamSynchronize(s), "read total length");
+    return h;
 }
 }  // namespace
 
@@ -67,6 +87,7 @@ struct JoinBuildState {
     std::vector<DevArray<uint8_t>> colValues;
     std::vector<DevArray<uint8_t>> colNulls;
     std::vector<bool> colHasNull;
+    std::vector<DevArray<int64_t>> colOffs;  // VARCHAR/CHAR columns: rows + 1 offsets into colValues
     DevArray<int64_t> entries;
     DevArray<uint64_t> hashKeys;
     DevArray<int32_t> csr;
@@ -106,17 +127,24 @@ void JoinBuildState::Build()
     colValues.assign(nCols, DevArray<uint8_t>());
     colNulls.assign(nCols, DevArray<uint8_t>());
     colHasNull.assign(nCols, false);
+    colOffs.assign(nCols, DevArray<int64_t>());
     const int32_t keyCol = hashCols[0];
     const int32_t keyWidth = multiKey ? 8 : buildTypes.GetType(keyCol)->ByteWidth();
     table.keyWidth = keyWidth;
     // Gather every build column into one contiguous HBM array (reading host-pinned or
     // device batches directly).
     for (int c = 0; c < nCols; ++c) {
+        const bool varlen = Varlen(buildTypes.GetType(c));
         const int w = buildTypes.GetType(c)->ByteWidth();
-        if (w <= 0) {
+        if (w <= 0 && !varlen) {
             throw OmniException("UNSUPPORTED_ERROR", "unsupported build column type", -2);
         }
-        colValues[c].Reset(static_cast<size_t>(rows) * w + 16, s);
+        if (varlen) {
+            colOffs[c].Reset(static_cast<size_t>(rows) + 1, s, true);
+            colValues[c].Reset(16, s);
+        } else {
+            colValues[c].Reset(static_cast<size_t>(rows) * w + 16, s);
+        }
         if (rows == 0) {
             continue;
         }
@@ -126,6 +154,18 @@ void JoinBuildState::Build()
         if (bt.AnyNulls(0)) {
             colHasNull[c] = true;
             colNulls[c].Reset(omg::NullBitmapBytes(rows), s, true);
+        }
+        if (varlen) {
+            // Lengths, their scan, then the characters: one contiguous column with 64-bit offsets.
+            DevArray<uint32_t> lens(static_cast<size_t>(rows), s);
+            CudaCheck(omg::LaunchVarlenTileLens(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(),
+                          bt.DeviceTileOutRows(), 0, lens.Get(), s),
+                "build column lengths");
+            const int64_t bytes = ScanLengths(lens.Get(), rows, colOffs[c], s);
+            colValues[c].Reset(static_cast<size_t>(bytes) + 16, s);
+            CudaCheck(omg::LaunchVarlenTileCopy(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(),
+                          bt.DeviceTileOutRows(), 0, colOffs[c].Get(), colValues[c].Get(), s),
+                "build column characters");
         }
         CudaCheck(omg::LaunchGatherColumn(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(), bt.DeviceTileOutRows(),
                       0, w, colValues[c].Get(), colHasNull[c] ? colNulls[c].Get() : nullptr, s),
@@ -150,6 +190,7 @@ void JoinBuildState::Build()
             kc.widths[k] = buildTypes.GetType(c)->ByteWidth();
             kc.cols[k] = colValues[c].Get();
             kc.nulls[k] = colHasNull[c] ? colNulls[c].Get() : nullptr;
+            kc.offs[k] = colOffs[c].Get();
             anyNull = anyNull || colHasNull[c];
         }
         keyHash.Reset(static_cast<size_t>(rows), s);
@@ -309,7 +350,8 @@ HashBuilderOperatorFactory::HashBuilderOperatorFactory(JoinType joinType, BuildS
     state_->kind = kind;
     state_->buildTypes = buildTypes;
     state_->hashCols.assign(buildHashCols, buildHashCols + buildHashColsCount);
-    state_->multiKey = buildHashColsCount > 1 || buildTypes.GetType(buildHashCols[0])->ByteWidth() == 16;
+    state_->multiKey = buildHashColsCount > 1 || buildTypes.GetType(buildHashCols[0])->ByteWidth() == 16 ||
+        Varlen(buildTypes.GetType(buildHashCols[0]));
     state_->operatorCount = operatorCount;
 }
 
@@ -567,6 +609,7 @@ void LookupJoinOperator::ProcessPending()
             p.keyCols[k].input = static_cast<int16_t>(inputOf[f_.probeHashCols[k]]);
             p.keyCols[k].width = static_cast<int16_t>(f_.probeTypes.GetType(f_.probeHashCols[k])->ByteWidth());
             p.keyCols[k].buildValues = b.colValues[b.hashCols[k]].Get();
+            p.keyCols[k].buildOffs = b.colOffs[b.hashCols[k]].Get();
         }
     }
     p.table = b.table;
@@ -664,7 +707,9 @@ void LookupJoinOperator::ProcessPending()
     for (int attempt = 0; attempt < 2; ++attempt) {
         const uint64_t capacity = regionCap * static_cast<uint64_t>(nRegions);
         for (size_t o = 0; o < nOut; ++o) {
-            cols[o].values = omg::Buffer::NewDevice(capacity * cols[o].width + 16, s, false);
+            // VARCHAR columns hold an 8-byte row handle per output row until the second pass.
+            const size_t vw = cols[o].width == 0 ? 8 : static_cast<size_t>(cols[o].width);
+            cols[o].values = omg::Buffer::NewDevice(capacity * vw + 16, s, false);
             cols[o].nulls = cols[o].hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(capacity), s, true) : nullptr;
             p.out[o].values = cols[o].values->Data();
             p.out[o].nulls = cols[o].nulls ? static_cast<uint8_t *>(cols[o].nulls->Data()) : nullptr;
@@ -691,6 +736,37 @@ void LookupJoinOperator::ProcessPending()
         }
         regionCap = (most + 63) / 64 * 64;  // exact size known now: run once more
         ++counters_[1];
+    }
+    // VARCHAR outputs: row handles -> lengths -> offsets -> characters, over all regions at once
+    // (positions past a region's count contribute nothing).
+    for (size_t o = 0; o < nOut; ++o) {
+        if (cols[o].width != 0) {
+            continue;
+        }
+        const omg::JoinOutCol &oc = p.out[o];
+        const int64_t nPos = static_cast<int64_t>(regionCap) * nRegions;
+        const int64_t *handles = static_cast<const int64_t *>(cols[o].values->Data());
+        const int64_t *bOffs = oc.side == 1 ? b.colOffs[oc.src].Get() : nullptr;
+        const uint8_t *bChars = oc.side == 1 ? b.colValues[oc.src].Get() : nullptr;
+        DevArray<uint32_t> lens(static_cast<size_t>(nPos), s);
+        CudaCheck(omg::LaunchVarlenOutLens(handles, nPos, regionCap, count.Get(), oc.side, bt.DeviceBatches(), oc.src,
+                      bOffs, lens.Get(), s),
+            "output string lengths");
+        DevArray<int64_t> offs64;
+        const int64_t total = ScanLengths(lens.Get(), nPos, offs64, s);
+        if (total >= (int64_t(1) << 31)) {
+            throw OmniException("UNSUPPORTED_ERROR", "more than 2 GiB of VARCHAR output in one probe call", -2);
+        }
+        auto chars = omg::Buffer::NewDevice(static_cast<size_t>(total) + 16, s, false);
+        auto offs32 = omg::Buffer::NewDevice((static_cast<size_t>(nPos) + 1) * sizeof(int32_t), s, false);
+        CudaCheck(omg::LaunchVarlenOutCopy(handles, nPos, regionCap, count.Get(), oc.side, bt.DeviceBatches(), oc.src,
+                      bOffs, bChars, offs64.Get(), static_cast<uint8_t *>(chars->Data()),
+                      static_cast<int32_t *>(offs32->Data()), total, s),
+            "output strings");
+        impl_->stream.Sync();  // the scratch arrays above are freed on return
+        cols[o].values = chars;
+        cols[o].offsets = offs32;
+        cols[o].dataBytes = total;
     }
     int64_t rows = 0;
     for (int32_t r = 0; r < nRegions; ++r) {
@@ -1185,11 +1261,38 @@ void LookupOuterJoinOperator::Prepare()
         const auto &t = probe ? f_.probeOutputTypes.GetType(o) : f_.buildOutputTypes.GetType(o - nProbe);
         c.type = t->GetId();
         c.width = t->ByteWidth();
+        const bool varlen = Varlen(t);
         c.values = omg::Buffer::NewDevice(static_cast<size_t>(m) * c.width + 16, s, probe);
+        if (varlen) {
+            c.offsets = omg::Buffer::NewDevice((static_cast<size_t>(m) + 1) * sizeof(int32_t), s, true);
+        }
         if (probe) {
             c.hasNull = true;
             c.nulls = omg::Buffer::NewDevice(omg::NullBitmapBytes(m), s, false);
             CudaCheck(cudaMemsetAsync(c.nulls->Data(), 0xff, omg::NullBitmapBytes(m), s), "NULL probe columns");
+        } else if (varlen) {
+            const int32_t bc = f_.buildOutputCols[o - nProbe];
+            c.hasNull = b.colHasNull[bc];
+            c.nulls = c.hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(m), s, true) : nullptr;
+            DevArray<uint32_t> lens(static_cast<size_t>(m), s);
+            CudaCheck(omg::LaunchVarlenRowsLens(rows.Get(), m, b.colOffs[bc].Get(), lens.Get(), s), "string lengths");
+            DevArray<int64_t> offs64;
+            const int64_t total = ScanLengths(lens.Get(), m, offs64, s);
+            if (total >= (int64_t(1) << 31)) {
+                throw OmniException("UNSUPPORTED_ERROR", "more than 2 GiB of VARCHAR output in one batch set", -2);
+            }
+            c.values = omg::Buffer::NewDevice(static_cast<size_t>(total) + 16, s, false);
+            c.dataBytes = total;
+            CudaCheck(omg::LaunchVarlenRowsCopy(rows.Get(), m, b.colOffs[bc].Get(), b.colValues[bc].Get(),
+                          offs64.Get(), static_cast<uint8_t *>(c.values->Data()),
+                          static_cast<int32_t *>(c.offsets->Data()), total, s),
+                "gather unvisited build strings");
+            if (c.hasNull) {
+                CudaCheck(omg::LaunchGatherRows(b.colValues[bc].Get(), b.colNulls[bc].Get(), rows.Get(), m, 0,
+                              c.values->Data(), static_cast<uint8_t *>(c.nulls->Data()), s),
+                    "gather unvisited build NULLs");
+            }
+            impl_->stream.Sync();
         } else {
             const int32_t bc = f_.buildOutputCols[o - nProbe];
             c.hasNull = b.colHasNull[bc];

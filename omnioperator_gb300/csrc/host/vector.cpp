@@ -44,6 +44,32 @@ BaseVector::BaseVector(DataTypeId type, int32_t width, int32_t size, omg::Buffer
       valuesOffset_(valuesOffset), nulls_(std::move(nulls)), nullsOffset_(nullsOffset)
 {}
 
+BaseVector::BaseVector(DataTypeId type, int32_t size, int64_t dataBytes, bool device, void *stream)
+    : type_(type), width_(0), size_(size), dataBytes_(dataBytes)
+{
+    if (!IsVarlen() || dataBytes < 0) {
+        throw exception::OmniException("UNSUPPORTED_ERROR", "not a variable-length vector type", -2);
+    }
+    const size_t cb = static_cast<size_t>(dataBytes) + 16;
+    const size_t ob = (static_cast<size_t>(size) + 1) * sizeof(int32_t);
+    if (device) {
+        values_ = omg::Buffer::NewDevice(cb, stream, false);
+        offsets_ = omg::Buffer::NewDevice(ob, stream, true);
+        nulls_ = omg::Buffer::NewDevice(NullsBytes(size), stream, true);
+    } else {
+        values_ = omg::Buffer::NewHost(cb, false);
+        offsets_ = omg::Buffer::NewHost(ob, true);
+        nulls_ = omg::Buffer::NewHost(NullsBytes(size), true);
+    }
+}
+
+BaseVector::BaseVector(DataTypeId type, int32_t size, omg::BufferPtr chars, int64_t dataBytes, omg::BufferPtr offsets,
+    size_t offsetsOffset, omg::BufferPtr nulls, size_t nullsOffset, bool hasNull)
+    : type_(type), width_(0), size_(size), hasNull_(hasNull), values_(std::move(chars)), valuesOffset_(0),
+      nulls_(std::move(nulls)), nullsOffset_(nullsOffset), offsets_(std::move(offsets)),
+      offsetsOffset_(offsetsOffset), dataBytes_(dataBytes)
+{}
+
 bool BaseVector::HasNull()
 {
     if (hasNull_) {
@@ -107,10 +133,23 @@ VectorBatch *VectorHelper::CopyBatch(VectorBatch *batch, bool toDevice, void *st
     try {
         for (int32_t i = 0; i < batch->GetVectorCount(); ++i) {
             BaseVector *src = batch->Get(i);
-            auto *dst = new BaseVector(src->GetTypeId(), src->GetWidth(), src->GetSize(), toDevice, stream);
-            out->Append(dst);
-            const size_t vb = static_cast<size_t>(src->GetWidth()) * src->GetSize();
             cudaMemcpyKind kind = cudaMemcpyDefault;
+            BaseVector *dst;
+            size_t vb;
+            if (src->IsVarlen()) {
+                dst = new BaseVector(src->GetTypeId(), src->GetSize(), src->DataBytes(), toDevice, stream);
+                vb = static_cast<size_t>(src->DataBytes());
+                const size_t ob = (static_cast<size_t>(src->GetSize()) + 1) * sizeof(int32_t);
+                if (cudaMemcpyAsync(dst->RawOffsets(), src->RawOffsets(), ob, kind,
+                        static_cast<cudaStream_t>(stream)) != cudaSuccess) {
+                    delete dst;
+                    throw exception::OmniException("CUDA_ERROR", "batch copy failed", -3);
+                }
+            } else {
+                dst = new BaseVector(src->GetTypeId(), src->GetWidth(), src->GetSize(), toDevice, stream);
+                vb = static_cast<size_t>(src->GetWidth()) * src->GetSize();
+            }
+            out->Append(dst);
             if (vb > 0 && cudaMemcpyAsync(dst->RawValues(), src->RawValues(), vb, kind,
                               static_cast<cudaStream_t>(stream)) != cudaSuccess) {
                 throw exception::OmniException("CUDA_ERROR", "batch copy failed", -3);

@@ -1669,6 +1669,7 @@ __global__ void PartLayoutKernel(const __grid_constant__ PartArgs a)
         for (int i = 0; i < kMaxInputs; ++i) {
             d.cols[i] = nullptr;
             d.nulls[i] = nullptr;
+            d.offs[i] = nullptr;
         }
         for (int i = 0; i < a.nInputs; ++i) {
             d.cols[i] = static_cast<char *>(a.cols[i]) + offset[q] * a.width[i];

@@ -118,6 +118,22 @@ __device__ __forceinline__ uint64_t KeyTupleStep(uint64_t h, uint64_t v)
     return Mix64(h ^ (v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2)));
 }
 
+// A VARCHAR value in a key tuple hash: its length, then its bytes as little-endian 8-byte words
+// (the last zero-padded).
+__device__ __forceinline__ uint64_t KeyTupleBytes(uint64_t h, const uint8_t *p, int64_t len)
+{
+    h = KeyTupleStep(h, static_cast<uint64_t>(len));
+    for (int64_t i = 0; i < len; i += 8) {
+        uint64_t v = 0;
+        const int64_t m = len - i < 8 ? len - i : 8;
+        for (int64_t j = 0; j < m; ++j) {
+            v |= static_cast<uint64_t>(p[i + j]) << (8 * j);
+        }
+        h = KeyTupleStep(h, v);
+    }
+    return h;
+}
+
 // Order-preserving map of a non-NaN double onto int64 (-0.0 sorts just below +0.0).
 __device__ __forceinline__ int64_t OrderedFromDouble(double x)
 {

@@ -418,11 +418,25 @@ __device__ __forceinline__ void CopyValueRO(void *dst, uint64_t dpos, const void
 
 // Write one output row: probe columns from the probe batch (the key from registers), build
 // columns gathered by build row.
+// VARCHAR outputs get a handle to the source row (see JoinOutCol).
+__device__ __forceinline__ int64_t ProbeHandle(const ProbeLaunch &p, const BatchDesc &b, int64_t row)
+{
+    return (static_cast<int64_t>(&b - p.batches) << 32) | row;
+}
+
 __device__ __forceinline__ void WriteJoinRow(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t key,
     int64_t buildRow, uint64_t pos)
 {
     for (int o = 0; o < p.nOut; ++o) {
         const JoinOutCol &oc = p.out[o];
+        if (oc.width == 0) {
+            static_cast<int64_t *>(oc.values)[pos] = oc.side == 0 ? ProbeHandle(p, b, row) : buildRow;
+            if (oc.nulls != nullptr &&
+                RowIsNullRO(oc.side == 0 ? b.nulls[oc.src] : oc.buildNulls, oc.side == 0 ? row : buildRow)) {
+                SetBit(oc.nulls, pos);
+            }
+            continue;
+        }
         if (oc.side == 0) {
             if (oc.src == p.keyInput) {
                 StoreKey(oc.values, pos, oc.width, key);
@@ -447,6 +461,13 @@ __device__ __forceinline__ void WriteJoinRowPayload(const ProbeLaunch &p, const 
 {
     for (int o = 0; o < p.nOut; ++o) {
         const JoinOutCol &oc = p.out[o];
+        if (oc.width == 0) {  // a probe VARCHAR column (build ones have no slot payload)
+            static_cast<int64_t *>(oc.values)[pos] = ProbeHandle(p, b, row);
+            if (oc.nulls != nullptr && RowIsNullRO(b.nulls[oc.src], row)) {
+                SetBit(oc.nulls, pos);
+            }
+            continue;
+        }
         if (oc.side == 0) {
             if (oc.src == p.keyInput) {
                 StoreKey(oc.values, pos, oc.width, key);
@@ -491,6 +512,13 @@ __device__ __forceinline__ void WriteProbeOnlyRow(const ProbeLaunch &p, const Ba
 {
     for (int o = 0; o < p.nOut; ++o) {
         const JoinOutCol &oc = p.out[o];
+        if (oc.width == 0) {
+            static_cast<int64_t *>(oc.values)[pos] = oc.side == 0 ? ProbeHandle(p, b, row) : -1;
+            if (oc.side != 0 || RowIsNullRO(b.nulls[oc.src], row)) {
+                SetBit(oc.nulls, pos);
+            }
+            continue;
+        }
         if (oc.side == 0) {
             // Unlike a matched row, this one may carry a NULL probe key (outer and anti joins).
             if (oc.src == p.keyInput) {
@@ -726,7 +754,10 @@ __device__ __forceinline__ bool ProbeTupleHash(const ProbeLaunch &p, const Batch
         if (RowIsNullRO(b.nulls[kc.input], row)) {
             return false;
         }
-        if (kc.width == 16) {
+        if (kc.width == 0) {
+            const int32_t *offs = b.offs[kc.input];
+            h = KeyTupleBytes(h, static_cast<const uint8_t *>(b.cols[kc.input]) + offs[row], offs[row + 1] - offs[row]);
+        } else if (kc.width == 16) {
             const longlong2 v = __ldg(static_cast<const longlong2 *>(b.cols[kc.input]) + row);
             h = KeyTupleStep(KeyTupleStep(h, static_cast<uint64_t>(v.x)), static_cast<uint64_t>(v.y));
         } else {
@@ -741,7 +772,21 @@ __device__ __forceinline__ bool TupleEquals(const ProbeLaunch &p, const BatchDes
 {
     for (int k = 0; k < p.nKeyCols; ++k) {
         const JoinKeyCol &kc = p.keyCols[k];
-        if (kc.width == 16) {
+        if (kc.width == 0) {
+            const int32_t *offs = b.offs[kc.input];
+            const int64_t len = offs[row + 1] - offs[row];
+            const int64_t b0 = kc.buildOffs[br];
+            if (kc.buildOffs[br + 1] - b0 != len) {
+                return false;
+            }
+            const uint8_t *x = static_cast<const uint8_t *>(b.cols[kc.input]) + offs[row];
+            const uint8_t *y = static_cast<const uint8_t *>(kc.buildValues) + b0;
+            for (int64_t i = 0; i < len; ++i) {
+                if (x[i] != y[i]) {
+                    return false;
+                }
+            }
+        } else if (kc.width == 16) {
             const longlong2 x = __ldg(static_cast<const longlong2 *>(b.cols[kc.input]) + row);
             const longlong2 y = __ldg(static_cast<const longlong2 *>(kc.buildValues) + br);
             if (x.x != y.x || x.y != y.y) {
@@ -875,6 +920,9 @@ __global__ void JoinKeyHashKernel(const JoinKeyCols kc, int64_t n, uint64_t *out
         for (int k = 0; k < kc.nKeys; ++k) {
             if (RowIsNull(kc.nulls[k], i)) {
                 isNull = true;
+            } else if (kc.widths[k] == 0) {
+                const int64_t o = kc.offs[k][i];
+                h = KeyTupleBytes(h, static_cast<const uint8_t *>(kc.cols[k]) + o, kc.offs[k][i + 1] - o);
             } else if (kc.widths[k] == 16) {
                 const uint64_t *v = static_cast<const uint64_t *>(kc.cols[k]) + 2 * i;
                 h = KeyTupleStep(KeyTupleStep(h, v[0]), v[1]);

@@ -73,6 +73,26 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream);
 // One output column of AlignSchema (adaptive partial aggregation) for every input row.
 cudaError_t LaunchAlignColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
     const int64_t *tileOutRow, const AlignCol &c, void *out, uint8_t *outNulls, cudaStream_t stream);
+// VARCHAR columns: lengths / characters of a batch input in tile output order; output columns
+// from per-row handles over regions (see JoinOutCol); rows of a contiguous column.  Offsets
+// passed in are exclusive scans of the lengths (LaunchScanCounts) with the total at [n]
+// (LaunchOffsetsTail).
+cudaError_t LaunchVarlenTileLens(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, int32_t input, uint32_t *lens, cudaStream_t stream);
+cudaError_t LaunchVarlenTileCopy(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
+    const int64_t *tileOutRow, int32_t input, const int64_t *dstOffs, uint8_t *dst, cudaStream_t stream);
+cudaError_t LaunchVarlenOutLens(const int64_t *handles, int64_t nPos, uint64_t regionCap,
+    const unsigned long long *regionCounts, int side, const BatchDesc *batches, int32_t input,
+    const int64_t *buildOffs, uint32_t *lens, cudaStream_t stream);
+cudaError_t LaunchVarlenOutCopy(const int64_t *handles, int64_t nPos, uint64_t regionCap,
+    const unsigned long long *regionCounts, int side, const BatchDesc *batches, int32_t input,
+    const int64_t *buildOffs, const uint8_t *buildChars, const int64_t *offs64, uint8_t *chars, int32_t *offs32,
+    long long total, cudaStream_t stream);
+cudaError_t LaunchVarlenRowsLens(const int32_t *rows, int64_t n, const int64_t *srcOffs, uint32_t *lens,
+    cudaStream_t stream);
+cudaError_t LaunchVarlenRowsCopy(const int32_t *rows, int64_t n, const int64_t *srcOffs, const uint8_t *srcChars,
+    const int64_t *offs64, uint8_t *chars, int32_t *offs32, long long total, cudaStream_t stream);
+cudaError_t LaunchOffsetsTail(int64_t *offs, int64_t n, const long long *total, cudaStream_t stream);
 // Multi-column join keys: the tuple hash of each build row (NULL if a key column is NULL).
 cudaError_t LaunchJoinKeyHash(const JoinKeyCols &kc, int64_t n, uint64_t *out, uint8_t *outNulls, cudaStream_t stream);
 // Outer joins: flags[i] = 1 for build rows never matched; their row numbers in order (offsets =

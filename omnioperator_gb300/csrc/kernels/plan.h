@@ -19,8 +19,9 @@ constexpr int kTileRows = 4096;  // rows per tile
 // bitmap (LSB-first, set bit = NULL) of kernel input i; nulls[i] == nullptr means the
 // column has no nulls in this batch.
 struct BatchDesc {
-    const void *cols[kMaxInputs];
+    const void *cols[kMaxInputs];       // values (VARCHAR/CHAR: the character buffer)
     const uint8_t *nulls[kMaxInputs];
+    const int32_t *offs[kMaxInputs];    // VARCHAR/CHAR: n + 1 offsets into cols[i]; else nullptr
     int64_t rows;
     int64_t rowBase;  // index of the batch's first row in arrival order
 };
@@ -308,7 +309,9 @@ enum JoinKind : int32_t {
 struct JoinOutCol {
     int16_t side;    // 0 = probe column, 1 = build column, 2 = existence flag (1 byte)
     int16_t src;     // probe kernel input index / build column index
-    int16_t width;   // bytes
+    int16_t width;   // bytes; 0 = VARCHAR: the probe writes an 8-byte row handle per output row
+                     // (probe: batch << 32 | row, build: build row, -1: NULL) that a second
+                     // pass turns into offsets and characters
     int16_t shift;   // side 1 with a slot payload: bit offset of the value in the packed payload
     const void *buildValues;     // side 1: contiguous build column in HBM
     const uint8_t *buildNulls;   // side 1: contiguous build null bitmap (nullptr = no nulls)
@@ -322,17 +325,19 @@ constexpr int kMaxJoinKeys = 4;
 
 struct JoinKeyCol {
     int16_t input;             // probe kernel input index
-    int16_t width;             // bytes (1, 2, 4, 8 or 16); build and probe widths are equal
+    int16_t width;             // bytes (1, 2, 4, 8 or 16), 0 = VARCHAR; equal on both sides
     int32_t pad;
-    const void *buildValues;   // contiguous build key column in HBM
+    const void *buildValues;   // contiguous build key column in HBM (VARCHAR: characters)
+    const int64_t *buildOffs;  // VARCHAR: rows + 1 offsets into buildValues
 };
 
 // Key columns of one side, for hashing (build: contiguous columns).
 struct JoinKeyCols {
     int32_t nKeys;
-    int32_t widths[kMaxJoinKeys];
+    int32_t widths[kMaxJoinKeys];       // 0 = VARCHAR
     const void *cols[kMaxJoinKeys];
     const uint8_t *nulls[kMaxJoinKeys];
+    const int64_t *offs[kMaxJoinKeys];  // VARCHAR offsets
 };
 
 constexpr int kRegionStride = 16;  // counters 128 bytes apart

@@ -2,6 +2,8 @@
 //
 // Layout follows the reference (vector/vector.h:45-404, vector/nulls_buffer.h:16-114):
 //  - flat values, one fixed-width element per row;
+//  - VARCHAR / CHAR: n + 1 int32 offsets into a character buffer (value i is bytes
+//    [offsets[i], offsets[i + 1])), the LargeStringContainer layout of vector/vector.h;
 //  - a null bitmap, LSB-first, bit set = NULL, of NullsBuffer::CalculateNbytes(n) =
 //    ceil(n/8) + 8 bytes (the 8 spare bytes let 64-bit word loads run past the end).
 // Both live in one Buffer each, host-pinned or in HBM (Residency).  A vector may be a
@@ -35,7 +37,24 @@ public:
     // `nullsOffset`; nulls may be null).
     BaseVector(DataTypeId type, int32_t width, int32_t size, omg::BufferPtr values, size_t valuesOffset,
         omg::BufferPtr nulls, size_t nullsOffset, bool hasNull);
+    // New owned VARCHAR/CHAR vector with `dataBytes` bytes of character storage; offsets and
+    // nulls zeroed.
+    BaseVector(DataTypeId type, int32_t size, int64_t dataBytes, bool device, void *stream = nullptr);
+    // VARCHAR/CHAR view: offsets at byte offset `offsetsOffset` of `offsets` (absolute positions
+    // in `chars`).
+    BaseVector(DataTypeId type, int32_t size, omg::BufferPtr chars, int64_t dataBytes, omg::BufferPtr offsets,
+        size_t offsetsOffset, omg::BufferPtr nulls, size_t nullsOffset, bool hasNull);
     virtual ~BaseVector() = default;
+
+    bool IsVarlen() const { return type_ == OMNI_VARCHAR || type_ == OMNI_CHAR; }
+    // VARCHAR/CHAR: n + 1 offsets (nullptr for fixed-width vectors) and the character buffer's size.
+    int32_t *RawOffsets() const
+    {
+        return offsets_ ? reinterpret_cast<int32_t *>(static_cast<uint8_t *>(offsets_->Data()) + offsetsOffset_)
+                        : nullptr;
+    }
+    int64_t DataBytes() const { return dataBytes_; }
+    const omg::BufferPtr &OffsetsBuffer() const { return offsets_; }
 
     int32_t GetSize() const { return size_; }
     DataTypeId GetTypeId() const { return type_; }
@@ -83,6 +102,9 @@ protected:
     size_t valuesOffset_ = 0;
     omg::BufferPtr nulls_;
     size_t nullsOffset_ = 0;
+    omg::BufferPtr offsets_;  // VARCHAR/CHAR only
+    size_t offsetsOffset_ = 0;
+    int64_t dataBytes_ = 0;
 };
 
 // Typed host accessor (vector/vector.h Vector<T>::GetValue/SetValue).
