@@ -1,5 +1,6 @@
 // Host-side launch helpers (see gpu_runtime.h).
 #include "host/gpu_runtime.h"
+#include "kernels/launch.h"
 
 #include <algorithm>
 #include <atomic>
@@ -131,6 +132,16 @@ long long WaitBudget()
 }
 void SetWaitBudget(long long ticks) { g_waitBudget.store(ticks); }
 
+namespace {
+std::atomic<int64_t> g_aggFlushRows{0};
+}
+int64_t AggFlushRows()
+{
+    const int64_t r = g_aggFlushRows.load();
+    return r > 0 ? r : (int64_t(1) << 28);
+}
+void SetAggFlushRows(int64_t rows) { g_aggFlushRows.store(rows); }
+
 std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows, int32_t rowsPerBatch,
     int64_t firstRow)
 {
@@ -208,6 +219,22 @@ std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int
         host.push_back(h);
     }
     return host;
+}
+
+// A VARCHAR column from per-row lengths: exclusive offsets (n + 1, 64-bit) and the total.
+int64_t ScanLengths(const uint32_t *lens, int64_t n, DevArray<int64_t> &offs, cudaStream_t s)
+{
+    offs.Reset(static_cast<size_t>(n) + 1, s);
+    DevArray<int64_t> blockSums(static_cast<size_t>((n + 1023) / 1024 + 1), s);
+    DevArray<long long> total(1, s, true);
+    if (n > 0) {
+        CudaCheck(LaunchScanCounts(lens, n, offs.Get(), blockSums.Get(), total.Get(), s), "scan lengths");
+    }
+    CudaCheck(LaunchOffsetsTail(offs.Get(), n, total.Get(), s), "offsets tail");
+    long long h = 0;
+    CudaCheck(cudaMemcpyAsync(&h, total.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read total length");
+    CudaCheck(cudaStreamSynchronize(s), "read total length");
+    return h;
 }
 
 }  // namespace omg

@@ -157,8 +157,17 @@ class BatchTable {
 public:
     void Build(const std::vector<omniruntime::vec::VectorBatch *> &batches, const std::vector<int32_t> &inputCols,
         int32_t tileRows = kTileRows);
-    // Copy descriptors to the device on `s`.
+    // Copy descriptors to the device on `s` (again after SetInput).
     void Upload(cudaStream_t s);
+    // Point input `input` of batch `batch` at other fixed-width values (e.g. dictionary ids of
+    // a VARCHAR column; the NULL bitmap stays the column's own).
+    void SetInput(size_t batch, int32_t input, const void *values)
+    {
+        descs_[batch].cols[input] = values;
+        descs_[batch].offs[input] = nullptr;
+    }
+    int64_t BatchRowBase(size_t batch) { return descs_[batch].rowBase; }
+    size_t NumBatches() const { return descs_.Size(); }
     const BatchDesc *DeviceBatches() const { return dBatches_.Get(); }
     const TileDesc *DeviceTiles() const { return dTiles_.Get(); }
     const int64_t *DeviceTileOutRows() const { return dTileOut_.Get(); }
@@ -188,9 +197,16 @@ inline int32_t AlignedBatchRows(int32_t maxRows)
 
 size_t NullBitmapBytes(int64_t rows);
 
+// A VARCHAR column from per-row lengths: exclusive offsets (n + 1, 64-bit, the total last) and
+// the total, read back to the host (synchronises `s`).
+int64_t ScanLengths(const uint32_t *lens, int64_t n, DevArray<int64_t> &offs, cudaStream_t s);
+
 // Budget of device-side bounded waits (clock64 ticks); 0 restores the default.
 long long WaitBudget();
 void SetWaitBudget(long long ticks);
+// Staged rows at which an aggregation operator flushes its queued batches; 0 restores 2^28.
+int64_t AggFlushRows();
+void SetAggFlushRows(int64_t rows);
 
 // Cut `rows` rows of contiguous output columns into VectorBatches of at most
 // `rowsPerBatch` rows that are views of the given buffers (host or device).

@@ -84,6 +84,17 @@ int64_t OrderedBits(double x)
     return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
 }
 
+bool IsVarlen(DataTypeId id) { return id == OMNI_VARCHAR || id == OMNI_CHAR; }
+
+// Bytes a VARCHAR/CHAR value counts for in the output batch size rule: the declared width, or
+// 200 when none is declared (operator_util.h:72-82).
+int VarlenRowBytes(const DataTypePtr &t)
+{
+    const int32_t w = t->GetWidth();
+    const int32_t unset = t->GetId() == OMNI_CHAR ? 65536 : INT_MAX;
+    return w > 0 && w < unset ? w : 200;
+}
+
 uint64_t NextPow2(uint64_t v)
 {
     uint64_t p = 1;
@@ -95,7 +106,6 @@ uint64_t NextPow2(uint64_t v)
 
 constexpr uint64_t kDefaultCapacity = uint64_t(1) << 16;
 constexpr int kGlobalMaxProbe = 96;
-constexpr int64_t kFlushRows = int64_t(1) << 28;     // aggregate at most 256M staged rows per launch
 constexpr size_t kSmemBudget = 96 * 1024;            // shared bytes per CTA for pre-aggregation
 
 }  // namespace
@@ -160,14 +170,22 @@ OmniStatus HashAggregationOperatorFactory::Init()
     int rowBytes = 0;
     for (int i = 0; i < nKey; ++i) {
         const auto &t = groupTypes_.GetType(i);
-        const int w = t->ByteWidth();
+        // A VARCHAR/CHAR key is aggregated as the int32 id of its string in the operator's
+        // string dictionary (the reference serialises the bytes into the key instead,
+        // vector_marshaller.cpp:155-232); the strings come back at output time.
+        const bool varlen = IsVarlen(t->GetId());
+        const int w = varlen ? 4 : t->ByteWidth();
         if (w == 0 || (w > 8 && w != 16)) {
             throw OmniException("UNSUPPORTED_ERROR", "unsupported group-by type " + std::to_string(t->GetId()), -2);
         }
-        p.key.cols[i].input = static_cast<int16_t>(inputFor(groupByCols_[i], w));
+        const int32_t input = inputFor(groupByCols_[i], w);
+        if (varlen && std::find(p.dictInputs.begin(), p.dictInputs.end(), input) == p.dictInputs.end()) {
+            p.dictInputs.push_back(input);
+        }
+        p.key.cols[i].input = static_cast<int16_t>(input);
         p.key.cols[i].width = static_cast<int16_t>(w);
         p.outTypes.push_back(t);
-        rowBytes += w;
+        rowBytes += varlen ? VarlenRowBytes(t) : w;
     }
     if (nKey == 1 && p.key.cols[0].width <= 8) {
         p.key.kind = omg::KEY_SINGLE;
@@ -458,12 +476,18 @@ OmniStatus HashAggregationOperatorFactory::Init()
             }
         }
     }
+    // Inputs without a fixed width are VARCHAR/CHAR columns that only COUNT reads (for NULLs).
+    for (size_t i = 0; i < p.inputWidths.size(); ++i) {
+        if (p.inputWidths[i] == 0) {
+            p.varlenInputs.push_back(static_cast<int32_t>(i));
+        }
+    }
     p.stateWords = word;
     p.slotWords = p.keyWords + p.stateWords;
     p.smemSlots = static_cast<int32_t>(kSmemBudget / (p.slotWords * sizeof(uint64_t)));
     p.rowsPerBatch = GetMaxRowCount(rowBytes);
     // AlignSchema columns: each output of a raw-input partial plan restated for one row.
-    bool alignable = nAgg > 0;
+    bool alignable = nAgg > 0 && p.dictInputs.empty() && p.varlenInputs.empty();
     for (size_t a = 0; a < nAgg; ++a) {
         const bool raw = a < inputRaws_.size() ? static_cast<bool>(inputRaws_[a]) : true;
         const bool partial = a < outputPartials_.size() ? static_cast<bool>(outputPartials_[a]) : false;
@@ -521,6 +545,23 @@ Operator *HashAggregationOperatorFactory::CreateOperator()
 }
 
 // ------------------------------------------------------------------------------ operator
+namespace {
+// String dictionary of one VARCHAR/CHAR group-by input (kernels/dict.cu): open-addressing
+// slots (string hash, id, representative row of the batch set being inserted) and the
+// characters of every id, in id order, in an arena with 64-bit offsets.  Ids are dense and
+// never change, so the aggregation table keyed by ids stays valid across flushes.
+struct StringDict {
+    DevArray<unsigned long long> hash;
+    DevArray<int32_t> id;
+    DevArray<unsigned long long> rep;
+    uint64_t cap = 0;
+    int64_t nIds = 0;
+    DevArray<int64_t> arenaOff;  // nIds + 1 entries used
+    DevArray<uint8_t> arena;     // arenaBytes used
+    int64_t arenaBytes = 0;
+};
+}  // namespace
+
 struct HashAggregationOperator::Impl {
     omg::OpStream stream;
     omg::KernelTimer timer;
@@ -541,6 +582,12 @@ struct HashAggregationOperator::Impl {
     uint64_t plainEstimate = 0;
     bool learned = false;
     int32_t partBits = -1;
+    // VARCHAR/CHAR group-by inputs: one dictionary per plan dictInputs entry.  For
+    // order-dependent plans the id (and zero) columns of the retained batches stay alive
+    // (retainedInputs[b]: the columns of retained batch b for dictInputs, then varlenInputs).
+    std::vector<StringDict> dicts;
+    std::vector<DevArray<int32_t>> keptIds;
+    std::vector<std::vector<const void *>> retainedInputs;
 };
 
 HashAggregationOperator::HashAggregationOperator(const AggPlan &plan, omg::SizingModel *sizer)
@@ -597,7 +644,7 @@ int32_t HashAggregationOperator::AddInput(VectorBatch *vecBatch)
     }
     pending_.push_back(vecBatch);
     pendingRows_ += vecBatch->GetRowCount();
-    if (pendingRows_ >= kFlushRows) {
+    if (pendingRows_ >= omg::AggFlushRows()) {
         Flush();
     }
     return 0;
@@ -850,6 +897,126 @@ void HashAggregationOperator::Partition(omg::BatchTable &bt, omg::AggLaunch &p, 
     p.partTileStart = pb.tileStart.Get();
 }
 
+namespace {
+// Grow a device array to at least `need` elements (doubling), keeping its first `used`.
+template <typename T> void GrowKeep(DevArray<T> &a, size_t used, size_t need, cudaStream_t s)
+{
+    if (a.Get() != nullptr && a.Size() >= need) {
+        return;
+    }
+    DevArray<T> b(std::max<size_t>(need, 2 * a.Size()), s);
+    if (used > 0) {
+        CudaCheck(cudaMemcpyAsync(b.Get(), a.Get(), used * sizeof(T), cudaMemcpyDeviceToDevice, s), "grow array");
+    }
+    a = b;
+}
+
+// Insert the strings of input `input` of every row of `bt` into `d` and return each row's id
+// (tile output order; 0 for NULL rows, whose key stays NULL through the column's bitmap).
+DevArray<int32_t> DictEncode(StringDict &d, omg::BatchTable &bt, int32_t input, cudaStream_t s)
+{
+    const int64_t rows = bt.TotalRows();
+    DevArray<int32_t> err(1, s, true);
+    // At most half full after this batch set, even if every row brings a new string.
+    const uint64_t need = NextPow2(std::max<uint64_t>(1024, 2 * static_cast<uint64_t>(d.nIds + rows)));
+    if (need > d.cap) {
+        DevArray<unsigned long long> hash(need, s);
+        DevArray<int32_t> id(need, s);
+        CudaCheck(cudaMemsetAsync(hash.Get(), 0xff, need * sizeof(unsigned long long), s), "init dictionary");
+        CudaCheck(cudaMemsetAsync(id.Get(), 0xff, need * sizeof(int32_t), s), "init dictionary");
+        if (d.cap > 0) {
+            CudaCheck(omg::LaunchDictRehash(d.hash.Get(), d.id.Get(), d.cap, hash.Get(), id.Get(), need, err.Get(), s),
+                "grow dictionary");
+        }
+        d.hash = hash;
+        d.id = id;
+        d.rep.Reset(need, s);
+        d.cap = need;
+    }
+    if (d.arenaOff.Get() == nullptr) {
+        d.arenaOff.Reset(1024, s, true);
+        d.arena.Reset(4096, s);
+    }
+    CudaCheck(cudaMemsetAsync(d.rep.Get(), 0xff, d.cap * sizeof(unsigned long long), s), "reset dictionary");
+    DevArray<int32_t> rowSlot(static_cast<size_t>(rows), s);
+    CudaCheck(omg::LaunchDictInsert(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(), bt.DeviceTileOutRows(), input,
+                  d.hash.Get(), d.id.Get(), d.rep.Get(), d.cap, d.arenaOff.Get(), d.arena.Get(), rowSlot.Get(),
+                  err.Get(), s),
+        "dictionary insert");
+    const size_t maxNew = static_cast<size_t>(std::min<uint64_t>(static_cast<uint64_t>(rows), d.cap));
+    DevArray<unsigned int> counter(1, s, true);
+    DevArray<unsigned long long> newRep(maxNew, s);
+    DevArray<uint32_t> newLen(maxNew, s);
+    CudaCheck(omg::LaunchDictMaterialize(d.hash.Get(), d.id.Get(), d.rep.Get(), d.cap, static_cast<int32_t>(d.nIds),
+                  counter.Get(), newRep.Get(), newLen.Get(), bt.DeviceBatches(), input, s),
+        "dictionary ids");
+    unsigned int h[2] = {0, 0};
+    CudaCheck(cudaMemcpyAsync(h, counter.Get(), sizeof(unsigned int), cudaMemcpyDeviceToHost, s), "read new ids");
+    CudaCheck(cudaMemcpyAsync(h + 1, err.Get(), sizeof(int32_t), cudaMemcpyDeviceToHost, s), "read new ids");
+    CudaCheck(cudaStreamSynchronize(s), "read new ids");
+    if (h[1] != 0) {
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "string dictionary overflow", -9);
+    }
+    const int64_t nNew = h[0];
+    if (d.nIds + nNew >= (int64_t(1) << 31)) {
+        throw OmniException("UNSUPPORTED_ERROR", "more than 2^31 distinct strings in one group-by column", -2);
+    }
+    if (nNew > 0) {
+        DevArray<int64_t> offs;
+        const int64_t bytes = omg::ScanLengths(newLen.Get(), nNew, offs, s);
+        GrowKeep(d.arenaOff, static_cast<size_t>(d.nIds + 1), static_cast<size_t>(d.nIds + nNew + 1), s);
+        CudaCheck(omg::LaunchDictShiftOffsets(offs.Get(), nNew, d.arenaBytes, d.arenaOff.Get() + d.nIds, s),
+            "dictionary offsets");
+        GrowKeep(d.arena, static_cast<size_t>(d.arenaBytes), static_cast<size_t>(d.arenaBytes + bytes + 16), s);
+        CudaCheck(omg::LaunchDictAppend(newRep.Get(), nNew, static_cast<int32_t>(d.nIds), d.arenaOff.Get(),
+                      d.arena.Get(), bt.DeviceBatches(), input, s),
+            "dictionary characters");
+        d.nIds += nNew;
+        d.arenaBytes += bytes;
+    }
+    DevArray<int32_t> ids(static_cast<size_t>(rows), s);
+    CudaCheck(omg::LaunchDictRowIds(rowSlot.Get(), rows, d.id.Get(), ids.Get(), s), "row ids");
+    return ids;
+}
+}  // namespace
+
+// VARCHAR/CHAR inputs of a batch set: group-by columns become dictionary ids, COUNT-only
+// columns a zero byte per row (their NULL bitmaps stay the batches' own); the batch
+// descriptors are uploaded again.
+void HashAggregationOperator::EncodeStrings(omg::BatchTable &bt, cudaStream_t s)
+{
+    Impl &im = *impl_;
+    const size_t nb = bt.NumBatches();
+    std::vector<std::vector<const void *>> perBatch(nb);
+    im.dicts.resize(plan_.dictInputs.size());
+    for (size_t j = 0; j < plan_.dictInputs.size(); ++j) {
+        DevArray<int32_t> ids = DictEncode(im.dicts[j], bt, plan_.dictInputs[j], s);
+        for (size_t b = 0; b < nb; ++b) {
+            const int32_t *p = ids.Get() + bt.BatchRowBase(b);
+            bt.SetInput(b, plan_.dictInputs[j], p);
+            perBatch[b].push_back(p);
+        }
+        im.keptIds.push_back(ids);
+    }
+    if (!plan_.varlenInputs.empty()) {
+        DevArray<int32_t> zeros(static_cast<size_t>(bt.TotalRows() + 16) / 4 + 1, s, true);
+        for (size_t b = 0; b < nb; ++b) {
+            const uint8_t *p = reinterpret_cast<const uint8_t *>(zeros.Get()) + bt.BatchRowBase(b);
+            for (int32_t in : plan_.varlenInputs) {
+                bt.SetInput(b, in, p);
+                perBatch[b].push_back(p);
+            }
+        }
+        im.keptIds.push_back(zeros);
+    }
+    bt.Upload(s);
+    if (plan_.orderDependent) {
+        for (auto &v : perBatch) {
+            im.retainedInputs.push_back(v);
+        }
+    }
+}
+
 void HashAggregationOperator::Flush()
 {
     if (pending_.empty()) {
@@ -868,6 +1035,9 @@ void HashAggregationOperator::Flush()
     bt.Build(pending_, plan_.inputCols);
     bt.Upload(s);
     const int64_t rows = bt.TotalRows();
+    if (!plan_.dictInputs.empty() || !plan_.varlenInputs.empty()) {
+        EncodeStrings(bt, s);
+    }
     if (!im.decided) {
         Decide(bt, s);
     }
@@ -989,6 +1159,9 @@ void HashAggregationOperator::Flush()
         im.stream.Sync();
     }
     counters_[3] = static_cast<int64_t>(im.groups);
+    if (!plan_.orderDependent) {
+        im.keptIds.clear();  // freed stream-ordered, after the kernels that read them
+    }
     if (plan_.orderDependent) {
         for (auto *b : pending_) {
             im.retained.push_back(b);
@@ -997,6 +1170,43 @@ void HashAggregationOperator::Flush()
         pendingRows_ = 0;
     } else {
         ReleasePending();
+    }
+}
+
+// VARCHAR/CHAR key columns of the extracted groups: dictionary ids back to strings (lengths,
+// a scan to offsets, then the characters), on the device.
+void HashAggregationOperator::DecodeStrings(std::vector<omg::OutColumn> &cols, int64_t rows, cudaStream_t s)
+{
+    Impl &im = *impl_;
+    for (size_t o = 0; o < plan_.outs.size(); ++o) {
+        const OutSpec &os = plan_.outs[o];
+        if (os.kind != omg::OUT_KEY || !IsVarlen(plan_.outTypes[o]->GetId())) {
+            continue;
+        }
+        const int32_t input = plan_.key.cols[os.src].input;
+        const size_t j = static_cast<size_t>(
+            std::find(plan_.dictInputs.begin(), plan_.dictInputs.end(), input) - plan_.dictInputs.begin());
+        StringDict &d = im.dicts.at(j);
+        omg::OutColumn &c = cols[o];
+        const int32_t *ids = static_cast<const int32_t *>(c.values->Data());
+        const uint8_t *nulls = static_cast<const uint8_t *>(c.nulls->Data());
+        DevArray<uint32_t> lens(static_cast<size_t>(rows), s);
+        CudaCheck(omg::LaunchDictDecodeLens(ids, nulls, rows, d.arenaOff.Get(), lens.Get(), s), "key string lengths");
+        DevArray<int64_t> offs64;
+        const int64_t total = omg::ScanLengths(lens.Get(), rows, offs64, s);
+        if (total >= (int64_t(1) << 31)) {
+            throw OmniException("UNSUPPORTED_ERROR", "more than 2 GiB of VARCHAR group-by keys in the output", -2);
+        }
+        omg::BufferPtr chars = omg::Buffer::NewDevice(static_cast<size_t>(total) + 16, s, false);
+        omg::BufferPtr offs32 = omg::Buffer::NewDevice((static_cast<size_t>(rows) + 1) * sizeof(int32_t), s, false);
+        CudaCheck(omg::LaunchDictDecodeCopy(ids, nulls, rows, d.arenaOff.Get(), d.arena.Get(), offs64.Get(),
+                      static_cast<uint8_t *>(chars->Data()), static_cast<int32_t *>(offs32->Data()), total, s),
+            "key strings");
+        ++counters_[0];
+        c.width = 0;
+        c.values = chars;
+        c.offsets = offs32;
+        c.dataBytes = total;
     }
 }
 
@@ -1071,6 +1281,14 @@ void HashAggregationOperator::Extract()
         counters_[4] = static_cast<int64_t>(hc[2]);
         omg::BatchTable bt;
         bt.Build(im.retained, plan_.inputCols, 1 << 30);
+        // VARCHAR inputs read through the id / zero columns their flush made (same order).
+        const size_t nDict = plan_.dictInputs.size();
+        for (size_t b = 0; b < im.retainedInputs.size() && b < bt.NumBatches(); ++b) {
+            for (size_t j = 0; j < im.retainedInputs[b].size(); ++j) {
+                const int32_t in = j < nDict ? plan_.dictInputs[j] : plan_.varlenInputs[j - nDict];
+                bt.SetInput(b, in, im.retainedInputs[b][j]);
+            }
+        }
         bt.Upload(s);
         DevArray<uint8_t> forced(im.capacity + 2, s, true);
         omg::AggLaunch p = base;
@@ -1092,6 +1310,9 @@ void HashAggregationOperator::Extract()
         throw OmniException("OPERATOR_RUNTIME_ERROR", "sum_aggregator overflow.", -5);
     }
     const int64_t rows = static_cast<int64_t>(hc[0]);
+    if (!plan_.dictInputs.empty()) {
+        DecodeStrings(cols, rows, s);
+    }
     std::vector<omg::OutColumn> outCols = cols;
     if (!deviceOutput_) {
         outCols = omg::CopyColumnsToHost(cols, rows, s);

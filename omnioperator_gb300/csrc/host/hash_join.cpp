@@ -52,21 +52,6 @@ bool JoinKeyType(DataTypeId id)
 
 bool Varlen(const DataTypePtr &t) { return t->GetId() == OMNI_VARCHAR || t->GetId() == OMNI_CHAR; }
 
-// A VARCHAR column from per-row lengths: exclusive offsets (n + 1, 64-bit) and the total.
-int64_t ScanLengths(const uint32_t *lens, int64_t n, DevArray<int64_t> &offs, cudaStream_t s)
-{
-    offs.Reset(static_cast<size_t>(n) + 1, s);
-    DevArray<int64_t> blockSums(static_cast<size_t>((n + 1023) / 1024 + 1), s);
-    DevArray<long long> total(1, s, true);
-    if (n > 0) {
-        CudaCheck(omg::LaunchScanCounts(lens, n, offs.Get(), blockSums.Get(), total.Get(), s), "scan lengths");
-    }
-    CudaCheck(omg::LaunchOffsetsTail(offs.Get(), n, total.Get(), s), "offsets tail");
-    long long h = 0;
-    CudaCheck(cudaMemcpyAsync(&h, total.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read total length");
-    CudaCheck(cudaStreamSynchronize(s), "read total length");
-    return h;
-}
 }  // namespace
 
 // Device-side build: contiguous build columns plus the ARRAY or HASH table.
@@ -161,7 +146,7 @@ void JoinBuildState::Build()
             CudaCheck(omg::LaunchVarlenTileLens(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(),
                           bt.DeviceTileOutRows(), 0, lens.Get(), s),
                 "build column lengths");
-            const int64_t bytes = ScanLengths(lens.Get(), rows, colOffs[c], s);
+            const int64_t bytes = omg::ScanLengths(lens.Get(), rows, colOffs[c], s);
             colValues[c].Reset(static_cast<size_t>(bytes) + 16, s);
             CudaCheck(omg::LaunchVarlenTileCopy(bt.DeviceBatches(), bt.DeviceTiles(), bt.NumTiles(),
                           bt.DeviceTileOutRows(), 0, colOffs[c].Get(), colValues[c].Get(), s),
@@ -753,7 +738,7 @@ void LookupJoinOperator::ProcessPending()
                       bOffs, lens.Get(), s),
             "output string lengths");
         DevArray<int64_t> offs64;
-        const int64_t total = ScanLengths(lens.Get(), nPos, offs64, s);
+        const int64_t total = omg::ScanLengths(lens.Get(), nPos, offs64, s);
         if (total >= (int64_t(1) << 31)) {
             throw OmniException("UNSUPPORTED_ERROR", "more than 2 GiB of VARCHAR output in one probe call", -2);
         }
@@ -1277,7 +1262,7 @@ void LookupOuterJoinOperator::Prepare()
             DevArray<uint32_t> lens(static_cast<size_t>(m), s);
             CudaCheck(omg::LaunchVarlenRowsLens(rows.Get(), m, b.colOffs[bc].Get(), lens.Get(), s), "string lengths");
             DevArray<int64_t> offs64;
-            const int64_t total = ScanLengths(lens.Get(), m, offs64, s);
+            const int64_t total = omg::ScanLengths(lens.Get(), m, offs64, s);
             if (total >= (int64_t(1) << 31)) {
                 throw OmniException("UNSUPPORTED_ERROR", "more than 2 GiB of VARCHAR output in one batch set", -2);
             }

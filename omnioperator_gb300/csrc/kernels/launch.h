@@ -93,6 +93,27 @@ cudaError_t LaunchVarlenRowsLens(const int32_t *rows, int64_t n, const int64_t *
 cudaError_t LaunchVarlenRowsCopy(const int32_t *rows, int64_t n, const int64_t *srcOffs, const uint8_t *srcChars,
     const int64_t *offs64, uint8_t *chars, int32_t *offs32, long long total, cudaStream_t stream);
 cudaError_t LaunchOffsetsTail(int64_t *offs, int64_t n, const long long *total, cudaStream_t stream);
+// String dictionary of VARCHAR group-by columns (kernels/dict.cu): insert a batch set's strings
+// (rowSlot per row in tile output order, -1 for NULL), give new slots ids, append their
+// characters to the arena, grow the table, map rows to ids, and turn ids back into strings.
+cudaError_t LaunchDictInsert(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, const int64_t *tileOutRow,
+    int32_t input, unsigned long long *hash, const int32_t *id, unsigned long long *rep, uint64_t cap,
+    const int64_t *arenaOff, const uint8_t *arena, int32_t *rowSlot, int32_t *error, cudaStream_t stream);
+cudaError_t LaunchDictMaterialize(const unsigned long long *hash, int32_t *id, const unsigned long long *rep,
+    uint64_t cap, int32_t firstId, unsigned int *counter, unsigned long long *newRep, uint32_t *newLen,
+    const BatchDesc *batches, int32_t input, cudaStream_t stream);
+cudaError_t LaunchDictAppend(const unsigned long long *newRep, int64_t nNew, int32_t firstId, const int64_t *arenaOff,
+    uint8_t *arena, const BatchDesc *batches, int32_t input, cudaStream_t stream);
+cudaError_t LaunchDictRehash(const unsigned long long *oldHash, const int32_t *oldId, uint64_t oldCap,
+    unsigned long long *hash, int32_t *id, uint64_t cap, int32_t *error, cudaStream_t stream);
+cudaError_t LaunchDictShiftOffsets(const int64_t *offs, int64_t nNew, int64_t base, int64_t *arenaOff,
+    cudaStream_t stream);
+cudaError_t LaunchDictRowIds(const int32_t *rowSlot, int64_t n, const int32_t *id, int32_t *ids, cudaStream_t stream);
+cudaError_t LaunchDictDecodeLens(const int32_t *ids, const uint8_t *nulls, int64_t n, const int64_t *arenaOff,
+    uint32_t *lens, cudaStream_t stream);
+cudaError_t LaunchDictDecodeCopy(const int32_t *ids, const uint8_t *nulls, int64_t n, const int64_t *arenaOff,
+    const uint8_t *arena, const int64_t *offs64, uint8_t *chars, int32_t *offs32, long long total,
+    cudaStream_t stream);
 // Multi-column join keys: the tuple hash of each build row (NULL if a key column is NULL).
 cudaError_t LaunchJoinKeyHash(const JoinKeyCols &kc, int64_t n, uint64_t *out, uint8_t *outNulls, cudaStream_t stream);
 // Outer joins: flags[i] = 1 for build rows never matched; their row numbers in order (offsets =

@@ -27,6 +27,7 @@ class SizingModel;
 namespace omg {
 class OpStream;
 template <typename T> class DevArray;
+struct OutColumn;
 }
 
 namespace omniruntime {
@@ -52,6 +53,9 @@ struct AggPlan {
     bool orderDependent = false;           // has an OUT_SUM_EXACT column (sticky overflow)
     std::vector<omg::AlignCol> align;      // AlignSchema columns; empty unless every aggregator
                                            // reads raw input and emits partials
+    std::vector<int32_t> dictInputs;       // kernel inputs of VARCHAR/CHAR group-by columns: the
+                                           // kernels read per-row string dictionary ids (int32)
+    std::vector<int32_t> varlenInputs;     // other VARCHAR/CHAR inputs (COUNT reads their NULLs)
 };
 
 // Kernel launch parameters of a plan (table fields as given; stats: [groups, retry count,
@@ -126,6 +130,8 @@ private:
     void Decide(omg::BatchTable &bt, cudaStream_t s);
     void Partition(omg::BatchTable &bt, omg::AggLaunch &p, PartBuffers &pb, cudaStream_t s);
     void Flush();
+    void EncodeStrings(omg::BatchTable &bt, cudaStream_t s);
+    void DecodeStrings(std::vector<omg::OutColumn> &cols, int64_t rows, cudaStream_t s);
     void Extract();
     void ReleasePending();
 
