@@ -133,6 +133,15 @@ int32_t omg_vec_wrap_device(int32_t type_id, int32_t width, int32_t size, void *
     void **out_vec);
 /* Delete a vector that is not owned by a batch. */
 int32_t omg_vec_free(void *vec);
+/* Dictionary-encoded host vector (VectorHelper::CreateDictionaryVector,
+ * core/src/vector/vector_helper.h:381-420): row i is row ids[i] of the flat vector `dictionary`
+ * (host or device), whose buffers the new vector shares (the dictionary handle stays the caller's
+ * and may be freed).  A row is NULL when its dictionary row is.  Ids outside
+ * [0, omg_vec_size(dictionary)) are refused with OMG_ERR_INVALID.  Operators flatten such
+ * vectors on the device when they take a batch. */
+int32_t omg_vec_new_dictionary(const int32_t *ids, int32_t size, void *dictionary, void **out_vec);
+/* Vector encoding (BaseVector::GetEncoding, vector/vector.h:107): 0 flat, 1 dictionary. */
+int32_t omg_vec_encoding(void *vec);
 /* Raw accessors (unsafe/unsafe_vector.h:19-48).  Pointers are host or device
  * addresses according to omg_vec_is_device. */
 void *omg_vec_values(void *vec);

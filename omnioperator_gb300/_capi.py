@@ -37,6 +37,8 @@ _SIGS = {
     "omg_vec_new_device": (I32, [I32, I32, I32, C.POINTER(P)]),
     "omg_vec_wrap_device": (I32, [I32, I32, I32, P, P, C.POINTER(P)]),
     "omg_vec_free": (I32, [P]),
+    "omg_vec_new_dictionary": (I32, [P, I32, P, C.POINTER(P)]),
+    "omg_vec_encoding": (I32, [P]),
     "omg_vec_values": (P, [P]),
     "omg_vec_nulls": (P, [P]),
     "omg_vec_size": (I32, [P]),

@@ -156,6 +156,55 @@ def new_host_vector(dtype: DataType, values: np.ndarray, nulls: np.ndarray | Non
     return vec
 
 
+def new_dictionary_vector(ids, dictionary: int) -> int:
+    """A dictionary-encoded host vector: row i is row ids[i] of the flat vector `dictionary`
+    (which stays the caller's)."""
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    out = C.c_void_p()
+    check(lib().omg_vec_new_dictionary(ids.ctypes.data if ids.size else None, len(ids), dictionary, C.byref(out)))
+    return out.value
+
+
+def make_dict_batch(types, columns, nulls=None, encode=()) -> int:
+    """make_batch, with the columns whose indices are in `encode` dictionary-encoded: each such
+    column becomes ids into a dictionary of its distinct (value, null) entries, in reverse order
+    of first appearance so that ids differ from row numbers."""
+    n = len(columns[0]) if columns else 0
+    out = C.c_void_p()
+    check(lib().omg_batch_new(n, C.byref(out)))
+    batch = out.value
+    for i, (t, col) in enumerate(zip(types, columns)):
+        m = None if nulls is None else nulls[i]
+        if i not in encode:
+            check(lib().omg_batch_append(batch, new_host_vector(t, col, m)))
+            continue
+        keys = {}
+        ids = np.empty(n, dtype=np.int32)
+        for r in range(n):
+            isnull = m is not None and bool(m[r])
+            v = col[r]
+            k = (True, None) if isnull else (False, bytes(v) if isinstance(v, (bytes, bytearray, str)) else
+                                               np.asarray(v).tobytes())
+            ids[r] = keys.setdefault(k, len(keys))
+        order = list(keys.items())[::-1]
+        remap = {old: new for new, (_, old) in enumerate(order)}
+        ids = np.array([remap[x] for x in ids], dtype=np.int32)
+        first = {}
+        for r in range(n):
+            first.setdefault(ids[r], r)
+        rows = [first[j] for j in range(len(order))]
+        dvals = [col[r] for r in rows] if col.dtype == object else np.asarray(col)[rows]
+        if col.dtype == object:
+            dvals = np.array(dvals, dtype=object)
+        dnull = None if m is None else np.asarray(m)[rows]
+        dvec = new_host_vector(t, dvals, dnull)
+        try:
+            check(lib().omg_batch_append(batch, new_dictionary_vector(ids, dvec)))
+        finally:
+            check(lib().omg_vec_free(dvec))
+    return batch
+
+
 def make_batch(types, columns, nulls=None) -> int:
     """A host VectorBatch from numpy columns (all of equal length)."""
     n = len(columns[0]) if columns else 0

@@ -165,6 +165,17 @@ int32_t omg_vec_new_varchar(int32_t type_id, int32_t size, int64_t data_bytes, v
     });
 }
 
+int32_t omg_vec_new_dictionary(const int32_t *ids, int32_t size, void *dictionary, void **out_vec)
+{
+    return Guard([&] {
+        Require(out_vec != nullptr && dictionary != nullptr && size >= 0 && (size == 0 || ids != nullptr),
+            "invalid arguments");
+        *out_vec = VectorHelper::CreateDictionaryVector(ids, size, *static_cast<BaseVector *>(dictionary));
+    });
+}
+
+int32_t omg_vec_encoding(void *vec) { return vec ? static_cast<int32_t>(static_cast<BaseVector *>(vec)->GetEncoding()) : -1; }
+
 int32_t *omg_vec_offsets(void *vec) { return vec ? static_cast<BaseVector *>(vec)->RawOffsets() : nullptr; }
 int64_t omg_vec_data_bytes(void *vec) { return vec ? static_cast<BaseVector *>(vec)->DataBytes() : -1; }
 

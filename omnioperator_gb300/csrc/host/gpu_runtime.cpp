@@ -43,6 +43,9 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
                     -1);
             }
             BaseVector *v = b->Get(c);
+            if (v->GetEncoding() != omniruntime::vec::OMNI_FLAT) {
+                throw OmniException("OPERATOR_RUNTIME_ERROR", "dictionary vector reached a kernel unflattened", -1);
+            }
             if (v->GetSize() < b->GetRowCount()) {
                 throw OmniException("OPERATOR_RUNTIME_ERROR", "vector shorter than the batch row count", -1);
             }
@@ -219,6 +222,98 @@ std::vector<OutColumn> CopyColumnsToHost(const std::vector<OutColumn> &cols, int
         host.push_back(h);
     }
     return host;
+}
+
+BaseVector *FlattenDictionary(const BaseVector &v, cudaStream_t s)
+{
+    using omniruntime::vec::OMNI_DICTIONARY;
+    if (v.GetEncoding() != OMNI_DICTIONARY) {
+        throw OmniException("INVALID_ARGUMENT", "not a dictionary-encoded vector", -1);
+    }
+    RequireDevice();
+    const BaseVector &d = *v.Dictionary();
+    const int64_t n = v.GetSize();
+    const int32_t *ids = v.RawIds();
+    DevArray<int32_t> err(1, s, true);
+    const size_t nullBytes = static_cast<size_t>(((n + 31) / 32) * 4 + 8);
+    BufferPtr nulls = Buffer::NewDevice(nullBytes, s, true);
+    BaseVector *out = nullptr;
+    if (d.IsVarlen()) {
+        DevArray<uint32_t> lens(static_cast<size_t>(n), s);
+        CudaCheck(LaunchDictGatherLens(ids, n, d.RawOffsets(), d.RawNulls(), d.GetSize(), lens.Get(),
+                      static_cast<uint32_t *>(nulls->Data()), err.Get(), s),
+            "dictionary string lengths");
+        DevArray<int64_t> offs64;
+        const int64_t total = ScanLengths(lens.Get(), n, offs64, s);
+        if (total >= (int64_t(1) << 31)) {
+            throw OmniException("UNSUPPORTED_ERROR", "more than 2 GiB of characters in one vector", -2);
+        }
+        BufferPtr chars = Buffer::NewDevice(static_cast<size_t>(total) + 16, s, false);
+        BufferPtr offs = Buffer::NewDevice((static_cast<size_t>(n) + 1) * sizeof(int32_t), s, true);
+        CudaCheck(LaunchDictGatherChars(ids, n, d.RawOffsets(), d.RawValues(), d.RawNulls(), d.GetSize(),
+                      offs64.Get(), static_cast<uint8_t *>(chars->Data()), static_cast<int32_t *>(offs->Data()), total,
+                      s),
+            "dictionary strings");
+        out = new BaseVector(v.GetTypeId(), v.GetSize(), chars, total, offs, 0, nulls, 0, d.NullFlag());
+    } else {
+        const int w = d.GetWidth();
+        if (w != 1 && w != 2 && w != 4 && w != 8 && w != 16) {
+            throw OmniException("UNSUPPORTED_ERROR", "dictionary vectors of " + std::to_string(w) + "-byte values", -2);
+        }
+        BufferPtr values = Buffer::NewDevice(((static_cast<size_t>(d.GetWidth()) * (n < 1 ? 1 : n)) + 15) & ~size_t(15),
+            s, false);
+        CudaCheck(LaunchDictGatherFixed(ids, n, d.RawValues(), d.RawNulls(), d.GetSize(), d.GetWidth(),
+                      static_cast<uint8_t *>(values->Data()), static_cast<uint32_t *>(nulls->Data()), err.Get(), s),
+            "dictionary values");
+        out = new BaseVector(v.GetTypeId(), v.GetWidth(), v.GetSize(), values, 0, nulls, 0, d.NullFlag());
+    }
+    int32_t h = 0;
+    CudaCheck(cudaMemcpyAsync(&h, err.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read dictionary check");
+    CudaCheck(cudaStreamSynchronize(s), "read dictionary check");
+    if (h != 0) {
+        delete out;
+        throw OmniException("INVALID_ARGUMENT", "dictionary id out of range", -1);
+    }
+    return out;
+}
+
+bool HasDictionary(const VectorBatch *batch)
+{
+    for (int32_t i = 0; i < batch->GetVectorCount(); ++i) {
+        if (batch->Get(i)->GetEncoding() == omniruntime::vec::OMNI_DICTIONARY) {
+            return true;
+        }
+    }
+    return false;
+}
+
+void FlattenTaken(VectorBatch *batch)
+{
+    if (!HasDictionary(batch)) {
+        return;
+    }
+    cudaStream_t s = nullptr;
+    try {
+        RequireDevice();
+        s = AcquirePooledStream();
+        FlattenDictionaries(batch, s);
+    } catch (...) {
+        if (s != nullptr) {
+            ReleasePooledStream(s);
+        }
+        omniruntime::vec::VectorHelper::FreeVecBatch(batch);
+        throw;
+    }
+    ReleasePooledStream(s);
+}
+
+void FlattenDictionaries(VectorBatch *batch, cudaStream_t s)
+{
+    for (int32_t i = 0; i < batch->GetVectorCount(); ++i) {
+        if (batch->Get(i)->GetEncoding() == omniruntime::vec::OMNI_DICTIONARY) {
+            batch->Set(i, FlattenDictionary(*batch->Get(i), s));
+        }
+    }
 }
 
 // A VARCHAR column from per-row lengths: exclusive offsets (n + 1, 64-bit) and the total.

@@ -201,6 +201,16 @@ size_t NullBitmapBytes(int64_t rows);
 // the total, read back to the host (synchronises `s`).
 int64_t ScanLengths(const uint32_t *lens, int64_t n, DevArray<int64_t> &offs, cudaStream_t s);
 
+// A dictionary-encoded vector as a new flat DEVICE vector (gathered on `s`; synchronises `s` to
+// check the ids).  Throws INVALID_ARGUMENT for an id outside the dictionary.
+omniruntime::vec::BaseVector *FlattenDictionary(const omniruntime::vec::BaseVector &v, cudaStream_t s);
+// Replace every dictionary-encoded vector of `batch` by its flat device form.
+void FlattenDictionaries(omniruntime::vec::VectorBatch *batch, cudaStream_t s);
+bool HasDictionary(const omniruntime::vec::VectorBatch *batch);
+// For a batch an operator has taken: flatten it on a pooled stream, freeing the batch if that
+// fails (the error is rethrown).
+void FlattenTaken(omniruntime::vec::VectorBatch *batch);
+
 // Budget of device-side bounded waits (clock64 ticks); 0 restores the default.
 long long WaitBudget();
 void SetWaitBudget(long long ticks);

@@ -642,6 +642,7 @@ int32_t HashAggregationOperator::AddInput(VectorBatch *vecBatch)
         vec::VectorHelper::FreeVecBatch(vecBatch);
         throw OmniException("OPERATOR_RUNTIME_ERROR", "AddInput after GetOutput started", -6);
     }
+    omg::FlattenTaken(vecBatch);  // dictionary-encoded vectors -> flat device vectors
     pending_.push_back(vecBatch);
     pendingRows_ += vecBatch->GetRowCount();
     if (pendingRows_ >= omg::AggFlushRows()) {
@@ -725,6 +726,7 @@ VectorBatch *HashAggregationOperator::AlignSchema(VectorBatch *inputVecBatch)
         impl_->stream.SetUser(userStream_);
     }
     cudaStream_t s = impl_->stream.Get();
+    omg::FlattenDictionaries(inputVecBatch, s);
     std::vector<omg::OutColumn> cols(plan_.align.size());
     omg::BatchTable bt;
     if (rows > 0) {

@@ -376,6 +376,7 @@ int32_t HashBuilderOperator::AddInput(VectorBatch *vecBatch)
         vec::VectorHelper::FreeVecBatch(vecBatch);
         throw OmniException("OPERATOR_RUNTIME_ERROR", "build batch has fewer vectors than build types", -1);
     }
+    omg::FlattenTaken(vecBatch);  // dictionary-encoded vectors -> flat device vectors
     std::lock_guard<std::mutex> g(state_->mu);
     if (state_->built) {
         vec::VectorHelper::FreeVecBatch(vecBatch);
@@ -541,6 +542,7 @@ int32_t LookupJoinOperator::AddInput(VectorBatch *vecBatch)
         vec::VectorHelper::FreeVecBatch(vecBatch);
         throw OmniException("OPERATOR_RUNTIME_ERROR", "probe batch has fewer vectors than probe types", -1);
     }
+    omg::FlattenTaken(vecBatch);  // dictionary-encoded vectors -> flat device vectors
     pending_.push_back(vecBatch);
     pendingRows_ += vecBatch->GetRowCount();
     SetStatus(OMNI_STATUS_NORMAL);

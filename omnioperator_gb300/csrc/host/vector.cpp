@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "host/gpu_runtime.h"
 #include "omniop/types.h"
 
 namespace omniruntime {
@@ -70,10 +71,52 @@ BaseVector::BaseVector(DataTypeId type, int32_t size, omg::BufferPtr chars, int6
       offsetsOffset_(offsetsOffset), dataBytes_(dataBytes)
 {}
 
+BaseVector::BaseVector(omg::BufferPtr ids, int32_t size, const BaseVector &dictionary)
+    : type_(dictionary.type_), width_(dictionary.width_), size_(size), hasNull_(dictionary.hasNull_),
+      values_(std::move(ids)), dataBytes_(dictionary.dataBytes_)
+{
+    if (dictionary.dictionary_) {
+        throw exception::OmniException("UNSUPPORTED_ERROR", "a dictionary of a dictionary vector", -2);
+    }
+    if (dictionary.IsVarlen()) {
+        dictionary_ = std::make_shared<BaseVector>(dictionary.type_, dictionary.size_, dictionary.values_,
+            dictionary.dataBytes_, dictionary.offsets_, dictionary.offsetsOffset_, dictionary.nulls_,
+            dictionary.nullsOffset_, dictionary.hasNull_);
+    } else {
+        dictionary_ = std::make_shared<BaseVector>(dictionary.type_, dictionary.width_, dictionary.size_,
+            dictionary.values_, dictionary.valuesOffset_, dictionary.nulls_, dictionary.nullsOffset_,
+            dictionary.hasNull_);
+    }
+}
+
+BaseVector *VectorHelper::CreateDictionaryVector(const int32_t *values, int32_t valueSize, const BaseVector &vector)
+{
+    if (valueSize < 0 || (valueSize > 0 && values == nullptr)) {
+        throw exception::OmniException("INVALID_ARGUMENT", "invalid dictionary ids", -1);
+    }
+    if (vector.GetEncoding() != OMNI_FLAT) {
+        throw exception::OmniException("UNSUPPORTED_ERROR", "a dictionary of a dictionary vector", -2);
+    }
+    for (int32_t i = 0; i < valueSize; ++i) {
+        if (values[i] < 0 || values[i] >= vector.GetSize()) {
+            throw exception::OmniException("INVALID_ARGUMENT",
+                "dictionary id " + std::to_string(values[i]) + " out of range", -1);
+        }
+    }
+    auto ids = omg::Buffer::NewHost(ValuesBytes(sizeof(int32_t), valueSize), false);
+    if (valueSize > 0) {
+        std::memcpy(ids->Data(), values, sizeof(int32_t) * static_cast<size_t>(valueSize));
+    }
+    return new BaseVector(ids, valueSize, vector);
+}
+
 bool BaseVector::HasNull()
 {
     if (hasNull_) {
         return true;
+    }
+    if (dictionary_) {
+        return false;  // takes the dictionary's flag
     }
     if (nulls_ == nullptr || IsDevice()) {
         return false;  // device vectors rely on the writer's flag
@@ -133,6 +176,11 @@ VectorBatch *VectorHelper::CopyBatch(VectorBatch *batch, bool toDevice, void *st
     try {
         for (int32_t i = 0; i < batch->GetVectorCount(); ++i) {
             BaseVector *src = batch->Get(i);
+            std::unique_ptr<BaseVector> flat;
+            if (src->GetEncoding() == OMNI_DICTIONARY) {
+                flat.reset(omg::FlattenDictionary(*src, static_cast<cudaStream_t>(stream)));
+                src = flat.get();
+            }
             cudaMemcpyKind kind = cudaMemcpyDefault;
             BaseVector *dst;
             size_t vb;

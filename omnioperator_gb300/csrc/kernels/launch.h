@@ -114,6 +114,16 @@ cudaError_t LaunchDictDecodeLens(const int32_t *ids, const uint8_t *nulls, int64
 cudaError_t LaunchDictDecodeCopy(const int32_t *ids, const uint8_t *nulls, int64_t n, const int64_t *arenaOff,
     const uint8_t *arena, const int64_t *offs64, uint8_t *chars, int32_t *offs32, long long total,
     cudaStream_t stream);
+// Dictionary-encoded input vectors (kernels/dictvec.cu): fixed-width values and null bits
+// gathered through the ids; VARCHAR lengths (with null bits), then characters.  Out-of-range ids
+// set *error and give NULL rows.
+cudaError_t LaunchDictGatherFixed(const int32_t *ids, int64_t n, const uint8_t *dictValues, const uint8_t *dictNulls,
+    int32_t dictSize, int width, uint8_t *out, uint32_t *outNulls, int32_t *error, cudaStream_t stream);
+cudaError_t LaunchDictGatherLens(const int32_t *ids, int64_t n, const int32_t *dictOffs, const uint8_t *dictNulls,
+    int32_t dictSize, uint32_t *lens, uint32_t *outNulls, int32_t *error, cudaStream_t stream);
+cudaError_t LaunchDictGatherChars(const int32_t *ids, int64_t n, const int32_t *dictOffs, const uint8_t *dictChars,
+    const uint8_t *dictNulls, int32_t dictSize, const int64_t *offs64, uint8_t *chars, int32_t *offs32,
+    long long total, cudaStream_t stream);
 // Multi-column join keys: the tuple hash of each build row (NULL if a key column is NULL).
 cudaError_t LaunchJoinKeyHash(const JoinKeyCols &kc, int64_t n, uint64_t *out, uint8_t *outNulls, cudaStream_t stream);
 // Outer joins: flags[i] = 1 for build rows never matched; their row numbers in order (offsets =

@@ -13,6 +13,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "memory.h"
@@ -44,6 +45,12 @@ public:
     // in `chars`).
     BaseVector(DataTypeId type, int32_t size, omg::BufferPtr chars, int64_t dataBytes, omg::BufferPtr offsets,
         size_t offsetsOffset, omg::BufferPtr nulls, size_t nullsOffset, bool hasNull);
+    // Dictionary-encoded vector (VectorHelper::CreateDictionaryVector, vector/vector_helper.h:
+    // 70-82,381-420): row i is row ids[i] of `dictionary`, whose buffers this vector shares, and
+    // is NULL when that dictionary row is.  `ids` holds `size` int32 values in
+    // [0, dictionary.GetSize()).  The operators flatten such vectors on the device when they
+    // take a batch (omg::FlattenDictionaries).
+    BaseVector(omg::BufferPtr ids, int32_t size, const BaseVector &dictionary);
     virtual ~BaseVector() = default;
 
     bool IsVarlen() const { return type_ == OMNI_VARCHAR || type_ == OMNI_CHAR; }
@@ -59,7 +66,10 @@ public:
     int32_t GetSize() const { return size_; }
     DataTypeId GetTypeId() const { return type_; }
     int32_t GetWidth() const { return width_; }
-    Encoding GetEncoding() const { return OMNI_FLAT; }
+    Encoding GetEncoding() const { return dictionary_ ? OMNI_DICTIONARY : OMNI_FLAT; }
+    // Dictionary encoding: the row ids (int32) and the dictionary (a flat view).
+    const int32_t *RawIds() const { return dictionary_ ? reinterpret_cast<const int32_t *>(RawValues()) : nullptr; }
+    const BaseVector *Dictionary() const { return dictionary_.get(); }
     bool IsDevice() const { return values_->IsDevice(); }
 
     uint8_t *RawValues() const { return static_cast<uint8_t *>(values_->Data()) + valuesOffset_; }
@@ -78,6 +88,9 @@ public:
     void SetNotNull(int32_t i) { RawNulls()[i >> 3] &= static_cast<uint8_t>(~(1u << (i & 7))); }
     bool IsNull(int32_t i) const
     {
+        if (dictionary_) {
+            return dictionary_->IsNull(RawIds()[i]);
+        }
         const uint8_t *n = RawNulls();
         return n != nullptr && ((n[i >> 3] >> (i & 7)) & 1u);
     }
@@ -105,6 +118,7 @@ protected:
     omg::BufferPtr offsets_;  // VARCHAR/CHAR only
     size_t offsetsOffset_ = 0;
     int64_t dataBytes_ = 0;
+    std::shared_ptr<BaseVector> dictionary_;  // dictionary encoding only (values_ = the ids)
 };
 
 // Typed host accessor (vector/vector.h Vector<T>::GetValue/SetValue).
@@ -128,6 +142,12 @@ public:
     VectorBatch &operator=(const VectorBatch &) = delete;
 
     void Append(BaseVector *vector) { vectors_.push_back(vector); }
+    // Replace vector `index` (the old one is deleted).
+    void Set(int32_t index, BaseVector *vector)
+    {
+        delete vectors_.at(index);
+        vectors_.at(index) = vector;
+    }
     BaseVector *Get(int32_t index) const { return vectors_.at(index); }
     int32_t GetRowCount() const { return static_cast<int32_t>(rowCnt_); }
     int32_t GetVectorCount() const { return static_cast<int32_t>(vectors_.size()); }
@@ -155,6 +175,9 @@ public:
     {
         return new BaseVector(type, TypeWidth(type, width), size, false);
     }
+    // VectorHelper::CreateDictionaryVector (vector/vector_helper.h:381-420): a host vector of
+    // `valueSize` rows selecting rows `values` of `vector`; ids out of range are refused.
+    static BaseVector *CreateDictionaryVector(const int32_t *values, int32_t valueSize, const BaseVector &vector);
     // Deep copy of a batch into host or device residency.
     static VectorBatch *CopyBatch(VectorBatch *batch, bool toDevice, void *stream);
 };

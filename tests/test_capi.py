@@ -184,3 +184,20 @@ def test_batched_aggregation_rejects_sticky_overflow_plans_and_empty_tasks():
     omg.free_batches([b, empty])
     fac.close()
     fac2.close()
+
+
+def test_dictionary_vectors_on_the_host():
+    """VectorHelper::CreateDictionaryVector: ids index a flat dictionary whose buffers the new vector
+    shares; NULL-ness comes from the dictionary row; out-of-range ids are refused."""
+    L = omg.lib()
+    d = omg.new_host_vector(omg.LongType(), np.array([5, 6, 7], dtype=np.int64), np.array([False, True, False]))
+    v = omg.new_dictionary_vector(np.array([2, 1, 0, 2], dtype=np.int32), d)
+    assert L.omg_vec_encoding(v) == 1 and L.omg_vec_encoding(d) == 0
+    assert L.omg_vec_size(v) == 4 and L.omg_vec_type(v) == omg.OMNI_LONG and L.omg_vec_width(v) == 8
+    assert L.omg_vec_has_null(v) == 1
+    for bad in ([0, 3], [-1]):
+        with pytest.raises(omg.OmgError) as ei:
+            omg.new_dictionary_vector(np.array(bad, dtype=np.int32), d)
+        assert ei.value.status == -1
+    L.omg_vec_free(d)
+    L.omg_vec_free(v)
