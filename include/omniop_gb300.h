@@ -220,6 +220,23 @@ int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_
     const OmgDataType *build_output_types, int64_t hash_builder_factory_addr, const void *filter_expr,
     int32_t is_shuffle_exchange_build_plan, void **out_factory);
 
+/* ---- join filter expressions (core/src/expression/expressions.h:22-62) -------------
+ * Trees of FieldExpr / LiteralExpr / BinaryExpr / UnaryExpr / IsNullExpr nodes for the
+ * filter_expr of omg_lookupjoin_factory_create; a field is a column of the joined row (probe
+ * columns first, then build columns).  Binary, unary and is-null nodes take ownership of their
+ * children; free the root with omg_expr_free (the factory compiles the tree and keeps no pointer
+ * into it).  Operator codes follow expressions::Operator: 0 EQ, 1 NEQ, 2 LT, 3 LTE, 4 GT, 5 GTE,
+ * 6 AND, 7 OR, 8 NOT.  The GB300 join runs comparisons, AND, OR, NOT and IS NULL over integer-
+ * like and DOUBLE columns and literals; other trees are refused by the factory with
+ * OMG_ERR_UNSUPPORTED, as the reference refuses what its code generator cannot compile. */
+int32_t omg_expr_field(int32_t col, const OmgDataType *type, void **out_expr);
+int32_t omg_expr_literal_long(int64_t value, const OmgDataType *type, int32_t is_null, void **out_expr);
+int32_t omg_expr_literal_double(double value, int32_t is_null, void **out_expr);
+int32_t omg_expr_binary(int32_t op, void *left, void *right, void **out_expr);
+int32_t omg_expr_unary(int32_t op, void *child, void **out_expr);
+int32_t omg_expr_is_null(void *child, void **out_expr);
+int32_t omg_expr_free(void *expr);
+
 /* OperatorFactory::CreateOperator (operator/operator_factory.h:18). */
 int32_t omg_factory_create_operator(void *factory, void **out_op);
 /* Factory destructor (the JNI closeNative on a factory). */

@@ -57,6 +57,13 @@ _SIGS = {
     "omg_batch_to_host": (I32, [P, C.POINTER(P)]),
     "omg_hashagg_factory_create": (I32, [P, P, I32, P, I32, P, P, P, P, P, P, P, P, I32, C.POINTER(P)]),
     "omg_hashbuilder_factory_create": (I32, [I32, P, I32, P, I32, I32, C.POINTER(P)]),
+    "omg_expr_field": (I32, [I32, P, C.POINTER(P)]),
+    "omg_expr_literal_long": (I32, [I64, P, I32, C.POINTER(P)]),
+    "omg_expr_literal_double": (I32, [C.c_double, I32, C.POINTER(P)]),
+    "omg_expr_binary": (I32, [I32, P, P, C.POINTER(P)]),
+    "omg_expr_unary": (I32, [I32, P, C.POINTER(P)]),
+    "omg_expr_is_null": (I32, [P, C.POINTER(P)]),
+    "omg_expr_free": (I32, [P]),
     "omg_lookupjoin_factory_create": (I32, [P, I32, P, I32, P, I32, P, I32, P, I64, P, I32, C.POINTER(P)]),
     "omg_hashbuilder_factory_create_side": (I32, [I32, I32, P, I32, P, I32, I32, C.POINTER(P)]),
     "omg_lookupouterjoin_factory_create": (I32, [P, I32, P, I32, P, I32, P, I64, I32, C.POINTER(P)]),

@@ -477,6 +477,77 @@ class HashBuilderOperatorFactory(OperatorFactory):
         super().__init__(out.value)
 
 
+# --------------------------------------------------------------------------- join filter expressions
+EXPR_EQ, EXPR_NEQ, EXPR_LT, EXPR_LTE, EXPR_GT, EXPR_GTE, EXPR_AND, EXPR_OR, EXPR_NOT = range(9)
+
+
+class Field:
+    """FieldExpr: column `col` of the joined row (probe columns first, then build columns)."""
+
+    def __init__(self, col: int, dtype: DataType):
+        self.col, self.dtype = col, dtype
+
+
+class Literal:
+    """LiteralExpr of an integer-like / BOOLEAN (int value) or DOUBLE (float value) type."""
+
+    def __init__(self, value, dtype: DataType, is_null: bool = False):
+        self.value, self.dtype, self.is_null = value, dtype, is_null
+
+
+class Binary:
+    """BinaryExpr(op, left, right) with op one of EXPR_EQ .. EXPR_OR."""
+
+    def __init__(self, op: int, left, right):
+        self.op, self.left, self.right = op, left, right
+
+
+class Not:
+    def __init__(self, child):
+        self.child = child
+
+
+class IsNull:
+    def __init__(self, child):
+        self.child = child
+
+
+def _expr_handle(e) -> int:
+    """The C expression tree of `e` (the caller frees the root with omg_expr_free)."""
+    out = C.c_void_p()
+    L = lib()
+    if isinstance(e, Field):
+        t = _types([e.dtype])
+        check(L.omg_expr_field(e.col, t, C.byref(out)))
+    elif isinstance(e, Literal):
+        if e.dtype.id == OMNI_DOUBLE:
+            check(L.omg_expr_literal_double(float(e.value), 1 if e.is_null else 0, C.byref(out)))
+        else:
+            check(L.omg_expr_literal_long(int(e.value), _types([e.dtype]), 1 if e.is_null else 0, C.byref(out)))
+    elif isinstance(e, Binary):
+        left = _expr_handle(e.left)
+        try:
+            right = _expr_handle(e.right)
+        except Exception:
+            L.omg_expr_free(left)
+            raise
+        rc = L.omg_expr_binary(e.op, left, right, C.byref(out))
+        if rc != 0:
+            L.omg_expr_free(left)
+            L.omg_expr_free(right)
+        check(rc)
+    elif isinstance(e, (Not, IsNull)):
+        child = _expr_handle(e.child)
+        rc = (L.omg_expr_unary(EXPR_NOT, child, C.byref(out)) if isinstance(e, Not)
+              else L.omg_expr_is_null(child, C.byref(out)))
+        if rc != 0:
+            L.omg_expr_free(child)
+        check(rc)
+    else:
+        raise TypeError(f"not a filter expression node: {e!r}")
+    return out.value
+
+
 class LookupJoinOperatorFactory(OperatorFactory):
     """LookupJoinOperatorFactory::CreateLookupJoinOperatorFactory(probeTypes, probeOutputCols,
     probeHashCols, buildOutputCols, buildOutputTypes, hashBuilderFactoryAddr, filterExpr,
@@ -485,14 +556,17 @@ class LookupJoinOperatorFactory(OperatorFactory):
     def __init__(self, probe_types, probe_output_cols, probe_hash_cols, build_output_cols, build_output_types,
                  hash_builder_factory: HashBuilderOperatorFactory, filter_expr=None,
                  is_shuffle_exchange_build_plan=False):
-        if filter_expr is not None:
-            raise OmgError(-2, "join filter expressions are not supported")
         out = C.c_void_p()
-        check(lib().omg_lookupjoin_factory_create(
-            _types(probe_types), len(probe_types), _i32(probe_output_cols), len(probe_output_cols),
-            _i32(probe_hash_cols), len(probe_hash_cols), _i32(build_output_cols), len(build_output_cols),
-            _types(build_output_types), int(hash_builder_factory.handle), None,
-            1 if is_shuffle_exchange_build_plan else 0, C.byref(out)))
+        expr = _expr_handle(filter_expr) if filter_expr is not None else None
+        try:
+            check(lib().omg_lookupjoin_factory_create(
+                _types(probe_types), len(probe_types), _i32(probe_output_cols), len(probe_output_cols),
+                _i32(probe_hash_cols), len(probe_hash_cols), _i32(build_output_cols), len(build_output_cols),
+                _types(build_output_types), int(hash_builder_factory.handle), expr,
+                1 if is_shuffle_exchange_build_plan else 0, C.byref(out)))
+        finally:
+            if expr is not None:
+                lib().omg_expr_free(expr)
         super().__init__(out.value)
 
 

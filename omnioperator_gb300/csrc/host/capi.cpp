@@ -14,6 +14,7 @@
 #include "kernels/launch.h"
 #include "omniop/batched_agg.h"
 #include "omniop/hash_aggregation.h"
+#include "omniop/expressions.h"
 #include "omniop/hash_join.h"
 #include "omniop/memory.h"
 #include "omniop/operator.h"
@@ -368,6 +369,75 @@ int32_t omg_lookupouterjoin_factory_create(const OmgDataType *probe_types, int32
             static_cast<omniruntime::op::BuildSide>(build_side));
         *out_factory = static_cast<OperatorFactory *>(f);
     });
+}
+
+// ---- join filter expressions
+namespace {
+namespace ex = omniruntime::expressions;
+}
+
+int32_t omg_expr_field(int32_t col, const OmgDataType *type, void **out_expr)
+{
+    return Guard([&] {
+        Require(type != nullptr && out_expr != nullptr && col >= 0, "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(new ex::FieldExpr(col, ToType(*type)));
+    });
+}
+
+int32_t omg_expr_literal_long(int64_t value, const OmgDataType *type, int32_t is_null, void **out_expr)
+{
+    return Guard([&] {
+        Require(type != nullptr && out_expr != nullptr, "invalid arguments");
+        auto *l = new ex::LiteralExpr(value, ToType(*type));
+        l->isNull = is_null != 0;
+        *out_expr = static_cast<ex::Expr *>(l);
+    });
+}
+
+int32_t omg_expr_literal_double(double value, int32_t is_null, void **out_expr)
+{
+    return Guard([&] {
+        Require(out_expr != nullptr, "invalid arguments");
+        auto *l = new ex::LiteralExpr(value, omniruntime::type::DoubleType());
+        l->isNull = is_null != 0;
+        *out_expr = static_cast<ex::Expr *>(l);
+    });
+}
+
+int32_t omg_expr_binary(int32_t op, void *left, void *right, void **out_expr)
+{
+    return Guard([&] {
+        Require(left != nullptr && right != nullptr && out_expr != nullptr && op >= 0 &&
+                op < static_cast<int32_t>(ex::Operator::INVALIDOP),
+            "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(new ex::BinaryExpr(static_cast<ex::Operator>(op),
+            static_cast<ex::Expr *>(left), static_cast<ex::Expr *>(right), omniruntime::type::BooleanType()));
+    });
+}
+
+int32_t omg_expr_unary(int32_t op, void *child, void **out_expr)
+{
+    return Guard([&] {
+        Require(child != nullptr && out_expr != nullptr && op >= 0 &&
+                op < static_cast<int32_t>(ex::Operator::INVALIDOP),
+            "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(new ex::UnaryExpr(static_cast<ex::Operator>(op),
+            static_cast<ex::Expr *>(child), omniruntime::type::BooleanType()));
+    });
+}
+
+int32_t omg_expr_is_null(void *child, void **out_expr)
+{
+    return Guard([&] {
+        Require(child != nullptr && out_expr != nullptr, "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(new ex::IsNullExpr(static_cast<ex::Expr *>(child)));
+    });
+}
+
+int32_t omg_expr_free(void *expr)
+{
+    delete static_cast<ex::Expr *>(expr);
+    return OMG_OK;
 }
 
 int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_probe_types,

@@ -7,6 +7,7 @@
 #include <memory>
 
 #include "host/gpu_runtime.h"
+#include "omniop/expressions.h"
 #include "kernels/join_part.h"
 #include "kernels/launch.h"
 
@@ -479,6 +480,137 @@ LookupJoinOperatorFactory::LookupJoinOperatorFactory(const DataTypes &probeTypes
     rowsPerBatch = GetMaxRowCount(rowSize);
 }
 
+namespace {
+using omniruntime::expressions::Expr;
+using omniruntime::expressions::ExprType;
+using ExprOp = omniruntime::expressions::Operator;
+
+// Value kind of a filter operand type: 0 integer-like (compared as int64), 1 double, -1 none.
+int FilterKind(const DataTypePtr &t)
+{
+    switch (t->GetId()) {
+        case OMNI_BYTE:
+        case OMNI_BOOLEAN:
+        case OMNI_SHORT:
+        case OMNI_INT:
+        case OMNI_DATE32:
+        case OMNI_LONG:
+        case OMNI_DATE64:
+        case OMNI_TIMESTAMP:
+            return 0;
+        case OMNI_DOUBLE:
+            return 1;
+        default:
+            return -1;
+    }
+}
+
+[[noreturn]] void FilterUnsupported(const std::string &what)
+{
+    throw OmniException("EXPRESSION_NOT_SUPPORT", "The expression is not supported yet: " + what, -2);
+}
+
+// Postfix code of `e`; `depth` is the evaluation stack depth before it.
+void CompileFilter(const Expr *e, const DataTypes &probeTypes, const DataTypes &buildTypes,
+    std::vector<omg::FilterInstr> &code, std::vector<int32_t> &cols, int depth)
+{
+    if (e == nullptr) {
+        FilterUnsupported("null node");
+    }
+    omg::FilterInstr in;
+    std::memset(&in, 0, sizeof(in));
+    auto push = [&](int32_t col) {
+        if (depth + 1 > omg::kMaxFilterDepth || code.size() >= static_cast<size_t>(omg::kMaxFilterInstrs)) {
+            FilterUnsupported("filter too large");
+        }
+        code.push_back(in);
+        cols.push_back(col);
+    };
+    auto emit = [&](int16_t op) {
+        if (code.size() >= static_cast<size_t>(omg::kMaxFilterInstrs)) {
+            FilterUnsupported("filter too large");
+        }
+        in.op = op;
+        code.push_back(in);
+        cols.push_back(-1);
+    };
+    switch (e->GetType()) {
+        case ExprType::FIELD_E: {
+            const auto *f = static_cast<const omniruntime::expressions::FieldExpr *>(e);
+            const int32_t nProbe = probeTypes.GetSize();
+            const bool probe = f->colVal < nProbe;
+            const int32_t c = probe ? f->colVal : f->colVal - nProbe;
+            if (f->colVal < 0 || (!probe && c >= buildTypes.GetSize())) {
+                throw OmniException("INVALID_ARGUMENT", "filter column out of range", -1);
+            }
+            const DataTypePtr &t = probe ? probeTypes.GetType(c) : buildTypes.GetType(c);
+            const int kind = FilterKind(t);
+            if (kind < 0) {
+                FilterUnsupported("column of type " + std::to_string(t->GetId()));
+            }
+            in.op = probe ? omg::FOP_PROBE_COL : omg::FOP_BUILD_COL;
+            in.width = static_cast<int16_t>(t->ByteWidth());
+            in.dbl = static_cast<int16_t>(kind);
+            push(c);
+            return;
+        }
+        case ExprType::LITERAL_E: {
+            const auto *l = static_cast<const omniruntime::expressions::LiteralExpr *>(e);
+            const int kind = FilterKind(l->dataType);
+            if (kind < 0) {
+                FilterUnsupported("literal of type " + std::to_string(l->dataType->GetId()));
+            }
+            in.op = omg::FOP_LITERAL;
+            in.dbl = static_cast<int16_t>(kind);
+            in.isNull = l->isNull ? 1 : 0;
+            if (kind == 1) {
+                std::memcpy(&in.imm, &l->doubleVal, sizeof(double));
+            } else {
+                in.imm = l->longVal;
+            }
+            push(-1);
+            return;
+        }
+        case ExprType::BINARY_E: {
+            const auto *b = static_cast<const omniruntime::expressions::BinaryExpr *>(e);
+            int16_t op;
+            switch (b->op) {
+                case ExprOp::EQ: op = omg::FOP_EQ; break;
+                case ExprOp::NEQ: op = omg::FOP_NEQ; break;
+                case ExprOp::LT: op = omg::FOP_LT; break;
+                case ExprOp::LTE: op = omg::FOP_LTE; break;
+                case ExprOp::GT: op = omg::FOP_GT; break;
+                case ExprOp::GTE: op = omg::FOP_GTE; break;
+                case ExprOp::AND: op = omg::FOP_AND; break;
+                case ExprOp::OR: op = omg::FOP_OR; break;
+                default: FilterUnsupported("binary operator " + std::to_string(static_cast<int>(b->op)));
+            }
+            CompileFilter(b->left, probeTypes, buildTypes, code, cols, depth);
+            CompileFilter(b->right, probeTypes, buildTypes, code, cols, depth + 1);
+            emit(op);
+            return;
+        }
+        case ExprType::UNARY_E: {
+            const auto *u = static_cast<const omniruntime::expressions::UnaryExpr *>(e);
+            if (u->op != ExprOp::NOT) {
+                FilterUnsupported("unary operator " + std::to_string(static_cast<int>(u->op)));
+            }
+            CompileFilter(u->exp, probeTypes, buildTypes, code, cols, depth);
+            emit(omg::FOP_NOT);
+            return;
+        }
+        case ExprType::IS_NULL_E: {
+            const auto *n = static_cast<const omniruntime::expressions::IsNullExpr *>(e);
+            CompileFilter(n->value, probeTypes, buildTypes, code, cols, depth);
+            emit(omg::FOP_IS_NULL);
+            return;
+        }
+        default:
+            FilterUnsupported("expression kind " + std::to_string(static_cast<int>(e->GetType())));
+    }
+}
+}  // namespace
+
 LookupJoinOperatorFactory *LookupJoinOperatorFactory::CreateLookupJoinOperatorFactory(const DataTypes &probeTypes,
     int32_t *probeOutputCols, int32_t probeOutputColsCount, int32_t *probeHashCols, int32_t probeHashColsCount,
     int32_t *buildOutputCols, int32_t buildOutputColsCount, const DataTypes &buildOutputTypes,
@@ -486,15 +618,22 @@ LookupJoinOperatorFactory *LookupJoinOperatorFactory::CreateLookupJoinOperatorFa
 {
     (void)isShuffleExchangeBuildPlan;
     (void)overflowConfig;
-    if (filterExpr != nullptr) {
-        throw OmniException("UNSUPPORTED_ERROR", "join filter expressions are not supported", -2);
-    }
     auto *builder = reinterpret_cast<HashBuilderOperatorFactory *>(hashBuilderFactoryAddr);
     if (builder == nullptr) {
         throw OmniException("INVALID_ARGUMENT", "null hash builder factory", -1);
     }
-    return new LookupJoinOperatorFactory(probeTypes, probeOutputCols, probeOutputColsCount, probeHashCols,
-        probeHashColsCount, buildOutputCols, buildOutputColsCount, buildOutputTypes, builder);
+    std::unique_ptr<LookupJoinOperatorFactory> f(new LookupJoinOperatorFactory(probeTypes, probeOutputCols,
+        probeOutputColsCount, probeHashCols, probeHashColsCount, buildOutputCols, buildOutputColsCount,
+        buildOutputTypes, builder));
+    if (filterExpr != nullptr) {
+        // JoinFilterCodeGen (lookup_join.cpp:175-187): compiled once per factory.
+        CompileFilter(static_cast<const Expr *>(filterExpr), probeTypes, f->build->buildTypes, f->filter,
+            f->filterCols, 0);
+        if (f->filter.empty()) {
+            FilterUnsupported("empty filter");
+        }
+    }
+    return f.release();
 }
 
 Operator *LookupJoinOperatorFactory::CreateOperator() { return new LookupJoinOperator(*this); }
@@ -576,6 +715,16 @@ void LookupJoinOperator::ProcessPending()
             inputCols.push_back(c);
         }
     }
+    for (size_t i = 0; i < f_.filter.size(); ++i) {
+        const int32_t c = f_.filterCols[i];
+        if (f_.filter[i].op == omg::FOP_PROBE_COL && inputOf.count(c) == 0) {
+            if (inputCols.size() >= static_cast<size_t>(omg::kMaxInputs)) {
+                throw OmniException("UNSUPPORTED_ERROR", "too many probe columns for the join kernels", -2);
+            }
+            inputOf[c] = static_cast<int32_t>(inputCols.size());
+            inputCols.push_back(c);
+        }
+    }
     omg::BatchTable bt;
     bt.Build(pending_, inputCols);
     bt.Upload(s);
@@ -602,6 +751,19 @@ void LookupJoinOperator::ProcessPending()
     p.table = b.table;
     p.joinKind = b.kind;
     p.visited = b.TracksVisits() ? b.visited.Get() : nullptr;
+    // Join filter: bind probe operands to kernel inputs and build operands to the build columns.
+    p.nFilter = static_cast<int32_t>(f_.filter.size());
+    for (size_t i = 0; i < f_.filter.size(); ++i) {
+        omg::FilterInstr in = f_.filter[i];
+        const int32_t c = f_.filterCols[i];
+        if (in.op == omg::FOP_PROBE_COL) {
+            in.input = inputOf[c];
+        } else if (in.op == omg::FOP_BUILD_COL) {
+            in.values = b.colValues[c].Get();
+            in.nulls = b.colHasNull[c] ? b.colNulls[c].Get() : nullptr;
+        }
+        p.filter[i] = in;
+    }
     const bool nullBuild = b.kind == omg::JOIN_KIND_PROBE_OUTER || b.kind == omg::JOIN_KIND_FULL ||
         b.kind == omg::JOIN_KIND_ANTI;  // rows without a match carry NULL build columns
     p.nOut = static_cast<int32_t>(nOut);
@@ -950,7 +1112,7 @@ bool LookupJoinOperator::ProcessPartitioned()
 {
     JoinBuildState &b = *f_.build;
     const int32_t keyCol = f_.probeHashCols[0];
-    if (!b.table.unique || b.table.keyWidth != 8 || f_.probeTypes.GetType(keyCol)->ByteWidth() != 8 ||
+    if (!f_.filter.empty() || !b.table.unique || b.table.keyWidth != 8 || f_.probeTypes.GetType(keyCol)->ByteWidth() != 8 ||
         b.kind != omg::JOIN_KIND_INNER || b.buildSide == OMNI_BUILD_LEFT || b.multiKey) {
         return false;
     }

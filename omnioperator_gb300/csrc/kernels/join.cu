@@ -806,6 +806,118 @@ __device__ __forceinline__ bool TupleEquals(const ProbeLaunch &p, const BatchDes
 // (by kind), the warp prefix-sums those counts, reserves its output range with one atomicAdd and
 // writes the rows in probe-row order.  BUILD_OUTER and FULL also mark every matched build row
 // visited (a plain byte store: every writer stores the same value).
+// One value of a filter operand: the raw bits (an int64, or a double's bits) and flags.
+constexpr uint32_t kFNull = 1;
+constexpr uint32_t kFDouble = 2;
+
+__device__ __forceinline__ double FilterAsDouble(uint64_t v, uint32_t fl)
+{
+    return (fl & kFDouble) ? __longlong_as_double(static_cast<long long>(v))
+                           : static_cast<double>(static_cast<int64_t>(v));
+}
+
+// The filter program over the candidate pair (probe row `row` of batch b, build row `br`).
+__device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br)
+{
+    uint64_t v[kMaxFilterDepth];
+    uint32_t fl[kMaxFilterDepth];
+    int sp = 0;
+    for (int i = 0; i < p.nFilter; ++i) {
+        const FilterInstr &f = p.filter[i];
+        const int op = f.op;
+        if (op == FOP_PROBE_COL || op == FOP_BUILD_COL || op == FOP_LITERAL) {
+            if (sp >= kMaxFilterDepth) {
+                return false;  // the host limits the depth; never taken
+            }
+            uint64_t bits = static_cast<uint64_t>(f.imm);
+            bool isNull = f.isNull != 0;
+            if (op != FOP_LITERAL) {
+                const void *col = op == FOP_PROBE_COL ? b.cols[f.input] : f.values;
+                const uint8_t *nulls = op == FOP_PROBE_COL ? b.nulls[f.input] : f.nulls;
+                const int64_t r = op == FOP_PROBE_COL ? row : br;
+                isNull = RowIsNullRO(nulls, r);
+                bits = isNull ? 0ull
+                              : (f.dbl ? static_cast<uint64_t>(LoadIntRO(col, r, 8))
+                                       : static_cast<uint64_t>(LoadIntRO(col, r, f.width)));
+            }
+            v[sp] = bits;
+            fl[sp] = (isNull ? kFNull : 0u) | (f.dbl ? kFDouble : 0u);
+            ++sp;
+            continue;
+        }
+        if (op == FOP_NOT || op == FOP_IS_NULL || op == FOP_IS_NOT_NULL) {
+            if (sp < 1) {
+                return false;
+            }
+            const bool n = (fl[sp - 1] & kFNull) != 0;
+            if (op == FOP_NOT) {
+                v[sp - 1] = n ? 0ull : (v[sp - 1] == 0 ? 1ull : 0ull);
+                fl[sp - 1] = n ? kFNull : 0u;
+            } else {
+                v[sp - 1] = (n == (op == FOP_IS_NULL)) ? 1ull : 0ull;
+                fl[sp - 1] = 0u;
+            }
+            continue;
+        }
+        if (sp < 2) {
+            return false;
+        }
+        const uint64_t bv = v[sp - 1];
+        const uint32_t bf = fl[sp - 1];
+        const uint64_t av = v[sp - 2];
+        const uint32_t af = fl[sp - 2];
+        --sp;
+        const bool an = (af & kFNull) != 0;
+        const bool bn = (bf & kFNull) != 0;
+        uint64_t res = 0;
+        bool resNull = false;
+        if (op == FOP_AND) {
+            const bool aFalse = !an && av == 0;
+            const bool bFalse = !bn && bv == 0;
+            resNull = !(aFalse || bFalse) && (an || bn);
+            res = (!aFalse && !bFalse && !resNull) ? 1ull : 0ull;
+        } else if (op == FOP_OR) {
+            const bool aTrue = !an && av != 0;
+            const bool bTrue = !bn && bv != 0;
+            resNull = !(aTrue || bTrue) && (an || bn);
+            res = (aTrue || bTrue) ? 1ull : 0ull;
+        } else if (an || bn) {
+            resNull = true;
+        } else {
+            int c;
+            if ((af | bf) & kFDouble) {
+                const double x = FilterAsDouble(av, af);
+                const double y = FilterAsDouble(bv, bf);
+                c = x < y ? -1 : (x > y ? 1 : (x == y ? 0 : 2));  // 2: unordered (NaN)
+            } else {
+                const int64_t x = static_cast<int64_t>(av);
+                const int64_t y = static_cast<int64_t>(bv);
+                c = x < y ? -1 : (x > y ? 1 : 0);
+            }
+            bool t = false;
+            switch (op) {
+                case FOP_EQ: t = c == 0; break;
+                case FOP_NEQ: t = c != 0; break;
+                case FOP_LT: t = c == -1; break;
+                case FOP_LTE: t = c == -1 || c == 0; break;
+                case FOP_GT: t = c == 1; break;
+                default: t = c == 1 || c == 0; break;  // FOP_GTE
+            }
+            res = t ? 1ull : 0ull;
+        }
+        v[sp - 1] = res;
+        fl[sp - 1] = resNull ? kFNull : 0u;
+    }
+    return sp == 1 && (fl[0] & kFNull) == 0 && v[0] != 0;
+}
+
+// A candidate build row counts as a match: equal key tuple (multi-column keys) and passing the
+// join filter (when there is one).
+__device__ __forceinline__ bool Accept(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br, bool multi)
+{
+    return (!multi || TupleEquals(p, b, row, br)) && (p.nFilter == 0 || FilterPasses(p, b, row, br));
+}
+
 __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_constant__ ProbeLaunch p)
 {
     const int lane = threadIdx.x & 31;
@@ -816,6 +928,7 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
         kind == JOIN_KIND_BUILD_OUTER || kind == JOIN_KIND_FULL;
     const bool unique = p.table.unique != 0;
     const bool multi = p.nKeyCols > 0;
+    const bool check = multi || p.nFilter > 0;  // candidates are tested one by one
     for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
         const TileDesc tile = p.tiles[t];
         const BatchDesc &b = p.batches[tile.batch];
@@ -835,17 +948,20 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
                     uint64_t h;
                     if (ProbeTupleHash(p, b, row, h)) {
                         m = Lookup(p.table, h);
-                        for (uint32_t k = 0; k < m.count; ++k) {
-                            const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
-                            nMatch += TupleEquals(p, b, row, br) ? 1u : 0u;
-                        }
                     }
                 } else {
                     key = LoadIntRO(keyCol, row, p.keyWidth);
                     if (!RowIsNullRO(keyNulls, row)) {
                         m = Lookup(p.table, static_cast<uint64_t>(key));
-                        nMatch = m.count;
                     }
+                }
+                if (check) {
+                    for (uint32_t k = 0; k < m.count; ++k) {
+                        const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
+                        nMatch += Accept(p, b, row, br, multi) ? 1u : 0u;
+                    }
+                } else {
+                    nMatch = m.count;
                 }
             }
             const bool matched = nMatch != 0;
@@ -870,7 +986,7 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
             if (p.visited != nullptr && matched) {
                 for (uint32_t k = 0; k < m.count; ++k) {
                     const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
-                    if ((!multi || TupleEquals(p, b, row, br)) && p.visited[br] == 0) {
+                    if ((!check || Accept(p, b, row, br, multi)) && p.visited[br] == 0) {
                         p.visited[br] = 1;
                     }
                 }
@@ -897,7 +1013,7 @@ __global__ void __launch_bounds__(kProbeThreads) ProbeKindKernel(const __grid_co
                 uint64_t j = at;
                 for (uint32_t k = 0; k < m.count && j < p.regionCap; ++k) {
                     const int64_t br = unique ? m.entry : __ldg(p.table.csrRows + m.entry + k);
-                    if (!multi || TupleEquals(p, b, row, br)) {
+                    if (!check || Accept(p, b, row, br, multi)) {
                         WriteJoinRow(p, b, row, key, br, regionBase + j);
                         ++j;
                     }
@@ -1411,7 +1527,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     if (p.nTiles <= 0) {
         return cudaSuccess;
     }
-    if (p.nKeyCols > 0) {
+    if (p.nKeyCols > 0 || p.nFilter > 0) {
         static int kindBlocks = 0;
         if (kindBlocks <= 0) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kindBlocks, ProbeKindKernel, kProbeThreads, 0);

@@ -340,6 +340,33 @@ struct JoinKeyCols {
     const int64_t *offs[kMaxJoinKeys];  // VARCHAR offsets
 };
 
+// Join filter (the LookupJoin filter expression, lookup_join.cpp:175-187,1440-1466) compiled to a
+// postfix program over one (probe row, build row) candidate pair.  Values are 64-bit integers or
+// doubles with a NULL flag; comparisons and NOT/AND/OR follow SQL three-valued logic, and a pair
+// passes when the program leaves TRUE (NULL fails).
+enum FilterOp : int16_t {
+    FOP_PROBE_COL = 0,  // push probe input `input` (width, dbl)
+    FOP_BUILD_COL,      // push build column values/nulls (width, dbl)
+    FOP_LITERAL,        // push imm (dbl: double bits), NULL when isNull
+    FOP_EQ, FOP_NEQ, FOP_LT, FOP_LTE, FOP_GT, FOP_GTE,
+    FOP_AND, FOP_OR, FOP_NOT,
+    FOP_IS_NULL, FOP_IS_NOT_NULL,
+};
+constexpr int kMaxFilterInstrs = 24;
+constexpr int kMaxFilterDepth = 8;
+
+struct FilterInstr {
+    int16_t op;
+    int16_t width;    // column value bytes (1, 2, 4, 8)
+    int16_t dbl;      // 1: the value is a double (columns: DOUBLE; literals: imm is double bits)
+    int16_t isNull;   // literals: NULL
+    int32_t input;    // FOP_PROBE_COL: probe kernel input index
+    int32_t pad;
+    const void *values;    // FOP_BUILD_COL: contiguous build column
+    const uint8_t *nulls;  // FOP_BUILD_COL: its NULL bitmap (may be null)
+    int64_t imm;
+};
+
 constexpr int kRegionStride = 16;  // counters 128 bytes apart
 constexpr int kMaxRegions = 16;
 
@@ -366,6 +393,8 @@ struct ProbeLaunch {
     uint8_t *visited;   // BUILD_OUTER / FULL: one byte per build row, set to 1 when matched
     int32_t nKeyCols;   // > 0: hashed multi-column key (keyInput unused, -1)
     JoinKeyCol keyCols[kMaxJoinKeys];
+    int32_t nFilter;    // > 0: candidate pairs must pass the filter program
+    FilterInstr filter[kMaxFilterInstrs];
 };
 
 }  // namespace omg

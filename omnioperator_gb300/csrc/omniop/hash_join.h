@@ -87,6 +87,11 @@ public:
     type::DataTypes buildOutputTypes;
     JoinBuildState *build;
     int32_t rowsPerBatch;
+    // Join filter compiled to a postfix program (empty: none).  Column operands are bound per
+    // probe call: filterCols[i] is the probe column (side 0) or build column (side 1) of
+    // instruction i, -1 for the others.
+    std::vector<omg::FilterInstr> filter;
+    std::vector<int32_t> filterCols;
     // Build output values packed per table slot, built by the first probe that can use it.
     mutable std::mutex payloadMu;
     mutable omg::BufferPtr slotPayload;

@@ -192,6 +192,44 @@ def join(kind, build_keys, build_nulls, probe_keys, probe_nulls):
         cap = n
 
 
+def join_filtered(kind, build_keys, build_nulls, probe_keys, probe_nulls, passes):
+    """join() with a join filter: a (probe, build) pair whose keys are equal counts as a match
+    only when passes(probe_rows, build_rows) (a vectorised predicate over pair arrays) is true.
+    Restates the reference's filtered probes (lookup_join.cpp:1037-1438, the filter evaluated
+    per candidate at :1440-1466; unmatched build rows, lookup_outer_join.cpp:173-374): inner
+    rows are the passing pairs; outer kinds add the probe (build) rows without a passing pair,
+    with -1 on the missing side; semi keeps probe rows with one, anti those without; existence
+    flags every probe row."""
+    pi, bi = join_inner(build_keys, build_nulls, probe_keys, probe_nulls)
+    ok = np.asarray(passes(pi, bi), dtype=bool) if len(pi) else np.zeros(0, bool)
+    pp, pb = pi[ok], bi[ok]
+    n_probe, n_build = len(probe_keys), len(build_keys)
+    probe_has = np.zeros(n_probe, bool)
+    probe_has[pp] = True
+    build_has = np.zeros(n_build, bool)
+    build_has[pb] = True
+    none_p = np.nonzero(~probe_has)[0]
+    none_b = np.nonzero(~build_has)[0]
+    neg_p = -np.ones(len(none_b), np.int64)
+    neg_b = -np.ones(len(none_p), np.int64)
+    if kind == "inner":
+        return pp, pb
+    if kind == "probe_outer":
+        return np.concatenate([pp, none_p]), np.concatenate([pb, neg_b])
+    if kind == "build_outer":
+        return np.concatenate([pp, neg_p]), np.concatenate([pb, none_b])
+    if kind == "full":
+        return np.concatenate([pp, none_p, neg_p]), np.concatenate([pb, neg_b, none_b])
+    if kind == "semi":
+        rows = np.nonzero(probe_has)[0]
+        return rows, -np.ones(len(rows), np.int64)
+    if kind == "anti":
+        return none_p, neg_b
+    if kind == "existence":
+        return np.arange(n_probe, dtype=np.int64), probe_has.astype(np.int64)
+    raise ValueError(kind)
+
+
 def exact_group_sums(group_ids: np.ndarray, values: np.ndarray, valid: np.ndarray | None, ngroups: int):
     """Correctly rounded per-group sums (math.fsum) and per-group sums of |x|, the reference
     values of the double tolerance."""

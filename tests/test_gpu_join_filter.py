@@ -1,0 +1,176 @@
+"""Join filters on the GPU: LookupJoin with a filter expression (lookup_join.cpp:175-187,
+1440-1466).  A candidate pair whose keys are equal is a match only when the filter, evaluated over
+the joined row (probe columns first, then build columns), is TRUE; NULL fails.  Every join kind
+must equal the oracle's filtered join (oracle.join_filtered) as an exact row multiset, and the
+reference's integer-filter join test must give its expected rows."""
+import numpy as np
+import pytest
+
+import omnioperator_gb300 as omg
+import oracle
+from helpers import split
+
+pytestmark = pytest.mark.gpu
+
+L, I, D = omg.LongType(), omg.IntType(), omg.DoubleType()
+F, B = omg.Field, omg.Binary
+
+
+def _rows(batches):
+    rows = []
+    for b in batches:
+        cols = omg.batch_to_numpy(b)
+        omg.free_batch(b)
+        n = len(cols[0][0]) if cols else 0
+        for i in range(n):
+            rows.append(tuple(None if m[i] else (float(v[i]) if isinstance(v[i], np.floating) else int(v[i]))
+                              for v, m in cols))
+    return rows
+
+
+def run(join_type, build_side, btypes, bcols, bmasks, ptypes, pcols, pmasks, pout, bout, filt,
+        batch_sizes=(1000,)):
+    """Build on two builder operators, probe in ragged batches, drain the outer-join operator."""
+    kind = oracle.join_kind(join_type, build_side)
+    bf = omg.HashBuilderOperatorFactory(oracle.JOIN_TYPES[join_type], btypes, [0], operator_count=2,
+                                        build_side=oracle.BUILD_SIDES[build_side])
+    ops = [bf.create_operator() for _ in range(2)]
+    nb = len(bcols[0])
+    for op, (s, e) in zip(ops, [(0, nb // 2), (nb // 2, nb)]):
+        op.add_input(omg.make_batch(btypes, [c[s:e] for c in bcols], [m[s:e] for m in bmasks]))
+    for op in ops:
+        op.get_output()
+    bo_types = [btypes[c] for c in bout]
+    pf = omg.LookupJoinOperatorFactory(ptypes, pout, [0], bout, bo_types, bf, filter_expr=filt)
+    pop = pf.create_operator()
+    outs = []
+    for s, e in split(len(pcols[0]), list(batch_sizes)):
+        pop.add_input(omg.make_batch(ptypes, [c[s:e] for c in pcols], [m[s:e] for m in pmasks]))
+        outs += pop.drain()
+    outs += pop.drain()
+    pop.delete()
+    rows = _rows(outs)
+    if kind in ("build_outer", "full"):
+        of = omg.LookupOuterJoinOperatorFactory(ptypes, pout, bout, bo_types, bf)
+        oop = of.create_operator()
+        rows += _rows(oop.drain())
+        oop.delete()
+        of.close()
+    for op in ops:
+        op.delete()
+    pf.close()
+    bf.close()
+    return rows
+
+
+def _key(r):
+    return tuple((x is None, 0 if x is None else x) for x in r)
+
+
+def test_reference_inner_join_with_int_filter():
+    """join_test.cpp:1545-1625 (TestInnerEqualityJoinWithIntFilter): build (int, int), probe
+    (int, int) with the probe's second column NULL at rows 4 and 9, filter #1 != #3; expected
+    rows (20, 35709, 20, 31904), (16, 35709, 16, 31904), (19, 35709, 19, 31904)."""
+    b0 = np.array([19, 14, 7, 19, 1, 20, 10, 13, 20, 16], dtype=np.int32)
+    b1 = np.array([35709, 31904, 35709, 31904, 35709, 31904, 35709, 31904, 35709, 31904], dtype=np.int32)
+    p0 = np.array([20, 16, 13, 4, 20, 4, 22, 19, 8, 7], dtype=np.int32)
+    p1 = np.array([35709, 35709, 31904, 12477, 31904, 38721, 90419, 35709, 88371, 35709], dtype=np.int32)
+    pm = np.array([i % 5 == 4 for i in range(10)])
+    none = np.zeros(10, bool)
+    filt = B(omg.EXPR_NEQ, F(1, I), F(3, I))
+    rows = run("INNER", "UNKNOWN", [I, I], [b0, b1], [none, none], [I, I], [p0, p1], [none, pm], [0, 1], [0, 1],
+               filt, batch_sizes=(10,))
+    assert sorted(rows) == sorted([(20, 35709, 20, 31904), (16, 35709, 16, 31904), (19, 35709, 19, 31904)])
+
+
+def _eval(e, pi, bi, pcols, pmasks, bcols, bmasks):
+    """(values, null mask, is_double) of expression `e` over candidate pairs, SQL three-valued."""
+    n_probe = len(pcols)
+    if isinstance(e, omg.Field):
+        probe = e.col < n_probe
+        c = e.col if probe else e.col - n_probe
+        rows = pi if probe else bi
+        col, m = (pcols[c], pmasks[c]) if probe else (bcols[c], bmasks[c])
+        return col[rows], m[rows].copy(), col.dtype.kind == "f"
+    if isinstance(e, omg.Literal):
+        dbl = e.dtype.id == omg.OMNI_DOUBLE
+        v = np.full(len(pi), float(e.value) if dbl else int(e.value), dtype=np.float64 if dbl else np.int64)
+        return v, np.full(len(pi), bool(e.is_null)), dbl
+    if isinstance(e, omg.Not):
+        v, m, _ = _eval(e.child, pi, bi, pcols, pmasks, bcols, bmasks)
+        return (v == 0).astype(np.int64), m, False
+    if isinstance(e, omg.IsNull):
+        _, m, _ = _eval(e.child, pi, bi, pcols, pmasks, bcols, bmasks)
+        return m.astype(np.int64), np.zeros(len(pi), bool), False
+    a, am, ad = _eval(e.left, pi, bi, pcols, pmasks, bcols, bmasks)
+    b, bm, bd = _eval(e.right, pi, bi, pcols, pmasks, bcols, bmasks)
+    if e.op == omg.EXPR_AND:
+        af, bf_ = ~am & (a == 0), ~bm & (b == 0)
+        null = ~(af | bf_) & (am | bm)
+        return (~af & ~bf_ & ~null).astype(np.int64), null, False
+    if e.op == omg.EXPR_OR:
+        at, bt = ~am & (a != 0), ~bm & (b != 0)
+        null = ~(at | bt) & (am | bm)
+        return (at | bt).astype(np.int64), null, False
+    if ad or bd:
+        a, b = a.astype(np.float64), b.astype(np.float64)
+    cmp = {omg.EXPR_EQ: a == b, omg.EXPR_NEQ: a != b, omg.EXPR_LT: a < b, omg.EXPR_LTE: a <= b,
+           omg.EXPR_GT: a > b, omg.EXPR_GTE: a >= b}[e.op]
+    return cmp.astype(np.int64), am | bm, False
+
+
+def _passes(e, pcols, pmasks, bcols, bmasks):
+    def f(pi, bi):
+        v, m, _ = _eval(e, pi, bi, pcols, pmasks, bcols, bmasks)
+        return (v != 0) & ~m
+    return f
+
+
+FILTERS = {
+    "int_lt": B(omg.EXPR_LT, F(1, L), F(4, L)),
+    "double_or_null": B(omg.EXPR_OR, B(omg.EXPR_GTE, F(2, D), F(5, D)), omg.IsNull(F(4, L))),
+    "not_eq_and_literal": B(omg.EXPR_AND, omg.Not(B(omg.EXPR_EQ, F(1, L), F(4, L))),
+                            B(omg.EXPR_GT, F(2, D), omg.Literal(0.25, D))),
+    "build_only_and_null_literal": B(omg.EXPR_OR, B(omg.EXPR_GTE, F(4, L), omg.Literal(0, L)),
+                                     B(omg.EXPR_EQ, F(1, L), omg.Literal(0, L, is_null=True))),
+}
+
+
+@pytest.mark.parametrize("join_type,build_side", [("INNER", "UNKNOWN"), ("LEFT", "UNKNOWN"), ("FULL", "UNKNOWN"),
+                                                  ("RIGHT", "RIGHT"), ("LEFT_SEMI", "UNKNOWN"),
+                                                  ("LEFT_ANTI", "UNKNOWN"), ("EXISTENCE", "UNKNOWN")])
+@pytest.mark.parametrize("fname", list(FILTERS))
+@pytest.mark.parametrize("unique", [True, False])
+def test_filtered_join_kinds_match_oracle(join_type, build_side, fname, unique):
+    rng = np.random.default_rng(len(join_type) * 13 + len(fname) + unique)
+    nb, npr = 3000, 20000
+    bkey = rng.permutation(nb).astype(np.int64) if unique else rng.integers(0, nb // 4, nb).astype(np.int64)
+    bv = rng.integers(-20, 20, nb).astype(np.int64)
+    bd = rng.random(nb)
+    bm = [rng.random(nb) < 0.03, rng.random(nb) < 0.1, rng.random(nb) < 0.1]
+    pkey = rng.integers(0, nb + nb // 5, npr).astype(np.int64)
+    pv = rng.integers(-20, 20, npr).astype(np.int64)
+    pd = rng.random(npr)
+    pm = [rng.random(npr) < 0.03, rng.random(npr) < 0.1, rng.random(npr) < 0.1]
+    bcols, pcols = [bkey, bv, bd], [pkey, pv, pd]
+    kind = oracle.join_kind(join_type, build_side)
+    pout = [0, 1, 2]
+    bout = [] if kind in ("semi", "anti", "existence") else [1, 2]
+    filt = FILTERS[fname]
+    got = run(join_type, build_side, [L, L, D], bcols, bm, [L, L, D], pcols, pm, pout, bout, filt,
+              batch_sizes=(1000, 4096, 777))
+    pi, bi = oracle.join_filtered(kind, bkey, bm[0], pkey, pm[0], _passes(filt, pcols, pm, bcols, bm))
+
+    def val(cols, masks, c, r):
+        if r < 0 or masks[c][r]:
+            return None
+        v = cols[c][r]
+        return float(v) if isinstance(v, np.floating) else int(v)
+
+    want = []
+    for i, j in zip(pi.tolist(), bi.tolist()):
+        r = [val(pcols, pm, c, i) for c in pout]
+        r += [j] if kind == "existence" else [val(bcols, bm, c, j) for c in bout]
+        want.append(tuple(r))
+    assert len(want) > 0
+    assert sorted(got, key=_key) == sorted(want, key=_key)

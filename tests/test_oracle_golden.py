@@ -180,3 +180,22 @@ def test_oracle_generic_sticky_overflow_is_order_dependent():
     _, _, vals, vn = oracle.hashagg([key], [oracle.T_LONG], [None], [agg], policy=0)
     assert not vn[0].any()            # Spark policy wraps: both groups sum to 0
     assert all(int(x) == 0 for x in vals[0])
+
+
+def test_filtered_join_restatement_reduces_to_the_plain_join():
+    """oracle.join_filtered with an always-true filter equals oracle.join for every kind, and
+    an always-false filter leaves no match (random keys with NULLs and duplicate build keys)."""
+    rng = np.random.default_rng(3)
+    bk = rng.integers(0, 50, 300).astype(np.int64)
+    bn = rng.random(300) < 0.05
+    pk = rng.integers(0, 80, 500).astype(np.int64)
+    pn = rng.random(500) < 0.05
+    for kind in oracle.JOIN_KINDS:
+        a = oracle.join(kind, bk, bn, pk, pn)
+        b = oracle.join_filtered(kind, bk, bn, pk, pn, lambda p, q: np.ones(len(p), bool))
+        assert sorted(zip(*[x.tolist() for x in a])) == sorted(zip(*[x.tolist() for x in b]))
+        none = oracle.join_filtered(kind, bk, bn, pk, pn, lambda p, q: np.zeros(len(p), bool))
+        if kind in ("inner", "semi"):
+            assert len(none[0]) == 0
+        if kind == "existence":
+            assert not none[1].any()
