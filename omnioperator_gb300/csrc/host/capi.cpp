@@ -943,11 +943,16 @@ int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const 
         SetError("not a hash aggregation factory");
         return OMG_ERR_INVALID_ARG;
     }
+    const auto &ap = f->Plan();
+    if (!ap.dictInputs.empty() || !ap.varlenInputs.empty()) {
+        // String columns need the operator's per-call string dictionary (device allocations).
+        SetError("VARCHAR/CHAR columns are not supported by the allocation-free entry point");
+        return OMG_ERR_UNSUPPORTED;
+    }
     if (!omg::DeviceAvailable()) {
         SetError("no CUDA device is available");
         return OMG_ERR_NO_DEVICE;
     }
-    const auto &ap = f->Plan();
     omg::NoAllocPlan np;
     np.nInputs = static_cast<int32_t>(ap.inputCols.size());
     for (int32_t i = 0; i < np.nInputs; ++i) {

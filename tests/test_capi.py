@@ -215,3 +215,12 @@ def test_dictionary_vectors_on_the_host():
         assert ei.value.status == -1
     L.omg_vec_free(d)
     L.omg_vec_free(v)
+
+
+def test_noalloc_entry_refuses_string_columns_before_touching_a_device():
+    V, L = omg.VarcharType(8), omg.LongType()
+    f = omg.HashAggregationOperatorFactory([0], [V], [[1]], [[L]], [[L]], [omg.OMNI_AGGREGATION_TYPE_SUM])
+    n = C.c_int64(0)
+    rc = omg.lib().omg_hashagg_run_noalloc(f.handle, None, None, 0, 0, None, None, 0, 16, C.byref(n), None)
+    assert rc == -2
+    f.close()
