@@ -358,6 +358,10 @@ BatchedAggregation::BatchedAggregation(HashAggregationOperatorFactory &factory, 
         throw OmniException("UNSUPPORTED_ERROR",
             "batched aggregation does not run plans with sticky-overflow sums; use one operator per task", -2);
     }
+    if (!impl_->plan.dictInputs.empty() || !impl_->plan.varlenInputs.empty()) {
+        throw OmniException("UNSUPPORTED_ERROR",
+            "batched aggregation does not run plans with VARCHAR/CHAR columns; use one operator per task", -2);
+    }
     if (sizer != nullptr && sizer->Dims()[0] != omg::kSizerFeatures) {
         throw OmniException("INVALID_ARGUMENT", "sizing model input width must be 12", -1);
     }

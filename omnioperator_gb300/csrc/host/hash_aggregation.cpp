@@ -429,6 +429,19 @@ OmniStatus HashAggregationOperatorFactory::Init()
                     o.kind = isMin ? omg::OUT_MIN_DOUBLE : omg::OUT_MAX_DOUBLE;
                     o.src = static_cast<int16_t>(accFor(isMin ? omg::ACC_DMIN : omg::ACC_DMAX, input, inKind, inW,
                         OrderedBits(isMin ? lim : -lim)));
+                } else if (IsVarlen(inId)) {
+                    // MIN/MAX of VARCHAR (min_aggregator.cpp / max_aggregator.cpp over string_view):
+                    // the input is read as its string dictionary ids and the state keeps the id of
+                    // the least / greatest string, compared byte-wise on the device.
+                    p.inputWidths[input] = std::max(p.inputWidths[input], 4);
+                    if (std::find(p.dictInputs.begin(), p.dictInputs.end(), input) == p.dictInputs.end()) {
+                        p.dictInputs.push_back(input);
+                    }
+                    o.kind = omg::OUT_STR_ID;
+                    o.src = static_cast<int16_t>(
+                        accFor(isMin ? omg::ACC_SMIN : omg::ACC_SMAX, input, omg::IN_INT, 4, -1));
+                    o.outWidth = 4;
+                    rowBytes += VarlenRowBytes(outT) - o.outWidth;
                 } else {
                     throw OmniException("UNSUPPORTED_ERROR", "unsupported MIN/MAX input type " + std::to_string(inId), -2);
                 }
@@ -982,6 +995,17 @@ DevArray<int32_t> DictEncode(StringDict &d, omg::BatchTable &bt, int32_t input, 
 }
 }  // namespace
 
+// The string dictionaries SMIN/SMAX compare through (their arenas move when they grow, so a
+// launch binds them after the batch set was encoded).
+void HashAggregationOperator::BindStrings(omg::AggLaunch &p) const
+{
+    const Impl &im = *impl_;
+    for (size_t j = 0; j < plan_.dictInputs.size() && j < im.dicts.size(); ++j) {
+        p.strOff[plan_.dictInputs[j]] = im.dicts[j].arenaOff.Get();
+        p.strChars[plan_.dictInputs[j]] = im.dicts[j].arena.Get();
+    }
+}
+
 // VARCHAR/CHAR inputs of a batch set: group-by columns become dictionary ids, COUNT-only
 // columns a zero byte per row (their NULL bitmaps stay the batches' own); the batch
 // descriptors are uploaded again.
@@ -1070,6 +1094,7 @@ void HashAggregationOperator::Flush()
     DevArray<unsigned long long> retryA(static_cast<size_t>(rows), s);
     DevArray<unsigned long long> retryB;
     omg::AggLaunch p = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
+    BindStrings(p);
     p.batches = bt.DeviceBatches();
     p.tiles = bt.DeviceTiles();
     p.nTiles = bt.NumTiles();
@@ -1123,6 +1148,7 @@ void HashAggregationOperator::Flush()
         spillB.Reset(std::max<uint64_t>(nSpillH, 1) * plan_.slotWords, s);
         CudaCheck(cudaMemsetAsync(im.stats.Get() + 1, 0, 3 * sizeof(unsigned long long), s), "reset stats");
         omg::AggLaunch r = MakeLaunch(plan_, im.slots.Get(), im.capacity, im.special.Get(), im.stats.Get());
+        BindStrings(r);
         r.batches = rowBatches;
         r.retry = retryB.Get();
         r.retryCap = static_cast<uint32_t>(std::max<uint64_t>(nRetry, 1));
@@ -1175,17 +1201,17 @@ void HashAggregationOperator::Flush()
     }
 }
 
-// VARCHAR/CHAR key columns of the extracted groups: dictionary ids back to strings (lengths,
-// a scan to offsets, then the characters), on the device.
+// VARCHAR/CHAR key and MIN/MAX columns of the extracted groups: dictionary ids back to strings
+// (lengths, a scan to offsets, then the characters), on the device.
 void HashAggregationOperator::DecodeStrings(std::vector<omg::OutColumn> &cols, int64_t rows, cudaStream_t s)
 {
     Impl &im = *impl_;
     for (size_t o = 0; o < plan_.outs.size(); ++o) {
         const OutSpec &os = plan_.outs[o];
-        if (os.kind != omg::OUT_KEY || !IsVarlen(plan_.outTypes[o]->GetId())) {
+        if ((os.kind != omg::OUT_KEY && os.kind != omg::OUT_STR_ID) || !IsVarlen(plan_.outTypes[o]->GetId())) {
             continue;
         }
-        const int32_t input = plan_.key.cols[os.src].input;
+        const int32_t input = os.kind == omg::OUT_KEY ? plan_.key.cols[os.src].input : plan_.accs[os.src].input;
         const size_t j = static_cast<size_t>(
             std::find(plan_.dictInputs.begin(), plan_.dictInputs.end(), input) - plan_.dictInputs.begin());
         StringDict &d = im.dicts.at(j);
@@ -1294,6 +1320,7 @@ void HashAggregationOperator::Extract()
         bt.Upload(s);
         DevArray<uint8_t> forced(im.capacity + 2, s, true);
         omg::AggLaunch p = base;
+        BindStrings(p);
         p.batches = bt.DeviceBatches();
         CudaCheck(omg::LaunchAggOrdered(p, static_cast<int32_t>(im.retained.size()), e, ambSlots.Get(),
                       static_cast<uint32_t>(hc[2]), forced.Get(), s),

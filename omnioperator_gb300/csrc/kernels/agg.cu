@@ -155,6 +155,50 @@ __device__ __forceinline__ void Red(uint64_t *w, uint64_t v)
     }
 }
 
+// ------------------------------------------------------------------ VARCHAR min / max
+// Order of the strings of dictionary ids a and b of input `input`: bytes compared as unsigned,
+// a proper prefix first (std::string_view::compare, as the reference's MIN/MAX of VARCHAR).
+__device__ __forceinline__ int CompareDictStrings(const AggLaunch &p, int input, int64_t a, int64_t b)
+{
+    const int64_t *off = p.strOff[input];
+    const uint8_t *chars = p.strChars[input];
+    const int64_t la = off[a + 1] - off[a];
+    const int64_t lb = off[b + 1] - off[b];
+    const uint8_t *x = chars + off[a];
+    const uint8_t *y = chars + off[b];
+    const int64_t n = la < lb ? la : lb;
+    for (int64_t i = 0; i < n; ++i) {
+        if (x[i] != y[i]) {
+            return x[i] < y[i] ? -1 : 1;
+        }
+    }
+    return la < lb ? -1 : (la > lb ? 1 : 0);
+}
+
+// Lock-free min / max of dictionary ids by their strings: a CAS succeeds only with a strictly
+// better string, so every retry follows another thread's improvement and the loop ends.
+__device__ __forceinline__ void AtomicStrMinMax(const AggLaunch &p, int input, uint64_t *w, int64_t id, bool isMin)
+{
+    unsigned long long *a = reinterpret_cast<unsigned long long *>(w);
+    unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(a);
+    while (true) {
+        if (static_cast<int64_t>(cur) >= 0) {
+            if (static_cast<int64_t>(cur) == id) {
+                return;
+            }
+            const int c = CompareDictStrings(p, input, id, static_cast<int64_t>(cur));
+            if (isMin ? c >= 0 : c <= 0) {
+                return;
+            }
+        }
+        const unsigned long long prev = atomicCAS(a, cur, static_cast<unsigned long long>(id));
+        if (prev == cur) {
+            return;
+        }
+        cur = prev;
+    }
+}
+
 // ------------------------------------------------------------------ state updates
 // `st` points at the group's state words, in shared or global memory.
 __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc &b, int64_t row, const RowIn &in,
@@ -228,6 +272,10 @@ __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc
                 }
                 break;
             }
+            case ACC_SMIN:
+            case ACC_SMAX:
+                AtomicStrMinMax(p, s.input, w, AccInt(s, b, row, in), s.kind == ACC_SMIN);
+                break;
             default:
                 break;
         }
@@ -235,7 +283,8 @@ __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc
 }
 
 // Merge a partial state (shared table entry or spilled record) into `dst`.
-__device__ __forceinline__ void MergeStates(const AccSpec *accs, int nAccs, const uint64_t *src, uint64_t *dst)
+__device__ __forceinline__ void MergeStates(const AggLaunch &p, const AccSpec *accs, int nAccs, const uint64_t *src,
+    uint64_t *dst)
 {
     for (int a = 0; a < nAccs; ++a) {
         const AccSpec &s = accs[a];
@@ -274,6 +323,12 @@ __device__ __forceinline__ void MergeStates(const AccSpec *accs, int nAccs, cons
             case ACC_DMAX:
                 if (static_cast<int64_t>(v[0]) != s.init) {
                     AtomicMaxI64(w, static_cast<int64_t>(v[0]));
+                }
+                break;
+            case ACC_SMIN:
+            case ACC_SMAX:
+                if (static_cast<int64_t>(v[0]) >= 0) {
+                    AtomicStrMinMax(p, s.input, w, static_cast<int64_t>(v[0]), s.kind == ACC_SMIN);
                 }
                 break;
             default:
@@ -524,7 +579,7 @@ __device__ __forceinline__ void MergeRecord(const AggLaunch &p, const SpillArgs 
     if (inserted) {
         atomicAdd(newGroups, 1u);
     }
-    MergeStates(p.accs, p.nAccs, rec + kw, p.table.slots + g * sw + kw);
+    MergeStates(p, p.accs, p.nAccs, rec + kw, p.table.slots + g * sw + kw);
 }
 
 // ------------------------------------------------------------------ partitioned tiles
@@ -697,6 +752,17 @@ __device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batc
                     Red(side + 1, lo >> 32);
                     Red(side + 2, hi & 0xffffffffull);
                     Red(side + 3, hi >> 32);
+                }
+                break;
+            case ACC_SMIN:
+            case ACC_SMAX:
+#pragma unroll
+                for (int k = 0; k < kPartRows; ++k) {
+                    const int64_t row = row0 + k * 1024;
+                    if (slot[k] < 0 || NullRO(nulls, row)) {
+                        continue;
+                    }
+                    AtomicStrMinMax(p, s.input, st + slot[k] * sw + s.word, LoadIntW<4>(col, row), s.kind == ACC_SMIN);
                 }
                 break;
             default:
@@ -1159,6 +1225,7 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
             case OUT_SUM_WRAP:
             case OUT_MIN_INT:
             case OUT_MAX_INT:
+            case OUT_STR_ID:  // a dictionary id; the host turns it back into the string
                 StoreWidth(os.values, pos, os.outWidth, w[0]);
                 break;
             case OUT_SUM_DOUBLE:

@@ -67,6 +67,7 @@ struct KeySpec {
 //  DSUM       compensated double sum (s, c)              2 words
 //  IMIN/IMAX  int64 min / max                            1 word
 //  DMIN/DMAX  double min / max as order-preserving int64 1 word
+//  SMIN/SMAX  VARCHAR min / max: the string dictionary id 1 word (-1: no value yet)
 // WSUM keeps the positive and the negative values apart, each as sums of 32-bit chunks: word k
 // of a side accumulates bits [32k, 32k+32) of every magnitude.  A word therefore never carries
 // for fewer than 2^32 rows per group, every update is a fire-and-forget atomic add, the exact
@@ -82,6 +83,8 @@ enum AccKind : int16_t {
     ACC_IMAX = 7,
     ACC_DMIN = 8,
     ACC_DMAX = 9,
+    ACC_SMIN = 10,
+    ACC_SMAX = 11,
 };
 
 struct AccSpec {
@@ -161,6 +164,10 @@ struct AggLaunch {
     // task whose group does not fit sets taskFailed[i] (the host re-runs it exactly).
     const AggTable *taskTables;
     uint32_t *taskFailed;
+    // VARCHAR inputs aggregated by SMIN/SMAX: the input's string dictionary (id k's characters
+    // are strChars[strOff[k], strOff[k + 1])), for comparing two ids' strings.
+    const int64_t *strOff[kMaxInputs];
+    const uint8_t *strChars[kMaxInputs];
 };
 
 constexpr int kTaskSketchRows = 1024;   // rows sampled per task by the batched sketch
@@ -213,6 +220,7 @@ enum OutKind : int16_t {
                                // (count: COUNT_ALL - NULLS(countAcc), or the ISUM countAcc when
                                // boundKind == 1)
     OUT_AVG_MERGE = 12,        // final AVG: sum (acc src, DSUM) / count (acc countAcc, ISUM), NULL if 0
+    OUT_STR_ID = 13,           // VARCHAR MIN/MAX: the dictionary id (int32) of acc src, NULL if none
 };
 
 struct OutSpec {

@@ -131,6 +131,7 @@ private:
     void Partition(omg::BatchTable &bt, omg::AggLaunch &p, PartBuffers &pb, cudaStream_t s);
     void Flush();
     void EncodeStrings(omg::BatchTable &bt, cudaStream_t s);
+    void BindStrings(omg::AggLaunch &p) const;
     void DecodeStrings(std::vector<omg::OutColumn> &cols, int64_t rows, cudaStream_t s);
     void Extract();
     void ReleasePending();

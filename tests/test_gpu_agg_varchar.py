@@ -8,8 +8,9 @@ each distinct string replaced by a distinct int64 (a bijection), which gives the
 GPU output keys are mapped back through the same table.  Integer results bit-exact, double
 SUM/AVG within 1e-12 * max(|exact|, sum|x|) of the correctly rounded sum.
 
-Known answers: the COUNT part of the reference's VARCHAR and CHAR group-by tests
-(aggregation_test.cpp:1195-1283).  MIN/MAX of VARCHAR values is not supported and is refused."""
+Known answers: the reference's VARCHAR and CHAR group-by tests (aggregation_test.cpp:1195-1283)
+and its two-stage MIN/MAX of VARCHAR tests (:1664-1737, :1806-1890).  MIN/MAX of VARCHAR values
+compare bytes as unsigned, a proper prefix first."""
 import numpy as np
 import pytest
 
@@ -120,11 +121,80 @@ def test_reference_varchar_group_by_count(key_type):
     assert _count_rows(cols) == {b"0": 3, b"1": 3, b"2": 2}
 
 
-def test_varchar_min_max_values_refused():
-    """MIN/MAX of VARCHAR values (the rest of the reference test above) is not supported."""
-    with pytest.raises(omg.OmgError) as ei:
-        omg.HashAggregationOperatorFactory([0], [V], [[1]], [[V]], [[V]], [MIN]).create_operator()
-    assert ei.value.status == -2
+def _str_rows(cols, nkeys):
+    """{key tuple: value tuple} with strings as bytes, NULL as None."""
+    def v(col, m, i):
+        return None if m[i] else (bytes(col[i]) if isinstance(col[i], (bytes, bytearray)) else int(col[i]))
+    n = len(cols[0][0])
+    return {tuple(v(c, m, i) for c, m in cols[:nkeys]): tuple(v(c, m, i) for c, m in cols[nkeys:])
+            for i in range(n)}
+
+
+def test_reference_varchar_group_by_count_min_max():
+    """aggregation_test.cpp:1195-1240 in full: group by VARCHAR(1), COUNT(VARCHAR(1)),
+    MIN(VARCHAR(1)), MAX(VARCHAR(4)) -> ("0", 3, "0", "6.6"), ("1", 3, "1", "5.5"), ("2", 2, "2", "4.4")."""
+    d0 = np.array([b"0", b"1", b"2", b"0", b"1", b"2", b"0", b"1"], dtype=object)
+    d3 = np.array([b"6.6", b"5.5", b"4.4", b"3.3", b"2.2", b"1.1", b"1.1", b"1"], dtype=object)
+    V1, V4 = omg.VarcharType(1), omg.VarcharType(4)
+    cols, _ = run_agg([0], [V1], [[1], [2], [3]], [[V1], [V1], [V4]], [[L], [V1], [V4]], [CNT, MIN, MAX],
+                      [d0, d0.copy(), d0.copy(), d3], [V1, V1, V1, V4])
+    assert _str_rows(cols, 1) == {(b"0",): (3, b"0", b"6.6"), (b"1",): (3, b"1", b"5.5"),
+                                  (b"2",): (2, b"2", b"4.4")}
+
+
+def _two_stage_no_group(data, masks, funcs):
+    """The reference's partial -> final MIN/MAX tests without group-by columns, in flat form:
+    a constant group-by column stands in for the non-grouped aggregation."""
+    n = len(data[0])
+    k = np.zeros(n, dtype=np.int64)
+    T = omg.VarcharType(100)
+    m = len(data)
+    pf = omg.HashAggregationOperatorFactory([0], [L], [[i + 1] for i in range(m)], [[T]] * m, [[T]] * m, funcs,
+                                            output_partials=[True] * m)
+    op = pf.create_operator()
+    op.add_input(omg.make_batch([L] + [T] * m, [k] + list(data), [None] + list(masks)))
+    partial = op.drain()
+    op.delete()
+    pf.close()
+    ff = omg.HashAggregationOperatorFactory([0], [L], [[i + 1] for i in range(m)], [[T]] * m, [[T]] * m, funcs,
+                                            input_raws=[False] * m)
+    op = ff.create_operator()
+    for b in partial:
+        op.add_input(b)
+    outs = op.drain()
+    op.delete()
+    ff.close()
+    assert len(outs) == 1
+    cols = omg.batch_to_numpy(outs[0])
+    omg.free_batch(outs[0])
+    return _str_rows(cols, 1)[(0,)]
+
+
+def test_reference_min_max_varchar_two_stage():
+    """aggregation_test.cpp:1664-1737 (min_max_varchar): MIN over a column NULL at rows 1 and 4,
+    MAX over one NULL at rows 0 and 3 -> the Aaron.Anderson and Zulma.Carter strings."""
+    d0 = np.array([b"Zulma.Carter@MfvjVN43Udd95KeZ.com", b"*", b"Aaron.Anderson@0CQ4QUkBY2Q.edu",
+                   b"Zulema.Ruiz@J2XvbX7.com", b"*", b"Aaron.Artis@bv.org"], dtype=object)
+    d1 = np.array([b"*", b"Zulma.Carter@MfvjVN43Udd95KeZ.com", b"Aaron.Anderson@0CQ4QUkBY2Q.edu", b"*",
+                   b"Zulema.Ruiz@J2XvbX7.com", b"Aaron.Artis@bv.org"], dtype=object)
+    m0 = np.array([0, 1, 0, 0, 1, 0], bool)
+    m1 = np.array([1, 0, 0, 1, 0, 0], bool)
+    got = _two_stage_no_group([d0, d1], [m0, m1], [MIN, MAX])
+    assert got == (b"Aaron.Anderson@0CQ4QUkBY2Q.edu", b"Zulma.Carter@MfvjVN43Udd95KeZ.com")
+
+
+def test_reference_min_max_varchar_mix_with_nulls():
+    """aggregation_test.cpp:1806-1890: MAX, MAX, MIN, MIN over columns with empty strings, the
+    first two NULL at rows 4-5 and the last two at rows 0-1 -> ("", "Zulma.Carter...", "", "")."""
+    e = np.array([b""] * 6, dtype=object)
+    d2 = np.array([b"Zulma.Carter@MfvjVN43Udd95KeZ.com", b"*", b"", b"Zulema.Ruiz@J2XvbX7.com", b"*", b""],
+                  dtype=object)
+    d4 = np.array([b"*", b"", b"Aaron.Anderson@0CQ4QUkBY2Q.edu", b"", b"Zulema.R", b"Aaron.Artis@bv.org"],
+                  dtype=object)
+    a = np.array([0, 0, 0, 0, 1, 1], bool)
+    b = np.array([1, 1, 0, 0, 0, 0], bool)
+    got = _two_stage_no_group([e, d2, e.copy(), d4], [a, a, b, b], [MAX, MAX, MIN, MIN])
+    assert got == (b"", b"Zulma.Carter@MfvjVN43Udd95KeZ.com", b"", b"")
 
 
 def test_empty_string_null_and_prefixes_are_distinct_groups():
@@ -275,3 +345,42 @@ def test_high_cardinality_strings():
     keys = _strings(rng, n, 600_000, max_len=24)
     km = rng.random(n) < 0.01
     _check([keys], [V], [km], *_values(rng, n), batch_sizes=(4096,), device_input=True)
+
+
+def _expected_min_max(keys, kmask, vals, vmask):
+    want = {}
+    for k, km, v, vm in zip(keys.tolist(), kmask.tolist(), vals, vmask.tolist()):
+        g = (None if km else int(k),)
+        lo, hi, c = want.get(g, (None, None, 0))
+        if not vm:
+            b = bytes(v)
+            lo = b if lo is None or b < lo else lo
+            hi = b if hi is None or b > hi else hi
+            c += 1
+        want[g] = (lo, hi, c)
+    return want
+
+
+@pytest.mark.parametrize("strategy", [omg.AGG_STRATEGY_AUTO, omg.AGG_STRATEGY_GLOBAL, omg.AGG_STRATEGY_SMEM,
+                                      omg.AGG_STRATEGY_PARTITIONED])
+@pytest.mark.parametrize("flush_rows", [0, 9000])
+def test_varchar_min_max_match_python(strategy, flush_rows):
+    """MIN and MAX of a VARCHAR column (with NULLs, empty strings, shared prefixes and bytes above
+    0x7f) per int64 group, against byte-wise comparison; small flushes make later batch sets
+    compare new strings with ids stored by earlier ones."""
+    rng = np.random.default_rng(31 + strategy + flush_rows)
+    n = 150_000
+    pool = [bytes(rng.integers(0, 256, l, dtype=np.uint8)) for l in rng.integers(0, 12, 3000)]
+    pool += [b"", b"a", b"ab", b"abc", b"\xff", b"\xff\x00"]
+    vals = np.array([pool[i] for i in rng.integers(0, len(pool), n)], dtype=object)
+    vm = rng.random(n) < 0.05
+    keys = rng.integers(0, 700, n).astype(np.int64)
+    km = rng.random(n) < 0.01
+    if flush_rows:
+        omg.lib().omg_debug_set_agg_flush_rows(flush_rows)
+    try:
+        cols, _ = run_agg([0], [L], [[1], [1], [1]], [[V], [V], [V]], [[V], [V], [L]], [MIN, MAX, CNT],
+                          [keys, vals], [L, V], nulls=[km, vm], batch_sizes=(4096, 1003), strategy=strategy)
+    finally:
+        omg.lib().omg_debug_set_agg_flush_rows(0)
+    assert _str_rows(cols, 1) == _expected_min_max(keys, km, vals, vm)
