@@ -373,6 +373,14 @@ int32_t omg_op_set_stream(void *op, void *stream);
 int32_t omg_op_set_device_output(void *op, int32_t on);
 /* Aggregation: strategy hint and initial global-table capacity (groups); 0 = automatic. */
 int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hint);
+/* Aggregation spill (SpillConfig, core/src/operator/config/operator_config.h:28-100): with
+ * enabled != 0 the operator stages its input until GetOutput and, when the estimated group table
+ * would exceed device_budget_bytes, hash-partitions the rows into pinned host memory and
+ * aggregates one partition at a time.  Call before the first AddInput.  Plans with VARCHAR/CHAR
+ * columns or order-dependent sticky-overflow sums return OMG_ERR_UNSUPPORTED. */
+int32_t omg_op_set_spill(void *op, int32_t enabled, int64_t device_budget_bytes);
+/* Operator::GetSpilledBytes (core/src/operator/operator.h:66): bytes moved to host memory. */
+int64_t omg_op_spilled_bytes(void *op);
 /* Counters of the last run: [0]=kernel launches, [1]=table resizes, [2]=retried rows,
  * [3]=groups, [4]=ordered-fallback groups, [5]=output rows. */
 int32_t omg_op_get_counters(void *op, int64_t *out, int32_t n);

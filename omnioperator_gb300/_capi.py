@@ -111,6 +111,8 @@ _SIGS = {
     "omg_op_set_stream": (I32, [P, P]),
     "omg_op_set_device_output": (I32, [P, I32]),
     "omg_op_set_agg_strategy": (I32, [P, I32, I64]),
+    "omg_op_set_spill": (I32, [P, I32, I64]),
+    "omg_op_spilled_bytes": (I64, [P]),
     "omg_op_get_counters": (I32, [P, C.POINTER(I64), I32]),
     "omg_hashagg_run_noalloc": (I32, [P, P, P, I32, I64, P, P, I32, I64, C.POINTER(I64), P]),
 }

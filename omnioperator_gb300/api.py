@@ -385,6 +385,13 @@ class Operator:
     def set_agg_strategy(self, strategy: int, capacity_hint: int = 0):
         check(lib().omg_op_set_agg_strategy(self.handle, strategy, capacity_hint))
 
+    def set_spill(self, enabled: bool, device_budget_bytes: int = 0):
+        """Aggregation spill to pinned host memory above a device-memory budget."""
+        check(lib().omg_op_set_spill(self.handle, 1 if enabled else 0, device_budget_bytes))
+
+    def spilled_bytes(self) -> int:
+        return lib().omg_op_spilled_bytes(self.handle)
+
     def counters(self):
         arr = (C.c_int64 * 8)()
         check(lib().omg_op_get_counters(self.handle, arr, 8))

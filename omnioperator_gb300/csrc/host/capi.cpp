@@ -933,6 +933,21 @@ int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hin
     });
 }
 
+int32_t omg_op_set_spill(void *op, int32_t enabled, int64_t device_budget_bytes)
+{
+    return Guard([&] {
+        auto *a = dynamic_cast<HashAggregationOperator *>(AsOp(op));
+        Require(a != nullptr, "not a hash aggregation operator");
+        Require(device_budget_bytes >= 0, "invalid budget");
+        a->SetSpill(enabled != 0, static_cast<uint64_t>(device_budget_bytes));
+    });
+}
+
+int64_t omg_op_spilled_bytes(void *op)
+{
+    return op ? static_cast<int64_t>(AsOp(op)->GetSpilledBytes()) : -1;
+}
+
 int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const uint8_t *const *d_nulls,
     int32_t n_cols, int64_t n_rows, void *const *d_out_values, uint8_t *const *d_out_nulls, int32_t n_out,
     int64_t max_groups, int64_t *num_groups, void *stream)

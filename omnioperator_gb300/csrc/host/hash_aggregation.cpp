@@ -658,7 +658,7 @@ int32_t HashAggregationOperator::AddInput(VectorBatch *vecBatch)
     omg::FlattenTaken(vecBatch);  // dictionary-encoded vectors -> flat device vectors
     pending_.push_back(vecBatch);
     pendingRows_ += vecBatch->GetRowCount();
-    if (pendingRows_ >= omg::AggFlushRows()) {
+    if (!spillEnabled_ && pendingRows_ >= omg::AggFlushRows()) {
         Flush();
     }
     return 0;
@@ -1238,8 +1238,204 @@ void HashAggregationOperator::DecodeStrings(std::vector<omg::OutColumn> &cols, i
     }
 }
 
+void HashAggregationOperator::SetSpill(bool enabled, uint64_t deviceBudgetBytes)
+{
+    if (enabled && (!plan_.dictInputs.empty() || !plan_.varlenInputs.empty() || plan_.orderDependent)) {
+        throw OmniException("UNSUPPORTED_ERROR",
+            "spill does not take plans with VARCHAR/CHAR columns or order-dependent sticky-overflow sums", -2);
+    }
+    if (enabled && deviceBudgetBytes == 0) {
+        throw OmniException("INVALID_ARGUMENT", "spill needs a device memory budget", -1);
+    }
+    if (enabled && impl_->capacity != 0) {
+        throw OmniException("OPERATOR_RUNTIME_ERROR", "spill must be enabled before input is aggregated", -6);
+    }
+    spillEnabled_ = enabled;
+    spillBudget_ = deviceBudgetBytes;
+}
+
+namespace {
+constexpr int kMaxSpillBits = 6;  // up to 64 partitions
+}
+
+// Spill path: when the estimated group table of all staged rows exceeds the budget, the rows are
+// hash-partitioned (the partitioned strategy's kernels, with pinned host memory as the target,
+// written by the GPU directly) and each partition is aggregated by its own operator of the same
+// plan, one at a time, so the device holds one partition's table.  Returns false when everything
+// fits (the ordinary path then runs).
+bool HashAggregationOperator::ExtractSpilled()
+{
+    if (pending_.empty()) {
+        return false;
+    }
+    omg::RequireDevice();
+    Impl &im = *impl_;
+    if (userStreamSet_) {
+        im.stream.SetUser(userStream_);
+    }
+    cudaStream_t s = im.stream.Get();
+    if (im.stats.Get() == nullptr) {
+        im.stats.Reset(8, s, true);
+    }
+    const size_t slotBytes = static_cast<size_t>(plan_.slotWords) * sizeof(uint64_t);
+    uint64_t estimate = 0;
+    {
+        omg::BatchTable bt;
+        bt.Build(pending_, plan_.inputCols);
+        bt.Upload(s);
+        if (!im.decided) {
+            Decide(bt, s);
+        }
+        estimate = im.estimate > 0 ? im.estimate : static_cast<uint64_t>(bt.TotalRows());
+        im.stream.Sync();
+    }
+    const double need = 2.0 * static_cast<double>(estimate) * static_cast<double>(slotBytes);  // load <= 1/2
+    if (need <= static_cast<double>(spillBudget_)) {
+        return false;
+    }
+    int bits = 1;
+    while (bits < kMaxSpillBits && need / static_cast<double>(1 << bits) > static_cast<double>(spillBudget_)) {
+        ++bits;
+    }
+    const int32_t nParts = 1 << bits;
+    // Column types and the widest column index of the batches, for the partition views.
+    int32_t nCols = 0;
+    for (int32_t c : plan_.inputCols) {
+        nCols = std::max(nCols, c + 1);
+    }
+    std::vector<DataTypeId> colType(static_cast<size_t>(nCols), OMNI_BYTE);
+    for (int32_t c : plan_.inputCols) {
+        colType[static_cast<size_t>(c)] = pending_.front()->Get(c)->GetTypeId();
+    }
+    std::vector<std::vector<VectorBatch *>> parts(static_cast<size_t>(nParts));
+    auto dummy = omg::Buffer::NewHost(16, true);
+    const int64_t chunkRows = omg::AggFlushRows();
+    size_t next = 0;
+    try {
+        while (next < pending_.size()) {
+            std::vector<VectorBatch *> chunk;
+            int64_t rows = 0;
+            while (next < pending_.size() && (chunk.empty() || rows + pending_[next]->GetRowCount() <= chunkRows)) {
+                rows += pending_[next]->GetRowCount();
+                chunk.push_back(pending_[next++]);
+            }
+            omg::BatchTable bt;
+            bt.Build(chunk, plan_.inputCols);
+            bt.Upload(s);
+            omg::AggLaunch p = MakeLaunch(plan_, nullptr, 0, nullptr, nullptr);
+            p.batches = bt.DeviceBatches();
+            p.tiles = bt.DeviceTiles();
+            p.nTiles = bt.NumTiles();
+            omg::PartArgs a;
+            std::memset(&a, 0, sizeof(a));
+            a.partBits = bits;
+            a.nInputs = static_cast<int32_t>(plan_.inputCols.size());
+            const int64_t capRows = rows + static_cast<int64_t>(nParts) * 64;
+            std::vector<omg::BufferPtr> hostCols(static_cast<size_t>(a.nInputs));
+            std::vector<omg::BufferPtr> hostNulls(static_cast<size_t>(a.nInputs));
+            for (int32_t i = 0; i < a.nInputs; ++i) {
+                const int32_t w = std::max(plan_.inputWidths[i], 1);
+                a.width[i] = w;
+                hostCols[i] = omg::Buffer::NewHost(static_cast<size_t>(capRows) * w + 16, false);
+                a.cols[i] = hostCols[i]->Data();
+                spilledBytes_ += static_cast<uint64_t>(rows) * static_cast<uint64_t>(w);
+                if (bt.AnyNulls(i)) {
+                    hostNulls[i] = omg::Buffer::NewHost(omg::NullBitmapBytes(capRows), true);
+                    a.nulls[i] = static_cast<uint32_t *>(hostNulls[i]->Data());
+                    spilledBytes_ += static_cast<uint64_t>(rows + 7) / 8;
+                }
+            }
+            DevArray<unsigned long long> counters(2 * static_cast<size_t>(nParts), s, true);
+            a.hist = counters.Get();
+            a.cursor = counters.Get() + nParts;
+            DevArray<omg::BatchDesc> partBatches(static_cast<size_t>(nParts), s);
+            a.partBatches = partBatches.Get();
+            a.maxTiles = static_cast<int32_t>(rows / omg::kTileRows + nParts + 1);
+            DevArray<omg::TileDesc> tiles(static_cast<size_t>(a.maxTiles), s);
+            DevArray<int32_t> tileStart(static_cast<size_t>(nParts) + 1, s);
+            a.partTiles = tiles.Get();
+            a.partTileStart = tileStart.Get();
+            CudaCheck(omg::LaunchAggPartition(p, a, s), "spill partition");
+            counters_[0] += 3;
+            std::vector<omg::BatchDesc> desc(static_cast<size_t>(nParts));
+            CudaCheck(cudaMemcpyAsync(desc.data(), partBatches.Get(), sizeof(omg::BatchDesc) * nParts,
+                          cudaMemcpyDeviceToHost, s),
+                "read spill partitions");
+            im.stream.Sync();
+            for (int32_t q = 0; q < nParts; ++q) {
+                const int64_t n = desc[q].rows;
+                const int64_t base = desc[q].rowBase;  // a multiple of 64 rows
+                if (n == 0) {
+                    continue;
+                }
+                auto *vb = new VectorBatch(static_cast<size_t>(n));
+                for (int32_t c = 0; c < nCols; ++c) {
+                    const auto it = std::find(plan_.inputCols.begin(), plan_.inputCols.end(), c);
+                    if (it == plan_.inputCols.end()) {
+                        vb->Append(new vec::BaseVector(OMNI_BYTE, 1, 0, dummy, 0, nullptr, 0, false));
+                        continue;
+                    }
+                    const size_t i = static_cast<size_t>(it - plan_.inputCols.begin());
+                    const int32_t w = a.width[i];
+                    vb->Append(new vec::BaseVector(colType[static_cast<size_t>(c)], w, static_cast<int32_t>(n), hostCols[i],
+                        static_cast<size_t>(base) * w, hostNulls[i], static_cast<size_t>(base / 8),
+                        hostNulls[i] != nullptr));
+                }
+                parts[static_cast<size_t>(q)].push_back(vb);
+            }
+        }
+    } catch (...) {
+        for (auto &pl : parts) {
+            for (auto *b : pl) {
+                vec::VectorHelper::FreeVecBatch(b);
+            }
+        }
+        throw;
+    }
+    ReleasePending();
+    // One operator of the same plan per partition; its output batches become this operator's.
+    uniqueKeys_ = 0;
+    for (auto &pl : parts) {
+        if (pl.empty()) {
+            continue;
+        }
+        HashAggregationOperator part(plan_, sizer_);
+        part.SetStrategy(strategy_, 0);
+        part.SetDeviceOutput(deviceOutput_);
+        if (userStreamSet_) {
+            part.SetStream(userStream_);
+        }
+        size_t k = 0;
+        try {
+            for (; k < pl.size(); ++k) {
+                part.AddInput(pl[k]);
+            }
+        } catch (...) {
+            for (++k; k < pl.size(); ++k) {
+                vec::VectorHelper::FreeVecBatch(pl[k]);
+            }
+            throw;
+        }
+        VectorBatch *out = nullptr;
+        while (part.GetOutput(&out) != 0 && out != nullptr) {
+            outputs_.push_back(out);
+            counters_[5] += out->GetRowCount();
+            out = nullptr;
+        }
+        uniqueKeys_ += part.GetHashMapUniqueKeys();
+        counters_[0] += part.Counters()[0];
+        counters_[6] += part.Counters()[6];
+        counters_[7] += part.Counters()[7];
+    }
+    counters_[3] = static_cast<int64_t>(uniqueKeys_);
+    return true;
+}
+
 void HashAggregationOperator::Extract()
 {
+    if (spillEnabled_ && ExtractSpilled()) {
+        return;
+    }
     Flush();
     Impl &im = *impl_;
     if (im.capacity == 0) {

@@ -111,6 +111,15 @@ public:
     // is freed.  Only for plans whose aggregators all read raw input and emit partials.
     VectorBatch *AlignSchema(VectorBatch *inputVecBatch) override;
 
+    // Spill (the reference's SpillConfig, operator/config/operator_config.h:28-100, and its spill
+    // path, group_aggregation.cpp:1034-1475): with spill enabled the operator keeps its input
+    // staged until GetOutput and, when the estimated group table would exceed `deviceBudgetBytes`
+    // of device memory, hash-partitions the rows into pinned host memory and aggregates one
+    // partition at a time (partitions hold disjoint groups).  Plans with VARCHAR/CHAR columns or
+    // order-dependent sticky-overflow sums are refused (UNSUPPORTED).
+    void SetSpill(bool enabled, uint64_t deviceBudgetBytes);
+    uint64_t GetSpilledBytes() override { return spilledBytes_; }
+
     // Strategy hint (OMG_AGG_STRATEGY_*) and initial capacity in groups (0 = default).
     void SetStrategy(int32_t strategy, int64_t capacityHint)
     {
@@ -134,6 +143,7 @@ private:
     void BindStrings(omg::AggLaunch &p) const;
     void DecodeStrings(std::vector<omg::OutColumn> &cols, int64_t rows, cudaStream_t s);
     void Extract();
+    bool ExtractSpilled();
     void ReleasePending();
 
     AggPlan plan_;
@@ -146,6 +156,9 @@ private:
     uint64_t uniqueKeys_ = 0;
     int32_t strategy_ = 0;
     int64_t capacityHint_ = 0;
+    bool spillEnabled_ = false;
+    uint64_t spillBudget_ = 0;
+    uint64_t spilledBytes_ = 0;
     omg::SizingModel *sizer_ = nullptr;
 };
 

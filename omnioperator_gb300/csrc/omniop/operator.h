@@ -34,6 +34,8 @@ public:
     virtual OmniStatus Init() { return OMNI_STATUS_NORMAL; }
     virtual OmniStatus Close() { return OMNI_STATUS_NORMAL; }
     virtual uint64_t GetHashMapUniqueKeys() { return 0; }
+    // Bytes this operator moved out of device memory (Operator::GetSpilledBytes, operator.h:66).
+    virtual uint64_t GetSpilledBytes() { return 0; }
     // Operators without a partial schema return the batch itself (operator.h:92-95).
     virtual VectorBatch *AlignSchema(VectorBatch *inputVecBatch) { return inputVecBatch; }
     virtual BlockingReason IsBlocked() { return BlockingReason::kNotBlocked; }

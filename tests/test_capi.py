@@ -224,3 +224,26 @@ def test_noalloc_entry_refuses_string_columns_before_touching_a_device():
     rc = omg.lib().omg_hashagg_run_noalloc(f.handle, None, None, 0, 0, None, None, 0, 16, C.byref(n), None)
     assert rc == -2
     f.close()
+
+
+def test_spill_settings_are_checked_on_the_host():
+    """Spill takes fixed-width plans without order-dependent sums, and needs a budget."""
+    L, V = omg.LongType(), omg.VarcharType(8)
+    ok = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [omg.OMNI_AGGREGATION_TYPE_SUM])
+    op = ok.create_operator()
+    op.set_spill(True, 1 << 20)
+    assert op.spilled_bytes() == 0
+    with pytest.raises(omg.OmgError) as e:
+        op.set_spill(True, 0)
+    assert e.value.status == -1
+    op.delete()
+    ok.close()
+    d64, d128 = omg.Decimal64Type(18, 2), omg.Decimal128Type(38, 2)
+    for fac in (omg.HashAggregationOperatorFactory([0], [V], [[1]], [[L]], [[L]], [omg.OMNI_AGGREGATION_TYPE_SUM]),
+                omg.HashAggregationOperatorFactory([0], [L], [[1]], [[d64]], [[d128]], [omg.OMNI_AGGREGATION_TYPE_SUM])):
+        op = fac.create_operator()
+        with pytest.raises(omg.OmgError) as e:
+            op.set_spill(True, 1 << 20)
+        assert e.value.status == -2
+        op.delete()
+        fac.close()
