@@ -278,7 +278,8 @@ def run_gpu(args, rank, world):
     if args.only == "skew":
         sk = run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
         return dict(value=sk["learned"]["value"], ms=sk["learned"]["ms_per_step"], build_ms=0.0, launches=0,
-                    roofline=None, clocks=None, e2e=None, agg=None, rows=sk["learned"]["groups"], skew=sk)
+                    roofline=None, clocks=None, e2e=None, agg=None, rows=sk["learned"]["groups"], skew=sk,
+                    batched=None, join5=None)
 
     # ---- device-resident join inputs (torch tensors seen as OmniVec device vectors)
     bkey = torch.randperm(N_BUILD, generator=g, device=dev).to(torch.int64)

@@ -328,7 +328,9 @@ class Operator:
     def get_outputs(self, max_batches: int = 4096):
         """GetOutput until no batch is produced or `max_batches` were returned, one C call
         (omg_op_get_outputs) -> (list of batch handles, total rows)."""
-        arr = (C.c_void_p * max_batches)()
+        arr = getattr(self, "_outs", None)
+        if arr is None or len(arr) < max_batches:
+            arr = self._outs = (C.c_void_p * max_batches)()  # reused across calls
         n = C.c_int32(0)
         rows = C.c_int64(0)
         check(lib().omg_op_get_outputs(self.handle, arr, max_batches, C.byref(n), C.byref(rows)))

@@ -853,13 +853,23 @@ void LookupJoinOperator::ProcessPending()
     p.nRegions = nRegions;
     p.singleBatch = pending_.size() == 1 ? 1 : 0;
     std::vector<int64_t> regionCount(nRegions, 0);
+    // Host output without VARCHAR columns: the kernel writes the rows straight into pinned host
+    // memory over the CPU-GPU link, so no device-to-host copy follows the probe.
+    bool hostDirect = !deviceOutput_;
+    for (size_t o = 0; o < nOut; ++o) {
+        hostDirect = hostDirect && cols[o].width != 0;
+    }
     for (int attempt = 0; attempt < 2; ++attempt) {
         const uint64_t capacity = regionCap * static_cast<uint64_t>(nRegions);
         for (size_t o = 0; o < nOut; ++o) {
             // VARCHAR columns hold an 8-byte row handle per output row until the second pass.
             const size_t vw = cols[o].width == 0 ? 8 : static_cast<size_t>(cols[o].width);
-            cols[o].values = omg::Buffer::NewDevice(capacity * vw + 16, s, false);
-            cols[o].nulls = cols[o].hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(capacity), s, true) : nullptr;
+            const size_t nb = omg::NullBitmapBytes(static_cast<int64_t>(capacity));
+            cols[o].values = hostDirect ? omg::Buffer::NewHost(capacity * vw + 16, false)
+                                        : omg::Buffer::NewDevice(capacity * vw + 16, s, false);
+            cols[o].nulls = !cols[o].hasNull ? nullptr
+                                             : (hostDirect ? omg::Buffer::NewHost(nb, true)
+                                                           : omg::Buffer::NewDevice(nb, s, true));
             p.out[o].values = cols[o].values->Data();
             p.out[o].nulls = cols[o].nulls ? static_cast<uint8_t *>(cols[o].nulls->Data()) : nullptr;
         }
@@ -926,9 +936,11 @@ void LookupJoinOperator::ProcessPending()
         const int64_t first = static_cast<int64_t>(r) * static_cast<int64_t>(regionCap);
         std::vector<omg::OutColumn> outCols = cols;
         int64_t firstRow = first;
-        if (!deviceOutput_) {
+        if (!deviceOutput_ && !hostDirect) {
             outCols = omg::CopyColumnsToHost(cols, n, s, first);
             firstRow = 0;
+        }
+        if (!deviceOutput_) {
             for (auto &c : outCols) {
                 c.hasNull = false;  // host vectors: HasNull() scans the bitmap
             }
