@@ -199,16 +199,33 @@ __device__ __forceinline__ void AtomicStrMinMax(const AggLaunch &p, int input, u
     }
 }
 
+// Double sums: the first kPlainSumRows rows of a table slot (by their COUNT_ALL arrival order)
+// are added with a plain atomic add, the later ones with the compensated add.  A slot of a
+// shared table or of the global table therefore leaves at most kPlainSumRows additions
+// uncompensated, whose rounding errors add up to at most kPlainSumRows * 2^-53 * sum|x|
+// (7.1e-15 relative to sum|x| for 64); shared-table partials are merged compensated.
+constexpr unsigned long long kPlainSumRows = 64;
+
+__device__ __forceinline__ void AddDoubleState(uint64_t *w, double x, unsigned long long arrival)
+{
+    if (arrival < kPlainSumRows) {
+        atomicAdd(reinterpret_cast<double *>(w), x);  // result unused: a fire-and-forget add
+    } else {
+        AtomicAddCompensated(w, x, 0.0);
+    }
+}
+
 // ------------------------------------------------------------------ state updates
 // `st` points at the group's state words, in shared or global memory.
 __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc &b, int64_t row, const RowIn &in,
     uint64_t *st)
 {
+    unsigned long long arrival = kPlainSumRows;  // rows of the slot before this one (COUNT_ALL is accs[0])
     for (int a = 0; a < p.nAccs; ++a) {
         const AccSpec &s = p.accs[a];
         uint64_t *w = st + s.word;
         if (s.kind == ACC_COUNT_ALL) {
-            atomicAdd(reinterpret_cast<unsigned long long *>(w), 1ull);
+            arrival = atomicAdd(reinterpret_cast<unsigned long long *>(w), 1ull);
             continue;
         }
         const bool isNull = AccNull(s, b, row, in);
@@ -250,7 +267,7 @@ __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc
                 break;
             }
             case ACC_DSUM:
-                AtomicAddCompensated(w, AccDouble(s, b, row, in), 0.0);
+                AddDoubleState(w, AccDouble(s, b, row, in), arrival);
                 break;
             case ACC_IMIN:
                 AtomicMinI64(w, AccInt(s, b, row, in));
@@ -647,9 +664,11 @@ __device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batc
     const int kw = p.table.keyWords;
     const int64_t row0 = static_cast<int64_t>(tile.row0) + threadIdx.x;
     int slot[kPartRows];  // >= 0: slot index in the shared table, -1: nothing to do in pass 2
+    uint32_t arrival[kPartRows];  // the row's COUNT_ALL arrival order in its slot (capped)
 #pragma unroll
     for (int k = 0; k < kPartRows; ++k) {
         slot[k] = -1;
+        arrival[k] = static_cast<uint32_t>(kPlainSumRows);
         const int r = static_cast<int>(threadIdx.x) + k * 1024;
         if (r < tile.rows) {
             const RowKey key = ReadKey(p.key, b, row0 + k * 1024, kKind);
@@ -675,7 +694,9 @@ __device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batc
 #pragma unroll
                 for (int k = 0; k < kPartRows; ++k) {
                     if (slot[k] >= 0) {
-                        atomicAdd(reinterpret_cast<unsigned long long *>(st + slot[k] * sw + s.word), 1ull);
+                        arrival[k] = static_cast<uint32_t>(
+                            min(atomicAdd(reinterpret_cast<unsigned long long *>(st + slot[k] * sw + s.word), 1ull),
+                                kPlainSumRows));
                     }
                 }
                 break;
@@ -721,7 +742,7 @@ __device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batc
                     }
                     uint64_t *w = st + slot[k] * sw + s.word;
                     if (s.kind == ACC_DSUM) {
-                        AtomicAddCompensated(w, x[k], 0.0);
+                        AddDoubleState(w, x[k], arrival[k]);
                     } else if (!isnan(x[k])) {
                         if (s.kind == ACC_DMIN) {
                             AtomicMinI64(w, OrderedFromDouble(x[k]));
