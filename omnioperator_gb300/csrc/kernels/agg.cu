@@ -621,6 +621,9 @@ __device__ __forceinline__ int64_t LoadIntW(const void *col, int64_t row)
     }
 }
 
+// The low 32 bits of a little-endian 64-bit state word.
+__device__ __forceinline__ unsigned int *LowWord(uint64_t *w) { return reinterpret_cast<unsigned int *>(w); }
+
 template <int kW>
 __device__ __forceinline__ void ApplyIntAcc(const AccSpec &s, const void *col, const uint8_t *nulls, int64_t row0,
     const int (&slot)[kPartRows], uint64_t *sm, int sw)
@@ -694,9 +697,11 @@ __device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batc
 #pragma unroll
                 for (int k = 0; k < kPartRows; ++k) {
                     if (slot[k] >= 0) {
-                        arrival[k] = static_cast<uint32_t>(
-                            min(atomicAdd(reinterpret_cast<unsigned long long *>(st + slot[k] * sw + s.word), 1ull),
-                                kPlainSumRows));
+                        // A shared table counts the rows of one launch (< 2^32): a 32-bit add on the
+                        // word's low half (little-endian) is exact and faster than a 64-bit one.
+                        arrival[k] = static_cast<uint32_t>(min(
+                            static_cast<unsigned long long>(atomicAdd(LowWord(st + slot[k] * sw + s.word), 1u)),
+                            kPlainSumRows));
                     }
                 }
                 break;
@@ -705,7 +710,7 @@ __device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batc
 #pragma unroll
                     for (int k = 0; k < kPartRows; ++k) {
                         if (slot[k] >= 0 && NullRO(nulls, row0 + k * 1024)) {
-                            atomicAdd(reinterpret_cast<unsigned long long *>(st + slot[k] * sw + s.word), 1ull);
+                            atomicAdd(LowWord(st + slot[k] * sw + s.word), 1u);
                         }
                     }
                 }
