@@ -638,9 +638,41 @@ LookupJoinOperatorFactory *LookupJoinOperatorFactory::CreateLookupJoinOperatorFa
 
 Operator *LookupJoinOperatorFactory::CreateOperator() { return new LookupJoinOperator(*this); }
 
+// One direct probe call between its launch and its completion: the batches it reads, its
+// kernel parameters and outputs, and the event that marks its kernel and count copy done.
+struct LookupJoinOperator::ProbeCall {
+    std::vector<VectorBatch *> batches;
+    omg::BatchTable bt;
+    omg::ProbeLaunch p;
+    std::vector<omg::OutColumn> cols;
+    size_t nOut = 0;
+    size_t nProbeOut = 0;
+    int32_t nRegions = 0;
+    uint64_t regionCap = 0;
+    bool hostDirect = false;
+    DevArray<unsigned long long> count;
+    omg::PinnedArray<unsigned long long> hostCount;
+    omg::KernelTimer timer;
+    cudaEvent_t done = nullptr;
+    cudaStream_t s = nullptr;
+    ~ProbeCall()
+    {
+        if (done != nullptr) {
+            cudaEventSynchronize(done);  // the kernel may still read `batches`
+            cudaEventDestroy(done);
+            cudaGetLastError();
+        }
+        for (auto *b : batches) {
+            vec::VectorHelper::FreeVecBatch(b);
+        }
+    }
+};
+
 struct LookupJoinOperator::Impl {
     omg::OpStream stream;
     omg::KernelTimer timer;
+    // Probe calls launched by AddInput (pipelined callers), oldest first.
+    std::deque<std::unique_ptr<ProbeCall>> inflight;
 };
 
 LookupJoinOperator::LookupJoinOperator(const LookupJoinOperatorFactory &f) : f_(f), impl_(new Impl()) {}
@@ -649,6 +681,7 @@ LookupJoinOperator::~LookupJoinOperator() { Close(); }
 
 OmniStatus LookupJoinOperator::Close()
 {
+    impl_->inflight.clear();  // waits for their kernels, frees their batches
     for (auto *b : pending_) {
         vec::VectorHelper::FreeVecBatch(b);
     }
@@ -685,6 +718,12 @@ int32_t LookupJoinOperator::AddInput(VectorBatch *vecBatch)
     pending_.push_back(vecBatch);
     pendingRows_ += vecBatch->GetRowCount();
     SetStatus(OMNI_STATUS_NORMAL);
+    // Pipelined callers: a full chunk is launched at once, so that its kernel runs while the
+    // caller queues the next chunk and GetOutput carves the previous one.
+    if (!noMoreInput_ && pendingRows_ >= kProbeChunkRows && strategy_ == kJoinDirect && f_.build->built &&
+        impl_->inflight.size() < 2) {
+        impl_->inflight.push_back(LaunchPending());
+    }
     return 0;
 }
 
@@ -693,6 +732,17 @@ void LookupJoinOperator::ProcessPending()
     if (strategy_ != kJoinDirect && ProcessPartitioned()) {
         return;
     }
+    std::unique_ptr<ProbeCall> pc = LaunchPending();
+    FinishProbe(*pc);
+}
+
+// Take the queued batches, set up the probe and launch it; FinishProbe completes it.
+std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending()
+{
+    std::unique_ptr<ProbeCall> call(new ProbeCall());
+    ProbeCall &pc = *call;
+    pc.batches.swap(pending_);
+    pendingRows_ = 0;
     JoinBuildState &b = *f_.build;
     omg::RequireDevice();
     if (userStreamSet_) {
@@ -725,14 +775,15 @@ void LookupJoinOperator::ProcessPending()
             inputCols.push_back(c);
         }
     }
-    omg::BatchTable bt;
-    bt.Build(pending_, inputCols);
+    omg::BatchTable &bt = pc.bt;
+    bt.Build(pc.batches, inputCols);
     bt.Upload(s);
     const int64_t probeRows = bt.TotalRows();
     const size_t nProbeOut = f_.probeOutputCols.size();
     const size_t nOut = nProbeOut + (b.kind == omg::JOIN_KIND_EXISTENCE ? 1 : f_.buildOutputCols.size());
-    std::vector<omg::OutColumn> cols(nOut);
-    omg::ProbeLaunch p;
+    pc.cols.assign(nOut, omg::OutColumn{});
+    std::vector<omg::OutColumn> &cols = pc.cols;
+    omg::ProbeLaunch &p = pc.p;
     std::memset(&p, 0, sizeof(p));
     p.batches = bt.DeviceBatches();
     p.tiles = bt.DeviceTiles();
@@ -847,55 +898,92 @@ void LookupJoinOperator::ProcessPending()
         regionCap *= std::min<uint32_t>(b.maxDup, 2);
     }
     regionCap = (regionCap + 63) / 64 * 64;
-    DevArray<unsigned long long> count(static_cast<size_t>(nRegions) * omg::kRegionStride, s, true);
-    omg::PinnedArray<unsigned long long> hostCount(static_cast<size_t>(nRegions) * omg::kRegionStride);
-    p.outCount = count.Get();
+    pc.count.Reset(static_cast<size_t>(nRegions) * omg::kRegionStride, s, true);
+    pc.hostCount.Reset(static_cast<size_t>(nRegions) * omg::kRegionStride);
+    p.outCount = pc.count.Get();
     p.nRegions = nRegions;
-    p.singleBatch = pending_.size() == 1 ? 1 : 0;
-    std::vector<int64_t> regionCount(nRegions, 0);
+    p.singleBatch = pc.batches.size() == 1 ? 1 : 0;
     // Host output without VARCHAR columns: the kernel writes the rows straight into pinned host
     // memory over the CPU-GPU link, so no device-to-host copy follows the probe.
     bool hostDirect = !deviceOutput_;
     for (size_t o = 0; o < nOut; ++o) {
         hostDirect = hostDirect && cols[o].width != 0;
     }
+    pc.hostDirect = hostDirect;
+    pc.regionCap = regionCap;
+    pc.nRegions = nRegions;
+    pc.nOut = nOut;
+    pc.nProbeOut = nProbeOut;
+    pc.s = s;
+    LaunchAttempt(pc);
+    return call;
+}
+
+// Output buffers for the call's region capacity, the kernel, and the asynchronous copy of the
+// region counts; the call's event marks the end.
+void LookupJoinOperator::LaunchAttempt(ProbeCall &pc)
+{
+    cudaStream_t s = pc.s;
+    omg::ProbeLaunch &p = pc.p;
+    const uint64_t capacity = pc.regionCap * static_cast<uint64_t>(pc.nRegions);
+    for (size_t o = 0; o < pc.nOut; ++o) {
+        omg::OutColumn &c = pc.cols[o];
+        // VARCHAR columns hold an 8-byte row handle per output row until the second pass.
+        const size_t vw = c.width == 0 ? 8 : static_cast<size_t>(c.width);
+        const size_t nb = omg::NullBitmapBytes(static_cast<int64_t>(capacity));
+        c.values = pc.hostDirect ? omg::Buffer::NewHost(capacity * vw + 16, false)
+                                 : omg::Buffer::NewDevice(capacity * vw + 16, s, false);
+        c.nulls = !c.hasNull ? nullptr
+                             : (pc.hostDirect ? omg::Buffer::NewHost(nb, true) : omg::Buffer::NewDevice(nb, s, true));
+        p.out[o].values = c.values->Data();
+        p.out[o].nulls = c.nulls ? static_cast<uint8_t *>(c.nulls->Data()) : nullptr;
+    }
+    p.regionCap = pc.regionCap;
+    CudaCheck(cudaMemsetAsync(pc.count.Get(), 0, sizeof(unsigned long long) * pc.count.Size(), s), "reset counts");
+    pc.timer.Start(s);
+    CudaCheck(omg::LaunchProbe(p, s), "probe kernel");
+    pc.timer.Stop(s);
+    ++counters_[0];
+    CudaCheck(cudaMemcpyAsync(pc.hostCount.Get(), pc.count.Get(), sizeof(unsigned long long) * pc.count.Size(),
+                  cudaMemcpyDeviceToHost, s),
+        "read counts");
+    if (pc.done == nullptr) {
+        CudaCheck(cudaEventCreateWithFlags(&pc.done, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    CudaCheck(cudaEventRecord(pc.done, s), "cudaEventRecord");
+}
+
+// Wait for a launched probe, run it once more at the exact size if a region overflowed, then
+// build VARCHAR outputs, carve the output batches and free the probe batches.
+void LookupJoinOperator::FinishProbe(ProbeCall &pc)
+{
+    JoinBuildState &b = *f_.build;
+    cudaStream_t s = pc.s;
+    omg::ProbeLaunch &p = pc.p;
+    omg::BatchTable &bt = pc.bt;
+    std::vector<omg::OutColumn> &cols = pc.cols;
+    const size_t nOut = pc.nOut;
+    const size_t nProbeOut = pc.nProbeOut;
+    const int32_t nRegions = pc.nRegions;
+    const bool hostDirect = pc.hostDirect;
+    std::vector<int64_t> regionCount(nRegions, 0);
     for (int attempt = 0; attempt < 2; ++attempt) {
-        const uint64_t capacity = regionCap * static_cast<uint64_t>(nRegions);
-        for (size_t o = 0; o < nOut; ++o) {
-            // VARCHAR columns hold an 8-byte row handle per output row until the second pass.
-            const size_t vw = cols[o].width == 0 ? 8 : static_cast<size_t>(cols[o].width);
-            const size_t nb = omg::NullBitmapBytes(static_cast<int64_t>(capacity));
-            cols[o].values = hostDirect ? omg::Buffer::NewHost(capacity * vw + 16, false)
-                                        : omg::Buffer::NewDevice(capacity * vw + 16, s, false);
-            cols[o].nulls = !cols[o].hasNull ? nullptr
-                                             : (hostDirect ? omg::Buffer::NewHost(nb, true)
-                                                           : omg::Buffer::NewDevice(nb, s, true));
-            p.out[o].values = cols[o].values->Data();
-            p.out[o].nulls = cols[o].nulls ? static_cast<uint8_t *>(cols[o].nulls->Data()) : nullptr;
-        }
-        p.regionCap = regionCap;
-        CudaCheck(cudaMemsetAsync(count.Get(), 0, sizeof(unsigned long long) * count.Size(), s), "reset counts");
-        impl_->timer.Start(s);
-        CudaCheck(omg::LaunchProbe(p, s), "probe kernel");
-        impl_->timer.Stop(s);
-        ++counters_[0];
-        CudaCheck(cudaMemcpyAsync(hostCount.Get(), count.Get(), sizeof(unsigned long long) * count.Size(),
-                      cudaMemcpyDeviceToHost, s),
-            "read counts");
-        impl_->stream.Sync();
-        counters_[6] += impl_->timer.ElapsedNs();
+        CudaCheck(cudaEventSynchronize(pc.done), "probe kernel");
+        counters_[6] += pc.timer.ElapsedNs();
         ++counters_[7];
         uint64_t most = 0;
         for (int32_t r = 0; r < nRegions; ++r) {
-            regionCount[r] = static_cast<int64_t>(hostCount[static_cast<size_t>(r) * omg::kRegionStride]);
+            regionCount[r] = static_cast<int64_t>(pc.hostCount[static_cast<size_t>(r) * omg::kRegionStride]);
             most = std::max<uint64_t>(most, static_cast<uint64_t>(regionCount[r]));
         }
-        if (most <= regionCap) {
+        if (most <= pc.regionCap) {
             break;
         }
-        regionCap = (most + 63) / 64 * 64;  // exact size known now: run once more
+        pc.regionCap = (most + 63) / 64 * 64;  // exact size known now: run once more
         ++counters_[1];
+        LaunchAttempt(pc);
     }
+    const uint64_t regionCap = pc.regionCap;
     // VARCHAR outputs: row handles -> lengths -> offsets -> characters, over all regions at once
     // (positions past a region's count contribute nothing).
     for (size_t o = 0; o < nOut; ++o) {
@@ -908,7 +996,7 @@ void LookupJoinOperator::ProcessPending()
         const int64_t *bOffs = oc.side == 1 ? b.colOffs[oc.src].Get() : nullptr;
         const uint8_t *bChars = oc.side == 1 ? b.colValues[oc.src].Get() : nullptr;
         DevArray<uint32_t> lens(static_cast<size_t>(nPos), s);
-        CudaCheck(omg::LaunchVarlenOutLens(handles, nPos, regionCap, count.Get(), oc.side, bt.DeviceBatches(), oc.src,
+        CudaCheck(omg::LaunchVarlenOutLens(handles, nPos, regionCap, pc.count.Get(), oc.side, bt.DeviceBatches(), oc.src,
                       bOffs, lens.Get(), s),
             "output string lengths");
         DevArray<int64_t> offs64;
@@ -918,7 +1006,7 @@ void LookupJoinOperator::ProcessPending()
         }
         auto chars = omg::Buffer::NewDevice(static_cast<size_t>(total) + 16, s, false);
         auto offs32 = omg::Buffer::NewDevice((static_cast<size_t>(nPos) + 1) * sizeof(int32_t), s, false);
-        CudaCheck(omg::LaunchVarlenOutCopy(handles, nPos, regionCap, count.Get(), oc.side, bt.DeviceBatches(), oc.src,
+        CudaCheck(omg::LaunchVarlenOutCopy(handles, nPos, regionCap, pc.count.Get(), oc.side, bt.DeviceBatches(), oc.src,
                       bOffs, bChars, offs64.Get(), static_cast<uint8_t *>(chars->Data()),
                       static_cast<int32_t *>(offs32->Data()), total, s),
             "output strings");
@@ -953,15 +1041,14 @@ void LookupJoinOperator::ProcessPending()
         }
         rows += n;
     }
-    if (!deviceOutput_) {
-        impl_->stream.Sync();
+    if (!deviceOutput_ && !hostDirect) {
+        impl_->stream.Sync();  // the copies to host batches (direct host output was complete at the event)
     }
     counters_[5] += rows;
-    for (auto *pb : pending_) {
+    for (auto *pb : pc.batches) {
         vec::VectorHelper::FreeVecBatch(pb);
     }
-    pending_.clear();
-    pendingRows_ = 0;
+    pc.batches.clear();
 }
 
 
@@ -1281,7 +1368,24 @@ bool LookupJoinOperator::ProcessPartitioned()
 int32_t LookupJoinOperator::GetOutput(VectorBatch **outputVecBatch)
 {
     *outputVecBatch = nullptr;
-    if (outputs_.empty() && !pending_.empty() && f_.build->built &&
+    // Launched probe calls finish oldest first: when another is queued behind it, when its kernel
+    // is done, or when no more input will come.
+    auto &fl = impl_->inflight;
+    while (outputs_.empty() && !fl.empty()) {
+        bool ready = fl.size() > 1 || noMoreInput_;
+        if (!ready) {
+            const cudaError_t q = cudaEventQuery(fl.front()->done);
+            cudaGetLastError();  // "not ready" is not an error of this operator
+            ready = q != cudaErrorNotReady;
+        }
+        if (!ready) {
+            break;
+        }
+        std::unique_ptr<ProbeCall> pc = std::move(fl.front());
+        fl.pop_front();
+        FinishProbe(*pc);
+    }
+    if (outputs_.empty() && fl.empty() && !pending_.empty() && f_.build->built &&
         (noMoreInput_ || pendingRows_ >= kProbeChunkRows)) {
         ProcessPending();
     }
@@ -1289,7 +1393,7 @@ int32_t LookupJoinOperator::GetOutput(VectorBatch **outputVecBatch)
         *outputVecBatch = outputs_.front();
         outputs_.pop_front();
     }
-    if (outputs_.empty() && pending_.empty() && noMoreInput_) {
+    if (outputs_.empty() && pending_.empty() && fl.empty() && noMoreInput_) {
         SetStatus(OMNI_STATUS_FINISHED);
     }
     return 0;

@@ -119,7 +119,11 @@ public:
 
 private:
     struct Impl;
+    struct ProbeCall;
     void ProcessPending();
+    std::unique_ptr<ProbeCall> LaunchPending();
+    void LaunchAttempt(ProbeCall &pc);
+    void FinishProbe(ProbeCall &pc);
     bool ProcessPartitioned();
     int32_t strategy_ = kJoinDirect;
     int32_t partBits_ = 0;

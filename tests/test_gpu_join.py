@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 import omnioperator_gb300 as omg
+import oracle
 from helpers import expected_join_rows, join_rows_canonical, run_join
 
 pytestmark = pytest.mark.gpu
@@ -184,3 +185,63 @@ def test_bulk_add_inputs_and_get_outputs(gpu):
     bf.close()
     exp = expected_join_rows([pkey], [pnull], [bkey, p1, p2], None, 0, 0, [0], [1, 2])
     assert join_rows_canonical(cols) == exp
+
+
+@pytest.mark.parametrize("join_type", [omg.OMNI_JOIN_TYPE_INNER, omg.OMNI_JOIN_TYPE_LEFT])
+def test_pipelined_probe_chunks_in_flight(gpu, join_type):
+    """Pipelined callers: every full 2^22-row chunk of queued batches is launched by AddInput and
+    finished by a later GetOutput (up to two in flight), outputs written straight to host memory.
+    Three and a half chunks of probe rows give the same row multiset as the oracle."""
+    rng = np.random.default_rng(21 + join_type)
+    nb = 1 << 16
+    bkey = rng.permutation(nb).astype(np.int64)
+    p1 = rng.integers(-1000, 1000, nb).astype(np.int32)
+    p2 = rng.integers(-1000, 1000, nb).astype(np.int32)
+    n = 7 << 21
+    pkey = rng.integers(0, nb + nb // 4, n).astype(np.int64)
+    pnull = rng.random(n) < 0.01
+    bf = omg.HashBuilderOperatorFactory(join_type, [L, I, I], [0])
+    bop = bf.create_operator()
+    bop.add_input(omg.make_batch([L, I, I], [bkey, p1, p2]))
+    bop.get_output()
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1, 2], [I, I], bf)
+    op = pf.create_operator()
+    op.set_no_more_input(False)
+    cols = [[], [], []]
+    masks = [[], [], []]
+
+    def take(outs):
+        for b in outs:
+            for c, (v, m) in enumerate(omg.batch_to_numpy(b)):
+                cols[c].append(v)
+                masks[c].append(m)
+        omg.free_batches(outs)
+
+    step = 1024 * 4096
+    for s in range(0, n, step):
+        batches = [omg.make_batch([L], [pkey[i:i + 4096]], [pnull[i:i + 4096]])
+                   for i in range(s, min(n, s + step), 4096)]
+        op.add_inputs(batches)
+        take(op.get_outputs(1 << 12)[0])
+    op.no_more_input()
+    take(op.get_outputs(1 << 12)[0])
+    assert op.get_status() == omg.OMNI_STATUS_FINISHED
+    op.delete()
+    pf.close()
+    bop.delete()
+    bf.close()
+    got = [np.concatenate(c) for c in cols]
+    gm = [np.concatenate(m) for m in masks]
+    kind = "inner" if join_type == omg.OMNI_JOIN_TYPE_INNER else "probe_outer"
+    pi, bi = oracle.join(kind, bkey, None, pkey, pnull)
+    want_k = np.where(pnull[pi], 0, pkey[pi])
+    want_p1 = np.where(bi >= 0, p1[np.maximum(bi, 0)], 0)
+    want_p2 = np.where(bi >= 0, p2[np.maximum(bi, 0)], 0)
+    want_m = [pnull[pi], bi < 0, bi < 0]
+    got_rows = np.stack([np.where(gm[0], 0, got[0]), gm[0], np.where(gm[1], 0, got[1]), gm[1],
+                         np.where(gm[2], 0, got[2]), gm[2]]).astype(np.int64)
+    want_rows = np.stack([want_k, want_m[0], want_p1, want_m[1], want_p2, want_m[2]]).astype(np.int64)
+    assert got_rows.shape == want_rows.shape
+    g_sorted = got_rows[:, np.lexsort(got_rows[::-1])]
+    w_sorted = want_rows[:, np.lexsort(want_rows[::-1])]
+    assert np.array_equal(g_sorted, w_sorted)
