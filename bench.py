@@ -351,6 +351,8 @@ def run_gpu(args, rank, world):
     agg = None if args.skip_agg else run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world)
     two_stage = None if args.skip_ext else run_agg_two_stage(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                               world)
+    features = None if args.skip_ext else run_features(args, omg, torch, dev, stream, barrier, max_over_ranks, world,
+                                                        bf, pkey, pbits)
     pop.delete()
     bop.delete()
     pf.close()
@@ -364,7 +366,7 @@ def run_gpu(args, rank, world):
                                                           world, rank)
     return dict(value=value, ms=ms / args.steps, build_ms=build_ms, launches=launches, roofline=roofline,
                 clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew, batched=batched, join5=join5,
-                kinds=kinds, two_stage=two_stage)
+                kinds=kinds, two_stage=two_stage, features=features)
 
 
 def run_join_kinds(args, omg, torch, stream, barrier, max_over_ranks, world, bkey, p1, p2, pkey, pbits, pnull):
@@ -455,6 +457,117 @@ def run_join_kinds(args, omg, torch, stream, barrier, max_over_ranks, world, bke
             of.close()
         pf.close()
         bf.close()
+    return out
+
+
+def run_features(args, omg, torch, dev, stream, barrier, max_over_ranks, world, bf, pkey_t, pnull_bits):
+    """Throughput of the operator features beyond the two headline plans, each timed with CUDA
+    events around whole operator calls (host work included), inputs in HBM:
+    * agg_varchar: 2^22 rows grouped by a VARCHAR key over 10,000 distinct strings of 8-24 bytes,
+      SUM and COUNT of an int64 column (string dictionary, aggregation on ids, strings restored);
+    * join_filter: the headline probe (2^26 rows) with the filter build.p1 >= 0 (about half the
+      matches pass), general probe kernel;
+    * agg_spill: the uniform aggregation (2^22 rows) with a 256 KiB device budget, so its rows are
+      partitioned into pinned host memory and aggregated one partition at a time, next to the
+      unspilled run."""
+    L, I, D, V = omg.LongType(), omg.IntType(), omg.DoubleType(), omg.VarcharType(24)
+    SUM, CNT, MIN, MAX, AVG = (omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_COUNT_COLUMN,
+                               omg.OMNI_AGGREGATION_TYPE_MIN, omg.OMNI_AGGREGATION_TYPE_MAX,
+                               omg.OMNI_AGGREGATION_TYPE_AVG)
+    out = {"workload": "operator features, inputs in HBM, whole operator calls timed: VARCHAR group-by keys "
+                       "(2^22 rows, 10,000 strings), a join filter on the headline probe (2^26 rows), "
+                       "aggregation spill (2^22 rows, 256 KiB device budget)"}
+
+    def timed(fn, n_steps, n_warm):
+        for _ in range(n_warm):
+            fn()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_steps):
+            fn()
+        torch.cuda.synchronize()
+        barrier()
+        return max_over_ranks(time.perf_counter() - t0) / n_steps
+
+    # VARCHAR keys
+    rng = np.random.default_rng(5)
+    words = [bytes(rng.integers(97, 123, l, dtype=np.uint8)) for l in rng.integers(8, 25, 10_000)]
+    idx = rng.integers(0, len(words), AGG_ROWS)
+    keys = np.array([words[i] for i in idx], dtype=object)
+    vals = rng.integers(-10**6, 10**6, AGG_ROWS, dtype=np.int64)
+    host = omg.make_batch([V, L], [keys, vals])
+    fac = omg.HashAggregationOperatorFactory([0], [V], [[1], [1]], [[L], [L]], [[L], [L]], [SUM, CNT])
+    n_steps, n_warm = max(1, min(args.steps, 5)), max(1, min(args.warmup, 2))
+    dev_batches = [omg.batch_to_device(host) for _ in range(n_steps + n_warm)]
+    omg.free_batch(host)
+    groups = []
+
+    def agg_varchar():
+        op = fac.create_operator()
+        op.set_stream(stream.cuda_stream)
+        op.set_device_output(True)
+        op.add_input(dev_batches.pop())
+        outs = op.drain()
+        groups.append(sum(omg.batch_row_count(b) for b in outs))
+        omg.free_batches(outs)
+        op.delete()
+
+    t = timed(agg_varchar, n_steps, n_warm)
+    fac.close()
+    assert all(g == len(set(idx.tolist())) for g in groups)
+    out["agg_varchar"] = {"value": world * AGG_ROWS / t, "unit": "rows/s", "ms_per_step": round(t * 1e3, 3),
+                          "groups": groups[-1]}
+
+    # join filter over the headline build and probe
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1, 2], [I, I], bf,
+                                       filter_expr=omg.Binary(omg.EXPR_GTE, omg.Field(2, I), omg.Literal(0, I)))
+    rows = []
+
+    def join_filter():
+        op = pf.create_operator()
+        op.set_stream(stream.cuda_stream)
+        op.set_device_output(True)
+        op.add_input(omg.wrap_device_batch([L], N_PROBE, [pkey_t.data_ptr()], [pnull_bits.data_ptr()]))
+        outs = op.drain()
+        rows.append(sum(omg.batch_row_count(b) for b in outs))
+        omg.free_batches(outs)
+        op.delete()
+
+    t = timed(join_filter, max(1, min(args.steps, 5)), n_warm)
+    pf.close()
+    out["join_filter"] = {"value": world * N_PROBE / t, "unit": "probe rows/s", "ms_per_step": round(t * 1e3, 3),
+                          "output_rows": rows[-1]}
+
+    # spill
+    key, v1, v2 = agg_data_numpy(2)
+    tk, t1, t2 = (torch.from_numpy(x).to(dev) for x in (key, v1, v2))
+    afac = omg.HashAggregationOperatorFactory(
+        [0], [L], [[1], [1], [1], [1], [2], [2]], [[L], [L], [L], [L], [D], [D]], [[L], [L], [L], [L], [D], [D]],
+        [SUM, CNT, MIN, MAX, SUM, AVG])
+    spilled = []
+
+    def agg(budget):
+        def run():
+            op = afac.create_operator()
+            op.set_stream(stream.cuda_stream)
+            op.set_device_output(True)
+            if budget:
+                op.set_spill(True, budget)
+            op.add_input(omg.wrap_device_batch([L, L, D], AGG_ROWS, [tk.data_ptr(), t1.data_ptr(), t2.data_ptr()]))
+            outs = op.drain()
+            assert sum(omg.batch_row_count(b) for b in outs) == AGG_GROUPS
+            omg.free_batches(outs)
+            spilled.append(op.spilled_bytes())
+            op.delete()
+        return run
+
+    t_plain = timed(agg(0), n_steps, n_warm)
+    t_spill = timed(agg(256 << 10), n_steps, n_warm)
+    afac.close()
+    out["agg_spill"] = {"value": world * AGG_ROWS / t_spill, "unit": "rows/s", "ms_per_step": round(t_spill * 1e3, 3),
+                        "unspilled_ms_per_step": round(t_plain * 1e3, 3), "spilled_bytes": spilled[-1],
+                        "device_budget_bytes": 256 << 10}
     return out
 
 
@@ -1024,7 +1137,8 @@ def main():
                             "build_ms": round(r["build_ms"], 3), "output_rows_per_step": r["rows"]},
                  "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"],
                  "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"], "agg_batched": r["batched"],
-                 "join_skewed": r["join5"], "join_kinds": r.get("kinds"), "agg_two_stage": r.get("two_stage")})
+                 "join_skewed": r["join5"], "join_kinds": r.get("kinds"), "agg_two_stage": r.get("two_stage"),
+                 "features": r.get("features")})
     print(json.dumps(line), flush=True)
 
 
