@@ -228,6 +228,35 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def replica_sync(dist, device):
+    """barrier() and max_over_ranks(x) for N independent replicas (one process per GPU, no
+    data-path collective): the timed region is bracketed by barriers and each rank's elapsed
+    time is reduced with MAX, so a whole-job rate is world * units per rank / that maximum.
+    `dist` is torch.distributed (None for one process); `device` holds the reduction tensor (the
+    rank's GPU, or the CPU under gloo)."""
+    import torch
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        if device.type == "cuda":
+            torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Units all ranks processed per second of the slowest rank."""
+    return world * units_per_rank / seconds
+
+
 # ------------------------------------------------------------------------------ GPU arm
 def run_gpu(args, rank, world):
     import torch
@@ -243,18 +272,7 @@ def run_gpu(args, rank, world):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = replica_sync(dist, dev)
 
     L, I, D = omg.LongType(), omg.IntType(), omg.DoubleType()
     stream = torch.cuda.current_stream()
@@ -331,7 +349,7 @@ def run_gpu(args, rank, world):
     assert rows == expected_rows
     c1 = pop.counters()
     ms = max_over_ranks(ev0.elapsed_time(ev1))
-    value = world * N_PROBE * args.steps / (ms / 1e3)
+    value = whole_job_rate(world, N_PROBE * args.steps, ms / 1e3)
     kernel_s = (c1["kernel_ns"] - c0["kernel_ns"]) / max(c1["kernel_launches"] - c0["kernel_launches"], 1) / 1e9
     launches = c1["launches"] - c0["launches"]
     # Algorithmic bytes of one probe launch: 8 B key + 1/8 B validity per probe row, 16 B per output row.
@@ -717,7 +735,7 @@ def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
     bf2.close()
     h2d = N_PROBE * 8 + N_PROBE // 8
     d2h = expected * 16 + 3 * ((expected + 31) // 32 * 4)
-    return {"value": world * N_PROBE * args.steps / t, "unit": "rows/s", "h2d_bytes_per_step": h2d,
+    return {"value": whole_job_rate(world, N_PROBE * args.steps, t), "unit": "rows/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps}
 
 
