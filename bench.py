@@ -285,7 +285,7 @@ def run_gpu(args, rank, world):
                     batched=None, join5=None)
     if args.only == "join5":
         j5 = run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world, rank)
-        d = j5["s=1.1"]["learned_range_partitioned"]
+        d = j5["s=1.1"]["learned_choice"]
         return dict(value=d["value"], ms=d["ms_per_step"], build_ms=0.0, launches=0, roofline=None, clocks=None,
                     e2e=None, agg=None, rows=d["output_rows"], skew=None, batched=None, join5=j5)
     if args.only == "batched":
@@ -965,13 +965,17 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         splits = omg.learn_splits(sample, bits=bits, epochs=2000)
         learn_ms = (time.perf_counter() - t0) * 1e3
         per = {}
+        chosen = {}
         for name, strat in (("direct", omg.JOIN_DIRECT), ("hash_partitioned", omg.JOIN_HASH_PARTITIONED),
-                            ("learned_range_partitioned", omg.JOIN_RANGE_PARTITIONED)):
+                            ("learned_range_partitioned", omg.JOIN_RANGE_PARTITIONED),
+                            ("learned_choice", omg.JOIN_LEARNED)):
             def step(fp=False):
                 op = pf.create_operator()
                 op.set_stream(stream.cuda_stream)
                 op.set_device_output(True)
-                op.set_join_strategy(strat, bits, splits if strat == omg.JOIN_RANGE_PARTITIONED else None)
+                op.set_join_strategy(strat, bits,
+                                     splits if strat in (omg.JOIN_RANGE_PARTITIONED, omg.JOIN_LEARNED) else None)
+                chosen[name] = op.join_strategy()
                 op.add_input(omg.wrap_device_batch([L], npb, [pkey.data_ptr()]))
                 outs, rows = op.get_outputs(1 << 20)
                 f = omg.batches_fingerprint(outs) if fp else None
@@ -992,6 +996,8 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         ref = per["direct"]["fingerprint"]
         assert all(v["fingerprint"] == ref and v["output_rows"] == per["direct"]["output_rows"] for v in per.values())
         top = float(cdf_top_share(torch, nb, s, dev))
+        per["learned_choice"]["strategy"] = {0: "direct", 1: "hash_partitioned", 2: "range_partitioned"}[
+            chosen["learned_choice"]]
         per["splits_learn_ms"] = round(learn_ms, 1)
         per["top_key_share"] = round(top, 4)
         out[f"s={s}"] = per

@@ -335,7 +335,14 @@ int32_t omg_agg_batch_destroy(void *batch);
 #define OMG_JOIN_DIRECT 0
 #define OMG_JOIN_HASH_PARTITIONED 1
 #define OMG_JOIN_RANGE_PARTITIONED 2
+/* OMG_JOIN_LEARNED: learned splits (omg_join_learn_splits) decide the strategy: a run of equal
+ * splits longer than 7.5% of the partitions (a key with about 15% of the probe rows) selects the
+ * direct probe, which keeps such hot keys in cache; otherwise the hash-partitioned probe with
+ * 2^bits partitions. */
+#define OMG_JOIN_LEARNED 3
 int32_t omg_op_set_join_strategy(void *op, int32_t strategy, int32_t bits, const int64_t *splits, int32_t n_splits);
+/* The strategy in effect (OMG_JOIN_LEARNED resolved to the one it chose). */
+int32_t omg_op_join_strategy(void *op, int32_t *strategy);
 /* Range splits learned from a sample of probe keys: a two-stage model of the keys' CDF (a small
  * network trained on the GPU routes each key to a linear leaf); splits are its 1/2^bits quantile
  * crossings.  Writes 2^bits - 1 sorted splits to `splits`. */

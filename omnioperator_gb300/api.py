@@ -345,6 +345,12 @@ class Operator:
             check(lib().omg_op_set_join_strategy(self.handle, strategy, bits,
                                                  a.ctypes.data_as(C.POINTER(C.c_int64)), len(a)))
 
+    def join_strategy(self) -> int:
+        """The probe strategy in effect (JOIN_LEARNED resolved)."""
+        out = C.c_int32(0)
+        check(lib().omg_op_join_strategy(self.handle, C.byref(out)))
+        return out.value
+
     def sizing_log(self) -> dict:
         """HashAggregation sizing record (omg_op_get_sizing_log)."""
         arr = (C.c_int64 * 32)()
@@ -649,7 +655,7 @@ class AggBatch:
             self.handle = None
 
 
-JOIN_DIRECT, JOIN_HASH_PARTITIONED, JOIN_RANGE_PARTITIONED = 0, 1, 2
+JOIN_DIRECT, JOIN_HASH_PARTITIONED, JOIN_RANGE_PARTITIONED, JOIN_LEARNED = 0, 1, 2, 3
 
 
 def learn_splits(sample, bits: int = 12, epochs: int = 2000, seed: int = 1) -> np.ndarray:

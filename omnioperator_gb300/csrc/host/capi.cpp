@@ -787,6 +787,15 @@ int32_t omg_op_set_join_strategy(void *op, int32_t strategy, int32_t bits, const
     });
 }
 
+int32_t omg_op_join_strategy(void *op, int32_t *strategy)
+{
+    return Guard([&] {
+        auto *j = dynamic_cast<omniruntime::op::LookupJoinOperator *>(AsOp(op));
+        Require(j != nullptr && strategy != nullptr, "not a LookupJoin operator");
+        *strategy = j->JoinStrategy();
+    });
+}
+
 int32_t omg_join_learn_splits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed,
     int64_t *splits)
 {

@@ -34,6 +34,15 @@ struct JoinPartBuild;
 constexpr int32_t kJoinDirect = 0;           // one table for the whole build (default)
 constexpr int32_t kJoinHashPartitioned = 1;  // 2^bits hash partitions per side
 constexpr int32_t kJoinRangePartitioned = 2; // 2^bits key ranges per side, from 2^bits - 1 splits
+// Learned: the splits learned from the probe keys decide.  A run of equal splits longer than
+// kLearnedDirectRun of the partitions marks a hot key of about twice that probe share (the leaf
+// models put a repeated key's CDF at its mid rank, so a key holding a share q of the rows repeats
+// as about q/2 * 2^bits splits); such a key makes the direct probe, which keeps it in cache, the
+// choice.  Otherwise the probe is hash-partitioned: on the skewed join workload hash partitions,
+// with equal build keys each, probe faster than range partitions balanced by probe rows, whose
+// cold partitions hold most build keys.
+constexpr int32_t kJoinLearned = 3;
+constexpr double kLearnedDirectRun = 0.075;
 
 class HashBuilderOperatorFactory : public OperatorFactory {
 public:
@@ -116,6 +125,8 @@ public:
     // 8-byte keys, NULL-free build output columns and the probe key as the only probe output;
     // other shapes keep the direct probe.  Results do not depend on the strategy.
     void SetJoinStrategy(int32_t strategy, int32_t bits, const int64_t *splits, int32_t nSplits);
+    // The strategy the batches processed afterwards use (kJoinLearned resolved).
+    int32_t JoinStrategy() const { return strategy_; }
 
 private:
     struct Impl;

@@ -247,3 +247,23 @@ def test_spill_settings_are_checked_on_the_host():
         assert e.value.status == -2
         op.delete()
         fac.close()
+
+
+def test_learned_join_strategy_choice():
+    """JOIN_LEARNED reads a hot key off the learned splits (a run of equal splits longer than 7.5%
+    of the partitions): then the direct probe, otherwise hash partitions."""
+    L = omg.LongType()
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L], [0])
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1], [L], bf)
+    op = pf.create_operator()
+    spread = np.arange(15, dtype=np.int64) * 100  # 2^4 - 1 distinct splits
+    hot = np.array([0, 100, 200, 500, 500, 500, 500, 500, 600, 700, 800, 900, 1000, 1100, 1200], dtype=np.int64)
+    op.set_join_strategy(omg.JOIN_LEARNED, 4, spread)
+    assert op.join_strategy() == omg.JOIN_HASH_PARTITIONED
+    op.set_join_strategy(omg.JOIN_LEARNED, 4, hot)  # a run of 5 of 16 splits
+    assert op.join_strategy() == omg.JOIN_DIRECT
+    op.set_join_strategy(omg.JOIN_RANGE_PARTITIONED, 4, hot)
+    assert op.join_strategy() == omg.JOIN_RANGE_PARTITIONED
+    op.delete()
+    pf.close()
+    bf.close()
