@@ -67,19 +67,23 @@ def _key(r):
     return tuple((x is None, 0 if x is None else x) for x in r)
 
 
-def test_reference_inner_join_with_int_filter():
-    """join_test.cpp:1545-1625 (TestInnerEqualityJoinWithIntFilter): build (int, int), probe
-    (int, int) with the probe's second column NULL at rows 4 and 9, filter #1 != #3; expected
-    rows (20, 35709, 20, 31904), (16, 35709, 16, 31904), (19, 35709, 19, 31904)."""
-    b0 = np.array([19, 14, 7, 19, 1, 20, 10, 13, 20, 16], dtype=np.int32)
-    b1 = np.array([35709, 31904, 35709, 31904, 35709, 31904, 35709, 31904, 35709, 31904], dtype=np.int32)
-    p0 = np.array([20, 16, 13, 4, 20, 4, 22, 19, 8, 7], dtype=np.int32)
-    p1 = np.array([35709, 35709, 31904, 12477, 31904, 38721, 90419, 35709, 88371, 35709], dtype=np.int32)
-    pm = np.array([i % 5 == 4 for i in range(10)])
-    none = np.zeros(10, bool)
+@pytest.mark.parametrize("odd", [False, True])
+def test_reference_inner_join_with_int_filter(odd):
+    """join_test.cpp:1545-1625 (TestInnerEqualityJoinWithIntFilter) and :1627-1705 (its odd-size
+    twin with an 11th row on both sides): build (int, int), probe (int, int) with the probe's second
+    column NULL at every fifth row from row 4, filter #1 != #3; expected rows
+    (20, 35709, 20, 31904), (16, 35709, 16, 31904), (19, 35709, 19, 31904)."""
+    b0 = [19, 14, 7, 19, 1, 20, 10, 13, 20, 16] + ([15] if odd else [])
+    b1 = [35709, 31904, 35709, 31904, 35709, 31904, 35709, 31904, 35709, 31904] + ([31904] if odd else [])
+    p0 = [20, 16, 13, 4, 20, 4, 22, 19, 8, 7] + ([11] if odd else [])
+    p1 = [35709, 35709, 31904, 12477, 31904, 38721, 90419, 35709, 88371, 35709] + ([35709] if odd else [])
+    n = len(p0)
+    b0, b1, p0, p1 = (np.array(x, dtype=np.int32) for x in (b0, b1, p0, p1))
+    pm = np.array([i % 5 == 4 for i in range(n)])
+    none = np.zeros(n, bool)
     filt = B(omg.EXPR_NEQ, F(1, I), F(3, I))
     rows = run("INNER", "UNKNOWN", [I, I], [b0, b1], [none, none], [I, I], [p0, p1], [none, pm], [0, 1], [0, 1],
-               filt, batch_sizes=(10,))
+               filt, batch_sizes=(n,))
     assert sorted(rows) == sorted([(20, 35709, 20, 31904), (16, 35709, 16, 31904), (19, 35709, 19, 31904)])
 
 
