@@ -124,3 +124,37 @@ def test_dictionary_batch_copies_flatten():
         omg.free_batch(h)
     assert list(mask) == [False, False, True, True, False, False, False]
     assert [int(x) for x, m in zip(got, mask) if not m] == [40, 10, 30, 40, 10]
+
+
+def test_reference_inner_join_on_dictionary_keys():
+    """join_test.cpp:1333-1398 (TestInnerEqualityJoinDictionary): build (long, dictionary long)
+    and probe (long, dictionary long) joined on their dictionary columns -> (1, 11, 2, 11) and
+    (3, 33, 4, 33)."""
+    ids = np.array([0, 1, 2, 3], dtype=np.int32)
+
+    def batch(flat, dict_values):
+        d = omg.new_host_vector(L, np.array(dict_values, dtype=np.int64))
+        out = C.c_void_p()
+        omg.check(omg.lib().omg_batch_new(4, C.byref(out)))
+        omg.check(omg.lib().omg_batch_append(out.value, omg.new_host_vector(L, np.array(flat, dtype=np.int64))))
+        omg.check(omg.lib().omg_batch_append(out.value, omg.new_dictionary_vector(ids, d)))
+        omg.lib().omg_vec_free(d)
+        return out.value
+
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L], [1])
+    bop = bf.create_operator()
+    bop.add_input(batch([1, 2, 3, 4], [111, 11, 333, 33]))
+    bop.get_output()
+    pf = omg.LookupJoinOperatorFactory([L, L], [0, 1], [1], [0, 1], [L, L], bf)
+    pop = pf.create_operator()
+    pop.add_input(batch([1, 2, 3, 4], [11, 22, 33, 44]))
+    rows = []
+    for b in pop.drain():
+        cols = omg.batch_to_numpy(b)
+        omg.free_batch(b)
+        rows += [tuple(int(v[i]) for v, _ in cols) for i in range(len(cols[0][0]))]
+    pop.delete()
+    pf.close()
+    bop.delete()
+    bf.close()
+    assert sorted(rows) == [(1, 11, 2, 11), (3, 33, 4, 33)]
