@@ -1721,12 +1721,22 @@ __global__ void __launch_bounds__(512) PartHistKernel(const __grid_constant__ Ag
     for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
         const TileDesc tile = p.tiles[t];
         const BatchDesc &b = p.batches[tile.batch];
-        for (int r0 = 0; r0 < tile.rows; r0 += blockDim.x) {
-            const int r = r0 + threadIdx.x;
-            const unsigned int active = __ballot_sync(0xffffffffu, r < tile.rows);
-            if (r < tile.rows) {
-                const RowKey k = ReadKey(p.key, b, static_cast<int64_t>(tile.row0) + r, kKind);
-                WarpAggAdd(h, PartOf(k.hash, a.partBits), active);
+        // Four rows per thread per step: their key loads are in flight together.
+        for (int r0 = 0; r0 < tile.rows; r0 += 4 * static_cast<int>(blockDim.x)) {
+            int q[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int r = r0 + j * static_cast<int>(blockDim.x) + static_cast<int>(threadIdx.x);
+                q[j] = r < tile.rows ? PartOf(ReadKey(p.key, b, static_cast<int64_t>(tile.row0) + r, kKind).hash,
+                                              a.partBits)
+                                     : -1;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const unsigned int active = __ballot_sync(0xffffffffu, q[j] >= 0);
+                if (q[j] >= 0) {
+                    WarpAggAdd(h, q[j], active);
+                }
             }
         }
     }
