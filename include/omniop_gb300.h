@@ -400,7 +400,8 @@ int32_t omg_op_get_counters(void *op, int64_t *out, int32_t n);
  * The group table and launch descriptors live in a fixed 64 MiB device array inside the
  * library (held by every GPU that loads it, until the process exits); a call is rejected with
  * OMG_ERR_INVALID_ARG when max_groups and n_rows would not fit in it, or when the input turns
- * out to have more than max_groups groups.
+ * out to have more than max_groups groups (num_groups is then left unchanged); a bounded
+ * device-side wait that ran out returns OMG_ERR_TIMEOUT (omg_debug_set_wait_budget applies).
  *   d_cols[n_cols], d_nulls[n_cols]: device values / null bitmaps by batch column index
  *     (d_nulls or an entry may be NULL: no nulls); the factory's column indices select from them.
  *   d_out_values[n_out], d_out_nulls[n_out]: the caller's device output columns (group-by

@@ -1001,6 +1001,7 @@ int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const 
     }
     np.overflowAsNull = ap.overflowAsNull;
     np.smemSlots = ap.smemSlots;
+    np.waitBudget = omg::WaitBudget();
     const omg::NoAllocStatus st = omg::RunAggNoAlloc(np, d_cols, d_nulls, n_cols, n_rows, d_out_values, d_out_nulls,
         n_out, max_groups, num_groups, static_cast<cudaStream_t>(stream));
     if (st.code != 0) {

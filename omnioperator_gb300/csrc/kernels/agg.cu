@@ -1972,19 +1972,7 @@ __global__ void SketchStatsKernel(const unsigned long long *tabKeys, const unsig
     }
 }
 
-int NumSMs()
-{
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) {
-            n = 1;
-        }
-    }
-    return n;
-}
+int NumSMs() { return DeviceSMCount(); }
 
 }  // namespace
 
@@ -2024,35 +2012,21 @@ cudaError_t LaunchAgg(const AggLaunch &p, uint64_t *spill, unsigned int *nSpill,
             return cudaErrorInvalidValue;
         }
         auto pk = p.key.kind == KEY_SINGLE ? AggPartKernel<KEY_SINGLE> : AggPartKernel<KEY_PACKED>;
-        static bool partConfigured[2] = {false, false};
-        bool &pc = partConfigured[p.key.kind == KEY_SINGLE ? 0 : 1];
-        if (!pc) {
-            cudaError_t err =
-                cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kPartSmemBytes));
-            if (err != cudaSuccess) {
-                return err;
-            }
-            pc = true;
+        cudaError_t err = EnsureDynamicSmem(reinterpret_cast<const void *>(pk), kPartSmemBytes);
+        if (err != cudaSuccess) {
+            return err;
         }
         const int perPart = NumSMs() / p.nParts > 0 ? NumSMs() / p.nParts : 1;
         pk<<<perPart * p.nParts, kPartThreads, smemBytes, stream>>>(p, sp);
         return cudaGetLastError();
     }
     auto kernel = p.key.kind == KEY_SINGLE ? AggKernel<KEY_SINGLE> : AggKernel<KEY_PACKED>;
-    static size_t configured[2] = {0, 0};
-    size_t &conf = configured[p.key.kind == KEY_SINGLE ? 0 : 1];
-    if (smemBytes > 48 * 1024 && smemBytes > conf) {
-        cudaError_t err =
-            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smemBytes));
-        if (err != cudaSuccess) {
-            return err;
-        }
-        conf = smemBytes;
+    cudaError_t err = EnsureDynamicSmem(reinterpret_cast<const void *>(kernel), smemBytes);
+    if (err != cudaSuccess) {
+        return err;
     }
     if (gridBlocks <= 0) {
-        int perSM = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, kAggThreads, smemBytes);
-        gridBlocks = NumSMs() * (perSM > 0 ? perSM : 1);
+        gridBlocks = NumSMs() * BlocksPerSM(reinterpret_cast<const void *>(kernel), kAggThreads, smemBytes);
     }
     kernel<<<gridBlocks, kAggThreads, smemBytes, stream>>>(p, sp);
     return cudaGetLastError();
@@ -2111,8 +2085,6 @@ cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtr
     return err;
 }
 
-int DeviceSMCount() { return NumSMs(); }
-
 cudaError_t LaunchAggTaskSketch(const AggLaunch &p, int32_t nTasks, unsigned long long *stats, cudaStream_t stream)
 {
     if (nTasks <= 0) {
@@ -2162,9 +2134,8 @@ cudaError_t LaunchAggTasks(const AggLaunch &p, int32_t variant, cudaStream_t str
         return cudaErrorInvalidValue;
     }
     const TasksVariant &v = kTasksVariants[variant];
-    int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, p.key.kind == KEY_SINGLE ? v.single : v.packed, v.threads, 0);
-    perSM = perSM < 1 ? 1 : (perSM > v.blocksPerSM ? v.blocksPerSM : perSM);
+    int perSM = BlocksPerSM(reinterpret_cast<const void *>(p.key.kind == KEY_SINGLE ? v.single : v.packed), v.threads, 0);
+    perSM = perSM > v.blocksPerSM ? v.blocksPerSM : perSM;
     int grid = NumSMs() * perSM;
     if (grid > p.nTiles) {
         grid = p.nTiles;

@@ -185,7 +185,7 @@ NoAllocStatus RunAggNoAlloc(const NoAllocPlan &plan, const void *const *cols, co
     p.nRetry = reinterpret_cast<unsigned int *>(ctr + 1);
     p.retryCap = 0;  // nowhere to queue a row: an unplaceable row is an error
     p.error = reinterpret_cast<int32_t *>(ctr + 3);
-    p.waitBudget = kDefaultWaitBudget;
+    p.waitBudget = plan.waitBudget > 0 ? plan.waitBudget : kDefaultWaitBudget;
     p.batches = desc;
     p.tiles = tiles;
     p.nTiles = nTiles;
@@ -207,8 +207,17 @@ NoAllocStatus RunAggNoAlloc(const NoAllocPlan &plan, const void *const *cols, co
         (err = cudaStreamSynchronize(stream)) != cudaSuccess) {
         return fail(err, "read counters");
     }
-    if (h[3] != 0 || h[1] != 0 || h[2] != 0 || static_cast<int64_t>(h[4]) > maxGroups) {
+    // h[3] is the device error word: 7 = a bounded wait for another thread's slot publication
+    // ran out; 4 = a row found no slot within the probe limit (no retry queue here, so the table
+    // of 2 * max_groups slots overflowed).
+    if (h[3] == 7) {
+        return error(-7, "a bounded device-side wait ran out (slot publication)");
+    }
+    if (h[3] == 4 || h[1] != 0 || static_cast<int64_t>(h[4]) > maxGroups) {
         return error(-1, "the input has more than max_groups = %lld groups", maxGroups);
+    }
+    if (h[3] != 0 || h[2] != 0) {
+        return error(-9, "internal error %lld in the aggregation kernel", static_cast<long long>(h[3]));
     }
     const int64_t groups = static_cast<int64_t>(h[4]);
     AggExtract e;

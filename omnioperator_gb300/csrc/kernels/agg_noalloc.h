@@ -32,6 +32,7 @@ struct NoAllocPlan {
     OutSpec outs[kMaxOutCols] = {};
     bool overflowAsNull = false;
     int32_t smemSlots = 0;
+    long long waitBudget = kDefaultWaitBudget;  // clock64 ticks of a bounded device-side wait
 };
 
 struct NoAllocStatus {

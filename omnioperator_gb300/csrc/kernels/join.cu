@@ -1528,12 +1528,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         return cudaSuccess;
     }
     if (p.nKeyCols > 0 || p.nFilter > 0) {
-        static int kindBlocks = 0;
-        if (kindBlocks <= 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kindBlocks, ProbeKindKernel, kProbeThreads, 0);
-            kindBlocks = kindBlocks <= 0 ? 1 : kindBlocks;
-        }
-        const int maxGrid = SMs() * kindBlocks;
+        const int maxGrid = SMs() * BlocksPerSM(reinterpret_cast<const void *>(ProbeKindKernel), kProbeThreads, 0);
         ProbeKindKernel<<<p.nTiles < maxGrid ? p.nTiles : maxGrid, kProbeThreads, 0, stream>>>(p);
         return cudaGetLastError();
     }
@@ -1587,7 +1582,6 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
                 reinterpret_cast<const void *>(ProbeBitsKernel<4, 0, false>)},
         };
         constexpr int kInsts = static_cast<int>(sizeof(insts) / sizeof(insts[0]));
-        static bool smemSet[kInsts][2] = {};
         int pick = -1;
         for (int i = 0; i < kInsts && pick < 0; ++i) {
             if (insts[i].nOut != p.nOut) {
@@ -1602,13 +1596,9 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         }
         const int single = p.singleBatch ? 0 : 1;
         const void *kernel = single == 0 ? insts[pick].single : insts[pick].tiled;
-        if (!smemSet[pick][single]) {
-            cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                static_cast<int>(kBitsMaxSmem));
-            if (err != cudaSuccess) {
-                return err;
-            }
-            smemSet[pick][single] = true;
+        cudaError_t err = EnsureDynamicSmem(kernel, kBitsMaxSmem);
+        if (err != cudaSuccess) {
+            return err;
         }
         const int64_t items = static_cast<int64_t>(p.nTiles) * kBitsSegsPerTile;
         const int64_t warpsPerCta = kBitsThreads / 32;
@@ -1621,35 +1611,20 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         auto kk = !p.table.unique ? ProbeKernel<false, false, true>
                                   : (p.table.slotPayload != nullptr ? ProbeKernel<true, true, true>
                                                                     : ProbeKernel<true, false, true>);
-        static int kkBlocks[3] = {0, 0, 0};
-        const int w = !p.table.unique ? 0 : (p.table.slotPayload != nullptr ? 2 : 1);
-        if (kkBlocks[w] <= 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kkBlocks[w], kk, kProbeThreads, 0);
-            kkBlocks[w] = kkBlocks[w] <= 0 ? 1 : kkBlocks[w];
-        }
-        const int maxGrid = SMs() * kkBlocks[w];
+        const int maxGrid = SMs() * BlocksPerSM(reinterpret_cast<const void *>(kk), kProbeThreads, 0);
         kk<<<p.nTiles < maxGrid ? p.nTiles : maxGrid, kProbeThreads, 0, stream>>>(p);
         return cudaGetLastError();
     }
     auto kernel = !p.table.unique ? ProbeKernel<false, false, false>
                                   : (p.table.slotPayload != nullptr ? ProbeKernel<true, true, false>
                                                                     : ProbeKernel<true, false, false>);
-    int which = !p.table.unique ? 0 : (p.table.slotPayload != nullptr ? 2 : 1);
     if (fast) {
         const void *fk[kFastMaxOut] = {reinterpret_cast<const void *>(ProbeFastKernel<1>),
             reinterpret_cast<const void *>(ProbeFastKernel<2>), reinterpret_cast<const void *>(ProbeFastKernel<3>),
             reinterpret_cast<const void *>(ProbeFastKernel<4>)};
         kernel = reinterpret_cast<decltype(kernel)>(fk[p.nOut - 1]);
-        which = 2 + p.nOut;
     }
-    static int blocksPerSM[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (blocksPerSM[which] <= 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM[which], kernel, kProbeThreads, 0);
-        if (blocksPerSM[which] <= 0) {
-            blocksPerSM[which] = 1;
-        }
-    }
-    const int maxGrid = SMs() * blocksPerSM[which];
+    const int maxGrid = SMs() * BlocksPerSM(reinterpret_cast<const void *>(kernel), kProbeThreads, 0);
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
     kernel<<<grid, kProbeThreads, 0, stream>>>(p);
     return cudaGetLastError();

@@ -405,19 +405,14 @@ cudaError_t LaunchKeyPartition(const int64_t *keys, const uint8_t *nulls, int64_
     uint8_t *outPay, cudaStream_t stream)
 {
     const int P = 1 << f.bits;
-    static bool configured = false;
     const size_t smemHist = kRangeSmem + sizeof(unsigned int) * P;
     const size_t smemScatter = kRangeSmem + sizeof(unsigned long long) * P;
-    if (!configured) {
-        const int maxBytes = static_cast<int>(kRangeSmem + sizeof(unsigned long long) * kMaxJoinParts);
-        cudaError_t err = cudaFuncSetAttribute(KeyHistKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxBytes);
-        if (err == cudaSuccess) {
-            err = cudaFuncSetAttribute(KeyScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxBytes);
-        }
-        if (err != cudaSuccess) {
-            return err;
-        }
-        configured = true;
+    cudaError_t err = EnsureDynamicSmem(reinterpret_cast<const void *>(KeyHistKernel), smemHist);
+    if (err == cudaSuccess) {
+        err = EnsureDynamicSmem(reinterpret_cast<const void *>(KeyScatterKernel), smemScatter);
+    }
+    if (err != cudaSuccess) {
+        return err;
     }
     const int grid = nChunks < SMs() * 4 ? nChunks : SMs() * 4;
     KeyHistKernel<<<grid, kPartThreads, smemHist, stream>>>(keys, nulls, n, f, nChunks, hist);
@@ -442,20 +437,14 @@ cudaError_t LaunchPartProbe(const PartProbeLaunch &q, cudaStream_t stream)
     if (q.n <= 0) {
         return cudaSuccess;
     }
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t err = cudaFuncSetAttribute(PartProbeKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-            static_cast<int>(kRangeSmem));
-        if (err != cudaSuccess) {
-            return err;
-        }
-        configured = true;
+    cudaError_t err = EnsureDynamicSmem(reinterpret_cast<const void *>(PartProbeKernel), kRangeSmem);
+    if (err != cudaSuccess) {
+        return err;
     }
-    int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, PartProbeKernel, 256, SplitsSmem(q.fn));
+    const int perSM = BlocksPerSM(reinterpret_cast<const void *>(PartProbeKernel), 256, SplitsSmem(q.fn));
     const int64_t segs = (q.n + kProbeRounds * 32 - 1) / (kProbeRounds * 32);
     const int64_t want = (segs + 7) / 8;
-    const int64_t cap = static_cast<int64_t>(SMs()) * (perSM > 0 ? perSM : 1);
+    const int64_t cap = static_cast<int64_t>(SMs()) * perSM;
     PartProbeKernel<<<static_cast<unsigned>(want < cap ? want : cap), 256, SplitsSmem(q.fn), stream>>>(q);
     return cudaGetLastError();
 }

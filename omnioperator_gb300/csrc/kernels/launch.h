@@ -8,7 +8,15 @@
 
 namespace omg {
 
+// SM count of the current device (cached per device).
 int DeviceSMCount();
+// Raises `kernel`'s dynamic shared-memory limit on the current device to at least `bytes`.
+// The attribute belongs to one device, so the record of what was set is kept per device (and
+// guarded by a mutex: operators launch from several host threads).
+cudaError_t EnsureDynamicSmem(const void *kernel, size_t bytes);
+// CTAs of `kernel` resident per SM at (threads, dynamic shared memory) on the current device,
+// at least 1; cached per (device, kernel, threads, bytes).
+int BlocksPerSM(const void *kernel, int threads, size_t smemBytes);
 
 // ---- aggregation (agg.cu)
 cudaError_t LaunchAggInitTable(const AggLaunch &p, cudaStream_t stream);

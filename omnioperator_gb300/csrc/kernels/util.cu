@@ -2,6 +2,9 @@
 // runs produced the same row multiset without copying the rows out).
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "device_common.cuh"
 #include "launch.h"
@@ -53,7 +56,78 @@ __global__ void FingerprintKernel(const BatchDesc *batches, const TileDesc *tile
     }
 }
 
+std::mutex g_attrMutex;
+// (device, kernel) -> dynamic shared-memory limit set so far.
+std::map<std::tuple<int, const void *>, size_t> g_smemSet;
+// (device, kernel, threads, bytes) -> CTAs per SM.
+std::map<std::tuple<int, const void *, int, size_t>, int> g_blocksPerSM;
+std::map<int, int> g_smCount;
+
+int CurrentDevice()
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev;
+}
+
 }  // namespace
+
+int DeviceSMCount()
+{
+    const int dev = CurrentDevice();
+    std::lock_guard<std::mutex> lock(g_attrMutex);
+    auto it = g_smCount.find(dev);
+    if (it != g_smCount.end()) {
+        return it->second;
+    }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 1;
+    }
+    g_smCount[dev] = n;
+    return n;
+}
+
+cudaError_t EnsureDynamicSmem(const void *kernel, size_t bytes)
+{
+    if (bytes <= 48 * 1024) {
+        return cudaSuccess;
+    }
+    const auto key = std::make_tuple(CurrentDevice(), kernel);
+    std::lock_guard<std::mutex> lock(g_attrMutex);
+    auto it = g_smemSet.find(key);
+    if (it != g_smemSet.end() && it->second >= bytes) {
+        return cudaSuccess;
+    }
+    const cudaError_t err =
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    if (err == cudaSuccess) {
+        g_smemSet[key] = bytes;
+    }
+    return err;
+}
+
+int BlocksPerSM(const void *kernel, int threads, size_t smemBytes)
+{
+    const auto key = std::make_tuple(CurrentDevice(), kernel, threads, smemBytes);
+    {
+        std::lock_guard<std::mutex> lock(g_attrMutex);
+        auto it = g_blocksPerSM.find(key);
+        if (it != g_blocksPerSM.end()) {
+            return it->second;
+        }
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smemBytes) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    n = n > 0 ? n : 1;
+    std::lock_guard<std::mutex> lock(g_attrMutex);
+    g_blocksPerSM[key] = n;
+    return n;
+}
 
 cudaError_t LaunchFingerprint(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, int32_t nCols,
     const int32_t *widths, unsigned long long *out, cudaStream_t stream)

@@ -2,10 +2,13 @@
 
 It exists for callers that cannot let the library allocate device memory: an engine that keeps
 all device memory in its own pre-reserved pool, or code running where allocation calls are not
-permitted.  Its scratch is a fixed device array inside the library, shared by every call.  This
-test checks its output against the operator API (the existing entry point) on the same inputs,
-for two calls in a row (the second call must not see the first call's leftovers).  It sits in a
-file of its own that pytest collects last, and passes alone in a fresh process as well.
+permitted.  Its scratch is a fixed device array inside the library, shared by every call.  These
+tests check its output against the operator API (the existing entry point) and against the
+oracle on the same inputs, for two calls in a row (the second call must not see the first
+call's leftovers), with and without null bitmaps, and its two rejections: a size beyond the
+scratch (before any device work) and an input with more groups than max_groups (found on the
+device).  They sit in a file of their own that pytest collects last, and pass alone in a fresh
+process as well.
 """
 import ctypes as C
 
@@ -13,7 +16,8 @@ import numpy as np
 import pytest
 
 import omnioperator_gb300 as omg
-from helpers import DOUBLE_TOL, run_agg
+import oracle
+from helpers import DOUBLE_TOL, assert_agg_equal, exact_by_key, run_agg
 
 pytestmark = pytest.mark.gpu
 
@@ -47,7 +51,10 @@ def _rows(cols):
     return out
 
 
-def _run_noalloc(fac, key, v1, v2, km, m1, max_groups, out_rows=None):
+def _run_noalloc(fac, key, v1, v2, km, m1, max_groups, out_rows=None, num_groups=None):
+    """One omg_hashagg_run_noalloc call over device copies of the columns.  km / m1 None: the
+    call gets a NULL null-bitmap array (no column has nulls).  Returns (output columns, groups);
+    `num_groups` (a c_int64) receives the group count when given."""
     L_ = omg.lib()
     host = omg.make_batch([L, L, D], [key, v1, v2], [km, m1, None])
     dev = omg.batch_to_device(host)
@@ -55,8 +62,11 @@ def _run_noalloc(fac, key, v1, v2, km, m1, max_groups, out_rows=None):
     outs = []
     try:
         cols = (C.c_void_p * 3)(*[L_.omg_vec_values(L_.omg_batch_get(dev, i)) for i in range(3)])
-        nulls = (C.c_void_p * 3)(*[L_.omg_vec_nulls(L_.omg_batch_get(dev, i)) if L_.omg_vec_has_null(
-            L_.omg_batch_get(dev, i)) else None for i in range(3)])
+        if km is None and m1 is None:
+            nulls = None
+        else:
+            nulls = (C.c_void_p * 3)(*[L_.omg_vec_nulls(L_.omg_batch_get(dev, i)) if L_.omg_vec_has_null(
+                L_.omg_batch_get(dev, i)) else None for i in range(3)])
         # The caller allocates the outputs (here through the library's device vectors).
         for t in OUT_TYPES:
             v = C.c_void_p()
@@ -65,7 +75,7 @@ def _run_noalloc(fac, key, v1, v2, km, m1, max_groups, out_rows=None):
             outs.append(v.value)
         ov = (C.c_void_p * len(outs))(*[L_.omg_vec_values(v) for v in outs])
         on = (C.c_void_p * len(outs))(*[L_.omg_vec_nulls(v) for v in outs])
-        ng = C.c_int64(-1)
+        ng = C.c_int64(-1) if num_groups is None else num_groups
         rc = L_.omg_hashagg_run_noalloc(fac.handle, cols, nulls, 3, len(key), ov, on, len(outs), max_groups,
                                         C.byref(ng), None)
         omg._capi.check(rc)
@@ -99,6 +109,60 @@ def _assert_same(a, b):
                 assert abs(float(x) - float(y)) <= DOUBLE_TOL * max(abs(float(y)), 1.0), (k, j, x, y)
             else:
                 assert int(x) == int(y), (k, j, x, y)
+
+
+def _assert_matches_oracle(got, key, km, v1, m1, v2):
+    ora = oracle.hashagg(
+        [key], [oracle.T_LONG], [km],
+        [dict(func=oracle.F_SUM, col=v1, in_type=oracle.T_LONG, out_type=oracle.T_LONG, nulls=m1),
+         dict(func=oracle.F_COUNT_COL, col=v1, in_type=oracle.T_LONG, out_type=oracle.T_LONG, nulls=m1),
+         dict(func=oracle.F_MIN, col=v1, in_type=oracle.T_LONG, out_type=oracle.T_LONG, nulls=m1),
+         dict(func=oracle.F_MAX, col=v1, in_type=oracle.T_LONG, out_type=oracle.T_LONG, nulls=m1),
+         dict(func=oracle.F_SUM, col=v2, in_type=oracle.T_DOUBLE, out_type=oracle.T_DOUBLE),
+         dict(func=oracle.F_AVG, col=v2, in_type=oracle.T_DOUBLE, out_type=oracle.T_DOUBLE)])
+    ex_sum = exact_by_key([key], [km], v2, None)
+    ex_avg = exact_by_key([key], [km], v2, None, divide_by_count=True)
+    assert_agg_equal(got, ora, 1, double_aggs=(4, 5), exact={4: ex_sum, 5: ex_avg})
+
+
+def test_noalloc_matches_oracle_twice_with_and_without_nulls(gpu):
+    """Two calls in a row on one factory: the first with NULL keys and values, the second with
+    no null bitmaps at all (d_nulls = NULL) and fewer groups, each against the oracle."""
+    fac = omg.HashAggregationOperatorFactory([0], [L], SPEC["aggs_cols"], SPEC["agg_in_types"],
+                                             SPEC["agg_out_types"], SPEC["funcs"])
+    try:
+        key, v1, v2, km, m1 = _data(11, groups=2500)
+        got, ng = _run_noalloc(fac, key, v1, v2, km, m1, max_groups=4096)
+        _assert_matches_oracle(got, key, km, v1, m1, v2)
+        key, v1, v2, _, _ = _data(12, groups=300)
+        got, ng = _run_noalloc(fac, key, v1, v2, None, None, max_groups=4096)
+        assert ng == len(np.unique(key))
+        _assert_matches_oracle(got, key, None, v1, None, v2)
+    finally:
+        fac.close()
+
+
+def test_noalloc_rejects_more_groups_than_max_groups(gpu):
+    """5,000 distinct keys with max_groups = 1,024: the table (2,048 slots) overflows on the
+    device; the call returns OMG_ERR_INVALID_ARG and leaves num_groups untouched.  A call that
+    follows on the same factory still agrees with the oracle."""
+    fac = omg.HashAggregationOperatorFactory([0], [L], SPEC["aggs_cols"], SPEC["agg_in_types"],
+                                             SPEC["agg_out_types"], SPEC["funcs"])
+    try:
+        key = np.arange(5000, dtype=np.int64) * 7919
+        rng = np.random.default_rng(5)
+        v1 = rng.integers(-100, 100, len(key), dtype=np.int64)
+        v2 = rng.random(len(key))
+        ng = C.c_int64(-12345)
+        with pytest.raises(omg.OmgError) as e:
+            _run_noalloc(fac, key, v1, v2, None, None, max_groups=1024, num_groups=ng)
+        assert e.value.status == -1 and "max_groups" in e.value.message  # OMG_ERR_INVALID_ARG
+        assert ng.value == -12345
+        key, v1, v2, km, m1 = _data(13, n=40_000, groups=900)
+        got, _ = _run_noalloc(fac, key, v1, v2, km, m1, max_groups=1024)
+        _assert_matches_oracle(got, key, km, v1, m1, v2)
+    finally:
+        fac.close()
 
 
 def test_noalloc_matches_operator_api_twice(gpu):
