@@ -62,6 +62,19 @@ def lib() -> C.CDLL:
         L.orc_join_probe_bench.argtypes = [I64, P, P, I32, P, I64, P, P, I32, P]
         L.orc_agg_bench.restype = I64
         L.orc_agg_bench.argtypes = [I64, P, P, P, I32]
+        L.orc_fingerprint_cols.restype = None
+        L.orc_fingerprint_cols.argtypes = [I64, I32, P, P, P, P]
+        L.orc_jtable_new.restype = P
+        L.orc_jtable_new.argtypes = [I64, P, P]
+        L.orc_jtable_free.restype = None
+        L.orc_jtable_free.argtypes = [P]
+        L.orc_jtable_fingerprint.restype = I32
+        L.orc_jtable_fingerprint.argtypes = [P, I32, P, P, I64, P, P, I32, P, P]
+        L.orc_jtable_pairs.restype = I64
+        L.orc_jtable_pairs.argtypes = [P, I64, P, P, P, P, I64]
+        L.orc_hashagg_mt.restype = I64
+        L.orc_hashagg_mt.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P, P, P,
+                                     I32]
         _lib = L
     return _lib
 
@@ -248,3 +261,127 @@ def exact_group_sums(group_ids: np.ndarray, values: np.ndarray, valid: np.ndarra
             exact[i] = math.fsum(seg.tolist())
             absum[i] = math.fsum(np.abs(seg).tolist())
     return exact, absum
+
+
+# ------------------------------------------------------------------ checks at full configuration size
+def fingerprint_cols(cols, nulls=None):
+    """(rows, f1, f2): the order-independent fingerprint of the rows of `cols` (numpy arrays,
+    decimal128 as (n, 2) uint64; `nulls` bool arrays or None), the row hash the library's
+    fingerprint kernel computes on the device (omg_batches_fingerprint)."""
+    L = lib()
+    cols = [np.ascontiguousarray(c) for c in cols]
+    n = len(cols[0]) if cols else 0
+    widths = np.array([c.dtype.itemsize * (2 if c.ndim == 2 else 1) for c in cols], dtype=np.int32)
+    nl = [None if m is None else np.ascontiguousarray(m, dtype=np.uint8) for m in (nulls or [None] * len(cols))]
+    out = (C.c_uint64 * 3)()
+    L.orc_fingerprint_cols(n, len(cols), _ptr_array(cols), _ptr(widths), _ptr_array(nl), out)
+    return tuple(int(x) for x in out)
+
+
+class JoinTable:
+    """A build side (int64 keys, bool NULL mask or None) kept for many probes of the checks."""
+
+    def __init__(self, keys, nulls=None):
+        self._keys = np.ascontiguousarray(keys, dtype=np.int64)
+        self._nulls = None if nulls is None else np.ascontiguousarray(nulls, dtype=np.uint8)
+        self.handle = lib().orc_jtable_new(len(self._keys), _ptr(self._keys), _ptr(self._nulls))
+        if not self.handle:
+            raise MemoryError("oracle join table")
+
+    def fingerprint(self, payloads, probe_keys, probe_nulls=None, threads=1):
+        """(fingerprint of the inner-join rows (probe key, payload columns), probe seconds)."""
+        pays = [np.ascontiguousarray(p) for p in payloads]
+        pw = np.array([p.dtype.itemsize for p in pays], dtype=np.int32)
+        pk = np.ascontiguousarray(probe_keys, dtype=np.int64)
+        pn = None if probe_nulls is None else np.ascontiguousarray(probe_nulls, dtype=np.uint8)
+        out = (C.c_uint64 * 3)()
+        secs = C.c_double(0.0)
+        rc = lib().orc_jtable_fingerprint(self.handle, len(pays), _ptr_array(pays), _ptr(pw), len(pk), _ptr(pk),
+                                          _ptr(pn), threads, out, C.byref(secs))
+        if rc != 0:
+            raise RuntimeError("oracle join fingerprint failed")
+        return tuple(int(x) for x in out), secs.value
+
+    def pairs(self, probe_keys, probe_nulls=None):
+        """(probe row, build row) index pairs of the inner join, probe rows in order."""
+        pk = np.ascontiguousarray(probe_keys, dtype=np.int64)
+        pn = None if probe_nulls is None else np.ascontiguousarray(probe_nulls, dtype=np.uint8)
+        cap = max(len(pk), 1)
+        while True:
+            op = np.empty(cap, dtype=np.int64)
+            ob = np.empty(cap, dtype=np.int64)
+            n = lib().orc_jtable_pairs(self.handle, len(pk), _ptr(pk), _ptr(pn), _ptr(op), _ptr(ob), cap)
+            if n < 0:
+                raise RuntimeError("oracle join failed")
+            if n <= cap:
+                return op[:n], ob[:n]
+            cap = n
+
+    def close(self):
+        if self.handle:
+            lib().orc_jtable_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
+def hashagg_mt(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=False, threads=1, max_groups=None):
+    """hashagg() over `threads` threads (each group's rows folded in row order by one thread).
+    Returns (key_values, key_nulls, agg_values, agg_nulls, exact, absum): for aggregates over a
+    DOUBLE column, exact[j] / absum[j] are per-group double-double sums of the non-NULL values
+    and sums of |x| (None for other aggregates).  Output arrays hold `max_groups` groups
+    (default: one per row); more groups raise."""
+    L = lib()
+    n = len(keys[0]) if keys else 0
+    kw = [WIDTH[t] for t in key_types]
+    kcols = [np.ascontiguousarray(k) for k in keys]
+    knulls = [None if m is None else np.ascontiguousarray(m, dtype=np.uint8) for m in key_nulls]
+    funcs = np.array([a["func"] for a in aggs], dtype=np.int32)
+    cols, in_types, in_widths, anulls, out_types, rescale = [], [], [], [], [], []
+    for a in aggs:
+        col = a.get("col")
+        if col is None:
+            col = np.zeros(max(n, 1), dtype=np.int64)
+            in_types.append(T_LONG)
+        else:
+            in_types.append(a["in_type"])
+        cols.append(np.ascontiguousarray(col))
+        in_widths.append(WIDTH[in_types[-1]])
+        m = a.get("nulls")
+        anulls.append(None if m is None else np.ascontiguousarray(m, dtype=np.uint8))
+        out_types.append(a["out_type"])
+        rescale.append(a.get("rescale", 0))
+    in_types_a = np.array(in_types, dtype=np.int32)
+    maxg = max(n if max_groups is None else min(n, max_groups), 1)
+    okeys = [np.zeros((maxg, 2) if w == 16 else maxg, dtype=np.uint64 if w == 16 else
+                      {1: np.int8, 2: np.int16, 4: np.int32, 8: np.int64}[w]) for w in kw]
+    oknulls = [np.zeros(maxg, dtype=np.uint8) for _ in kw]
+    ovals = [np.zeros(maxg * (2 if t == T_DEC128 else 1), dtype=np.uint64) for t in out_types]
+    ovnulls = [np.zeros(maxg, dtype=np.uint8) for _ in aggs]
+    dbl = [a["func"] in (F_SUM, F_AVG) and t == T_DOUBLE for a, t in zip(aggs, in_types)]
+    exact = [np.zeros(maxg) if d else None for d in dbl]
+    absum = [np.zeros(maxg) if d else None for d in dbl]
+    g = L.orc_hashagg_mt(n, len(keys), _ptr_array(kcols), _ptr(np.array(kw, dtype=np.int32)), _ptr_array(knulls),
+                         len(aggs), _ptr(funcs), _ptr_array(cols), _ptr(in_types_a),
+                         _ptr(np.array(in_widths, dtype=np.int32)), _ptr_array(anulls),
+                         _ptr(np.array(out_types, dtype=np.int32)), _ptr(np.array(rescale, dtype=np.int32)), policy,
+                         1 if overflow_as_null else 0, maxg, _ptr_array(okeys), _ptr_array(oknulls),
+                         _ptr_array(ovals), _ptr_array(ovnulls), _ptr_array(exact), _ptr_array(absum), threads)
+    if g == -2:
+        raise OverflowError("sum_aggregator overflow.")
+    if g == -3:
+        raise RuntimeError(f"more than max_groups = {maxg} groups")
+    if g < 0:
+        raise RuntimeError(f"oracle hashagg failed ({g})")
+    vals = []
+    for t, ov in zip(out_types, ovals):
+        if t == T_DEC128:
+            vals.append(ov.reshape(maxg, 2)[:g].copy())
+        else:
+            dt = {T_DOUBLE: np.float64, T_FLOAT: np.float32, T_INT: np.int32, T_DATE32: np.int32,
+                  T_SHORT: np.int16, T_BYTE: np.int8, T_BOOLEAN: np.int8}.get(t, np.int64)
+            vals.append(ov.view(np.uint8).view(dt)[:g].copy())
+    return ([k[:g] for k in okeys], [m[:g].astype(bool) for m in oknulls], vals,
+            [m[:g].astype(bool) for m in ovnulls], [None if e is None else e[:g] for e in exact],
+            [None if a is None else a[:g] for a in absum])

@@ -818,3 +818,424 @@ int64_t orc_agg_bench(int64_t n, const int64_t *key, const int64_t *v1, const do
     free(w);
     return groups;
 }
+
+/* ---------------------------------------------------------------- checks at full configuration size */
+/*
+ * Order-independent row-multiset fingerprint, the same row hash the library's fingerprint
+ * kernel computes on the device (a chain of the 64-bit finaliser over the column values,
+ * zero-extended, 16-byte values as two words, a NULL as a per-column tag; per row
+ * out[0] += 1, out[1] += mix64(h), out[2] += mix64(h ^ c)).  Two row sets with equal counts and
+ * equal sums are the same multiset up to a 2^-128 chance.  Used to compare a GPU output that
+ * stays on the device with the rows this file computes, without moving the rows.
+ */
+static uint64_t fp_row_start(void) { return 0x243f6a8885a308d3ULL; }
+static uint64_t fp_null(uint64_t h, int c) { return mix64(h ^ 0x9e3779b97f4a7c15ULL ^ (uint64_t)c); }
+static uint64_t fp_value(uint64_t h, const void *col, int64_t r, int w)
+{
+    switch (w) {
+        case 1: return mix64(h ^ (uint64_t)((const uint8_t *)col)[r]);
+        case 2: return mix64(h ^ (uint64_t)((const uint16_t *)col)[r]);
+        case 4: return mix64(h ^ (uint64_t)((const uint32_t *)col)[r]);
+        case 16: {
+            const uint64_t *p = (const uint64_t *)col + 2 * r;
+            return mix64(mix64(h ^ p[0]) ^ p[1]);
+        }
+        default: return mix64(h ^ ((const uint64_t *)col)[r]);
+    }
+}
+static void fp_add(uint64_t *acc, uint64_t h)
+{
+    acc[0] += 1;
+    acc[1] += mix64(h);
+    acc[2] += mix64(h ^ 0xc2b2ae3d27d4eb4fULL);
+}
+
+/* Fingerprint of n rows of ncols columns (nulls: byte per row, 1 = NULL; NULL = none). */
+void orc_fingerprint_cols(int64_t n, int32_t ncols, const void **cols, const int32_t *widths, const uint8_t **nulls,
+    uint64_t *out)
+{
+    out[0] = out[1] = out[2] = 0;
+    for (int64_t r = 0; r < n; ++r) {
+        uint64_t h = fp_row_start();
+        for (int c = 0; c < ncols; ++c) {
+            h = (nulls && nulls[c] && nulls[c][r]) ? fp_null(h, c) : fp_value(h, cols[c], r, widths[c]);
+        }
+        fp_add(out, h);
+    }
+}
+
+/* A join build kept across calls (one build, many probes of the full-size checks). */
+void *orc_jtable_new(int64_t n_build, const int64_t *build_keys, const uint8_t *build_nulls)
+{
+    jtable_t *t = (jtable_t *)calloc(1, sizeof(jtable_t));
+    if (!t) return NULL;
+    if (jbuild(t, n_build, build_keys, 8, build_nulls) != 0) {
+        jfree(t);
+        free(t);
+        return NULL;
+    }
+    return t;
+}
+
+void orc_jtable_free(void *t)
+{
+    if (t) {
+        jfree((jtable_t *)t);
+        free(t);
+    }
+}
+
+typedef struct {
+    const jtable_t *t;
+    const int64_t *pkeys;
+    const uint8_t *pnulls;
+    int64_t r0, r1;
+    int32_t npay;
+    const void **pay;
+    const int32_t *payw;
+    uint64_t acc[3];
+} jfp_work_t;
+
+static void *jfp_thread(void *arg)
+{
+    jfp_work_t *w = (jfp_work_t *)arg;
+    w->acc[0] = w->acc[1] = w->acc[2] = 0;
+    for (int64_t r = w->r0; r < w->r1; ++r) {
+        if (w->pnulls && w->pnulls[r]) continue;
+        const int64_t k = w->pkeys[r];
+        for (int64_t b = jfind(w->t, k); b >= 0; b = w->t->next[b]) {
+            uint64_t h = mix64(fp_row_start() ^ (uint64_t)k);
+            for (int p = 0; p < w->npay; ++p) h = fp_value(h, w->pay[p], b, w->payw[p]);
+            fp_add(w->acc, h);
+        }
+    }
+    return NULL;
+}
+
+/*
+ * Inner-join output fingerprint: the rows (probe key, payload columns of the matched build
+ * row) of every match, NULL probe keys skipped -- the rows ProbeBatchForInnerJoin emits
+ * (lookup_join.cpp:924-1035) -- hashed as orc_fingerprint_cols would hash them, over
+ * `nthreads` threads owning contiguous probe slices of a shared build.  Payload columns are
+ * NULL-free.  out[3] as orc_fingerprint_cols; returns the probe seconds in *seconds.
+ */
+int32_t orc_jtable_fingerprint(const void *table, int32_t npay, const void **pay, const int32_t *payw,
+    int64_t n_probe, const int64_t *probe_keys, const uint8_t *probe_nulls, int32_t nthreads, uint64_t *out,
+    double *seconds)
+{
+    if (!table) return -1;
+    if (nthreads < 1) nthreads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    jfp_work_t *w = (jfp_work_t *)calloc(nthreads, sizeof(jfp_work_t));
+    if (!th || !w) {
+        free(th);
+        free(w);
+        return -1;
+    }
+    const double t0 = now_seconds();
+    for (int i = 0; i < nthreads; ++i) {
+        w[i].t = (const jtable_t *)table;
+        w[i].pkeys = probe_keys;
+        w[i].pnulls = probe_nulls;
+        w[i].r0 = n_probe * i / nthreads;
+        w[i].r1 = n_probe * (i + 1) / nthreads;
+        w[i].npay = npay;
+        w[i].pay = pay;
+        w[i].payw = payw;
+        pthread_create(&th[i], NULL, jfp_thread, &w[i]);
+    }
+    out[0] = out[1] = out[2] = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        pthread_join(th[i], NULL);
+        out[0] += w[i].acc[0];
+        out[1] += w[i].acc[1];
+        out[2] += w[i].acc[2];
+    }
+    if (seconds) *seconds = now_seconds() - t0;
+    free(th);
+    free(w);
+    return 0;
+}
+
+/* (probe row, build row) pairs of every inner-join match against a kept build, probe rows in
+ * order; returns the number of pairs (only the first `capacity` written). */
+int64_t orc_jtable_pairs(const void *table, int64_t n_probe, const int64_t *probe_keys, const uint8_t *probe_nulls,
+    int64_t *out_probe, int64_t *out_build, int64_t capacity)
+{
+    const jtable_t *t = (const jtable_t *)table;
+    if (!t) return -1;
+    int64_t n = 0;
+    for (int64_t r = 0; r < n_probe; ++r) {
+        if (probe_nulls && probe_nulls[r]) continue;
+        for (int64_t b = jfind(t, probe_keys[r]); b >= 0; b = t->next[b]) {
+            if (n < capacity) {
+                out_probe[n] = r;
+                out_build[n] = b;
+            }
+            n++;
+        }
+    }
+    return n;
+}
+
+/*
+ * Multi-threaded single-stage hash aggregation for checks at full configuration size.  Every
+ * group's rows go to one thread (thread = hash of the packed key mod nthreads), which folds
+ * them in row order with the same per-row state updates as orc_hashagg, so each group's result
+ * is the one orc_hashagg computes.  Outputs as orc_hashagg (groups in thread order).
+ * For every aggregator over a DOUBLE column (SUM, AVG), out_exact[a] / out_abs[a] (when given)
+ * receive the group's sum of the non-NULL values accumulated in double-double arithmetic
+ * (Knuth's TwoSum, error at most n * 2^-104 * sum|x|, about 10^10 times below the 1e-12
+ * tolerance these checks use) and the sum of |x|.  Returns the number of groups, -1 on
+ * allocation failure, -2 if an overflow must raise, -3 if max_groups is too small.
+ */
+typedef struct {
+    int tid, nthreads;
+    int64_t n_rows;
+    const uint8_t *part;
+    int32_t nkey;
+    const void **key_cols;
+    const int32_t *key_widths;
+    const uint8_t **key_nulls;
+    int keybytes;
+    aggctx_t c;
+    table_t t;
+    double *ehi, *elo, *eabs; /* per group, per aggregator (double inputs only) */
+    int64_t ecap;
+    int rc;
+} hmt_work_t;
+
+static void two_sum(double a, double b, double *s, double *e)
+{
+    const double x = a + b;
+    const double bv = x - a;
+    *e = (a - (x - bv)) + (b - bv);
+    *s = x;
+}
+
+/* (hi, lo) += x in double-double arithmetic. */
+static void dd_add(double *hi, double *lo, double x)
+{
+    double s, e;
+    two_sum(*hi, x, &s, &e);
+    e += *lo;
+    const double h = s + e;
+    *lo = e - (h - s);
+    *hi = h;
+}
+
+static void *hmt_thread(void *arg)
+{
+    hmt_work_t *w = (hmt_work_t *)arg;
+    const int nagg = w->c.nagg;
+    const int na = nagg > 0 ? nagg : 1;
+    w->rc = 0;
+    if (table_init(&w->t, w->nkey, w->keybytes, 1024) != 0) {
+        w->rc = -1;
+        return NULL;
+    }
+    w->c.stcap = 1024;
+    w->c.st = (state_t *)malloc((uint64_t)w->c.stcap * na * sizeof(state_t));
+    w->ecap = 1024;
+    w->ehi = (double *)calloc((uint64_t)w->ecap * na, sizeof(double));
+    w->elo = (double *)calloc((uint64_t)w->ecap * na, sizeof(double));
+    w->eabs = (double *)calloc((uint64_t)w->ecap * na, sizeof(double));
+    uint8_t *k = (uint8_t *)malloc(w->keybytes + 1);
+    if (!w->c.st || !w->ehi || !w->elo || !w->eabs || !k) {
+        w->rc = -1;
+        free(k);
+        return NULL;
+    }
+    for (int64_t r = 0; r < w->n_rows; ++r) {
+        if (w->part[r] != (uint8_t)w->tid) continue;
+        pack_key(w->nkey, w->key_cols, w->key_widths, w->key_nulls, r, k);
+        int isnew = 0;
+        const int64_t g = table_find_insert(&w->t, k, &isnew);
+        if (g < 0) {
+            w->rc = -1;
+            break;
+        }
+        if (isnew) {
+            if (g >= w->c.stcap) {
+                state_t *ns = (state_t *)realloc(w->c.st, (uint64_t)w->c.stcap * 2 * na * sizeof(state_t));
+                if (!ns) {
+                    w->rc = -1;
+                    break;
+                }
+                w->c.st = ns;
+                w->c.stcap *= 2;
+            }
+            if (g >= w->ecap) {
+                const int64_t nc = w->ecap * 2;
+                double *a = (double *)realloc(w->ehi, (uint64_t)nc * na * sizeof(double));
+                if (a) w->ehi = a;
+                double *b = a ? (double *)realloc(w->elo, (uint64_t)nc * na * sizeof(double)) : NULL;
+                if (b) w->elo = b;
+                double *d = b ? (double *)realloc(w->eabs, (uint64_t)nc * na * sizeof(double)) : NULL;
+                if (d) w->eabs = d;
+                if (!a || !b || !d) {
+                    w->rc = -1;
+                    break;
+                }
+                w->ecap = nc;
+            }
+            for (int a = 0; a < nagg; ++a) {
+                state_init(&w->c.aggs[a], &w->c.st[g * nagg + a]);
+                w->ehi[g * na + a] = w->elo[g * na + a] = w->eabs[g * na + a] = 0.0;
+            }
+        }
+        for (int a = 0; a < nagg; ++a) {
+            const agg_t *ag = &w->c.aggs[a];
+            state_update(&w->c, ag, &w->c.st[g * nagg + a], r);
+            if (ag->in_type == T_DOUBLE && (ag->func == F_SUM || ag->func == F_AVG) && !(ag->nulls && ag->nulls[r])) {
+                const double x = ((const double *)ag->col)[r];
+                dd_add(&w->ehi[g * na + a], &w->elo[g * na + a], x);
+                w->eabs[g * na + a] += x < 0 ? -x : x;
+            }
+        }
+    }
+    free(k);
+    return NULL;
+}
+
+typedef struct {
+    int64_t r0, r1;
+    int32_t nkey;
+    const void **key_cols;
+    const int32_t *key_widths;
+    const uint8_t **key_nulls;
+    int keybytes;
+    int nthreads;
+    uint8_t *part;
+} hpart_work_t;
+
+static void *hpart_thread(void *arg)
+{
+    hpart_work_t *w = (hpart_work_t *)arg;
+    uint8_t *k = (uint8_t *)malloc(w->keybytes + 1);
+    if (!k) return NULL;
+    for (int64_t r = w->r0; r < w->r1; ++r) {
+        pack_key(w->nkey, w->key_cols, w->key_widths, w->key_nulls, r, k);
+        w->part[r] = (uint8_t)((hash_bytes(k, w->keybytes) >> 40) % (uint64_t)w->nthreads);
+    }
+    free(k);
+    return NULL;
+}
+
+int64_t orc_hashagg_mt(int64_t n_rows, int32_t nkey, const void **key_cols, const int32_t *key_widths,
+    const uint8_t **key_nulls, int32_t nagg, const int32_t *funcs, const void **agg_cols, const int32_t *in_types,
+    const int32_t *in_widths, const uint8_t **agg_nulls, const int32_t *out_types, const int32_t *rescale,
+    int32_t policy, int32_t overflow_as_null, int64_t max_groups, void **out_keys, uint8_t **out_key_nulls,
+    void **out_vals, uint8_t **out_val_nulls, double **out_exact, double **out_abs, int32_t nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 255) nthreads = 255;
+    int keybytes = 0;
+    for (int i = 0; i < nkey; ++i) keybytes += 1 + key_widths[i];
+    uint8_t *part = (uint8_t *)malloc((size_t)(n_rows > 0 ? n_rows : 1));
+    agg_t *aggs = (agg_t *)calloc(nagg > 0 ? nagg : 1, sizeof(agg_t));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    hpart_work_t *pw = (hpart_work_t *)calloc(nthreads, sizeof(hpart_work_t));
+    hmt_work_t *w = (hmt_work_t *)calloc(nthreads, sizeof(hmt_work_t));
+    int64_t ret = 0;
+    if (!part || !aggs || !th || !pw || !w) {
+        ret = -1;
+        goto out;
+    }
+    for (int a = 0; a < nagg; ++a) {
+        aggs[a].func = funcs[a];
+        aggs[a].col = agg_cols[a];
+        aggs[a].in_type = in_types[a];
+        aggs[a].in_width = in_widths[a];
+        aggs[a].nulls = agg_nulls ? agg_nulls[a] : NULL;
+        aggs[a].out_type = out_types[a];
+        aggs[a].rescale = rescale ? rescale[a] : 0;
+    }
+    for (int i = 0; i < nthreads; ++i) {
+        pw[i].r0 = n_rows * i / nthreads;
+        pw[i].r1 = n_rows * (i + 1) / nthreads;
+        pw[i].nkey = nkey;
+        pw[i].key_cols = key_cols;
+        pw[i].key_widths = key_widths;
+        pw[i].key_nulls = key_nulls;
+        pw[i].keybytes = keybytes;
+        pw[i].nthreads = nthreads;
+        pw[i].part = part;
+        pthread_create(&th[i], NULL, hpart_thread, &pw[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    for (int i = 0; i < nthreads; ++i) {
+        w[i].tid = i;
+        w[i].nthreads = nthreads;
+        w[i].n_rows = n_rows;
+        w[i].part = part;
+        w[i].nkey = nkey;
+        w[i].key_cols = key_cols;
+        w[i].key_widths = key_widths;
+        w[i].key_nulls = key_nulls;
+        w[i].keybytes = keybytes;
+        w[i].c.nagg = nagg;
+        w[i].c.aggs = aggs;
+        w[i].c.policy = policy;
+        pthread_create(&th[i], NULL, hmt_thread, &w[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    int64_t total = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        if (w[i].rc != 0) {
+            ret = -1;
+            goto out;
+        }
+        total += w[i].t.ngroups;
+    }
+    if (total > max_groups) {
+        ret = -3;
+        goto out;
+    }
+    {
+        const int na = nagg > 0 ? nagg : 1;
+        int64_t base = 0;
+        for (int i = 0; i < nthreads && ret == 0; ++i) {
+            for (int64_t g = 0; g < w[i].t.ngroups; ++g) {
+                const int64_t o = base + g;
+                const uint8_t *gk = w[i].t.gkeys + (uint64_t)g * keybytes;
+                int off = 0;
+                for (int c = 0; c < nkey; ++c) {
+                    out_key_nulls[c][o] = gk[off];
+                    memcpy((uint8_t *)out_keys[c] + (int64_t)key_widths[c] * o, gk + off + 1, key_widths[c]);
+                    off += 1 + key_widths[c];
+                }
+                for (int a = 0; a < nagg; ++a) {
+                    const int rc = state_extract(&w[i].c, &aggs[a], &w[i].c.st[g * nagg + a], overflow_as_null,
+                        out_vals[a], o);
+                    if (rc == 2) {
+                        ret = -2;
+                        break;
+                    }
+                    out_val_nulls[a][o] = (uint8_t)(rc == 1);
+                    if (out_exact && out_exact[a]) out_exact[a][o] = w[i].ehi[g * na + a] + w[i].elo[g * na + a];
+                    if (out_abs && out_abs[a]) out_abs[a][o] = w[i].eabs[g * na + a];
+                }
+                if (ret != 0) break;
+            }
+            base += w[i].t.ngroups;
+        }
+        if (ret == 0) ret = total;
+    }
+out:
+    if (w) {
+        for (int i = 0; i < nthreads; ++i) {
+            if (w[i].t.keys || w[i].t.used || w[i].t.gid || w[i].t.gkeys) table_free(&w[i].t);
+            free(w[i].c.st);
+            free(w[i].ehi);
+            free(w[i].elo);
+            free(w[i].eabs);
+        }
+    }
+    free(part);
+    free(aggs);
+    free(th);
+    free(pw);
+    free(w);
+    return ret;
+}
