@@ -61,6 +61,14 @@ JOIN_WORKLOAD = ("inner hash join probe: build 2^20 unique int64 keys + 2 int32 
                  "keys (1% null, 80% match) in 4096-row batches, output (probe key, p1, p2)")
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Progress of the run on stderr (elapsed seconds), so that a slow leg can be found."""
+    print(f"[bench {time.perf_counter() - _T0:8.1f} s] {msg}", file=sys.stderr, flush=True)
+
+
 def measured_peak_gbs():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -194,6 +202,106 @@ def cpu_agg_rows_per_s(data, threads, reps=1):
         times.append(time.perf_counter() - t0)
         assert g == AGG_GROUPS
     return len(key) / statistics.median(times)
+
+
+# ------------------------------------------------------------------------------ parity at full size
+# The oracle is the checker here: every check runs outside the timed regions, on the same
+# inputs as the timed steps, and its verdict goes into the bench line as "oracle_match".
+DOUBLE_TOL = 1e-12
+
+
+def host_threads():
+    return os.cpu_count() or 1
+
+
+def mem_available_bytes():
+    """MemAvailable of this host (bytes), or None when unknown."""
+    try:
+        for line in Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+def host_columns(omg, batches):
+    """Concatenated [(values, NULL mask)] of host output batches (frees them)."""
+    parts = []
+    for b in batches:
+        parts.append(omg.batch_to_numpy(b))
+        omg.free_batch(b)
+    if not parts:
+        return None
+    return [(np.concatenate([p[c][0] for p in parts]), np.concatenate([p[c][1] for p in parts]))
+            for c in range(len(parts[0]))]
+
+
+def _key_order(keys, masks):
+    """Row order sorting by the key columns (NULL first per column)."""
+    parts = []
+    for v, m in zip(keys, masks):
+        m = np.asarray(m, dtype=bool)
+        parts.append(np.where(m, 0, np.asarray(v).astype(np.int64)))
+        parts.append(~m)
+    return np.lexsort(parts[::-1])
+
+
+def compare_agg_full(gpu_cols, ora, nkeys, double_aggs):
+    """Compare GPU output columns [(values, mask)] with oracle.hashagg_mt's result group for
+    group: keys, integer / decimal / COUNT / MIN / MAX values and NULLs bit-exact; the double
+    SUM / AVG aggregates in `double_aggs` ({output index: (oracle exact index, divisor index or
+    None)}) within 1e-12 * max(|exact|, sum|x|) (divided by the non-NULL count for AVG) of the
+    double-double sum.  Returns a summary dict with "oracle_match"."""
+    okeys, oknulls, ovals, onulls, oexact, oabs = ora
+    ng = len(okeys[0])
+    res = {"groups": ng}
+    if gpu_cols is None or len(gpu_cols[0][0]) != ng:
+        res.update(oracle_match=False, why=f"group count {0 if gpu_cols is None else len(gpu_cols[0][0])} != {ng}")
+        return res
+    go = _key_order([c[0] for c in gpu_cols[:nkeys]], [c[1] for c in gpu_cols[:nkeys]])
+    oo = _key_order(okeys, oknulls)
+    for k in range(nkeys):
+        gv, gm = gpu_cols[k][0][go], gpu_cols[k][1][go]
+        ov, om = okeys[k][oo], oknulls[k][oo]
+        if not np.array_equal(gm, om) or not np.array_equal(np.where(gm, 0, gv), np.where(om, 0, ov)):
+            res.update(oracle_match=False, why=f"key column {k} differs")
+            return res
+    worst = 0.0
+    naive = 0.0
+    for j in range(len(gpu_cols) - nkeys):
+        gv, gm = gpu_cols[nkeys + j][0][go], gpu_cols[nkeys + j][1][go]
+        ov, om = ovals[j][oo], onulls[j][oo]
+        if not np.array_equal(gm, om):
+            res.update(oracle_match=False, why=f"NULLs of aggregate {j} differ")
+            return res
+        live = ~gm
+        if j in double_aggs:
+            ei, di = double_aggs[j]
+            ex, ab = oexact[ei][oo][live], oabs[ei][oo][live]
+            div = np.ones(int(live.sum())) if di is None else ovals[di][oo][live].astype(np.float64)
+            target = ex / div
+            tol = DOUBLE_TOL * np.maximum(np.abs(ex), ab) / div
+            tol = np.where(tol > 0, tol, np.finfo(np.float64).tiny)
+            err = np.abs(gv[live].astype(np.float64) - target)
+            worst = max(worst, float((err / tol).max()) if len(err) else 0.0)
+            scale = np.maximum(np.abs(ex), ab) / div
+            scale = np.where(scale > 0, scale, 1.0)
+            naive = max(naive, float((np.abs(ov[live].astype(np.float64) - target) / scale).max()) if len(err) else 0.0)
+        else:
+            a = np.asarray(gv[live])
+            b = np.asarray(ov[live])
+            if a.ndim == 2 or b.ndim == 2:
+                same = np.array_equal(a.view(np.uint64).reshape(-1, 2), b.view(np.uint64).reshape(-1, 2))
+            else:
+                same = np.array_equal(a.astype(np.int64), b.astype(np.int64))
+            if not same:
+                res.update(oracle_match=False, why=f"aggregate {j} differs")
+                return res
+    res.update(oracle_match=worst <= 1.0, double_err_over_tol=round(worst, 6))
+    if double_aggs:
+        res["reference_fold_max_rel_err"] = float(f"{naive:.3g}")
+    return res
 
 
 def base_line(args, value, ms):
@@ -337,6 +445,14 @@ def run_gpu(args, rank, world):
     for _ in range(args.warmup):
         rows = probe_step()
         assert rows == expected_rows, (rows, expected_rows)
+    # Parity at full size (outside the timed steps): the row-multiset fingerprint of one probe
+    # pass against the oracle's join of the same build and probe rows.
+    pop.add_input(omg.wrap_device_batch([L], N_PROBE, [pkey.data_ptr()], [pbits.data_ptr()]))
+    outs, _ = pop.get_outputs(1 << 16)
+    gpu_fp = omg.batches_fingerprint(outs)
+    omg.free_batches(outs)
+    join_check = check_join_fingerprint(gpu_fp, bkey.cpu().numpy(), [p1.cpu().numpy(), p2.cpu().numpy()],
+                                        pkey.cpu().numpy(), pnull.cpu().numpy())
     c0 = pop.counters()
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -363,12 +479,17 @@ def run_gpu(args, rank, world):
                 "kernel": "ProbeBitsKernel", "kernel_ms": round(kernel_s * 1e3, 4),
                 "algorithmic_bytes": int(alg_bytes)}
 
+    log(f"headline probe timed ({ms / args.steps:.3f} ms per step), oracle match {join_check['oracle_match']}")
     e2e = None if args.skip_e2e else run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank)
+    log("e2e done")
     kinds = None if args.skip_ext else run_join_kinds(args, omg, torch, stream, barrier, max_over_ranks, world, bkey,
                                                        p1, p2, pkey, pbits, pnull)
+    log("join kinds done")
     agg = None if args.skip_agg else run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world)
+    log("uniform aggregation done")
     two_stage = None if args.skip_ext else run_agg_two_stage(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                               world)
+    log("two-stage aggregation done")
     features = None if args.skip_ext else run_features(args, omg, torch, dev, stream, barrier, max_over_ranks, world,
                                                         bf, pkey, pbits)
     pop.delete()
@@ -376,15 +497,34 @@ def run_gpu(args, rank, world):
     pf.close()
     bf.close()
     del bkey, p1, p2, pkey, pnull, pbits
+    log("features done")
     skew = None if args.skip_skew else run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                        world, rank)
+    log("skewed aggregation done")
     batched = None if args.skip_batched else run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                               world, rank)
+    log("batched aggregation done")
     join5 = None if args.skip_join5 else run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks,
                                                           world, rank)
     return dict(value=value, ms=ms / args.steps, build_ms=build_ms, launches=launches, roofline=roofline,
                 clocks=clk.summary(), e2e=e2e, agg=agg, rows=expected_rows, skew=skew, batched=batched, join5=join5,
-                kinds=kinds, two_stage=two_stage, features=features)
+                kinds=kinds, two_stage=two_stage, features=features, join_check=join_check)
+
+
+def check_join_fingerprint(gpu_fp, bkey, pays, pkey, pnull, table=None):
+    """Inner-join output of the GPU (its fingerprint) against the oracle's join of the same
+    rows: equal row counts and equal 128-bit row-multiset fingerprints."""
+    import oracle
+
+    oracle.build()
+    t0 = time.perf_counter()
+    jt = table if table is not None else oracle.JoinTable(bkey)
+    fp, probe_s = jt.fingerprint(pays, pkey, pnull, threads=host_threads())
+    if table is None:
+        jt.close()
+    return {"oracle_match": tuple(gpu_fp) == tuple(fp), "rows": int(fp[0]), "gpu_rows": int(gpu_fp[0]),
+            "fingerprint": f"{fp[1]:016x}{fp[2]:016x}", "check_s": round(time.perf_counter() - t0, 2),
+            "oracle_probe_s": round(probe_s, 3)}
 
 
 def run_join_kinds(args, omg, torch, stream, barrier, max_over_ranks, world, bkey, p1, p2, pkey, pbits, pnull):
@@ -702,22 +842,35 @@ def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
         hs = [omg.make_batch([L], [pkey[s:s + BATCH]], [pnull[s:s + BATCH]]) for s in range(0, N_PROBE, BATCH)]
         return [(C.c_void_p * len(hs[i:i + 1024]))(*hs[i:i + 1024]) for i in range(0, len(hs), 1024)]
 
-    def step(chunks):
+    fp = [0, 0, 0]
+
+    def step(chunks, fingerprint=False):
         op = pf.create_operator()
         op.set_no_more_input(False)
         rows = 0
+
+        def take(outs):
+            if fingerprint and outs:
+                f = omg.batches_fingerprint(outs)
+                for i in range(3):
+                    fp[i] = (fp[i] + f[i]) & ((1 << 64) - 1)
+            omg.free_batches(outs)
+
         for chunk in chunks:
             op.add_inputs(chunk)  # AddInput per batch, in C
             outs, n = op.get_outputs(1 << 16)
             rows += n
-            omg.free_batches(outs)
+            take(outs)
         op.no_more_input()
         outs, n = op.get_outputs(1 << 16)
         rows += n
-        omg.free_batches(outs)
+        take(outs)
         op.delete()
         return rows
 
+    # Parity (outside the timed steps): the host output batches of one pass against the oracle.
+    assert step(make_batches(), fingerprint=True) == expected
+    check = check_join_fingerprint(fp, bkey, [p1, p2], pkey, pnull)
     for _ in range(max(1, min(args.warmup, 2))):
         assert step(make_batches()) == expected
     total = 0.0
@@ -736,7 +889,7 @@ def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
     h2d = N_PROBE * 8 + N_PROBE // 8
     d2h = expected * 16 + 3 * ((expected + 31) // 32 * 4)
     return {"value": whole_job_rate(world, N_PROBE * args.steps, t), "unit": "rows/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps}
+            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps, "oracle_match": check["oracle_match"]}
 
 
 def run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world):
@@ -787,8 +940,17 @@ def run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world):
     alg = AGG_ROWS * 24 + AGG_GROUPS * 56
     peak, kind = measured_peak_gbs()
     traffic_per_row = profiled_traffic("agg_partitioned_kernel_agg2e22.md")
+    # Parity at full size (outside the timed steps): one more operator over the same rows with
+    # host output, every group against the oracle.
+    op = fac.create_operator()
+    op.set_stream(stream.cuda_stream)
+    op.add_input(omg.wrap_device_batch([L, L, D], AGG_ROWS, [tk.data_ptr(), t1.data_ptr(), t2.data_ptr()]))
+    gpu_cols = host_columns(omg, op.drain())
+    op.delete()
     fac.close()
+    check = check_agg_uniform(key, v1, v2, gpu_cols)
     return {"value": world * AGG_ROWS / (ms / 1e3), "unit": "rows/s", "ms_per_step": ms, "gpu_launches": launches,
+            "oracle_check": check, "oracle_match": check["oracle_match"],
             "workload": "hash aggregation: 2^22 rows, int64 key over 10,000 values, SUM/COUNT/MIN/MAX(int64), "
                         "SUM/AVG(double); input resident in HBM, L2 flushed between steps",
             "roofline": {"bound": "hbm", "achieved": round(alg / kernel_s / 1e9, 1), "peak": peak, "unit": "GB/s",
@@ -796,6 +958,24 @@ def run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world):
                          "traffic": None if traffic_per_row is None else round(traffic_per_row * AGG_ROWS),
                          "kernel": "AggPartKernel", "kernel_ms": round(kernel_s * 1e3, 4),
                          "algorithmic_bytes": alg}}
+
+
+def check_agg_uniform(key, v1, v2, gpu_cols):
+    """The uniform aggregation's GPU groups against the oracle (all rows, all groups)."""
+    import oracle
+
+    oracle.build()
+    aggs = [dict(func=f, col=v1, in_type=oracle.T_LONG, out_type=oracle.T_LONG)
+            for f in (oracle.F_SUM, oracle.F_COUNT_COL, oracle.F_MIN, oracle.F_MAX)]
+    aggs += [dict(func=oracle.F_SUM, col=v2, in_type=oracle.T_DOUBLE, out_type=oracle.T_DOUBLE),
+             dict(func=oracle.F_AVG, col=v2, in_type=oracle.T_DOUBLE, out_type=oracle.T_DOUBLE),
+             dict(func=oracle.F_COUNT_COL, col=v2, in_type=oracle.T_DOUBLE, out_type=oracle.T_LONG)]
+    t0 = time.perf_counter()
+    ora = oracle.hashagg_mt([key], [oracle.T_LONG], [None], aggs, threads=host_threads())
+    res = compare_agg_full(gpu_cols, ora, 1, {4: (4, None), 5: (5, 6)})
+    res["check_s"] = round(time.perf_counter() - t0, 2)
+    res["rows"] = len(key)
+    return res
 
 
 SKEW_ROWS = 1 << 28
@@ -876,9 +1056,9 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
         outs, groups = op.get_outputs(1 << 16)
         omg.free_batches(outs)
         c = op.counters()
-        log = op.sizing_log()
+        slog = op.sizing_log()
         op.delete()
-        return groups, c, log
+        return groups, c, slog
 
     steps = max(1, min(args.steps, 3))
     res = {}
@@ -892,21 +1072,93 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
-            groups, c, log = step(fac)
+            groups, c, slog = step(fac)
         e1.record(stream)
         barrier()
         ms = max_over_ranks(e0.elapsed_time(e1)) / steps
         fac.close()
         res[arm] = {"value": world * n / (ms / 1e3), "unit": "rows/s", "ms_per_step": round(ms, 3),
-                    "groups": groups, "estimate": log["estimate"], "plain_estimate": log["plain_estimate"],
+                    "kernel_s": c["kernel_ns"] / max(c["kernel_launches"], 1) / 1e9,
+                    "groups": groups, "estimate": slog["estimate"], "plain_estimate": slog["plain_estimate"],
                     "table_resizes": c["resizes"], "retried_rows": c["retried_rows"],
-                    "shared_front_table": log["smem_front"], "part_bits": log["part_bits"]}
+                    "shared_front_table": slog["smem_front"], "part_bits": slog["part_bits"]}
     assert res["plain"]["groups"] == res["learned"]["groups"] == res["exact_count"]["groups"]
+    # Roofline of the aggregation kernel (the learned arm's launches): 28.25 B read per row
+    # (4 + 8 + 8 + 8 B and two validity bits), 45 B written per group.
+    groups = res["learned"]["groups"]
+    alg = n * 28.25 + groups * 45
+    peak, kind = measured_peak_gbs()
+    for arm in res:
+        res[arm]["kernel_ms"] = round(res[arm].pop("kernel_s") * 1e3, 3)
+    kern_s = res["learned"]["kernel_ms"] / 1e3
+    roofline = {"bound": "hbm", "achieved": round(alg / kern_s / 1e9, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(alg / kern_s / 1e9 / peak, 4), "peak_kind": kind, "traffic": None,
+                "kernel": "AggKernel (global table)", "kernel_ms": round(kern_s * 1e3, 3), "algorithmic_bytes": int(alg)}
+    # Parity at full size (outside the timed steps): the learned operator's groups, with host
+    # output, against the oracle over every row.
+    fac = factory("learned")
+    op = fac.create_operator()
+    op.set_stream(stream.cuda_stream)
+    op.add_input(omg.wrap_device_batch([I, L, d64, D], n, [k1.data_ptr(), k2.data_ptr(), dec.data_ptr(),
+                                                          dbl.data_ptr()],
+                                       [None, None, dec_nulls.data_ptr(), dbl_nulls.data_ptr()]))
+    gpu_cols = host_columns(omg, op.drain())
+    op.delete()
+    fac.close()
     model.close()
+
+    # All rows when the host has room for them and the oracle's tables, else the rows of one
+    # eighth of the groups (k2 mod 8 == 0; k2 identifies the pair) against the same GPU groups.
+    need = n * 40 + groups * 400
+    avail = mem_available_bytes()
+    sel = None
+    if avail is not None and avail < 2 * need:
+        sel = (k2 & 7) == 0
+        keep = ~((gpu_cols[1][0] & 7).astype(bool))
+        gpu_cols = [(v[keep], m[keep]) for v, m in gpu_cols]
+        groups = len(gpu_cols[0][0])
+
+    def host(t):
+        return (t[sel] if sel is not None else t).cpu().numpy()
+
+    def unbits(t):
+        m = torch.from_numpy(np.unpackbits(t.cpu().numpy(), bitorder="little")[:n].astype(bool))
+        return (m[sel.cpu()] if sel is not None else m).numpy()
+
+    log("skewed aggregation timed; oracle check")
+    check, cpu = check_agg_skewed(host(k1), host(k2), host(dec), host(dbl), unbits(dec_nulls), unbits(dbl_nulls),
+                                  gpu_cols, groups)
+    check["scope"] = "all rows" if sel is None else "rows of the groups with k2 mod 8 == 0 (host memory)"
     return {"workload": SKEW_WORKLOAD if n == SKEW_ROWS else SKEW_WORKLOAD.replace("2^28", f"2^{n.bit_length() - 1}"),
             "steps": steps, "sizer": model_src, "plain": res["plain"], "learned": res["learned"],
             "exact_count": res["exact_count"],
-            "learned_over_plain": round(res["learned"]["value"] / res["plain"]["value"], 3)}
+            "learned_over_plain": round(res["learned"]["value"] / res["plain"]["value"], 3),
+            "roofline": roofline, "cpu_baseline": cpu, "oracle_check": check, "oracle_match": check["oracle_match"]}
+
+
+def check_agg_skewed(k1, k2, dec, dbl, dec_null, dbl_null, gpu_cols, groups):
+    """The skewed aggregation's GPU groups against the oracle over every row (SUM(decimal64) ->
+    decimal128 and COUNT(*) bit-exact, AVG(double) within 1e-12 * max(|exact|, sum|x|) / count);
+    the oracle run, on all host threads, is also the CPU baseline."""
+    import oracle
+
+    oracle.build()
+    aggs = [dict(func=oracle.F_SUM, col=dec, in_type=oracle.T_DEC64, out_type=oracle.T_DEC128, nulls=dec_null),
+            dict(func=oracle.F_COUNT_ALL, col=None, in_type=oracle.T_LONG, out_type=oracle.T_LONG),
+            dict(func=oracle.F_AVG, col=dbl, in_type=oracle.T_DOUBLE, out_type=oracle.T_DOUBLE, nulls=dbl_null),
+            dict(func=oracle.F_COUNT_COL, col=dbl, in_type=oracle.T_DOUBLE, out_type=oracle.T_LONG, nulls=dbl_null)]
+    threads = host_threads()
+    t0 = time.perf_counter()
+    ora = oracle.hashagg_mt([k1, k2], [oracle.T_INT, oracle.T_LONG], [None, None], aggs, threads=threads,
+                            max_groups=max(2 * groups, 1 << 20))
+    secs = time.perf_counter() - t0
+    res = compare_agg_full(gpu_cols, ora, 2, {2: (2, 3)})
+    res["check_s"] = round(time.perf_counter() - t0, 2)
+    res["rows"] = len(k1)
+    cpu = {"value": len(k1) / secs, "unit": "rows/s", "cores": threads, "kind": "port",
+           "sample": f"all {len(k1)} rows, {threads} threads (rows split by key hash, each group folded in row "
+                     "order by one thread; includes the double-double check sums)"}
+    return res, cpu
 
 
 JOIN5_BUILD = 1 << 26
@@ -948,6 +1200,14 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
     steps = max(1, min(args.steps, 3))
     bits = 12
     out = {"workload": JOIN5_WORKLOAD, "build_rows": nb, "probe_rows": npb, "partitions": 1 << bits, "steps": steps}
+    import oracle
+
+    oracle.build()
+    t0 = time.perf_counter()
+    bkey_h, pay_h = bkey.cpu().numpy(), [pay1.cpu().numpy(), pay2.cpu().numpy()]
+    jt = oracle.JoinTable(bkey_h)
+    out["oracle_build_s"] = round(time.perf_counter() - t0, 2)
+    peak, peak_kind = measured_peak_gbs()
     for s in (0.9, 1.1, 1.3):
         cdf = sizer_train.zipf_cdf(torch, nb, s, dev)
         pkey = torch.empty(npb, dtype=torch.int64, device=dev)
@@ -966,6 +1226,7 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         learn_ms = (time.perf_counter() - t0) * 1e3
         per = {}
         chosen = {}
+        gpu_fp = {}
         for name, strat in (("direct", omg.JOIN_DIRECT), ("hash_partitioned", omg.JOIN_HASH_PARTITIONED),
                             ("learned_range_partitioned", omg.JOIN_RANGE_PARTITIONED),
                             ("learned_choice", omg.JOIN_LEARNED)):
@@ -980,8 +1241,10 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
                 outs, rows = op.get_outputs(1 << 20)
                 f = omg.batches_fingerprint(outs) if fp else None
                 omg.free_batches(outs)
+                kern[name] = op.counters()
                 op.delete()
                 return rows, f
+            kern = {}
             rows, fp = step(fp=True)  # warm-up (also builds the partitioned build tables) + fingerprint
             barrier()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -991,10 +1254,56 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
             e1.record(stream)
             barrier()
             ms = max_over_ranks(e0.elapsed_time(e1)) / steps
+            c = kern[name]
+            dev_ms = c["kernel_ns"] / max(c["kernel_launches"], 1) / 1e6
             per[name] = {"value": world * npb / (ms / 1e3), "unit": "rows/s", "ms_per_step": round(ms, 2),
-                         "output_rows": rows, "fingerprint": f"{fp[1]:016x}{fp[2]:016x}"}
+                         "device_ms": round(dev_ms, 2), "output_rows": rows,
+                         "fingerprint": f"{fp[1]:016x}{fp[2]:016x}"}
+            gpu_fp[name] = fp
         ref = per["direct"]["fingerprint"]
         assert all(v["fingerprint"] == ref and v["output_rows"] == per["direct"]["output_rows"] for v in per.values())
+        log(f"skewed join s={s} timed; oracle check")
+        # Parity at full size (outside the timed steps): the output's fingerprint against the
+        # oracle's join of all 2^30 probe rows (probed in chunks; the fingerprint is a sum), and
+        # the exact rows of the probe keys with (key >> 1) mod 64 == 0 against the oracle's.
+        t0 = time.perf_counter()
+        ofp, osecs = [0, 0, 0], 0.0
+        for c0 in range(0, npb, 1 << 27):
+            f, sec = jt.fingerprint(pay_h, pkey[c0:c0 + (1 << 27)].cpu().numpy(), None, threads=host_threads())
+            ofp = [(a + b) & ((1 << 64) - 1) for a, b in zip(ofp, f)]
+            osecs += sec
+        fp_match = all(tuple(v) == tuple(ofp) for v in gpu_fp.values())
+        slice_keys = pkey[((pkey >> 1) & 63) == 0].contiguous()
+        op = pf.create_operator()
+        op.set_stream(stream.cuda_stream)
+        op.add_input(omg.wrap_device_batch([L], len(slice_keys), [slice_keys.data_ptr()]))
+        gcols = host_columns(omg, op.drain())
+        op.delete()
+        sk = slice_keys.cpu().numpy()
+        pi, bi = jt.pairs(sk)
+        ocols = [sk[pi], pay_h[0][bi], pay_h[1][bi]]
+        if gcols is None:
+            slice_match = len(pi) == 0
+        else:
+            go, oo = np.argsort(gcols[0][0], kind="stable"), np.argsort(ocols[0], kind="stable")
+            slice_match = len(go) == len(oo) and all(
+                np.array_equal(g[0][go], o[oo]) and not g[1].any() for g, o in zip(gcols, ocols))
+        del slice_keys
+        per["oracle_check"] = {"oracle_match": bool(fp_match and slice_match), "fingerprint_match": fp_match,
+                               "rows": int(ofp[0]), "slice_rows": int(len(pi)), "slice_match": bool(slice_match),
+                               "check_s": round(time.perf_counter() - t0, 2)}
+        per["cpu_baseline"] = {"value": npb / osecs, "unit": "rows/s", "cores": host_threads(), "kind": "port",
+                               "sample": f"all {npb} probe rows against the 2^26-row build, "
+                                         f"{host_threads()} threads, output rows hashed (not materialised)"}
+        best = min(("direct", "hash_partitioned", "learned_range_partitioned", "learned_choice"),
+                   key=lambda k: per[k]["device_ms"])
+        alg = npb * 8 + per["direct"]["output_rows"] * 24
+        dev_s = per["learned_choice"]["device_ms"] / 1e3
+        per["roofline"] = {"bound": "hbm", "achieved": round(alg / dev_s / 1e9, 1), "peak": peak, "unit": "GB/s",
+                           "frac": round(alg / dev_s / 1e9 / peak, 4), "peak_kind": peak_kind, "traffic": None,
+                           "kernel": "learned choice's device time (partition passes + probes, or the direct probe)",
+                           "kernel_ms": round(dev_s * 1e3, 3), "algorithmic_bytes": int(alg),
+                           "fastest_strategy": best}
         top = float(cdf_top_share(torch, nb, s, dev))
         per["learned_choice"]["strategy"] = {0: "direct", 1: "hash_partitioned", 2: "range_partitioned"}[
             chosen["learned_choice"]]
@@ -1002,6 +1311,8 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         per["top_key_share"] = round(top, 4)
         out[f"s={s}"] = per
         del pkey
+    jt.close()
+    out["oracle_match"] = all(out[f"s={s}"]["oracle_check"]["oracle_match"] for s in (0.9, 1.1, 1.3))
     pf.close()
     bop.delete()
     bf.close()
@@ -1087,6 +1398,16 @@ def run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         barrier()
         ms = max_over_ranks(e0.elapsed_time(e1)) / steps
         info = b.info()
+        if arm == "batched_learned" or model is None:
+            # Parity (outside the timed runs): one more run, a sample of the tasks' outputs
+            # against the oracle's per-task aggregation of the same rows.
+            log(f"batched {arm} timed; oracle check")
+            b.run(stream.cuda_stream)
+            outs = b.outputs()
+            check, cpu = check_tasks(omg, keys, vals, spans, outs, args.batch_check_every)
+            omg.free_batches([x for _, x in outs])
+            res["oracle_check"] = check
+            res["cpu_baseline"] = cpu
         b.close()
         omg.free_batches(handles)
         fac.close()
@@ -1097,13 +1418,70 @@ def run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
                     "device_ms": info["run_us"] / 1e3}
     if model is not None:
         model.close()
+    arm = res.get("batched_learned", res.get("batched_plain"))
+    if arm is not None:
+        alg = total_rows * 16 + arm["groups"] * 24
+        dev_s = arm["device_ms"] / 1e3
+        peak, kind = measured_peak_gbs()
+        res["roofline"] = {"bound": "hbm", "achieved": round(alg / dev_s / 1e9, 1), "peak": peak, "unit": "GB/s",
+                           "frac": round(alg / dev_s / 1e9 / peak, 4), "peak_kind": kind, "traffic": None,
+                           "kernel": "the batched launch (graph: table init, AggTasksKernel, counts, extraction)",
+                           "kernel_ms": round(dev_s * 1e3, 3), "algorithmic_bytes": int(alg)}
     out = {"workload": BATCH_WORKLOAD if n_tasks == BATCH_TASKS else BATCH_WORKLOAD.replace("10,000", str(n_tasks)),
            "tasks": n_tasks, "rows": total_rows, "steps": steps, **res}
+    if "oracle_check" in res:
+        out["oracle_match"] = res["oracle_check"]["oracle_match"]
     if "batched_plain" in res:
         out["batched_over_operators"] = round(res["batched_plain"]["value"] / res["operators"]["value"], 2)
     if "batched_learned" in res:
         out["learned_over_plain"] = round(res["batched_learned"]["value"] / res["batched_plain"]["value"], 3)
     return out
+
+
+def check_tasks(omg, keys, vals, spans, outs, every):
+    """Every `every`-th task of a batched run against the oracle: the task's output rows (key,
+    SUM, COUNT) fingerprinted on the GPU against the fingerprint of the oracle's aggregation of
+    the task's rows (groups and values bit-exact).  The oracle runs one task per host thread;
+    its rate is the CPU baseline."""
+    import concurrent.futures as cf
+
+    import oracle
+
+    oracle.build()
+    by_task = {}
+    for t, bh in outs:
+        by_task.setdefault(t, []).append(bh)
+    picked = list(range(0, len(spans), max(1, every)))
+    threads = host_threads()
+    host_keys = {t: (keys[spans[t][0]:spans[t][0] + spans[t][1]].cpu().numpy(),
+                     vals[spans[t][0]:spans[t][0] + spans[t][1]].cpu().numpy()) for t in picked}
+
+    def one(t):
+        k, v = host_keys[t]
+        aggs = [dict(func=f, col=v, in_type=oracle.T_LONG, out_type=oracle.T_LONG)
+                for f in (oracle.F_SUM, oracle.F_COUNT_COL)]
+        t0 = time.perf_counter()
+        ks, kn, vs, vn = oracle.hashagg([k], [oracle.T_LONG], [None], aggs)
+        dt = time.perf_counter() - t0
+        return oracle.fingerprint_cols([ks[0], vs[0], vs[1]], [kn[0], vn[0], vn[1]]), len(k), dt
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        results = list(ex.map(one, picked))
+    wall = time.perf_counter() - t0
+    bad = []
+    for t, (fp, _, _) in zip(picked, results):
+        gfp = omg.batches_fingerprint(by_task.get(t, []))
+        if tuple(gfp) != tuple(fp):
+            bad.append(t)
+    rows = sum(n for _, n, _ in results)
+    cpu_s = sum(dt for _, _, dt in results)
+    check = {"oracle_match": not bad, "tasks_checked": len(picked), "rows_checked": rows,
+             "mismatched_tasks": bad[:8], "check_s": round(wall, 2)}
+    cpu = {"value": rows / (cpu_s / threads), "unit": "rows/s", "cores": threads, "kind": "port",
+           "sample": f"{len(picked)} of {len(spans)} tasks ({rows} rows), one single-threaded operator per task; "
+                     f"rate = rows / (sum of per-task seconds / {threads} threads)"}
+    return check, cpu
 
 
 def main():
@@ -1130,6 +1508,8 @@ def main():
     ap.add_argument("--batch-tasks", type=int, default=None, help="tasks of the batched aggregation (default 10,000)")
     ap.add_argument("--batch-operator-sample", type=int, default=500,
                     help="tasks run one operator each for the per-operator comparison")
+    ap.add_argument("--batch-check-every", type=int, default=10,
+                    help="every n-th task of the batched run is checked against the oracle")
     args = ap.parse_args()
     global N_PROBE
     N_PROBE = 1 << args.probe_log2
@@ -1160,10 +1540,68 @@ def main():
                             "l2": "inputs+outputs (1.4 GB/step) larger than L2; no flush needed",
                             "build_ms": round(r["build_ms"], 3), "output_rows_per_step": r["rows"]},
                  "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"],
-                 "clocks": r["clocks"], "agg": r["agg"], "agg_skewed": r["skew"], "agg_batched": r["batched"],
+                 "clocks": r["clocks"], "oracle_match": None if r.get("join_check") is None else
+                 r["join_check"]["oracle_match"], "oracle_check": r.get("join_check"),
+                 "agg": r["agg"], "agg_skewed": r["skew"], "agg_batched": r["batched"],
                  "join_skewed": r["join5"], "join_kinds": r.get("kinds"), "agg_two_stage": r.get("two_stage"),
                  "features": r.get("features")})
+    line["summary"] = summary(line)  # last key: a compact per-configuration digest
     print(json.dumps(line), flush=True)
+
+
+def _sig(x, d=3):
+    """x rounded to d significant digits (None stays None)."""
+    if x is None:
+        return None
+    if x == 0:
+        return 0
+    return float(f"{x:.{d}g}")
+
+
+def summary(line):
+    """One short object per configuration (rows/s, ms, roofline fraction, CPU baseline, oracle
+    verdict), placed at the end of the JSON line so that a reader of its tail sees them all."""
+    out = {}
+    e2e = line.get("e2e") or {}
+    cpu = line.get("cpu_baseline") or {}
+    out["cfg2_probe"] = {"rows_s": _sig(line["value"]), "ms": _sig(line["ms_per_step"]),
+                         "frac": (line.get("roofline") or {}).get("frac"), "e2e_rows_s": _sig(e2e.get("value")),
+                         "e2e_ms": _sig(e2e.get("ms_per_step")), "cpu_rows_s": _sig(cpu.get("value")),
+                         "oracle_match": line.get("oracle_match"), "e2e_oracle_match": e2e.get("oracle_match")}
+    a = line.get("agg")
+    if a:
+        out["cfg1_agg"] = {"rows_s": _sig(a["value"]), "ms": _sig(a["ms_per_step"]), "frac": a["roofline"]["frac"],
+                           "kernel_ms": a["roofline"]["kernel_ms"],
+                           "cpu_rows_s": _sig((a.get("cpu_baseline") or {}).get("value")),
+                           "oracle_match": a.get("oracle_match")}
+    k = line.get("agg_skewed")
+    if k:
+        out["cfg3_skew"] = {"plain_ms": k["plain"]["ms_per_step"], "learned_ms": k["learned"]["ms_per_step"],
+                            "exact_count_ms": k["exact_count"]["ms_per_step"],
+                            "learned_over_plain": k["learned_over_plain"], "frac": k["roofline"]["frac"],
+                            "cpu_rows_s": _sig(k["cpu_baseline"]["value"]), "oracle_match": k.get("oracle_match")}
+    b = line.get("agg_batched")
+    if b:
+        out["cfg4_batched"] = {"operators_rows_s": _sig(b["operators"]["value"]),
+                               "plain_rows_s": _sig((b.get("batched_plain") or {}).get("value")),
+                               "learned_rows_s": _sig((b.get("batched_learned") or {}).get("value")),
+                               "learned_over_plain": b.get("learned_over_plain"),
+                               "frac": (b.get("roofline") or {}).get("frac"),
+                               "cpu_rows_s": _sig((b.get("cpu_baseline") or {}).get("value")),
+                               "oracle_match": b.get("oracle_match")}
+    j = line.get("join_skewed")
+    if j:
+        d = {}
+        for sk in ("s=0.9", "s=1.1", "s=1.3"):
+            if sk in j:
+                v = j[sk]
+                d[sk] = [v["direct"]["ms_per_step"], v["hash_partitioned"]["ms_per_step"],
+                         v["learned_range_partitioned"]["ms_per_step"], v["learned_choice"]["ms_per_step"],
+                         v["roofline"]["frac"]]
+        out["cfg5_join_ms_direct_hash_range_choice_frac"] = d
+        out["cfg5_cpu_rows_s"] = _sig(j["s=1.1"]["cpu_baseline"]["value"]) if "s=1.1" in j else None
+        out["cfg5_oracle_match"] = j.get("oracle_match")
+    return out
 
 
 if __name__ == "__main__":
