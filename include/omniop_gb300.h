@@ -173,9 +173,11 @@ int32_t omg_batch_to_host(void *batch, void **out_batch);
  *   (jni_operator_factory.cpp:177-236).
  * Aggregator i reads the columns agg_cols[agg_col_offsets[i] .. agg_col_offsets[i+1]) whose
  * types are agg_input_types at the same positions; its output types are
- * agg_output_types[agg_out_offsets[i] .. agg_out_offsets[i+1]).  Mask columns must all be -1
- * (no mask) and input_raws/output_partials must be 1/0 (single-stage); other values return
- * OMG_ERR_UNSUPPORTED. */
+ * agg_output_types[agg_out_offsets[i] .. agg_out_offsets[i+1]).  mask_cols[i] >= 0 names a
+ * BOOLEAN column: aggregator i then sees only the rows where that column is TRUE (NULL counts
+ * as FALSE; every row still creates its group), as MaskColAggregator does
+ * (aggregator/mask_column_assistant_aggregator.h:44-53); -1 means no mask.  input_raws[i] = 0
+ * reads partial results and output_partials[i] = 1 emits them (two-stage aggregation). */
 int32_t omg_hashagg_factory_create(const uint32_t *group_cols, const OmgDataType *group_types,
     int32_t n_group, const uint32_t *agg_func_types, int32_t n_agg, const int32_t *agg_col_offsets,
     const uint32_t *agg_cols, const OmgDataType *agg_input_types, const int32_t *agg_out_offsets,

@@ -70,6 +70,10 @@ def DoubleType():
     return DataType(OMNI_DOUBLE)
 
 
+def BooleanType():
+    return DataType(OMNI_BOOLEAN)
+
+
 def Decimal64Type(precision=18, scale=0):
     return DataType(OMNI_DECIMAL64, precision, scale)
 
@@ -456,6 +460,8 @@ class HashAggregationOperatorFactory(OperatorFactory):
         for t in agg_output_types:
             out_types.extend(t)
             out_off.append(len(out_types))
+        if mask_cols is not None and len(mask_cols) != n_agg:
+            raise ValueError("one mask column entry per aggregator is required")
         masks = [-1] * n_agg if mask_cols is None else [(-1 if m in (None, -1, 0xFFFFFFFF) else m) for m in mask_cols]
         raws = [1] * n_agg if input_raws is None else [1 if r else 0 for r in input_raws]
         partials = [0] * n_agg if output_partials is None else [1 if p else 0 for p in output_partials]

@@ -187,7 +187,7 @@ struct BatchedAggregation::Impl {
     {
         const int64_t t0 = NowUs();
         n = static_cast<int32_t>(tasks.size());
-        bt.Build(tasks, plan.inputCols);
+        bt.Build(tasks, plan.inputCols, omg::kTileRows, &plan.inputMasks);
         bt.Upload(s);
         rows = bt.TotalRows();
         scratch.Reset(8, s, true);

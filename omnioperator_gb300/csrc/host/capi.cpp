@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -971,6 +972,11 @@ int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const 
     if (!ap.dictInputs.empty() || !ap.varlenInputs.empty()) {
         // String columns need the operator's per-call string dictionary (device allocations).
         SetError("VARCHAR/CHAR columns are not supported by the allocation-free entry point");
+        return OMG_ERR_UNSUPPORTED;
+    }
+    if (std::any_of(ap.inputMasks.begin(), ap.inputMasks.end(), [](int32_t m) { return m >= 0; })) {
+        // A mask turns into a per-call NULL bitmap of the masked inputs (a device allocation).
+        SetError("aggregation mask columns are not supported by the allocation-free entry point");
         return OMG_ERR_UNSUPPORTED;
     }
     if (!omg::DeviceAvailable()) {

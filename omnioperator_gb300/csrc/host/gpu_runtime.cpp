@@ -13,8 +13,12 @@ using omniruntime::vec::BaseVector;
 using omniruntime::vec::VectorBatch;
 
 void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vector<int32_t> &inputCols,
-    int32_t tileRows)
+    int32_t tileRows, const std::vector<int32_t> *inputMasks)
 {
+    maskSlots_.clear();
+    maskJobs_.clear();
+    maskWords_ = 0;
+    masksDone_ = false;
     if (inputCols.size() > static_cast<size_t>(kMaxInputs)) {
         throw OmniException("UNSUPPORTED_ERROR", "too many input columns for one kernel", -2);
     }
@@ -56,6 +60,31 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
             if (hasNull) {
                 anyNulls_[i] = true;
             }
+            const int32_t m = inputMasks != nullptr && i < inputMasks->size() ? (*inputMasks)[i] : -1;
+            if (m < 0) {
+                continue;
+            }
+            if (m >= b->GetVectorCount()) {
+                throw OmniException("OPERATOR_RUNTIME_ERROR",
+                    "input batch has " + std::to_string(b->GetVectorCount()) + " vectors, mask column " +
+                        std::to_string(m) + " requested",
+                    -1);
+            }
+            BaseVector *mv = b->Get(m);
+            if (mv->GetEncoding() != omniruntime::vec::OMNI_FLAT || mv->GetSize() < b->GetRowCount()) {
+                throw OmniException("OPERATOR_RUNTIME_ERROR", "mask column is not a flat vector of the batch's rows", -1);
+            }
+            MaskJob job{};
+            job.valueNulls = d.nulls[i];
+            job.maskValues = static_cast<const uint8_t *>(mv->RawValues());
+            job.maskNulls = mv->RawNulls() != nullptr && mv->HasNull() ? mv->RawNulls() : nullptr;
+            job.out = nullptr;
+            job.rows = d.rows;
+            maskJobs_.push_back(job);
+            maskSlots_.push_back(MaskSlot{bi, static_cast<int32_t>(i), maskWords_});
+            maskWords_ += (d.rows + 31) / 32;
+            d.nulls[i] = nullptr;  // set at Upload, once the bitmap exists
+            anyNulls_[i] = true;
         }
         for (int64_t r = 0; r < d.rows; r += tileRows) {
             TileDesc &td = tiles_[t];
@@ -72,6 +101,23 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
 
 void BatchTable::Upload(cudaStream_t s)
 {
+    if (!maskJobs_.empty() && !masksDone_) {
+        maskBits_.Reset(static_cast<size_t>(std::max<int64_t>(maskWords_, 1)), s);
+        hMaskJobs_.Reset(maskJobs_.size());
+        for (size_t j = 0; j < maskJobs_.size(); ++j) {
+            const MaskSlot &ms = maskSlots_[j];
+            MaskJob job = maskJobs_[j];
+            job.out = maskBits_.Get() + ms.word;
+            hMaskJobs_[j] = job;
+            descs_[ms.batch].nulls[ms.input] = reinterpret_cast<const uint8_t *>(job.out);
+        }
+        dMaskJobs_.Reset(maskJobs_.size(), s);
+        CudaCheck(cudaMemcpyAsync(dMaskJobs_.Get(), hMaskJobs_.Get(), sizeof(MaskJob) * maskJobs_.size(),
+                      cudaMemcpyHostToDevice, s),
+            "upload mask jobs");
+        CudaCheck(LaunchMaskNulls(dMaskJobs_.Get(), static_cast<int32_t>(maskJobs_.size()), s), "mask NULL bitmaps");
+        masksDone_ = true;
+    }
     dBatches_.Reset(std::max<size_t>(descs_.Size(), 1), s);
     dTiles_.Reset(std::max<size_t>(tiles_.Size(), 1), s);
     dTileOut_.Reset(std::max<size_t>(tileOut_.Size(), 1), s);

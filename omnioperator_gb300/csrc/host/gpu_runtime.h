@@ -152,11 +152,14 @@ private:
 };
 
 // Descriptors of a list of batches for one launch.  Kernel input i of batch b is column
-// inputCols[i] of the batch.
+// inputCols[i] of the batch.  With inputMasks (one entry per input, -1 = none), an input whose
+// entry is column m reads its values as usual but its NULL bitmap is computed on the device at
+// Upload: the value column's NULLs plus every row whose BOOLEAN column m is NULL or FALSE
+// (aggregation mask columns).
 class BatchTable {
 public:
     void Build(const std::vector<omniruntime::vec::VectorBatch *> &batches, const std::vector<int32_t> &inputCols,
-        int32_t tileRows = kTileRows);
+        int32_t tileRows = kTileRows, const std::vector<int32_t> *inputMasks = nullptr);
     // Copy descriptors to the device on `s` (again after SetInput).
     void Upload(cudaStream_t s);
     // Point input `input` of batch `batch` at other fixed-width values (e.g. dictionary ids of
@@ -178,6 +181,18 @@ public:
     bool AnyNulls(int32_t input) const { return input < static_cast<int32_t>(anyNulls_.size()) && anyNulls_[input]; }
 
 private:
+    struct MaskSlot {
+        size_t batch;
+        int32_t input;
+        int64_t word;  // offset of the input's bitmap in maskBits_ (32-bit words)
+    };
+    std::vector<MaskSlot> maskSlots_;
+    std::vector<MaskJob> maskJobs_;
+    int64_t maskWords_ = 0;
+    bool masksDone_ = false;
+    DevArray<uint32_t> maskBits_;
+    PinnedArray<MaskJob> hMaskJobs_;
+    DevArray<MaskJob> dMaskJobs_;
     PinnedArray<BatchDesc> descs_;
     PinnedArray<TileDesc> tiles_;
     PinnedArray<int64_t> tileOut_;

@@ -134,18 +134,25 @@ OmniStatus HashAggregationOperatorFactory::Init()
     if (aggCols_.size() != nAgg || aggInputTypes_.size() != nAgg || aggOutputTypes_.size() != nAgg) {
         throw OmniException("INVALID_ARGUMENT", "aggregator columns/types/functions disagree", -1);
     }
-    for (uint32_t m : maskCols_) {
-        if (m != UINT32_MAX) {
-            throw OmniException("UNSUPPORTED_ERROR", "aggregation mask columns are not supported", -2);
-        }
+    // Mask columns (aggregation.cpp:12-18, MaskColAggregator): aggregator a sees only the rows
+    // whose BOOLEAN column maskCols_[a] is TRUE (a NULL mask counts as FALSE); UINT32_MAX (the
+    // reference's static_cast<uint32_t>(-1)) means no mask.  Every row still creates its group.
+    if (!maskCols_.empty() && maskCols_.size() != nAgg) {
+        throw OmniException("INVALID_ARGUMENT", "one mask column entry per aggregator is required", -1);
     }
+    auto maskOf = [&](size_t a) {
+        return a < maskCols_.size() && maskCols_[a] != UINT32_MAX ? static_cast<int32_t>(maskCols_[a]) : -1;
+    };
 
     AggPlan &p = plan_;
     p = AggPlan();
     p.overflowAsNull = overflowAsNull_;
-    std::map<uint32_t, int32_t> inputOf;  // batch column -> kernel input
-    auto inputFor = [&](uint32_t col, int width) {
-        auto it = inputOf.find(col);
+    // (batch column, mask column or -1) -> kernel input.  A masked input reads the column's values
+    // with the rows its mask drops turned into NULLs (BatchTable builds that bitmap), so every
+    // accumulator, strategy and merge handles masks the way it handles NULL values.
+    std::map<std::pair<uint32_t, int32_t>, int32_t> inputOf;
+    auto inputFor = [&](uint32_t col, int width, int32_t mask = -1) {
+        auto it = inputOf.find(std::make_pair(col, mask));
         if (it != inputOf.end()) {
             p.inputWidths[it->second] = std::max(p.inputWidths[it->second], width);
             return it->second;
@@ -156,7 +163,8 @@ OmniStatus HashAggregationOperatorFactory::Init()
         }
         p.inputCols.push_back(static_cast<int32_t>(col));
         p.inputWidths.push_back(width);
-        inputOf[col] = idx;
+        p.inputMasks.push_back(mask);
+        inputOf[std::make_pair(col, mask)] = idx;
         return idx;
     };
 
@@ -282,13 +290,14 @@ OmniStatus HashAggregationOperatorFactory::Init()
         o.outType = static_cast<int16_t>(outT->GetId());
         o.outWidth = static_cast<int16_t>(outT->ByteWidth());
         o.countAcc = -1;
+        const int32_t mask = maskOf(a);
         if (!raw && (fn == OMNI_AGGREGATION_TYPE_COUNT_ALL || fn == OMNI_AGGREGATION_TYPE_COUNT_COLUMN)) {
             // final COUNT / COUNT(*): the sum of the partial counts
             if (aggCols_[a].size() != 1 || aggInputTypes_[a].GetSize() != 1 ||
                 !IsIntegerLike(aggInputTypes_[a].GetType(0)->GetId())) {
                 throw OmniException("INVALID_ARGUMENT", "a final COUNT reads one integer column of partial counts", -1);
             }
-            const int in = inputFor(aggCols_[a][0], aggInputTypes_[a].GetType(0)->ByteWidth());
+            const int in = inputFor(aggCols_[a][0], aggInputTypes_[a].GetType(0)->ByteWidth(), mask);
             accFor(omg::ACC_NULLS, in, omg::IN_NONE, 0, 0);
             o.kind = omg::OUT_COUNT_MERGE;
             o.src = static_cast<int16_t>(
@@ -299,6 +308,13 @@ OmniStatus HashAggregationOperatorFactory::Init()
         if (fn == OMNI_AGGREGATION_TYPE_COUNT_ALL) {
             o.kind = omg::OUT_COUNT;
             o.src = 0;
+            if (mask >= 0) {
+                // COUNT(*) of the rows the mask keeps: COUNT_ALL minus the NULLs of the mask
+                // column read through its own mask (its NULL and FALSE rows).
+                o.countAcc = static_cast<int16_t>(
+                    accFor(omg::ACC_NULLS, inputFor(static_cast<uint32_t>(mask), 1, mask), omg::IN_NONE, 0, 0));
+                o.boundKind = 2;  // marks a masked COUNT(*) (AlignSchema emits 1 for it)
+            }
             p.outs.push_back(o);
             p.outTypes.push_back(outT);
             rowBytes += o.outWidth;
@@ -311,8 +327,8 @@ OmniStatus HashAggregationOperatorFactory::Init()
                 !IsIntegerLike(aggInputTypes_[a].GetType(1)->GetId())) {
                 throw OmniException("INVALID_ARGUMENT", "a final AVG reads (double sum, long count) partial columns", -1);
             }
-            const int inSum = inputFor(aggCols_[a][0], 8);
-            const int inCnt = inputFor(aggCols_[a][1], aggInputTypes_[a].GetType(1)->ByteWidth());
+            const int inSum = inputFor(aggCols_[a][0], 8, mask);
+            const int inCnt = inputFor(aggCols_[a][1], aggInputTypes_[a].GetType(1)->ByteWidth(), mask);
             accFor(omg::ACC_NULLS, inSum, omg::IN_NONE, 0, 0);
             accFor(omg::ACC_NULLS, inCnt, omg::IN_NONE, 0, 0);
             const int sumAcc = accFor(omg::ACC_DSUM, inSum, omg::IN_DOUBLE, 8, 0);
@@ -343,7 +359,7 @@ OmniStatus HashAggregationOperatorFactory::Init()
         const DataTypePtr &inT = aggInputTypes_[a].GetType(0);
         const DataTypeId inId = inT->GetId();
         const int inW = inT->ByteWidth();
-        const int input = inputFor(aggCols_[a][0], inW);
+        const int input = inputFor(aggCols_[a][0], inW, mask);
         const int nulls = accFor(omg::ACC_NULLS, input, omg::IN_NONE, 0, 0);
         o.countAcc = static_cast<int16_t>(nulls);
         const bool isInt = IsIntegerLike(inId);
@@ -518,8 +534,11 @@ OmniStatus HashAggregationOperatorFactory::Init()
                 c.inWidth = p.key.cols[o.src].width;
                 break;
             case omg::OUT_COUNT:
-                c.op = o.countAcc < 0 ? omg::ALIGN_ONE : omg::ALIGN_VALID;
-                c.input = o.countAcc < 0 ? -1 : p.accs[o.countAcc].input;
+                // AlignSchema reads each aggregator's own input columns and ignores its mask
+                // (MaskColAggregator::AlignAggSchema, mask_column_assistant_aggregator.h:75-85);
+                // its batch table is built without the masks, so masked inputs read plain NULLs.
+                c.op = o.countAcc < 0 || o.boundKind == 2 ? omg::ALIGN_ONE : omg::ALIGN_VALID;
+                c.input = c.op == omg::ALIGN_ONE ? -1 : p.accs[o.countAcc].input;
                 break;
             case omg::OUT_SUM_WRAP:
             case omg::OUT_MIN_INT:
@@ -1058,7 +1077,7 @@ void HashAggregationOperator::Flush()
         im.stats.Reset(8, s, true);
     }
     omg::BatchTable bt;
-    bt.Build(pending_, plan_.inputCols);
+    bt.Build(pending_, plan_.inputCols, omg::kTileRows, &plan_.inputMasks);
     bt.Upload(s);
     const int64_t rows = bt.TotalRows();
     if (!plan_.dictInputs.empty() || !plan_.varlenInputs.empty()) {
@@ -1281,7 +1300,7 @@ bool HashAggregationOperator::ExtractSpilled()
     uint64_t estimate = 0;
     {
         omg::BatchTable bt;
-        bt.Build(pending_, plan_.inputCols);
+        bt.Build(pending_, plan_.inputCols, omg::kTileRows, &plan_.inputMasks);
         bt.Upload(s);
         if (!im.decided) {
             Decide(bt, s);
@@ -1298,17 +1317,20 @@ bool HashAggregationOperator::ExtractSpilled()
         ++bits;
     }
     const int32_t nParts = 1 << bits;
-    // Column types and the widest column index of the batches, for the partition views.
-    int32_t nCols = 0;
-    for (int32_t c : plan_.inputCols) {
-        nCols = std::max(nCols, c + 1);
+    // A partition batch holds one column per kernel input (values and NULLs as the kernels read
+    // them, masks applied), and the partitions are aggregated by a plan reading input i from
+    // column i without masks.
+    const int32_t nInputs = static_cast<int32_t>(plan_.inputCols.size());
+    std::vector<DataTypeId> colType(static_cast<size_t>(nInputs), OMNI_BYTE);
+    for (int32_t i = 0; i < nInputs; ++i) {
+        colType[static_cast<size_t>(i)] = pending_.front()->Get(plan_.inputCols[i])->GetTypeId();
     }
-    std::vector<DataTypeId> colType(static_cast<size_t>(nCols), OMNI_BYTE);
-    for (int32_t c : plan_.inputCols) {
-        colType[static_cast<size_t>(c)] = pending_.front()->Get(c)->GetTypeId();
+    AggPlan partPlan = plan_;
+    for (int32_t i = 0; i < nInputs; ++i) {
+        partPlan.inputCols[i] = i;
+        partPlan.inputMasks[i] = -1;
     }
     std::vector<std::vector<VectorBatch *>> parts(static_cast<size_t>(nParts));
-    auto dummy = omg::Buffer::NewHost(16, true);
     const int64_t chunkRows = omg::AggFlushRows();
     size_t next = 0;
     try {
@@ -1320,7 +1342,7 @@ bool HashAggregationOperator::ExtractSpilled()
                 chunk.push_back(pending_[next++]);
             }
             omg::BatchTable bt;
-            bt.Build(chunk, plan_.inputCols);
+            bt.Build(chunk, plan_.inputCols, omg::kTileRows, &plan_.inputMasks);
             bt.Upload(s);
             omg::AggLaunch p = MakeLaunch(plan_, nullptr, 0, nullptr, nullptr);
             p.batches = bt.DeviceBatches();
@@ -1369,15 +1391,9 @@ bool HashAggregationOperator::ExtractSpilled()
                     continue;
                 }
                 auto *vb = new VectorBatch(static_cast<size_t>(n));
-                for (int32_t c = 0; c < nCols; ++c) {
-                    const auto it = std::find(plan_.inputCols.begin(), plan_.inputCols.end(), c);
-                    if (it == plan_.inputCols.end()) {
-                        vb->Append(new vec::BaseVector(OMNI_BYTE, 1, 0, dummy, 0, nullptr, 0, false));
-                        continue;
-                    }
-                    const size_t i = static_cast<size_t>(it - plan_.inputCols.begin());
+                for (int32_t i = 0; i < nInputs; ++i) {
                     const int32_t w = a.width[i];
-                    vb->Append(new vec::BaseVector(colType[static_cast<size_t>(c)], w, static_cast<int32_t>(n), hostCols[i],
+                    vb->Append(new vec::BaseVector(colType[static_cast<size_t>(i)], w, static_cast<int32_t>(n), hostCols[i],
                         static_cast<size_t>(base) * w, hostNulls[i], static_cast<size_t>(base / 8),
                         hostNulls[i] != nullptr));
                 }
@@ -1399,7 +1415,7 @@ bool HashAggregationOperator::ExtractSpilled()
         if (pl.empty()) {
             continue;
         }
-        HashAggregationOperator part(plan_, sizer_);
+        HashAggregationOperator part(partPlan, sizer_);
         part.SetStrategy(strategy_, 0);
         part.SetDeviceOutput(deviceOutput_);
         if (userStreamSet_) {
@@ -1504,7 +1520,7 @@ void HashAggregationOperator::Extract()
         }
         counters_[4] = static_cast<int64_t>(hc[2]);
         omg::BatchTable bt;
-        bt.Build(im.retained, plan_.inputCols, 1 << 30);
+        bt.Build(im.retained, plan_.inputCols, 1 << 30, &plan_.inputMasks);
         // VARCHAR inputs read through the id / zero columns their flush made (same order).
         const size_t nDict = plan_.dictInputs.size();
         for (size_t b = 0; b < im.retainedInputs.size() && b < bt.NumBatches(); ++b) {

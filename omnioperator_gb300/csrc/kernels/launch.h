@@ -51,6 +51,8 @@ cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtr
     const unsigned long long *ambSlots, uint32_t nAmb, uint8_t *forced, cudaStream_t stream);
 
 // ---- utilities (util.cu)
+// Masked-input NULL bitmaps, one per job (see MaskJob).
+cudaError_t LaunchMaskNulls(const MaskJob *jobs, int32_t nJobs, cudaStream_t stream);
 // [0] rows, [1] and [2] two order-independent 64-bit sums of per-row column hashes.
 cudaError_t LaunchFingerprint(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, int32_t nCols,
     const int32_t *widths, unsigned long long *out, cudaStream_t stream);

@@ -26,6 +26,18 @@ struct BatchDesc {
     int64_t rowBase;  // index of the batch's first row in arrival order
 };
 
+// An aggregation input whose rows are filtered by a mask column
+// (MaskColAggregator::ProcessGroup, mask_column_assistant_aggregator.h:44-53): `out` receives
+// the input's NULL bitmap with every row whose mask value is NULL or FALSE added to it, so
+// every accumulator skips those rows as it skips NULL values.
+struct MaskJob {
+    const uint8_t *valueNulls;  // the value column's NULL bitmap (nullptr: none)
+    const uint8_t *maskValues;  // BOOLEAN mask column, one byte per row
+    const uint8_t *maskNulls;   // its NULL bitmap (nullptr: none)
+    uint32_t *out;              // ceil(rows / 32) words
+    int64_t rows;
+};
+
 struct TileDesc {
     int32_t batch;
     int32_t row0;

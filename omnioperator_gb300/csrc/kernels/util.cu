@@ -56,6 +56,29 @@ __global__ void FingerprintKernel(const BatchDesc *batches, const TileDesc *tile
     }
 }
 
+// One warp per 32-row word of one job: lane l decides row 32w + l, the ballot is the word.
+__global__ void MaskNullsKernel(const MaskJob *jobs, int32_t nJobs)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.y) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t warps = (static_cast<int64_t>(gridDim.y) * blockDim.x) >> 5;
+    for (int j = blockIdx.x; j < nJobs; j += gridDim.x) {
+        const MaskJob job = jobs[j];
+        const int64_t words = (job.rows + 31) >> 5;
+        for (int64_t w = warp; w < words; w += warps) {
+            const int64_t row = (w << 5) + lane;
+            bool skip = false;
+            if (row < job.rows) {
+                skip = __ldg(job.maskValues + row) == 0 || NullRO(job.maskNulls, row) || NullRO(job.valueNulls, row);
+            }
+            const unsigned bits = __ballot_sync(0xffffffffu, skip);
+            if (lane == 0) {
+                job.out[w] = bits;
+            }
+        }
+    }
+}
+
 std::mutex g_attrMutex;
 // (device, kernel) -> dynamic shared-memory limit set so far.
 std::map<std::tuple<int, const void *>, size_t> g_smemSet;
@@ -127,6 +150,16 @@ int BlocksPerSM(const void *kernel, int threads, size_t smemBytes)
     std::lock_guard<std::mutex> lock(g_attrMutex);
     g_blocksPerSM[key] = n;
     return n;
+}
+
+cudaError_t LaunchMaskNulls(const MaskJob *jobs, int32_t nJobs, cudaStream_t stream)
+{
+    if (nJobs <= 0) {
+        return cudaSuccess;
+    }
+    const dim3 grid(static_cast<unsigned>(nJobs < 65535 ? nJobs : 65535), 8);
+    MaskNullsKernel<<<grid, 256, 0, stream>>>(jobs, nJobs);
+    return cudaGetLastError();
 }
 
 cudaError_t LaunchFingerprint(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, int32_t nCols,

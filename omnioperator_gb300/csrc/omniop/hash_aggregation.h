@@ -38,6 +38,8 @@ namespace op {
 struct AggPlan {
     std::vector<int32_t> inputCols;        // batch column of each kernel input
     std::vector<int32_t> inputWidths;      // value bytes of each kernel input
+    std::vector<int32_t> inputMasks;       // mask column of each kernel input (-1: none): the
+                                           // rows whose mask is NULL or FALSE read as NULL
     omg::KeySpec key{};
     std::vector<omg::AccSpec> accs;
     std::vector<int16_t> regInput;         // kernel inputs cached in registers per row

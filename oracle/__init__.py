@@ -53,7 +53,7 @@ def lib() -> C.CDLL:
         L = C.CDLL(str(LIB))
         P, I32, I64 = C.c_void_p, C.c_int32, C.c_int64
         L.orc_hashagg.restype = I64
-        L.orc_hashagg.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P]
+        L.orc_hashagg.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P, P]
         L.orc_join_inner.restype = I64
         L.orc_join_inner.argtypes = [I64, P, I32, P, I64, P, I32, P, P, P, I64]
         L.orc_join.restype = I64
@@ -74,7 +74,7 @@ def lib() -> C.CDLL:
         L.orc_jtable_pairs.argtypes = [P, I64, P, P, P, P, I64]
         L.orc_hashagg_mt.restype = I64
         L.orc_hashagg_mt.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P, P, P,
-                                     I32]
+                                     I32, P]
         _lib = L
     return _lib
 
@@ -87,12 +87,31 @@ def _ptr_array(arrs):
     return (C.c_void_p * max(len(arrs), 1))(*[(a.ctypes.data if a is not None else None) for a in arrs])
 
 
+def _masks(aggs):
+    """Per aggregator: a byte per row, 1 where the row reaches the aggregator (its mask value
+    is TRUE and not NULL), or None for an aggregator without a mask column."""
+    out = []
+    for a in aggs:
+        m = a.get("mask")
+        if m is None:
+            out.append(None)
+            continue
+        m = np.asarray(m, dtype=bool)
+        mn = a.get("mask_nulls")
+        if mn is not None:
+            m = m & ~np.asarray(mn, dtype=bool)
+        out.append(np.ascontiguousarray(m, dtype=np.uint8))
+    return out
+
+
 def hashagg(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=False):
     """Single-stage hash aggregation with the reference's semantics.
 
     keys: list of value arrays (int types as their numpy ints, decimal128 as (n, 2) uint64).
     key_nulls: list of bool arrays or None.  aggs: list of dicts with keys func, col (array or
-    None for COUNT(*)), in_type, out_type, nulls (bool array or None), rescale (int).
+    None for COUNT(*)), in_type, out_type, nulls (bool array or None), rescale (int), and
+    optionally mask / mask_nulls (bool arrays: the aggregator's mask column; a row reaches it
+    only where the mask is TRUE and not NULL).
     Returns (key_values, key_nulls, agg_values, agg_nulls) per group (unordered), or raises
     OverflowError when an overflow must raise (overflow-as-null off)."""
     L = lib()
@@ -125,11 +144,12 @@ def hashagg(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=False):
     oknulls = [np.zeros(maxg, dtype=np.uint8) for _ in kw]
     ovals = [np.zeros((maxg, 2), dtype=np.uint64) for _ in aggs]
     ovnulls = [np.zeros(maxg, dtype=np.uint8) for _ in aggs]
+    masks = _masks(aggs)  # kept alive across the call (the pointer array holds raw addresses)
     g = L.orc_hashagg(n, len(keys), _ptr_array(kcols), _ptr(np.array(kw, dtype=np.int32)),
                       _ptr_array(knulls), len(aggs), _ptr(funcs), _ptr_array(cols), _ptr(in_types),
                       _ptr(in_widths), _ptr_array(anulls), _ptr(out_types), _ptr(rescale), policy,
                       1 if overflow_as_null else 0, maxg, _ptr_array(okeys), _ptr_array(oknulls),
-                      _ptr_array(ovals), _ptr_array(ovnulls))
+                      _ptr_array(ovals), _ptr_array(ovnulls), _ptr_array(masks))
     if g == -2:
         raise OverflowError("sum_aggregator overflow.")
     if g < 0:
@@ -362,12 +382,14 @@ def hashagg_mt(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=Fals
     dbl = [a["func"] in (F_SUM, F_AVG) and t == T_DOUBLE for a, t in zip(aggs, in_types)]
     exact = [np.zeros(maxg) if d else None for d in dbl]
     absum = [np.zeros(maxg) if d else None for d in dbl]
+    masks = _masks(aggs)  # kept alive across the call (the pointer array holds raw addresses)
     g = L.orc_hashagg_mt(n, len(keys), _ptr_array(kcols), _ptr(np.array(kw, dtype=np.int32)), _ptr_array(knulls),
                          len(aggs), _ptr(funcs), _ptr_array(cols), _ptr(in_types_a),
                          _ptr(np.array(in_widths, dtype=np.int32)), _ptr_array(anulls),
                          _ptr(np.array(out_types, dtype=np.int32)), _ptr(np.array(rescale, dtype=np.int32)), policy,
                          1 if overflow_as_null else 0, maxg, _ptr_array(okeys), _ptr_array(oknulls),
-                         _ptr_array(ovals), _ptr_array(ovnulls), _ptr_array(exact), _ptr_array(absum), threads)
+                         _ptr_array(ovals), _ptr_array(ovnulls), _ptr_array(exact), _ptr_array(absum), threads,
+                         _ptr_array(masks))
     if g == -2:
         raise OverflowError("sum_aggregator overflow.")
     if g == -3:

@@ -171,6 +171,7 @@ typedef struct {
     int func, in_type, in_width, out_type, rescale;
     const void *col;
     const uint8_t *nulls; /* byte per row, 1 = null; NULL = no nulls */
+    const uint8_t *mask;  /* byte per row, 1 = the row reaches this aggregator; NULL = no mask */
 } agg_t;
 
 typedef struct {
@@ -213,6 +214,10 @@ static void state_init(const agg_t *a, state_t *s)
 
 static void state_update(const aggctx_t *c, const agg_t *a, state_t *s, int64_t r)
 {
+    /* A masked aggregator sees only the rows whose mask value is TRUE; a NULL or FALSE mask
+     * skips the row (MaskColAggregator::ProcessGroup, mask_column_assistant_aggregator.h:44-53).
+     * The row's group exists either way. */
+    if (a->mask && !a->mask[r]) return;
     if (a->func == F_COUNT_ALL) {
         s->i64++;
         return;
@@ -374,7 +379,7 @@ int64_t orc_hashagg(int64_t n_rows, int32_t nkey, const void **key_cols, const i
     const uint8_t **key_nulls, int32_t nagg, const int32_t *funcs, const void **agg_cols, const int32_t *in_types,
     const int32_t *in_widths, const uint8_t **agg_nulls, const int32_t *out_types, const int32_t *rescale,
     int32_t policy, int32_t overflow_as_null, int64_t max_groups, void **out_keys, uint8_t **out_key_nulls,
-    void **out_vals, uint8_t **out_val_nulls)
+    void **out_vals, uint8_t **out_val_nulls, const uint8_t **agg_masks)
 {
     int keybytes = 0;
     for (int i = 0; i < nkey; ++i) keybytes += 1 + key_widths[i];
@@ -396,6 +401,7 @@ int64_t orc_hashagg(int64_t n_rows, int32_t nkey, const void **key_cols, const i
         c.aggs[a].nulls = agg_nulls ? agg_nulls[a] : NULL;
         c.aggs[a].out_type = out_types[a];
         c.aggs[a].rescale = rescale ? rescale[a] : 0;
+        c.aggs[a].mask = agg_masks ? agg_masks[a] : NULL;
     }
     int64_t ret = 0;
     for (int64_t r = 0; r < n_rows; ++r) {
@@ -1087,7 +1093,8 @@ static void *hmt_thread(void *arg)
         for (int a = 0; a < nagg; ++a) {
             const agg_t *ag = &w->c.aggs[a];
             state_update(&w->c, ag, &w->c.st[g * nagg + a], r);
-            if (ag->in_type == T_DOUBLE && (ag->func == F_SUM || ag->func == F_AVG) && !(ag->nulls && ag->nulls[r])) {
+            if (ag->in_type == T_DOUBLE && (ag->func == F_SUM || ag->func == F_AVG) && !(ag->nulls && ag->nulls[r]) &&
+                !(ag->mask && !ag->mask[r])) {
                 const double x = ((const double *)ag->col)[r];
                 dd_add(&w->ehi[g * na + a], &w->elo[g * na + a], x);
                 w->eabs[g * na + a] += x < 0 ? -x : x;
@@ -1126,7 +1133,8 @@ int64_t orc_hashagg_mt(int64_t n_rows, int32_t nkey, const void **key_cols, cons
     const uint8_t **key_nulls, int32_t nagg, const int32_t *funcs, const void **agg_cols, const int32_t *in_types,
     const int32_t *in_widths, const uint8_t **agg_nulls, const int32_t *out_types, const int32_t *rescale,
     int32_t policy, int32_t overflow_as_null, int64_t max_groups, void **out_keys, uint8_t **out_key_nulls,
-    void **out_vals, uint8_t **out_val_nulls, double **out_exact, double **out_abs, int32_t nthreads)
+    void **out_vals, uint8_t **out_val_nulls, double **out_exact, double **out_abs, int32_t nthreads,
+    const uint8_t **agg_masks)
 {
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 255) nthreads = 255;
@@ -1150,6 +1158,7 @@ int64_t orc_hashagg_mt(int64_t n_rows, int32_t nkey, const void **key_cols, cons
         aggs[a].nulls = agg_nulls ? agg_nulls[a] : NULL;
         aggs[a].out_type = out_types[a];
         aggs[a].rescale = rescale ? rescale[a] : 0;
+        aggs[a].mask = agg_masks ? agg_masks[a] : NULL;
     }
     for (int i = 0; i < nthreads; ++i) {
         pw[i].r0 = n_rows * i / nthreads;

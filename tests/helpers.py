@@ -24,14 +24,16 @@ def split(n, sizes):
 
 def run_agg(group_cols, group_types, aggs_cols, agg_in_types, agg_out_types, funcs, columns, types, nulls=None,
             batch_sizes=(4096,), overflow_as_null=False, strategy=None, capacity_hint=0, device_input=False,
-            pipeline=False):
+            pipeline=False, mask_cols=None, spill_budget=None):
     """Run HashAggregation on the GPU; returns (output columns as [(values, mask)], op counters)."""
     fac = omg.HashAggregationOperatorFactory(group_cols, group_types, aggs_cols, agg_in_types, agg_out_types, funcs,
-                                             overflow_as_null=overflow_as_null)
+                                             mask_cols=mask_cols, overflow_as_null=overflow_as_null)
     op = fac.create_operator()
     try:
         if strategy is not None:
             op.set_agg_strategy(strategy, capacity_hint)
+        if spill_budget is not None:
+            op.set_spill(True, spill_budget)
         if pipeline:
             op.set_no_more_input(False)
         n = len(columns[0])

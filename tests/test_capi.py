@@ -226,6 +226,23 @@ def test_noalloc_entry_refuses_string_columns_before_touching_a_device():
     f.close()
 
 
+def test_mask_columns_are_checked_on_the_host():
+    """A mask list has one entry per aggregator; the allocation-free entry refuses masked plans
+    (their NULL bitmaps are per-call device allocations) before it touches a device."""
+    L = omg.LongType()
+    with pytest.raises(ValueError):
+        omg.HashAggregationOperatorFactory([0], [L], [[1], [1]], [[L], [L]], [[L], [L]],
+                                           [omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_MIN],
+                                           mask_cols=[2, 0xFFFFFFFF, 2])
+    f = omg.HashAggregationOperatorFactory([0], [L], [[1], [1]], [[L], [L]], [[L], [L]],
+                                           [omg.OMNI_AGGREGATION_TYPE_SUM, omg.OMNI_AGGREGATION_TYPE_MIN],
+                                           mask_cols=[2, 0xFFFFFFFF])
+    n = C.c_int64(0)
+    rc = omg.lib().omg_hashagg_run_noalloc(f.handle, None, None, 0, 0, None, None, 0, 16, C.byref(n), None)
+    assert rc == -2
+    f.close()
+
+
 def test_spill_settings_are_checked_on_the_host():
     """Spill takes fixed-width plans without order-dependent sums, and needs a budget."""
     L, V = omg.LongType(), omg.VarcharType(8)

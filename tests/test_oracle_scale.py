@@ -127,3 +127,33 @@ def test_join_table_fingerprint_and_pairs(dense):
             assert fp == oracle.fingerprint_cols([pkey[pi], p1[bi], p2[bi]])
     finally:
         jt.close()
+
+
+def test_masked_aggregator_equals_aggregator_over_kept_rows():
+    """The oracle's mask rule (MaskColAggregator::ProcessGroup): a masked aggregator equals the
+    unmasked one over the rows whose mask is TRUE and not NULL, and every row still makes its
+    group (groups without kept rows give NULL / 0)."""
+    rng = np.random.default_rng(8)
+    n = 20_000
+    key = rng.integers(0, 300, n).astype(np.int64)
+    v = rng.integers(-10**6, 10**6, n).astype(np.int64)
+    vn = rng.random(n) < 0.05
+    mask = rng.random(n) < 0.5
+    mask[key < 20] = False
+    mn = rng.random(n) < 0.1
+    funcs = (oracle.F_SUM, oracle.F_COUNT_COL, oracle.F_COUNT_ALL, oracle.F_MIN, oracle.F_MAX)
+    masked = oracle.hashagg_mt([key], [oracle.T_LONG], [None],
+                               [dict(func=f, col=v, in_type=oracle.T_LONG, out_type=oracle.T_LONG, nulls=vn,
+                                     mask=mask, mask_nulls=mn) for f in funcs], threads=3)
+    keep = mask & ~mn
+    plain = oracle.hashagg([key[keep]], [oracle.T_LONG], [None],
+                           [dict(func=f, col=v[keep], in_type=oracle.T_LONG, out_type=oracle.T_LONG, nulls=vn[keep])
+                            for f in funcs])
+    got, want = _groups(masked), _groups(plain)
+
+    assert len(got) == len(np.unique(key))
+    for k, vals in got.items():
+        if k in want:
+            assert vals == want[k]
+        else:  # no kept row: NULL SUM/MIN/MAX, zero counts
+            assert vals == (None, 0, 0, None, None)
