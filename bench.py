@@ -296,7 +296,15 @@ def compare_agg_full(gpu_cols, ora, nkeys, double_aggs):
             else:
                 same = np.array_equal(a.astype(np.int64), b.astype(np.int64))
             if not same:
-                res.update(oracle_match=False, why=f"aggregate {j} differs")
+                if a.ndim == 2 or b.ndim == 2:
+                    bad = np.nonzero((a.view(np.uint64).reshape(-1, 2) != b.view(np.uint64).reshape(-1, 2)).any(1))[0]
+                else:
+                    bad = np.nonzero(a.astype(np.int64) != b.astype(np.int64))[0]
+                rows = np.nonzero(live)[0][bad[:3]]
+                sample = [{"keys": [str(gpu_cols[k][0][go][r]) for k in range(nkeys)],
+                           "gpu": str(gpu_cols[nkeys + j][0][go][r].tolist()), "oracle": str(ovals[j][oo][r].tolist())}
+                          for r in rows]
+                res.update(oracle_match=False, why=f"aggregate {j} differs in {len(bad)} groups", sample=sample)
                 return res
     res.update(oracle_match=worst <= 1.0, double_err_over_tol=round(worst, 6))
     if double_aggs:

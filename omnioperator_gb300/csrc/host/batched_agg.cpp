@@ -273,7 +273,7 @@ struct BatchedAggregation::Impl {
             outCols[o].width = plan.outs[o].outWidth;
             outCols[o].values = omg::Buffer::NewDevice(outBound * plan.outs[o].outWidth + 16, s, false);
             outCols[o].nulls = omg::Buffer::NewDevice(omg::NullBitmapBytes(static_cast<int64_t>(outBound)), s, true);
-            outCols[o].hasNull = plan.outs[o].kind != omg::OUT_COUNT;
+            outCols[o].hasNull = plan.outs[o].kind != omg::OUT_COUNT && plan.outs[o].kind != omg::OUT_IS_EMPTY;
         }
         CudaCheck(cudaStreamSynchronize(s), "cudaStreamSynchronize");  // hostTables is on the stack
         prepareUs = NowUs() - t0;

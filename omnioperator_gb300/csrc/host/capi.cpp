@@ -974,7 +974,7 @@ int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const 
         SetError("VARCHAR/CHAR columns are not supported by the allocation-free entry point");
         return OMG_ERR_UNSUPPORTED;
     }
-    if (std::any_of(ap.inputMasks.begin(), ap.inputMasks.end(), [](int32_t m) { return m >= 0; })) {
+    if (std::any_of(ap.inputMasks.begin(), ap.inputMasks.end(), [](int32_t m) { return m != -1; })) {
         // A mask turns into a per-call NULL bitmap of the masked inputs (a device allocation).
         SetError("aggregation mask columns are not supported by the allocation-free entry point");
         return OMG_ERR_UNSUPPORTED;

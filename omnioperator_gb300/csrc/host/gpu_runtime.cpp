@@ -60,10 +60,12 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
             if (hasNull) {
                 anyNulls_[i] = true;
             }
-            const int32_t m = inputMasks != nullptr && i < inputMasks->size() ? (*inputMasks)[i] : -1;
-            if (m < 0) {
+            const int32_t entry = inputMasks != nullptr && i < inputMasks->size() ? (*inputMasks)[i] : -1;
+            if (entry == -1) {
                 continue;
             }
+            const bool invert = entry < -1;
+            const int32_t m = invert ? -2 - entry : entry;
             if (m >= b->GetVectorCount()) {
                 throw OmniException("OPERATOR_RUNTIME_ERROR",
                     "input batch has " + std::to_string(b->GetVectorCount()) + " vectors, mask column " +
@@ -80,6 +82,7 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
             job.maskNulls = mv->RawNulls() != nullptr && mv->HasNull() ? mv->RawNulls() : nullptr;
             job.out = nullptr;
             job.rows = d.rows;
+            job.invert = invert ? 1 : 0;
             maskJobs_.push_back(job);
             maskSlots_.push_back(MaskSlot{bi, static_cast<int32_t>(i), maskWords_});
             maskWords_ += (d.rows + 31) / 32;

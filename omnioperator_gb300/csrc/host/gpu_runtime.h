@@ -153,9 +153,11 @@ private:
 
 // Descriptors of a list of batches for one launch.  Kernel input i of batch b is column
 // inputCols[i] of the batch.  With inputMasks (one entry per input, -1 = none), an input whose
-// entry is column m reads its values as usual but its NULL bitmap is computed on the device at
-// Upload: the value column's NULLs plus every row whose BOOLEAN column m is NULL or FALSE
-// (aggregation mask columns).
+// entry is column m >= 0 reads its values as usual but its NULL bitmap is computed on the device
+// at Upload: the value column's NULLs plus every row whose BOOLEAN column m is NULL or FALSE
+// (aggregation mask columns).  An entry InvertedMask(m) drops the rows whose column m is TRUE
+// instead (the isEmpty column of partial decimal sums), without reading m's NULLs.
+constexpr int32_t InvertedMask(int32_t col) { return -2 - col; }
 class BatchTable {
 public:
     void Build(const std::vector<omniruntime::vec::VectorBatch *> &batches, const std::vector<int32_t> &inputCols,

@@ -280,10 +280,14 @@ OmniStatus HashAggregationOperatorFactory::Init()
         const bool partial = a < outputPartials_.size() ? static_cast<bool>(outputPartials_[a]) : false;
         const auto &outTypes = aggOutputTypes_[a];
         const bool avgPair = fn == OMNI_AGGREGATION_TYPE_AVG && partial;
-        if (outTypes.GetSize() != (avgPair ? 2 : 1)) {
+        const DataTypeId in0 = aggInputTypes_[a].GetSize() > 0 ? aggInputTypes_[a].GetType(0)->GetId() : OMNI_NONE;
+        const bool decSum = fn == OMNI_AGGREGATION_TYPE_SUM && (in0 == OMNI_DECIMAL64 || in0 == OMNI_DECIMAL128);
+        const bool decPair = decSum && partial;
+        if (outTypes.GetSize() != (avgPair || decPair ? 2 : 1)) {
             throw OmniException("INVALID_ARGUMENT",
                 avgPair ? "a partial AVG has two output types (double sum, long count)"
-                        : "this aggregator has one output type", -1);
+                        : (decPair ? "a partial decimal SUM has two output types (decimal sum, boolean isEmpty)"
+                                   : "this aggregator has one output type"), -1);
         }
         const DataTypePtr &outT = outTypes.GetType(0);
         OutSpec o{};
@@ -353,6 +357,64 @@ OmniStatus HashAggregationOperatorFactory::Init()
             }
             continue;
         }
+        if (decSum && (!raw || partial)) {
+            // Spark decimal SUM across stages (sum_spark_decimal_aggregator.h:74-412): a partial
+            // emits (sum, isEmpty) -- the sum NULL when it overflowed, 0 for an empty group; a
+            // merging stage skips rows whose isEmpty is TRUE, turns a NULL partial sum into a
+            // sticky overflow and adds the other partial sums with the same checked, sticky
+            // addition (AddDecimalUseRowIndex, :14-66), which the exact sum plus the ordered
+            // replay reproduce.
+            if (!spark) {
+                throw OmniException("UNSUPPORTED_ERROR",
+                    "two-stage decimal SUM under the container-vector policy is not supported", -2);
+            }
+            const DataTypePtr &inT = aggInputTypes_[a].GetType(0);
+            const int inW = inT->ByteWidth();
+            const int inKind = in0 == OMNI_DECIMAL128 ? omg::IN_DEC128 : omg::IN_INT;
+            const int accKind = in0 == OMNI_DECIMAL128 ? omg::ACC_WSUM3 : omg::ACC_WSUM2;
+            const int diff = outT->GetScale() - inT->GetScale();
+            if (diff < 0 || diff > 38) {
+                throw OmniException("UNSUPPORTED_ERROR", "decimal SUM output scale below input scale", -2);
+            }
+            OutSpec s1{};
+            s1.kind = omg::OUT_SUM_EXACT;
+            s1.boundKind = outT->GetId() == OMNI_DECIMAL128 ? 1 : 0;
+            s1.rescalePow = static_cast<int16_t>(diff);
+            s1.pad = static_cast<int16_t>(exactIndex++);
+            s1.partial = partial ? 1 : 0;
+            if (raw) {
+                if (aggCols_[a].size() != 1 || aggInputTypes_[a].GetSize() != 1) {
+                    throw OmniException("INVALID_ARGUMENT", "a partial decimal SUM reads one decimal column", -1);
+                }
+                const int input = inputFor(aggCols_[a][0], inW, mask);
+                s1.countAcc = static_cast<int16_t>(accFor(omg::ACC_NULLS, input, omg::IN_NONE, 0, 0));
+                s1.src = static_cast<int16_t>(accFor(accKind, input, inKind, inW, 0));
+            } else {
+                if (aggCols_[a].size() != 2 || aggInputTypes_[a].GetSize() != 2 ||
+                    aggInputTypes_[a].GetType(1)->GetId() != OMNI_BOOLEAN) {
+                    throw OmniException("INVALID_ARGUMENT",
+                        "a merging decimal SUM reads (decimal sum, boolean isEmpty) partial columns", -1);
+                }
+                if (mask >= 0) {
+                    throw OmniException("UNSUPPORTED_ERROR", "a mask column on a merging decimal SUM is not supported",
+                        -2);
+                }
+                const int sums = inputFor(aggCols_[a][0], inW);
+                const int kept = inputFor(aggCols_[a][0], inW, omg::InvertedMask(static_cast<int32_t>(aggCols_[a][1])));
+                s1.flagAcc = static_cast<int16_t>(accFor(omg::ACC_NULLS, sums, omg::IN_NONE, 0, 0));
+                s1.countAcc = static_cast<int16_t>(accFor(omg::ACC_NULLS, kept, omg::IN_NONE, 0, 0));
+                s1.src = static_cast<int16_t>(accFor(accKind, kept, inKind, inW, 0));
+            }
+            pushOut(s1, outT);
+            if (partial) {
+                OutSpec s2{};
+                s2.kind = omg::OUT_IS_EMPTY;
+                s2.countAcc = s1.countAcc;
+                s2.flagAcc = s1.flagAcc;
+                pushOut(s2, outTypes.GetType(1));
+            }
+            continue;
+        }
         if (aggCols_[a].size() != 1 || aggInputTypes_[a].GetSize() != 1) {
             throw OmniException("UNSUPPORTED_ERROR", "aggregator must read exactly one column", -2);
         }
@@ -373,9 +435,9 @@ OmniStatus HashAggregationOperatorFactory::Init()
                 o.src = 0;
                 break;
             case OMNI_AGGREGATION_TYPE_SUM: {
-                if ((!raw || partial) && (inId == OMNI_DECIMAL64 || inId == OMNI_DECIMAL128 || (!spark && inW == 8))) {
+                if ((!raw || partial) && !spark && inW == 8 && isInt) {
                     throw OmniException("UNSUPPORTED_ERROR",
-                        "two-stage SUM with sticky overflow (decimal, generic-policy int64) is not supported", -2);
+                        "two-stage int64 SUM under the container-vector policy is not supported", -2);
                 }
                 if (isDouble) {
                     o.kind = omg::OUT_SUM_DOUBLE;
@@ -1481,7 +1543,7 @@ void HashAggregationOperator::Extract()
         cols[o].width = os.outWidth;
         cols[o].values = omg::Buffer::NewDevice(static_cast<size_t>(nGroups) * os.outWidth + 16, s, false);
         cols[o].nulls = omg::Buffer::NewDevice(omg::NullBitmapBytes(static_cast<int64_t>(nGroups)), s, true);
-        cols[o].hasNull = os.kind != omg::OUT_COUNT;
+        cols[o].hasNull = os.kind != omg::OUT_COUNT && os.kind != omg::OUT_IS_EMPTY;
     }
     omg::AggExtract e;
     std::memset(&e, 0, sizeof(e));

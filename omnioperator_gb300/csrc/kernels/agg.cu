@@ -1163,6 +1163,18 @@ __device__ __forceinline__ bool ExceedsBound(const uint64_t *m, bool negative, i
     return v > Dec38Max();
 }
 
+// A zero value at output row `pos` (a 16-byte column holds two words per row).
+__device__ __forceinline__ void StoreZero(const OutSpec &os, uint64_t pos)
+{
+    if (os.outWidth == 16) {
+        uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
+        dst[0] = 0;
+        dst[1] = 0;
+    } else {
+        StoreWidth(os.values, pos, os.outWidth, 0);
+    }
+}
+
 // Output row `pos` of the group in slot s (occupied) of table t: keys, counts and aggregates.
 __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &t, uint64_t s, const uint64_t *slot,
     uint64_t pos)
@@ -1206,6 +1218,15 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
             StoreWidth(os.values, pos, 8, st[e.accs[os.src].word]);
             continue;
         }
+        // A merging stage's decimal SUM saw a NULL partial sum: that partial overflowed, and the
+        // overflow is sticky whatever the row order (sum_spark_decimal_aggregator.h, final stage).
+        const bool flagged = os.flagAcc > 0 && st[e.accs[os.flagAcc].word] != 0;
+        if (os.kind == OUT_IS_EMPTY) {
+            const int64_t n = static_cast<int64_t>(st[e.accs[0].word]) -
+                static_cast<int64_t>(st[e.accs[os.countAcc].word]);
+            StoreWidth(os.values, pos, 1, (n == 0 && !flagged) ? 1u : 0u);
+            continue;
+        }
         if (os.kind == OUT_AVG_MERGE || os.kind == OUT_AVG_PARTIAL_SUM) {
             const uint64_t *w = st + e.accs[os.src].word;
             double sum = __dadd_rn(__longlong_as_double(static_cast<long long>(w[0])),
@@ -1237,12 +1258,21 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
             StoreWidth(os.values, pos, 8, static_cast<uint64_t>(cnt));
             continue;
         }
+        if (flagged || (cnt == 0 && os.partial != 0)) {
+            // An overflowed merge: NULL (an error unless overflow is NULL or the output is a
+            // partial).  An empty partial sum: 0, not NULL.
+            if (flagged) {
+                SetOutNull(os.nulls, pos);
+                if (!e.overflowAsNull && os.partial == 0) {
+                    SetError(e.error, 5);
+                }
+            }
+            StoreZero(os, pos);
+            continue;
+        }
         if (cnt == 0) {
             SetOutNull(os.nulls, pos);
-            StoreWidth(os.values, pos, os.outWidth == 16 ? 8 : os.outWidth, 0);
-            if (os.outWidth == 16) {
-                static_cast<uint64_t *>(os.values)[2 * pos + 1] = 0;
-            }
+            StoreZero(os, pos);
             continue;
         }
         const AccSpec &acc = e.accs[os.src];
@@ -1305,7 +1335,7 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
                 }
                 if (overflow) {
                     SetOutNull(os.nulls, pos);
-                    if (!e.overflowAsNull) {
+                    if (!e.overflowAsNull && os.partial == 0) {
                         SetError(e.error, 5);
                     }
                     mag = 0;

@@ -36,6 +36,8 @@ struct MaskJob {
     const uint8_t *maskNulls;   // its NULL bitmap (nullptr: none)
     uint32_t *out;              // ceil(rows / 32) words
     int64_t rows;
+    int32_t invert;             // 1: drop the rows whose mask byte is non-zero (NULL flag not read)
+    int32_t pad;
 };
 
 struct TileDesc {
@@ -233,6 +235,8 @@ enum OutKind : int16_t {
                                // boundKind == 1)
     OUT_AVG_MERGE = 12,        // final AVG: sum (acc src, DSUM) / count (acc countAcc, ISUM), NULL if 0
     OUT_STR_ID = 13,           // VARCHAR MIN/MAX: the dictionary id (int32) of acc src, NULL if none
+    OUT_IS_EMPTY = 14,         // decimal SUM partial: BOOLEAN, 1 when no value reached the group's sum
+                               // (count as for OUT_COUNT, and no partial sum overflowed: flagAcc)
 };
 
 struct OutSpec {
@@ -243,7 +247,12 @@ struct OutSpec {
     int16_t outType;    // DataTypeId of the output
     int16_t boundKind;  // OUT_SUM_EXACT: 0 = int64 range, 1 = decimal(38) range
     int16_t rescalePow; // OUT_SUM_EXACT: multiply the sum by 10^rescalePow
-    int16_t pad;
+    int16_t pad;        // OUT_SUM_EXACT: index of the exact sum (bit of the ordered-replay flags)
+    int16_t flagAcc;    // OUT_SUM_EXACT / OUT_IS_EMPTY of a merging stage: NULLS accumulator of the
+                        // partial sums; a NULL partial sum is an overflow of that partial (0: none)
+    int16_t partial;    // OUT_SUM_EXACT: 1 = partial output (overflow -> NULL without an error,
+                        // empty -> 0, not NULL)
+    int16_t pad2[2];
     void *values;       // device output column
     uint8_t *nulls;     // device output null bitmap (zeroed by the host)
 };

@@ -69,7 +69,8 @@ __global__ void MaskNullsKernel(const MaskJob *jobs, int32_t nJobs)
             const int64_t row = (w << 5) + lane;
             bool skip = false;
             if (row < job.rows) {
-                skip = __ldg(job.maskValues + row) == 0 || NullRO(job.maskNulls, row) || NullRO(job.valueNulls, row);
+                const uint8_t m = __ldg(job.maskValues + row);
+                skip = (job.invert ? m != 0 : (m == 0 || NullRO(job.maskNulls, row))) || NullRO(job.valueNulls, row);
             }
             const unsigned bits = __ballot_sync(0xffffffffu, skip);
             if (lane == 0) {

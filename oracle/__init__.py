@@ -407,3 +407,51 @@ def hashagg_mt(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=Fals
     return ([k[:g] for k in okeys], [m[:g].astype(bool) for m in oknulls], vals,
             [m[:g].astype(bool) for m in ovnulls], [None if e is None else e[:g] for e in exact],
             [None if a is None else a[:g] for a in absum])
+
+
+# ------------------------------------------------------------------ two-stage decimal SUM
+DEC38_MAX = 10**38 - 1
+
+
+def decimal_sum_merge(keys, sums, sum_nulls, empties, partial=False, rescale=0):
+    """The merging stage of the Spark decimal SUM over partial rows in arrival order
+    (AddDecimalUseRowIndex, sum_spark_decimal_aggregator.h:14-66): per group the state starts
+    EMPTY; a row with a NULL partial sum makes it OVERFLOWED; a row whose isEmpty is true is
+    skipped; any other row is added with the checked addition (a result beyond +-(10^38 - 1)
+    overflows); an OVERFLOWED state takes no further rows.  Output (ExtractValues, :165-241):
+    final -- NULL for an overflowed or empty group ("overflow" marks the former), else the sum
+    times 10^rescale (NULL-or-error if that overflows); partial -- (sum or NULL, isEmpty), the sum
+    0 for an empty group.  Pure Python, for small cases.  Returns {key: (value or None, flag)}
+    where flag is "overflow"/"empty"/None (final) or the isEmpty boolean (partial)."""
+    state = {}
+    for k, s, n, e in zip(keys, sums, sum_nulls, empties):
+        st = state.setdefault(k, ["empty", 0])
+        if st[0] == "overflow":
+            continue
+        if n:
+            st[0] = "overflow"
+            continue
+        if e:
+            continue
+        v = st[1] + int(s)
+        if abs(v) > DEC38_MAX:
+            st[0] = "overflow"
+        else:
+            st[0], st[1] = "normal", v
+    out = {}
+    for k, (kind, v) in state.items():
+        if partial:
+            if kind == "overflow":
+                out[k] = (None, False)
+            elif kind == "empty":
+                out[k] = (0, True)
+            else:
+                r = v * 10**rescale
+                out[k] = (None if abs(r) > DEC38_MAX else r, False)
+        else:
+            if kind != "normal":
+                out[k] = (None, kind)
+            else:
+                r = v * 10**rescale
+                out[k] = (None, "overflow") if abs(r) > DEC38_MAX else (r, None)
+    return out

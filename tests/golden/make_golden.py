@@ -228,8 +228,51 @@ JOIN_TYPED = {
 }
 
 
+# aggregation_test.cpp:632-1190 (verify_group_colum_array_map_*): two batches of 21 rows built by
+# BuildAggInput (:254-271): group key j % 3 (BuildHashInput, :60-175), five LONG aggregate inputs
+# all 1 (BuildAggregateInput, :180-252); SUM(c1), AVG(c2), COUNT(c3), MIN(c4), MAX(c5).  Both
+# batches: key NULL at rows 0 and 11, c2 NULL at rows 0-4, c3/c4/c5 NULL at rows 0 and 1; the
+# second batch also has key NULL at row 20.  "resize" sets the second batch's key at row 2 to
+# 1000; "switch" sets it at rows 2 and 5 to the key type's max and min (the reference builds that
+# key column as a dictionary vector over those values with identity ids; restated flat here).  The
+# reference runs every case for SHORT, INT, DATE32, LONG, TIMESTAMP and DECIMAL64 keys; each
+# *_without_agg variant has the same keys and no aggregates.  Expected rows: (key, SUM, AVG,
+# COUNT, MIN, MAX), key None = NULL, AVG None = NULL.
+KEY_LIMITS = {"SHORT": (-2**15, 2**15 - 1), "INT": (-2**31, 2**31 - 1), "DATE32": (-2**31, 2**31 - 1),
+              "LONG": (-2**63, 2**63 - 1), "TIMESTAMP": (-2**63, 2**63 - 1), "DECIMAL64": (-2**63, 2**63 - 1)}
+
+
+def _array_map_batch(second, edits):
+    keys = [j % 3 for j in range(21)]
+    for row, v in edits.items():
+        keys[row] = v
+    key_nulls = [0, 11] + ([20] if second else [])
+    agg_nulls = [[], [0, 1, 2, 3, 4], [0, 1], [0, 1], [0, 1]]
+    return dict(keys=keys, key_nulls=key_nulls, agg_nulls=agg_nulls)
+
+
+def _array_map_cases():
+    out = {}
+    for key_type, (lo, hi) in KEY_LIMITS.items():
+        regular = [[None, 5, 1.0, 3, 1, 1], [0, 12, 1.0, 12, 1, 1], [1, 14, 1.0, 12, 1, 1], [2, 11, 1.0, 11, 1, 1]]
+        resize = [[None, 5, 1.0, 3, 1, 1], [0, 12, 1.0, 12, 1, 1], [1, 14, 1.0, 12, 1, 1], [2, 10, 1.0, 10, 1, 1],
+                  [1000, 1, None, 1, 1, 1]]
+        switch = [[0, 12, 1.0, 12, 1, 1], [lo, 1, 1.0, 1, 1, 1], [1, 14, 1.0, 12, 1, 1], [hi, 1, None, 1, 1, 1],
+                  [2, 9, 1.0, 9, 1, 1], [None, 5, 1.0, 3, 1, 1]]
+        for name, edits, rows, src in (("regular", {}, regular, "632-718"), ("resize", {2: 1000}, resize, "804-890"),
+                                       ("switch", {2: hi, 5: lo}, switch, "1000-1093")):
+            batches = [_array_map_batch(False, {}), _array_map_batch(True, edits)]
+            out[f"{name}_{key_type}"] = dict(source=f"core/test/operator/aggregation_test.cpp:{src}",
+                                             key_type=key_type, batches=batches, expected=rows)
+            out[f"{name}_without_agg_{key_type}"] = dict(
+                source=f"core/test/operator/aggregation_test.cpp:{src} (without_agg variant)", key_type=key_type,
+                batches=batches, expected=[[r[0]] for r in rows], no_aggs=True)
+    return out
+
+
 def main():
-    (HERE / "agg_kats.json").write_text(json.dumps({"single": AGG, "multi": AGG_MULTI}, indent=1) + "\n")
+    (HERE / "agg_kats.json").write_text(json.dumps({"single": AGG, "multi": AGG_MULTI,
+                                                    "array_map": _array_map_cases()}, indent=1) + "\n")
     (HERE / "join_kats.json").write_text(json.dumps({"inner_join_one_build_op": _join_one_build_op(),
                                                     "array_table_short": _join_array_table_short()}, indent=1)
                                          + "\n")

@@ -66,11 +66,19 @@ def test_factory_validation_matches_reference_rules():
     with pytest.raises(omg.OmgError) as e:
         omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [9])
     assert e.value.status == -2
-    # two-stage decimal SUM is not built (plain int/double SUM, COUNT, MIN, MAX, AVG are)
+    # a partial decimal SUM emits (decimal sum, boolean isEmpty): two output types
     d64, d128 = omg.Decimal64Type(18, 2), omg.Decimal128Type(38, 2)
     with pytest.raises(omg.OmgError) as e:
         omg.HashAggregationOperatorFactory([0], [L], [[1]], [[d64]], [[d128]], [0], output_partials=[True])
-    assert e.value.status == -2
+    assert e.value.status == -1
+    # under the container-vector policy the partial int64 SUM is a container: not built
+    omg.set_policy(omg.POLICY_GENERIC)
+    try:
+        with pytest.raises(omg.OmgError) as e:
+            omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [0], output_partials=[True])
+        assert e.value.status == -2
+    finally:
+        omg.set_policy(omg.POLICY_SPARK)
     # a partial AVG emits (double sum, long count): two output types
     with pytest.raises(omg.OmgError) as e:
         omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[omg.DoubleType()]], [omg.OMNI_AGGREGATION_TYPE_AVG],
@@ -241,6 +249,23 @@ def test_mask_columns_are_checked_on_the_host():
     rc = omg.lib().omg_hashagg_run_noalloc(f.handle, None, None, 0, 0, None, None, 0, 16, C.byref(n), None)
     assert rc == -2
     f.close()
+
+
+def test_two_stage_decimal_sum_plans_are_checked_on_the_host():
+    """Partial decimal SUM: (decimal sum, boolean isEmpty) outputs; a merging stage reads the
+    pair; the wrong shapes are refused while the factory compiles its plan."""
+    L, B, D128 = omg.LongType(), omg.BooleanType(), omg.Decimal128Type(38, 2)
+    SUM = omg.OMNI_AGGREGATION_TYPE_SUM
+    for cols, ins, outs, raw, partial in (([[1]], [[D128]], [[D128, B]], True, True),
+                                          ([[1, 2]], [[D128, B]], [[D128]], False, False),
+                                          ([[1, 2]], [[D128, B]], [[D128, B]], False, True)):
+        omg.HashAggregationOperatorFactory([0], [L], cols, ins, outs, [SUM], input_raws=[raw],
+                                           output_partials=[partial]).close()
+    for cols, ins, outs in (([[1]], [[D128]], [[D128]]), ([[1, 2]], [[D128, L]], [[D128]])):
+        with pytest.raises(omg.OmgError) as e:
+            omg.HashAggregationOperatorFactory([0], [L], cols, ins, outs, [SUM], input_raws=[len(cols[0]) == 1],
+                                               output_partials=[len(cols[0]) == 1])
+        assert e.value.status == -1
 
 
 def test_spill_settings_are_checked_on_the_host():

@@ -369,3 +369,22 @@ def test_partitioned_composite_key_decimal_count_all_avg(gpu):
                           dict(func=oracle.F_AVG, col=v, in_type=oracle.T_DOUBLE, out_type=oracle.T_DOUBLE, nulls=vm)])
     ex_a = exact_by_key([k1, k2], [km1, None], v, ~vm, divide_by_count=True)
     assert_agg_equal(cols, ora, 2, double_aggs=(2,), exact={2: ex_a})
+
+
+@pytest.mark.parametrize("strategy", [omg.AGG_STRATEGY_SMEM, omg.AGG_STRATEGY_GLOBAL])
+def test_decimal128_sums_next_to_empty_groups(gpu, strategy):
+    """Many groups whose decimal inputs are all NULL (a NULL 16-byte result written next to
+    non-NULL ones, in every output position parity): each group's two result words stay its
+    own.  Negative sums set the high word, positive ones leave it zero."""
+    rng = np.random.default_rng(77)
+    n, groups = 400_000, 150_000
+    key = rng.integers(0, groups, n).astype(np.int64)
+    dec = rng.integers(-10**9, 10**9, n).astype(np.int64)
+    nulls = (key % 2 == 0) | (rng.random(n) < 0.02)
+    D64, D128 = omg.Decimal64Type(18, 2), omg.Decimal128Type(38, 2)
+    cols, _ = run_agg([0], [L], [[1]], [[D64]], [[D128]], [SUM], [key, dec], [L, D64], nulls=[None, nulls],
+                      strategy=strategy, batch_sizes=(65536,))
+    ora = oracle.hashagg([key], [oracle.T_LONG], [None],
+                         [dict(func=oracle.F_SUM, col=dec, in_type=oracle.T_DEC64, out_type=oracle.T_DEC128,
+                               nulls=nulls)])
+    assert_agg_equal(cols, ora, 1)

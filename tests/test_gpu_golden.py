@@ -78,3 +78,42 @@ def test_verify_null_correctness_on_gpu(gpu):
     row = [int(cols[0][0][0])] + [float(c[0][0]) if t == "DOUBLE" else int(c[0][0])
                                   for c, t in zip(cols[1:], k["out_types"])]
     assert row == k["expected"][0]
+
+
+ARRAY_MAP = AGG["array_map"]
+KEY_TYPES = {"SHORT": (np.int16, omg.ShortType()), "INT": (np.int32, omg.IntType()),
+             "DATE32": (np.int32, omg.DataType(omg.OMNI_DATE32)), "LONG": (np.int64, omg.LongType()),
+             "TIMESTAMP": (np.int64, omg.DataType(omg.OMNI_TIMESTAMP)), "DECIMAL64": (np.int64, omg.Decimal64Type(18, 0))}
+
+
+@pytest.mark.parametrize("name", sorted(ARRAY_MAP))
+def test_array_map_kats_on_gpu(gpu, name):
+    """The reference's ArrayMap tests (aggregation_test.cpp:632-1190): NULL keys, NULL values,
+    a key far outside the first batch's range and the key type's min / max, two batches."""
+    k = ARRAY_MAP[name]
+    dt, kt = KEY_TYPES[k["key_type"]]
+    L, D = omg.LongType(), omg.DoubleType()
+    keys, knull, anulls = [], [], [[] for _ in range(5)]
+    for b in k["batches"]:
+        keys += b["keys"]
+        knull += [r in b["key_nulls"] for r in range(21)]
+        for c in range(5):
+            anulls[c] += [r in b["agg_nulls"][c] for r in range(21)]
+    key = np.array(keys, dtype=dt)
+    ones = np.ones(len(keys), dtype=np.int64)
+    no_aggs = k.get("no_aggs", False)
+    funcs = [] if no_aggs else [FUNCS[f] for f in ("SUM", "AVG", "COUNT_COLUMN", "MIN", "MAX")]
+    n_agg = len(funcs)
+    cols, _ = run_agg([0], [kt], [[1 + j] for j in range(n_agg)], [[L]] * n_agg,
+                      [[D] if j == 1 else [L] for j in range(n_agg)], funcs, [key] + [ones] * n_agg,
+                      [kt] + [L] * n_agg, nulls=[np.array(knull)] + [np.array(m) for m in anulls[:n_agg]],
+                      batch_sizes=(21,))
+    rows = []
+    for i in range(len(cols[0][0])):
+        r = [None if cols[0][1][i] else int(cols[0][0][i])]
+        for j in range(n_agg):
+            v, m = cols[1 + j]
+            r.append(None if m[i] else (float(v[i]) if j == 1 else int(v[i])))
+        rows.append(r)
+    order = lambda r: (r[0] is None, r[0] if r[0] is not None else 0)  # noqa: E731
+    assert sorted(rows, key=order) == sorted(k["expected"], key=order)

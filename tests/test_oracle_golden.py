@@ -199,3 +199,47 @@ def test_filtered_join_restatement_reduces_to_the_plain_join():
             assert len(none[0]) == 0
         if kind == "existence":
             assert not none[1].any()
+
+
+ARRAY_MAP = AGG["array_map"]
+KEY_NP = {"SHORT": (np.int16, oracle.T_SHORT), "INT": (np.int32, oracle.T_INT), "DATE32": (np.int32, oracle.T_DATE32),
+          "LONG": (np.int64, oracle.T_LONG), "TIMESTAMP": (np.int64, oracle.T_LONG),
+          "DECIMAL64": (np.int64, oracle.T_DEC64)}
+
+
+def array_map_inputs(k):
+    """Concatenated key column, key NULLs, five aggregate columns (ones) and their NULLs."""
+    dt = KEY_NP[k["key_type"]][0]
+    keys, knull, anulls = [], [], [[] for _ in range(5)]
+    for b in k["batches"]:
+        keys += b["keys"]
+        knull += [r in b["key_nulls"] for r in range(21)]
+        for c in range(5):
+            anulls[c] += [r in b["agg_nulls"][c] for r in range(21)]
+    return (np.array(keys, dtype=dt), np.array(knull, dtype=bool), np.ones(len(keys), dtype=np.int64),
+            [np.array(m, dtype=bool) for m in anulls])
+
+
+def array_map_rows(keys, knulls, vals, vnulls, n_aggs):
+    rows = []
+    for i in range(len(keys)):
+        r = [None if knulls[i] else int(keys[i])]
+        for j in range(n_aggs):
+            v = vals[j][i]
+            r.append(None if vnulls[j][i] else (float(v) if j == 1 else int(v)))
+        rows.append(r)
+    return sorted(rows, key=lambda r: (r[0] is None, r[0] if r[0] is not None else 0))
+
+
+@pytest.mark.parametrize("name", sorted(ARRAY_MAP))
+def test_oracle_array_map_kats(name):
+    k = ARRAY_MAP[name]
+    key, knull, ones, anulls = array_map_inputs(k)
+    funcs = [] if k.get("no_aggs") else ["SUM", "AVG", "COUNT_COLUMN", "MIN", "MAX"]
+    outs = [oracle.T_DOUBLE if f == "AVG" else oracle.T_LONG for f in funcs]
+    aggs = [dict(func=FUNCS[f], col=ones, in_type=oracle.T_LONG, out_type=o, nulls=anulls[j])
+            for j, (f, o) in enumerate(zip(funcs, outs))]
+    keys, knulls, vals, vnulls = oracle.hashagg([key], [KEY_NP[k["key_type"]][1]], [knull], aggs)
+    got = array_map_rows(keys[0], knulls[0], vals, vnulls, len(funcs))
+    want = sorted(k["expected"], key=lambda r: (r[0] is None, r[0] if r[0] is not None else 0))
+    assert got == want
