@@ -131,6 +131,12 @@ int32_t omg_debug_set_wait_budget(int64_t ticks)
     return OMG_OK;
 }
 
+int32_t omg_debug_set_staged_probe(int32_t on)
+{
+    omg::SetStagedProbe(on != 0);
+    return OMG_OK;
+}
+
 int32_t omg_debug_set_agg_flush_rows(int64_t rows)
 {
     omg::SetAggFlushRows(rows < 0 ? 0 : rows);

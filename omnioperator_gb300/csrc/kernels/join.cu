@@ -11,6 +11,7 @@
 // (round, warp) so that the tile's matches get one contiguous output range from a single
 // atomicAdd, and writes probe columns plus gathered build columns in probe-row order within the
 // tile.
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -1438,6 +1439,229 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
     }
 }
 
+// ------------------------------------------------------------------ staged inner probe
+// Inner joins on an ARRAY table with its occupancy bitmap in shared memory and a packed slot
+// payload, outputs being the 8-byte probe key and payload fields.  The CTA's warps form groups
+// of kGroupWarps; a group probes a group tile of kGroupRows rows at a time: its warps resolve
+// their 128-row segments as ProbeBitsKernel does, the group prefix-sums the warps' match counts,
+// reserves the group tile's output range with one atomic, stages the compacted (key, payload)
+// rows in shared memory and writes every output column of the group tile as one contiguous run
+// with 16-byte stores.  Each output column of a group tile is then written as whole lines (no
+// per-warp partial lines, a quarter of the store instructions), which matters most when the
+// output is pinned host memory written over the CPU-GPU link.  Groups synchronise on their own
+// named barriers, so one group's stores overlap the other groups' loads.
+constexpr int kGroupWarps = 8;
+constexpr int kGroupThreads = kGroupWarps * 32;
+constexpr int kGroupsPerCta = kBitsThreads / kGroupThreads;
+constexpr int kGroupRows = kGroupWarps * kBitsSegRows;
+constexpr int kGroupTilesPerTile = kTileRows / kGroupRows;
+constexpr uint32_t kGroupStageBytes = static_cast<uint32_t>(kGroupRows) * 16u + 64u;
+constexpr uint32_t kGroupMaxSmem = 227u * 1024u;
+std::atomic<bool> g_stagedProbe{true};
+
+__device__ __forceinline__ void GroupBarrier(int group)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(group + 1), "r"(kGroupThreads) : "memory");
+}
+
+// Rows [0, n) of one staged output column to `col` rows [at0, at0 + n): rows up to the first
+// 16-byte boundary and after the last one singly, the rest 16 bytes per store.
+template <uint32_t kLayout, int kO>
+__device__ __forceinline__ void WriteStagedColumn(void *col, int width, bool isKey, int shift,
+    const long long *sKey, const unsigned long long *sPay, uint64_t at0, uint32_t n, uint32_t t)
+{
+    constexpr int code = static_cast<int>((kLayout >> (3 * kO)) & 7u);
+    const int w = code == 0 ? width : (1 << (code - 1));
+    auto value = [&](uint32_t r) -> uint64_t {
+        return isKey ? static_cast<uint64_t>(sKey[r]) : (sPay[r] >> shift);
+    };
+    if (w != 8 && w != 4) {
+        for (uint32_t r = t; r < n; r += kGroupThreads) {
+            StoreOut<kLayout, kO>(col, at0 + r, width, static_cast<int64_t>(value(r)));
+        }
+        return;
+    }
+    uint8_t *dst = static_cast<uint8_t *>(col) + at0 * static_cast<uint64_t>(w);
+    const uint32_t mis = static_cast<uint32_t>(reinterpret_cast<uintptr_t>(dst) & 15u);
+    uint32_t head = mis == 0 ? 0u : (16u - mis) / static_cast<uint32_t>(w);
+    head = head < n ? head : n;
+    const uint32_t per = 16u / static_cast<uint32_t>(w);
+    const uint32_t nvec = (n - head) / per;
+    const uint32_t tail0 = head + nvec * per;
+    if (t < head) {
+        StoreOut<kLayout, kO>(col, at0 + t, width, static_cast<int64_t>(value(t)));
+    }
+    if (t < n - tail0) {
+        StoreOut<kLayout, kO>(col, at0 + tail0 + t, width, static_cast<int64_t>(value(tail0 + t)));
+    }
+    uint4 *vdst = reinterpret_cast<uint4 *>(dst + static_cast<uint64_t>(head) * w);
+    for (uint32_t v = t; v < nvec; v += kGroupThreads) {
+        const uint32_t r = head + v * per;
+        uint4 q;
+        if (w == 8) {
+            const uint64_t a = value(r);
+            const uint64_t b = value(r + 1);
+            q = make_uint4(static_cast<uint32_t>(a), static_cast<uint32_t>(a >> 32), static_cast<uint32_t>(b),
+                static_cast<uint32_t>(b >> 32));
+        } else {
+            q = make_uint4(static_cast<uint32_t>(value(r)), static_cast<uint32_t>(value(r + 1)),
+                static_cast<uint32_t>(value(r + 2)), static_cast<uint32_t>(value(r + 3)));
+        }
+        vdst[v] = q;
+    }
+}
+
+template <int kNumOut, uint32_t kLayout, bool kSingle>
+__global__ void __launch_bounds__(kBitsThreads, 1) ProbeGroupKernel(const __grid_constant__ ProbeLaunch p,
+    uint32_t bitsVecs)
+{
+    extern __shared__ uint4 sGroupSmem[];
+    {
+        const uint4 *g = reinterpret_cast<const uint4 *>(p.table.slotBits);
+        for (uint32_t i = threadIdx.x; i < bitsVecs; i += kBitsThreads) {
+            sGroupSmem[i] = __ldg(g + i);
+        }
+    }
+    __syncthreads();
+    const uint32_t *sBits = reinterpret_cast<const uint32_t *>(sGroupSmem);
+    const int group = static_cast<int>(threadIdx.x) / kGroupThreads;
+    const uint32_t gt = threadIdx.x % kGroupThreads;  // thread within the group
+    const int gw = static_cast<int>(gt >> 5);         // warp within the group
+    const int lane = threadIdx.x & 31;
+    const unsigned int lanesBelow = (1u << lane) - 1u;
+    uint8_t *stage = reinterpret_cast<uint8_t *>(sGroupSmem + bitsVecs) + static_cast<size_t>(group) * kGroupStageBytes;
+    long long *sKey = reinterpret_cast<long long *>(stage);
+    unsigned long long *sPay = reinterpret_cast<unsigned long long *>(stage + kGroupRows * 8);
+    unsigned int *sOff = reinterpret_cast<unsigned int *>(stage + kGroupRows * 16);  // [kGroupWarps]
+    unsigned long long *sBase = reinterpret_cast<unsigned long long *>(stage + kGroupRows * 16 + 32);
+    unsigned int *sTotal = reinterpret_cast<unsigned int *>(stage + kGroupRows * 16 + 40);
+
+    const unsigned long long *payloadTab = reinterpret_cast<const unsigned long long *>(p.table.slotPayload);
+    const uint64_t minKey = static_cast<uint64_t>(p.table.minKey);
+    const uint64_t range = p.table.range;
+    void *vals[kNumOut];
+    int width[kNumOut];
+    int shift[kNumOut];
+    bool isKey[kNumOut];
+#pragma unroll
+    for (int o = 0; o < kNumOut; ++o) {
+        vals[o] = p.out[o].values;
+        width[o] = p.out[o].width;
+        shift[o] = p.out[o].shift;
+        isKey[o] = p.out[o].side == 0;
+    }
+    const long long *singleKeys = nullptr;
+    const uint8_t *singleNulls = nullptr;
+    int64_t singleRows = 0;
+    if (kSingle) {
+        singleKeys = static_cast<const long long *>(p.batches[0].cols[p.keyInput]);
+        singleNulls = p.batches[0].nulls[p.keyInput];
+        singleRows = p.batches[0].rows;
+    }
+    const int64_t nItems = kSingle ? (singleRows + kGroupRows - 1) / kGroupRows
+                                   : static_cast<int64_t>(p.nTiles) * kGroupTilesPerTile;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * kGroupsPerCta;
+    for (int64_t item = static_cast<int64_t>(blockIdx.x) * kGroupsPerCta + group; item < nItems; item += stride) {
+        const int t = static_cast<int>(item / kGroupTilesPerTile);
+        const long long *keyCol;
+        const uint8_t *keyNulls;
+        int64_t base;
+        int64_t batchRows;
+        if (kSingle) {
+            keyCol = singleKeys;
+            keyNulls = singleNulls;
+            base = item * kGroupRows + gw * kBitsSegRows;
+            batchRows = singleRows;
+        } else {
+            const int s0 = static_cast<int>(item % kGroupTilesPerTile) * kGroupRows;
+            const TileDesc tile = p.tiles[t];
+            if (s0 >= tile.rows) {
+                continue;  // the same for every thread of the group
+            }
+            const BatchDesc &b = p.batches[tile.batch];
+            keyCol = static_cast<const long long *>(b.cols[p.keyInput]);
+            keyNulls = b.nulls[p.keyInput];
+            base = static_cast<int64_t>(tile.row0) + s0 + gw * kBitsSegRows;
+            batchRows = static_cast<int64_t>(tile.row0) + tile.rows;
+        }
+        int64_t key[kBitsRounds];
+        const uint32_t live = LoadKeySegment(keyCol, keyNulls, base, batchRows, lane, key);
+        uint32_t hit = 0;
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            const uint64_t d = static_cast<uint64_t>(key[i]) - minKey;
+            if (((live >> i) & 1u) && key[i] >= p.table.minKey && d < range) {
+                hit |= ((sBits[d >> 5] >> (d & 31)) & 1u) << i;
+            }
+        }
+        uint64_t payload[kBitsRounds];
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            payload[i] = ((hit >> i) & 1u) ? __ldg(payloadTab + (static_cast<uint64_t>(key[i]) - minKey)) : 0ull;
+        }
+        uint32_t count = 0;
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            count += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
+        }
+        if (lane == 0) {
+            sOff[gw] = count;
+        }
+        GroupBarrier(group);
+        if (gw == 0) {
+            // Exclusive offsets of the group's warps and one output reservation for the group.
+            unsigned int c = lane < kGroupWarps ? sOff[lane] : 0u;
+            unsigned int incl = c;
+#pragma unroll
+            for (int d = 1; d < kGroupWarps; d <<= 1) {
+                const unsigned int v = __shfl_up_sync(0xffffffffu, incl, d);
+                incl += lane >= d ? v : 0u;
+            }
+            const unsigned int total = __shfl_sync(0xffffffffu, incl, kGroupWarps - 1);
+            if (lane < kGroupWarps) {
+                sOff[lane] = incl - c;
+            }
+            if (lane == 0) {
+                const int region = t % p.nRegions;
+                *sBase = total != 0 ? atomicAdd(p.outCount + region * kRegionStride, static_cast<unsigned long long>(total))
+                                    : 0ull;
+                *sTotal = total;
+            }
+        }
+        GroupBarrier(group);
+        const unsigned int total = *sTotal;
+        if (p.countOnly || total == 0) {
+            continue;  // uniform over the group
+        }
+        unsigned int off = sOff[gw];
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
+            if ((hit >> i) & 1u) {
+                const unsigned int r = off + __popc(m & lanesBelow);
+                sKey[r] = key[i];
+                sPay[r] = payload[i];
+            }
+            off += __popc(m);
+        }
+        GroupBarrier(group);
+        const uint64_t pos = *sBase;
+        const uint32_t n = pos >= p.regionCap ? 0u
+            : static_cast<uint32_t>(pos + total <= p.regionCap ? total : p.regionCap - pos);
+        const uint64_t at0 = static_cast<uint64_t>(t % p.nRegions) * p.regionCap + pos;
+        WriteStagedColumn<kLayout, 0>(vals[0], width[0], isKey[0], shift[0], sKey, sPay, at0, n, gt);
+        if (kNumOut > 1) {
+            WriteStagedColumn<kLayout, 1>(vals[1], width[1], isKey[1], shift[1], sKey, sPay, at0, n, gt);
+        }
+        if (kNumOut > 2) {
+            WriteStagedColumn<kLayout, 2>(vals[2], width[2], isKey[2], shift[2], sKey, sPay, at0, n, gt);
+        }
+        if (kNumOut > 3) {
+            WriteStagedColumn<kLayout, 3>(vals[3], width[3], isKey[3], shift[3], sKey, sPay, at0, n, gt);
+        }
+    }
+}
+
 // Occupancy bitmap of an ARRAY table: bit d of word d / 32 set iff entries[d] >= 0.  Words past
 // the range (up to the 16-byte padding) are zero.
 __global__ void BuildSlotBitsKernel(const int64_t *entries, uint64_t range, uint32_t *bits, uint64_t nWords)
@@ -1522,6 +1746,8 @@ cudaError_t LaunchBuildFill(JoinTable t, const void *keys, const uint8_t *nulls,
 
 uint64_t SlotBitsBytes(uint64_t range) { return ((range + 127) / 128) * 16; }
 
+void SetStagedProbe(bool on) { g_stagedProbe.store(on); }
+
 cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
 {
     if (p.nTiles <= 0) {
@@ -1565,6 +1791,15 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             const void *single;
             const void *tiled;
         };
+#define OMG_GROUP_INST(n, layout)                                                                  \
+    {layout, n, reinterpret_cast<const void *>(ProbeGroupKernel<n, layout, true>),                 \
+        reinterpret_cast<const void *>(ProbeGroupKernel<n, layout, false>)}
+        static const Inst groupInsts[] = {
+            OMG_GROUP_INST(3, OutLayout(kW8, kW4, kW4)), OMG_GROUP_INST(2, OutLayout(kW8, kW8)),
+            OMG_GROUP_INST(2, OutLayout(kW8, kW4)), OMG_GROUP_INST(1, 0), OMG_GROUP_INST(2, 0), OMG_GROUP_INST(3, 0),
+            OMG_GROUP_INST(4, 0),
+        };
+#undef OMG_GROUP_INST
         static const Inst insts[] = {
             {OutLayout(kW8, kW4, kW4), 3, reinterpret_cast<const void *>(ProbeBitsKernel<3, OutLayout(kW8, kW4, kW4), true>),
                 reinterpret_cast<const void *>(ProbeBitsKernel<3, OutLayout(kW8, kW4, kW4), false>)},
@@ -1595,6 +1830,27 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             pick = match ? i : -1;
         }
         const int single = p.singleBatch ? 0 : 1;
+        // Inner joins whose outputs are the probe key and payload fields take the staged kernel
+        // when its shared memory (bitmap + the groups' staging) fits.
+        const uint32_t groupSmem = static_cast<uint32_t>(bitsBytes) + kGroupsPerCta * kGroupStageBytes;
+        bool staged = p.joinKind == JOIN_KIND_INNER && p.table.slotPayload != nullptr && groupSmem <= kGroupMaxSmem &&
+            g_stagedProbe.load();
+        for (int o = 0; staged && o < p.nOut; ++o) {
+            staged = p.out[o].side != 2;
+        }
+        if (staged) {
+            const void *gk = single == 0 ? groupInsts[pick].single : groupInsts[pick].tiled;
+            cudaError_t gerr = EnsureDynamicSmem(gk, kGroupMaxSmem);
+            if (gerr != cudaSuccess) {
+                return gerr;
+            }
+            const int64_t items = static_cast<int64_t>(p.nTiles) * kGroupTilesPerTile;
+            const int64_t wanted = (items + kGroupsPerCta - 1) / kGroupsPerCta;
+            const int grid = static_cast<int>(wanted < SMs() ? (wanted > 0 ? wanted : 1) : SMs());
+            uint32_t bitsVecs = static_cast<uint32_t>(bitsBytes / 16);
+            void *gargs[] = {const_cast<ProbeLaunch *>(&p), &bitsVecs};
+            return cudaLaunchKernel(gk, dim3(grid), dim3(kBitsThreads), gargs, static_cast<size_t>(groupSmem), stream);
+        }
         const void *kernel = single == 0 ? insts[pick].single : insts[pick].tiled;
         cudaError_t err = EnsureDynamicSmem(kernel, kBitsMaxSmem);
         if (err != cudaSuccess) {

@@ -50,6 +50,10 @@ cudaError_t LaunchAggExtract(const AggExtract &e, cudaStream_t stream);
 cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtract &e,
     const unsigned long long *ambSlots, uint32_t nAmb, uint8_t *forced, cudaStream_t stream);
 
+// Inner probes on a bitmap ARRAY table use the group-staged kernel when it fits (default on);
+// off selects the per-warp bitmap kernel.  Process-wide; for tests and measurements.
+void SetStagedProbe(bool on);
+
 // ---- utilities (util.cu)
 // Masked-input NULL bitmaps, one per job (see MaskJob).
 cudaError_t LaunchMaskNulls(const MaskJob *jobs, int32_t nJobs, cudaStream_t stream);

@@ -245,3 +245,17 @@ def test_pipelined_probe_chunks_in_flight(gpu, join_type):
     g_sorted = got_rows[:, np.lexsort(got_rows[::-1])]
     w_sorted = want_rows[:, np.lexsort(want_rows[::-1])]
     assert np.array_equal(g_sorted, w_sorted)
+
+
+@pytest.mark.parametrize("device_input", [False, True])
+@pytest.mark.parametrize("batch", [4096, 3000, 1 << 20])
+def test_staged_and_per_warp_probe_kernels_agree(gpu, device_input, batch):
+    """The group-staged inner probe (whole-line output runs) and the per-warp bitmap probe give
+    the oracle's rows, for one large batch and for many ragged batches, host and HBM input."""
+    bkey, p1, p2, pkey, pnull = _cfg2_like(1 << 16, 600_000, 41)
+    try:
+        for staged in (1, 0):
+            omg.lib().omg_debug_set_staged_probe(staged)
+            _check(bkey, p1, p2, pkey, pnull, batch_sizes=(batch,), device_input=device_input)
+    finally:
+        omg.lib().omg_debug_set_staged_probe(1)
