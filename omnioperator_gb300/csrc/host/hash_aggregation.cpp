@@ -239,6 +239,9 @@ OmniStatus HashAggregationOperatorFactory::Init()
         a.input = static_cast<int16_t>(input);
         a.inKind = static_cast<int16_t>(inKind);
         a.inWidth = static_cast<int16_t>(inWidth);
+        if ((kind == omg::ACC_XMIN || kind == omg::ACC_XMAX) && ((p.keyWords + word) & 1) != 0) {
+            ++word;  // 16-byte states sit on a 16-byte boundary of the (even-sized) slot
+        }
         a.word = word;
         a.init = init;
         word += omg::AccWords(kind);
@@ -507,6 +510,12 @@ OmniStatus HashAggregationOperatorFactory::Init()
                     o.kind = isMin ? omg::OUT_MIN_DOUBLE : omg::OUT_MAX_DOUBLE;
                     o.src = static_cast<int16_t>(accFor(isMin ? omg::ACC_DMIN : omg::ACC_DMAX, input, inKind, inW,
                         OrderedBits(isMin ? lim : -lim)));
+                } else if (inId == OMNI_DECIMAL128 && outT->GetId() == OMNI_DECIMAL128) {
+                    // Decimal128 MIN/MAX (min_aggregator.h, MinAggregator<OMNI_DECIMAL128,
+                    // OMNI_DECIMAL128>): a 16-byte state updated by a 128-bit CAS loop.
+                    o.kind = omg::OUT_MINMAX_DEC128;
+                    o.src = static_cast<int16_t>(
+                        accFor(isMin ? omg::ACC_XMIN : omg::ACC_XMAX, input, omg::IN_DEC128, 16, 0));
                 } else if (IsVarlen(inId)) {
                     // MIN/MAX of VARCHAR (min_aggregator.cpp / max_aggregator.cpp over string_view):
                     // the input is read as its string dictionary ids and the state keeps the id of
@@ -575,6 +584,13 @@ OmniStatus HashAggregationOperatorFactory::Init()
     }
     p.stateWords = word;
     p.slotWords = p.keyWords + p.stateWords;
+    for (const auto &a : p.accs) {
+        if ((a.kind == omg::ACC_XMIN || a.kind == omg::ACC_XMAX) && (p.slotWords & 1) != 0) {
+            ++p.stateWords;  // even slots keep every slot's 16-byte states aligned
+            ++p.slotWords;
+            break;
+        }
+    }
     p.smemSlots = static_cast<int32_t>(kSmemBudget / (p.slotWords * sizeof(uint64_t)));
     p.rowsPerBatch = GetMaxRowCount(rowBytes);
     // AlignSchema columns: each output of a raw-input partial plan restated for one row.

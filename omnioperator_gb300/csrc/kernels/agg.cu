@@ -217,6 +217,56 @@ __device__ __forceinline__ void AddDoubleState(uint64_t *w, double x, unsigned l
     }
 }
 
+// ------------------------------------------------------------------ decimal128 min / max
+// The state is a 16-byte (low, high) word pair; its initial value is +-(10^38 - 1), the
+// reference's GetMax<Decimal128> (min_aggregator.h:31-34).
+constexpr uint64_t kDec38MaxLo = 687399551400673279ull;
+constexpr uint64_t kDec38MaxHi = 5421010862427522170ull;
+constexpr uint64_t kDec38MinLo = ~kDec38MaxLo + 1ull;  // two's complement of 10^38 - 1
+constexpr uint64_t kDec38MinHi = ~kDec38MaxHi;          // the low word is not zero: no carry
+
+struct alignas(16) Dec128Word {
+    unsigned long long lo;
+    unsigned long long hi;
+};
+
+__device__ __forceinline__ void InitMinMax128(int kind, uint64_t *w)
+{
+    w[0] = kind == ACC_XMIN ? kDec38MaxLo : kDec38MinLo;
+    w[1] = kind == ACC_XMIN ? kDec38MaxHi : kDec38MinHi;
+}
+
+__device__ __forceinline__ bool IsInitMinMax128(int kind, const uint64_t *w)
+{
+    return kind == ACC_XMIN ? (w[0] == kDec38MaxLo && w[1] == kDec38MaxHi) : (w[0] == kDec38MinLo && w[1] == kDec38MinHi);
+}
+
+// Lock-free 128-bit min / max: the current value is read with a no-op compare-and-swap (one
+// atomic 16-byte read), and a CAS installs the value only while it is strictly better, so every
+// retry follows another thread's improvement and the loop ends.
+__device__ __forceinline__ void AtomicMinMax128(uint64_t *w, uint64_t lo, uint64_t hi, bool isMin)
+{
+    Dec128Word *a = reinterpret_cast<Dec128Word *>(w);
+    Dec128Word val;
+    val.lo = lo;
+    val.hi = hi;
+    Dec128Word cur = atomicCAS(a, val, val);
+    while (true) {
+        const int64_t vh = static_cast<int64_t>(hi);
+        const int64_t ch = static_cast<int64_t>(cur.hi);
+        const bool less = vh < ch || (vh == ch && lo < cur.lo);
+        const bool greater = vh > ch || (vh == ch && lo > cur.lo);
+        if (isMin ? !less : !greater) {
+            return;
+        }
+        const Dec128Word prev = atomicCAS(a, cur, val);
+        if (prev.lo == cur.lo && prev.hi == cur.hi) {
+            return;
+        }
+        cur = prev;
+    }
+}
+
 // ------------------------------------------------------------------ state updates
 // `st` points at the group's state words, in shared or global memory.
 __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc &b, int64_t row, const RowIn &in,
@@ -295,6 +345,12 @@ __device__ __forceinline__ void UpdateStates(const AggLaunch &p, const BatchDesc
             case ACC_SMAX:
                 AtomicStrMinMax(p, s.input, w, AccInt(s, b, row, in), s.kind == ACC_SMIN);
                 break;
+            case ACC_XMIN:
+            case ACC_XMAX: {
+                const uint64_t *v = static_cast<const uint64_t *>(b.cols[s.input]) + 2 * row;
+                AtomicMinMax128(w, v[0], v[1], s.kind == ACC_XMIN);
+                break;
+            }
             default:
                 break;
         }
@@ -350,6 +406,12 @@ __device__ __forceinline__ void MergeStates(const AggLaunch &p, const AccSpec *a
                     AtomicStrMinMax(p, s.input, w, static_cast<int64_t>(v[0]), s.kind == ACC_SMIN);
                 }
                 break;
+            case ACC_XMIN:
+            case ACC_XMAX:
+                if (!IsInitMinMax128(s.kind, v)) {
+                    AtomicMinMax128(w, v[0], v[1], s.kind == ACC_XMIN);
+                }
+                break;
             default:
                 break;
         }
@@ -363,6 +425,9 @@ __device__ __forceinline__ void InitStates(const AccSpec *accs, int nAccs, int s
     }
     for (int a = 0; a < nAccs; ++a) {
         st[accs[a].word] = static_cast<uint64_t>(accs[a].init);
+        if (accs[a].kind == ACC_XMIN || accs[a].kind == ACC_XMAX) {
+            InitMinMax128(accs[a].kind, st + accs[a].word);
+        }
     }
 }
 
@@ -791,6 +856,18 @@ __device__ __forceinline__ void ProcessPartTile(const AggLaunch &p, int32_t batc
                         continue;
                     }
                     AtomicStrMinMax(p, s.input, st + slot[k] * sw + s.word, LoadIntW<4>(col, row), s.kind == ACC_SMIN);
+                }
+                break;
+            case ACC_XMIN:
+            case ACC_XMAX:
+#pragma unroll
+                for (int k = 0; k < kPartRows; ++k) {
+                    const int64_t row = row0 + k * 1024;
+                    if (slot[k] < 0 || NullRO(nulls, row)) {
+                        continue;
+                    }
+                    const ulonglong2 v = __ldg(static_cast<const ulonglong2 *>(col) + row);
+                    AtomicMinMax128(st + slot[k] * sw + s.word, v.x, v.y, s.kind == ACC_XMIN);
                 }
                 break;
             default:
@@ -1286,6 +1363,12 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
             case OUT_STR_ID:  // a dictionary id; the host turns it back into the string
                 StoreWidth(os.values, pos, os.outWidth, w[0]);
                 break;
+            case OUT_MINMAX_DEC128: {
+                uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
+                dst[0] = w[0];
+                dst[1] = w[1];
+                break;
+            }
             case OUT_SUM_DOUBLE:
             case OUT_AVG: {
                 double sum = __dadd_rn(__longlong_as_double(static_cast<long long>(w[0])),

@@ -82,6 +82,7 @@ struct KeySpec {
 //  IMIN/IMAX  int64 min / max                            1 word
 //  DMIN/DMAX  double min / max as order-preserving int64 1 word
 //  SMIN/SMAX  VARCHAR min / max: the string dictionary id 1 word (-1: no value yet)
+//  XMIN/XMAX  decimal128 min / max (low, high word)     2 words, 16-byte aligned in the slot
 // WSUM keeps the positive and the negative values apart, each as sums of 32-bit chunks: word k
 // of a side accumulates bits [32k, 32k+32) of every magnitude.  A word therefore never carries
 // for fewer than 2^32 rows per group, every update is a fire-and-forget atomic add, the exact
@@ -99,6 +100,8 @@ enum AccKind : int16_t {
     ACC_DMAX = 9,
     ACC_SMIN = 10,
     ACC_SMAX = 11,
+    ACC_XMIN = 12,
+    ACC_XMAX = 13,
 };
 
 struct AccSpec {
@@ -119,6 +122,8 @@ inline int AccWords(int kind)
         case ACC_WSUM3:
             return 8;
         case ACC_DSUM:
+        case ACC_XMIN:
+        case ACC_XMAX:
             return 2;
         default:
             return 1;
@@ -237,6 +242,7 @@ enum OutKind : int16_t {
     OUT_STR_ID = 13,           // VARCHAR MIN/MAX: the dictionary id (int32) of acc src, NULL if none
     OUT_IS_EMPTY = 14,         // decimal SUM partial: BOOLEAN, 1 when no value reached the group's sum
                                // (count as for OUT_COUNT, and no partial sum overflowed: flagAcc)
+    OUT_MINMAX_DEC128 = 15,    // decimal128 MIN / MAX: the two words of acc src
 };
 
 struct OutSpec {

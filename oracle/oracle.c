@@ -204,6 +204,9 @@ static void state_init(const agg_t *a, state_t *s)
         if (a->in_type == T_DOUBLE || a->in_type == T_FLOAT) {
             const double lim = a->in_type == T_FLOAT ? 3.4028234663852886e38 : 1.7976931348623157e308;
             s->d = a->func == F_MIN ? lim : -lim;
+        } else if (a->in_type == T_DEC128) {
+            /* Decimal128 MIN/MAX start at +-(10^38 - 1) (GetMax<Decimal128>, min_aggregator.h:31-34) */
+            s->wide = a->func == F_MIN ? DEC38_MAX : -DEC38_MAX;
         } else {
             int64_t mx = ow == 1 ? INT8_MAX : ow == 2 ? INT16_MAX : ow == 4 ? INT32_MAX : INT64_MAX;
             int64_t mn = ow == 1 ? INT8_MIN : ow == 2 ? INT16_MIN : ow == 4 ? INT32_MIN : INT64_MIN;
@@ -277,6 +280,11 @@ static void state_update(const aggctx_t *c, const agg_t *a, state_t *s, int64_t 
                 double x = load_double(a->col, r, a->in_type, a->in_width);
                 if (a->func == F_MIN) s->d = (x < s->d) ? x : s->d;
                 else s->d = (s->d < x) ? x : s->d;
+            } else if (a->in_type == T_DEC128) {
+                const uint64_t *p = (const uint64_t *)a->col + 2 * r;
+                const i128 x = (i128)(((unsigned __int128)p[1] << 64) | p[0]);
+                if (a->func == F_MIN) s->wide = (x < s->wide) ? x : s->wide;
+                else s->wide = (s->wide < x) ? x : s->wide;
             } else {
                 int64_t x = load_int(a->col, r, a->in_width);
                 if (a->func == F_MIN) s->i64 = (x < s->i64) ? x : s->i64;
@@ -310,6 +318,12 @@ static int state_extract(const aggctx_t *c, const agg_t *a, const state_t *s, in
         case F_MIN:
         case F_MAX: {
             if (s->state == ST_EMPTY) return 1;
+            if (a->in_type == T_DEC128) {
+                uint64_t *o = (uint64_t *)out + 2 * g;
+                o[0] = (uint64_t)s->wide;
+                o[1] = (uint64_t)((unsigned __int128)s->wide >> 64);
+                return 0;
+            }
             if (a->out_type == T_DOUBLE) ((double *)out)[g] = s->d;
             else if (a->out_type == T_FLOAT) ((float *)out)[g] = (float)s->d;
             else if (a->out_type == T_INT || a->out_type == T_DATE32) ((int32_t *)out)[g] = (int32_t)s->i64;

@@ -388,3 +388,35 @@ def test_decimal128_sums_next_to_empty_groups(gpu, strategy):
                          [dict(func=oracle.F_SUM, col=dec, in_type=oracle.T_DEC64, out_type=oracle.T_DEC128,
                                nulls=nulls)])
     assert_agg_equal(cols, ora, 1)
+
+
+@pytest.mark.parametrize("strategy", [omg.AGG_STRATEGY_AUTO, omg.AGG_STRATEGY_SMEM, omg.AGG_STRATEGY_GLOBAL,
+                                      omg.AGG_STRATEGY_PARTITIONED])
+def test_decimal128_min_max(gpu, strategy):
+    """MIN / MAX of decimal128 values (min_aggregator.h, MinAggregator<DECIMAL128, DECIMAL128>):
+    values of both signs up to +-(10^38 - 1), equal high words with different low words, NULLs
+    and all-NULL groups, bit-exact against the oracle."""
+    rng = np.random.default_rng(91)
+    n, groups = 200_000, 3000
+    key = rng.integers(0, groups, n).astype(np.int64)
+    big = 10**38 - 1
+    vals = []
+    for i in range(n):
+        r = rng.random()
+        if r < 0.3:
+            v = int(rng.integers(-10**18, 10**18))
+        elif r < 0.6:
+            v = int(rng.integers(-2**62, 2**62)) * (1 << 64) + int(rng.integers(0, 2**63))
+        else:
+            v = int(rng.integers(-2**31, 2**31)) << 64 | int(rng.integers(0, 2**63)) * 2
+        vals.append(max(-big, min(big, v)))
+    vals[5], vals[6] = big, -big
+    dec = np.array([[v & (2**64 - 1), (v >> 64) & (2**64 - 1)] for v in vals], dtype=np.uint64)
+    nulls = (rng.random(n) < 0.05) | (key % 97 == 0)
+    D128 = omg.Decimal128Type(38, 3)
+    cols, _ = run_agg([0], [L], [[1], [1]], [[D128], [D128]], [[D128], [D128]], [MIN, MAX], [key, dec], [L, D128],
+                      nulls=[None, nulls], strategy=strategy, batch_sizes=(4096, 777))
+    ora = oracle.hashagg([key], [oracle.T_LONG], [None],
+                         [dict(func=f, col=dec, in_type=oracle.T_DEC128, out_type=oracle.T_DEC128, nulls=nulls)
+                          for f in (oracle.F_MIN, oracle.F_MAX)])
+    assert_agg_equal(cols, ora, 1)

@@ -157,3 +157,26 @@ def test_masked_aggregator_equals_aggregator_over_kept_rows():
             assert vals == want[k]
         else:  # no kept row: NULL SUM/MIN/MAX, zero counts
             assert vals == (None, 0, 0, None, None)
+
+
+def test_decimal128_min_max_restatement():
+    """The oracle's decimal128 MIN / MAX against Python integers, group by group."""
+    rng = np.random.default_rng(12)
+    n = 5000
+    key = rng.integers(0, 60, n).astype(np.int64)
+    vals = [int(rng.integers(-2**62, 2**62)) * (1 << 64) + int(rng.integers(0, 2**63)) for _ in range(n)]
+    dec = np.array([[v & M64, (v >> 64) & M64] for v in vals], dtype=np.uint64)
+    nulls = rng.random(n) < 0.1
+    nulls[key == 3] = True
+    res = oracle.hashagg([key], [oracle.T_LONG], [None],
+                         [dict(func=f, col=dec, in_type=oracle.T_DEC128, out_type=oracle.T_DEC128, nulls=nulls)
+                          for f in (oracle.F_MIN, oracle.F_MAX)])
+    got = _groups(res)
+    for k in np.unique(key):
+        xs = [vals[i] for i in range(n) if key[i] == k and not nulls[i]]
+        g = got[(int(k),)]
+        if not xs:
+            assert g == (None, None)
+            continue
+        lo, hi = min(xs), max(xs)
+        assert g == ((lo & M64, (lo >> 64) & M64), (hi & M64, (hi >> 64) & M64))
