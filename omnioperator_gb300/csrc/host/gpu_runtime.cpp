@@ -64,8 +64,8 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
             if (entry == -1) {
                 continue;
             }
-            const bool invert = entry < -1;
-            const int32_t m = invert ? -2 - entry : entry;
+            const int mode = entry < -1 ? 1 : (entry >= kNullsOfMaskBase ? 2 : 0);
+            const int32_t m = mode == 1 ? -2 - entry : (mode == 2 ? entry - kNullsOfMaskBase : entry);
             if (m >= b->GetVectorCount()) {
                 throw OmniException("OPERATOR_RUNTIME_ERROR",
                     "input batch has " + std::to_string(b->GetVectorCount()) + " vectors, mask column " +
@@ -82,7 +82,7 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
             job.maskNulls = mv->RawNulls() != nullptr && mv->HasNull() ? mv->RawNulls() : nullptr;
             job.out = nullptr;
             job.rows = d.rows;
-            job.invert = invert ? 1 : 0;
+            job.mode = mode;
             maskJobs_.push_back(job);
             maskSlots_.push_back(MaskSlot{bi, static_cast<int32_t>(i), maskWords_});
             maskWords_ += (d.rows + 31) / 32;

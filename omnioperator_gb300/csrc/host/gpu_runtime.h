@@ -156,8 +156,11 @@ private:
 // entry is column m >= 0 reads its values as usual but its NULL bitmap is computed on the device
 // at Upload: the value column's NULLs plus every row whose BOOLEAN column m is NULL or FALSE
 // (aggregation mask columns).  An entry InvertedMask(m) drops the rows whose column m is TRUE
-// instead (the isEmpty column of partial decimal sums), without reading m's NULLs.
+// instead (the isEmpty column of partial decimal sums), without reading m's NULLs; an entry
+// NullsOfMask(m) drops the rows where column m is NULL (a partial count whose partial sum is).
 constexpr int32_t InvertedMask(int32_t col) { return -2 - col; }
+constexpr int32_t kNullsOfMaskBase = 1 << 24;
+constexpr int32_t NullsOfMask(int32_t col) { return kNullsOfMaskBase + col; }
 class BatchTable {
 public:
     void Build(const std::vector<omniruntime::vec::VectorBatch *> &batches, const std::vector<int32_t> &inputCols,

@@ -327,6 +327,90 @@ OmniStatus HashAggregationOperatorFactory::Init()
             rowBytes += o.outWidth;
             continue;
         }
+        if (fn == OMNI_AGGREGATION_TYPE_AVG && (in0 == OMNI_DECIMAL64 || in0 == OMNI_DECIMAL128)) {
+            // Spark decimal AVG (AverageSparkDecimalAggregator, average_spark_decimal_aggregator.h):
+            // a checked sum with sticky overflow -- int64 for a decimal64 input and output,
+            // within +-(10^38 - 1) otherwise -- and the non-NULL count.  A partial emits (sum
+            // rescaled to the output scale, count): 0 and 0 for a group without values, the sum
+            // NULL (or an error) on overflow; a merging stage adds the partial sums (checked) and
+            // counts, skipping rows whose partial sum is NULL; the final value is CalcAvg (:477).
+            if (!spark) {
+                throw OmniException("UNSUPPORTED_ERROR", "decimal AVG under the container-vector policy is not supported",
+                    -2);
+            }
+            const DataTypePtr &inT = aggInputTypes_[a].GetType(0);
+            const int inW = inT->ByteWidth();
+            const int inKind = in0 == OMNI_DECIMAL128 ? omg::IN_DEC128 : omg::IN_INT;
+            const int accKind = in0 == OMNI_DECIMAL128 ? omg::ACC_WSUM3 : omg::ACC_WSUM2;
+            // The sum's bound: int64 when both the input and the intermediate are decimal64.
+            const DataTypeId midId = partial ? outTypes.GetType(0)->GetId() : outT->GetId();
+            const int16_t bound = (in0 == OMNI_DECIMAL64 && midId == OMNI_DECIMAL64) ? 0 : 1;
+            int sumAcc;
+            int cntAcc;
+            bool summed;
+            if (raw) {
+                if (aggCols_[a].size() != 1 || aggInputTypes_[a].GetSize() != 1) {
+                    throw OmniException("INVALID_ARGUMENT", "a decimal AVG reads one decimal column", -1);
+                }
+                const int input = inputFor(aggCols_[a][0], inW, mask);
+                cntAcc = accFor(omg::ACC_NULLS, input, omg::IN_NONE, 0, 0);
+                sumAcc = accFor(accKind, input, inKind, inW, 0);
+                summed = false;
+            } else {
+                if (aggCols_[a].size() != 2 || aggInputTypes_[a].GetSize() != 2 ||
+                    !IsIntegerLike(aggInputTypes_[a].GetType(1)->GetId())) {
+                    throw OmniException("INVALID_ARGUMENT", "a merging decimal AVG reads (decimal sum, long count) partial columns",
+                        -1);
+                }
+                if (mask >= 0) {
+                    throw OmniException("UNSUPPORTED_ERROR", "a mask column on a merging decimal AVG is not supported", -2);
+                }
+                const int sums = inputFor(aggCols_[a][0], inW);
+                const int cntW = aggInputTypes_[a].GetType(1)->ByteWidth();
+                const int counts = inputFor(aggCols_[a][1], cntW, omg::NullsOfMask(static_cast<int32_t>(aggCols_[a][0])));
+                accFor(omg::ACC_NULLS, sums, omg::IN_NONE, 0, 0);
+                sumAcc = accFor(accKind, sums, inKind, inW, 0);
+                cntAcc = accFor(omg::ACC_ISUM, counts, omg::IN_INT, cntW, 0);
+                summed = true;
+            }
+            OutSpec s1{};
+            s1.src = static_cast<int16_t>(sumAcc);
+            s1.countAcc = static_cast<int16_t>(cntAcc);
+            s1.countSummed = summed ? 1 : 0;
+            s1.boundKind = bound;
+            s1.pad = static_cast<int16_t>(exactIndex++);
+            if (partial) {
+                // (sum, count): the sum rescaled to the partial's output scale
+                // (ExtractValues, :276-295); a partial of p digits is declared (p + 10, s).
+                const DataTypePtr &sumT = outTypes.GetType(0);
+                const int diff = sumT->GetScale() - inT->GetScale();
+                if (diff < 0 || diff > 38) {
+                    throw OmniException("UNSUPPORTED_ERROR", "decimal AVG partial scale below input scale", -2);
+                }
+                s1.kind = omg::OUT_SUM_EXACT;
+                s1.boundKind = sumT->GetId() == OMNI_DECIMAL128 ? bound : 0;
+                s1.rescalePow = static_cast<int16_t>(diff);
+                s1.partial = 2;
+                pushOut(s1, sumT);
+                OutSpec s2{};
+                s2.kind = summed ? omg::OUT_COUNT_MERGE : omg::OUT_COUNT;
+                s2.src = summed ? static_cast<int16_t>(cntAcc) : 0;
+                s2.countAcc = summed ? -1 : static_cast<int16_t>(cntAcc);
+                pushOut(s2, outTypes.GetType(1));
+                continue;
+            }
+            if (outT->GetId() != OMNI_DECIMAL64 && outT->GetId() != OMNI_DECIMAL128) {
+                throw OmniException("UNSUPPORTED_ERROR", "decimal AVG needs a decimal output type", -2);
+            }
+            s1.kind = omg::OUT_AVG_DEC;
+            // A single-stage AVG sums at precision p + 10 (CalcAvg, :485-488); a final stage sums
+            // the partial sums at their declared precision.
+            s1.sumPrec = static_cast<int16_t>(raw ? std::min(inT->GetPrecision() + 10, 38) : inT->GetPrecision());
+            s1.sumScale = static_cast<int16_t>(inT->GetScale());
+            s1.rescalePow = static_cast<int16_t>(outT->GetScale());
+            pushOut(s1, outT);
+            continue;
+        }
         if (fn == OMNI_AGGREGATION_TYPE_AVG && !raw) {
             // final AVG over (double sum, long count) partial columns
             if (aggCols_[a].size() != 2 || aggInputTypes_[a].GetSize() != 2 ||
@@ -476,9 +560,6 @@ OmniStatus HashAggregationOperatorFactory::Init()
             case OMNI_AGGREGATION_TYPE_AVG: {
                 if (!isInt && !isDouble) {
                     throw OmniException("UNSUPPORTED_ERROR", "unsupported AVG input type " + std::to_string(inId), -2);
-                }
-                if (inId == OMNI_DECIMAL64) {
-                    throw OmniException("UNSUPPORTED_ERROR", "decimal AVG is not supported", -2);
                 }
                 o.src = static_cast<int16_t>(accFor(omg::ACC_DSUM, input, inKind, inW, 0));
                 if (partial) {  // (double sum, long count); 0 and 0 for a group without values

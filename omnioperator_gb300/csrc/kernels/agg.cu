@@ -1242,6 +1242,72 @@ __device__ __forceinline__ bool ExceedsBound(const uint64_t *m, bool negative, i
     return v > Dec38Max();
 }
 
+// Whether an exact sum's sticky-overflow outcome is an overflow: the total beyond the bound
+// always is; a total within it whose sum of magnitudes exceeds the bound depends on the row
+// order and is decided by the ordered replay (the slot is queued for it, or its answer read).
+__device__ __forceinline__ bool ExactSumOverflowed(const AggExtract &e, const OutSpec &os, const WideSum &ws,
+    uint64_t s)
+{
+    bool overflow = ExceedsBound(ws.mag, ws.negative, os.boundKind);
+    if (!overflow && ExceedsBound(ws.abs, false, os.boundKind)) {
+        if (e.forcedOverflow != nullptr) {
+            overflow = ((e.forcedOverflow[s] >> os.pad) & 1u) != 0;
+        } else {
+            unsigned long long k = atomicAdd(e.nAmbiguous, 1ull);
+            if (k < e.ambiguousCap) {
+                e.ambiguousSlots[k] = s;
+            }
+        }
+    }
+    return overflow;
+}
+
+__device__ __forceinline__ unsigned __int128 Pow10U128(int n)
+{
+    unsigned __int128 p = 1;
+    for (int i = 0; i < n; ++i) {
+        p *= 10;
+    }
+    return p;
+}
+
+// Spark's decimal average of a checked sum (magnitude `sum`, the sign applied by the caller)
+// over `count` rows (CalcAvg, average_spark_decimal_aggregator.h:477-546): the quotient's scale
+// is max(6, sumScale + 21) at precision sumPrec - sumScale + scale, cut back to 38 digits
+// keeping the integer digits and at least min(scale, 6) fractional ones; the sum is rescaled to
+// it (checked against 10^38 - 1), divided by the count rounding half away from zero, and
+// rescaled to the output scale (multiplied, checked, or divided, rounded again).  Magnitudes
+// round the same way as the signed values.  False on overflow.
+__device__ __forceinline__ bool DecimalAverage(unsigned __int128 sum, uint64_t count, int sumPrec, int sumScale,
+    int outScale, unsigned __int128 *out)
+{
+    int scale = sumScale + 21 > 6 ? sumScale + 21 : 6;
+    const int prec = sumPrec - sumScale + scale;
+    if (prec > 38) {
+        const int intDigits = prec - scale;
+        const int minScale = scale < 6 ? scale : 6;
+        scale = 38 - intDigits > minScale ? 38 - intDigits : minScale;
+    }
+    const unsigned __int128 f = Pow10U128(scale - sumScale);
+    if (sum != 0 && sum > Dec38Max() / f) {
+        return false;
+    }
+    const unsigned __int128 dividend = sum * f;
+    const unsigned __int128 avg = (dividend + count / 2) / count;
+    const int diff = outScale - scale;
+    if (diff >= 0) {
+        const unsigned __int128 g = Pow10U128(diff);
+        if (avg != 0 && avg > Dec38Max() / g) {
+            return false;
+        }
+        *out = avg * g;
+    } else {
+        const unsigned __int128 g = Pow10U128(-diff);
+        *out = (avg + g / 2) / g;
+    }
+    return true;
+}
+
 // A zero value at output row `pos` (a 16-byte column holds two words per row).
 __device__ __forceinline__ void StoreZero(const OutSpec &os, uint64_t pos)
 {
@@ -1331,7 +1397,8 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
         }
         int64_t cnt = static_cast<int64_t>(st[e.accs[0].word]);  // accs[0] is COUNT_ALL
         if (os.countAcc >= 0) {
-            cnt -= static_cast<int64_t>(st[e.accs[os.countAcc].word]);
+            cnt = os.countSummed ? static_cast<int64_t>(st[e.accs[os.countAcc].word])
+                                 : cnt - static_cast<int64_t>(st[e.accs[os.countAcc].word]);
         }
         if (os.kind == OUT_COUNT) {
             StoreWidth(os.values, pos, 8, static_cast<uint64_t>(cnt));
@@ -1342,7 +1409,7 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
             // partial).  An empty partial sum: 0, not NULL.
             if (flagged) {
                 SetOutNull(os.nulls, pos);
-                if (!e.overflowAsNull && os.partial == 0) {
+                if (!e.overflowAsNull && os.partial != 1) {
                     SetError(e.error, 5);
                 }
             }
@@ -1390,21 +1457,36 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
                 }
                 break;
             }
+            case OUT_AVG_DEC: {
+                WideSum ws = DecodeWide(acc, w);
+                bool overflow = ExactSumOverflowed(e, os, ws, s);
+                unsigned __int128 mag = 0;
+                if (!overflow) {
+                    const unsigned __int128 sum = (static_cast<unsigned __int128>(ws.mag[1]) << 64) | ws.mag[0];
+                    overflow = !DecimalAverage(sum, static_cast<uint64_t>(cnt), os.sumPrec, os.sumScale, os.rescalePow,
+                        &mag);
+                }
+                if (overflow) {
+                    SetOutNull(os.nulls, pos);
+                    if (!e.overflowAsNull) {
+                        SetError(e.error, 5);
+                    }
+                    StoreZero(os, pos);
+                    break;
+                }
+                const unsigned __int128 v = ws.negative ? (~mag + 1) : mag;
+                if (os.outWidth == 16) {
+                    uint64_t *dst = static_cast<uint64_t *>(os.values) + 2 * pos;
+                    dst[0] = static_cast<uint64_t>(v);
+                    dst[1] = static_cast<uint64_t>(v >> 64);
+                } else {
+                    StoreWidth(os.values, pos, os.outWidth, static_cast<uint64_t>(v));  // cut to 64 bits
+                }
+                break;
+            }
             case OUT_SUM_EXACT: {
                 WideSum ws = DecodeWide(acc, w);
-                bool overflow = ExceedsBound(ws.mag, ws.negative, os.boundKind);
-                if (!overflow && ExceedsBound(ws.abs, false, os.boundKind)) {
-                    // Some prefix of the row-ordered sum may have overflowed: decided by
-                    // the ordered path on the host side of this operator.
-                    if (e.forcedOverflow != nullptr) {
-                        overflow = ((e.forcedOverflow[s] >> os.pad) & 1u) != 0;
-                    } else {
-                        unsigned long long k = atomicAdd(e.nAmbiguous, 1ull);
-                        if (k < e.ambiguousCap) {
-                            e.ambiguousSlots[k] = s;
-                        }
-                    }
-                }
+                bool overflow = ExactSumOverflowed(e, os, ws, s);
                 unsigned __int128 mag = (static_cast<unsigned __int128>(ws.mag[1]) << 64) | ws.mag[0];
                 if (!overflow && os.rescalePow > 0) {
                     unsigned __int128 f = 1;
@@ -1420,7 +1502,7 @@ __device__ __forceinline__ void WriteGroup(const AggExtract &e, const AggTable &
                 }
                 if (overflow) {
                     SetOutNull(os.nulls, pos);
-                    if (!e.overflowAsNull && os.partial == 0) {
+                    if (!e.overflowAsNull && os.partial != 1) {
                         SetError(e.error, 5);
                     }
                     mag = 0;
@@ -1754,7 +1836,7 @@ __global__ void OrderedOverflowKernel(const __grid_constant__ AggLaunch p, int32
             const int32_t d = denseOf[slot];
             for (int o = 0; o < e.nOut; ++o) {
                 const OutSpec &os = e.out[o];
-                if (os.kind != OUT_SUM_EXACT) {
+                if (os.kind != OUT_SUM_EXACT && os.kind != OUT_AVG_DEC) {
                     continue;
                 }
                 const uint8_t bit = static_cast<uint8_t>(1u << os.pad);

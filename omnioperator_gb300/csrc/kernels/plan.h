@@ -36,7 +36,9 @@ struct MaskJob {
     const uint8_t *maskNulls;   // its NULL bitmap (nullptr: none)
     uint32_t *out;              // ceil(rows / 32) words
     int64_t rows;
-    int32_t invert;             // 1: drop the rows whose mask byte is non-zero (NULL flag not read)
+    int32_t mode;               // 0: drop rows whose mask is NULL or FALSE; 1: drop rows whose mask
+                                // byte is non-zero (its NULL flag not read); 2: drop rows whose mask
+                                // column is NULL (its values not read)
     int32_t pad;
 };
 
@@ -243,6 +245,8 @@ enum OutKind : int16_t {
     OUT_IS_EMPTY = 14,         // decimal SUM partial: BOOLEAN, 1 when no value reached the group's sum
                                // (count as for OUT_COUNT, and no partial sum overflowed: flagAcc)
     OUT_MINMAX_DEC128 = 15,    // decimal128 MIN / MAX: the two words of acc src
+    OUT_AVG_DEC = 16,          // decimal AVG: the exact sum of acc src (sticky overflow as for
+                               // OUT_SUM_EXACT) over the count, rescaled and rounded as Spark does
 };
 
 struct OutSpec {
@@ -256,9 +260,13 @@ struct OutSpec {
     int16_t pad;        // OUT_SUM_EXACT: index of the exact sum (bit of the ordered-replay flags)
     int16_t flagAcc;    // OUT_SUM_EXACT / OUT_IS_EMPTY of a merging stage: NULLS accumulator of the
                         // partial sums; a NULL partial sum is an overflow of that partial (0: none)
-    int16_t partial;    // OUT_SUM_EXACT: 1 = partial output (overflow -> NULL without an error,
-                        // empty -> 0, not NULL)
-    int16_t pad2[2];
+    int16_t partial;    // OUT_SUM_EXACT: 1 = decimal SUM partial (overflow -> NULL without an
+                        // error, empty -> 0, not NULL); 2 = decimal AVG partial sum (overflow ->
+                        // NULL or an error, empty -> 0)
+    int16_t sumPrec;    // OUT_AVG_DEC: precision and scale of the summed values' decimal type
+    int16_t sumScale;
+    int16_t countSummed;  // 1: countAcc is an ISUM of partial counts (else a NULLS accumulator)
+    int16_t pad2[3];
     void *values;       // device output column
     uint8_t *nulls;     // device output null bitmap (zeroed by the host)
 };

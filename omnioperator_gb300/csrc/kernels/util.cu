@@ -69,8 +69,14 @@ __global__ void MaskNullsKernel(const MaskJob *jobs, int32_t nJobs)
             const int64_t row = (w << 5) + lane;
             bool skip = false;
             if (row < job.rows) {
-                const uint8_t m = __ldg(job.maskValues + row);
-                skip = (job.invert ? m != 0 : (m == 0 || NullRO(job.maskNulls, row))) || NullRO(job.valueNulls, row);
+                bool drop;
+                if (job.mode == 2) {
+                    drop = NullRO(job.maskNulls, row);
+                } else {
+                    const uint8_t m = __ldg(job.maskValues + row);
+                    drop = job.mode == 1 ? m != 0 : (m == 0 || NullRO(job.maskNulls, row));
+                }
+                skip = drop || NullRO(job.valueNulls, row);
             }
             const unsigned bits = __ballot_sync(0xffffffffu, skip);
             if (lane == 0) {

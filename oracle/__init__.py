@@ -53,7 +53,7 @@ def lib() -> C.CDLL:
         L = C.CDLL(str(LIB))
         P, I32, I64 = C.c_void_p, C.c_int32, C.c_int64
         L.orc_hashagg.restype = I64
-        L.orc_hashagg.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P, P]
+        L.orc_hashagg.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P, P, P]
         L.orc_join_inner.restype = I64
         L.orc_join_inner.argtypes = [I64, P, I32, P, I64, P, I32, P, P, P, I64]
         L.orc_join.restype = I64
@@ -74,7 +74,7 @@ def lib() -> C.CDLL:
         L.orc_jtable_pairs.argtypes = [P, I64, P, P, P, P, I64]
         L.orc_hashagg_mt.restype = I64
         L.orc_hashagg_mt.argtypes = [I64, I32, P, P, P, I32, P, P, P, P, P, P, P, I32, I32, I64, P, P, P, P, P, P,
-                                     I32, P]
+                                     I32, P, P]
         _lib = L
     return _lib
 
@@ -85,6 +85,12 @@ def _ptr(a):
 
 def _ptr_array(arrs):
     return (C.c_void_p * max(len(arrs), 1))(*[(a.ctypes.data if a is not None else None) for a in arrs])
+
+
+def _dec_params(aggs):
+    """Per aggregator (input precision, input scale, output scale) of a decimal AVG."""
+    return np.array([[a.get("in_prec", 18), a.get("in_scale", 0), a.get("out_scale", 0)] for a in aggs] or [[0, 0, 0]],
+                    dtype=np.int32).reshape(-1)
 
 
 def _masks(aggs):
@@ -109,7 +115,8 @@ def hashagg(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=False):
 
     keys: list of value arrays (int types as their numpy ints, decimal128 as (n, 2) uint64).
     key_nulls: list of bool arrays or None.  aggs: list of dicts with keys func, col (array or
-    None for COUNT(*)), in_type, out_type, nulls (bool array or None), rescale (int), and
+    None for COUNT(*)), in_type, out_type, nulls (bool array or None), rescale (int), for a
+    decimal AVG in_prec / in_scale / out_scale, and
     optionally mask / mask_nulls (bool arrays: the aggregator's mask column; a row reaches it
     only where the mask is TRUE and not NULL).
     Returns (key_values, key_nulls, agg_values, agg_nulls) per group (unordered), or raises
@@ -149,7 +156,7 @@ def hashagg(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=False):
                       _ptr_array(knulls), len(aggs), _ptr(funcs), _ptr_array(cols), _ptr(in_types),
                       _ptr(in_widths), _ptr_array(anulls), _ptr(out_types), _ptr(rescale), policy,
                       1 if overflow_as_null else 0, maxg, _ptr_array(okeys), _ptr_array(oknulls),
-                      _ptr_array(ovals), _ptr_array(ovnulls), _ptr_array(masks))
+                      _ptr_array(ovals), _ptr_array(ovnulls), _ptr_array(masks), _ptr(_dec_params(aggs)))
     if g == -2:
         raise OverflowError("sum_aggregator overflow.")
     if g < 0:
@@ -389,7 +396,7 @@ def hashagg_mt(keys, key_types, key_nulls, aggs, policy=0, overflow_as_null=Fals
                          _ptr(np.array(out_types, dtype=np.int32)), _ptr(np.array(rescale, dtype=np.int32)), policy,
                          1 if overflow_as_null else 0, maxg, _ptr_array(okeys), _ptr_array(oknulls),
                          _ptr_array(ovals), _ptr_array(ovnulls), _ptr_array(exact), _ptr_array(absum), threads,
-                         _ptr_array(masks))
+                         _ptr_array(masks), _ptr(_dec_params(aggs)))
     if g == -2:
         raise OverflowError("sum_aggregator overflow.")
     if g == -3:

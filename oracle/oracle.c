@@ -172,6 +172,7 @@ typedef struct {
     const void *col;
     const uint8_t *nulls; /* byte per row, 1 = null; NULL = no nulls */
     const uint8_t *mask;  /* byte per row, 1 = the row reaches this aggregator; NULL = no mask */
+    int in_prec, in_scale, out_scale; /* decimal AVG: input precision / scale, output scale */
 } agg_t;
 
 typedef struct {
@@ -271,6 +272,37 @@ static void state_update(const aggctx_t *c, const agg_t *a, state_t *s, int64_t 
             }
             return;
         case F_AVG:
+            if (a->in_type == T_DEC64 || a->in_type == T_DEC128) {
+                /* Spark decimal AVG (AverageSparkDecimalAggregator::UpdateState with SumOp,
+                 * average_spark_decimal_aggregator.h:38-49, sum_aggregator.h:13-53): a checked sum,
+                 * int64 for a decimal64 result and int128 within +-(10^38 - 1) otherwise; an
+                 * overflow makes count -1 and stops the state. */
+                if (s->count < 0) return;
+                i128 x;
+                if (a->in_type == T_DEC128) {
+                    const uint64_t *p = (const uint64_t *)a->col + 2 * r;
+                    x = (i128)(((unsigned __int128)p[1] << 64) | p[0]);
+                } else {
+                    x = (i128)load_int(a->col, r, 8);
+                }
+                if (a->out_type == T_DEC64) {
+                    int64_t res;
+                    if (__builtin_add_overflow((int64_t)s->wide, (int64_t)x, &res)) {
+                        s->count = -1;
+                        return;
+                    }
+                    s->wide = res;
+                } else {
+                    i128 res;
+                    if (__builtin_add_overflow(s->wide, x, &res) || res > DEC38_MAX || res < -DEC38_MAX) {
+                        s->count = -1;
+                        return;
+                    }
+                    s->wide = res;
+                }
+                s->count++;
+                return;
+            }
             s->d += load_double(a->col, r, a->in_type, a->in_width);
             s->count++;
             return;
@@ -302,6 +334,50 @@ static i128 pow10_i128(int n)
     return p;
 }
 
+/* MulCheckedOverflow (type/base_operations.h:30-35): product beyond +-(10^38 - 1) overflows. */
+static int mul_checked(i128 a, i128 b, i128 *r)
+{
+    return __builtin_mul_overflow(a, b, r) || *r > DEC38_MAX || *r < -DEC38_MAX;
+}
+
+/* DivideRoundUp (type/base_operations.h:37-48): half away from zero. */
+static i128 divide_round_up(i128 l, i128 r)
+{
+    i128 t = r / 2;
+    if ((l > 0 && r < 0) || (l < 0 && r > 0)) t = -t;
+    return (l + t) / r;
+}
+
+/*
+ * CalcAvg (average_spark_decimal_aggregator.h:477-512) with GetDivideResultDecimalType (:522-546):
+ * the quotient's scale is max(6, sumScale + 21) at precision sumPrec - sumScale + scale, cut back
+ * to 38 digits keeping the integer digits and at least min(scale, 6) fractional ones; the sum
+ * is rescaled to it, divided by the count (rounded half away from zero) and rescaled to the
+ * output scale (multiplied, checked, or divided, rounded again).  Returns 1 on overflow.
+ */
+static int calc_decimal_avg(i128 sum, int64_t count, int sum_prec, int sum_scale, int out_scale, i128 *out)
+{
+    i128 wider;
+    if (mul_checked(sum, pow10_i128((sum_scale > 0 ? sum_scale : 0) - sum_scale), &wider)) return 1;
+    int scale = sum_scale + 21 > 6 ? sum_scale + 21 : 6;
+    int prec = sum_prec - sum_scale + scale;
+    if (prec > 38) {
+        const int int_digits = prec - scale;
+        const int min_scale = scale < 6 ? scale : 6;
+        scale = 38 - int_digits > min_scale ? 38 - int_digits : min_scale;
+    }
+    i128 dividend;
+    int ovf = mul_checked(sum, pow10_i128(scale - sum_scale), &dividend);
+    const i128 avg = divide_round_up(dividend, (i128)count);
+    const int diff = out_scale - scale;
+    if (diff >= 0) {
+        ovf = ovf || mul_checked(avg, pow10_i128(diff), out);
+    } else {
+        *out = divide_round_up(avg, pow10_i128(-diff));
+    }
+    return ovf;
+}
+
 /* Writes the output value of one aggregator; returns 1 if NULL, 2 on an overflow error. */
 static int state_extract(const aggctx_t *c, const agg_t *a, const state_t *s, int overflow_as_null, void *out,
     int64_t g)
@@ -312,6 +388,24 @@ static int state_extract(const aggctx_t *c, const agg_t *a, const state_t *s, in
             ((int64_t *)out)[g] = s->i64;
             return 0;
         case F_AVG:
+            if (a->in_type == T_DEC64 || a->in_type == T_DEC128) {
+                if (s->count < 0) return overflow_as_null ? 1 : 2;
+                if (s->count == 0) return 1;
+                /* a single-stage (raw input, final output) AVG sums at precision p + 10 */
+                const int sum_prec = a->in_prec + 10 < 38 ? a->in_prec + 10 : 38;
+                i128 res;
+                if (calc_decimal_avg(s->wide, s->count, sum_prec, a->in_scale, a->out_scale, &res)) {
+                    return overflow_as_null ? 1 : 2;
+                }
+                if (a->out_type == T_DEC128) {
+                    uint64_t *o = (uint64_t *)out + 2 * g;
+                    o[0] = (uint64_t)res;
+                    o[1] = (uint64_t)((unsigned __int128)res >> 64);
+                } else {
+                    ((int64_t *)out)[g] = (int64_t)res;
+                }
+                return 0;
+            }
             if (s->count == 0) return 1;
             ((double *)out)[g] = s->d / (double)s->count;
             return 0;
@@ -393,7 +487,7 @@ int64_t orc_hashagg(int64_t n_rows, int32_t nkey, const void **key_cols, const i
     const uint8_t **key_nulls, int32_t nagg, const int32_t *funcs, const void **agg_cols, const int32_t *in_types,
     const int32_t *in_widths, const uint8_t **agg_nulls, const int32_t *out_types, const int32_t *rescale,
     int32_t policy, int32_t overflow_as_null, int64_t max_groups, void **out_keys, uint8_t **out_key_nulls,
-    void **out_vals, uint8_t **out_val_nulls, const uint8_t **agg_masks)
+    void **out_vals, uint8_t **out_val_nulls, const uint8_t **agg_masks, const int32_t *dec_params)
 {
     int keybytes = 0;
     for (int i = 0; i < nkey; ++i) keybytes += 1 + key_widths[i];
@@ -416,6 +510,11 @@ int64_t orc_hashagg(int64_t n_rows, int32_t nkey, const void **key_cols, const i
         c.aggs[a].out_type = out_types[a];
         c.aggs[a].rescale = rescale ? rescale[a] : 0;
         c.aggs[a].mask = agg_masks ? agg_masks[a] : NULL;
+        if (dec_params) {
+            c.aggs[a].in_prec = dec_params[3 * a];
+            c.aggs[a].in_scale = dec_params[3 * a + 1];
+            c.aggs[a].out_scale = dec_params[3 * a + 2];
+        }
     }
     int64_t ret = 0;
     for (int64_t r = 0; r < n_rows; ++r) {
@@ -1148,7 +1247,7 @@ int64_t orc_hashagg_mt(int64_t n_rows, int32_t nkey, const void **key_cols, cons
     const int32_t *in_widths, const uint8_t **agg_nulls, const int32_t *out_types, const int32_t *rescale,
     int32_t policy, int32_t overflow_as_null, int64_t max_groups, void **out_keys, uint8_t **out_key_nulls,
     void **out_vals, uint8_t **out_val_nulls, double **out_exact, double **out_abs, int32_t nthreads,
-    const uint8_t **agg_masks)
+    const uint8_t **agg_masks, const int32_t *dec_params)
 {
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 255) nthreads = 255;
@@ -1173,6 +1272,11 @@ int64_t orc_hashagg_mt(int64_t n_rows, int32_t nkey, const void **key_cols, cons
         aggs[a].out_type = out_types[a];
         aggs[a].rescale = rescale ? rescale[a] : 0;
         aggs[a].mask = agg_masks ? agg_masks[a] : NULL;
+        if (dec_params) {
+            aggs[a].in_prec = dec_params[3 * a];
+            aggs[a].in_scale = dec_params[3 * a + 1];
+            aggs[a].out_scale = dec_params[3 * a + 2];
+        }
     }
     for (int i = 0; i < nthreads; ++i) {
         pw[i].r0 = n_rows * i / nthreads;

@@ -180,3 +180,79 @@ def test_decimal128_min_max_restatement():
             continue
         lo, hi = min(xs), max(xs)
         assert g == ((lo & M64, (lo >> 64) & M64), (hi & M64, (hi >> 64) & M64))
+
+
+def _py_decimal_avg(vals, in_prec, in_scale, out_scale, out_dec64=False):
+    """Spark's decimal AVG in Python integers: checked sum (None on overflow), then CalcAvg."""
+    big = 10**38 - 1
+    s, n = 0, 0
+    for v in vals:
+        s += v
+        n += 1
+        if (out_dec64 and not -2**63 <= s < 2**63) or (not out_dec64 and abs(s) > big):
+            return None
+    if n == 0:
+        return None
+
+    def rnd(a, b):  # half away from zero
+        q = (abs(a) + abs(b) // 2) // abs(b)
+        return q if (a >= 0) == (b > 0) else -q
+    sp = min(in_prec + 10, 38)
+    scale = max(6, in_scale + 21)
+    prec = sp - in_scale + scale
+    if prec > 38:
+        scale = max(38 - (prec - scale), min(scale, 6))
+    dividend = s * 10**(scale - in_scale)
+    ovf = abs(dividend) > big
+    avg = rnd(dividend, n)
+    diff = out_scale - scale
+    if diff >= 0:
+        out = avg * 10**diff
+        ovf = ovf or abs(out) > big
+    else:
+        out = rnd(avg, 10**-diff)
+    if ovf:
+        return None
+    # a decimal64 result is the 128-bit value cut to 64 bits (static_cast<int64_t>)
+    return ((out + 2**63) % 2**64) - 2**63 if out_dec64 else out
+
+
+@pytest.mark.parametrize("case", ["dec64_to_dec128", "dec128_to_dec128", "dec64_to_dec64"])
+def test_decimal_avg_restatement(case):
+    """AVG of decimals (AverageSparkDecimalAggregator): a hand-checked value, then random groups
+    (with overflowing ones for the 128-bit cases) against a Python-integer restatement."""
+    # 1.00, 2.00, 2.00 as decimal(18,2) -> decimal(22,6): 5.00 / 3 at scale 12, then scale 6 = 1.666667
+    got = oracle.hashagg([np.zeros(3, np.int64)], [oracle.T_LONG], [None],
+                         [dict(func=oracle.F_AVG, col=np.array([100, 200, 200], np.int64), in_type=oracle.T_DEC64,
+                               out_type=oracle.T_DEC128, in_prec=18, in_scale=2, out_scale=6)])
+    assert int(got[2][0][0][0]) == 1666667
+    rng = np.random.default_rng(4)
+    n = 20_000
+    key = rng.integers(0, 400, n).astype(np.int64)
+    nulls = rng.random(n) < 0.05
+    if case == "dec128_to_dec128":
+        vals = [int(rng.integers(-10**18, 10**18)) * 10**int(rng.integers(0, 19)) for _ in range(n)]
+        in_t, out_t, prec, sc, osc = oracle.T_DEC128, oracle.T_DEC128, 38, 4, 8
+        col = np.array([[v & M64, (v >> 64) & M64] for v in vals], dtype=np.uint64)
+    else:
+        vals = [int(x) for x in rng.integers(-10**17, 10**17, n)]
+        in_t, prec, sc = oracle.T_DEC64, 18, 2
+        out_t, osc = (oracle.T_DEC64, 6) if case == "dec64_to_dec64" else (oracle.T_DEC128, 6)
+        col = np.array(vals, dtype=np.int64)
+    res = oracle.hashagg([key], [oracle.T_LONG], [None],
+                         [dict(func=oracle.F_AVG, col=col, in_type=in_t, out_type=out_t, nulls=nulls, in_prec=prec,
+                               in_scale=sc, out_scale=osc)], overflow_as_null=True)
+    keys, _, vals_out, vnulls = res
+    for i in range(len(keys[0])):
+        k = int(keys[0][i])
+        xs = [vals[j] for j in range(n) if key[j] == k and not nulls[j]]
+        want = _py_decimal_avg(xs, prec, sc, osc, out_dec64=out_t == oracle.T_DEC64)
+        if want is None:
+            assert vnulls[0][i]
+            continue
+        assert not vnulls[0][i]
+        v = vals_out[0][i]
+        got = (int(v[1]) << 64 | int(v[0])) if np.ndim(v) else int(v)
+        if np.ndim(v) and got >> 127:
+            got -= 1 << 128
+        assert got == want, (k, got, want)
