@@ -1232,18 +1232,22 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         t0 = time.perf_counter()
         splits = omg.learn_splits(sample, bits=bits, epochs=2000)
         learn_ms = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        qsplits = omg.quantile_splits(sample, bits=bits)  # the method without a network
+        quantile_ms = (time.perf_counter() - t0) * 1e3
         per = {}
         chosen = {}
         gpu_fp = {}
         for name, strat in (("direct", omg.JOIN_DIRECT), ("hash_partitioned", omg.JOIN_HASH_PARTITIONED),
                             ("learned_range_partitioned", omg.JOIN_RANGE_PARTITIONED),
-                            ("learned_choice", omg.JOIN_LEARNED)):
+                            ("learned_choice", omg.JOIN_LEARNED), ("quantile_choice", omg.JOIN_QUANTILE)):
             def step(fp=False):
                 op = pf.create_operator()
                 op.set_stream(stream.cuda_stream)
                 op.set_device_output(True)
                 op.set_join_strategy(strat, bits,
-                                     splits if strat in (omg.JOIN_RANGE_PARTITIONED, omg.JOIN_LEARNED) else None)
+                                     splits if strat in (omg.JOIN_RANGE_PARTITIONED, omg.JOIN_LEARNED) else
+                                     (qsplits if strat == omg.JOIN_QUANTILE else None))
                 chosen[name] = op.join_strategy()
                 op.add_input(omg.wrap_device_batch([L], npb, [pkey.data_ptr()]))
                 outs, rows = op.get_outputs(1 << 20)
@@ -1303,7 +1307,7 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         per["cpu_baseline"] = {"value": npb / osecs, "unit": "rows/s", "cores": host_threads(), "kind": "port",
                                "sample": f"all {npb} probe rows against the 2^26-row build, "
                                          f"{host_threads()} threads, output rows hashed (not materialised)"}
-        best = min(("direct", "hash_partitioned", "learned_range_partitioned", "learned_choice"),
+        best = min(("direct", "hash_partitioned", "learned_range_partitioned", "learned_choice", "quantile_choice"),
                    key=lambda k: per[k]["device_ms"])
         alg = npb * 8 + per["direct"]["output_rows"] * 24
         dev_s = per["learned_choice"]["device_ms"] / 1e3
@@ -1315,7 +1319,13 @@ def run_join_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         top = float(cdf_top_share(torch, nb, s, dev))
         per["learned_choice"]["strategy"] = {0: "direct", 1: "hash_partitioned", 2: "range_partitioned"}[
             chosen["learned_choice"]]
+        per["quantile_choice"]["strategy"] = {0: "direct", 1: "hash_partitioned", 2: "range_partitioned"}[
+            chosen["quantile_choice"]]
         per["splits_learn_ms"] = round(learn_ms, 1)
+        per["splits_quantile_ms"] = round(quantile_ms, 2)
+        # One query pays its split learning: the learned choice's time with it included.
+        per["learned_choice"]["ms_incl_learning"] = round(per["learned_choice"]["ms_per_step"] + learn_ms, 1)
+        per["quantile_choice"]["ms_incl_splits"] = round(per["quantile_choice"]["ms_per_step"] + quantile_ms, 2)
         per["top_key_share"] = round(top, 4)
         out[f"s={s}"] = per
         del pkey
@@ -1605,8 +1615,8 @@ def summary(line):
                 v = j[sk]
                 d[sk] = [v["direct"]["ms_per_step"], v["hash_partitioned"]["ms_per_step"],
                          v["learned_range_partitioned"]["ms_per_step"], v["learned_choice"]["ms_per_step"],
-                         v["roofline"]["frac"]]
-        out["cfg5_join_ms_direct_hash_range_choice_frac"] = d
+                         v["quantile_choice"]["ms_per_step"], v["roofline"]["frac"]]
+        out["cfg5_join_ms_direct_hash_range_learned_quantile_frac"] = d
         out["cfg5_cpu_rows_s"] = _sig(j["s=1.1"]["cpu_baseline"]["value"]) if "s=1.1" in j else None
         out["cfg5_oracle_match"] = j.get("oracle_match")
     return out

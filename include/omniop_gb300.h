@@ -346,6 +346,10 @@ int32_t omg_agg_batch_destroy(void *batch);
  * direct probe, which keeps such hot keys in cache; otherwise the hash-partitioned probe with
  * 2^bits partitions. */
 #define OMG_JOIN_LEARNED 3
+/* OMG_JOIN_QUANTILE: the same choice from exact sample quantiles (omg_join_quantile_splits): a
+ * run of equal splits longer than 15% of the partitions selects the direct probe.  No reference
+ * counterpart. */
+#define OMG_JOIN_QUANTILE 4
 int32_t omg_op_set_join_strategy(void *op, int32_t strategy, int32_t bits, const int64_t *splits, int32_t n_splits);
 /* The strategy in effect (OMG_JOIN_LEARNED resolved to the one it chose). */
 int32_t omg_op_join_strategy(void *op, int32_t *strategy);
@@ -354,6 +358,9 @@ int32_t omg_op_join_strategy(void *op, int32_t *strategy);
  * crossings.  Writes 2^bits - 1 sorted splits to `splits`. */
 int32_t omg_join_learn_splits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed,
     int64_t *splits);
+/* Exact sample quantiles as range splits: split k is the sorted sample's key at rank
+ * floor(k * n / 2^bits); writes 2^bits - 1 sorted splits.  No reference counterpart. */
+int32_t omg_join_quantile_splits(const int64_t *sample, int64_t n, int32_t bits, int64_t *splits);
 /* Order-independent fingerprint of the rows of n batches (host or device, same column
  * layout): out[0] = rows, out[1], out[2] = two 64-bit sums of per-row hashes over all columns
  * (NULLs included).  Equal row multisets give equal fingerprints (no reference counterpart;

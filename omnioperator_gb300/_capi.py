@@ -101,6 +101,7 @@ _SIGS = {
     "omg_op_join_strategy": (I32, [P, C.POINTER(I32)]),
     "omg_batches_fingerprint": (I32, [C.POINTER(P), I32, C.POINTER(C.c_uint64)]),
     "omg_join_learn_splits": (I32, [C.POINTER(I64), I64, I32, I32, C.c_uint64, C.POINTER(I64)]),
+    "omg_join_quantile_splits": (I32, [C.POINTER(I64), I64, I32, C.POINTER(I64)]),
     "omg_op_status": (I32, [P]),
     "omg_op_no_more_input": (I32, [P]),
     "omg_op_set_no_more_input": (I32, [P, I32]),

@@ -661,7 +661,16 @@ class AggBatch:
             self.handle = None
 
 
-JOIN_DIRECT, JOIN_HASH_PARTITIONED, JOIN_RANGE_PARTITIONED, JOIN_LEARNED = 0, 1, 2, 3
+JOIN_DIRECT, JOIN_HASH_PARTITIONED, JOIN_RANGE_PARTITIONED, JOIN_LEARNED, JOIN_QUANTILE = 0, 1, 2, 3, 4
+
+
+def quantile_splits(sample, bits: int = 12) -> np.ndarray:
+    """2^bits - 1 range splits from the exact quantiles of a sample of probe keys (no network)."""
+    a = np.ascontiguousarray(sample, dtype=np.int64)
+    out = np.zeros((1 << bits) - 1, dtype=np.int64)
+    check(lib().omg_join_quantile_splits(a.ctypes.data_as(C.POINTER(C.c_int64)), len(a), bits,
+                                         out.ctypes.data_as(C.POINTER(C.c_int64))))
+    return out
 
 
 def learn_splits(sample, bits: int = 12, epochs: int = 2000, seed: int = 1) -> np.ndarray:

@@ -812,6 +812,14 @@ int32_t omg_join_learn_splits(const int64_t *sample, int64_t n, int32_t bits, in
     });
 }
 
+int32_t omg_join_quantile_splits(const int64_t *sample, int64_t n, int32_t bits, int64_t *splits)
+{
+    return Guard([&] {
+        Require(sample != nullptr && splits != nullptr, "null array");
+        omg::QuantileSplits(sample, n, bits, splits);
+    });
+}
+
 int32_t omg_batches_fingerprint(void *const *batches, int32_t n, uint64_t *out)
 {
     return Guard([&] {

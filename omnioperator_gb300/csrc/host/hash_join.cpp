@@ -1186,11 +1186,12 @@ void LookupJoinOperator::SetJoinStrategy(int32_t strategy, int32_t bits, const i
         strategy_ = kJoinDirect;
         return;
     }
-    if ((strategy != kJoinHashPartitioned && strategy != kJoinRangePartitioned && strategy != kJoinLearned) ||
+    if ((strategy != kJoinHashPartitioned && strategy != kJoinRangePartitioned && strategy != kJoinLearned &&
+            strategy != kJoinQuantile) ||
         bits < 1 || (1 << bits) > omg::kMaxJoinParts) {
         throw OmniException("INVALID_ARGUMENT", "join strategy: unknown strategy or bits outside [1, 12]", -1);
     }
-    if (strategy == kJoinRangePartitioned || strategy == kJoinLearned) {
+    if (strategy == kJoinRangePartitioned || strategy == kJoinLearned || strategy == kJoinQuantile) {
         if (splits == nullptr || nSplits != (1 << bits) - 1) {
             throw OmniException("INVALID_ARGUMENT", "range partitioning needs 2^bits - 1 splits", -1);
         }
@@ -1205,8 +1206,9 @@ void LookupJoinOperator::SetJoinStrategy(int32_t strategy, int32_t bits, const i
     }
     strategy_ = strategy;
     partBits_ = bits;
-    if (strategy == kJoinLearned) {
-        // Splits are learned quantiles of the probe keys: a hot key repeats as a run of equal splits.
+    if (strategy == kJoinLearned || strategy == kJoinQuantile) {
+        // Splits are (learned or exact) quantiles of the probe keys: a hot key repeats as a run of
+        // equal splits.
         int32_t run = 1;
         int32_t longest = 1;
         for (int32_t i = 1; i < nSplits; ++i) {
@@ -1214,7 +1216,8 @@ void LookupJoinOperator::SetJoinStrategy(int32_t strategy, int32_t bits, const i
             longest = std::max(longest, run);
         }
         const double runShare = static_cast<double>(longest) / static_cast<double>(1 << bits);
-        strategy_ = runShare > kLearnedDirectRun ? kJoinDirect : kJoinHashPartitioned;
+        const double threshold = strategy == kJoinLearned ? kLearnedDirectRun : kQuantileDirectRun;
+        strategy_ = runShare > threshold ? kJoinDirect : kJoinHashPartitioned;
     }
 }
 

@@ -293,6 +293,19 @@ float SizingModel::Train(const float *X, const float *T, int32_t n, int32_t epoc
     return loss;
 }
 
+void QuantileSplits(const int64_t *sample, int64_t n, int32_t bits, int64_t *splits)
+{
+    if (n <= 0 || bits < 1 || bits > 12) {
+        throw OmniException("INVALID_ARGUMENT", "quantile splits need a sample and 1 <= bits <= 12", -1);
+    }
+    std::vector<int64_t> keys(sample, sample + n);
+    std::sort(keys.begin(), keys.end());
+    const int64_t P = int64_t(1) << bits;
+    for (int64_t k = 1; k < P; ++k) {
+        splits[k - 1] = keys[std::min<int64_t>(n - 1, (k * n) / P)];
+    }
+}
+
 void LearnRangeSplits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed, int64_t *splits)
 {
     if (n <= 0 || bits < 1 || bits > 12) {

@@ -34,6 +34,9 @@ float SizerTarget(const int64_t *log, int64_t groups);
 // its keys.  Split i (1 <= i < 2^bits) is the first sample key whose predicted CDF reaches
 // i / 2^bits (predictions made monotone by a running maximum).  Writes 2^bits - 1 sorted splits.
 void LearnRangeSplits(const int64_t *sample, int64_t n, int32_t bits, int32_t epochs, uint64_t seed, int64_t *splits);
+// Exact sample quantiles as 2^bits - 1 range splits: split k is the sorted sample's key at rank
+// floor(k * n / 2^bits) (the method without a network, for comparison with the learned splits).
+void QuantileSplits(const int64_t *sample, int64_t n, int32_t bits, int64_t *splits);
 
 class SizingModel {
 public:

@@ -43,6 +43,11 @@ constexpr int32_t kJoinRangePartitioned = 2; // 2^bits key ranges per side, from
 // cold partitions hold most build keys.
 constexpr int32_t kJoinLearned = 3;
 constexpr double kLearnedDirectRun = 0.075;
+// Quantile: the same choice from exact sample quantiles (no network), where a key holding a share
+// q of the rows repeats as about q * 2^bits splits: a run longer than kQuantileDirectRun (a key
+// with about 15% of the probe rows, as for the learned rule) selects the direct probe.
+constexpr int32_t kJoinQuantile = 4;
+constexpr double kQuantileDirectRun = 0.15;
 
 class HashBuilderOperatorFactory : public OperatorFactory {
 public:

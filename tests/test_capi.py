@@ -309,3 +309,26 @@ def test_learned_join_strategy_choice():
     op.delete()
     pf.close()
     bf.close()
+
+
+def test_quantile_join_strategy_choice():
+    """JOIN_QUANTILE takes the choice from exact sample quantiles (no network): a key holding a
+    share q of the sample repeats as about q * 2^bits splits, and a run longer than 15% of the
+    partitions selects the direct probe."""
+    rng = np.random.default_rng(3)
+    L = omg.LongType()
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L], [0])
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1], [L], bf)
+    op = pf.create_operator()
+    for share, want in ((0.30, omg.JOIN_DIRECT), (0.05, omg.JOIN_HASH_PARTITIONED)):
+        sample = rng.integers(0, 2**40, 65536).astype(np.int64)
+        sample[: int(share * len(sample))] = 12345
+        splits = omg.quantile_splits(sample, bits=8)
+        assert np.all(np.diff(splits) >= 0)
+        ranks = np.searchsorted(np.sort(sample), splits, side="left")
+        assert np.all(np.abs(ranks - np.arange(1, 256) * len(sample) // 256) <= share * len(sample) + 1)
+        op.set_join_strategy(omg.JOIN_QUANTILE, 8, splits)
+        assert op.join_strategy() == want
+    op.delete()
+    pf.close()
+    bf.close()

@@ -143,3 +143,28 @@ def test_fingerprint_is_order_independent_and_sensitive(gpu):
     assert fx == fy and fx[0] == 100_000
     assert fz[0] == fx[0] and fz[1:] != fx[1:]
     omg.free_batches(x + y + z)
+
+
+@pytest.mark.parametrize("s", [0.9, 1.1, 1.3])
+def test_quantile_choice_matches_learned_choice(gpu, s):
+    """The strategy read off exact sample quantiles equals the one read off the learned splits
+    (what the network adds to this decision: nothing), and both probes give the oracle's rows."""
+    data = _skewed(8, 100_000, 400_000, s=s)
+    pkey, pnull = data[3], data[4]
+    sample = pkey[~pnull][:: max(1, len(pkey) // 65536)]
+    learned = omg.learn_splits(sample, bits=10, epochs=1000)
+    quantile = omg.quantile_splits(sample, bits=10)
+    got_l, _ = _join(*data, strategy=omg.JOIN_LEARNED, bits=10, splits=learned)
+    got_q, _ = _join(*data, strategy=omg.JOIN_QUANTILE, bits=10, splits=quantile)
+    assert got_l == got_q == _expected(*data)
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L], [0])
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1], [L], bf)
+    op = pf.create_operator()
+    op.set_join_strategy(omg.JOIN_LEARNED, 10, learned)
+    chose_l = op.join_strategy()
+    op.set_join_strategy(omg.JOIN_QUANTILE, 10, quantile)
+    chose_q = op.join_strategy()
+    op.delete()
+    pf.close()
+    bf.close()
+    assert chose_l == chose_q
