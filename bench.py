@@ -897,7 +897,52 @@ def run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank):
     h2d = N_PROBE * 8 + N_PROBE // 8
     d2h = expected * 16 + 3 * ((expected + 31) // 32 * 4)
     return {"value": whole_job_rate(world, N_PROBE * args.steps, t), "unit": "rows/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps, "oracle_match": check["oracle_match"]}
+            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps, "oracle_match": check["oracle_match"],
+            "link": link_ceiling(torch, h2d, d2h, t / args.steps)}
+
+
+def link_ceiling(torch, h2d, d2h, step_s):
+    """The CPU-GPU link's measured copy rates (1 GiB pinned <-> HBM, cudaMemcpyAsync, best of 5:
+    each direction alone and both at once on two streams) and the e2e step's time against the
+    time its host<->device bytes need at those rates (the link roofline of the e2e path)."""
+    n = 1 << 30
+    host = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    dev = torch.empty(n, dtype=torch.uint8, device="cuda")
+    host2 = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    dev2 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def best(fn):
+        times = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            torch.cuda.synchronize()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        return min(times)
+
+    def both():
+        with torch.cuda.stream(s1):
+            dev.copy_(host, non_blocking=True)
+        with torch.cuda.stream(s2):
+            host2.copy_(dev2, non_blocking=True)
+        torch.cuda.current_stream().wait_stream(s1)
+        torch.cuda.current_stream().wait_stream(s2)
+
+    h2d_s = best(lambda: dev.copy_(host, non_blocking=True))
+    d2h_s = best(lambda: host.copy_(dev, non_blocking=True))
+    dup_s = best(both)
+    h2d_gbs, d2h_gbs, dup_gbs = n / h2d_s / 1e9, n / d2h_s / 1e9, 2 * n / dup_s / 1e9
+    # The step's bytes at the link's rates: each direction at its own rate, and the two together at
+    # the duplex rate; the slower bound is the floor for this step.
+    floor_s = max(h2d / (h2d_gbs * 1e9), d2h / (d2h_gbs * 1e9), (h2d + d2h) / (dup_gbs * 1e9))
+    del host, dev, host2, dev2
+    return {"h2d_gbs": round(h2d_gbs, 1), "d2h_gbs": round(d2h_gbs, 1), "duplex_gbs": round(dup_gbs, 1),
+            "step_floor_ms": round(floor_s * 1e3, 3), "frac_of_link": round(floor_s / step_s, 3)}
 
 
 def run_agg(args, omg, torch, dev, stream, barrier, max_over_ranks, world):
@@ -1584,7 +1629,8 @@ def summary(line):
     cpu = line.get("cpu_baseline") or {}
     out["cfg2_probe"] = {"rows_s": _sig(line["value"]), "ms": _sig(line["ms_per_step"]),
                          "frac": (line.get("roofline") or {}).get("frac"), "e2e_rows_s": _sig(e2e.get("value")),
-                         "e2e_ms": _sig(e2e.get("ms_per_step")), "cpu_rows_s": _sig(cpu.get("value")),
+                         "e2e_ms": _sig(e2e.get("ms_per_step")), "e2e_link_frac": (e2e.get("link") or {}).get("frac_of_link"),
+                         "cpu_rows_s": _sig(cpu.get("value")),
                          "oracle_match": line.get("oracle_match"), "e2e_oracle_match": e2e.get("oracle_match")}
     a = line.get("agg")
     if a:
