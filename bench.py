@@ -1101,6 +1101,8 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
         op = fac.create_operator()
         if hint.get("groups"):
             op.set_agg_strategy(omg.AGG_STRATEGY_AUTO, hint["groups"])
+        if hint.get("hll"):
+            op.set_agg_sizing(omg.AGG_SIZING_HLL)
         op.set_stream(stream.cuda_stream)
         op.set_device_output(True)
         op.add_input(omg.wrap_device_batch([I, L, d64, D], n, [k1.data_ptr(), k2.data_ptr(), dec.data_ptr(),
@@ -1115,11 +1117,16 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
 
     steps = max(1, min(args.steps, 3))
     res = {}
-    # exact_count: the true group count given as the capacity hint (the best any estimate can do).
-    for arm in ("plain", "learned", "exact_count"):
+    # exact_count: the true group count given as the capacity hint (the best any estimate can do);
+    # hll: a HyperLogLog sketch of every row's key (a distinct-count sketch, the competent
+    # non-learned estimate; its extra pass over the keys is inside the timed step).
+    for arm in ("plain", "learned", "hll", "exact_count"):
         fac = factory(arm)
+        hint.clear()
         if arm == "exact_count":
             hint["groups"] = res["plain"]["groups"]
+        if arm == "hll":
+            hint["hll"] = True
         step(fac)  # warm-up
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1135,7 +1142,7 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
                     "groups": groups, "estimate": slog["estimate"], "plain_estimate": slog["plain_estimate"],
                     "table_resizes": c["resizes"], "retried_rows": c["retried_rows"],
                     "shared_front_table": slog["smem_front"], "part_bits": slog["part_bits"]}
-    assert res["plain"]["groups"] == res["learned"]["groups"] == res["exact_count"]["groups"]
+    assert res["plain"]["groups"] == res["learned"]["groups"] == res["exact_count"]["groups"] == res["hll"]["groups"]
     # Roofline of the aggregation kernel (the learned arm's launches): 28.25 B read per row
     # (4 + 8 + 8 + 8 B and two validity bits), 45 B written per group.
     groups = res["learned"]["groups"]
@@ -1183,9 +1190,10 @@ def run_agg_skewed(args, omg, torch, dev, stream, barrier, max_over_ranks, world
                                   gpu_cols, groups)
     check["scope"] = "all rows" if sel is None else "rows of the groups with k2 mod 8 == 0 (host memory)"
     return {"workload": SKEW_WORKLOAD if n == SKEW_ROWS else SKEW_WORKLOAD.replace("2^28", f"2^{n.bit_length() - 1}"),
-            "steps": steps, "sizer": model_src, "plain": res["plain"], "learned": res["learned"],
+            "steps": steps, "sizer": model_src, "plain": res["plain"], "learned": res["learned"], "hll": res["hll"],
             "exact_count": res["exact_count"],
             "learned_over_plain": round(res["learned"]["value"] / res["plain"]["value"], 3),
+            "learned_over_hll": round(res["learned"]["value"] / res["hll"]["value"], 3),
             "roofline": roofline, "cpu_baseline": cpu, "oracle_check": check, "oracle_match": check["oracle_match"]}
 
 
@@ -1641,6 +1649,7 @@ def summary(line):
     k = line.get("agg_skewed")
     if k:
         out["cfg3_skew"] = {"plain_ms": k["plain"]["ms_per_step"], "learned_ms": k["learned"]["ms_per_step"],
+                            "hll_ms": k["hll"]["ms_per_step"],
                             "exact_count_ms": k["exact_count"]["ms_per_step"],
                             "learned_over_plain": k["learned_over_plain"], "frac": k["roofline"]["frac"],
                             "cpu_rows_s": _sig(k["cpu_baseline"]["value"]), "oracle_match": k.get("oracle_match")}

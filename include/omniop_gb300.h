@@ -393,6 +393,14 @@ int32_t omg_op_set_stream(void *op, void *stream);
 int32_t omg_op_set_device_output(void *op, int32_t on);
 /* Aggregation: strategy hint and initial global-table capacity (groups); 0 = automatic. */
 int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hint);
+/* How an aggregation operator estimates its group count when no capacity hint is given
+ * (no reference counterpart): OMG_AGG_SIZING_SAMPLE (default) -- the key sketch of a 65,536-row
+ * sample, with the factory's sizing model when one is set; OMG_AGG_SIZING_HLL -- a HyperLogLog
+ * sketch (2^14 registers) of every row's key, one extra pass over the keys.  Results never
+ * depend on it. */
+#define OMG_AGG_SIZING_SAMPLE 0
+#define OMG_AGG_SIZING_HLL 1
+int32_t omg_op_set_agg_sizing(void *op, int32_t mode);
 /* Aggregation spill (SpillConfig, core/src/operator/config/operator_config.h:28-100): with
  * enabled != 0 the operator stages its input until GetOutput and, when the estimated group table
  * would exceed device_budget_bytes, hash-partitions the rows into pinned host memory and

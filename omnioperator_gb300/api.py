@@ -33,6 +33,7 @@ OMNI_STATUS_NORMAL, OMNI_STATUS_FINISHED, OMNI_STATUS_ERROR = 0, 1, -1
 # SupportContainerVecRule (util/policy.h:160-167)
 POLICY_SPARK, POLICY_GENERIC = 0, 1
 AGG_STRATEGY_AUTO, AGG_STRATEGY_SMEM, AGG_STRATEGY_GLOBAL, AGG_STRATEGY_PARTITIONED = 0, 1, 2, 3
+AGG_SIZING_SAMPLE, AGG_SIZING_HLL = 0, 1
 
 _NP = {OMNI_INT: np.int32, OMNI_LONG: np.int64, OMNI_DOUBLE: np.float64, OMNI_BOOLEAN: np.int8,
        OMNI_SHORT: np.int16, OMNI_DECIMAL64: np.int64, OMNI_DATE32: np.int32, OMNI_DATE64: np.int64,
@@ -396,6 +397,11 @@ class Operator:
 
     def set_agg_strategy(self, strategy: int, capacity_hint: int = 0):
         check(lib().omg_op_set_agg_strategy(self.handle, strategy, capacity_hint))
+
+    def set_agg_sizing(self, mode: int):
+        """AGG_SIZING_SAMPLE (row-sample key sketch, default) or AGG_SIZING_HLL (HyperLogLog of
+        every row's key) for the group-count estimate."""
+        check(lib().omg_op_set_agg_sizing(self.handle, mode))
 
     def set_spill(self, enabled: bool, device_budget_bytes: int = 0):
         """Aggregation spill to pinned host memory above a device-memory budget."""

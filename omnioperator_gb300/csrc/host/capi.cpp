@@ -957,6 +957,16 @@ int32_t omg_op_set_agg_strategy(void *op, int32_t strategy, int64_t capacity_hin
     });
 }
 
+int32_t omg_op_set_agg_sizing(void *op, int32_t mode)
+{
+    return Guard([&] {
+        auto *a = dynamic_cast<HashAggregationOperator *>(AsOp(op));
+        Require(a != nullptr, "not a hash aggregation operator");
+        Require(mode == OMG_AGG_SIZING_SAMPLE || mode == OMG_AGG_SIZING_HLL, "unknown sizing mode");
+        a->SetSizing(mode);
+    });
+}
+
 int32_t omg_op_set_spill(void *op, int32_t enabled, int64_t device_budget_bytes)
 {
     return Guard([&] {

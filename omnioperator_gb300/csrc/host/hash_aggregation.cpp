@@ -994,6 +994,22 @@ void HashAggregationOperator::Decide(omg::BatchTable &bt, cudaStream_t s)
     const int64_t rows = bt.TotalRows();
     if (capacityHint_ > 0) {
         im.estimate = static_cast<uint64_t>(capacityHint_);  // the caller's (or a sizing model's) estimate
+    } else if (sizing_ == 1 && rows > 0 && (strategy_ == 0 || strategy_ == 3)) {
+        // HyperLogLog over every row's key: one pass over the keys, ~0.8% standard error.
+        DevArray<unsigned int> regs(omg::kHllRegs + 2, s);
+        omg::AggLaunch p = MakeLaunch(plan_, nullptr, 0, nullptr, nullptr);
+        p.batches = bt.DeviceBatches();
+        p.tiles = bt.DeviceTiles();
+        p.nTiles = bt.NumTiles();
+        CudaCheck(omg::LaunchAggHll(p, regs.Get(), s), "HyperLogLog sketch");
+        ++counters_[0];
+        std::vector<unsigned int> h(omg::kHllRegs + 2);
+        CudaCheck(cudaMemcpyAsync(h.data(), regs.Get(), h.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, s),
+            "read HyperLogLog registers");
+        im.stream.Sync();
+        im.sketchRows = rows;
+        im.plainEstimate = omg::HllGroupEstimate(h.data(), rows);
+        im.estimate = im.plainEstimate;
     } else if (rows >= kSketchMinRows && (strategy_ == 0 || strategy_ == 3)) {
         DevArray<unsigned long long> tabKeys(omg::kSketchCap, s);
         DevArray<unsigned int> tabCounts(omg::kSketchCap, s);

@@ -39,6 +39,25 @@ struct SplitMix {
 };
 }  // namespace
 
+uint64_t HllGroupEstimate(const unsigned int *regs, int64_t rows)
+{
+    const double m = static_cast<double>(kHllRegs);
+    double z = 0.0;
+    int64_t zeros = 0;
+    for (int i = 0; i < kHllRegs; ++i) {
+        z += std::ldexp(1.0, -static_cast<int>(regs[i]));
+        zeros += regs[i] == 0 ? 1 : 0;
+    }
+    const double alpha = 0.7213 / (1.0 + 1.079 / m);
+    double e = alpha * m * m / z;
+    if (e <= 2.5 * m && zeros > 0) {
+        e = m * std::log(m / static_cast<double>(zeros));
+    }
+    e += static_cast<double>(regs[kHllRegs] + regs[kHllRegs + 1]);
+    const double capped = std::min(std::max(e, 1.0), static_cast<double>(std::max<int64_t>(rows, 1)));
+    return static_cast<uint64_t>(std::llround(capped));
+}
+
 uint64_t PlainGroupEstimate(const unsigned long long *st, int64_t total)
 {
     const double n = static_cast<double>(st[0] - st[1]);

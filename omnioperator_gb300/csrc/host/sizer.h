@@ -17,6 +17,10 @@ namespace omg {
 // `rows`: the GEE estimator sqrt(rows / n) * f1 + (d - f1), clamped to [d, rows], plus the
 // special groups the sample saw.
 uint64_t PlainGroupEstimate(const unsigned long long *sketch, int64_t rows);
+// HyperLogLog estimate from 2^kHllBits registers plus the two special-key flags (Flajolet et
+// al. 2007: alpha_m m^2 / sum 2^-M[j], with linear counting m ln(m / V) below 2.5 m when V
+// registers are zero); at most `rows`.
+uint64_t HllGroupEstimate(const unsigned int *regs, int64_t rows);
 
 // Features of a sizing record (the layout written by HashAggregationOperator::GetSizingLog):
 // scale-free functions of the rows N, the sampled rows n, the distinct hashes d of the sample,

@@ -2414,6 +2414,53 @@ cudaError_t LaunchAggSketch(const AggLaunch &p, int32_t nSample, unsigned long l
     return cudaGetLastError();
 }
 
+// One CTA's registers in shared memory, merged into the global ones with atomicMax.
+template <int kKind>
+__global__ void __launch_bounds__(512) HllKernel(const __grid_constant__ AggLaunch p, unsigned int *regs)
+{
+    __shared__ unsigned int r[kHllRegs + 2];
+    for (int i = threadIdx.x; i < kHllRegs + 2; i += blockDim.x) {
+        r[i] = 0;
+    }
+    __syncthreads();
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        for (int row = threadIdx.x; row < tile.rows; row += blockDim.x) {
+            const RowKey k = ReadKey(p.key, b, static_cast<int64_t>(tile.row0) + row, kKind);
+            if (k.special >= 0) {
+                r[kHllRegs + k.special] = 1u;
+                continue;
+            }
+            const uint64_t h = Mix64(k.hash ^ 0x5851f42d4c957f2dull);  // bits independent of the table's
+            const unsigned int reg = static_cast<unsigned int>(h >> (64 - kHllBits));
+            const uint64_t rest = (h << kHllBits) | (1ull << (kHllBits - 1));
+            atomicMax(&r[reg], static_cast<unsigned int>(__clzll(static_cast<long long>(rest)) + 1));
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kHllRegs + 2; i += blockDim.x) {
+        if (r[i] != 0) {
+            atomicMax(&regs[i], r[i]);
+        }
+    }
+}
+
+cudaError_t LaunchAggHll(const AggLaunch &p, unsigned int *regs, cudaStream_t stream)
+{
+    cudaError_t err = cudaMemsetAsync(regs, 0, (kHllRegs + 2) * sizeof(unsigned int), stream);
+    if (err != cudaSuccess || p.nTiles <= 0) {
+        return err;
+    }
+    const int grid = p.nTiles < DeviceSMCount() * 2 ? p.nTiles : DeviceSMCount() * 2;
+    if (p.key.kind == KEY_SINGLE) {
+        HllKernel<KEY_SINGLE><<<grid, 512, 0, stream>>>(p, regs);
+    } else {
+        HllKernel<KEY_PACKED><<<grid, 512, 0, stream>>>(p, regs);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t LaunchAlignColumn(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles,
     const int64_t *tileOutRow, const AlignCol &c, void *out, uint8_t *outNulls, cudaStream_t stream)
 {

@@ -31,6 +31,8 @@ cudaError_t LaunchAggPartition(const AggLaunch &p, const PartArgs &a, cudaStream
 // tabKeys / tabCounts hold kSketchCap entries.
 cudaError_t LaunchAggSketch(const AggLaunch &p, int32_t nSample, unsigned long long *tabKeys,
     unsigned int *tabCounts, unsigned long long *stats, cudaStream_t stream);
+// HyperLogLog registers over every row of p's tiles into regs[kHllRegs + 2] (zeroed here).
+cudaError_t LaunchAggHll(const AggLaunch &p, unsigned int *regs, cudaStream_t stream);
 // Batched tasks: per-task sketch (kSketchStats per task), the persistent aggregation over all
 // tasks' tiles (autotuned threads per CTA and grid), per-task group counts and extraction at
 // per-task output offsets.

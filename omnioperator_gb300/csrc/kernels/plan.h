@@ -221,6 +221,13 @@ constexpr int kSketchStats = 16;
 // [3] f1 (hashes seen once), [4] f2, [5] f3, [6] hashes seen 4-7 times, [7] 8+ times,
 // [8] largest count, [9] rows held by hashes seen 8+ times.
 
+// HyperLogLog sketch of every row's key (the distinct-count sizing baseline): 2^kHllBits
+// registers; register = top kHllBits bits of the key hash, value = the position of the first set
+// bit of the remaining bits (1-based).  regs[kHllRegs] and regs[kHllRegs + 1] flag the NULL key and
+// the EMPTY-sentinel key, which are groups of their own.
+constexpr int kHllBits = 14;
+constexpr int kHllRegs = 1 << kHllBits;
+
 // Default bounded-wait budget (clock64 ticks, about two seconds at 2 GHz).
 constexpr long long kDefaultWaitBudget = 1ll << 32;
 

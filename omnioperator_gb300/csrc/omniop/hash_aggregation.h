@@ -128,6 +128,9 @@ public:
         strategy_ = strategy;
         capacityHint_ = capacityHint;
     }
+    // How the group count is estimated when no capacity hint is given: 0 = the key sketch of a row
+    // sample (and the factory's sizing model, if any); 1 = a HyperLogLog sketch of every row's key.
+    void SetSizing(int32_t mode) { sizing_ = mode; }
 
     // Sizing record of the first flush: [0] rows flushed, [1..kSketchStats] the key sketch of a
     // row sample, then the group estimate used, the partition bits (-1 = global table), the
@@ -158,6 +161,7 @@ private:
     uint64_t uniqueKeys_ = 0;
     int32_t strategy_ = 0;
     int64_t capacityHint_ = 0;
+    int32_t sizing_ = 0;
     bool spillEnabled_ = false;
     uint64_t spillBudget_ = 0;
     uint64_t spilledBytes_ = 0;

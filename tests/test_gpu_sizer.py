@@ -116,3 +116,27 @@ def test_learned_sizing_avoids_resizes_and_stays_exact(gpu):
     assert res[False][2]["estimate"] < 0.5 * groups  # the plain estimate undersizes this workload
     assert res[True][1] < res[False][1], res
     m.close()
+
+
+@pytest.mark.parametrize("groups", [300, 40_000, 1_500_000])
+def test_hll_sizing_estimates_the_group_count(gpu, groups):
+    """The HyperLogLog sizing (every row's key, 2^14 registers) lands within 4% of the true group
+    count on uniform and skewed keys (NULL keys counted as one group), and the result is exact."""
+    rng = np.random.default_rng(groups)
+    n = 1 << 22
+    uniq = rng.integers(-2**62, 2**62, groups, dtype=np.int64)
+    keys = uniq[np.minimum(rng.zipf(1.2, n) - 1, groups - 1)] if groups > 1000 else uniq[rng.integers(0, groups, n)]
+    nulls = rng.random(n) < 0.001
+    true = len(np.unique(keys[~nulls])) + 1
+    fac = omg.HashAggregationOperatorFactory([0], [L], [[]], [[]], [[L]], [omg.OMNI_AGGREGATION_TYPE_COUNT_ALL])
+    op = fac.create_operator()
+    op.set_agg_sizing(omg.AGG_SIZING_HLL)
+    op.add_input(omg.make_batch([L], [keys], [nulls]))
+    outs = op.drain()
+    got = sum(omg.batch_row_count(b) for b in outs)
+    omg.free_batches(outs)
+    est = op.sizing_log()["estimate"]
+    op.delete()
+    fac.close()
+    assert got == true
+    assert abs(est - true) <= 0.04 * true + 2, (est, true)
