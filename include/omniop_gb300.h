@@ -410,7 +410,9 @@ int32_t omg_op_set_spill(void *op, int32_t enabled, int64_t device_budget_bytes)
 /* Operator::GetSpilledBytes (core/src/operator/operator.h:66): bytes moved to host memory. */
 int64_t omg_op_spilled_bytes(void *op);
 /* Counters of the last run: [0]=kernel launches, [1]=table resizes, [2]=retried rows,
- * [3]=groups, [4]=ordered-fallback groups, [5]=output rows. */
+ * [3]=groups, [4]=ordered-fallback groups, [5]=output rows, [6]=kernel ns, [7]=timed kernel
+ * launches; LookupJoin host time: [8]=ns setting up and launching probe calls, [9]=ns waiting
+ * for their kernels, [10]=ns carving output batches, [11]=ns freeing probe input batches. */
 int32_t omg_op_get_counters(void *op, int64_t *out, int32_t n);
 
 /* ---- allocation-free aggregation (no counterpart in the reference) ----------------------

@@ -411,10 +411,11 @@ class Operator:
         return lib().omg_op_spilled_bytes(self.handle)
 
     def counters(self):
-        arr = (C.c_int64 * 8)()
-        check(lib().omg_op_get_counters(self.handle, arr, 8))
+        arr = (C.c_int64 * 12)()
+        check(lib().omg_op_get_counters(self.handle, arr, 12))
         return {"launches": arr[0], "resizes": arr[1], "retried_rows": arr[2], "groups": arr[3],
-                "ordered_groups": arr[4], "output_rows": arr[5], "kernel_ns": arr[6], "kernel_launches": arr[7]}
+                "ordered_groups": arr[4], "output_rows": arr[5], "kernel_ns": arr[6], "kernel_launches": arr[7],
+                "launch_host_ns": arr[8], "wait_ns": arr[9], "carve_ns": arr[10], "free_input_ns": arr[11]}
 
     def close(self):
         check(lib().omg_op_close(self.handle))

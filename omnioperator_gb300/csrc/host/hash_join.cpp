@@ -1,6 +1,8 @@
 // HashBuilder / LookupJoin operators (see omniop/hash_join.h).
 #include "omniop/hash_join.h"
 
+#include <chrono>
+
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -722,7 +724,9 @@ int32_t LookupJoinOperator::AddInput(VectorBatch *vecBatch)
     // caller queues the next chunk and GetOutput carves the previous one.
     if (!noMoreInput_ && pendingRows_ >= kProbeChunkRows && strategy_ == kJoinDirect && f_.build->built &&
         impl_->inflight.size() < 2) {
+        const auto t0 = std::chrono::steady_clock::now();
         impl_->inflight.push_back(LaunchPending());
+        counters_[8] += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
     }
     return 0;
 }
@@ -968,7 +972,9 @@ void LookupJoinOperator::FinishProbe(ProbeCall &pc)
     const bool hostDirect = pc.hostDirect;
     std::vector<int64_t> regionCount(nRegions, 0);
     for (int attempt = 0; attempt < 2; ++attempt) {
+        const auto tw = std::chrono::steady_clock::now();
         CudaCheck(cudaEventSynchronize(pc.done), "probe kernel");
+        counters_[9] += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - tw).count();
         counters_[6] += pc.timer.ElapsedNs();
         ++counters_[7];
         uint64_t most = 0;
@@ -1016,6 +1022,7 @@ void LookupJoinOperator::FinishProbe(ProbeCall &pc)
         cols[o].dataBytes = total;
     }
     int64_t rows = 0;
+    const auto tc = std::chrono::steady_clock::now();
     for (int32_t r = 0; r < nRegions; ++r) {
         const int64_t n = regionCount[r];
         if (n == 0) {
@@ -1045,10 +1052,13 @@ void LookupJoinOperator::FinishProbe(ProbeCall &pc)
         impl_->stream.Sync();  // the copies to host batches (direct host output was complete at the event)
     }
     counters_[5] += rows;
+    const auto tf = std::chrono::steady_clock::now();
+    counters_[10] += std::chrono::duration_cast<std::chrono::nanoseconds>(tf - tc).count();
     for (auto *pb : pc.batches) {
         vec::VectorHelper::FreeVecBatch(pb);
     }
     pc.batches.clear();
+    counters_[11] += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - tf).count();
 }
 
 

@@ -65,7 +65,11 @@ protected:
     void *userStream_ = nullptr;
     bool userStreamSet_ = false;
     bool deviceOutput_ = false;
-    std::vector<int64_t> counters_ = std::vector<int64_t>(8, 0);
+    // [0] launches, [1] resizes / re-runs, [2] retried rows, [3] groups, [4] ordered groups,
+    // [5] output rows, [6] kernel ns, [7] timed kernel launches, and host time of the probe
+    // pipeline: [8] ns setting up and launching probe calls, [9] ns waiting for their kernels,
+    // [10] ns carving output batches, [11] ns freeing the probe input batches.
+    std::vector<int64_t> counters_ = std::vector<int64_t>(12, 0);
 
 private:
     OmniStatus status_ = OMNI_STATUS_NORMAL;
