@@ -232,13 +232,19 @@ int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_
  * columns first, then build columns).  Binary, unary and is-null nodes take ownership of their
  * children; free the root with omg_expr_free (the factory compiles the tree and keeps no pointer
  * into it).  Operator codes follow expressions::Operator: 0 EQ, 1 NEQ, 2 LT, 3 LTE, 4 GT, 5 GTE,
- * 6 AND, 7 OR, 8 NOT.  The GB300 join runs comparisons, AND, OR, NOT and IS NULL over integer-
- * like and DOUBLE columns and literals; other trees are refused by the factory with
- * OMG_ERR_UNSUPPORTED, as the reference refuses what its code generator cannot compile. */
+ * 6 AND, 7 OR, 8 NOT, 9 ADD, 10 SUB, 11 MUL, 12 DIV, 13 MOD, 14 TRY_ADD, 15 TRY_SUB, 16 TRY_MUL,
+ * 17 TRY_DIV.  The GB300 join runs comparisons, AND, OR, NOT, IS NULL and arithmetic (with the
+ * reference's math-function semantics: integers wrap at the node's INT or LONG width, DIV/MOD by
+ * zero and TRY_* overflow give NULL) over integer-like and DOUBLE columns and literals; other
+ * trees (strings, functions, IN, CASE) are refused by the factory with OMG_ERR_UNSUPPORTED, as the
+ * reference refuses what its code generator cannot compile. */
 int32_t omg_expr_field(int32_t col, const OmgDataType *type, void **out_expr);
 int32_t omg_expr_literal_long(int64_t value, const OmgDataType *type, int32_t is_null, void **out_expr);
 int32_t omg_expr_literal_double(double value, int32_t is_null, void **out_expr);
 int32_t omg_expr_binary(int32_t op, void *left, void *right, void **out_expr);
+/* BinaryExpr with an explicit return type (the reference's BinaryExpr(op, left, right, type)),
+ * for arithmetic nodes (ADD .. TRY_DIV: the result is INT, LONG or DOUBLE). */
+int32_t omg_expr_binary_typed(int32_t op, void *left, void *right, const OmgDataType *type, void **out_expr);
 int32_t omg_expr_unary(int32_t op, void *child, void **out_expr);
 int32_t omg_expr_is_null(void *child, void **out_expr);
 int32_t omg_expr_free(void *expr);

@@ -63,6 +63,7 @@ _SIGS = {
     "omg_expr_literal_long": (I32, [I64, P, I32, C.POINTER(P)]),
     "omg_expr_literal_double": (I32, [C.c_double, I32, C.POINTER(P)]),
     "omg_expr_binary": (I32, [I32, P, P, C.POINTER(P)]),
+    "omg_expr_binary_typed": (I32, [I32, P, P, P, C.POINTER(P)]),
     "omg_expr_unary": (I32, [I32, P, C.POINTER(P)]),
     "omg_expr_is_null": (I32, [P, C.POINTER(P)]),
     "omg_expr_free": (I32, [P]),

@@ -507,6 +507,7 @@ class HashBuilderOperatorFactory(OperatorFactory):
 
 # --------------------------------------------------------------------------- join filter expressions
 EXPR_EQ, EXPR_NEQ, EXPR_LT, EXPR_LTE, EXPR_GT, EXPR_GTE, EXPR_AND, EXPR_OR, EXPR_NOT = range(9)
+EXPR_ADD, EXPR_SUB, EXPR_MUL, EXPR_DIV, EXPR_MOD, EXPR_TRY_ADD, EXPR_TRY_SUB, EXPR_TRY_MUL, EXPR_TRY_DIV = range(9, 18)
 
 
 class Field:
@@ -524,10 +525,11 @@ class Literal:
 
 
 class Binary:
-    """BinaryExpr(op, left, right) with op one of EXPR_EQ .. EXPR_OR."""
+    """BinaryExpr(op, left, right[, dtype]): a comparison / AND / OR (BOOLEAN), or arithmetic
+    (EXPR_ADD .. EXPR_TRY_DIV) whose result type `dtype` is INT, LONG or DOUBLE."""
 
-    def __init__(self, op: int, left, right):
-        self.op, self.left, self.right = op, left, right
+    def __init__(self, op: int, left, right, dtype: DataType | None = None):
+        self.op, self.left, self.right, self.dtype = op, left, right, dtype
 
 
 class Not:
@@ -559,7 +561,8 @@ def _expr_handle(e) -> int:
         except Exception:
             L.omg_expr_free(left)
             raise
-        rc = L.omg_expr_binary(e.op, left, right, C.byref(out))
+        rc = (L.omg_expr_binary(e.op, left, right, C.byref(out)) if e.dtype is None else
+              L.omg_expr_binary_typed(e.op, left, right, _types([e.dtype]), C.byref(out)))
         if rc != 0:
             L.omg_expr_free(left)
             L.omg_expr_free(right)

@@ -422,6 +422,17 @@ int32_t omg_expr_binary(int32_t op, void *left, void *right, void **out_expr)
     });
 }
 
+int32_t omg_expr_binary_typed(int32_t op, void *left, void *right, const OmgDataType *type, void **out_expr)
+{
+    return Guard([&] {
+        Require(left != nullptr && right != nullptr && out_expr != nullptr && type != nullptr && op >= 0 &&
+                op < static_cast<int32_t>(ex::Operator::INVALIDOP),
+            "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(new ex::BinaryExpr(static_cast<ex::Operator>(op),
+            static_cast<ex::Expr *>(left), static_cast<ex::Expr *>(right), ToType(*type)));
+    });
+}
+
 int32_t omg_expr_unary(int32_t op, void *child, void **out_expr)
 {
     return Guard([&] {

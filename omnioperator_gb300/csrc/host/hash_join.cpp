@@ -585,10 +585,31 @@ void CompileFilter(const Expr *e, const DataTypes &probeTypes, const DataTypes &
                 case ExprOp::GTE: op = omg::FOP_GTE; break;
                 case ExprOp::AND: op = omg::FOP_AND; break;
                 case ExprOp::OR: op = omg::FOP_OR; break;
+                case ExprOp::ADD: op = omg::FOP_ADD; break;
+                case ExprOp::SUB: op = omg::FOP_SUB; break;
+                case ExprOp::MUL: op = omg::FOP_MUL; break;
+                case ExprOp::DIV: op = omg::FOP_DIV; break;
+                case ExprOp::MOD: op = omg::FOP_MOD; break;
+                case ExprOp::TRY_ADD: op = omg::FOP_TRY_ADD; break;
+                case ExprOp::TRY_SUB: op = omg::FOP_TRY_SUB; break;
+                case ExprOp::TRY_MUL: op = omg::FOP_TRY_MUL; break;
+                case ExprOp::TRY_DIV: op = omg::FOP_TRY_DIV; break;
                 default: FilterUnsupported("binary operator " + std::to_string(static_cast<int>(b->op)));
             }
             CompileFilter(b->left, probeTypes, buildTypes, code, cols, depth);
             CompileFilter(b->right, probeTypes, buildTypes, code, cols, depth + 1);
+            if (op >= omg::FOP_ADD) {
+                // Arithmetic (the reference's math functions): the node's return type sets the
+                // result width (int32 or int64, which wrap) or double.
+                const DataTypePtr &rt = b->GetReturnType();
+                const int kind = rt ? FilterKind(rt) : -1;
+                const int w = kind == 0 ? rt->ByteWidth() : 8;
+                if (kind < 0 || (kind == 0 && w != 4 && w != 8)) {
+                    FilterUnsupported("arithmetic result of type " + std::to_string(rt ? rt->GetId() : -1));
+                }
+                in.width = static_cast<int16_t>(w);
+                in.dbl = static_cast<int16_t>(kind);
+            }
             emit(op);
             return;
         }

@@ -872,6 +872,79 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
         const bool bn = (bf & kFNull) != 0;
         uint64_t res = 0;
         bool resNull = false;
+        if (op >= FOP_ADD) {
+            resNull = an || bn;
+            if (!resNull) {
+                if (f.dbl) {
+                    const double x = FilterAsDouble(av, af);
+                    const double y = FilterAsDouble(bv, bf);
+                    double r = 0.0;
+                    switch (op) {
+                        case FOP_ADD:
+                        case FOP_TRY_ADD: r = x + y; break;
+                        case FOP_SUB:
+                        case FOP_TRY_SUB: r = x - y; break;
+                        case FOP_MUL:
+                        case FOP_TRY_MUL: r = x * y; break;
+                        case FOP_MOD:
+                            resNull = y == 0.0;
+                            r = resNull ? 0.0 : fmod(x, y);
+                            break;
+                        default:  // FOP_DIV, FOP_TRY_DIV
+                            resNull = y == 0.0;
+                            r = resNull ? 0.0 : x / y;
+                            break;
+                    }
+                    res = static_cast<uint64_t>(__double_as_longlong(r));
+                } else {
+                    const int64_t x = static_cast<int64_t>(av);
+                    const int64_t y = static_cast<int64_t>(bv);
+                    const uint64_t ux = av;
+                    const uint64_t uy = bv;
+                    int64_t r = 0;
+                    bool ovf = false;  // beyond the result width (TRY_* only)
+                    switch (op) {
+                        case FOP_ADD:
+                        case FOP_TRY_ADD:
+                            r = static_cast<int64_t>(ux + uy);
+                            ovf = f.width == 8 ? ((x >= 0) == (y >= 0) && (r >= 0) != (x >= 0))
+                                               : r != static_cast<int32_t>(r);
+                            break;
+                        case FOP_SUB:
+                        case FOP_TRY_SUB:
+                            r = static_cast<int64_t>(ux - uy);
+                            ovf = f.width == 8 ? ((x >= 0) != (y >= 0) && (r >= 0) != (x >= 0))
+                                               : r != static_cast<int32_t>(r);
+                            break;
+                        case FOP_MUL:
+                        case FOP_TRY_MUL:
+                            r = static_cast<int64_t>(ux * uy);
+                            if (f.width == 8) {
+                                ovf = __mul64hi(x, y) != (r >> 63);
+                            } else {
+                                ovf = r != static_cast<int32_t>(r);
+                            }
+                            break;
+                        case FOP_MOD:
+                            resNull = y == 0;
+                            r = resNull ? 0 : (y == -1 ? 0 : x % y);
+                            break;
+                        default:  // FOP_DIV, FOP_TRY_DIV; INT_MIN / -1 wraps
+                            resNull = y == 0;
+                            r = resNull ? 0 : (y == -1 ? static_cast<int64_t>(0ull - ux) : x / y);
+                            break;
+                    }
+                    if (f.width == 4) {
+                        r = static_cast<int32_t>(r);  // wrap at 32 bits
+                    }
+                    resNull = resNull || (ovf && op >= FOP_TRY_ADD && op != FOP_TRY_DIV);
+                    res = static_cast<uint64_t>(r);
+                }
+            }
+            v[sp - 1] = resNull ? 0ull : res;
+            fl[sp - 1] = (resNull ? kFNull : 0u) | (f.dbl ? kFDouble : 0u);
+            continue;
+        }
         if (op == FOP_AND) {
             const bool aFalse = !an && av == 0;
             const bool bFalse = !bn && bv == 0;

@@ -401,6 +401,12 @@ enum FilterOp : int16_t {
     FOP_EQ, FOP_NEQ, FOP_LT, FOP_LTE, FOP_GT, FOP_GTE,
     FOP_AND, FOP_OR, FOP_NOT,
     FOP_IS_NULL, FOP_IS_NOT_NULL,
+    // Arithmetic (the reference's math functions, codegen/functions/mathfunctions.cpp): integers
+    // wrap at the result width (width 4 or 8), DIV / MOD by zero give NULL, TRY_* give NULL on
+    // overflow (TRY_DIV is DIV); doubles (dbl = 1) are IEEE, DIV / MOD by zero give NULL, MOD is
+    // fmod.  A NULL operand gives NULL.
+    FOP_ADD, FOP_SUB, FOP_MUL, FOP_DIV, FOP_MOD,
+    FOP_TRY_ADD, FOP_TRY_SUB, FOP_TRY_MUL, FOP_TRY_DIV,
 };
 constexpr int kMaxFilterInstrs = 24;
 constexpr int kMaxFilterDepth = 8;

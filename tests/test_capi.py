@@ -109,13 +109,17 @@ def test_factory_validation_matches_reference_rules():
     omg.LookupOuterJoinOperatorFactory([L], [0], [1], [L], ff).close()
     ff.close()
     # join filters: compiled on the host when the factory is made; comparisons / AND / OR / NOT /
-    # IS NULL over integer-like and DOUBLE columns are accepted, anything else is refused with
-    # UNSUPPORTED (lookup_join.cpp:175-187 refuses what its code generator cannot compile)
+    # IS NULL and INT / LONG / DOUBLE arithmetic over integer-like and DOUBLE columns are accepted,
+    # anything else is refused with UNSUPPORTED (lookup_join.cpp:175-187 refuses what its code
+    # generator cannot compile)
     bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, L], [0])
     ok = omg.Binary(omg.EXPR_AND, omg.Binary(omg.EXPR_NEQ, omg.Field(0, L), omg.Field(2, L)),
                     omg.Not(omg.IsNull(omg.Field(1, L))))
     omg.LookupJoinOperatorFactory([L, L], [0], [0], [1], [L], bf, filter_expr=ok).close()
-    for bad in (omg.Binary(9, omg.Field(0, L), omg.Field(2, L)),  # ADD
+    arith = omg.Binary(omg.EXPR_GT, omg.Binary(omg.EXPR_ADD, omg.Field(0, L), omg.Field(2, L), L),
+                       omg.Literal(5, L))
+    omg.LookupJoinOperatorFactory([L, L], [0], [0], [1], [L], bf, filter_expr=arith).close()
+    for bad in (omg.Binary(omg.EXPR_ADD, omg.Field(0, L), omg.Field(2, L)),  # arithmetic with a BOOLEAN result
                 omg.Binary(omg.EXPR_EQ, omg.Field(0, omg.VarcharType(4)), omg.Field(2, L))):
         with pytest.raises(omg.OmgError) as e:
             omg.LookupJoinOperatorFactory([omg.VarcharType(4), L], [0], [0], [1], [L], bf, filter_expr=bad)

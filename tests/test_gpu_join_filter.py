@@ -108,6 +108,8 @@ def _eval(e, pi, bi, pcols, pmasks, bcols, bmasks):
         return m.astype(np.int64), np.zeros(len(pi), bool), False
     a, am, ad = _eval(e.left, pi, bi, pcols, pmasks, bcols, bmasks)
     b, bm, bd = _eval(e.right, pi, bi, pcols, pmasks, bcols, bmasks)
+    if e.op >= omg.EXPR_ADD:
+        return _arith(e, a, am, ad, b, bm, bd)
     if e.op == omg.EXPR_AND:
         af, bf_ = ~am & (a == 0), ~bm & (b == 0)
         null = ~(af | bf_) & (am | bm)
@@ -121,6 +123,49 @@ def _eval(e, pi, bi, pcols, pmasks, bcols, bmasks):
     cmp = {omg.EXPR_EQ: a == b, omg.EXPR_NEQ: a != b, omg.EXPR_LT: a < b, omg.EXPR_LTE: a <= b,
            omg.EXPR_GT: a > b, omg.EXPR_GTE: a >= b}[e.op]
     return cmp.astype(np.int64), am | bm, False
+
+
+def _arith(e, a, am, ad, b, bm, bd):
+    """The reference's math functions (codegen/functions/mathfunctions.cpp) in Python numbers:
+    integers wrap at the node's width, DIV / MOD by zero are NULL, TRY_* overflow is NULL (TRY_DIV
+    is DIV), doubles are IEEE with fmod; C division truncates toward zero."""
+    null = am | bm
+    if e.dtype.id == omg.OMNI_DOUBLE:
+        x, y = a.astype(np.float64), b.astype(np.float64)
+        with np.errstate(all="ignore"):
+            if e.op in (omg.EXPR_ADD, omg.EXPR_TRY_ADD):
+                r = x + y
+            elif e.op in (omg.EXPR_SUB, omg.EXPR_TRY_SUB):
+                r = x - y
+            elif e.op in (omg.EXPR_MUL, omg.EXPR_TRY_MUL):
+                r = x * y
+            else:
+                zero = y == 0
+                null = null | zero
+                r = np.where(zero, 0.0, np.fmod(x, np.where(zero, 1.0, y)) if e.op == omg.EXPR_MOD
+                             else x / np.where(zero, 1.0, y))
+        return r, null, True
+    bits = 8 * (4 if e.dtype.id == omg.OMNI_INT else 8)
+    lo, hi = -(1 << (bits - 1)), (1 << (bits - 1)) - 1
+    out = np.zeros(len(a), dtype=np.int64)
+    for i, (x, y) in enumerate(zip(a.tolist(), b.tolist())):
+        if null[i]:
+            continue
+        x, y = int(x), int(y)
+        if e.op in (omg.EXPR_DIV, omg.EXPR_TRY_DIV, omg.EXPR_MOD):
+            if y == 0:
+                null[i] = True
+                continue
+            q = abs(x) // abs(y) * (1 if (x >= 0) == (y > 0) else -1)
+            r = q if e.op != omg.EXPR_MOD else x - q * y
+        else:
+            r = {omg.EXPR_ADD: x + y, omg.EXPR_TRY_ADD: x + y, omg.EXPR_SUB: x - y, omg.EXPR_TRY_SUB: x - y,
+                 omg.EXPR_MUL: x * y, omg.EXPR_TRY_MUL: x * y}[e.op]
+            if not lo <= r <= hi and e.op in (omg.EXPR_TRY_ADD, omg.EXPR_TRY_SUB, omg.EXPR_TRY_MUL):
+                null[i] = True
+                continue
+        out[i] = ((r - lo) % (1 << bits)) + lo  # wrap at the width
+    return out, null, False
 
 
 def _passes(e, pcols, pmasks, bcols, bmasks):
@@ -137,6 +182,13 @@ FILTERS = {
                             B(omg.EXPR_GT, F(2, D), omg.Literal(0.25, D))),
     "build_only_and_null_literal": B(omg.EXPR_OR, B(omg.EXPR_GTE, F(4, L), omg.Literal(0, L)),
                                      B(omg.EXPR_EQ, F(1, L), omg.Literal(0, L, is_null=True))),
+    "arith_add_div_mod": B(omg.EXPR_AND, B(omg.EXPR_LT, B(omg.EXPR_ADD, F(1, L), F(4, L), L), omg.Literal(3, L)),
+                           B(omg.EXPR_NEQ, B(omg.EXPR_MOD, F(1, L), F(4, L), L),
+                             B(omg.EXPR_DIV, F(4, L), omg.Literal(3, L), L))),
+    "arith_double_and_try": B(omg.EXPR_OR, B(omg.EXPR_GT, B(omg.EXPR_SUB, B(omg.EXPR_MUL, F(2, D),
+                                                                           omg.Literal(2.0, D), D),
+                                                         F(5, D), D), omg.Literal(0.5, D)),
+                              omg.IsNull(B(omg.EXPR_TRY_MUL, F(1, L), omg.Literal(1 << 62, L), L))),
 }
 
 
@@ -178,3 +230,20 @@ def test_filtered_join_kinds_match_oracle(join_type, build_side, fname, unique):
         want.append(tuple(r))
     assert len(want) > 0
     assert sorted(got, key=_key) == sorted(want, key=_key)
+
+
+def test_int_arithmetic_wraps_at_32_bits():
+    """INT arithmetic wraps at 32 bits (AddInt32, MultiplyInt32) while TRY_ADD gives NULL on
+    overflow: pairs with p + b beyond 2^31 - 1 wrap negative, so `p + b < 0` holds for them, and
+    `TRY_ADD(p, b) IS NULL` marks the same pairs."""
+    n = 200
+    key = np.arange(n, dtype=np.int64)
+    pv = np.array([2**31 - 1 - (i % 7) for i in range(n)], dtype=np.int32)
+    bv = np.array([i % 11 for i in range(n)], dtype=np.int32)
+    none = np.zeros(n, bool)
+    for filt in (B(omg.EXPR_LT, B(omg.EXPR_ADD, F(1, I), F(3, I), I), omg.Literal(0, I)),
+                 omg.IsNull(B(omg.EXPR_TRY_ADD, F(1, I), F(3, I), I))):
+        rows = run("INNER", "UNKNOWN", [L, I], [key, bv], [none, none], [L, I], [key, pv], [none, none], [0, 1],
+                   [1], filt, batch_sizes=(n,))
+        want = sorted((int(k), int(p), int(b)) for k, p, b in zip(key, pv, bv) if int(p) + int(b) > 2**31 - 1)
+        assert len(want) > 0 and sorted(rows) == want
