@@ -107,8 +107,9 @@ int32_t omg_config_get_policy(void);
 int32_t omg_debug_fail_next_allocs(int32_t n);
 /* Device-side bounded-wait budget in clock64 ticks (0 = library default). */
 int32_t omg_debug_set_wait_budget(int64_t ticks);
-/* Inner probes on a bitmap ARRAY table: 1 (default) = the group-staged kernel (whole-line output
- * runs), 0 = the per-warp bitmap kernel.  Both give the same rows; for tests and measurements.
+/* Inner probes on a bitmap ARRAY table that write pinned host output: 1 (default) = the
+ * group-staged kernel (whole-line output runs over the CPU-GPU link), 0 = the per-warp bitmap
+ * kernel (always used for HBM output).  Both give the same rows; for tests and measurements.
  * No reference counterpart. */
 int32_t omg_debug_set_staged_probe(int32_t on);
 /* Staged rows at which a HashAggregation operator aggregates its queued batches before

@@ -4,8 +4,11 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
 #include <mutex>
+#include <thread>
 
 namespace omg {
 
@@ -99,6 +102,64 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
             ++t;
         }
         totalRows_ += d.rows;
+    }
+}
+
+namespace {
+class BatchReaper {
+public:
+    BatchReaper() : thread_([this] { Run(); }) {}
+    ~BatchReaper()
+    {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_one();
+        thread_.join();
+    }
+    void Add(std::vector<VectorBatch *> &&batches)
+    {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            queue_.push_back(std::move(batches));
+        }
+        cv_.notify_one();
+    }
+
+private:
+    void Run()
+    {
+        std::unique_lock<std::mutex> lock(mu_);
+        while (true) {
+            cv_.wait(lock, [this] { return stop_ || !queue_.empty(); });
+            while (!queue_.empty()) {
+                std::vector<VectorBatch *> work = std::move(queue_.front());
+                queue_.pop_front();
+                lock.unlock();
+                for (auto *b : work) {
+                    omniruntime::vec::VectorHelper::FreeVecBatch(b);
+                }
+                lock.lock();
+            }
+            if (stop_) {
+                return;
+            }
+        }
+    }
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<std::vector<VectorBatch *>> queue_;
+    bool stop_ = false;
+    std::thread thread_;  // last member: starts after the others exist
+};
+}  // namespace
+
+void FreeBatchesLater(std::vector<VectorBatch *> &&batches)
+{
+    static BatchReaper reaper;
+    if (!batches.empty()) {
+        reaper.Add(std::move(batches));
     }
 }
 

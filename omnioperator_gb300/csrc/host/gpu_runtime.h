@@ -217,6 +217,11 @@ inline int32_t AlignedBatchRows(int32_t maxRows)
 
 size_t NullBitmapBytes(int64_t rows);
 
+// Frees batches an operator is done with on a background thread, off the operator's path: a
+// pipelined probe takes thousands of small host batches per step, and each free returns its
+// pinned buffers to the pool.  The batches must no longer be read by any kernel.
+void FreeBatchesLater(std::vector<omniruntime::vec::VectorBatch *> &&batches);
+
 // A VARCHAR column from per-row lengths: exclusive offsets (n + 1, 64-bit, the total last) and
 // the total, read back to the host (synchronises `s`).
 int64_t ScanLengths(const uint32_t *lens, int64_t n, DevArray<int64_t> &offs, cudaStream_t s);

@@ -935,6 +935,7 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending
         hostDirect = hostDirect && cols[o].width != 0;
     }
     pc.hostDirect = hostDirect;
+    p.hostOutput = hostDirect ? 1 : 0;
     pc.regionCap = regionCap;
     pc.nRegions = nRegions;
     pc.nOut = nOut;
@@ -1075,9 +1076,7 @@ void LookupJoinOperator::FinishProbe(ProbeCall &pc)
     counters_[5] += rows;
     const auto tf = std::chrono::steady_clock::now();
     counters_[10] += std::chrono::duration_cast<std::chrono::nanoseconds>(tf - tc).count();
-    for (auto *pb : pc.batches) {
-        vec::VectorHelper::FreeVecBatch(pb);
-    }
+    omg::FreeBatchesLater(std::move(pc.batches));  // the probe kernel is done with them
     pc.batches.clear();
     counters_[11] += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - tf).count();
 }

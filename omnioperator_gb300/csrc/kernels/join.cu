@@ -1903,11 +1903,13 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             pick = match ? i : -1;
         }
         const int single = p.singleBatch ? 0 : 1;
-        // Inner joins whose outputs are the probe key and payload fields take the staged kernel
-        // when its shared memory (bitmap + the groups' staging) fits.
+        // Inner joins whose outputs are the probe key and payload fields, written to pinned host
+        // memory, take the staged kernel when its shared memory (bitmap + the groups' staging)
+        // fits: whole-line output runs carry the link at its rate (with HBM output the per-warp
+        // kernel, without the group barriers, is faster).
         const uint32_t groupSmem = static_cast<uint32_t>(bitsBytes) + kGroupsPerCta * kGroupStageBytes;
         bool staged = p.joinKind == JOIN_KIND_INNER && p.table.slotPayload != nullptr && groupSmem <= kGroupMaxSmem &&
-            g_stagedProbe.load();
+            p.hostOutput != 0 && g_stagedProbe.load();
         for (int o = 0; staged && o < p.nOut; ++o) {
             staged = p.out[o].side != 2;
         }

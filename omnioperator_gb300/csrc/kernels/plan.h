@@ -442,6 +442,8 @@ struct ProbeLaunch {
     unsigned long long *outCount;
     int32_t nRegions;
     int32_t singleBatch;  // 1: one batch, tiles t cover its rows [t * kTileRows, ...) in order
+    int32_t hostOutput;   // 1: the output columns are pinned host memory (written over the link)
+    int32_t pad0;
     uint64_t regionCap;
     int32_t countOnly;
     int32_t *error;
