@@ -51,6 +51,9 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+# omg_debug_last_probe_kernel codes
+PROBE_KERNEL_NAMES = {1: "ProbeKindKernel", 2: "ProbeKernel", 3: "ProbeFastKernel", 4: "ProbeBitsKernel",
+                      5: "ProbeGroupKernel", 6: "ProbeBulkKernel"}
 N_BUILD = 1 << 20
 N_PROBE = 1 << 26
 AGG_ROWS = 1 << 22
@@ -443,6 +446,7 @@ def run_gpu(args, rank, world):
     pop = pf.create_operator()
     pop.set_stream(stream.cuda_stream)
     pop.set_device_output(True)
+    omg.lib().omg_debug_set_bulk_probe(args.bulk_probe)
 
     def probe_step():
         pop.add_input(omg.wrap_device_batch([L], N_PROBE, [pkey.data_ptr()], [pbits.data_ptr()]))
@@ -484,9 +488,11 @@ def run_gpu(args, rank, world):
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                 "traffic": None if traffic_per_row is None else traffic_per_row * N_PROBE,
-                "kernel": "ProbeBitsKernel", "kernel_ms": round(kernel_s * 1e3, 4),
+                "kernel": PROBE_KERNEL_NAMES.get(omg.lib().omg_debug_last_probe_kernel(), "?"),
+                "kernel_ms": round(kernel_s * 1e3, 4),
                 "algorithmic_bytes": int(alg_bytes)}
 
+    omg.lib().omg_debug_set_bulk_probe(0)
     log(f"headline probe timed ({ms / args.steps:.3f} ms per step), oracle match {join_check['oracle_match']}")
     e2e = None if args.skip_e2e else run_e2e(args, omg, bf, torch, barrier, max_over_ranks, world, rank)
     log("e2e done")
@@ -615,7 +621,8 @@ def run_join_kinds(args, omg, torch, stream, barrier, max_over_ranks, world, bke
                      "output_rows": n, "outer_rows": n_outer,
                      "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                                   "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                                  "kernel": "ProbeKindKernel", "kernel_ms": round(kernel_s * 1e3, 4),
+                                  "kernel": PROBE_KERNEL_NAMES.get(omg.lib().omg_debug_last_probe_kernel(), "?"),
+                                  "kernel_ms": round(kernel_s * 1e3, 4),
                                   "algorithmic_bytes": int(alg)}}
         pop.delete()
         bop.delete()
@@ -1567,6 +1574,9 @@ def main():
     ap.add_argument("--only", default="all", choices=["all", "agg", "skew", "batched", "join5"],
                     help="agg / skew: time only that aggregation workload (profiling runs)")
     ap.add_argument("--probe-log2", type=int, default=26, help="log2 of probe rows (profiling runs use fewer)")
+    ap.add_argument("--bulk-probe", type=int, default=0, choices=[0, 1, 2],
+                    help="headline probe kernel: 0 per-lane bitmap kernel, 1 bulk-copy key loads, "
+                         "2 bulk-copy key loads and output stores")
     ap.add_argument("--skip-skew", action="store_true", help="skip the skewed aggregation (plain vs learned)")
     ap.add_argument("--skew-log2", type=int, default=None, help="log2 rows of the skewed aggregation (default 28)")
     ap.add_argument("--sizer", default=None, help="sizing model weights (JSON) for the learned arm")

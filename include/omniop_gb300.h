@@ -112,6 +112,16 @@ int32_t omg_debug_set_wait_budget(int64_t ticks);
  * kernel (always used for HBM output).  Both give the same rows; for tests and measurements.
  * No reference counterpart. */
 int32_t omg_debug_set_staged_probe(int32_t on);
+/* Inner probes on a bitmap ARRAY table from device-resident keys to HBM output: 0 (default) =
+ * the per-lane bitmap kernel, 1 = the bulk-copy kernel with keys moved into shared memory by
+ * cp.async.bulk, 2 = the same with output runs stored back by cp.async.bulk.  All give the same
+ * rows; for tests and measurements.  No reference counterpart. */
+int32_t omg_debug_set_bulk_probe(int32_t mode);
+/* Which probe kernel the latest probe launch in this process started: 1 multi-column keys or
+ * filters, 2 general, 3 fast (unique table, register outputs), 4 bitmap with per-lane loads
+ * and stores, 5 group-staged (pinned host output), 6 bulk-copy; 0 none yet.  For tests and
+ * measurements.  No reference counterpart. */
+int32_t omg_debug_last_probe_kernel(void);
 /* Staged rows at which a HashAggregation operator aggregates its queued batches before
  * GetOutput (0 = library default, 2^28).  Process-wide; lets tests run many batch sets
  * through one operator. */

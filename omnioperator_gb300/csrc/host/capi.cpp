@@ -137,6 +137,16 @@ int32_t omg_debug_set_staged_probe(int32_t on)
     return OMG_OK;
 }
 
+int32_t omg_debug_last_probe_kernel(void) { return omg::LastProbeKernel(); }
+
+int32_t omg_debug_set_bulk_probe(int32_t mode)
+{
+    return Guard([&] {
+        Require(mode >= 0 && mode <= 2, "bulk probe mode must be 0, 1 or 2");
+        omg::SetBulkProbe(mode);
+    });
+}
+
 int32_t omg_debug_set_agg_flush_rows(int64_t rows)
 {
     omg::SetAggFlushRows(rows < 0 ? 0 : rows);

@@ -27,6 +27,7 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
     }
     descs_.Reset(batches.size());
     anyNulls_.assign(inputCols.size(), false);
+    allDevice_.assign(inputCols.size(), true);
     size_t nTiles = 0;
     for (auto *b : batches) {
         nTiles += (static_cast<size_t>(b->GetRowCount()) + tileRows - 1) / tileRows;
@@ -58,6 +59,9 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
             }
             d.cols[i] = v->RawValues();
             d.offs[i] = v->RawOffsets();
+            if (!v->IsDevice()) {
+                allDevice_[i] = false;
+            }
             const bool hasNull = v->RawNulls() != nullptr && v->HasNull();
             d.nulls[i] = hasNull ? v->RawNulls() : nullptr;
             if (hasNull) {

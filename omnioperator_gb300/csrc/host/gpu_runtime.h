@@ -184,6 +184,11 @@ public:
     std::vector<int64_t> RegionRows(int32_t nRegions) const;
     int64_t TotalRows() const { return totalRows_; }
     bool AnyNulls(int32_t input) const { return input < static_cast<int32_t>(anyNulls_.size()) && anyNulls_[input]; }
+    // True when input `input` of every batch is device memory (no pinned host vectors).
+    bool AllOnDevice(int32_t input) const
+    {
+        return input >= 0 && input < static_cast<int32_t>(allDevice_.size()) && allDevice_[input];
+    }
 
 private:
     struct MaskSlot {
@@ -205,6 +210,7 @@ private:
     DevArray<TileDesc> dTiles_;
     DevArray<int64_t> dTileOut_;
     std::vector<bool> anyNulls_;
+    std::vector<bool> allDevice_;
     int64_t totalRows_ = 0;
 };
 

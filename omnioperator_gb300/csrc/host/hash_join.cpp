@@ -923,9 +923,12 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending
         regionCap *= std::min<uint32_t>(b.maxDup, 2);
     }
     regionCap = (regionCap + 63) / 64 * 64;
-    pc.count.Reset(static_cast<size_t>(nRegions) * omg::kRegionStride, s, true);
-    pc.hostCount.Reset(static_cast<size_t>(nRegions) * omg::kRegionStride);
+    // The region counters, then one more 128-byte line whose first word is the kernel's error.
+    pc.count.Reset(static_cast<size_t>(nRegions + 1) * omg::kRegionStride, s, true);
+    pc.hostCount.Reset(static_cast<size_t>(nRegions + 1) * omg::kRegionStride);
     p.outCount = pc.count.Get();
+    p.error = reinterpret_cast<int32_t *>(pc.count.Get() + static_cast<size_t>(nRegions) * omg::kRegionStride);
+    p.waitBudget = omg::WaitBudget();
     p.nRegions = nRegions;
     p.singleBatch = pc.batches.size() == 1 ? 1 : 0;
     // Host output without VARCHAR columns: the kernel writes the rows straight into pinned host
@@ -936,6 +939,7 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending
     }
     pc.hostDirect = hostDirect;
     p.hostOutput = hostDirect ? 1 : 0;
+    p.deviceKeys = !b.multiKey && bt.AllOnDevice(p.keyInput) ? 1 : 0;
     pc.regionCap = regionCap;
     pc.nRegions = nRegions;
     pc.nOut = nOut;
@@ -999,6 +1003,12 @@ void LookupJoinOperator::FinishProbe(ProbeCall &pc)
         counters_[9] += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - tw).count();
         counters_[6] += pc.timer.ElapsedNs();
         ++counters_[7];
+        const int32_t kerr = static_cast<int32_t>(pc.hostCount[static_cast<size_t>(nRegions) * omg::kRegionStride]);
+        if (kerr != 0) {
+            throw OmniException("OPERATOR_RUNTIME_ERROR",
+                kerr == 7 ? "probe kernel: a bounded wait for a bulk copy ran out" : "probe kernel error " + std::to_string(kerr),
+                kerr == 7 ? -7 : -9);
+        }
         uint64_t most = 0;
         for (int32_t r = 0; r < nRegions; ++r) {
             regionCount[r] = static_cast<int64_t>(pc.hostCount[static_cast<size_t>(r) * omg::kRegionStride]);

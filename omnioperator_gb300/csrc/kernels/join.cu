@@ -11,10 +11,12 @@
 // (round, warp) so that the tile's matches get one contiguous output range from a single
 // atomicAdd, and writes probe columns plus gathered build columns in probe-row order within the
 // tile.
+#include <algorithm>
 #include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "bulk_copy.cuh"
 #include "device_common.cuh"
 #include "launch.h"
 #include "plan.h"
@@ -1531,6 +1533,8 @@ constexpr int kGroupTilesPerTile = kTileRows / kGroupRows;
 constexpr uint32_t kGroupStageBytes = static_cast<uint32_t>(kGroupRows) * 16u + 64u;
 constexpr uint32_t kGroupMaxSmem = 227u * 1024u;
 std::atomic<bool> g_stagedProbe{true};
+std::atomic<int> g_bulkProbe{0};  // bulk-copy probe: 0 off, 1 bulk key loads, 2 and bulk output stores
+std::atomic<int> g_lastProbeKernel{0};  // ProbeKernelId of the latest LaunchProbe
 
 __device__ __forceinline__ void GroupBarrier(int group)
 {
@@ -1735,6 +1739,382 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeGroupKernel(const __grid
     }
 }
 
+// ------------------------------------------------------------------ bulk-copy inner probe
+// Inner joins on an ARRAY table (occupancy bitmap in shared memory, packed slot payload) whose
+// outputs are the 8-byte probe key and payload fields of compile-time widths, written to device
+// memory.  Columns move by the bulk-copy (TMA) engine instead of per-lane requests through L1:
+// - keys (kIn): every warp owns two key buffers in shared memory; while it resolves one segment
+//   of kRounds * 32 rows, one lane's `cp.async.bulk` fills the other with the next segment (and
+//   its validity bytes), completing on that buffer's mbarrier;
+// - outputs (kOut): the warp compacts a segment's matches into one of two staging buffers, each
+//   column laid out with its destination's 16-byte phase, and one bulk store per column writes
+//   the 16-byte aligned middle of the column's run; the rows before and after it (at most 15
+//   bytes each) are plain stores.
+// Segments that are not whole or whose columns are not 16-byte aligned read their keys with
+// plain loads.  A bounded mbarrier wait that runs out sets error 7 and ends the warp after
+// waiting (again bounded) for its copies in flight.
+template <int kNumOut, uint32_t kLayout, int kRounds, bool kIn, bool kOut>
+struct BulkProbeSmem {
+    static constexpr int kRows = kRounds * 32;
+    static constexpr uint32_t kKeyBytes = kIn ? static_cast<uint32_t>(kRows) * 8u : 0u;
+    static constexpr uint32_t kNullBytes = kIn ? 16u : 0u;  // kRows / 8 validity bytes, padded
+    static constexpr uint32_t Width(int o)
+    {
+        return o < kNumOut ? (1u << (((kLayout >> (3 * o)) & 7u) - 1u)) : 0u;
+    }
+    // A column's staging run: kRows rows plus up to 15 bytes of destination phase.
+    static constexpr uint32_t ColBytes(int o) { return o < kNumOut ? static_cast<uint32_t>(kRows) * Width(o) + 16u : 0u; }
+    static constexpr uint32_t ColOffset(int o) { return o == 0 ? 0u : ColOffset(o - 1) + ColBytes(o - 1); }
+    static constexpr uint32_t kStageBytes = kOut ? ColOffset(4) : 0u;
+    static constexpr uint32_t kKeyOff = 0;
+    static constexpr uint32_t kNullOff = 2 * kKeyBytes;
+    static constexpr uint32_t kStageOff = kNullOff + 2 * kNullBytes;
+    static constexpr uint32_t kBarOff = kStageOff + 2 * kStageBytes;
+    static constexpr uint32_t kBytes = kBarOff + (kIn ? 16u : 0u);  // two mbarriers
+    // With output staging, 128-row segments fit 16 warps beside a 128 KiB bitmap; capping the
+    // CTA there leaves each thread up to 128 registers.
+    static constexpr int kMaxThreads = kRounds >= 4 && kOut ? 512 : 1024;
+};
+
+struct BulkSeg {
+    const long long *keys;
+    const uint8_t *nulls;
+    int64_t base;
+    int64_t batchRows;
+    int t;
+    bool valid;
+    bool bulk;
+};
+
+template <bool kSingle, int kRows>
+__device__ __forceinline__ BulkSeg BulkSegOf(const ProbeLaunch &p, int64_t item)
+{
+    BulkSeg s;
+    if (kSingle) {
+        s.keys = static_cast<const long long *>(p.batches[0].cols[p.keyInput]);
+        s.nulls = p.batches[0].nulls[p.keyInput];
+        s.base = item * kRows;
+        s.batchRows = p.batches[0].rows;
+        s.t = static_cast<int>(s.base / kTileRows);
+        s.valid = true;
+    } else {
+        constexpr int kSegsPerTile = kTileRows / kRows;
+        s.t = static_cast<int>(item / kSegsPerTile);
+        const int s0 = static_cast<int>(item % kSegsPerTile) * kRows;
+        const TileDesc tile = p.tiles[s.t];
+        s.valid = s0 < tile.rows;
+        const BatchDesc &b = p.batches[tile.batch];
+        s.keys = static_cast<const long long *>(b.cols[p.keyInput]);
+        s.nulls = b.nulls[p.keyInput];
+        s.base = static_cast<int64_t>(tile.row0) + s0;
+        s.batchRows = static_cast<int64_t>(tile.row0) + tile.rows;
+    }
+    // Whole segments of 16-byte aligned columns move by bulk copy: the key run starts at
+    // base * 8 bytes and the validity run at base / 8 bytes (a multiple of 16 for 128-row
+    // segments; 64-row segments read validity words with plain loads).
+    const uintptr_t nullAlign = kRows % 128 == 0 ? 15u : 3u;
+    s.bulk = s.valid && s.base + kRows <= s.batchRows && (reinterpret_cast<uintptr_t>(s.keys) & 15u) == 0 &&
+        (reinterpret_cast<uintptr_t>(s.nulls) & nullAlign) == 0;
+    return s;
+}
+
+template <int kRows>
+__device__ __forceinline__ void BulkSegLoad(const BulkSeg &s, long long *keyBuf, uint8_t *nullBuf, uint64_t *bar)
+{
+    const bool bulkNulls = s.nulls != nullptr && kRows % 128 == 0;
+    const uint32_t bytes = static_cast<uint32_t>(kRows) * 8u + (bulkNulls ? static_cast<uint32_t>(kRows / 8) : 0u);
+    MbarArmTx(bar, bytes);
+    BulkLoad(keyBuf, s.keys + s.base, static_cast<uint32_t>(kRows) * 8u, bar);
+    if (bulkNulls) {
+        BulkLoad(nullBuf, s.nulls + (s.base >> 3), static_cast<uint32_t>(kRows / 8), bar);
+    }
+}
+
+// Keys and validity of one segment with plain loads: whole segments with word-aligned validity
+// branch-free, others row by row.
+template <int kRounds>
+__device__ __forceinline__ uint32_t LoadKeysPlain(const BulkSeg &s, int lane, int64_t (&key)[kRounds])
+{
+    uint32_t live = 0;
+    if (s.base + kRounds * 32 <= s.batchRows && (reinterpret_cast<uintptr_t>(s.nulls) & 3u) == 0) {
+        uint32_t w[kRounds];
+#pragma unroll
+        for (int i = 0; i < kRounds; ++i) {
+            key[i] = __ldg(s.keys + s.base + i * 32 + lane);
+            w[i] = s.nulls == nullptr ? 0u : __ldg(reinterpret_cast<const unsigned int *>(s.nulls) + ((s.base >> 5) + i));
+        }
+#pragma unroll
+        for (int i = 0; i < kRounds; ++i) {
+            live |= (((w[i] >> lane) & 1u) ^ 1u) << i;
+        }
+        return live;
+    }
+#pragma unroll
+    for (int i = 0; i < kRounds; ++i) {
+        const int64_t row = s.base + i * 32 + lane;
+        key[i] = 0;
+        if (row < s.batchRows) {
+            key[i] = __ldg(s.keys + row);
+            if (!RowIsNullRO(s.nulls, row)) {
+                live |= 1u << i;
+            }
+        }
+    }
+    return live;
+}
+
+// Widths below are compile-time constants once the column loops are unrolled.
+__device__ __forceinline__ void StageOut(uint8_t *col, uint32_t byteAt, uint64_t v, uint32_t width)
+{
+    if (width == 8) {
+        *reinterpret_cast<uint64_t *>(col + byteAt) = v;
+    } else if (width == 4) {
+        *reinterpret_cast<uint32_t *>(col + byteAt) = static_cast<uint32_t>(v);
+    } else if (width == 2) {
+        *reinterpret_cast<uint16_t *>(col + byteAt) = static_cast<uint16_t>(v);
+    } else {
+        col[byteAt] = static_cast<uint8_t>(v);
+    }
+}
+
+__device__ __forceinline__ void CopyStaged(uint8_t *dst, const uint8_t *src, uint32_t width)
+{
+    if (width == 8) {
+        *reinterpret_cast<uint64_t *>(dst) = *reinterpret_cast<const uint64_t *>(src);
+    } else if (width == 4) {
+        *reinterpret_cast<uint32_t *>(dst) = *reinterpret_cast<const uint32_t *>(src);
+    } else if (width == 2) {
+        *reinterpret_cast<uint16_t *>(dst) = *reinterpret_cast<const uint16_t *>(src);
+    } else {
+        *dst = *src;
+    }
+}
+
+template <int kNumOut, uint32_t kLayout, bool kSingle, int kRounds, bool kIn, bool kOut>
+__global__ void __launch_bounds__(BulkProbeSmem<kNumOut, kLayout, kRounds, kIn, kOut>::kMaxThreads, 1)
+    ProbeBulkKernel(const __grid_constant__ ProbeLaunch p, uint32_t bitsVecs)
+{
+    using G = BulkProbeSmem<kNumOut, kLayout, kRounds, kIn, kOut>;
+    constexpr int kRows = G::kRows;
+    extern __shared__ uint4 sBulkSmem[];
+    const int warp = static_cast<int>(threadIdx.x >> 5);
+    const int lane = static_cast<int>(threadIdx.x & 31);
+    const unsigned int lanesBelow = (1u << lane) - 1u;
+    uint8_t *mine = reinterpret_cast<uint8_t *>(sBulkSmem + bitsVecs) + static_cast<size_t>(warp) * G::kBytes;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(mine + G::kBarOff);
+    if (kIn && lane == 0) {
+        MbarInit(bar, 1);
+        MbarInit(bar + 1, 1);
+        MbarInitFence();
+    }
+    {
+        const uint4 *g = reinterpret_cast<const uint4 *>(p.table.slotBits);
+        for (uint32_t i = threadIdx.x; i < bitsVecs; i += blockDim.x) {
+            sBulkSmem[i] = __ldg(g + i);
+        }
+    }
+    __syncthreads();
+    const uint32_t *sBits = reinterpret_cast<const uint32_t *>(sBulkSmem);
+    const unsigned long long *payloadTab = reinterpret_cast<const unsigned long long *>(p.table.slotPayload);
+    const uint64_t minKey = static_cast<uint64_t>(p.table.minKey);
+    const uint64_t range = p.table.range;
+    const long long budget = p.waitBudget;
+    uint8_t *vals[kNumOut];
+    int shift[kNumOut];
+    bool isKey[kNumOut];
+#pragma unroll
+    for (int o = 0; o < kNumOut; ++o) {
+        vals[o] = static_cast<uint8_t *>(p.out[o].values);
+        shift[o] = p.out[o].shift;
+        isKey[o] = p.out[o].side == 0;
+    }
+    const int64_t nItems = kSingle ? (p.batches[0].rows + kRows - 1) / kRows
+                                   : static_cast<int64_t>(p.nTiles) * (kTileRows / kRows);
+    const int warpsPerCta = static_cast<int>(blockDim.x >> 5);
+    const int64_t warpsTotal = static_cast<int64_t>(gridDim.x) * warpsPerCta;
+    int64_t item = static_cast<int64_t>(blockIdx.x) * warpsPerCta + warp;
+    uint32_t parity = 0;        // bit b: the parity of bar[b]'s next phase
+    uint32_t pendingLoads = 0;  // bit b: a load into buffer b is in flight
+    int buf = 0;
+    int stage = 0;
+    bool failed = false;
+    BulkSeg cur = BulkSegOf<kSingle, kRows>(p, item < nItems ? item : 0);
+    if (kIn && item < nItems && cur.bulk) {
+        if (lane == 0) {
+            BulkSegLoad<kRows>(cur, reinterpret_cast<long long *>(mine + G::kKeyOff), mine + G::kNullOff, bar);
+        }
+        pendingLoads |= 1u;
+    }
+    for (; item < nItems; item += warpsTotal) {
+        const int64_t nextItem = item + warpsTotal;
+        BulkSeg next = cur;
+        next.valid = false;
+        next.bulk = false;
+        if (nextItem < nItems) {
+            next = BulkSegOf<kSingle, kRows>(p, nextItem);
+            // Prefetch the next segment into the other buffer; its keys were read into
+            // registers by every lane in the previous iteration.
+            if (kIn && next.bulk) {
+                FenceProxyAsyncShared();
+                __syncwarp();
+                if (lane == 0) {
+                    BulkSegLoad<kRows>(next, reinterpret_cast<long long *>(mine + G::kKeyOff + (buf ^ 1) * G::kKeyBytes),
+                        mine + G::kNullOff + (buf ^ 1) * G::kNullBytes, bar + (buf ^ 1));
+                }
+                pendingLoads |= 1u << (buf ^ 1);
+            }
+        }
+        if (cur.valid) {
+            int64_t key[kRounds];
+            uint32_t live = 0;
+            if (kIn && cur.bulk) {
+                const bool ok = __all_sync(0xffffffffu, MbarWaitBounded(bar + buf, (parity >> buf) & 1u, budget));
+                if (!ok) {
+                    failed = true;
+                    break;
+                }
+                parity ^= 1u << buf;
+                pendingLoads &= ~(1u << buf);
+                const long long *kb = reinterpret_cast<const long long *>(mine + G::kKeyOff + buf * G::kKeyBytes);
+#pragma unroll
+                for (int i = 0; i < kRounds; ++i) {
+                    key[i] = kb[i * 32 + lane];
+                }
+                if (cur.nulls == nullptr) {
+                    live = (1u << kRounds) - 1u;
+                } else {
+                    const uint32_t *nw = kRows % 128 == 0
+                        ? reinterpret_cast<const uint32_t *>(mine + G::kNullOff + buf * G::kNullBytes)
+                        : nullptr;
+#pragma unroll
+                    for (int i = 0; i < kRounds; ++i) {
+                        const uint32_t w = nw != nullptr
+                            ? nw[i]
+                            : __ldg(reinterpret_cast<const unsigned int *>(cur.nulls) + ((cur.base >> 5) + i));
+                        live |= (((w >> lane) & 1u) ^ 1u) << i;
+                    }
+                }
+            } else {
+                live = LoadKeysPlain<kRounds>(cur, lane, key);
+            }
+            uint32_t hit = 0;
+#pragma unroll
+            for (int i = 0; i < kRounds; ++i) {
+                const uint64_t d = static_cast<uint64_t>(key[i]) - minKey;
+                if (((live >> i) & 1u) && key[i] >= p.table.minKey && d < range) {
+                    hit |= ((sBits[d >> 5] >> (d & 31)) & 1u) << i;
+                }
+            }
+            uint64_t payload[kRounds];
+#pragma unroll
+            for (int i = 0; i < kRounds; ++i) {
+                payload[i] = ((hit >> i) & 1u) ? __ldg(payloadTab + (static_cast<uint64_t>(key[i]) - minKey)) : 0ull;
+            }
+            uint32_t total = 0;
+#pragma unroll
+            for (int i = 0; i < kRounds; ++i) {
+                total += __popc(__ballot_sync(0xffffffffu, (hit >> i) & 1u));
+            }
+            const int region = cur.t % p.nRegions;
+            unsigned long long pos = 0;
+            if (lane == 0 && total != 0) {
+                pos = atomicAdd(p.outCount + region * kRegionStride, static_cast<unsigned long long>(total));
+            }
+            pos = __shfl_sync(0xffffffffu, pos, 0);
+            const uint32_t n = p.countOnly || pos >= p.regionCap
+                ? 0u
+                : static_cast<uint32_t>(pos + total <= p.regionCap ? total : p.regionCap - pos);
+            const uint64_t at0 = static_cast<uint64_t>(region) * p.regionCap + pos;
+            if (!kOut && n != 0) {
+                uint32_t off = 0;
+#pragma unroll
+                for (int i = 0; i < kRounds; ++i) {
+                    const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
+                    const uint32_t j = off + __popc(m & lanesBelow);
+                    if (((hit >> i) & 1u) && j < n) {
+#pragma unroll
+                        for (int o = 0; o < kNumOut; ++o) {
+                            const uint64_t v = isKey[o] ? static_cast<uint64_t>(key[i]) : (payload[i] >> shift[o]);
+                            StageOut(vals[o] + (at0 + j) * G::Width(o), 0u, v, G::Width(o));
+                        }
+                    }
+                    off += __popc(m);
+                }
+            }
+            if (kOut && n != 0) {
+                uint8_t *st = mine + G::kStageOff + stage * G::kStageBytes;
+                // The staging buffer was last read by the bulk stores of two segments ago.
+                if (lane == 0) {
+                    BulkWaitRead<1>();
+                }
+                __syncwarp();
+                uint32_t phase[kNumOut];
+#pragma unroll
+                for (int o = 0; o < kNumOut; ++o) {
+                    phase[o] = static_cast<uint32_t>(reinterpret_cast<uintptr_t>(vals[o] + at0 * G::Width(o)) & 15u);
+                }
+                uint32_t off = 0;
+#pragma unroll
+                for (int i = 0; i < kRounds; ++i) {
+                    const unsigned int m = __ballot_sync(0xffffffffu, (hit >> i) & 1u);
+                    const uint32_t j = off + __popc(m & lanesBelow);
+                    if (((hit >> i) & 1u) && j < n) {
+#pragma unroll
+                        for (int o = 0; o < kNumOut; ++o) {
+                            const uint64_t v = isKey[o] ? static_cast<uint64_t>(key[i]) : (payload[i] >> shift[o]);
+                            StageOut(st + G::ColOffset(o), phase[o] + j * G::Width(o), v, G::Width(o));
+                        }
+                    }
+                    off += __popc(m);
+                }
+                FenceProxyAsyncShared();
+                __syncwarp();
+                // Per column: bytes [head, head + mid) of the run go by one bulk store, the rows
+                // before it (fewer than 16 bytes) and after it (likewise) by lane l writing row l.
+#pragma unroll
+                for (int o = 0; o < kNumOut; ++o) {
+                    const uint32_t runBytes = n * G::Width(o);
+                    const uint32_t head = (16u - phase[o]) & 15u;
+                    const uint32_t mid = runBytes > head ? ((runBytes - head) & ~15u) : 0u;
+                    if (lane == 0 && mid != 0) {
+                        BulkStore(vals[o] + at0 * G::Width(o) + head, st + G::ColOffset(o) + phase[o] + head, mid);
+                    }
+                    const uint32_t headEnd = head < runBytes ? head : runBytes;
+                    const uint32_t tail = headEnd + mid;
+                    const uint32_t lb = static_cast<uint32_t>(lane) * G::Width(o);
+                    if (lb < headEnd) {
+                        CopyStaged(vals[o] + at0 * G::Width(o) + lb, st + G::ColOffset(o) + phase[o] + lb, G::Width(o));
+                    }
+                    if (tail + lb < runBytes) {
+                        CopyStaged(vals[o] + at0 * G::Width(o) + tail + lb, st + G::ColOffset(o) + phase[o] + tail + lb,
+                            G::Width(o));
+                    }
+                }
+                if (lane == 0) {
+                    BulkCommit();
+                }
+                stage ^= 1;
+            }
+        }
+        cur = next;
+        buf ^= 1;
+    }
+    if (kIn && failed) {
+        if (lane == 0 && p.error != nullptr) {
+            atomicExch(p.error, 7);
+        }
+        // Let the loads still in flight land before the CTA's shared memory is released.
+        for (int b = 0; b < 2; ++b) {
+            if ((pendingLoads >> b) & 1u) {
+                MbarWaitBounded(bar + b, (parity >> b) & 1u, budget);
+            }
+        }
+    }
+    if (kOut && lane == 0) {
+        BulkWaitAll();
+    }
+}
+
 // Occupancy bitmap of an ARRAY table: bit d of word d / 32 set iff entries[d] >= 0.  Words past
 // the range (up to the 16-byte padding) are zero.
 __global__ void BuildSlotBitsKernel(const int64_t *entries, uint64_t range, uint32_t *bits, uint64_t nWords)
@@ -1821,6 +2201,10 @@ uint64_t SlotBitsBytes(uint64_t range) { return ((range + 127) / 128) * 16; }
 
 void SetStagedProbe(bool on) { g_stagedProbe.store(on); }
 
+void SetBulkProbe(int mode) { g_bulkProbe.store(mode == 1 || mode == 2 ? mode : 0); }
+
+int LastProbeKernel() { return g_lastProbeKernel.load(); }
+
 cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
 {
     if (p.nTiles <= 0) {
@@ -1828,6 +2212,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     }
     if (p.nKeyCols > 0 || p.nFilter > 0) {
         const int maxGrid = SMs() * BlocksPerSM(reinterpret_cast<const void *>(ProbeKindKernel), kProbeThreads, 0);
+        g_lastProbeKernel.store(PROBE_KERNEL_KIND);
         ProbeKindKernel<<<p.nTiles < maxGrid ? p.nTiles : maxGrid, kProbeThreads, 0, stream>>>(p);
         return cudaGetLastError();
     }
@@ -1913,6 +2298,63 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         for (int o = 0; staged && o < p.nOut; ++o) {
             staged = p.out[o].side != 2;
         }
+        // Opt-in (omg_debug_set_bulk_probe): inner joins with compile-time output widths written
+        // to HBM from device-resident keys run the bulk-copy kernel when its columns are 16-byte
+        // aligned and at least 8 warps' buffers fit beside the bitmap.  Measured slower than the
+        // per-lane kernel on this path (bulk copies travel the same L1-to-L2 request path, and
+        // small bulk stores are slow), so it is not the default.
+        const int bulkMode = g_bulkProbe.load();
+        bool bulk = !staged && p.hostOutput == 0 && p.deviceKeys != 0 && bulkMode != 0 && p.joinKind == JOIN_KIND_INNER &&
+            p.table.slotPayload != nullptr && insts[pick].layout != 0;
+        for (int o = 0; bulk && o < p.nOut; ++o) {
+            bulk = p.out[o].side != 2 && (reinterpret_cast<uintptr_t>(p.out[o].values) & 15u) == 0 &&
+                (p.regionCap * static_cast<uint64_t>(p.out[o].width)) % 16u == 0;
+        }
+        if (bulk) {
+            struct BulkInst {
+                uint32_t layout;
+                int nOut;
+                int mode;  // 1: bulk key loads, 2: bulk key loads and output stores
+                uint32_t warpBytes;
+                int maxWarps;
+                const void *single;
+                const void *tiled;
+            };
+#define OMG_BULK_INST(n, layout, out)                                                                       \
+    {layout, n, (out) ? 2 : 1, BulkProbeSmem<n, layout, kBitsRounds, true, out>::kBytes,                    \
+        BulkProbeSmem<n, layout, kBitsRounds, true, out>::kMaxThreads / 32,                                  \
+        reinterpret_cast<const void *>(ProbeBulkKernel<n, layout, true, kBitsRounds, true, out>),           \
+        reinterpret_cast<const void *>(ProbeBulkKernel<n, layout, false, kBitsRounds, true, out>)}
+            static const BulkInst bulkInsts[] = {
+                OMG_BULK_INST(3, OutLayout(kW8, kW4, kW4), false), OMG_BULK_INST(3, OutLayout(kW8, kW4, kW4), true),
+                OMG_BULK_INST(2, OutLayout(kW8, kW8), false), OMG_BULK_INST(2, OutLayout(kW8, kW8), true),
+                OMG_BULK_INST(2, OutLayout(kW8, kW4), false), OMG_BULK_INST(2, OutLayout(kW8, kW4), true),
+            };
+#undef OMG_BULK_INST
+            const BulkInst *bi = nullptr;
+            for (const BulkInst &c : bulkInsts) {
+                if (c.layout == insts[pick].layout && c.nOut == p.nOut && c.mode == bulkMode) {
+                    bi = &c;
+                }
+            }
+            const uint32_t room = kGroupMaxSmem - static_cast<uint32_t>(bitsBytes);
+            const int warps = bi == nullptr ? 0 : static_cast<int>(std::min<uint32_t>(room / bi->warpBytes, bi->maxWarps));
+            if (warps >= 8) {
+                const void *bk = single == 0 ? bi->single : bi->tiled;
+                cudaError_t berr = EnsureDynamicSmem(bk, kGroupMaxSmem);
+                if (berr != cudaSuccess) {
+                    return berr;
+                }
+                const int64_t items = static_cast<int64_t>(p.nTiles) * kBitsSegsPerTile;
+                const int64_t wanted = (items + warps - 1) / warps;
+                const int grid = static_cast<int>(wanted < SMs() ? (wanted > 0 ? wanted : 1) : SMs());
+                uint32_t bitsVecs = static_cast<uint32_t>(bitsBytes / 16);
+                const size_t smem = static_cast<size_t>(bitsBytes) + static_cast<size_t>(warps) * bi->warpBytes;
+                void *bargs[] = {const_cast<ProbeLaunch *>(&p), &bitsVecs};
+                g_lastProbeKernel.store(PROBE_KERNEL_BULK);
+                return cudaLaunchKernel(bk, dim3(grid), dim3(warps * 32), bargs, smem, stream);
+            }
+        }
         if (staged) {
             const void *gk = single == 0 ? groupInsts[pick].single : groupInsts[pick].tiled;
             cudaError_t gerr = EnsureDynamicSmem(gk, kGroupMaxSmem);
@@ -1924,6 +2366,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             const int grid = static_cast<int>(wanted < SMs() ? (wanted > 0 ? wanted : 1) : SMs());
             uint32_t bitsVecs = static_cast<uint32_t>(bitsBytes / 16);
             void *gargs[] = {const_cast<ProbeLaunch *>(&p), &bitsVecs};
+            g_lastProbeKernel.store(PROBE_KERNEL_GROUP);
             return cudaLaunchKernel(gk, dim3(grid), dim3(kBitsThreads), gargs, static_cast<size_t>(groupSmem), stream);
         }
         const void *kernel = single == 0 ? insts[pick].single : insts[pick].tiled;
@@ -1936,6 +2379,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         const int64_t wanted = (items + warpsPerCta - 1) / warpsPerCta;
         const int grid = static_cast<int>(wanted < SMs() ? wanted : SMs());
         void *args[] = {const_cast<ProbeLaunch *>(&p)};
+        g_lastProbeKernel.store(PROBE_KERNEL_BITS);
         return cudaLaunchKernel(kernel, dim3(grid), dim3(kBitsThreads), args, static_cast<size_t>(bitsBytes), stream);
     }
     if (p.nKeyCols == 0 && p.joinKind != JOIN_KIND_INNER) {
@@ -1943,6 +2387,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
                                   : (p.table.slotPayload != nullptr ? ProbeKernel<true, true, true>
                                                                     : ProbeKernel<true, false, true>);
         const int maxGrid = SMs() * BlocksPerSM(reinterpret_cast<const void *>(kk), kProbeThreads, 0);
+        g_lastProbeKernel.store(PROBE_KERNEL_GENERAL);
         kk<<<p.nTiles < maxGrid ? p.nTiles : maxGrid, kProbeThreads, 0, stream>>>(p);
         return cudaGetLastError();
     }
@@ -1957,6 +2402,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     }
     const int maxGrid = SMs() * BlocksPerSM(reinterpret_cast<const void *>(kernel), kProbeThreads, 0);
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
+    g_lastProbeKernel.store(fast ? PROBE_KERNEL_FAST : PROBE_KERNEL_GENERAL);
     kernel<<<grid, kProbeThreads, 0, stream>>>(p);
     return cudaGetLastError();
 }

@@ -55,6 +55,20 @@ cudaError_t LaunchAggOrdered(const AggLaunch &p, int32_t nBatches, const AggExtr
 // Inner probes on a bitmap ARRAY table use the group-staged kernel when it fits (default on);
 // off selects the per-warp bitmap kernel.  Process-wide; for tests and measurements.
 void SetStagedProbe(bool on);
+// Bulk-copy inner probe for HBM output: 0 off (default), 1 keys by cp.async.bulk, 2 keys and
+// output runs by cp.async.bulk.
+void SetBulkProbe(int mode);
+// Which probe kernel the latest LaunchProbe in this process started.
+enum ProbeKernelId {
+    PROBE_KERNEL_NONE = 0,
+    PROBE_KERNEL_KIND = 1,     // ProbeKindKernel: multi-column keys, filters
+    PROBE_KERNEL_GENERAL = 2,  // ProbeKernel
+    PROBE_KERNEL_FAST = 3,     // ProbeFastKernel
+    PROBE_KERNEL_BITS = 4,     // ProbeBitsKernel: bitmap in shared memory, per-lane loads and stores
+    PROBE_KERNEL_GROUP = 5,    // ProbeGroupKernel: group-staged output runs (pinned host output)
+    PROBE_KERNEL_BULK = 6,     // ProbeBulkKernel: keys and output runs by cp.async.bulk
+};
+int LastProbeKernel();
 
 // ---- utilities (util.cu)
 // Masked-input NULL bitmaps, one per job (see MaskJob).

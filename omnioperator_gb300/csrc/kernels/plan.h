@@ -443,10 +443,11 @@ struct ProbeLaunch {
     int32_t nRegions;
     int32_t singleBatch;  // 1: one batch, tiles t cover its rows [t * kTileRows, ...) in order
     int32_t hostOutput;   // 1: the output columns are pinned host memory (written over the link)
-    int32_t pad0;
+    int32_t deviceKeys;   // 1: every batch's probe key column (and its validity) is device memory
     uint64_t regionCap;
     int32_t countOnly;
-    int32_t *error;
+    int32_t *error;     // nonzero after the kernel: 7 = a bounded wait for a bulk copy ran out
+    long long waitBudget;  // clock64 ticks of a bounded device-side wait
     int32_t joinKind;   // JoinKind
     uint8_t *visited;   // BUILD_OUTER / FULL: one byte per build row, set to 1 when matched
     int32_t nKeyCols;   // > 0: hashed multi-column key (keyInput unused, -1)

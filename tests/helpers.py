@@ -141,7 +141,7 @@ def exact_by_key(key_cols, key_nulls, values, valid, divide_by_count=False):
 
 def run_join(build_types, build_cols, build_nulls, build_hash_cols, probe_types, probe_cols, probe_nulls,
              probe_hash_cols, probe_out, build_out, batch_sizes=(4096,), build_batch=1 << 20, pipeline=False,
-             device_input=False):
+             device_input=False, device_output=False):
     bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, build_types, build_hash_cols)
     bop = bf.create_operator()
     pf = pop = None
@@ -157,6 +157,8 @@ def run_join(build_types, build_cols, build_nulls, build_hash_cols, probe_types,
                                            [build_types[c] for c in build_out], bf)
         pop = pf.create_operator()
         assert not pop.is_blocked()
+        if device_output:
+            pop.set_device_output(True)
         if pipeline:
             pop.set_no_more_input(False)
         n = len(probe_cols[0])
@@ -180,6 +182,10 @@ def run_join(build_types, build_cols, build_nulls, build_hash_cols, probe_types,
         max_rows = 0
         for b in outs:
             max_rows = max(max_rows, omg.batch_row_count(b))
+            if device_output:
+                h = omg.batch_to_host(b)
+                omg.free_batch(b)
+                b = h
             c = omg.batch_to_numpy(b)
             omg.free_batch(b)
             cols = c if cols is None else [(np.concatenate([a[0], x[0]]), np.concatenate([a[1], x[1]]))

@@ -259,3 +259,47 @@ def test_staged_and_per_warp_probe_kernels_agree(gpu, device_input, batch):
             _check(bkey, p1, p2, pkey, pnull, batch_sizes=(batch,), device_input=device_input)
     finally:
         omg.lib().omg_debug_set_staged_probe(1)
+
+
+@pytest.mark.parametrize("bulk", [1, 2, 0])
+@pytest.mark.parametrize("batch", [1 << 20, 4096, 3000, 1000])
+def test_bulk_copy_probe_kernel_hbm_output(gpu, bulk, batch):
+    """Device input and HBM output: the bulk-copy probe (keys staged into shared memory by
+    cp.async.bulk; mode 2 also stores the output runs back by cp.async.bulk) and the per-lane
+    bitmap probe (mode 0) give the expected rows, for one large batch, whole tiles and ragged
+    batches (partial segments read their keys with plain loads)."""
+    bkey, p1, p2, pkey, pnull = _cfg2_like(1 << 16, 700_000, 43)
+    try:
+        assert omg.lib().omg_debug_set_bulk_probe(bulk) == 0
+        _check(bkey, p1, p2, pkey, pnull, batch_sizes=(batch,), device_input=True, device_output=True,
+               pipeline=True)
+        assert omg.lib().omg_debug_last_probe_kernel() == (6 if bulk else 4)
+    finally:
+        omg.lib().omg_debug_set_bulk_probe(0)
+
+
+@pytest.mark.parametrize("bulk", [1, 2])
+def test_bulk_copy_probe_two_payload_layouts(gpu, bulk):
+    """The (8-byte key, 8-byte payload) and (8-byte key, 4-byte payload) layouts of the
+    bulk-copy probe, no NULL keys, against the expected rows."""
+    rng = np.random.default_rng(44)
+    nb, n = 1 << 16, 600_000
+    bkey = rng.permutation(nb).astype(np.int64)
+    pay8 = rng.integers(-2**62, 2**62, nb, dtype=np.int64)
+    pay4 = rng.integers(-2**31, 2**31, nb, dtype=np.int64).astype(np.int32)
+    pkey = rng.integers(0, 2 * nb, n).astype(np.int64)
+    try:
+        assert omg.lib().omg_debug_set_bulk_probe(bulk) == 0
+        for btypes, bcols in (([L, L], [bkey, pay8]), ([L, I], [bkey, pay4])):
+            got, _ = run_join(btypes, bcols, None, [0], [L], [pkey], None, [0], [0], [1],
+                              batch_sizes=(n,), device_input=True, device_output=True)
+            exp = expected_join_rows([pkey], None, bcols, None, 0, 0, [0], [1])
+            assert join_rows_canonical(got) == exp
+            assert omg.lib().omg_debug_last_probe_kernel() == 6
+    finally:
+        omg.lib().omg_debug_set_bulk_probe(0)
+
+
+def test_bulk_probe_knob_rejects_other_modes():
+    assert omg.lib().omg_debug_set_bulk_probe(3) != 0
+    assert omg.lib().omg_debug_set_bulk_probe(0) == 0
