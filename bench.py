@@ -639,7 +639,8 @@ def run_features(args, omg, torch, dev, stream, barrier, max_over_ranks, world, 
     * agg_varchar: 2^22 rows grouped by a VARCHAR key over 10,000 distinct strings of 8-24 bytes,
       SUM and COUNT of an int64 column (string dictionary, aggregation on ids, strings restored);
     * join_filter: the headline probe (2^26 rows) with the filter build.p1 >= 0 (about half the
-      matches pass), general probe kernel;
+      matches pass), evaluated in the bitmap probe on each row's one candidate, with the kernel's
+      roofline (8 B key + 1/8 B validity per probe row and 16 B per output row);
     * agg_spill: the uniform aggregation (2^22 rows) with a 256 KiB device budget, so its rows are
       partitioned into pinned host memory and aggregated one partition at a time, next to the
       unspilled run."""
@@ -696,6 +697,7 @@ def run_features(args, omg, torch, dev, stream, barrier, max_over_ranks, world, 
     pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1, 2], [I, I], bf,
                                        filter_expr=omg.Binary(omg.EXPR_GTE, omg.Field(2, I), omg.Literal(0, I)))
     rows = []
+    kern = []
 
     def join_filter():
         op = pf.create_operator()
@@ -705,12 +707,22 @@ def run_features(args, omg, torch, dev, stream, barrier, max_over_ranks, world, 
         outs = op.drain()
         rows.append(sum(omg.batch_row_count(b) for b in outs))
         omg.free_batches(outs)
+        c = op.counters()
+        kern.append(c["kernel_ns"] / max(c["kernel_launches"], 1) / 1e9)
         op.delete()
 
     t = timed(join_filter, max(1, min(args.steps, 5)), n_warm)
     pf.close()
+    kernel_s = float(np.median(kern[n_warm:] or kern))
+    alg = N_PROBE * 8 + N_PROBE / 8 + rows[-1] * 16
+    peak, peak_kind = measured_peak_gbs()
     out["join_filter"] = {"value": world * N_PROBE / t, "unit": "probe rows/s", "ms_per_step": round(t * 1e3, 3),
-                          "output_rows": rows[-1]}
+                          "output_rows": rows[-1],
+                          "roofline": {"bound": "hbm", "achieved": round(alg / kernel_s / 1e9, 1), "peak": peak,
+                                       "unit": "GB/s", "frac": round(alg / kernel_s / 1e9 / peak, 4),
+                                       "peak_kind": peak_kind,
+                                       "kernel": PROBE_KERNEL_NAMES.get(omg.lib().omg_debug_last_probe_kernel(), "?"),
+                                       "kernel_ms": round(kernel_s * 1e3, 4), "algorithmic_bytes": int(alg)}}
 
     # spill
     key, v1, v2 = agg_data_numpy(2)
@@ -1684,6 +1696,13 @@ def summary(line):
         out["cfg5_join_ms_direct_hash_range_learned_quantile_frac"] = d
         out["cfg5_cpu_rows_s"] = _sig(j["s=1.1"]["cpu_baseline"]["value"]) if "s=1.1" in j else None
         out["cfg5_oracle_match"] = j.get("oracle_match")
+    kinds = line.get("join_kinds") or {}
+    feats = line.get("features") or {}
+    fr = {name: v["roofline"]["frac"] for name, v in kinds.items() if isinstance(v, dict) and "roofline" in v}
+    if "join_filter" in feats and "roofline" in feats["join_filter"]:
+        fr["filter"] = feats["join_filter"]["roofline"]["frac"]
+    if fr:
+        out["probe_kind_frac"] = fr
     return out
 
 

@@ -174,6 +174,9 @@ public:
         descs_[batch].cols[input] = values;
         descs_[batch].offs[input] = nullptr;
     }
+    // Point the NULL bitmap of input `input` of batch `batch` elsewhere (nullptr: no NULLs).
+    void SetInputNulls(size_t batch, int32_t input, const uint8_t *nulls) { descs_[batch].nulls[input] = nulls; }
+    int64_t BatchRows(size_t batch) { return descs_[batch].rows; }
     int64_t BatchRowBase(size_t batch) { return descs_[batch].rowBase; }
     size_t NumBatches() const { return descs_.Size(); }
     const BatchDesc *DeviceBatches() const { return dBatches_.Get(); }

@@ -82,8 +82,13 @@ struct JoinBuildState {
     omg::JoinTable table{};
     uint32_t maxDup = 0;
     DevArray<uint8_t> visited;  // BUILD_OUTER / FULL: one byte per build row, set by the probes
-    // Several key columns (or one 16-byte key): the table is keyed by the tuple hash of each row.
+    // Several key columns (or one 16-byte key): the table is keyed by the tuple hash of each row,
+    // unless the key columns are fixed widths of 1-8 bytes whose build value ranges multiply to at
+    // most 2^62: then each row's parts are packed into one 64-bit key (`packed`, multiKey false)
+    // and the table is a single-key ARRAY or HASH table over the packed keys.
     bool multiKey = false;
+    bool packed = false;
+    omg::JoinKeyPack pack{};
     DevArray<uint64_t> keyHash;
     DevArray<uint8_t> keyHashNulls;
 
@@ -97,7 +102,72 @@ struct JoinBuildState {
     }
 
     void Build();
+    bool TryPackKeys();
 };
+
+// Packs the key parts of every build row into keyHash (see `packed`) when they qualify.
+bool JoinBuildState::TryPackKeys()
+{
+    cudaStream_t s = stream.Get();
+    const int n = static_cast<int>(hashCols.size());
+    omg::JoinKeyPack kp{};
+    kp.nParts = n;
+    omg::JoinKeyCols kc{};
+    kc.nKeys = n;
+    bool anyNull = false;
+    for (int k = 0; k < n; ++k) {
+        const int32_t c = hashCols[k];
+        const auto &t = buildTypes.GetType(c);
+        const int w = t->ByteWidth();
+        if (Varlen(t) || (w != 1 && w != 2 && w != 4 && w != 8)) {
+            return false;
+        }
+        kc.widths[k] = w;
+        kc.cols[k] = colValues[c].Get();
+        kc.nulls[k] = colHasNull[c] ? colNulls[c].Get() : nullptr;
+        anyNull = anyNull || colHasNull[c];
+        kp.width[k] = w;
+    }
+    // Per-part value ranges over the part's non-NULL build rows.
+    DevArray<long long> stats(8, s, true);
+    unsigned __int128 product = 1;
+    for (int k = 0; k < n; ++k) {
+        CudaCheck(cudaMemsetAsync(stats.Get(), 0, 8 * sizeof(long long), s), "reset");
+        CudaCheck(omg::LaunchKeyStats(kc.cols[k], kc.nulls[k], rows, kc.widths[k], stats.Get(), s), "key part stats");
+        long long h[3];
+        CudaCheck(cudaMemcpyAsync(h, stats.Get(), sizeof(h), cudaMemcpyDeviceToHost, s), "read key part stats");
+        stream.Sync();
+        if (h[2] == 0) {
+            return false;  // a part that is always NULL: no build row can match
+        }
+        const uint64_t span = static_cast<uint64_t>(h[1]) - static_cast<uint64_t>(h[0]) + 1;
+        if (span == 0) {
+            return false;
+        }
+        product *= span;
+        if (product > (static_cast<unsigned __int128>(1) << 62)) {
+            return false;
+        }
+        kp.minv[k] = h[0];
+        kp.span[k] = span;
+    }
+    uint64_t stride = 1;
+    for (int k = n - 1; k >= 0; --k) {
+        kp.stride[k] = stride;
+        stride *= kp.span[k];
+    }
+    keyHash.Reset(static_cast<size_t>(rows), s);
+    if (anyNull) {
+        keyHashNulls.Reset(omg::NullBitmapBytes(rows), s, true);
+    }
+    CudaCheck(omg::LaunchPackBuildKeys(kc, kp, rows, reinterpret_cast<int64_t *>(keyHash.Get()),
+                  anyNull ? keyHashNulls.Get() : nullptr, s),
+        "pack build keys");
+    pack = kp;
+    packed = true;
+    multiKey = false;
+    return true;
+}
 
 void JoinBuildState::Build()
 {
@@ -169,7 +239,10 @@ void JoinBuildState::Build()
     }
     const void *keys = colValues[keyCol].Get();
     const uint8_t *keyNulls = colHasNull[keyCol] ? colNulls[keyCol].Get() : nullptr;
-    if (multiKey) {
+    if (multiKey && TryPackKeys()) {
+        keys = keyHash.Get();
+        keyNulls = keyHashNulls.Get();
+    } else if (multiKey) {
         omg::JoinKeyCols kc{};
         kc.nKeys = static_cast<int32_t>(hashCols.size());
         bool anyNull = false;
@@ -675,6 +748,8 @@ struct LookupJoinOperator::ProbeCall {
     bool hostDirect = false;
     DevArray<unsigned long long> count;
     omg::PinnedArray<unsigned long long> hostCount;
+    DevArray<int64_t> packKeys;   // packed multi-column probe keys (scratch input)
+    DevArray<uint8_t> packNulls;
     omg::KernelTimer timer;
     cudaEvent_t done = nullptr;
     cudaStream_t s = nullptr;
@@ -800,9 +875,18 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending
             inputCols.push_back(c);
         }
     }
+    // Packed multi-column keys: one more kernel input, a scratch column per batch (64-row aligned,
+    // so that each batch's NULL bitmap starts on a word) that a packing pass fills before the probe.
+    int32_t packInput = -1;
+    if (b.packed) {
+        if (inputCols.size() >= static_cast<size_t>(omg::kMaxInputs)) {
+            throw OmniException("UNSUPPORTED_ERROR", "too many probe columns for the join kernels", -2);
+        }
+        packInput = static_cast<int32_t>(inputCols.size());
+        inputCols.push_back(f_.probeHashCols[0]);  // placeholder, repointed below
+    }
     omg::BatchTable &bt = pc.bt;
     bt.Build(pc.batches, inputCols);
-    bt.Upload(s);
     const int64_t probeRows = bt.TotalRows();
     const size_t nProbeOut = f_.probeOutputCols.size();
     const size_t nOut = nProbeOut + (b.kind == omg::JOIN_KIND_EXISTENCE ? 1 : f_.buildOutputCols.size());
@@ -810,11 +894,19 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending
     std::vector<omg::OutColumn> &cols = pc.cols;
     omg::ProbeLaunch &p = pc.p;
     std::memset(&p, 0, sizeof(p));
-    p.batches = bt.DeviceBatches();
-    p.tiles = bt.DeviceTiles();
     p.nTiles = bt.NumTiles();
-    p.keyInput = b.multiKey ? -1 : 0;
-    p.keyWidth = f_.probeTypes.GetType(f_.probeHashCols[0])->ByteWidth();
+    p.keyInput = b.multiKey ? -1 : (b.packed ? packInput : 0);
+    p.keyWidth = b.packed ? 8 : f_.probeTypes.GetType(f_.probeHashCols[0])->ByteWidth();
+    if (b.packed) {
+        // The bitmap kernel packs the parts as it reads them; for the other kernels LaunchProbe
+        // fills the scratch input first.
+        p.pack = b.pack;
+        p.pack.outInput = packInput;
+        for (int k = 0; k < p.pack.nParts; ++k) {
+            p.pack.input[k] = inputOf[f_.probeHashCols[k]];
+            p.pack.width[k] = f_.probeTypes.GetType(f_.probeHashCols[k])->ByteWidth();
+        }
+    }
     if (b.multiKey) {
         p.nKeyCols = static_cast<int32_t>(f_.probeHashCols.size());
         for (int32_t k = 0; k < p.nKeyCols; ++k) {
@@ -939,12 +1031,34 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending
     }
     pc.hostDirect = hostDirect;
     p.hostOutput = hostDirect ? 1 : 0;
-    p.deviceKeys = !b.multiKey && bt.AllOnDevice(p.keyInput) ? 1 : 0;
+    p.deviceKeys = b.packed || (!b.multiKey && bt.AllOnDevice(p.keyInput)) ? 1 : 0;
     pc.regionCap = regionCap;
     pc.nRegions = nRegions;
     pc.nOut = nOut;
     pc.nProbeOut = nProbeOut;
     pc.s = s;
+    if (b.packed && !omg::ProbePacksKeys(p)) {
+        // A packing pass fills the scratch key input before the probe (see LaunchProbe).
+        bool anyNull = false;
+        for (int32_t c : f_.probeHashCols) {
+            anyNull = anyNull || bt.AnyNulls(inputOf[c]);
+        }
+        std::vector<int64_t> base(pc.batches.size() + 1, 0);
+        for (size_t i = 0; i < pc.batches.size(); ++i) {
+            base[i + 1] = base[i] + (bt.BatchRows(i) + 63) / 64 * 64;
+        }
+        pc.packKeys.Reset(static_cast<size_t>(std::max<int64_t>(base.back(), 1)), s);
+        if (anyNull) {
+            pc.packNulls.Reset(static_cast<size_t>(std::max<int64_t>(base.back() / 8, 8)), s, false);
+        }
+        for (size_t i = 0; i < pc.batches.size(); ++i) {
+            bt.SetInput(i, packInput, pc.packKeys.Get() + base[i]);
+            bt.SetInputNulls(i, packInput, anyNull ? pc.packNulls.Get() + base[i] / 8 : nullptr);
+        }
+    }
+    bt.Upload(s);
+    p.batches = bt.DeviceBatches();
+    p.tiles = bt.DeviceTiles();
     LaunchAttempt(pc);
     return call;
 }
@@ -1266,7 +1380,7 @@ bool LookupJoinOperator::ProcessPartitioned()
     JoinBuildState &b = *f_.build;
     const int32_t keyCol = f_.probeHashCols[0];
     if (!f_.filter.empty() || !b.table.unique || b.table.keyWidth != 8 || f_.probeTypes.GetType(keyCol)->ByteWidth() != 8 ||
-        b.kind != omg::JOIN_KIND_INNER || b.buildSide == OMNI_BUILD_LEFT || b.multiKey) {
+        b.kind != omg::JOIN_KIND_INNER || b.buildSide == OMNI_BUILD_LEFT || b.multiKey || b.packed) {
         return false;
     }
     for (int32_t c : f_.probeOutputCols) {

@@ -13,6 +13,7 @@
 // tile.
 #include <algorithm>
 #include <atomic>
+#include <type_traits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -1129,6 +1130,70 @@ __global__ void JoinKeyHashKernel(const JoinKeyCols kc, int64_t n, uint64_t *out
     }
 }
 
+// ------------------------------------------------------------------ packed multi-column keys
+// Part k of a packed multi-column key added to `acc` (JoinKeyPack); -1 once any part is outside
+// the build's range.
+__device__ __forceinline__ int64_t PackKeyPart(const JoinKeyPack &kp, int k, int64_t v, int64_t acc)
+{
+    const uint64_t d = static_cast<uint64_t>(v) - static_cast<uint64_t>(kp.minv[k]);
+    if (acc < 0 || v < kp.minv[k] || d >= kp.span[k]) {
+        return -1;
+    }
+    return acc + static_cast<int64_t>(d * kp.stride[k]);
+}
+
+// Build side: the packed key of every build row (contiguous key columns), NULL when a part is.
+__global__ void PackBuildKeysKernel(const JoinKeyCols kc, const JoinKeyPack kp, int64_t n, int64_t *out,
+    uint32_t *outNulls)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i0 = static_cast<int64_t>(blockIdx.x) * blockDim.x; i0 < n; i0 += stride) {
+        const int64_t i = i0 + threadIdx.x;
+        bool isNull = false;
+        int64_t key = 0;
+        if (i < n) {
+            for (int k = 0; k < kp.nParts; ++k) {
+                isNull = isNull || RowIsNullRO(kc.nulls[k], i);
+                key = PackKeyPart(kp, k, LoadInt(kc.cols[k], i, kc.widths[k]), key);
+            }
+            out[i] = isNull ? 0 : key;
+        }
+        const unsigned int m = __ballot_sync(0xffffffffu, isNull);
+        if (outNulls != nullptr && (threadIdx.x & 31) == 0 && i < n) {
+            outNulls[i >> 5] = m;  // i is a multiple of 32 here
+        }
+    }
+}
+
+// Probe side: the packed key of every probe row into input kp.outInput of its batch (a scratch
+// column), with its NULL bitmap when that input has one.  One CTA per tile.
+__global__ void PackProbeKeysKernel(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, const JoinKeyPack kp)
+{
+    for (int32_t t = blockIdx.x; t < nTiles; t += gridDim.x) {
+        const TileDesc tile = tiles[t];
+        const BatchDesc &b = batches[tile.batch];
+        int64_t *out = static_cast<int64_t *>(const_cast<void *>(b.cols[kp.outInput]));
+        uint32_t *outNulls = reinterpret_cast<uint32_t *>(const_cast<uint8_t *>(b.nulls[kp.outInput]));
+        for (int r0 = 0; r0 < tile.rows; r0 += blockDim.x) {
+            const int r = r0 + static_cast<int>(threadIdx.x);
+            const int64_t row = static_cast<int64_t>(tile.row0) + r;
+            bool isNull = false;
+            int64_t key = 0;
+            if (r < tile.rows) {
+                for (int k = 0; k < kp.nParts; ++k) {
+                    isNull = isNull || RowIsNullRO(b.nulls[kp.input[k]], row);
+                    key = PackKeyPart(kp, k, LoadInt(b.cols[kp.input[k]], row, kp.width[k]), key);
+                }
+                out[row] = isNull ? 0 : key;
+            }
+            const unsigned int m = __ballot_sync(0xffffffffu, isNull);
+            if (outNulls != nullptr && (threadIdx.x & 31) == 0 && r < tile.rows) {
+                outNulls[row >> 5] = m;  // tiles and warps start on 32-row boundaries
+            }
+        }
+    }
+}
+
 // Build rows no probe matched (lookup_outer_join.cpp:270-374): flags, then their row numbers in
 // build-row order after a scan of the flags.
 __global__ void UnvisitedFlagsKernel(const uint8_t *visited, int64_t n, uint32_t *flags)
@@ -1360,16 +1425,143 @@ __device__ __forceinline__ uint32_t LoadKeySegment(const long long *keyCol, cons
     return live;
 }
 
-template <int kNumOut, uint32_t kLayout, bool kSingle>
-__global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_constant__ ProbeLaunch p)
+// The kernels that pack multi-column keys as they read them take keys of at most this many parts
+// (longer keys are packed by a separate pass).
+constexpr int kFusedPackParts = 2;
+
+// Part columns of a packed key in one batch.
+struct PackCols {
+    const void *col[kFusedPackParts];
+    const uint8_t *nulls[kFusedPackParts];
+};
+
+__device__ __forceinline__ PackCols PackColsOf(const JoinKeyPack &kp, const BatchDesc &b)
 {
+    PackCols pc;
+#pragma unroll
+    for (int k = 0; k < kFusedPackParts; ++k) {
+        const int in = kp.input[k < kp.nParts ? k : 0];
+        pc.col[k] = b.cols[in];
+        pc.nulls[k] = b.nulls[in];
+    }
+    return pc;
+}
+
+// Keys of one warp segment packed from (up to kFusedPackParts) key parts, the part values kept in
+// v[k][i] and each part's NULL rows in nullBits[k] (bit i: round i).  Whole segments with
+// word-aligned NULL bitmaps read a 32-bit validity word per round and part.
+// kTwo32: two parts of 4 bytes each (the widths are not read).
+template <bool kTwo32, typename PartT>
+__device__ __forceinline__ uint32_t LoadPackedSegment(const JoinKeyPack &kp, const PackCols &pc, int64_t base,
+    int64_t batchRows, int lane, int64_t (&key)[kBitsRounds], PartT (&v)[kFusedPackParts][kBitsRounds],
+    uint32_t (&nullBits)[kFusedPackParts])
+{
+    const bool whole = base + kBitsSegRows <= batchRows &&
+        ((reinterpret_cast<uintptr_t>(pc.nulls[0]) | reinterpret_cast<uintptr_t>(pc.nulls[1])) & 3u) == 0;
+    if (kTwo32 && whole) {
+        // Two int32 parts: 32-bit offsets into ranges of at most 2^32 values, one wide multiply.
+        const int32_t *c0 = static_cast<const int32_t *>(pc.col[0]);
+        const int32_t *c1 = static_cast<const int32_t *>(pc.col[1]);
+        const unsigned int *n0 = reinterpret_cast<const unsigned int *>(pc.nulls[0]);
+        const unsigned int *n1 = reinterpret_cast<const unsigned int *>(pc.nulls[1]);
+        uint32_t w0[kBitsRounds];
+        uint32_t w1[kBitsRounds];
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            v[0][i] = static_cast<PartT>(__ldg(c0 + base + i * 32 + lane));
+            v[1][i] = static_cast<PartT>(__ldg(c1 + base + i * 32 + lane));
+            w0[i] = n0 == nullptr ? 0u : __ldg(n0 + (base >> 5) + i);
+            w1[i] = n1 == nullptr ? 0u : __ldg(n1 + (base >> 5) + i);
+        }
+        const uint32_t min0 = static_cast<uint32_t>(kp.minv[0]);
+        const uint32_t min1 = static_cast<uint32_t>(kp.minv[1]);
+        const uint64_t span0 = kp.span[0];
+        const uint64_t span1 = kp.span[1];
+        uint32_t live = 0;
+        nullBits[0] = 0;
+        nullBits[1] = 0;
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            const uint32_t d0 = static_cast<uint32_t>(v[0][i]) - min0;
+            const uint32_t d1 = static_cast<uint32_t>(v[1][i]) - min1;
+            const bool in = d0 < span0 && d1 < span1;
+            key[i] = in ? static_cast<int64_t>(static_cast<uint64_t>(d0) * span1 + d1) : -1;
+            const uint32_t b0 = (w0[i] >> lane) & 1u;
+            const uint32_t b1 = (w1[i] >> lane) & 1u;
+            nullBits[0] |= b0 << i;
+            nullBits[1] |= b1 << i;
+            live |= ((b0 | b1) ^ 1u) << i;
+        }
+        return live;
+    }
+#pragma unroll
+    for (int k = 0; k < kFusedPackParts; ++k) {
+        nullBits[k] = 0;
+        const bool part = kTwo32 || k < kp.nParts;
+#pragma unroll
+        for (int i = 0; i < kBitsRounds; ++i) {
+            const int64_t row = base + i * 32 + lane;
+            v[k][i] = 0;
+            if (part && row < batchRows) {
+                v[k][i] = kTwo32 ? static_cast<PartT>(__ldg(static_cast<const int32_t *>(pc.col[k]) + row))
+                                 : static_cast<PartT>(LoadInt(pc.col[k], row, kp.width[k]));
+                bool isNull;
+                if (whole) {
+                    const uint32_t w = pc.nulls[k] == nullptr
+                        ? 0u
+                        : __ldg(reinterpret_cast<const unsigned int *>(pc.nulls[k]) + ((base >> 5) + i));
+                    isNull = (w >> lane) & 1u;
+                } else {
+                    isNull = RowIsNullRO(pc.nulls[k], row);
+                }
+                nullBits[k] |= (isNull ? 1u : 0u) << i;
+            }
+        }
+    }
+    uint32_t live = 0;
+#pragma unroll
+    for (int i = 0; i < kBitsRounds; ++i) {
+        const int64_t row = base + i * 32 + lane;
+        int64_t acc = 0;
+#pragma unroll
+        for (int k = 0; k < kFusedPackParts; ++k) {
+            if (kTwo32 || k < kp.nParts) {
+                acc = PackKeyPart(kp, k, static_cast<int64_t>(v[k][i]), acc);
+            }
+        }
+        key[i] = acc;
+        const bool isNull = (((nullBits[0] | nullBits[1]) >> i) & 1u) != 0;
+        live |= (row < batchRows && !isNull ? 1u : 0u) << i;
+    }
+    return live;
+}
+
+// kProbeCols: some output is a probe column other than the key (its values, and its NULLs when
+// the output column has a bitmap, are read from the probe batch for each emitted row).
+// kPacked: the key is packed from the parts of a multi-column key (p.pack) as the rows are read.
+// kPack: 0 one key column, 1 a packed key of up to kFusedPackParts parts of run-time widths,
+// 2 a packed key of two 4-byte parts.
+// kFilter: each candidate pair (probe row, its one build row) must also pass the join filter.
+template <int kPack, bool kFilter>
+struct BitsThreads {
+    // Packed keys and filters: more registers per thread.
+    static constexpr int value = kPack != 0 || kFilter ? 768 : kBitsThreads;
+};
+
+template <int kNumOut, uint32_t kLayout, bool kSingle, bool kProbeCols, int kPack, bool kFilter = false>
+__global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
+    ProbeBitsKernel(const __grid_constant__ ProbeLaunch p)
+{
+    constexpr int kThreads = BitsThreads<kPack, kFilter>::value;
+    constexpr bool kPacked = kPack != 0;
+    using PartT = typename std::conditional<kPack == 2, int32_t, int64_t>::type;
     extern __shared__ uint4 sBitsVec[];
     const uint32_t *sBits = reinterpret_cast<const uint32_t *>(sBitsVec);
     {
         // The bitmap buffer holds a whole number of 16-byte vectors (see LaunchBuildSlotBits).
         const uint32_t nVec = static_cast<uint32_t>((p.table.range + 127) / 128);
         const uint4 *g = reinterpret_cast<const uint4 *>(p.table.slotBits);
-        for (uint32_t i = threadIdx.x; i < nVec; i += kBitsThreads) {
+        for (uint32_t i = threadIdx.x; i < nVec; i += kThreads) {
             sBitsVec[i] = __ldg(g + i);
         }
     }
@@ -1384,13 +1576,15 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
     int shift[kNumOut];
     bool isKey[kNumOut];
     bool isFlag[kNumOut];
+    bool isProbe[kNumOut];
 #pragma unroll
     for (int o = 0; o < kNumOut; ++o) {
         vals[o] = p.out[o].values;
         width[o] = p.out[o].width;
         shift[o] = p.out[o].shift;
-        isKey[o] = p.out[o].side == 0;
+        isKey[o] = p.out[o].side == 0 && (!kProbeCols || p.out[o].src == p.keyInput);
         isFlag[o] = p.out[o].side == 2;
+        isProbe[o] = kProbeCols && p.out[o].side == 0 && p.out[o].src != p.keyInput;
     }
     // Join kinds without visited marks (inner, probe-side outer, semi, anti, existence): which
     // rows are emitted follows EmitCount; unmatched rows get NULL build fields, emitted rows of a
@@ -1408,8 +1602,23 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
     }
     const int64_t nItems = kSingle ? (singleRows + kBitsSegRows - 1) / kBitsSegRows
                                    : static_cast<int64_t>(p.nTiles) * kBitsSegsPerTile;
-    const int64_t warpsTotal = static_cast<int64_t>(gridDim.x) * (kBitsThreads / 32);
-    for (int64_t item = static_cast<int64_t>(blockIdx.x) * (kBitsThreads / 32) + (threadIdx.x >> 5); item < nItems;
+    // Packed keys: which output reads which key part (-1: none) and the part columns.
+    int partOf[kNumOut];
+#pragma unroll
+    for (int o = 0; o < kNumOut; ++o) {
+        partOf[o] = -1;
+        for (int k = 0; kPacked && k < p.pack.nParts; ++k) {
+            if (isProbe[o] && p.out[o].src == p.pack.input[k]) {
+                partOf[o] = k;
+            }
+        }
+    }
+    PackCols packCols{};
+    if (kPacked && kSingle) {
+        packCols = PackColsOf(p.pack, p.batches[0]);
+    }
+    const int64_t warpsTotal = static_cast<int64_t>(gridDim.x) * (kThreads / 32);
+    for (int64_t item = static_cast<int64_t>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5); item < nItems;
          item += warpsTotal) {
         const int t = static_cast<int>(item / kBitsSegsPerTile);
         const long long *keyCol;
@@ -1433,14 +1642,40 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
             base = static_cast<int64_t>(tile.row0) + s0;
             batchRows = static_cast<int64_t>(tile.row0) + tile.rows;  // rows of the batch up to this tile's end
         }
+        const BatchDesc *segBatch = nullptr;
+        if (kProbeCols || kPacked || kFilter) {
+            segBatch = kSingle ? p.batches : p.batches + p.tiles[t].batch;
+        }
         int64_t key[kBitsRounds];
-        const uint32_t live = LoadKeySegment(keyCol, keyNulls, base, batchRows, lane, key);
+        PartT partVal[kFusedPackParts][kBitsRounds];
+        uint32_t partNull[kFusedPackParts];
+        uint32_t live;
+        if (kPacked) {
+            if (!kSingle) {
+                packCols = PackColsOf(p.pack, *segBatch);
+            }
+            live = LoadPackedSegment<kPack == 2>(p.pack, packCols, base, batchRows, lane, key, partVal, partNull);
+        } else {
+            live = LoadKeySegment(keyCol, keyNulls, base, batchRows, lane, key);
+        }
         uint32_t hit = 0;
 #pragma unroll
         for (int i = 0; i < kBitsRounds; ++i) {
             const uint64_t d = static_cast<uint64_t>(key[i]) - minKey;
             if (((live >> i) & 1u) && key[i] >= p.table.minKey && d < range) {
                 hit |= ((sBits[d >> 5] >> (d & 31)) & 1u) << i;
+            }
+        }
+        if (kFilter) {
+            // A unique ARRAY table: the slot's entry is the one build row of the key.
+#pragma unroll
+            for (int i = 0; i < kBitsRounds; ++i) {
+                if ((hit >> i) & 1u) {
+                    const int64_t br = p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey];
+                    if (!FilterPasses(p, *segBatch, base + i * 32 + lane, br)) {
+                        hit &= ~(1u << i);
+                    }
+                }
             }
         }
         uint64_t payload[kBitsRounds];
@@ -1484,25 +1719,41 @@ __global__ void __launch_bounds__(kBitsThreads, 1) ProbeBitsKernel(const __grid_
                     const bool h = (hit >> i) & 1u;
                     // Unmatched rows of a probe-side outer join carry zero build fields (NULL below).
                     const int64_t flag = h ? 1 : 0;
-                    StoreOut<kLayout, 0>(vals[0], at, width[0],
-                        isKey[0] ? key[i] : (isFlag[0] ? flag : static_cast<int64_t>(payload[i] >> shift[0])));
+                    const int64_t row = base + i * 32 + lane;
+                    int64_t v[kNumOut];
+#pragma unroll
+                    for (int o = 0; o < kNumOut; ++o) {
+                        v[o] = isKey[o] ? key[i] : (isFlag[o] ? flag : static_cast<int64_t>(payload[i] >> shift[o]));
+                        if (kProbeCols && isProbe[o]) {
+                            bool srcNull;
+                            if (kPacked && partOf[o] >= 0) {
+                                const int k = partOf[o];
+                                v[o] = static_cast<int64_t>(k == 0 ? partVal[0][i] : partVal[kFusedPackParts - 1][i]);
+                                srcNull = (((k == 0 ? partNull[0] : partNull[kFusedPackParts - 1]) >> i) & 1u) != 0;
+                            } else {
+                                v[o] = LoadInt(segBatch->cols[p.out[o].src], row, width[o]);
+                                srcNull = RowIsNullRO(segBatch->nulls[p.out[o].src], row);
+                            }
+                            if (p.out[o].nulls != nullptr && srcNull) {
+                                SetBit(p.out[o].nulls, at);
+                            }
+                        }
+                    }
+                    StoreOut<kLayout, 0>(vals[0], at, width[0], v[0]);
                     if (kNumOut > 1) {
-                        StoreOut<kLayout, 1>(vals[1], at, width[1],
-                            isKey[1] ? key[i] : (isFlag[1] ? flag : static_cast<int64_t>(payload[i] >> shift[1])));
+                        StoreOut<kLayout, 1>(vals[1], at, width[1], v[1]);
                     }
                     if (kNumOut > 2) {
-                        StoreOut<kLayout, 2>(vals[2], at, width[2],
-                            isKey[2] ? key[i] : (isFlag[2] ? flag : static_cast<int64_t>(payload[i] >> shift[2])));
+                        StoreOut<kLayout, 2>(vals[2], at, width[2], v[2]);
                     }
                     if (kNumOut > 3) {
-                        StoreOut<kLayout, 3>(vals[3], at, width[3],
-                            isKey[3] ? key[i] : (isFlag[3] ? flag : static_cast<int64_t>(payload[i] >> shift[3])));
+                        StoreOut<kLayout, 3>(vals[3], at, width[3], v[3]);
                     }
                     if (!inner) {
                         const bool nullKey = !((live >> i) & 1u);
 #pragma unroll
                         for (int o = 0; o < kNumOut; ++o) {
-                            if ((isKey[o] && nullKey) || (!isKey[o] && !isFlag[o] && !h)) {
+                            if ((isKey[o] && nullKey) || (!isKey[o] && !isFlag[o] && !isProbe[o] && !h)) {
                                 SetBit(p.out[o].nulls, at);
                             }
                         }
@@ -2205,12 +2456,53 @@ void SetBulkProbe(int mode) { g_bulkProbe.store(mode == 1 || mode == 2 ? mode : 
 
 int LastProbeKernel() { return g_lastProbeKernel.load(); }
 
+// The bitmap kernel takes the kinds that mark no build rows on an ARRAY table whose occupancy
+// bitmap fits in shared memory, on launches large enough to amortise staging it into every CTA;
+// its outputs are the probe key, other fixed-width probe columns (*probeCols), payload fields
+// (a slot payload present) and the existence flag.
+bool BitsProbeEligible(const ProbeLaunch &p, bool *probeCols)
+{
+    const bool bitsKind = p.joinKind == JOIN_KIND_INNER || p.joinKind == JOIN_KIND_PROBE_OUTER ||
+        p.joinKind == JOIN_KIND_SEMI || p.joinKind == JOIN_KIND_ANTI || p.joinKind == JOIN_KIND_EXISTENCE;
+    bool ok = bitsKind && p.nKeyCols == 0 && p.table.unique && p.keyWidth == 8 && p.nOut >= 1 &&
+        p.nOut <= kFastMaxOut && p.table.mode == JOIN_ARRAY && p.table.slotBits != nullptr &&
+        SlotBitsBytes(p.table.range) <= kBitsMaxSmem && p.nTiles >= kBitsMinTiles;
+    bool cols = false;
+    for (int o = 0; ok && o < p.nOut; ++o) {
+        const JoinOutCol &oc = p.out[o];
+        ok = ((oc.side == 1 && p.table.slotPayload != nullptr) || (oc.side == 0 && oc.src == p.keyInput && oc.width == 8) ||
+                 (oc.side == 0 && oc.src != p.keyInput) || oc.side == 2) &&
+            (oc.width == 1 || oc.width == 2 || oc.width == 4 || oc.width == 8);
+        cols = cols || (oc.side == 0 && oc.src != p.keyInput);
+    }
+    if (probeCols != nullptr) {
+        *probeCols = cols;
+    }
+    return ok;
+}
+
+// Only the bitmap kernel packs multi-column keys as it reads them (keys of up to two parts).
+bool ProbePacksKeys(const ProbeLaunch &p)
+{
+    return p.pack.nParts <= kFusedPackParts && p.nFilter == 0 && BitsProbeEligible(p, nullptr);
+}
+
 cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
 {
     if (p.nTiles <= 0) {
         return cudaSuccess;
     }
-    if (p.nKeyCols > 0 || p.nFilter > 0) {
+    if (p.pack.nParts > 0 && !ProbePacksKeys(p)) {
+        // The chosen kernel reads the packed keys from the scratch input: fill it first.
+        ProbeLaunch q = p;
+        cudaError_t err = LaunchPackProbeKeys(p.batches, p.tiles, p.nTiles, p.pack, stream);
+        if (err != cudaSuccess) {
+            return err;
+        }
+        q.pack.nParts = 0;
+        return LaunchProbe(q, stream);
+    }
+    if (p.nKeyCols > 0 || (p.nFilter > 0 && !BitsProbeEligible(p, nullptr))) {
         const int maxGrid = SMs() * BlocksPerSM(reinterpret_cast<const void *>(ProbeKindKernel), kProbeThreads, 0);
         g_lastProbeKernel.store(PROBE_KERNEL_KIND);
         ProbeKindKernel<<<p.nTiles < maxGrid ? p.nTiles : maxGrid, kProbeThreads, 0, stream>>>(p);
@@ -2224,23 +2516,9 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
         fast = (oc.side == 1 || (oc.side == 0 && oc.src == p.keyInput && oc.width == 8)) &&
             (oc.width == 1 || oc.width == 2 || oc.width == 4 || oc.width == 8);
     }
-    // The bitmap kernel also takes the kinds that mark no build rows; its outputs are the probe
-    // key, payload fields (a slot payload present) and the existence flag.
-    const bool bitsKind = p.joinKind == JOIN_KIND_INNER || p.joinKind == JOIN_KIND_PROBE_OUTER ||
-        p.joinKind == JOIN_KIND_SEMI || p.joinKind == JOIN_KIND_ANTI || p.joinKind == JOIN_KIND_EXISTENCE;
-    bool bitsOk = bitsKind && p.nKeyCols == 0 && p.table.unique && p.keyWidth == 8 && p.nOut >= 1 &&
-        p.nOut <= kFastMaxOut;
-    for (int o = 0; bitsOk && o < p.nOut; ++o) {
-        const JoinOutCol &oc = p.out[o];
-        bitsOk = ((oc.side == 1 && p.table.slotPayload != nullptr) ||
-                     (oc.side == 0 && oc.src == p.keyInput && oc.width == 8) || oc.side == 2) &&
-            (oc.width == 1 || oc.width == 2 || oc.width == 4 || oc.width == 8);
-    }
-    // ARRAY tables whose occupancy bitmap fits in shared memory, on launches large enough to
-    // amortise staging it into every CTA.
+    bool probeCols = false;  // an output is a probe column other than the key
     const uint64_t bitsBytes = SlotBitsBytes(p.table.range);
-    if (bitsOk && p.table.mode == JOIN_ARRAY && p.table.slotBits != nullptr && bitsBytes <= kBitsMaxSmem &&
-        p.nTiles >= kBitsMinTiles) {
+    if (BitsProbeEligible(p, &probeCols)) {
         // Instances: run-time widths for 1-4 outputs, and compile-time widths for the common
         // layouts (8-byte key followed by payload fields).
         struct Inst {
@@ -2258,22 +2536,36 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             OMG_GROUP_INST(4, 0),
         };
 #undef OMG_GROUP_INST
+#define OMG_BITS_INST(n, layout, cols, packed)                                                              \
+    {layout, n, reinterpret_cast<const void *>(ProbeBitsKernel<n, layout, true, cols, packed>),            \
+        reinterpret_cast<const void *>(ProbeBitsKernel<n, layout, false, cols, packed>)}
+#define OMG_FILTER_INST(n)                                                                                  \
+    {0, n, reinterpret_cast<const void *>(ProbeBitsKernel<n, 0, true, true, 0, true>),                     \
+        reinterpret_cast<const void *>(ProbeBitsKernel<n, 0, false, true, 0, true>)}
         static const Inst insts[] = {
-            {OutLayout(kW8, kW4, kW4), 3, reinterpret_cast<const void *>(ProbeBitsKernel<3, OutLayout(kW8, kW4, kW4), true>),
-                reinterpret_cast<const void *>(ProbeBitsKernel<3, OutLayout(kW8, kW4, kW4), false>)},
-            {OutLayout(kW8, kW8), 2, reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW8), true>),
-                reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW8), false>)},
-            {OutLayout(kW8, kW4), 2, reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW4), true>),
-                reinterpret_cast<const void *>(ProbeBitsKernel<2, OutLayout(kW8, kW4), false>)},
-            {0, 1, reinterpret_cast<const void *>(ProbeBitsKernel<1, 0, true>),
-                reinterpret_cast<const void *>(ProbeBitsKernel<1, 0, false>)},
-            {0, 2, reinterpret_cast<const void *>(ProbeBitsKernel<2, 0, true>),
-                reinterpret_cast<const void *>(ProbeBitsKernel<2, 0, false>)},
-            {0, 3, reinterpret_cast<const void *>(ProbeBitsKernel<3, 0, true>),
-                reinterpret_cast<const void *>(ProbeBitsKernel<3, 0, false>)},
-            {0, 4, reinterpret_cast<const void *>(ProbeBitsKernel<4, 0, true>),
-                reinterpret_cast<const void *>(ProbeBitsKernel<4, 0, false>)},
+            OMG_BITS_INST(3, OutLayout(kW8, kW4, kW4), false, 0), OMG_BITS_INST(2, OutLayout(kW8, kW8), false, 0),
+            OMG_BITS_INST(2, OutLayout(kW8, kW4), false, 0), OMG_BITS_INST(1, 0, false, 0),
+            OMG_BITS_INST(2, 0, false, 0), OMG_BITS_INST(3, 0, false, 0), OMG_BITS_INST(4, 0, false, 0),
         };
+        // Probe columns other than the key among the outputs, or a packed key: run-time widths.
+        static const Inst colInsts[] = {
+            OMG_BITS_INST(1, 0, true, 0), OMG_BITS_INST(2, 0, true, 0), OMG_BITS_INST(3, 0, true, 0),
+            OMG_BITS_INST(4, 0, true, 0),
+        };
+        static const Inst packedInsts[] = {
+            OMG_BITS_INST(1, 0, true, 1), OMG_BITS_INST(2, 0, true, 1), OMG_BITS_INST(3, 0, true, 1),
+            OMG_BITS_INST(4, 0, true, 1),
+        };
+        // Two 4-byte key parts: the two parts and two 4-byte payload fields, or run-time widths.
+        static const Inst two32Insts[] = {
+            OMG_BITS_INST(4, OutLayout(kW4, kW4, kW4, kW4), true, 2), OMG_BITS_INST(1, 0, true, 2),
+            OMG_BITS_INST(2, 0, true, 2), OMG_BITS_INST(3, 0, true, 2), OMG_BITS_INST(4, 0, true, 2),
+        };
+        static const Inst filterInsts[] = {
+            OMG_FILTER_INST(1), OMG_FILTER_INST(2), OMG_FILTER_INST(3), OMG_FILTER_INST(4),
+        };
+#undef OMG_BITS_INST
+#undef OMG_FILTER_INST
         constexpr int kInsts = static_cast<int>(sizeof(insts) / sizeof(insts[0]));
         int pick = -1;
         for (int i = 0; i < kInsts && pick < 0; ++i) {
@@ -2288,6 +2580,31 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             pick = match ? i : -1;
         }
         const int single = p.singleBatch ? 0 : 1;
+        if (probeCols || p.pack.nParts > 0 || p.nFilter > 0) {
+            const bool filter = p.nFilter > 0;
+            const bool packed = p.pack.nParts > 0 && !filter;
+            const bool two32 = packed && p.pack.nParts == 2 && p.pack.width[0] == 4 && p.pack.width[1] == 4;
+            const Inst *ci = filter ? &filterInsts[p.nOut - 1] : (packed ? &packedInsts[p.nOut - 1] : &colInsts[p.nOut - 1]);
+            if (two32) {
+                bool w4 = p.nOut == 4;
+                for (int o = 0; w4 && o < p.nOut; ++o) {
+                    w4 = p.out[o].width == 4;
+                }
+                ci = w4 ? &two32Insts[0] : &two32Insts[p.nOut];
+            }
+            const void *ck = single == 0 ? ci->single : ci->tiled;
+            cudaError_t cerr = EnsureDynamicSmem(ck, kBitsMaxSmem);
+            if (cerr != cudaSuccess) {
+                return cerr;
+            }
+            const int threads = packed || filter ? BitsThreads<1, true>::value : BitsThreads<0, false>::value;
+            const int64_t items = static_cast<int64_t>(p.nTiles) * kBitsSegsPerTile;
+            const int64_t wanted = (items + threads / 32 - 1) / (threads / 32);
+            const int grid = static_cast<int>(wanted < SMs() ? wanted : SMs());
+            void *cargs[] = {const_cast<ProbeLaunch *>(&p)};
+            g_lastProbeKernel.store(PROBE_KERNEL_BITS);
+            return cudaLaunchKernel(ck, dim3(grid), dim3(threads), cargs, static_cast<size_t>(bitsBytes), stream);
+        }
         // Inner joins whose outputs are the probe key and payload fields, written to pinned host
         // memory, take the staged kernel when its shared memory (bitmap + the groups' staging)
         // fits: whole-line output runs carry the link at its rate (with HBM output the per-warp
@@ -2404,6 +2721,27 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
     const int grid = p.nTiles < maxGrid ? p.nTiles : maxGrid;
     g_lastProbeKernel.store(fast ? PROBE_KERNEL_FAST : PROBE_KERNEL_GENERAL);
     kernel<<<grid, kProbeThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchPackBuildKeys(const JoinKeyCols &kc, const JoinKeyPack &kp, int64_t n, int64_t *out,
+    uint8_t *outNulls, cudaStream_t stream)
+{
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    PackBuildKeysKernel<<<GridFor(n, 256, 8), 256, 0, stream>>>(kc, kp, n, out, reinterpret_cast<uint32_t *>(outNulls));
+    return cudaGetLastError();
+}
+
+cudaError_t LaunchPackProbeKeys(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, const JoinKeyPack &kp,
+    cudaStream_t stream)
+{
+    if (nTiles <= 0) {
+        return cudaSuccess;
+    }
+    const int grid = nTiles < SMs() * 8 ? nTiles : SMs() * 8;
+    PackProbeKeysKernel<<<grid, 256, 0, stream>>>(batches, tiles, nTiles, kp);
     return cudaGetLastError();
 }
 

@@ -155,6 +155,15 @@ cudaError_t LaunchDictGatherChars(const int32_t *ids, int64_t n, const int32_t *
     const uint8_t *dictNulls, int32_t dictSize, const int64_t *offs64, uint8_t *chars, int32_t *offs32,
     long long total, cudaStream_t stream);
 // Multi-column join keys: the tuple hash of each build row (NULL if a key column is NULL).
+// Packed multi-column join keys (JoinKeyPack): of the build's contiguous key columns into `out`
+// (+ NULL bitmap), and of the probe batches' key parts into input kp.outInput of each batch.
+cudaError_t LaunchPackBuildKeys(const JoinKeyCols &kc, const JoinKeyPack &kp, int64_t n, int64_t *out,
+    uint8_t *outNulls, cudaStream_t stream);
+// True when LaunchProbe's kernel for `p` packs the key parts (p.pack) itself; otherwise it runs
+// the packing pass into the scratch input p.pack.outInput first.
+bool ProbePacksKeys(const ProbeLaunch &p);
+cudaError_t LaunchPackProbeKeys(const BatchDesc *batches, const TileDesc *tiles, int32_t nTiles, const JoinKeyPack &kp,
+    cudaStream_t stream);
 cudaError_t LaunchJoinKeyHash(const JoinKeyCols &kc, int64_t n, uint64_t *out, uint8_t *outNulls, cudaStream_t stream);
 // Outer joins: flags[i] = 1 for build rows never matched; their row numbers in order (offsets =
 // exclusive scan of the flags); dst[i] = src[rows[i]] with NULL bits.

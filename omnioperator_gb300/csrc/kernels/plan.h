@@ -390,6 +390,21 @@ struct JoinKeyCols {
     const int64_t *offs[kMaxJoinKeys];  // VARCHAR offsets
 };
 
+// Multi-column join keys of fixed widths (1-8 bytes each) packed into one 64-bit key: part k of
+// a row, its value sign-extended from width[k] bytes, contributes (v - minv[k]) * stride[k].  The
+// build's per-part value ranges [minv[k], minv[k] + span[k]) multiply to at most 2^62, so packed
+// build keys are non-negative; a probe row with a part outside its range gets key -1, which no
+// build row has.  NULL in any part makes the packed key NULL.
+struct JoinKeyPack {
+    int32_t nParts;
+    int32_t outInput;  // probe side: the kernel input whose column the packed keys are written to
+    int32_t input[kMaxJoinKeys];
+    int32_t width[kMaxJoinKeys];
+    int64_t minv[kMaxJoinKeys];
+    uint64_t span[kMaxJoinKeys];
+    uint64_t stride[kMaxJoinKeys];
+};
+
 // Join filter (the LookupJoin filter expression, lookup_join.cpp:175-187,1440-1466) compiled to a
 // postfix program over one (probe row, build row) candidate pair.  Values are 64-bit integers or
 // doubles with a NULL flag; comparisons and NOT/AND/OR follow SQL three-valued logic, and a pair
@@ -454,6 +469,9 @@ struct ProbeLaunch {
     JoinKeyCol keyCols[kMaxJoinKeys];
     int32_t nFilter;    // > 0: candidate pairs must pass the filter program
     FilterInstr filter[kMaxFilterInstrs];
+    // nParts > 0: the key is the packed multi-column key; keyInput (= pack.outInput) is a scratch
+    // column that LaunchProbe fills with a packing pass unless the kernel packs the parts itself.
+    JoinKeyPack pack;
 };
 
 }  // namespace omg

@@ -247,3 +247,45 @@ def test_int_arithmetic_wraps_at_32_bits():
                    [1], filt, batch_sizes=(n,))
         want = sorted((int(k), int(p), int(b)) for k, p, b in zip(key, pv, bv) if int(p) + int(b) > 2**31 - 1)
         assert len(want) > 0 and sorted(rows) == want
+
+
+@pytest.mark.parametrize("join_type", ["INNER", "LEFT", "LEFT_SEMI", "LEFT_ANTI", "EXISTENCE"])
+@pytest.mark.parametrize("fname", list(FILTERS))
+def test_filtered_bitmap_probe_matches_oracle(join_type, fname):
+    """A unique ARRAY build probed in one large batch: the bitmap kernel evaluates the filter on
+    each probe row's one candidate (its slot's build row) and must equal the oracle's filtered
+    join; build output columns are NULL-free so that they come from the packed slot payload."""
+    rng = np.random.default_rng(len(join_type) * 7 + len(fname))
+    nb, npr = 1 << 15, 300_000
+    bkey = rng.permutation(nb).astype(np.int64)
+    bv = rng.integers(-20, 20, nb).astype(np.int64)
+    bd = rng.random(nb)
+    bw = rng.integers(-2**31, 2**31, nb, dtype=np.int64).astype(np.int32)
+    bm = [np.zeros(nb, bool), rng.random(nb) < 0.1, rng.random(nb) < 0.1, np.zeros(nb, bool)]
+    pkey = rng.integers(0, nb + nb // 5, npr).astype(np.int64)
+    pv = rng.integers(-20, 20, npr).astype(np.int64)
+    pd = rng.random(npr)
+    pm = [rng.random(npr) < 0.03, rng.random(npr) < 0.1, rng.random(npr) < 0.1]
+    bcols, pcols = [bkey, bv, bd, bw], [pkey, pv, pd]
+    kind = oracle.join_kind(join_type, "UNKNOWN")
+    pout = [0, 1, 2]
+    bout = [] if kind in ("semi", "anti", "existence") else [3]
+    filt = FILTERS[fname]
+    got = run(join_type, "UNKNOWN", [L, L, D, I], bcols, bm, [L, L, D], pcols, pm, pout, bout, filt,
+              batch_sizes=(npr,))
+    assert omg.lib().omg_debug_last_probe_kernel() == 4  # the bitmap kernel
+    pi, bi = oracle.join_filtered(kind, bkey, bm[0], pkey, pm[0], _passes(filt, pcols, pm, bcols, bm))
+
+    def val(cols, masks, c, r):
+        if r < 0 or masks[c][r]:
+            return None
+        v = cols[c][r]
+        return float(v) if isinstance(v, np.floating) else int(v)
+
+    want = []
+    for i, j in zip(pi.tolist(), bi.tolist()):
+        r = [val(pcols, pm, c, i) for c in pout]
+        r += [j] if kind == "existence" else [val(bcols, bm, c, j) for c in bout]
+        want.append(tuple(r))
+    assert len(want) > 0
+    assert sorted(got, key=_key) == sorted(want, key=_key)
