@@ -122,6 +122,11 @@ int32_t omg_debug_set_bulk_probe(int32_t mode);
  * and stores, 5 group-staged (pinned host output), 6 bulk-copy; 0 none yet.  For tests and
  * measurements.  No reference counterpart. */
 int32_t omg_debug_last_probe_kernel(void);
+/* Train sizing and CDF models of two hidden layers (input <= 16, hidden widths multiples of 4 up
+ * to 64) with the fused kernel, all epochs in one cooperative launch (1, default), or layer by
+ * layer with one launch per layer and step (0).  For tests and measurements.  No reference
+ * counterpart. */
+int32_t omg_debug_set_fused_training(int32_t on);
 /* Staged rows at which a HashAggregation operator aggregates its queued batches before
  * GetOutput (0 = library default, 2^28).  Process-wide; lets tests run many batch sets
  * through one operator. */

@@ -31,6 +31,7 @@ _SIGS = {
     "omg_debug_set_staged_probe": (I32, [I32]),
     "omg_debug_set_bulk_probe": (I32, [I32]),
     "omg_debug_last_probe_kernel": (I32, []),
+    "omg_debug_set_fused_training": (I32, [I32]),
     "omg_op_set_agg_sizing": (I32, [P, I32]),
     "omg_debug_set_agg_flush_rows": (I32, [I64]),
     "omg_vec_new": (I32, [I32, I32, C.POINTER(P)]),

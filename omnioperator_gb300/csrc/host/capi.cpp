@@ -139,6 +139,12 @@ int32_t omg_debug_set_staged_probe(int32_t on)
 
 int32_t omg_debug_last_probe_kernel(void) { return omg::LastProbeKernel(); }
 
+int32_t omg_debug_set_fused_training(int32_t on)
+{
+    omg::SetFusedTraining(on != 0);
+    return OMG_OK;
+}
+
 int32_t omg_debug_set_bulk_probe(int32_t mode)
 {
     return Guard([&] {

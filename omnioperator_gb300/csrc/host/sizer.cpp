@@ -1,4 +1,5 @@
 // Learned sizing model (see sizer.h).
+#include <atomic>
 #include "host/sizer.h"
 
 #include <algorithm>
@@ -260,12 +261,64 @@ float SizingModel::Gradients(const float *X, const float *T, int32_t n, float *g
         throw OmniException("INVALID_ARGUMENT", "empty batch", -1);
     }
     Upload(X, T, n);
-    Forward(n);
-    const float loss = Backward(n);
+    float loss;
+    if (Fused()) {
+        loss = RunFused(n, 1, 0.f, grads_.Get());
+    } else {
+        Forward(n);
+        loss = Backward(n);
+    }
     CudaCheck(cudaMemcpyAsync(grad, grads_.Get(), sizeof(float) * nParams_, cudaMemcpyDeviceToHost, stream_),
         "read gradients");
     CudaCheck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
     return loss;
+}
+
+namespace {
+std::atomic<bool> g_fusedTraining{true};
+}
+
+void SetFusedTraining(bool on) { g_fusedTraining.store(on); }
+
+bool SizingModel::Fused() const
+{
+    return g_fusedTraining.load() && dims_.size() == 4 && MlpFusedSupported(dims_[0], dims_[1], dims_[2]);
+}
+
+// The fused kernel over the uploaded batch: `epochs` Adam steps, or (gradOut non-null) the
+// gradient of one pass into gradOut with nothing updated.  Returns the mean squared error of the
+// last pass.
+float SizingModel::RunFused(int32_t n, int32_t epochs, float lr, float *gradOut)
+{
+    const int grid = MlpFusedGrid(n);
+    partial_.Reset(static_cast<size_t>(grid) * static_cast<size_t>(nParams_), stream_);
+    CudaCheck(cudaMemsetAsync(loss_.Get(), 0, sizeof(float), stream_), "reset loss");
+    MlpFusedArgs a{};
+    a.X = x_.Get();
+    a.T = t_.Get();
+    a.n = n;
+    a.F = dims_[0];
+    a.H1 = dims_[1];
+    a.H2 = dims_[2];
+    a.nParams = static_cast<int32_t>(nParams_);
+    a.epochs = epochs;
+    a.params = params_.Get();
+    a.adamM = adamM_.Get();
+    a.adamV = adamV_.Get();
+    a.partial = partial_.Get();
+    a.loss = loss_.Get();
+    a.gradOut = gradOut;
+    a.lr = lr;
+    a.b1 = 0.9f;
+    a.b2 = 0.999f;
+    a.eps = 1e-8f;
+    a.b1Pow = std::pow(static_cast<double>(a.b1), step_);
+    a.b2Pow = std::pow(static_cast<double>(a.b2), step_);
+    CudaCheck(LaunchMlpTrainFused(a, grid, stream_), "fused training");
+    float loss = 0.f;
+    CudaCheck(cudaMemcpyAsync(&loss, loss_.Get(), sizeof(float), cudaMemcpyDeviceToHost, stream_), "read loss");
+    CudaCheck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return loss / static_cast<float>(n);
 }
 
 float SizingModel::Train(const float *X, const float *T, int32_t n, int32_t epochs, float lr)
@@ -275,6 +328,12 @@ float SizingModel::Train(const float *X, const float *T, int32_t n, int32_t epoc
         throw OmniException("INVALID_ARGUMENT", "empty batch or no epochs", -1);
     }
     Upload(X, T, n);
+    if (Fused()) {
+        // All epochs in one cooperative launch.
+        const float loss = RunFused(n, epochs, lr, nullptr);
+        step_ += epochs;
+        return loss;
+    }
     float loss = 0.f;
     for (int32_t e = 0; e < epochs; ++e) {
         Forward(n);

@@ -42,6 +42,10 @@ void LearnRangeSplits(const int64_t *sample, int64_t n, int32_t bits, int32_t ep
 // floor(k * n / 2^bits) (the method without a network, for comparison with the learned splits).
 void QuantileSplits(const int64_t *sample, int64_t n, int32_t bits, int64_t *splits);
 
+// Process-wide: train the two-hidden-layer shapes with the fused kernel (default) or layer by
+// layer; for tests and measurements.
+void SetFusedTraining(bool on);
+
 class SizingModel {
 public:
     // dims: input width, hidden widths..., 1.  Weights: He-uniform from `seed`, biases zero.
@@ -66,6 +70,8 @@ private:
     void Forward(int32_t n);
     float Backward(int32_t n);
     void Upload(const float *X, const float *T, int32_t n);
+    bool Fused() const;
+    float RunFused(int32_t n, int32_t epochs, float lr, float *gradOut);
 
     std::vector<int32_t> dims_;
     std::vector<int64_t> wOff_, bOff_;  // offsets of each layer's W and b in the parameter vector
@@ -74,6 +80,7 @@ private:
     cudaStream_t stream_ = nullptr;
     DevArray<float> params_, grads_, adamM_, adamV_;
     DevArray<float> x_, t_, loss_;
+    DevArray<float> partial_;  // fused training: per-CTA gradient sums
     std::vector<DevArray<float>> act_;   // activations per layer output
     std::vector<DevArray<float>> dact_;  // their gradients
     int32_t capacity_ = 0;

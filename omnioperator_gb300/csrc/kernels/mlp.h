@@ -23,4 +23,31 @@ cudaError_t LaunchMseGrad(const float *Y, const float *T, float *dY, int64_t tot
 cudaError_t LaunchAdam(float *w, const float *g, float *m, float *v, int64_t n, float lr, float b1, float b2,
     float eps, int step, cudaStream_t s);
 
+// Fused full-batch training of a network F -> H1 -> H2 -> 1 (ReLU hidden layers, MSE loss, Adam):
+// all epochs in one cooperative launch.  Each CTA keeps the weights in shared memory, runs the
+// forward and backward passes over tiles of its share of the points and writes its gradient sums;
+// after a grid barrier every CTA reduces a slice of the parameters over all CTAs' sums (in CTA
+// order, so the result is deterministic) and applies Adam to it; after a second barrier every CTA
+// reloads the weights.  Parameter layout as SizingModel: W1 (F x H1), b1, W2 (H1 x H2), b2, W3, b3.
+struct MlpFusedArgs {
+    const float *X;   // [n, F]
+    const float *T;   // [n]
+    int32_t n, F, H1, H2;
+    int32_t nParams;
+    int32_t epochs;
+    float *params;    // updated in place
+    float *adamM;
+    float *adamV;
+    float *partial;   // [grid, nParams] scratch
+    float *loss;      // sum of squared errors of the last epoch (before its update), may be null
+    float *gradOut;   // non-null: write the mean-loss gradient of the first epoch here, update nothing
+    float lr, b1, b2, eps;
+    double b1Pow, b2Pow;  // b1^step and b2^step before the first epoch
+};
+// True when the fused trainer takes these dims (F <= 16, H1 and H2 multiples of 4 up to 64).
+bool MlpFusedSupported(int F, int H1, int H2);
+// Launches the fused trainer; `grid` (<= the SM count, from MlpFusedGrid) CTAs.
+int MlpFusedGrid(int n);
+cudaError_t LaunchMlpTrainFused(const MlpFusedArgs &a, int grid, cudaStream_t s);
+
 }  // namespace omg

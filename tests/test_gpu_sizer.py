@@ -24,18 +24,63 @@ def test_forward_matches_oracle(gpu):
     m.close()
 
 
-def test_gradients_match_oracle(gpu):
-    """fp32 kernels against float64 backpropagation: |g - g_ref| <= 1e-3 * max|g_ref| + 1e-6."""
-    m = sz.SizingModel((12, 32, 32, 1), seed=4)
-    rng = np.random.default_rng(2)
-    X = rng.random((200, 12)).astype(np.float32)
-    T = rng.random(200).astype(np.float32)
-    g, loss = m.gradients(X, T)
-    ref_loss, ref_g = mlp_ref.loss_and_grad(m.get_params().astype(np.float64), m.dims, X.astype(np.float64),
-                                            T.astype(np.float64))
-    assert abs(loss - ref_loss) <= 1e-4 * max(ref_loss, 1e-6)
-    np.testing.assert_allclose(g, ref_g, rtol=0, atol=1e-3 * np.abs(ref_g).max() + 1e-6)
-    m.close()
+@pytest.mark.parametrize("fused", [1, 0])
+@pytest.mark.parametrize("dims,n", [((12, 32, 32, 1), 200), ((1, 32, 32, 1), 5000), ((12, 64, 64, 1), 3000),
+                                    ((12, 16, 8, 1), 200)])
+def test_gradients_match_oracle(gpu, fused, dims, n):
+    """fp32 kernels against float64 backpropagation: |g - g_ref| <= 1e-3 * max|g_ref| + 1e-6, for
+    the fused trainer (one cooperative launch, gradients summed per CTA then over CTAs) and the
+    layer-by-layer kernels ((12, 16, 8, 1) is not a fused shape: layer by layer either way)."""
+    try:
+        omg.lib().omg_debug_set_fused_training(fused)
+        m = sz.SizingModel(dims, seed=4)
+        rng = np.random.default_rng(2)
+        X = rng.random((n, dims[0])).astype(np.float32)
+        T = rng.random(n).astype(np.float32)
+        g, loss = m.gradients(X, T)
+        ref_loss, ref_g = mlp_ref.loss_and_grad(m.get_params().astype(np.float64), m.dims, X.astype(np.float64),
+                                                T.astype(np.float64))
+        assert abs(loss - ref_loss) <= 1e-4 * max(ref_loss, 1e-6)
+        np.testing.assert_allclose(g, ref_g, rtol=0, atol=1e-3 * np.abs(ref_g).max() + 1e-6)
+        m.close()
+    finally:
+        omg.lib().omg_debug_set_fused_training(1)
+
+
+def test_fused_and_layer_by_layer_training_agree(gpu):
+    """The same model trained fused and layer by layer: Adam steps of at most lr per weight, so
+    their weights stay within a few steps of each other and their losses agree."""
+    rng = np.random.default_rng(8)
+    X = rng.random((2048, 12)).astype(np.float32)
+    T = (0.5 * X[:, 0] + 0.25 * np.sin(3 * X[:, 1]) + 0.1 * X[:, 2] * X[:, 3]).astype(np.float32)
+    out = {}
+    try:
+        for fused in (1, 0):
+            omg.lib().omg_debug_set_fused_training(fused)
+            m = sz.SizingModel((12, 64, 64, 1), seed=9)
+            m.train(X, T, epochs=300, lr=1e-3)
+            out[fused] = (m.get_params(), float(np.mean((m.predict(X) - T) ** 2)))
+            m.close()
+    finally:
+        omg.lib().omg_debug_set_fused_training(1)
+    (p1, l1), (p0, l0) = out[1], out[0]
+    assert np.median(np.abs(p1 - p0)) < 1e-3 and np.abs(p1 - p0).max() < 0.3
+    assert abs(l1 - l0) <= 0.2 * max(l0, 1e-4), (l1, l0)
+
+
+def test_learned_splits_train_in_milliseconds(gpu):
+    """The CDF network of the learned range partitioner (1 -> 32 -> 32 -> 1, 16,384 points, 2,000
+    Adam epochs) trains in one fused launch; the splits cut a skewed sample into near-equal ranges."""
+    import time
+    rng = np.random.default_rng(10)
+    sample = (rng.zipf(1.3, 1 << 16) % (1 << 30)).astype(np.int64)
+    omg.learn_splits(sample, bits=8, epochs=10)  # warm-up: module load, allocations
+    t0 = time.perf_counter()
+    splits = omg.learn_splits(sample, bits=8, epochs=2000)
+    ms = (time.perf_counter() - t0) * 1e3
+    print(f"learned 255 splits from {len(sample)} keys in {ms:.1f} ms")
+    assert ms < 500, ms
+    assert np.all(np.diff(splits) >= 0)
 
 
 def test_training_fits_a_smooth_function(gpu):
