@@ -154,6 +154,7 @@ SizingModel::~SizingModel()
         x_.Release();
         t_.Release();
         loss_.Release();
+        partial_.Release();
         act_.clear();
         dact_.clear();
         cudaStreamSynchronize(stream_);
