@@ -131,6 +131,10 @@ int32_t omg_debug_set_fused_training(int32_t on);
  * GetOutput (0 = library default, 2^28).  Process-wide; lets tests run many batch sets
  * through one operator. */
 int32_t omg_debug_set_agg_flush_rows(int64_t rows);
+/* Queued probe rows at which a pipelined LookupJoin operator (SetNoMoreInput(false) callers)
+ * hands a chunk to its worker thread (0 = library default, 2^22).  Process-wide; lets tests run
+ * the worker pipeline on small inputs. */
+int32_t omg_debug_set_probe_chunk_rows(int64_t rows);
 
 /* ---- OmniVec: vectors and batches -------------------------------------------------- */
 /* New flat host vector (VectorHelper::CreateFlatVector, vector/vector_helper.h).

@@ -34,6 +34,7 @@ _SIGS = {
     "omg_debug_set_fused_training": (I32, [I32]),
     "omg_op_set_agg_sizing": (I32, [P, I32]),
     "omg_debug_set_agg_flush_rows": (I32, [I64]),
+    "omg_debug_set_probe_chunk_rows": (I32, [I64]),
     "omg_vec_new": (I32, [I32, I32, C.POINTER(P)]),
     "omg_vec_new_fixed": (I32, [I32, I32, C.POINTER(P)]),
     "omg_vec_new_varchar": (I32, [I32, I32, I64, C.POINTER(P)]),

@@ -159,6 +159,12 @@ int32_t omg_debug_set_agg_flush_rows(int64_t rows)
     return OMG_OK;
 }
 
+int32_t omg_debug_set_probe_chunk_rows(int64_t rows)
+{
+    omg::SetProbeChunkRows(rows < 0 ? 0 : rows);
+    return OMG_OK;
+}
+
 // ---- vectors
 int32_t omg_vec_new(int32_t type_id, int32_t size, void **out_vec)
 {

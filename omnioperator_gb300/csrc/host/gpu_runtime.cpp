@@ -259,6 +259,16 @@ int64_t AggFlushRows()
 }
 void SetAggFlushRows(int64_t rows) { g_aggFlushRows.store(rows); }
 
+namespace {
+std::atomic<int64_t> g_probeChunkRows{0};
+}
+int64_t ProbeChunkRows()
+{
+    const int64_t r = g_probeChunkRows.load();
+    return r > 0 ? r : (int64_t(1) << 22);
+}
+void SetProbeChunkRows(int64_t rows) { g_probeChunkRows.store(rows); }
+
 std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows, int32_t rowsPerBatch,
     int64_t firstRow)
 {

@@ -251,6 +251,9 @@ void SetWaitBudget(long long ticks);
 // Staged rows at which an aggregation operator flushes its queued batches; 0 restores 2^28.
 int64_t AggFlushRows();
 void SetAggFlushRows(int64_t rows);
+// Queued probe rows at which a pipelined probe operator launches a chunk; 0 restores 2^22.
+int64_t ProbeChunkRows();
+void SetProbeChunkRows(int64_t rows);
 
 // Cut `rows` rows of contiguous output columns into VectorBatches of at most
 // `rowsPerBatch` rows that are views of the given buffers (host or device).

@@ -1,12 +1,15 @@
 // HashBuilder / LookupJoin operators (see omniop/hash_join.h).
 #include "omniop/hash_join.h"
 
-#include <chrono>
-
 #include <algorithm>
+#include <chrono>
+#include <condition_variable>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <memory>
+#include <mutex>
+#include <thread>
 
 #include "host/gpu_runtime.h"
 #include "omniop/expressions.h"
@@ -22,7 +25,6 @@ using omg::DevArray;
 using namespace type;
 
 namespace {
-constexpr int64_t kProbeChunkRows = int64_t(1) << 22;  // pipelined callers: probe 4M rows per launch
 
 uint64_t NextPow2(uint64_t v)
 {
@@ -769,16 +771,61 @@ struct LookupJoinOperator::ProbeCall {
 struct LookupJoinOperator::Impl {
     omg::OpStream stream;
     omg::KernelTimer timer;
-    // Probe calls launched by AddInput (pipelined callers), oldest first.
+    // Probe calls launched and not yet finished, oldest first (the worker's once it runs).
     std::deque<std::unique_ptr<ProbeCall>> inflight;
+    // Worker pipeline (pipelined callers).  The caller hands over full chunks of batches; the
+    // worker launches each chunk's probe, finishes the oldest call once another is queued behind
+    // it (or its kernel is done, or a flush was asked for) and moves its output batches to
+    // `ready`.  `busy` counts chunks handed over and not finished.
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable wake;      // to the worker: a chunk, a flush or stop
+    std::condition_variable progress;  // to the caller: a chunk finished, or an error
+    std::deque<std::vector<VectorBatch *>> chunks;
+    std::deque<VectorBatch *> ready;
+    int32_t busy = 0;
+    bool flush = false;
+    bool stop = false;
+    std::exception_ptr error;
+    int device = 0;
 };
+
+namespace {
+constexpr int32_t kMaxChunksAhead = 3;  // chunks handed to the worker before AddInput waits
+}
 
 LookupJoinOperator::LookupJoinOperator(const LookupJoinOperatorFactory &f) : f_(f), impl_(new Impl()) {}
 
 LookupJoinOperator::~LookupJoinOperator() { Close(); }
 
+void LookupJoinOperator::StopWorker()
+{
+    Impl &im = *impl_;
+    if (!im.worker.joinable()) {
+        return;
+    }
+    {
+        std::lock_guard<std::mutex> g(im.mu);
+        im.stop = true;
+    }
+    im.wake.notify_all();
+    im.worker.join();
+    for (auto &c : im.chunks) {
+        for (auto *b : c) {
+            vec::VectorHelper::FreeVecBatch(b);
+        }
+    }
+    im.chunks.clear();
+    for (auto *b : im.ready) {
+        vec::VectorHelper::FreeVecBatch(b);
+    }
+    im.ready.clear();
+    im.busy = 0;
+}
+
 OmniStatus LookupJoinOperator::Close()
 {
+    StopWorker();
     impl_->inflight.clear();  // waits for their kernels, frees their batches
     for (auto *b : pending_) {
         vec::VectorHelper::FreeVecBatch(b);
@@ -816,13 +863,139 @@ int32_t LookupJoinOperator::AddInput(VectorBatch *vecBatch)
     pending_.push_back(vecBatch);
     pendingRows_ += vecBatch->GetRowCount();
     SetStatus(OMNI_STATUS_NORMAL);
-    // Pipelined callers: a full chunk is launched at once, so that its kernel runs while the
-    // caller queues the next chunk and GetOutput carves the previous one.
-    if (!noMoreInput_ && pendingRows_ >= kProbeChunkRows && strategy_ == kJoinDirect && f_.build->built &&
-        impl_->inflight.size() < 2) {
-        const auto t0 = std::chrono::steady_clock::now();
-        impl_->inflight.push_back(LaunchPending());
-        counters_[8] += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+    // Pipelined callers: a full chunk goes to the worker thread, which launches it at once, so
+    // that its kernel runs while the caller queues the next chunk.
+    if (!noMoreInput_ && pendingRows_ >= omg::ProbeChunkRows() &&
+        (impl_->worker.joinable() || (strategy_ == kJoinDirect && f_.build->built))) {
+        HandOff();
+    }
+    return 0;
+}
+
+void LookupJoinOperator::HandOff()
+{
+    Impl &im = *impl_;
+    if (!im.worker.joinable()) {
+        omg::RequireDevice();
+        CudaCheck(cudaGetDevice(&im.device), "cudaGetDevice");
+        im.worker = std::thread([this] { RunWorker(); });
+    }
+    std::unique_lock<std::mutex> lk(im.mu);
+    im.progress.wait(lk, [&] { return im.busy < kMaxChunksAhead || im.error; });
+    if (im.error) {
+        std::exception_ptr e = im.error;
+        lk.unlock();
+        std::rethrow_exception(e);
+    }
+    im.chunks.push_back(std::move(pending_));
+    pending_.clear();
+    pendingRows_ = 0;
+    ++im.busy;
+    lk.unlock();
+    im.wake.notify_one();
+}
+
+void LookupJoinOperator::RunWorker()
+{
+    Impl &im = *impl_;
+    cudaSetDevice(im.device);
+    auto &fl = im.inflight;
+    for (;;) {
+        std::vector<VectorBatch *> chunk;
+        bool finish = false;
+        {
+            std::unique_lock<std::mutex> lk(im.mu);
+            for (;;) {
+                if (im.stop) {
+                    return;
+                }
+                if (!im.chunks.empty() && !im.error) {
+                    chunk = std::move(im.chunks.front());
+                    im.chunks.pop_front();
+                    break;
+                }
+                if (!fl.empty()) {
+                    finish = im.flush || fl.size() > 1;
+                    if (!finish) {
+                        const cudaError_t q = cudaEventQuery(fl.front()->done);
+                        cudaGetLastError();  // "not ready" is not an error
+                        finish = q != cudaErrorNotReady;
+                    }
+                    if (finish) {
+                        break;
+                    }
+                    im.wake.wait_for(lk, std::chrono::microseconds(50));  // poll the kernel
+                    continue;
+                }
+                im.wake.wait(lk);
+            }
+        }
+        try {
+            if (!chunk.empty()) {
+                const auto t0 = std::chrono::steady_clock::now();
+                fl.push_back(LaunchBatches(std::move(chunk)));
+                counters_[8] +=
+                    std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+            } else if (finish) {
+                std::unique_ptr<ProbeCall> pc = std::move(fl.front());
+                fl.pop_front();
+                std::deque<VectorBatch *> out;
+                FinishProbe(*pc, out);
+                pc.reset();
+                {
+                    std::lock_guard<std::mutex> g(im.mu);
+                    for (auto *b : out) {
+                        im.ready.push_back(b);
+                    }
+                    --im.busy;
+                }
+                im.progress.notify_all();
+            }
+        } catch (...) {
+            fl.clear();  // waits for their kernels, frees their batches
+            {
+                std::lock_guard<std::mutex> g(im.mu);
+                im.error = std::current_exception();
+                for (auto &c : im.chunks) {
+                    for (auto *b : c) {
+                        vec::VectorHelper::FreeVecBatch(b);
+                    }
+                }
+                im.chunks.clear();
+                im.busy = 0;
+            }
+            im.progress.notify_all();
+        }
+    }
+}
+
+int32_t LookupJoinOperator::GetOutputFromWorker(VectorBatch **outputVecBatch)
+{
+    Impl &im = *impl_;
+    std::unique_lock<std::mutex> lk(im.mu);
+    if (noMoreInput_) {
+        // The last, partial chunk, then wait for an output batch or the end of the work.
+        if (!pending_.empty() && !im.error) {
+            im.chunks.push_back(std::move(pending_));
+            pending_.clear();
+            pendingRows_ = 0;
+            ++im.busy;
+        }
+        im.flush = true;
+        im.wake.notify_one();
+        im.progress.wait(lk, [&] { return !im.ready.empty() || im.busy == 0 || im.error; });
+    }
+    if (im.error) {
+        std::exception_ptr e = im.error;
+        lk.unlock();
+        std::rethrow_exception(e);
+    }
+    if (!im.ready.empty()) {
+        *outputVecBatch = im.ready.front();
+        im.ready.pop_front();
+    }
+    if (noMoreInput_ && im.busy == 0 && im.ready.empty() && pending_.empty()) {
+        SetStatus(OMNI_STATUS_FINISHED);
     }
     return 0;
 }
@@ -833,16 +1006,23 @@ void LookupJoinOperator::ProcessPending()
         return;
     }
     std::unique_ptr<ProbeCall> pc = LaunchPending();
-    FinishProbe(*pc);
+    FinishProbe(*pc, outputs_);
 }
 
 // Take the queued batches, set up the probe and launch it; FinishProbe completes it.
 std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending()
 {
+    std::vector<VectorBatch *> batches;
+    batches.swap(pending_);
+    pendingRows_ = 0;
+    return LaunchBatches(std::move(batches));
+}
+
+std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchBatches(std::vector<VectorBatch *> &&batches)
+{
     std::unique_ptr<ProbeCall> call(new ProbeCall());
     ProbeCall &pc = *call;
-    pc.batches.swap(pending_);
-    pendingRows_ = 0;
+    pc.batches = std::move(batches);
     JoinBuildState &b = *f_.build;
     omg::RequireDevice();
     if (userStreamSet_) {
@@ -987,7 +1167,7 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchPending
         }
         // Occupancy bitmap of a unique ARRAY table, for the bitmap probe (kinds that mark no
         // build rows; with or without a slot payload).
-        const bool wantBits = b.table.unique && b.table.mode == omg::JOIN_ARRAY && !b.multiKey && !b.TracksVisits();
+        const bool wantBits = b.table.unique && b.table.mode == omg::JOIN_ARRAY && !b.multiKey;
         if (wantBits && !f_.slotBits) {
             f_.slotBits = omg::Buffer::NewDevice(omg::SlotBitsBytes(b.table.range), s, false);
             CudaCheck(omg::LaunchBuildSlotBits(b.table.arrayEntries, b.table.range,
@@ -1099,7 +1279,7 @@ void LookupJoinOperator::LaunchAttempt(ProbeCall &pc)
 
 // Wait for a launched probe, run it once more at the exact size if a region overflowed, then
 // build VARCHAR outputs, carve the output batches and free the probe batches.
-void LookupJoinOperator::FinishProbe(ProbeCall &pc)
+void LookupJoinOperator::FinishProbe(ProbeCall &pc, std::deque<VectorBatch *> &out)
 {
     JoinBuildState &b = *f_.build;
     cudaStream_t s = pc.s;
@@ -1190,7 +1370,7 @@ void LookupJoinOperator::FinishProbe(ProbeCall &pc)
             std::rotate(outCols.begin(), outCols.begin() + static_cast<std::ptrdiff_t>(nProbeOut), outCols.end());
         }
         for (auto *ob : omg::CarveBatches(outCols, n, f_.rowsPerBatch, firstRow)) {
-            outputs_.push_back(ob);
+            out.push_back(ob);
         }
         rows += n;
     }
@@ -1536,6 +1716,9 @@ bool LookupJoinOperator::ProcessPartitioned()
 int32_t LookupJoinOperator::GetOutput(VectorBatch **outputVecBatch)
 {
     *outputVecBatch = nullptr;
+    if (impl_->worker.joinable()) {
+        return GetOutputFromWorker(outputVecBatch);
+    }
     // Launched probe calls finish oldest first: when another is queued behind it, when its kernel
     // is done, or when no more input will come.
     auto &fl = impl_->inflight;
@@ -1551,10 +1734,10 @@ int32_t LookupJoinOperator::GetOutput(VectorBatch **outputVecBatch)
         }
         std::unique_ptr<ProbeCall> pc = std::move(fl.front());
         fl.pop_front();
-        FinishProbe(*pc);
+        FinishProbe(*pc, outputs_);
     }
     if (outputs_.empty() && fl.empty() && !pending_.empty() && f_.build->built &&
-        (noMoreInput_ || pendingRows_ >= kProbeChunkRows)) {
+        (noMoreInput_ || pendingRows_ >= omg::ProbeChunkRows())) {
         ProcessPending();
     }
     if (!outputs_.empty()) {

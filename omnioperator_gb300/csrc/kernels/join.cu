@@ -988,6 +988,60 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
     return sp == 1 && (fl[0] & kFNull) == 0 && v[0] != 0;
 }
 
+// The filter programs of one comparison between two operands (columns of either side or
+// literals): evaluated without the interpreter's stack, with its semantics (NULL fails, doubles
+// compare unordered NaN as neither less, greater nor equal).
+__device__ __forceinline__ bool SimpleFilterShape(const ProbeLaunch &p)
+{
+    auto operand = [](int op) { return op == FOP_PROBE_COL || op == FOP_BUILD_COL || op == FOP_LITERAL; };
+    return p.nFilter == 3 && operand(p.filter[0].op) && operand(p.filter[1].op) && p.filter[2].op >= FOP_EQ &&
+        p.filter[2].op <= FOP_GTE;
+}
+
+__device__ __forceinline__ bool FilterOperand(const FilterInstr &f, const BatchDesc &b, int64_t row, int64_t br,
+    uint64_t &bits)
+{
+    if (f.op == FOP_LITERAL) {
+        bits = static_cast<uint64_t>(f.imm);
+        return f.isNull == 0;
+    }
+    const bool probe = f.op == FOP_PROBE_COL;
+    const int64_t r = probe ? row : br;
+    if (RowIsNullRO(probe ? b.nulls[f.input] : f.nulls, r)) {
+        return false;
+    }
+    bits = static_cast<uint64_t>(LoadIntRO(probe ? b.cols[f.input] : f.values, r, f.dbl ? 8 : f.width));
+    return true;
+}
+
+__device__ __forceinline__ bool SimpleFilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br)
+{
+    const FilterInstr &fa = p.filter[0];
+    const FilterInstr &fb = p.filter[1];
+    uint64_t av = 0, bv = 0;
+    if (!FilterOperand(fa, b, row, br, av) || !FilterOperand(fb, b, row, br, bv)) {
+        return false;  // NULL: the comparison is NULL, which fails
+    }
+    int c;
+    if (fa.dbl || fb.dbl) {
+        const double x = FilterAsDouble(av, fa.dbl ? kFDouble : 0u);
+        const double y = FilterAsDouble(bv, fb.dbl ? kFDouble : 0u);
+        c = x < y ? -1 : (x > y ? 1 : (x == y ? 0 : 2));
+    } else {
+        const int64_t x = static_cast<int64_t>(av);
+        const int64_t y = static_cast<int64_t>(bv);
+        c = x < y ? -1 : (x > y ? 1 : 0);
+    }
+    switch (p.filter[2].op) {
+        case FOP_EQ: return c == 0;
+        case FOP_NEQ: return c != 0;
+        case FOP_LT: return c == -1;
+        case FOP_LTE: return c == -1 || c == 0;
+        case FOP_GT: return c == 1;
+        default: return c == 1 || c == 0;  // FOP_GTE
+    }
+}
+
 // A candidate build row counts as a match: equal key tuple (multi-column keys) and passing the
 // join filter (when there is one).
 __device__ __forceinline__ bool Accept(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br, bool multi)
@@ -1586,9 +1640,8 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
         isFlag[o] = p.out[o].side == 2;
         isProbe[o] = kProbeCols && p.out[o].side == 0 && p.out[o].src != p.keyInput;
     }
-    // Join kinds without visited marks (inner, probe-side outer, semi, anti, existence): which
-    // rows are emitted follows EmitCount; unmatched rows get NULL build fields, emitted rows of a
-    // NULL probe key a NULL key.
+    // Which rows are emitted follows EmitCount; unmatched rows get NULL build fields, emitted rows
+    // of a NULL probe key a NULL key; BUILD_OUTER and FULL also mark matched build rows visited.
     const int kind = p.joinKind;
     const bool inner = kind == JOIN_KIND_INNER;
     // kSingle: the segments of the one batch are indexed directly (no descriptor loads per segment).
@@ -1666,14 +1719,27 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                 hit |= ((sBits[d >> 5] >> (d & 31)) & 1u) << i;
             }
         }
+        if (p.visited != nullptr) {
+            // BUILD_OUTER / FULL: the slot's entry is the one build row of the key.
+#pragma unroll
+            for (int i = 0; i < kBitsRounds; ++i) {
+                if (!kFilter && ((hit >> i) & 1u)) {
+                    p.visited[p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey]] = 1;
+                }
+            }
+        }
         if (kFilter) {
             // A unique ARRAY table: the slot's entry is the one build row of the key.
+            const bool simple = SimpleFilterShape(p);
 #pragma unroll
             for (int i = 0; i < kBitsRounds; ++i) {
                 if ((hit >> i) & 1u) {
                     const int64_t br = p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey];
-                    if (!FilterPasses(p, *segBatch, base + i * 32 + lane, br)) {
+                    const int64_t row = base + i * 32 + lane;
+                    if (!(simple ? SimpleFilterPasses(p, *segBatch, row, br) : FilterPasses(p, *segBatch, row, br))) {
                         hit &= ~(1u << i);
+                    } else if (p.visited != nullptr) {
+                        p.visited[br] = 1;
                     }
                 }
             }
@@ -2456,14 +2522,17 @@ void SetBulkProbe(int mode) { g_bulkProbe.store(mode == 1 || mode == 2 ? mode : 
 
 int LastProbeKernel() { return g_lastProbeKernel.load(); }
 
-// The bitmap kernel takes the kinds that mark no build rows on an ARRAY table whose occupancy
+// The bitmap kernel takes every join kind (marking a matched build row visited through its slot's
+// entry for the kinds that keep unmatched build rows) on a unique ARRAY table whose occupancy
 // bitmap fits in shared memory, on launches large enough to amortise staging it into every CTA;
 // its outputs are the probe key, other fixed-width probe columns (*probeCols), payload fields
 // (a slot payload present) and the existence flag.
 bool BitsProbeEligible(const ProbeLaunch &p, bool *probeCols)
 {
+    const bool visits = p.joinKind == JOIN_KIND_BUILD_OUTER || p.joinKind == JOIN_KIND_FULL;
     const bool bitsKind = p.joinKind == JOIN_KIND_INNER || p.joinKind == JOIN_KIND_PROBE_OUTER ||
-        p.joinKind == JOIN_KIND_SEMI || p.joinKind == JOIN_KIND_ANTI || p.joinKind == JOIN_KIND_EXISTENCE;
+        p.joinKind == JOIN_KIND_SEMI || p.joinKind == JOIN_KIND_ANTI || p.joinKind == JOIN_KIND_EXISTENCE ||
+        (visits && p.visited != nullptr && p.table.arrayEntries != nullptr);
     bool ok = bitsKind && p.nKeyCols == 0 && p.table.unique && p.keyWidth == 8 && p.nOut >= 1 &&
         p.nOut <= kFastMaxOut && p.table.mode == JOIN_ARRAY && p.table.slotBits != nullptr &&
         SlotBitsBytes(p.table.range) <= kBitsMaxSmem && p.nTiles >= kBitsMinTiles;

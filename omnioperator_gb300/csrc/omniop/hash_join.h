@@ -138,8 +138,15 @@ private:
     struct ProbeCall;
     void ProcessPending();
     std::unique_ptr<ProbeCall> LaunchPending();
+    std::unique_ptr<ProbeCall> LaunchBatches(std::vector<VectorBatch *> &&batches);
     void LaunchAttempt(ProbeCall &pc);
-    void FinishProbe(ProbeCall &pc);
+    void FinishProbe(ProbeCall &pc, std::deque<VectorBatch *> &out);
+    // Pipelined callers: full chunks go to a worker thread that launches and finishes the probe
+    // calls (RunWorker), so the caller's AddInput / GetOutput overlap with the launches.
+    void HandOff();
+    void RunWorker();
+    void StopWorker();
+    int32_t GetOutputFromWorker(VectorBatch **outputVecBatch);
     bool ProcessPartitioned();
     int32_t strategy_ = kJoinDirect;
     int32_t partBits_ = 0;

@@ -2,6 +2,7 @@
 // machine (operator/operator.h:22-266, operator/operator_factory.h:13-29).
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -58,7 +59,15 @@ public:
         userStreamSet_ = true;
     }
     void SetDeviceOutput(bool on) { deviceOutput_ = on; }
-    const std::vector<int64_t> &Counters() const { return counters_; }
+    std::vector<int64_t> Counters() const
+    {
+        std::vector<int64_t> v(kCounters);
+        for (int i = 0; i < kCounters; ++i) {
+            v[i] = counters_[i].load(std::memory_order_relaxed);
+        }
+        return v;
+    }
+    static constexpr int kCounters = 12;
 
 protected:
     bool noMoreInput_ = true;
@@ -69,7 +78,8 @@ protected:
     // [5] output rows, [6] kernel ns, [7] timed kernel launches, and host time of the probe
     // pipeline: [8] ns setting up and launching probe calls, [9] ns waiting for their kernels,
     // [10] ns carving output batches, [11] ns freeing the probe input batches.
-    std::vector<int64_t> counters_ = std::vector<int64_t>(12, 0);
+    // Atomic: a probe operator's worker thread updates them while the caller may read them.
+    std::atomic<int64_t> counters_[kCounters]{};
 
 private:
     OmniStatus status_ = OMNI_STATUS_NORMAL;

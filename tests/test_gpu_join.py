@@ -303,3 +303,54 @@ def test_bulk_copy_probe_two_payload_layouts(gpu, bulk):
 def test_bulk_probe_knob_rejects_other_modes():
     assert omg.lib().omg_debug_set_bulk_probe(3) != 0
     assert omg.lib().omg_debug_set_bulk_probe(0) == 0
+
+
+@pytest.mark.parametrize("device_input,device_output", [(False, False), (True, False), (True, True)])
+def test_worker_pipeline_matches_oracle(gpu, device_input, device_output):
+    """Pipelined callers (SetNoMoreInput(false)) hand full chunks to the operator's worker
+    thread, which launches and finishes the probe calls while the caller keeps adding batches:
+    small chunks (40,000 rows) so that many chunks run, ragged batches, against the oracle."""
+    bkey, p1, p2, pkey, pnull = _cfg2_like(1 << 16, 700_000, 45)
+    try:
+        omg.lib().omg_debug_set_probe_chunk_rows(40_000)
+        _check(bkey, p1, p2, pkey, pnull, batch_sizes=(4096, 777, 10_000), pipeline=True,
+               device_input=device_input, device_output=device_output)
+    finally:
+        omg.lib().omg_debug_set_probe_chunk_rows(0)
+
+
+def test_worker_pipeline_error_reaches_the_caller(gpu):
+    """An allocation failure inside the worker thread (host-side fault injection) comes back to
+    the caller as OMG_ERR_OOM from a later AddInput or GetOutput, and the operator is deleted
+    cleanly afterwards."""
+    bkey, p1, p2, pkey, pnull = _cfg2_like(1 << 14, 200_000, 46)
+    bf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, I, I], [0])
+    bop = bf.create_operator()
+    bop.add_input(omg.make_batch([L, I, I], [bkey, p1, p2]))
+    bop.get_output()
+    pf = omg.LookupJoinOperatorFactory([L], [0], [0], [1, 2], [I, I], bf)
+    pop = pf.create_operator()
+    batches = [omg.make_batch([L], [pkey[s:s + 4096]], [pnull[s:s + 4096]]) for s in range(0, len(pkey), 4096)]
+    errors = []
+    try:
+        omg.lib().omg_debug_set_probe_chunk_rows(20_000)
+        pop.set_no_more_input(False)
+        omg.lib().omg_debug_fail_next_allocs(1000)
+        for i, b in enumerate(batches):
+            try:
+                pop.add_input(b)
+            except omg.OmgError as e:
+                errors.append(e.status)
+        pop.no_more_input()
+        try:
+            pop.drain()
+        except omg.OmgError as e:
+            errors.append(e.status)
+    finally:
+        omg.lib().omg_debug_fail_next_allocs(0)
+        omg.lib().omg_debug_set_probe_chunk_rows(0)
+    assert errors and all(s == -4 for s in errors), errors  # OMG_ERR_OOM
+    pop.delete()
+    pf.close()
+    bop.delete()
+    bf.close()

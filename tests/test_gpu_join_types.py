@@ -299,3 +299,30 @@ def test_multi_column_keys_match_oracle(join_type, shape):
         want_m = rows_matrix(want)
         assert got_m.shape[0] == want_m.shape[0] and len(pi) > 0, part
         assert np.array_equal(got_m, want_m), part
+
+
+@pytest.mark.parametrize("join_type,build_side", CASES)
+def test_bitmap_probe_every_kind_matches_oracle(join_type, build_side):
+    """A unique ARRAY build (NULL-free build output: the packed slot payload) probed in one large
+    batch: the bitmap kernel takes every join kind, marking matched build rows visited through
+    the slot's entry for the kinds that keep unmatched build rows; probe-side and outer-join rows
+    against the oracle."""
+    n_build, n_probe = 60_000, 400_000
+    bcols, bmasks, pcols, pmasks = _random_join_input(n_build, n_probe, True, False, 77 + CASES.index(
+        (join_type, build_side)))
+    kind = oracle.join_kind(join_type, build_side)
+    probe_out = [0, 1]
+    build_out = [] if kind in ("semi", "existence") else [2]
+    cols, outer, _ = run_typed_join(join_type, build_side, [L, I, L], bcols, bmasks, 0, [L, I], pcols, pmasks,
+                                    0, probe_out, build_out, batch_sizes=(n_probe,))
+    assert omg.lib().omg_debug_last_probe_kernel() == 4
+    exp_probe, exp_outer = _expected_cols(kind, bcols, bmasks, pcols, pmasks, probe_out, build_out)
+    got = rows_matrix(cols) if cols is not None else np.zeros((0, 0), np.int64)
+    want = rows_matrix(exp_probe)
+    assert got.shape[0] == want.shape[0] > 0
+    assert np.array_equal(got, want)
+    if kind in ("build_outer", "full"):
+        want_outer = rows_matrix(exp_outer)
+        got_outer = rows_matrix(outer) if outer is not None else np.zeros((0, 0), np.int64)
+        assert got_outer.shape[0] == want_outer.shape[0] > 0
+        assert np.array_equal(got_outer, want_outer)
