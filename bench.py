@@ -1503,7 +1503,8 @@ def run_agg_batched(args, omg, torch, dev, stream, barrier, max_over_ranks, worl
         fac.close()
         res[arm] = {"value": world * total_rows / (ms / 1e3), "unit": "rows/s", "ms_per_step": round(ms, 3),
                     "first_run_ms": round(first_ms, 1), "groups": info["groups"], "table_slots": info["table_slots"],
-                    "tasks_rerun_exactly": info["reruns"], "threads": info["threads"],
+                    "tasks_rerun_exactly": info["reruns"], "tasks_grown_batched": info.get("grown"),
+                    "tasks_rerun_by_operator": info.get("operator_reruns"), "threads": info["threads"],
                     "ctas_per_sm": info["ctas_per_sm"], "graph": bool(info["graph"]), "tune_ms": info["tune_us"] / 1e3,
                     "device_ms": info["run_us"] / 1e3}
     if model is not None:

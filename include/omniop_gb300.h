@@ -343,16 +343,20 @@ int32_t omg_hashagg_factory_set_sizer(void *factory, void *model);
 #define OMG_BATCH_DEVICE_OUTPUT 1    /* output batches stay in HBM */
 #define OMG_BATCH_NO_GRAPH 2         /* launch the sequence directly instead of a CUDA graph */
 #define OMG_BATCH_NO_TUNE 4          /* default launch shape */
-#define OMG_BATCH_DEBUG_TINY_TABLES 8 /* tests: 64-slot tables, forcing the exact re-run path */
+#define OMG_BATCH_DEBUG_TINY_TABLES 8 /* tests: 64-slot tables, overflowing tasks re-run by operators */
+#define OMG_BATCH_DEBUG_TINY_GROW 16  /* tests: 64-slot tables, overflowing tasks take the grow pass */
 int32_t omg_agg_batch_create(void *factory, void *const *task_batches, int32_t n_tasks, void *sizer, int32_t flags,
     void **out_batch);
 int32_t omg_agg_batch_run(void *batch, void *stream);
 /* Output batches of the last run in task order (caller frees each); call until *n == 0.
  * task_of[i] receives the task of out_batches[i]. */
 int32_t omg_agg_batch_outputs(void *batch, void **out_batches, int32_t *task_of, int32_t max, int32_t *n);
-/* [0] tasks, [1] input rows, [2] table slots, [3] tasks re-run exactly, [4] threads per CTA,
- * [5] CTAs per SM, [6] runs, [7] groups, [8] tuning us, [9] preparation us, [10] last run's
- * device time us, [11] 1 if a sizing model sized the tables, [12] 1 if runs replay a graph. */
+/* [0] tasks, [1] input rows, [2] table slots, [3] tasks that outgrew their tables and were
+ * re-run exactly, [4] threads per CTA, [5] CTAs per SM, [6] runs, [7] groups, [8] tuning us,
+ * [9] preparation us, [10] last run's device time us (grow pass included), [11] 1 if a sizing
+ * model sized the tables, [12] 1 if runs replay a graph, [13] of [3], tasks finished by the
+ * batched grow pass (tables of twice their rows), [14] of [3], tasks re-run through a regular
+ * operator. */
 int32_t omg_agg_batch_info(void *batch, int64_t *out, int32_t n, int32_t *written);
 /* Per task, a sizing record laid out as omg_op_get_sizing_log's (23 values per task). */
 int32_t omg_agg_batch_sizing_logs(void *batch, int64_t *out, int64_t n, int64_t *written);

@@ -618,9 +618,9 @@ class LookupOuterJoinOperatorFactory(OperatorFactory):
 
 
 # --------------------------------------------------------------------------- batched aggregation
-BATCH_DEVICE_OUTPUT, BATCH_NO_GRAPH, BATCH_NO_TUNE, BATCH_DEBUG_TINY_TABLES = 1, 2, 4, 8
+BATCH_DEVICE_OUTPUT, BATCH_NO_GRAPH, BATCH_NO_TUNE, BATCH_DEBUG_TINY_TABLES, BATCH_DEBUG_TINY_GROW = 1, 2, 4, 8, 16
 _BATCH_INFO = ["tasks", "rows", "table_slots", "reruns", "threads", "ctas_per_sm", "runs", "groups", "tune_us",
-               "prepare_us", "run_us", "learned", "graph"]
+               "prepare_us", "run_us", "learned", "graph", "grown", "operator_reruns"]
 
 
 class AggBatch:

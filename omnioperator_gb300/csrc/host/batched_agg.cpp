@@ -112,8 +112,15 @@ struct BatchedAggregation::Impl {
 
     // Results of the last run.
     std::vector<int64_t> taskGroups;
-    std::vector<bool> taskRerun;
+    std::vector<bool> taskRerun;  // the task outgrew its first table
+    std::vector<bool> taskGrown;  // ... and was finished by the grow pass
     std::vector<std::vector<VectorBatch *>> rerunOutputs;
+    // The grow pass: one more batched run over the tasks that outgrew their tables, each with a
+    // table of at least twice its rows (forcedCapacity), so none can outgrow it; a task that
+    // still fails (its probe limit) is re-run through a regular operator.
+    std::vector<uint64_t> forcedCapacity;
+    std::unique_ptr<Impl> grow;
+    std::vector<int32_t> growTasks;
 
     ~Impl()
     {
@@ -191,9 +198,10 @@ struct BatchedAggregation::Impl {
         bt.Upload(s);
         rows = bt.TotalRows();
         scratch.Reset(8, s, true);
-        // Sizing: one sketch per task, then the plain estimate or the model's, batched.
+        // Sizing: one sketch per task, then the plain estimate or the model's, batched (the grow
+        // pass has its capacities already).
         sketch.assign(static_cast<size_t>(n) * omg::kSketchStats, 0);
-        {
+        if (forcedCapacity.empty()) {
             DevArray<unsigned long long> st(static_cast<size_t>(n) * omg::kSketchStats, s);
             omg::AggLaunch p = MakeAggLaunch(plan, nullptr, 0, nullptr, nullptr);
             p.batches = bt.DeviceBatches();
@@ -209,10 +217,12 @@ struct BatchedAggregation::Impl {
         std::vector<int64_t> logs;
         for (int32_t t = 0; t < n; ++t) {
             const int64_t r = tasks[t]->GetRowCount();
-            plainEstimate[t] = omg::PlainGroupEstimate(&sketch[static_cast<size_t>(t) * omg::kSketchStats], r);
+            plainEstimate[t] = forcedCapacity.empty()
+                ? omg::PlainGroupEstimate(&sketch[static_cast<size_t>(t) * omg::kSketchStats], r)
+                : forcedCapacity[t] / 2;
             estimate[t] = plainEstimate[t];
         }
-        if (sizer != nullptr) {
+        if (sizer != nullptr && forcedCapacity.empty()) {
             X.resize(static_cast<size_t>(n) * omg::kSizerFeatures);
             std::vector<int64_t> log(1 + omg::kSketchStats);
             std::vector<std::vector<int64_t>> allLogs(n);
@@ -236,7 +246,11 @@ struct BatchedAggregation::Impl {
         totalSlots = 0;
         outBound = 0;
         for (int32_t t = 0; t < n; ++t) {
-            const uint64_t want = (flags & kBatchTinyTables) ? kMinTaskSlots : NextPow2(2 * std::max<uint64_t>(estimate[t], 1));
+            uint64_t want = (flags & (kBatchTinyTables | kBatchTinyGrow)) ? kMinTaskSlots
+                                                                          : NextPow2(2 * std::max<uint64_t>(estimate[t], 1));
+            if (!forcedCapacity.empty()) {
+                want = forcedCapacity[t];
+            }
             capacity[t] = std::max(want, kMinTaskSlots);
             const uint64_t bound = std::min<uint64_t>(capacity[t] + 2, static_cast<uint64_t>(tasks[t]->GetRowCount()));
             outBound += (bound + 63) / 64 * 64;
@@ -419,15 +433,65 @@ void BatchedAggregation::Run(void *stream)
     }
     im.taskGroups.assign(im.n, 0);
     im.taskRerun.assign(im.n, false);
+    im.taskGrown.assign(im.n, false);
     im.rerunOutputs.assign(im.n, {});
     const bool device = (im.flags & kBatchDeviceOutput) != 0;
+    std::vector<int32_t> failedTasks;
     for (int32_t t = 0; t < im.n; ++t) {
         im.taskGroups[t] = im.hGroups[t];
-        if (im.hFailed[t] == 0) {
+        if (im.hFailed[t] != 0) {
+            im.taskRerun[t] = true;
+            failedTasks.push_back(t);
+        }
+    }
+    if (!failedTasks.empty() && !(im.flags & kBatchTinyTables)) {
+        // The grow pass (prepared once per set of failed tasks; graph replays fail the same tasks).
+        if (!im.grow || im.growTasks != failedTasks) {
+            std::unique_ptr<Impl> g(new Impl());
+            g->factory = im.factory;
+            g->plan = im.plan;
+            g->flags = (im.flags & kBatchDeviceOutput) | kBatchNoGraph | kBatchNoTune;
+            for (int32_t t : failedTasks) {
+                g->tasks.push_back(im.tasks[t]);
+                g->forcedCapacity.push_back(
+                    std::max(kMinTaskSlots, NextPow2(2 * static_cast<uint64_t>(im.tasks[t]->GetRowCount()))));
+            }
+            g->Prepare(s);
+            g->variant = im.variant;
+            im.grow = std::move(g);
+            im.growTasks = failedTasks;
+        }
+        Impl &g = *im.grow;
+        g.timer.Start(s);
+        g.Sequence(s);
+        g.timer.Stop(s);
+        CudaCheck(cudaMemcpyAsync(g.hGroups.Get(), g.groups.Get(), sizeof(uint32_t) * g.n, cudaMemcpyDeviceToHost, s),
+            "read grown task groups");
+        CudaCheck(cudaMemcpyAsync(g.hFailed.Get(), g.failed.Get(), sizeof(uint32_t) * g.n, cudaMemcpyDeviceToHost, s),
+            "read grown task flags");
+        CudaCheck(cudaMemcpyAsync(g.hOffsets.Get(), g.offsets.Get(), sizeof(int64_t) * g.n, cudaMemcpyDeviceToHost, s),
+            "read grown task offsets");
+        unsigned long long gerr[3] = {0, 0, 0};
+        CudaCheck(cudaMemcpyAsync(gerr, g.scratch.Get(), sizeof(gerr), cudaMemcpyDeviceToHost, s), "read errors");
+        im.stream.Sync();
+        im.lastRunNs += g.timer.ElapsedNs();
+        if (gerr[0] != 0 || gerr[2] != 0) {
+            const int32_t code = static_cast<int32_t>(gerr[0] != 0 ? gerr[0] : gerr[2]);
+            throw OmniException("OPERATOR_RUNTIME_ERROR", "batched aggregation kernel error " + std::to_string(code),
+                code == 7 ? -7 : (code == 5 ? -5 : -9));
+        }
+        for (int32_t i = 0; i < g.n; ++i) {
+            if (g.hFailed[i] == 0) {
+                im.taskGrown[failedTasks[i]] = true;
+                im.taskGroups[failedTasks[i]] = g.hGroups[i];
+            }
+        }
+    }
+    for (int32_t t = 0; t < im.n; ++t) {
+        if (im.hFailed[t] == 0 || im.taskGrown[t]) {
             continue;
         }
-        // The task outgrew its table: aggregate it through a regular operator (exact resize path).
-        im.taskRerun[t] = true;
+        // The task outgrew its tables: aggregate it through a regular operator (exact resize path).
         std::unique_ptr<Operator> op(im.factory->CreateOperator());
         op->SetStream(s);
         op->SetDeviceOutput(device);
@@ -468,7 +532,36 @@ void BatchedAggregation::Outputs(std::vector<VectorBatch *> &batches, std::vecto
             c.hasNull = false;  // host vectors: HasNull() scans the bitmap
         }
     }
+    // Grown tasks: their rows from the grow pass's output columns.
+    std::vector<omg::OutColumn> growCols;
+    std::vector<int32_t> growIndex(im.n, -1);
+    if (im.grow) {
+        Impl &g = *im.grow;
+        growCols = g.outCols;
+        if (!(im.flags & kBatchDeviceOutput)) {
+            int64_t used = 0;
+            for (int32_t i = 0; i < g.n; ++i) {
+                used = std::max<int64_t>(used, g.hOffsets[i] + static_cast<int64_t>(g.hGroups[i]));
+            }
+            growCols = omg::CopyColumnsToHost(g.outCols, used, s, 0);
+            im.stream.Sync();
+            for (auto &c : growCols) {
+                c.hasNull = false;
+            }
+        }
+        for (int32_t i = 0; i < g.n; ++i) {
+            growIndex[im.growTasks[i]] = i;
+        }
+    }
     for (int32_t t = 0; t < im.n; ++t) {
+        if (im.taskGrown[t]) {
+            const int32_t i = growIndex[t];
+            for (auto *b : omg::CarveBatches(growCols, im.grow->hGroups[i], im.plan.rowsPerBatch, im.grow->hOffsets[i])) {
+                batches.push_back(b);
+                taskOf.push_back(t);
+            }
+            continue;
+        }
         if (im.taskRerun[t]) {
             for (auto *b : im.rerunOutputs[t]) {
                 batches.push_back(b);
@@ -489,13 +582,15 @@ std::vector<int64_t> BatchedAggregation::Info() const
     const Impl &im = *impl_;
     int32_t threads = 0, perSM = 0;
     omg::AggTasksVariantShape(im.variant, &threads, &perSM);
-    int64_t reruns = 0, groups = 0;
+    int64_t reruns = 0, groups = 0, grown = 0;
     for (size_t t = 0; t < im.taskGroups.size(); ++t) {
         reruns += im.taskRerun[t] ? 1 : 0;
+        grown += im.taskGrown[t] ? 1 : 0;
         groups += im.taskGroups[t];
     }
     return {im.n, im.rows, static_cast<int64_t>(im.totalSlots), reruns, threads, perSM, im.runs, groups, im.tuneUs,
-        im.prepareUs, im.lastRunNs / 1000, im.sizer != nullptr ? 1 : 0, im.exec != nullptr ? 1 : 0};
+        im.prepareUs, im.lastRunNs / 1000, im.sizer != nullptr ? 1 : 0, im.exec != nullptr ? 1 : 0, grown,
+        reruns - grown};
 }
 
 std::vector<int64_t> BatchedAggregation::SizingLogs() const

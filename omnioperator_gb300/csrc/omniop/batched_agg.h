@@ -22,7 +22,8 @@ namespace op {
 constexpr int32_t kBatchDeviceOutput = 1;  // outputs stay in HBM
 constexpr int32_t kBatchNoGraph = 2;       // launch the sequence directly instead of a CUDA graph
 constexpr int32_t kBatchNoTune = 4;        // default launch shape, no autotuning
-constexpr int32_t kBatchTinyTables = 8;    // test hook: 64-slot tables (forces the exact re-run path)
+constexpr int32_t kBatchTinyTables = 8;    // test hook: 64-slot tables, overflowing tasks re-run by operators
+constexpr int32_t kBatchTinyGrow = 16;     // test hook: 64-slot tables, overflowing tasks take the grow pass
 
 class BatchedAggregation {
 public:

@@ -93,6 +93,17 @@ def test_batched_overflowing_tasks_rerun_exactly(gpu):
     assert info["reruns"] >= 5
 
 
+@pytest.mark.parametrize("flags", [0, omg.BATCH_DEVICE_OUTPUT | omg.BATCH_NO_GRAPH])
+def test_batched_grow_pass_finishes_overflowing_tasks(gpu, flags):
+    """64-slot first tables: the tasks that outgrow them take one more batched run with tables of
+    twice their rows (no operator re-runs), equal to the oracle task by task, over graph replays."""
+    tasks = _tasks(5, 40, max_rows=20_000, nulls=True)
+    (first, second), info = _run(tasks, flags=flags | omg.BATCH_DEBUG_TINY_GROW, runs=2)
+    _check(tasks, first)
+    _check(tasks, second)
+    assert info["reruns"] >= 5 and info["grown"] == info["reruns"] and info["operator_reruns"] == 0
+
+
 def test_batched_device_output_without_graph(gpu):
     tasks = _tasks(4, 50)
     (per,), info = _run(tasks, flags=omg.BATCH_DEVICE_OUTPUT | omg.BATCH_NO_GRAPH | omg.BATCH_NO_TUNE)
