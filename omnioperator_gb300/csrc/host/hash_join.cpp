@@ -1103,6 +1103,7 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchBatches
     p.nFilter = static_cast<int32_t>(f_.filter.size());
     for (size_t i = 0; i < f_.filter.size(); ++i) {
         omg::FilterInstr in = f_.filter[i];
+        in.payloadShift = 0;  // set below when the column is a slot-payload field
         const int32_t c = f_.filterCols[i];
         if (in.op == omg::FOP_PROBE_COL) {
             in.input = inputOf[c];
@@ -1177,6 +1178,16 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchBatches
         }
         if (eligible && f_.slotPayload) {
             p.table.slotPayload = static_cast<const uint64_t *>(f_.slotPayload->Data());
+            // Filter operands that are build output columns packed into the payload.
+            for (int32_t i = 0; i < p.nFilter; ++i) {
+                omg::FilterInstr &in = p.filter[i];
+                in.payloadShift = 0;
+                for (size_t o = nProbeOut; in.op == omg::FOP_BUILD_COL && o < nOut; ++o) {
+                    if (p.out[o].src == f_.filterCols[i] && p.out[o].width == in.width) {
+                        in.payloadShift = p.out[o].shift + 1;
+                    }
+                }
+            }
         }
         if (wantBits && f_.slotBits) {
             p.table.slotBits = static_cast<const uint32_t *>(f_.slotBits->Data());

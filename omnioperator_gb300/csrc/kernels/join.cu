@@ -820,8 +820,21 @@ __device__ __forceinline__ double FilterAsDouble(uint64_t v, uint32_t fl)
                            : static_cast<double>(static_cast<int64_t>(v));
 }
 
-// The filter program over the candidate pair (probe row `row` of batch b, build row `br`).
-__device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br)
+// A build column that is also a slot-payload field: its value from the candidate's slot payload
+// (payload fields are NULL-free), sign-extended from its width.
+__device__ __forceinline__ uint64_t PayloadField(const FilterInstr &f, uint64_t payload)
+{
+    const uint64_t v = payload >> (f.payloadShift - 1);
+    if (f.dbl || f.width == 8) {
+        return v;
+    }
+    return static_cast<uint64_t>(SignExtend(v, f.width));
+}
+
+// The filter program over the candidate pair (probe row `row` of batch b, build row `br`);
+// `payload` (when not null) is the candidate's slot payload.
+__device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br,
+    bool hasPayload = false, uint64_t payload = 0)
 {
     uint64_t v[kMaxFilterDepth];
     uint32_t fl[kMaxFilterDepth];
@@ -835,7 +848,10 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
             }
             uint64_t bits = static_cast<uint64_t>(f.imm);
             bool isNull = f.isNull != 0;
-            if (op != FOP_LITERAL) {
+            if (op == FOP_BUILD_COL && hasPayload && f.payloadShift > 0) {
+                bits = PayloadField(f, payload);
+                isNull = false;
+            } else if (op != FOP_LITERAL) {
                 const void *col = op == FOP_PROBE_COL ? b.cols[f.input] : f.values;
                 const uint8_t *nulls = op == FOP_PROBE_COL ? b.nulls[f.input] : f.nulls;
                 const int64_t r = op == FOP_PROBE_COL ? row : br;
@@ -999,11 +1015,15 @@ __device__ __forceinline__ bool SimpleFilterShape(const ProbeLaunch &p)
 }
 
 __device__ __forceinline__ bool FilterOperand(const FilterInstr &f, const BatchDesc &b, int64_t row, int64_t br,
-    uint64_t &bits)
+    bool hasPayload, uint64_t payload, uint64_t &bits)
 {
     if (f.op == FOP_LITERAL) {
         bits = static_cast<uint64_t>(f.imm);
         return f.isNull == 0;
+    }
+    if (f.op == FOP_BUILD_COL && hasPayload && f.payloadShift > 0) {
+        bits = PayloadField(f, payload);
+        return true;
     }
     const bool probe = f.op == FOP_PROBE_COL;
     const int64_t r = probe ? row : br;
@@ -1014,12 +1034,14 @@ __device__ __forceinline__ bool FilterOperand(const FilterInstr &f, const BatchD
     return true;
 }
 
-__device__ __forceinline__ bool SimpleFilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br)
+__device__ __forceinline__ bool SimpleFilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br,
+    bool hasPayload, uint64_t payload)
 {
     const FilterInstr &fa = p.filter[0];
     const FilterInstr &fb = p.filter[1];
     uint64_t av = 0, bv = 0;
-    if (!FilterOperand(fa, b, row, br, av) || !FilterOperand(fb, b, row, br, bv)) {
+    if (!FilterOperand(fa, b, row, br, hasPayload, payload, av) ||
+        !FilterOperand(fb, b, row, br, hasPayload, payload, bv)) {
         return false;  // NULL: the comparison is NULL, which fails
     }
     int c;
@@ -1670,6 +1692,18 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
     if (kPacked && kSingle) {
         packCols = PackColsOf(p.pack, p.batches[0]);
     }
+    // Filters: whether every build operand comes from the slot payload (then the build row is
+    // needed only to mark it visited).
+    bool simpleFilter = false;
+    bool filterNeedsRow = false;
+    if (kFilter) {
+        simpleFilter = SimpleFilterShape(p);
+        filterNeedsRow = p.visited != nullptr;
+        for (int f = 0; f < p.nFilter; ++f) {
+            filterNeedsRow = filterNeedsRow ||
+                (p.filter[f].op == FOP_BUILD_COL && (payloadTab == nullptr || p.filter[f].payloadShift == 0));
+        }
+    }
     const int64_t warpsTotal = static_cast<int64_t>(gridDim.x) * (kThreads / 32);
     for (int64_t item = static_cast<int64_t>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5); item < nItems;
          item += warpsTotal) {
@@ -1728,28 +1762,30 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                 }
             }
         }
-        if (kFilter) {
-            // A unique ARRAY table: the slot's entry is the one build row of the key.
-            const bool simple = SimpleFilterShape(p);
-#pragma unroll
-            for (int i = 0; i < kBitsRounds; ++i) {
-                if ((hit >> i) & 1u) {
-                    const int64_t br = p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey];
-                    const int64_t row = base + i * 32 + lane;
-                    if (!(simple ? SimpleFilterPasses(p, *segBatch, row, br) : FilterPasses(p, *segBatch, row, br))) {
-                        hit &= ~(1u << i);
-                    } else if (p.visited != nullptr) {
-                        p.visited[br] = 1;
-                    }
-                }
-            }
-        }
         uint64_t payload[kBitsRounds];
 #pragma unroll
         for (int i = 0; i < kBitsRounds; ++i) {
             payload[i] = ((hit >> i) & 1u) && payloadTab != nullptr
                 ? __ldg(payloadTab + (static_cast<uint64_t>(key[i]) - minKey))
                 : 0ull;
+        }
+        if (kFilter) {
+            // A unique ARRAY table: the slot's entry is the one build row of the key; build columns
+            // that are slot-payload fields are read from the payload instead.
+#pragma unroll
+            for (int i = 0; i < kBitsRounds; ++i) {
+                if ((hit >> i) & 1u) {
+                    const int64_t br = filterNeedsRow ? p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey] : -1;
+                    const int64_t row = base + i * 32 + lane;
+                    const bool hasPayload = payloadTab != nullptr;
+                    if (!(simpleFilter ? SimpleFilterPasses(p, *segBatch, row, br, hasPayload, payload[i])
+                                       : FilterPasses(p, *segBatch, row, br, hasPayload, payload[i]))) {
+                        hit &= ~(1u << i);
+                    } else if (p.visited != nullptr) {
+                        p.visited[br] = 1;
+                    }
+                }
+            }
         }
         uint32_t emit = hit;  // bit i: this lane's row of round i yields an output row
         if (!inner) {

@@ -432,7 +432,7 @@ struct FilterInstr {
     int16_t dbl;      // 1: the value is a double (columns: DOUBLE; literals: imm is double bits)
     int16_t isNull;   // literals: NULL
     int32_t input;    // FOP_PROBE_COL: probe kernel input index
-    int32_t pad;
+    int32_t payloadShift;  // FOP_BUILD_COL: s + 1 when the column is also a slot-payload field at bit s
     const void *values;    // FOP_BUILD_COL: contiguous build column
     const uint8_t *nulls;  // FOP_BUILD_COL: its NULL bitmap (may be null)
     int64_t imm;
