@@ -1617,14 +1617,15 @@ __device__ __forceinline__ uint32_t LoadPackedSegment(const JoinKeyPack &kp, con
 // kPacked: the key is packed from the parts of a multi-column key (p.pack) as the rows are read.
 // kPack: 0 one key column, 1 a packed key of up to kFusedPackParts parts of run-time widths,
 // 2 a packed key of two 4-byte parts.
-// kFilter: each candidate pair (probe row, its one build row) must also pass the join filter.
-template <int kPack, bool kFilter>
+// kFilter: each candidate pair (probe row, its one build row) must also pass the join filter;
+// 1 = any filter program (the interpreter), 2 = one comparison of two operands (no stack).
+template <int kPack, int kFilter>
 struct BitsThreads {
-    // Packed keys and filters: more registers per thread.
-    static constexpr int value = kPack != 0 || kFilter ? 768 : kBitsThreads;
+    // Packed keys and the interpreter: more registers per thread.
+    static constexpr int value = kPack != 0 || kFilter == 1 ? 768 : kBitsThreads;
 };
 
-template <int kNumOut, uint32_t kLayout, bool kSingle, bool kProbeCols, int kPack, bool kFilter = false>
+template <int kNumOut, uint32_t kLayout, bool kSingle, bool kProbeCols, int kPack, int kFilter = 0>
 __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
     ProbeBitsKernel(const __grid_constant__ ProbeLaunch p)
 {
@@ -1696,8 +1697,8 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
     // needed only to mark it visited).
     bool simpleFilter = false;
     bool filterNeedsRow = false;
-    if (kFilter) {
-        simpleFilter = SimpleFilterShape(p);
+    if (kFilter != 0) {
+        simpleFilter = kFilter == 2 || SimpleFilterShape(p);
         filterNeedsRow = p.visited != nullptr;
         for (int f = 0; f < p.nFilter; ++f) {
             filterNeedsRow = filterNeedsRow ||
@@ -1730,7 +1731,7 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
             batchRows = static_cast<int64_t>(tile.row0) + tile.rows;  // rows of the batch up to this tile's end
         }
         const BatchDesc *segBatch = nullptr;
-        if (kProbeCols || kPacked || kFilter) {
+        if (kProbeCols || kPacked || kFilter != 0) {
             segBatch = kSingle ? p.batches : p.batches + p.tiles[t].batch;
         }
         int64_t key[kBitsRounds];
@@ -1757,7 +1758,7 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
             // BUILD_OUTER / FULL: the slot's entry is the one build row of the key.
 #pragma unroll
             for (int i = 0; i < kBitsRounds; ++i) {
-                if (!kFilter && ((hit >> i) & 1u)) {
+                if (kFilter == 0 && ((hit >> i) & 1u)) {
                     p.visited[p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey]] = 1;
                 }
             }
@@ -1769,7 +1770,7 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                 ? __ldg(payloadTab + (static_cast<uint64_t>(key[i]) - minKey))
                 : 0ull;
         }
-        if (kFilter) {
+        if (kFilter != 0) {
             // A unique ARRAY table: the slot's entry is the one build row of the key; build columns
             // that are slot-payload fields are read from the payload instead.
 #pragma unroll
@@ -1778,8 +1779,10 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                     const int64_t br = filterNeedsRow ? p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey] : -1;
                     const int64_t row = base + i * 32 + lane;
                     const bool hasPayload = payloadTab != nullptr;
-                    if (!(simpleFilter ? SimpleFilterPasses(p, *segBatch, row, br, hasPayload, payload[i])
-                                       : FilterPasses(p, *segBatch, row, br, hasPayload, payload[i]))) {
+                    const bool pass = (kFilter == 2 || simpleFilter)
+                        ? SimpleFilterPasses(p, *segBatch, row, br, hasPayload, payload[i])
+                        : (kFilter == 1 && FilterPasses(p, *segBatch, row, br, hasPayload, payload[i]));
+                    if (!pass) {
                         hit &= ~(1u << i);
                     } else if (p.visited != nullptr) {
                         p.visited[br] = 1;
@@ -2586,6 +2589,14 @@ bool BitsProbeEligible(const ProbeLaunch &p, bool *probeCols)
     return ok;
 }
 
+// SimpleFilterShape on the host.
+bool HostSimpleFilterShape(const ProbeLaunch &p)
+{
+    auto operand = [](int op) { return op == FOP_PROBE_COL || op == FOP_BUILD_COL || op == FOP_LITERAL; };
+    return p.nFilter == 3 && operand(p.filter[0].op) && operand(p.filter[1].op) && p.filter[2].op >= FOP_EQ &&
+        p.filter[2].op <= FOP_GTE;
+}
+
 // Only the bitmap kernel packs multi-column keys as it reads them (keys of up to two parts).
 bool ProbePacksKeys(const ProbeLaunch &p)
 {
@@ -2644,9 +2655,9 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
 #define OMG_BITS_INST(n, layout, cols, packed)                                                              \
     {layout, n, reinterpret_cast<const void *>(ProbeBitsKernel<n, layout, true, cols, packed>),            \
         reinterpret_cast<const void *>(ProbeBitsKernel<n, layout, false, cols, packed>)}
-#define OMG_FILTER_INST(n)                                                                                  \
-    {0, n, reinterpret_cast<const void *>(ProbeBitsKernel<n, 0, true, true, 0, true>),                     \
-        reinterpret_cast<const void *>(ProbeBitsKernel<n, 0, false, true, 0, true>)}
+#define OMG_FILTER_INST(n, layout, cols, kind)                                                              \
+    {layout, n, reinterpret_cast<const void *>(ProbeBitsKernel<n, layout, true, cols, 0, kind>),           \
+        reinterpret_cast<const void *>(ProbeBitsKernel<n, layout, false, cols, 0, kind>)}
         static const Inst insts[] = {
             OMG_BITS_INST(3, OutLayout(kW8, kW4, kW4), false, 0), OMG_BITS_INST(2, OutLayout(kW8, kW8), false, 0),
             OMG_BITS_INST(2, OutLayout(kW8, kW4), false, 0), OMG_BITS_INST(1, 0, false, 0),
@@ -2667,8 +2678,15 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             OMG_BITS_INST(2, 0, true, 2), OMG_BITS_INST(3, 0, true, 2), OMG_BITS_INST(4, 0, true, 2),
         };
         static const Inst filterInsts[] = {
-            OMG_FILTER_INST(1), OMG_FILTER_INST(2), OMG_FILTER_INST(3), OMG_FILTER_INST(4),
+            OMG_FILTER_INST(1, 0, true, 1), OMG_FILTER_INST(2, 0, true, 1), OMG_FILTER_INST(3, 0, true, 1),
+            OMG_FILTER_INST(4, 0, true, 1),
         };
+        // One comparison: run-time widths, and the headline layout (8-byte key, two 4-byte fields).
+        static const Inst cmpInsts[] = {
+            OMG_FILTER_INST(1, 0, true, 2), OMG_FILTER_INST(2, 0, true, 2), OMG_FILTER_INST(3, 0, true, 2),
+            OMG_FILTER_INST(4, 0, true, 2),
+        };
+        static const Inst cmpKeyInst = OMG_FILTER_INST(3, OutLayout(kW8, kW4, kW4), false, 2);
 #undef OMG_BITS_INST
 #undef OMG_FILTER_INST
         constexpr int kInsts = static_cast<int>(sizeof(insts) / sizeof(insts[0]));
@@ -2689,7 +2707,12 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             const bool filter = p.nFilter > 0;
             const bool packed = p.pack.nParts > 0 && !filter;
             const bool two32 = packed && p.pack.nParts == 2 && p.pack.width[0] == 4 && p.pack.width[1] == 4;
-            const Inst *ci = filter ? &filterInsts[p.nOut - 1] : (packed ? &packedInsts[p.nOut - 1] : &colInsts[p.nOut - 1]);
+            bool cmp = filter && HostSimpleFilterShape(p);
+            const Inst *ci = filter ? (cmp ? &cmpInsts[p.nOut - 1] : &filterInsts[p.nOut - 1])
+                                    : (packed ? &packedInsts[p.nOut - 1] : &colInsts[p.nOut - 1]);
+            if (cmp && !probeCols && !packed && insts[pick].layout == OutLayout(kW8, kW4, kW4)) {
+                ci = &cmpKeyInst;
+            }
             if (two32) {
                 bool w4 = p.nOut == 4;
                 for (int o = 0; w4 && o < p.nOut; ++o) {
@@ -2702,7 +2725,7 @@ cudaError_t LaunchProbe(const ProbeLaunch &p, cudaStream_t stream)
             if (cerr != cudaSuccess) {
                 return cerr;
             }
-            const int threads = packed || filter ? BitsThreads<1, true>::value : BitsThreads<0, false>::value;
+            const int threads = packed || (filter && !cmp) ? BitsThreads<1, 1>::value : BitsThreads<0, 0>::value;
             const int64_t items = static_cast<int64_t>(p.nTiles) * kBitsSegsPerTile;
             const int64_t wanted = (items + threads / 32 - 1) / (threads / 32);
             const int grid = static_cast<int>(wanted < SMs() ? wanted : SMs());

@@ -289,3 +289,30 @@ def test_filtered_bitmap_probe_matches_oracle(join_type, fname):
         want.append(tuple(r))
     assert len(want) > 0
     assert sorted(got, key=_key) == sorted(want, key=_key)
+
+
+@pytest.mark.parametrize("fop,lit", [(omg.EXPR_GTE, 0), (omg.EXPR_LT, -5), (omg.EXPR_NEQ, 7)])
+def test_filter_on_payload_fields_headline_layout(fop, lit):
+    """The headline shape (8-byte probe key out, two int32 build payload fields out) with one
+    comparison on a payload field: the bitmap kernel's compile-time layout evaluates it from the
+    slot payload; rows against a direct restatement."""
+    rng = np.random.default_rng(60 + fop)
+    nb, npr = 1 << 16, 400_000
+    bkey = rng.permutation(nb).astype(np.int64)
+    p1 = rng.integers(-20, 20, nb).astype(np.int32)
+    p2 = rng.integers(-2**31, 2**31, nb, dtype=np.int64).astype(np.int32)
+    pkey = rng.integers(0, nb + nb // 4, npr).astype(np.int64)
+    pm = rng.random(npr) < 0.01
+    none_b = np.zeros(nb, bool)
+    filt = B(fop, F(2, I), omg.Literal(lit, I))
+    got = run("INNER", "UNKNOWN", [L, I, I], [bkey, p1, p2], [none_b, none_b, none_b], [L], [pkey], [pm], [0], [1, 2],
+              filt, batch_sizes=(npr,))
+    assert omg.lib().omg_debug_last_probe_kernel() == 4
+    pos = np.full(nb + nb // 4, -1, np.int64)
+    pos[bkey] = np.arange(nb)
+    bi = pos[pkey]
+    ok = (bi >= 0) & ~pm
+    cmp = {omg.EXPR_GTE: np.greater_equal, omg.EXPR_LT: np.less, omg.EXPR_NEQ: np.not_equal}[fop]
+    ok &= cmp(p1[np.where(ok, bi, 0)].astype(np.int64), lit)
+    want = sorted(zip(pkey[ok].tolist(), p1[bi[ok]].tolist(), p2[bi[ok]].tolist()))
+    assert len(want) > 0 and sorted(got) == want
