@@ -164,8 +164,14 @@ int32_t omg_vec_free(void *vec);
  * [0, omg_vec_size(dictionary)) are refused with OMG_ERR_INVALID.  Operators flatten such
  * vectors on the device when they take a batch. */
 int32_t omg_vec_new_dictionary(const int32_t *ids, int32_t size, void *dictionary, void **out_vec);
-/* Vector encoding (BaseVector::GetEncoding, vector/vector.h:107): 0 flat, 1 dictionary. */
+/* Vector encoding (BaseVector::GetEncoding, vector/vector.h:107): 0 flat, 1 dictionary,
+ * 2 container (operator/aggregation/container_vector.h: a partial AVG's (double sum, long count)
+ * under the container-vector policy; type id OMNI_CONTAINER, 17). */
 int32_t omg_vec_encoding(void *vec);
+/* Container vectors: the number of fields (0 for other vectors) and field i, a flat vector owned
+ * by the container (borrowed: do not free it). */
+int32_t omg_vec_num_fields(void *vec);
+void *omg_vec_field(void *vec, int32_t i);
 /* Raw accessors (unsafe/unsafe_vector.h:19-48).  Pointers are host or device
  * addresses according to omg_vec_is_device. */
 void *omg_vec_values(void *vec);

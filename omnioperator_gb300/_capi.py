@@ -45,6 +45,8 @@ _SIGS = {
     "omg_vec_free": (I32, [P]),
     "omg_vec_new_dictionary": (I32, [P, I32, P, C.POINTER(P)]),
     "omg_vec_encoding": (I32, [P]),
+    "omg_vec_num_fields": (I32, [P]),
+    "omg_vec_field": (P, [P, I32]),
     "omg_vec_values": (P, [P]),
     "omg_vec_nulls": (P, [P]),
     "omg_vec_size": (I32, [P]),

@@ -19,7 +19,7 @@ from ._capi import OmgDataType, OmgError, check, lib
 OMNI_INT, OMNI_LONG, OMNI_DOUBLE, OMNI_BOOLEAN, OMNI_SHORT = 1, 2, 3, 4, 5
 OMNI_DECIMAL64, OMNI_DECIMAL128, OMNI_DATE32, OMNI_DATE64, OMNI_TIMESTAMP = 6, 7, 8, 9, 12
 OMNI_BYTE, OMNI_FLOAT, OMNI_FIXEDBINARY = 18, 19, 40
-OMNI_VARCHAR, OMNI_CHAR = 15, 16
+OMNI_VARCHAR, OMNI_CHAR, OMNI_CONTAINER = 15, 16, 17
 # FunctionType (operator/util/function_type.h:11-27)
 OMNI_AGGREGATION_TYPE_SUM, OMNI_AGGREGATION_TYPE_COUNT_COLUMN = 0, 1
 OMNI_AGGREGATION_TYPE_COUNT_ALL, OMNI_AGGREGATION_TYPE_AVG = 2, 3
@@ -50,8 +50,8 @@ class DataType:
 
     @property
     def byte_width(self) -> int:
-        if self.id in (OMNI_VARCHAR, OMNI_CHAR):
-            return 0  # variable length
+        if self.id in (OMNI_VARCHAR, OMNI_CHAR, OMNI_CONTAINER):
+            return 0  # variable length, or a container of field vectors
         return self.width if self.id == OMNI_FIXEDBINARY else _WIDTH[self.id]
 
 
@@ -77,6 +77,13 @@ def BooleanType():
 
 def Decimal64Type(precision=18, scale=0):
     return DataType(OMNI_DECIMAL64, precision, scale)
+
+
+def ContainerType():
+    """OMNI_CONTAINER: a partial AVG's (double sum, long count) as one container column, the
+    output type of a partial AVG (and the input type of a final AVG) under the container-vector
+    policy (operator/aggregation/container_vector.h)."""
+    return DataType(OMNI_CONTAINER)
 
 
 def Decimal128Type(precision=38, scale=0):
@@ -266,12 +273,23 @@ def free_batches(batches) -> None:
 
 
 def batch_to_numpy(batch: int):
-    """[(values, null_mask)] of a host batch (copies)."""
+    """[(values, null_mask)] of a host batch (copies); a container vector (a partial AVG under
+    the container-vector policy) gives ("container", [(values, null_mask) per field])."""
     L = lib()
     n = L.omg_batch_row_count(batch)
     cols = []
     for i in range(L.omg_batch_vector_count(batch)):
         v = L.omg_batch_get(batch, i)
+        nf = L.omg_vec_num_fields(v)
+        if nf > 0:
+            cols.append(("container", [_vec_to_numpy(L, L.omg_vec_field(v, f), n) for f in range(nf)]))
+            continue
+        cols.append(_vec_to_numpy(L, v, n))
+    return cols
+
+
+def _vec_to_numpy(L, v, n):
+    if True:
         if L.omg_vec_is_device(v):
             raise ValueError("device batch: copy it to the host first (batch_to_host)")
         t = L.omg_vec_type(v)
@@ -296,8 +314,7 @@ def batch_to_numpy(batch: int):
             mask = np.unpackbits(bits, bitorder="little")[:n].astype(bool)
         else:
             mask = np.zeros(n, dtype=bool)
-        cols.append((vals, mask))
-    return cols
+        return vals, mask
 
 
 # --------------------------------------------------------------------------------- operators

@@ -372,6 +372,12 @@ BatchedAggregation::BatchedAggregation(HashAggregationOperatorFactory &factory, 
         throw OmniException("UNSUPPORTED_ERROR",
             "batched aggregation does not run plans with sticky-overflow sums; use one operator per task", -2);
     }
+    for (int32_t c : impl_->plan.outContainer) {
+        if (c > 0) {
+            throw OmniException("UNSUPPORTED_ERROR",
+                "batched aggregation does not emit container vectors; use one operator per task", -2);
+        }
+    }
     if (!impl_->plan.dictInputs.empty() || !impl_->plan.varlenInputs.empty()) {
         throw OmniException("UNSUPPORTED_ERROR",
             "batched aggregation does not run plans with VARCHAR/CHAR columns; use one operator per task", -2);

@@ -206,6 +206,14 @@ int32_t omg_vec_new_dictionary(const int32_t *ids, int32_t size, void *dictionar
 
 int32_t omg_vec_encoding(void *vec) { return vec ? static_cast<int32_t>(static_cast<BaseVector *>(vec)->GetEncoding()) : -1; }
 
+int32_t omg_vec_num_fields(void *vec) { return vec ? static_cast<BaseVector *>(vec)->NumFields() : -1; }
+
+void *omg_vec_field(void *vec, int32_t i)
+{
+    auto *v = static_cast<BaseVector *>(vec);
+    return v != nullptr && i >= 0 && i < v->NumFields() ? v->Field(i) : nullptr;
+}
+
 int32_t *omg_vec_offsets(void *vec) { return vec ? static_cast<BaseVector *>(vec)->RawOffsets() : nullptr; }
 int64_t omg_vec_data_bytes(void *vec) { return vec ? static_cast<BaseVector *>(vec)->DataBytes() : -1; }
 
@@ -1040,9 +1048,19 @@ int32_t omg_hashagg_run_noalloc(void *factory, const void *const *d_cols, const 
         SetError("no CUDA device is available");
         return OMG_ERR_NO_DEVICE;
     }
+    for (int32_t c : ap.outContainer) {
+        if (c > 0) {
+            SetError("container-vector outputs are not supported by the allocation-free entry point");
+            return OMG_ERR_UNSUPPORTED;
+        }
+    }
     omg::NoAllocPlan np;
     np.nInputs = static_cast<int32_t>(ap.inputCols.size());
     for (int32_t i = 0; i < np.nInputs; ++i) {
+        if (ap.inputCols[i] >= omg::kFieldRefBase) {
+            SetError("container-vector inputs are not supported by the allocation-free entry point");
+            return OMG_ERR_UNSUPPORTED;
+        }
         np.inputCols[i] = ap.inputCols[i];
     }
     np.key = ap.key;

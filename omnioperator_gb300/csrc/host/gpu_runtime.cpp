@@ -43,7 +43,8 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
         d.rows = b->GetRowCount();
         d.rowBase = totalRows_;
         for (size_t i = 0; i < inputCols.size(); ++i) {
-            const int32_t c = inputCols[i];
+            const bool fieldRef = inputCols[i] >= kFieldRefBase;
+            const int32_t c = fieldRef ? FieldRefColumn(inputCols[i]) : inputCols[i];
             if (c < 0 || c >= b->GetVectorCount()) {
                 throw OmniException("OPERATOR_RUNTIME_ERROR",
                     "input batch has " + std::to_string(b->GetVectorCount()) + " vectors, column " +
@@ -51,8 +52,19 @@ void BatchTable::Build(const std::vector<VectorBatch *> &batches, const std::vec
                     -1);
             }
             BaseVector *v = b->Get(c);
+            if (fieldRef) {
+                const int32_t f = FieldRefField(inputCols[i]);
+                if (v->GetEncoding() != omniruntime::vec::OMNI_ENCODING_CONTAINER || f >= v->NumFields()) {
+                    throw OmniException("OPERATOR_RUNTIME_ERROR",
+                        "column " + std::to_string(c) + " is not a container vector with field " + std::to_string(f), -1);
+                }
+                v = v->Field(f);
+            }
             if (v->GetEncoding() != omniruntime::vec::OMNI_FLAT) {
-                throw OmniException("OPERATOR_RUNTIME_ERROR", "dictionary vector reached a kernel unflattened", -1);
+                throw OmniException("OPERATOR_RUNTIME_ERROR",
+                    v->GetEncoding() == omniruntime::vec::OMNI_DICTIONARY ? "dictionary vector reached a kernel unflattened"
+                                                                           : "container vector used as a plain column",
+                    -1);
             }
             if (v->GetSize() < b->GetRowCount()) {
                 throw OmniException("OPERATOR_RUNTIME_ERROR", "vector shorter than the batch row count", -1);
@@ -280,15 +292,26 @@ std::vector<VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int6
     for (int64_t r0 = 0; r0 < rows; r0 += step) {
         const int32_t n = static_cast<int32_t>(std::min<int64_t>(step, rows - r0));
         auto *b = new VectorBatch(n);
-        for (const auto &c : cols) {
+        auto view = [&](const OutColumn &c) -> BaseVector * {
             const size_t nOff = static_cast<size_t>((firstRow + r0) / 8);
             if (c.width == 0) {
                 const size_t oOff = static_cast<size_t>(firstRow + r0) * sizeof(int32_t);
-                b->Append(new BaseVector(c.type, n, c.values, c.dataBytes, c.offsets, oOff, c.nulls, nOff, c.hasNull));
-                continue;
+                return new BaseVector(c.type, n, c.values, c.dataBytes, c.offsets, oOff, c.nulls, nOff, c.hasNull);
             }
             const size_t vOff = static_cast<size_t>(firstRow + r0) * c.width;
-            b->Append(new BaseVector(c.type, c.width, n, c.values, vOff, c.nulls, nOff, c.hasNull));
+            return new BaseVector(c.type, c.width, n, c.values, vOff, c.nulls, nOff, c.hasNull);
+        };
+        for (size_t i = 0; i < cols.size(); ++i) {
+            if (cols[i].containerFields > 0) {
+                std::vector<BaseVector *> fields;
+                for (int32_t f = 0; f < cols[i].containerFields; ++f) {
+                    fields.push_back(view(cols.at(i + f)));
+                }
+                b->Append(new BaseVector(fields));
+                i += static_cast<size_t>(cols[i].containerFields - 1);
+                continue;
+            }
+            b->Append(view(cols[i]));
         }
         out.push_back(b);
     }

@@ -161,6 +161,12 @@ private:
 constexpr int32_t InvertedMask(int32_t col) { return -2 - col; }
 constexpr int32_t kNullsOfMaskBase = 1 << 24;
 constexpr int32_t NullsOfMask(int32_t col) { return kNullsOfMaskBase + col; }
+// Kernel inputs that are field `f` of the container vector in column `c` (BatchTable::Build).
+constexpr int32_t kFieldRefBase = int32_t(1) << 29;
+inline int32_t FieldRef(int32_t c, int32_t f) { return kFieldRefBase + (c << 4) + f; }
+inline int32_t FieldRefColumn(int32_t ref) { return (ref - kFieldRefBase) >> 4; }
+inline int32_t FieldRefField(int32_t ref) { return (ref - kFieldRefBase) & 15; }
+
 class BatchTable {
 public:
     void Build(const std::vector<omniruntime::vec::VectorBatch *> &batches, const std::vector<int32_t> &inputCols,
@@ -265,6 +271,9 @@ struct OutColumn {
     bool hasNull;
     BufferPtr offsets;       // VARCHAR/CHAR: absolute positions in `values`
     int64_t dataBytes = 0;   // VARCHAR/CHAR: size of `values`
+    // > 0: this column and the next containerFields - 1 columns are the fields of one container
+    // vector in the output batches (a partial AVG under the container-vector policy).
+    int32_t containerFields = 0;
 };
 // The rows start at row `firstRow` of the buffers (a multiple of 8).
 std::vector<omniruntime::vec::VectorBatch *> CarveBatches(const std::vector<OutColumn> &cols, int64_t rows,

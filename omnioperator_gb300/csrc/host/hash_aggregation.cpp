@@ -277,6 +277,19 @@ OmniStatus HashAggregationOperatorFactory::Init()
         p.outTypes.push_back(t);
         rowBytes += o.outWidth;
     };
+    std::vector<size_t> containerAt;  // outs that start a two-field container output
+    // The (double sum, count) pair of a partial AVG: two flat outputs of the given types, or
+    // (avgContainer) the fields of one container output.
+    auto pushAvgPair = [&](const OutSpec &s1, const OutSpec &s2, const DataTypes &outTypes, bool avgContainer) {
+        if (avgContainer) {
+            containerAt.push_back(p.outs.size());
+            pushOut(s1, DoubleType());
+            pushOut(s2, LongType());
+        } else {
+            pushOut(s1, outTypes.GetType(0));
+            pushOut(s2, outTypes.GetType(1));
+        }
+    };
     for (size_t a = 0; a < nAgg; ++a) {
         const uint32_t fn = aggFuncTypes_[a];
         const bool raw = a < inputRaws_.size() ? static_cast<bool>(inputRaws_[a]) : true;
@@ -286,7 +299,21 @@ OmniStatus HashAggregationOperatorFactory::Init()
         const DataTypeId in0 = aggInputTypes_[a].GetSize() > 0 ? aggInputTypes_[a].GetType(0)->GetId() : OMNI_NONE;
         const bool decSum = fn == OMNI_AGGREGATION_TYPE_SUM && (in0 == OMNI_DECIMAL64 || in0 == OMNI_DECIMAL128);
         const bool decPair = decSum && partial;
-        if (outTypes.GetSize() != (avgPair || decPair ? 2 : 1)) {
+        // A partial AVG under the container-vector policy (average_aggregator.cpp:13-38): one
+        // CONTAINER output of (double sum, long count) fields in place of the two flat columns.
+        const bool avgContainer = avgPair && outTypes.GetSize() == 1 && outTypes.GetType(0)->GetId() == OMNI_CONTAINER;
+        for (int32_t t = 0; t < outTypes.GetSize() && !avgContainer; ++t) {
+            if (outTypes.GetType(t)->GetId() == OMNI_CONTAINER) {
+                throw OmniException("INVALID_ARGUMENT", "only a partial AVG emits a container column", -1);
+            }
+        }
+        for (int32_t t = 0; t < aggInputTypes_[a].GetSize(); ++t) {
+            if (aggInputTypes_[a].GetType(t)->GetId() == OMNI_CONTAINER &&
+                !(fn == OMNI_AGGREGATION_TYPE_AVG && !raw && aggInputTypes_[a].GetSize() == 1)) {
+                throw OmniException("INVALID_ARGUMENT", "only a merging AVG reads a container column", -1);
+            }
+        }
+        if (!avgContainer && outTypes.GetSize() != (avgPair || decPair ? 2 : 1)) {
             throw OmniException("INVALID_ARGUMENT",
                 avgPair ? "a partial AVG has two output types (double sum, long count)"
                         : (decPair ? "a partial decimal SUM has two output types (decimal sum, boolean isEmpty)"
@@ -412,30 +439,37 @@ OmniStatus HashAggregationOperatorFactory::Init()
             continue;
         }
         if (fn == OMNI_AGGREGATION_TYPE_AVG && !raw) {
-            // final AVG over (double sum, long count) partial columns
-            if (aggCols_[a].size() != 2 || aggInputTypes_[a].GetSize() != 2 ||
-                aggInputTypes_[a].GetType(0)->GetId() != OMNI_DOUBLE ||
-                !IsIntegerLike(aggInputTypes_[a].GetType(1)->GetId())) {
-                throw OmniException("INVALID_ARGUMENT", "a final AVG reads (double sum, long count) partial columns", -1);
+            // final AVG over (double sum, long count) partial columns, or over the fields of one
+            // CONTAINER column (average_aggregator.cpp:230-300)
+            const bool fromContainer = aggCols_[a].size() == 1 && aggInputTypes_[a].GetSize() == 1 &&
+                aggInputTypes_[a].GetType(0)->GetId() == OMNI_CONTAINER;
+            if (!fromContainer &&
+                (aggCols_[a].size() != 2 || aggInputTypes_[a].GetSize() != 2 ||
+                    aggInputTypes_[a].GetType(0)->GetId() != OMNI_DOUBLE ||
+                    !IsIntegerLike(aggInputTypes_[a].GetType(1)->GetId()))) {
+                throw OmniException("INVALID_ARGUMENT",
+                    "a final AVG reads (double sum, long count) partial columns or one container column", -1);
             }
-            const int inSum = inputFor(aggCols_[a][0], 8, mask);
-            const int inCnt = inputFor(aggCols_[a][1], aggInputTypes_[a].GetType(1)->ByteWidth(), mask);
+            const int cntW = fromContainer ? 8 : aggInputTypes_[a].GetType(1)->ByteWidth();
+            const int inSum = fromContainer ? inputFor(static_cast<uint32_t>(omg::FieldRef(aggCols_[a][0], 0)), 8, mask)
+                                            : inputFor(aggCols_[a][0], 8, mask);
+            const int inCnt = fromContainer ? inputFor(static_cast<uint32_t>(omg::FieldRef(aggCols_[a][0], 1)), 8, mask)
+                                            : inputFor(aggCols_[a][1], cntW, mask);
             accFor(omg::ACC_NULLS, inSum, omg::IN_NONE, 0, 0);
             accFor(omg::ACC_NULLS, inCnt, omg::IN_NONE, 0, 0);
             const int sumAcc = accFor(omg::ACC_DSUM, inSum, omg::IN_DOUBLE, 8, 0);
-            const int cntAcc = accFor(omg::ACC_ISUM, inCnt, omg::IN_INT, aggInputTypes_[a].GetType(1)->ByteWidth(), 0);
+            const int cntAcc = accFor(omg::ACC_ISUM, inCnt, omg::IN_INT, cntW, 0);
             if (partial) {  // an intermediate merge: still (sum, count)
                 OutSpec s1{};
                 s1.kind = omg::OUT_AVG_PARTIAL_SUM;
                 s1.src = static_cast<int16_t>(sumAcc);
                 s1.countAcc = static_cast<int16_t>(cntAcc);
                 s1.boundKind = 1;  // countAcc holds a summed count
-                pushOut(s1, outTypes.GetType(0));
                 OutSpec s2{};
                 s2.kind = omg::OUT_COUNT_MERGE;
                 s2.src = static_cast<int16_t>(cntAcc);
                 s2.countAcc = -1;
-                pushOut(s2, outTypes.GetType(1));
+                pushAvgPair(s1, s2, outTypes, avgContainer);
             } else {
                 o.kind = omg::OUT_AVG_MERGE;
                 o.src = static_cast<int16_t>(sumAcc);
@@ -567,12 +601,11 @@ OmniStatus HashAggregationOperatorFactory::Init()
                     s1.kind = omg::OUT_AVG_PARTIAL_SUM;
                     s1.countAcc = static_cast<int16_t>(nulls);
                     s1.boundKind = 0;  // countAcc holds the NULL count
-                    pushOut(s1, outTypes.GetType(0));
                     OutSpec s2{};
                     s2.kind = omg::OUT_COUNT;
                     s2.src = 0;
                     s2.countAcc = static_cast<int16_t>(nulls);
-                    pushOut(s2, outTypes.GetType(1));
+                    pushAvgPair(s1, s2, outTypes, avgContainer);
                     continue;
                 }
                 o.kind = omg::OUT_AVG;
@@ -674,6 +707,10 @@ OmniStatus HashAggregationOperatorFactory::Init()
     }
     p.smemSlots = static_cast<int32_t>(kSmemBudget / (p.slotWords * sizeof(uint64_t)));
     p.rowsPerBatch = GetMaxRowCount(rowBytes);
+    p.outContainer.assign(p.outs.size(), 0);
+    for (size_t i : containerAt) {
+        p.outContainer[i] = 2;
+    }
     // AlignSchema columns: each output of a raw-input partial plan restated for one row.
     bool alignable = nAgg > 0 && p.dictInputs.empty() && p.varlenInputs.empty();
     for (size_t a = 0; a < nAgg; ++a) {
@@ -929,7 +966,10 @@ VectorBatch *HashAggregationOperator::AlignSchema(VectorBatch *inputVecBatch)
         omg::OutColumn &oc = cols[o];
         oc.type = plan_.outTypes[o]->GetId();
         oc.width = plan_.outTypes[o]->ByteWidth();
-        oc.hasNull = c.input >= 0 && rows > 0 && bt.AnyNulls(c.input) &&
+        oc.containerFields = o < plan_.outContainer.size() ? plan_.outContainer[o] : 0;
+        const bool inContainer = (o < plan_.outContainer.size() && plan_.outContainer[o] > 0) ||
+            (o > 0 && o - 1 < plan_.outContainer.size() && plan_.outContainer[o - 1] > 1);
+        oc.hasNull = !inContainer && c.input >= 0 && rows > 0 && bt.AnyNulls(c.input) &&
             (c.op == omg::ALIGN_COPY || c.op == omg::ALIGN_INT || c.op == omg::ALIGN_DOUBLE);
         oc.values = omg::Buffer::NewDevice(static_cast<size_t>(rows) * oc.width + 16, s, false);
         oc.nulls = oc.hasNull ? omg::Buffer::NewDevice(omg::NullBitmapBytes(rows), s, true) : nullptr;
@@ -950,8 +990,21 @@ VectorBatch *HashAggregationOperator::AlignSchema(VectorBatch *inputVecBatch)
     impl_->stream.Sync();
     if (rows == 0) {
         auto *b = new VectorBatch(0);
-        for (const auto &c : cols) {
-            b->Append(new vec::BaseVector(c.type, c.width, 0, omg::Buffer::NewHost(16, false), 0, nullptr, 0, false));
+        for (size_t o = 0; o < cols.size(); ++o) {
+            const auto &c = cols[o];
+            auto empty = [](const omg::OutColumn &x) {
+                return new vec::BaseVector(x.type, x.width, 0, omg::Buffer::NewHost(16, false), 0, nullptr, 0, false);
+            };
+            if (c.containerFields > 0) {
+                std::vector<vec::BaseVector *> fields;
+                for (int32_t f = 0; f < c.containerFields; ++f) {
+                    fields.push_back(empty(cols[o + f]));
+                }
+                b->Append(new vec::BaseVector(fields));
+                o += static_cast<size_t>(c.containerFields - 1);
+                continue;
+            }
+            b->Append(empty(c));
         }
         return b;
     }
@@ -1498,7 +1551,11 @@ bool HashAggregationOperator::ExtractSpilled()
     const int32_t nInputs = static_cast<int32_t>(plan_.inputCols.size());
     std::vector<DataTypeId> colType(static_cast<size_t>(nInputs), OMNI_BYTE);
     for (int32_t i = 0; i < nInputs; ++i) {
-        colType[static_cast<size_t>(i)] = pending_.front()->Get(plan_.inputCols[i])->GetTypeId();
+        const int32_t c = plan_.inputCols[i];
+        const vec::BaseVector *v = c >= omg::kFieldRefBase
+            ? pending_.front()->Get(omg::FieldRefColumn(c))->Field(omg::FieldRefField(c))
+            : pending_.front()->Get(c);
+        colType[static_cast<size_t>(i)] = v->GetTypeId();
     }
     AggPlan partPlan = plan_;
     for (int32_t i = 0; i < nInputs; ++i) {
@@ -1657,6 +1714,13 @@ void HashAggregationOperator::Extract()
         cols[o].values = omg::Buffer::NewDevice(static_cast<size_t>(nGroups) * os.outWidth + 16, s, false);
         cols[o].nulls = omg::Buffer::NewDevice(omg::NullBitmapBytes(static_cast<int64_t>(nGroups)), s, true);
         cols[o].hasNull = os.kind != omg::OUT_COUNT && os.kind != omg::OUT_IS_EMPTY;
+    }
+    for (size_t o = 0; o < nOut && o < plan_.outContainer.size(); ++o) {
+        // A container's fields (a partial AVG's sum and count) are never NULL.
+        cols[o].containerFields = plan_.outContainer[o];
+        for (int32_t f = 0; f < plan_.outContainer[o]; ++f) {
+            cols[o + f].hasNull = false;
+        }
     }
     omg::AggExtract e;
     std::memset(&e, 0, sizeof(e));

@@ -170,12 +170,54 @@ bool VectorBatch::IsDevice() const
     return false;
 }
 
+BaseVector::BaseVector(std::vector<BaseVector *> fields) : type_(OMNI_CONTAINER), width_(0), size_(0)
+{
+    if (fields.empty()) {
+        throw exception::OmniException("INVALID_ARGUMENT", "a container vector needs fields", -1);
+    }
+    for (auto *f : fields) {
+        fields_.emplace_back(f);  // owned from here on
+    }
+    size_ = fields[0]->GetSize();
+    for (auto *f : fields) {
+        if (f->GetSize() != size_ || f->GetEncoding() != OMNI_FLAT) {
+            throw exception::OmniException("INVALID_ARGUMENT", "container fields are flat vectors of one length", -1);
+        }
+    }
+    // Values and residency are the first field's; no row is NULL unless every field has NULLs,
+    // which the operators' container outputs never have.
+    values_ = fields[0]->ValuesBuffer();
+    valuesOffset_ = fields[0]->ValuesOffset();
+    bool allNullable = true;
+    for (auto *f : fields) {
+        allNullable = allNullable && f->RawNulls() != nullptr && f->NullFlag();
+    }
+    if (allNullable) {
+        throw exception::OmniException("UNSUPPORTED_ERROR", "container vectors whose every field has NULLs", -2);
+    }
+}
+
 VectorBatch *VectorHelper::CopyBatch(VectorBatch *batch, bool toDevice, void *stream)
 {
     auto *out = new VectorBatch(batch->GetRowCount());
     try {
         for (int32_t i = 0; i < batch->GetVectorCount(); ++i) {
             BaseVector *src = batch->Get(i);
+            if (src->GetEncoding() == OMNI_ENCODING_CONTAINER) {
+                // Each field copied as a one-vector batch, then wrapped again.
+                std::vector<BaseVector *> fields;
+                for (int32_t f = 0; f < src->NumFields(); ++f) {
+                    VectorBatch one(batch->GetRowCount());
+                    one.Append(src->Field(f));
+                    VectorBatch *c = CopyBatch(&one, toDevice, stream);
+                    one.ClearVectors();  // the field stays the container's
+                    fields.push_back(c->Get(0));
+                    c->ClearVectors();
+                    delete c;
+                }
+                out->Append(new BaseVector(fields));
+                continue;
+            }
             std::unique_ptr<BaseVector> flat;
             if (src->GetEncoding() == OMNI_DICTIONARY) {
                 flat.reset(omg::FlattenDictionary(*src, static_cast<cudaStream_t>(stream)));

@@ -53,6 +53,9 @@ struct AggPlan {
     int32_t smemSlots = 0;                 // per-CTA shared pre-aggregation slots
     bool overflowAsNull = false;
     bool orderDependent = false;           // has an OUT_SUM_EXACT column (sticky overflow)
+    // Per output: > 0 when it starts a container output of that many fields (a partial AVG under
+    // the container-vector policy), 0 otherwise.
+    std::vector<int32_t> outContainer;
     std::vector<omg::AlignCol> align;      // AlignSchema columns; empty unless every aggregator
                                            // reads raw input and emits partials
     std::vector<int32_t> dictInputs;       // kernel inputs of VARCHAR/CHAR group-by columns: the

@@ -23,7 +23,7 @@ namespace omniruntime {
 namespace vec {
 using namespace omniruntime::type;
 
-enum Encoding { OMNI_FLAT = 0, OMNI_DICTIONARY = 1 };
+enum Encoding { OMNI_FLAT = 0, OMNI_DICTIONARY = 1, OMNI_ENCODING_CONTAINER = 2 };
 
 class NullsBuffer {
 public:
@@ -51,6 +51,11 @@ public:
     // [0, dictionary.GetSize()).  The operators flatten such vectors on the device when they
     // take a batch (omg::FlattenDictionaries).
     BaseVector(omg::BufferPtr ids, int32_t size, const BaseVector &dictionary);
+    // Container vector (operator/aggregation/container_vector.h:20-80): each row holds the values
+    // of several equally long field vectors, owned by this vector (a partial AVG's double sum and
+    // long count under the container-vector policy).  A row is NULL when it is NULL in every
+    // field; the fields the operators produce are never NULL.
+    explicit BaseVector(std::vector<BaseVector *> fields);
     virtual ~BaseVector() = default;
 
     bool IsVarlen() const { return type_ == OMNI_VARCHAR || type_ == OMNI_CHAR; }
@@ -66,7 +71,13 @@ public:
     int32_t GetSize() const { return size_; }
     DataTypeId GetTypeId() const { return type_; }
     int32_t GetWidth() const { return width_; }
-    Encoding GetEncoding() const { return dictionary_ ? OMNI_DICTIONARY : OMNI_FLAT; }
+    Encoding GetEncoding() const
+    {
+        return dictionary_ ? OMNI_DICTIONARY : (fields_.empty() ? OMNI_FLAT : OMNI_ENCODING_CONTAINER);
+    }
+    // Container encoding: the field vectors.
+    int32_t NumFields() const { return static_cast<int32_t>(fields_.size()); }
+    BaseVector *Field(int32_t i) const { return fields_.at(i).get(); }
     // Dictionary encoding: the row ids (int32) and the dictionary (a flat view).
     const int32_t *RawIds() const { return dictionary_ ? reinterpret_cast<const int32_t *>(RawValues()) : nullptr; }
     const BaseVector *Dictionary() const { return dictionary_.get(); }
@@ -119,6 +130,7 @@ protected:
     size_t offsetsOffset_ = 0;
     int64_t dataBytes_ = 0;
     std::shared_ptr<BaseVector> dictionary_;  // dictionary encoding only (values_ = the ids)
+    std::vector<std::shared_ptr<BaseVector>> fields_;  // container encoding only
 };
 
 // Typed host accessor (vector/vector.h Vector<T>::GetValue/SetValue).

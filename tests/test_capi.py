@@ -336,3 +336,20 @@ def test_quantile_join_strategy_choice():
     op.delete()
     pf.close()
     bf.close()
+
+
+def test_container_avg_types_accepted_only_for_avg():
+    """A partial AVG may emit one CONTAINER column and a merging AVG may read one; other
+    aggregators refuse container types (CPU: plan compilation only)."""
+    L, D, C_ = omg.LongType(), omg.DoubleType(), omg.ContainerType()
+    AVG, SUM = omg.OMNI_AGGREGATION_TYPE_AVG, omg.OMNI_AGGREGATION_TYPE_SUM
+    omg.HashAggregationOperatorFactory([0], [L], [[1]], [[D]], [[C_]], [AVG], output_partials=[True]).close()
+    omg.HashAggregationOperatorFactory([0], [L], [[1]], [[C_]], [[D]], [AVG], input_raws=[False]).close()
+    omg.HashAggregationOperatorFactory([0], [L], [[1]], [[C_]], [[C_]], [AVG], input_raws=[False],
+                                       output_partials=[True]).close()
+    for args, kw in [(([0], [L], [[1]], [[L]], [[C_]], [SUM]), {}),
+                     (([0], [L], [[1]], [[C_]], [[L]], [SUM]), {"input_raws": [False]}),
+                     (([0], [L], [[1]], [[C_]], [[D]], [AVG]), {})]:
+        with pytest.raises(omg.OmgError) as e:
+            omg.HashAggregationOperatorFactory(*args, **kw)
+        assert e.value.status == -1

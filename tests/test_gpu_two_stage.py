@@ -256,3 +256,81 @@ def test_adaptive_partial_aggregation_equals_single_stage(strategy):
     exact = {5: exact_by_key([key], [knull], vdbl, ~dnull, divide_by_count=True),
              6: exact_by_key([key], [knull], vdbl, ~dnull)}
     assert_agg_equal(cols, ora, 1, double_aggs=(5, 6), exact=exact)
+
+
+@pytest.mark.parametrize("policy", [omg.POLICY_GENERIC, omg.POLICY_SPARK])
+def test_container_avg_partial_intermediate_final(policy):
+    """The reference's container-vector form of a partial AVG (average_aggregator.cpp:13-38,
+    230-300): the partial emits one CONTAINER column of (double sum, long count) fields, an
+    intermediate stage reads and emits containers, the final AVG reads the container; the result
+    equals the flat-pair stages and single-stage AVG; AlignSchema emits the same container."""
+    C_ = omg.ContainerType()
+    n = 200_000
+    key, knull, vlong, vnull, vdbl, dnull, dead = _random_input(n, 21)
+    types = [L, L, D]
+    funcs = [AVG, AVG, CNT]
+    try:
+        omg.set_policy(policy)
+        part = omg.HashAggregationOperatorFactory([0], [L], [[2], [1], [1]], [[D], [L], [L]], [[C_], [C_], [L]], funcs,
+                                                  output_partials=[True] * 3)
+        partials = []
+        for s, e in [(0, n // 2), (n // 2, n)]:
+            batches = _batches(types, [key[s:e], vlong[s:e], vdbl[s:e]], [knull[s:e], vnull[s:e], dnull[s:e]],
+                               [4096, 777])
+            partials += _run(part, batches)
+        # the partial output: key | container(sum, count) | container(sum, count) | count
+        peek = omg.batch_to_numpy(partials[0])
+        assert peek[1][0] == "container" and len(peek[1][1]) == 2 and peek[1][1][0][0].dtype == np.float64
+        assert peek[1][1][1][0].dtype == np.int64 and not peek[1][1][0][1].any()
+        # AlignSchema of raw rows gives the same container layout
+        op = part.create_operator()
+        aligned = op.align_schema(_batches(types, [key[:5000], vlong[:5000], vdbl[:5000]],
+                                           [knull[:5000], vnull[:5000], dnull[:5000]], [5000])[0])
+        op.delete()
+        a = omg.batch_to_numpy(aligned)
+        assert a[1][0] == "container" and a[2][0] == "container" and len(a) == 4
+        cnt = a[1][1][1][0]
+        assert set(np.unique(cnt).tolist()) <= {0, 1}
+        partials.append(aligned)
+        part.close()
+        inter = omg.HashAggregationOperatorFactory([0], [L], [[1], [2], [3]], [[C_], [C_], [L]], [[C_], [C_], [L]],
+                                                   funcs, input_raws=[False] * 3, output_partials=[True] * 3)
+        mids = _run(inter, partials)
+        inter.close()
+        fin = omg.HashAggregationOperatorFactory([0], [L], [[1], [2], [3]], [[C_], [C_], [L]], [[D], [D], [L]],
+                                                 funcs, input_raws=[False] * 3)
+        cols = _columns(_run(fin, mids))
+        fin.close()
+    finally:
+        omg.set_policy(omg.POLICY_SPARK)
+    # single stage over all rows plus the AlignSchema rows counted twice
+    import math
+    k2 = np.concatenate([key, key[:5000]])
+    kn2 = np.concatenate([knull, knull[:5000]])
+    vl2, vn2 = np.concatenate([vlong, vlong[:5000]]), np.concatenate([vnull, vnull[:5000]])
+    vd2, dn2 = np.concatenate([vdbl, vdbl[:5000]]), np.concatenate([dnull, dnull[:5000]])
+    groups = {}
+    for kk, knn, xl, xln, xd, xdn in zip(k2.tolist(), kn2.tolist(), vl2.tolist(), vn2.tolist(), vd2.tolist(),
+                                         dn2.tolist()):
+        g = groups.setdefault(None if knn else kk, ([], [], [0]))
+        if not xdn:
+            g[0].append(xd)
+        if not xln:
+            g[1].append(float(xl))
+            g[2][0] += 1
+    got = {}
+    for i in range(len(cols[0][0])):
+        kk = None if cols[0][1][i] else int(cols[0][0][i])
+        got[kk] = (None if cols[1][1][i] else float(cols[1][0][i]), None if cols[2][1][i] else float(cols[2][0][i]),
+                   int(cols[3][0][i]))
+    assert set(got) == set(groups)
+    for kk, (avg_d, avg_l, c) in got.items():
+        ds, ls, cnt = groups[kk]
+        assert c == cnt[0]
+        assert (avg_d is None) == (len(ds) == 0) and (avg_l is None) == (len(ls) == 0)
+        if ds:
+            w = math.fsum(ds) / len(ds)
+            assert abs(avg_d - w) <= 1e-12 * max(1.0, abs(w)) + 1e-12 * max(abs(x) for x in ds)
+        if ls:
+            w = math.fsum(ls) / len(ls)
+            assert abs(avg_l - w) <= 1e-9 * max(1.0, abs(w))
