@@ -860,7 +860,8 @@ int32_t HashAggregationOperator::AddInput(VectorBatch *vecBatch)
         vec::VectorHelper::FreeVecBatch(vecBatch);
         return 0;
     }
-    for (int32_t c : plan_.inputCols) {
+    for (int32_t ref : plan_.inputCols) {
+        const int32_t c = ref >= omg::kFieldRefBase ? omg::FieldRefColumn(ref) : ref;  // a container's field
         if (c >= vecBatch->GetVectorCount()) {
             vec::VectorHelper::FreeVecBatch(vecBatch);
             throw OmniException("OPERATOR_RUNTIME_ERROR", "input batch lacks column " + std::to_string(c), -1);
@@ -943,8 +944,8 @@ VectorBatch *HashAggregationOperator::AlignSchema(VectorBatch *inputVecBatch)
     }
     const int64_t rows = inputVecBatch->GetRowCount();
     int32_t maxCol = 0;
-    for (int32_t c : plan_.inputCols) {
-        maxCol = std::max(maxCol, c + 1);
+    for (int32_t ref : plan_.inputCols) {
+        maxCol = std::max(maxCol, (ref >= omg::kFieldRefBase ? omg::FieldRefColumn(ref) : ref) + 1);
     }
     if (inputVecBatch->GetVectorCount() < maxCol) {
         throw OmniException("OPERATOR_RUNTIME_ERROR", "AlignSchema batch has too few vectors", -1);
