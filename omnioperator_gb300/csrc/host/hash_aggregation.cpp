@@ -1488,9 +1488,8 @@ void HashAggregationOperator::DecodeStrings(std::vector<omg::OutColumn> &cols, i
 
 void HashAggregationOperator::SetSpill(bool enabled, uint64_t deviceBudgetBytes)
 {
-    if (enabled && (!plan_.dictInputs.empty() || !plan_.varlenInputs.empty() || plan_.orderDependent)) {
-        throw OmniException("UNSUPPORTED_ERROR",
-            "spill does not take plans with VARCHAR/CHAR columns or order-dependent sticky-overflow sums", -2);
+    if (enabled && (!plan_.dictInputs.empty() || !plan_.varlenInputs.empty())) {
+        throw OmniException("UNSUPPORTED_ERROR", "spill does not take plans with VARCHAR/CHAR columns", -2);
     }
     if (enabled && deviceBudgetBytes == 0) {
         throw OmniException("INVALID_ARGUMENT", "spill needs a device memory budget", -1);
@@ -1603,6 +1602,14 @@ bool HashAggregationOperator::ExtractSpilled()
             DevArray<unsigned long long> counters(2 * static_cast<size_t>(nParts), s, true);
             a.hist = counters.Get();
             a.cursor = counters.Get() + nParts;
+            // Plans whose results depend on row order (sticky-overflow sums resolved by the
+            // ordered replay) keep the input order of each group's rows in its partition.
+            DevArray<unsigned int> tileHist;
+            if (plan_.orderDependent) {
+                tileHist.Reset(static_cast<size_t>(std::max(bt.NumTiles(), 1)) * static_cast<size_t>(nParts), s);
+                a.stable = 1;
+                a.tileHist = tileHist.Get();
+            }
             DevArray<omg::BatchDesc> partBatches(static_cast<size_t>(nParts), s);
             a.partBatches = partBatches.Get();
             a.maxTiles = static_cast<int32_t>(rows / omg::kTileRows + nParts + 1);

@@ -2071,6 +2071,152 @@ __global__ void __launch_bounds__(kScatterThreads) PartScatterKernel(const __gri
     }
 }
 
+// ---- stable partitioning (order-dependent plans) ----
+// Per tile: rows per partition.
+template <int kKind>
+__global__ void __launch_bounds__(512) PartTileHistKernel(const __grid_constant__ AggLaunch p,
+    const __grid_constant__ PartArgs a)
+{
+    __shared__ unsigned int h[kMaxParts];
+    const int nParts = 1 << a.partBits;
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+            h[i] = 0;
+        }
+        __syncthreads();
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        for (int r = threadIdx.x; r < tile.rows; r += blockDim.x) {
+            atomicAdd(&h[PartOf(ReadKey(p.key, b, static_cast<int64_t>(tile.row0) + r, kKind).hash, a.partBits)], 1u);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+            a.tileHist[static_cast<int64_t>(t) * nParts + i] = h[i];
+        }
+        __syncthreads();
+    }
+}
+
+// One block per partition: the exclusive prefix of its per-tile counts in tile order (in place)
+// and its total rows.
+__global__ void __launch_bounds__(1024) PartTileScanKernel(const __grid_constant__ PartArgs a, int32_t nTiles)
+{
+    __shared__ unsigned long long warpSum[32];
+    __shared__ unsigned long long carry;
+    const int q = blockIdx.x;
+    const int nParts = 1 << a.partBits;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        carry = 0;
+    }
+    __syncthreads();
+    for (int t0 = 0; t0 < nTiles; t0 += blockDim.x) {
+        const int t = t0 + static_cast<int>(threadIdx.x);
+        const unsigned long long v = t < nTiles ? a.tileHist[static_cast<int64_t>(t) * nParts + q] : 0ull;
+        unsigned long long incl = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long u = __shfl_up_sync(0xffffffffu, incl, d);
+            incl += lane >= d ? u : 0ull;
+        }
+        if (lane == 31) {
+            warpSum[warp] = incl;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const unsigned long long w = lane < static_cast<int>(blockDim.x >> 5) ? warpSum[lane] : 0ull;
+            unsigned long long wi = w;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long u = __shfl_up_sync(0xffffffffu, wi, d);
+                wi += lane >= d ? u : 0ull;
+            }
+            warpSum[lane] = wi - w;  // exclusive prefix of the warps
+        }
+        __syncthreads();
+        const unsigned long long excl = carry + warpSum[warp] + incl - v;
+        if (t < nTiles) {
+            a.tileHist[static_cast<int64_t>(t) * nParts + q] = static_cast<unsigned int>(excl);
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) {
+            carry = excl + v;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.hist[q] = carry;
+    }
+}
+
+// Per tile: each row to its partition at the tile's offset there plus its rank among the tile's
+// earlier rows of that partition (rounds in order; within a round, warps in order, then lanes).
+template <int kKind>
+__global__ void __launch_bounds__(kScatterThreads) PartScatterStableKernel(const __grid_constant__ AggLaunch p,
+    const __grid_constant__ PartArgs a)
+{
+    constexpr int kWarps = kScatterThreads / 32;
+    __shared__ unsigned int warpCnt[kWarps][kMaxParts];  // counts, then exclusive prefixes over warps
+    __shared__ unsigned int roundTotal[kMaxParts];
+    __shared__ unsigned long long running[kMaxParts];
+    const int nParts = 1 << a.partBits;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const unsigned int below = (1u << lane) - 1u;
+    for (int t = blockIdx.x; t < p.nTiles; t += gridDim.x) {
+        const TileDesc tile = p.tiles[t];
+        const BatchDesc &b = p.batches[tile.batch];
+        for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+            running[i] = a.cursor[i] + a.tileHist[static_cast<int64_t>(t) * nParts + i];
+        }
+        for (int j = 0; j < kScatterRows; ++j) {
+            for (int i = threadIdx.x; i < kWarps * kMaxParts; i += blockDim.x) {
+                warpCnt[i / kMaxParts][i % kMaxParts] = 0;
+            }
+            __syncthreads();
+            const int r = j * kScatterThreads + static_cast<int>(threadIdx.x);
+            const bool live = r < tile.rows;
+            const unsigned int active = __ballot_sync(0xffffffffu, live);
+            int q = 0;
+            unsigned int peers = 0;
+            if (live) {
+                q = PartOf(ReadKey(p.key, b, static_cast<int64_t>(tile.row0) + r, kKind).hash, a.partBits);
+                peers = __match_any_sync(active, q);
+                if ((peers & below) == 0) {
+                    warpCnt[warp][q] = __popc(peers);  // written by the partition's first lane
+                }
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+                unsigned int acc = 0;
+                for (int w = 0; w < kWarps; ++w) {
+                    const unsigned int c = warpCnt[w][i];
+                    warpCnt[w][i] = acc;
+                    acc += c;
+                }
+                roundTotal[i] = acc;
+            }
+            __syncthreads();
+            if (live) {
+                const uint64_t pos = running[q] + warpCnt[warp][q] + __popc(peers & below);
+                const int64_t row = static_cast<int64_t>(tile.row0) + r;
+                for (int i = 0; i < a.nInputs; ++i) {
+                    CopyInput(b.cols[i], row, a.cols[i], pos, a.width[i]);
+                    if (a.nulls[i] != nullptr && RowIsNull(b.nulls[i], row)) {
+                        atomicOr(&a.nulls[i][pos >> 5], 1u << (pos & 31));
+                    }
+                }
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < nParts; i += blockDim.x) {
+                running[i] += roundTotal[i];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ key sketch
 // A sample of the rows, stratified over the tiles of the launch (sample s reads a hashed row of
 // tile s * nTiles / nSample), is hashed into an open-addressing table of (hash, count);
@@ -2383,6 +2529,22 @@ cudaError_t LaunchAggPartition(const AggLaunch &p, const PartArgs &a, cudaStream
         return cudaSuccess;
     }
     const int grid = p.nTiles < NumSMs() * 4 ? p.nTiles : NumSMs() * 4;
+    if (a.stable) {
+        // Per-tile counts, their prefixes in tile order, the layout, then the ordered scatter.
+        if (p.key.kind == KEY_SINGLE) {
+            PartTileHistKernel<KEY_SINGLE><<<grid, 512, 0, stream>>>(p, a);
+        } else {
+            PartTileHistKernel<KEY_PACKED><<<grid, 512, 0, stream>>>(p, a);
+        }
+        PartTileScanKernel<<<1 << a.partBits, 1024, 0, stream>>>(a, p.nTiles);
+        PartLayoutKernel<<<1, kMaxParts, 0, stream>>>(a);
+        if (p.key.kind == KEY_SINGLE) {
+            PartScatterStableKernel<KEY_SINGLE><<<grid, kScatterThreads, 0, stream>>>(p, a);
+        } else {
+            PartScatterStableKernel<KEY_PACKED><<<grid, kScatterThreads, 0, stream>>>(p, a);
+        }
+        return cudaGetLastError();
+    }
     if (p.key.kind == KEY_SINGLE) {
         PartHistKernel<KEY_SINGLE><<<grid, 512, 0, stream>>>(p, a);
     } else {

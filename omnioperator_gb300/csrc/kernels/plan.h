@@ -212,6 +212,11 @@ struct PartArgs {
     TileDesc *partTiles;               // [maxTiles]
     int32_t *partTileStart;            // [nParts + 1]
     int32_t maxTiles;
+    // stable: rows keep their input order within every partition (tiles in order, rows of a tile
+    // in order), for plans whose results depend on row order; tileHist is then a [nTiles][nParts]
+    // scratch of per-tile counts.
+    int32_t stable;
+    unsigned int *tileHist;
 };
 
 // ---- key sketch of a row sample (feeds the group-count estimate) ----------------------------

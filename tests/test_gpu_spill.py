@@ -127,3 +127,31 @@ def test_spilled_partial_stage_feeds_a_final_stage():
                          [dict(func=f, col=v1, in_type=oracle.T_LONG, out_type=oracle.T_LONG, nulls=m1)
                           for f in (oracle.F_SUM, oracle.F_COUNT_COL)])
     assert_agg_equal(fcols, ora, 1)
+
+
+@pytest.mark.parametrize("device_input", [False, True])
+def test_spilled_order_dependent_sums_keep_row_order(device_input):
+    """Generic policy int64 SUM with sticky overflow (overflow -> NULL): whether a group overflows
+    depends on the order of its rows, so the spill partitions keep each group's rows in input
+    order; against the oracle folding the rows in order, and the unspilled run."""
+    rng = np.random.default_rng(71)
+    n, groups = 200_000, 3000
+    big = 2**62
+    key = rng.integers(0, groups, n).astype(np.int64) * 7919
+    val = np.where(rng.random(n) < 0.5, rng.choice(np.array([big, -big], dtype=np.int64), n),
+                   rng.integers(-10**6, 10**6, n, dtype=np.int64))
+    args = ([0], [L], [[1]], [[L]], [[L]], [SUM], {"overflow_as_null": True})
+    omg.set_policy(omg.POLICY_GENERIC)
+    try:
+        got, spilled, _ = _run(args, [key, val], [L, L], [None, None], 64 << 10, device_input=device_input)
+        plain, spilled0, _ = _run(args, [key, val], [L, L], [None, None], 0)
+        ora = oracle.hashagg([key], [oracle.T_LONG], [None],
+                             [dict(func=oracle.F_SUM, col=val, in_type=oracle.T_LONG, out_type=oracle.T_LONG)],
+                             policy=1, overflow_as_null=True)
+    finally:
+        omg.set_policy(omg.POLICY_SPARK)
+    assert spilled > 0 and spilled0 == 0
+    assert_agg_equal(got, ora, 1)
+    assert_agg_equal(plain, ora, 1)
+    nulls = int(got[1][1].sum())
+    assert 0 < nulls < groups  # both outcomes occur
