@@ -1486,10 +1486,59 @@ void HashAggregationOperator::DecodeStrings(std::vector<omg::OutColumn> &cols, i
     }
 }
 
+// A spilled partition's output batch (device) with the id columns `outs` turned back into
+// VARCHAR/CHAR vectors through this operator's dictionaries; copied to the host unless the
+// operator outputs device vectors.  Takes the batch, returns the result.
+VectorBatch *HashAggregationOperator::DecodeKeyIds(VectorBatch *batch, const std::vector<size_t> &outs, cudaStream_t s)
+{
+    Impl &im = *impl_;
+    std::unique_ptr<VectorBatch, void (*)(VectorBatch *)> b(batch, [](VectorBatch *x) { vec::VectorHelper::FreeVecBatch(x); });
+    const int64_t rows = b->GetRowCount();
+    for (size_t o : outs) {
+        const OutSpec &os = plan_.outs[o];
+        const int32_t input = plan_.key.cols[os.src].input;
+        const size_t j = static_cast<size_t>(
+            std::find(plan_.dictInputs.begin(), plan_.dictInputs.end(), input) - plan_.dictInputs.begin());
+        StringDict &d = im.dicts.at(j);
+        vec::BaseVector *v = b->Get(static_cast<int32_t>(o));
+        const int32_t *ids = reinterpret_cast<const int32_t *>(v->RawValues());
+        const uint8_t *nulls = v->NullFlag() ? v->RawNulls() : nullptr;
+        DevArray<uint32_t> lens(static_cast<size_t>(std::max<int64_t>(rows, 1)), s);
+        CudaCheck(omg::LaunchDictDecodeLens(ids, nulls, rows, d.arenaOff.Get(), lens.Get(), s), "key string lengths");
+        DevArray<int64_t> offs64;
+        const int64_t total = omg::ScanLengths(lens.Get(), rows, offs64, s);
+        if (total >= (int64_t(1) << 31)) {
+            throw OmniException("UNSUPPORTED_ERROR", "more than 2 GiB of VARCHAR group-by keys in one output batch", -2);
+        }
+        omg::BufferPtr chars = omg::Buffer::NewDevice(static_cast<size_t>(total) + 16, s, false);
+        omg::BufferPtr offs32 = omg::Buffer::NewDevice((static_cast<size_t>(rows) + 1) * sizeof(int32_t), s, false);
+        CudaCheck(omg::LaunchDictDecodeCopy(ids, nulls, rows, d.arenaOff.Get(), d.arena.Get(), offs64.Get(),
+                      static_cast<uint8_t *>(chars->Data()), static_cast<int32_t *>(offs32->Data()), total, s),
+            "key strings");
+        ++counters_[0];
+        im.stream.Sync();  // lens / offs64 are freed on return
+        b->Set(static_cast<int32_t>(o), new vec::BaseVector(plan_.outTypes[o]->GetId(), static_cast<int32_t>(rows), chars,
+                                            total, offs32, 0, v->NullsBufferPtr(), v->NullsOffset(), v->NullFlag()));
+    }
+    if (deviceOutput_) {
+        return b.release();
+    }
+    VectorBatch *h = vec::VectorHelper::CopyBatch(b.get(), false, s);
+    for (int32_t i = 0; i < h->GetVectorCount(); ++i) {
+        h->Get(i)->SetNullFlag(false);  // host vectors: HasNull() scans the bitmap
+    }
+    return h;
+}
+
 void HashAggregationOperator::SetSpill(bool enabled, uint64_t deviceBudgetBytes)
 {
-    if (enabled && (!plan_.dictInputs.empty() || !plan_.varlenInputs.empty())) {
-        throw OmniException("UNSUPPORTED_ERROR", "spill does not take plans with VARCHAR/CHAR columns", -2);
+    bool strAgg = !plan_.varlenInputs.empty();
+    for (const auto &o : plan_.outs) {
+        strAgg = strAgg || o.kind == omg::OUT_STR_ID;
+    }
+    if (enabled && strAgg) {
+        throw OmniException("UNSUPPORTED_ERROR",
+            "spill takes VARCHAR/CHAR group-by keys but not MIN/MAX or COUNT of VARCHAR/CHAR values", -2);
     }
     if (enabled && deviceBudgetBytes == 0) {
         throw OmniException("INVALID_ARGUMENT", "spill needs a device memory budget", -1);
@@ -1526,10 +1575,24 @@ bool HashAggregationOperator::ExtractSpilled()
     }
     const size_t slotBytes = static_cast<size_t>(plan_.slotWords) * sizeof(uint64_t);
     uint64_t estimate = 0;
+    // VARCHAR/CHAR keys: every pending row's string goes into this operator's dictionaries once;
+    // the partitions carry the int32 ids and the partitions' key ids come back as strings.
+    std::map<const VectorBatch *, std::vector<const void *>> idsOf;
     {
         omg::BatchTable bt;
         bt.Build(pending_, plan_.inputCols, omg::kTileRows, &plan_.inputMasks);
         bt.Upload(s);
+        if (!plan_.dictInputs.empty()) {
+            EncodeStrings(bt, s);
+            const size_t nIds = plan_.dictInputs.size();
+            for (size_t b = 0; b < pending_.size(); ++b) {
+                std::vector<const void *> &v = idsOf[pending_[b]];
+                for (size_t j = 0; j < nIds; ++j) {
+                    const omg::DevArray<int32_t> &ids = im.keptIds[im.keptIds.size() - nIds + j];
+                    v.push_back(ids.Get() + bt.BatchRowBase(b));
+                }
+            }
+        }
         if (!im.decided) {
             Decide(bt, s);
         }
@@ -1561,6 +1624,18 @@ bool HashAggregationOperator::ExtractSpilled()
     for (int32_t i = 0; i < nInputs; ++i) {
         partPlan.inputCols[i] = i;
         partPlan.inputMasks[i] = -1;
+        if (std::find(plan_.dictInputs.begin(), plan_.dictInputs.end(), i) != plan_.dictInputs.end()) {
+            colType[static_cast<size_t>(i)] = OMNI_INT;  // string ids
+        }
+    }
+    // The partitions aggregate the key ids as INT keys; the ids become strings afterwards.
+    partPlan.dictInputs.clear();
+    std::vector<size_t> strKeyOuts;
+    for (size_t o = 0; o < partPlan.outs.size(); ++o) {
+        if (partPlan.outs[o].kind == omg::OUT_KEY && IsVarlen(plan_.outTypes[o]->GetId())) {
+            partPlan.outTypes[o] = IntType();
+            strKeyOuts.push_back(o);
+        }
     }
     std::vector<std::vector<VectorBatch *>> parts(static_cast<size_t>(nParts));
     const int64_t chunkRows = omg::AggFlushRows();
@@ -1575,6 +1650,12 @@ bool HashAggregationOperator::ExtractSpilled()
             }
             omg::BatchTable bt;
             bt.Build(chunk, plan_.inputCols, omg::kTileRows, &plan_.inputMasks);
+            for (size_t b = 0; b < chunk.size() && !plan_.dictInputs.empty(); ++b) {
+                const std::vector<const void *> &v = idsOf.at(chunk[b]);
+                for (size_t j = 0; j < plan_.dictInputs.size(); ++j) {
+                    bt.SetInput(b, plan_.dictInputs[j], v[j]);
+                }
+            }
             bt.Upload(s);
             omg::AggLaunch p = MakeLaunch(plan_, nullptr, 0, nullptr, nullptr);
             p.batches = bt.DeviceBatches();
@@ -1657,7 +1738,8 @@ bool HashAggregationOperator::ExtractSpilled()
         }
         HashAggregationOperator part(partPlan, sizer_);
         part.SetStrategy(strategy_, 0);
-        part.SetDeviceOutput(deviceOutput_);
+        // String keys are decoded on the device: the partition's output stays there until then.
+        part.SetDeviceOutput(deviceOutput_ || !strKeyOuts.empty());
         if (userStreamSet_) {
             part.SetStream(userStream_);
         }
@@ -1674,6 +1756,9 @@ bool HashAggregationOperator::ExtractSpilled()
         }
         VectorBatch *out = nullptr;
         while (part.GetOutput(&out) != 0 && out != nullptr) {
+            if (!strKeyOuts.empty()) {
+                out = DecodeKeyIds(out, strKeyOuts, s);
+            }
             outputs_.push_back(out);
             counters_[5] += out->GetRowCount();
             out = nullptr;

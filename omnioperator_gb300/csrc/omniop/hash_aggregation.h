@@ -150,6 +150,7 @@ private:
     void EncodeStrings(omg::BatchTable &bt, cudaStream_t s);
     void BindStrings(omg::AggLaunch &p) const;
     void DecodeStrings(std::vector<omg::OutColumn> &cols, int64_t rows, cudaStream_t s);
+    VectorBatch *DecodeKeyIds(VectorBatch *batch, const std::vector<size_t> &outs, cudaStream_t s);
     void Extract();
     bool ExtractSpilled();
     void ReleasePending();

@@ -273,7 +273,8 @@ def test_two_stage_decimal_sum_plans_are_checked_on_the_host():
 
 
 def test_spill_settings_are_checked_on_the_host():
-    """Spill takes fixed-width plans (order-dependent sums included), and needs a budget."""
+    """Spill takes fixed-width plans (order-dependent sums included) and VARCHAR keys, not
+    VARCHAR MIN/MAX, and needs a budget."""
     L, V = omg.LongType(), omg.VarcharType(8)
     ok = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [omg.OMNI_AGGREGATION_TYPE_SUM])
     op = ok.create_operator()
@@ -285,7 +286,13 @@ def test_spill_settings_are_checked_on_the_host():
     op.delete()
     ok.close()
     d64, d128 = omg.Decimal64Type(18, 2), omg.Decimal128Type(38, 2)
+    # VARCHAR keys spill as dictionary ids; MIN/MAX of VARCHAR values does not spill
     fac = omg.HashAggregationOperatorFactory([0], [V], [[1]], [[L]], [[L]], [omg.OMNI_AGGREGATION_TYPE_SUM])
+    op = fac.create_operator()
+    op.set_spill(True, 1 << 20)
+    op.delete()
+    fac.close()
+    fac = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[V]], [[V]], [omg.OMNI_AGGREGATION_TYPE_MIN])
     op = fac.create_operator()
     with pytest.raises(omg.OmgError) as e:
         op.set_spill(True, 1 << 20)

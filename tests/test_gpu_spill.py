@@ -155,3 +155,41 @@ def test_spilled_order_dependent_sums_keep_row_order(device_input):
     assert_agg_equal(plain, ora, 1)
     nulls = int(got[1][1].sum())
     assert 0 < nulls < groups  # both outcomes occur
+
+
+@pytest.mark.parametrize("device_input", [False, True])
+def test_spilled_varchar_keys_equal_the_unspilled_run(device_input):
+    """VARCHAR group-by keys spill as their dictionary ids (the operator's string dictionary takes
+    every pending row first); the partitions aggregate the ids and their key columns come back as
+    strings.  Equal, row for row, to the unspilled run (itself checked against the oracle by the
+    VARCHAR aggregation tests), NULL keys and empty strings included."""
+    rng = np.random.default_rng(72)
+    n = 120_000
+    pool = [b""] + [bytes(rng.integers(97, 123, int(rng.integers(1, 20)), dtype=np.uint8)) for _ in range(6000)]
+    keys = np.array([pool[i] for i in rng.integers(0, len(pool), n)], dtype=object)
+    km = rng.random(n) < 0.01
+    v1 = rng.integers(-10**6, 10**6, n, dtype=np.int64)
+    m1 = rng.random(n) < 0.05
+    v2 = rng.random(n)
+    V = omg.VarcharType(24)
+    args = ([0], [V], [[1], [1], [1], [1], [2]], [[L], [L], [L], [L], [D]], [[L], [L], [L], [L], [D]],
+            [SUM, CNT, MIN, MAX, AVG])
+    got, spilled, _ = _run(args, [keys, v1, v2], [V, L, D], [km, m1, None], 32 << 10, device_input=device_input)
+    plain, spilled0, _ = _run(args, [keys, v1, v2], [V, L, D], [km, m1, None], 0)
+    assert spilled > 0 and spilled0 == 0
+
+    def rows(cols):
+        out = {}
+        for i in range(len(cols[0][0])):
+            k = None if cols[0][1][i] else bytes(cols[0][0][i])
+            out[k] = tuple(None if c[1][i] else (float(c[0][i]) if c[0].dtype.kind == "f" else int(c[0][i]))
+                           for c in cols[1:])
+        return out
+
+    a, b = rows(got), rows(plain)
+    assert set(a) == set(b) and len(a) > 5000
+    for k in a:
+        assert a[k][:4] == b[k][:4]
+        assert (a[k][4] is None) == (b[k][4] is None)
+        if a[k][4] is not None:
+            assert abs(a[k][4] - b[k][4]) <= 1e-12 * max(1.0, abs(b[k][4]))
