@@ -102,6 +102,11 @@ int32_t omg_device_available(void);
  * util/config_util.h).  OMG_POLICY_SPARK is the default. */
 int32_t omg_config_set_policy(int32_t policy);
 int32_t omg_config_get_policy(void);
+/* substr policies (util/policy.h:70-100, ConfigUtil::SetNegativeStartIndexOutOfBoundsRule and
+ * SetZeroStartIndexSupportRule): negative_rule 0 EMPTY_STRING, 1 INTERCEPT_FROM_BEYOND (default);
+ * zero_rule 0 IS_NOT_SUPPORT, 1 IS_SUPPORT (default).  Read by join factories created afterwards. */
+int32_t omg_config_set_substr_rules(int32_t negative_rule, int32_t zero_rule);
+int32_t omg_config_get_substr_rules(int32_t *negative_rule, int32_t *zero_rule);
 /* Fault injection on the host: the next `n` device allocations of this library fail
  * with OMG_ERR_OOM (0 disables).  Used by the tests; never touches the GPU. */
 int32_t omg_debug_fail_next_allocs(int32_t n);
@@ -261,12 +266,23 @@ int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_
  * 6 AND, 7 OR, 8 NOT, 9 ADD, 10 SUB, 11 MUL, 12 DIV, 13 MOD, 14 TRY_ADD, 15 TRY_SUB, 16 TRY_MUL,
  * 17 TRY_DIV.  The GB300 join runs comparisons, AND, OR, NOT, IS NULL and arithmetic (with the
  * reference's math-function semantics: integers wrap at the node's INT or LONG width, DIV/MOD by
- * zero and TRY_* overflow give NULL) over integer-like and DOUBLE columns and literals; other
- * trees (strings, functions, IN, CASE) are refused by the factory with OMG_ERR_UNSUPPORTED, as the
- * reference refuses what its code generator cannot compile. */
+ * zero and TRY_* overflow give NULL) over integer-like and DOUBLE columns and literals, and
+ * comparisons of VARCHAR/CHAR columns, literals and substr results (byte-wise unsigned, a
+ * proper prefix first: codegen/functions/stringfunctions.cpp StrCompare); other trees (other
+ * functions, IN, CASE) are refused by the factory with OMG_ERR_UNSUPPORTED, as the reference
+ * refuses what its code generator cannot compile. */
 int32_t omg_expr_field(int32_t col, const OmgDataType *type, void **out_expr);
 int32_t omg_expr_literal_long(int64_t value, const OmgDataType *type, int32_t is_null, void **out_expr);
 int32_t omg_expr_literal_double(double value, int32_t is_null, void **out_expr);
+/* LiteralExpr(std::string *, VarcharType/CharType): `len` bytes at `bytes` (copied). */
+int32_t omg_expr_literal_string(const char *bytes, int32_t len, const OmgDataType *type, int32_t is_null,
+    void **out_expr);
+/* FuncExpr(name, args, returnType) (expressions.h:243-266): takes ownership of the n_args
+ * argument trees.  The join filter compiles "substr" (2 or 3 arguments: a string, then INT or
+ * LONG start and length in UTF-8 code points; stringfunctions.h:215-318) under the substr
+ * policies in force when the join factory is created. */
+int32_t omg_expr_func(const char *name, void *const *args, int32_t n_args, const OmgDataType *return_type,
+    void **out_expr);
 int32_t omg_expr_binary(int32_t op, void *left, void *right, void **out_expr);
 /* BinaryExpr with an explicit return type (the reference's BinaryExpr(op, left, right, type)),
  * for arithmetic nodes (ADD .. TRY_DIV: the result is INT, LONG or DOUBLE). */

@@ -26,6 +26,8 @@ _SIGS = {
     "omg_device_available": (I32, []),
     "omg_config_set_policy": (I32, [I32]),
     "omg_config_get_policy": (I32, []),
+    "omg_config_set_substr_rules": (I32, [I32, I32]),
+    "omg_config_get_substr_rules": (I32, [C.POINTER(I32), C.POINTER(I32)]),
     "omg_debug_fail_next_allocs": (I32, [I32]),
     "omg_debug_set_wait_budget": (I32, [I64]),
     "omg_debug_set_staged_probe": (I32, [I32]),
@@ -68,6 +70,8 @@ _SIGS = {
     "omg_expr_field": (I32, [I32, P, C.POINTER(P)]),
     "omg_expr_literal_long": (I32, [I64, P, I32, C.POINTER(P)]),
     "omg_expr_literal_double": (I32, [C.c_double, I32, C.POINTER(P)]),
+    "omg_expr_literal_string": (I32, [C.c_char_p, I32, P, I32, C.POINTER(P)]),
+    "omg_expr_func": (I32, [C.c_char_p, C.POINTER(P), I32, P, C.POINTER(P)]),
     "omg_expr_binary": (I32, [I32, P, P, C.POINTER(P)]),
     "omg_expr_binary_typed": (I32, [I32, P, P, P, C.POINTER(P)]),
     "omg_expr_unary": (I32, [I32, P, C.POINTER(P)]),

@@ -119,6 +119,19 @@ def set_policy(policy: int) -> None:
     check(lib().omg_config_set_policy(policy))
 
 
+def set_substr_rules(negative: int, zero: int) -> None:
+    """ConfigUtil::SetNegativeStartIndexOutOfBoundsRule / SetZeroStartIndexSupportRule for join
+    factories created afterwards: negative 1 INTERCEPT_FROM_BEYOND (default) or 0 EMPTY_STRING,
+    zero 1 IS_SUPPORT (default) or 0 IS_NOT_SUPPORT."""
+    check(lib().omg_config_set_substr_rules(negative, zero))
+
+
+def get_substr_rules() -> tuple[int, int]:
+    n, z = C.c_int32(), C.c_int32()
+    check(lib().omg_config_get_substr_rules(C.byref(n), C.byref(z)))
+    return n.value, z.value
+
+
 def device_available() -> bool:
     return bool(lib().omg_device_available())
 
@@ -535,7 +548,8 @@ class Field:
 
 
 class Literal:
-    """LiteralExpr of an integer-like / BOOLEAN (int value) or DOUBLE (float value) type."""
+    """LiteralExpr of an integer-like / BOOLEAN (int value), DOUBLE (float value) or VARCHAR/CHAR
+    (bytes or str value, str as UTF-8) type."""
 
     def __init__(self, value, dtype: DataType, is_null: bool = False):
         self.value, self.dtype, self.is_null = value, dtype, is_null
@@ -547,6 +561,14 @@ class Binary:
 
     def __init__(self, op: int, left, right, dtype: DataType | None = None):
         self.op, self.left, self.right, self.dtype = op, left, right, dtype
+
+
+class Func:
+    """FuncExpr(name, args, dtype): a function call; the join filter compiles "substr" (a string,
+    then INT or LONG start and optional length), returning VARCHAR/CHAR `dtype`."""
+
+    def __init__(self, name: str, args: list, dtype: DataType):
+        self.name, self.args, self.dtype = name, list(args), dtype
 
 
 class Not:
@@ -566,6 +588,24 @@ def _expr_handle(e) -> int:
     if isinstance(e, Field):
         t = _types([e.dtype])
         check(L.omg_expr_field(e.col, t, C.byref(out)))
+    elif isinstance(e, Literal) and e.dtype.id in (OMNI_VARCHAR, OMNI_CHAR):
+        raw = b"" if e.is_null else (e.value.encode() if isinstance(e.value, str) else bytes(e.value))
+        check(L.omg_expr_literal_string(raw, len(raw), _types([e.dtype]), 1 if e.is_null else 0, C.byref(out)))
+    elif isinstance(e, Func):
+        args = []
+        try:
+            for a in e.args:
+                args.append(_expr_handle(a))
+        except Exception:
+            for h in args:
+                L.omg_expr_free(h)
+            raise
+        arr = (C.c_void_p * max(len(args), 1))(*args)
+        rc = L.omg_expr_func(e.name.encode(), arr, len(args), _types([e.dtype]), C.byref(out))
+        if rc != 0:
+            for h in args:
+                L.omg_expr_free(h)
+        check(rc)
     elif isinstance(e, Literal):
         if e.dtype.id == OMNI_DOUBLE:
             check(L.omg_expr_literal_double(float(e.value), 1 if e.is_null else 0, C.byref(out)))

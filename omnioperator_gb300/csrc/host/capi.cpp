@@ -119,6 +119,34 @@ int32_t omg_config_get_policy(void)
         : OMG_POLICY_GENERIC;
 }
 
+int32_t omg_config_set_substr_rules(int32_t negative_rule, int32_t zero_rule)
+{
+    return Guard([&] {
+        Require((negative_rule == 0 || negative_rule == 1) && (zero_rule == 0 || zero_rule == 1), "unknown rule");
+        omniruntime::op::SetNegativeStartIndexOutOfBoundsRule(negative_rule == 1
+                ? omniruntime::op::NegativeStartIndexOutOfBoundsRule::INTERCEPT_FROM_BEYOND
+                : omniruntime::op::NegativeStartIndexOutOfBoundsRule::EMPTY_STRING);
+        omniruntime::op::SetZeroStartIndexSupportRule(zero_rule == 1
+                ? omniruntime::op::ZeroStartIndexSupportRule::IS_SUPPORT
+                : omniruntime::op::ZeroStartIndexSupportRule::IS_NOT_SUPPORT);
+    });
+}
+
+int32_t omg_config_get_substr_rules(int32_t *negative_rule, int32_t *zero_rule)
+{
+    return Guard([&] {
+        Require(negative_rule != nullptr && zero_rule != nullptr, "invalid arguments");
+        *negative_rule = omniruntime::op::GetNegativeStartIndexOutOfBoundsRule() ==
+                omniruntime::op::NegativeStartIndexOutOfBoundsRule::INTERCEPT_FROM_BEYOND
+            ? 1
+            : 0;
+        *zero_rule =
+            omniruntime::op::GetZeroStartIndexSupportRule() == omniruntime::op::ZeroStartIndexSupportRule::IS_SUPPORT
+            ? 1
+            : 0;
+    });
+}
+
 int32_t omg_debug_fail_next_allocs(int32_t n)
 {
     omg::SetFailNextDeviceAllocs(n < 0 ? 0 : n);
@@ -438,6 +466,35 @@ int32_t omg_expr_literal_double(double value, int32_t is_null, void **out_expr)
         auto *l = new ex::LiteralExpr(value, omniruntime::type::DoubleType());
         l->isNull = is_null != 0;
         *out_expr = static_cast<ex::Expr *>(l);
+    });
+}
+
+int32_t omg_expr_literal_string(const char *bytes, int32_t len, const OmgDataType *type, int32_t is_null,
+    void **out_expr)
+{
+    return Guard([&] {
+        Require(type != nullptr && out_expr != nullptr && len >= 0 && (bytes != nullptr || len == 0) &&
+                (type->id == omniruntime::type::OMNI_VARCHAR || type->id == omniruntime::type::OMNI_CHAR),
+            "invalid arguments");
+        auto *l = new ex::LiteralExpr(new std::string(bytes == nullptr ? "" : std::string(bytes, len)), ToType(*type));
+        l->isNull = is_null != 0;
+        *out_expr = static_cast<ex::Expr *>(l);
+    });
+}
+
+int32_t omg_expr_func(const char *name, void *const *args, int32_t n_args, const OmgDataType *return_type,
+    void **out_expr)
+{
+    return Guard([&] {
+        Require(name != nullptr && return_type != nullptr && out_expr != nullptr && n_args >= 0 &&
+                (args != nullptr || n_args == 0),
+            "invalid arguments");
+        std::vector<ex::Expr *> a(static_cast<size_t>(n_args));
+        for (int32_t i = 0; i < n_args; ++i) {
+            Require(args[i] != nullptr, "null function argument");
+            a[i] = static_cast<ex::Expr *>(args[i]);
+        }
+        *out_expr = static_cast<ex::Expr *>(new ex::FuncExpr(name, std::move(a), ToType(*return_type)));
     });
 }
 

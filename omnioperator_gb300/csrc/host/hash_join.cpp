@@ -562,7 +562,12 @@ using omniruntime::expressions::Expr;
 using omniruntime::expressions::ExprType;
 using ExprOp = omniruntime::expressions::Operator;
 
-// Value kind of a filter operand type: 0 integer-like (compared as int64), 1 double, -1 none.
+// Value kind of a filter operand type: 0 integer-like (compared as int64), 1 double, 2 string
+// (VARCHAR/CHAR), -1 none.
+constexpr int kFilterInt = 0;
+constexpr int kFilterDouble = 1;
+constexpr int kFilterString = 2;
+
 int FilterKind(const DataTypePtr &t)
 {
     switch (t->GetId()) {
@@ -574,9 +579,12 @@ int FilterKind(const DataTypePtr &t)
         case OMNI_LONG:
         case OMNI_DATE64:
         case OMNI_TIMESTAMP:
-            return 0;
+            return kFilterInt;
         case OMNI_DOUBLE:
-            return 1;
+            return kFilterDouble;
+        case OMNI_VARCHAR:
+        case OMNI_CHAR:
+            return kFilterString;
         default:
             return -1;
     }
@@ -587,9 +595,18 @@ int FilterKind(const DataTypePtr &t)
     throw OmniException("EXPRESSION_NOT_SUPPORT", "The expression is not supported yet: " + what, -2);
 }
 
-// Postfix code of `e`; `depth` is the evaluation stack depth before it.
-void CompileFilter(const Expr *e, const DataTypes &probeTypes, const DataTypes &buildTypes,
-    std::vector<omg::FilterInstr> &code, std::vector<int32_t> &cols, int depth)
+// The postfix program being compiled, with the factory's literal bytes.
+struct FilterCode {
+    const DataTypes &probeTypes;
+    const DataTypes &buildTypes;
+    std::vector<omg::FilterInstr> &code;
+    std::vector<int32_t> &cols;
+    std::string &text;
+};
+
+// Postfix code of `e`; `depth` is the evaluation stack depth before it.  Returns the kind of
+// the value it leaves (FilterKind's codes).
+int CompileFilter(const Expr *e, FilterCode &fc, int depth)
 {
     if (e == nullptr) {
         FilterUnsupported("null node");
@@ -597,39 +614,43 @@ void CompileFilter(const Expr *e, const DataTypes &probeTypes, const DataTypes &
     omg::FilterInstr in;
     std::memset(&in, 0, sizeof(in));
     auto push = [&](int32_t col) {
-        if (depth + 1 > omg::kMaxFilterDepth || code.size() >= static_cast<size_t>(omg::kMaxFilterInstrs)) {
+        if (depth + 1 > omg::kMaxFilterDepth || fc.code.size() >= static_cast<size_t>(omg::kMaxFilterInstrs)) {
             FilterUnsupported("filter too large");
         }
-        code.push_back(in);
-        cols.push_back(col);
+        fc.code.push_back(in);
+        fc.cols.push_back(col);
     };
     auto emit = [&](int16_t op) {
-        if (code.size() >= static_cast<size_t>(omg::kMaxFilterInstrs)) {
+        if (fc.code.size() >= static_cast<size_t>(omg::kMaxFilterInstrs)) {
             FilterUnsupported("filter too large");
         }
         in.op = op;
-        code.push_back(in);
-        cols.push_back(-1);
+        fc.code.push_back(in);
+        fc.cols.push_back(-1);
     };
     switch (e->GetType()) {
         case ExprType::FIELD_E: {
             const auto *f = static_cast<const omniruntime::expressions::FieldExpr *>(e);
-            const int32_t nProbe = probeTypes.GetSize();
+            const int32_t nProbe = fc.probeTypes.GetSize();
             const bool probe = f->colVal < nProbe;
             const int32_t c = probe ? f->colVal : f->colVal - nProbe;
-            if (f->colVal < 0 || (!probe && c >= buildTypes.GetSize())) {
+            if (f->colVal < 0 || (!probe && c >= fc.buildTypes.GetSize())) {
                 throw OmniException("INVALID_ARGUMENT", "filter column out of range", -1);
             }
-            const DataTypePtr &t = probe ? probeTypes.GetType(c) : buildTypes.GetType(c);
+            const DataTypePtr &t = probe ? fc.probeTypes.GetType(c) : fc.buildTypes.GetType(c);
             const int kind = FilterKind(t);
             if (kind < 0) {
                 FilterUnsupported("column of type " + std::to_string(t->GetId()));
             }
-            in.op = probe ? omg::FOP_PROBE_COL : omg::FOP_BUILD_COL;
-            in.width = static_cast<int16_t>(t->ByteWidth());
-            in.dbl = static_cast<int16_t>(kind);
+            if (kind == kFilterString) {
+                in.op = probe ? omg::FOP_PROBE_STR : omg::FOP_BUILD_STR;
+            } else {
+                in.op = probe ? omg::FOP_PROBE_COL : omg::FOP_BUILD_COL;
+                in.width = static_cast<int16_t>(t->ByteWidth());
+                in.dbl = static_cast<int16_t>(kind);
+            }
             push(c);
-            return;
+            return kind;
         }
         case ExprType::LITERAL_E: {
             const auto *l = static_cast<const omniruntime::expressions::LiteralExpr *>(e);
@@ -637,16 +658,30 @@ void CompileFilter(const Expr *e, const DataTypes &probeTypes, const DataTypes &
             if (kind < 0) {
                 FilterUnsupported("literal of type " + std::to_string(l->dataType->GetId()));
             }
+            in.isNull = l->isNull ? 1 : 0;
+            if (kind == kFilterString) {
+                const std::string *v = l->isNull ? nullptr : l->stringVal;
+                if (v != nullptr && v->size() > static_cast<size_t>(INT32_MAX - 16)) {
+                    FilterUnsupported("string literal too long");
+                }
+                in.op = omg::FOP_STR_LITERAL;
+                in.input = v == nullptr ? 0 : static_cast<int32_t>(v->size());
+                in.imm = static_cast<int64_t>(fc.text.size());
+                if (v != nullptr) {
+                    fc.text += *v;
+                }
+                push(-1);
+                return kind;
+            }
             in.op = omg::FOP_LITERAL;
             in.dbl = static_cast<int16_t>(kind);
-            in.isNull = l->isNull ? 1 : 0;
-            if (kind == 1) {
+            if (kind == kFilterDouble) {
                 std::memcpy(&in.imm, &l->doubleVal, sizeof(double));
             } else {
                 in.imm = l->longVal;
             }
             push(-1);
-            return;
+            return kind;
         }
         case ExprType::BINARY_E: {
             const auto *b = static_cast<const omniruntime::expressions::BinaryExpr *>(e);
@@ -671,37 +706,72 @@ void CompileFilter(const Expr *e, const DataTypes &probeTypes, const DataTypes &
                 case ExprOp::TRY_DIV: op = omg::FOP_TRY_DIV; break;
                 default: FilterUnsupported("binary operator " + std::to_string(static_cast<int>(b->op)));
             }
-            CompileFilter(b->left, probeTypes, buildTypes, code, cols, depth);
-            CompileFilter(b->right, probeTypes, buildTypes, code, cols, depth + 1);
+            const int lk = CompileFilter(b->left, fc, depth);
+            const int rk = CompileFilter(b->right, fc, depth + 1);
+            const bool compare = op >= omg::FOP_EQ && op <= omg::FOP_GTE;
+            if ((lk == kFilterString || rk == kFilterString) && !(compare && lk == rk)) {
+                FilterUnsupported("string operand of binary operator " + std::to_string(static_cast<int>(b->op)));
+            }
             if (op >= omg::FOP_ADD) {
                 // Arithmetic (the reference's math functions): the node's return type sets the
                 // result width (int32 or int64, which wrap) or double.
                 const DataTypePtr &rt = b->GetReturnType();
                 const int kind = rt ? FilterKind(rt) : -1;
-                const int w = kind == 0 ? rt->ByteWidth() : 8;
-                if (kind < 0 || (kind == 0 && w != 4 && w != 8)) {
+                const int w = kind == kFilterInt ? rt->ByteWidth() : 8;
+                if ((kind != kFilterInt && kind != kFilterDouble) || (kind == kFilterInt && w != 4 && w != 8)) {
                     FilterUnsupported("arithmetic result of type " + std::to_string(rt ? rt->GetId() : -1));
                 }
                 in.width = static_cast<int16_t>(w);
                 in.dbl = static_cast<int16_t>(kind);
+                emit(op);
+                return kind;
             }
             emit(op);
-            return;
+            return kFilterInt;
         }
         case ExprType::UNARY_E: {
             const auto *u = static_cast<const omniruntime::expressions::UnaryExpr *>(e);
             if (u->op != ExprOp::NOT) {
                 FilterUnsupported("unary operator " + std::to_string(static_cast<int>(u->op)));
             }
-            CompileFilter(u->exp, probeTypes, buildTypes, code, cols, depth);
+            if (CompileFilter(u->exp, fc, depth) == kFilterString) {
+                FilterUnsupported("NOT of a string");
+            }
             emit(omg::FOP_NOT);
-            return;
+            return kFilterInt;
         }
         case ExprType::IS_NULL_E: {
             const auto *n = static_cast<const omniruntime::expressions::IsNullExpr *>(e);
-            CompileFilter(n->value, probeTypes, buildTypes, code, cols, depth);
+            CompileFilter(n->value, fc, depth);
             emit(omg::FOP_IS_NULL);
-            return;
+            return kFilterInt;
+        }
+        case ExprType::FUNC_E: {
+            // substr(str, start[, length]) with INT or LONG positions (func_registry_string.cpp:
+            // 440-466), under the substr policies in force when the factory is created.
+            const auto *fn = static_cast<const omniruntime::expressions::FuncExpr *>(e);
+            const size_t n = fn->arguments.size();
+            if (fn->funcName != "substr" || (n != 2 && n != 3)) {
+                FilterUnsupported("function " + fn->funcName + " with " + std::to_string(n) + " arguments");
+            }
+            if (CompileFilter(fn->arguments[0], fc, depth) != kFilterString) {
+                FilterUnsupported("substr of a non-string");
+            }
+            for (size_t a = 1; a < n; ++a) {
+                const Expr *arg = fn->arguments[a];
+                const DataTypePtr &t = arg->GetReturnType();
+                if (CompileFilter(arg, fc, depth + static_cast<int>(a)) != kFilterInt || t == nullptr ||
+                    (t->GetId() != OMNI_INT && t->GetId() != OMNI_LONG)) {
+                    FilterUnsupported("substr position of type " + std::to_string(t ? t->GetId() : -1));
+                }
+            }
+            in.width = static_cast<int16_t>(n);
+            const bool negative =
+                GetNegativeStartIndexOutOfBoundsRule() == NegativeStartIndexOutOfBoundsRule::INTERCEPT_FROM_BEYOND;
+            const bool zero = GetZeroStartIndexSupportRule() == ZeroStartIndexSupportRule::IS_SUPPORT;
+            in.input = (negative ? omg::kFilterSubstrNegative : 0) | (zero ? omg::kFilterSubstrZero : 0);
+            emit(omg::FOP_SUBSTR);
+            return kFilterString;
         }
         default:
             FilterUnsupported("expression kind " + std::to_string(static_cast<int>(e->GetType())));
@@ -725,8 +795,10 @@ LookupJoinOperatorFactory *LookupJoinOperatorFactory::CreateLookupJoinOperatorFa
         buildOutputTypes, builder));
     if (filterExpr != nullptr) {
         // JoinFilterCodeGen (lookup_join.cpp:175-187): compiled once per factory.
-        CompileFilter(static_cast<const Expr *>(filterExpr), probeTypes, f->build->buildTypes, f->filter,
-            f->filterCols, 0);
+        FilterCode fc{probeTypes, f->build->buildTypes, f->filter, f->filterCols, f->filterText};
+        if (CompileFilter(static_cast<const Expr *>(filterExpr), fc, 0) == kFilterString) {
+            FilterUnsupported("a string-valued filter");
+        }
         if (f->filter.empty()) {
             FilterUnsupported("empty filter");
         }
@@ -788,6 +860,7 @@ struct LookupJoinOperator::Impl {
     bool stop = false;
     std::exception_ptr error;
     int device = 0;
+    omg::DevArray<uint8_t> filterText;  // the filter's string literals in HBM
 };
 
 namespace {
@@ -1047,7 +1120,8 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchBatches
     }
     for (size_t i = 0; i < f_.filter.size(); ++i) {
         const int32_t c = f_.filterCols[i];
-        if (f_.filter[i].op == omg::FOP_PROBE_COL && inputOf.count(c) == 0) {
+        const int16_t op = f_.filter[i].op;
+        if ((op == omg::FOP_PROBE_COL || op == omg::FOP_PROBE_STR) && inputOf.count(c) == 0) {
             if (inputCols.size() >= static_cast<size_t>(omg::kMaxInputs)) {
                 throw OmniException("UNSUPPORTED_ERROR", "too many probe columns for the join kernels", -2);
             }
@@ -1101,15 +1175,25 @@ std::unique_ptr<LookupJoinOperator::ProbeCall> LookupJoinOperator::LaunchBatches
     p.visited = b.TracksVisits() ? b.visited.Get() : nullptr;
     // Join filter: bind probe operands to kernel inputs and build operands to the build columns.
     p.nFilter = static_cast<int32_t>(f_.filter.size());
+    if (!f_.filterText.empty() && impl_->filterText.Get() == nullptr) {
+        // The string literals' bytes, once per operator (the factory's copy outlives the copy).
+        impl_->filterText.Reset(f_.filterText.size(), s);
+        CudaCheck(cudaMemcpyAsync(impl_->filterText.Get(), f_.filterText.data(), f_.filterText.size(),
+                      cudaMemcpyHostToDevice, s),
+            "filter literals");
+    }
     for (size_t i = 0; i < f_.filter.size(); ++i) {
         omg::FilterInstr in = f_.filter[i];
         in.payloadShift = 0;  // set below when the column is a slot-payload field
         const int32_t c = f_.filterCols[i];
-        if (in.op == omg::FOP_PROBE_COL) {
+        if (in.op == omg::FOP_PROBE_COL || in.op == omg::FOP_PROBE_STR) {
             in.input = inputOf[c];
-        } else if (in.op == omg::FOP_BUILD_COL) {
+        } else if (in.op == omg::FOP_BUILD_COL || in.op == omg::FOP_BUILD_STR) {
             in.values = b.colValues[c].Get();
             in.nulls = b.colHasNull[c] ? b.colNulls[c].Get() : nullptr;
+            in.offs = in.op == omg::FOP_BUILD_STR ? b.colOffs[c].Get() : nullptr;
+        } else if (in.op == omg::FOP_STR_LITERAL) {
+            in.values = impl_->filterText.Get() + in.imm;
         }
         p.filter[i] = in;
     }

@@ -268,8 +268,14 @@ VectorBatch *VectorHelper::CopyBatch(VectorBatch *batch, bool toDevice, void *st
 namespace op {
 namespace {
 SupportContainerVecRule g_rule = SupportContainerVecRule::NOT_SUPPORT;
-}
+NegativeStartIndexOutOfBoundsRule g_negativeStart = NegativeStartIndexOutOfBoundsRule::INTERCEPT_FROM_BEYOND;
+ZeroStartIndexSupportRule g_zeroStart = ZeroStartIndexSupportRule::IS_SUPPORT;
+}  // namespace
 SupportContainerVecRule GetSupportContainerVecRule() { return g_rule; }
 void SetSupportContainerVecRule(SupportContainerVecRule rule) { g_rule = rule; }
+NegativeStartIndexOutOfBoundsRule GetNegativeStartIndexOutOfBoundsRule() { return g_negativeStart; }
+void SetNegativeStartIndexOutOfBoundsRule(NegativeStartIndexOutOfBoundsRule rule) { g_negativeStart = rule; }
+ZeroStartIndexSupportRule GetZeroStartIndexSupportRule() { return g_zeroStart; }
+void SetZeroStartIndexSupportRule(ZeroStartIndexSupportRule rule) { g_zeroStart = rule; }
 }  // namespace op
 }  // namespace omniruntime

@@ -831,6 +831,100 @@ __device__ __forceinline__ uint64_t PayloadField(const FilterInstr &f, uint64_t 
     return static_cast<uint64_t>(SignExtend(v, f.width));
 }
 
+// ---- strings in filters: a value is (pointer, byte length) ------------------------------------
+constexpr uint32_t kFString = 4;
+
+// Byte offset of the code point `count` places after byte `pos` of s[0, len), or -1 when the
+// string ends first (utf8_util.h:22-60): a code point starts at every byte that is not a UTF-8
+// continuation byte (10xxxxxx), so the answer is the (count + 1)-th such byte from `pos`.
+__device__ int32_t Utf8Offset(const uint8_t *s, int32_t len, int32_t pos, int32_t count)
+{
+    if (len - pos <= count) {
+        return -1;
+    }
+    if (count == 0) {
+        return pos;
+    }
+    int32_t seen = 0;
+    for (int32_t i = pos; i < len; ++i) {
+        if ((s[i] & 0xC0) != 0x80 && ++seen == count + 1) {
+            return i;
+        }
+    }
+    return -1;
+}
+
+// Code points of s[0, len): its bytes less its continuation bytes (utf8_util.h:62-91).
+__device__ int32_t Utf8Count(const uint8_t *s, int32_t len)
+{
+    int32_t cont = 0;
+    for (int32_t i = 0; i < len; ++i) {
+        cont += (s[i] & 0xC0) == 0x80 ? 1 : 0;
+    }
+    return len - cont;
+}
+
+// substr of s[0, len) as a byte range [*from, *from + *outLen) (stringfunctions.h:215-318,
+// SubstrVarcharWithStart and SubstrVarchar, start and length in code points, counted from 1 or,
+// when negative, from the end).  hasLength false: to the end of the string.  Where the
+// reference's result is undefined (a negative start into malformed UTF-8) the result is empty.
+__device__ void SubstrRange(const uint8_t *s, int32_t len, int64_t start, bool hasLength, int64_t length,
+    int rules, int32_t *from, int32_t *outLen)
+{
+    *from = 0;
+    *outLen = 0;
+    if ((rules & kFilterSubstrZero) != 0 && start == 0) {
+        start = 1;
+    }
+    if (start == 0 || (hasLength && length <= 0) || len == 0 || start > len) {
+        return;
+    }
+    int32_t startIndex;
+    int32_t endIndex = len;
+    if (start > 0) {
+        startIndex = Utf8Offset(s, len, 0, static_cast<int32_t>(start - 1));
+        if (startIndex < 0) {
+            return;
+        }
+        if (hasLength) {
+            endIndex = Utf8Offset(s, len, startIndex, static_cast<int32_t>(length));
+            endIndex = endIndex < 0 ? len : endIndex;
+        }
+    } else {
+        const int64_t points = Utf8Count(s, len);
+        int64_t startPoint = start + points;
+        if (startPoint < 0) {
+            if ((rules & kFilterSubstrNegative) == 0 || (hasLength && startPoint + length <= 0)) {
+                return;
+            }
+            length += startPoint;
+            startPoint = 0;
+        }
+        startIndex = Utf8Offset(s, len, 0, static_cast<int32_t>(startPoint));
+        if (startIndex < 0) {
+            return;
+        }
+        if (hasLength && startPoint + length < points) {
+            endIndex = Utf8Offset(s, len, startIndex, static_cast<int32_t>(length));
+            endIndex = endIndex < startIndex ? len : endIndex;
+        }
+    }
+    *from = startIndex;
+    *outLen = endIndex - startIndex;
+}
+
+// Byte-wise unsigned comparison, then by length: <0, 0 or >0 (stringfunctions.cpp StrCompare).
+__device__ int StrCompare(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb)
+{
+    const int32_t n = la < lb ? la : lb;
+    for (int32_t i = 0; i < n; ++i) {
+        if (a[i] != b[i]) {
+            return a[i] < b[i] ? -1 : 1;
+        }
+    }
+    return la < lb ? -1 : (la > lb ? 1 : 0);
+}
+
 // The filter program over the candidate pair (probe row `row` of batch b, build row `br`);
 // `payload` (when not null) is the candidate's slot payload.
 __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br,
@@ -838,10 +932,58 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
 {
     uint64_t v[kMaxFilterDepth];
     uint32_t fl[kMaxFilterDepth];
+    int32_t sl[kMaxFilterDepth];  // string values: byte length (v holds the address)
     int sp = 0;
     for (int i = 0; i < p.nFilter; ++i) {
         const FilterInstr &f = p.filter[i];
         const int op = f.op;
+        if (op == FOP_PROBE_STR || op == FOP_BUILD_STR || op == FOP_STR_LITERAL) {
+            if (sp >= kMaxFilterDepth) {
+                return false;  // the host limits the depth; never taken
+            }
+            const uint8_t *ptr = static_cast<const uint8_t *>(f.values);
+            int32_t len = f.input;
+            bool isNull = f.isNull != 0;
+            if (op == FOP_PROBE_STR) {
+                isNull = RowIsNullRO(b.nulls[f.input], row);
+                const int32_t *offs = b.offs[f.input];
+                const int32_t o0 = isNull ? 0 : offs[row];
+                ptr = static_cast<const uint8_t *>(b.cols[f.input]) + o0;
+                len = isNull ? 0 : offs[row + 1] - o0;
+            } else if (op == FOP_BUILD_STR) {
+                isNull = RowIsNullRO(f.nulls, br);
+                const int64_t o0 = isNull ? 0 : f.offs[br];
+                ptr += o0;
+                len = isNull ? 0 : static_cast<int32_t>(f.offs[br + 1] - o0);
+            }
+            v[sp] = reinterpret_cast<uint64_t>(ptr);
+            sl[sp] = len;
+            fl[sp] = (isNull ? kFNull : 0u) | kFString;
+            ++sp;
+            continue;
+        }
+        if (op == FOP_SUBSTR) {
+            const int nArgs = f.width;
+            if (sp < nArgs) {
+                return false;
+            }
+            const int base = sp - nArgs;
+            bool isNull = false;
+            for (int a = 0; a < nArgs; ++a) {
+                isNull = isNull || (fl[base + a] & kFNull) != 0;
+            }
+            int32_t from = 0, len = 0;
+            const uint8_t *str = reinterpret_cast<const uint8_t *>(v[base]);
+            if (!isNull) {
+                SubstrRange(str, sl[base], static_cast<int64_t>(v[base + 1]), nArgs == 3,
+                    nArgs == 3 ? static_cast<int64_t>(v[base + 2]) : 0, f.input, &from, &len);
+            }
+            v[base] = reinterpret_cast<uint64_t>(str + from);
+            sl[base] = len;
+            fl[base] = (isNull ? kFNull : 0u) | kFString;
+            sp = base + 1;
+            continue;
+        }
         if (op == FOP_PROBE_COL || op == FOP_BUILD_COL || op == FOP_LITERAL) {
             if (sp >= kMaxFilterDepth) {
                 return false;  // the host limits the depth; never taken
@@ -891,7 +1033,7 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
         const bool bn = (bf & kFNull) != 0;
         uint64_t res = 0;
         bool resNull = false;
-        if (op >= FOP_ADD) {
+        if (op >= FOP_ADD && op <= FOP_TRY_DIV) {
             resNull = an || bn;
             if (!resNull) {
                 if (f.dbl) {
@@ -978,7 +1120,14 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
             resNull = true;
         } else {
             int c;
-            if ((af | bf) & kFDouble) {
+            if ((af & bf) & kFString) {
+                const uint8_t *x = reinterpret_cast<const uint8_t *>(av);
+                const uint8_t *y = reinterpret_cast<const uint8_t *>(bv);
+                const int32_t lx = sl[sp - 1];
+                const int32_t ly = sl[sp];
+                c = (op == FOP_EQ || op == FOP_NEQ) && lx != ly ? 1 : StrCompare(x, lx, y, ly);
+                c = c < 0 ? -1 : (c > 0 ? 1 : 0);
+            } else if ((af | bf) & kFDouble) {
                 const double x = FilterAsDouble(av, af);
                 const double y = FilterAsDouble(bv, bf);
                 c = x < y ? -1 : (x > y ? 1 : (x == y ? 0 : 2));  // 2: unordered (NaN)
@@ -1701,7 +1850,7 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
         simpleFilter = kFilter == 2 || SimpleFilterShape(p);
         filterNeedsRow = p.visited != nullptr;
         for (int f = 0; f < p.nFilter; ++f) {
-            filterNeedsRow = filterNeedsRow ||
+            filterNeedsRow = filterNeedsRow || p.filter[f].op == FOP_BUILD_STR ||
                 (p.filter[f].op == FOP_BUILD_COL && (payloadTab == nullptr || p.filter[f].payloadShift == 0));
         }
     }

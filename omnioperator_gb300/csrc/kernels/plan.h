@@ -427,7 +427,20 @@ enum FilterOp : int16_t {
     // fmod.  A NULL operand gives NULL.
     FOP_ADD, FOP_SUB, FOP_MUL, FOP_DIV, FOP_MOD,
     FOP_TRY_ADD, FOP_TRY_SUB, FOP_TRY_MUL, FOP_TRY_DIV,
+    // Strings (VARCHAR/CHAR): a string value is a (pointer, byte length) pair; the comparisons
+    // above compare two strings byte-wise as unsigned, a proper prefix first
+    // (codegen/functions/stringfunctions.cpp StrCompare / StrEquals).
+    FOP_PROBE_STR,    // push probe input `input` (characters and int32 offsets of its batch)
+    FOP_BUILD_STR,    // push build column: values = characters, offs = int64 offsets, nulls
+    FOP_STR_LITERAL,  // push values (device bytes) of length `input`, NULL when isNull
+    // substr(str, start[, length]) over UTF-8 code points (stringfunctions.h:215-318): width =
+    // 2 or 3 arguments, input bit 0: a negative start before the string keeps the part inside it
+    // (INTERCEPT_FROM_BEYOND), bit 1: start 0 means 1 (ZeroStartIndexSupportRule IS_SUPPORT).
+    // A NULL argument gives NULL.
+    FOP_SUBSTR,
 };
+constexpr int kFilterSubstrNegative = 1;
+constexpr int kFilterSubstrZero = 2;
 constexpr int kMaxFilterInstrs = 24;
 constexpr int kMaxFilterDepth = 8;
 
@@ -438,8 +451,9 @@ struct FilterInstr {
     int16_t isNull;   // literals: NULL
     int32_t input;    // FOP_PROBE_COL: probe kernel input index
     int32_t payloadShift;  // FOP_BUILD_COL: s + 1 when the column is also a slot-payload field at bit s
-    const void *values;    // FOP_BUILD_COL: contiguous build column
-    const uint8_t *nulls;  // FOP_BUILD_COL: its NULL bitmap (may be null)
+    const void *values;    // FOP_BUILD_COL / FOP_BUILD_STR: contiguous build column
+    const uint8_t *nulls;  // FOP_BUILD_COL / FOP_BUILD_STR: its NULL bitmap (may be null)
+    const int64_t *offs;   // FOP_BUILD_STR: the column's row offsets into values
     int64_t imm;
 };
 

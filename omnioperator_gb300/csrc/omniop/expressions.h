@@ -5,13 +5,15 @@
 // joined row (probe columns first, then build columns, as LookupJoinOperator numbers them,
 // lookup_join.cpp:215-240), a BinaryExpr owns its two children.  The GB300 join compiles a
 // filter tree into a postfix program that the probe kernel runs per candidate pair
-// (CompileJoinFilter in host/hash_join.cpp); comparisons, NOT, AND, OR and IS [NOT] NULL over
-// fixed-width integer-like and double columns and literals are supported, anything else is
-// refused with EXPRESSION_NOT_SUPPORT as the reference refuses expressions its code generator
-// cannot handle (lookup_join.cpp:175-187).
+// (CompileJoinFilter in host/hash_join.cpp); comparisons, NOT, AND, OR, IS [NOT] NULL and
+// arithmetic over fixed-width integer-like and double columns and literals, VARCHAR/CHAR columns
+// and literals, and the substr function (a FuncExpr) are supported, anything else is refused
+// with EXPRESSION_NOT_SUPPORT as the reference refuses expressions its code generator cannot
+// handle (lookup_join.cpp:175-187).
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include "types.h"
@@ -58,9 +60,16 @@ public:
     // Integer-like and BOOLEAN literals (the value as int64); isNull for a NULL literal.
     LiteralExpr(int64_t v, type::DataTypePtr t) : Expr(std::move(t)), longVal(v) {}
     LiteralExpr(double v, type::DataTypePtr t) : Expr(std::move(t)), doubleVal(v) {}
+    // VARCHAR/CHAR literal; takes ownership of `v`, as the reference's LiteralExpr(std::string *,
+    // DataTypePtr) does.
+    LiteralExpr(std::string *v, type::DataTypePtr t) : Expr(std::move(t)), stringVal(v) {}
+    ~LiteralExpr() override { delete stringVal; }
+    LiteralExpr(const LiteralExpr &) = delete;
+    LiteralExpr &operator=(const LiteralExpr &) = delete;
     ExprType GetType() const override { return ExprType::LITERAL_E; }
     int64_t longVal = 0;
     double doubleVal = 0.0;
+    std::string *stringVal = nullptr;
     bool isNull = false;
 };
 
@@ -87,6 +96,20 @@ public:
     ExprType GetType() const override { return ExprType::UNARY_E; }
     Operator op;
     Expr *exp;
+};
+
+// A function call by name (expressions.h FuncExpr): owns its arguments.
+class FuncExpr : public Expr {
+public:
+    FuncExpr(std::string fnName, std::vector<Expr *> args, type::DataTypePtr returnType)
+        : Expr(std::move(returnType)), funcName(std::move(fnName)), arguments(std::move(args))
+    {}
+    ~FuncExpr() override { DeleteExprs(arguments); }
+    FuncExpr(const FuncExpr &) = delete;
+    FuncExpr &operator=(const FuncExpr &) = delete;
+    ExprType GetType() const override { return ExprType::FUNC_E; }
+    std::string funcName;
+    std::vector<Expr *> arguments;
 };
 
 class IsNullExpr : public Expr {

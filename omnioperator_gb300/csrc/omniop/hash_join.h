@@ -19,6 +19,7 @@
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "kernels/plan.h"
@@ -106,6 +107,8 @@ public:
     // instruction i, -1 for the others.
     std::vector<omg::FilterInstr> filter;
     std::vector<int32_t> filterCols;
+    // Bytes of the filter's string literals (FOP_STR_LITERAL: imm is the offset of its bytes).
+    std::string filterText;
     // Build output values packed per table slot, built by the first probe that can use it.
     mutable std::mutex payloadMu;
     mutable omg::BufferPtr slotPayload;

@@ -186,6 +186,15 @@ enum class SupportContainerVecRule { NOT_SUPPORT = 0, SUPPORT = 1 };
 SupportContainerVecRule GetSupportContainerVecRule();
 void SetSupportContainerVecRule(SupportContainerVecRule rule);
 
+// substr policies (util/policy.h:70-100); the Spark defaults are INTERCEPT_FROM_BEYOND and
+// IS_SUPPORT.  A join filter reads them when its factory compiles it.
+enum class NegativeStartIndexOutOfBoundsRule { EMPTY_STRING = 0, INTERCEPT_FROM_BEYOND = 1 };
+enum class ZeroStartIndexSupportRule { IS_NOT_SUPPORT = 0, IS_SUPPORT = 1 };
+NegativeStartIndexOutOfBoundsRule GetNegativeStartIndexOutOfBoundsRule();
+void SetNegativeStartIndexOutOfBoundsRule(NegativeStartIndexOutOfBoundsRule rule);
+ZeroStartIndexSupportRule GetZeroStartIndexSupportRule();
+void SetZeroStartIndexSupportRule(ZeroStartIndexSupportRule rule);
+
 // Rows per output VectorBatch: ceil(1 MiB / rowSize) (operator/util/operator_util.h:33,111-115).
 inline int32_t GetMaxRowCount(int32_t rowSize)
 {

@@ -232,6 +232,78 @@ def join(kind, build_keys, build_nulls, probe_keys, probe_nulls):
         cap = n
 
 
+def utf8_offset(data: bytes, pos: int, count: int) -> int:
+    """Byte offset of the code point `count` places after byte `pos`, or -1 when the string ends
+    first (utf8_util.h:22-60, OffsetOfCodePoint).  The reference adds the continuation bytes
+    (10xxxxxx) it passes to the target index until it reaches it; the answer is the
+    (count + 1)-th byte from `pos` that is not a continuation byte."""
+    n = len(data)
+    if n - pos <= count:
+        return -1
+    if count == 0:
+        return pos
+    seen = 0
+    for i in range(pos, n):
+        if data[i] & 0xC0 != 0x80:
+            seen += 1
+            if seen == count + 1:
+                return i
+    return -1
+
+
+def utf8_count(data: bytes) -> int:
+    """Code points: bytes less continuation bytes (utf8_util.h:62-91, CountCodePoints)."""
+    return len(data) - sum(1 for c in data if c & 0xC0 == 0x80)
+
+
+def _i32(x: int) -> int:
+    """The int32 parameter of OffsetOfCodePoint receiving an int64 (two's-complement truncation)."""
+    return ((x + 2**31) % 2**32) - 2**31
+
+
+def substr(data: bytes, start: int, length=None, negative: bool = True, zero: bool = True) -> bytes:
+    """substr over UTF-8 code points (stringfunctions.h:215-250 SubstrVarcharWithStart when
+    length is None, :258-318 SubstrVarchar).  negative: NegativeStartIndexOutOfBoundsRule
+    INTERCEPT_FROM_BEYOND (a start before the string keeps the part inside it; EMPTY_STRING
+    otherwise); zero: ZeroStartIndexSupportRule IS_SUPPORT (start 0 means 1).  Both default to
+    the Spark policy (policy.h:160-167).  Where the reference reads outside the string (a
+    negative start into malformed UTF-8) the result is empty."""
+    n = len(data)
+    if zero and start == 0:
+        start = 1
+    if start == 0 or (length is not None and length <= 0) or n == 0 or start > n:
+        return b""
+    if start > 0:
+        si = utf8_offset(data, 0, _i32(start - 1))
+        if si < 0:
+            return b""
+        if length is None:
+            return data[si:]
+        ei = utf8_offset(data, si, _i32(length))
+        return data[si:n if ei < 0 else ei]
+    points = utf8_count(data)
+    sp = start + points
+    ln = 0 if length is None else length
+    if sp < 0:
+        if not negative or (length is not None and sp + ln <= 0):
+            return b""
+        ln += sp
+        sp = 0
+    si = utf8_offset(data, 0, _i32(sp))
+    if si < 0:
+        return b""
+    if length is None or sp + ln >= points:
+        return data[si:]
+    ei = utf8_offset(data, si, _i32(ln))
+    return data[si:n if ei < si else ei]
+
+
+def str_compare(a: bytes, b: bytes) -> int:
+    """Byte-wise unsigned comparison, then by length: -1, 0 or 1 (stringfunctions.cpp:86-98,
+    StrCompare; StrEquals at :75-84 after equal lengths)."""
+    return -1 if a < b else (1 if a > b else 0)
+
+
 def join_filtered(kind, build_keys, build_nulls, probe_keys, probe_nulls, passes):
     """join() with a join filter: a (probe, build) pair whose keys are equal counts as a match
     only when passes(probe_rows, build_rows) (a vectorised predicate over pair arrays) is true.

@@ -270,6 +270,60 @@ def _array_map_cases():
     return out
 
 
+# core/test/codegen/function_test.cpp:2030-2506 -- substr over UTF-8 code points, each call as
+# (string, start, length or None for SubstrVarcharWithStart, supports negative start,
+# supports zero start, expected).  SubstrChar takes the same (str, strLen) and gives the same.
+_MAGIC = "Magic Johnson 123@#$"
+_ZH = "时欧基乌斯侧后解 hello! 回复哦黑色的and magic粉色的圣诞袜"
+_ABC = "ABC efg 123 $%^"
+_ZH9 = "时欧基乌斯侧后解 h"
+SUBSTR = {
+    "Substr": ("core/test/codegen/function_test.cpp:2030-2070", [
+        (_MAGIC, 1, 20, False, False, _MAGIC), (_MAGIC, 1, 5, False, False, "Magic"),
+        (_MAGIC, 10, 10, False, False, "nson 123@#"), (_MAGIC, -5, 7, False, False, "23@#$"),
+        (_MAGIC, 0, 0, False, False, ""), (_MAGIC, 20, 25, False, False, "$")]),
+    "SubstrZh": ("core/test/codegen/function_test.cpp:2072-2138", [
+        (_ZH, 1, 37, False, False, _ZH), (_ZH, 0, 37, False, True, _ZH), (_ZH, 1, 5, False, False, "时欧基乌斯"),
+        (_ZH, 0, 5, False, True, "时欧基乌斯"), (_ZH, 10, 10, False, False, "hello! 回复哦"),
+        (_ZH, -5, 7, False, False, "色的圣诞袜"), (_ZH, 0, 0, False, False, ""), (_ZH, 0, 0, False, True, ""),
+        (_ZH, 37, len(_ZH.encode()) + 5, False, False, "袜"), (_ZH, -38, 10, False, False, ""),
+        (_ZH, -37, 37, False, False, _ZH)]),
+    "SubstrChar": ("core/test/codegen/function_test.cpp:2140-2198", [
+        (_MAGIC, 1, 20, False, False, _MAGIC), (_MAGIC, 0, 20, False, True, _MAGIC),
+        (_MAGIC, 1, 5, False, False, "Magic"), (_MAGIC, 0, 5, False, True, "Magic"),
+        (_MAGIC, 10, 10, False, False, "nson 123@#"), (_MAGIC, -5, 7, False, False, "23@#$"),
+        (_MAGIC, 0, 0, False, False, ""), (_MAGIC, 0, 0, False, True, ""), (_MAGIC, 20, 25, False, False, "$")]),
+    "SubstrCharZh": ("core/test/codegen/function_test.cpp:2200-2267", [
+        (_ZH, 1, 37, False, False, _ZH), (_ZH, 0, 37, False, True, _ZH), (_ZH, 1, 5, False, False, "时欧基乌斯"),
+        (_ZH, 0, 5, False, True, "时欧基乌斯"), (_ZH, 10, 10, False, False, "hello! 回复哦"),
+        (_ZH, -5, 7, False, False, "色的圣诞袜"), (_ZH, 0, 0, False, False, ""), (_ZH, 0, 0, False, True, ""),
+        (_ZH, 37, len(_ZH.encode()) + 5, False, False, "袜"), (_ZH, -38, 10, False, False, ""),
+        (_ZH, -37, 37, False, False, _ZH)]),
+    "SubstrWithStart": ("core/test/codegen/function_test.cpp:2269-2305", [
+        (_ABC, 1, None, False, False, _ABC), (_ABC, 0, None, False, True, _ABC),
+        (_ABC, 9, None, False, False, "123 $%^"), (_ABC, -3, None, False, False, "$%^"),
+        (_ABC, 0, None, False, False, "")]),
+    "SubstrWithZh": ("core/test/codegen/function_test.cpp:2307-2358", [
+        (_ZH, 1, None, False, False, _ZH), (_ZH, 0, None, False, True, _ZH),
+        (_ZH, 9, None, False, False, " hello! 回复哦黑色的and magic粉色的圣诞袜"), (_ZH, -3, None, False, False, "圣诞袜"),
+        (_ZH, 0, None, False, False, ""), (_ZH, 37, None, False, False, "袜"), (_ZH, -38, None, False, False, "")]),
+    "SubstrWithZhForSpark": ("core/test/codegen/function_test.cpp:2360-2414", [
+        (_ZH9, -15, None, True, False, _ZH9), (_ZH9, 0, None, True, True, _ZH9), (_ZH9, -15, 5, True, False, ""),
+        (_ZH9, -15, 6, True, False, "时"), (_ZH9, -15, 14, True, False, "时欧基乌斯侧后解 "),
+        (_ZH9, -15, 20, True, False, _ZH9), ("apple", -7, 3, True, False, "a"),
+        ("apple", -7, None, True, False, "apple")]),
+    "SubstrCharWithStart": ("core/test/codegen/function_test.cpp:2416-2452", [
+        (_ABC, 1, None, False, False, _ABC), (_ABC, 0, None, False, True, _ABC),
+        (_ABC, 9, None, False, False, "123 $%^"), (_ABC, -3, None, False, False, "$%^"),
+        (_ABC, 0, None, False, False, "")]),
+    "SubstrCharWithStartZh": ("core/test/codegen/function_test.cpp:2454-2506", [
+        (_ZH, 1, None, False, False, _ZH), (_ZH, 0, None, False, True, _ZH),
+        (_ZH, 9, None, False, False, " hello! 回复哦黑色的and magic粉色的圣诞袜"), (_ZH, -3, None, False, False, "圣诞袜"),
+        (_ZH, 0, None, False, False, ""), (_ZH, 37, None, False, False, "袜"), (_ZH, -38, None, False, False, ""),
+        (_ZH, -37, None, False, False, _ZH)]),
+}
+
+
 def main():
     (HERE / "agg_kats.json").write_text(json.dumps({"single": AGG, "multi": AGG_MULTI,
                                                     "array_map": _array_map_cases()}, indent=1) + "\n")
@@ -280,6 +334,10 @@ def main():
     typed["full_join_one_build_op"] = dict(typed["full_join_one_build_op"],
                                            expected_rows=_join_one_build_op()["expected_rows"])
     (HERE / "join_type_kats.json").write_text(json.dumps(typed, indent=1) + "\n")
+    substr = {name: dict(source=src, cases=[dict(string=c[0], start=c[1], length=c[2], negative=c[3], zero=c[4],
+                                                 expected=c[5]) for c in cases])
+              for name, (src, cases) in SUBSTR.items()}
+    (HERE / "substr_kats.json").write_text(json.dumps(substr, indent=1, ensure_ascii=False) + "\n")
 
 
 if __name__ == "__main__":

@@ -120,7 +120,7 @@ def test_factory_validation_matches_reference_rules():
                        omg.Literal(5, L))
     omg.LookupJoinOperatorFactory([L, L], [0], [0], [1], [L], bf, filter_expr=arith).close()
     for bad in (omg.Binary(omg.EXPR_ADD, omg.Field(0, L), omg.Field(2, L)),  # arithmetic with a BOOLEAN result
-                omg.Binary(omg.EXPR_EQ, omg.Field(0, omg.VarcharType(4)), omg.Field(2, L))):
+                omg.Binary(omg.EXPR_EQ, omg.Field(0, omg.VarcharType(4)), omg.Field(2, L))):  # string = long
         with pytest.raises(omg.OmgError) as e:
             omg.LookupJoinOperatorFactory([omg.VarcharType(4), L], [0], [0], [1], [L], bf, filter_expr=bad)
         assert e.value.status == -2
@@ -131,6 +131,34 @@ def test_factory_validation_matches_reference_rules():
     with pytest.raises(TypeError):
         omg.LookupJoinOperatorFactory([L], [0], [0], [1], [L], bf, filter_expr=object())
     bf.close()
+    # strings: VARCHAR columns, literals and substr results compare with one another; substr takes a
+    # string and INT / LONG positions; other functions, mixed comparisons and a string-valued
+    # filter are refused
+    V, I = omg.VarcharType(8), omg.IntType()
+    sf = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, V], [0])
+    sub = omg.Func("substr", [omg.Field(1, V), omg.Literal(1, I), omg.Literal(3, L)], V)
+    for good in (omg.Binary(omg.EXPR_NEQ, sub, omg.Field(3, V)),
+                 omg.Binary(omg.EXPR_LT, omg.Field(1, V), omg.Literal("abc", V)),
+                 omg.IsNull(omg.Func("substr", [omg.Field(3, V), omg.Field(0, L)], V))):
+        omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=good).close()
+    for bad in (omg.Func("upper", [omg.Field(1, V)], V),
+                omg.Binary(omg.EXPR_EQ, sub, omg.Field(0, L)),
+                omg.Binary(omg.EXPR_AND, omg.Field(1, V), omg.Literal(1, omg.BooleanType())),
+                omg.Binary(omg.EXPR_EQ, omg.Func("substr", [omg.Field(0, L), omg.Literal(1, I)], V),
+                           omg.Field(3, V)),
+                omg.Binary(omg.EXPR_EQ, omg.Func("substr", [omg.Field(1, V), omg.Literal(1.5, omg.DoubleType())],
+                                                 V), omg.Field(3, V)),
+                sub):
+        with pytest.raises(omg.OmgError) as e:
+            omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=bad)
+        assert e.value.status == -2
+    sf.close()
+    assert omg.get_substr_rules() == (1, 1)
+    omg.set_substr_rules(0, 0)
+    assert omg.get_substr_rules() == (0, 0)
+    omg.set_substr_rules(1, 1)
+    with pytest.raises(omg.OmgError):
+        omg.set_substr_rules(2, 1)
 
 
 def test_operator_state_machine_without_gpu():

@@ -243,3 +243,22 @@ def test_oracle_array_map_kats(name):
     got = array_map_rows(keys[0], knulls[0], vals, vnulls, len(funcs))
     want = sorted(k["expected"], key=lambda r: (r[0] is None, r[0] if r[0] is not None else 0))
     assert got == want
+
+
+SUBSTR = json.loads((Path(__file__).parent / "golden" / "substr_kats.json").read_text(encoding="utf-8"))
+
+
+@pytest.mark.parametrize("name", sorted(SUBSTR))
+def test_oracle_substr_kats(name):
+    """oracle.substr against the reference's substr function tests (UTF-8 code points, the four
+    start-index policies)."""
+    for c in SUBSTR[name]["cases"]:
+        got = oracle.substr(c["string"].encode(), c["start"], c["length"], c["negative"], c["zero"])
+        assert got == c["expected"].encode(), c
+
+
+def test_oracle_str_compare_is_unsigned_bytes_then_length():
+    assert oracle.str_compare(b"abc", b"abd") == -1
+    assert oracle.str_compare(b"ab", b"abc") == -1
+    assert oracle.str_compare(b"\xc3\xa9", b"z") == 1  # bytes above 0x7f compare as unsigned
+    assert oracle.str_compare(b"", b"") == 0
