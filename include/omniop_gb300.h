@@ -268,9 +268,10 @@ int32_t omg_lookupjoin_factory_create(const OmgDataType *probe_types, int32_t n_
  * reference's math-function semantics: integers wrap at the node's INT or LONG width, DIV/MOD by
  * zero and TRY_* overflow give NULL) over integer-like and DOUBLE columns and literals, and
  * comparisons of VARCHAR/CHAR columns, literals and substr results (byte-wise unsigned, a
- * proper prefix first: codegen/functions/stringfunctions.cpp StrCompare); other trees (other
- * functions, IN, CASE) are refused by the factory with OMG_ERR_UNSUPPORTED, as the reference
- * refuses what its code generator cannot compile. */
+ * proper prefix first: codegen/functions/stringfunctions.cpp StrCompare), IF, CASE, COALESCE,
+ * IN and BETWEEN; other trees (other functions, a filter that does not return BOOLEAN) are
+ * refused by the factory with OMG_ERR_UNSUPPORTED, as the reference refuses what its code
+ * generator cannot compile. */
 int32_t omg_expr_field(int32_t col, const OmgDataType *type, void **out_expr);
 int32_t omg_expr_literal_long(int64_t value, const OmgDataType *type, int32_t is_null, void **out_expr);
 int32_t omg_expr_literal_double(double value, int32_t is_null, void **out_expr);
@@ -288,6 +289,17 @@ int32_t omg_expr_binary(int32_t op, void *left, void *right, void **out_expr);
  * for arithmetic nodes (ADD .. TRY_DIV: the result is INT, LONG or DOUBLE). */
 int32_t omg_expr_binary_typed(int32_t op, void *left, void *right, const OmgDataType *type, void **out_expr);
 int32_t omg_expr_unary(int32_t op, void *child, void **out_expr);
+/* IfExpr(cond, texp, fexp), SwitchExpr(whens, fexp) (n_whens pairs conds[i] -> results[i]),
+ * CoalesceExpr(val1, val2), InExpr(args: the value, then the list), BetweenExpr(val, low, up)
+ * (expressions.h:166-230); each takes ownership of its children.  Semantics as the reference's
+ * row code generator (codegen/expression_codegen.cpp:352-760): IF / CASE take a branch only on
+ * TRUE; IN is TRUE on a match, else NULL when the value or an item is NULL; BETWEEN is NULL when
+ * any operand is NULL.  IN and BETWEEN take INT, LONG, DATE32, TIMESTAMP, DOUBLE, VARCHAR, CHAR. */
+int32_t omg_expr_if(void *cond, void *then_expr, void *else_expr, void **out_expr);
+int32_t omg_expr_switch(void *const *conds, void *const *results, int32_t n_whens, void *else_expr, void **out_expr);
+int32_t omg_expr_coalesce(void *value1, void *value2, void **out_expr);
+int32_t omg_expr_in(void *const *args, int32_t n_args, void **out_expr);
+int32_t omg_expr_between(void *value, void *lower, void *upper, void **out_expr);
 int32_t omg_expr_is_null(void *child, void **out_expr);
 int32_t omg_expr_free(void *expr);
 

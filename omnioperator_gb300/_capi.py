@@ -76,6 +76,11 @@ _SIGS = {
     "omg_expr_binary_typed": (I32, [I32, P, P, P, C.POINTER(P)]),
     "omg_expr_unary": (I32, [I32, P, C.POINTER(P)]),
     "omg_expr_is_null": (I32, [P, C.POINTER(P)]),
+    "omg_expr_if": (I32, [P, P, P, C.POINTER(P)]),
+    "omg_expr_switch": (I32, [C.POINTER(P), C.POINTER(P), I32, P, C.POINTER(P)]),
+    "omg_expr_coalesce": (I32, [P, P, C.POINTER(P)]),
+    "omg_expr_in": (I32, [C.POINTER(P), I32, C.POINTER(P)]),
+    "omg_expr_between": (I32, [P, P, P, C.POINTER(P)]),
     "omg_expr_free": (I32, [P]),
     "omg_lookupjoin_factory_create": (I32, [P, I32, P, I32, P, I32, P, I32, P, I64, P, I32, C.POINTER(P)]),
     "omg_hashbuilder_factory_create_side": (I32, [I32, I32, P, I32, P, I32, I32, C.POINTER(P)]),

@@ -571,6 +571,37 @@ class Func:
         self.name, self.args, self.dtype = name, list(args), dtype
 
 
+class If:
+    """IfExpr(cond, then, else): `then` when cond is TRUE, else `else_`."""
+
+    def __init__(self, cond, then, else_):
+        self.cond, self.then, self.else_ = cond, then, else_
+
+
+class Switch:
+    """SwitchExpr: CASE WHEN whens[0][0] THEN whens[0][1] ... ELSE else_ END."""
+
+    def __init__(self, whens: list, else_):
+        self.whens, self.else_ = [tuple(w) for w in whens], else_
+
+
+class Coalesce:
+    def __init__(self, value1, value2):
+        self.value1, self.value2 = value1, value2
+
+
+class In:
+    """InExpr: value IN (items...)."""
+
+    def __init__(self, value, items: list):
+        self.value, self.items = value, list(items)
+
+
+class Between:
+    def __init__(self, value, lower, upper):
+        self.value, self.lower, self.upper = value, lower, upper
+
+
 class Not:
     def __init__(self, child):
         self.child = child
@@ -591,19 +622,45 @@ def _expr_handle(e) -> int:
     elif isinstance(e, Literal) and e.dtype.id in (OMNI_VARCHAR, OMNI_CHAR):
         raw = b"" if e.is_null else (e.value.encode() if isinstance(e.value, str) else bytes(e.value))
         check(L.omg_expr_literal_string(raw, len(raw), _types([e.dtype]), 1 if e.is_null else 0, C.byref(out)))
-    elif isinstance(e, Func):
-        args = []
+    elif isinstance(e, (Func, If, Switch, Coalesce, In, Between)):
+        if isinstance(e, Func):
+            kids = e.args
+        elif isinstance(e, If):
+            kids = [e.cond, e.then, e.else_]
+        elif isinstance(e, Switch):
+            kids = [x for w in e.whens for x in w] + [e.else_]
+        elif isinstance(e, Coalesce):
+            kids = [e.value1, e.value2]
+        elif isinstance(e, In):
+            kids = [e.value] + e.items
+        else:
+            kids = [e.value, e.lower, e.upper]
+        hs = []
         try:
-            for a in e.args:
-                args.append(_expr_handle(a))
+            for a in kids:
+                hs.append(_expr_handle(a))
         except Exception:
-            for h in args:
+            for h in hs:
                 L.omg_expr_free(h)
             raise
-        arr = (C.c_void_p * max(len(args), 1))(*args)
-        rc = L.omg_expr_func(e.name.encode(), arr, len(args), _types([e.dtype]), C.byref(out))
+
+        def arr(xs):
+            return (C.c_void_p * max(len(xs), 1))(*xs)
+
+        if isinstance(e, Func):
+            rc = L.omg_expr_func(e.name.encode(), arr(hs), len(hs), _types([e.dtype]), C.byref(out))
+        elif isinstance(e, If):
+            rc = L.omg_expr_if(hs[0], hs[1], hs[2], C.byref(out))
+        elif isinstance(e, Switch):
+            rc = L.omg_expr_switch(arr(hs[0:-1:2]), arr(hs[1:-1:2]), len(e.whens), hs[-1], C.byref(out))
+        elif isinstance(e, Coalesce):
+            rc = L.omg_expr_coalesce(hs[0], hs[1], C.byref(out))
+        elif isinstance(e, In):
+            rc = L.omg_expr_in(arr(hs), len(hs), C.byref(out))
+        else:
+            rc = L.omg_expr_between(hs[0], hs[1], hs[2], C.byref(out))
         if rc != 0:
-            for h in args:
+            for h in hs:
                 L.omg_expr_free(h)
         check(rc)
     elif isinstance(e, Literal):

@@ -531,6 +531,61 @@ int32_t omg_expr_unary(int32_t op, void *child, void **out_expr)
     });
 }
 
+int32_t omg_expr_if(void *cond, void *then_expr, void *else_expr, void **out_expr)
+{
+    return Guard([&] {
+        Require(cond != nullptr && then_expr != nullptr && else_expr != nullptr && out_expr != nullptr,
+            "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(new ex::IfExpr(static_cast<ex::Expr *>(cond),
+            static_cast<ex::Expr *>(then_expr), static_cast<ex::Expr *>(else_expr)));
+    });
+}
+
+int32_t omg_expr_switch(void *const *conds, void *const *results, int32_t n_whens, void *else_expr, void **out_expr)
+{
+    return Guard([&] {
+        Require(conds != nullptr && results != nullptr && n_whens > 0 && else_expr != nullptr && out_expr != nullptr,
+            "invalid arguments");
+        std::vector<std::pair<ex::Expr *, ex::Expr *>> whens;
+        for (int32_t i = 0; i < n_whens; ++i) {
+            Require(conds[i] != nullptr && results[i] != nullptr, "null CASE clause");
+            whens.emplace_back(static_cast<ex::Expr *>(conds[i]), static_cast<ex::Expr *>(results[i]));
+        }
+        *out_expr = static_cast<ex::Expr *>(new ex::SwitchExpr(std::move(whens), static_cast<ex::Expr *>(else_expr)));
+    });
+}
+
+int32_t omg_expr_coalesce(void *value1, void *value2, void **out_expr)
+{
+    return Guard([&] {
+        Require(value1 != nullptr && value2 != nullptr && out_expr != nullptr, "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(
+            new ex::CoalesceExpr(static_cast<ex::Expr *>(value1), static_cast<ex::Expr *>(value2)));
+    });
+}
+
+int32_t omg_expr_in(void *const *args, int32_t n_args, void **out_expr)
+{
+    return Guard([&] {
+        Require(args != nullptr && n_args >= 2 && out_expr != nullptr, "invalid arguments");
+        std::vector<ex::Expr *> a(static_cast<size_t>(n_args));
+        for (int32_t i = 0; i < n_args; ++i) {
+            Require(args[i] != nullptr, "null IN argument");
+            a[i] = static_cast<ex::Expr *>(args[i]);
+        }
+        *out_expr = static_cast<ex::Expr *>(new ex::InExpr(std::move(a)));
+    });
+}
+
+int32_t omg_expr_between(void *value, void *lower, void *upper, void **out_expr)
+{
+    return Guard([&] {
+        Require(value != nullptr && lower != nullptr && upper != nullptr && out_expr != nullptr, "invalid arguments");
+        *out_expr = static_cast<ex::Expr *>(new ex::BetweenExpr(static_cast<ex::Expr *>(value),
+            static_cast<ex::Expr *>(lower), static_cast<ex::Expr *>(upper)));
+    });
+}
+
 int32_t omg_expr_is_null(void *child, void **out_expr)
 {
     return Guard([&] {

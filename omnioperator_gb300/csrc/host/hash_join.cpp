@@ -773,6 +773,99 @@ int CompileFilter(const Expr *e, FilterCode &fc, int depth)
             emit(omg::FOP_SUBSTR);
             return kFilterString;
         }
+        case ExprType::IF_E: {
+            const auto *x = static_cast<const omniruntime::expressions::IfExpr *>(e);
+            if (CompileFilter(x->condition, fc, depth) == kFilterString) {
+                FilterUnsupported("IF on a string condition");
+            }
+            const int tk = CompileFilter(x->trueExpr, fc, depth + 1);
+            if (CompileFilter(x->falseExpr, fc, depth + 2) != tk) {
+                FilterUnsupported("IF branches of different kinds");
+            }
+            emit(omg::FOP_IF);
+            return tk;
+        }
+        case ExprType::SWITCH_E: {
+            // CASE WHEN c1 THEN r1 ... ELSE e END as IF(c1, r1, IF(c2, r2, ... e)): the clauses'
+            // conditions and results, the ELSE value, then one IF per clause.
+            const auto *x = static_cast<const omniruntime::expressions::SwitchExpr *>(e);
+            if (x->whenClause.empty()) {
+                FilterUnsupported("CASE without WHEN");
+            }
+            int d = depth;
+            int kind = -2;
+            for (const auto &w : x->whenClause) {
+                if (CompileFilter(w.first, fc, d++) == kFilterString) {
+                    FilterUnsupported("CASE on a string condition");
+                }
+                const int rk = CompileFilter(w.second, fc, d++);
+                if (kind != -2 && rk != kind) {
+                    FilterUnsupported("CASE results of different kinds");
+                }
+                kind = rk;
+            }
+            if (CompileFilter(x->falseExpr, fc, d) != kind) {
+                FilterUnsupported("CASE results of different kinds");
+            }
+            for (size_t i = 0; i < x->whenClause.size(); ++i) {
+                emit(omg::FOP_IF);
+            }
+            return kind;
+        }
+        case ExprType::COALESCE_E: {
+            const auto *x = static_cast<const omniruntime::expressions::CoalesceExpr *>(e);
+            const int k = CompileFilter(x->value1, fc, depth);
+            if (CompileFilter(x->value2, fc, depth + 1) != k) {
+                FilterUnsupported("COALESCE of different kinds");
+            }
+            emit(omg::FOP_COALESCE);
+            return k;
+        }
+        case ExprType::BETWEEN_E:
+        case ExprType::IN_E: {
+            // The value's type must be one the reference's IN / BETWEEN code handles
+            // (expression_codegen.cpp:599-640, :2119-2160), and every operand of its kind.
+            const bool between = e->GetType() == ExprType::BETWEEN_E;
+            std::vector<const Expr *> args;
+            if (between) {
+                const auto *x = static_cast<const omniruntime::expressions::BetweenExpr *>(e);
+                args = {x->value, x->lowerBound, x->upperBound};
+            } else {
+                const auto *x = static_cast<const omniruntime::expressions::InExpr *>(e);
+                args.assign(x->arguments.begin(), x->arguments.end());
+                if (args.size() < 2) {
+                    FilterUnsupported("IN without a list");
+                }
+            }
+            const DataTypePtr vt = args[0] == nullptr ? nullptr : args[0]->GetReturnType();
+            const int32_t id = vt ? vt->GetId() : -1;
+            if (id != OMNI_INT && id != OMNI_LONG && id != OMNI_DATE32 && id != OMNI_TIMESTAMP && id != OMNI_DOUBLE &&
+                id != OMNI_VARCHAR && id != OMNI_CHAR) {
+                FilterUnsupported(std::string(between ? "BETWEEN" : "IN") + " of type " + std::to_string(id));
+            }
+            if (!between) {
+                in.op = omg::FOP_IN_BEGIN;
+                push(-1);
+            }
+            const int base = between ? depth : depth + 1;
+            const int k = CompileFilter(args[0], fc, base);
+            auto isString = [](int32_t t) { return t == OMNI_VARCHAR || t == OMNI_CHAR; };
+            for (size_t a = 1; a < args.size(); ++a) {
+                // ExprVerifier::AreInvalidDataTypes (expr_verifier.cpp:25-29): the same type, or both
+                // strings.
+                const DataTypePtr at = args[a] == nullptr ? nullptr : args[a]->GetReturnType();
+                const int32_t aid = at ? at->GetId() : -1;
+                if (CompileFilter(args[a], fc, between ? base + static_cast<int>(a) : base + 1) != k ||
+                    (aid != id && !(isString(aid) && isString(id)))) {
+                    FilterUnsupported(std::string(between ? "BETWEEN" : "IN") + " operands of different types");
+                }
+                if (!between) {
+                    emit(omg::FOP_IN_STEP);
+                }
+            }
+            emit(between ? omg::FOP_BETWEEN : omg::FOP_IN_END);
+            return kFilterInt;
+        }
         default:
             FilterUnsupported("expression kind " + std::to_string(static_cast<int>(e->GetType())));
     }
@@ -795,10 +888,13 @@ LookupJoinOperatorFactory *LookupJoinOperatorFactory::CreateLookupJoinOperatorFa
         buildOutputTypes, builder));
     if (filterExpr != nullptr) {
         // JoinFilterCodeGen (lookup_join.cpp:175-187): compiled once per factory.
-        FilterCode fc{probeTypes, f->build->buildTypes, f->filter, f->filterCols, f->filterText};
-        if (CompileFilter(static_cast<const Expr *>(filterExpr), fc, 0) == kFilterString) {
-            FilterUnsupported("a string-valued filter");
+        // The filter returns BOOLEAN (SimpleFilter::Initialize, filter_and_project.cpp:51-54).
+        const auto *root = static_cast<const Expr *>(filterExpr);
+        if (root->GetReturnType() == nullptr || root->GetReturnType()->GetId() != OMNI_BOOLEAN) {
+            FilterUnsupported("a filter that does not return BOOLEAN");
         }
+        FilterCode fc{probeTypes, f->build->buildTypes, f->filter, f->filterCols, f->filterText};
+        CompileFilter(root, fc, 0);
         if (f->filter.empty()) {
             FilterUnsupported("empty filter");
         }

@@ -984,9 +984,97 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
             sp = base + 1;
             continue;
         }
-        if (op == FOP_PROBE_COL || op == FOP_BUILD_COL || op == FOP_LITERAL) {
+        if (op == FOP_IF || op == FOP_BETWEEN) {
+            if (sp < 3) {
+                return false;
+            }
+            const int c = sp - 3;
+            if (op == FOP_IF) {
+                const int pick = ((fl[c] & kFNull) == 0 && v[c] != 0) ? c + 1 : c + 2;
+                v[c] = v[pick];
+                sl[c] = sl[pick];
+                fl[c] = fl[pick];
+            } else {
+                const uint32_t all = fl[c] | fl[c + 1] | fl[c + 2];
+                bool in = false;
+                if ((all & kFNull) == 0) {
+                    if (fl[c] & kFString) {
+                        const auto *x = reinterpret_cast<const uint8_t *>(v[c]);
+                        in = StrCompare(reinterpret_cast<const uint8_t *>(v[c + 1]), sl[c + 1], x, sl[c]) <= 0 &&
+                            StrCompare(x, sl[c], reinterpret_cast<const uint8_t *>(v[c + 2]), sl[c + 2]) <= 0;
+                    } else if (all & kFDouble) {
+                        const double x = FilterAsDouble(v[c], fl[c]);
+                        in = !(FilterAsDouble(v[c + 1], fl[c + 1]) > x) && !(x > FilterAsDouble(v[c + 2], fl[c + 2]));
+                    } else {
+                        const int64_t x = static_cast<int64_t>(v[c]);
+                        in = static_cast<int64_t>(v[c + 1]) <= x && x <= static_cast<int64_t>(v[c + 2]);
+                    }
+                }
+                v[c] = in ? 1ull : 0ull;
+                sl[c] = 0;
+                fl[c] = (all & kFNull) ? kFNull : 0u;
+            }
+            sp = c + 1;
+            continue;
+        }
+        if (op == FOP_COALESCE) {
+            if (sp < 2) {
+                return false;
+            }
+            if (fl[sp - 2] & kFNull) {
+                v[sp - 2] = v[sp - 1];
+                sl[sp - 2] = sl[sp - 1];
+                fl[sp - 2] = fl[sp - 1];
+            }
+            --sp;
+            continue;
+        }
+        if (op == FOP_IN_STEP) {
+            if (sp < 3) {
+                return false;
+            }
+            const int t = sp - 1;
+            const int x = sp - 2;
+            if (fl[t] & kFNull) {
+                v[sp - 3] |= 2ull;
+            } else if ((fl[x] & kFNull) == 0) {
+                bool eq;
+                if (fl[x] & kFString) {
+                    eq = sl[x] == sl[t] &&
+                        StrCompare(reinterpret_cast<const uint8_t *>(v[x]), sl[x],
+                            reinterpret_cast<const uint8_t *>(v[t]), sl[t]) == 0;
+                } else if ((fl[x] | fl[t]) & kFDouble) {
+                    eq = FilterAsDouble(v[x], fl[x]) == FilterAsDouble(v[t], fl[t]);
+                } else {
+                    eq = v[x] == v[t];
+                }
+                v[sp - 3] |= eq ? 1ull : 0ull;
+            }
+            --sp;
+            continue;
+        }
+        if (op == FOP_IN_END) {
+            if (sp < 2) {
+                return false;
+            }
+            const uint64_t acc = v[sp - 2];
+            const bool isNull = (acc & 1ull) == 0 && ((acc & 2ull) != 0 || (fl[sp - 1] & kFNull) != 0);
+            v[sp - 2] = (acc & 1ull) ? 1ull : 0ull;
+            sl[sp - 2] = 0;
+            fl[sp - 2] = isNull ? kFNull : 0u;
+            --sp;
+            continue;
+        }
+        if (op == FOP_PROBE_COL || op == FOP_BUILD_COL || op == FOP_LITERAL || op == FOP_IN_BEGIN) {
             if (sp >= kMaxFilterDepth) {
                 return false;  // the host limits the depth; never taken
+            }
+            if (op == FOP_IN_BEGIN) {
+                v[sp] = 0;
+                sl[sp] = 0;
+                fl[sp] = 0;
+                ++sp;
+                continue;
             }
             uint64_t bits = static_cast<uint64_t>(f.imm);
             bool isNull = f.isNull != 0;
@@ -1003,6 +1091,7 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
                                        : static_cast<uint64_t>(LoadIntRO(col, r, f.width)));
             }
             v[sp] = bits;
+            sl[sp] = 0;
             fl[sp] = (isNull ? kFNull : 0u) | (f.dbl ? kFDouble : 0u);
             ++sp;
             continue;

@@ -438,10 +438,19 @@ enum FilterOp : int16_t {
     // (INTERCEPT_FROM_BEYOND), bit 1: start 0 means 1 (ZeroStartIndexSupportRule IS_SUPPORT).
     // A NULL argument gives NULL.
     FOP_SUBSTR,
+    // Conditionals and sets (codegen/expression_codegen.cpp:352-760), over numbers or strings:
+    FOP_IF,        // (cond, then, else): then when cond is TRUE, else otherwise (NULL included)
+    FOP_COALESCE,  // (a, b): a unless it is NULL
+    FOP_BETWEEN,   // (v, lo, hi): NULL if any is NULL, else lo <= v <= hi (doubles: unordered counts
+                   // as <=, the reference's ULE)
+    FOP_IN_BEGIN,  // push the IN accumulator (bit 0: a list item equalled the value, bit 1: an item
+                   // was NULL) before the value
+    FOP_IN_STEP,   // (acc, v, item) -> (acc, v): fold one list item in
+    FOP_IN_END,    // (acc, v): TRUE if matched, else NULL if v or an item was NULL, else FALSE
 };
 constexpr int kFilterSubstrNegative = 1;
 constexpr int kFilterSubstrZero = 2;
-constexpr int kMaxFilterInstrs = 24;
+constexpr int kMaxFilterInstrs = 32;
 constexpr int kMaxFilterDepth = 8;
 
 struct FilterInstr {

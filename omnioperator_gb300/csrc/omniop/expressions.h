@@ -7,13 +7,15 @@
 // filter tree into a postfix program that the probe kernel runs per candidate pair
 // (CompileJoinFilter in host/hash_join.cpp); comparisons, NOT, AND, OR, IS [NOT] NULL and
 // arithmetic over fixed-width integer-like and double columns and literals, VARCHAR/CHAR columns
-// and literals, and the substr function (a FuncExpr) are supported, anything else is refused
+// and literals, the substr function (a FuncExpr), IF, CASE (SwitchExpr), IN, BETWEEN and
+// COALESCE are supported, anything else is refused
 // with EXPRESSION_NOT_SUPPORT as the reference refuses expressions its code generator cannot
 // handle (lookup_join.cpp:175-187).
 #pragma once
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "types.h"
@@ -110,6 +112,91 @@ public:
     ExprType GetType() const override { return ExprType::FUNC_E; }
     std::string funcName;
     std::vector<Expr *> arguments;
+};
+
+// Conditional and set nodes (expressions.h:166-230), owning their children; their return
+// types follow the reference's constructors (expressions.cpp:211-276).
+class InExpr : public Expr {
+public:
+    explicit InExpr(std::vector<Expr *> args) : Expr(type::BooleanType()), arguments(std::move(args)) {}
+    ~InExpr() override { DeleteExprs(arguments); }
+    InExpr(const InExpr &) = delete;
+    InExpr &operator=(const InExpr &) = delete;
+    ExprType GetType() const override { return ExprType::IN_E; }
+    std::vector<Expr *> arguments;  // the value, then the list
+};
+
+class BetweenExpr : public Expr {
+public:
+    BetweenExpr(Expr *val, Expr *lowBound, Expr *upBound)
+        : Expr(type::BooleanType()), value(val), lowerBound(lowBound), upperBound(upBound)
+    {}
+    ~BetweenExpr() override
+    {
+        delete value;
+        delete lowerBound;
+        delete upperBound;
+    }
+    BetweenExpr(const BetweenExpr &) = delete;
+    BetweenExpr &operator=(const BetweenExpr &) = delete;
+    ExprType GetType() const override { return ExprType::BETWEEN_E; }
+    Expr *value;
+    Expr *lowerBound;
+    Expr *upperBound;
+};
+
+class IfExpr : public Expr {
+public:
+    IfExpr(Expr *cond, Expr *texp, Expr *fexp)
+        : Expr(texp->GetReturnType()), condition(cond), trueExpr(texp), falseExpr(fexp)
+    {}
+    ~IfExpr() override
+    {
+        delete condition;
+        delete trueExpr;
+        delete falseExpr;
+    }
+    IfExpr(const IfExpr &) = delete;
+    IfExpr &operator=(const IfExpr &) = delete;
+    ExprType GetType() const override { return ExprType::IF_E; }
+    Expr *condition;
+    Expr *trueExpr;
+    Expr *falseExpr;
+};
+
+class SwitchExpr : public Expr {
+public:
+    SwitchExpr(std::vector<std::pair<Expr *, Expr *>> whens, Expr *fexp)
+        : Expr(fexp->GetReturnType()), whenClause(std::move(whens)), falseExpr(fexp)
+    {}
+    ~SwitchExpr() override
+    {
+        for (auto &w : whenClause) {
+            delete w.first;
+            delete w.second;
+        }
+        delete falseExpr;
+    }
+    SwitchExpr(const SwitchExpr &) = delete;
+    SwitchExpr &operator=(const SwitchExpr &) = delete;
+    ExprType GetType() const override { return ExprType::SWITCH_E; }
+    std::vector<std::pair<Expr *, Expr *>> whenClause;
+    Expr *falseExpr;
+};
+
+class CoalesceExpr : public Expr {
+public:
+    CoalesceExpr(Expr *val1, Expr *val2) : Expr(val1->GetReturnType()), value1(val1), value2(val2) {}
+    ~CoalesceExpr() override
+    {
+        delete value1;
+        delete value2;
+    }
+    CoalesceExpr(const CoalesceExpr &) = delete;
+    CoalesceExpr &operator=(const CoalesceExpr &) = delete;
+    ExprType GetType() const override { return ExprType::COALESCE_E; }
+    Expr *value1;
+    Expr *value2;
 };
 
 class IsNullExpr : public Expr {

@@ -152,6 +152,24 @@ def test_factory_validation_matches_reference_rules():
         with pytest.raises(omg.OmgError) as e:
             omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=bad)
         assert e.value.status == -2
+    # conditionals and sets: operands of one type (strings interchangeable), IN / BETWEEN over the
+    # types the reference's code generator handles, a BOOLEAN root
+    S = omg.ShortType()
+    for good in (omg.In(omg.Field(0, L), [omg.Literal(1, L), omg.Field(2, L)]),
+                 omg.Between(omg.Field(1, V), omg.Literal("a", omg.VarcharType(2)), omg.Field(3, V)),
+                 omg.If(omg.IsNull(omg.Field(1, V)), omg.Literal(1, omg.BooleanType()),
+                        omg.Binary(omg.EXPR_EQ, omg.Coalesce(omg.Field(1, V), omg.Literal("x", V)), omg.Field(3, V))),
+                 omg.Switch([(omg.IsNull(omg.Field(1, V)), omg.Literal(0, omg.BooleanType()))],
+                            omg.Literal(1, omg.BooleanType()))):
+        omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=good).close()
+    for bad in (omg.In(omg.Field(0, L), [omg.Literal(1, I)]),  # LONG IN (INT)
+                omg.In(omg.Literal(1, S), [omg.Literal(1, S)]),  # SHORT: not an IN type
+                omg.Between(omg.Field(0, L), omg.Literal(1, L), omg.Literal(2.0, omg.DoubleType())),
+                omg.If(omg.IsNull(omg.Field(1, V)), omg.Field(1, V), omg.Literal(1, omg.BooleanType())),
+                omg.Binary(omg.EXPR_ADD, omg.Field(0, L), omg.Field(2, L), L)):  # not BOOLEAN
+        with pytest.raises(omg.OmgError) as e:
+            omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=bad)
+        assert e.value.status == -2
     sf.close()
     assert omg.get_substr_rules() == (1, 1)
     omg.set_substr_rules(0, 0)

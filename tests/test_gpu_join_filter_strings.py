@@ -1,6 +1,7 @@
-"""Join filters over strings on the GPU: VARCHAR/CHAR columns and literals of both sides compared
-byte-wise (unsigned, a proper prefix first), and substr over UTF-8 code points under the four
-start-index policies (lookup_join.cpp:175-187,1440-1466; codegen/functions/stringfunctions.h:
+"""Join filters over strings and conditionals on the GPU: VARCHAR/CHAR columns and literals of both
+sides compared byte-wise (unsigned, a proper prefix first), substr over UTF-8 code points under
+the four start-index policies, and IF / CASE / COALESCE / IN / BETWEEN with the reference's NULL
+rules (codegen/expression_codegen.cpp:352-760) (lookup_join.cpp:175-187,1440-1466; codegen/functions/stringfunctions.h:
 215-318).  Known answers: the reference's CHAR-filter join tests (join_test.cpp:1796-2150) with
 their expected rows, and its substr function tests (function_test.cpp:2030-2506, the vectors in
 tests/golden/substr_kats.json) evaluated by the probe kernel.  Random joins of every kind equal
@@ -174,6 +175,32 @@ def _eval(e, pcols, pmasks, bcols, bmasks, i, j, nprobe):
             return None
         neg, zero = omg.get_substr_rules()
         return oracle.substr(a[0], a[1], a[2] if len(a) == 3 else None, bool(neg), bool(zero))
+    if isinstance(e, omg.If):
+        c = _eval(e.cond, pcols, pmasks, bcols, bmasks, i, j, nprobe)
+        return _eval(e.then if c not in (None, 0) else e.else_, pcols, pmasks, bcols, bmasks, i, j, nprobe)
+    if isinstance(e, omg.Switch):
+        for cond, res in e.whens:
+            if _eval(cond, pcols, pmasks, bcols, bmasks, i, j, nprobe) not in (None, 0):
+                return _eval(res, pcols, pmasks, bcols, bmasks, i, j, nprobe)
+        return _eval(e.else_, pcols, pmasks, bcols, bmasks, i, j, nprobe)
+    if isinstance(e, omg.Coalesce):
+        a = _eval(e.value1, pcols, pmasks, bcols, bmasks, i, j, nprobe)
+        return a if a is not None else _eval(e.value2, pcols, pmasks, bcols, bmasks, i, j, nprobe)
+    if isinstance(e, omg.In):
+        # expression_codegen.cpp:545-659: TRUE on a match, else NULL if the value or an item is NULL
+        v = _eval(e.value, pcols, pmasks, bcols, bmasks, i, j, nprobe)
+        items = [_eval(x, pcols, pmasks, bcols, bmasks, i, j, nprobe) for x in e.items]
+        if v is not None and any(x is not None and x == v for x in items):
+            return 1
+        return None if v is None or any(x is None for x in items) else 0
+    if isinstance(e, omg.Between):
+        # expression_codegen.cpp:661-711: NULL if any operand is NULL; doubles compare unordered as <=
+        v, lo, hi = (_eval(x, pcols, pmasks, bcols, bmasks, i, j, nprobe) for x in (e.value, e.lower, e.upper))
+        if v is None or lo is None or hi is None:
+            return None
+        if isinstance(v, bytes):
+            return int(oracle.str_compare(lo, v) <= 0 and oracle.str_compare(v, hi) <= 0)
+        return int(not (lo > v) and not (v > hi))
     if isinstance(e, omg.IsNull):
         return int(_eval(e.child, pcols, pmasks, bcols, bmasks, i, j, nprobe) is None)
     if isinstance(e, omg.Not):
@@ -196,7 +223,10 @@ def _eval(e, pcols, pmasks, bcols, bmasks, i, j, nprobe):
                 omg.EXPR_GT: c > 0, omg.EXPR_GTE: c >= 0}[e.op])
 
 
-# Probe (key, s, pos), build (key, t, payload): probe fields 0-2, build fields 3-5.
+D = omg.DoubleType()
+NULL_V = Lit(b"", V, is_null=True)
+
+# Probe (key, s, pos), build (key, t, payload, x): probe fields 0-2, build fields 3-6.
 FILTERS = {
     "substr_lt": B(omg.EXPR_LT, Fn("substr", [F(1, V), Lit(2, I), Lit(3, I)], V),
                    Fn("substr", [F(4, V), Lit(1, I), Lit(3, I)], V)),
@@ -206,6 +236,20 @@ FILTERS = {
                           Fn("substr", [F(4, V), Lit(1, I), Lit(2, I)], V)),
     "null_and_payload": B(omg.EXPR_AND, omg.Not(omg.IsNull(F(4, V))),
                           B(omg.EXPR_OR, B(omg.EXPR_NEQ, F(1, V), Lit(b"", V)), B(omg.EXPR_GT, F(5, L), Lit(0, L)))),
+    "in_strings_and_if": B(omg.EXPR_AND,
+                           omg.In(Fn("substr", [F(1, V), Lit(1, I), Lit(1, I)], V),
+                                  [Lit("a", V), Lit("中", V), Lit(b"", V), F(4, V)]),
+                           omg.If(B(omg.EXPR_GT, F(2, I), Lit(0, I)), B(omg.EXPR_GT, F(5, L), Lit(0, L)),
+                                  B(omg.EXPR_LTE, F(5, L), Lit(0, L)))),
+    "not_in_with_null_item": B(omg.EXPR_OR, omg.Not(omg.In(F(2, I), [Lit(1, I), Lit(2, I), Lit(0, I, is_null=True)])),
+                               omg.Not(omg.In(F(5, L), [Lit(1, L), Lit(-1, L)]))),
+    "between_case_coalesce": B(omg.EXPR_OR, omg.Between(F(6, D), Lit(-0.5, D), Lit(0.5, D)),
+                               omg.Switch([(omg.IsNull(F(4, V)), B(omg.EXPR_EQ, F(2, I), Lit(0, I))),
+                                           (B(omg.EXPR_GT, F(5, L), Lit(2, L)),
+                                            omg.Between(F(1, V), Lit("b", V), F(4, V)))],
+                                          B(omg.EXPR_EQ, omg.Coalesce(F(4, V), Lit("x", V)), Lit("x", V)))),
+    "not_between_if": omg.Not(omg.Between(F(5, L), Lit(-2, L),
+                                                  omg.If(omg.IsNull(F(6, D)), Lit(0, L), Lit(3, L)))),
 }
 
 
@@ -214,12 +258,13 @@ def _string_join_data(seed, unique, nb=3000, npr=20000):
     bkey = rng.permutation(nb).astype(np.int64) if unique else rng.integers(0, nb // 4, nb).astype(np.int64)
     bstr = _utf8_words(rng, nb, 300)
     bpay = rng.integers(-5, 5, nb).astype(np.int64)
+    bx = np.where(rng.random(nb) < 0.05, np.nan, rng.normal(0, 1, nb))
     pkey = rng.integers(0, nb + nb // 5, npr).astype(np.int64)
     pstr = _utf8_words(rng, npr, 300)
     ppos = rng.integers(-6, 7, npr).astype(np.int32)
-    bm = [rng.random(nb) < 0.03, rng.random(nb) < 0.1, np.zeros(nb, bool)]
+    bm = [rng.random(nb) < 0.03, rng.random(nb) < 0.1, np.zeros(nb, bool), rng.random(nb) < 0.05]
     pm = [rng.random(npr) < 0.03, rng.random(npr) < 0.1, rng.random(npr) < 0.05]
-    return [bkey, bstr, bpay], bm, [pkey, pstr, ppos], pm
+    return [bkey, bstr, bpay, bx], bm, [pkey, pstr, ppos], pm
 
 
 def _expected(kind, bcols, bm, pcols, pm, pout, bout, filt):
@@ -249,20 +294,20 @@ def test_string_filtered_join_kinds_match_oracle(join_type, build_side, fname, u
     pout = [0, 1, 2]
     bout = [] if kind in ("semi", "anti", "existence") else [1, 2]
     filt = FILTERS[fname]
-    got, _ = run(join_type, [L, V, L], bcols, bm, [L, V, I], pcols, pm, pout, bout, filt,
+    got, _ = run(join_type, [L, V, L, D], bcols, bm, [L, V, I], pcols, pm, pout, bout, filt,
                  batch_sizes=(1000, 4096, 777), build_side=build_side)
     want = _expected(kind, bcols, bm, pcols, pm, pout, bout, filt)
     assert len(want) > 0
     assert sorted(got, key=_key) == sorted(want, key=_key)
 
 
-@pytest.mark.parametrize("fname", ["substr_lt", "column_positions"])
+@pytest.mark.parametrize("fname", ["substr_lt", "column_positions", "between_case_coalesce"])
 def test_string_filter_on_the_bitmap_probe(fname):
     """A unique ARRAY build probed in one large batch with fixed-width outputs: the bitmap kernel
     runs the string filter on each probe row's one candidate."""
     bcols, bm, pcols, pm = _string_join_data(90 + len(fname), True, nb=1 << 14, npr=300_000)
     bm[0][:] = False
-    got, kernel = run("INNER", [L, V, L], bcols, bm, [L, V, I], pcols, pm, [0, 2], [2], FILTERS[fname],
+    got, kernel = run("INNER", [L, V, L, D], bcols, bm, [L, V, I], pcols, pm, [0, 2], [2], FILTERS[fname],
                       batch_sizes=(300_000,))
     assert kernel == 4  # the bitmap kernel
     want = _expected("inner", bcols, bm, pcols, pm, [0, 2], [2], FILTERS[fname])
