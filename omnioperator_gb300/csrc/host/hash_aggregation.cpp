@@ -556,10 +556,9 @@ OmniStatus HashAggregationOperatorFactory::Init()
                 o.src = 0;
                 break;
             case OMNI_AGGREGATION_TYPE_SUM: {
-                if ((!raw || partial) && !spark && inW == 8 && isInt) {
-                    throw OmniException("UNSUPPORTED_ERROR",
-                        "two-stage int64 SUM under the container-vector policy is not supported", -2);
-                }
+                // Under the container-vector policy a two-stage int64 SUM is the same sticky SUM at
+                // every stage: a partial emits the sum (NULL when it overflowed or had no values) and
+                // a merging stage sums those, skipping NULL rows (sum_aggregator.cpp:11-57,168-190).
                 if (isDouble) {
                     o.kind = omg::OUT_SUM_DOUBLE;
                     o.src = static_cast<int16_t>(accFor(omg::ACC_DSUM, input, inKind, inW, 0));

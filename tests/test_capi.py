@@ -71,12 +71,16 @@ def test_factory_validation_matches_reference_rules():
     with pytest.raises(omg.OmgError) as e:
         omg.HashAggregationOperatorFactory([0], [L], [[1]], [[d64]], [[d128]], [0], output_partials=[True])
     assert e.value.status == -1
-    # under the container-vector policy the partial int64 SUM is a container: not built
+    # under the container-vector policy a partial int64 SUM declared LONG is SumAggregator<LONG, LONG>
+    # (aggregator_factory.h:26-62 picks by the output type): a flat sticky-overflow sum; a SUM
+    # declared CONTAINER is refused
     omg.set_policy(omg.POLICY_GENERIC)
     try:
-        with pytest.raises(omg.OmgError) as e:
-            omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [0], output_partials=[True])
-        assert e.value.status == -2
+        omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [0], output_partials=[True]).close()
+        omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [0], input_raws=[False]).close()
+        with pytest.raises(omg.OmgError):
+            omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[omg.ContainerType()]], [0],
+                                               output_partials=[True])
     finally:
         omg.set_policy(omg.POLICY_SPARK)
     # a partial AVG emits (double sum, long count): two output types

@@ -334,3 +334,57 @@ def test_container_avg_partial_intermediate_final(policy):
         if ls:
             w = math.fsum(ls) / len(ls)
             assert abs(avg_l - w) <= 1e-9 * max(1.0, abs(w))
+
+
+def test_generic_int64_sum_partial_and_final():
+    """Two-stage int64 SUM under the container-vector policy (sum_aggregator.cpp:11-57,
+    :168-190): each stage is the generic sticky-overflow SUM -- a partial emits the sum, NULL for a
+    group that overflowed (overflow-as-null) or had no values, and the final stage sums the partial
+    sums in the order it receives them, skipping NULL rows.  Both stages equal the oracle run on
+    each stage's own input; a group that overflowed in one partial drops that partial's part."""
+    rng = np.random.default_rng(33)
+    n = 120_000
+    key = rng.integers(0, 2000, n).astype(np.int64)
+    knull = rng.random(n) < 0.01
+    v = rng.integers(-10**6, 10**6, n).astype(np.int64)
+    big = rng.random(n) < 0.002  # a few rows near 2^62: some groups overflow, some come back
+    v = np.where(big, rng.choice([2**62, -(2**62), 2**62 + 12345], n), v).astype(np.int64)
+    vnull = rng.random(n) < 0.05
+    aggs = lambda col, nulls: [dict(func=oracle.F_SUM, col=col, in_type=oracle.T_LONG, out_type=oracle.T_LONG,
+                                    nulls=nulls)]
+
+    def rows_of(cols):
+        return {None if cols[0][1][i] else int(cols[0][0][i]): None if cols[1][1][i] else int(cols[1][0][i])
+                for i in range(len(cols[0][0]))}
+
+    def oracle_rows(k, kn, val, vn):
+        keys, knulls, vals, vnulls = oracle.hashagg([k], [oracle.T_LONG], [kn], aggs(val, vn), policy=1,
+                                                    overflow_as_null=True)
+        return {None if knulls[0][i] else int(keys[0][i]): None if vnulls[0][i] else int(vals[0][i])
+                for i in range(len(keys[0]))}
+
+    try:
+        omg.set_policy(omg.POLICY_GENERIC)
+        part = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [SUM], output_partials=[True],
+                                                  overflow_as_null=True)
+        partials, pk, pkn, pv, pvn = [], [], [], [], []
+        for s, e in [(0, n // 2), (n // 2, n)]:
+            outs = _run(part, _batches([L, L], [key[s:e], v[s:e]], [knull[s:e], vnull[s:e]], [4096, 777]))
+            for b in outs:
+                c = omg.batch_to_numpy(b)
+                pk.append(c[0][0]), pkn.append(c[0][1]), pv.append(c[1][0]), pvn.append(c[1][1])
+            got = {}
+            for b in outs:
+                got.update(rows_of(omg.batch_to_numpy(b)))
+            assert got == oracle_rows(key[s:e], knull[s:e], v[s:e], vnull[s:e])
+            partials += outs
+        part.close()
+        fin = omg.HashAggregationOperatorFactory([0], [L], [[1]], [[L]], [[L]], [SUM], input_raws=[False],
+                                                 overflow_as_null=True)
+        cols = _columns(_run(fin, partials))
+        fin.close()
+    finally:
+        omg.set_policy(omg.POLICY_SPARK)
+    pk, pkn, pv, pvn = (np.concatenate(x) for x in (pk, pkn, pv, pvn))
+    assert pvn.any() and not pvn.all()  # some partial sums are NULL (overflowed or empty)
+    assert rows_of(cols) == oracle_rows(pk, pkn, pv, pvn)
