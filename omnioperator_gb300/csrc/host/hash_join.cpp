@@ -751,6 +751,37 @@ int CompileFilter(const Expr *e, FilterCode &fc, int depth)
             // 440-466), under the substr policies in force when the factory is created.
             const auto *fn = static_cast<const omniruntime::expressions::FuncExpr *>(e);
             const size_t n = fn->arguments.size();
+            // Buffer-free string functions (func_registry_string.cpp:286-380): their registered
+            // argument types, NULL in, NULL out except Greatest / Least.
+            static const std::map<std::string, std::pair<int16_t, int>> kStrFns = {
+                {"length", {omg::SFN_LENGTH, 1}}, {"char_length", {omg::SFN_LENGTH, 1}},
+                {"instr", {omg::SFN_INSTR, 2}}, {"StartsWith", {omg::SFN_STARTS_WITH, 2}},
+                {"EndsWith", {omg::SFN_ENDS_WITH, 2}}, {"Contains", {omg::SFN_CONTAINS, 2}},
+                {"Greatest", {omg::SFN_GREATEST, 2}}, {"Least", {omg::SFN_LEAST, 2}}};
+            const auto sf = kStrFns.find(fn->funcName);
+            if (sf != kStrFns.end()) {
+                if (n != static_cast<size_t>(sf->second.second)) {
+                    FilterUnsupported("function " + fn->funcName + " with " + std::to_string(n) + " arguments");
+                }
+                in.imm = -1;
+                for (size_t a = 0; a < n; ++a) {
+                    const Expr *arg = fn->arguments[a];
+                    const DataTypePtr &t = arg == nullptr ? nullptr : arg->GetReturnType();
+                    const int32_t id = t ? t->GetId() : -1;
+                    // length / char_length also take CHAR (LengthChar: the declared width)
+                    const bool ok = id == OMNI_VARCHAR || (id == OMNI_CHAR && sf->second.first == omg::SFN_LENGTH);
+                    if (CompileFilter(arg, fc, depth + static_cast<int>(a)) != kFilterString || !ok) {
+                        FilterUnsupported(fn->funcName + " of type " + std::to_string(id));
+                    }
+                    if (id == OMNI_CHAR) {
+                        in.imm = t->GetWidth();
+                    }
+                }
+                in.width = sf->second.first;
+                emit(omg::FOP_STRFN);
+                const bool str = sf->second.first == omg::SFN_GREATEST || sf->second.first == omg::SFN_LEAST;
+                return str ? kFilterString : kFilterInt;
+            }
             if (fn->funcName != "substr" || (n != 2 && n != 3)) {
                 FilterUnsupported("function " + fn->funcName + " with " + std::to_string(n) + " arguments");
             }

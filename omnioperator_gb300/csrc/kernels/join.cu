@@ -925,6 +925,74 @@ __device__ int StrCompare(const uint8_t *a, int32_t la, const uint8_t *b, int32_
     return la < lb ? -1 : (la > lb ? 1 : 0);
 }
 
+// Byte offset of the first occurrence of sub[0, ls) in s[0, l), or -1.
+__device__ int32_t StrFind(const uint8_t *s, int32_t l, const uint8_t *sub, int32_t ls)
+{
+    for (int32_t pos = 0; pos + ls <= l; ++pos) {
+        int32_t i = 0;
+        while (i < ls && s[pos + i] == sub[i]) {
+            ++i;
+        }
+        if (i == ls) {
+            return pos;
+        }
+    }
+    return -1;
+}
+
+// One FOP_STRFN over the stack entries from `a` on; leaves its result at `a`.
+__device__ void StrFunction(const FilterInstr &f, uint64_t *v, uint32_t *fl, int32_t *sl, int a)
+{
+    const bool an = (fl[a] & kFNull) != 0;
+    const auto *x = reinterpret_cast<const uint8_t *>(v[a]);
+    const int32_t lx = sl[a];
+    if (f.width == SFN_LENGTH) {
+        v[a] = an ? 0ull : static_cast<uint64_t>(f.imm >= 0 ? f.imm : Utf8Count(x, lx));
+        fl[a] = an ? kFNull : 0u;
+        sl[a] = 0;
+        return;
+    }
+    const bool bn = (fl[a + 1] & kFNull) != 0;
+    const auto *y = reinterpret_cast<const uint8_t *>(v[a + 1]);
+    const int32_t ly = sl[a + 1];
+    if (f.width == SFN_GREATEST || f.width == SFN_LEAST) {
+        // ExtremeStr (stringfunctions.cpp): a NULL side yields the other
+        bool right = an;
+        if (!an && !bn) {
+            const int c = StrCompare(x, lx, y, ly);
+            right = f.width == SFN_GREATEST ? c < 0 : c > 0;
+        }
+        if (right) {
+            v[a] = v[a + 1];
+            sl[a] = ly;
+        }
+        fl[a] = (an && bn) ? kFNull : kFString;
+        return;
+    }
+    uint64_t r = 0;
+    if (!an && !bn) {
+        switch (f.width) {
+            case SFN_INSTR: {
+                const int32_t pos = ly > lx ? -1 : StrFind(x, lx, y, ly);
+                r = pos < 0 ? 0ull : static_cast<uint64_t>(Utf8Count(x, pos) + 1);
+                break;
+            }
+            case SFN_STARTS_WITH:
+                r = ly <= lx && StrCompare(x, ly, y, ly) == 0 ? 1ull : 0ull;
+                break;
+            case SFN_ENDS_WITH:
+                r = ly <= lx && StrCompare(x + lx - ly, ly, y, ly) == 0 ? 1ull : 0ull;
+                break;
+            default:  // SFN_CONTAINS
+                r = ly <= lx && StrFind(x, lx, y, ly) >= 0 ? 1ull : 0ull;
+                break;
+        }
+    }
+    v[a] = r;
+    sl[a] = 0;
+    fl[a] = (an || bn) ? kFNull : 0u;
+}
+
 // The filter program over the candidate pair (probe row `row` of batch b, build row `br`);
 // `payload` (when not null) is the candidate's slot payload.
 __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t row, int64_t br,
@@ -960,6 +1028,15 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
             sl[sp] = len;
             fl[sp] = (isNull ? kFNull : 0u) | kFString;
             ++sp;
+            continue;
+        }
+        if (op == FOP_STRFN) {
+            const int nArgs = f.width == SFN_LENGTH ? 1 : 2;
+            if (sp < nArgs) {
+                return false;
+            }
+            StrFunction(f, v, fl, sl, sp - nArgs);
+            sp -= nArgs - 1;
             continue;
         }
         if (op == FOP_SUBSTR) {

@@ -447,6 +447,18 @@ enum FilterOp : int16_t {
                    // was NULL) before the value
     FOP_IN_STEP,   // (acc, v, item) -> (acc, v): fold one list item in
     FOP_IN_END,    // (acc, v): TRUE if matched, else NULL if v or an item was NULL, else FALSE
+    // String functions that need no result buffer (stringfunctions.cpp:2064-2092, 2801-2944),
+    // function in `width` (FilterStrFn); NULL if an argument is NULL unless stated:
+    FOP_STRFN,
+};
+enum FilterStrFn : int16_t {
+    SFN_LENGTH = 0,  // (s): code points; imm >= 0: a CHAR column's declared width instead
+    SFN_INSTR,       // (s, sub): 1-based code point position of the first occurrence, 0 if none
+    SFN_STARTS_WITH, // (s, prefix)
+    SFN_ENDS_WITH,   // (s, suffix)
+    SFN_CONTAINS,    // (s, sub)
+    SFN_GREATEST,    // (a, b): the greater string, NULL only when both are NULL
+    SFN_LEAST,       // (a, b): the lesser string, NULL only when both are NULL
 };
 constexpr int kFilterSubstrNegative = 1;
 constexpr int kFilterSubstrZero = 2;

@@ -304,6 +304,35 @@ def str_compare(a: bytes, b: bytes) -> int:
     return -1 if a < b else (1 if a > b else 0)
 
 
+def string_function(name: str, args: list, char_width=None):
+    """The buffer-free string functions of a filter (codegen/functions/stringfunctions.cpp:
+    2064-2092 length / char_length, 2801-2820 InStr, 2822-2844 StartsWith / EndsWith, 2900-2944
+    Contains / Greatest / Least) over bytes arguments, None for NULL: NULL in gives NULL out
+    (the INPUT_DATA registrations) except Greatest / Least, which return the other argument when
+    one is NULL.  char_width: length of a CHAR argument is its declared width."""
+    if name in ("Greatest", "Least"):
+        a, b = args
+        if a is None or b is None:
+            return b if a is None else a
+        c = str_compare(a, b)
+        return b if (c < 0 if name == "Greatest" else c > 0) else a
+    if any(x is None for x in args):
+        return None
+    if name in ("length", "char_length"):
+        return char_width if char_width is not None else utf8_count(args[0])
+    s, sub = args
+    if name == "instr":
+        pos = s.find(sub) if len(sub) <= len(s) else -1
+        return 0 if pos < 0 else utf8_count(s[:pos]) + 1
+    if name == "StartsWith":
+        return int(s.startswith(sub))
+    if name == "EndsWith":
+        return int(s.endswith(sub))
+    if name == "Contains":
+        return int(sub in s)
+    raise ValueError(name)
+
+
 def join_filtered(kind, build_keys, build_nulls, probe_keys, probe_nulls, passes):
     """join() with a join filter: a (probe, build) pair whose keys are equal counts as a match
     only when passes(probe_rows, build_rows) (a vectorised predicate over pair arrays) is true.

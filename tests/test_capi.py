@@ -145,6 +145,15 @@ def test_factory_validation_matches_reference_rules():
                  omg.Binary(omg.EXPR_LT, omg.Field(1, V), omg.Literal("abc", V)),
                  omg.IsNull(omg.Func("substr", [omg.Field(3, V), omg.Field(0, L)], V))):
         omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=good).close()
+    C8 = omg.DataType(omg.OMNI_CHAR, 0, 0, 8)
+    bf_c = omg.HashBuilderOperatorFactory(omg.OMNI_JOIN_TYPE_INNER, [L, C8], [0])
+    omg.LookupJoinOperatorFactory([L, C8], [0], [0], [1], [C8], bf_c, filter_expr=omg.Binary(
+        omg.EXPR_GT, omg.Func("length", [omg.Field(1, C8)], L), omg.Literal(3, L))).close()
+    with pytest.raises(omg.OmgError) as e:  # StartsWith is registered for VARCHAR only
+        omg.LookupJoinOperatorFactory([L, C8], [0], [0], [1], [C8], bf_c, filter_expr=omg.Func(
+            "StartsWith", [omg.Field(1, C8), omg.Literal("a", V)], omg.BooleanType()))
+    assert e.value.status == -2
+    bf_c.close()
     for bad in (omg.Func("upper", [omg.Field(1, V)], V),
                 omg.Binary(omg.EXPR_EQ, sub, omg.Field(0, L)),
                 omg.Binary(omg.EXPR_AND, omg.Field(1, V), omg.Literal(1, omg.BooleanType())),

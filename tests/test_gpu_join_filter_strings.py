@@ -171,6 +171,8 @@ def _eval(e, pcols, pmasks, bcols, bmasks, i, j, nprobe):
         return None if e.is_null else (e.value if isinstance(e.value, (bytes, int, float)) else e.value.encode())
     if isinstance(e, omg.Func):
         a = [_eval(x, pcols, pmasks, bcols, bmasks, i, j, nprobe) for x in e.args]
+        if e.name != "substr":
+            return oracle.string_function(e.name, a)
         if any(x is None for x in a):
             return None
         neg, zero = omg.get_substr_rules()
@@ -248,6 +250,13 @@ FILTERS = {
                                            (B(omg.EXPR_GT, F(5, L), Lit(2, L)),
                                             omg.Between(F(1, V), Lit("b", V), F(4, V)))],
                                           B(omg.EXPR_EQ, omg.Coalesce(F(4, V), Lit("x", V)), Lit("x", V)))),
+    "string_functions": B(omg.EXPR_OR,
+                          B(omg.EXPR_AND, Fn("StartsWith", [F(1, V), Fn("substr", [F(4, V), Lit(1, I), Lit(1, I)], V)], omg.BooleanType()),
+                            B(omg.EXPR_LT, Fn("length", [F(1, V)], L), Fn("instr", [F(4, V), Lit("中", V)], I))),
+                          B(omg.EXPR_OR, Fn("Contains", [Fn("Greatest", [F(1, V), F(4, V)], V), Lit("ab", V)],
+                                            omg.BooleanType()),
+                            B(omg.EXPR_AND, Fn("EndsWith", [F(4, V), Lit("z", V)], omg.BooleanType()),
+                              B(omg.EXPR_EQ, Fn("Least", [F(1, V), F(4, V)], V), F(1, V))))),
     "not_between_if": omg.Not(omg.Between(F(5, L), Lit(-2, L),
                                                   omg.If(omg.IsNull(F(6, D)), Lit(0, L), Lit(3, L)))),
 }
@@ -313,3 +322,30 @@ def test_string_filter_on_the_bitmap_probe(fname):
     want = _expected("inner", bcols, bm, pcols, pm, [0, 2], [2], FILTERS[fname])
     assert len(want) > 0
     assert sorted(got, key=_key) == sorted(want, key=_key)
+
+
+def test_string_function_kats_on_the_probe_kernel():
+    """The reference's instr / StartsWith / EndsWith / length / Contains known answers
+    (function_test.cpp:2623-2800, 3741-3797), evaluated by the probe kernel: fn(build.s[,
+    probe.arg]) = probe.expected keeps the row, and a wrong expected value drops it."""
+    from test_oracle_golden import STRING_FN_KATS
+    got, want = set(), set()
+    for name in sorted({k[0] for k in STRING_FN_KATS}):
+        cases = [k for k in STRING_FN_KATS if k[0] == name]
+        n = len(cases)
+        ret = {"length": L, "instr": I, "char_length": I}.get(name, omg.BooleanType())
+        dtype = {omg.OMNI_LONG: np.int64, omg.OMNI_INT: np.int32, omg.OMNI_BOOLEAN: np.bool_}[ret.id]
+        bkey = np.arange(n, dtype=np.int64)
+        bstr = np.array([k[1][0].encode() for k in cases], dtype=object)
+        pkey = np.repeat(bkey, 2)
+        parg = np.repeat(np.array([(k[1][1] if len(k[1]) > 1 else "").encode() for k in cases], dtype=object), 2)
+        right = [k[2] for k in cases]
+        wrong = [(1 - x) if ret.id == omg.OMNI_BOOLEAN else x + 7 for x in right]
+        pexp = np.array([x for pair in zip(right, wrong) for x in pair], dtype=dtype)
+        args = [F(4, V)] + ([F(1, V)] if len(cases[0][1]) > 1 else [])
+        none_b, none_p = np.zeros(n, bool), np.zeros(2 * n, bool)
+        rows, _ = run("INNER", [L, V], [bkey, bstr], [none_b, none_b], [L, V, ret], [pkey, parg, pexp],
+                      [none_p] * 3, [0], [], B(omg.EXPR_EQ, Fn(name, args, ret), F(2, ret)), batch_sizes=(2 * n,))
+        got |= {(name, r[0]) for r in rows}
+        want |= {(name, i) for i in range(n)}
+    assert got == want

@@ -262,3 +262,35 @@ def test_oracle_str_compare_is_unsigned_bytes_then_length():
     assert oracle.str_compare(b"ab", b"abc") == -1
     assert oracle.str_compare(b"\xc3\xa9", b"z") == 1  # bytes above 0x7f compare as unsigned
     assert oracle.str_compare(b"", b"") == 0
+
+
+# core/test/codegen/function_test.cpp:2623-2800 (InStr, StartsWithStr, EndsWithStr, LengthStr,
+# LengthStrZh, CharLengthStr, LengthChar, CharLengthChar) and :3741-3797 (ContainsStr): the
+# non-NULL calls; a NULL argument makes the expression NULL (the INPUT_DATA registrations).
+STRING_FN_KATS = [
+    ("instr", ["abc", "abcd"], 0), ("instr", ["abc", "bd"], 0), ("instr", ["abc", "bc"], 2),
+    ("instr", ["", "ab"], 0), ("instr", ["abc", ""], 1), ("instr", ["", ""], 1),
+    ("instr", ["一丁丂七丄丅丆万丈三上下丌不与丏", "万丈"], 8), ("instr", ["壹貳叁肆伍", "叁肆"], 3),
+    ("StartsWith", ["abc", "abcd"], 0), ("StartsWith", ["abc", "bd"], 0), ("StartsWith", ["abc", "ab"], 1),
+    ("StartsWith", ["", "ab"], 0), ("StartsWith", ["abc", ""], 1), ("StartsWith", ["", ""], 1),
+    ("EndsWith", ["abc", "abcd"], 0), ("EndsWith", ["abc", "bd"], 0), ("EndsWith", ["abc", "bc"], 1),
+    ("EndsWith", ["", "ab"], 0), ("EndsWith", ["abc", ""], 1), ("EndsWith", ["", ""], 1),
+    ("length", ["abcd"], 4), ("length", ["时欧基乌斯侧后解 hello! 回复哦黑色的and magic粉色的圣诞袜"], 37),
+    ("char_length", ["m"], 1),
+    ("Contains", ["", "abc"], 0), ("Contains", ["abc", "abd"], 0), ("Contains", ["abcd", "abd"], 0),
+    ("Contains", ["abcd", "acd"], 0),
+]
+
+
+@pytest.mark.parametrize("name,args,expected", STRING_FN_KATS)
+def test_oracle_string_function_kats(name, args, expected):
+    assert oracle.string_function(name, [a.encode() for a in args]) == expected
+
+
+def test_oracle_string_function_nulls_and_extremes():
+    assert oracle.string_function("instr", [None, b"a"]) is None
+    assert oracle.string_function("length", [b"abcd"], char_width=10) == 10  # LengthChar: the width
+    assert oracle.string_function("Greatest", [b"ab", b"abc"]) == b"abc"
+    assert oracle.string_function("Least", [b"ab", b"abc"]) == b"ab"
+    assert oracle.string_function("Greatest", [None, b"x"]) == b"x"
+    assert oracle.string_function("Least", [None, None]) is None
