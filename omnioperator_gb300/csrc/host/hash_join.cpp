@@ -758,6 +758,26 @@ int CompileFilter(const Expr *e, FilterCode &fc, int depth)
                 {"instr", {omg::SFN_INSTR, 2}}, {"StartsWith", {omg::SFN_STARTS_WITH, 2}},
                 {"EndsWith", {omg::SFN_ENDS_WITH, 2}}, {"Contains", {omg::SFN_CONTAINS, 2}},
                 {"Greatest", {omg::SFN_GREATEST, 2}}, {"Least", {omg::SFN_LEAST, 2}}};
+            if (fn->funcName == "CAST" && n == 1) {
+                // Numeric CAST (func_registry_math.cpp:172-194,355-366): integer-like to integer-
+                // like or DOUBLE, DOUBLE to LONG / INT (RoundingRule::DOWN, the default).
+                const DataTypePtr &rt = fn->GetReturnType();
+                const Expr *arg = fn->arguments[0];
+                const DataTypePtr at = arg == nullptr ? nullptr : arg->GetReturnType();
+                const int rk = rt ? FilterKind(rt) : -1;
+                const int ak = CompileFilter(arg, fc, depth);
+                const int rw = rk == kFilterInt ? rt->ByteWidth() : 8;
+                const bool intTarget = rk == kFilterInt && (rw == 1 || rw == 2 || rw == 4 || rw == 8);
+                if (ak == kFilterString || (rk != kFilterDouble && !intTarget) ||
+                    (ak == kFilterDouble && rk == kFilterInt && rw != 4 && rw != 8) || at == nullptr) {
+                    FilterUnsupported("CAST from type " + std::to_string(at ? at->GetId() : -1) + " to " +
+                        std::to_string(rt ? rt->GetId() : -1));
+                }
+                in.width = static_cast<int16_t>(rw);
+                in.dbl = static_cast<int16_t>(rk == kFilterDouble ? 1 : 0);
+                emit(omg::FOP_CAST);
+                return rk;
+            }
             const auto sf = kStrFns.find(fn->funcName);
             if (sf != kStrFns.end()) {
                 if (n != static_cast<size_t>(sf->second.second)) {

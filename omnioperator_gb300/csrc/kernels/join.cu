@@ -1030,6 +1030,36 @@ __device__ bool FilterPasses(const ProbeLaunch &p, const BatchDesc &b, int64_t r
             ++sp;
             continue;
         }
+        if (op == FOP_CAST) {
+            if (sp < 1) {
+                return false;
+            }
+            const int a = sp - 1;
+            if ((fl[a] & kFNull) == 0) {
+                const bool fromDouble = (fl[a] & kFDouble) != 0;
+                if (f.dbl) {
+                    v[a] = fromDouble ? v[a]
+                                      : static_cast<uint64_t>(__double_as_longlong(
+                                            static_cast<double>(static_cast<int64_t>(v[a]))));
+                } else {
+                    int64_t x;
+                    if (fromDouble) {
+                        // NaN gives 0 and out-of-range values saturate, stated explicitly rather than
+                        // left to the conversion instruction
+                        const double d = __longlong_as_double(static_cast<long long>(v[a]));
+                        const double lim = f.width == 8 ? 9223372036854775808.0 : 2147483648.0;
+                        const int64_t hi = f.width == 8 ? INT64_MAX : INT32_MAX;
+                        const int64_t lo = f.width == 8 ? INT64_MIN : INT32_MIN;
+                        x = d != d ? 0 : (d >= lim ? hi : (d <= -lim ? lo : static_cast<int64_t>(__double2ll_rz(d))));
+                    } else {
+                        x = static_cast<int64_t>(v[a]);
+                    }
+                    v[a] = static_cast<uint64_t>(f.width == 8 ? x : SignExtend(static_cast<uint64_t>(x), f.width));
+                }
+            }
+            fl[a] = (fl[a] & kFNull) | (f.dbl ? kFDouble : 0u);
+            continue;
+        }
         if (op == FOP_STRFN) {
             const int nArgs = f.width == SFN_LENGTH ? 1 : 2;
             if (sp < nArgs) {

@@ -450,6 +450,11 @@ enum FilterOp : int16_t {
     // String functions that need no result buffer (stringfunctions.cpp:2064-2092, 2801-2944),
     // function in `width` (FilterStrFn); NULL if an argument is NULL unless stated:
     FOP_STRFN,
+    // CAST between numbers (codegen/functions/mathfunctions.cpp:24-113, the RoundingRule::DOWN
+    // registry): to the width in `width` (wrapping, as static_cast) or to DOUBLE (dbl = 1); a
+    // DOUBLE to LONG / INT truncates toward zero, saturating out of range, NaN to 0 (the
+    // conversion of the Arm hosts the reference runs on).  NULL stays NULL.
+    FOP_CAST,
 };
 enum FilterStrFn : int16_t {
     SFN_LENGTH = 0,  // (s): code points; imm >= 0: a CHAR column's declared width instead

@@ -154,6 +154,15 @@ def test_factory_validation_matches_reference_rules():
             "StartsWith", [omg.Field(1, C8), omg.Literal("a", V)], omg.BooleanType()))
     assert e.value.status == -2
     bf_c.close()
+    # numeric CAST: integer-like to integer-like or DOUBLE, DOUBLE to LONG / INT
+    omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=omg.Binary(
+        omg.EXPR_GT, omg.Func("CAST", [omg.Field(0, L)], omg.DoubleType()), omg.Literal(0.5, omg.DoubleType()))).close()
+    for bad_cast in (omg.Func("CAST", [omg.Field(1, V)], L),
+                     omg.Func("CAST", [omg.Literal(1.5, omg.DoubleType())], omg.ShortType())):
+        with pytest.raises(omg.OmgError) as e:
+            omg.LookupJoinOperatorFactory([L, V], [0], [0], [1], [V], sf, filter_expr=omg.Binary(
+                omg.EXPR_EQ, bad_cast, omg.Literal(1, bad_cast.dtype)))
+        assert e.value.status == -2
     for bad in (omg.Func("upper", [omg.Field(1, V)], V),
                 omg.Binary(omg.EXPR_EQ, sub, omg.Field(0, L)),
                 omg.Binary(omg.EXPR_AND, omg.Field(1, V), omg.Literal(1, omg.BooleanType())),

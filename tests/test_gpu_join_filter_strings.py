@@ -160,6 +160,20 @@ def _utf8_words(rng, n, pool):
     return np.array([words[i].encode() for i in rng.integers(0, pool, n)], dtype=object)
 
 
+def _cast(x, dtype):
+    """Numeric CAST (mathfunctions.cpp:24-113, RoundingRule::DOWN): integers wrap to the target
+    width, DOUBLE truncates toward zero, saturating at the target's range, NaN giving 0."""
+    if x is None:
+        return None
+    if dtype.id == omg.OMNI_DOUBLE:
+        return float(x)
+    bits = {omg.OMNI_LONG: 64, omg.OMNI_INT: 32, omg.OMNI_SHORT: 16}[dtype.id]
+    lo, hi = -(1 << (bits - 1)), (1 << (bits - 1)) - 1
+    if isinstance(x, float):
+        return 0 if x != x else max(lo, min(hi, int(x)))
+    return ((int(x) - lo) % (1 << bits)) + lo
+
+
 def _eval(e, pcols, pmasks, bcols, bmasks, i, j, nprobe):
     """Value of filter node `e` for probe row i and build row j (None for NULL), SQL semantics."""
     if isinstance(e, omg.Field):
@@ -171,6 +185,8 @@ def _eval(e, pcols, pmasks, bcols, bmasks, i, j, nprobe):
         return None if e.is_null else (e.value if isinstance(e.value, (bytes, int, float)) else e.value.encode())
     if isinstance(e, omg.Func):
         a = [_eval(x, pcols, pmasks, bcols, bmasks, i, j, nprobe) for x in e.args]
+        if e.name == "CAST":
+            return _cast(a[0], e.dtype)
         if e.name != "substr":
             return oracle.string_function(e.name, a)
         if any(x is None for x in a):
@@ -257,6 +273,9 @@ FILTERS = {
                                             omg.BooleanType()),
                             B(omg.EXPR_AND, Fn("EndsWith", [F(4, V), Lit("z", V)], omg.BooleanType()),
                               B(omg.EXPR_EQ, Fn("Least", [F(1, V), F(4, V)], V), F(1, V))))),
+    "numeric_casts": B(omg.EXPR_OR, B(omg.EXPR_EQ, Fn("CAST", [F(6, D)], I), Fn("CAST", [F(5, L)], I)),
+                       B(omg.EXPR_AND, B(omg.EXPR_GT, Fn("CAST", [F(2, I)], D), F(6, D)),
+                         B(omg.EXPR_EQ, Fn("CAST", [F(5, L)], omg.ShortType()), Fn("CAST", [F(2, I)], omg.ShortType())))),
     "not_between_if": omg.Not(omg.Between(F(5, L), Lit(-2, L),
                                                   omg.If(omg.IsNull(F(6, D)), Lit(0, L), Lit(3, L)))),
 }
