@@ -2050,6 +2050,31 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                 (p.filter[f].op == FOP_BUILD_COL && (payloadTab == nullptr || p.filter[f].payloadShift == 0));
         }
     }
+    // One comparison of an integer slot-payload field with a non-NULL integer literal, decoded once
+    // here: per candidate the field is shifted out, sign-extended and compared without branching
+    // on the program (plMask bit 0: passes when less, 1: equal, 2: greater).
+    bool plCmp = false;
+    int plShift = 0;
+    int plWidth = 8;
+    int64_t plLit = 0;
+    uint32_t plMask = 0;
+    if (kFilter == 2 && payloadTab != nullptr && p.nFilter == 3) {
+        const FilterInstr &fa = p.filter[0];
+        const FilterInstr &fb = p.filter[1];
+        plCmp = fa.op == FOP_BUILD_COL && fa.payloadShift > 0 && fa.dbl == 0 && fb.op == FOP_LITERAL &&
+            fb.dbl == 0 && fb.isNull == 0;
+        plShift = fa.payloadShift - 1;
+        plWidth = fa.width;
+        plLit = fb.imm;
+        switch (p.filter[2].op) {
+            case FOP_EQ: plMask = 2u; break;
+            case FOP_NEQ: plMask = 5u; break;
+            case FOP_LT: plMask = 1u; break;
+            case FOP_LTE: plMask = 3u; break;
+            case FOP_GT: plMask = 4u; break;
+            default: plMask = 6u; break;  // FOP_GTE
+        }
+    }
     const int64_t warpsTotal = static_cast<int64_t>(gridDim.x) * (kThreads / 32);
     for (int64_t item = static_cast<int64_t>(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5); item < nItems;
          item += warpsTotal) {
@@ -2124,9 +2149,17 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                     const int64_t br = filterNeedsRow ? p.table.arrayEntries[static_cast<uint64_t>(key[i]) - minKey] : -1;
                     const int64_t row = base + i * 32 + lane;
                     const bool hasPayload = payloadTab != nullptr;
-                    const bool pass = (kFilter == 2 || simpleFilter)
-                        ? SimpleFilterPasses(p, *segBatch, row, br, hasPayload, payload[i])
-                        : (kFilter == 1 && FilterPasses(p, *segBatch, row, br, hasPayload, payload[i]));
+                    bool pass;
+                    if (plCmp) {
+                        const uint64_t bits = payload[i] >> plShift;
+                        const int64_t x = plWidth == 8 ? static_cast<int64_t>(bits) : SignExtend(bits, plWidth);
+                        const uint32_t c = (x < plLit ? 1u : 0u) | (x == plLit ? 2u : 0u) | (x > plLit ? 4u : 0u);
+                        pass = (c & plMask) != 0;
+                    } else {
+                        pass = (kFilter == 2 || simpleFilter)
+                            ? SimpleFilterPasses(p, *segBatch, row, br, hasPayload, payload[i])
+                            : (kFilter == 1 && FilterPasses(p, *segBatch, row, br, hasPayload, payload[i]));
+                    }
                     if (!pass) {
                         hit &= ~(1u << i);
                     } else if (p.visited != nullptr) {
