@@ -2050,22 +2050,32 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                 (p.filter[f].op == FOP_BUILD_COL && (payloadTab == nullptr || p.filter[f].payloadShift == 0));
         }
     }
-    // One comparison of an integer slot-payload field with a non-NULL integer literal, decoded once
-    // here: per candidate the field is shifted out, sign-extended and compared without branching
-    // on the program (plMask bit 0: passes when less, 1: equal, 2: greater).
+    // One comparison of an integer slot-payload field with a non-NULL integer literal or an integer
+    // probe column, in either order, decoded once here: per candidate the field is shifted out,
+    // sign-extended and compared without branching on the program (plMask bit 0: passes when the
+    // field is less, 1: equal, 2: greater; a NULL probe value fails).
     bool plCmp = false;
     int plShift = 0;
     int plWidth = 8;
     int64_t plLit = 0;
+    int plInput = -1;  // >= 0: the other operand is this probe input
+    int plInWidth = 8;
     uint32_t plMask = 0;
     if (kFilter == 2 && payloadTab != nullptr && p.nFilter == 3) {
-        const FilterInstr &fa = p.filter[0];
-        const FilterInstr &fb = p.filter[1];
-        plCmp = fa.op == FOP_BUILD_COL && fa.payloadShift > 0 && fa.dbl == 0 && fb.op == FOP_LITERAL &&
-            fb.dbl == 0 && fb.isNull == 0;
-        plShift = fa.payloadShift - 1;
-        plWidth = fa.width;
-        plLit = fb.imm;
+        auto isField = [](const FilterInstr &f) { return f.op == FOP_BUILD_COL && f.payloadShift > 0 && f.dbl == 0; };
+        auto isOther = [](const FilterInstr &f) {
+            return (f.op == FOP_LITERAL && f.dbl == 0 && f.isNull == 0) || (f.op == FOP_PROBE_COL && f.dbl == 0);
+        };
+        const bool fieldFirst = isField(p.filter[0]) && isOther(p.filter[1]);
+        const bool fieldSecond = !fieldFirst && isOther(p.filter[0]) && isField(p.filter[1]);
+        plCmp = fieldFirst || fieldSecond;
+        const FilterInstr &fld = fieldFirst ? p.filter[0] : p.filter[1];
+        const FilterInstr &oth = fieldFirst ? p.filter[1] : p.filter[0];
+        plShift = fld.payloadShift - 1;
+        plWidth = fld.width;
+        plLit = oth.imm;
+        plInput = oth.op == FOP_PROBE_COL ? oth.input : -1;
+        plInWidth = oth.width;
         switch (p.filter[2].op) {
             case FOP_EQ: plMask = 2u; break;
             case FOP_NEQ: plMask = 5u; break;
@@ -2073,6 +2083,9 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
             case FOP_LTE: plMask = 3u; break;
             case FOP_GT: plMask = 4u; break;
             default: plMask = 6u; break;  // FOP_GTE
+        }
+        if (fieldSecond) {  // other OP field: swap the less and greater outcomes
+            plMask = (plMask & 2u) | ((plMask & 1u) << 2) | ((plMask >> 2) & 1u);
         }
     }
     const int64_t warpsTotal = static_cast<int64_t>(gridDim.x) * (kThreads / 32);
@@ -2153,8 +2166,14 @@ __global__ void __launch_bounds__(BitsThreads<kPack, kFilter>::value, 1)
                     if (plCmp) {
                         const uint64_t bits = payload[i] >> plShift;
                         const int64_t x = plWidth == 8 ? static_cast<int64_t>(bits) : SignExtend(bits, plWidth);
-                        const uint32_t c = (x < plLit ? 1u : 0u) | (x == plLit ? 2u : 0u) | (x > plLit ? 4u : 0u);
-                        pass = (c & plMask) != 0;
+                        int64_t y = plLit;
+                        bool known = true;
+                        if (plInput >= 0) {
+                            known = !RowIsNullRO(segBatch->nulls[plInput], row);
+                            y = known ? LoadIntRO(segBatch->cols[plInput], row, plInWidth) : 0;
+                        }
+                        const uint32_t c = (x < y ? 1u : 0u) | (x == y ? 2u : 0u) | (x > y ? 4u : 0u);
+                        pass = known && (c & plMask) != 0;
                     } else {
                         pass = (kFilter == 2 || simpleFilter)
                             ? SimpleFilterPasses(p, *segBatch, row, br, hasPayload, payload[i])

@@ -316,3 +316,36 @@ def test_filter_on_payload_fields_headline_layout(fop, lit):
     ok &= cmp(p1[np.where(ok, bi, 0)].astype(np.int64), lit)
     want = sorted(zip(pkey[ok].tolist(), p1[bi[ok]].tolist(), p2[bi[ok]].tolist()))
     assert len(want) > 0 and sorted(got) == want
+
+
+@pytest.mark.parametrize("fop", [omg.EXPR_LT, omg.EXPR_GTE, omg.EXPR_EQ])
+@pytest.mark.parametrize("probe_first", [True, False])
+def test_filter_probe_column_against_payload_field(fop, probe_first):
+    """The headline shape with one comparison between a probe column (INT, with NULLs) and a build
+    payload field, in either order: the bitmap kernel decodes the comparison once and reads the
+    field from the slot payload; rows against a direct restatement (a NULL probe value fails)."""
+    rng = np.random.default_rng(70 + fop + 3 * probe_first)
+    nb, npr = 1 << 16, 400_000
+    bkey = rng.permutation(nb).astype(np.int64)
+    p1 = rng.integers(-20, 20, nb).astype(np.int32)
+    p2 = rng.integers(-2**31, 2**31, nb, dtype=np.int64).astype(np.int32)
+    pkey = rng.integers(0, nb + nb // 4, npr).astype(np.int64)
+    pv = rng.integers(-20, 20, npr).astype(np.int32)
+    pm, vm = rng.random(npr) < 0.01, rng.random(npr) < 0.05
+    none_b = np.zeros(nb, bool)
+    a, b = (F(1, I), F(3, I)) if probe_first else (F(3, I), F(1, I))
+    got = run("INNER", "UNKNOWN", [L, I, I], [bkey, p1, p2], [none_b, none_b, none_b], [L, I], [pkey, pv], [pm, vm],
+              [0], [1, 2], B(fop, a, b), batch_sizes=(npr,))
+    assert omg.lib().omg_debug_last_probe_kernel() == 4
+    pos = np.full(nb + nb // 4, -1, np.int64)
+    pos[bkey] = np.arange(nb)
+    bi = pos[pkey]
+    ok = (bi >= 0) & ~pm & ~vm
+    x = pv.astype(np.int64)
+    y = p1[np.where(ok, bi, 0)].astype(np.int64)
+    if not probe_first:
+        x, y = y, x
+    cmp = {omg.EXPR_GTE: np.greater_equal, omg.EXPR_LT: np.less, omg.EXPR_EQ: np.equal}[fop]
+    ok &= cmp(x, y)
+    want = sorted(zip(pkey[ok].tolist(), p1[bi[ok]].tolist(), p2[bi[ok]].tolist()))
+    assert len(want) > 0 and sorted(got) == want
